@@ -1,0 +1,257 @@
+/*
+ * xara_gpu.h -- C ABI of libxara_gpu.so, the GB300 implementation of the
+ * xara/OpenSees Newton-iteration hot path (element state determination,
+ * material updates, global assembly and the linear solve of one load or
+ * time step).
+ *
+ * Conventions (all entry points):
+ *   - return 0 on success, a negative XG_E* code on failure; the last error
+ *     text is available from xg_last_error();
+ *   - host arrays are borrowed for the duration of the call only;
+ *   - device memory never crosses the boundary: every handle owns its device
+ *     buffers and one CUDA stream, and calls on one handle are synchronous
+ *     and not reentrant (the reference path is single threaded as well);
+ *   - all arithmetic is IEEE FP64, all counts and indices are int32.
+ *
+ * Each entry point names the reference interface it replaces
+ * (paths are relative to the reference's SRC/ directory).
+ */
+#ifndef XARA_GPU_H
+#define XARA_GPU_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ----------------------------------------------------------------------- */
+/* error codes                                                               */
+/* ----------------------------------------------------------------------- */
+#define XG_OK              0
+#define XG_EINVAL         -1   /* bad argument or model description        */
+#define XG_ECUDA          -2   /* CUDA runtime error                       */
+#define XG_ENOMEM         -3   /* device allocation failed                 */
+#define XG_ESOLVE         -4   /* linear solve failed (breakdown / maxit)  */
+#define XG_ENOCONV        -5   /* Newton test failed (TestFailed)          */
+#define XG_EELEMENT       -6   /* element state determination failed       */
+#define XG_ESTATE         -7   /* call out of sequence                     */
+
+/* element families (one family per model) */
+#define XG_ELE_QUAD        1   /* element/Plane/FourNodeQuad.cpp           */
+#define XG_ELE_BRICK       2   /* element/Brick/Brick.cpp                  */
+#define XG_ELE_FBC2D       3   /* element/Frame/Other/Force/ForceBeamColumn2d.cpp */
+#define XG_ELE_FBC3D       4   /* element/Frame/Other/Force/ForceBeamColumn3d.cpp */
+
+/* uniaxial material laws (fiber sections) */
+#define XG_UNI_STEEL02     1   /* material/uniaxial/steel/Steel02.cpp      */
+#define XG_UNI_CONCRETE02  2   /* material/uniaxial/concrete/Concrete02.cpp */
+#define XG_UNI_ELASTIC     3   /* linear elastic fiber (known-answer tests) */
+
+/* constraint handlers (analysis/handler) */
+#define XG_HANDLER_PLAIN           0  /* PlainHandler.cpp                   */
+#define XG_HANDLER_TRANSFORMATION  1  /* TransformationConstraintHandler.cpp */
+
+/* integrators */
+#define XG_INT_LOAD_CONTROL   0  /* analysis/integrator/Static/LoadControl.cpp          */
+#define XG_INT_DISP_CONTROL   1  /* analysis/integrator/Static/DisplacementControl.cpp  */
+#define XG_INT_NEWMARK        2  /* analysis/integrator/Dynamic/Newmark.cpp              */
+
+/* convergence tests */
+#define XG_TEST_NORM_DISP_INCR  0  /* analysis/criteria/CTestNormDispIncr.cpp */
+#define XG_TEST_NORM_UNBALANCE  1  /* analysis/criteria/CTestNormUnbalance.cpp */
+
+/* linear systems */
+#define XG_SYSTEM_BJPCG    0   /* block-Jacobi PCG on the device (new `system CudaBJPCG`) */
+
+/* J2 parameter row (nDMaterial J2Plasticity, material/plastic/J2Plasticity.cpp:84-111) */
+#define XG_J2_NPARAM 8         /* K G sigma0 sigma_inf delta H eta rho */
+/* uniaxial parameter row, Steel02: fy E0 b R0 cR1 cR2 a1 a2 a3 a4 sigInit
+   (material/uniaxial/steel/Steel02.h:47-50); Concrete02: fc epsc0 fcu epscu
+   rat ft Ets (material/uniaxial/concrete/Concrete02.h:48-49); Elastic: E */
+#define XG_UNI_NPARAM 12
+
+/*
+ * Model description: the data the reference's modelling commands
+ * (`node`, `fix`, `element quad|stdBrick|forceBeamColumn`, `nDMaterial
+ * J2Plasticity`, `uniaxialMaterial Steel02|Concrete02`, `section Fiber`,
+ * `geomTransf`, `pattern Plain`/`load`/`sp`, `mass`) put into a Domain,
+ * flattened into structure-of-arrays form.  Node and element tags must be
+ * strictly ascending: the reference iterates its MapOfTaggedObjects storage
+ * in ascending tag order (tagged/storage/MapOfTaggedObjects.cpp), which fixes
+ * both the DOF numbering and the assembly order.
+ */
+typedef struct xg_model_desc {
+  int ndm, ndf;                 /* 2/2 quad, 3/3 brick, 2/3 frame2d, 3/6 frame3d */
+
+  int num_nodes;
+  const int    *node_tag;       /* [num_nodes] ascending                     */
+  const double *node_crd;       /* [num_nodes*ndm]                           */
+  const double *node_mass;      /* [num_nodes*ndf] lumped mass or NULL       */
+
+  int elem_type;                /* XG_ELE_*                                  */
+  int num_elems;
+  const int    *elem_tag;       /* [num_elems] ascending                     */
+  const int    *elem_conn;      /* [num_elems*nen] node tags                 */
+  const int    *elem_mat;       /* [num_elems] J2 row (quad/brick) or section row (frames) */
+  double        thickness;      /* quad thickness                            */
+
+  /* frames */
+  const double *elem_vecxz;     /* [num_elems*3] frame3d orientation (geomTransf vecxz) */
+  int geom_transf;              /* 0 Linear, 1 PDelta                        */
+  int fbc_num_ip;               /* Lobatto points per element (reference default 5) */
+  int fbc_max_iters;            /* element compatibility iterations (default 10) */
+  double fbc_tol;               /* element energy tolerance (default 1e-12)   */
+
+  /* material tables */
+  int num_j2;
+  const double *j2_param;       /* [num_j2*XG_J2_NPARAM]                     */
+  int num_uni;
+  const int    *uni_type;       /* [num_uni] XG_UNI_*                        */
+  const double *uni_param;      /* [num_uni*XG_UNI_NPARAM]                   */
+
+  /* fiber sections: fibers of section s are [sec_fiber_start[s], sec_fiber_start[s+1]) */
+  int num_sec;
+  const int    *sec_fiber_start;/* [num_sec+1]                               */
+  const double *fib_y;          /* [total fibers]                            */
+  const double *fib_z;          /* [total fibers] (frame3d)                  */
+  const double *fib_area;       /* [total fibers]                            */
+  const int    *fib_mat;        /* [total fibers] uniaxial row               */
+  const double *sec_GJ;         /* [num_sec] elastic torsion (frame3d)       */
+
+  /* single-point constraints: pattern < 0 is a fixed homogeneous `fix`;
+     pattern p >= 0 imposes value*lambda_p (an `sp` inside `pattern Plain p`) */
+  int num_sp;
+  const int    *sp_node;        /* node tag                                  */
+  const int    *sp_dof;         /* 0-based dof                               */
+  const int    *sp_pattern;
+  const double *sp_value;
+  int handler;                  /* XG_HANDLER_*                              */
+
+  /* `equalDOF rNode cNode dof`: MP_Constraint with an identity constraint
+     matrix (domain/constraints/MP_Constraint.h:62-66).  PlainHandler gives the
+     constrained dof the retained dof's equation number
+     (analysis/handler/PlainHandler.cpp:128-180, DOF_Numberer.cpp:155-185). */
+  int num_mp;
+  const int    *mp_retained;    /* retained node tag                         */
+  const int    *mp_constrained; /* constrained node tag                      */
+  const int    *mp_dof;         /* 0-based dof, same on both nodes           */
+
+  /* nodal loads of `pattern Plain p { load ... }`, linear time series */
+  int num_loads;
+  const int    *load_node;      /* node tag                                  */
+  const int    *load_pattern;
+  const double *load_value;     /* [num_loads*ndf]                           */
+} xg_model_desc;
+
+/*
+ * One analysis phase (`integrator ...; test ...; algorithm Newton;
+ * analysis Static|Transient; analyze num_steps [dt]`).  Phase p drives load
+ * pattern p; at the end of a phase with load_const != 0 every pattern is
+ * held constant and the domain time reset to 0 (`loadConst -time 0.0`).
+ */
+typedef struct xg_phase_desc {
+  int integrator;               /* XG_INT_*                                  */
+  int pattern;                  /* pattern driven by this phase              */
+  int num_steps;
+  double d_lambda;              /* LoadControl increment                     */
+  int dc_node, dc_dof;          /* DisplacementControl node tag, 0-based dof */
+  double dc_incr;               /* DisplacementControl increment             */
+  double dt, gamma, beta;       /* Newmark                                   */
+  double alpha_m, beta_k, beta_k_init, beta_k_comm;  /* rayleigh           */
+  int gm_dof;                   /* UniformExcitation direction (0-based)     */
+  int gm_npts;                  /* ground acceleration samples               */
+  double gm_dt;
+  const double *gm_accel;       /* [gm_npts]                                 */
+  int test;                     /* XG_TEST_*                                 */
+  double tol;
+  int max_iter;
+  int load_const;
+} xg_phase_desc;
+
+/* per-step statistics written by xg_analyze */
+typedef struct xg_step_stats {
+  int newton_iters;             /* Newton iterations of the step             */
+  int solver_iters;             /* total PCG iterations of the step          */
+  int elem_iters;               /* total element (compatibility) iterations  */
+  int status;                   /* 0 ok, < 0 XG_E*                           */
+} xg_step_stats;
+
+typedef struct xg_model xg_model;   /* opaque handle */
+
+const char *xg_last_error(void);
+int xg_version(void);
+
+/* ------------------------------------------------------------------------ */
+/* Domain + handler + numberer (analysis/handler/PlainHandler.cpp:60-260,   */
+/* analysis/numberer/DOF_Numberer.cpp:93-205, graph/numberer/RCM.cpp:67-277,*/
+/* analysis/model/AnalysisModel.cpp:286-400) and the device element set.     */
+/* ------------------------------------------------------------------------ */
+
+/* Build the device model: SoA element/material store, DOF numbering, the
+   sparsity pattern and the element-to-slot map.  Replaces
+   BasicAnalysisBuilder::domainChanged (runtime/runtime/BasicAnalysisBuilder.cpp:225-300). */
+int xg_model_create(const xg_model_desc *desc, xg_model **out);
+int xg_model_destroy(xg_model *m);
+
+/* Number of equations and scalar non-zeros of the system (the CSR/CSC
+   pattern of sparseGEN/SparseGenColLinSOE.cpp:161-261, symmetric). */
+int xg_model_sizes(const xg_model *m, int *num_eqn, int *nnz);
+
+/* Equation number of every (node, dof) as DOF_Group::getID() holds it after
+   numbering: >= 0 equation, -1 constrained.  eqn[num_nodes*ndf]. */
+int xg_model_numbering(const xg_model *m, int *eqn);
+
+/* Scalar CSR pattern in equation order: rowptr[num_eqn+1], colidx[nnz],
+   columns ascending within a row (identical to the reference's CSC since
+   the pattern is symmetric). */
+int xg_model_pattern(const xg_model *m, int *rowptr, int *colidx);
+
+/* ---- element set: Element::update / getTangentStiff / getResistingForce,
+        commitState / revertToLastCommit (element/Element.h:51-103) ---- */
+
+/* Copy trial nodal displacements (host, [num_nodes*ndf]) to the device. */
+int xg_elemset_set_trial_disp(xg_model *m, const double *u);
+
+/* Domain::update (domain/domain/Domain.cpp:1988-2006): state determination
+   of every element from its committed state and the trial displacements,
+   then deterministic assembly of the tangent and the resisting force.
+   csr_vals[nnz] (may be NULL) receives the assembled tangent in the order
+   of xg_model_pattern; resid[num_eqn] (may be NULL) receives the assembled
+   resisting force P_int (no external load).  Returns the number of
+   elements whose state determination failed as a negative code. */
+int xg_elemset_update(xg_model *m, double *csr_vals, double *resid);
+
+int xg_elemset_commit(xg_model *m);             /* Domain::commit          */
+int xg_elemset_revert(xg_model *m);             /* revertToLastCommit      */
+int xg_elemset_revert_to_start(xg_model *m);    /* revertToStart           */
+
+/* Committed material history, SoA, for checkpoints and tests.
+   which = 0: J2 plastic strain (ncomp x nip) + xi; 1: fiber uniaxial state.
+   Writes at most cap doubles, returns the count written (or < 0). */
+int xg_elemset_get_history(const xg_model *m, int which, double *out, long cap);
+int xg_elemset_set_history(xg_model *m, int which, const double *in, long n);
+
+/* ---- LinearSOE (system_of_eqn/linearSOE/LinearSOE.h) on the model's
+        pattern: block-Jacobi PCG on the device ---- */
+
+/* Solve K x = b with the tangent assembled by the last xg_elemset_update.
+   b, x are host arrays [num_eqn].  Returns XG_ESOLVE on breakdown or when
+   maxit is reached; iters/relres report the final state. */
+int xg_soe_solve(xg_model *m, const double *b, double *x,
+                 double rtol, int maxit, int *iters, double *relres);
+
+/* ---- NewtonRaphson::solveCurrentStep (analysis/algorithm/equiSolnAlgo/
+        NewtonRaphson.cpp:125-222) with its integrator and convergence test,
+        all resident on the device ---- */
+int xg_analysis_set_phase(xg_model *m, const xg_phase_desc *ph);
+int xg_analysis_set_solver(xg_model *m, double rtol, int maxit);
+/* Run num_steps steps of the current phase; stats[num_steps] may be NULL. */
+int xg_analyze(xg_model *m, int num_steps, xg_step_stats *stats);
+/* Committed nodal displacements [num_nodes*ndf] and the load factor. */
+int xg_get_disp(const xg_model *m, double *u, double *lambda);
+/* Reset displacements, time and material state to the start. */
+int xg_reset(xg_model *m);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* XARA_GPU_H */

@@ -1,0 +1,107 @@
+"""ctypes binding of ``oracle/_ref/libxara_ref.so`` (test infrastructure).
+
+The library holds the reference's own CPU classes compiled from its sources
+(``build_ref.py``) plus the harness in ``ref_harness.cpp``.  It exists only
+in the container that has the reference sources; GPU tests use the fixtures
+generated from it (``tests/golden/make_golden.py``) and the C restatement in
+``xara_oracle.c``.
+"""
+import ctypes as C
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB = os.path.join(HERE, "_ref", "libxara_ref.so")
+
+_lib = None
+
+
+def available():
+    return os.path.exists(LIB)
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        _lib = C.CDLL(LIB)
+        _lib.xref_create.restype = C.c_void_p
+        _lib.xref_create.argtypes = [C.c_void_p]
+        _lib.xref_destroy.argtypes = [C.c_void_p]
+        _lib.xref_run_phase.argtypes = [C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_int,
+                                        C.c_void_p, C.c_void_p, C.c_void_p]
+        _lib.xref_numbering.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]
+        _lib.xref_pattern.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p]
+        _lib.xref_num_captured.argtypes = [C.c_void_p]
+        _lib.xref_captured.argtypes = [C.c_void_p] + [C.c_void_p] * 6
+        _lib.xref_times.argtypes = [C.c_void_p] + [C.c_void_p] * 3
+        _lib.xref_j2_path.argtypes = [C.c_int, C.c_void_p, C.c_int, C.c_void_p, C.c_void_p,
+                                      C.c_void_p, C.c_void_p]
+    return _lib
+
+
+def _p(a):
+    return None if a is None else a.ctypes.data_as(C.c_void_p)
+
+
+class RefRun:
+    """Run a model through the reference's analysis loop and keep the record."""
+
+    def __init__(self, desc, phases, capture=(0, 0), cap_solves=0):
+        L = lib()
+        self.desc = desc
+        self._s = desc.struct()
+        self.h = L.xref_create(C.byref(self._s))
+        if not self.h:
+            raise RuntimeError("xref_create failed")
+        nu = desc.num_nodes * desc.ndf
+        self.step_u, self.step_lambda, self.step_iters = [], [], []
+        for ph in phases:
+            n = ph.num_steps
+            su = np.zeros((n, nu))
+            sl = np.zeros(n)
+            si = np.zeros(n, np.int32)
+            ps = ph.struct()
+            r = L.xref_run_phase(self.h, C.byref(ps), capture[0], capture[1], cap_solves,
+                                 _p(su), _p(sl), _p(si))
+            if r != 0:
+                raise RuntimeError(f"reference analysis failed: {r}")
+            self.step_u.append(su)
+            self.step_lambda.append(sl)
+            self.step_iters.append(si)
+        self.step_u = np.concatenate(self.step_u)
+        self.step_lambda = np.concatenate(self.step_lambda)
+        self.step_iters = np.concatenate(self.step_iters)
+        eqn = np.zeros(nu, np.int32)
+        neq, nnz = C.c_int(), C.c_int()
+        L.xref_numbering(self.h, _p(eqn), C.byref(neq), C.byref(nnz))
+        self.eqn, self.neq, self.nnz = eqn, neq.value, nnz.value
+        self.colstart = np.zeros(self.neq + 1, np.int32)
+        self.rowidx = np.zeros(self.nnz, np.int32)
+        L.xref_pattern(self.h, _p(self.colstart), _p(self.rowidx))
+        ns = L.xref_num_captured(self.h)
+        self.cap_step = np.zeros(ns, np.int32)
+        self.cap_iter = np.zeros(ns, np.int32)
+        self.cap_B = np.zeros((ns, self.neq))
+        self.cap_A = np.zeros((ns, self.nnz))
+        self.cap_X = np.zeros((ns, self.neq))
+        self.cap_U = np.zeros((ns, nu))
+        L.xref_captured(self.h, _p(self.cap_step), _p(self.cap_iter), _p(self.cap_B),
+                        _p(self.cap_A), _p(self.cap_X), _p(self.cap_U))
+        e, s, t = C.c_double(), C.c_double(), C.c_double()
+        L.xref_times(self.h, C.byref(e), C.byref(s), C.byref(t))
+        self.elem_seconds, self.solve_seconds, self.step_seconds = e.value, s.value, t.value
+
+
+def j2_path(dim, param, strain, commit):
+    """Stress and tangent of J2PlaneStrain (dim=2) / J2ThreeDimensional (dim=3)."""
+    L = lib()
+    ns = 3 if dim == 2 else 6
+    strain = np.ascontiguousarray(strain, np.float64).reshape(-1, ns)
+    npts = strain.shape[0]
+    commit = np.ascontiguousarray(commit, np.int32)
+    param = np.ascontiguousarray(param, np.float64)
+    stress = np.zeros((npts, ns))
+    tang = np.zeros((npts, ns, ns))
+    L.xref_j2_path(dim, _p(param), npts, _p(strain), _p(commit), _p(stress), _p(tang))
+    return stress, tang

@@ -1,0 +1,486 @@
+// ref_harness.cpp -- test infrastructure, never part of the product.
+//
+// Builds a model with the reference's own C++ classes (compiled unchanged
+// from its SRC/ tree by build_ref.py) from the flat xg_model_desc used by
+// libxara_gpu.so, runs the reference's analysis loop and records, for every
+// linear solve, the assembled right-hand side, the tangent values on the
+// SparseGenColLinSOE pattern, the solution and the nodal trial
+// displacements at that moment.  Model construction follows the reference's
+// C++ unit-test pattern (tests/Other/UnitTests/Example1/main.cpp); the
+// analysis objects are wired as BasicAnalysisBuilder::setLinks does
+// (runtime/runtime/BasicAnalysisBuilder.cpp:134-180) and each step runs as in
+// BasicAnalysisBuilder::analyzeStatic / analyzeTransient (:337-520).
+#include <chrono>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <vector>
+#include <array>
+
+#include <OPS_Globals.h>
+#include <StandardStream.h>
+#include <DummyStream.h>
+
+#include <Domain.h>
+#include <Node.h>
+#include <SP_Constraint.h>
+#include <MP_Constraint.h>
+#include <LoadPattern.h>
+#include <LinearSeries.h>
+#include <NodalLoad.h>
+
+#include <FourNodeQuad.h>
+#include <Brick.h>
+#include <J2PlaneStrain.h>
+#include <J2ThreeDimensional.h>
+
+#include <AnalysisModel.h>
+#include <PlainHandler.h>
+#include <TransformationConstraintHandler.h>
+#include <DOF_Numberer.h>
+#include <RCM.h>
+#include <LoadControl.h>
+#include <DisplacementControl.h>
+#include <NewtonRaphson.h>
+#include <CTestNormDispIncr.h>
+#include <CTestNormUnbalance.h>
+#include <LinearSOE.h>
+#include <ProfileSPDLinSOE.h>
+#include <ProfileSPDLinDirectSolver.h>
+#include <SparseGenColLinSOE.h>
+#include <SparseGenColLinSolver.h>
+#include <Graph.h>
+#include <DOF_Group.h>
+#include <Vector.h>
+#include <Matrix.h>
+#include <ID.h>
+
+#include "../include/xara_gpu.h"
+
+// Globals that the reference's Tcl runtime normally defines
+// (SRC/logging/logging.cpp needs tcl.h, so they are defined here).
+static StandardStream ref_sserr;
+static DummyStream ref_ssnul;
+OPS_Stream *opserrPtr = &ref_ssnul;
+OPS_Stream *opsdbgPtr = &ref_ssnul;
+OPS_Stream *opslogPtr = &ref_ssnul;
+OPS_Stream *opswrnPtr = &ref_ssnul;
+OPS_Stream *opsmrdPtr = &ref_ssnul;
+
+namespace {
+
+using clk = std::chrono::steady_clock;
+
+// SparseGenColLinSOE with its CSC storage readable by the harness.
+class NoSolve : public SparseGenColLinSolver {
+ public:
+  NoSolve() : SparseGenColLinSolver(0) {}
+  int solve() override { return 0; }
+  int setSize() override { return 0; }
+  int sendSelf(int, Channel &) override { return 0; }
+  int recvSelf(int, Channel &, FEM_ObjectBroker &) override { return 0; }
+};
+
+class GenAccess : public SparseGenColLinSOE {
+ public:
+  explicit GenAccess(SparseGenColLinSolver &s) : SparseGenColLinSOE(s) {}
+  int n() const { return size; }
+  int nz() const { return nnz; }
+  const double *a() const { return A; }
+  const int *rows() const { return rowA; }
+  const int *colStart() const { return colStartA; }
+};
+
+struct Capture {
+  int enabled = 0;
+  int cap = 0;
+  int count = 0;
+  int step = 0;       // global step index
+  int iter = 0;       // solve index within the step
+  std::vector<int> stepOf, iterOf;
+  std::vector<double> B, A, X, U;
+};
+
+struct Harness;
+
+// LinearSOE that forwards every call to a ProfileSPDLinSOE (the reference
+// default system, BasicAnalysisBuilder.cpp:820) for solving and to a
+// SparseGenColLinSOE for the pattern and the tangent values.
+class CaptureSOE : public LinearSOE {
+ public:
+  CaptureSOE(Harness *h)
+      : LinearSOE(0), h_(h), gen_(nosolve_),
+        prof_(*(new ProfileSPDLinDirectSolver())) {}
+  int setLinks(AnalysisModel &m) override {
+    LinearSOE::setLinks(m);
+    gen_.setLinks(m);
+    prof_.setLinks(m);
+    return 0;
+  }
+  int setSize(Graph &g) override {
+    int r = gen_.setSize(g);
+    if (r < 0) return r;
+    return prof_.setSize(g);
+  }
+  int getNumEqn() const override { return prof_.getNumEqn(); }
+  int addA(const Matrix &m, const ID &id, double f) override {
+    gen_.addA(m, id, f);
+    return prof_.addA(m, id, f);
+  }
+  int addB(const Vector &v, const ID &id, double f) override {
+    gen_.addB(v, id, f);
+    return prof_.addB(v, id, f);
+  }
+  int setB(const Vector &v, double f) override {
+    gen_.setB(v, f);
+    return prof_.setB(v, f);
+  }
+  void zeroA() override { gen_.zeroA(); prof_.zeroA(); }
+  void zeroB() override { gen_.zeroB(); prof_.zeroB(); }
+  const Vector &getX() override { return prof_.getX(); }
+  const Vector &getB() override { return prof_.getB(); }
+  double normRHS() override { return prof_.normRHS(); }
+  void setX(int loc, double v) override { prof_.setX(loc, v); }
+  void setX(const Vector &x) override { prof_.setX(x); }
+  int solve() override;
+  int sendSelf(int, Channel &) override { return 0; }
+  int recvSelf(int, Channel &, FEM_ObjectBroker &) override { return 0; }
+
+  GenAccess &gen() { return gen_; }
+  double solveSeconds = 0.0;
+
+ private:
+  Harness *h_;
+  NoSolve nosolve_;
+  GenAccess gen_;
+  ProfileSPDLinSOE prof_;
+};
+
+struct Harness {
+  xg_model_desc d{};
+  Domain *domain = nullptr;
+  std::vector<Node *> nodes;
+  AnalysisModel *model = nullptr;
+  ConstraintHandler *handler = nullptr;
+  DOF_Numberer *numberer = nullptr;
+  CaptureSOE *soe = nullptr;
+  Capture cap;
+  int numbered = 0;
+  int totalSteps = 0;
+  double elemSeconds = 0.0, stepSeconds = 0.0;
+  std::vector<LoadPattern *> patterns;
+
+  void snapshotU(double *out) {
+    int ndf = d.ndf;
+    for (size_t i = 0; i < nodes.size(); i++) {
+      const Vector &u = nodes[i]->getTrialDisp();
+      for (int j = 0; j < ndf; j++) out[i * ndf + j] = u(j);
+    }
+  }
+};
+
+int CaptureSOE::solve() {
+  Capture &c = h_->cap;
+  if (c.enabled && c.count < c.cap) {
+    int n = gen_.n(), nz = gen_.nz();
+    int nu = h_->d.num_nodes * h_->d.ndf;
+    c.stepOf.push_back(c.step);
+    c.iterOf.push_back(c.iter);
+    const Vector &b = prof_.getB();
+    for (int i = 0; i < n; i++) c.B.push_back(b(i));
+    c.A.insert(c.A.end(), gen_.a(), gen_.a() + nz);
+    size_t off = c.U.size();
+    c.U.resize(off + nu);
+    h_->snapshotU(&c.U[off]);
+  }
+  auto t0 = clk::now();
+  int r = prof_.solve();
+  solveSeconds += std::chrono::duration<double>(clk::now() - t0).count();
+  if (c.enabled && c.count < c.cap) {
+    const Vector &x = prof_.getX();
+    for (int i = 0; i < gen_.n(); i++) c.X.push_back(x(i));
+    c.count++;
+  }
+  c.iter++;
+  return r;
+}
+
+int nen_of(int type) {
+  switch (type) {
+    case XG_ELE_QUAD: return 4;
+    case XG_ELE_BRICK: return 8;
+    default: return 2;
+  }
+}
+
+}  // namespace
+
+extern "C" {
+
+int xref_version(void) { return 1; }
+
+// Build the reference Domain for a model description.
+void *xref_create(const xg_model_desc *desc) {
+  Harness *h = new Harness();
+  h->d = *desc;
+  const xg_model_desc &d = *desc;
+  h->domain = new Domain();
+  Domain *dom = h->domain;
+  for (int i = 0; i < d.num_nodes; i++) {
+    const double *x = d.node_crd + (size_t)i * d.ndm;
+    Node *n = nullptr;
+    if (d.ndm == 2)
+      n = new Node(d.node_tag[i], d.ndf, x[0], x[1]);
+    else
+      n = new Node(d.node_tag[i], d.ndf, x[0], x[1], x[2]);
+    dom->addNode(n);
+    h->nodes.push_back(n);
+  }
+  int nen = nen_of(d.elem_type);
+  for (int e = 0; e < d.num_elems; e++) {
+    const int *c = d.elem_conn + (size_t)e * nen;
+    const double *p = d.j2_param + (size_t)d.elem_mat[e] * XG_J2_NPARAM;
+    Element *ele = nullptr;
+    if (d.elem_type == XG_ELE_QUAD) {
+      J2PlaneStrain mat(1, p[0], p[1], p[2], p[3], p[4], p[5], p[6], p[7]);
+      std::array<int, 4> nd{c[0], c[1], c[2], c[3]};
+      ele = new FourNodeQuad(d.elem_tag[e], nd, mat, d.thickness, 0.0, 0.0, 0.0, 0.0);
+    } else if (d.elem_type == XG_ELE_BRICK) {
+      J2ThreeDimensional mat(1, p[0], p[1], p[2], p[3], p[4], p[5], p[6], p[7]);
+      ele = new Brick(d.elem_tag[e], c[0], c[1], c[2], c[3], c[4], c[5], c[6], c[7], mat);
+    } else {
+      fprintf(stderr, "xref_create: element type %d not supported by the harness\n", d.elem_type);
+      return nullptr;
+    }
+    dom->addElement(ele);
+  }
+  // constraints: homogeneous fixes in the domain, imposed values in patterns
+  int maxPat = -1;
+  for (int i = 0; i < d.num_sp; i++) maxPat = std::max(maxPat, d.sp_pattern[i]);
+  for (int i = 0; i < d.num_loads; i++) maxPat = std::max(maxPat, d.load_pattern[i]);
+  for (int p = 0; p <= maxPat; p++) h->patterns.push_back(nullptr);
+  for (int i = 0; i < d.num_sp; i++) {
+    if (d.sp_pattern[i] < 0) {
+      SP_Constraint *sp = new SP_Constraint(d.sp_node[i], d.sp_dof[i], 0.0, true);
+      dom->addSP_Constraint(sp);
+    }
+  }
+  // equalDOF: MP_Constraint with an identity 1x1 constraint matrix
+  for (int i = 0; i < d.num_mp; i++) {
+    Matrix Ccr(1, 1);
+    Ccr(0, 0) = 1.0;
+    ID cdof(1), rdof(1);
+    cdof(0) = d.mp_dof[i];
+    rdof(0) = d.mp_dof[i];
+    MP_Constraint *mp = new MP_Constraint(d.mp_retained[i], d.mp_constrained[i], Ccr, cdof, rdof);
+    dom->addMP_Constraint(mp);
+  }
+  return h;
+}
+
+void xref_destroy(void *hp) {
+  Harness *h = (Harness *)hp;
+  if (!h) return;
+  // The reference Domain owns a large object graph whose destructors reach
+  // code the harness does not link; the process exits soon after, so the
+  // objects are left to it.
+  delete h;
+}
+
+// Add load pattern p (its nodal loads and imposed SP values) to the domain.
+static void add_pattern(Harness *h, int p) {
+  const xg_model_desc &d = h->d;
+  if (p < 0 || p >= (int)h->patterns.size() || h->patterns[p] != nullptr) return;
+  LoadPattern *lp = new LoadPattern(p + 1);
+  lp->setTimeSeries(new LinearSeries());
+  h->domain->addLoadPattern(lp);
+  h->patterns[p] = lp;
+  int tag = 1000000 * (p + 1);
+  for (int i = 0; i < d.num_sp; i++) {
+    if (d.sp_pattern[i] == p) {
+      SP_Constraint *sp = new SP_Constraint(d.sp_node[i], d.sp_dof[i], d.sp_value[i], false);
+      h->domain->addSP_Constraint(sp, p + 1);
+    }
+  }
+  for (int i = 0; i < d.num_loads; i++) {
+    if (d.load_pattern[i] == p) {
+      Vector v(d.ndf);
+      for (int j = 0; j < d.ndf; j++) v(j) = d.load_value[(size_t)i * d.ndf + j];
+      NodalLoad *nl = new NodalLoad(tag++, d.load_node[i], v);
+      h->domain->addNodalLoad(nl, p + 1);
+    }
+  }
+}
+
+// Run one phase of the analysis.  Steps whose global index lies in
+// [cap_begin, cap_end) have every solve captured (up to cap_solves solves).
+// step_u[num_steps*num_nodes*ndf], step_lambda[num_steps] and
+// step_iters[num_steps] receive the committed state after each step.
+int xref_run_phase(void *hp, const xg_phase_desc *ph, int cap_begin, int cap_end,
+                   int cap_solves, double *step_u, double *step_lambda, int *step_iters) {
+  Harness *h = (Harness *)hp;
+  const xg_model_desc &d = h->d;
+  add_pattern(h, ph->pattern);
+
+  ConvergenceTest *test = nullptr;
+  if (ph->test == XG_TEST_NORM_DISP_INCR)
+    test = new CTestNormDispIncr(ph->tol, ph->max_iter, 0);
+  else
+    test = new CTestNormUnbalance(ph->tol, ph->max_iter, 0);
+  NewtonRaphson *algo = new NewtonRaphson(*test);
+  StaticIntegrator *integ = nullptr;
+  if (ph->integrator == XG_INT_LOAD_CONTROL)
+    integ = new LoadControl(ph->d_lambda, 1, ph->d_lambda, ph->d_lambda);
+  else if (ph->integrator == XG_INT_DISP_CONTROL)
+    integ = new DisplacementControl(ph->dc_node, ph->dc_dof, ph->dc_incr, h->domain, 1,
+                                    ph->dc_incr, ph->dc_incr);
+  else {
+    fprintf(stderr, "xref_run_phase: integrator %d not supported\n", ph->integrator);
+    return -1;
+  }
+
+  if (!h->model) {
+    h->model = new AnalysisModel();
+    if (d.handler == XG_HANDLER_TRANSFORMATION)
+      h->handler = new TransformationConstraintHandler();
+    else
+      h->handler = new PlainHandler();
+    h->numberer = new DOF_Numberer(*(new RCM(false)));
+    h->soe = new CaptureSOE(h);
+  }
+  // wiring as BasicAnalysisBuilder::setLinks(STATIC_ANALYSIS)
+  h->soe->setLinks(*h->model);
+  h->model->setLinks(*h->domain, *h->handler);
+  h->numberer->setLinks(*h->model);
+  h->handler->setLinks(*h->domain, *h->model, *integ);
+  algo->setLinks(*h->model, *integ, *h->soe, test);
+  integ->setLinks(*h->model, *h->soe, test);
+
+  // domainChanged (BasicAnalysisBuilder.cpp:225-300)
+  h->model->clearAll();
+  h->handler->clearAll();
+  if (h->handler->handle() < 0) return -2;
+  if (h->numberer->numberDOF() < 0) return -3;
+  if (h->handler->doneNumberingDOF() < 0) return -3;
+  Graph &g = h->model->getDOFGraph();
+  if (h->soe->setSize(g) < 0) return -4;
+  h->model->clearDOFGraph();
+  if (integ->domainChanged() < 0) return -5;
+  h->numbered = 1;
+
+  int nu = d.num_nodes * d.ndf;
+  Capture &c = h->cap;
+  c.cap = cap_solves;
+  for (int s = 0; s < ph->num_steps; s++) {
+    int gstep = h->totalSteps;
+    c.enabled = (gstep >= cap_begin && gstep < cap_end);
+    c.step = gstep;
+    c.iter = 0;
+    auto t0 = clk::now();
+    double solve0 = h->soe->solveSeconds;
+    if (integ->newStep() < 0) return -10 - s;
+    int r = algo->solveCurrentStep();
+    if (r < 0) {
+      fprintf(stderr, "xref_run_phase: step %d failed (%d)\n", gstep, r);
+      return -1000 - s;
+    }
+    if (integ->commit() < 0) return -20;
+    double dt = std::chrono::duration<double>(clk::now() - t0).count();
+    h->stepSeconds += dt;
+    h->elemSeconds += dt - (h->soe->solveSeconds - solve0);
+    if (step_u) {
+      for (int i = 0; i < d.num_nodes; i++) {
+        const Vector &u = h->nodes[i]->getDisp();
+        for (int j = 0; j < d.ndf; j++) step_u[(size_t)s * nu + i * d.ndf + j] = u(j);
+      }
+    }
+    if (step_lambda) step_lambda[s] = h->domain->getCurrentTime();
+    if (step_iters) step_iters[s] = algo->getNumIterations();
+    h->totalSteps++;
+  }
+  if (ph->load_const) {
+    h->domain->setLoadConstant();
+    h->domain->setCurrentTime(0.0);
+    h->domain->setCommittedTime(0.0);
+  }
+  return 0;
+}
+
+// Equation numbers per (node, dof) after the first phase was set up.
+int xref_numbering(void *hp, int *eqn, int *num_eqn, int *nnz) {
+  Harness *h = (Harness *)hp;
+  if (!h->numbered) return -1;
+  int ndf = h->d.ndf;
+  for (size_t i = 0; i < h->nodes.size(); i++) {
+    DOF_Group *g = h->nodes[i]->getDOF_GroupPtr();
+    const ID &id = g->getID();
+    for (int j = 0; j < ndf; j++) eqn[i * ndf + j] = (j < id.Size()) ? id(j) : -1;
+    // TransformationDOF_Group keeps a reduced ID; map it back per dof
+    if (id.Size() != ndf) {
+      for (int j = 0; j < ndf; j++) eqn[i * ndf + j] = -1;
+    }
+  }
+  *num_eqn = h->soe->gen().n();
+  *nnz = h->soe->gen().nz();
+  return 0;
+}
+
+int xref_pattern(void *hp, int *colstart, int *rowidx) {
+  Harness *h = (Harness *)hp;
+  GenAccess &g = h->soe->gen();
+  memcpy(colstart, g.colStart(), sizeof(int) * (g.n() + 1));
+  memcpy(rowidx, g.rows(), sizeof(int) * g.nz());
+  return 0;
+}
+
+int xref_num_captured(void *hp) { return ((Harness *)hp)->cap.count; }
+
+int xref_captured(void *hp, int *step, int *iter, double *B, double *A, double *X, double *U) {
+  Capture &c = ((Harness *)hp)->cap;
+  int n = c.count;
+  if (step) memcpy(step, c.stepOf.data(), sizeof(int) * n);
+  if (iter) memcpy(iter, c.iterOf.data(), sizeof(int) * n);
+  if (B) memcpy(B, c.B.data(), sizeof(double) * c.B.size());
+  if (A) memcpy(A, c.A.data(), sizeof(double) * c.A.size());
+  if (X) memcpy(X, c.X.data(), sizeof(double) * c.X.size());
+  if (U) memcpy(U, c.U.data(), sizeof(double) * c.U.size());
+  return n;
+}
+
+void xref_times(void *hp, double *elem_s, double *solve_s, double *step_s) {
+  Harness *h = (Harness *)hp;
+  *elem_s = h->elemSeconds;
+  *solve_s = h->soe->solveSeconds;
+  *step_s = h->stepSeconds;
+}
+
+// Material-point driver: J2 plane strain (dim 2) or 3D (dim 3) through a
+// strain path; commit[k] != 0 commits after point k.  stress/tangent out:
+// [npts*nstress], [npts*nstress*nstress].
+int xref_j2_path(int dim, const double *param, int npts, const double *strain,
+                 const int *commit, double *stress, double *tangent) {
+  NDMaterial *m;
+  int ns;
+  if (dim == 2) {
+    m = new J2PlaneStrain(1, param[0], param[1], param[2], param[3], param[4], param[5], param[6], param[7]);
+    ns = 3;
+  } else {
+    m = new J2ThreeDimensional(1, param[0], param[1], param[2], param[3], param[4], param[5], param[6], param[7]);
+    ns = 6;
+  }
+  Vector eps(ns);
+  for (int k = 0; k < npts; k++) {
+    for (int i = 0; i < ns; i++) eps(i) = strain[k * ns + i];
+    m->setTrialStrain(eps);
+    const Vector &s = m->getStress();
+    const Matrix &t = m->getTangent();
+    for (int i = 0; i < ns; i++) stress[k * ns + i] = s(i);
+    for (int i = 0; i < ns; i++)
+      for (int j = 0; j < ns; j++) tangent[(k * ns + i) * ns + j] = t(i, j);
+    if (commit[k]) m->commitState();
+  }
+  delete m;
+  return 0;
+}
+
+}  // extern "C"
