@@ -192,6 +192,13 @@ int xg_version(void);
 int xg_model_create(const xg_model_desc *desc, xg_model **out);
 int xg_model_destroy(xg_model *m);
 
+/* Host-only planning (no device work): the equation number of every
+   (node, dof) and the scalar CSR pattern, exactly as DOF_Numberer::numberDOF
+   and SparseGenColLinSOE::setSize produce them.  Any output may be NULL;
+   call once with NULL arrays to learn num_eqn and nnz. */
+int xg_model_plan(const xg_model_desc *desc, int *eqn, int *rowptr, int *colidx,
+                  int *num_eqn, int *nnz);
+
 /* Number of equations and scalar non-zeros of the system (the CSR/CSC
    pattern of sparseGEN/SparseGenColLinSOE.cpp:161-261, symmetric). */
 int xg_model_sizes(const xg_model *m, int *num_eqn, int *nnz);

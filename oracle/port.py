@@ -19,7 +19,14 @@ _lib = None
 
 def build(force=False):
     """Compile the oracle with gcc (seconds); used by __graft_entry__.build()."""
-    if not force and os.path.exists(LIB) and os.path.getmtime(LIB) >= os.path.getmtime(SRC):
+    import platform
+    machine = {"x86_64": 62, "aarch64": 183}.get(platform.machine(), -1)
+    same_arch = False
+    if os.path.exists(LIB):
+        with open(LIB, "rb") as f:
+            head = f.read(20)
+        same_arch = head[:4] == b"\x7fELF" and int.from_bytes(head[18:20], "little") == machine
+    if not force and same_arch and os.path.getmtime(LIB) >= os.path.getmtime(SRC):
         return LIB
     tmp = LIB + ".tmp"
     subprocess.run(["gcc", "-O2", "-fPIC", "-shared", "-std=c11", "-ffp-contract=off",

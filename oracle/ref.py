@@ -88,6 +88,9 @@ class RefRun:
         self.cap_U = np.zeros((ns, nu))
         L.xref_captured(self.h, _p(self.cap_step), _p(self.cap_iter), _p(self.cap_B),
                         _p(self.cap_A), _p(self.cap_X), _p(self.cap_U))
+        self.cap_lambda = np.zeros(ns)
+        L.xref_captured_lambda.argtypes = [C.c_void_p, C.c_void_p]
+        L.xref_captured_lambda(self.h, _p(self.cap_lambda))
         e, s, t = C.c_double(), C.c_double(), C.c_double()
         L.xref_times(self.h, C.byref(e), C.byref(s), C.byref(t))
         self.elem_seconds, self.solve_seconds, self.step_seconds = e.value, s.value, t.value

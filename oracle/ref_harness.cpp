@@ -98,7 +98,7 @@ struct Capture {
   int step = 0;       // global step index
   int iter = 0;       // solve index within the step
   std::vector<int> stepOf, iterOf;
-  std::vector<double> B, A, X, U;
+  std::vector<double> B, A, X, U, lam;
 };
 
 struct Harness;
@@ -186,6 +186,7 @@ int CaptureSOE::solve() {
     int nu = h_->d.num_nodes * h_->d.ndf;
     c.stepOf.push_back(c.step);
     c.iterOf.push_back(c.iter);
+    c.lam.push_back(h_->domain->getCurrentTime());
     const Vector &b = prof_.getB();
     for (int i = 0; i < n; i++) c.B.push_back(b(i));
     c.A.insert(c.A.end(), gen_.a(), gen_.a() + nz);
@@ -484,3 +485,10 @@ int xref_j2_path(int dim, const double *param, int npts, const double *strain,
 }
 
 }  // extern "C"
+
+// Domain time (the load factor of LinearSeries patterns) at every captured solve.
+extern "C" int xref_captured_lambda(void *hp, double *lam) {
+  Capture &c = ((Harness *)hp)->cap;
+  memcpy(lam, c.lam.data(), sizeof(double) * c.lam.size());
+  return (int)c.lam.size();
+}

@@ -1,0 +1,97 @@
+"""Generate the golden fixtures in this folder from the reference itself.
+
+Runs in the container that holds the reference sources: it needs
+``oracle/_ref/libxara_ref.so`` (``python oracle/build_ref.py``), i.e. the
+reference's own CPU classes (J2Plasticity, FourNodeQuad, Brick, Domain,
+PlainHandler, RCM, DOF_Numberer, SparseGenColLinSOE, ProfileSPD,
+NewtonRaphson, DisplacementControl, ...) compiled from source.  The GPU machine
+has no reference; tests there read these fixtures.
+
+Usage: python tests/golden/make_golden.py
+"""
+import os
+import sys
+
+import numpy as np
+
+ROOT = os.path.abspath(os.path.join(os.path.dirname(__file__), "..", ".."))
+sys.path.insert(0, ROOT)
+
+from oracle import port, ref  # noqa: E402
+from xara_gb300 import configs  # noqa: E402
+from xara_gb300._abi import PhaseDesc  # noqa: E402
+
+OUT = os.path.dirname(os.path.abspath(__file__))
+
+
+def save(name, **arrays):
+    path = os.path.join(OUT, name + ".npz")
+    np.savez_compressed(path, **arrays)
+    print(f"{name}.npz: {os.path.getsize(path) / 1024:.0f} KB")
+
+
+def j2_paths(seed=1):
+    """Random strain paths through J2PlaneStrain / J2ThreeDimensional."""
+    rng = np.random.default_rng(seed)
+    out = {}
+    for dim, ns in ((2, 3), (3, 6)):
+        n = 200
+        steps = rng.normal(0.0, 6e-4, size=(n, ns))
+        strain = np.cumsum(steps, axis=0)
+        commit = (rng.random(n) < 0.6).astype(np.int32)
+        param = np.array([166.7e9, 76.9e9, 250e6, 300e6, 8.0, 1e9, 0.0, 0.0])
+        s, t = ref.j2_path(dim, param, strain, commit)
+        out[f"d{dim}_param"] = param
+        out[f"d{dim}_strain"] = strain
+        out[f"d{dim}_commit"] = commit
+        out[f"d{dim}_stress"] = s
+        out[f"d{dim}_tangent"] = t
+    save("j2_paths", **out)
+
+
+def model_fixture(name, builder, args, kw, capture_steps=(), cap_solves=400):
+    desc, phases = builder(*args, **kw)
+    lo = min(capture_steps) if capture_steps else 0
+    hi = max(capture_steps) + 1 if capture_steps else 0
+    r = ref.RefRun(desc, phases, capture=(lo, hi), cap_solves=cap_solves)
+    keep = np.isin(r.cap_step, np.asarray(capture_steps, np.int32))
+    arrays = dict(
+        builder=np.array(builder.__name__), args=np.asarray(args),
+        kw_keys=np.array(list(kw.keys())), kw_vals=np.asarray(list(kw.values()), np.float64),
+        eqn=r.eqn, colstart=r.colstart, rowidx=r.rowidx,
+        step_u=r.step_u, step_lambda=r.step_lambda, step_iters=r.step_iters,
+    )
+    if capture_steps:
+        arrays.update(cap_step=r.cap_step[keep], cap_iter=r.cap_iter[keep],
+                      cap_B=r.cap_B[keep], cap_A=r.cap_A[keep], cap_U=r.cap_U[keep],
+                      cap_lambda=r.cap_lambda[keep])
+        # committed material history at the start of every captured step,
+        # from the oracle (itself pinned against the reference by these files)
+        nip = 4 if desc.elem_type == 1 else 8
+        hist_ep, hist_xi = [], []
+        for s in sorted(capture_steps):
+            o = port.OracleModel(desc)
+            if s > 0:
+                o.run([PhaseDesc(**{**phases[0].kw, "num_steps": s})])
+            ep, xi = o.history(nip)
+            o.close()
+            hist_ep.append(ep[:, [0, 4, 8, 1, 5, 6]])  # xx yy zz xy yz zx
+            hist_xi.append(xi)
+        arrays.update(hist_steps=np.asarray(sorted(capture_steps), np.int32),
+                      hist_ep=np.asarray(hist_ep), hist_xi=np.asarray(hist_xi))
+    save(name, **arrays)
+
+
+def main():
+    if not ref.available():
+        sys.exit("oracle/_ref/libxara_ref.so missing: run python oracle/build_ref.py")
+    j2_paths()
+    model_fixture("quad_8x4", configs.quad_block, (8, 4), {}, capture_steps=(0, 6))
+    model_fixture("quad_64x16", configs.quad_block, (64, 16), {})
+    model_fixture("brick_4x3x2", configs.brick_block, (4, 3, 2), {"steps": 5},
+                  capture_steps=(0, 2))
+    model_fixture("brick_8x8x4", configs.brick_block, (8, 8, 4), {"steps": 10})
+
+
+if __name__ == "__main__":
+    main()

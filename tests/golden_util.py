@@ -1,0 +1,76 @@
+"""Helpers shared by the tests: load a golden fixture and rebuild its model."""
+import os
+
+import numpy as np
+
+from xara_gb300 import configs
+
+GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+
+# tolerance for floating-point parity (relative, norm-wise per vector)
+RTOL_STATE = 1e-12      # resisting force / tangent values per iteration
+RTOL_HISTORY = 1e-8     # converged displacement histories
+
+
+def load(name):
+    z = np.load(os.path.join(GOLDEN, name + ".npz"), allow_pickle=False)
+    return {k: z[k] for k in z.files}
+
+
+def model_of(fx):
+    builder = getattr(configs, str(fx["builder"]))
+    args = tuple(int(a) for a in fx["args"])
+    kw = {str(k): (int(v) if float(v).is_integer() else float(v))
+          for k, v in zip(fx["kw_keys"], fx["kw_vals"])}
+    return builder(*args, **kw)
+
+
+def relerr(a, b):
+    a = np.asarray(a, np.float64).ravel()
+    b = np.asarray(b, np.float64).ravel()
+    den = np.linalg.norm(b)
+    return np.linalg.norm(a - b) / (den if den > 0 else 1.0)
+
+
+def unbalance_solves(fx, desc, phase):
+    """Indices of the captured solves whose right-hand side is the unbalance.
+
+    DisplacementControl solves phat once in newStep, then per iteration the
+    unbalance and phat (DisplacementControl.cpp:121-250): ordinal 0 and the
+    even ordinals are phat solves.
+    """
+    it = fx["cap_iter"]
+    if phase.integrator == 1:
+        return np.nonzero(it % 2 == 1)[0]
+    return np.arange(len(it))
+
+
+def external_load(fx, desc, k, eqn):
+    """F_ext of captured solve k: lambda times the pattern's reference loads."""
+    neq = len(fx["colstart"]) - 1
+    f = np.zeros(neq)
+    lam = fx["cap_lambda"][k]
+    if desc.load_node is None:
+        return f
+    for i, n in enumerate(desc.load_node):
+        idx = np.searchsorted(desc.node_tag, n)
+        for j in range(desc.ndf):
+            r = eqn[idx * desc.ndf + j]
+            if r >= 0:
+                f[r] += lam * desc.load_value[i * desc.ndf + j]
+    return f
+
+
+def csc_to_csr_values(fx, vals_csc):
+    """The pattern is symmetric, so CSC (column-major) of the reference and
+    CSR of this library share index arrays; the values of entry (r, c) sit at
+    the same position as those of (c, r).  Map CSC values to CSR order."""
+    cs, ri = fx["colstart"], fx["rowidx"]
+    n = len(cs) - 1
+    cols = np.repeat(np.arange(n), np.diff(cs)).astype(np.int64)
+    # CSC position p holds A[ri[p], cols[p]]; keys (col, row) ascend with p.
+    key_csc = cols * n + ri
+    # CSR position k (same index arrays) holds A[cols[k], ri[k]], which sits
+    # at the CSC position whose (col, row) key is (ri[k], cols[k]).
+    p = np.searchsorted(key_csc, ri.astype(np.int64) * n + cols)
+    return vals_csc[p]

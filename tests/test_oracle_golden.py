@@ -1,0 +1,64 @@
+"""The oracle (oracle/xara_oracle.c) against fixtures produced by the
+reference's own CPU classes (tests/golden/make_golden.py).  CPU only."""
+import numpy as np
+import pytest
+
+from oracle import port
+from golden_util import (RTOL_HISTORY, RTOL_STATE, csc_to_csr_values, external_load, load,
+                         model_of, relerr, unbalance_solves)
+
+MODELS = ["quad_8x4", "quad_64x16", "brick_4x3x2", "brick_8x8x4"]
+
+
+def test_j2_material_paths():
+    fx = load("j2_paths")
+    for dim in (2, 3):
+        s, t = port.j2_path(dim, fx[f"d{dim}_param"], fx[f"d{dim}_strain"], fx[f"d{dim}_commit"])
+        for k in range(len(s)):
+            assert relerr(s[k], fx[f"d{dim}_stress"][k]) < RTOL_STATE
+            assert relerr(t[k], fx[f"d{dim}_tangent"][k]) < RTOL_STATE
+
+
+@pytest.mark.parametrize("name", MODELS)
+def test_numbering_and_pattern_bit_exact(name):
+    fx = load(name)
+    desc, phases = model_of(fx)
+    o = port.OracleModel(desc)
+    assert np.array_equal(o.numbering(), fx["eqn"])
+    rp, ci = o.pattern()
+    assert np.array_equal(rp, fx["colstart"])
+    assert np.array_equal(ci, fx["rowidx"])
+
+
+@pytest.mark.parametrize("name", MODELS)
+def test_history(name):
+    fx = load(name)
+    desc, phases = model_of(fx)
+    o = port.OracleModel(desc)
+    U, lam, its = o.run(phases)
+    assert relerr(U, fx["step_u"]) < RTOL_HISTORY
+    assert relerr(lam, fx["step_lambda"]) < RTOL_HISTORY
+    assert np.array_equal(its, fx["step_iters"])
+
+
+@pytest.mark.parametrize("name", ["quad_8x4", "brick_4x3x2"])
+def test_replay_element_state(name):
+    """Resisting force and tangent of every captured Newton iteration."""
+    fx = load(name)
+    desc, phases = model_of(fx)
+    eqn = fx["eqn"]
+    for si, step in enumerate(fx["hist_steps"]):
+        o = port.OracleModel(desc)
+        ep = fx["hist_ep"][si]
+        full = np.zeros((ep.shape[0], 9))
+        full[:, [0, 4, 8, 1, 5, 6]] = ep
+        full[:, [3, 7, 2]] = ep[:, [3, 4, 5]]
+        o.set_history(full, fx["hist_xi"][si])
+        for k in unbalance_solves(fx, desc, phases[0]):
+            if fx["cap_step"][k] != step:
+                continue
+            vals, resid = o.elem_state(fx["cap_U"][k])
+            fext = external_load(fx, desc, k, eqn)
+            assert relerr(resid, fext - fx["cap_B"][k]) < RTOL_STATE
+            assert relerr(vals, csc_to_csr_values(fx, fx["cap_A"][k])) < RTOL_STATE
+        o.close()

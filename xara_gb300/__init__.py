@@ -1,0 +1,20 @@
+"""xara_gb300 -- GB300 implementation of the xara/OpenSees Newton-iteration hot path.
+
+The compute path is ``libxara_gpu.so`` (hand-written sm_103a CUDA behind a C
+ABI, ``include/xara_gpu.h``).  This package is the Python layer above it:
+
+* :mod:`xara_gb300._abi`   -- ctypes mirror of the C structs;
+* :mod:`xara_gb300.gpu`    -- the device model handle (element set, system,
+  Newton driver);
+* :mod:`xara_gb300.model`  -- the reference's modelling commands
+  (``node``, ``fix``, ``equalDOF``, ``element``, ``nDMaterial``, ``pattern``,
+  ``integrator``, ``test``, ``algorithm``, ``system``, ``analysis``,
+  ``analyze``) building a model for the device;
+* :mod:`xara_gb300.configs` -- seeded synthetic workloads.
+
+There is no CPU fallback: loading the package on a machine without the
+built library raises ``ImportError`` from :func:`xara_gb300.gpu.lib`.
+"""
+from ._abi import ModelDesc, PhaseDesc  # noqa: F401
+
+__all__ = ["ModelDesc", "PhaseDesc"]

@@ -1,0 +1,89 @@
+// xg_internal.h -- shared declarations of libxara_gpu.so (host C++ and CUDA).
+#pragma once
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <string>
+#include <vector>
+
+#include "../../include/xara_gpu.h"
+
+namespace xg {
+
+// ---------------------------------------------------------------------------
+// device views
+// ---------------------------------------------------------------------------
+
+// Continuum element set (quad / brick) with J2 plasticity at every point.
+struct ContinuumView {
+  int ne, nn, nen, nip, ndf, ndm;
+  const int *conn;        // [nen][ne] node indices (SoA)
+  const double *crd;      // [ndm][nn] coordinates (SoA)
+  const double *U;        // [nn*ndf] trial displacements
+  const int *mat;         // [ne] J2 row
+  const double *j2;       // [nmat*8]
+  double thickness;
+  // history, point-major SoA: comp*npts + (e*nip + ip)
+  const double *ep_c;     // committed plastic strain (4 comps plane strain: xx yy zz xy; 6 in 3D)
+  const double *xi_c;
+  double *ep_t, *xi_t;    // trial
+  double *sig;            // trial stress (3 plane strain: xx yy xy; 6 in 3D)
+  double *tan;            // trial tangent: quad 6 unique D entries; brick a b c n(6)
+  int *status;            // [ne] element status (0 ok, 1 return map failed)
+  // element outputs (element-major scratch)
+  double *Ke;             // quad: [ne][64]; brick: [ne][324] upper node-pair blocks
+  double *Re;             // [ne][ned]
+};
+
+// CSR system and deterministic gather assembly.
+struct GatherMap {
+  int nslots;             // nnz or neq
+  int nchunks;
+  const int *chunk_slot;  // [nchunks]
+  const int64_t *chunk_begin;  // [nchunks+1] into src
+  const int *slot_chunk;  // [nslots+1] chunk range per slot
+  const int64_t *src;     // contribution source indices into the scratch
+};
+
+// ---------------------------------------------------------------------------
+// kernel launchers (xg_kernels.cu)
+// ---------------------------------------------------------------------------
+int launch_quad_update(const ContinuumView &v, cudaStream_t s);
+int launch_quad_assemble(const ContinuumView &v, cudaStream_t s);
+int launch_brick_update(const ContinuumView &v, cudaStream_t s);
+int launch_brick_assemble(const ContinuumView &v, cudaStream_t s);
+int launch_gather(const GatherMap &g, const double *scratch, double *partial, double *out,
+                  cudaStream_t s);
+int launch_j2_zero_state(const ContinuumView &v, cudaStream_t s);
+
+// Block-Jacobi preconditioned CG (xg_pcg.cu)
+struct PcgSystem {
+  int n;
+  const int *rowptr, *colidx;
+  const double *vals;
+  int nblk;
+  const int *blk_start;   // [nblk+1] equation ranges of the diagonal blocks (<= 6)
+  double *binv;           // [nblk*36] inverted diagonal blocks (row major, padded to 6x6)
+  // work vectors [n]
+  double *r, *z, *p, *q;
+  double *partials;       // [2*max_blocks + 8]
+  unsigned int *barrier;  // [2] grid barrier state
+  int *flags;             // [4] status words
+  double *scalars;        // [8]
+};
+int pcg_factor_blocks(const PcgSystem &S, cudaStream_t s);
+// Solve A x = b (device vectors).  x holds the initial guess (usually 0).
+// Returns 0 when converged, XG_ESOLVE on breakdown, maxit or a barrier timeout.
+int pcg_solve(const PcgSystem &S, const double *b, double *x, double rtol, int maxit,
+              int *iters, double *relres, cudaStream_t s);
+int pcg_max_blocks();
+
+// small device helpers (xg_kernels.cu)
+int launch_axpy(int n, double a, const double *x, double *y, cudaStream_t s);
+int launch_scatter_incr(int nu, const int *eqn, const double *dU, double f, double *U,
+                        cudaStream_t s);
+int launch_sub(int n, const double *a, const double *b, double *out, cudaStream_t s);
+// deterministic 2-norm squared of x (n) into *out (device), partials scratch
+int launch_norm2(int n, const double *x, double *partials, double *out, cudaStream_t s);
+
+}  // namespace xg

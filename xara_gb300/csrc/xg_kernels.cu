@@ -1,0 +1,666 @@
+// xg_kernels.cu -- element state determination and deterministic assembly.
+//
+// FP64 throughout.  Per-point work (the J2 return map) runs one thread per
+// integration point over structure-of-arrays history; per-element stiffness
+// is formed from the stored trial state of the points, as the reference's
+// Element::getTangentStiff reads NDMaterial::getTangent; assembly is a gather
+// through a precomputed slot -> contribution map, so the summation order is
+// fixed (element tag order) and the result is bit-identical run to run.
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+#include "xg_internal.h"
+
+namespace xg {
+
+namespace {
+
+constexpr int kThreads = 256;
+
+inline int nblocks(long n, int t = kThreads) { return (int)((n + t - 1) / t); }
+
+// ---------------------------------------------------------------------------
+// J2 plasticity: J2Plasticity::plastic_integrator
+// (material/plastic/J2Plasticity.cpp:228-395), rate independent.
+// Symmetric tensors are held as [xx yy zz xy yz zx] (tensor components).
+// ---------------------------------------------------------------------------
+struct J2Out {
+  double sig[6];        // stress tensor components
+  double ep[6];         // trial plastic strain
+  double xi;
+  double c2, c3;        // plastic tangent coefficients (0 when elastic)
+  double n[6];          // unit normal (0 when |s| <= tol)
+  int status;
+};
+
+__device__ __forceinline__ double j2_q(const double *p, double xi) {
+  return p[5] * xi + p[3] + (p[2] - p[3]) * exp(-p[4] * xi);
+}
+__device__ __forceinline__ double j2_qprime(const double *p, double xi) {
+  return (p[2] - p[3]) * (-p[4]) * exp(-p[4] * xi) + p[5];
+}
+
+__device__ void j2_return_map(const double *p, const double eps[6], const double epn[6],
+                              double xin, J2Out &o) {
+  const double bulk = p[0], shear = p[1], sigma0 = p[2];
+  const double tolerance = 1.0e-10 * sigma0;
+  const double root23 = sqrt(2.0 / 3.0);
+  const double trace = eps[0] + eps[1] + eps[2];
+  double dev[6], s[6];
+#pragma unroll
+  for (int i = 0; i < 6; i++) dev[i] = eps[i];
+#pragma unroll
+  for (int i = 0; i < 3; i++) dev[i] -= 1. / 3. * trace;
+#pragma unroll
+  for (int i = 0; i < 6; i++) s[i] = (dev[i] - epn[i]) * (2.0 * shear);
+  double norm_tau = s[0] * s[0] + s[1] * s[1] + s[2] * s[2] +
+                    2.0 * (s[3] * s[3] + s[4] * s[4] + s[5] * s[5]);
+  norm_tau = sqrt(norm_tau);
+  double inv_norm_tau = 0.0;
+  if (norm_tau > tolerance) {
+    inv_norm_tau = 1.0 / norm_tau;
+#pragma unroll
+    for (int i = 0; i < 6; i++) o.n[i] = inv_norm_tau * s[i];
+  } else {
+#pragma unroll
+    for (int i = 0; i < 6; i++) o.n[i] = 0.0;
+  }
+  const double phi = norm_tau - root23 * j2_q(p, xin);
+  double gamma = 0.0, theta_inv = 0.0;
+  o.status = 0;
+  if (phi > 0.0) {
+    double resid = 1.0;
+    int it = 0;
+    while (fabs(resid) > tolerance) {
+      resid = norm_tau - (2.0 * shear) * gamma - root23 * j2_q(p, xin + root23 * gamma);
+      const double tang = -(2.0 * shear) - 2. / 3. * j2_qprime(p, xin + root23 * gamma);
+      gamma -= (resid / tang);
+      if (++it > 25) { o.status = 1; break; }
+    }
+    gamma *= 1.0 - 1e-08;
+#pragma unroll
+    for (int i = 0; i < 6; i++) o.ep[i] = epn[i] + gamma * o.n[i];
+    o.xi = xin + root23 * gamma;
+#pragma unroll
+    for (int i = 0; i < 6; i++) s[i] = (2.0 * shear) * (dev[i] - o.ep[i]);
+    theta_inv = 1.0 / ((2.0 * shear) + 2. / 3. * j2_qprime(p, o.xi));
+  } else {
+#pragma unroll
+    for (int i = 0; i < 6; i++) o.ep[i] = epn[i];
+    o.xi = xin;
+  }
+#pragma unroll
+  for (int i = 0; i < 6; i++) o.sig[i] = s[i];
+#pragma unroll
+  for (int i = 0; i < 3; i++) o.sig[i] += bulk * trace;
+  const double c1 = -4.0 * shear * shear;
+  o.c2 = c1 * theta_inv;
+  o.c3 = c1 * gamma * inv_norm_tau;
+}
+
+// One tangent entry as the reference forms it (J2Plasticity.cpp:362-388):
+// K*IbunI + 2G*IIdev + c2*NbunN + c3*(IIdev - NbunN).
+__device__ __forceinline__ double j2_tangent_entry(double bulk, double shear, double c2,
+                                                   double c3, double ibuni, double iidev,
+                                                   double nn) {
+  double t = bulk * ibuni;
+  t += (2.0 * shear) * iidev;
+  t += c2 * nn;
+  t += c3 * (iidev - nn);
+  return t;
+}
+
+// ---------------------------------------------------------------------------
+// FourNodeQuad + J2PlaneStrain
+// ---------------------------------------------------------------------------
+__device__ __constant__ double kQuadPts[4][2] = {
+    {-0.57735026918962573, -0.57735026918962573},
+    {-0.57735026918962573, 0.57735026918962573},
+    {0.57735026918962573, -0.57735026918962573},
+    {0.57735026918962573, 0.57735026918962573}};
+
+// FourNodeQuad::shapeFunction (element/Plane/FourNodeQuad.cpp:1128-1196)
+__device__ double quad_shape(const double x[4], const double y[4], double xi, double eta,
+                             double dN[2][4]) {
+  const double oneMinuseta = 1.0 - eta, onePluseta = 1.0 + eta;
+  const double oneMinusxi = 1.0 - xi, onePlusxi = 1.0 + xi;
+  const double J00 = 0.25 * (-x[0] * oneMinuseta + x[1] * oneMinuseta + x[2] * onePluseta -
+                             x[3] * onePluseta);
+  const double J01 = 0.25 * (-x[0] * oneMinusxi - x[1] * onePlusxi + x[2] * onePlusxi +
+                             x[3] * oneMinusxi);
+  const double J10 = 0.25 * (-y[0] * oneMinuseta + y[1] * oneMinuseta + y[2] * onePluseta -
+                             y[3] * onePluseta);
+  const double J11 = 0.25 * (-y[0] * oneMinusxi - y[1] * onePlusxi + y[2] * onePlusxi +
+                             y[3] * oneMinusxi);
+  const double detJ = J00 * J11 - J01 * J10;
+  const double r = 1.0 / detJ;
+  const double L00 = 0.25 * (J11 * r), L10 = 0.25 * (-J01 * r);
+  const double L01 = 0.25 * (-J10 * r), L11 = 0.25 * (J00 * r);
+  dN[0][0] = -L00 * oneMinuseta - L01 * oneMinusxi;
+  dN[0][1] = L00 * oneMinuseta - L01 * onePlusxi;
+  dN[0][2] = L00 * onePluseta + L01 * onePlusxi;
+  dN[0][3] = -L00 * onePluseta + L01 * oneMinusxi;
+  dN[1][0] = -L10 * oneMinuseta - L11 * oneMinusxi;
+  dN[1][1] = L10 * oneMinuseta - L11 * onePlusxi;
+  dN[1][2] = L10 * onePluseta + L11 * onePlusxi;
+  dN[1][3] = -L10 * onePluseta + L11 * oneMinusxi;
+  return detJ;
+}
+
+__device__ __forceinline__ void quad_nodes(const ContinuumView &v, int e, double x[4],
+                                           double y[4]) {
+#pragma unroll
+  for (int a = 0; a < 4; a++) {
+    const int nd = v.conn[a * v.ne + e];
+    x[a] = v.crd[nd];
+    y[a] = v.crd[v.nn + nd];
+  }
+}
+
+// One thread per integration point: FourNodeQuad::update (FourNodeQuad.cpp:
+// 190-224) + J2PlaneStrain::setTrialStrain/getStress/getTangent
+// (material/Plane/J2PlaneStrain.cpp:124-213).  Plane-strain history holds
+// ep xx yy zz xy; the stored tangent holds D00 D01 D02 D11 D12 D22 and the
+// stress sxx syy sxy.
+__global__ void k_quad_update(ContinuumView v) {
+  const long npts = (long)v.ne * 4;
+  const long pt = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (pt >= npts) return;
+  const int e = (int)(pt >> 2), ip = (int)(pt & 3);
+  double x[4], y[4], ux[4], uy[4];
+#pragma unroll
+  for (int a = 0; a < 4; a++) {
+    const int nd = v.conn[a * v.ne + e];
+    x[a] = v.crd[nd];
+    y[a] = v.crd[v.nn + nd];
+    ux[a] = v.U[2 * (long)nd];
+    uy[a] = v.U[2 * (long)nd + 1];
+  }
+  double dN[2][4];
+  quad_shape(x, y, kQuadPts[ip][0], kQuadPts[ip][1], dN);
+  double e0 = 0.0, e1 = 0.0, e2 = 0.0;
+#pragma unroll
+  for (int b = 0; b < 4; b++) {
+    e0 += dN[0][b] * ux[b];
+    e1 += dN[1][b] * uy[b];
+    e2 += dN[0][b] * uy[b] + dN[1][b] * ux[b];
+  }
+  const double *p = v.j2 + (long)v.mat[e] * XG_J2_NPARAM;
+  const double eps[6] = {e0, e1, 0.0, 0.50 * e2, 0.0, 0.0};
+  double epn[6];
+  epn[0] = v.ep_c[pt];
+  epn[1] = v.ep_c[npts + pt];
+  epn[2] = v.ep_c[2 * npts + pt];
+  epn[3] = v.ep_c[3 * npts + pt];
+  epn[4] = 0.0;
+  epn[5] = 0.0;
+  J2Out o;
+  j2_return_map(p, eps, epn, v.xi_c[pt], o);
+  v.ep_t[pt] = o.ep[0];
+  v.ep_t[npts + pt] = o.ep[1];
+  v.ep_t[2 * npts + pt] = o.ep[2];
+  v.ep_t[3 * npts + pt] = o.ep[3];
+  v.xi_t[pt] = o.xi;
+  v.sig[pt] = o.sig[0];
+  v.sig[npts + pt] = o.sig[1];
+  v.sig[2 * npts + pt] = o.sig[3];
+  const double K = p[0], G = p[1];
+  const double n00 = o.n[0], n11 = o.n[1], n01 = o.n[3];
+  v.tan[pt] = j2_tangent_entry(K, G, o.c2, o.c3, 1.0, 2. / 3., n00 * n00);
+  v.tan[npts + pt] = j2_tangent_entry(K, G, o.c2, o.c3, 1.0, -1. / 3., n00 * n11);
+  v.tan[2 * npts + pt] = j2_tangent_entry(K, G, o.c2, o.c3, 0.0, 0.0, n00 * n01);
+  v.tan[3 * npts + pt] = j2_tangent_entry(K, G, o.c2, o.c3, 1.0, 2. / 3., n11 * n11);
+  v.tan[4 * npts + pt] = j2_tangent_entry(K, G, o.c2, o.c3, 0.0, 0.0, n11 * n01);
+  v.tan[5 * npts + pt] = j2_tangent_entry(K, G, o.c2, o.c3, 0.0, 0.5, n01 * n01);
+  if (ip == 0) v.status[e] = 0;
+}
+
+// One thread per element: FourNodeQuad::getTangentStiff / getResistingForce
+// (FourNodeQuad.cpp:226-282, 507-552) from the stored point state.
+// Ke[e*64 + 8*i + j], Re[e*8 + i].
+__global__ void k_quad_assemble(ContinuumView v) {
+  const int e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= v.ne) return;
+  const long npts = (long)v.ne * 4;
+  double x[4], y[4];
+  quad_nodes(v, e, x, y);
+  double K[64], P[8];
+#pragma unroll
+  for (int i = 0; i < 64; i++) K[i] = 0.0;
+#pragma unroll
+  for (int i = 0; i < 8; i++) P[i] = 0.0;
+  for (int ip = 0; ip < 4; ip++) {
+    double dN[2][4];
+    const double detJ = quad_shape(x, y, kQuadPts[ip][0], kQuadPts[ip][1], dN);
+    const double dvol = detJ * (v.thickness * 1.0);
+    const long pt = (long)e * 4 + ip;
+    const double D00 = v.tan[pt], D01 = v.tan[npts + pt], D02 = v.tan[2 * npts + pt];
+    const double D11 = v.tan[3 * npts + pt], D12 = v.tan[4 * npts + pt];
+    const double D22 = v.tan[5 * npts + pt];
+    const double D10 = D01, D20 = D02, D21 = D12;
+    const double s0 = v.sig[pt], s1 = v.sig[npts + pt], s2 = v.sig[2 * npts + pt];
+#pragma unroll
+    for (int a = 0; a < 4; a++) {
+      const int ia = 2 * a;
+#pragma unroll
+      for (int b = 0; b < 4; b++) {
+        const int ib = 2 * b;
+        const double DB00 = dvol * (D00 * dN[0][b] + D02 * dN[1][b]);
+        const double DB10 = dvol * (D10 * dN[0][b] + D12 * dN[1][b]);
+        const double DB20 = dvol * (D20 * dN[0][b] + D22 * dN[1][b]);
+        const double DB01 = dvol * (D01 * dN[1][b] + D02 * dN[0][b]);
+        const double DB11 = dvol * (D11 * dN[1][b] + D12 * dN[0][b]);
+        const double DB21 = dvol * (D21 * dN[1][b] + D22 * dN[0][b]);
+        K[8 * ia + ib] += dN[0][a] * DB00 + dN[1][a] * DB20;
+        K[8 * ia + ib + 1] += dN[0][a] * DB01 + dN[1][a] * DB21;
+        K[8 * (ia + 1) + ib] += dN[1][a] * DB10 + dN[0][a] * DB20;
+        K[8 * (ia + 1) + ib + 1] += dN[1][a] * DB11 + dN[0][a] * DB21;
+      }
+      P[ia] += dvol * (dN[0][a] * s0 + dN[1][a] * s2);
+      P[ia + 1] += dvol * (dN[1][a] * s1 + dN[0][a] * s2);
+    }
+  }
+  double *Ke = v.Ke + (long)e * 64;
+#pragma unroll
+  for (int i = 0; i < 64; i++) Ke[i] = K[i];
+  double *Re = v.Re + (long)e * 8;
+#pragma unroll
+  for (int i = 0; i < 8; i++) Re[i] = P[i];
+}
+
+// ---------------------------------------------------------------------------
+// Brick + J2ThreeDimensional
+// ---------------------------------------------------------------------------
+
+// shp3d (interpolate/shp3d.cpp:31-180): natural derivatives, Jacobian,
+// global derivatives.  xl[3][8] nodal coordinates; g[3][8] out; returns xsj.
+__device__ double shp3d_grad(const double xn[3], const double xl[3][8], double g[3][8]) {
+  const double ap1 = 1.0 + xn[0], am1 = 1.0 - xn[0];
+  const double ap2 = 1.0 + xn[1], am2 = 1.0 - xn[1];
+  const double ap3 = 1.0 + xn[2], am3 = 1.0 - xn[2];
+  double s[3][8];
+  double c1, c2, c3;
+  c1 = 0.125 * am1 * am2; c2 = 0.125 * am2 * am3; c3 = 0.125 * am1 * am3;
+  s[0][0] = -c2; s[0][1] = c2; s[1][0] = -c3; s[1][3] = c3; s[2][0] = -c1; s[2][4] = c1;
+  c1 = 0.125 * ap1 * ap2; c2 = 0.125 * ap2 * ap3; c3 = 0.125 * ap1 * ap3;
+  s[0][7] = -c2; s[0][6] = c2; s[1][5] = -c3; s[1][6] = c3; s[2][2] = -c1; s[2][6] = c1;
+  c1 = 0.125 * am1 * ap2; c2 = 0.125 * am2 * ap3; c3 = 0.125 * am1 * ap3;
+  s[0][4] = -c2; s[0][5] = c2; s[1][4] = -c3; s[1][7] = c3; s[2][3] = -c1; s[2][7] = c1;
+  c1 = 0.125 * ap1 * am2; c2 = 0.125 * ap2 * am3; c3 = 0.125 * ap1 * am3;
+  s[0][3] = -c2; s[0][2] = c2; s[1][1] = -c3; s[1][2] = c3; s[2][1] = -c1; s[2][5] = c1;
+  double xs[3][3];
+#pragma unroll
+  for (int j = 0; j < 3; j++) {
+    xs[j][0] = (xl[j][1] - xl[j][0]) * s[0][1] + (xl[j][2] - xl[j][3]) * s[0][2] +
+               (xl[j][5] - xl[j][4]) * s[0][5] + (xl[j][6] - xl[j][7]) * s[0][6];
+    xs[j][1] = (xl[j][2] - xl[j][1]) * s[1][2] + (xl[j][3] - xl[j][0]) * s[1][3] +
+               (xl[j][6] - xl[j][5]) * s[1][6] + (xl[j][7] - xl[j][4]) * s[1][7];
+    xs[j][2] = (xl[j][4] - xl[j][0]) * s[2][4] + (xl[j][5] - xl[j][1]) * s[2][5] +
+               (xl[j][6] - xl[j][2]) * s[2][6] + (xl[j][7] - xl[j][3]) * s[2][7];
+  }
+  double ad[3][3];
+  ad[0][0] = xs[1][1] * xs[2][2] - xs[1][2] * xs[2][1];
+  ad[0][1] = xs[2][1] * xs[0][2] - xs[2][2] * xs[0][1];
+  ad[0][2] = xs[0][1] * xs[1][2] - xs[0][2] * xs[1][1];
+  ad[1][0] = xs[1][2] * xs[2][0] - xs[1][0] * xs[2][2];
+  ad[1][1] = xs[2][2] * xs[0][0] - xs[2][0] * xs[0][2];
+  ad[1][2] = xs[0][2] * xs[1][0] - xs[0][0] * xs[1][2];
+  ad[2][0] = xs[1][0] * xs[2][1] - xs[1][1] * xs[2][0];
+  ad[2][1] = xs[2][0] * xs[0][1] - xs[2][1] * xs[0][0];
+  ad[2][2] = xs[0][0] * xs[1][1] - xs[0][1] * xs[1][0];
+  const double xsj = xs[0][0] * ad[0][0] + xs[0][1] * ad[1][0] + xs[0][2] * ad[2][0];
+  const double rxsj = 1.0 / xsj;
+  double inv[3][3];
+#pragma unroll
+  for (int j = 0; j < 3; j++)
+#pragma unroll
+    for (int i = 0; i < 3; i++) inv[i][j] = ad[i][j] * rxsj;
+#pragma unroll
+  for (int k = 0; k < 8; k++) {
+    g[0][k] = s[0][k] * inv[0][0] + s[1][k] * inv[1][0] + s[2][k] * inv[2][0];
+    g[1][k] = s[0][k] * inv[0][1] + s[1][k] * inv[1][1] + s[2][k] * inv[2][1];
+    g[2][k] = s[0][k] * inv[0][2] + s[1][k] * inv[1][2] + s[2][k] * inv[2][2];
+  }
+  return xsj;
+}
+
+__device__ __forceinline__ void brick_gauss(int ip, double xn[3]) {
+  // Brick.cpp:56-59 and the (i,j,k) nested point order of Brick::update (:754-773)
+  const double r = 1.0 / sqrt(3.0);
+  xn[0] = (ip & 4) ? r : -r;
+  xn[1] = (ip & 2) ? r : -r;
+  xn[2] = (ip & 1) ? r : -r;
+}
+
+// One thread per point: Brick::update (Brick.cpp:719-840) +
+// J2ThreeDimensional::setTrialStrain (J2ThreeDimensional.cpp:123-141).
+// History ep xx yy zz xy yz zx; stored tangent a b c n(6) with
+// D_ijkl = a d_ij d_kl + b I^sym_ijkl + c n_ij n_kl, which equals the
+// reference's K IbunI + 2G IIdev + c2 NbunN + c3 (IIdev - NbunN) for
+// a = K - b/3, b = 2G + c3, c = c2 - c3.
+__global__ void k_brick_update(ContinuumView v) {
+  const long npts = (long)v.ne * 8;
+  const long pt = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (pt >= npts) return;
+  const int e = (int)(pt >> 3), ip = (int)(pt & 7);
+  double xl[3][8], g[3][8], eps[6] = {0, 0, 0, 0, 0, 0};
+  int nd[8];
+#pragma unroll
+  for (int a = 0; a < 8; a++) {
+    nd[a] = v.conn[a * v.ne + e];
+    xl[0][a] = v.crd[nd[a]];
+    xl[1][a] = v.crd[v.nn + nd[a]];
+    xl[2][a] = v.crd[2 * (long)v.nn + nd[a]];
+  }
+  double xn[3];
+  brick_gauss(ip, xn);
+  shp3d_grad(xn, xl, g);
+#pragma unroll
+  for (int a = 0; a < 8; a++) {
+    const double u0 = v.U[3 * (long)nd[a]], u1 = v.U[3 * (long)nd[a] + 1];
+    const double u2 = v.U[3 * (long)nd[a] + 2];
+    eps[0] += g[0][a] * u0;
+    eps[1] += g[1][a] * u1;
+    eps[2] += g[2][a] * u2;
+    eps[3] += g[1][a] * u0 + g[0][a] * u1;
+    eps[4] += g[2][a] * u1 + g[1][a] * u2;
+    eps[5] += g[2][a] * u0 + g[0][a] * u2;
+  }
+  const double strain[6] = {eps[0], eps[1], eps[2], 0.50 * eps[3], 0.50 * eps[4], 0.50 * eps[5]};
+  double epn[6];
+#pragma unroll
+  for (int c = 0; c < 6; c++) epn[c] = v.ep_c[c * npts + pt];
+  const double *p = v.j2 + (long)v.mat[e] * XG_J2_NPARAM;
+  J2Out o;
+  j2_return_map(p, strain, epn, v.xi_c[pt], o);
+#pragma unroll
+  for (int c = 0; c < 6; c++) v.ep_t[c * npts + pt] = o.ep[c];
+  v.xi_t[pt] = o.xi;
+#pragma unroll
+  for (int c = 0; c < 6; c++) v.sig[c * npts + pt] = o.sig[c];
+  const double b = 2.0 * p[1] + o.c3;
+  v.tan[pt] = p[0] - b / 3.0;
+  v.tan[npts + pt] = b;
+  v.tan[2 * npts + pt] = o.c2 - o.c3;
+#pragma unroll
+  for (int c = 0; c < 6; c++) v.tan[(3 + c) * npts + pt] = o.n[c];
+  if (o.status) v.status[e] = 1;
+}
+
+__device__ __constant__ unsigned char kPairA[36] = {
+    0, 0, 0, 0, 0, 0, 0, 0, 1, 1, 1, 1, 1, 1, 1, 2, 2, 2,
+    2, 2, 2, 3, 3, 3, 3, 3, 4, 4, 4, 4, 5, 5, 5, 6, 6, 7};
+__device__ __constant__ unsigned char kPairB[36] = {
+    0, 1, 2, 3, 4, 5, 6, 7, 1, 2, 3, 4, 5, 6, 7, 2, 3, 4,
+    5, 6, 7, 3, 4, 5, 6, 7, 4, 5, 6, 7, 5, 6, 7, 6, 7, 7};
+
+constexpr int kBrickWarps = 4;
+
+// One warp per element: Brick::formResidAndTangent (Brick.cpp:844-1021) from
+// the stored point state, K in upper node-pair blocks:
+// Ke[e*324 + p*9 + 3*i + k] = K(3a+i, 3b+k) for the pair p = (a <= b).
+// Re[e*24 + 3a + i].
+__global__ void __launch_bounds__(32 * kBrickWarps) k_brick_assemble(ContinuumView v) {
+  __shared__ double sg[kBrickWarps][8][8][3];   // dN/dx per point, node
+  __shared__ double sh[kBrickWarps][8][8][3];   // N . dN/dx
+  __shared__ double sc[kBrickWarps][8][3];      // dvol*a, dvol*b/2, dvol*c
+  __shared__ double ss[kBrickWarps][8][6];      // dvol*stress
+  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int e = blockIdx.x * kBrickWarps + w;
+  if (e >= v.ne) return;
+  const long npts = (long)v.ne * 8;
+  if (lane < 8) {
+    const int ip = lane;
+    const long pt = (long)e * 8 + ip;
+    double xl[3][8], g[3][8];
+#pragma unroll
+    for (int a = 0; a < 8; a++) {
+      const int nd = v.conn[a * v.ne + e];
+      xl[0][a] = v.crd[nd];
+      xl[1][a] = v.crd[v.nn + nd];
+      xl[2][a] = v.crd[2 * (long)v.nn + nd];
+    }
+    double xn[3];
+    brick_gauss(ip, xn);
+    const double dvol = 1.0 * shp3d_grad(xn, xl, g);
+    const double ca = v.tan[pt], cb = v.tan[npts + pt], cc = v.tan[2 * npts + pt];
+    double n[6];
+#pragma unroll
+    for (int c = 0; c < 6; c++) n[c] = v.tan[(3 + c) * npts + pt];
+    sc[w][ip][0] = dvol * ca;
+    sc[w][ip][1] = dvol * (0.5 * cb);
+    sc[w][ip][2] = dvol * cc;
+#pragma unroll
+    for (int c = 0; c < 6; c++) ss[w][ip][c] = dvol * v.sig[c * npts + pt];
+#pragma unroll
+    for (int a = 0; a < 8; a++) {
+      const double g0 = g[0][a], g1 = g[1][a], g2 = g[2][a];
+      sg[w][ip][a][0] = g0;
+      sg[w][ip][a][1] = g1;
+      sg[w][ip][a][2] = g2;
+      sh[w][ip][a][0] = n[0] * g0 + n[3] * g1 + n[5] * g2;
+      sh[w][ip][a][1] = n[3] * g0 + n[1] * g1 + n[4] * g2;
+      sh[w][ip][a][2] = n[5] * g0 + n[4] * g1 + n[2] * g2;
+    }
+  }
+  __syncwarp();
+  if (lane < 24) {
+    const int a = lane / 3, i = lane % 3;
+    // stress tensor row i in [xx yy zz xy yz zx] storage
+    const int r0 = (i == 0) ? 0 : (i == 1) ? 3 : 5;
+    const int r1 = (i == 0) ? 3 : (i == 1) ? 1 : 4;
+    const int r2 = (i == 0) ? 5 : (i == 1) ? 4 : 2;
+    double r = 0.0;
+#pragma unroll
+    for (int ip = 0; ip < 8; ip++)
+      r += sg[w][ip][a][0] * ss[w][ip][r0] + sg[w][ip][a][1] * ss[w][ip][r1] +
+           sg[w][ip][a][2] * ss[w][ip][r2];
+    v.Re[(long)e * 24 + lane] = r;
+  }
+  for (int pp = lane; pp < 36; pp += 32) {
+    const int a = kPairA[pp], b = kPairB[pp];
+    double acc[3][3];
+#pragma unroll
+    for (int i = 0; i < 3; i++)
+#pragma unroll
+      for (int k = 0; k < 3; k++) acc[i][k] = 0.0;
+#pragma unroll 2
+    for (int ip = 0; ip < 8; ip++) {
+      const double ga0 = sg[w][ip][a][0], ga1 = sg[w][ip][a][1], ga2 = sg[w][ip][a][2];
+      const double gb0 = sg[w][ip][b][0], gb1 = sg[w][ip][b][1], gb2 = sg[w][ip][b][2];
+      const double ha[3] = {sh[w][ip][a][0], sh[w][ip][a][1], sh[w][ip][a][2]};
+      const double hb[3] = {sh[w][ip][b][0], sh[w][ip][b][1], sh[w][ip][b][2]};
+      const double da = sc[w][ip][0], dbh = sc[w][ip][1], dc = sc[w][ip][2];
+      const double ga[3] = {ga0, ga1, ga2}, gb[3] = {gb0, gb1, gb2};
+      const double dot = dbh * (ga0 * gb0 + ga1 * gb1 + ga2 * gb2);
+      double ua[3], va[3], wa[3];
+#pragma unroll
+      for (int i = 0; i < 3; i++) { ua[i] = da * ga[i]; va[i] = dbh * ga[i]; wa[i] = dc * ha[i]; }
+#pragma unroll
+      for (int i = 0; i < 3; i++) {
+#pragma unroll
+        for (int k = 0; k < 3; k++)
+          acc[i][k] += ua[i] * gb[k] + va[k] * gb[i] + wa[i] * hb[k];
+        acc[i][i] += dot;
+      }
+    }
+    double *Ke = v.Ke + (long)e * 324 + pp * 9;
+#pragma unroll
+    for (int i = 0; i < 3; i++)
+#pragma unroll
+      for (int k = 0; k < 3; k++) Ke[3 * i + k] = acc[i][k];
+  }
+}
+
+// Zero-strain trial state (the material constructors call the integrator at
+// zero strain, J2Plasticity.cpp:84-111): history zero, elastic tangent.
+__global__ void k_j2_zero(ContinuumView v) {
+  const long npts = (long)v.ne * v.nip;
+  const long pt = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (pt >= npts) return;
+  const int e = (int)(pt / v.nip);
+  const double *p = v.j2 + (long)v.mat[e] * XG_J2_NPARAM;
+  const int nh = v.nip == 4 ? 4 : 6;
+  for (int c = 0; c < nh; c++) {
+    const_cast<double *>(v.ep_c)[c * npts + pt] = 0.0;
+    v.ep_t[c * npts + pt] = 0.0;
+  }
+  const_cast<double *>(v.xi_c)[pt] = 0.0;
+  v.xi_t[pt] = 0.0;
+  const double K = p[0], G = p[1];
+  if (v.nip == 4) {
+    for (int c = 0; c < 3; c++) v.sig[c * npts + pt] = 0.0;
+    v.tan[pt] = j2_tangent_entry(K, G, 0.0, 0.0, 1.0, 2. / 3., 0.0);
+    v.tan[npts + pt] = j2_tangent_entry(K, G, 0.0, 0.0, 1.0, -1. / 3., 0.0);
+    v.tan[2 * npts + pt] = 0.0;
+    v.tan[3 * npts + pt] = j2_tangent_entry(K, G, 0.0, 0.0, 1.0, 2. / 3., 0.0);
+    v.tan[4 * npts + pt] = 0.0;
+    v.tan[5 * npts + pt] = j2_tangent_entry(K, G, 0.0, 0.0, 0.0, 0.5, 0.0);
+  } else {
+    for (int c = 0; c < 6; c++) v.sig[c * npts + pt] = 0.0;
+    const double b = 2.0 * G;
+    v.tan[pt] = K - b / 3.0;
+    v.tan[npts + pt] = b;
+    v.tan[2 * npts + pt] = 0.0;
+    for (int c = 0; c < 6; c++) v.tan[(3 + c) * npts + pt] = 0.0;
+  }
+  if (pt % v.nip == 0) v.status[e] = 0;
+}
+
+// ---------------------------------------------------------------------------
+// deterministic gather assembly
+// ---------------------------------------------------------------------------
+__global__ void k_gather_chunks(GatherMap g, const double *__restrict__ scratch,
+                                double *__restrict__ partial) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= g.nchunks) return;
+  double s = 0.0;
+  const int64_t b = g.chunk_begin[c], end = g.chunk_begin[c + 1];
+  for (int64_t k = b; k < end; k++) s += scratch[g.src[k]];
+  partial[c] = s;
+}
+
+__global__ void k_gather_slots(GatherMap g, const double *__restrict__ partial,
+                               double *__restrict__ out) {
+  const int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= g.nslots) return;
+  double v = 0.0;
+  for (int c = g.slot_chunk[s]; c < g.slot_chunk[s + 1]; c++) v += partial[c];
+  out[s] = v;
+}
+
+// ---------------------------------------------------------------------------
+// vector helpers
+// ---------------------------------------------------------------------------
+__global__ void k_axpy(int n, double a, const double *x, double *y) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) y[i] += a * x[i];
+}
+
+__global__ void k_scatter_incr(int nu, const int *eqn, const double *dU, double f, double *U) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= nu) return;
+  const int e = eqn[i];
+  if (e >= 0) U[i] += f * dU[e];
+}
+
+__global__ void k_sub(int n, const double *a, const double *b, double *out) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) out[i] = a[i] - b[i];
+}
+
+__device__ double block_sum(double v) {
+  __shared__ double wsum[32];
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  __syncthreads();
+  if (lane == 0) wsum[w] = v;
+  __syncthreads();
+  double t = 0.0;
+  if (w == 0) {
+    t = (lane < (int)(blockDim.x >> 5)) ? wsum[lane] : 0.0;
+    for (int o = 16; o > 0; o >>= 1) t += __shfl_down_sync(0xffffffffu, t, o);
+  }
+  return t;  // valid in thread 0
+}
+
+__global__ void k_norm2_partial(int n, const double *x, double *partials) {
+  double s = 0.0;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+    s += x[i] * x[i];
+  s = block_sum(s);
+  if (threadIdx.x == 0) partials[blockIdx.x] = s;
+}
+
+__global__ void k_norm2_final(int nb, const double *partials, double *out) {
+  double s = 0.0;
+  for (int i = threadIdx.x; i < nb; i += blockDim.x) s += partials[i];
+  s = block_sum(s);
+  if (threadIdx.x == 0) *out = s;
+}
+
+inline int check_launch() {
+  return cudaGetLastError() == cudaSuccess ? 0 : XG_ECUDA;
+}
+
+}  // namespace
+
+int launch_quad_update(const ContinuumView &v, cudaStream_t s) {
+  if (v.ne == 0) return 0;
+  k_quad_update<<<nblocks((long)v.ne * 4), kThreads, 0, s>>>(v);
+  return check_launch();
+}
+int launch_quad_assemble(const ContinuumView &v, cudaStream_t s) {
+  if (v.ne == 0) return 0;
+  k_quad_assemble<<<nblocks(v.ne, 128), 128, 0, s>>>(v);
+  return check_launch();
+}
+int launch_brick_update(const ContinuumView &v, cudaStream_t s) {
+  if (v.ne == 0) return 0;
+  k_brick_update<<<nblocks((long)v.ne * 8), kThreads, 0, s>>>(v);
+  return check_launch();
+}
+int launch_brick_assemble(const ContinuumView &v, cudaStream_t s) {
+  if (v.ne == 0) return 0;
+  k_brick_assemble<<<(v.ne + kBrickWarps - 1) / kBrickWarps, 32 * kBrickWarps, 0, s>>>(v);
+  return check_launch();
+}
+int launch_j2_zero_state(const ContinuumView &v, cudaStream_t s) {
+  if (v.ne == 0) return 0;
+  k_j2_zero<<<nblocks((long)v.ne * v.nip), kThreads, 0, s>>>(v);
+  return check_launch();
+}
+int launch_gather(const GatherMap &g, const double *scratch, double *partial, double *out,
+                  cudaStream_t s) {
+  if (g.nslots == 0) return 0;
+  k_gather_chunks<<<nblocks(g.nchunks), kThreads, 0, s>>>(g, scratch, partial);
+  k_gather_slots<<<nblocks(g.nslots), kThreads, 0, s>>>(g, partial, out);
+  return check_launch();
+}
+int launch_axpy(int n, double a, const double *x, double *y, cudaStream_t s) {
+  if (n == 0) return 0;
+  k_axpy<<<nblocks(n), kThreads, 0, s>>>(n, a, x, y);
+  return check_launch();
+}
+int launch_scatter_incr(int nu, const int *eqn, const double *dU, double f, double *U,
+                        cudaStream_t s) {
+  if (nu == 0) return 0;
+  k_scatter_incr<<<nblocks(nu), kThreads, 0, s>>>(nu, eqn, dU, f, U);
+  return check_launch();
+}
+int launch_sub(int n, const double *a, const double *b, double *out, cudaStream_t s) {
+  if (n == 0) return 0;
+  k_sub<<<nblocks(n), kThreads, 0, s>>>(n, a, b, out);
+  return check_launch();
+}
+int launch_norm2(int n, const double *x, double *partials, double *out, cudaStream_t s) {
+  int nb = nblocks(n);
+  if (nb > 1024) nb = 1024;
+  if (nb < 1) nb = 1;
+  k_norm2_partial<<<nb, kThreads, 0, s>>>(n, x, partials);
+  k_norm2_final<<<1, 1024, 0, s>>>(nb, partials, out);
+  return check_launch();
+}
+
+}  // namespace xg

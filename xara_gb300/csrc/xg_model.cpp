@@ -1,0 +1,992 @@
+// xg_model.cpp -- host side of libxara_gpu.so: the model store, DOF
+// numbering, sparsity pattern, gather maps, and the Newton-Raphson driver
+// that keeps every vector of a step on the device.
+//
+// The integer pipeline (handler IDs, RCM order, equation numbers, CSR
+// pattern) restates the reference's algorithm and is bit-exact against it:
+//   PlainHandler::handle            analysis/handler/PlainHandler.cpp:60-200
+//   AnalysisModel::getDOFGroupGraph analysis/model/AnalysisModel.cpp:356-392
+//   RCM::number (no GPS)            graph/numberer/RCM.cpp:67-277
+//   DOF_Numberer::numberDOF         analysis/numberer/DOF_Numberer.cpp:93-205
+//   SparseGenColLinSOE::setSize     system_of_eqn/linearSOE/sparseGEN/SparseGenColLinSOE.cpp:161-261
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <numeric>
+#include <string>
+#include <vector>
+
+#include "xg_internal.h"
+
+using namespace xg;
+
+namespace {
+
+thread_local std::string g_err;
+
+int fail(int code, const char *fmt, ...) {
+  char buf[512];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof buf, fmt, ap);
+  va_end(ap);
+  g_err = buf;
+  return code;
+}
+
+#define CK(call)                                                                   \
+  do {                                                                             \
+    cudaError_t e_ = (call);                                                       \
+    if (e_ != cudaSuccess)                                                         \
+      return fail(XG_ECUDA, "%s: %s (%s:%d)", #call, cudaGetErrorString(e_), __FILE__, \
+                  __LINE__);                                                       \
+  } while (0)
+
+#define RET(call)                                                                  \
+  do {                                                                             \
+    int r_ = (call);                                                               \
+    if (r_ != 0) {                                                                 \
+      if (g_err.empty()) fail(r_, "%s failed (%d)", #call, r_);                    \
+      return r_;                                                                   \
+    }                                                                              \
+  } while (0)
+
+template <class T>
+struct DBuf {
+  T *p = nullptr;
+  size_t n = 0;
+  int alloc(size_t count) {
+    free();
+    n = count;
+    if (count == 0) return 0;
+    if (cudaMalloc(&p, count * sizeof(T)) != cudaSuccess) {
+      p = nullptr;
+      return fail(XG_ENOMEM, "cudaMalloc of %zu bytes failed", count * sizeof(T));
+    }
+    return 0;
+  }
+  int upload(const T *h, size_t count, cudaStream_t s) {
+    RET(alloc(count));
+    if (count) CK(cudaMemcpyAsync(p, h, count * sizeof(T), cudaMemcpyHostToDevice, s));
+    return 0;
+  }
+  void free() {
+    if (p) cudaFree(p);
+    p = nullptr;
+    n = 0;
+  }
+  ~DBuf() { free(); }
+};
+
+struct HostGather {
+  std::vector<int> slot_chunk, chunk_slot;
+  std::vector<int64_t> chunk_begin;
+  std::vector<int64_t> src;
+};
+
+// Build chunked gather lists from (slot, src) pairs given in assembly order.
+void build_gather(int nslots, const std::vector<int> &slot_of, const std::vector<int64_t> &src_of,
+                  HostGather &g, int chunk = 32) {
+  std::vector<int64_t> cnt(nslots + 1, 0);
+  for (int s : slot_of) cnt[s + 1]++;
+  std::vector<int64_t> ptr(nslots + 1, 0);
+  for (int i = 0; i < nslots; i++) ptr[i + 1] = ptr[i] + cnt[i + 1];
+  g.src.assign(ptr[nslots], 0);
+  std::vector<int64_t> fill(ptr.begin(), ptr.end() - 1);
+  for (size_t k = 0; k < slot_of.size(); k++) g.src[fill[slot_of[k]]++] = src_of[k];
+  g.slot_chunk.assign(nslots + 1, 0);
+  g.chunk_slot.clear();
+  g.chunk_begin.clear();
+  for (int s = 0; s < nslots; s++) {
+    g.slot_chunk[s] = (int)g.chunk_slot.size();
+    int64_t b = ptr[s], e = ptr[s + 1];
+    if (b == e) {
+      g.chunk_slot.push_back(s);
+      g.chunk_begin.push_back(b);
+    }
+    for (int64_t c = b; c < e; c += chunk) {
+      g.chunk_slot.push_back(s);
+      g.chunk_begin.push_back(c);
+    }
+  }
+  g.slot_chunk[nslots] = (int)g.chunk_slot.size();
+  g.chunk_begin.push_back(ptr[nslots]);
+  // chunk c sums src[chunk_begin[c], chunk_begin[c+1]): the chunks of a slot
+  // and of consecutive slots tile [0, total) (an empty slot has one empty
+  // chunk starting where the next slot starts).
+}
+
+}  // namespace
+
+struct xg_model {
+  // description (copied)
+  int ndm = 0, ndf = 0, nn = 0, ne = 0, nen = 0, nip = 0, ned = 0, etype = 0;
+  double thickness = 1.0;
+  std::vector<int> node_tag, elem_tag, conn;   // conn: node indices [ne*nen]
+  std::vector<double> crd;                     // [nn*ndm]
+  std::vector<int> mat;
+  std::vector<double> j2;
+  int num_sp = 0, num_mp = 0, num_loads = 0, handler = 0;
+  std::vector<int> sp_node, sp_dof, sp_pat, mp_r, mp_c, mp_dof, load_node, load_pat;
+  std::vector<double> sp_val, load_val;
+
+  // numbering
+  int neq = 0, nnz = 0;
+  std::vector<int> eqn;                        // [nn*ndf]
+  std::vector<int> rowptr, colidx;
+  std::vector<int> blk_start;
+
+  // device
+  cudaStream_t stream = nullptr;
+  DBuf<int> d_conn, d_mat, d_eqn, d_rowptr, d_colidx, d_blk, d_status;
+  DBuf<double> d_crd, d_j2, d_U, d_Uc;
+  DBuf<double> d_epc, d_xic, d_ept, d_xit, d_sig, d_tan;
+  DBuf<double> d_sig_c, d_tan_c;               // trial state at the last commit
+  DBuf<double> d_Ke, d_Re, d_partial;
+  DBuf<double> d_vals, d_resid;
+  DBuf<int> d_gk_slot_chunk, d_gk_chunk_slot, d_gr_slot_chunk, d_gr_chunk_slot;
+  DBuf<int64_t> d_gk_chunk_begin, d_gk_src, d_gr_chunk_begin, d_gr_src;
+  GatherMap gk{}, gr{};
+  // solver
+  DBuf<double> d_binv, d_r, d_z, d_p, d_q, d_pcg_part, d_scalars;
+  DBuf<unsigned int> d_barrier;
+  DBuf<int> d_flags;
+  PcgSystem pcg{};
+  bool blocks_factored = false;
+  double rtol = 1e-12;
+  int maxit = 20000;
+  // Newton vectors
+  DBuf<double> d_fext, d_B, d_dU, d_phat, d_dUhat, d_x, d_b, d_norm, d_Fref;
+  std::vector<int> ref_patterns;               // pattern id of each d_Fref row
+  // analysis state
+  xg_phase_desc phase{};
+  bool have_phase = false;
+  std::vector<double> gm;
+  double time = 0.0, time_c = 0.0;
+  double lambda_const[8] = {0};
+  int pattern_const[8] = {0}, added[8] = {0};
+  int dc_eq = -1;
+  int last_solver_iters = 0;
+  int phase_steps_done = 0;
+  bool phase_closed = false;
+
+  ContinuumView view() {
+    ContinuumView v{};
+    v.ne = ne; v.nn = nn; v.nen = nen; v.nip = nip; v.ndf = ndf; v.ndm = ndm;
+    v.conn = d_conn.p; v.crd = d_crd.p; v.U = d_U.p; v.mat = d_mat.p; v.j2 = d_j2.p;
+    v.thickness = thickness;
+    v.ep_c = d_epc.p; v.xi_c = d_xic.p; v.ep_t = d_ept.p; v.xi_t = d_xit.p;
+    v.sig = d_sig.p; v.tan = d_tan.p; v.status = d_status.p;
+    v.Ke = d_Ke.p; v.Re = d_Re.p;
+    return v;
+  }
+  int nhist() const { return etype == XG_ELE_QUAD ? 4 : 6; }
+  int nsig() const { return etype == XG_ELE_QUAD ? 3 : 6; }
+  int ntan() const { return etype == XG_ELE_QUAD ? 6 : 9; }
+  long npts() const { return (long)ne * nip; }
+  int ke_size() const { return etype == XG_ELE_QUAD ? 64 : 324; }
+
+  ~xg_model() {
+    if (stream) cudaStreamDestroy(stream);
+  }
+
+  int number();
+  int build_maps(HostGather &gk_h, HostGather &gr_h);
+  int upload(const HostGather &gk_h, const HostGather &gr_h);
+  int element_state(bool compute);
+  int solve(const double *b, double *x, int *iters);
+  int form_fext(double t);
+  int step(xg_step_stats *st);
+  int init_phase();
+  double lambda_of(int p, double t) const {
+    if (p < 0 || p >= 8 || !added[p]) return 0.0;
+    return pattern_const[p] ? lambda_const[p] : t;
+  }
+};
+
+// ---------------------------------------------------------------------------
+// numbering and pattern
+// ---------------------------------------------------------------------------
+int xg_model::number() {
+  // handler IDs: -2 free, -1 SP, -4 MP-constrained
+  eqn.assign((size_t)nn * ndf, -2);
+  auto index_of = [&](int tag) -> int {
+    auto it = std::lower_bound(node_tag.begin(), node_tag.end(), tag);
+    if (it == node_tag.end() || *it != tag) return -1;
+    return (int)(it - node_tag.begin());
+  };
+  for (int s = 0; s < num_sp; s++) {
+    int n = index_of(sp_node[s]);
+    if (n < 0 || sp_dof[s] < 0 || sp_dof[s] >= ndf) return fail(XG_EINVAL, "bad sp %d", s);
+    sp_node[s] = n;
+    eqn[(size_t)n * ndf + sp_dof[s]] = -1;
+  }
+  for (int q = 0; q < num_mp; q++) {
+    int c = index_of(mp_c[q]), r = index_of(mp_r[q]);
+    if (c < 0 || r < 0 || mp_dof[q] < 0 || mp_dof[q] >= ndf) return fail(XG_EINVAL, "bad mp %d", q);
+    mp_c[q] = c;
+    mp_r[q] = r;
+    if (eqn[(size_t)c * ndf + mp_dof[q]] == -2) eqn[(size_t)c * ndf + mp_dof[q]] = -4;
+  }
+  for (int i = 0; i < num_loads; i++) {
+    int n = index_of(load_node[i]);
+    if (n < 0) return fail(XG_EINVAL, "bad load node %d", load_node[i]);
+    load_node[i] = n;
+  }
+  // node graph: vertices in tag order, edges between the nodes of an element
+  std::vector<int64_t> deg(nn + 1, 0);
+  for (int e = 0; e < ne; e++)
+    for (int a = 0; a < nen; a++) deg[conn[(size_t)e * nen + a] + 1] += nen - 1;
+  std::vector<int64_t> aptr(nn + 1, 0);
+  for (int i = 0; i < nn; i++) aptr[i + 1] = aptr[i] + deg[i + 1];
+  std::vector<int> araw(aptr[nn]);
+  std::vector<int64_t> fill(aptr.begin(), aptr.end() - 1);
+  for (int e = 0; e < ne; e++) {
+    const int *c = &conn[(size_t)e * nen];
+    for (int a = 0; a < nen; a++)
+      for (int b = 0; b < nen; b++)
+        if (a != b) araw[fill[c[a]]++] = c[b];
+  }
+  std::vector<int64_t> adjp(nn + 1, 0);
+  std::vector<int> adj;
+  adj.reserve(araw.size());
+  for (int n = 0; n < nn; n++) {
+    auto b = araw.begin() + aptr[n], en = araw.begin() + aptr[n + 1];
+    std::sort(b, en);
+    auto last = std::unique(b, en);
+    for (auto it = b; it != last; ++it)
+      if (*it != n) adj.push_back(*it);
+    adjp[n + 1] = (int64_t)adj.size();
+  }
+  std::vector<int>().swap(araw);
+  // reverse Cuthill-McKee from the first vertex (RCM(false))
+  std::vector<int> mark(nn, -1), res(nn, 0);
+  if (nn > 0) {
+    int cur = nn - 1, next = cur - 1, iter = 0;
+    res[cur] = 0;
+    mark[0] = cur;
+    while (next >= 0) {
+      const int v = res[cur];
+      for (int64_t k = adjp[v]; k < adjp[v + 1]; k++) {
+        const int w = adj[k];
+        if (mark[w] == -1) {
+          mark[w] = next;
+          res[next--] = w;
+        }
+      }
+      cur--;
+      if (cur == next && cur >= 0) {
+        while (iter < nn && mark[iter] != -1) iter++;
+        if (iter >= nn) break;
+        const int w = iter++;
+        next--;
+        mark[w] = cur;
+        res[cur] = w;
+      }
+    }
+  }
+  // equations in RCM order; diagonal blocks = the free dofs of one node
+  int eq = 0;
+  blk_start.clear();
+  for (int i = 0; i < nn; i++) {
+    const int n = res[i];
+    const int before = eq;
+    for (int j = 0; j < ndf; j++)
+      if (eqn[(size_t)n * ndf + j] == -2) eqn[(size_t)n * ndf + j] = eq++;
+    if (eq > before) blk_start.push_back(before);
+  }
+  blk_start.push_back(eq);
+  neq = eq;
+  for (int q = 0; q < num_mp; q++) {
+    int &id = eqn[(size_t)mp_c[q] * ndf + mp_dof[q]];
+    if (id == -4) id = eqn[(size_t)mp_r[q] * ndf + mp_dof[q]];
+    if (id < 0) return fail(XG_EINVAL, "equalDOF on a constrained retained dof (mp %d)", q);
+  }
+  // pattern: row r = diagonal + equations sharing an element with r
+  std::vector<int> owners(neq, -1);      // single owner node, or -2 when shared
+  for (int n = 0; n < nn; n++)
+    for (int j = 0; j < ndf; j++) {
+      const int r = eqn[(size_t)n * ndf + j];
+      if (r < 0) continue;
+      if (owners[r] == -1) owners[r] = n;
+      else if (owners[r] != n) owners[r] = -2;
+    }
+  auto node_cols = [&](int n, std::vector<int> &out) {
+    out.clear();
+    for (int j = 0; j < ndf; j++)
+      if (eqn[(size_t)n * ndf + j] >= 0) out.push_back(eqn[(size_t)n * ndf + j]);
+    for (int64_t k = adjp[n]; k < adjp[n + 1]; k++) {
+      const int o = adj[k];
+      for (int j = 0; j < ndf; j++)
+        if (eqn[(size_t)o * ndf + j] >= 0) out.push_back(eqn[(size_t)o * ndf + j]);
+    }
+    std::sort(out.begin(), out.end());
+    out.erase(std::unique(out.begin(), out.end()), out.end());
+  };
+  std::vector<std::vector<int>> shared_rows;
+  std::vector<int> shared_index(neq, -1);
+  for (int r = 0; r < neq; r++)
+    if (owners[r] == -2) {
+      shared_index[r] = (int)shared_rows.size();
+      shared_rows.emplace_back();
+    }
+  std::vector<int> rowlen(neq, 0), tmp;
+  for (int n = 0; n < nn; n++) {
+    bool any = false;
+    for (int j = 0; j < ndf; j++) any |= eqn[(size_t)n * ndf + j] >= 0;
+    if (!any) continue;
+    node_cols(n, tmp);
+    for (int j = 0; j < ndf; j++) {
+      const int r = eqn[(size_t)n * ndf + j];
+      if (r < 0) continue;
+      if (owners[r] >= 0) rowlen[r] = (int)tmp.size();
+      else shared_rows[shared_index[r]].insert(shared_rows[shared_index[r]].end(), tmp.begin(),
+                                                tmp.end());
+    }
+  }
+  for (auto &row : shared_rows) {
+    std::sort(row.begin(), row.end());
+    row.erase(std::unique(row.begin(), row.end()), row.end());
+  }
+  for (int r = 0; r < neq; r++)
+    if (owners[r] == -2) rowlen[r] = (int)shared_rows[shared_index[r]].size();
+  rowptr.assign(neq + 1, 0);
+  for (int r = 0; r < neq; r++) rowptr[r + 1] = rowptr[r] + rowlen[r];
+  nnz = rowptr[neq];
+  colidx.assign((size_t)nnz, 0);
+  for (int n = 0; n < nn; n++) {
+    bool need = false;
+    for (int j = 0; j < ndf; j++) {
+      const int r = eqn[(size_t)n * ndf + j];
+      need |= r >= 0 && owners[r] >= 0;
+    }
+    if (!need) continue;
+    node_cols(n, tmp);
+    for (int j = 0; j < ndf; j++) {
+      const int r = eqn[(size_t)n * ndf + j];
+      if (r >= 0 && owners[r] >= 0) std::copy(tmp.begin(), tmp.end(), colidx.begin() + rowptr[r]);
+    }
+  }
+  for (int r = 0; r < neq; r++)
+    if (owners[r] == -2)
+      std::copy(shared_rows[shared_index[r]].begin(), shared_rows[shared_index[r]].end(),
+                colidx.begin() + rowptr[r]);
+  return 0;
+}
+
+// Element -> CSR slot contributions, in assembly order (element tag order,
+// then the element matrix in row-major order), as FE_Element::addKtToTang /
+// SparseGenColLinSOE::addA accumulate them.
+int xg_model::build_maps(HostGather &gk_h, HostGather &gr_h) {
+  const int ks = ke_size();
+  std::vector<int> slot_of;
+  std::vector<int64_t> src_of;
+  slot_of.reserve((size_t)ne * ned * ned);
+  src_of.reserve((size_t)ne * ned * ned);
+  std::vector<int> ids(ned);
+  // pair index for the brick's upper node-pair blocks
+  int pair_of[8][8];
+  for (int a = 0, p = 0; a < 8; a++)
+    for (int b = a; b < 8; b++, p++) { pair_of[a][b] = p; pair_of[b][a] = p; }
+  for (int e = 0; e < ne; e++) {
+    for (int a = 0; a < nen; a++)
+      for (int j = 0; j < ndf; j++) ids[a * ndf + j] = eqn[(size_t)conn[(size_t)e * nen + a] * ndf + j];
+    for (int i = 0; i < ned; i++) {
+      const int r = ids[i];
+      if (r < 0) continue;
+      const int *rb = &colidx[rowptr[r]], *re = &colidx[rowptr[r + 1]];
+      for (int j = 0; j < ned; j++) {
+        const int c = ids[j];
+        if (c < 0) continue;
+        const int *pos = std::lower_bound(rb, re, c);
+        if (pos == re || *pos != c) return fail(XG_EINVAL, "pattern lookup failed");
+        slot_of.push_back((int)(pos - colidx.data()));
+        int64_t src;
+        if (etype == XG_ELE_QUAD) {
+          src = (int64_t)e * ks + i * ned + j;
+        } else {
+          const int a = i / 3, ii = i % 3, b = j / 3, kk = j % 3;
+          const int p = pair_of[a][b];
+          src = (int64_t)e * ks + p * 9 + (a <= b ? ii * 3 + kk : kk * 3 + ii);
+        }
+        src_of.push_back(src);
+      }
+    }
+  }
+  build_gather(nnz, slot_of, src_of, gk_h);
+  slot_of.clear();
+  src_of.clear();
+  for (int e = 0; e < ne; e++)
+    for (int a = 0; a < nen; a++)
+      for (int j = 0; j < ndf; j++) {
+        const int r = eqn[(size_t)conn[(size_t)e * nen + a] * ndf + j];
+        if (r < 0) continue;
+        slot_of.push_back(r);
+        src_of.push_back((int64_t)e * ned + a * ndf + j);
+      }
+  build_gather(neq, slot_of, src_of, gr_h);
+  return 0;
+}
+
+int xg_model::upload(const HostGather &gk_h, const HostGather &gr_h) {
+  cudaStream_t s = stream;
+  // SoA connectivity and coordinates
+  std::vector<int> conn_soa((size_t)ne * nen);
+  for (int e = 0; e < ne; e++)
+    for (int a = 0; a < nen; a++) conn_soa[(size_t)a * ne + e] = conn[(size_t)e * nen + a];
+  std::vector<double> crd_soa((size_t)nn * ndm);
+  for (int n = 0; n < nn; n++)
+    for (int k = 0; k < ndm; k++) crd_soa[(size_t)k * nn + n] = crd[(size_t)n * ndm + k];
+  RET(d_conn.upload(conn_soa.data(), conn_soa.size(), s));
+  RET(d_crd.upload(crd_soa.data(), crd_soa.size(), s));
+  RET(d_mat.upload(mat.data(), mat.size(), s));
+  RET(d_j2.upload(j2.data(), j2.size(), s));
+  RET(d_eqn.upload(eqn.data(), eqn.size(), s));
+  RET(d_rowptr.upload(rowptr.data(), rowptr.size(), s));
+  RET(d_colidx.upload(colidx.data(), colidx.size(), s));
+  RET(d_blk.upload(blk_start.data(), blk_start.size(), s));
+  const size_t nu = (size_t)nn * ndf;
+  RET(d_U.alloc(nu)); RET(d_Uc.alloc(nu));
+  CK(cudaMemsetAsync(d_U.p, 0, nu * sizeof(double), s));
+  CK(cudaMemsetAsync(d_Uc.p, 0, nu * sizeof(double), s));
+  const long np = npts();
+  RET(d_epc.alloc(np * nhist())); RET(d_ept.alloc(np * nhist()));
+  RET(d_xic.alloc(np)); RET(d_xit.alloc(np));
+  RET(d_sig.alloc(np * nsig())); RET(d_tan.alloc(np * ntan()));
+  RET(d_sig_c.alloc(np * nsig())); RET(d_tan_c.alloc(np * ntan()));
+  RET(d_status.alloc(ne));
+  RET(d_Ke.alloc((size_t)ne * ke_size()));
+  RET(d_Re.alloc((size_t)ne * ned));
+  RET(d_vals.alloc(nnz > 0 ? nnz : 1)); RET(d_resid.alloc(neq > 0 ? neq : 1));
+  RET(d_gk_slot_chunk.upload(gk_h.slot_chunk.data(), gk_h.slot_chunk.size(), s));
+  RET(d_gk_chunk_slot.upload(gk_h.chunk_slot.data(), gk_h.chunk_slot.size(), s));
+  RET(d_gk_chunk_begin.upload(gk_h.chunk_begin.data(), gk_h.chunk_begin.size(), s));
+  RET(d_gk_src.upload(gk_h.src.data(), gk_h.src.size(), s));
+  RET(d_gr_slot_chunk.upload(gr_h.slot_chunk.data(), gr_h.slot_chunk.size(), s));
+  RET(d_gr_chunk_slot.upload(gr_h.chunk_slot.data(), gr_h.chunk_slot.size(), s));
+  RET(d_gr_chunk_begin.upload(gr_h.chunk_begin.data(), gr_h.chunk_begin.size(), s));
+  RET(d_gr_src.upload(gr_h.src.data(), gr_h.src.size(), s));
+  gk.nslots = nnz; gk.nchunks = (int)gk_h.chunk_slot.size();
+  gk.chunk_slot = d_gk_chunk_slot.p; gk.chunk_begin = d_gk_chunk_begin.p;
+  gk.slot_chunk = d_gk_slot_chunk.p; gk.src = d_gk_src.p;
+  gr.nslots = neq; gr.nchunks = (int)gr_h.chunk_slot.size();
+  gr.chunk_slot = d_gr_chunk_slot.p; gr.chunk_begin = d_gr_chunk_begin.p;
+  gr.slot_chunk = d_gr_slot_chunk.p; gr.src = d_gr_src.p;
+  RET(d_partial.alloc(std::max(gk.nchunks, gr.nchunks) + 1));
+  // solver
+  const int nblk = (int)blk_start.size() - 1;
+  RET(d_binv.alloc((size_t)std::max(nblk, 1) * 36));
+  const size_t nv = neq > 0 ? neq : 1;
+  RET(d_r.alloc(nv)); RET(d_z.alloc(nv)); RET(d_p.alloc(nv)); RET(d_q.alloc(nv));
+  RET(d_pcg_part.alloc(3 * (size_t)pcg_max_blocks() + 8));
+  RET(d_scalars.alloc(8));
+  RET(d_barrier.alloc(2));
+  RET(d_flags.alloc(4));
+  pcg.n = neq; pcg.rowptr = d_rowptr.p; pcg.colidx = d_colidx.p; pcg.vals = d_vals.p;
+  pcg.nblk = nblk; pcg.blk_start = d_blk.p; pcg.binv = d_binv.p;
+  pcg.r = d_r.p; pcg.z = d_z.p; pcg.p = d_p.p; pcg.q = d_q.p;
+  pcg.partials = d_pcg_part.p; pcg.barrier = d_barrier.p; pcg.flags = d_flags.p;
+  pcg.scalars = d_scalars.p;
+  RET(d_fext.alloc(nv)); RET(d_B.alloc(nv)); RET(d_dU.alloc(nv)); RET(d_phat.alloc(nv));
+  RET(d_dUhat.alloc(nv)); RET(d_x.alloc(nv)); RET(d_b.alloc(nv)); RET(d_norm.alloc(1));
+  // reference load vector of every pattern that has nodal loads
+  std::vector<int> pats;
+  for (int i = 0; i < num_loads; i++)
+    if (std::find(pats.begin(), pats.end(), load_pat[i]) == pats.end()) pats.push_back(load_pat[i]);
+  ref_patterns = pats;
+  std::vector<double> F(pats.size() * nv, 0.0);
+  for (size_t k = 0; k < pats.size(); k++)
+    for (int i = 0; i < num_loads; i++) {
+      if (load_pat[i] != pats[k]) continue;
+      for (int j = 0; j < ndf; j++) {
+        const int r = eqn[(size_t)load_node[i] * ndf + j];
+        if (r >= 0) F[k * nv + r] += load_val[(size_t)i * ndf + j];
+      }
+    }
+  if (!F.empty()) RET(d_Fref.upload(F.data(), F.size(), s));
+  // zero-strain material state
+  RET(launch_j2_zero_state(view(), s));
+  CK(cudaMemcpyAsync(d_sig_c.p, d_sig.p, np * nsig() * sizeof(double), cudaMemcpyDeviceToDevice, s));
+  CK(cudaMemcpyAsync(d_tan_c.p, d_tan.p, np * ntan() * sizeof(double), cudaMemcpyDeviceToDevice, s));
+  CK(cudaStreamSynchronize(s));
+  return 0;
+}
+
+// Domain::update (when compute) and the element K / P assembled into the
+// CSR values and the resisting force.
+int xg_model::element_state(bool compute) {
+  ContinuumView v = view();
+  cudaStream_t s = stream;
+  if (etype == XG_ELE_QUAD) {
+    if (compute) RET(launch_quad_update(v, s));
+    RET(launch_quad_assemble(v, s));
+  } else {
+    if (compute) RET(launch_brick_update(v, s));
+    RET(launch_brick_assemble(v, s));
+  }
+  RET(launch_gather(gk, d_Ke.p, d_partial.p, d_vals.p, s));
+  RET(launch_gather(gr, d_Re.p, d_partial.p, d_resid.p, s));
+  blocks_factored = false;
+  return 0;
+}
+
+int xg_model::solve(const double *b, double *x, int *iters) {
+  if (!blocks_factored) {
+    RET(pcg_factor_blocks(pcg, stream));
+    blocks_factored = true;
+  }
+  CK(cudaMemsetAsync(x, 0, (neq > 0 ? neq : 1) * sizeof(double), stream));
+  double relres = 0.0;
+  int it = 0;
+  int r = pcg_solve(pcg, b, x, rtol, maxit, &it, &relres, stream);
+  last_solver_iters += it;
+  if (iters) *iters = it;
+  if (r != 0)
+    return fail(XG_ESOLVE, "PCG did not converge: %d iterations, relative residual %.3e", it,
+                relres);
+  return 0;
+}
+
+int xg_model::form_fext(double t) {
+  CK(cudaMemsetAsync(d_fext.p, 0, (neq > 0 ? neq : 1) * sizeof(double), stream));
+  for (size_t k = 0; k < ref_patterns.size(); k++) {
+    const double lam = lambda_of(ref_patterns[k], t);
+    if (lam != 0.0) RET(launch_axpy(neq, lam, d_Fref.p + k * (size_t)(neq > 0 ? neq : 1), d_fext.p, stream));
+  }
+  return 0;
+}
+
+// Phase set-up: DisplacementControl::domainChanged (phat, :372-392).
+int xg_model::init_phase() {
+  if (phase.pattern >= 0 && phase.pattern < 8) added[phase.pattern] = 1;
+  dc_eq = -1;
+  if (phase.integrator == XG_INT_DISP_CONTROL) {
+    auto it = std::lower_bound(node_tag.begin(), node_tag.end(), phase.dc_node);
+    if (it == node_tag.end() || *it != phase.dc_node) return fail(XG_EINVAL, "bad control node");
+    const int n = (int)(it - node_tag.begin());
+    if (phase.dc_dof < 0 || phase.dc_dof >= ndf) return fail(XG_EINVAL, "bad control dof");
+    dc_eq = eqn[(size_t)n * ndf + phase.dc_dof];
+    if (dc_eq < 0) return fail(XG_EINVAL, "control dof is constrained");
+    RET(form_fext(time + 1.0));
+    RET(element_state(false));
+    RET(launch_sub(neq, d_fext.p, d_resid.p, d_phat.p, stream));
+  } else if (phase.integrator != XG_INT_LOAD_CONTROL) {
+    return fail(XG_EINVAL, "integrator %d not supported by the continuum set", phase.integrator);
+  }
+  return 0;
+}
+
+static int read_scalar(const double *d, double *h, cudaStream_t s) {
+  if (cudaMemcpyAsync(h, d, sizeof(double), cudaMemcpyDeviceToHost, s) != cudaSuccess) return XG_ECUDA;
+  if (cudaStreamSynchronize(s) != cudaSuccess) return XG_ECUDA;
+  return 0;
+}
+
+// One step: integrator newStep, NewtonRaphson::solveCurrentStep, commit
+// (runtime/runtime/BasicAnalysisBuilder.cpp:337-420).
+int xg_model::step(xg_step_stats *st) {
+  cudaStream_t s = stream;
+  last_solver_iters = 0;
+  const int nu = nn * ndf;
+  const double t_commit = time;
+  if (phase.integrator == XG_INT_LOAD_CONTROL) {
+    // LoadControl::newStep (Static/LoadControl.cpp:70-100); PlainHandler
+    // updates no element before formUnbalance
+    time += phase.d_lambda;
+    RET(element_state(false));
+  } else {
+    // DisplacementControl::newStep (Static/DisplacementControl.cpp:121-200)
+    RET(element_state(false));
+    RET(solve(d_phat.p, d_dUhat.p, nullptr));
+    double dUahat;
+    RET(read_scalar(d_dUhat.p + dc_eq, &dUahat, s));
+    if (dUahat == 0.0) return fail(XG_ESOLVE, "zero reference displacement at the control dof");
+    const double dlambda = phase.dc_incr / dUahat;
+    time += dlambda;
+    RET(launch_scatter_incr(nu, d_eqn.p, d_dUhat.p, dlambda, d_U.p, s));
+    RET(element_state(true));
+  }
+  RET(form_fext(time));
+  RET(launch_sub(neq, d_fext.p, d_resid.p, d_B.p, s));
+  int it = 0;
+  bool ok = false;
+  while (true) {
+    RET(solve(d_B.p, d_dU.p, nullptr));
+    if (phase.integrator == XG_INT_DISP_CONTROL) {
+      // DisplacementControl::update (:202-250)
+      RET(solve(d_phat.p, d_dUhat.p, nullptr));
+      double dUahat, dUabar;
+      RET(read_scalar(d_dUhat.p + dc_eq, &dUahat, s));
+      RET(read_scalar(d_dU.p + dc_eq, &dUabar, s));
+      if (dUahat == 0.0) return fail(XG_ESOLVE, "zero reference displacement at the control dof");
+      const double dLambda = -dUabar / dUahat;
+      RET(launch_axpy(neq, dLambda, d_dUhat.p, d_dU.p, s));
+      time += dLambda;
+    }
+    RET(launch_scatter_incr(nu, d_eqn.p, d_dU.p, 1.0, d_U.p, s));
+    RET(element_state(true));
+    RET(form_fext(time));
+    RET(launch_sub(neq, d_fext.p, d_resid.p, d_B.p, s));
+    it++;
+    RET(launch_norm2(neq, phase.test == XG_TEST_NORM_DISP_INCR ? d_dU.p : d_B.p, d_partial.p,
+                     d_norm.p, s));
+    double n2;
+    RET(read_scalar(d_norm.p, &n2, s));
+    if (std::sqrt(n2) <= phase.tol) { ok = true; break; }
+    if (it >= phase.max_iter) break;
+  }
+  if (st) {
+    st->newton_iters = it;
+    st->solver_iters = last_solver_iters;
+    st->elem_iters = 0;
+    st->status = ok ? 0 : XG_ENOCONV;
+  }
+  if (!ok) {
+    time = t_commit;
+    return fail(XG_ENOCONV, "Newton did not converge in %d iterations", it);
+  }
+  // commit (Domain::commit -> material commitState)
+  const long np = npts();
+  CK(cudaMemcpyAsync(d_epc.p, d_ept.p, np * nhist() * sizeof(double), cudaMemcpyDeviceToDevice, s));
+  CK(cudaMemcpyAsync(d_xic.p, d_xit.p, np * sizeof(double), cudaMemcpyDeviceToDevice, s));
+  CK(cudaMemcpyAsync(d_sig_c.p, d_sig.p, np * nsig() * sizeof(double), cudaMemcpyDeviceToDevice, s));
+  CK(cudaMemcpyAsync(d_tan_c.p, d_tan.p, np * ntan() * sizeof(double), cudaMemcpyDeviceToDevice, s));
+  CK(cudaMemcpyAsync(d_Uc.p, d_U.p, (size_t)nu * sizeof(double), cudaMemcpyDeviceToDevice, s));
+  time_c = time;
+  return 0;
+}
+
+// ---------------------------------------------------------------------------
+// C ABI
+// ---------------------------------------------------------------------------
+extern "C" {
+
+const char *xg_last_error(void) { return g_err.c_str(); }
+int xg_version(void) { return 1; }
+
+static int plan_model(const xg_model_desc *d, xg_model **out);
+
+int xg_model_create(const xg_model_desc *d, xg_model **out) {
+  g_err.clear();
+  if (!d || !out) return fail(XG_EINVAL, "null argument");
+  *out = nullptr;
+  xg_model *m = nullptr;
+  int r = plan_model(d, &m);
+  if (r) return r;
+  HostGather gk_h, gr_h;
+  r = m->build_maps(gk_h, gr_h);
+  if (r) { delete m; return r; }
+  if (cudaStreamCreateWithFlags(&m->stream, cudaStreamNonBlocking) != cudaSuccess) {
+    delete m;
+    return fail(XG_ECUDA, "no CUDA device");
+  }
+  r = m->upload(gk_h, gr_h);
+  if (r) { delete m; return r; }
+  *out = m;
+  return 0;
+}
+
+int xg_model_plan(const xg_model_desc *d, int *eqn, int *rowptr, int *colidx, int *num_eqn,
+                  int *nnz) {
+  g_err.clear();
+  if (!d) return fail(XG_EINVAL, "null argument");
+  xg_model *m = nullptr;
+  int r = plan_model(d, &m);
+  if (r) return r;
+  if (num_eqn) *num_eqn = m->neq;
+  if (nnz) *nnz = m->nnz;
+  if (eqn) std::copy(m->eqn.begin(), m->eqn.end(), eqn);
+  if (rowptr) std::copy(m->rowptr.begin(), m->rowptr.end(), rowptr);
+  if (colidx) std::copy(m->colidx.begin(), m->colidx.end(), colidx);
+  delete m;
+  return 0;
+}
+
+// Host part of model creation: validate and copy the description, number
+// the DOFs and build the pattern.  No device work.
+static int plan_model(const xg_model_desc *d, xg_model **out) {
+  if (d->elem_type != XG_ELE_QUAD && d->elem_type != XG_ELE_BRICK)
+    return fail(XG_EINVAL, "element type %d not supported", d->elem_type);
+  if (d->elem_type == XG_ELE_QUAD && (d->ndm != 2 || d->ndf != 2))
+    return fail(XG_EINVAL, "quad needs ndm 2, ndf 2");
+  if (d->elem_type == XG_ELE_BRICK && (d->ndm != 3 || d->ndf != 3))
+    return fail(XG_EINVAL, "stdBrick needs ndm 3, ndf 3");
+  if (d->num_nodes <= 0 || d->num_elems < 0 || !d->node_tag || !d->node_crd)
+    return fail(XG_EINVAL, "empty model");
+  if (d->num_elems > 0 && (!d->elem_tag || !d->elem_conn || !d->elem_mat || !d->j2_param))
+    return fail(XG_EINVAL, "missing element arrays");
+  if (d->handler != XG_HANDLER_PLAIN)
+    return fail(XG_EINVAL, "only the Plain constraint handler is supported");
+  for (int i = 0; i < d->num_sp; i++)
+    if (d->sp_pattern && d->sp_pattern[i] >= 0)
+      return fail(XG_EINVAL, "imposed sp values need the Transformation handler");
+  auto *m = new xg_model();
+  m->ndm = d->ndm; m->ndf = d->ndf; m->nn = d->num_nodes; m->ne = d->num_elems;
+  m->etype = d->elem_type;
+  m->nen = d->elem_type == XG_ELE_QUAD ? 4 : 8;
+  m->nip = m->nen;
+  m->ned = m->nen * m->ndf;
+  m->thickness = d->thickness;
+  m->node_tag.assign(d->node_tag, d->node_tag + m->nn);
+  for (int i = 1; i < m->nn; i++)
+    if (m->node_tag[i] <= m->node_tag[i - 1]) {
+      delete m;
+      return fail(XG_EINVAL, "node tags must be strictly ascending");
+    }
+  m->crd.assign(d->node_crd, d->node_crd + (size_t)m->nn * m->ndm);
+  m->elem_tag.assign(d->elem_tag, d->elem_tag + m->ne);
+  for (int i = 1; i < m->ne; i++)
+    if (m->elem_tag[i] <= m->elem_tag[i - 1]) {
+      delete m;
+      return fail(XG_EINVAL, "element tags must be strictly ascending");
+    }
+  m->conn.resize((size_t)m->ne * m->nen);
+  for (size_t k = 0; k < m->conn.size(); k++) {
+    auto it = std::lower_bound(m->node_tag.begin(), m->node_tag.end(), d->elem_conn[k]);
+    if (it == m->node_tag.end() || *it != d->elem_conn[k]) {
+      const size_t bad_elem = k / m->nen;
+      delete m;
+      return fail(XG_EINVAL, "element %zu refers to a missing node", bad_elem);
+    }
+    m->conn[k] = (int)(it - m->node_tag.begin());
+  }
+  m->mat.assign(d->elem_mat, d->elem_mat + m->ne);
+  m->j2.assign(d->j2_param, d->j2_param + (size_t)d->num_j2 * XG_J2_NPARAM);
+  for (int e = 0; e < m->ne; e++)
+    if (m->mat[e] < 0 || m->mat[e] >= d->num_j2) {
+      delete m;
+      return fail(XG_EINVAL, "element %d: J2 row out of range", e);
+    }
+  m->num_sp = d->num_sp; m->num_mp = d->num_mp; m->num_loads = d->num_loads;
+  m->handler = d->handler;
+  if (m->num_sp) {
+    m->sp_node.assign(d->sp_node, d->sp_node + m->num_sp);
+    m->sp_dof.assign(d->sp_dof, d->sp_dof + m->num_sp);
+  }
+  if (m->num_mp) {
+    m->mp_r.assign(d->mp_retained, d->mp_retained + m->num_mp);
+    m->mp_c.assign(d->mp_constrained, d->mp_constrained + m->num_mp);
+    m->mp_dof.assign(d->mp_dof, d->mp_dof + m->num_mp);
+  }
+  if (m->num_loads) {
+    m->load_node.assign(d->load_node, d->load_node + m->num_loads);
+    m->load_pat.assign(d->load_pattern, d->load_pattern + m->num_loads);
+    m->load_val.assign(d->load_value, d->load_value + (size_t)m->num_loads * m->ndf);
+    for (int p : m->load_pat)
+      if (p < 0 || p >= 8) {
+        delete m;
+        return fail(XG_EINVAL, "load pattern must be in [0, 8)");
+      }
+  }
+  int r = m->number();
+  if (r) { delete m; return r; }
+  *out = m;
+  return 0;
+}
+
+int xg_model_destroy(xg_model *m) {
+  delete m;
+  return 0;
+}
+
+int xg_model_sizes(const xg_model *m, int *num_eqn, int *nnz) {
+  if (!m) return fail(XG_EINVAL, "null model");
+  if (num_eqn) *num_eqn = m->neq;
+  if (nnz) *nnz = m->nnz;
+  return 0;
+}
+
+int xg_model_numbering(const xg_model *m, int *eqn) {
+  if (!m || !eqn) return fail(XG_EINVAL, "null argument");
+  std::copy(m->eqn.begin(), m->eqn.end(), eqn);
+  return 0;
+}
+
+int xg_model_pattern(const xg_model *m, int *rowptr, int *colidx) {
+  if (!m || !rowptr || !colidx) return fail(XG_EINVAL, "null argument");
+  std::copy(m->rowptr.begin(), m->rowptr.end(), rowptr);
+  std::copy(m->colidx.begin(), m->colidx.end(), colidx);
+  return 0;
+}
+
+int xg_elemset_set_trial_disp(xg_model *m, const double *u) {
+  if (!m || !u) return fail(XG_EINVAL, "null argument");
+  CK(cudaMemcpyAsync(m->d_U.p, u, (size_t)m->nn * m->ndf * sizeof(double), cudaMemcpyHostToDevice,
+                     m->stream));
+  CK(cudaStreamSynchronize(m->stream));
+  return 0;
+}
+
+int xg_elemset_update(xg_model *m, double *csr_vals, double *resid) {
+  if (!m) return fail(XG_EINVAL, "null model");
+  RET(m->element_state(true));
+  if (csr_vals)
+    CK(cudaMemcpyAsync(csr_vals, m->d_vals.p, (size_t)m->nnz * sizeof(double),
+                       cudaMemcpyDeviceToHost, m->stream));
+  if (resid)
+    CK(cudaMemcpyAsync(resid, m->d_resid.p, (size_t)m->neq * sizeof(double),
+                       cudaMemcpyDeviceToHost, m->stream));
+  std::vector<int> st(m->ne);
+  if (m->ne)
+    CK(cudaMemcpyAsync(st.data(), m->d_status.p, (size_t)m->ne * sizeof(int),
+                       cudaMemcpyDeviceToHost, m->stream));
+  CK(cudaStreamSynchronize(m->stream));
+  int bad = 0;
+  for (int v : st) bad += v != 0;
+  return bad ? -bad : 0;
+}
+
+int xg_elemset_commit(xg_model *m) {
+  if (!m) return fail(XG_EINVAL, "null model");
+  const long np = m->npts();
+  cudaStream_t s = m->stream;
+  CK(cudaMemcpyAsync(m->d_epc.p, m->d_ept.p, np * m->nhist() * sizeof(double), cudaMemcpyDeviceToDevice, s));
+  CK(cudaMemcpyAsync(m->d_xic.p, m->d_xit.p, np * sizeof(double), cudaMemcpyDeviceToDevice, s));
+  CK(cudaMemcpyAsync(m->d_sig_c.p, m->d_sig.p, np * m->nsig() * sizeof(double), cudaMemcpyDeviceToDevice, s));
+  CK(cudaMemcpyAsync(m->d_tan_c.p, m->d_tan.p, np * m->ntan() * sizeof(double), cudaMemcpyDeviceToDevice, s));
+  CK(cudaMemcpyAsync(m->d_Uc.p, m->d_U.p, (size_t)m->nn * m->ndf * sizeof(double), cudaMemcpyDeviceToDevice, s));
+  CK(cudaStreamSynchronize(s));
+  return 0;
+}
+
+// revertToLastCommit: the trial state returns to the state at the last commit
+int xg_elemset_revert(xg_model *m) {
+  if (!m) return fail(XG_EINVAL, "null model");
+  const long np = m->npts();
+  cudaStream_t s = m->stream;
+  CK(cudaMemcpyAsync(m->d_ept.p, m->d_epc.p, np * m->nhist() * sizeof(double), cudaMemcpyDeviceToDevice, s));
+  CK(cudaMemcpyAsync(m->d_xit.p, m->d_xic.p, np * sizeof(double), cudaMemcpyDeviceToDevice, s));
+  CK(cudaMemcpyAsync(m->d_sig.p, m->d_sig_c.p, np * m->nsig() * sizeof(double), cudaMemcpyDeviceToDevice, s));
+  CK(cudaMemcpyAsync(m->d_tan.p, m->d_tan_c.p, np * m->ntan() * sizeof(double), cudaMemcpyDeviceToDevice, s));
+  CK(cudaMemcpyAsync(m->d_U.p, m->d_Uc.p, (size_t)m->nn * m->ndf * sizeof(double), cudaMemcpyDeviceToDevice, s));
+  CK(cudaStreamSynchronize(s));
+  m->time = m->time_c;
+  return 0;
+}
+
+int xg_elemset_revert_to_start(xg_model *m) { return xg_reset(m); }
+
+int xg_elemset_get_history(const xg_model *m, int which, double *out, long cap) {
+  if (!m || !out) return fail(XG_EINVAL, "null argument");
+  if (which != 0) return fail(XG_EINVAL, "history kind %d not held by this model", which);
+  const long np = m->npts(), nh = m->nhist();
+  const long need = np * (nh + 1);
+  if (cap < need) return fail(XG_EINVAL, "history needs %ld doubles", need);
+  CK(cudaMemcpyAsync(out, m->d_epc.p, np * nh * sizeof(double), cudaMemcpyDeviceToHost, m->stream));
+  CK(cudaMemcpyAsync(out + np * nh, m->d_xic.p, np * sizeof(double), cudaMemcpyDeviceToHost, m->stream));
+  CK(cudaStreamSynchronize(m->stream));
+  return (int)std::min<long>(need, 0x7fffffff);
+}
+
+int xg_elemset_set_history(xg_model *m, int which, const double *in, long n) {
+  if (!m || !in) return fail(XG_EINVAL, "null argument");
+  if (which != 0) return fail(XG_EINVAL, "history kind %d not held by this model", which);
+  const long np = m->npts(), nh = m->nhist();
+  if (n != np * (nh + 1)) return fail(XG_EINVAL, "history needs %ld doubles", np * (nh + 1));
+  CK(cudaMemcpyAsync(m->d_epc.p, in, np * nh * sizeof(double), cudaMemcpyHostToDevice, m->stream));
+  CK(cudaMemcpyAsync(m->d_xic.p, in + np * nh, np * sizeof(double), cudaMemcpyHostToDevice, m->stream));
+  CK(cudaStreamSynchronize(m->stream));
+  return 0;
+}
+
+int xg_soe_solve(xg_model *m, const double *b, double *x, double rtol, int maxit, int *iters,
+                 double *relres) {
+  if (!m || !b || !x) return fail(XG_EINVAL, "null argument");
+  CK(cudaMemcpyAsync(m->d_b.p, b, (size_t)m->neq * sizeof(double), cudaMemcpyHostToDevice, m->stream));
+  if (!m->blocks_factored) {
+    RET(pcg_factor_blocks(m->pcg, m->stream));
+    m->blocks_factored = true;
+  }
+  CK(cudaMemsetAsync(m->d_x.p, 0, (size_t)std::max(m->neq, 1) * sizeof(double), m->stream));
+  int it = 0;
+  double rr = 0.0;
+  int r = pcg_solve(m->pcg, m->d_b.p, m->d_x.p, rtol, maxit, &it, &rr, m->stream);
+  if (iters) *iters = it;
+  if (relres) *relres = rr;
+  CK(cudaMemcpyAsync(x, m->d_x.p, (size_t)m->neq * sizeof(double), cudaMemcpyDeviceToHost, m->stream));
+  CK(cudaStreamSynchronize(m->stream));
+  if (r) return fail(XG_ESOLVE, "PCG: %d iterations, relative residual %.3e", it, rr);
+  return 0;
+}
+
+int xg_analysis_set_phase(xg_model *m, const xg_phase_desc *ph) {
+  if (!m || !ph) return fail(XG_EINVAL, "null argument");
+  m->phase = *ph;
+  m->have_phase = true;
+  m->phase_steps_done = 0;
+  m->phase_closed = false;
+  return m->init_phase();
+}
+
+int xg_analysis_set_solver(xg_model *m, double rtol, int maxit) {
+  if (!m || rtol <= 0.0 || maxit <= 0) return fail(XG_EINVAL, "bad solver settings");
+  m->rtol = rtol;
+  m->maxit = maxit;
+  return 0;
+}
+
+int xg_analyze(xg_model *m, int num_steps, xg_step_stats *stats) {
+  if (!m) return fail(XG_EINVAL, "null model");
+  if (!m->have_phase) return fail(XG_ESTATE, "no analysis phase set");
+  g_err.clear();
+  for (int i = 0; i < num_steps; i++) {
+    int r = m->step(stats ? &stats[i] : nullptr);
+    if (r) {
+      // BasicAnalysisBuilder::analyzeStatic: revert to the last commit
+      std::string keep = g_err;
+      xg_elemset_revert(m);
+      g_err = keep;
+      return r;
+    }
+    m->phase_steps_done++;
+  }
+  // `loadConst -time 0.0` once the phase has run all of its steps
+  if (m->phase.load_const && m->phase_steps_done >= m->phase.num_steps && !m->phase_closed) {
+    m->phase_closed = true;
+    for (int p = 0; p < 8; p++)
+      if (m->added[p] && !m->pattern_const[p]) {
+        m->pattern_const[p] = 1;
+        m->lambda_const[p] = m->time;
+      }
+    m->time = m->time_c = 0.0;
+  }
+  return 0;
+}
+
+int xg_get_disp(const xg_model *m, double *u, double *lambda) {
+  if (!m) return fail(XG_EINVAL, "null model");
+  if (u) {
+    CK(cudaMemcpyAsync(u, m->d_Uc.p, (size_t)m->nn * m->ndf * sizeof(double),
+                       cudaMemcpyDeviceToHost, m->stream));
+    CK(cudaStreamSynchronize(m->stream));
+  }
+  if (lambda) *lambda = m->time_c;
+  return 0;
+}
+
+int xg_reset(xg_model *m) {
+  if (!m) return fail(XG_EINVAL, "null model");
+  cudaStream_t s = m->stream;
+  const size_t nu = (size_t)m->nn * m->ndf;
+  CK(cudaMemsetAsync(m->d_U.p, 0, nu * sizeof(double), s));
+  CK(cudaMemsetAsync(m->d_Uc.p, 0, nu * sizeof(double), s));
+  RET(launch_j2_zero_state(m->view(), s));
+  const long np = m->npts();
+  CK(cudaMemcpyAsync(m->d_sig_c.p, m->d_sig.p, np * m->nsig() * sizeof(double), cudaMemcpyDeviceToDevice, s));
+  CK(cudaMemcpyAsync(m->d_tan_c.p, m->d_tan.p, np * m->ntan() * sizeof(double), cudaMemcpyDeviceToDevice, s));
+  CK(cudaStreamSynchronize(s));
+  m->time = m->time_c = 0.0;
+  for (int p = 0; p < 8; p++) {
+    m->pattern_const[p] = 0;
+    m->added[p] = 0;
+    m->lambda_const[p] = 0.0;
+  }
+  m->have_phase = false;
+  return 0;
+}
+
+}  // extern "C"

@@ -1,0 +1,323 @@
+// xg_pcg.cu -- block-Jacobi preconditioned conjugate gradients, FP64.
+//
+// The whole solve is one cooperative, persistent launch: every block owns a
+// grid-stride share of the rows, SpMV runs warp-per-row over the CSR arrays,
+// and the three inner products of an iteration are reduced deterministically
+// (fixed-order block partials, then every block sums the partials in the same
+// order), so the iterates are bit-identical run to run.  Blocks meet at a
+// grid barrier whose wait is bounded by the global timer: a block that waits
+// longer than kBarrierTimeoutNs raises flags[0] and every block leaves the
+// solve, so a fault can never hang the GPU.
+#include <cooperative_groups.h>
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+#include "xg_internal.h"
+
+namespace xg {
+
+namespace {
+
+constexpr int kPcgThreads = 512;
+constexpr unsigned long long kBarrierTimeoutNs = 2000000000ull;  // 2 s
+
+__device__ __forceinline__ unsigned long long global_ns() {
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+
+// Sense-reversing grid barrier: bar[0] arrivals, bar[1] generation.
+// Returns false (and sets flags[0]) on timeout or when another block did.
+__device__ bool grid_barrier(unsigned int *bar, volatile int *flags) {
+  __syncthreads();
+  __shared__ int ok;
+  if (threadIdx.x == 0) {
+    ok = 1;
+    volatile unsigned int *vgen = bar + 1;
+    const unsigned int gen = *vgen;
+    __threadfence();
+    const unsigned int arrived = atomicAdd(bar, 1u);
+    if (arrived == gridDim.x - 1) {
+      atomicExch(bar, 0u);
+      __threadfence();
+      atomicAdd(bar + 1, 1u);
+    } else {
+      const unsigned long long t0 = global_ns();
+      while (*vgen == gen) {
+        if (flags[0] != 0) { ok = 0; break; }
+        if (global_ns() - t0 > kBarrierTimeoutNs) { flags[0] = 2; ok = 0; break; }
+        __nanosleep(64);
+      }
+    }
+    __threadfence();
+    if (flags[0] != 0) ok = 0;
+  }
+  __syncthreads();
+  return ok != 0;
+}
+
+__device__ double block_reduce(double v, double *smem) {
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  if (lane == 0) smem[w] = v;
+  __syncthreads();
+  double t = 0.0;
+  if (w == 0) {
+    t = (lane < (int)(blockDim.x >> 5)) ? smem[lane] : 0.0;
+    for (int o = 16; o > 0; o >>= 1) t += __shfl_down_sync(0xffffffffu, t, o);
+  }
+  __syncthreads();
+  return t;  // valid in thread 0
+}
+
+// Sum of partials[0..nb) in a fixed order, broadcast to the whole block.
+__device__ double sum_partials(const double *partials, int nb, double *smem) {
+  double s = 0.0;
+  for (int i = threadIdx.x; i < nb; i += blockDim.x) s += partials[i];
+  s = block_reduce(s, smem);
+  if (threadIdx.x == 0) smem[32] = s;
+  __syncthreads();
+  const double r = smem[32];
+  __syncthreads();
+  return r;
+}
+
+__device__ __forceinline__ double spmv_row(const PcgSystem &S, int row, const double *x,
+                                           int lane) {
+  double s = 0.0;
+  const int b = S.rowptr[row], e = S.rowptr[row + 1];
+  for (int k = b + lane; k < e; k += 32) s += S.vals[k] * x[S.colidx[k]];
+  for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+  return s;  // lane 0
+}
+
+// Vector work is done per diagonal block (<= 6 equations of one node), so
+// every equation is read and written by exactly one thread in a phase.
+struct BlockRange { int b, m; };
+__device__ __forceinline__ BlockRange block_range(const PcgSystem &S, int k) {
+  BlockRange r;
+  r.b = S.blk_start[k];
+  r.m = S.blk_start[k + 1] - r.b;
+  return r;
+}
+
+// z = Binv r on block k
+__device__ __forceinline__ void precondition_block(const PcgSystem &S, int k, BlockRange br) {
+  const double *B = S.binv + (long)k * 36;
+  double rr[6];
+  for (int i = 0; i < br.m; i++) rr[i] = S.r[br.b + i];
+  for (int i = 0; i < br.m; i++) {
+    double t = 0.0;
+    for (int j = 0; j < br.m; j++) t += B[6 * i + j] * rr[j];
+    S.z[br.b + i] = t;
+  }
+}
+
+// scalars: [0] rz  [1] bb  [2] rr  [3] iterations  [4] relres
+__global__ void __launch_bounds__(kPcgThreads) k_pcg(PcgSystem S, const double *b, double *x,
+                                                     double rtol, int maxit) {
+  __shared__ double smem[40];
+  volatile int *flags = S.flags;
+  const int gtid = blockIdx.x * blockDim.x + threadIdx.x;
+  const int gthreads = gridDim.x * blockDim.x;
+  const int lane = threadIdx.x & 31;
+  const int gwarp = gtid >> 5, nwarps = gthreads >> 5;
+  const int nb = gridDim.x;
+  double *part = S.partials;          // [3*nb]
+
+  // r = b - A x ; (x is the initial guess)
+  for (int row = gwarp; row < S.n; row += nwarps) {
+    const double ax = spmv_row(S, row, x, lane);
+    if (lane == 0) S.r[row] = b[row] - ax;
+  }
+  if (!grid_barrier(S.barrier, flags)) return;
+  double lrz = 0.0, lbb = 0.0, lrr = 0.0;
+  for (int k = gtid; k < S.nblk; k += gthreads) {
+    const BlockRange br = block_range(S, k);
+    precondition_block(S, k, br);
+    for (int i = br.b; i < br.b + br.m; i++) {
+      S.p[i] = S.z[i];
+      lrz += S.r[i] * S.z[i];
+      lbb += b[i] * b[i];
+      lrr += S.r[i] * S.r[i];
+    }
+  }
+  // p = z is read across blocks in the next SpMV: barrier before it
+  lrz = block_reduce(lrz, smem);
+  if (threadIdx.x == 0) part[blockIdx.x] = lrz;
+  lbb = block_reduce(lbb, smem);
+  if (threadIdx.x == 0) part[nb + blockIdx.x] = lbb;
+  lrr = block_reduce(lrr, smem);
+  if (threadIdx.x == 0) part[2 * nb + blockIdx.x] = lrr;
+  if (!grid_barrier(S.barrier, flags)) return;
+  double rz = sum_partials(part, nb, smem);
+  const double bb = sum_partials(part + nb, nb, smem);
+  double rr = sum_partials(part + 2 * nb, nb, smem);
+  const double bnorm = sqrt(bb);
+  int it = 0;
+  int status = 0;
+  if (bnorm == 0.0 || sqrt(rr) <= rtol * bnorm) {
+    status = 1;
+  }
+  while (status == 0 && it < maxit) {
+    // q = A p ; pq = p.q
+    if (!grid_barrier(S.barrier, flags)) return;   // partial sums consumed
+    double lpq = 0.0;
+    for (int row = gwarp; row < S.n; row += nwarps) {
+      const double ap = spmv_row(S, row, S.p, lane);
+      if (lane == 0) {
+        S.q[row] = ap;
+        lpq += ap * S.p[row];
+      }
+    }
+    lpq = block_reduce(lpq, smem);
+    if (threadIdx.x == 0) part[blockIdx.x] = lpq;
+    if (!grid_barrier(S.barrier, flags)) return;
+    const double pq = sum_partials(part, nb, smem);
+    if (!(pq > 0.0)) { status = -1; break; }
+    const double alpha = rz / pq;
+    if (!grid_barrier(S.barrier, flags)) return;   // partial sums consumed
+    lrz = 0.0; lrr = 0.0;
+    for (int k = gtid; k < S.nblk; k += gthreads) {
+      const BlockRange br = block_range(S, k);
+      for (int i = br.b; i < br.b + br.m; i++) {
+        x[i] += alpha * S.p[i];
+        S.r[i] -= alpha * S.q[i];
+      }
+      precondition_block(S, k, br);
+      for (int i = br.b; i < br.b + br.m; i++) {
+        lrz += S.r[i] * S.z[i];
+        lrr += S.r[i] * S.r[i];
+      }
+    }
+    lrz = block_reduce(lrz, smem);
+    if (threadIdx.x == 0) part[blockIdx.x] = lrz;
+    lrr = block_reduce(lrr, smem);
+    if (threadIdx.x == 0) part[nb + blockIdx.x] = lrr;
+    if (!grid_barrier(S.barrier, flags)) return;
+    const double rz_new = sum_partials(part, nb, smem);
+    rr = sum_partials(part + nb, nb, smem);
+    it++;
+    if (sqrt(rr) <= rtol * bnorm) { status = 1; break; }
+    const double beta = rz_new / rz;
+    rz = rz_new;
+    for (int k = gtid; k < S.nblk; k += gthreads) {
+      const BlockRange br = block_range(S, k);
+      for (int i = br.b; i < br.b + br.m; i++) S.p[i] = S.z[i] + beta * S.p[i];
+    }
+  }
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    S.scalars[3] = it;
+    S.scalars[4] = bnorm > 0.0 ? sqrt(rr) / bnorm : 0.0;
+    S.flags[1] = status;
+  }
+}
+
+// Diagonal blocks of the CSR matrix, inverted by Gauss-Jordan with partial
+// pivoting (blocks are at most 6 x 6: the free dofs of one node).
+__global__ void k_factor_blocks(PcgSystem S) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= S.nblk) return;
+  const int b = S.blk_start[k], m = S.blk_start[k + 1] - b;
+  double A[6][12];
+  for (int i = 0; i < m; i++) {
+    for (int j = 0; j < 2 * m; j++) A[i][j] = (j == m + i) ? 1.0 : 0.0;
+    const int row = b + i;
+    for (int q = S.rowptr[row]; q < S.rowptr[row + 1]; q++) {
+      const int c = S.colidx[q];
+      if (c >= b && c < b + m) A[i][c - b] = S.vals[q];
+    }
+  }
+  bool singular = false;
+  for (int c = 0; c < m; c++) {
+    int piv = c;
+    double best = fabs(A[c][c]);
+    for (int i = c + 1; i < m; i++)
+      if (fabs(A[i][c]) > best) { best = fabs(A[i][c]); piv = i; }
+    if (best == 0.0) { singular = true; break; }
+    if (piv != c)
+      for (int j = 0; j < 2 * m; j++) { double t = A[c][j]; A[c][j] = A[piv][j]; A[piv][j] = t; }
+    const double inv = 1.0 / A[c][c];
+    for (int j = 0; j < 2 * m; j++) A[c][j] *= inv;
+    for (int i = 0; i < m; i++) {
+      if (i == c) continue;
+      const double f = A[i][c];
+      if (f != 0.0)
+        for (int j = 0; j < 2 * m; j++) A[i][j] -= f * A[c][j];
+    }
+  }
+  double *B = S.binv + (long)k * 36;
+  for (int i = 0; i < 36; i++) B[i] = 0.0;
+  if (singular) {
+    // fall back to the point-Jacobi inverse of whatever diagonal exists
+    for (int i = 0; i < m; i++) {
+      double d = 0.0;
+      const int row = b + i;
+      for (int q = S.rowptr[row]; q < S.rowptr[row + 1]; q++)
+        if (S.colidx[q] == row) d = S.vals[q];
+      B[6 * i + i] = d != 0.0 ? 1.0 / d : 1.0;
+    }
+    return;
+  }
+  for (int i = 0; i < m; i++)
+    for (int j = 0; j < m; j++) B[6 * i + j] = A[i][m + j];
+}
+
+int g_max_blocks = -1;
+
+}  // namespace
+
+int pcg_max_blocks() {
+  if (g_max_blocks < 0) {
+    int dev = 0, sms = 0, per = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_pcg, kPcgThreads, 0);
+    if (per < 1) per = 1;
+    g_max_blocks = sms * per;
+  }
+  return g_max_blocks;
+}
+
+int pcg_factor_blocks(const PcgSystem &S, cudaStream_t s) {
+  if (S.nblk == 0) return 0;
+  k_factor_blocks<<<(S.nblk + 127) / 128, 128, 0, s>>>(S);
+  return cudaGetLastError() == cudaSuccess ? 0 : XG_ECUDA;
+}
+
+int pcg_solve(const PcgSystem &S, const double *b, double *x, double rtol, int maxit,
+              int *iters, double *relres, cudaStream_t s) {
+  if (S.n == 0) {
+    if (iters) *iters = 0;
+    if (relres) *relres = 0.0;
+    return 0;
+  }
+  // rows per block: small systems use few blocks to keep barriers cheap
+  long want = ((long)S.n + 2047) / 2048;
+  int nb = (int)(want < 1 ? 1 : want);
+  const int maxb = pcg_max_blocks();
+  if (nb > maxb) nb = maxb;
+  if (cudaMemsetAsync(S.barrier, 0, 2 * sizeof(unsigned int), s) != cudaSuccess) return XG_ECUDA;
+  if (cudaMemsetAsync(S.flags, 0, 4 * sizeof(int), s) != cudaSuccess) return XG_ECUDA;
+  PcgSystem Sv = S;
+  void *args[] = {(void *)&Sv, (void *)&b, (void *)&x, (void *)&rtol, (void *)&maxit};
+  cudaError_t err = cudaLaunchCooperativeKernel((void *)k_pcg, dim3(nb), dim3(kPcgThreads), args,
+                                                0, s);
+  if (err != cudaSuccess) return XG_ECUDA;
+  int hflags[4];
+  double hs[8];
+  if (cudaMemcpyAsync(hflags, S.flags, sizeof hflags, cudaMemcpyDeviceToHost, s) != cudaSuccess)
+    return XG_ECUDA;
+  if (cudaMemcpyAsync(hs, S.scalars, sizeof hs, cudaMemcpyDeviceToHost, s) != cudaSuccess)
+    return XG_ECUDA;
+  if (cudaStreamSynchronize(s) != cudaSuccess) return XG_ECUDA;
+  if (iters) *iters = (int)hs[3];
+  if (relres) *relres = hs[4];
+  if (hflags[0] != 0) return XG_ESOLVE;      // barrier timeout
+  if (hflags[1] != 1) return XG_ESOLVE;      // breakdown or maxit
+  return 0;
+}
+
+}  // namespace xg

@@ -1,0 +1,225 @@
+"""ctypes binding of ``libxara_gpu.so`` and the device model handle.
+
+The library is built in-tree by :func:`xara_gb300._build.build` (nvcc,
+sm_103a).  Nothing here falls back to a CPU path: a missing library or a
+failing CUDA call raises.
+"""
+import ctypes as C
+import os
+import re
+
+import numpy as np
+
+from . import _abi
+from ._abi import xg_step_stats
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB = os.path.join(HERE, "libxara_gpu.so")
+HEADER = os.path.join(HERE, "..", "include", "xara_gpu.h")
+
+_lib = None
+
+
+class XaraGpuError(RuntimeError):
+    """A negative status from the C ABI, with xg_last_error()'s text."""
+
+    def __init__(self, code, msg):
+        super().__init__(f"xara_gpu error {code}: {msg}")
+        self.code = code
+
+
+def declared_symbols():
+    """Names of the entry points declared in include/xara_gpu.h."""
+    with open(HEADER) as f:
+        text = f.read()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    return sorted(set(re.findall(r"\b(xg_[a-z0-9_]+)\s*\(", text)))
+
+
+def lib():
+    """Load libxara_gpu.so (ImportError when it has not been built)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB):
+        raise ImportError(f"{LIB} not built: run __graft_entry__.build()")
+    L = C.CDLL(LIB)
+    vp, ip, dp = C.c_void_p, C.POINTER(C.c_int), C.POINTER(C.c_double)
+    L.xg_last_error.restype = C.c_char_p
+    L.xg_model_create.argtypes = [vp, C.POINTER(vp)]
+    L.xg_model_destroy.argtypes = [vp]
+    L.xg_model_sizes.argtypes = [vp, ip, ip]
+    L.xg_model_numbering.argtypes = [vp, vp]
+    L.xg_model_pattern.argtypes = [vp, vp, vp]
+    L.xg_elemset_set_trial_disp.argtypes = [vp, vp]
+    L.xg_elemset_update.argtypes = [vp, vp, vp]
+    L.xg_elemset_commit.argtypes = [vp]
+    L.xg_elemset_revert.argtypes = [vp]
+    L.xg_elemset_revert_to_start.argtypes = [vp]
+    L.xg_elemset_get_history.argtypes = [vp, C.c_int, vp, C.c_long]
+    L.xg_elemset_set_history.argtypes = [vp, C.c_int, vp, C.c_long]
+    L.xg_soe_solve.argtypes = [vp, vp, vp, C.c_double, C.c_int, ip, dp]
+    L.xg_analysis_set_phase.argtypes = [vp, vp]
+    L.xg_analysis_set_solver.argtypes = [vp, C.c_double, C.c_int]
+    L.xg_analyze.argtypes = [vp, C.c_int, vp]
+    L.xg_get_disp.argtypes = [vp, vp, dp]
+    L.xg_reset.argtypes = [vp]
+    L.xg_model_plan.argtypes = [vp, vp, vp, vp, ip, ip]
+    _lib = L
+    return _lib
+
+
+def plan(desc):
+    """Host-only DOF numbering and CSR pattern (no GPU needed).
+
+    Returns (eqn[num_nodes*ndf], rowptr, colidx) as DOF_Numberer and
+    SparseGenColLinSOE would produce them.
+    """
+    L = lib()
+    s = desc.struct()
+    neq, nnz = C.c_int(), C.c_int()
+    _check(L.xg_model_plan(C.byref(s), None, None, None, C.byref(neq), C.byref(nnz)))
+    eqn = np.zeros(desc.num_nodes * desc.ndf, np.int32)
+    rp = np.zeros(neq.value + 1, np.int32)
+    ci = np.zeros(nnz.value, np.int32)
+    _check(L.xg_model_plan(C.byref(s), _p(eqn), _p(rp), _p(ci), C.byref(neq), C.byref(nnz)))
+    return eqn, rp, ci
+
+
+def _p(a):
+    return None if a is None else a.ctypes.data_as(C.c_void_p)
+
+
+def _check(code):
+    if code < 0:
+        msg = lib().xg_last_error()
+        raise XaraGpuError(code, msg.decode() if msg else "")
+    return code
+
+
+class DeviceModel:
+    """A model resident on the GPU: element set, system and Newton driver."""
+
+    def __init__(self, desc):
+        L = lib()
+        self.desc = desc
+        self._s = desc.struct()
+        h = C.c_void_p()
+        _check(L.xg_model_create(C.byref(self._s), C.byref(h)))
+        self.h = h
+        neq, nnz = C.c_int(), C.c_int()
+        _check(L.xg_model_sizes(self.h, C.byref(neq), C.byref(nnz)))
+        self.neq, self.nnz = neq.value, nnz.value
+        self.nu = desc.num_nodes * desc.ndf
+
+    def close(self):
+        if getattr(self, "h", None):
+            lib().xg_model_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    # -- DOF numbering and pattern -----------------------------------------
+    def numbering(self):
+        eqn = np.zeros(self.nu, np.int32)
+        _check(lib().xg_model_numbering(self.h, _p(eqn)))
+        return eqn
+
+    def pattern(self):
+        rp = np.zeros(self.neq + 1, np.int32)
+        ci = np.zeros(self.nnz, np.int32)
+        _check(lib().xg_model_pattern(self.h, _p(rp), _p(ci)))
+        return rp, ci
+
+    # -- element set ---------------------------------------------------------
+    def set_trial_disp(self, U):
+        U = np.ascontiguousarray(U, np.float64)
+        assert U.size == self.nu
+        _check(lib().xg_elemset_set_trial_disp(self.h, _p(U)))
+
+    def update(self, want_vals=True, want_resid=True):
+        vals = np.zeros(self.nnz) if want_vals else None
+        resid = np.zeros(self.neq) if want_resid else None
+        r = lib().xg_elemset_update(self.h, _p(vals), _p(resid))
+        if r < 0 and lib().xg_last_error():
+            _check(r)
+        return vals, resid, r
+
+    def commit(self):
+        _check(lib().xg_elemset_commit(self.h))
+
+    def revert(self):
+        _check(lib().xg_elemset_revert(self.h))
+
+    def history(self):
+        n = 1 << 62
+        buf = np.zeros(1)
+        r = lib().xg_elemset_get_history(self.h, 0, _p(buf), 0)
+        # the error text carries the size; ask with the exact size instead
+        nip = 4 if self.desc.elem_type == _abi.XG_ELE_QUAD else 8
+        nh = 4 if nip == 4 else 6
+        n = self.desc.num_elems * nip * (nh + 1)
+        buf = np.zeros(n)
+        _check(lib().xg_elemset_get_history(self.h, 0, _p(buf), n))
+        del r
+        return buf
+
+    def set_history(self, buf):
+        buf = np.ascontiguousarray(buf, np.float64)
+        _check(lib().xg_elemset_set_history(self.h, 0, _p(buf), buf.size))
+
+    # -- linear system -------------------------------------------------------
+    def solve(self, b, rtol=1e-12, maxit=20000):
+        b = np.ascontiguousarray(b, np.float64)
+        x = np.zeros(self.neq)
+        it, rr = C.c_int(), C.c_double()
+        _check(lib().xg_soe_solve(self.h, _p(b), _p(x), rtol, maxit, C.byref(it), C.byref(rr)))
+        return x, it.value, rr.value
+
+    # -- analysis ------------------------------------------------------------
+    def set_solver(self, rtol=1e-12, maxit=20000):
+        _check(lib().xg_analysis_set_solver(self.h, rtol, maxit))
+
+    def set_phase(self, phase):
+        self._ps = phase.struct()
+        _check(lib().xg_analysis_set_phase(self.h, C.byref(self._ps)))
+
+    def analyze(self, num_steps):
+        stats = (xg_step_stats * max(num_steps, 1))()
+        r = lib().xg_analyze(self.h, num_steps, stats)
+        out = [(s.newton_iters, s.solver_iters, s.status) for s in stats[:num_steps]]
+        _check(r)
+        return out
+
+    def disp(self):
+        u = np.zeros(self.nu)
+        lam = C.c_double()
+        _check(lib().xg_get_disp(self.h, _p(u), C.byref(lam)))
+        return u, lam.value
+
+    def reset(self):
+        _check(lib().xg_reset(self.h))
+
+    def run(self, phases, record=True):
+        """Run phases step by step; returns (U per step, lambda per step, stats)."""
+        us, ls, stats = [], [], []
+        for ph in phases:
+            self.set_phase(ph)
+            for _ in range(ph.num_steps):
+                st = self.analyze(1)
+                stats.extend(st)
+                if record:
+                    u, lam = self.disp()
+                    us.append(u)
+                    ls.append(lam)
+        return (np.array(us) if record else None), np.array(ls), stats
