@@ -258,6 +258,21 @@ int xg_get_disp(const xg_model *m, double *u, double *lambda);
 /* Reset displacements, time and material state to the start. */
 int xg_reset(xg_model *m);
 
+/* ---- tracing: CUDA-event timing of every kernel group on the model's
+        stream (the reference times phases with its Timer class,
+        utility/Timer.cpp, and the `totalCPU`/`solveCPU` commands) ---- */
+/* Enable (1) or disable (0) and reset the per-kernel counters. */
+int xg_profile_enable(xg_model *m, int enable);
+/* Slot k (0..): name, accumulated milliseconds and launch count.  The slot
+   after the last kernel reports the number of return maps that hit their
+   iteration cap in the last update (in `launches`).  Returns XG_EINVAL past
+   the end. */
+int xg_profile_get(const xg_model *m, int k, char *name, int cap, double *ms, long *launches);
+
+/* FP64 FMA throughput of the current device in TFLOP/s (a short probe
+   kernel with no memory traffic), the ceiling of the FP64 element kernels. */
+int xg_measure_fp64_peak(double *tflops);
+
 #ifdef __cplusplus
 }
 #endif

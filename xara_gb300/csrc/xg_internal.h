@@ -29,7 +29,7 @@ struct ContinuumView {
   double *ep_t, *xi_t;    // trial
   double *sig;            // trial stress (3 plane strain: xx yy xy; 6 in 3D)
   double *tan;            // trial tangent: quad 6 unique D entries; brick a b c n(6)
-  int *status;            // [ne] element status (0 ok, 1 return map failed)
+  int *nfail;             // [1] points whose return map hit the iteration cap
   // element outputs (element-major scratch)
   double *Ke;             // quad: [ne][64]; brick: [ne][324] upper node-pair blocks
   double *Re;             // [ne][ned]

@@ -213,7 +213,6 @@ __global__ void k_quad_update(ContinuumView v) {
   v.tan[3 * npts + pt] = j2_tangent_entry(K, G, o.c2, o.c3, 1.0, 2. / 3., n11 * n11);
   v.tan[4 * npts + pt] = j2_tangent_entry(K, G, o.c2, o.c3, 0.0, 0.0, n11 * n01);
   v.tan[5 * npts + pt] = j2_tangent_entry(K, G, o.c2, o.c3, 0.0, 0.5, n01 * n01);
-  if (ip == 0) v.status[e] = 0;
 }
 
 // One thread per element: FourNodeQuad::getTangentStiff / getResistingForce
@@ -385,7 +384,7 @@ __global__ void k_brick_update(ContinuumView v) {
   v.tan[2 * npts + pt] = o.c2 - o.c3;
 #pragma unroll
   for (int c = 0; c < 6; c++) v.tan[(3 + c) * npts + pt] = o.n[c];
-  if (o.status) v.status[e] = 1;
+  if (o.status) atomicAdd(v.nfail, 1);
 }
 
 __device__ __constant__ unsigned char kPairA[36] = {
@@ -525,7 +524,7 @@ __global__ void k_j2_zero(ContinuumView v) {
     v.tan[2 * npts + pt] = 0.0;
     for (int c = 0; c < 6; c++) v.tan[(3 + c) * npts + pt] = 0.0;
   }
-  if (pt % v.nip == 0) v.status[e] = 0;
+
 }
 
 // ---------------------------------------------------------------------------
@@ -664,3 +663,53 @@ int launch_norm2(int n, const double *x, double *partials, double *out, cudaStre
 }
 
 }  // namespace xg
+
+// ---------------------------------------------------------------------------
+// FP64 peak probe: independent FMA chains, no memory traffic.  Used to put
+// the element kernels' FP64 rate next to what this GPU delivers.
+// ---------------------------------------------------------------------------
+namespace xg {
+namespace {
+__global__ void k_fp64_fma(double *out, int iters) {
+  double a0 = threadIdx.x * 1e-9, a1 = a0 + 1e-9, a2 = a0 + 2e-9, a3 = a0 + 3e-9;
+  double a4 = a0 + 4e-9, a5 = a0 + 5e-9, a6 = a0 + 6e-9, a7 = a0 + 7e-9;
+  const double m = 0.999999999, c = 1e-12;
+  for (int i = 0; i < iters; i++) {
+#pragma unroll
+    for (int k = 0; k < 8; k++) {
+      a0 = fma(a0, m, c); a1 = fma(a1, m, c); a2 = fma(a2, m, c); a3 = fma(a3, m, c);
+      a4 = fma(a4, m, c); a5 = fma(a5, m, c); a6 = fma(a6, m, c); a7 = fma(a7, m, c);
+    }
+  }
+  const double s = a0 + a1 + a2 + a3 + a4 + a5 + a6 + a7;
+  if (s == 12345.678) out[blockIdx.x] = s;  // keeps the chains live
+}
+}  // namespace
+}  // namespace xg
+
+extern "C" int xg_measure_fp64_peak(double *tflops) {
+  if (!tflops) return XG_EINVAL;
+  int dev = 0, sms = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  double *out = nullptr;
+  if (cudaMalloc(&out, sizeof(double) * 4096) != cudaSuccess) return XG_ENOMEM;
+  const int blocks = sms * 8, threads = 256, iters = 4096;
+  cudaEvent_t a, b;
+  cudaEventCreate(&a);
+  cudaEventCreate(&b);
+  xg::k_fp64_fma<<<blocks, threads>>>(out, 64);  // warm up
+  cudaEventRecord(a);
+  xg::k_fp64_fma<<<blocks, threads>>>(out, iters);
+  cudaEventRecord(b);
+  cudaEventSynchronize(b);
+  float ms = 0.f;
+  cudaEventElapsedTime(&ms, a, b);
+  cudaEventDestroy(a);
+  cudaEventDestroy(b);
+  cudaFree(out);
+  if (cudaGetLastError() != cudaSuccess || ms <= 0.f) return XG_ECUDA;
+  const double flops = 2.0 * 64.0 * (double)iters * blocks * threads;
+  *tflops = flops / (ms * 1e-3) / 1e12;
+  return 0;
+}

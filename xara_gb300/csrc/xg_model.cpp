@@ -142,7 +142,7 @@ struct xg_model {
 
   // device
   cudaStream_t stream = nullptr;
-  DBuf<int> d_conn, d_mat, d_eqn, d_rowptr, d_colidx, d_blk, d_status;
+  DBuf<int> d_conn, d_mat, d_eqn, d_rowptr, d_colidx, d_blk, d_nfail;
   DBuf<double> d_crd, d_j2, d_U, d_Uc;
   DBuf<double> d_epc, d_xic, d_ept, d_xit, d_sig, d_tan;
   DBuf<double> d_sig_c, d_tan_c;               // trial state at the last commit
@@ -173,6 +173,49 @@ struct xg_model {
   int last_solver_iters = 0;
   int phase_steps_done = 0;
   bool phase_closed = false;
+  int last_nfail = 0;
+  // per-kernel CUDA-event timing on the model's stream (xg_profile_*)
+  struct ProfSlot {
+    const char *name;
+    double ms;
+    long launches;
+    cudaEvent_t a, b;
+    bool pending;
+  };
+  std::vector<ProfSlot> prof;
+  bool prof_on = false;
+  enum { P_UPDATE, P_ASSEMBLE, P_GATHER_K, P_GATHER_R, P_PCG_FACTOR, P_PCG };
+  void prof_init() {
+    const char *names[6] = {etype == XG_ELE_QUAD ? "quad_update" : "brick_update",
+                            etype == XG_ELE_QUAD ? "quad_assemble" : "brick_assemble",
+                            "gather_tangent", "gather_resid", "pcg_factor_blocks", "pcg"};
+    for (int k = 0; k < 6; k++) {
+      ProfSlot p{names[k], 0.0, 0, nullptr, nullptr, false};
+      cudaEventCreate(&p.a);
+      cudaEventCreate(&p.b);
+      prof.push_back(p);
+    }
+  }
+  void prof_begin(int k) {
+    if (prof_on) cudaEventRecord(prof[k].a, stream);
+  }
+  void prof_end(int k, int launches) {
+    if (!prof_on) return;
+    cudaEventRecord(prof[k].b, stream);
+    prof[k].launches += launches;
+    prof[k].pending = true;
+  }
+  void prof_flush() {
+    if (!prof_on) return;
+    for (auto &p : prof)
+      if (p.pending) {
+        cudaEventSynchronize(p.b);
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, p.a, p.b);
+        p.ms += ms;
+        p.pending = false;
+      }
+  }
 
   ContinuumView view() {
     ContinuumView v{};
@@ -180,7 +223,7 @@ struct xg_model {
     v.conn = d_conn.p; v.crd = d_crd.p; v.U = d_U.p; v.mat = d_mat.p; v.j2 = d_j2.p;
     v.thickness = thickness;
     v.ep_c = d_epc.p; v.xi_c = d_xic.p; v.ep_t = d_ept.p; v.xi_t = d_xit.p;
-    v.sig = d_sig.p; v.tan = d_tan.p; v.status = d_status.p;
+    v.sig = d_sig.p; v.tan = d_tan.p; v.nfail = d_nfail.p;
     v.Ke = d_Ke.p; v.Re = d_Re.p;
     return v;
   }
@@ -191,6 +234,10 @@ struct xg_model {
   int ke_size() const { return etype == XG_ELE_QUAD ? 64 : 324; }
 
   ~xg_model() {
+    for (auto &p : prof) {
+      cudaEventDestroy(p.a);
+      cudaEventDestroy(p.b);
+    }
     if (stream) cudaStreamDestroy(stream);
   }
 
@@ -458,7 +505,8 @@ int xg_model::upload(const HostGather &gk_h, const HostGather &gr_h) {
   RET(d_xic.alloc(np)); RET(d_xit.alloc(np));
   RET(d_sig.alloc(np * nsig())); RET(d_tan.alloc(np * ntan()));
   RET(d_sig_c.alloc(np * nsig())); RET(d_tan_c.alloc(np * ntan()));
-  RET(d_status.alloc(ne));
+  RET(d_nfail.alloc(1));
+  CK(cudaMemsetAsync(d_nfail.p, 0, sizeof(int), s));
   RET(d_Ke.alloc((size_t)ne * ke_size()));
   RET(d_Re.alloc((size_t)ne * ned));
   RET(d_vals.alloc(nnz > 0 ? nnz : 1)); RET(d_resid.alloc(neq > 0 ? neq : 1));
@@ -521,28 +569,40 @@ int xg_model::upload(const HostGather &gk_h, const HostGather &gr_h) {
 int xg_model::element_state(bool compute) {
   ContinuumView v = view();
   cudaStream_t s = stream;
-  if (etype == XG_ELE_QUAD) {
-    if (compute) RET(launch_quad_update(v, s));
-    RET(launch_quad_assemble(v, s));
-  } else {
-    if (compute) RET(launch_brick_update(v, s));
-    RET(launch_brick_assemble(v, s));
+  if (compute) {
+    CK(cudaMemsetAsync(d_nfail.p, 0, sizeof(int), s));
+    prof_begin(P_UPDATE);
+    RET(etype == XG_ELE_QUAD ? launch_quad_update(v, s) : launch_brick_update(v, s));
+    prof_end(P_UPDATE, 1);
   }
+  prof_begin(P_ASSEMBLE);
+  RET(etype == XG_ELE_QUAD ? launch_quad_assemble(v, s) : launch_brick_assemble(v, s));
+  prof_end(P_ASSEMBLE, 1);
+  prof_begin(P_GATHER_K);
   RET(launch_gather(gk, d_Ke.p, d_partial.p, d_vals.p, s));
+  prof_end(P_GATHER_K, 2);
+  prof_begin(P_GATHER_R);
   RET(launch_gather(gr, d_Re.p, d_partial.p, d_resid.p, s));
+  prof_end(P_GATHER_R, 2);
+  prof_flush();
   blocks_factored = false;
   return 0;
 }
 
 int xg_model::solve(const double *b, double *x, int *iters) {
   if (!blocks_factored) {
+    prof_begin(P_PCG_FACTOR);
     RET(pcg_factor_blocks(pcg, stream));
+    prof_end(P_PCG_FACTOR, 1);
     blocks_factored = true;
   }
   CK(cudaMemsetAsync(x, 0, (neq > 0 ? neq : 1) * sizeof(double), stream));
   double relres = 0.0;
   int it = 0;
+  prof_begin(P_PCG);
   int r = pcg_solve(pcg, b, x, rtol, maxit, &it, &relres, stream);
+  prof_end(P_PCG, 1);
+  prof_flush();
   last_solver_iters += it;
   if (iters) *iters = it;
   if (r != 0)
@@ -684,6 +744,7 @@ int xg_model_create(const xg_model_desc *d, xg_model **out) {
     delete m;
     return fail(XG_ECUDA, "no CUDA device");
   }
+  m->prof_init();
   r = m->upload(gk_h, gr_h);
   if (r) { delete m; return r; }
   *out = m;
@@ -830,14 +891,35 @@ int xg_elemset_update(xg_model *m, double *csr_vals, double *resid) {
   if (resid)
     CK(cudaMemcpyAsync(resid, m->d_resid.p, (size_t)m->neq * sizeof(double),
                        cudaMemcpyDeviceToHost, m->stream));
-  std::vector<int> st(m->ne);
-  if (m->ne)
-    CK(cudaMemcpyAsync(st.data(), m->d_status.p, (size_t)m->ne * sizeof(int),
-                       cudaMemcpyDeviceToHost, m->stream));
+  CK(cudaMemcpyAsync(&m->last_nfail, m->d_nfail.p, sizeof(int), cudaMemcpyDeviceToHost,
+                     m->stream));
   CK(cudaStreamSynchronize(m->stream));
-  int bad = 0;
-  for (int v : st) bad += v != 0;
-  return bad ? -bad : 0;
+  // Brick::update and J2PlaneStrain::setTrialStrain discard the return-map
+  // status (Brick.cpp:839, J2PlaneStrain.cpp:133); the count is kept for
+  // xg_profile_get ("return_map_cap_hits") only.
+  return 0;
+}
+
+int xg_profile_enable(xg_model *m, int enable) {
+  if (!m) return fail(XG_EINVAL, "null model");
+  m->prof_on = enable != 0;
+  for (auto &p : m->prof) { p.ms = 0.0; p.launches = 0; }
+  return 0;
+}
+
+int xg_profile_get(const xg_model *m, int k, char *name, int cap, double *ms, long *launches) {
+  if (!m) return fail(XG_EINVAL, "null model");
+  if (k == (int)m->prof.size()) {
+    if (name && cap > 0) snprintf(name, cap, "%s", "return_map_cap_hits");
+    if (ms) *ms = 0.0;
+    if (launches) *launches = m->last_nfail;
+    return 0;
+  }
+  if (k < 0 || k > (int)m->prof.size()) return fail(XG_EINVAL, "no profile slot %d", k);
+  if (name && cap > 0) snprintf(name, cap, "%s", m->prof[k].name);
+  if (ms) *ms = m->prof[k].ms;
+  if (launches) *launches = m->prof[k].launches;
+  return 0;
 }
 
 int xg_elemset_commit(xg_model *m) {

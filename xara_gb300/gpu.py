@@ -223,3 +223,24 @@ class DeviceModel:
                     us.append(u)
                     ls.append(lam)
         return (np.array(us) if record else None), np.array(ls), stats
+
+
+def profile_enable(model, on=True):
+    _check(lib().xg_profile_enable(model.h, 1 if on else 0))
+
+
+def profile_read(model):
+    """{kernel group: (milliseconds, launches)} accumulated since enabling."""
+    L = lib()
+    L.xg_profile_get.argtypes = [C.c_void_p, C.c_int, C.c_char_p, C.c_int,
+                                 C.POINTER(C.c_double), C.POINTER(C.c_long)]
+    out = {}
+    k = 0
+    buf = C.create_string_buffer(64)
+    while True:
+        ms, n = C.c_double(), C.c_long()
+        if L.xg_profile_get(model.h, k, buf, 64, C.byref(ms), C.byref(n)) < 0:
+            break
+        out[buf.value.decode()] = (ms.value, n.value)
+        k += 1
+    return out
