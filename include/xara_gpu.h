@@ -273,6 +273,29 @@ int xg_profile_get(const xg_model *m, int k, char *name, int cap, double *ms, lo
    kernel with no memory traffic), the ceiling of the FP64 element kernels. */
 int xg_measure_fp64_peak(double *tflops);
 
+/* ---- Allocation-free solve.  No counterpart in the reference: it exists
+        for callers that cannot allocate device memory when they solve -- a
+        host application or framework whose device memory is owned by its own
+        pool (PyTorch's caching allocator, say), or a latency-bound loop that
+        cannot pay for cudaMalloc/cudaFree, which synchronise the whole device.
+   Solves A x = b by the same block-Jacobi PCG as xg_soe_solve, on CSR arrays
+   and vectors the caller already holds on the device: rowptr[n+1],
+   colidx[nnz], vals[nnz], blk_start[nblk+1] (diagonal blocks of 1..6
+   consecutive equations), b[n], x[n] (output; zeroed first).  stream may be
+   NULL; the call returns when the solve is done.  Its scratch is a fixed
+   device array of XG_NOALLOC_MAX_DOUBLES doubles (32 MiB) that every GPU
+   using the library holds until the process exits; a system needing more
+   than 36*nblk + 4*n + 3*(cooperative blocks) + 24 doubles of it (about
+   260,000 equations with 3x3 node blocks, 100,000 with 1x1 blocks) is
+   rejected with XG_EINVAL.  The first call on a device looks up the array's
+   device address; make that first call before any stream capture.  All
+   calls share the one array: calls that overlap on the GPU race and must be
+   serialised by the caller.  Allocates no device memory. ---- */
+#define XG_NOALLOC_MAX_DOUBLES 4194304
+int xg_pcg_solve_noalloc(int n, const int *rowptr, const int *colidx, const double *vals,
+                         int nblk, const int *blk_start, const double *b, double *x,
+                         double rtol, int maxit, void *stream, int *iters, double *relres);
+
 #ifdef __cplusplus
 }
 #endif

@@ -87,3 +87,8 @@ int launch_sub(int n, const double *a, const double *b, double *out, cudaStream_
 int launch_norm2(int n, const double *x, double *partials, double *out, cudaStream_t s);
 
 }  // namespace xg
+
+namespace xg {
+// Sets the text returned by xg_last_error() (xg_model.cpp).
+void record_error(const char *msg);
+}  // namespace xg

@@ -1072,3 +1072,9 @@ int xg_reset(xg_model *m) {
 }
 
 }  // extern "C"
+
+namespace xg {
+// Sets the text xg_last_error() returns (used by entry points defined in
+// other translation units).
+void record_error(const char *msg) { g_err = msg ? msg : ""; }
+}  // namespace xg
