@@ -61,6 +61,7 @@ material/uniaxial/UniaxialMaterial.cpp
 material/plastic/J2Plasticity.cpp material/Plane/J2PlaneStrain.cpp
 material/plastic/J2ThreeDimensional.cpp
 material/uniaxial/steel/Steel02.cpp material/uniaxial/concrete/Concrete02.cpp
+material/uniaxial/ElasticMaterial.cpp
 material/section/SectionForceDeformation.cpp
 material/section/FiberSection2d.cpp material/section/FiberSection3d.cpp
 quadrature/Frame/BeamIntegration.cpp quadrature/Frame/LobattoBeamIntegration.cpp
@@ -95,7 +96,7 @@ system_of_eqn/linearSOE/sparseGEN/SparseGenColLinSOE.cpp
 system_of_eqn/linearSOE/sparseGEN/SparseGenColLinSolver.cpp
 """.split()
 
-HARNESS = ["ref_harness.cpp"]
+HARNESS = ["ref_harness.cpp", "ref_blas.c"]
 
 
 def sh(cmd, **kw):

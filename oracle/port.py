@@ -12,6 +12,7 @@ import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 SRC = os.path.join(HERE, "xara_oracle.c")
+INC = os.path.join(HERE, "xara_oracle_frame.inc")
 LIB = os.path.join(HERE, "libxara_oracle.so")
 
 _lib = None
@@ -26,7 +27,8 @@ def build(force=False):
         with open(LIB, "rb") as f:
             head = f.read(20)
         same_arch = head[:4] == b"\x7fELF" and int.from_bytes(head[18:20], "little") == machine
-    if not force and same_arch and os.path.getmtime(LIB) >= os.path.getmtime(SRC):
+    newest = max(os.path.getmtime(SRC), os.path.getmtime(INC))
+    if not force and same_arch and os.path.getmtime(LIB) >= newest:
         return LIB
     tmp = LIB + ".tmp"
     subprocess.run(["gcc", "-O2", "-fPIC", "-shared", "-std=c11", "-ffp-contract=off",
@@ -54,6 +56,7 @@ def lib():
         L.xo_history.argtypes = [vp, vp, vp]
         L.xo_set_history.argtypes = [vp, vp, vp]
         L.xo_j2_path.argtypes = [C.c_int, vp, C.c_int, vp, vp, vp, vp]
+        L.xo_uniaxial_path.argtypes = [C.c_int, vp, C.c_int, vp, vp, vp, vp]
         _lib = L
     return _lib
 
@@ -151,3 +154,15 @@ def j2_path(dim, param, strain, commit):
     tang = np.zeros((npts, ns, ns))
     L.xo_j2_path(dim, _p(param), npts, _p(strain), _p(commit), _p(stress), _p(tang))
     return stress, tang
+
+
+def uniaxial_path(kind, param, strain, commit):
+    """Stress and tangent of Steel02 / Concrete02 / elastic along a strain path."""
+    L = lib()
+    strain = np.ascontiguousarray(strain, np.float64)
+    commit = np.ascontiguousarray(commit, np.int32)
+    param = np.ascontiguousarray(param, np.float64)
+    s = np.zeros(len(strain))
+    t = np.zeros(len(strain))
+    L.xo_uniaxial_path(kind, _p(param), len(strain), _p(strain), _p(commit), _p(s), _p(t))
+    return s, t

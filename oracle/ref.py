@@ -108,3 +108,17 @@ def j2_path(dim, param, strain, commit):
     tang = np.zeros((npts, ns, ns))
     L.xref_j2_path(dim, _p(param), npts, _p(strain), _p(commit), _p(stress), _p(tang))
     return stress, tang
+
+
+def uniaxial_path(kind, param, strain, commit):
+    """Stress and tangent of the reference's Steel02 / Concrete02 along a path."""
+    L = lib()
+    L.xref_uniaxial_path.argtypes = [C.c_int, C.c_void_p, C.c_int, C.c_void_p, C.c_void_p,
+                                     C.c_void_p, C.c_void_p]
+    strain = np.ascontiguousarray(strain, np.float64)
+    commit = np.ascontiguousarray(commit, np.int32)
+    param = np.ascontiguousarray(param, np.float64)
+    s = np.zeros(len(strain))
+    t = np.zeros(len(strain))
+    L.xref_uniaxial_path(kind, _p(param), len(strain), _p(strain), _p(commit), _p(s), _p(t))
+    return s, t

@@ -33,6 +33,21 @@
 #include <Brick.h>
 #include <J2PlaneStrain.h>
 #include <J2ThreeDimensional.h>
+#include <Steel02.h>
+#include <Concrete02.h>
+#include <ElasticMaterial.h>
+#include <FiberSection2d.h>
+#include <FiberSection3d.h>
+#include <ForceBeamColumn2d.h>
+#include <ForceBeamColumn3d.h>
+#include <LobattoBeamIntegration.h>
+#include <LinearCrdTransf2d.h>
+#include <PDeltaCrdTransf2d.h>
+#include <BasicFrameTransf.h>
+#include <Vector3D.h>
+#include <FrameTransform.h>
+#include <LinearFrameTransf.hpp>
+#include <PDeltaFrameTransf3d.hpp>
 
 #include <AnalysisModel.h>
 #include <PlainHandler.h>
@@ -206,6 +221,40 @@ int CaptureSOE::solve() {
   return r;
 }
 
+UniaxialMaterial *make_uniaxial(int type, const double *q, int tag) {
+  switch (type) {
+    case XG_UNI_STEEL02:
+      return new Steel02(tag, q[0], q[1], q[2], q[3], q[4], q[5], q[6], q[7], q[8], q[9], q[10]);
+    case XG_UNI_CONCRETE02:
+      return new Concrete02(tag, q[0], q[1], q[2], q[3], q[4], q[5], q[6]);
+    case XG_UNI_ELASTIC:
+      return new ElasticMaterial(tag, q[0]);
+  }
+  return nullptr;
+}
+
+// `section Fiber` with fibers (y[, z], A, material) and, in 3D, elastic torsion GJ.
+SectionForceDeformation *make_section(const xg_model_desc &d, int s, int tag) {
+  const int f0 = d.sec_fiber_start[s], f1 = d.sec_fiber_start[s + 1];
+  std::vector<UniaxialMaterial *> protos(d.num_uni, nullptr);
+  for (int u = 0; u < d.num_uni; u++)
+    protos[u] = make_uniaxial(d.uni_type[u], d.uni_param + (size_t)u * XG_UNI_NPARAM, u + 1);
+  SectionForceDeformation *sec = nullptr;
+  if (d.ndm == 2) {
+    FiberSection2d *fs = new FiberSection2d(tag, f1 - f0);
+    for (int k = f0; k < f1; k++) fs->addFiber(*protos[d.fib_mat[k]], d.fib_area[k], d.fib_y[k]);
+    sec = fs;
+  } else {
+    ElasticMaterial torsion(0, d.sec_GJ[s]);
+    FiberSection3d *fs = new FiberSection3d(tag, f1 - f0, torsion);
+    for (int k = f0; k < f1; k++)
+      fs->addFiber(*protos[d.fib_mat[k]], d.fib_area[k], d.fib_y[k], d.fib_z[k]);
+    sec = fs;
+  }
+  for (auto *p : protos) delete p;
+  return sec;
+}
+
 int nen_of(int type) {
   switch (type) {
     case XG_ELE_QUAD: return 4;
@@ -240,8 +289,33 @@ void *xref_create(const xg_model_desc *desc) {
   int nen = nen_of(d.elem_type);
   for (int e = 0; e < d.num_elems; e++) {
     const int *c = d.elem_conn + (size_t)e * nen;
-    const double *p = d.j2_param + (size_t)d.elem_mat[e] * XG_J2_NPARAM;
     Element *ele = nullptr;
+    if (d.elem_type == XG_ELE_FBC2D || d.elem_type == XG_ELE_FBC3D) {
+      const int nip = d.fbc_num_ip;
+      SectionForceDeformation *proto = make_section(d, d.elem_mat[e], 1);
+      std::vector<SectionForceDeformation *> secs(nip, proto);
+      LobattoBeamIntegration lobatto;
+      if (d.elem_type == XG_ELE_FBC2D) {
+        CrdTransf *tr = d.geom_transf ? (CrdTransf *)new PDeltaCrdTransf2d(1)
+                                      : (CrdTransf *)new LinearCrdTransf2d(1);
+        ele = new ForceBeamColumn2d(d.elem_tag[e], c[0], c[1], nip, secs.data(), lobatto, *tr,
+                                    0.0, d.fbc_max_iters, d.fbc_tol);
+        delete tr;
+      } else {
+        const double *vz = d.elem_vecxz + 3 * (size_t)e;
+        Vector3D vecxz{vz[0], vz[1], vz[2]};
+        FrameTransform<2, 6> *t = d.geom_transf
+                                      ? (FrameTransform<2, 6> *)new PDeltaFrameTransf<2, 6>(1, vecxz)
+                                      : (FrameTransform<2, 6> *)new LinearFrameTransf<2, 6>(1, vecxz);
+        BasicFrameTransf3d tr(t);
+        ele = new ForceBeamColumn3d(d.elem_tag[e], c[0], c[1], nip, secs.data(), lobatto, tr,
+                                    0.0, d.fbc_max_iters, d.fbc_tol);
+      }
+      delete proto;
+      dom->addElement(ele);
+      continue;
+    }
+    const double *p = d.j2_param + (size_t)d.elem_mat[e] * XG_J2_NPARAM;
     if (d.elem_type == XG_ELE_QUAD) {
       J2PlaneStrain mat(1, p[0], p[1], p[2], p[3], p[4], p[5], p[6], p[7]);
       std::array<int, 4> nd{c[0], c[1], c[2], c[3]};
@@ -491,4 +565,21 @@ extern "C" int xref_captured_lambda(void *hp, double *lam) {
   Capture &c = ((Harness *)hp)->cap;
   memcpy(lam, c.lam.data(), sizeof(double) * c.lam.size());
   return (int)c.lam.size();
+}
+
+// Uniaxial material path (Steel02 / Concrete02): stress and tangent at each
+// trial strain; commit[k] != 0 commits after point k.
+extern "C" int xref_uniaxial_path(int type, const double *param, int npts, const double *strain,
+                                  const int *commit, double *stress, double *tangent) {
+  UniaxialMaterial *m = make_uniaxial(type, param, 1);
+  if (!m) return -1;
+  for (int k = 0; k < npts; k++) {
+    double s = 0, t = 0;
+    m->setTrial(strain[k], s, t);
+    stress[k] = s;
+    tangent[k] = t;
+    if (commit[k]) m->commitState();
+  }
+  delete m;
+  return 0;
 }

@@ -417,7 +417,18 @@ typedef struct xo_model {
   int pattern_const[8], added[8];
   double time, time_c;
   double elem_s, solve_s;
+  /* force-based frames (xara_oracle_frame.inc) */
+  int fr_nb, fr_order, fr_nip;
+  double *ybar, *zbar;               /* section centroids                   */
+  double *fr_L, *fr_R;               /* length, local axes [ne*9]           */
+  long *fr_foff;                     /* fiber record offset per element     */
+  double *fr_fh_c, *fr_fh_t;         /* fiber records                       */
+  double *fr_Se, *fr_kv, *fr_Se_c, *fr_kv_c, *fr_vs, *fr_vs_c, *fr_fs, *fr_Ssr, *fr_vlast;
+  int *fr_init;
 } xo_model;
+
+static int csr_find(const struct xo_model *m, int row, int col);
+#include "xara_oracle_frame.inc"
 
 static int node_index(const xg_model_desc *d, int tag) {
   int lo = 0, hi = d->num_nodes - 1;
@@ -589,13 +600,16 @@ static int xo_number(xo_model *m) {
 }
 
 int xo_elem_update_flag(xo_model *m, int compute);
+void xo_destroy(xo_model *m);
 
 xo_model *xo_create(const xg_model_desc *desc) {
   xo_model *m = (xo_model *)calloc(1, sizeof(xo_model));
   m->d = *desc;
   const xg_model_desc *d = &m->d;
+  int frames = d->elem_type == XG_ELE_FBC2D || d->elem_type == XG_ELE_FBC3D;
   if (d->elem_type == XG_ELE_QUAD) { m->nen = 4; m->nip = 4; }
   else if (d->elem_type == XG_ELE_BRICK) { m->nen = 8; m->nip = 8; }
+  else if (frames) { m->nen = 2; m->nip = 0; }
   else { free(m); return NULL; }
   m->nu = d->num_nodes * d->ndf;
   m->conn = (int *)malloc(sizeof(int) * (size_t)d->num_elems * m->nen);
@@ -621,14 +635,17 @@ xo_model *xo_create(const xg_model_desc *desc) {
   m->B = (double *)calloc(m->neq, sizeof(double));
   m->invD = (double *)calloc(m->neq, sizeof(double));
   m->sky = (double *)calloc(m->diag[m->neq], sizeof(double));
-  /* the material constructors evaluate the zero-strain state
-     (J2Plasticity.cpp:84-111 calls plastic_integrator) */
+  if (frames && xo_frame_setup(m) < 0) { xo_destroy(m); return NULL; }
+  /* Domain::addElement calls Element::update once (domain/domain/Domain.cpp:
+     390-392); the J2 constructors also evaluate the zero-strain state
+     (J2Plasticity.cpp:84-111) */
   xo_elem_update_flag(m, 1);
   return m;
 }
 
 void xo_destroy(xo_model *m) {
   if (!m) return;
+  if (m->d.elem_type == XG_ELE_FBC2D || m->d.elem_type == XG_ELE_FBC3D) xo_frame_free(m);
   free(m->conn); free(m->eqn); free(m->rowptr); free(m->colidx); free(m->rowtop);
   free(m->diag); free(m->sky); free(m->invD); free(m->U); free(m->Uc); free(m->ep_c);
   free(m->ep_t); free(m->xi_c); free(m->xi_t); free(m->sig_t); free(m->D_t); free(m->vals); free(m->resid);
@@ -643,7 +660,7 @@ void xo_pattern(const xo_model *m, int *rowptr, int *colidx) {
   memcpy(colidx, m->colidx, sizeof(int) * (size_t)m->nnz);
 }
 
-static int csr_find(const xo_model *m, int row, int col) {
+static int csr_find(const struct xo_model *m, int row, int col) {
   int lo = m->rowptr[row], hi = m->rowptr[row + 1] - 1;
   while (lo <= hi) {
     int mid = (lo + hi) / 2;
@@ -662,6 +679,8 @@ static int csr_find(const xo_model *m, int row, int col) {
  */
 int xo_elem_update_flag(xo_model *m, int compute) {
   const xg_model_desc *d = &m->d;
+  if (d->elem_type == XG_ELE_FBC2D || d->elem_type == XG_ELE_FBC3D)
+    return xo_frame_elem_phase(m, compute);
   int ndf = d->ndf, nen = m->nen, nip = m->nip, ned = nen * ndf;
   memset(m->vals, 0, sizeof(double) * (size_t)m->nnz);
   memset(m->resid, 0, sizeof(double) * m->neq);
@@ -718,6 +737,7 @@ int xo_elem_state(xo_model *m, const double *U, double *vals, double *resid) {
 
 void xo_commit(xo_model *m) {
   size_t nh = (size_t)m->d.num_elems * m->nip;
+  if (m->d.elem_type == XG_ELE_FBC2D || m->d.elem_type == XG_ELE_FBC3D) xo_frame_commit(m);
   memcpy(m->ep_c, m->ep_t, sizeof(double) * nh * 9);
   memcpy(m->xi_c, m->xi_t, sizeof(double) * nh);
   memcpy(m->Uc, m->U, sizeof(double) * m->nu);

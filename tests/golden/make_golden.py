@@ -49,6 +49,21 @@ def j2_paths(seed=1):
     save("j2_paths", **out)
 
 
+def uniaxial_paths(seed=2):
+    """Random strain paths through Steel02 and Concrete02."""
+    rng = np.random.default_rng(seed)
+    out = {}
+    for kind, param, scale in ((1, configs.steel02_row(350e6, 200e9, 0.01), 4e-3),
+                               (2, configs.concrete02_row(30e6), 2e-3)):
+        n = 400
+        strain = np.cumsum(rng.normal(0.0, scale / 3, size=n))
+        commit = (rng.random(n) < 0.5).astype(np.int32)
+        s, t = ref.uniaxial_path(kind, param, strain, commit)
+        out.update({f"k{kind}_param": param, f"k{kind}_strain": strain,
+                    f"k{kind}_commit": commit, f"k{kind}_stress": s, f"k{kind}_tangent": t})
+    save("uniaxial_paths", **out)
+
+
 def model_fixture(name, builder, args, kw, capture_steps=(), cap_solves=400):
     desc, phases = builder(*args, **kw)
     lo = min(capture_steps) if capture_steps else 0
@@ -67,6 +82,9 @@ def model_fixture(name, builder, args, kw, capture_steps=(), cap_solves=400):
                       cap_lambda=r.cap_lambda[keep])
         # committed material history at the start of every captured step,
         # from the oracle (itself pinned against the reference by these files)
+        if desc.elem_type in (3, 4):       # frames: replay from the start only
+            save(name, **arrays)
+            return
         nip = 4 if desc.elem_type == 1 else 8
         hist_ep, hist_xi = [], []
         for s in sorted(capture_steps):
@@ -91,6 +109,14 @@ def main():
     model_fixture("brick_4x3x2", configs.brick_block, (4, 3, 2), {"steps": 5},
                   capture_steps=(0, 2))
     model_fixture("brick_8x8x4", configs.brick_block, (8, 8, 4), {"steps": 10})
+    uniaxial_paths()
+    model_fixture("frame2d_2x3", configs.steel_frame_2d, (2, 3), {"steps": 10},
+                  capture_steps=(0,))
+    model_fixture("frame3d_1x1x2", configs.rc_frame_3d, (1, 1, 2),
+                  {"col_fibers": 40, "beam_fibers": 24, "steps": 10, "pdelta": 1},
+                  capture_steps=(0,))
+    model_fixture("frame3d_2x1x3", configs.rc_frame_3d, (2, 1, 3),
+                  {"col_fibers": 60, "beam_fibers": 40, "steps": 30, "pdelta": 1})
 
 
 if __name__ == "__main__":

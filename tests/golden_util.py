@@ -45,14 +45,18 @@ def unbalance_solves(fx, desc, phase):
     return np.arange(len(it))
 
 
-def external_load(fx, desc, k, eqn):
-    """F_ext of captured solve k: lambda times the pattern's reference loads."""
+def external_load(fx, desc, k, eqn, pattern=0):
+    """F_ext of captured solve k (a solve of the first phase): lambda times the
+    reference loads of that phase's pattern (later patterns are not yet in
+    the domain)."""
     neq = len(fx["colstart"]) - 1
     f = np.zeros(neq)
     lam = fx["cap_lambda"][k]
     if desc.load_node is None:
         return f
     for i, n in enumerate(desc.load_node):
+        if desc.load_pattern[i] != pattern:
+            continue
         idx = np.searchsorted(desc.node_tag, n)
         for j in range(desc.ndf):
             r = eqn[idx * desc.ndf + j]

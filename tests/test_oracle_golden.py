@@ -62,3 +62,45 @@ def test_replay_element_state(name):
             assert relerr(resid, fext - fx["cap_B"][k]) < RTOL_STATE
             assert relerr(vals, csc_to_csr_values(fx, fx["cap_A"][k])) < RTOL_STATE
         o.close()
+
+
+FRAMES = ["frame2d_2x3", "frame3d_1x1x2", "frame3d_2x1x3"]
+
+
+def test_uniaxial_paths():
+    fx = load("uniaxial_paths")
+    for kind in (1, 2):
+        s, t = port.uniaxial_path(kind, fx[f"k{kind}_param"], fx[f"k{kind}_strain"],
+                                  fx[f"k{kind}_commit"])
+        assert relerr(s, fx[f"k{kind}_stress"]) < RTOL_STATE
+        assert relerr(t, fx[f"k{kind}_tangent"]) < RTOL_STATE
+
+
+@pytest.mark.parametrize("name", FRAMES)
+def test_frame_numbering_and_history(name):
+    fx = load(name)
+    desc, phases = model_of(fx)
+    o = port.OracleModel(desc)
+    assert np.array_equal(o.numbering(), fx["eqn"])
+    rp, ci = o.pattern()
+    assert np.array_equal(rp, fx["colstart"]) and np.array_equal(ci, fx["rowidx"])
+    U, lam, its = o.run(phases)
+    assert relerr(U, fx["step_u"]) < RTOL_HISTORY
+    assert relerr(lam, fx["step_lambda"]) < RTOL_HISTORY
+    assert np.array_equal(its, fx["step_iters"])
+
+
+@pytest.mark.parametrize("name", ["frame2d_2x3", "frame3d_1x1x2"])
+def test_frame_replay_first_step(name):
+    """Every Newton iteration of the first gravity step, replayed in order
+    (the force-based element state is incremental, so the trial displacements
+    are applied in the reference's sequence)."""
+    fx = load(name)
+    desc, phases = model_of(fx)
+    o = port.OracleModel(desc)
+    eqn = fx["eqn"]
+    for k in range(len(fx["cap_step"])):
+        vals, resid = o.elem_state(fx["cap_U"][k])
+        fext = external_load(fx, desc, k, eqn)
+        assert relerr(resid, fext - fx["cap_B"][k]) < RTOL_STATE
+        assert relerr(vals, csc_to_csr_values(fx, fx["cap_A"][k])) < RTOL_STATE

@@ -134,3 +134,255 @@ def brick_block(nx=128, ny=128, nz=64, strain=0.01, steps=50, j2=J2_STEEL,
                       dc_node=master, dc_dof=2, dc_incr=-strain * nz / steps,
                       test=XG_TEST_NORM_DISP_INCR, tol=tol, max_iter=max_iter)
     return desc, [phase]
+
+
+# ---------------------------------------------------------------------------
+# frames: `element forceBeamColumn` with Lobatto points and fiber sections
+# ---------------------------------------------------------------------------
+from ._abi import (XG_ELE_FBC2D, XG_ELE_FBC3D, XG_INT_LOAD_CONTROL,  # noqa: E402
+                   XG_UNI_CONCRETE02, XG_UNI_ELASTIC, XG_UNI_STEEL02, XG_UNI_NPARAM)
+
+
+def steel02_row(fy=350e6, E=200e9, b=0.01, R0=18.0, cR1=0.925, cR2=0.15):
+    """`uniaxialMaterial Steel02 tag fy E b R0 cR1 cR2` (a1..a4 = 0 1 0 1)."""
+    r = np.zeros(XG_UNI_NPARAM)
+    r[:11] = [fy, E, b, R0, cR1, cR2, 0.0, 1.0, 0.0, 1.0, 0.0]
+    return r
+
+
+def concrete02_row(fc, epsc0=0.002, fcu_ratio=0.2, epscu=0.006, rat=0.1, ft_ratio=0.1):
+    """`uniaxialMaterial Concrete02 tag fc epsc0 fcu epscu lambda ft Ets` with
+    ft = ft_ratio*fc and Ets = ft_ratio*fc/epsc0 (magnitudes; signs forced
+    negative by the material for the compressive values)."""
+    r = np.zeros(XG_UNI_NPARAM)
+    r[:7] = [-fc, -epsc0, -fcu_ratio * fc, -epscu, rat, ft_ratio * fc, ft_ratio * fc / epsc0]
+    return r
+
+
+def wide_flange_fibers(d=0.4, bf=0.2, tf=0.015, tw=0.01, nf=40):
+    """Fibers (y, A) of a wide-flange section about its strong axis: nf/4 per
+    flange, nf/2 in the web."""
+    nfl, nw = nf // 4, nf - 2 * (nf // 4)
+    ys, As = [], []
+    hw = d - 2 * tf
+    for k in range(nfl):                       # top flange
+        ys.append(d / 2 - tf * (k + 0.5) / nfl)
+        As.append(bf * tf / nfl)
+    for k in range(nw):                        # web
+        ys.append(hw / 2 - hw * (k + 0.5) / nw)
+        As.append(tw * hw / nw)
+    for k in range(nfl):                       # bottom flange
+        ys.append(-d / 2 + tf * (k + 0.5) / nfl)
+        As.append(bf * tf / nfl)
+    return np.array(ys), np.array(As)
+
+
+def steel_frame_2d(bays=2, stories=3, bay=6.0, story=3.5, nfib=40, fy=350e6, E=200e9,
+                   b=0.01, pdelta=0, gravity=-150e3, drift=0.02, steps=20, grav_steps=10,
+                   max_iter=50, tol=1e-10, seed=None):
+    """2D steel moment frame: `forceBeamColumn` columns and beams with 5
+    Lobatto points and Steel02 wide-flange fiber sections, base fixed,
+    gravity at every floor node (LoadControl, then `loadConst -time 0`), and a
+    lateral pushover of the roof-left node by DisplacementControl against a
+    triangular reference load pattern."""
+    rng = np.random.default_rng(seed) if seed is not None else None
+    nx = bays + 1
+    tags, crd = [], []
+    for j in range(stories + 1):
+        for i in range(nx):
+            tags.append(j * nx + i + 1)
+            crd.append([i * bay, j * story])
+    crd = np.asarray(crd)
+    conn, sec = [], []
+    for j in range(stories):                   # columns
+        for i in range(nx):
+            conn.append([j * nx + i + 1, (j + 1) * nx + i + 1])
+            sec.append(0)
+    for j in range(1, stories + 1):            # beams
+        for i in range(bays):
+            conn.append([j * nx + i + 1, j * nx + i + 2])
+            sec.append(1)
+    ne = len(conn)
+    if rng is not None:
+        fy = float(np.exp(rng.normal(np.log(fy), 0.1)))
+        b = float(rng.uniform(0.005, 0.02))
+    yc, Ac = wide_flange_fibers(0.45, 0.3, 0.022, 0.014, nfib)
+    yb, Ab = wide_flange_fibers(0.5, 0.2, 0.016, 0.010, nfib)
+    uni = np.stack([steel02_row(fy, E, b)])
+    fib_y = np.concatenate([yc, yb])
+    fib_A = np.concatenate([Ac, Ab])
+    fib_m = np.zeros(len(fib_y), np.int32)
+    sp_node = np.repeat(np.arange(1, nx + 1), 3)
+    sp_dof = np.tile([0, 1, 2], nx)
+    floors = np.arange(nx + 1, (stories + 1) * nx + 1)
+    roof_left = stories * nx + 1
+    load_node = list(floors) + [j * nx + 1 for j in range(1, stories + 1)]
+    load_pat = [0] * len(floors) + [1] * stories
+    load_val = [[0.0, gravity, 0.0]] * len(floors) + \
+               [[float(j) / stories, 0.0, 0.0] for j in range(1, stories + 1)]
+    desc = ModelDesc(
+        ndm=2, ndf=3, elem_type=XG_ELE_FBC2D, geom_transf=pdelta, fbc_num_ip=5,
+        node_tag=tags, node_crd=crd,
+        elem_tag=np.arange(1, ne + 1), elem_conn=conn, elem_mat=sec,
+        uni_type=[XG_UNI_STEEL02], uni_param=uni,
+        sec_fiber_start=[0, nfib, 2 * nfib], fib_y=fib_y, fib_area=fib_A, fib_mat=fib_m,
+        sp_node=sp_node, sp_dof=sp_dof, sp_pattern=np.full(len(sp_node), -1),
+        sp_value=np.zeros(len(sp_node)),
+        load_node=load_node, load_pattern=load_pat, load_value=load_val,
+    )
+    H = stories * story
+    desc.meta = dict(workload=f"2D steel frame {bays}x{stories}", fibers=ne * 5 * nfib,
+                     roof=roof_left)
+    phases = [
+        PhaseDesc(integrator=XG_INT_LOAD_CONTROL, pattern=0, num_steps=grav_steps,
+                  d_lambda=1.0 / grav_steps, tol=tol, max_iter=max_iter, load_const=1),
+        PhaseDesc(integrator=XG_INT_DISP_CONTROL, pattern=1, num_steps=steps,
+                  dc_node=roof_left, dc_dof=0, dc_incr=drift * H / steps, tol=tol,
+                  max_iter=max_iter),
+    ]
+    return desc, phases
+
+
+def rc_section_fibers(b, h, cover, n_core_y, n_core_z, n_cover, n_bars, bar_area):
+    """Fibers (y, z, A, kind) of a rectangular RC section: a core patch
+    n_core_y x n_core_z, a cover ring of n_cover fibers, and n_bars bars on
+    the core perimeter.  kind 0 core concrete, 1 cover concrete, 2 steel."""
+    ys, zs, As, kind = [], [], [], []
+    bc, hc = b - 2 * cover, h - 2 * cover
+    for i in range(n_core_y):
+        for k in range(n_core_z):
+            ys.append(-hc / 2 + hc * (i + 0.5) / n_core_y)
+            zs.append(-bc / 2 + bc * (k + 0.5) / n_core_z)
+            As.append(bc * hc / (n_core_y * n_core_z))
+            kind.append(0)
+    per_side = n_cover // 4
+    sides = [((-h / 2 + cover / 2, -b / 2), (-h / 2 + cover / 2, b / 2), b * cover),
+             ((h / 2 - cover / 2, -b / 2), (h / 2 - cover / 2, b / 2), b * cover),
+             ((-hc / 2, -b / 2 + cover / 2), (hc / 2, -b / 2 + cover / 2), hc * cover),
+             ((-hc / 2, b / 2 - cover / 2), (hc / 2, b / 2 - cover / 2), hc * cover)]
+    for (p0, p1, area) in sides:
+        for k in range(per_side):
+            t = (k + 0.5) / per_side
+            ys.append(p0[0] + t * (p1[0] - p0[0]))
+            zs.append(p0[1] + t * (p1[1] - p0[1]))
+            As.append(area / per_side)
+            kind.append(1)
+    per = n_bars // 4
+    corners = [(-hc / 2, -bc / 2), (-hc / 2, bc / 2), (hc / 2, bc / 2), (hc / 2, -bc / 2)]
+    for s in range(4):
+        a, c = corners[s], corners[(s + 1) % 4]
+        for k in range(per):
+            t = k / per
+            ys.append(a[0] + t * (c[0] - a[0]))
+            zs.append(a[1] + t * (c[1] - a[1]))
+            As.append(bar_area)
+            kind.append(2)
+    return np.array(ys), np.array(zs), np.array(As), np.array(kind)
+
+
+def rc_frame_3d(bays_x=10, bays_y=10, stories=20, bay=6.0, story=3.5, col_fibers=120,
+                beam_fibers=64, pdelta=1, drift=0.02, steps=200, grav_steps=10, seed=0,
+                gravity=-250e3, max_iter=50, tol=1e-10):
+    """3D RC frame of `forceBeamColumn` elements (5 Lobatto points) with
+    Concrete02 (cover fc 28 MPa, core fc 45 MPa at the base falling linearly
+    to 28 MPa at the roof) and Steel02 (fy 420 MPa, E 200 GPa, b 0.01, R0 18)
+    fiber sections and elastic torsion, `geomTransf PDelta`; gravity at every
+    floor node by LoadControl then `loadConst`; pushover of a roof corner in x
+    by DisplacementControl to ``drift`` of the height against a triangular
+    reference pattern.  Column sections have ``col_fibers`` fibers, beams
+    ``beam_fibers``."""
+    rng = np.random.default_rng(seed)
+    nxn, nyn = bays_x + 1, bays_y + 1
+    per_floor = nxn * nyn
+
+    def nid(i, j, k):
+        return k * per_floor + j * nxn + i + 1
+
+    tags, crd = [], []
+    for k in range(stories + 1):
+        for j in range(nyn):
+            for i in range(nxn):
+                tags.append(nid(i, j, k))
+                crd.append([i * bay, j * bay, k * story])
+    crd = np.asarray(crd)
+    # materials: 0 cover, 1..stories core by story, last steel
+    core_fc = 45e6 - (45e6 - 28e6) * np.arange(stories) / max(stories - 1, 1)
+    core_fc *= 1.0 + 0.02 * rng.uniform(-1, 1, size=stories)
+    uni_rows = [concrete02_row(28e6, 0.002, 0.2, 0.006)]
+    for fc in core_fc:
+        uni_rows.append(concrete02_row(fc, 0.002, 0.2, 0.02))
+    uni_rows.append(steel02_row(420e6, 200e9, 0.01, 18.0))
+    steel = len(uni_rows) - 1
+    uni_type = [XG_UNI_CONCRETE02] * (stories + 1) + [XG_UNI_STEEL02]
+    # sections: columns per story, beams per story
+    def fibers_for(total, b, h):
+        n_bars = 16 if total >= 100 else (8 if total >= 40 else 4)
+        n_cover = 40 if total >= 100 else (16 if total >= 40 else 8)
+        rest = total - n_bars - n_cover
+        ny = int(np.floor(np.sqrt(rest)))
+        while rest % ny:
+            ny -= 1
+        return rc_section_fibers(b, h, 0.04, ny, rest // ny, n_cover, n_bars,
+                                 0.0005 if total >= 100 else 0.0004)
+    sec_start, fy_, fz_, fA_, fm_, GJ = [0], [], [], [], [], []
+    Gc = 12e9
+    for k in range(stories):
+        for (total, b, h) in ((col_fibers, 0.6, 0.6), (beam_fibers, 0.4, 0.6)):
+            y, z, A, kind = fibers_for(total, b, h)
+            mat = np.where(kind == 0, 1 + k, np.where(kind == 1, 0, steel))
+            fy_.append(y); fz_.append(z); fA_.append(A); fm_.append(mat)
+            sec_start.append(sec_start[-1] + len(y))
+            J = 0.141 * max(b, h) * min(b, h) ** 3
+            GJ.append(Gc * J)
+    conn, sec, vecxz = [], [], []
+    for k in range(stories):                    # columns
+        for j in range(nyn):
+            for i in range(nxn):
+                conn.append([nid(i, j, k), nid(i, j, k + 1)])
+                sec.append(2 * k)
+                vecxz.append([1.0, 0.0, 0.0])
+    for k in range(1, stories + 1):             # beams in x, then in y
+        for j in range(nyn):
+            for i in range(bays_x):
+                conn.append([nid(i, j, k), nid(i + 1, j, k)])
+                sec.append(2 * (k - 1) + 1)
+                vecxz.append([0.0, 0.0, 1.0])
+        for j in range(bays_y):
+            for i in range(nxn):
+                conn.append([nid(i, j, k), nid(i, j + 1, k)])
+                sec.append(2 * (k - 1) + 1)
+                vecxz.append([0.0, 0.0, 1.0])
+    ne = len(conn)
+    base = [nid(i, j, 0) for j in range(nyn) for i in range(nxn)]
+    sp_node = np.repeat(base, 6)
+    sp_dof = np.tile(np.arange(6), len(base))
+    floors = [nid(i, j, k) for k in range(1, stories + 1) for j in range(nyn) for i in range(nxn)]
+    roof = nid(0, 0, stories)
+    lat_nodes = [nid(0, 0, k) for k in range(1, stories + 1)]
+    load_node = floors + lat_nodes
+    load_pat = [0] * len(floors) + [1] * len(lat_nodes)
+    load_val = [[0.0, 0.0, gravity, 0.0, 0.0, 0.0]] * len(floors) + \
+               [[float(k) / stories, 0, 0, 0, 0, 0] for k in range(1, stories + 1)]
+    desc = ModelDesc(
+        ndm=3, ndf=6, elem_type=XG_ELE_FBC3D, geom_transf=pdelta, fbc_num_ip=5,
+        node_tag=tags, node_crd=crd,
+        elem_tag=np.arange(1, ne + 1), elem_conn=conn, elem_mat=sec, elem_vecxz=vecxz,
+        uni_type=uni_type, uni_param=np.stack(uni_rows),
+        sec_fiber_start=sec_start, fib_y=np.concatenate(fy_), fib_z=np.concatenate(fz_),
+        fib_area=np.concatenate(fA_), fib_mat=np.concatenate(fm_), sec_GJ=GJ,
+        sp_node=sp_node, sp_dof=sp_dof, sp_pattern=np.full(len(sp_node), -1),
+        sp_value=np.zeros(len(sp_node)),
+        load_node=load_node, load_pattern=load_pat, load_value=load_val,
+    )
+    H = stories * story
+    nfib = sum(np.diff(sec_start)[sec[e]] for e in range(ne)) * 5
+    desc.meta = dict(workload=f"3D RC frame {bays_x}x{bays_y}x{stories}", roof=roof,
+                     fiber_points=int(nfib), elements=ne)
+    phases = [
+        PhaseDesc(integrator=XG_INT_LOAD_CONTROL, pattern=0, num_steps=grav_steps,
+                  d_lambda=1.0 / grav_steps, tol=tol, max_iter=max_iter, load_const=1),
+        PhaseDesc(integrator=XG_INT_DISP_CONTROL, pattern=1, num_steps=steps,
+                  dc_node=roof, dc_dof=0, dc_incr=drift * H / steps, tol=tol,
+                  max_iter=max_iter),
+    ]
+    return desc, phases
