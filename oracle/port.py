@@ -51,6 +51,7 @@ def lib():
         L.xo_pattern.argtypes = [vp, vp, vp]
         L.xo_elem_state.argtypes = [vp, vp, vp, vp]
         L.xo_commit.argtypes = [vp]
+        L.xo_revert.argtypes = [vp]
         L.xo_run_phase.argtypes = [vp, vp, vp, vp, vp]
         L.xo_times.argtypes = [vp, vp, vp]
         L.xo_history.argtypes = [vp, vp, vp]
@@ -111,6 +112,9 @@ class OracleModel:
 
     def commit(self):
         lib().xo_commit(self.h)
+
+    def revert(self):
+        lib().xo_revert(self.h)
 
     def run(self, phases):
         L = lib()

@@ -95,6 +95,22 @@ class RefRun:
         L.xref_times(self.h, C.byref(e), C.byref(s), C.byref(t))
         self.elem_seconds, self.solve_seconds, self.step_seconds = e.value, s.value, t.value
 
+    def elem_response(self, U, revert_first=False):
+        """Per-element global tangent [ne, ned, ned] and resisting force
+        [ne, ned] at trial displacements U (after Domain::revertToLastCommit
+        when revert_first)."""
+        L = lib()
+        L.xref_elem_response.argtypes = [C.c_void_p, C.c_void_p, C.c_int, C.c_void_p, C.c_void_p]
+        d = self.desc
+        ned = (2 if d.elem_type in (3, 4) else 4 if d.elem_type == 1 else 8) * d.ndf
+        K = np.zeros((d.num_elems, ned, ned))
+        P = np.zeros((d.num_elems, ned))
+        U = np.ascontiguousarray(U, np.float64)
+        r = L.xref_elem_response(self.h, _p(U), int(revert_first), _p(K), _p(P))
+        if r != 0:
+            raise RuntimeError(f"reference element response failed: {r}")
+        return K, P
+
 
 def j2_path(dim, param, strain, commit):
     """Stress and tangent of J2PlaneStrain (dim=2) / J2ThreeDimensional (dim=3)."""

@@ -583,3 +583,31 @@ extern "C" int xref_uniaxial_path(int type, const double *param, int npts, const
   delete m;
   return 0;
 }
+
+// Element response at trial displacements U[num_nodes*ndf]: optionally
+// Domain::revertToLastCommit first, then Node::setTrialDisp on every node,
+// Domain::update, and each element's global tangent and resisting force
+// (element order of the description; K[ne*ned*ned] row major, P[ne*ned]).
+extern "C" int xref_elem_response(void *hp, const double *U, int revert_first, double *K,
+                                  double *P) {
+  Harness *h = (Harness *)hp;
+  const xg_model_desc &d = h->d;
+  if (revert_first && h->domain->revertToLastCommit() < 0) return -1;
+  for (int i = 0; i < d.num_nodes; i++) {
+    Vector u(d.ndf);
+    for (int j = 0; j < d.ndf; j++) u(j) = U[(size_t)i * d.ndf + j];
+    h->nodes[i]->setTrialDisp(u);
+  }
+  if (h->domain->update() < 0) return -2;
+  const int ned = nen_of(d.elem_type) * d.ndf;
+  for (int e = 0; e < d.num_elems; e++) {
+    Element *ele = h->domain->getElement(d.elem_tag[e]);
+    const Matrix &k = ele->getTangentStiff();
+    const Vector &p = ele->getResistingForce();
+    for (int a = 0; a < ned; a++) {
+      P[(size_t)e * ned + a] = p(a);
+      for (int b = 0; b < ned; b++) K[((size_t)e * ned + a) * ned + b] = k(a, b);
+    }
+  }
+  return 0;
+}

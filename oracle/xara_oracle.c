@@ -744,6 +744,18 @@ void xo_commit(xo_model *m) {
   m->time_c = m->time;
 }
 
+/* Domain::revertToLastCommit (domain/domain/Domain.cpp:1925-1949): nodes
+   and elements back to the last commit, then Domain::update. */
+void xo_revert(xo_model *m) {
+  size_t nh = (size_t)m->d.num_elems * m->nip;
+  memcpy(m->U, m->Uc, sizeof(double) * m->nu);
+  memcpy(m->ep_t, m->ep_c, sizeof(double) * nh * 9);
+  memcpy(m->xi_t, m->xi_c, sizeof(double) * nh);
+  m->time = m->time_c;
+  if (m->d.elem_type == XG_ELE_FBC2D || m->d.elem_type == XG_ELE_FBC3D) xo_frame_revert(m);
+  xo_elem_update(m);   /* Domain::revertToLastCommit ends with update() */
+}
+
 /*
  * ProfileSPDLinDirectSolver::solve (profileSPD/ProfileSPDLinDirectSolver.cpp:
  * 100-250): skyline LDL^T of the assembled tangent, then forward and back

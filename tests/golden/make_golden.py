@@ -100,6 +100,23 @@ def model_fixture(name, builder, args, kw, capture_steps=(), cap_solves=400):
     save(name, **arrays)
 
 
+def revert_fixture(name, builder, args, kw, seed=5, scale=2e-4):
+    """Element responses around the end of the first phase: at U + dU, then
+    after Domain::revertToLastCommit at U + dU/2 (the committed state's
+    bookkeeping: initialFlag, section re-evaluation, fiber records)."""
+    desc, phases = builder(*args, **kw)
+    r = ref.RefRun(desc, phases[:1])
+    u = r.step_u[-1]
+    du = scale * np.random.default_rng(seed).normal(size=u.size)
+    du[r.eqn < 0] = 0.0
+    K1, P1 = r.elem_response(u + du)
+    K2, P2 = r.elem_response(u + 0.5 * du, revert_first=True)
+    save(name, builder=np.array(builder.__name__), args=np.asarray(args),
+         kw_keys=np.array(list(kw.keys())), kw_vals=np.asarray(list(kw.values()), np.float64),
+         eqn=r.eqn, colstart=r.colstart, rowidx=r.rowidx, u=u, du=du,
+         K1=K1, P1=P1, K2=K2, P2=P2)
+
+
 def main():
     if not ref.available():
         sys.exit("oracle/_ref/libxara_ref.so missing: run python oracle/build_ref.py")
@@ -117,6 +134,10 @@ def main():
                   capture_steps=(0,))
     model_fixture("frame3d_2x1x3", configs.rc_frame_3d, (2, 1, 3),
                   {"col_fibers": 60, "beam_fibers": 40, "steps": 30, "pdelta": 1})
+    revert_fixture("revert_frame2d_2x3", configs.steel_frame_2d, (2, 3), {"steps": 10})
+    revert_fixture("revert_frame3d_1x1x2", configs.rc_frame_3d, (1, 1, 2),
+                   {"col_fibers": 40, "beam_fibers": 24, "steps": 10, "pdelta": 1})
+    revert_fixture("revert_quad_8x4", configs.quad_block, (8, 4), {}, scale=1e-4)
 
 
 if __name__ == "__main__":

@@ -78,3 +78,29 @@ def csc_to_csr_values(fx, vals_csc):
     # at the CSC position whose (col, row) key is (ri[k], cols[k]).
     p = np.searchsorted(key_csc, ri.astype(np.int64) * n + cols)
     return vals_csc[p]
+
+
+def assemble_elements(desc, eqn, rowptr, colidx, K, P):
+    """Assemble per-element global tangents K[ne, ned, ned] and resisting
+    forces P[ne, ned] (element order of the description) into CSR values in
+    the order of (rowptr, colidx) and the resisting force per equation."""
+    ne, ned = P.shape
+    nen = ned // desc.ndf
+    conn = np.asarray(desc.elem_conn).reshape(ne, nen)
+    idx = np.searchsorted(np.asarray(desc.node_tag), conn)
+    ids = (idx[:, :, None] * desc.ndf + np.arange(desc.ndf)).reshape(ne, ned)
+    ids = np.asarray(eqn)[ids]
+    vals = np.zeros(len(colidx))
+    resid = np.zeros(len(rowptr) - 1)
+    for e in range(ne):
+        for a in range(ned):
+            r = ids[e, a]
+            if r < 0:
+                continue
+            resid[r] += P[e, a]
+            row = colidx[rowptr[r]:rowptr[r + 1]]
+            for b in range(ned):
+                c = ids[e, b]
+                if c >= 0:
+                    vals[rowptr[r] + np.searchsorted(row, c)] += K[e, a, b]
+    return vals, resid

@@ -9,8 +9,8 @@ numbers, CSR pattern) is bit-exact.
 import numpy as np
 import pytest
 
-from golden_util import (RTOL_HISTORY, RTOL_STATE, csc_to_csr_values, external_load, load,
-                         model_of, relerr, unbalance_solves)
+from golden_util import (RTOL_HISTORY, RTOL_STATE, assemble_elements, csc_to_csr_values,
+                         external_load, load, model_of, relerr, unbalance_solves)
 
 pytestmark = pytest.mark.gpu
 
@@ -135,3 +135,68 @@ def test_round_trip_history_checkpoint(gpu_mod):
         m.set_history(h)
         v2, r2, _ = m.update()
     assert np.array_equal(v1, v2) and np.array_equal(r1, r2)
+
+
+FRAMES = ["frame2d_2x3", "frame3d_1x1x2", "frame3d_2x1x3"]
+
+
+@pytest.mark.parametrize("name", FRAMES)
+def test_frame_numbering_pattern_and_history(gpu_mod, name):
+    """forceBeamColumn frames (Steel02 / Concrete02 fibers): bit-exact
+    numbering and pattern, then the whole gravity + pushover analysis on the
+    device against the reference's converged displacements."""
+    fx = load(name)
+    desc, phases = model_of(fx)
+    with gpu_mod.DeviceModel(desc) as m:
+        assert np.array_equal(m.numbering(), fx["eqn"])
+        rp, ci = m.pattern()
+        assert np.array_equal(rp, fx["colstart"]) and np.array_equal(ci, fx["rowidx"])
+        U, lam, stats = m.run(phases)
+    assert relerr(U, fx["step_u"]) < RTOL_HISTORY
+    assert relerr(lam, fx["step_lambda"]) < RTOL_HISTORY
+    iters = np.array([s[0] for s in stats])
+    assert np.mean(iters == fx["step_iters"]) >= 0.8, (iters, fx["step_iters"])
+
+
+@pytest.mark.parametrize("name", ["frame2d_2x3", "frame3d_1x1x2"])
+def test_frame_replay_first_step(gpu_mod, name):
+    """Every Newton iteration of the first gravity step, replayed in the
+    reference's order (the element state is incremental): resisting force
+    and tangent of each trial displacement."""
+    fx = load(name)
+    desc, _ = model_of(fx)
+    eqn = fx["eqn"]
+    with gpu_mod.DeviceModel(desc) as m:
+        for k in range(len(fx["cap_step"])):
+            m.set_trial_disp(fx["cap_U"][k])
+            vals, resid, st = m.update()
+            fext = external_load(fx, desc, k, eqn)
+            assert relerr(resid, fext - fx["cap_B"][k]) < RTOL_STATE
+            assert relerr(vals, csc_to_csr_values(fx, fx["cap_A"][k])) < RTOL_STATE
+
+
+@pytest.mark.parametrize("name", ["revert_frame2d_2x3", "revert_frame3d_1x1x2",
+                                  "revert_quad_8x4"])
+def test_revert_to_last_commit(gpu_mod, name):
+    """Element state at U + dU, then xg_elemset_revert (Domain::
+    revertToLastCommit) and the state at U + dU/2, against the reference's
+    element responses: initialFlag, the sections re-evaluated at their
+    committed deformations and the fiber records all return as the
+    reference's do."""
+    fx = load(name)
+    desc, phases = model_of(fx)
+    rp, ci = fx["colstart"], fx["rowidx"]
+    u = fx["u"]
+    with gpu_mod.DeviceModel(desc) as m:
+        m.run(phases[:1], record=False)
+        uc, _ = m.disp()
+        assert relerr(uc, u) < RTOL_HISTORY
+        for key, trial, revert in (("1", u + fx["du"], False), ("2", u + 0.5 * fx["du"], True)):
+            if revert:
+                m.revert()
+            m.set_trial_disp(trial)
+            vals, resid, st = m.update()
+            v_ref, r_ref = assemble_elements(desc, fx["eqn"], rp, ci, fx["K" + key],
+                                             fx["P" + key])
+            assert relerr(resid, r_ref) < RTOL_STATE, key
+            assert relerr(vals, v_ref) < RTOL_STATE, key

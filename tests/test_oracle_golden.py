@@ -4,8 +4,8 @@ import numpy as np
 import pytest
 
 from oracle import port
-from golden_util import (RTOL_HISTORY, RTOL_STATE, csc_to_csr_values, external_load, load,
-                         model_of, relerr, unbalance_solves)
+from golden_util import (RTOL_HISTORY, RTOL_STATE, assemble_elements, csc_to_csr_values,
+                         external_load, load, model_of, relerr, unbalance_solves)
 
 MODELS = ["quad_8x4", "quad_64x16", "brick_4x3x2", "brick_8x8x4"]
 
@@ -104,3 +104,27 @@ def test_frame_replay_first_step(name):
         fext = external_load(fx, desc, k, eqn)
         assert relerr(resid, fext - fx["cap_B"][k]) < RTOL_STATE
         assert relerr(vals, csc_to_csr_values(fx, fx["cap_A"][k])) < RTOL_STATE
+
+
+REVERTS = ["revert_frame2d_2x3", "revert_frame3d_1x1x2", "revert_quad_8x4"]
+
+
+@pytest.mark.parametrize("name", REVERTS)
+def test_revert_to_last_commit(name):
+    """Element state at U + dU, then Domain::revertToLastCommit and the state
+    at U + dU/2, against the reference's element responses."""
+    fx = load(name)
+    desc, phases = model_of(fx)
+    rp, ci = fx["colstart"], fx["rowidx"]
+    o = port.OracleModel(desc)
+    U, _, _ = o.run(phases[:1])
+    assert relerr(U[-1], fx["u"]) < RTOL_HISTORY
+    u = fx["u"]
+    for key, trial, revert in (("1", u + fx["du"], False), ("2", u + 0.5 * fx["du"], True)):
+        if revert:
+            o.revert()
+        vals, resid = o.elem_state(trial)
+        v_ref, r_ref = assemble_elements(desc, fx["eqn"], rp, ci, fx["K" + key], fx["P" + key])
+        assert relerr(resid, r_ref) < RTOL_STATE, key
+        assert relerr(vals, v_ref) < RTOL_STATE, key
+    o.close()

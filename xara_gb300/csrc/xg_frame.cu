@@ -1,0 +1,731 @@
+// xg_frame.cu -- force-based frame elements with fiber sections, FP64.
+//
+// k_fbc_update: one warp per ForceBeamColumn2d/3d element.  The element's
+// compatibility iteration (strategy cascade and subdivision) runs in lock
+// step in all 32 lanes; the element's small matrices live in the warp's
+// slice of shared memory; the fibers of a section are spread across the
+// lanes and their stiffness and force resultants are reduced with a fixed
+// xor butterfly, so every run gives the same bits.  Fiber history is one
+// 12-double record per (element, integration point, fiber): committed and
+// trial copies.  k_fbc_assemble forms the global tangent and resisting
+// force of each element from its basic stiffness and forces.
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+#include "xg_internal.h"
+
+namespace xg {
+
+namespace {
+
+constexpr double kDblEps = 2.220446049250313e-16;
+
+// ---------------------------------------------------------------------------
+// uniaxial laws on a 12-double record:
+//   Steel02: 0 epsmin 1 epsmax 2 epspl 3 epss0 4 sigs0 5 epsr 6 sigr 7 kon
+//   Concrete02: 0 ecmin 1 dept;  all: 8 e 9 sig 10 eps
+// ---------------------------------------------------------------------------
+
+// Steel02::setTrialStrain (material/uniaxial/steel/Steel02.cpp:113-227)
+__device__ void steel02_trial(const double *q, const double *hc, double trialStrain,
+                              double *ht) {
+  const double Fy = q[0], E0 = q[1], b = q[2], R0 = q[3], cR1 = q[4], cR2 = q[5];
+  const double a1 = q[6], a2 = q[7], a3 = q[8], a4 = q[9], sigini = q[10];
+  const double Esh = b * E0, epsy = Fy / E0;
+  double eps = trialStrain;
+  if (sigini != 0.0) eps = trialStrain + sigini / E0;
+  const double epsP = hc[10], sigP = hc[9];
+  const double deps = eps - epsP;
+  double epsmax = hc[1], epsmin = hc[0], epspl = hc[2], epss0 = hc[3], sigs0 = hc[4];
+  double epsr = hc[5], sigr = hc[6];
+  int kon = (int)hc[7];
+  ht[10] = eps;
+  if (kon == 0 || kon == 3) {
+    if (fabs(deps) < 10.0 * kDblEps) {
+      ht[0] = epsmin; ht[1] = epsmax; ht[2] = epspl; ht[3] = epss0; ht[4] = sigs0;
+      ht[5] = epsr; ht[6] = sigr; ht[7] = 3.0; ht[8] = E0; ht[9] = sigini;
+      return;
+    }
+    epsmax = epsy;
+    epsmin = -epsy;
+    if (deps < 0.0) { kon = 2; epss0 = epsmin; sigs0 = -Fy; epspl = epsmin; }
+    else { kon = 1; epss0 = epsmax; sigs0 = Fy; epspl = epsmax; }
+  }
+  if (kon == 2 && deps > 0.0) {
+    kon = 1;
+    epsr = epsP;
+    sigr = sigP;
+    if (epsP < epsmin) epsmin = epsP;
+    const double d1 = (epsmax - epsmin) / (2.0 * (a4 * epsy));
+    const double shft = 1.0 + a3 * pow(d1, 0.8);
+    epss0 = (Fy * shft - Esh * epsy * shft - sigr + E0 * epsr) / (E0 - Esh);
+    sigs0 = Fy * shft + Esh * (epss0 - epsy * shft);
+    epspl = epsmax;
+  } else if (kon == 1 && deps < 0.0) {
+    kon = 2;
+    epsr = epsP;
+    sigr = sigP;
+    if (epsP > epsmax) epsmax = epsP;
+    const double d1 = (epsmax - epsmin) / (2.0 * (a2 * epsy));
+    const double shft = 1.0 + a1 * pow(d1, 0.8);
+    epss0 = (-Fy * shft + Esh * epsy * shft - sigr + E0 * epsr) / (E0 - Esh);
+    sigs0 = -Fy * shft + Esh * (epss0 + epsy * shft);
+    epspl = epsmin;
+  }
+  const double xi = fabs((epspl - epss0) / epsy);
+  const double R = R0 * (1.0 - (cR1 * xi) / (cR2 + xi));
+  const double epsrat = (eps - epsr) / (epss0 - epsr);
+  const double dum1 = 1.0 + pow(fabs(epsrat), R);
+  const double dum2 = pow(dum1, (1 / R));
+  double sig = b * epsrat + (1.0 - b) * epsrat / dum2;
+  sig = sig * (sigs0 - sigr) + sigr;
+  double e = b + (1.0 - b) / (dum1 * dum2);
+  e = e * (sigs0 - sigr) / (epss0 - epsr);
+  ht[0] = epsmin; ht[1] = epsmax; ht[2] = epspl; ht[3] = epss0; ht[4] = sigs0;
+  ht[5] = epsr; ht[6] = sigr; ht[7] = (double)kon; ht[8] = e; ht[9] = sig;
+}
+
+struct C02 {
+  double fc, epsc0, fcu, epscu, rat, ft, Ets;
+};
+
+// Concrete02 constructor sign normalisation (Concrete02.cpp:97-111)
+__device__ __forceinline__ C02 c02_params(const double *q) {
+  C02 c;
+  c.fc = q[0] > 0 ? -q[0] : q[0];
+  c.epsc0 = q[1] > 0 ? -q[1] : q[1];
+  c.fcu = q[2] > 0 ? -q[2] : q[2];
+  c.epscu = q[3] > 0 ? -q[3] : q[3];
+  c.rat = q[4];
+  c.ft = q[5];
+  c.Ets = q[6];
+  return c;
+}
+
+// Concrete02::Tens_Envlp / Compr_Envlp (Concrete02.cpp:421-497)
+__device__ __forceinline__ void c02_tens(const C02 &c, double epsc, double &sigc, double &Ect) {
+  const double Ec0 = 2.0 * c.fc / c.epsc0;
+  const double eps0 = c.ft / Ec0;
+  const double epsu = c.ft * (1.0 / c.Ets + 1.0 / Ec0);
+  if (epsc <= eps0) { sigc = epsc * Ec0; Ect = Ec0; }
+  else if (epsc <= epsu) { Ect = -c.Ets; sigc = c.ft - c.Ets * (epsc - eps0); }
+  else { Ect = 1.0e-10; sigc = 0.0; }
+}
+__device__ __forceinline__ void c02_compr(const C02 &c, double epsc, double &sigc, double &Ect) {
+  const double Ec0 = 2.0 * c.fc / c.epsc0;
+  const double ratLocal = epsc / c.epsc0;
+  if (epsc >= c.epsc0) {
+    sigc = c.fc * ratLocal * (2.0 - ratLocal);
+    Ect = Ec0 * (1.0 - ratLocal);
+  } else if (epsc > c.epscu) {
+    sigc = (c.fcu - c.fc) * (epsc - c.epsc0) / (c.epscu - c.epsc0) + c.fc;
+    Ect = (c.fcu - c.fc) / (c.epscu - c.epsc0);
+  } else {
+    sigc = c.fcu;
+    Ect = 1.0e-10;
+  }
+}
+
+// Concrete02::setTrialStrain (Concrete02.cpp:167-271); the early return
+// keeps the record's previous trial stress and tangent.
+__device__ void concrete02_trial(const double *q, const double *hc, double eps, double *ht) {
+  const C02 c = c02_params(q);
+  const double ec0 = c.fc * 2. / c.epsc0;
+  double ecmin = hc[0], dept = hc[1];
+  ht[0] = ecmin;
+  ht[1] = dept;
+  ht[10] = eps;
+  const double epsP = hc[10], sigP = hc[9];
+  const double deps = eps - epsP;
+  if (fabs(deps) < kDblEps) return;
+  double sig, e;
+  if (eps < ecmin) {
+    c02_compr(c, eps, sig, e);
+    ecmin = eps;
+  } else {
+    const double epsr = (c.fcu - c.rat * ec0 * c.epscu) / (ec0 * (1.0 - c.rat));
+    const double sigmr = ec0 * epsr;
+    double sigmm, dumy;
+    c02_compr(c, ecmin, sigmm, dumy);
+    const double er = (sigmm - sigmr) / (ecmin - epsr);
+    const double ept = ecmin - sigmm / er;
+    if (eps <= ept) {
+      const double sigmin = sigmm + er * (eps - ecmin);
+      const double sigmax = er * .5 * (eps - ept);
+      sig = sigP + ec0 * deps;
+      e = ec0;
+      if (sig <= sigmin) { sig = sigmin; e = er; }
+      if (sig >= sigmax) { sig = sigmax; e = 0.5 * er; }
+    } else {
+      const double epn = ept + dept;
+      double sicn;
+      if (eps <= epn) {
+        c02_tens(c, dept, sicn, e);
+        if (dept != 0.0) e = sicn / dept;
+        else e = ec0;
+        sig = e * (eps - ept);
+      } else {
+        const double epstmp = eps - ept;
+        c02_tens(c, epstmp, sig, e);
+        dept = eps - ept;
+      }
+    }
+  }
+  ht[0] = ecmin;
+  ht[1] = dept;
+  ht[8] = e;
+  ht[9] = sig;
+}
+
+// UniaxialMaterial::setTrial (material/uniaxial/UniaxialMaterial.cpp:70-81)
+__device__ __forceinline__ void uni_trial(int type, const double *q, const double *hc, double eps,
+                                          double *ht, double &sig, double &tan) {
+  if (type == XG_UNI_STEEL02) steel02_trial(q, hc, eps, ht);
+  else if (type == XG_UNI_CONCRETE02) concrete02_trial(q, hc, eps, ht);
+  else { ht[10] = eps; ht[9] = q[0] * eps; ht[8] = q[0]; }
+  sig = ht[9];
+  tan = ht[8];
+}
+
+// ---------------------------------------------------------------------------
+// small dense helpers (every lane of a warp runs them on the same data)
+// ---------------------------------------------------------------------------
+// Gauss-Jordan inverse with partial pivoting; the reference uses explicit
+// cofactor formulas (matrix/routines/invGL*.c) -- agreement to rounding.
+template <int N>
+__device__ void inv_gj(const double *A, double *Ainv) {
+  double M[N][2 * N];
+#pragma unroll
+  for (int i = 0; i < N; i++)
+#pragma unroll
+    for (int j = 0; j < 2 * N; j++) M[i][j] = j < N ? A[i * N + j] : (j - N == i ? 1.0 : 0.0);
+#pragma unroll
+  for (int c = 0; c < N; c++) {
+    int piv = c;
+    double best = fabs(M[c][c]);
+#pragma unroll
+    for (int i = c + 1; i < N; i++)
+      if (fabs(M[i][c]) > best) { best = fabs(M[i][c]); piv = i; }
+    if (piv != c) {
+#pragma unroll
+      for (int j = 0; j < 2 * N; j++) {
+        // swap rows c and piv without dynamic register indexing
+#pragma unroll
+        for (int r = c + 1; r < N; r++)
+          if (r == piv) { const double t = M[c][j]; M[c][j] = M[r][j]; M[r][j] = t; }
+      }
+    }
+    const double inv = 1.0 / M[c][c];
+#pragma unroll
+    for (int j = 0; j < 2 * N; j++) M[c][j] *= inv;
+#pragma unroll
+    for (int i = 0; i < N; i++) {
+      if (i == c) continue;
+      const double f = M[i][c];
+#pragma unroll
+      for (int j = 0; j < 2 * N; j++) M[i][j] -= f * M[c][j];
+    }
+  }
+#pragma unroll
+  for (int i = 0; i < N; i++)
+#pragma unroll
+    for (int j = 0; j < N; j++) Ainv[i * N + j] = M[i][N + j];
+}
+
+__device__ __forceinline__ double warp_sum(double v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
+// element-major state record: Se[6] kv[36] vs[nip*4] fs[nip*16] Ssr[nip*4]
+// vlast[6] init[1]
+__device__ __forceinline__ int st_stride(int nip) { return 6 + 36 + nip * 24 + 6 + 1; }
+
+// Basic deformations: LinearCrdTransf2d::getBasicTrialDisp
+// (coordTransformation/LinearCrdTransf2d.cpp:248-299) and
+// BasicFrameTransf3d::getBasicTrialDisp (Frame/BasicFrameTransf.cpp:90-104)
+// over LinearFrameTransf<2,6> (Frame/LinearFrameTransf.tpp:258-386).
+template <int NB>
+__device__ void frame_basic(const FrameView &v, int e, double *ub) {
+  const int ndf = v.ndf;
+  const int a = v.conn[2 * e], b = v.conn[2 * e + 1];
+  const double *uI = v.U + (long)a * ndf, *uJ = v.U + (long)b * ndf;
+  const double L = v.L[e];
+  const double *R = v.R + 9 * (long)e;
+  if (NB == 3) {
+    const double cs = R[0], sn = R[1];
+    const double oneOverL = 1.0 / L, sl = sn * oneOverL, cl = cs * oneOverL;
+    ub[0] = -cs * uI[0] - sn * uI[1] + cs * uJ[0] + sn * uJ[1];
+    ub[1] = -sl * uI[0] + cl * uI[1] + uI[2] + sl * uJ[0] - cl * uJ[1];
+    ub[2] = ub[1] + uJ[2] - uI[2];
+  } else {
+    double du[3], tI[3], tJ[3], Du[3];
+#pragma unroll
+    for (int i = 0; i < 3; i++) du[i] = uJ[i] - uI[i];
+#pragma unroll
+    for (int j = 0; j < 3; j++) {
+      Du[j] = R[0 * 3 + j] * du[0] + R[1 * 3 + j] * du[1] + R[2 * 3 + j] * du[2];
+      tI[j] = R[0 * 3 + j] * uI[3] + R[1 * 3 + j] * uI[4] + R[2 * 3 + j] * uI[5];
+      tJ[j] = R[0 * 3 + j] * uJ[3] + R[1 * 3 + j] * uJ[4] + R[2 * 3 + j] * uJ[5];
+    }
+    ub[0] = Du[0];
+    ub[1] = tI[2] - Du[1] / L;
+    ub[2] = tJ[2] - Du[1] / L;
+    ub[3] = tI[1] + Du[2] / L;
+    ub[4] = tJ[1] + Du[2] / L;
+    ub[5] = tJ[0] - tI[0];
+  }
+}
+
+// Fiber section state determination: FiberSection2d / FiberSection3d
+// setTrialSectionDeformation (material/section/FiberSection2d.cpp:225-262,
+// FiberSection3d.cpp:423-478; order P MZ [MY T]).  Fibers across the warp's
+// lanes, trial records written, tangent ks[ORD*ORD] and resultant Ssr[ORD]
+// reduced with a fixed butterfly so every lane holds the same values.
+template <int ORD>
+__device__ __forceinline__ void fbc_section(const FrameView &v, int f0, int nf, double ybar,
+                                            double zbar, double GJ, long rec0, int lane,
+                                            const double *vsec, double *ks, double *Ssr) {
+  double k0 = 0, k1 = 0, k2 = 0, k5 = 0, k6 = 0, k10 = 0, s0 = 0, s1 = 0, s2 = 0;
+  for (int fi = lane; fi < nf; fi += 32) {
+    const int kf = f0 + fi;
+    const double y = v.fy[kf] - ybar, A = v.fA[kf];
+    const int u = v.fmat[kf];
+    double strain = vsec[0] - y * vsec[1];
+    double z = 0.0;
+    if (ORD == 4) {
+      z = v.fz[kf] - zbar;
+      strain += z * vsec[2];
+    }
+    const double *hc = v.fh_c + rec0 + 12L * fi;
+    double *ht = v.fh_t + rec0 + 12L * fi;
+    double hcl[12], htl[12];
+#pragma unroll
+    for (int c = 0; c < 11; c++) { hcl[c] = hc[c]; htl[c] = ht[c]; }
+    double stress, tangent;
+    uni_trial(v.utype[u], v.uparam + (long)u * XG_UNI_NPARAM, hcl, strain, htl, stress, tangent);
+#pragma unroll
+    for (int c = 0; c < 11; c++) ht[c] = htl[c];
+    if (ORD == 2) {
+      const double ks0 = tangent * A, ks1 = ks0 * -y;
+      k0 += ks0; k1 += ks1; k5 += ks1 * -y;
+      const double fs0v = stress * A;
+      s0 += fs0v; s1 += fs0v * -y;
+    } else {
+      const double EA = tangent * A;
+      k0 += EA; k1 += -y * EA; k2 += z * EA;
+      k5 += y * y * EA; k10 += z * z * EA; k6 += -y * z * EA;
+      const double fsv = stress * A;
+      s0 += fsv; s1 += -y * fsv; s2 += z * fsv;
+    }
+  }
+  k0 = warp_sum(k0); k1 = warp_sum(k1); k5 = warp_sum(k5);
+  s0 = warp_sum(s0); s1 = warp_sum(s1);
+  if (ORD == 2) {
+    ks[0] = k0; ks[1] = k1; ks[2] = k1; ks[3] = k5;
+    Ssr[0] = s0; Ssr[1] = s1;
+  } else {
+    k2 = warp_sum(k2); k6 = warp_sum(k6); k10 = warp_sum(k10); s2 = warp_sum(s2);
+    ks[0] = k0; ks[1] = k1; ks[2] = k2; ks[3] = 0.0;
+    ks[4] = k1; ks[5] = k5; ks[6] = k6; ks[7] = 0.0;
+    ks[8] = k2; ks[9] = k6; ks[10] = k10; ks[11] = 0.0;
+    ks[12] = 0.0; ks[13] = 0.0; ks[14] = 0.0; ks[15] = GJ;
+    Ssr[0] = s0; Ssr[1] = s1; Ssr[2] = s2; Ssr[3] = GJ * vsec[3];
+  }
+}
+
+constexpr int kFbcWarps = 4;
+constexpr int kMaxIp = 10;
+constexpr int kFbcMaxRounds = 4096;
+
+template <int NB, int ORD>
+struct FbcSmem {
+  double Se[6], kv[36], SeT[6], kvT[36], f[36], vr[6];
+  double vs[kMaxIp][4], fs[kMaxIp][16], Ssr[kMaxIp][4];
+  double vsS[kMaxIp][4], fsS[kMaxIp][16], SsrS[kMaxIp][4];
+};
+
+// ForceBeamColumn2d::update (element/Frame/Other/Force/ForceBeamColumn2d.cpp:
+// 559-935) and ForceBeamColumn3d::update (ForceBeamColumn3d.cpp:588-1066).
+template <int NB, int ORD>
+__global__ void __launch_bounds__(32 * kFbcWarps) k_fbc_update(FrameView v) {
+  __shared__ FbcSmem<NB, ORD> sm_all[kFbcWarps];
+  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int e = blockIdx.x * kFbcWarps + w;
+  if (e >= v.ne) return;
+  FbcSmem<NB, ORD> &S = sm_all[w];
+  const int nip = v.nip;
+  double *st = v.st + (long)e * st_stride(nip);
+  const int sec = v.sec[e];
+  const int f0 = v.sec_fstart[sec], nf = v.sec_fstart[sec + 1] - f0;
+  const double ybar = v.ybar[sec], zbar = ORD == 4 ? v.zbar[sec] : 0.0;
+  const double GJ = ORD == 4 ? v.GJ[sec] : 0.0;
+  const double *fs0 = v.fs0 + 16 * (long)sec;
+  const double L = v.L[e];
+  const long fbase = v.foff[e];
+
+  double ub[6], dv[6], vin[6], dvTrial[6], dvToDo[6];
+  frame_basic<NB>(v, e, ub);
+  double *vlast = st + 6 + 36 + nip * 24;
+  const int init = (int)st[6 + 36 + nip * 24 + 6];
+  double nrm = 0.0;
+#pragma unroll
+  for (int i = 0; i < NB; i++) { dv[i] = ub[i] - vlast[i]; nrm += dv[i] * dv[i]; }
+  if (init != 0 && sqrt(nrm) <= kDblEps) return;
+#pragma unroll
+  for (int i = 0; i < NB; i++) { vin[i] = ub[i] - dv[i]; dvTrial[i] = dvToDo[i] = dv[i]; }
+  // load the trial element state
+  for (int i = lane; i < NB; i += 32) S.Se[i] = st[i];
+  for (int i = lane; i < NB * NB; i += 32) S.kv[i] = st[6 + i];
+  for (int k = lane; k < nip * ORD; k += 32) {
+    const int ip = k / ORD, r = k % ORD;
+    S.vs[ip][r] = st[42 + ip * 4 + r];
+    S.Ssr[ip][r] = st[42 + nip * 20 + ip * 4 + r];
+  }
+  for (int k = lane; k < nip * ORD * ORD; k += 32) {
+    const int ip = k / (ORD * ORD), r = k % (ORD * ORD);
+    S.fs[ip][r] = st[42 + nip * 4 + ip * 16 + r];
+  }
+  __syncwarp();
+
+  const int maxSub = NB == 3 ? 4 : 10;
+  int numSub = 1;
+  bool converged = false;
+  // The reference loop has no bound of its own (partial convergence resets
+  // the subdivision count); a kernel must end, so an element that needs more
+  // than kFbcMaxRounds rounds reports a failed state determination.
+  int rounds = 0;
+  while (!converged && numSub <= maxSub && ++rounds <= kFbcMaxRounds) {
+    bool partial = false;
+    for (int l = 0; l < 3 && !partial && !converged; l++) {
+      // SeTrial = Se + kv dvTrial; section state copies
+#pragma unroll
+      for (int i = 0; i < NB; i++) {
+        double t = S.Se[i];
+        double acc = 0.0;
+#pragma unroll
+        for (int k = 0; k < NB; k++) acc += S.kv[i * NB + k] * dvTrial[k];
+        S.SeT[i] = t + acc;
+      }
+#pragma unroll
+      for (int i = 0; i < NB * NB; i++) S.kvT[i] = S.kv[i];
+      for (int ip = 0; ip < nip; ip++) {
+#pragma unroll
+        for (int r = 0; r < ORD; r++) { S.vsS[ip][r] = S.vs[ip][r]; S.SsrS[ip][r] = S.Ssr[ip][r]; }
+#pragma unroll
+        for (int r = 0; r < ORD * ORD; r++) S.fsS[ip][r] = S.fs[ip][r];
+      }
+      __syncwarp();
+      const int numIters = (l == 1) ? 10 * v.max_iters : v.max_iters;
+      for (int j = 0; j < numIters; j++) {
+        double f[NB * NB], vr[NB];
+#pragma unroll
+        for (int i = 0; i < NB * NB; i++) f[i] = 0.0;
+#pragma unroll
+        for (int i = 0; i < NB; i++) vr[i] = 0.0;
+        for (int ip = 0; ip < nip; ip++) {
+          const double xL = v.xi[ip], xL1 = xL - 1.0, wtL = v.wt[ip] * L;
+          // Ss = b SeT (codes P MZ [MY T])
+          double Ss[ORD], dSs[ORD], dvs[ORD];
+          Ss[0] = S.SeT[0];
+          Ss[1] = xL1 * S.SeT[1] + xL * S.SeT[2];
+          if (ORD == 4) {
+            Ss[2] = xL1 * S.SeT[3] + xL * S.SeT[4];
+            Ss[3] = S.SeT[5];
+          }
+#pragma unroll
+          for (int r = 0; r < ORD; r++) dSs[r] = Ss[r] - S.SsrS[ip][r];
+          const bool use_fs = (l == 0) || (l == 2 && j > 0);
+#pragma unroll
+          for (int r = 0; r < ORD; r++) {
+            double t = 0.0;
+#pragma unroll
+            for (int k = 0; k < ORD; k++) t += (use_fs ? S.fsS[ip][r * ORD + k] : fs0[r * ORD + k]) * dSs[k];
+            dvs[r] = t;
+          }
+          double vsec[ORD];
+#pragma unroll
+          for (int r = 0; r < ORD; r++) vsec[r] = S.vsS[ip][r] + (init != 0 ? dvs[r] : 0.0);
+          double ks[ORD * ORD], Ssr[ORD];
+          fbc_section<ORD>(v, f0, nf, ybar, zbar, GJ, (fbase + (long)ip * nf) * 12, lane, vsec,
+                           ks, Ssr);
+          double fsec[ORD * ORD];
+          inv_gj<ORD>(ks, fsec);
+#pragma unroll
+          for (int r = 0; r < ORD; r++) {
+            S.vsS[ip][r] = vsec[r];
+            S.SsrS[ip][r] = Ssr[r];
+            dSs[r] = Ss[r] - Ssr[r];
+          }
+#pragma unroll
+          for (int r = 0; r < ORD * ORD; r++) S.fsS[ip][r] = fsec[r];
+#pragma unroll
+          for (int r = 0; r < ORD; r++) {
+            double t = 0.0;
+#pragma unroll
+            for (int k = 0; k < ORD; k++) t += fsec[r * ORD + k] * dSs[k];
+            dvs[r] = t + vsec[r];
+          }
+          // f += b' fs b wL ; vr += b' (vs + dvs) wL, b from the codes
+          double bm[ORD][NB];
+#pragma unroll
+          for (int r = 0; r < ORD; r++)
+#pragma unroll
+            for (int c = 0; c < NB; c++) bm[r][c] = 0.0;
+          bm[0][0] = 1.0;
+          bm[1][1] = xL1; bm[1][2] = xL;
+          if (ORD == 4) { bm[2][3] = xL1; bm[2][4] = xL; bm[3][5] = 1.0; }
+#pragma unroll
+          for (int a = 0; a < NB; a++) {
+#pragma unroll
+            for (int c = 0; c < NB; c++) {
+              double t = 0.0;
+#pragma unroll
+              for (int r = 0; r < ORD; r++) {
+                if (bm[r][a] == 0.0) continue;
+                double u = 0.0;
+#pragma unroll
+                for (int k = 0; k < ORD; k++) u += fsec[r * ORD + k] * bm[k][c];
+                t += bm[r][a] * u;
+              }
+              f[a * NB + c] += t * wtL;
+            }
+            double t = 0.0;
+#pragma unroll
+            for (int r = 0; r < ORD; r++) t += bm[r][a] * dvs[r];
+            vr[a] += t * wtL;
+          }
+        }
+        double kvT[NB * NB];
+        inv_gj<NB>(f, kvT);
+        double dvv[NB], dW = 0.0;
+#pragma unroll
+        for (int i = 0; i < NB; i++) dvv[i] = vin[i] + dvTrial[i] - vr[i];
+#pragma unroll
+        for (int i = 0; i < NB; i++) {
+          double t = 0.0;
+#pragma unroll
+          for (int k = 0; k < NB; k++) t += kvT[i * NB + k] * dvv[k];
+          S.SeT[i] += t;
+          dW += dvv[i] * t;
+        }
+#pragma unroll
+        for (int i = 0; i < NB * NB; i++) S.kvT[i] = kvT[i];
+        __syncwarp();
+        if (fabs(dW) < v.tol) {
+          double n2 = 0.0;
+#pragma unroll
+          for (int i = 0; i < NB; i++) {
+            dvToDo[i] -= dvTrial[i];
+            vin[i] += dvTrial[i];
+            n2 += dvToDo[i] * dvToDo[i];
+          }
+          if (sqrt(n2) <= kDblEps) converged = true;
+          else {
+#pragma unroll
+            for (int i = 0; i < NB; i++) dvTrial[i] = dvToDo[i];
+            numSub = 1;
+            partial = true;
+          }
+#pragma unroll
+          for (int i = 0; i < NB * NB; i++) S.kv[i] = S.kvT[i];
+#pragma unroll
+          for (int i = 0; i < NB; i++) S.Se[i] = S.SeT[i];
+          for (int ip = 0; ip < nip; ip++) {
+#pragma unroll
+            for (int r = 0; r < ORD; r++) { S.vs[ip][r] = S.vsS[ip][r]; S.Ssr[ip][r] = S.SsrS[ip][r]; }
+#pragma unroll
+            for (int r = 0; r < ORD * ORD; r++) S.fs[ip][r] = S.fsS[ip][r];
+          }
+          __syncwarp();
+          break;
+        } else if (j == numIters - 1 && l == 2) {
+#pragma unroll
+          for (int i = 0; i < NB; i++) dvTrial[i] /= 10.0;
+          numSub++;
+        }
+      }
+    }
+  }
+  if (!converged) {
+    if (lane == 0) atomicAdd(v.nfail, 1);
+    return;
+  }
+  // store the trial element state
+  for (int i = lane; i < NB; i += 32) st[i] = S.Se[i];
+  for (int i = lane; i < NB * NB; i += 32) st[6 + i] = S.kv[i];
+  for (int k = lane; k < nip * ORD; k += 32) {
+    const int ip = k / ORD, r = k % ORD;
+    st[42 + ip * 4 + r] = S.vs[ip][r];
+    st[42 + nip * 20 + ip * 4 + r] = S.Ssr[ip][r];
+  }
+  for (int k = lane; k < nip * ORD * ORD; k += 32) {
+    const int ip = k / (ORD * ORD), r = k % (ORD * ORD);
+    st[42 + nip * 4 + ip * 16 + r] = S.fs[ip][r];
+  }
+  for (int i = lane; i < NB; i += 32) vlast[i] = ub[i];
+  if (lane == 0) st[6 + 36 + nip * 24 + 6] = 1.0;
+}
+
+// Global tangent and resisting force of each element: K = T' kv T, P = T' Se
+// (LinearCrdTransf2d::getGlobalStiffMatrix / getGlobalResistingForce,
+// coordTransformation/LinearCrdTransf2d.cpp:473-735; BasicFrameTransf3d,
+// Frame/BasicFrameTransf.cpp:150-290).  The reference's 3D P-Delta
+// transformation (Frame/PDeltaFrameTransf3d.tpp:95-140) adds its geometric
+// terms before LinearFrameTransf<2,6>::pushResponse maps the transverse
+// translations onto the chord rotation, which cancels them; its tangent and
+// force equal these.
+template <int NB>
+__global__ void k_fbc_assemble(FrameView v) {
+  const int e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= v.ne) return;
+  constexpr int NU = NB == 3 ? 6 : 12;
+  const double *st = v.st + (long)e * st_stride(v.nip);
+  const double L = v.L[e];
+  const double *R = v.R + 9 * (long)e;
+  double T[NB][NU];
+#pragma unroll
+  for (int i = 0; i < NB; i++)
+#pragma unroll
+    for (int j = 0; j < NU; j++) T[i][j] = 0.0;
+  if (NB == 3) {
+    const double cs = R[0], sn = R[1], sl = sn / L, cl = cs / L;
+    T[0][0] = -cs; T[0][1] = -sn; T[0][3] = cs; T[0][4] = sn;
+    T[1][0] = -sl; T[1][1] = cl; T[1][2] = 1.0; T[1][3] = sl; T[1][4] = -cl;
+    T[2][0] = -sl; T[2][1] = cl; T[2][3] = sl; T[2][4] = -cl; T[2][5] = 1.0;
+  } else {
+#pragma unroll
+    for (int j = 0; j < 3; j++) {
+      const double e1 = R[3 * j + 0], e2 = R[3 * j + 1], e3 = R[3 * j + 2];
+      T[0][0 + j] = -e1; T[0][6 + j] = e1;
+      T[1][3 + j] = e3; T[1][0 + j] = e2 / L; T[1][6 + j] = -e2 / L;
+      T[2][9 + j] = e3; T[2][0 + j] = e2 / L; T[2][6 + j] = -e2 / L;
+      T[3][3 + j] = e2; T[3][0 + j] = -e3 / L; T[3][6 + j] = e3 / L;
+      T[4][9 + j] = e2; T[4][0 + j] = -e3 / L; T[4][6 + j] = e3 / L;
+      T[5][3 + j] = -e1; T[5][9 + j] = e1;
+    }
+  }
+  const double *Se = st, *kv = st + 6;
+  double kT[NB][NU];
+#pragma unroll
+  for (int i = 0; i < NB; i++)
+#pragma unroll
+    for (int j = 0; j < NU; j++) {
+      double s = 0.0;
+#pragma unroll
+      for (int k = 0; k < NB; k++) s += kv[i * NB + k] * T[k][j];
+      kT[i][j] = s;
+    }
+  double *Ke = v.Ke + (long)e * NU * NU;
+  double *Re = v.Re + (long)e * NU;
+#pragma unroll
+  for (int i = 0; i < NU; i++) {
+#pragma unroll
+    for (int j = 0; j < NU; j++) {
+      double s = 0.0;
+#pragma unroll
+      for (int k = 0; k < NB; k++) s += T[k][i] * kT[k][j];
+      Ke[i * NU + j] = s;
+    }
+    double p = 0.0;
+#pragma unroll
+    for (int k = 0; k < NB; k++) p += T[k][i] * Se[k];
+    Re[i] = p;
+  }
+}
+
+// ForceBeamColumn*::commitState (ForceBeamColumn2d.cpp:277-306): committed
+// element state and fiber records take the trial ones.
+__global__ void k_fbc_commit(FrameView v, double *st_c, double *fh_c_mut, long nrec) {
+  const long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  const long nst = (long)v.ne * st_stride(v.nip);
+  if (i < nst) st_c[i] = v.st[i];
+  if (i < nrec) fh_c_mut[i] = v.fh_t[i];
+}
+
+// revertToLastCommit: trial state and fiber records back to the committed
+// ones (ForceBeamColumn2d.cpp:310-336)
+__global__ void k_fbc_revert(FrameView v, const double *st_c, long nrec) {
+  const long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  const long nst = (long)v.ne * st_stride(v.nip);
+  if (i < nst) v.st[i] = st_c[i];
+  if (i < nrec) v.fh_t[i] = v.fh_c[i];
+}
+
+// The rest of revertToLastCommit (ForceBeamColumn2d.cpp:315-338): each
+// section set to its committed deformation gives Ssr and fs again, and
+// initialFlag returns to 0.  Warp per element, after k_fbc_revert.
+template <int ORD>
+__global__ void __launch_bounds__(32 * kFbcWarps) k_fbc_revert_sections(FrameView v) {
+  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int e = blockIdx.x * kFbcWarps + w;
+  if (e >= v.ne) return;
+  const int nip = v.nip;
+  double *st = v.st + (long)e * st_stride(nip);
+  const int sec = v.sec[e];
+  const int f0 = v.sec_fstart[sec], nf = v.sec_fstart[sec + 1] - f0;
+  const double ybar = v.ybar[sec], zbar = ORD == 4 ? v.zbar[sec] : 0.0;
+  const double GJ = ORD == 4 ? v.GJ[sec] : 0.0;
+  for (int ip = 0; ip < nip; ip++) {
+    double vsec[ORD], ks[ORD * ORD], Ssr[ORD], fsec[ORD * ORD];
+#pragma unroll
+    for (int r = 0; r < ORD; r++) vsec[r] = st[42 + ip * 4 + r];
+    fbc_section<ORD>(v, f0, nf, ybar, zbar, GJ, (v.foff[e] + (long)ip * nf) * 12, lane, vsec, ks,
+                     Ssr);
+    inv_gj<ORD>(ks, fsec);
+    __syncwarp();
+    if (lane == 0) {
+#pragma unroll
+      for (int r = 0; r < ORD; r++) st[42 + nip * 20 + ip * 4 + r] = Ssr[r];
+#pragma unroll
+      for (int r = 0; r < ORD * ORD; r++) st[42 + nip * 4 + ip * 16 + r] = fsec[r];
+    }
+  }
+  if (lane == 0) st[6 + 36 + nip * 24 + 6] = 0.0;
+}
+
+}  // namespace
+
+int frame_state_stride(int nip) { return 6 + 36 + nip * 24 + 6 + 1; }
+
+int launch_fbc_update(const FrameView &v, cudaStream_t s) {
+  if (v.ne == 0) return 0;
+  if (v.nip > kMaxIp) return XG_EINVAL;
+  const int grid = (v.ne + kFbcWarps - 1) / kFbcWarps;
+  if (v.nb == 3) k_fbc_update<3, 2><<<grid, 32 * kFbcWarps, 0, s>>>(v);
+  else k_fbc_update<6, 4><<<grid, 32 * kFbcWarps, 0, s>>>(v);
+  return cudaGetLastError() == cudaSuccess ? 0 : XG_ECUDA;
+}
+
+int launch_fbc_assemble(const FrameView &v, cudaStream_t s) {
+  if (v.ne == 0) return 0;
+  const int grid = (v.ne + 127) / 128;
+  if (v.nb == 3) k_fbc_assemble<3><<<grid, 128, 0, s>>>(v);
+  else k_fbc_assemble<6><<<grid, 128, 0, s>>>(v);
+  return cudaGetLastError() == cudaSuccess ? 0 : XG_ECUDA;
+}
+
+int launch_fbc_commit(const FrameView &v, double *st_c, double *fh_c, long nrec, cudaStream_t s) {
+  const long nst = (long)v.ne * frame_state_stride(v.nip);
+  const long n = nst > nrec ? nst : nrec;
+  if (n == 0) return 0;
+  k_fbc_commit<<<(int)((n + 255) / 256), 256, 0, s>>>(v, st_c, fh_c, nrec);
+  return cudaGetLastError() == cudaSuccess ? 0 : XG_ECUDA;
+}
+
+int launch_fbc_revert(const FrameView &v, const double *st_c, long nrec, cudaStream_t s) {
+  const long nst = (long)v.ne * frame_state_stride(v.nip);
+  const long n = nst > nrec ? nst : nrec;
+  if (n == 0) return 0;
+  k_fbc_revert<<<(int)((n + 255) / 256), 256, 0, s>>>(v, st_c, nrec);
+  if (v.ne > 0) {
+    const int grid = (v.ne + kFbcWarps - 1) / kFbcWarps;
+    if (v.nb == 3) k_fbc_revert_sections<2><<<grid, 32 * kFbcWarps, 0, s>>>(v);
+    else k_fbc_revert_sections<4><<<grid, 32 * kFbcWarps, 0, s>>>(v);
+  }
+  return cudaGetLastError() == cudaSuccess ? 0 : XG_ECUDA;
+}
+
+}  // namespace xg

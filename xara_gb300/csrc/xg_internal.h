@@ -92,3 +92,35 @@ namespace xg {
 // Sets the text returned by xg_last_error() (xg_model.cpp).
 void record_error(const char *msg);
 }  // namespace xg
+
+namespace xg {
+// Force-based frame element set (ForceBeamColumn2d/3d with fiber sections).
+struct FrameView {
+  int ne, nb, nip, ndf;       // nb: basic dofs 3 (2D) or 6 (3D)
+  const double *U;            // [nn*ndf] trial displacements
+  const int *conn;            // [ne*2] node indices
+  const double *L, *R;        // [ne] length; [ne*9] local axes (2D: cos, sin)
+  const int *sec;             // [ne] section row
+  const int *sec_fstart;      // [nsec+1]
+  const double *fy, *fz, *fA; // fiber geometry per section
+  const int *fmat;            // fiber uniaxial row
+  const double *ybar, *zbar, *GJ;   // [nsec]
+  const double *fs0;          // [nsec*16] initial section flexibility
+  const int *utype;           // [nuni]
+  const double *uparam;       // [nuni*XG_UNI_NPARAM]
+  const long *foff;           // [ne+1] first fiber record of each element
+  const double *fh_c;         // committed fiber records [nrec*12]
+  double *fh_t;               // trial fiber records
+  double *st;                 // trial element state [ne*stride]
+  int max_iters;
+  double tol;
+  double xi[10], wt[10];      // Lobatto locations and weights
+  int *nfail;                 // elements whose compatibility iteration failed
+  double *Ke, *Re;            // element tangent / force scratch
+};
+int frame_state_stride(int nip);
+int launch_fbc_update(const FrameView &v, cudaStream_t s);
+int launch_fbc_assemble(const FrameView &v, cudaStream_t s);
+int launch_fbc_commit(const FrameView &v, double *st_c, double *fh_c, long nrec, cudaStream_t s);
+int launch_fbc_revert(const FrameView &v, const double *st_c, long nrec, cudaStream_t s);
+}  // namespace xg

@@ -186,8 +186,8 @@ struct xg_model {
   bool prof_on = false;
   enum { P_UPDATE, P_ASSEMBLE, P_GATHER_K, P_GATHER_R, P_PCG_FACTOR, P_PCG };
   void prof_init() {
-    const char *names[6] = {etype == XG_ELE_QUAD ? "quad_update" : "brick_update",
-                            etype == XG_ELE_QUAD ? "quad_assemble" : "brick_assemble",
+    const char *names[6] = {frames() ? "fbc_update" : etype == XG_ELE_QUAD ? "quad_update" : "brick_update",
+                            frames() ? "fbc_assemble" : etype == XG_ELE_QUAD ? "quad_assemble" : "brick_assemble",
                             "gather_tangent", "gather_resid", "pcg_factor_blocks", "pcg"};
     for (int k = 0; k < 6; k++) {
       ProfSlot p{names[k], 0.0, 0, nullptr, nullptr, false};
@@ -227,11 +227,43 @@ struct xg_model {
     v.Ke = d_Ke.p; v.Re = d_Re.p;
     return v;
   }
+  bool frames() const { return etype == XG_ELE_FBC2D || etype == XG_ELE_FBC3D; }
   int nhist() const { return etype == XG_ELE_QUAD ? 4 : 6; }
   int nsig() const { return etype == XG_ELE_QUAD ? 3 : 6; }
   int ntan() const { return etype == XG_ELE_QUAD ? 6 : 9; }
   long npts() const { return (long)ne * nip; }
-  int ke_size() const { return etype == XG_ELE_QUAD ? 64 : 324; }
+  int ke_size() const {
+    if (frames()) return ned * ned;
+    return etype == XG_ELE_QUAD ? 64 : 324;
+  }
+  // force-based frames: section and material tables, element state
+  int fb_nb = 0, fb_nip = 0, fb_max_iters = 10;
+  double fb_tol = 1e-12;
+  std::vector<int> sec_fstart, fmat, utype;
+  std::vector<double> fy, fz, fA, GJ, uparam;
+  long fb_nrec = 0;
+  DBuf<int> d_fconn, d_fsec, d_sec_fstart, d_fmat, d_utype;
+  DBuf<long> d_foff;
+  DBuf<double> d_fL, d_fR, d_fy, d_fz, d_fA, d_ybar, d_zbar, d_GJ, d_fs0, d_uparam;
+  DBuf<double> d_fh_c, d_fh_t, d_st, d_st_c;
+  std::vector<double> fh_init;
+  std::vector<double> crd_vecxz;
+  double lob_xi[10] = {0}, lob_wt[10] = {0};
+  FrameView fview() {
+    FrameView v{};
+    v.ne = ne; v.nb = fb_nb; v.nip = fb_nip; v.ndf = ndf;
+    v.U = d_U.p; v.conn = d_fconn.p; v.L = d_fL.p; v.R = d_fR.p; v.sec = d_fsec.p;
+    v.sec_fstart = d_sec_fstart.p; v.fy = d_fy.p; v.fz = d_fz.p; v.fA = d_fA.p;
+    v.fmat = d_fmat.p; v.ybar = d_ybar.p; v.zbar = d_zbar.p; v.GJ = d_GJ.p; v.fs0 = d_fs0.p;
+    v.utype = d_utype.p; v.uparam = d_uparam.p; v.foff = d_foff.p; v.fh_c = d_fh_c.p;
+    v.fh_t = d_fh_t.p; v.st = d_st.p; v.max_iters = fb_max_iters; v.tol = fb_tol;
+    for (int i = 0; i < 10; i++) { v.xi[i] = lob_xi[i]; v.wt[i] = lob_wt[i]; }
+    v.nfail = d_nfail.p; v.Ke = d_Ke.p; v.Re = d_Re.p;
+    return v;
+  }
+  int upload_frames();
+  int commit_state();
+  int revert_state();
 
   ~xg_model() {
     for (auto &p : prof) {
@@ -453,7 +485,7 @@ int xg_model::build_maps(HostGather &gk_h, HostGather &gr_h) {
         if (pos == re || *pos != c) return fail(XG_EINVAL, "pattern lookup failed");
         slot_of.push_back((int)(pos - colidx.data()));
         int64_t src;
-        if (etype == XG_ELE_QUAD) {
+        if (etype != XG_ELE_BRICK) {
           src = (int64_t)e * ks + i * ned + j;
         } else {
           const int a = i / 3, ii = i % 3, b = j / 3, kk = j % 3;
@@ -556,11 +588,199 @@ int xg_model::upload(const HostGather &gk_h, const HostGather &gr_h) {
       }
     }
   if (!F.empty()) RET(d_Fref.upload(F.data(), F.size(), s));
-  // zero-strain material state
-  RET(launch_j2_zero_state(view(), s));
-  CK(cudaMemcpyAsync(d_sig_c.p, d_sig.p, np * nsig() * sizeof(double), cudaMemcpyDeviceToDevice, s));
-  CK(cudaMemcpyAsync(d_tan_c.p, d_tan.p, np * ntan() * sizeof(double), cudaMemcpyDeviceToDevice, s));
+  if (frames()) {
+    RET(upload_frames());
+  } else {
+    // zero-strain material state
+    RET(launch_j2_zero_state(view(), s));
+    CK(cudaMemcpyAsync(d_sig_c.p, d_sig.p, np * nsig() * sizeof(double), cudaMemcpyDeviceToDevice, s));
+    CK(cudaMemcpyAsync(d_tan_c.p, d_tan.p, np * ntan() * sizeof(double), cudaMemcpyDeviceToDevice, s));
+  }
   CK(cudaStreamSynchronize(s));
+  return 0;
+}
+
+namespace {
+// LobattoBeamIntegration::getSectionLocations / getSectionWeights
+// (quadrature/Frame/LobattoBeamIntegration.cpp:110-320): the reference's
+// truncated constants, mapped to [0, 1], weights halved.
+void lobatto_points(int n, double *xi, double *wt) {
+  static const double x3[3] = {-1.0, 0.0, 1.0};
+  static const double w3[3] = {0.333333333333333, 1.333333333333333, 0.333333333333333};
+  static const double x4[4] = {-1.0, -0.44721360, 0.44721360, 1.0};
+  static const double w4[4] = {0.166666666666667, 0.833333333333333, 0.833333333333333,
+                               0.166666666666667};
+  static const double x5[5] = {-1.0, -0.65465367, 0.0, 0.65465367, 1.0};
+  static const double w5[5] = {0.1, 0.5444444444, 0.7111111111, 0.5444444444, 0.1};
+  const double *x = n == 3 ? x3 : n == 4 ? x4 : x5;
+  const double *w = n == 3 ? w3 : n == 4 ? w4 : w5;
+  for (int i = 0; i < n; i++) {
+    xi[i] = 0.5 * (x[i] + 1.0);
+    wt[i] = 0.5 * w[i];
+  }
+}
+
+// Initial tangent of a uniaxial row (Steel02 E0; Concrete02 2 fc / epsc0
+// after the constructor's sign normalisation, Concrete02.cpp:97-111).
+double uniaxial_initial_tangent(int type, const double *q) {
+  if (type == XG_UNI_STEEL02) return q[1];
+  if (type == XG_UNI_CONCRETE02) {
+    const double fc = q[0] > 0 ? -q[0] : q[0], e0 = q[1] > 0 ? -q[1] : q[1];
+    return 2.0 * fc / e0;
+  }
+  return q[0];
+}
+
+// Committed record of a fresh material (Steel02::revertToStart, Steel02.cpp:
+// 70-95; Concrete02 constructor, Concrete02.cpp:97-111).
+void uniaxial_initial_record(int type, const double *q, double *h) {
+  for (int c = 0; c < 12; c++) h[c] = 0.0;
+  if (type == XG_UNI_STEEL02) {
+    h[1] = q[0] / q[1];
+    h[0] = -h[1];
+    h[8] = q[1];
+    if (q[10] != 0.0) { h[10] = q[10] / q[1]; h[9] = q[10]; }
+  } else {
+    h[8] = uniaxial_initial_tangent(type, q);
+  }
+}
+
+// small dense inverse (Gauss-Jordan, partial pivoting)
+void host_inverse(int n, const double *A, double *Ai) {
+  double M[6][12];
+  for (int i = 0; i < n; i++)
+    for (int j = 0; j < 2 * n; j++) M[i][j] = j < n ? A[i * n + j] : (j - n == i ? 1.0 : 0.0);
+  for (int c = 0; c < n; c++) {
+    int piv = c;
+    for (int i = c + 1; i < n; i++)
+      if (std::fabs(M[i][c]) > std::fabs(M[piv][c])) piv = i;
+    if (piv != c)
+      for (int j = 0; j < 2 * n; j++) std::swap(M[c][j], M[piv][j]);
+    const double inv = 1.0 / M[c][c];
+    for (int j = 0; j < 2 * n; j++) M[c][j] *= inv;
+    for (int i = 0; i < n; i++) {
+      if (i == c) continue;
+      const double f = M[i][c];
+      for (int j = 0; j < 2 * n; j++) M[i][j] -= f * M[c][j];
+    }
+  }
+  for (int i = 0; i < n; i++)
+    for (int j = 0; j < n; j++) Ai[i * n + j] = M[i][n + j];
+}
+}  // namespace
+
+// Frame element set: geometry (LinearCrdTransf2d::computeElemtLengthAndOrient,
+// coordTransformation/LinearCrdTransf2d.cpp:175-220; FrameTransform::Orient,
+// coordTransformation/FrameTransform.h:105-129), section centroids
+// (FiberSection2d::addFiber, material/section/FiberSection2d.cpp:148-153),
+// initial section flexibilities, fresh fiber records, zero element state,
+// then the update Domain::addElement performs (domain/domain/Domain.cpp:390-392).
+int xg_model::upload_frames() {
+  cudaStream_t s = stream;
+  lobatto_points(fb_nip, lob_xi, lob_wt);
+  const int nsec = (int)sec_fstart.size() - 1;
+  std::vector<double> Lh(ne), Rh((size_t)ne * 9, 0.0);
+  for (int e = 0; e < ne; e++) {
+    const int a = conn[2 * (size_t)e], b = conn[2 * (size_t)e + 1];
+    double dx[3] = {0, 0, 0};
+    for (int k = 0; k < ndm; k++) dx[k] = crd[(size_t)b * ndm + k] - crd[(size_t)a * ndm + k];
+    const double L = std::sqrt(dx[0] * dx[0] + dx[1] * dx[1] + dx[2] * dx[2]);
+    if (L == 0.0) return fail(XG_EINVAL, "element %d has zero length", e);
+    Lh[e] = L;
+    double *R = &Rh[9 * (size_t)e];
+    if (ndm == 2) {
+      R[0] = dx[0] / L;
+      R[1] = dx[1] / L;
+    } else {
+      const double *vz = &crd_vecxz[3 * (size_t)e];
+      const double e1[3] = {dx[0] / L, dx[1] / L, dx[2] / L};
+      double e2[3] = {vz[1] * e1[2] - vz[2] * e1[1], vz[2] * e1[0] - vz[0] * e1[2],
+                      vz[0] * e1[1] - vz[1] * e1[0]};
+      const double yn = std::sqrt(e2[0] * e2[0] + e2[1] * e2[1] + e2[2] * e2[2]);
+      if (yn == 0.0) return fail(XG_EINVAL, "element %d: vecxz parallel to the axis", e);
+      for (int k = 0; k < 3; k++) e2[k] /= yn;
+      const double e3[3] = {e1[1] * e2[2] - e1[2] * e2[1], e1[2] * e2[0] - e1[0] * e2[2],
+                            e1[0] * e2[1] - e1[1] * e2[0]};
+      for (int k = 0; k < 3; k++) {
+        R[3 * k + 0] = e1[k];
+        R[3 * k + 1] = e2[k];
+        R[3 * k + 2] = e3[k];
+      }
+    }
+  }
+  const int order = fb_nb == 3 ? 2 : 4;
+  std::vector<double> ybar(nsec), zbar(nsec), fs0((size_t)nsec * 16, 0.0);
+  for (int sc = 0; sc < nsec; sc++) {
+    double A = 0, Qz = 0, Qy = 0;
+    double k[16] = {0};
+    for (int f = sec_fstart[sc]; f < sec_fstart[sc + 1]; f++) {
+      A += fA[f];
+      Qz += fy[f] * fA[f];
+      Qy += fz[f] * fA[f];
+    }
+    ybar[sc] = Qz / A;
+    zbar[sc] = Qy / A;
+    for (int f = sec_fstart[sc]; f < sec_fstart[sc + 1]; f++) {
+      const int u = fmat[f];
+      const double EA = uniaxial_initial_tangent(utype[u], &uparam[(size_t)u * XG_UNI_NPARAM]) * fA[f];
+      const double y = fy[f] - ybar[sc], z = fz[f] - zbar[sc];
+      if (order == 2) {
+        const double ks1 = EA * -y;
+        k[0] += EA; k[1] += ks1; k[3] += ks1 * -y;
+      } else {
+        k[0] += EA; k[1] += -y * EA; k[2] += z * EA;
+        k[5] += y * y * EA; k[10] += z * z * EA; k[6] += -y * z * EA;
+      }
+    }
+    if (order == 2) k[2] = k[1];
+    else { k[4] = k[1]; k[8] = k[2]; k[9] = k[6]; k[15] = GJ[sc]; }
+    host_inverse(order, k, &fs0[(size_t)sc * 16]);
+  }
+  std::vector<long> foff(ne + 1, 0);
+  for (int e = 0; e < ne; e++) {
+    const int sc = mat[e];
+    foff[e + 1] = foff[e] + (long)fb_nip * (sec_fstart[sc + 1] - sec_fstart[sc]);
+  }
+  fb_nrec = foff[ne];
+  fh_init.assign((size_t)fb_nrec * 12, 0.0);
+  for (int e = 0; e < ne; e++) {
+    const int sc = mat[e], nf = sec_fstart[sc + 1] - sec_fstart[sc];
+    for (int ip = 0; ip < fb_nip; ip++)
+      for (int f = 0; f < nf; f++) {
+        const int u = fmat[sec_fstart[sc] + f];
+        uniaxial_initial_record(utype[u], &uparam[(size_t)u * XG_UNI_NPARAM],
+                                &fh_init[((size_t)foff[e] + (size_t)ip * nf + f) * 12]);
+      }
+  }
+  RET(d_fconn.upload(conn.data(), conn.size(), s));
+  RET(d_fsec.upload(mat.data(), mat.size(), s));
+  RET(d_fL.upload(Lh.data(), Lh.size(), s));
+  RET(d_fR.upload(Rh.data(), Rh.size(), s));
+  RET(d_sec_fstart.upload(sec_fstart.data(), sec_fstart.size(), s));
+  RET(d_fy.upload(fy.data(), fy.size(), s));
+  RET(d_fz.upload(fz.data(), fz.size(), s));
+  RET(d_fA.upload(fA.data(), fA.size(), s));
+  RET(d_fmat.upload(fmat.data(), fmat.size(), s));
+  RET(d_ybar.upload(ybar.data(), ybar.size(), s));
+  RET(d_zbar.upload(zbar.data(), zbar.size(), s));
+  RET(d_GJ.upload(GJ.data(), GJ.size(), s));
+  RET(d_fs0.upload(fs0.data(), fs0.size(), s));
+  RET(d_utype.upload(utype.data(), utype.size(), s));
+  RET(d_uparam.upload(uparam.data(), uparam.size(), s));
+  RET(d_foff.upload(foff.data(), foff.size(), s));
+  RET(d_fh_c.upload(fh_init.data(), fh_init.size(), s));
+  RET(d_fh_t.upload(fh_init.data(), fh_init.size(), s));
+  const size_t nst = (size_t)ne * frame_state_stride(fb_nip);
+  RET(d_st.alloc(nst > 0 ? nst : 1));
+  RET(d_st_c.alloc(nst > 0 ? nst : 1));
+  CK(cudaMemsetAsync(d_st.p, 0, (nst > 0 ? nst : 1) * sizeof(double), s));
+  CK(cudaMemsetAsync(d_st_c.p, 0, (nst > 0 ? nst : 1) * sizeof(double), s));
+  // the update Domain::addElement performs, at zero displacement
+  RET(element_state(true));
+  int nf = 0;
+  CK(cudaMemcpyAsync(&nf, d_nfail.p, sizeof(int), cudaMemcpyDeviceToHost, s));
+  CK(cudaStreamSynchronize(s));
+  if (nf) return fail(XG_EELEMENT, "%d elements failed their initial state determination", nf);
   return 0;
 }
 
@@ -569,15 +789,28 @@ int xg_model::upload(const HostGather &gk_h, const HostGather &gr_h) {
 int xg_model::element_state(bool compute) {
   ContinuumView v = view();
   cudaStream_t s = stream;
-  if (compute) {
-    CK(cudaMemsetAsync(d_nfail.p, 0, sizeof(int), s));
-    prof_begin(P_UPDATE);
-    RET(etype == XG_ELE_QUAD ? launch_quad_update(v, s) : launch_brick_update(v, s));
-    prof_end(P_UPDATE, 1);
+  if (frames()) {
+    FrameView fv = fview();
+    if (compute) {
+      CK(cudaMemsetAsync(d_nfail.p, 0, sizeof(int), s));
+      prof_begin(P_UPDATE);
+      RET(launch_fbc_update(fv, s));
+      prof_end(P_UPDATE, 1);
+    }
+    prof_begin(P_ASSEMBLE);
+    RET(launch_fbc_assemble(fv, s));
+    prof_end(P_ASSEMBLE, 1);
+  } else {
+    if (compute) {
+      CK(cudaMemsetAsync(d_nfail.p, 0, sizeof(int), s));
+      prof_begin(P_UPDATE);
+      RET(etype == XG_ELE_QUAD ? launch_quad_update(v, s) : launch_brick_update(v, s));
+      prof_end(P_UPDATE, 1);
+    }
+    prof_begin(P_ASSEMBLE);
+    RET(etype == XG_ELE_QUAD ? launch_quad_assemble(v, s) : launch_brick_assemble(v, s));
+    prof_end(P_ASSEMBLE, 1);
   }
-  prof_begin(P_ASSEMBLE);
-  RET(etype == XG_ELE_QUAD ? launch_quad_assemble(v, s) : launch_brick_assemble(v, s));
-  prof_end(P_ASSEMBLE, 1);
   prof_begin(P_GATHER_K);
   RET(launch_gather(gk, d_Ke.p, d_partial.p, d_vals.p, s));
   prof_end(P_GATHER_K, 2);
@@ -709,15 +942,43 @@ int xg_model::step(xg_step_stats *st) {
     time = t_commit;
     return fail(XG_ENOCONV, "Newton did not converge in %d iterations", it);
   }
-  // commit (Domain::commit -> material commitState)
-  const long np = npts();
-  CK(cudaMemcpyAsync(d_epc.p, d_ept.p, np * nhist() * sizeof(double), cudaMemcpyDeviceToDevice, s));
-  CK(cudaMemcpyAsync(d_xic.p, d_xit.p, np * sizeof(double), cudaMemcpyDeviceToDevice, s));
-  CK(cudaMemcpyAsync(d_sig_c.p, d_sig.p, np * nsig() * sizeof(double), cudaMemcpyDeviceToDevice, s));
-  CK(cudaMemcpyAsync(d_tan_c.p, d_tan.p, np * ntan() * sizeof(double), cudaMemcpyDeviceToDevice, s));
-  CK(cudaMemcpyAsync(d_Uc.p, d_U.p, (size_t)nu * sizeof(double), cudaMemcpyDeviceToDevice, s));
+  // commit (Domain::commit -> element and material commitState)
+  RET(commit_state());
   time_c = time;
   return 0;
+}
+
+int xg_model::commit_state() {
+  cudaStream_t s = stream;
+  const size_t nu = (size_t)nn * ndf;
+  if (frames()) {
+    RET(launch_fbc_commit(fview(), d_st_c.p, d_fh_c.p, fb_nrec * 12, s));
+  } else {
+    const long np = npts();
+    CK(cudaMemcpyAsync(d_epc.p, d_ept.p, np * nhist() * sizeof(double), cudaMemcpyDeviceToDevice, s));
+    CK(cudaMemcpyAsync(d_xic.p, d_xit.p, np * sizeof(double), cudaMemcpyDeviceToDevice, s));
+    CK(cudaMemcpyAsync(d_sig_c.p, d_sig.p, np * nsig() * sizeof(double), cudaMemcpyDeviceToDevice, s));
+    CK(cudaMemcpyAsync(d_tan_c.p, d_tan.p, np * ntan() * sizeof(double), cudaMemcpyDeviceToDevice, s));
+  }
+  CK(cudaMemcpyAsync(d_Uc.p, d_U.p, nu * sizeof(double), cudaMemcpyDeviceToDevice, s));
+  return 0;
+}
+
+int xg_model::revert_state() {
+  cudaStream_t s = stream;
+  if (frames()) {
+    RET(launch_fbc_revert(fview(), d_st_c.p, fb_nrec * 12, s));
+  } else {
+    const long np = npts();
+    CK(cudaMemcpyAsync(d_ept.p, d_epc.p, np * nhist() * sizeof(double), cudaMemcpyDeviceToDevice, s));
+    CK(cudaMemcpyAsync(d_xit.p, d_xic.p, np * sizeof(double), cudaMemcpyDeviceToDevice, s));
+    CK(cudaMemcpyAsync(d_sig.p, d_sig_c.p, np * nsig() * sizeof(double), cudaMemcpyDeviceToDevice, s));
+    CK(cudaMemcpyAsync(d_tan.p, d_tan_c.p, np * ntan() * sizeof(double), cudaMemcpyDeviceToDevice, s));
+  }
+  CK(cudaMemcpyAsync(d_U.p, d_Uc.p, (size_t)nn * ndf * sizeof(double), cudaMemcpyDeviceToDevice, s));
+  // Domain::revertToLastCommit ends with Domain::update at the committed
+  // displacements (domain/domain/Domain.cpp:1925-1949)
+  return element_state(true);
 }
 
 // ---------------------------------------------------------------------------
@@ -770,15 +1031,29 @@ int xg_model_plan(const xg_model_desc *d, int *eqn, int *rowptr, int *colidx, in
 // Host part of model creation: validate and copy the description, number
 // the DOFs and build the pattern.  No device work.
 static int plan_model(const xg_model_desc *d, xg_model **out) {
-  if (d->elem_type != XG_ELE_QUAD && d->elem_type != XG_ELE_BRICK)
+  const bool fr = d->elem_type == XG_ELE_FBC2D || d->elem_type == XG_ELE_FBC3D;
+  if (d->elem_type != XG_ELE_QUAD && d->elem_type != XG_ELE_BRICK && !fr)
     return fail(XG_EINVAL, "element type %d not supported", d->elem_type);
+  if (d->elem_type == XG_ELE_FBC2D && (d->ndm != 2 || d->ndf != 3))
+    return fail(XG_EINVAL, "forceBeamColumn 2D needs ndm 2, ndf 3");
+  if (d->elem_type == XG_ELE_FBC3D && (d->ndm != 3 || d->ndf != 6))
+    return fail(XG_EINVAL, "forceBeamColumn 3D needs ndm 3, ndf 6");
+  if (fr && (d->fbc_num_ip < 3 || d->fbc_num_ip > 5))
+    return fail(XG_EINVAL, "forceBeamColumn needs 3..5 Lobatto points");
+  if (fr && d->elem_type == XG_ELE_FBC2D && d->geom_transf != 0)
+    return fail(XG_EINVAL, "2D P-Delta transformation not supported");
+  if (fr && (d->num_sec <= 0 || !d->sec_fiber_start || !d->fib_y || !d->fib_area ||
+             !d->fib_mat || d->num_uni <= 0 || !d->uni_type || !d->uni_param))
+    return fail(XG_EINVAL, "forceBeamColumn needs fiber sections and uniaxial materials");
+  if (d->elem_type == XG_ELE_FBC3D && (!d->fib_z || !d->sec_GJ || !d->elem_vecxz))
+    return fail(XG_EINVAL, "3D fiber sections need z, GJ and vecxz");
   if (d->elem_type == XG_ELE_QUAD && (d->ndm != 2 || d->ndf != 2))
     return fail(XG_EINVAL, "quad needs ndm 2, ndf 2");
   if (d->elem_type == XG_ELE_BRICK && (d->ndm != 3 || d->ndf != 3))
     return fail(XG_EINVAL, "stdBrick needs ndm 3, ndf 3");
   if (d->num_nodes <= 0 || d->num_elems < 0 || !d->node_tag || !d->node_crd)
     return fail(XG_EINVAL, "empty model");
-  if (d->num_elems > 0 && (!d->elem_tag || !d->elem_conn || !d->elem_mat || !d->j2_param))
+  if (d->num_elems > 0 && (!d->elem_tag || !d->elem_conn || !d->elem_mat || (!fr && !d->j2_param)))
     return fail(XG_EINVAL, "missing element arrays");
   if (d->handler != XG_HANDLER_PLAIN)
     return fail(XG_EINVAL, "only the Plain constraint handler is supported");
@@ -788,8 +1063,8 @@ static int plan_model(const xg_model_desc *d, xg_model **out) {
   auto *m = new xg_model();
   m->ndm = d->ndm; m->ndf = d->ndf; m->nn = d->num_nodes; m->ne = d->num_elems;
   m->etype = d->elem_type;
-  m->nen = d->elem_type == XG_ELE_QUAD ? 4 : 8;
-  m->nip = m->nen;
+  m->nen = fr ? 2 : (d->elem_type == XG_ELE_QUAD ? 4 : 8);
+  m->nip = fr ? 0 : m->nen;
   m->ned = m->nen * m->ndf;
   m->thickness = d->thickness;
   m->node_tag.assign(d->node_tag, d->node_tag + m->nn);
@@ -816,12 +1091,53 @@ static int plan_model(const xg_model_desc *d, xg_model **out) {
     m->conn[k] = (int)(it - m->node_tag.begin());
   }
   m->mat.assign(d->elem_mat, d->elem_mat + m->ne);
-  m->j2.assign(d->j2_param, d->j2_param + (size_t)d->num_j2 * XG_J2_NPARAM);
-  for (int e = 0; e < m->ne; e++)
-    if (m->mat[e] < 0 || m->mat[e] >= d->num_j2) {
-      delete m;
-      return fail(XG_EINVAL, "element %d: J2 row out of range", e);
-    }
+  if (!fr) {
+    m->j2.assign(d->j2_param, d->j2_param + (size_t)d->num_j2 * XG_J2_NPARAM);
+    for (int e = 0; e < m->ne; e++)
+      if (m->mat[e] < 0 || m->mat[e] >= d->num_j2) {
+        delete m;
+        return fail(XG_EINVAL, "element %d: J2 row out of range", e);
+      }
+  } else {
+    const int nsec = d->num_sec, nuni = d->num_uni;
+    m->fb_nb = d->elem_type == XG_ELE_FBC2D ? 3 : 6;
+    m->fb_nip = d->fbc_num_ip;
+    m->fb_max_iters = d->fbc_max_iters > 0 ? d->fbc_max_iters : 10;
+    m->fb_tol = d->fbc_tol > 0 ? d->fbc_tol : 1e-12;
+    m->sec_fstart.assign(d->sec_fiber_start, d->sec_fiber_start + nsec + 1);
+    const int nfib = m->sec_fstart[nsec];
+    for (int s2 = 0; s2 < nsec; s2++)
+      if (m->sec_fstart[s2 + 1] <= m->sec_fstart[s2]) {
+        delete m;
+        return fail(XG_EINVAL, "section %d has no fibers", s2);
+      }
+    m->fy.assign(d->fib_y, d->fib_y + nfib);
+    m->fA.assign(d->fib_area, d->fib_area + nfib);
+    m->fmat.assign(d->fib_mat, d->fib_mat + nfib);
+    if (d->fib_z) m->fz.assign(d->fib_z, d->fib_z + nfib);
+    else m->fz.assign(nfib, 0.0);
+    if (d->sec_GJ) m->GJ.assign(d->sec_GJ, d->sec_GJ + nsec);
+    else m->GJ.assign(nsec, 0.0);
+    m->utype.assign(d->uni_type, d->uni_type + nuni);
+    m->uparam.assign(d->uni_param, d->uni_param + (size_t)nuni * XG_UNI_NPARAM);
+    for (int k = 0; k < nfib; k++)
+      if (m->fmat[k] < 0 || m->fmat[k] >= nuni) {
+        delete m;
+        return fail(XG_EINVAL, "fiber %d: uniaxial row out of range", k);
+      }
+    for (int u = 0; u < nuni; u++)
+      if (m->utype[u] != XG_UNI_STEEL02 && m->utype[u] != XG_UNI_CONCRETE02 &&
+          m->utype[u] != XG_UNI_ELASTIC) {
+        delete m;
+        return fail(XG_EINVAL, "uniaxial row %d: unknown type %d", u, m->utype[u]);
+      }
+    for (int e = 0; e < m->ne; e++)
+      if (m->mat[e] < 0 || m->mat[e] >= nsec) {
+        delete m;
+        return fail(XG_EINVAL, "element %d: section row out of range", e);
+      }
+    if (d->elem_vecxz) m->crd_vecxz.assign(d->elem_vecxz, d->elem_vecxz + (size_t)m->ne * 3);
+  }
   m->num_sp = d->num_sp; m->num_mp = d->num_mp; m->num_loads = d->num_loads;
   m->handler = d->handler;
   if (m->num_sp) {
@@ -924,28 +1240,17 @@ int xg_profile_get(const xg_model *m, int k, char *name, int cap, double *ms, lo
 
 int xg_elemset_commit(xg_model *m) {
   if (!m) return fail(XG_EINVAL, "null model");
-  const long np = m->npts();
-  cudaStream_t s = m->stream;
-  CK(cudaMemcpyAsync(m->d_epc.p, m->d_ept.p, np * m->nhist() * sizeof(double), cudaMemcpyDeviceToDevice, s));
-  CK(cudaMemcpyAsync(m->d_xic.p, m->d_xit.p, np * sizeof(double), cudaMemcpyDeviceToDevice, s));
-  CK(cudaMemcpyAsync(m->d_sig_c.p, m->d_sig.p, np * m->nsig() * sizeof(double), cudaMemcpyDeviceToDevice, s));
-  CK(cudaMemcpyAsync(m->d_tan_c.p, m->d_tan.p, np * m->ntan() * sizeof(double), cudaMemcpyDeviceToDevice, s));
-  CK(cudaMemcpyAsync(m->d_Uc.p, m->d_U.p, (size_t)m->nn * m->ndf * sizeof(double), cudaMemcpyDeviceToDevice, s));
-  CK(cudaStreamSynchronize(s));
+  RET(m->commit_state());
+  CK(cudaStreamSynchronize(m->stream));
+  m->time_c = m->time;
   return 0;
 }
 
 // revertToLastCommit: the trial state returns to the state at the last commit
 int xg_elemset_revert(xg_model *m) {
   if (!m) return fail(XG_EINVAL, "null model");
-  const long np = m->npts();
-  cudaStream_t s = m->stream;
-  CK(cudaMemcpyAsync(m->d_ept.p, m->d_epc.p, np * m->nhist() * sizeof(double), cudaMemcpyDeviceToDevice, s));
-  CK(cudaMemcpyAsync(m->d_xit.p, m->d_xic.p, np * sizeof(double), cudaMemcpyDeviceToDevice, s));
-  CK(cudaMemcpyAsync(m->d_sig.p, m->d_sig_c.p, np * m->nsig() * sizeof(double), cudaMemcpyDeviceToDevice, s));
-  CK(cudaMemcpyAsync(m->d_tan.p, m->d_tan_c.p, np * m->ntan() * sizeof(double), cudaMemcpyDeviceToDevice, s));
-  CK(cudaMemcpyAsync(m->d_U.p, m->d_Uc.p, (size_t)m->nn * m->ndf * sizeof(double), cudaMemcpyDeviceToDevice, s));
-  CK(cudaStreamSynchronize(s));
+  RET(m->revert_state());
+  CK(cudaStreamSynchronize(m->stream));
   m->time = m->time_c;
   return 0;
 }
@@ -1056,10 +1361,14 @@ int xg_reset(xg_model *m) {
   const size_t nu = (size_t)m->nn * m->ndf;
   CK(cudaMemsetAsync(m->d_U.p, 0, nu * sizeof(double), s));
   CK(cudaMemsetAsync(m->d_Uc.p, 0, nu * sizeof(double), s));
-  RET(launch_j2_zero_state(m->view(), s));
-  const long np = m->npts();
-  CK(cudaMemcpyAsync(m->d_sig_c.p, m->d_sig.p, np * m->nsig() * sizeof(double), cudaMemcpyDeviceToDevice, s));
-  CK(cudaMemcpyAsync(m->d_tan_c.p, m->d_tan.p, np * m->ntan() * sizeof(double), cudaMemcpyDeviceToDevice, s));
+  if (m->frames()) {
+    RET(m->upload_frames());
+  } else {
+    RET(launch_j2_zero_state(m->view(), s));
+    const long np = m->npts();
+    CK(cudaMemcpyAsync(m->d_sig_c.p, m->d_sig.p, np * m->nsig() * sizeof(double), cudaMemcpyDeviceToDevice, s));
+    CK(cudaMemcpyAsync(m->d_tan_c.p, m->d_tan.p, np * m->ntan() * sizeof(double), cudaMemcpyDeviceToDevice, s));
+  }
   CK(cudaStreamSynchronize(s));
   m->time = m->time_c = 0.0;
   for (int p = 0; p < 8; p++) {
