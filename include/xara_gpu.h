@@ -145,8 +145,10 @@ typedef struct xg_model_desc {
 /*
  * One analysis phase (`integrator ...; test ...; algorithm Newton;
  * analysis Static|Transient; analyze num_steps [dt]`).  Phase p drives load
- * pattern p; at the end of a phase with load_const != 0 every pattern is
- * held constant and the domain time reset to 0 (`loadConst -time 0.0`).
+ * pattern p.  After a phase with load_const != 0 has run all of its steps,
+ * setting the next phase first holds every pattern constant and resets the
+ * domain time to 0 (`loadConst -time 0.0` between the two `analyze`
+ * commands), so xg_get_disp still reports the phase's last load factor.
  */
 typedef struct xg_phase_desc {
   int integrator;               /* XG_INT_*                                  */

@@ -1302,6 +1302,17 @@ int xg_soe_solve(xg_model *m, const double *b, double *x, double rtol, int maxit
 
 int xg_analysis_set_phase(xg_model *m, const xg_phase_desc *ph) {
   if (!m || !ph) return fail(XG_EINVAL, "null argument");
+  // `loadConst -time 0.0` after a finished phase that asks for it
+  if (m->have_phase && m->phase.load_const && m->phase_steps_done >= m->phase.num_steps &&
+      !m->phase_closed) {
+    m->phase_closed = true;
+    for (int p = 0; p < 8; p++)
+      if (m->added[p] && !m->pattern_const[p]) {
+        m->pattern_const[p] = 1;
+        m->lambda_const[p] = m->time;
+      }
+    m->time = m->time_c = 0.0;
+  }
   m->phase = *ph;
   m->have_phase = true;
   m->phase_steps_done = 0;
@@ -1330,16 +1341,6 @@ int xg_analyze(xg_model *m, int num_steps, xg_step_stats *stats) {
       return r;
     }
     m->phase_steps_done++;
-  }
-  // `loadConst -time 0.0` once the phase has run all of its steps
-  if (m->phase.load_const && m->phase_steps_done >= m->phase.num_steps && !m->phase_closed) {
-    m->phase_closed = true;
-    for (int p = 0; p < 8; p++)
-      if (m->added[p] && !m->pattern_const[p]) {
-        m->pattern_const[p] = 1;
-        m->lambda_const[p] = m->time;
-      }
-    m->time = m->time_c = 0.0;
   }
   return 0;
 }

@@ -294,8 +294,10 @@ int pcg_solve(const PcgSystem &S, const double *b, double *x, double rtol, int m
     if (relres) *relres = 0.0;
     return 0;
   }
-  // rows per block: small systems use few blocks to keep barriers cheap
-  long want = ((long)S.n + 2047) / 2048;
+  // about four rows per warp: SpMV rows are latency-bound chains (row
+  // pointer, column index, vector entry), so mid-size systems want many
+  // warps; the grid barrier's cost grows slowly with the block count
+  long want = ((long)S.n + 63) / 64;
   int nb = (int)(want < 1 ? 1 : want);
   const int maxb = pcg_max_blocks();
   if (nb > maxb) nb = maxb;
