@@ -61,6 +61,8 @@ extern "C" {
 
 /* linear systems */
 #define XG_SYSTEM_BJPCG    0   /* block-Jacobi PCG on the device (new `system CudaBJPCG`) */
+#define XG_SYSTEM_PROFILE_SPD 1 /* skyline LDL' on the device (`system ProfileSPD`,
+                                  system_of_eqn/linearSOE/profileSPD/ProfileSPDLinDirectSolver.cpp) */
 
 /* J2 parameter row (nDMaterial J2Plasticity, material/plastic/J2Plasticity.cpp:84-111) */
 #define XG_J2_NPARAM 8         /* K G sigma0 sigma_inf delta H eta rho */
@@ -240,11 +242,22 @@ int xg_elemset_get_history(const xg_model *m, int which, double *out, long cap);
 int xg_elemset_set_history(xg_model *m, int which, const double *in, long n);
 
 /* ---- LinearSOE (system_of_eqn/linearSOE/LinearSOE.h) on the model's
-        pattern: block-Jacobi PCG on the device ---- */
+        pattern: skyline LDL' (`system ProfileSPD`, the reference default,
+        runtime/runtime/BasicAnalysisBuilder.cpp:820) or block-Jacobi PCG,
+        both on the device ---- */
+
+/* Choose the system (XG_SYSTEM_*); the default is XG_SYSTEM_PROFILE_SPD.
+   Choosing the profile allocates its envelope tiles and fails with
+   XG_ENOMEM when they would take more than half the free device memory. */
+int xg_analysis_set_system(xg_model *m, int system);
 
 /* Solve K x = b with the tangent assembled by the last xg_elemset_update.
-   b, x are host arrays [num_eqn].  Returns XG_ESOLVE on breakdown or when
-   maxit is reached; iters/relres report the final state. */
+   b, x are host arrays [num_eqn].  ProfileSPD: factors once per tangent
+   (the reference's isAfactored) and returns XG_ESOLVE when a pivot fails
+   the reference's checks (first pivot <= 0, a pivot == 0 or |pivot| <=
+   1e-12); rtol and maxit are unused and iters = relres = 0.  PCG: returns
+   XG_ESOLVE on breakdown or when maxit is reached; iters/relres report the
+   final state. */
 int xg_soe_solve(xg_model *m, const double *b, double *x,
                  double rtol, int maxit, int *iters, double *relres);
 

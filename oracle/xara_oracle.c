@@ -792,7 +792,7 @@ static int xo_skyline_solve(xo_model *m, const double *b, double *x) {
       ci[j - ti] = lij;
       aii = aii - lij * aji;
     }
-    if (aii == 0.0 || fabs(aii) <= 1.0e-18) return -2;
+    if (aii == 0.0 || fabs(aii) <= 1.0e-12) return -2;   /* minDiagTol, ProfileSPDLinDirectSolver.h:49 */
     m->invD[i] = 1.0 / aii;
     x[i] += t;
   }

@@ -64,13 +64,17 @@ def test_replay_element_state(gpu_mod, name):
         assert checked >= 4
 
 
+@pytest.mark.parametrize("system", ["profile", "pcg"])
 @pytest.mark.parametrize("name", MODELS)
-def test_displacement_history(gpu_mod, name):
-    """Whole analysis (DisplacementControl + Newton + PCG on the device):
-    converged displacements and load factors per step vs the reference."""
+def test_displacement_history(gpu_mod, name, system):
+    """Whole analysis (DisplacementControl + Newton + the device solver,
+    skyline LDL' or block-Jacobi PCG): converged displacements and load
+    factors per step vs the reference."""
     fx = load(name)
     desc, phases = model_of(fx)
     with gpu_mod.DeviceModel(desc) as m:
+        m.set_system(gpu_mod.XG_SYSTEM_PROFILE_SPD if system == "profile"
+                     else gpu_mod.XG_SYSTEM_BJPCG)
         U, lam, stats = m.run(phases)
     assert relerr(U, fx["step_u"]) < RTOL_HISTORY
     assert relerr(lam, fx["step_lambda"]) < RTOL_HISTORY
@@ -90,10 +94,35 @@ def test_assembly_is_deterministic(gpu_mod):
     assert np.array_equal(v1, v2) and np.array_equal(r1, r2)
 
 
+@pytest.mark.parametrize("name", ["quad_8x4", "frame3d_2x1x3"])
+def test_profile_ldl_against_dense_solve(gpu_mod, name):
+    """Device skyline LDL' (envelope tiles, 32 x 32) against a dense solve,
+    on a quad tangent and on a 3D frame tangent whose envelope spans several
+    tiles; two right-hand sides per factorisation, as DisplacementControl
+    uses it."""
+    fx = load(name)
+    desc, _ = model_of(fx)
+    with gpu_mod.DeviceModel(desc) as m:
+        m.set_system(gpu_mod.XG_SYSTEM_PROFILE_SPD)
+        m.set_trial_disp(fx["step_u"][3] if name.startswith("frame") else fx["cap_U"][1])
+        vals, resid, _ = m.update()
+        rp, ci = m.pattern()
+        n = m.neq
+        A = np.zeros((n, n))
+        for r in range(n):
+            A[r, ci[rp[r]:rp[r + 1]]] = vals[rp[r]:rp[r + 1]]
+        rng = np.random.default_rng(4)
+        for _ in range(2):
+            b = rng.normal(size=n)
+            x, it, rr = m.solve(b)
+            assert relerr(x, np.linalg.solve(A, b)) < 1e-10
+
+
 def test_pcg_against_dense_solve(gpu_mod):
     fx = load("quad_8x4")
     desc, _ = model_of(fx)
     with gpu_mod.DeviceModel(desc) as m:
+        m.set_system(gpu_mod.XG_SYSTEM_BJPCG)
         m.set_trial_disp(fx["cap_U"][1])
         vals, resid, _ = m.update()
         rp, ci = m.pattern()

@@ -42,6 +42,7 @@ def test_noalloc_solve_matches_soe_solve(need_gpu):
                                        C.c_void_p, C.POINTER(C.c_int), C.POINTER(C.c_double)]
     desc, _ = configs.quad_block(64, 16)
     with gpu.DeviceModel(desc) as m:
+        m.set_system(gpu.XG_SYSTEM_BJPCG)
         u = np.zeros(m.nu)
         u[1::2] = -1e-4 * desc.node_crd.reshape(-1, 2)[:, 1]     # a uniform compression
         m.set_trial_disp(u)

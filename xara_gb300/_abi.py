@@ -12,6 +12,7 @@ XG_UNI_STEEL02, XG_UNI_CONCRETE02, XG_UNI_ELASTIC = 1, 2, 3
 XG_HANDLER_PLAIN, XG_HANDLER_TRANSFORMATION = 0, 1
 XG_INT_LOAD_CONTROL, XG_INT_DISP_CONTROL, XG_INT_NEWMARK = 0, 1, 2
 XG_TEST_NORM_DISP_INCR, XG_TEST_NORM_UNBALANCE = 0, 1
+XG_SYSTEM_BJPCG, XG_SYSTEM_PROFILE_SPD = 0, 1
 XG_J2_NPARAM = 8
 XG_UNI_NPARAM = 12
 

@@ -78,6 +78,30 @@ int pcg_solve(const PcgSystem &S, const double *b, double *x, double rtol, int m
               int *iters, double *relres, cudaStream_t s);
 int pcg_max_blocks();
 
+// Skyline LDL' without pivoting on 32 x 32 tiles (xg_profile.cu)
+struct ProfileSystem {
+  int n, nt, W;            // equations, tile rows, envelope width in tiles
+  const int *rowptr, *colidx;
+  const double *vals;
+  const int *ftile;        // [nt] first tile column of each tile row
+  double *L;               // [nt*(W+1)*1024] factor tiles
+  double *Wt;              // [max(W,1)*1024] panel scratch
+  double *invD;            // [nt*32] reciprocal pivots
+  unsigned int *barrier;   // [2]
+  int *flags;              // [4]
+  double min_diag_tol;
+};
+int profile_plan(int n, const int *rowptr, const int *colidx, std::vector<int> &ftile, int &nt,
+                 int &W);
+size_t profile_tile_doubles(int nt, int W);
+int profile_tile_edge();
+// Factor the CSR values into the tiles.  XG_ESOLVE on a failed pivot check
+// (*bad_eq = the equation) or a barrier timeout (*bad_eq = -1).
+int profile_factor(const ProfileSystem &S, cudaStream_t s, int *bad_eq);
+// Solve in place: x[r*ldx + i] holds right-hand side r on entry (ldx >=
+// nt*32, entries past n zero), the solution on return; nrhs <= 4.
+int profile_solve(const ProfileSystem &S, int nrhs, double *x, int ldx, cudaStream_t s);
+
 // small device helpers (xg_kernels.cu)
 int launch_axpy(int n, double a, const double *x, double *y, cudaStream_t s);
 int launch_scatter_incr(int nu, const int *eqn, const double *dU, double f, double *U,

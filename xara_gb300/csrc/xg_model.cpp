@@ -159,6 +159,17 @@ struct xg_model {
   bool blocks_factored = false;
   double rtol = 1e-12;
   int maxit = 20000;
+  // `system ProfileSPD` on the device (xg_profile.cu)
+  int system = XG_SYSTEM_PROFILE_SPD;
+  ProfileSystem psys{};
+  bool prof_ready = false, prof_factored = false;
+  std::vector<int> ftile;
+  DBuf<int> d_ftile, d_pflags;
+  DBuf<unsigned int> d_pbarrier;
+  DBuf<double> d_L, d_Wt, d_invD, d_px;
+  int prof_ldx = 0;
+  int ensure_profile();
+  int solve_profile(int nrhs, const double *const *b, double *const *x);
   // Newton vectors
   DBuf<double> d_fext, d_B, d_dU, d_phat, d_dUhat, d_x, d_b, d_norm, d_Fref;
   std::vector<int> ref_patterns;               // pattern id of each d_Fref row
@@ -184,12 +195,14 @@ struct xg_model {
   };
   std::vector<ProfSlot> prof;
   bool prof_on = false;
-  enum { P_UPDATE, P_ASSEMBLE, P_GATHER_K, P_GATHER_R, P_PCG_FACTOR, P_PCG };
+  enum { P_UPDATE, P_ASSEMBLE, P_GATHER_K, P_GATHER_R, P_PCG_FACTOR, P_PCG, P_LDL_FACTOR,
+         P_LDL_SOLVE, P_NSLOTS };
   void prof_init() {
-    const char *names[6] = {frames() ? "fbc_update" : etype == XG_ELE_QUAD ? "quad_update" : "brick_update",
-                            frames() ? "fbc_assemble" : etype == XG_ELE_QUAD ? "quad_assemble" : "brick_assemble",
-                            "gather_tangent", "gather_resid", "pcg_factor_blocks", "pcg"};
-    for (int k = 0; k < 6; k++) {
+    const char *names[P_NSLOTS] = {
+        frames() ? "fbc_update" : etype == XG_ELE_QUAD ? "quad_update" : "brick_update",
+        frames() ? "fbc_assemble" : etype == XG_ELE_QUAD ? "quad_assemble" : "brick_assemble",
+        "gather_tangent", "gather_resid", "pcg_factor_blocks", "pcg", "ldl_factor", "ldl_solve"};
+    for (int k = 0; k < P_NSLOTS; k++) {
       ProfSlot p{names[k], 0.0, 0, nullptr, nullptr, false};
       cudaEventCreate(&p.a);
       cudaEventCreate(&p.b);
@@ -278,6 +291,17 @@ struct xg_model {
   int upload(const HostGather &gk_h, const HostGather &gr_h);
   int element_state(bool compute);
   int solve(const double *b, double *x, int *iters);
+  // two systems with the same tangent (DisplacementControl::update solves
+  // the unbalance and the reference load with one factorisation)
+  int solve2(const double *b1, double *x1, const double *b2, double *x2) {
+    if (system == XG_SYSTEM_PROFILE_SPD) {
+      const double *bs[2] = {b1, b2};
+      double *xs[2] = {x1, x2};
+      return solve_profile(2, bs, xs);
+    }
+    RET(solve(b1, x1, nullptr));
+    return solve(b2, x2, nullptr);
+  }
   int form_fext(double t);
   int step(xg_step_stats *st);
   int init_phase();
@@ -819,10 +843,72 @@ int xg_model::element_state(bool compute) {
   prof_end(P_GATHER_R, 2);
   prof_flush();
   blocks_factored = false;
+  prof_factored = false;
+  return 0;
+}
+
+// Envelope plan and tile storage of the device LDL' (once per model).
+int xg_model::ensure_profile() {
+  if (prof_ready) return 0;
+  int nt = 0, W = 0;
+  RET(profile_plan(neq, rowptr.data(), colidx.data(), ftile, nt, W));
+  const size_t tiles = profile_tile_doubles(nt, W);
+  size_t free_b = 0, total_b = 0;
+  CK(cudaMemGetInfo(&free_b, &total_b));
+  if ((tiles + (size_t)nt * 32 * 6) * sizeof(double) > free_b / 2)
+    return fail(XG_ENOMEM, "ProfileSPD envelope needs %.1f GB (%d tile rows x %d): use the "
+                "block-Jacobi PCG system", tiles * 8e-9, nt, W + 1);
+  RET(d_ftile.upload(ftile.data(), ftile.size(), stream));
+  RET(d_L.alloc(tiles));
+  RET(d_Wt.alloc((size_t)std::max(W, 1) * 1024));
+  RET(d_invD.alloc((size_t)nt * 32));
+  prof_ldx = nt * 32;
+  RET(d_px.alloc((size_t)prof_ldx * 4));
+  CK(cudaMemsetAsync(d_px.p, 0, (size_t)prof_ldx * 4 * sizeof(double), stream));
+  RET(d_pbarrier.alloc(2));
+  RET(d_pflags.alloc(4));
+  psys.n = neq; psys.nt = nt; psys.W = W;
+  psys.rowptr = d_rowptr.p; psys.colidx = d_colidx.p; psys.vals = d_vals.p;
+  psys.ftile = d_ftile.p; psys.L = d_L.p; psys.Wt = d_Wt.p; psys.invD = d_invD.p;
+  psys.barrier = d_pbarrier.p; psys.flags = d_pflags.p;
+  psys.min_diag_tol = 1.0e-12;   // ProfileSPDLinDirectSolver.h:49 default
+  prof_ready = true;
+  return 0;
+}
+
+// Factor once per tangent, then solve nrhs systems sharing the factors.
+int xg_model::solve_profile(int nrhs, const double *const *b, double *const *x) {
+  RET(ensure_profile());
+  if (!prof_factored) {
+    prof_begin(P_LDL_FACTOR);
+    int bad = -1;
+    const int r = profile_factor(psys, stream, &bad);
+    prof_end(P_LDL_FACTOR, 2);
+    if (r) {
+      if (bad >= 0) return fail(XG_ESOLVE, "ProfileSPD: pivot %d fails the check (aii == 0, "
+                                "|aii| <= 1e-12, or a first pivot <= 0)", bad);
+      return fail(XG_ESOLVE, "ProfileSPD: factorisation barrier timed out");
+    }
+    prof_factored = true;
+  }
+  for (int r = 0; r < nrhs; r++)
+    CK(cudaMemcpyAsync(d_px.p + (size_t)r * prof_ldx, b[r], (size_t)neq * sizeof(double),
+                       cudaMemcpyDeviceToDevice, stream));
+  prof_begin(P_LDL_SOLVE);
+  RET(profile_solve(psys, nrhs, d_px.p, prof_ldx, stream));
+  prof_end(P_LDL_SOLVE, 1);
+  for (int r = 0; r < nrhs; r++)
+    CK(cudaMemcpyAsync(x[r], d_px.p + (size_t)r * prof_ldx, (size_t)neq * sizeof(double),
+                       cudaMemcpyDeviceToDevice, stream));
+  prof_flush();
   return 0;
 }
 
 int xg_model::solve(const double *b, double *x, int *iters) {
+  if (system == XG_SYSTEM_PROFILE_SPD) {
+    if (iters) *iters = 0;
+    return solve_profile(1, &b, &x);
+  }
   if (!blocks_factored) {
     prof_begin(P_PCG_FACTOR);
     RET(pcg_factor_blocks(pcg, stream));
@@ -908,10 +994,10 @@ int xg_model::step(xg_step_stats *st) {
   int it = 0;
   bool ok = false;
   while (true) {
-    RET(solve(d_B.p, d_dU.p, nullptr));
+    if (phase.integrator != XG_INT_DISP_CONTROL) RET(solve(d_B.p, d_dU.p, nullptr));
     if (phase.integrator == XG_INT_DISP_CONTROL) {
       // DisplacementControl::update (:202-250)
-      RET(solve(d_phat.p, d_dUhat.p, nullptr));
+      RET(solve2(d_B.p, d_dU.p, d_phat.p, d_dUhat.p));
       double dUahat, dUabar;
       RET(read_scalar(d_dUhat.p + dc_eq, &dUahat, s));
       RET(read_scalar(d_dU.p + dc_eq, &dUabar, s));
@@ -1284,6 +1370,16 @@ int xg_soe_solve(xg_model *m, const double *b, double *x, double rtol, int maxit
                  double *relres) {
   if (!m || !b || !x) return fail(XG_EINVAL, "null argument");
   CK(cudaMemcpyAsync(m->d_b.p, b, (size_t)m->neq * sizeof(double), cudaMemcpyHostToDevice, m->stream));
+  if (m->system == XG_SYSTEM_PROFILE_SPD) {
+    const double *bs[1] = {m->d_b.p};
+    double *xs[1] = {m->d_x.p};
+    RET(m->solve_profile(1, bs, xs));
+    CK(cudaMemcpyAsync(x, m->d_x.p, (size_t)m->neq * sizeof(double), cudaMemcpyDeviceToHost, m->stream));
+    CK(cudaStreamSynchronize(m->stream));
+    if (iters) *iters = 0;
+    if (relres) *relres = 0.0;
+    return 0;
+  }
   if (!m->blocks_factored) {
     RET(pcg_factor_blocks(m->pcg, m->stream));
     m->blocks_factored = true;
@@ -1318,6 +1414,15 @@ int xg_analysis_set_phase(xg_model *m, const xg_phase_desc *ph) {
   m->phase_steps_done = 0;
   m->phase_closed = false;
   return m->init_phase();
+}
+
+int xg_analysis_set_system(xg_model *m, int system) {
+  if (!m) return fail(XG_EINVAL, "null model");
+  if (system != XG_SYSTEM_BJPCG && system != XG_SYSTEM_PROFILE_SPD)
+    return fail(XG_EINVAL, "unknown system %d", system);
+  m->system = system;
+  if (system == XG_SYSTEM_PROFILE_SPD) RET(m->ensure_profile());
+  return 0;
 }
 
 int xg_analysis_set_solver(xg_model *m, double rtol, int maxit) {

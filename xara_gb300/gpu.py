@@ -11,7 +11,7 @@ import re
 import numpy as np
 
 from . import _abi
-from ._abi import xg_step_stats
+from ._abi import XG_SYSTEM_BJPCG, XG_SYSTEM_PROFILE_SPD, xg_step_stats  # noqa: F401
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB = os.path.join(HERE, "libxara_gpu.so")
@@ -61,6 +61,7 @@ def lib():
     L.xg_soe_solve.argtypes = [vp, vp, vp, C.c_double, C.c_int, ip, dp]
     L.xg_analysis_set_phase.argtypes = [vp, vp]
     L.xg_analysis_set_solver.argtypes = [vp, C.c_double, C.c_int]
+    L.xg_analysis_set_system.argtypes = [vp, C.c_int]
     L.xg_analyze.argtypes = [vp, C.c_int, vp]
     L.xg_get_disp.argtypes = [vp, vp, dp]
     L.xg_reset.argtypes = [vp]
@@ -188,7 +189,12 @@ class DeviceModel:
 
     # -- analysis ------------------------------------------------------------
     def set_solver(self, rtol=1e-12, maxit=20000):
+        """Block-Jacobi PCG settings (used when the system is XG_SYSTEM_BJPCG)."""
         _check(lib().xg_analysis_set_solver(self.h, rtol, maxit))
+
+    def set_system(self, system):
+        """XG_SYSTEM_PROFILE_SPD (device LDL', the default) or XG_SYSTEM_BJPCG."""
+        _check(lib().xg_analysis_set_system(self.h, int(system)))
 
     def set_phase(self, phase):
         self._ps = phase.struct()
