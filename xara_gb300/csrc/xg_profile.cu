@@ -141,7 +141,9 @@ __device__ bool factor_diag(const ProfileSystem &S, int J, double (*sA)[kT + 1],
   return bad == 0;
 }
 
-// Phase B on tile (I = J+o, J): W = A L_JJ^-T by rows, L = W D^-1.
+// Phase B on tile (I = J+o, J): W = A L_JJ^-T by rows, L = W D^-1.  Eight
+// threads share a row: w_c = a_c - sum_{k<c} w_k l_ck, the sum split by k
+// mod 8 and reduced with shuffles inside the eight lanes.
 __device__ void panel_solve(const ProfileSystem &S, int J, int o, double (*sA)[kT + 1],
                             double (*sB)[kT + 1]) {
   const double *Ljj = tile_at(S, J, 0);
@@ -151,12 +153,16 @@ __device__ void panel_solve(const ProfileSystem &S, int J, int o, double (*sA)[k
     sA[k / kT][k % kT] = g[k];
   }
   __syncthreads();
-  if (threadIdx.x < kT) {
-    const int r = threadIdx.x;
+  {
+    const int r = threadIdx.x >> 3, q = threadIdx.x & 7;   // blockDim.x == 256
     for (int c = 1; c < kT; c++) {
-      double w = sA[r][c];
-      for (int k = 0; k < c; k++) w -= sA[r][k] * sB[c][k];
-      sA[r][c] = w;
+      double part = 0.0;
+      for (int k = q; k < c; k += 8) part += sA[r][k] * sB[c][k];
+      part += __shfl_xor_sync(0xffffffffu, part, 4);
+      part += __shfl_xor_sync(0xffffffffu, part, 2);
+      part += __shfl_xor_sync(0xffffffffu, part, 1);
+      if (q == 0) sA[r][c] -= part;
+      __syncwarp();
     }
   }
   __syncthreads();
@@ -227,7 +233,9 @@ __global__ void __launch_bounds__(kFactorThreads) k_prof_factor(ProfileSystem S)
 }
 
 // Forward (L y = b), diagonal (z = D^-1 y) and backward (L' x = z)
-// substitution in one block; x[r * ldx + i] for right-hand side r.
+// substitution in one block; x[r * ldx + i] for right-hand side r.  Every
+// thread issues its loads of a whole tile row (column) before it uses them,
+// so a step costs about one memory latency plus the diagonal solve.
 __global__ void __launch_bounds__(kSolveThreads) k_prof_solve(ProfileSystem S, int nrhs,
                                                                double *x, int ldx) {
   __shared__ double red[kSolveThreads / 32][4][kT];
@@ -236,74 +244,83 @@ __global__ void __launch_bounds__(kSolveThreads) k_prof_solve(ProfileSystem S, i
   constexpr int nw = kSolveThreads / 32;
   const int nt = S.nt, W = S.W;
   // ---- forward: t = b_J - sum_o L(J, J-o) y_{J-o}; then unit-lower solve
-  for (int J = 0; J < nt; J++) {
-    // warp w handles tiles o = 1 + w, 1 + w + nw, ...; lane = row r
-    double acc[4] = {0.0, 0.0, 0.0, 0.0};
-    const int ohi = min(W, J - S.ftile[J]);
-    for (int o = 1 + w; o <= ohi; o += nw) {
-      const double *L = tile_at(S, J, o);
-      const int c0 = (J - o) * kT;
-      for (int c = 0; c < kT; c++) {
-        const double l = L[lane * kT + c];
-        for (int r = 0; r < nrhs; r++) acc[r] += l * x[(size_t)r * ldx + c0 + c];
+  {
+    const int r = tid >> 4, g = tid & 15;      // row of the tile, column group
+    for (int J = 0; J < nt; J++) {
+      double acc[4] = {0.0, 0.0, 0.0, 0.0};
+      const int ohi = min(W, J - S.ftile[J]);
+#pragma unroll 4
+      for (int o = 1; o <= ohi; o++) {
+        const double *Lt = tile_at(S, J, o) + r * kT;
+        const double l0 = Lt[g], l1 = Lt[g + 16];
+        const double *xc = x + (J - o) * kT;
+        for (int q = 0; q < nrhs; q++)
+          acc[q] += l0 * xc[(size_t)q * ldx + g] + l1 * xc[(size_t)q * ldx + g + 16];
       }
-    }
-    for (int r = 0; r < nrhs; r++) red[w][r][lane] = acc[r];
-    {
-      const double *L = tile_at(S, J, 0);
-      for (int k = tid; k < kTT; k += kSolveThreads) sL[k / kT][k % kT] = L[k];
-    }
-    __syncthreads();
-    if (w < nrhs) {
-      const int r = w;
-      double s = 0.0;
-      for (int q = 0; q < nw; q++) s += red[q][r][lane];
-      double v = x[(size_t)r * ldx + J * kT + lane] - s;
-      for (int c = 0; c < kT - 1; c++) {
-        const double yc = __shfl_sync(0xffffffffu, v, c);
-        if (lane > c) v -= sL[lane][c] * yc;
+      for (int q = 0; q < nrhs; q++) {
+        double v = acc[q];
+        v += __shfl_xor_sync(0xffffffffu, v, 8);
+        v += __shfl_xor_sync(0xffffffffu, v, 4);
+        v += __shfl_xor_sync(0xffffffffu, v, 2);
+        v += __shfl_xor_sync(0xffffffffu, v, 1);
+        if (g == 0) red[0][q][r] = v;
       }
-      x[(size_t)r * ldx + J * kT + lane] = v;
+      {
+        const double *L = tile_at(S, J, 0);
+        for (int k = tid; k < kTT; k += kSolveThreads) sL[k / kT][k % kT] = L[k];
+      }
+      __syncthreads();
+      if (w < nrhs) {
+        const int q = w;
+        double v = x[(size_t)q * ldx + J * kT + lane] - red[0][q][lane];
+        for (int c = 0; c < kT - 1; c++) {
+          const double yc = __shfl_sync(0xffffffffu, v, c);
+          if (lane > c) v -= sL[lane][c] * yc;
+        }
+        x[(size_t)q * ldx + J * kT + lane] = v;
+      }
+      __syncthreads();
     }
-    __syncthreads();
   }
   // ---- diagonal
-  for (int r = 0; r < nrhs; r++)
-    for (int i = tid; i < nt * kT; i += kSolveThreads) x[(size_t)r * ldx + i] *= S.invD[i];
+  for (int q = 0; q < nrhs; q++)
+    for (int i = tid; i < nt * kT; i += kSolveThreads) x[(size_t)q * ldx + i] *= S.invD[i];
   __syncthreads();
   // ---- backward: t = z_J - sum_o L(J+o, J)' x_{J+o}; then unit-upper solve
-  for (int J = nt - 1; J >= 0; J--) {
-    double acc[4] = {0.0, 0.0, 0.0, 0.0};
-    const int ohi = min(W, nt - 1 - J);
-    // warp w handles tiles o = 1 + w, ...; lane = column c of the tile
-    for (int o = 1 + w; o <= ohi; o += nw) {
-      if (S.ftile[J + o] > J) continue;
-      const double *L = tile_at(S, J + o, o);
-      const int r0 = (J + o) * kT;
-      for (int rr = 0; rr < kT; rr++) {
-        const double l = L[rr * kT + lane];
-        for (int r = 0; r < nrhs; r++) acc[r] += l * x[(size_t)r * ldx + r0 + rr];
+  {
+    const int c = lane, g = w;                 // column of the tile, row group
+    for (int J = nt - 1; J >= 0; J--) {
+      double acc[4] = {0.0, 0.0, 0.0, 0.0};
+      const int ohi = min(W, nt - 1 - J);
+#pragma unroll 4
+      for (int o = 1; o <= ohi; o++) {
+        if (S.ftile[J + o] > J) continue;
+        const double *Lt = tile_at(S, J + o, o);
+        const double l0 = Lt[g * kT + c], l1 = Lt[(g + nw) * kT + c];
+        const double *xr = x + (J + o) * kT;
+        for (int q = 0; q < nrhs; q++)
+          acc[q] += l0 * xr[(size_t)q * ldx + g] + l1 * xr[(size_t)q * ldx + g + nw];
       }
-    }
-    for (int r = 0; r < nrhs; r++) red[w][r][lane] = acc[r];
-    {
-      const double *L = tile_at(S, J, 0);
-      for (int k = tid; k < kTT; k += kSolveThreads) sL[k / kT][k % kT] = L[k];
-    }
-    __syncthreads();
-    if (w < nrhs) {
-      const int r = w;
-      double s = 0.0;
-      for (int q = 0; q < nw; q++) s += red[q][r][lane];
-      double v = x[(size_t)r * ldx + J * kT + lane] - s;
-      // x_c = v_c - sum_{k > c} L[k][c] x_k, from the last row up
-      for (int c = kT - 1; c > 0; c--) {
-        const double xc = __shfl_sync(0xffffffffu, v, c);
-        if (lane < c) v -= sL[c][lane] * xc;
+      for (int q = 0; q < nrhs; q++) red[g][q][c] = acc[q];
+      {
+        const double *L = tile_at(S, J, 0);
+        for (int k = tid; k < kTT; k += kSolveThreads) sL[k / kT][k % kT] = L[k];
       }
-      x[(size_t)r * ldx + J * kT + lane] = v;
+      __syncthreads();
+      if (w < nrhs) {
+        const int q = w;
+        double s = 0.0;
+        for (int h = 0; h < nw; h++) s += red[h][q][lane];
+        double v = x[(size_t)q * ldx + J * kT + lane] - s;
+        // x_c = v_c - sum_{k > c} L[k][c] x_k, from the last row up
+        for (int cc = kT - 1; cc > 0; cc--) {
+          const double xc = __shfl_sync(0xffffffffu, v, cc);
+          if (lane < cc) v -= sL[cc][lane] * xc;
+        }
+        x[(size_t)q * ldx + J * kT + lane] = v;
+      }
+      __syncthreads();
     }
-    __syncthreads();
   }
 }
 
