@@ -1,25 +1,35 @@
 #!/usr/bin/env python3
 """Benchmark of the Newton-iteration hot path on one GB300.
 
-Workload (default): the element phase of one Newton iteration of the
-stdBrick J2 block, 128 x 128 x 64 elements (1,048,576 bricks, 8,388,608
-integration points, 3,178,432 equations, 252,000,686 CSR non-zeros), FP64:
-material state determination of every integration point (J2 radial return),
-element tangents and resisting forces, and the deterministic assembly of the
-CSR tangent and the residual (Domain::update + formTangent + formUnbalance).
-A step is one such pass over all elements.  Inputs (model, history, trial
-displacements) are resident in HBM when the timed region starts; every array
-is far larger than the 129 MB L2, so no flush is needed between steps.
+Workload `frame3d` (default): the 3D RC frame of 10 x 10 bays x 20 stories
+(6,820 forceBeamColumn elements, 5 Lobatto sections each, 120-fiber columns
+and 64-fiber beams with Concrete02 / Steel02, 14,520 equations), FP64.  A
+step is one Newton iteration of the hot path at a seeded lateral trial
+displacement field: state determination of every element (the force-based
+compatibility iteration over every fiber of every section), assembly of the
+tangent and the resisting force, and the `system ProfileSPD` solve (LDL'
+factorisation and substitution) of the tangent.  The trial fields grow
+monotonically from step to step, so the fibers load along a pushover path.
+Inputs (model, trial fields, load vector) are resident in HBM when the timed
+region starts; the factor tiles (89 MB) and the fiber records (275 MB) are
+rewritten every step.
 
-Metric: integration-point updates per second (higher is better).
+Metric: IP updates/s -- fiber state determinations per second, every fiber
+counted once per inner compatibility iteration of its element; Newton
+iterations/s is reported beside it.
 
-  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl xara|reference]
+Workload `brick`: the element phase of the stdBrick J2 block 128 x 128 x 64
+(1,048,576 bricks, 8,388,608 integration points), one pass per step.
 
---impl reference times the reference algorithm's CPU path (the C oracle,
-a restatement of the reference's classes, compiled on this host) on the
-host's cores, on a bounded sample of the same workload.
+  python bench.py [--workload frame3d|brick] [--gpus N] [--steps K] [--warmup W]
+                  [--impl xara|reference]
+
+--impl reference times the reference algorithm's CPU path (the C oracle, a
+restatement of the reference's classes compiled on this host) on every host
+core, one model per process, on the same workload and metric.
 """
 import argparse
+import ctypes as C
 import json
 import os
 import subprocess
@@ -32,27 +42,16 @@ sys.path.insert(0, ROOT)
 
 import numpy as np  # noqa: E402
 
-WORKLOAD = dict(nx=128, ny=128, nz=64)
-SAMPLE = dict(nx=24, ny=24, nz=12)   # CPU baseline sample (6,912 bricks)
 METRIC = "IP updates/s"
-UNIT = "integration-point updates/s"
+UNIT = "material-point updates/s"
+FRAME = dict(bays_x=10, bays_y=10, stories=20)
+BRICK = dict(nx=128, ny=128, nz=64)
+BRICK_SAMPLE = dict(nx=24, ny=24, nz=12)
 
 
-def trial_field(desc, nx, ny, nz, eps=2.5e-3):
-    """A seeded, spatially varying compression field that leaves part of the
-    block elastic and part plastic (sigma0 is U[200, 300] MPa per element)."""
-    rng = np.random.default_rng(7)
-    crd = desc.node_crd.reshape(-1, 3)
-    x, y, z = crd[:, 0] / nx, crd[:, 1] / ny, crd[:, 2] / nz
-    shape = 1.0 + 0.6 * np.sin(2 * np.pi * x) * np.cos(np.pi * y)
-    u = np.zeros((len(crd), 3))
-    u[:, 2] = -eps * nz * z * shape
-    u[:, 0] = 0.3 * eps * nx * (x - 0.5) * z
-    u[:, 1] = 0.3 * eps * ny * (y - 0.5) * z
-    u += rng.normal(0.0, 1e-6, size=u.shape) * (z[:, None] > 0)
-    return u.ravel()
-
-
+# ---------------------------------------------------------------------------
+# shared helpers
+# ---------------------------------------------------------------------------
 class ClockSampler:
     """nvidia-smi clocks and throttle reasons sampled during the timed region."""
 
@@ -115,85 +114,360 @@ def measured_peaks():
     return 6800.0, "of fallback"
 
 
-def algorithmic_bytes(npts, ne, nn, nnz, neq):
-    """Bytes the element phase must move, per the per-unit figures:
-    per integration point 56 B of committed history read (plastic strain 6 +
-    xi), 56 B of trial history written; per node 48 B (coordinates and trial
-    displacements); 8 B per CSR value written; 8 B per residual entry."""
-    return {
-        "phase": npts * 112 + nn * 48 + nnz * 8 + neq * 8,
-        # the material-update kernel: history in/out plus the trial stress
-        # (6 doubles) and tangent parameters (9 doubles) it hands to the
-        # element kernel, and the nodal data
-        "brick_update": npts * (112 + 48 + 72) + nn * 48,
-        # element kernel: point stress + tangent parameters in, node-pair
-        # blocks (324 doubles) and element forces (24) out per element
-        "brick_assemble": npts * (48 + 72) + ne * (324 + 24) * 8 + nn * 24,
-        # gather of the tangent: every CSR value written once
-        "gather_tangent": nnz * 8,
-        "gather_resid": neq * 8,
-    }
+def fp64_peak_probe():
+    from xara_gb300 import gpu
+    L = gpu.lib()
+    v = C.c_double()
+    L.xg_measure_fp64_peak.argtypes = [C.POINTER(C.c_double)]
+    if L.xg_measure_fp64_peak(C.byref(v)) != 0:
+        return None
+    return v.value
 
 
-def flops_estimate(npts, ne):
-    """FP64 flops of the element phase (counted from the kernels' source):
-    J2 return map + strain + shape functions ~ 700 per point; node-pair
-    stiffness blocks 36 pairs x 8 points x 64 flops per element."""
-    return npts * 700 + ne * 36 * 8 * 64
+def ncu_traffic(workload, kernel):
+    """DRAM bytes per launch of the kernel from the committed ncu summary."""
+    p = os.path.join(ROOT, "profiles", "dram_traffic.json")
+    if not os.path.exists(p):
+        return None
+    with open(p) as f:
+        d = json.load(f)
+    return d.get(workload, {}).get(kernel)
 
 
-def cpu_baseline_sample(seconds=12.0):
-    """The oracle's element phase (single thread) on a sample of the workload."""
-    from oracle import port
+def dist_setup():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        # one replica per GPU: one model's Newton iteration does not shard
+        os.environ["CUDA_VISIBLE_DEVICES"] = str(local)
+    import torch
+    import torch.distributed as dist
+    if world > 1:
+        dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+        torch.cuda.set_device(0)
+    return world, rank, local, torch, dist
+
+
+def max_over_ranks(x, world, torch, dist):
+    if world == 1:
+        return x
+    t = torch.tensor([x], device="cuda")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+# ---------------------------------------------------------------------------
+# frame3d: one Newton iteration of the 3D RC frame per step
+# ---------------------------------------------------------------------------
+def frame_model():
     from xara_gb300 import configs
-    desc, _ = configs.brick_block(**SAMPLE, steps=1)
-    o = port.OracleModel(desc)
-    U = trial_field(desc, **SAMPLE)
-    npts = desc.num_elems * 8
-    o.elem_state(U)
-    n, t0 = 0, time.perf_counter()
-    while time.perf_counter() - t0 < seconds:
-        o.elem_state(U)
+    desc, phases = configs.rc_frame_3d(**FRAME)
+    return desc, phases
+
+
+def lateral_field(desc, frac, drift=0.02):
+    """Seeded lateral displacement field: roof drift frac*drift in x with a
+    first-mode shape, a smaller y component and twist, the matching floor
+    rotations; base nodes stay fixed."""
+    rng = np.random.default_rng(3)
+    crd = desc.node_crd.reshape(-1, 3)
+    H = crd[:, 2].max()
+    z = crd[:, 2] / H
+    shape = np.sin(0.5 * np.pi * z)
+    dshape = 0.5 * np.pi * np.cos(0.5 * np.pi * z) / H
+    u = np.zeros((len(crd), 6))
+    a = frac * drift * H
+    u[:, 0] = a * shape
+    u[:, 1] = 0.25 * a * shape
+    u[:, 4] = a * dshape                      # rotation about y follows dux/dz
+    u[:, 3] = -0.25 * a * dshape              # rotation about x follows -duy/dz
+    u[:, 5] = 1e-4 * frac * z
+    u[:, :3] += rng.normal(0.0, 1e-6, size=(len(crd), 3)) * (z[:, None] > 0)
+    u[z == 0] = 0.0
+    return u.ravel()
+
+
+def frame_fields(desc, n):
+    return [lateral_field(desc, (k + 1) / n) for k in range(n)]
+
+
+def profile_stats(rowptr, colidx):
+    """Envelope entries (the ProfileSPD storage) and FP64 FMAs of its LDL'."""
+    first = colidx[rowptr[:-1]]
+    h = np.arange(len(first)) - first + 1
+    return int(h.sum()), float((h.astype(np.float64) ** 2).sum() / 2.0)
+
+
+def frame_alg_bytes(desc, nnz, neq):
+    """Algorithmic bytes of the kernels of one Newton iteration, from the
+    per-unit figures: fiber history (Steel02 80 B, Concrete02 32 B) read
+    committed and written trial once per element update; element state
+    (Se, kv, 5 x (vs, fs, Ssr)) 1.3 KB read and written; nodal
+    displacements; CSR values and residual written; the LDL' reads the
+    envelope of the tangent and writes its factor."""
+    from xara_gb300._abi import XG_UNI_STEEL02
+    sec_start = np.asarray(desc.arrays["sec_fiber_start"])
+    fmat = np.asarray(desc.arrays["fib_mat"])
+    utype = np.asarray(desc.arrays["uni_type"])
+    per_fiber = np.where(utype[fmat] == XG_UNI_STEEL02, 160, 64)
+    sec_bytes = np.array([per_fiber[sec_start[s]:sec_start[s + 1]].sum()
+                          for s in range(len(sec_start) - 1)])
+    emat = np.asarray(desc.arrays["elem_mat"])
+    ne = len(emat)
+    fib = float(sec_bytes[emat].sum()) * 5
+    update = fib + ne * 2 * 1300 + desc.num_nodes * 48
+    return {"fbc_update": update, "fbc_assemble": ne * (1300 + 144 * 8 + 12 * 8),
+            "gather_tangent": nnz * 8.0, "gather_resid": neq * 8.0}
+
+
+def run_frame(args):
+    world, rank, local, torch, dist = dist_setup()
+    from xara_gb300 import gpu
+    L = gpu.lib()
+    L.xg_elemset_set_trial_disp_device.argtypes = [C.c_void_p, C.c_void_p]
+    L.xg_soe_solve_device.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_double, C.c_int,
+                                      C.c_void_p, C.c_void_p]
+    desc, phases = frame_model()
+    t_setup = time.perf_counter()
+    m = gpu.DeviceModel(desc)
+    m.set_system(gpu.XG_SYSTEM_PROFILE_SPD)
+    t_setup = time.perf_counter() - t_setup
+    rowptr, colidx = m.pattern()
+    envelope, ldl_fma = profile_stats(rowptr, colidx)
+    nsteps = args.warmup + args.steps
+    fields = frame_fields(desc, nsteps)
+    dev = torch.device("cuda")
+    U = torch.from_numpy(np.stack(fields)).to(dev)
+    b = torch.from_numpy(np.random.default_rng(5).normal(size=m.neq)).to(dev)
+    x = torch.empty(m.neq, dtype=torch.float64, device=dev)
+    stream = torch.cuda.ExternalStream(gpu.model_stream(m))
+    torch.cuda.synchronize()
+    fp64_peak = fp64_peak_probe()
+
+    def iteration(k):
+        gpu._check(L.xg_elemset_set_trial_disp_device(m.h, C.c_void_p(U[k].data_ptr())))
+        gpu._check(L.xg_elemset_update(m.h, None, None))
+        gpu._check(L.xg_soe_solve_device(m.h, C.c_void_p(b.data_ptr()),
+                                         C.c_void_p(x.data_ptr()), 1e-12, 20000, None, None))
+
+    def barrier():
+        if world > 1:
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    for k in range(args.warmup):
+        iteration(k)
+    gpu.profile_enable(m, True)
+    sampler = ClockSampler(local if world == 1 else 0)
+    sampler.start()
+    ev0 = torch.cuda.Event(enable_timing=True)
+    ev1 = torch.cuda.Event(enable_timing=True)
+    barrier()
+    ev0.record(stream)
+    for k in range(args.warmup, nsteps):
+        iteration(k)
+    ev1.record(stream)
+    barrier()
+    clocks = sampler.stop()
+    dt = ev0.elapsed_time(ev1) * 1e-3
+    points, sections, elems = gpu.profile_counters(m)
+    prof = gpu.profile_read(m)
+    gpu.profile_enable(m, False)
+    dt = max_over_ranks(dt, world, torch, dist)
+    value = points * world / dt
+
+    # end to end through the C ABI with host buffers (the reference-facing
+    # element-set + LinearSOE calls): trial displacements in, the resisting
+    # force out, the load vector in and the solution out, every step
+    m.revert()
+    Uh = [torch.from_numpy(f).pin_memory() for f in fields]
+    bh = torch.from_numpy(b.cpu().numpy()).pin_memory()
+    rh = torch.empty(m.neq, dtype=torch.float64).pin_memory()
+    xh = torch.empty(m.neq, dtype=torch.float64).pin_memory()
+    ptr = lambda t: C.c_void_p(t.data_ptr())  # noqa: E731
+    it_, rr_ = C.c_int(), C.c_double()
+    for k in range(args.warmup):
+        gpu._check(L.xg_elemset_set_trial_disp(m.h, ptr(Uh[k])))
+        gpu._check(L.xg_elemset_update(m.h, None, ptr(rh)))
+        gpu._check(L.xg_soe_solve(m.h, ptr(bh), ptr(xh), 1e-12, 20000, C.byref(it_),
+                                  C.byref(rr_)))
+    gpu.profile_enable(m, True)
+    barrier()
+    t0 = time.perf_counter()
+    for k in range(args.warmup, nsteps):
+        gpu._check(L.xg_elemset_set_trial_disp(m.h, ptr(Uh[k])))
+        gpu._check(L.xg_elemset_update(m.h, None, ptr(rh)))
+        gpu._check(L.xg_soe_solve(m.h, ptr(bh), ptr(xh), 1e-12, 20000, C.byref(it_),
+                                  C.byref(rr_)))
+    barrier()
+    dt_e2e = time.perf_counter() - t0
+    points_e2e, _, _ = gpu.profile_counters(m)
+    gpu.profile_enable(m, False)
+    dt_e2e = max_over_ranks(dt_e2e, world, torch, dist)
+    e2e_value = points_e2e * world / dt_e2e
+
+    # the full analysis through the device Newton driver: gravity, then
+    # pushover steps (DisplacementControl), for Newton iterations/s
+    analysis = None
+    if not args.no_analysis:
+        m.reset()
+        m.set_phase(phases[0])
+        m.analyze(phases[0].num_steps)
+        m.set_phase(phases[1])
+        m.analyze(2)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        st = m.analyze(args.analysis_steps)
+        dta = time.perf_counter() - t0
+        newton = sum(s[0] for s in st)
+        analysis = {"pushover_steps": args.analysis_steps, "newton_iterations": newton,
+                    "pushover_steps_per_s": args.analysis_steps / dta,
+                    "newton_iters_per_s": newton / dta,
+                    "note": "DisplacementControl pushover steps after gravity and loadConst, "
+                            "device Newton driver, host clock"}
+
+    if rank != 0:
+        dist.destroy_process_group()
+        return 0
+
+    kernels = {k: v for k, v in prof.items() if v[1] > 0 and k != "return_map_cap_hits"}
+    gpu_launches = sum(v[1] for v in kernels.values())
+    dominant = max(kernels, key=lambda k: kernels[k][0])
+    groups = {"ldl_factor": 1, "gather_tangent": 1, "gather_resid": 1}
+    dom_ms, dom_launches = kernels[dominant]
+    per_group_s = dom_ms * 1e-3 / max(dom_launches // (2 if dominant in groups else 1), 1)
+    alg = frame_alg_bytes(desc, m.nnz, m.neq)
+    alg["ldl_factor"] = envelope * 16.0        # envelope read, factor written
+    alg["ldl_solve"] = envelope * 16.0         # forward and backward sweeps
+    peak, peak_kind = measured_peaks()
+    achieved = alg[dominant] / per_group_s / 1e9
+    step_s = dt / args.steps
+    ldl_ms = kernels.get("ldl_factor", (0, 1))
+    ldl_s = ldl_ms[0] * 1e-3 / max(ldl_ms[1] // 2, 1)
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * step_s,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f64", "data": "synthetic (seeded model and lateral trial fields)",
+        "config": {"workload": "3D RC frame 10x10x20 (BASELINE config 1 model): one Newton "
+                               "iteration per step -- forceBeamColumn state determination, "
+                               "assembly, ProfileSPD LDL' solve",
+                   "elements": desc.num_elems, "equations": m.neq, "nnz": m.nnz,
+                   "fiber_points": desc.meta["fiber_points"], "envelope": envelope,
+                   "system": "ProfileSPD (device LDL')", "parallelism": f"replicas x{world}",
+                   "l2": "per-step working set (factor tiles 89 MB rewritten, fiber records "
+                         "275 MB) exceeds L2; no flush"},
+        "newton_iters_per_s": args.steps * world / dt,
+        "point_updates_per_step": points / args.steps,
+        "section_updates_per_step": sections / args.steps,
+        "e2e": {"value": e2e_value, "unit": UNIT,
+                "h2d_bytes_per_step": int(Uh[0].numel() * 8 + bh.numel() * 8),
+                "d2h_bytes_per_step": int(rh.numel() * 8 + xh.numel() * 8),
+                "path": "xg_elemset_set_trial_disp + xg_elemset_update + xg_soe_solve, "
+                        "pinned host buffers"},
+        "gpu_launches": int(gpu_launches),
+        "roofline": {"bound": "hbm", "kernel": dominant, "achieved": achieved, "peak": peak,
+                     "unit": "GB/s", "frac": achieved / peak if peak else None,
+                     "peak_source": peak_kind, "traffic": ncu_traffic("frame3d", dominant),
+                     "algorithmic_bytes_per_launch": alg[dominant]},
+        "fp64": {"ldl_factor_flops": 2.0 * ldl_fma, "ldl_factor_ms": 1e3 * ldl_s,
+                 "achieved_tflops": 2.0 * ldl_fma / ldl_s / 1e12 if ldl_s > 0 else None,
+                 "peak_tflops_probe": fp64_peak,
+                 "frac": (2.0 * ldl_fma / ldl_s / 1e12) / fp64_peak if fp64_peak and ldl_s else None,
+                 "note": "the LDL' is FP64-bound: its roofline is the FP64 rate, not HBM"},
+        "kernels_ms_per_step": {k: v[0] / args.steps for k, v in kernels.items()},
+        "analysis": analysis,
+        "clocks": clocks,
+        "setup_s": t_setup,
+    }
+    if not args.no_cpu_baseline:
+        rate, its, sample = frame_cpu_sample(seconds=args.cpu_seconds)
+        line["cpu_baseline"] = {"value": rate, "unit": UNIT, "cores": 1, "kind": "port",
+                                "sample": sample, "newton_iters_per_s": its}
+    print(json.dumps(line))
+    if world > 1:
+        dist.destroy_process_group()
+    return 0
+
+
+class FrameCpu:
+    """The oracle's path (element state, assembly, ProfileSPD) on one model."""
+
+    def __init__(self, nsteps):
+        from oracle import port
+        self.desc, _ = frame_model()
+        self.o = port.OracleModel(self.desc)
+        self.fields = frame_fields(self.desc, nsteps)
+        self.b = np.random.default_rng(5).normal(size=self.o.neq)
+
+    def iteration(self, k):
+        p0, _ = self.o.work()
+        self.o.elem_state(self.fields[k])
+        self.o.soe_solve(self.b)
+        return self.o.work()[0] - p0
+
+
+def frame_cpu_sample(seconds=12.0, nsteps=23):
+    t0 = time.perf_counter()
+    cpu = FrameCpu(nsteps)
+    pts, n, t1 = 0, 0, time.perf_counter()
+    while n < nsteps and (n < 2 or time.perf_counter() - t1 < seconds):
+        pts += cpu.iteration(n)
         n += 1
-    dt = time.perf_counter() - t0
-    return npts * n / dt, f"brick J2 {SAMPLE['nx']}x{SAMPLE['ny']}x{SAMPLE['nz']} " \
-                          f"({desc.num_elems} elements, {npts} points), {n} element phases"
+    dt = time.perf_counter() - t1
+    sample = (f"3D RC frame 10x10x20 at full size, {n} Newton iterations (element state, "
+              f"assembly, ProfileSPD factor + solve) along the seeded lateral fields, "
+              f"1 thread; model set-up {t1 - t0:.1f} s untimed")
+    return pts / dt, n / dt, sample
 
 
-def _ref_worker(args):
-    seconds, = args
-    rate, _ = cpu_baseline_sample(seconds)
-    return rate
+_CPU = None
 
 
-def run_reference(args):
-    """CPU path of the reference algorithm on all host cores (processes)."""
+def _frame_worker(args):
+    global _CPU
+    kind, k, nsteps = args
+    if kind == "init":
+        _CPU = FrameCpu(nsteps)
+        return 0
+    t0 = time.perf_counter()
+    pts = _CPU.iteration(k)
+    return pts, time.perf_counter() - t0
+
+
+def run_reference_frame(args):
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return 0
     import multiprocessing as mp
     cores = os.cpu_count() or 1
-    per_step = 4.0
+    nsteps = args.warmup + args.steps
     ctx = mp.get_context("spawn")
     with ctx.Pool(cores) as pool:
-        for _ in range(args.warmup):
-            pool.map(_ref_worker, [(0.5,)] * cores)
+        pool.map(_frame_worker, [("init", 0, nsteps)] * cores, chunksize=1)
+        for k in range(args.warmup):
+            pool.map(_frame_worker, [("step", k, nsteps)] * cores, chunksize=1)
         t0 = time.perf_counter()
-        rates = []
-        for _ in range(args.steps):
-            rates.append(sum(pool.map(_ref_worker, [(per_step,)] * cores)))
+        pts = 0
+        for k in range(args.warmup, nsteps):
+            res = pool.map(_frame_worker, [("step", k, nsteps)] * cores, chunksize=1)
+            pts += sum(r[0] for r in res)
         wall = time.perf_counter() - t0
-    value = float(np.mean(rates))
-    npts = WORKLOAD["nx"] * WORKLOAD["ny"] * WORKLOAD["nz"] * 8
-    sample = (f"brick J2 {SAMPLE['nx']}x{SAMPLE['ny']}x{SAMPLE['nz']} element phase, "
-              f"{cores} processes x {per_step:.0f} s per step")
+    value = pts / wall
+    sample = (f"3D RC frame 10x10x20 at full size, one model per process on {cores} "
+              f"processes, one Newton iteration (element state, assembly, ProfileSPD factor "
+              f"+ solve) per process per step")
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT,
         "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
-        "ms_per_step": 1e3 * npts / value, "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded)",
-        "config": {"workload": "stdBrick J2 128x128x64 element phase (one Newton iteration)",
-                   "elements": npts // 8, "points": npts, "l2": "inputs larger than L2"},
+        "ms_per_step": 1e3 * wall / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded model and lateral "
+                                                     "trial fields)",
+        "config": {"workload": "3D RC frame 10x10x20 (BASELINE config 1 model): one Newton "
+                               "iteration per step -- forceBeamColumn state determination, "
+                               "assembly, ProfileSPD LDL' solve"},
+        "newton_iters_per_s": args.steps * cores / wall,
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
                          "sample": sample},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
@@ -203,43 +477,111 @@ def run_reference(args):
     return 0
 
 
-def main():
-    ap = argparse.ArgumentParser()
-    ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=20)
-    ap.add_argument("--warmup", type=int, default=3)
-    ap.add_argument("--impl", default="xara", choices=["xara", "reference"])
-    ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--nx", type=int, default=WORKLOAD["nx"])
-    ap.add_argument("--ny", type=int, default=WORKLOAD["ny"])
-    ap.add_argument("--nz", type=int, default=WORKLOAD["nz"])
-    args = ap.parse_args()
-    WORKLOAD.update(nx=args.nx, ny=args.ny, nz=args.nz)
-    args.warmup = max(args.warmup, 3)
-    if args.impl == "reference":
-        return run_reference(args)
+# ---------------------------------------------------------------------------
+# brick: the element phase of the stdBrick J2 block
+# ---------------------------------------------------------------------------
+def brick_trial_field(desc, nx, ny, nz, eps=2.5e-3):
+    """A seeded, spatially varying compression field that leaves part of the
+    block elastic and part plastic (sigma0 is U[200, 300] MPa per element)."""
+    rng = np.random.default_rng(7)
+    crd = desc.node_crd.reshape(-1, 3)
+    x, y, z = crd[:, 0] / nx, crd[:, 1] / ny, crd[:, 2] / nz
+    shape = 1.0 + 0.6 * np.sin(2 * np.pi * x) * np.cos(np.pi * y)
+    u = np.zeros((len(crd), 3))
+    u[:, 2] = -eps * nz * z * shape
+    u[:, 0] = 0.3 * eps * nx * (x - 0.5) * z
+    u[:, 1] = 0.3 * eps * ny * (y - 0.5) * z
+    u += rng.normal(0.0, 1e-6, size=u.shape) * (z[:, None] > 0)
+    return u.ravel()
 
-    world = int(os.environ.get("WORLD_SIZE", "1"))
+
+def brick_alg_bytes(npts, ne, nn, nnz, neq):
+    """Bytes the element phase must move, per the per-unit figures: per
+    integration point 56 B of committed history read (plastic strain 6 + xi)
+    and 56 B of trial history written; per node 48 B (coordinates and trial
+    displacements); 8 B per CSR value written; 8 B per residual entry."""
+    return {
+        "phase": npts * 112 + nn * 48 + nnz * 8 + neq * 8,
+        "brick_update": npts * (112 + 48 + 72) + nn * 48,
+        "brick_assemble": npts * (48 + 72) + ne * (324 + 24) * 8 + nn * 24,
+        "gather_tangent": nnz * 8,
+        "gather_resid": neq * 8,
+    }
+
+
+def brick_cpu_sample(seconds=12.0):
+    from oracle import port
+    from xara_gb300 import configs
+    desc, _ = configs.brick_block(**BRICK_SAMPLE, steps=1)
+    o = port.OracleModel(desc)
+    U = brick_trial_field(desc, **BRICK_SAMPLE)
+    npts = desc.num_elems * 8
+    o.elem_state(U)
+    n, t0 = 0, time.perf_counter()
+    while time.perf_counter() - t0 < seconds:
+        o.elem_state(U)
+        n += 1
+    dt = time.perf_counter() - t0
+    s = BRICK_SAMPLE
+    return npts * n / dt, (f"brick J2 {s['nx']}x{s['ny']}x{s['nz']} ({desc.num_elems} "
+                           f"elements, {npts} points), {n} element phases")
+
+
+def _brick_worker(args):
+    seconds, = args
+    rate, _ = brick_cpu_sample(seconds)
+    return rate
+
+
+def run_reference_brick(args):
     rank = int(os.environ.get("RANK", "0"))
-    local = int(os.environ.get("LOCAL_RANK", "0"))
-    if world > 1:
-        # one replica per GPU: the element phase of one model does not shard
-        os.environ["CUDA_VISIBLE_DEVICES"] = str(local)
-    import torch
-    import torch.distributed as dist
-    if world > 1:
-        dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
-        torch.cuda.set_device(0)
+    if rank != 0:
+        return 0
+    import multiprocessing as mp
+    cores = os.cpu_count() or 1
+    per_step = 4.0
+    ctx = mp.get_context("spawn")
+    with ctx.Pool(cores) as pool:
+        for _ in range(args.warmup):
+            pool.map(_brick_worker, [(0.5,)] * cores)
+        t0 = time.perf_counter()
+        rates = []
+        for _ in range(args.steps):
+            rates.append(sum(pool.map(_brick_worker, [(per_step,)] * cores)))
+        wall = time.perf_counter() - t0
+    value = float(np.mean(rates))
+    npts = BRICK["nx"] * BRICK["ny"] * BRICK["nz"] * 8
+    s = BRICK_SAMPLE
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT,
+        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": 1e3 * npts / value, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded)",
+        "config": {"workload": "stdBrick J2 128x128x64 element phase (one Newton iteration)",
+                   "elements": npts // 8, "points": npts},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
+                         "sample": f"brick J2 {s['nx']}x{s['ny']}x{s['nz']} element phase, "
+                                   f"{cores} processes x {per_step:.0f} s per step"},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "wall_s": wall,
+    }
+    print(json.dumps(line))
+    return 0
 
+
+def run_brick(args):
+    world, rank, local, torch, dist = dist_setup()
     from xara_gb300 import configs, gpu
-    desc, _ = configs.brick_block(**WORKLOAD, steps=1)
+    desc, _ = configs.brick_block(**BRICK, steps=1)
     npts = desc.num_elems * 8
     t_setup = time.perf_counter()
     m = gpu.DeviceModel(desc)
+    m.set_system(gpu.XG_SYSTEM_BJPCG)
     t_setup = time.perf_counter() - t_setup
-    U = trial_field(desc, **WORKLOAD)
+    U = brick_trial_field(desc, **BRICK)
     m.set_trial_disp(U)
-    fp64_peak = C_double_probe()
+    fp64_peak = fp64_peak_probe()
+    stream = torch.cuda.ExternalStream(gpu.model_stream(m))
 
     def barrier():
         if world > 1:
@@ -251,30 +593,26 @@ def main():
     gpu.profile_enable(m, True)
     sampler = ClockSampler(local if world == 1 else 0)
     sampler.start()
+    ev0 = torch.cuda.Event(enable_timing=True)
+    ev1 = torch.cuda.Event(enable_timing=True)
     barrier()
-    t0 = time.perf_counter()
+    ev0.record(stream)
     for _ in range(args.steps):
         m.update(False, False)
+    ev1.record(stream)
     barrier()
-    dt = time.perf_counter() - t0
     clocks = sampler.stop()
+    dt = ev0.elapsed_time(ev1) * 1e-3
     prof = gpu.profile_read(m)
     gpu.profile_enable(m, False)
-    # max over ranks
-    if world > 1:
-        t = torch.tensor([dt], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        dt = float(t.item())
+    dt = max_over_ranks(dt, world, torch, dist)
     value = npts * args.steps * world / dt
 
-    # end to end through the C ABI with host buffers: trial displacements in
-    # from pinned host memory, the assembled resisting force back out
-    Uh = torch.from_numpy(U).pin_memory().numpy()
-    resid = torch.empty(m.neq, dtype=torch.float64).pin_memory().numpy()
+    Uh = torch.from_numpy(U).pin_memory()
+    resid = torch.empty(m.neq, dtype=torch.float64).pin_memory()
     L = gpu.lib()
-    import ctypes as C
-    ph = Uh.ctypes.data_as(C.c_void_p)
-    pr = resid.ctypes.data_as(C.c_void_p)
+    ph = C.c_void_p(Uh.data_ptr())
+    pr = C.c_void_p(resid.data_ptr())
     for _ in range(2):
         L.xg_elemset_set_trial_disp(m.h, ph)
         L.xg_elemset_update(m.h, None, pr)
@@ -284,19 +622,12 @@ def main():
         gpu._check(L.xg_elemset_set_trial_disp(m.h, ph))
         gpu._check(L.xg_elemset_update(m.h, None, pr))
     barrier()
-    dt_e2e = time.perf_counter() - t0
-    if world > 1:
-        t = torch.tensor([dt_e2e], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        dt_e2e = float(t.item())
+    dt_e2e = max_over_ranks(time.perf_counter() - t0, world, torch, dist)
     e2e_value = npts * args.steps * world / dt_e2e
-
     if rank != 0:
         dist.destroy_process_group()
         return 0
-
-    nn = desc.num_nodes
-    alg = algorithmic_bytes(npts, desc.num_elems, nn, m.nnz, m.neq)
+    alg = brick_alg_bytes(npts, desc.num_elems, desc.num_nodes, m.nnz, m.neq)
     kernels = {k: v for k, v in prof.items() if v[1] > 0 and k != "return_map_cap_hits"}
     dominant = max(kernels, key=lambda k: kernels[k][0])
     dom_ms, dom_launches = kernels[dominant]
@@ -305,39 +636,34 @@ def main():
         per_launch_s *= 2   # two kernels per gather launch group
     peak, peak_kind = measured_peaks()
     achieved = alg.get(dominant, alg["phase"]) / per_launch_s / 1e9
-    traffic = _ncu_traffic(dominant)
     phase_s = dt / args.steps
-    gpu_launches = sum(v[1] for v in kernels.values())
-    flops = flops_estimate(npts, desc.num_elems)
+    flops = npts * 700 + desc.num_elems * 36 * 8 * 64
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * phase_s,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f64", "data": "synthetic (seeded trial displacement field)",
-        "config": {"workload": f"stdBrick J2 {WORKLOAD['nx']}x{WORKLOAD['ny']}x{WORKLOAD['nz']} "
+        "config": {"workload": f"stdBrick J2 {BRICK['nx']}x{BRICK['ny']}x{BRICK['nz']} "
                                "element phase (one Newton iteration)",
                    "elements": desc.num_elems, "points": npts, "equations": m.neq,
                    "nnz": m.nnz, "parallelism": f"replicas x{world}",
                    "l2": "inputs larger than L2 (no flush needed)"},
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(U.nbytes),
-                "d2h_bytes_per_step": int(resid.nbytes)},
-        "gpu_launches": int(gpu_launches),
+                "d2h_bytes_per_step": int(resid.numel() * 8)},
+        "gpu_launches": int(sum(v[1] for v in kernels.values())),
         "roofline": {"bound": "hbm", "kernel": dominant, "achieved": achieved, "peak": peak,
                      "unit": "GB/s", "frac": achieved / peak if peak else None,
-                     "peak_source": peak_kind, "traffic": traffic,
+                     "peak_source": peak_kind, "traffic": ncu_traffic("brick", dominant),
                      "algorithmic_bytes_per_launch": alg.get(dominant, alg["phase"])},
-        "phase_roofline": {"algorithmic_bytes": alg["phase"],
-                           "achieved_gbs": alg["phase"] / phase_s / 1e9},
         "fp64": {"est_flops_per_step": flops, "achieved_tflops": flops / phase_s / 1e12,
                  "peak_tflops_probe": fp64_peak,
                  "frac": (flops / phase_s / 1e12) / fp64_peak if fp64_peak else None},
         "kernels_ms_per_step": {k: v[0] / args.steps for k, v in kernels.items()},
-        "return_map_cap_hits": prof.get("return_map_cap_hits", (0, 0))[1],
         "clocks": clocks,
         "setup_s": t_setup,
     }
     if not args.no_cpu_baseline:
-        rate, sample = cpu_baseline_sample()
+        rate, sample = brick_cpu_sample()
         line["cpu_baseline"] = {"value": rate, "unit": UNIT, "cores": 1, "kind": "port",
                                 "sample": sample}
     print(json.dumps(line))
@@ -346,25 +672,23 @@ def main():
     return 0
 
 
-def C_double_probe():
-    import ctypes as C
-    from xara_gb300 import gpu
-    L = gpu.lib()
-    v = C.c_double()
-    L.xg_measure_fp64_peak.argtypes = [C.POINTER(C.c_double)]
-    if L.xg_measure_fp64_peak(C.byref(v)) != 0:
-        return None
-    return v.value
-
-
-def _ncu_traffic(kernel):
-    """DRAM bytes per launch of the kernel from the committed ncu summary."""
-    p = os.path.join(ROOT, "profiles", "dram_traffic.json")
-    if not os.path.exists(p):
-        return None
-    with open(p) as f:
-        d = json.load(f)
-    return d.get(kernel)
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--workload", default="frame3d", choices=["frame3d", "brick"])
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="xara", choices=["xara", "reference"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-analysis", action="store_true")
+    ap.add_argument("--analysis-steps", type=int, default=5)
+    ap.add_argument("--cpu-seconds", type=float, default=12.0)
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3)
+    if args.impl == "reference":
+        return run_reference_frame(args) if args.workload == "frame3d" else \
+            run_reference_brick(args)
+    return run_frame(args) if args.workload == "frame3d" else run_brick(args)
 
 
 if __name__ == "__main__":

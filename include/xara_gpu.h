@@ -261,6 +261,13 @@ int xg_analysis_set_system(xg_model *m, int system);
 int xg_soe_solve(xg_model *m, const double *b, double *x,
                  double rtol, int maxit, int *iters, double *relres);
 
+/* Device-pointer forms for callers whose vectors already live on the GPU
+   (no host copies, ordered on the model's stream): u_dev [num_nodes*ndf];
+   b_dev, x_dev [num_eqn]. */
+int xg_elemset_set_trial_disp_device(xg_model *m, const double *u_dev);
+int xg_soe_solve_device(xg_model *m, const double *b_dev, double *x_dev,
+                        double rtol, int maxit, int *iters, double *relres);
+
 /* ---- NewtonRaphson::solveCurrentStep (analysis/algorithm/equiSolnAlgo/
         NewtonRaphson.cpp:125-222) with its integrator and convergence test,
         all resident on the device ---- */
@@ -283,6 +290,17 @@ int xg_profile_enable(xg_model *m, int enable);
    iteration cap in the last update (in `launches`).  Returns XG_EINVAL past
    the end. */
 int xg_profile_get(const xg_model *m, int k, char *name, int cap, double *ms, long *launches);
+
+/* The CUDA stream (a cudaStream_t) every kernel of the model runs on, for
+   callers that time or order their own work against it. */
+int xg_model_stream(const xg_model *m, void **stream);
+
+/* Work counters since xg_profile_enable: material-point state
+   determinations (J2 points; for frames every fiber of every section in
+   every compatibility iteration), section state determinations (frames)
+   and element state determinations. */
+int xg_profile_counters(xg_model *m, long long *point_updates, long long *section_updates,
+                        long long *element_updates);
 
 /* FP64 FMA throughput of the current device in TFLOP/s (a short probe
    kernel with no memory traffic), the ceiling of the FP64 element kernels. */

@@ -52,6 +52,8 @@ def lib():
         L.xo_elem_state.argtypes = [vp, vp, vp, vp]
         L.xo_commit.argtypes = [vp]
         L.xo_revert.argtypes = [vp]
+        L.xo_work.argtypes = [vp, vp, vp]
+        L.xo_soe_solve.argtypes = [vp, vp, vp]
         L.xo_run_phase.argtypes = [vp, vp, vp, vp, vp]
         L.xo_times.argtypes = [vp, vp, vp]
         L.xo_history.argtypes = [vp, vp, vp]
@@ -115,6 +117,21 @@ class OracleModel:
 
     def revert(self):
         lib().xo_revert(self.h)
+
+    def work(self):
+        """(material-point updates, section updates) so far."""
+        a, b = C.c_longlong(), C.c_longlong()
+        lib().xo_work(self.h, C.byref(a), C.byref(b))
+        return a.value, b.value
+
+    def soe_solve(self, b):
+        """ProfileSPD solve with the tangent of the last element update."""
+        b = np.ascontiguousarray(b, np.float64)
+        x = np.zeros_like(b)
+        r = lib().xo_soe_solve(self.h, _p(b), _p(x))
+        if r != 0:
+            raise RuntimeError(f"skyline solve failed: {r}")
+        return x
 
     def run(self, phases):
         L = lib()

@@ -425,6 +425,7 @@ typedef struct xo_model {
   double *fr_fh_c, *fr_fh_t;         /* fiber records                       */
   double *fr_Se, *fr_kv, *fr_Se_c, *fr_kv_c, *fr_vs, *fr_vs_c, *fr_fs, *fr_Ssr, *fr_vlast;
   int *fr_init;
+  long long work_pts, work_fib, work_sec;   /* work counters (benchmarks) */
 } xo_model;
 
 static int csr_find(const struct xo_model *m, int row, int col);
@@ -724,7 +725,18 @@ int xo_elem_update_flag(xo_model *m, int compute) {
   return -bad;
 }
 
-int xo_elem_update(xo_model *m) { return xo_elem_update_flag(m, 1); }
+int xo_elem_update(xo_model *m) {
+  if (m->d.elem_type == XG_ELE_QUAD || m->d.elem_type == XG_ELE_BRICK)
+    m->work_pts += (long long)m->d.num_elems * m->nip;
+  return xo_elem_update_flag(m, 1);
+}
+
+/* Work counters: material-point updates (J2 points, or fibers per
+   compatibility iteration) and section updates. */
+void xo_work(const xo_model *m, long long *points, long long *sections) {
+  *points = m->work_pts + m->work_fib;
+  *sections = m->work_sec;
+}
 
 /* Replay entry for tests: state from committed history + U, no commit. */
 int xo_elem_state(xo_model *m, const double *U, double *vals, double *resid) {
@@ -804,6 +816,10 @@ static int xo_skyline_solve(xo_model *m, const double *b, double *x) {
   }
   return 0;
 }
+
+/* ProfileSPD factor + solve of the tangent assembled by the last element
+   update (benchmarks and tests). */
+int xo_soe_solve(xo_model *m, const double *b, double *x) { return xo_skyline_solve(m, b, x); }
 
 /* Load factor of pattern p: a LinearSeries pattern follows the domain time
    until `loadConst` freezes it (domain/pattern/LoadPattern.cpp:setLoadConstant). */

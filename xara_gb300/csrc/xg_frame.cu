@@ -397,6 +397,7 @@ __global__ void __launch_bounds__(32 * kFbcWarps) k_fbc_update(FrameView v) {
   // the subdivision count); a kernel must end, so an element that needs more
   // than kFbcMaxRounds rounds reports a failed state determination.
   int rounds = 0;
+  unsigned long long nj = 0;   // compatibility iterations (each visits every section)
   while (!converged && numSub <= maxSub && ++rounds <= kFbcMaxRounds) {
     bool partial = false;
     for (int l = 0; l < 3 && !partial && !converged; l++) {
@@ -420,6 +421,7 @@ __global__ void __launch_bounds__(32 * kFbcWarps) k_fbc_update(FrameView v) {
       __syncwarp();
       const int numIters = (l == 1) ? 10 * v.max_iters : v.max_iters;
       for (int j = 0; j < numIters; j++) {
+        nj++;
         double f[NB * NB], vr[NB];
 #pragma unroll
         for (int i = 0; i < NB * NB; i++) f[i] = 0.0;
@@ -548,6 +550,10 @@ __global__ void __launch_bounds__(32 * kFbcWarps) k_fbc_update(FrameView v) {
         }
       }
     }
+  }
+  if (lane == 0 && v.work) {
+    atomicAdd(v.work, nj * (unsigned long long)(nip * nf));
+    atomicAdd(v.work + 1, nj * (unsigned long long)nip);
   }
   if (!converged) {
     if (lane == 0) atomicAdd(v.nfail, 1);

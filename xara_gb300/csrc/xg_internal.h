@@ -141,6 +141,7 @@ struct FrameView {
   double xi[10], wt[10];      // Lobatto locations and weights
   int *nfail;                 // elements whose compatibility iteration failed
   double *Ke, *Re;            // element tangent / force scratch
+  unsigned long long *work;   // [2] fiber and section state determinations
 };
 int frame_state_stride(int nip);
 int launch_fbc_update(const FrameView &v, cudaStream_t s);

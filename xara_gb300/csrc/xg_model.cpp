@@ -259,6 +259,8 @@ struct xg_model {
   DBuf<long> d_foff;
   DBuf<double> d_fL, d_fR, d_fy, d_fz, d_fA, d_ybar, d_zbar, d_GJ, d_fs0, d_uparam;
   DBuf<double> d_fh_c, d_fh_t, d_st, d_st_c;
+  DBuf<unsigned long long> d_work;        // frame work counters
+  long long point_updates = 0, elem_updates = 0;   // continuum work counters
   std::vector<double> fh_init;
   std::vector<double> crd_vecxz;
   double lob_xi[10] = {0}, lob_wt[10] = {0};
@@ -271,7 +273,7 @@ struct xg_model {
     v.utype = d_utype.p; v.uparam = d_uparam.p; v.foff = d_foff.p; v.fh_c = d_fh_c.p;
     v.fh_t = d_fh_t.p; v.st = d_st.p; v.max_iters = fb_max_iters; v.tol = fb_tol;
     for (int i = 0; i < 10; i++) { v.xi[i] = lob_xi[i]; v.wt[i] = lob_wt[i]; }
-    v.nfail = d_nfail.p; v.Ke = d_Ke.p; v.Re = d_Re.p;
+    v.nfail = d_nfail.p; v.Ke = d_Ke.p; v.Re = d_Re.p; v.work = d_work.p;
     return v;
   }
   int upload_frames();
@@ -792,6 +794,8 @@ int xg_model::upload_frames() {
   RET(d_utype.upload(utype.data(), utype.size(), s));
   RET(d_uparam.upload(uparam.data(), uparam.size(), s));
   RET(d_foff.upload(foff.data(), foff.size(), s));
+  RET(d_work.alloc(2));
+  CK(cudaMemsetAsync(d_work.p, 0, 2 * sizeof(unsigned long long), s));
   RET(d_fh_c.upload(fh_init.data(), fh_init.size(), s));
   RET(d_fh_t.upload(fh_init.data(), fh_init.size(), s));
   const size_t nst = (size_t)ne * frame_state_stride(fb_nip);
@@ -818,6 +822,7 @@ int xg_model::element_state(bool compute) {
     if (compute) {
       CK(cudaMemsetAsync(d_nfail.p, 0, sizeof(int), s));
       prof_begin(P_UPDATE);
+      elem_updates += ne;
       RET(launch_fbc_update(fv, s));
       prof_end(P_UPDATE, 1);
     }
@@ -828,6 +833,8 @@ int xg_model::element_state(bool compute) {
     if (compute) {
       CK(cudaMemsetAsync(d_nfail.p, 0, sizeof(int), s));
       prof_begin(P_UPDATE);
+      point_updates += (long long)npts();
+      elem_updates += ne;
       RET(etype == XG_ELE_QUAD ? launch_quad_update(v, s) : launch_brick_update(v, s));
       prof_end(P_UPDATE, 1);
     }
@@ -1284,6 +1291,13 @@ int xg_elemset_set_trial_disp(xg_model *m, const double *u) {
   return 0;
 }
 
+int xg_elemset_set_trial_disp_device(xg_model *m, const double *u_dev) {
+  if (!m || !u_dev) return fail(XG_EINVAL, "null argument");
+  CK(cudaMemcpyAsync(m->d_U.p, u_dev, (size_t)m->nn * m->ndf * sizeof(double),
+                     cudaMemcpyDeviceToDevice, m->stream));
+  return 0;
+}
+
 int xg_elemset_update(xg_model *m, double *csr_vals, double *resid) {
   if (!m) return fail(XG_EINVAL, "null model");
   RET(m->element_state(true));
@@ -1306,6 +1320,31 @@ int xg_profile_enable(xg_model *m, int enable) {
   if (!m) return fail(XG_EINVAL, "null model");
   m->prof_on = enable != 0;
   for (auto &p : m->prof) { p.ms = 0.0; p.launches = 0; }
+  m->point_updates = m->elem_updates = 0;
+  if (m->d_work.p) CK(cudaMemsetAsync(m->d_work.p, 0, 2 * sizeof(unsigned long long), m->stream));
+  return 0;
+}
+
+int xg_model_stream(const xg_model *m, void **stream) {
+  if (!m || !stream) return fail(XG_EINVAL, "null argument");
+  *stream = (void *)m->stream;
+  return 0;
+}
+
+int xg_profile_counters(xg_model *m, long long *point_updates, long long *section_updates,
+                        long long *element_updates) {
+  if (!m) return fail(XG_EINVAL, "null model");
+  long long pu = m->point_updates, su = 0;
+  if (m->frames() && m->d_work.p) {
+    unsigned long long w[2] = {0, 0};
+    CK(cudaMemcpyAsync(w, m->d_work.p, sizeof w, cudaMemcpyDeviceToHost, m->stream));
+    CK(cudaStreamSynchronize(m->stream));
+    pu = (long long)w[0];
+    su = (long long)w[1];
+  }
+  if (point_updates) *point_updates = pu;
+  if (section_updates) *section_updates = su;
+  if (element_updates) *element_updates = m->elem_updates;
   return 0;
 }
 
@@ -1392,6 +1431,30 @@ int xg_soe_solve(xg_model *m, const double *b, double *x, double rtol, int maxit
   if (relres) *relres = rr;
   CK(cudaMemcpyAsync(x, m->d_x.p, (size_t)m->neq * sizeof(double), cudaMemcpyDeviceToHost, m->stream));
   CK(cudaStreamSynchronize(m->stream));
+  if (r) return fail(XG_ESOLVE, "PCG: %d iterations, relative residual %.3e", it, rr);
+  return 0;
+}
+
+int xg_soe_solve_device(xg_model *m, const double *b_dev, double *x_dev, double rtol, int maxit,
+                        int *iters, double *relres) {
+  if (!m || !b_dev || !x_dev) return fail(XG_EINVAL, "null argument");
+  if (m->system == XG_SYSTEM_PROFILE_SPD) {
+    RET(m->solve_profile(1, &b_dev, &x_dev));
+    CK(cudaStreamSynchronize(m->stream));
+    if (iters) *iters = 0;
+    if (relres) *relres = 0.0;
+    return 0;
+  }
+  if (!m->blocks_factored) {
+    RET(pcg_factor_blocks(m->pcg, m->stream));
+    m->blocks_factored = true;
+  }
+  CK(cudaMemsetAsync(x_dev, 0, (size_t)std::max(m->neq, 1) * sizeof(double), m->stream));
+  int it = 0;
+  double rr = 0.0;
+  const int r = pcg_solve(m->pcg, b_dev, x_dev, rtol, maxit, &it, &rr, m->stream);
+  if (iters) *iters = it;
+  if (relres) *relres = rr;
   if (r) return fail(XG_ESOLVE, "PCG: %d iterations, relative residual %.3e", it, rr);
   return 0;
 }

@@ -235,6 +235,24 @@ def profile_enable(model, on=True):
     _check(lib().xg_profile_enable(model.h, 1 if on else 0))
 
 
+def model_stream(model):
+    """The model's CUDA stream as an integer handle (cudaStream_t)."""
+    L = lib()
+    L.xg_model_stream.argtypes = [C.c_void_p, C.POINTER(C.c_void_p)]
+    p = C.c_void_p()
+    _check(L.xg_model_stream(model.h, C.byref(p)))
+    return p.value or 0
+
+
+def profile_counters(model):
+    """(point updates, section updates, element updates) since enabling."""
+    L = lib()
+    L.xg_profile_counters.argtypes = [C.c_void_p] + [C.POINTER(C.c_longlong)] * 3
+    a, b, c = C.c_longlong(), C.c_longlong(), C.c_longlong()
+    _check(L.xg_profile_counters(model.h, C.byref(a), C.byref(b), C.byref(c)))
+    return a.value, b.value, c.value
+
+
 def profile_read(model):
     """{kernel group: (milliseconds, launches)} accumulated since enabling."""
     L = lib()
