@@ -178,15 +178,6 @@ __device__ void concrete02_trial(const double *q, const double *hc, double eps, 
   ht[9] = sig;
 }
 
-// UniaxialMaterial::setTrial (material/uniaxial/UniaxialMaterial.cpp:70-81)
-__device__ __forceinline__ void uni_trial(int type, const double *q, const double *hc, double eps,
-                                          double *ht, double &sig, double &tan) {
-  if (type == XG_UNI_STEEL02) steel02_trial(q, hc, eps, ht);
-  else if (type == XG_UNI_CONCRETE02) concrete02_trial(q, hc, eps, ht);
-  else { ht[10] = eps; ht[9] = q[0] * eps; ht[8] = q[0]; }
-  sig = ht[9];
-  tan = ht[8];
-}
 
 // ---------------------------------------------------------------------------
 // small dense helpers (every lane of a warp runs them on the same data)
@@ -231,6 +222,70 @@ __device__ void inv_gj(const double *A, double *Ainv) {
   for (int i = 0; i < N; i++)
 #pragma unroll
     for (int j = 0; j < N; j++) Ainv[i * N + j] = M[i][N + j];
+}
+
+// 3x3 inverse by cofactors (the reference's cmx_inv3, matrix/routines/
+// invGL3.c, is the same closed form); A and Ai row major with leading
+// dimension lda.
+__device__ __forceinline__ void inv3_cof(const double *A, int lda, double *Ai, int ldi) {
+  const double a00 = A[0], a01 = A[1], a02 = A[2];
+  const double a10 = A[lda], a11 = A[lda + 1], a12 = A[lda + 2];
+  const double a20 = A[2 * lda], a21 = A[2 * lda + 1], a22 = A[2 * lda + 2];
+  const double c00 = a11 * a22 - a12 * a21, c01 = a12 * a20 - a10 * a22;
+  const double c02 = a10 * a21 - a11 * a20;
+  const double det = a00 * c00 + a01 * c01 + a02 * c02;
+  const double id = 1.0 / det;
+  Ai[0] = c00 * id;
+  Ai[1] = (a02 * a21 - a01 * a22) * id;
+  Ai[2] = (a01 * a12 - a02 * a11) * id;
+  Ai[ldi] = c01 * id;
+  Ai[ldi + 1] = (a00 * a22 - a02 * a20) * id;
+  Ai[ldi + 2] = (a02 * a10 - a00 * a12) * id;
+  Ai[2 * ldi] = c02 * id;
+  Ai[2 * ldi + 1] = (a01 * a20 - a00 * a21) * id;
+  Ai[2 * ldi + 2] = (a00 * a11 - a01 * a10) * id;
+}
+
+// Section flexibility: 2x2 closed form, or (3D) the 3x3 axial-bending block
+// by cofactors with the uncoupled elastic torsion 1/GJ.
+template <int ORD>
+__device__ __forceinline__ void sec_inverse(const double *ks, double *fs) {
+  if (ORD == 2) {
+    const double id = 1.0 / (ks[0] * ks[3] - ks[1] * ks[2]);
+    fs[0] = ks[3] * id;
+    fs[1] = -ks[1] * id;
+    fs[2] = -ks[2] * id;
+    fs[3] = ks[0] * id;
+  } else {
+    inv3_cof(ks, 4, fs, 4);
+    fs[3] = fs[7] = fs[11] = fs[12] = fs[13] = fs[14] = 0.0;
+    fs[15] = 1.0 / ks[15];
+  }
+}
+
+// Element stiffness kv = f^-1: 3x3 cofactors (2D); in 3D the torsion row
+// and column of f are uncoupled (every section's T is), so the 5x5
+// axial-bending block is inverted by Gauss-Jordan and kv(5,5) = 1/f(5,5).
+template <int NB>
+__device__ __forceinline__ void elem_inverse(const double *f, double *kv) {
+  if (NB == 3) {
+    inv3_cof(f, 3, kv, 3);
+  } else {
+    double a[25], ai[25];
+#pragma unroll
+    for (int i = 0; i < 5; i++)
+#pragma unroll
+      for (int j = 0; j < 5; j++) a[i * 5 + j] = f[i * 6 + j];
+    inv_gj<5>(a, ai);
+#pragma unroll
+    for (int i = 0; i < 5; i++) {
+#pragma unroll
+      for (int j = 0; j < 5; j++) kv[i * 6 + j] = ai[i * 5 + j];
+      kv[i * 6 + 5] = 0.0;
+      kv[30 + i] = 0.0;
+    }
+    kv[35] = 1.0 / f[35];
+  }
 }
 
 __device__ __forceinline__ double warp_sum(double v) {
@@ -299,15 +354,41 @@ __device__ __forceinline__ void fbc_section(const FrameView &v, int f0, int nf, 
       z = v.fz[kf] - zbar;
       strain += z * vsec[2];
     }
+    // material state from the committed record and the trial strain; only
+    // the fields a law reads are loaded and only those it sets are stored
     const double *hc = v.fh_c + rec0 + 12L * fi;
     double *ht = v.fh_t + rec0 + 12L * fi;
-    double hcl[12], htl[12];
-#pragma unroll
-    for (int c = 0; c < 11; c++) { hcl[c] = hc[c]; htl[c] = ht[c]; }
+    const double *q = v.uparam + (long)u * XG_UNI_NPARAM;
+    const int type = v.utype[u];
     double stress, tangent;
-    uni_trial(v.utype[u], v.uparam + (long)u * XG_UNI_NPARAM, hcl, strain, htl, stress, tangent);
+    if (type == XG_UNI_STEEL02) {
+      double hcl[11], htl[11];
 #pragma unroll
-    for (int c = 0; c < 11; c++) ht[c] = htl[c];
+      for (int c = 0; c < 11; c++) hcl[c] = c == 8 ? 0.0 : hc[c];
+      steel02_trial(q, hcl, strain, htl);
+#pragma unroll
+      for (int c = 0; c < 11; c++) ht[c] = htl[c];
+      stress = htl[9];
+      tangent = htl[8];
+    } else if (type == XG_UNI_CONCRETE02) {
+      double hcl[11], htl[11];
+      hcl[0] = hc[0]; hcl[1] = hc[1]; hcl[9] = hc[9]; hcl[10] = hc[10];
+      if (fabs(strain - hcl[10]) < kDblEps) {
+        // Concrete02.cpp:182-183: the previous trial stress and tangent stay
+        ht[0] = hcl[0]; ht[1] = hcl[1]; ht[10] = strain;
+        stress = ht[9];
+        tangent = ht[8];
+      } else {
+        concrete02_trial(q, hcl, strain, htl);
+        ht[0] = htl[0]; ht[1] = htl[1]; ht[8] = htl[8]; ht[9] = htl[9]; ht[10] = htl[10];
+        stress = htl[9];
+        tangent = htl[8];
+      }
+    } else {
+      stress = q[0] * strain;
+      tangent = q[0];
+      ht[8] = tangent; ht[9] = stress; ht[10] = strain;
+    }
     if (ORD == 2) {
       const double ks0 = tangent * A, ks1 = ks0 * -y;
       k0 += ks0; k1 += ks1; k5 += ks1 * -y;
@@ -454,7 +535,7 @@ __global__ void __launch_bounds__(32 * kFbcWarps) k_fbc_update(FrameView v) {
           fbc_section<ORD>(v, f0, nf, ybar, zbar, GJ, (fbase + (long)ip * nf) * 12, lane, vsec,
                            ks, Ssr);
           double fsec[ORD * ORD];
-          inv_gj<ORD>(ks, fsec);
+          sec_inverse<ORD>(ks, fsec);
 #pragma unroll
           for (int r = 0; r < ORD; r++) {
             S.vsS[ip][r] = vsec[r];
@@ -470,38 +551,22 @@ __global__ void __launch_bounds__(32 * kFbcWarps) k_fbc_update(FrameView v) {
             for (int k = 0; k < ORD; k++) t += fsec[r * ORD + k] * dSs[k];
             dvs[r] = t + vsec[r];
           }
-          // f += b' fs b wL ; vr += b' (vs + dvs) wL, b from the codes
-          double bm[ORD][NB];
-#pragma unroll
-          for (int r = 0; r < ORD; r++)
-#pragma unroll
-            for (int c = 0; c < NB; c++) bm[r][c] = 0.0;
-          bm[0][0] = 1.0;
-          bm[1][1] = xL1; bm[1][2] = xL;
-          if (ORD == 4) { bm[2][3] = xL1; bm[2][4] = xL; bm[3][5] = 1.0; }
+          // f += b' fs b wL ; vr += b' (vs + dvs) wL.  Each column a of the
+          // force interpolation b has one entry: row kRow[a], value ca[a]
+          // (ForceBeamColumn3d::getForceInterpolatMatrix, :1068-1110).
+          constexpr int kRow[6] = {0, 1, 1, 2, 2, 3};
+          const double ca[6] = {1.0, xL1, xL, xL1, xL, 1.0};
 #pragma unroll
           for (int a = 0; a < NB; a++) {
+            const double wa = ca[a] * wtL;
 #pragma unroll
-            for (int c = 0; c < NB; c++) {
-              double t = 0.0;
-#pragma unroll
-              for (int r = 0; r < ORD; r++) {
-                if (bm[r][a] == 0.0) continue;
-                double u = 0.0;
-#pragma unroll
-                for (int k = 0; k < ORD; k++) u += fsec[r * ORD + k] * bm[k][c];
-                t += bm[r][a] * u;
-              }
-              f[a * NB + c] += t * wtL;
-            }
-            double t = 0.0;
-#pragma unroll
-            for (int r = 0; r < ORD; r++) t += bm[r][a] * dvs[r];
-            vr[a] += t * wtL;
+            for (int c = 0; c < NB; c++)
+              f[a * NB + c] += wa * (fsec[kRow[a] * ORD + kRow[c]] * ca[c]);
+            vr[a] += wa * dvs[kRow[a]];
           }
         }
         double kvT[NB * NB];
-        inv_gj<NB>(f, kvT);
+        elem_inverse<NB>(f, kvT);
         double dvv[NB], dW = 0.0;
 #pragma unroll
         for (int i = 0; i < NB; i++) dvv[i] = vin[i] + dvTrial[i] - vr[i];
