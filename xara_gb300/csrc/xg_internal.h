@@ -85,18 +85,21 @@ struct ProfileSystem {
   const double *vals;
   const int *ftile;        // [nt] first tile column of each tile row
   double *L;               // [nt*(W+1)*1024] factor tiles
-  double *Wt;              // [max(W,1)*1024] panel scratch
-  double *invD;            // [nt*32] reciprocal pivots
-  unsigned int *barrier;   // [2]
+  double *invD, *piv;      // [nt*32] reciprocal pivots, pivots
+  const int4 *tasks;       // [ntasks] factor tasks (type, I, K, J) in dataflow order
+  int ntasks;
+  int *next_task;          // [1] task counter
+  int *upd, *done;         // [nt*(W+1)] per tile: updates applied, factored
   int *flags;              // [4]
   double min_diag_tol;
 };
 int profile_plan(int n, const int *rowptr, const int *colidx, std::vector<int> &ftile, int &nt,
                  int &W);
+void profile_tasks(int nt, int W, const std::vector<int> &ftile, std::vector<int> &tasks);
 size_t profile_tile_doubles(int nt, int W);
 int profile_tile_edge();
 // Factor the CSR values into the tiles.  XG_ESOLVE on a failed pivot check
-// (*bad_eq = the equation) or a barrier timeout (*bad_eq = -1).
+// (*bad_eq = the equation) or a dependency wait that timed out (*bad_eq = -1).
 int profile_factor(const ProfileSystem &S, cudaStream_t s, int *bad_eq);
 // Solve in place: x[r*ldx + i] holds right-hand side r on entry (ldx >=
 // nt*32, entries past n zero), the solution on return; nrhs <= 4.

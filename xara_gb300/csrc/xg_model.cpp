@@ -164,9 +164,8 @@ struct xg_model {
   ProfileSystem psys{};
   bool prof_ready = false, prof_factored = false;
   std::vector<int> ftile;
-  DBuf<int> d_ftile, d_pflags;
-  DBuf<unsigned int> d_pbarrier;
-  DBuf<double> d_L, d_Wt, d_invD, d_px;
+  DBuf<int> d_ftile, d_pflags, d_ptasks, d_pnext, d_pupd, d_pdone;
+  DBuf<double> d_L, d_invD, d_piv, d_px;
   int prof_ldx = 0;
   int ensure_profile();
   int solve_profile(int nrhs, const double *const *b, double *const *x);
@@ -865,19 +864,27 @@ int xg_model::ensure_profile() {
   if ((tiles + (size_t)nt * 32 * 6) * sizeof(double) > free_b / 2)
     return fail(XG_ENOMEM, "ProfileSPD envelope needs %.1f GB (%d tile rows x %d): use the "
                 "block-Jacobi PCG system", tiles * 8e-9, nt, W + 1);
+  std::vector<int> tasks;
+  profile_tasks(nt, W, ftile, tasks);
   RET(d_ftile.upload(ftile.data(), ftile.size(), stream));
+  RET(d_ptasks.upload(tasks.data(), tasks.size(), stream));
   RET(d_L.alloc(tiles));
-  RET(d_Wt.alloc((size_t)std::max(W, 1) * 1024));
   RET(d_invD.alloc((size_t)nt * 32));
+  RET(d_piv.alloc((size_t)nt * 32));
   prof_ldx = nt * 32;
   RET(d_px.alloc((size_t)prof_ldx * 4));
   CK(cudaMemsetAsync(d_px.p, 0, (size_t)prof_ldx * 4 * sizeof(double), stream));
-  RET(d_pbarrier.alloc(2));
+  RET(d_pnext.alloc(1));
+  RET(d_pupd.alloc((size_t)nt * (W + 1)));
+  RET(d_pdone.alloc((size_t)nt * (W + 1)));
   RET(d_pflags.alloc(4));
   psys.n = neq; psys.nt = nt; psys.W = W;
   psys.rowptr = d_rowptr.p; psys.colidx = d_colidx.p; psys.vals = d_vals.p;
-  psys.ftile = d_ftile.p; psys.L = d_L.p; psys.Wt = d_Wt.p; psys.invD = d_invD.p;
-  psys.barrier = d_pbarrier.p; psys.flags = d_pflags.p;
+  psys.ftile = d_ftile.p; psys.L = d_L.p; psys.invD = d_invD.p; psys.piv = d_piv.p;
+  psys.tasks = reinterpret_cast<const int4 *>(d_ptasks.p);
+  psys.ntasks = (int)(tasks.size() / 4);
+  psys.next_task = d_pnext.p; psys.upd = d_pupd.p; psys.done = d_pdone.p;
+  psys.flags = d_pflags.p;
   psys.min_diag_tol = 1.0e-12;   // ProfileSPDLinDirectSolver.h:49 default
   prof_ready = true;
   return 0;

@@ -14,11 +14,16 @@
 //   B  every tile below it becomes W_IJ = A_IJ L_JJ^-T (kept in a scratch
 //      slot) and L_IJ = W_IJ D^-1 (stored in place);
 //   C  every trailing tile pair loses W_IJ L_KJ' (one 32^3 product each).
-// One cooperative launch runs all columns; phases meet at a grid barrier
-// whose wait is bounded by the global timer.  The block that updates the
-// next diagonal tile in phase C factors it right away, so a column costs
-// two barriers.  Pivot checks follow the reference: the first pivot must be
-// positive, later ones only non-zero and above minDiagTol in magnitude.
+// The tasks (A: diagonal, B: panel tile, C: tile pair of one column) run as
+// a dataflow: one persistent launch whose blocks take tasks from a list in a
+// fixed order -- for column J: A(J), B(., J), the C tasks of column J-1 that
+// reach columns J+1 and beyond, then the C tasks of column J that reach
+// column J+1 -- and wait (bounded by the global timer) on per-tile counters
+// for the tasks each one depends on.  Every dependency sits earlier in the
+// list, so the look-ahead is built in: column J+1's diagonal and panels run
+// while the rest of column J's trailing update is still going.  C recovers
+// W_IJ as L_IJ D_J.  Pivot checks follow the reference: the first pivot must
+// be positive, later ones only non-zero and above minDiagTol in magnitude.
 //
 // The substitutions stream the tiles through one block: every step reads
 // one tile row (forward) or tile column (backward), accumulates it against
@@ -27,6 +32,7 @@
 #include <cooperative_groups.h>
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cmath>
 #include <cstdint>
 
@@ -46,36 +52,6 @@ __device__ __forceinline__ unsigned long long global_ns() {
   unsigned long long t;
   asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
   return t;
-}
-
-// Sense-reversing grid barrier: bar[0] arrivals, bar[1] generation.  Returns
-// false on timeout (flags[0] = 2) or when a block raised flags[0].
-__device__ bool prof_barrier(unsigned int *bar, volatile int *flags) {
-  __syncthreads();
-  __shared__ int ok;
-  if (threadIdx.x == 0) {
-    ok = 1;
-    volatile unsigned int *vgen = bar + 1;
-    const unsigned int gen = *vgen;
-    __threadfence();
-    const unsigned int arrived = atomicAdd(bar, 1u);
-    if (arrived == gridDim.x - 1) {
-      atomicExch(bar, 0u);
-      __threadfence();
-      atomicAdd(bar + 1, 1u);
-    } else {
-      const unsigned long long t0 = global_ns();
-      while (*vgen == gen) {
-        if (flags[0] != 0) { ok = 0; break; }
-        if (global_ns() - t0 > kBarrierTimeoutNs) { flags[0] = 2; ok = 0; break; }
-        __nanosleep(32);
-      }
-    }
-    __threadfence();
-    if (flags[0] != 0) ok = 0;
-  }
-  __syncthreads();
-  return ok != 0;
 }
 
 __device__ __forceinline__ double *tile_at(const ProfileSystem &S, int I, int o) {
@@ -107,7 +83,7 @@ __global__ void k_prof_fill(ProfileSystem S) {
 __device__ bool factor_diag(const ProfileSystem &S, int J, double (*sA)[kT + 1], double *col,
                             volatile int *flags) {
   double *g = tile_at(S, J, 0);
-  for (int k = threadIdx.x; k < kTT; k += blockDim.x) sA[k / kT][k % kT] = g[k];
+  for (int k = threadIdx.x; k < kTT; k += blockDim.x) sA[k / kT][k % kT] = __ldcg(g + k);
   __syncthreads();
   __shared__ int bad;
   if (threadIdx.x == 0) bad = 0;
@@ -133,7 +109,10 @@ __device__ bool factor_diag(const ProfileSystem &S, int J, double (*sA)[kT + 1],
       if (s <= r) sA[r][s] -= (col[r] * inv) * col[s];
     }
     for (int r = c + 1 + threadIdx.x; r < kT; r += blockDim.x) sA[r][c] = col[r] * inv;
-    if (threadIdx.x == 0) S.invD[eq] = inv;
+    if (threadIdx.x == 0) {
+      S.invD[eq] = inv;
+      S.piv[eq] = d;
+    }
     __syncthreads();
   }
   for (int k = threadIdx.x; k < kTT; k += blockDim.x) g[k] = sA[k / kT][k % kT];
@@ -149,8 +128,8 @@ __device__ void panel_solve(const ProfileSystem &S, int J, int o, double (*sA)[k
   const double *Ljj = tile_at(S, J, 0);
   double *g = tile_at(S, J + o, o);
   for (int k = threadIdx.x; k < kTT; k += blockDim.x) {
-    sB[k / kT][k % kT] = Ljj[k];
-    sA[k / kT][k % kT] = g[k];
+    sB[k / kT][k % kT] = __ldcg(Ljj + k);
+    sA[k / kT][k % kT] = __ldcg(g + k);
   }
   __syncthreads();
   {
@@ -166,24 +145,21 @@ __device__ void panel_solve(const ProfileSystem &S, int J, int o, double (*sA)[k
     }
   }
   __syncthreads();
-  double *wt = S.Wt + (size_t)(o - 1) * kTT;
   const double *invD = S.invD + (size_t)J * kT;
-  for (int k = threadIdx.x; k < kTT; k += blockDim.x) {
-    const double w = sA[k / kT][k % kT];
-    wt[k] = w;
-    g[k] = w * invD[k % kT];
-  }
+  for (int k = threadIdx.x; k < kTT; k += blockDim.x)
+    g[k] = sA[k / kT][k % kT] * __ldcg(invD + k % kT);
   __syncthreads();
 }
 
-// Phase C on pair (I = J+a, K = J+b), b <= a: A_IK -= W_IJ L_KJ'.
+// Phase C on pair (I = J+a, K = J+b), b <= a: A_IK -= (L_IJ D_J) L_KJ'.
 __device__ void pair_update(const ProfileSystem &S, int J, int a, int b, double (*sA)[kT + 1],
                             double (*sB)[kT + 1]) {
-  const double *wt = S.Wt + (size_t)(a - 1) * kTT;
+  const double *li = tile_at(S, J + a, a);
   const double *lk = tile_at(S, J + b, b);
+  const double *piv = S.piv + (size_t)J * kT;
   for (int k = threadIdx.x; k < kTT; k += blockDim.x) {
-    sA[k / kT][k % kT] = wt[k];
-    sB[k / kT][k % kT] = lk[k];
+    sA[k / kT][k % kT] = __ldcg(li + k) * __ldcg(piv + k % kT);
+    sB[k / kT][k % kT] = __ldcg(lk + k);
   }
   __syncthreads();
   double *out = tile_at(S, J + a, a - b);
@@ -192,50 +168,87 @@ __device__ void pair_update(const ProfileSystem &S, int J, int a, int b, double 
     double acc = 0.0;
 #pragma unroll 8
     for (int c = 0; c < kT; c++) acc += sA[r][c] * sB[s][c];
-    out[k] -= acc;
+    out[k] = __ldcg(out + k) - acc;
   }
   __syncthreads();
 }
 
-__device__ __forceinline__ void decode_pair(int p, int &a, int &b) {
-  // p = a(a-1)/2 + (b-1), 1 <= b <= a
-  int aa = (int)((1.0 + sqrt(1.0 + 8.0 * (double)p)) * 0.5);
-  while (aa * (aa - 1) / 2 > p) aa--;
-  while ((aa + 1) * aa / 2 <= p) aa++;
-  a = aa;
-  b = p - aa * (aa - 1) / 2 + 1;
+// Wait until *p >= target (thread 0 of a block); false on a raised error
+// flag or after kBarrierTimeoutNs (flags[0] = 2).
+__device__ bool wait_geq(const int *p, int target, volatile int *flags) {
+  const volatile int *vp = p;
+  if (*vp >= target) return true;
+  const unsigned long long t0 = global_ns();
+  while (*vp < target) {
+    if (flags[0] != 0) return false;
+    if (global_ns() - t0 > kBarrierTimeoutNs) {
+      flags[0] = 2;
+      return false;
+    }
+    __nanosleep(20);
+  }
+  return true;
+}
+
+__device__ __forceinline__ int slot_of(const ProfileSystem &S, int I, int o) {
+  return I * (S.W + 1) + o;
+}
+
+// Dependencies of a task: every update of its tile from earlier columns
+// (the count of columns J' < J both tile rows reach), and the diagonal /
+// panel tiles it reads.
+__device__ bool wait_task(const ProfileSystem &S, int4 t, volatile int *flags) {
+  const int type = t.x, I = t.y, K = t.z, J = t.w;
+  if (type == 0)
+    return wait_geq(S.upd + slot_of(S, J, 0), J - S.ftile[J], flags);
+  if (type == 1)
+    return wait_geq(S.done + slot_of(S, J, 0), 1, flags) &&
+           wait_geq(S.upd + slot_of(S, I, I - J), J - max(S.ftile[I], S.ftile[J]), flags);
+  return wait_geq(S.done + slot_of(S, I, I - J), 1, flags) &&
+         wait_geq(S.done + slot_of(S, K, K - J), 1, flags) &&
+         wait_geq(S.upd + slot_of(S, I, I - K), J - max(S.ftile[I], S.ftile[K]), flags);
 }
 
 __global__ void __launch_bounds__(kFactorThreads) k_prof_factor(ProfileSystem S) {
   __shared__ double sA[kT][kT + 1], sB[kT][kT + 1];
   __shared__ double col[kT];
+  __shared__ int task, ok;
   volatile int *flags = S.flags;
-  const int nb = gridDim.x;
-  if (blockIdx.x == 0) factor_diag(S, 0, sA, col, flags);
-  if (!prof_barrier(S.barrier, flags)) return;
-  const int npairs = S.W * (S.W + 1) / 2;
-  for (int J = 0; J < S.nt; J++) {
-    const int omax = min(S.W, S.nt - 1 - J);
-    for (int o = 1 + blockIdx.x; o <= omax; o += nb)
-      if (S.ftile[J + o] <= J) panel_solve(S, J, o, sA, sB);
-    if (!prof_barrier(S.barrier, flags)) return;
-    for (int p = blockIdx.x; p < npairs; p += nb) {
-      int a, b;
-      decode_pair(p, a, b);
-      if (a > omax) continue;
-      if (S.ftile[J + a] > J || S.ftile[J + b] > J) continue;
-      pair_update(S, J, a, b, sA, sB);
+  while (true) {
+    if (threadIdx.x == 0) {
+      task = atomicAdd(S.next_task, 1);
+      ok = (task < S.ntasks && flags[0] == 0) ? 1 : 0;
+      if (ok) ok = wait_task(S, S.tasks[task], flags) ? 1 : 0;
+      __threadfence();
     }
-    // pair 0 is (J+1, J+1): its block factors the next diagonal tile now
-    if (blockIdx.x == 0 && J + 1 < S.nt) factor_diag(S, J + 1, sA, col, flags);
-    if (!prof_barrier(S.barrier, flags)) return;
+    __syncthreads();
+    if (!ok) break;
+    const int4 t = S.tasks[task];
+    if (t.x == 0) {
+      if (!factor_diag(S, t.w, sA, col, flags)) break;
+    } else if (t.x == 1) {
+      panel_solve(S, t.w, t.y - t.w, sA, sB);
+    } else {
+      pair_update(S, t.w, t.y - t.w, t.z - t.w, sA, sB);
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      __threadfence();
+      if (t.x == 2) atomicAdd(S.upd + slot_of(S, t.y, t.y - t.z), 1);
+      else atomicExch(S.done + slot_of(S, t.y, t.y - t.w), 1);
+    }
+    __syncthreads();
   }
 }
 
 // Forward (L y = b), diagonal (z = D^-1 y) and backward (L' x = z)
-// substitution in one block; x[r * ldx + i] for right-hand side r.  Every
-// thread issues its loads of a whole tile row (column) before it uses them,
-// so a step costs about one memory latency plus the diagonal solve.
+// substitution in one block; x[r * ldx + i] for right-hand side r.  A step
+// handles one tile row (forward) or tile column (backward): every thread
+// issues the loads of up to kChunk tiles before it uses them, and the
+// diagonal tile's loads go out first, so a step costs about one L2 latency
+// per chunk plus the 32-step shuffle solve of the diagonal tile.
+constexpr int kChunk = 8;
+
 __global__ void __launch_bounds__(kSolveThreads) k_prof_solve(ProfileSystem S, int nrhs,
                                                                double *x, int ldx) {
   __shared__ double red[kSolveThreads / 32][4][kT];
@@ -247,15 +260,41 @@ __global__ void __launch_bounds__(kSolveThreads) k_prof_solve(ProfileSystem S, i
   {
     const int r = tid >> 4, g = tid & 15;      // row of the tile, column group
     for (int J = 0; J < nt; J++) {
+      const double *Ld = tile_at(S, J, 0);
+      const double d0 = __ldcg(Ld + tid), d1 = __ldcg(Ld + tid + kSolveThreads);
       double acc[4] = {0.0, 0.0, 0.0, 0.0};
       const int ohi = min(W, J - S.ftile[J]);
-#pragma unroll 4
-      for (int o = 1; o <= ohi; o++) {
-        const double *Lt = tile_at(S, J, o) + r * kT;
-        const double l0 = Lt[g], l1 = Lt[g + 16];
-        const double *xc = x + (J - o) * kT;
-        for (int q = 0; q < nrhs; q++)
-          acc[q] += l0 * xc[(size_t)q * ldx + g] + l1 * xc[(size_t)q * ldx + g + 16];
+      for (int o0 = 1; o0 <= ohi; o0 += kChunk) {
+        double l0[kChunk], l1[kChunk], y0[kChunk][2], y1[kChunk][2];
+#pragma unroll
+        for (int c = 0; c < kChunk; c++) {
+          const int o = o0 + c;
+          l0[c] = l1[c] = 0.0;
+          y0[c][0] = y0[c][1] = y1[c][0] = y1[c][1] = 0.0;
+          if (o <= ohi) {
+            const double *Lt = tile_at(S, J, o) + r * kT;
+            l0[c] = __ldcg(Lt + g);
+            l1[c] = __ldcg(Lt + g + 16);
+            const double *yc = x + (J - o) * kT;
+            y0[c][0] = __ldcg(yc + g);
+            y1[c][0] = __ldcg(yc + g + 16);
+            if (nrhs > 1) {
+              y0[c][1] = __ldcg(yc + ldx + g);
+              y1[c][1] = __ldcg(yc + ldx + g + 16);
+            }
+          }
+        }
+#pragma unroll
+        for (int c = 0; c < kChunk; c++) {
+          acc[0] += l0[c] * y0[c][0] + l1[c] * y1[c][0];
+          acc[1] += l0[c] * y0[c][1] + l1[c] * y1[c][1];
+        }
+        for (int q = 2; q < nrhs; q++)
+          for (int c = 0; c < kChunk && o0 + c <= ohi; c++) {
+            const double *Lt = tile_at(S, J, o0 + c) + r * kT;
+            const double *yc = x + (size_t)q * ldx + (J - o0 - c) * kT;
+            acc[q] += __ldcg(Lt + g) * __ldcg(yc + g) + __ldcg(Lt + g + 16) * __ldcg(yc + g + 16);
+          }
       }
       for (int q = 0; q < nrhs; q++) {
         double v = acc[q];
@@ -265,14 +304,12 @@ __global__ void __launch_bounds__(kSolveThreads) k_prof_solve(ProfileSystem S, i
         v += __shfl_xor_sync(0xffffffffu, v, 1);
         if (g == 0) red[0][q][r] = v;
       }
-      {
-        const double *L = tile_at(S, J, 0);
-        for (int k = tid; k < kTT; k += kSolveThreads) sL[k / kT][k % kT] = L[k];
-      }
+      sL[tid / kT][tid % kT] = d0;
+      sL[(tid + kSolveThreads) / kT][(tid + kSolveThreads) % kT] = d1;
       __syncthreads();
       if (w < nrhs) {
         const int q = w;
-        double v = x[(size_t)q * ldx + J * kT + lane] - red[0][q][lane];
+        double v = __ldcg(x + (size_t)q * ldx + J * kT + lane) - red[0][q][lane];
         for (int c = 0; c < kT - 1; c++) {
           const double yc = __shfl_sync(0xffffffffu, v, c);
           if (lane > c) v -= sL[lane][c] * yc;
@@ -284,34 +321,60 @@ __global__ void __launch_bounds__(kSolveThreads) k_prof_solve(ProfileSystem S, i
   }
   // ---- diagonal
   for (int q = 0; q < nrhs; q++)
-    for (int i = tid; i < nt * kT; i += kSolveThreads) x[(size_t)q * ldx + i] *= S.invD[i];
+    for (int i = tid; i < nt * kT; i += kSolveThreads)
+      x[(size_t)q * ldx + i] = __ldcg(x + (size_t)q * ldx + i) * S.invD[i];
   __syncthreads();
   // ---- backward: t = z_J - sum_o L(J+o, J)' x_{J+o}; then unit-upper solve
   {
     const int c = lane, g = w;                 // column of the tile, row group
     for (int J = nt - 1; J >= 0; J--) {
+      const double *Ld = tile_at(S, J, 0);
+      const double d0 = __ldcg(Ld + tid), d1 = __ldcg(Ld + tid + kSolveThreads);
       double acc[4] = {0.0, 0.0, 0.0, 0.0};
       const int ohi = min(W, nt - 1 - J);
-#pragma unroll 4
-      for (int o = 1; o <= ohi; o++) {
-        if (S.ftile[J + o] > J) continue;
-        const double *Lt = tile_at(S, J + o, o);
-        const double l0 = Lt[g * kT + c], l1 = Lt[(g + nw) * kT + c];
-        const double *xr = x + (J + o) * kT;
-        for (int q = 0; q < nrhs; q++)
-          acc[q] += l0 * xr[(size_t)q * ldx + g] + l1 * xr[(size_t)q * ldx + g + nw];
+      for (int o0 = 1; o0 <= ohi; o0 += kChunk) {
+        double l0[kChunk], l1[kChunk], x0[kChunk][2], x1[kChunk][2];
+#pragma unroll
+        for (int k = 0; k < kChunk; k++) {
+          const int o = o0 + k;
+          l0[k] = l1[k] = 0.0;
+          x0[k][0] = x0[k][1] = x1[k][0] = x1[k][1] = 0.0;
+          if (o <= ohi && S.ftile[J + o] <= J) {
+            const double *Lt = tile_at(S, J + o, o);
+            l0[k] = __ldcg(Lt + g * kT + c);
+            l1[k] = __ldcg(Lt + (g + nw) * kT + c);
+            const double *xr = x + (J + o) * kT;
+            x0[k][0] = __ldcg(xr + g);
+            x1[k][0] = __ldcg(xr + g + nw);
+            if (nrhs > 1) {
+              x0[k][1] = __ldcg(xr + ldx + g);
+              x1[k][1] = __ldcg(xr + ldx + g + nw);
+            }
+          }
+        }
+#pragma unroll
+        for (int k = 0; k < kChunk; k++) {
+          acc[0] += l0[k] * x0[k][0] + l1[k] * x1[k][0];
+          acc[1] += l0[k] * x0[k][1] + l1[k] * x1[k][1];
+        }
+        for (int q = 2; q < nrhs; q++)
+          for (int k = 0; k < kChunk && o0 + k <= ohi; k++) {
+            if (S.ftile[J + o0 + k] > J) continue;
+            const double *Lt = tile_at(S, J + o0 + k, o0 + k);
+            const double *xr = x + (size_t)q * ldx + (J + o0 + k) * kT;
+            acc[q] += __ldcg(Lt + g * kT + c) * __ldcg(xr + g) +
+                      __ldcg(Lt + (g + nw) * kT + c) * __ldcg(xr + g + nw);
+          }
       }
       for (int q = 0; q < nrhs; q++) red[g][q][c] = acc[q];
-      {
-        const double *L = tile_at(S, J, 0);
-        for (int k = tid; k < kTT; k += kSolveThreads) sL[k / kT][k % kT] = L[k];
-      }
+      sL[tid / kT][tid % kT] = d0;
+      sL[(tid + kSolveThreads) / kT][(tid + kSolveThreads) % kT] = d1;
       __syncthreads();
       if (w < nrhs) {
         const int q = w;
-        double s = 0.0;
-        for (int h = 0; h < nw; h++) s += red[h][q][lane];
-        double v = x[(size_t)q * ldx + J * kT + lane] - s;
+        double sum = 0.0;
+        for (int h = 0; h < nw; h++) sum += red[h][q][lane];
+        double v = __ldcg(x + (size_t)q * ldx + J * kT + lane) - sum;
         // x_c = v_c - sum_{k > c} L[k][c] x_k, from the last row up
         for (int cc = kT - 1; cc > 0; cc--) {
           const double xc = __shfl_sync(0xffffffffu, v, cc);
@@ -345,6 +408,33 @@ int profile_plan(int n, const int *rowptr, const int *colidx, std::vector<int> &
   return 0;
 }
 
+// The dataflow order of the factor tasks (type, I, K, J): type 0 diagonal
+// tile J (I = K = J), 1 panel tile (I, J), 2 update of tile (I, K) by
+// column J.
+void profile_tasks(int nt, int W, const std::vector<int> &ftile, std::vector<int> &tasks) {
+  tasks.clear();
+  auto emit = [&](int type, int I, int K, int J) {
+    tasks.push_back(type); tasks.push_back(I); tasks.push_back(K); tasks.push_back(J);
+  };
+  auto updates = [&](int J, bool first_col) {
+    const int omax = std::min(W, nt - 1 - J);
+    for (int b = first_col ? 1 : 2; b <= (first_col ? 1 : omax); b++) {
+      if (ftile[J + b] > J) continue;
+      for (int a = b; a <= omax; a++)
+        if (ftile[J + a] <= J) emit(2, J + a, J + b, J);
+    }
+  };
+  for (int J = 0; J < nt; J++) {
+    emit(0, J, J, J);
+    const int omax = std::min(W, nt - 1 - J);
+    for (int o = 1; o <= omax; o++)
+      if (ftile[J + o] <= J) emit(1, J + o, J, J);
+    if (J > 0) updates(J - 1, false);
+    updates(J, true);
+  }
+  if (nt > 0) updates(nt - 1, false);
+}
+
 size_t profile_tile_doubles(int nt, int W) { return (size_t)nt * (W + 1) * kTT; }
 int profile_tile_edge() { return kT; }
 
@@ -362,26 +452,23 @@ int profile_factor(const ProfileSystem &S, cudaStream_t s, int *bad_eq) {
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_prof_factor, kFactorThreads, 0);
     if (per < 1) per = 1;
-    g_factor_blocks = sms * per;
+    g_factor_blocks = sms * (per < 2 ? per : 2);
   }
-  // enough blocks for the widest phase (W panel tiles, W(W+1)/2 pairs)
-  long want = (long)S.W * (S.W + 1) / 2;
-  if (want < 1) want = 1;
-  int nb = (int)(want < g_factor_blocks ? want : g_factor_blocks);
-  if (cudaMemsetAsync(S.barrier, 0, 2 * sizeof(unsigned int), s) != cudaSuccess) return XG_ECUDA;
+  const size_t nslots = (size_t)S.nt * (S.W + 1);
+  if (cudaMemsetAsync(S.upd, 0, nslots * sizeof(int), s) != cudaSuccess) return XG_ECUDA;
+  if (cudaMemsetAsync(S.done, 0, nslots * sizeof(int), s) != cudaSuccess) return XG_ECUDA;
+  if (cudaMemsetAsync(S.next_task, 0, sizeof(int), s) != cudaSuccess) return XG_ECUDA;
   if (cudaMemsetAsync(S.flags, 0, 4 * sizeof(int), s) != cudaSuccess) return XG_ECUDA;
-  ProfileSystem Sv = S;
-  void *args[] = {(void *)&Sv};
-  if (cudaLaunchCooperativeKernel((void *)k_prof_factor, dim3(nb), dim3(kFactorThreads), args, 0,
-                                  s) != cudaSuccess)
-    return XG_ECUDA;
+  const int nb = (int)std::min<long>(g_factor_blocks, std::max(S.ntasks, 1));
+  k_prof_factor<<<nb, kFactorThreads, 0, s>>>(S);
+  if (cudaGetLastError() != cudaSuccess) return XG_ECUDA;
   int hflags[4];
   if (cudaMemcpyAsync(hflags, S.flags, sizeof hflags, cudaMemcpyDeviceToHost, s) != cudaSuccess)
     return XG_ECUDA;
   if (cudaStreamSynchronize(s) != cudaSuccess) return XG_ECUDA;
   if (bad_eq) *bad_eq = hflags[0] == 3 ? hflags[1] : -1;
   if (hflags[0] == 3) return XG_ESOLVE;   // pivot check failed
-  if (hflags[0] != 0) return XG_ESOLVE;   // barrier timeout
+  if (hflags[0] != 0) return XG_ESOLVE;   // a dependency wait timed out
   return 0;
 }
 
