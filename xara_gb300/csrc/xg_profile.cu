@@ -45,7 +45,6 @@ namespace {
 constexpr int kT = 32;                 // tile edge
 constexpr int kTT = kT * kT;
 constexpr int kFactorThreads = 256;
-constexpr int kSolveThreads = 512;
 constexpr unsigned long long kBarrierTimeoutNs = 2000000000ull;  // 2 s
 
 __device__ __forceinline__ unsigned long long global_ns() {
@@ -53,6 +52,18 @@ __device__ __forceinline__ unsigned long long global_ns() {
   asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
   return t;
 }
+
+// (row << 5 | column) of the lower triangle of a tile, row by row
+struct LowerTable {
+  unsigned short rs[kT * (kT + 1) / 2];
+  constexpr LowerTable() : rs() {
+    int k = 0;
+    for (int r = 0; r < kT; r++)
+      for (int c = 0; c <= r; c++) rs[k++] = (unsigned short)(r * 32 + c);
+  }
+};
+__device__ const LowerTable kLowerTable{};
+#define kLowerRS (kLowerTable.rs)
 
 __device__ __forceinline__ double *tile_at(const ProfileSystem &S, int I, int o) {
   return S.L + ((size_t)I * (S.W + 1) + o) * kTT;
@@ -163,12 +174,23 @@ __device__ void pair_update(const ProfileSystem &S, int J, int a, int b, double 
   }
   __syncthreads();
   double *out = tile_at(S, J + a, a - b);
-  for (int k = threadIdx.x; k < kTT; k += blockDim.x) {
-    const int r = k / kT, s = k % kT;
-    double acc = 0.0;
+  if (a == b) {
+    // a diagonal tile: its lower triangle only (528 entries, packed table)
+    for (int k = threadIdx.x; k < kT * (kT + 1) / 2; k += blockDim.x) {
+      const int rs = kLowerRS[k], r = rs >> 5, s = rs & 31;
+      double acc = 0.0;
 #pragma unroll 8
-    for (int c = 0; c < kT; c++) acc += sA[r][c] * sB[s][c];
-    out[k] = __ldcg(out + k) - acc;
+      for (int c = 0; c < kT; c++) acc += sA[r][c] * sB[s][c];
+      out[r * kT + s] = __ldcg(out + r * kT + s) - acc;
+    }
+  } else {
+    for (int k = threadIdx.x; k < kTT; k += blockDim.x) {
+      const int r = k / kT, s = k % kT;
+      double acc = 0.0;
+#pragma unroll 8
+      for (int c = 0; c < kT; c++) acc += sA[r][c] * sB[s][c];
+      out[k] = __ldcg(out + k) - acc;
+    }
   }
   __syncthreads();
 }
@@ -224,166 +246,123 @@ __global__ void __launch_bounds__(kFactorThreads) k_prof_factor(ProfileSystem S)
     __syncthreads();
     if (!ok) break;
     const int4 t = S.tasks[task];
+    bool fine = true;
     if (t.x == 0) {
-      if (!factor_diag(S, t.w, sA, col, flags)) break;
+      fine = factor_diag(S, t.w, sA, col, flags);
     } else if (t.x == 1) {
       panel_solve(S, t.w, t.y - t.w, sA, sB);
     } else {
       pair_update(S, t.w, t.y - t.w, t.z - t.w, sA, sB);
+      // type 3: the last update of diagonal tile J+1, factored at once
+      if (t.x == 3) fine = factor_diag(S, t.y, sA, col, flags);
     }
+    if (!fine) break;
     __syncthreads();
     if (threadIdx.x == 0) {
       __threadfence();
-      if (t.x == 2) atomicAdd(S.upd + slot_of(S, t.y, t.y - t.z), 1);
-      else atomicExch(S.done + slot_of(S, t.y, t.y - t.w), 1);
+      if (t.x >= 2) atomicAdd(S.upd + slot_of(S, t.y, t.y - t.z), 1);
+      if (t.x == 3) atomicExch(S.done + slot_of(S, t.y, 0), 1);
+      if (t.x < 2) atomicExch(S.done + slot_of(S, t.y, t.y - t.w), 1);
     }
     __syncthreads();
   }
 }
 
 // Forward (L y = b), diagonal (z = D^-1 y) and backward (L' x = z)
-// substitution in one block; x[r * ldx + i] for right-hand side r.  A step
-// handles one tile row (forward) or tile column (backward): every thread
-// issues the loads of up to kChunk tiles before it uses them, and the
-// diagonal tile's loads go out first, so a step costs about one L2 latency
-// per chunk plus the 32-step shuffle solve of the diagonal tile.
-constexpr int kChunk = 8;
+// substitution in one block of 1024 threads; x[r * ldx + i] for right-hand
+// side r.  Warp w owns row w of every tile and lane c its column, so a
+// tile's 32 x 32 entries come in with one coalesced load per thread; a step
+// (one tile row forward, one tile column backward) issues the loads of up
+// to kChunk tiles at once, keeps the last W+1 solved tiles of every
+// right-hand side in shared memory, and solves the diagonal tile with warp
+// shuffles.  A step costs about one L2 latency plus the 32-step solve.
+constexpr int kChunk = 24;
+constexpr int kSolveBlock = 1024;
 
-__global__ void __launch_bounds__(kSolveThreads) k_prof_solve(ProfileSystem S, int nrhs,
-                                                               double *x, int ldx) {
-  __shared__ double red[kSolveThreads / 32][4][kT];
+__global__ void __launch_bounds__(kSolveBlock) k_prof_solve(ProfileSystem S, int nrhs,
+                                                             double *x, int ldx) {
+  extern __shared__ double win[];                 // [nrhs][W+1][32]
+  __shared__ double red[4][kT][kT + 1];
   __shared__ double sL[kT][kT + 1];
   const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
-  constexpr int nw = kSolveThreads / 32;
-  const int nt = S.nt, W = S.W;
+  const int nt = S.nt, W = S.W, span = W + 1;
+  auto ywin = [&](int q, int tile) -> double * { return win + ((size_t)q * span + tile % span) * kT; };
   // ---- forward: t = b_J - sum_o L(J, J-o) y_{J-o}; then unit-lower solve
-  {
-    const int r = tid >> 4, g = tid & 15;      // row of the tile, column group
-    for (int J = 0; J < nt; J++) {
-      const double *Ld = tile_at(S, J, 0);
-      const double d0 = __ldcg(Ld + tid), d1 = __ldcg(Ld + tid + kSolveThreads);
-      double acc[4] = {0.0, 0.0, 0.0, 0.0};
-      const int ohi = min(W, J - S.ftile[J]);
-      for (int o0 = 1; o0 <= ohi; o0 += kChunk) {
-        double l0[kChunk], l1[kChunk], y0[kChunk][2], y1[kChunk][2];
+  for (int J = 0; J < nt; J++) {
+    const double dval = __ldg(tile_at(S, J, 0) + w * kT + lane);
+    double acc[4] = {0.0, 0.0, 0.0, 0.0};
+    const int ohi = min(W, J - S.ftile[J]);
+    for (int o0 = 1; o0 <= ohi; o0 += kChunk) {
+      double l[kChunk];
 #pragma unroll
-        for (int c = 0; c < kChunk; c++) {
-          const int o = o0 + c;
-          l0[c] = l1[c] = 0.0;
-          y0[c][0] = y0[c][1] = y1[c][0] = y1[c][1] = 0.0;
-          if (o <= ohi) {
-            const double *Lt = tile_at(S, J, o) + r * kT;
-            l0[c] = __ldcg(Lt + g);
-            l1[c] = __ldcg(Lt + g + 16);
-            const double *yc = x + (J - o) * kT;
-            y0[c][0] = __ldcg(yc + g);
-            y1[c][0] = __ldcg(yc + g + 16);
-            if (nrhs > 1) {
-              y0[c][1] = __ldcg(yc + ldx + g);
-              y1[c][1] = __ldcg(yc + ldx + g + 16);
-            }
-          }
-        }
+      for (int k = 0; k < kChunk; k++)
+        l[k] = (o0 + k <= ohi) ? __ldg(tile_at(S, J, o0 + k) + w * kT + lane) : 0.0;
 #pragma unroll
-        for (int c = 0; c < kChunk; c++) {
-          acc[0] += l0[c] * y0[c][0] + l1[c] * y1[c][0];
-          acc[1] += l0[c] * y0[c][1] + l1[c] * y1[c][1];
-        }
-        for (int q = 2; q < nrhs; q++)
-          for (int c = 0; c < kChunk && o0 + c <= ohi; c++) {
-            const double *Lt = tile_at(S, J, o0 + c) + r * kT;
-            const double *yc = x + (size_t)q * ldx + (J - o0 - c) * kT;
-            acc[q] += __ldcg(Lt + g) * __ldcg(yc + g) + __ldcg(Lt + g + 16) * __ldcg(yc + g + 16);
-          }
+      for (int k = 0; k < kChunk; k++) {
+        if (o0 + k > ohi) break;
+        for (int q = 0; q < nrhs; q++) acc[q] += l[k] * ywin(q, J - o0 - k)[lane];
       }
-      for (int q = 0; q < nrhs; q++) {
-        double v = acc[q];
-        v += __shfl_xor_sync(0xffffffffu, v, 8);
-        v += __shfl_xor_sync(0xffffffffu, v, 4);
-        v += __shfl_xor_sync(0xffffffffu, v, 2);
-        v += __shfl_xor_sync(0xffffffffu, v, 1);
-        if (g == 0) red[0][q][r] = v;
-      }
-      sL[tid / kT][tid % kT] = d0;
-      sL[(tid + kSolveThreads) / kT][(tid + kSolveThreads) % kT] = d1;
-      __syncthreads();
-      if (w < nrhs) {
-        const int q = w;
-        double v = __ldcg(x + (size_t)q * ldx + J * kT + lane) - red[0][q][lane];
-        for (int c = 0; c < kT - 1; c++) {
-          const double yc = __shfl_sync(0xffffffffu, v, c);
-          if (lane > c) v -= sL[lane][c] * yc;
-        }
-        x[(size_t)q * ldx + J * kT + lane] = v;
-      }
-      __syncthreads();
     }
+    for (int q = 0; q < nrhs; q++) {
+      double v = acc[q];
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+      if (lane == 0) red[q][0][w] = v;
+    }
+    sL[w][lane] = dval;
+    __syncthreads();
+    if (w < nrhs) {
+      const int q = w;
+      double v = x[(size_t)q * ldx + J * kT + lane] - red[q][0][lane];
+      for (int c = 0; c < kT - 1; c++) {
+        const double yc = __shfl_sync(0xffffffffu, v, c);
+        if (lane > c) v -= sL[lane][c] * yc;
+      }
+      ywin(q, J)[lane] = v;
+      x[(size_t)q * ldx + J * kT + lane] = v;
+    }
+    __syncthreads();
   }
   // ---- diagonal
   for (int q = 0; q < nrhs; q++)
-    for (int i = tid; i < nt * kT; i += kSolveThreads)
-      x[(size_t)q * ldx + i] = __ldcg(x + (size_t)q * ldx + i) * S.invD[i];
+    for (int i = tid; i < nt * kT; i += kSolveBlock) x[(size_t)q * ldx + i] *= S.invD[i];
   __syncthreads();
   // ---- backward: t = z_J - sum_o L(J+o, J)' x_{J+o}; then unit-upper solve
-  {
-    const int c = lane, g = w;                 // column of the tile, row group
-    for (int J = nt - 1; J >= 0; J--) {
-      const double *Ld = tile_at(S, J, 0);
-      const double d0 = __ldcg(Ld + tid), d1 = __ldcg(Ld + tid + kSolveThreads);
-      double acc[4] = {0.0, 0.0, 0.0, 0.0};
-      const int ohi = min(W, nt - 1 - J);
-      for (int o0 = 1; o0 <= ohi; o0 += kChunk) {
-        double l0[kChunk], l1[kChunk], x0[kChunk][2], x1[kChunk][2];
+  for (int J = nt - 1; J >= 0; J--) {
+    const double dval = __ldg(tile_at(S, J, 0) + w * kT + lane);
+    double acc[4] = {0.0, 0.0, 0.0, 0.0};
+    const int ohi = min(W, nt - 1 - J);
+    for (int o0 = 1; o0 <= ohi; o0 += kChunk) {
+      double l[kChunk];
 #pragma unroll
-        for (int k = 0; k < kChunk; k++) {
-          const int o = o0 + k;
-          l0[k] = l1[k] = 0.0;
-          x0[k][0] = x0[k][1] = x1[k][0] = x1[k][1] = 0.0;
-          if (o <= ohi && S.ftile[J + o] <= J) {
-            const double *Lt = tile_at(S, J + o, o);
-            l0[k] = __ldcg(Lt + g * kT + c);
-            l1[k] = __ldcg(Lt + (g + nw) * kT + c);
-            const double *xr = x + (J + o) * kT;
-            x0[k][0] = __ldcg(xr + g);
-            x1[k][0] = __ldcg(xr + g + nw);
-            if (nrhs > 1) {
-              x0[k][1] = __ldcg(xr + ldx + g);
-              x1[k][1] = __ldcg(xr + ldx + g + nw);
-            }
-          }
-        }
+      for (int k = 0; k < kChunk; k++)
+        l[k] = (o0 + k <= ohi && S.ftile[J + o0 + k] <= J)
+                   ? __ldg(tile_at(S, J + o0 + k, o0 + k) + w * kT + lane)
+                   : 0.0;
+      // row w of tile (J+o, J) times x_{J+o}[w]; summed over rows below
 #pragma unroll
-        for (int k = 0; k < kChunk; k++) {
-          acc[0] += l0[k] * x0[k][0] + l1[k] * x1[k][0];
-          acc[1] += l0[k] * x0[k][1] + l1[k] * x1[k][1];
-        }
-        for (int q = 2; q < nrhs; q++)
-          for (int k = 0; k < kChunk && o0 + k <= ohi; k++) {
-            if (S.ftile[J + o0 + k] > J) continue;
-            const double *Lt = tile_at(S, J + o0 + k, o0 + k);
-            const double *xr = x + (size_t)q * ldx + (J + o0 + k) * kT;
-            acc[q] += __ldcg(Lt + g * kT + c) * __ldcg(xr + g) +
-                      __ldcg(Lt + (g + nw) * kT + c) * __ldcg(xr + g + nw);
-          }
+      for (int k = 0; k < kChunk; k++) {
+        if (o0 + k > ohi) break;
+        for (int q = 0; q < nrhs; q++) acc[q] += l[k] * ywin(q, J + o0 + k)[w];
       }
-      for (int q = 0; q < nrhs; q++) red[g][q][c] = acc[q];
-      sL[tid / kT][tid % kT] = d0;
-      sL[(tid + kSolveThreads) / kT][(tid + kSolveThreads) % kT] = d1;
-      __syncthreads();
-      if (w < nrhs) {
-        const int q = w;
-        double sum = 0.0;
-        for (int h = 0; h < nw; h++) sum += red[h][q][lane];
-        double v = __ldcg(x + (size_t)q * ldx + J * kT + lane) - sum;
-        // x_c = v_c - sum_{k > c} L[k][c] x_k, from the last row up
-        for (int cc = kT - 1; cc > 0; cc--) {
-          const double xc = __shfl_sync(0xffffffffu, v, cc);
-          if (lane < cc) v -= sL[cc][lane] * xc;
-        }
-        x[(size_t)q * ldx + J * kT + lane] = v;
-      }
-      __syncthreads();
     }
+    for (int q = 0; q < nrhs; q++) red[q][w][lane] = acc[q];
+    sL[w][lane] = dval;
+    __syncthreads();
+    if (w < nrhs) {
+      const int q = w;
+      double sum = 0.0;
+      for (int h = 0; h < kT; h++) sum += red[q][h][lane];
+      double v = x[(size_t)q * ldx + J * kT + lane] - sum;
+      // x_c = v_c - sum_{k > c} L[k][c] x_k, from the last row up
+      for (int cc = kT - 1; cc > 0; cc--) {
+        const double xc = __shfl_sync(0xffffffffu, v, cc);
+        if (lane < cc) v -= sL[cc][lane] * xc;
+      }
+      ywin(q, J)[lane] = v;
+      x[(size_t)q * ldx + J * kT + lane] = v;
+    }
+    __syncthreads();
   }
 }
 
@@ -410,7 +389,8 @@ int profile_plan(int n, const int *rowptr, const int *colidx, std::vector<int> &
 
 // The dataflow order of the factor tasks (type, I, K, J): type 0 diagonal
 // tile J (I = K = J), 1 panel tile (I, J), 2 update of tile (I, K) by
-// column J.
+// column J, 3 the update of diagonal tile J+1 by column J followed by its
+// factorisation (it is that tile's last update).
 void profile_tasks(int nt, int W, const std::vector<int> &ftile, std::vector<int> &tasks) {
   tasks.clear();
   auto emit = [&](int type, int I, int K, int J) {
@@ -421,11 +401,11 @@ void profile_tasks(int nt, int W, const std::vector<int> &ftile, std::vector<int
     for (int b = first_col ? 1 : 2; b <= (first_col ? 1 : omax); b++) {
       if (ftile[J + b] > J) continue;
       for (int a = b; a <= omax; a++)
-        if (ftile[J + a] <= J) emit(2, J + a, J + b, J);
+        if (ftile[J + a] <= J) emit(a == 1 && b == 1 ? 3 : 2, J + a, J + b, J);
     }
   };
   for (int J = 0; J < nt; J++) {
-    emit(0, J, J, J);
+    if (ftile[J] == J) emit(0, J, J, J);   // no column updates this tile
     const int omax = std::min(W, nt - 1 - J);
     for (int o = 1; o <= omax; o++)
       if (ftile[J + o] <= J) emit(1, J + o, J, J);
@@ -475,7 +455,14 @@ int profile_factor(const ProfileSystem &S, cudaStream_t s, int *bad_eq) {
 int profile_solve(const ProfileSystem &S, int nrhs, double *x, int ldx, cudaStream_t s) {
   if (S.n == 0) return 0;
   if (nrhs < 1 || nrhs > 4 || ldx < S.nt * kT) return XG_EINVAL;
-  k_prof_solve<<<1, kSolveThreads, 0, s>>>(S, nrhs, x, ldx);
+  const size_t win = (size_t)nrhs * (S.W + 1) * kT * sizeof(double);
+  const size_t stat = (4 * kT * (kT + 1) + kT * (kT + 1)) * sizeof(double);
+  if (win + stat > 227 * 1024)
+    return XG_EINVAL;   // envelope wider than the substitution window
+  if (cudaFuncSetAttribute(k_prof_solve, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           (int)win) != cudaSuccess)
+    return XG_ECUDA;
+  k_prof_solve<<<1, kSolveBlock, win, s>>>(S, nrhs, x, ldx);
   return cudaGetLastError() == cudaSuccess ? 0 : XG_ECUDA;
 }
 
