@@ -396,23 +396,30 @@ void profile_tasks(int nt, int W, const std::vector<int> &ftile, std::vector<int
   auto emit = [&](int type, int I, int K, int J) {
     tasks.push_back(type); tasks.push_back(I); tasks.push_back(K); tasks.push_back(J);
   };
-  auto updates = [&](int J, bool first_col) {
+  // the updates of column J (0 <= J < nt) whose target column is J+b for b
+  // in [blo, bhi]
+  auto updates = [&](int J, int blo, int bhi) {
+    if (J < 0) return;
     const int omax = std::min(W, nt - 1 - J);
-    for (int b = first_col ? 1 : 2; b <= (first_col ? 1 : omax); b++) {
+    for (int b = blo; b <= std::min(bhi, omax); b++) {
       if (ftile[J + b] > J) continue;
       for (int a = b; a <= omax; a++)
         if (ftile[J + a] <= J) emit(a == 1 && b == 1 ? 3 : 2, J + a, J + b, J);
     }
   };
+  // Column J: its panels, then what column J+1 still lacks (the updates of
+  // columns J-1 and J that reach it, the diagonal's fused one included),
+  // then the rest of column J-1's trailing update.
   for (int J = 0; J < nt; J++) {
     if (ftile[J] == J) emit(0, J, J, J);   // no column updates this tile
     const int omax = std::min(W, nt - 1 - J);
     for (int o = 1; o <= omax; o++)
       if (ftile[J + o] <= J) emit(1, J + o, J, J);
-    if (J > 0) updates(J - 1, false);
-    updates(J, true);
+    updates(J - 1, 2, 2);
+    updates(J, 1, 1);
+    updates(J - 1, 3, W);
   }
-  if (nt > 0) updates(nt - 1, false);
+  updates(nt - 1, 2, W);
 }
 
 size_t profile_tile_doubles(int nt, int W) { return (size_t)nt * (W + 1) * kTT; }
