@@ -90,75 +90,72 @@ __global__ void k_prof_fill(ProfileSystem S) {
 }
 
 // LDL' of diagonal tile J in shared memory (block-wide); returns false and
-// records the equation when a pivot fails the reference's checks.
+// records the equation when a pivot fails the reference's checks.  Column c
+// scales below the pivot and updates the trailing triangle; thread t works
+// on column c+1+(t%32) of rows c+1+t/32, c+9+t/32, ... (no divisions).
 __device__ bool factor_diag(const ProfileSystem &S, int J, double (*sA)[kT + 1], double *col,
                             volatile int *flags) {
   double *g = tile_at(S, J, 0);
-  for (int k = threadIdx.x; k < kTT; k += blockDim.x) sA[k / kT][k % kT] = __ldcg(g + k);
-  __syncthreads();
+  for (int k = threadIdx.x; k < kTT; k += blockDim.x) sA[k >> 5][k & 31] = __ldcg(g + k);
   __shared__ int bad;
   if (threadIdx.x == 0) bad = 0;
+  __syncthreads();
+  const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5, nty = blockDim.x >> 5;
   for (int c = 0; c < kT; c++) {
     const double d = sA[c][c];
-    const int eq = J * kT + c;
-    if (threadIdx.x == 0 && eq < S.n) {
-      // ProfileSPDLinDirectSolver.cpp:134-138 (first pivot), :189-199
-      const bool fail = (eq == 0) ? !(d > 0.0) : (d == 0.0 || fabs(d) <= S.min_diag_tol);
-      if (fail && !bad) {
-        bad = 1;
-        flags[1] = eq;
-        flags[0] = 3;
-      }
-    }
     const double inv = 1.0 / d;
-    for (int r = c + 1 + threadIdx.x; r < kT; r += blockDim.x) col[r] = sA[r][c];
-    __syncthreads();
-    // trailing update of the tile: a_rs -= (a_rc / d) a_sc for c < s <= r
-    const int m = kT - 1 - c;
-    for (int k = threadIdx.x; k < m * m; k += blockDim.x) {
-      const int r = c + 1 + k / m, s = c + 1 + k % m;
-      if (s <= r) sA[r][s] -= (col[r] * inv) * col[s];
-    }
-    for (int r = c + 1 + threadIdx.x; r < kT; r += blockDim.x) sA[r][c] = col[r] * inv;
     if (threadIdx.x == 0) {
+      const int eq = J * kT + c;
+      if (eq < S.n) {
+        // ProfileSPDLinDirectSolver.cpp:134-138 (first pivot), :189-199
+        const bool fail = (eq == 0) ? !(d > 0.0) : (d == 0.0 || fabs(d) <= S.min_diag_tol);
+        if (fail && !bad) {
+          bad = 1;
+          flags[1] = eq;
+          flags[0] = 3;
+        }
+      }
       S.invD[eq] = inv;
       S.piv[eq] = d;
     }
+    if (threadIdx.x < kT) col[threadIdx.x] = sA[threadIdx.x][c];
+    __syncthreads();
+    // a_rs -= (a_rc / d) a_sc for c < s <= r
+    const int s = c + 1 + tx;
+    if (s < kT) {
+      const double as = col[s];
+      for (int r = c + 1 + ty; r < kT; r += nty)
+        if (s <= r) sA[r][s] -= (col[r] * inv) * as;
+    }
+    if (threadIdx.x > c && threadIdx.x < kT) sA[threadIdx.x][c] = col[threadIdx.x] * inv;
     __syncthreads();
   }
-  for (int k = threadIdx.x; k < kTT; k += blockDim.x) g[k] = sA[k / kT][k % kT];
+  for (int k = threadIdx.x; k < kTT; k += blockDim.x) g[k] = sA[k >> 5][k & 31];
   __syncthreads();
   return bad == 0;
 }
 
-// Phase B on tile (I = J+o, J): W = A L_JJ^-T by rows, L = W D^-1.  Eight
-// threads share a row: w_c = a_c - sum_{k<c} w_k l_ck, the sum split by k
-// mod 8 and reduced with shuffles inside the eight lanes.
+// Phase B on tile (I = J+o, J): W = A L_JJ^-T, L = W D^-1.  Column sweep:
+// once column c of W is final, every later column s loses W(:, c) l_sc;
+// thread t updates row t%32 of columns c+1+t/32, c+1+t/32+8, ...
 __device__ void panel_solve(const ProfileSystem &S, int J, int o, double (*sA)[kT + 1],
                             double (*sB)[kT + 1]) {
   const double *Ljj = tile_at(S, J, 0);
   double *g = tile_at(S, J + o, o);
   for (int k = threadIdx.x; k < kTT; k += blockDim.x) {
-    sB[k / kT][k % kT] = __ldcg(Ljj + k);
-    sA[k / kT][k % kT] = __ldcg(g + k);
+    sB[k >> 5][k & 31] = __ldcg(Ljj + k);
+    sA[k >> 5][k & 31] = __ldcg(g + k);
   }
   __syncthreads();
-  {
-    const int r = threadIdx.x >> 3, q = threadIdx.x & 7;   // blockDim.x == 256
-    for (int c = 1; c < kT; c++) {
-      double part = 0.0;
-      for (int k = q; k < c; k += 8) part += sA[r][k] * sB[c][k];
-      part += __shfl_xor_sync(0xffffffffu, part, 4);
-      part += __shfl_xor_sync(0xffffffffu, part, 2);
-      part += __shfl_xor_sync(0xffffffffu, part, 1);
-      if (q == 0) sA[r][c] -= part;
-      __syncwarp();
-    }
+  const int r = threadIdx.x & 31, sy = threadIdx.x >> 5, nsy = blockDim.x >> 5;
+  for (int c = 0; c < kT - 1; c++) {
+    const double wc = sA[r][c];
+    for (int s = c + 1 + sy; s < kT; s += nsy) sA[r][s] -= wc * sB[s][c];
+    __syncthreads();
   }
-  __syncthreads();
   const double *invD = S.invD + (size_t)J * kT;
   for (int k = threadIdx.x; k < kTT; k += blockDim.x)
-    g[k] = sA[k / kT][k % kT] * __ldcg(invD + k % kT);
+    g[k] = sA[k >> 5][k & 31] * __ldcg(invD + (k & 31));
   __syncthreads();
 }
 
