@@ -101,10 +101,14 @@ __device__ bool factor_diag(const ProfileSystem &S, int J, double (*sA)[kT + 1],
   if (threadIdx.x == 0) bad = 0;
   __syncthreads();
   const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5, nty = blockDim.x >> 5;
+  __shared__ double sinv;
   for (int c = 0; c < kT; c++) {
-    const double d = sA[c][c];
-    const double inv = 1.0 / d;
+    // one thread takes the reciprocal: FP64 work done by every lane of a
+    // block occupies the FP64 pipe as if it were useful work
     if (threadIdx.x == 0) {
+      const double d = sA[c][c];
+      const double inv = 1.0 / d;
+      sinv = inv;
       const int eq = J * kT + c;
       if (eq < S.n) {
         // ProfileSPDLinDirectSolver.cpp:134-138 (first pivot), :189-199
@@ -120,12 +124,13 @@ __device__ bool factor_diag(const ProfileSystem &S, int J, double (*sA)[kT + 1],
     }
     if (threadIdx.x < kT) col[threadIdx.x] = sA[threadIdx.x][c];
     __syncthreads();
+    const double inv = sinv;
     // a_rs -= (a_rc / d) a_sc for c < s <= r
     const int s = c + 1 + tx;
     if (s < kT) {
       const double as = col[s];
-      for (int r = c + 1 + ty; r < kT; r += nty)
-        if (s <= r) sA[r][s] -= (col[r] * inv) * as;
+      for (int r = s + ((ty - (s - c - 1)) % nty + nty) % nty; r < kT; r += nty)
+        sA[r][s] -= (col[r] * inv) * as;
     }
     if (threadIdx.x > c && threadIdx.x < kT) sA[threadIdx.x][c] = col[threadIdx.x] * inv;
     __syncthreads();
