@@ -45,6 +45,7 @@ namespace {
 constexpr int kT = 32;                 // tile edge
 constexpr int kTT = kT * kT;
 constexpr int kFactorThreads = 256;
+constexpr int kFactorSoloSmem = 120 * 1024;   // more than half an SM's shared memory
 constexpr unsigned long long kBarrierTimeoutNs = 2000000000ull;  // 2 s
 
 __device__ __forceinline__ unsigned long long global_ns() {
@@ -441,7 +442,13 @@ int profile_factor(const ProfileSystem &S, cudaStream_t s, int *bad_eq) {
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_prof_factor, kFactorThreads, 0);
     if (per < 1) per = 1;
-    g_factor_blocks = sms * (per < 2 ? per : 2);
+    // one block per SM: a block that runs a task on the critical path (a
+    // diagonal tile, a panel) must not share its SM's few FP64 units with a
+    // bulk tile update; the dynamic shared memory requested below keeps a
+    // second block off the SM
+    g_factor_blocks = sms;
+    cudaFuncSetAttribute(k_prof_factor, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         kFactorSoloSmem);
   }
   const size_t nslots = (size_t)S.nt * (S.W + 1);
   if (cudaMemsetAsync(S.upd, 0, nslots * sizeof(int), s) != cudaSuccess) return XG_ECUDA;
@@ -449,7 +456,7 @@ int profile_factor(const ProfileSystem &S, cudaStream_t s, int *bad_eq) {
   if (cudaMemsetAsync(S.next_task, 0, sizeof(int), s) != cudaSuccess) return XG_ECUDA;
   if (cudaMemsetAsync(S.flags, 0, 4 * sizeof(int), s) != cudaSuccess) return XG_ECUDA;
   const int nb = (int)std::min<long>(g_factor_blocks, std::max(S.ntasks, 1));
-  k_prof_factor<<<nb, kFactorThreads, 0, s>>>(S);
+  k_prof_factor<<<nb, kFactorThreads, kFactorSoloSmem, s>>>(S);
   if (cudaGetLastError() != cudaSuccess) return XG_ECUDA;
   int hflags[4];
   if (cudaMemcpyAsync(hflags, S.flags, sizeof hflags, cudaMemcpyDeviceToHost, s) != cudaSuccess)
