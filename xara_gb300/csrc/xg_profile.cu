@@ -91,76 +91,87 @@ __global__ void k_prof_fill(ProfileSystem S) {
 }
 
 // LDL' of diagonal tile J in shared memory (block-wide); returns false and
-// records the equation when a pivot fails the reference's checks.  Column c
-// scales below the pivot and updates the trailing triangle; thread t works
-// on column c+1+(t%32) of rows c+1+t/32, c+9+t/32, ... (no divisions).
+// records the equation when a pivot fails the reference's checks.  Column c:
+// the column below the pivot is read and scaled by the reciprocal pivot,
+// then every trailing entry takes one FMA; the thread that finishes the
+// next pivot takes its reciprocal at once (__drcp_rn: the correctly rounded
+// 1/d, the value of the reference's 1.0/aii), so the chain of dependent
+// FP64 operations per column stays short.
 __device__ bool factor_diag(const ProfileSystem &S, int J, double (*sA)[kT + 1], double *col,
                             volatile int *flags) {
   double *g = tile_at(S, J, 0);
+  __shared__ double lcol[kT], sinv[kT + 1];
   for (int k = threadIdx.x; k < kTT; k += blockDim.x) sA[k >> 5][k & 31] = __ldcg(g + k);
-  __shared__ int bad;
-  if (threadIdx.x == 0) bad = 0;
+  __syncthreads();
+  if (threadIdx.x == 0) sinv[0] = __drcp_rn(sA[0][0]);
   __syncthreads();
   const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5, nty = blockDim.x >> 5;
-  __shared__ double sinv;
   for (int c = 0; c < kT; c++) {
-    // one thread takes the reciprocal: FP64 work done by every lane of a
-    // block occupies the FP64 pipe as if it were useful work
-    if (threadIdx.x == 0) {
-      const double d = sA[c][c];
-      const double inv = 1.0 / d;
-      sinv = inv;
-      const int eq = J * kT + c;
-      if (eq < S.n) {
-        // ProfileSPDLinDirectSolver.cpp:134-138 (first pivot), :189-199
-        const bool fail = (eq == 0) ? !(d > 0.0) : (d == 0.0 || fabs(d) <= S.min_diag_tol);
-        if (fail && !bad) {
-          bad = 1;
-          flags[1] = eq;
-          flags[0] = 3;
-        }
-      }
-      S.invD[eq] = inv;
-      S.piv[eq] = d;
+    const double inv = sinv[c];
+    if (threadIdx.x < kT) {
+      const double v = sA[threadIdx.x][c];
+      col[threadIdx.x] = v;
+      lcol[threadIdx.x] = v * inv;
     }
-    if (threadIdx.x < kT) col[threadIdx.x] = sA[threadIdx.x][c];
     __syncthreads();
-    const double inv = sinv;
-    // a_rs -= (a_rc / d) a_sc for c < s <= r
+    // a_rs -= l_r a_sc for c < s <= r
     const int s = c + 1 + tx;
     if (s < kT) {
       const double as = col[s];
-      for (int r = s + ((ty - (s - c - 1)) % nty + nty) % nty; r < kT; r += nty)
-        sA[r][s] -= (col[r] * inv) * as;
+      for (int r = s + ((ty - tx) % nty + nty) % nty; r < kT; r += nty) {
+        const double v = fma(-lcol[r], as, sA[r][s]);
+        sA[r][s] = v;
+        if (r == s && r == c + 1) sinv[c + 1] = __drcp_rn(v);
+      }
     }
-    if (threadIdx.x > c && threadIdx.x < kT) sA[threadIdx.x][c] = col[threadIdx.x] * inv;
+    if (threadIdx.x > c && threadIdx.x < kT) sA[threadIdx.x][c] = lcol[threadIdx.x];
     __syncthreads();
+  }
+  if (threadIdx.x < kT) {
+    const int eq = J * kT + threadIdx.x;
+    const double d = sA[threadIdx.x][threadIdx.x];
+    S.invD[eq] = sinv[threadIdx.x];
+    S.piv[eq] = d;
+    // ProfileSPDLinDirectSolver.cpp:134-138 (first pivot), :189-199; the
+    // first failing pivot of the tile is reported
+    const bool fail = eq < S.n && ((eq == 0) ? !(d > 0.0)
+                                             : (d == 0.0 || fabs(d) <= S.min_diag_tol));
+    const unsigned bad = __ballot_sync(0xffffffffu, fail);
+    if (bad && threadIdx.x == 0) {
+      flags[1] = J * kT + __ffs(bad) - 1;
+      __threadfence();
+      flags[0] = 3;
+    }
   }
   for (int k = threadIdx.x; k < kTT; k += blockDim.x) g[k] = sA[k >> 5][k & 31];
   __syncthreads();
-  return bad == 0;
+  return flags[0] != 3;
 }
 
-// Phase B on tile (I = J+o, J): W = A L_JJ^-T, L = W D^-1.  Column sweep:
-// once column c of W is final, every later column s loses W(:, c) l_sc;
-// thread t updates row t%32 of columns c+1+t/32, c+1+t/32+8, ...
-__device__ void panel_solve(const ProfileSystem &S, int J, int o, double (*sA)[kT + 1],
+// Phase B on rows 8q..8q+7 of tile (I = J+o, J): W = A L_JJ^-T, L = W
+// D^-1 (rows are independent, so a tile is four tasks).  Column sweep: once
+// column c of W is final, every later column s loses W(:, c) l_sc; thread t
+// updates row 8q + t%8 of columns c+1+t/8, c+33+t/8, ...
+constexpr int kPanelRows = 8;
+constexpr int kPanelParts = kT / kPanelRows;
+
+__device__ void panel_solve(const ProfileSystem &S, int J, int o, int q, double (*sA)[kT + 1],
                             double (*sB)[kT + 1]) {
   const double *Ljj = tile_at(S, J, 0);
-  double *g = tile_at(S, J + o, o);
-  for (int k = threadIdx.x; k < kTT; k += blockDim.x) {
-    sB[k >> 5][k & 31] = __ldcg(Ljj + k);
+  double *g = tile_at(S, J + o, o) + q * kPanelRows * kT;
+  for (int k = threadIdx.x; k < kTT; k += blockDim.x) sB[k >> 5][k & 31] = __ldcg(Ljj + k);
+  for (int k = threadIdx.x; k < kPanelRows * kT; k += blockDim.x)
     sA[k >> 5][k & 31] = __ldcg(g + k);
-  }
   __syncthreads();
-  const int r = threadIdx.x & 31, sy = threadIdx.x >> 5, nsy = blockDim.x >> 5;
+  const int r = threadIdx.x % kPanelRows, sy = threadIdx.x / kPanelRows;
+  const int nsy = blockDim.x / kPanelRows;
   for (int c = 0; c < kT - 1; c++) {
     const double wc = sA[r][c];
-    for (int s = c + 1 + sy; s < kT; s += nsy) sA[r][s] -= wc * sB[s][c];
+    for (int s = c + 1 + sy; s < kT; s += nsy) sA[r][s] = fma(-wc, sB[s][c], sA[r][s]);
     __syncthreads();
   }
   const double *invD = S.invD + (size_t)J * kT;
-  for (int k = threadIdx.x; k < kTT; k += blockDim.x)
+  for (int k = threadIdx.x; k < kPanelRows * kT; k += blockDim.x)
     g[k] = sA[k >> 5][k & 31] * __ldcg(invD + (k & 31));
   __syncthreads();
 }
@@ -229,8 +240,8 @@ __device__ bool wait_task(const ProfileSystem &S, int4 t, volatile int *flags) {
   if (type == 1)
     return wait_geq(S.done + slot_of(S, J, 0), 1, flags) &&
            wait_geq(S.upd + slot_of(S, I, I - J), J - max(S.ftile[I], S.ftile[J]), flags);
-  return wait_geq(S.done + slot_of(S, I, I - J), 1, flags) &&
-         wait_geq(S.done + slot_of(S, K, K - J), 1, flags) &&
+  return wait_geq(S.done + slot_of(S, I, I - J), kPanelParts, flags) &&
+         wait_geq(S.done + slot_of(S, K, K - J), kPanelParts, flags) &&
          wait_geq(S.upd + slot_of(S, I, I - K), J - max(S.ftile[I], S.ftile[K]), flags);
 }
 
@@ -253,7 +264,7 @@ __global__ void __launch_bounds__(kFactorThreads) k_prof_factor(ProfileSystem S)
     if (t.x == 0) {
       fine = factor_diag(S, t.w, sA, col, flags);
     } else if (t.x == 1) {
-      panel_solve(S, t.w, t.y - t.w, sA, sB);
+      panel_solve(S, t.w, t.y - t.w, t.z, sA, sB);
     } else {
       pair_update(S, t.w, t.y - t.w, t.z - t.w, sA, sB);
       // type 3: the last update of diagonal tile J+1, factored at once
@@ -265,7 +276,8 @@ __global__ void __launch_bounds__(kFactorThreads) k_prof_factor(ProfileSystem S)
       __threadfence();
       if (t.x >= 2) atomicAdd(S.upd + slot_of(S, t.y, t.y - t.z), 1);
       if (t.x == 3) atomicExch(S.done + slot_of(S, t.y, 0), 1);
-      if (t.x < 2) atomicExch(S.done + slot_of(S, t.y, t.y - t.w), 1);
+      if (t.x == 0) atomicExch(S.done + slot_of(S, t.y, 0), 1);
+      if (t.x == 1) atomicAdd(S.done + slot_of(S, t.y, t.y - t.w), 1);
     }
     __syncthreads();
   }
@@ -391,7 +403,8 @@ int profile_plan(int n, const int *rowptr, const int *colidx, std::vector<int> &
 }
 
 // The dataflow order of the factor tasks (type, I, K, J): type 0 diagonal
-// tile J (I = K = J), 1 panel tile (I, J), 2 update of tile (I, K) by
+// tile J (I = K = J), 1 rows 8K..8K+7 of panel tile (I, J), 2 update of
+// tile (I, K) by
 // column J, 3 the update of diagonal tile J+1 by column J followed by its
 // factorisation (it is that tile's last update).
 void profile_tasks(int nt, int W, const std::vector<int> &ftile, std::vector<int> &tasks) {
@@ -417,7 +430,8 @@ void profile_tasks(int nt, int W, const std::vector<int> &ftile, std::vector<int
     if (ftile[J] == J) emit(0, J, J, J);   // no column updates this tile
     const int omax = std::min(W, nt - 1 - J);
     for (int o = 1; o <= omax; o++)
-      if (ftile[J + o] <= J) emit(1, J + o, J, J);
+      if (ftile[J + o] <= J)
+        for (int q = 0; q < kPanelParts; q++) emit(1, J + o, q, J);
     updates(J - 1, 2, 2);
     updates(J, 1, 1);
     updates(J - 1, 3, W);
