@@ -161,10 +161,19 @@ typedef struct xg_phase_desc {
   double dc_incr;               /* DisplacementControl increment             */
   double dt, gamma, beta;       /* Newmark                                   */
   double alpha_m, beta_k, beta_k_init, beta_k_comm;  /* rayleigh           */
+  const double *alpha_m_node;   /* [num_nodes] alphaM per node or NULL       */
+  const double *beta_k_init_elem; /* [num_elems] betaK0 per element or NULL:
+                                   disconnected parts of one model with their
+                                   own `rayleigh` factors                    */
   int gm_dof;                   /* UniformExcitation direction (0-based)     */
-  int gm_npts;                  /* ground acceleration samples               */
+  int gm_npts;                  /* ground acceleration samples per record    */
   double gm_dt;
-  const double *gm_accel;       /* [gm_npts]                                 */
+  const double *gm_accel;       /* [gm_count*gm_npts] PathSeries values      */
+  int gm_count;                 /* records (0 or 1: one for every node)      */
+  const int *gm_node_record;    /* [num_nodes] record of each node, or NULL:
+                                   a separate UniformExcitation per group of
+                                   nodes, e.g. disconnected frames batched
+                                   into one model                            */
   int test;                     /* XG_TEST_*                                 */
   double tol;
   int max_iter;

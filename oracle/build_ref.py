@@ -44,7 +44,8 @@ domain/constraints/SP_Constraint.cpp domain/constraints/MP_Constraint.cpp
 domain/load/Load.cpp element/ElementalLoad.cpp
 domain/pattern/LoadPattern.cpp domain/pattern/LoadPatternIter.cpp
 domain/pattern/series/TimeSeries.cpp domain/pattern/series/LinearSeries.cpp
-domain/pattern/series/PathSeries.cpp
+domain/pattern/series/PathSeries.cpp domain/pattern/series/TimeSeriesIntegrator.cpp
+domain/pattern/series/TrapezoidalTimeSeriesIntegrator.cpp
 domain/pattern/UniformExcitation.cpp domain/pattern/EarthquakePattern.cpp
 domain/groundMotion/GroundMotion.cpp
 domain/domain/single/SingleDomEleIter.cpp domain/domain/single/SingleDomNodIter.cpp

@@ -56,6 +56,11 @@
 #include <RCM.h>
 #include <LoadControl.h>
 #include <DisplacementControl.h>
+#include <Newmark.h>
+#include <TransientIntegrator.h>
+#include <UniformExcitation.h>
+#include <GroundMotion.h>
+#include <PathSeries.h>
 #include <NewtonRaphson.h>
 #include <CTestNormDispIncr.h>
 #include <CTestNormUnbalance.h>
@@ -283,6 +288,11 @@ void *xref_create(const xg_model_desc *desc) {
       n = new Node(d.node_tag[i], d.ndf, x[0], x[1]);
     else
       n = new Node(d.node_tag[i], d.ndf, x[0], x[1], x[2]);
+    if (d.node_mass) {
+      Matrix M(d.ndf, d.ndf);
+      for (int j = 0; j < d.ndf; j++) M(j, j) = d.node_mass[(size_t)i * d.ndf + j];
+      n->setMass(M);
+    }
     dom->addNode(n);
     h->nodes.push_back(n);
   }
@@ -403,13 +413,33 @@ int xref_run_phase(void *hp, const xg_phase_desc *ph, int cap_begin, int cap_end
   else
     test = new CTestNormUnbalance(ph->tol, ph->max_iter, 0);
   NewtonRaphson *algo = new NewtonRaphson(*test);
-  StaticIntegrator *integ = nullptr;
+  IncrementalIntegrator *integ = nullptr;
+  TransientIntegrator *transient = nullptr;
   if (ph->integrator == XG_INT_LOAD_CONTROL)
     integ = new LoadControl(ph->d_lambda, 1, ph->d_lambda, ph->d_lambda);
   else if (ph->integrator == XG_INT_DISP_CONTROL)
     integ = new DisplacementControl(ph->dc_node, ph->dc_dof, ph->dc_incr, h->domain, 1,
                                     ph->dc_incr, ph->dc_incr);
-  else {
+  else if (ph->integrator == XG_INT_NEWMARK) {
+    // `integrator Newmark gamma beta`, `rayleigh ...`, and one
+    // `pattern UniformExcitation` over a `timeSeries Path -dt` record
+    transient = new Newmark(ph->gamma, ph->beta);
+    integ = transient;
+    h->domain->setRayleighDampingFactors(ph->alpha_m, ph->beta_k, ph->beta_k_init,
+                                         ph->beta_k_comm);
+    if (ph->gm_npts > 0) {
+      if (ph->gm_node_record || ph->gm_count > 1) {
+        fprintf(stderr, "xref_run_phase: one ground-motion record for all nodes only\n");
+        return -1;
+      }
+      Vector path(ph->gm_npts);
+      for (int k = 0; k < ph->gm_npts; k++) path(k) = ph->gm_accel[k];
+      PathSeries *series = new PathSeries(1, path, ph->gm_dt);
+      GroundMotion *motion = new GroundMotion(nullptr, nullptr, series);
+      UniformExcitation *ue = new UniformExcitation(*motion, ph->gm_dof, 900 + ph->pattern);
+      h->domain->addLoadPattern(ue);
+    }
+  } else {
     fprintf(stderr, "xref_run_phase: integrator %d not supported\n", ph->integrator);
     return -1;
   }
@@ -453,7 +483,9 @@ int xref_run_phase(void *hp, const xg_phase_desc *ph, int cap_begin, int cap_end
     c.iter = 0;
     auto t0 = clk::now();
     double solve0 = h->soe->solveSeconds;
-    if (integ->newStep() < 0) return -10 - s;
+    const int ns = transient ? transient->newStep(ph->dt)
+                             : static_cast<StaticIntegrator *>(integ)->newStep();
+    if (ns < 0) return -10 - s;
     int r = algo->solveCurrentStep();
     if (r < 0) {
       fprintf(stderr, "xref_run_phase: step %d failed (%d)\n", gstep, r);

@@ -426,6 +426,8 @@ typedef struct xo_model {
   double *fr_Se, *fr_kv, *fr_Se_c, *fr_kv_c, *fr_vs, *fr_vs_c, *fr_fs, *fr_Ssr, *fr_vlast;
   int *fr_init;
   long long work_pts, work_fib, work_sec;   /* work counters (benchmarks) */
+  double *V, *A, *Vc, *Ac;           /* Newmark trial / committed vel, accel [nu] */
+  double *K0vals;                    /* assembled initial stiffness (CSR)    */
 } xo_model;
 
 static int csr_find(const struct xo_model *m, int row, int col);
@@ -636,6 +638,10 @@ xo_model *xo_create(const xg_model_desc *desc) {
   m->B = (double *)calloc(m->neq, sizeof(double));
   m->invD = (double *)calloc(m->neq, sizeof(double));
   m->sky = (double *)calloc(m->diag[m->neq], sizeof(double));
+  m->V = (double *)calloc(m->nu, sizeof(double));
+  m->A = (double *)calloc(m->nu, sizeof(double));
+  m->Vc = (double *)calloc(m->nu, sizeof(double));
+  m->Ac = (double *)calloc(m->nu, sizeof(double));
   if (frames && xo_frame_setup(m) < 0) { xo_destroy(m); return NULL; }
   /* Domain::addElement calls Element::update once (domain/domain/Domain.cpp:
      390-392); the J2 constructors also evaluate the zero-strain state
@@ -651,6 +657,7 @@ void xo_destroy(xo_model *m) {
   free(m->diag); free(m->sky); free(m->invD); free(m->U); free(m->Uc); free(m->ep_c);
   free(m->ep_t); free(m->xi_c); free(m->xi_t); free(m->sig_t); free(m->D_t); free(m->vals); free(m->resid);
   free(m->fext); free(m->dU); free(m->B);
+  free(m->V); free(m->A); free(m->Vc); free(m->Ac); free(m->K0vals);
   free(m);
 }
 
@@ -753,6 +760,8 @@ void xo_commit(xo_model *m) {
   memcpy(m->ep_c, m->ep_t, sizeof(double) * nh * 9);
   memcpy(m->xi_c, m->xi_t, sizeof(double) * nh);
   memcpy(m->Uc, m->U, sizeof(double) * m->nu);
+  memcpy(m->Vc, m->V, sizeof(double) * m->nu);
+  memcpy(m->Ac, m->A, sizeof(double) * m->nu);
   m->time_c = m->time;
 }
 
@@ -905,10 +914,167 @@ static int xo_solve_timed(xo_model *m, const double *b, double *x, int refactor,
  *     372-392), newStep (:121-200) and update (:202-250); the second solve of
  *     every iteration reuses the factorisation as ProfileSPD does.
  */
+/* PathSeries::getFactor (domain/pattern/series/PathSeries.cpp:334-356) with
+   startTime 0, factor 1 and useLast false: linear between samples, 0 past
+   the next-to-last sample. */
+static double xo_path(const double *a, int npts, double dt, double t) {
+  if (t < 0.0) return 0.0;
+  const double incr = t / dt;
+  const int i1 = (int)floor(incr), i2 = i1 + 1;
+  if (i2 >= npts) return 0.0;
+  const double v1 = a[i1], v2 = a[i2];
+  return v1 + (v2 - v1) * (incr - i1);
+}
+
+/* Initial stiffness of every frame element assembled into CSR values
+   (Element::getInitialStiff, the K0 of Rayleigh's betaK0 term). */
+static int xo_assemble_k0(xo_model *m, double bk0, const double *bk0_elem) {
+  const xg_model_desc *d = &m->d;
+  if (d->elem_type != XG_ELE_FBC2D && d->elem_type != XG_ELE_FBC3D) return -1;
+  const int ndf = d->ndf, ned = 2 * ndf;
+  free(m->K0vals);
+  m->K0vals = (double *)calloc(m->nnz > 0 ? m->nnz : 1, sizeof(double));
+  double K[144];
+  for (int e = 0; e < d->num_elems; e++) {
+    xo_frame_initial_stiff(m, e, K);
+    const double f = bk0_elem ? bk0_elem[e] : bk0;
+    for (int k = 0; k < ned * ned; k++) K[k] *= f;
+    int ids[12];
+    for (int a = 0; a < 2; a++)
+      for (int j = 0; j < ndf; j++) ids[a * ndf + j] = m->eqn[m->conn[2 * e + a] * ndf + j];
+    for (int i = 0; i < ned; i++) {
+      if (ids[i] < 0) continue;
+      for (int j = 0; j < ned; j++)
+        if (ids[j] >= 0) m->K0vals[csr_find(m, ids[i], ids[j])] += K[i * ned + j];
+    }
+  }
+  return 0;
+}
+
+/*
+ * Transient phase: Newmark (displacement formulation, Dynamic/Newmark.cpp:
+ * 105-245 newStep, :262-300 tangents, :410-455 update) under NewtonRaphson.
+ * Effective tangent c1 Kt + c2 (betaK0 K0) + nodal c2 alphaM M + c3 M;
+ * unbalance = nodal loads (patterns, and UniformExcitation's -M r ag(t),
+ * EarthquakePattern.cpp:68-99, Node.cpp:668-689) - M a - alphaM M v
+ * (Node::getUnbalancedLoadIncInertia, Node.cpp:743-764) - (P_int + betaK0
+ * K0 v) (Element::getRayleighDampingForces, element/Element.cpp:284-330).
+ * Lumped nodal masses; betaK and betaKc must be 0.
+ */
+static int xo_run_newmark(xo_model *m, const xg_phase_desc *ph, double *step_u,
+                          double *step_lambda, int *step_iters) {
+  const xg_model_desc *d = &m->d;
+  const int n = m->neq, nu = m->nu, ndf = d->ndf;
+  if (ph->dt <= 0.0 || ph->beta == 0.0 || ph->beta_k != 0.0 || ph->beta_k_comm != 0.0)
+    return XG_EINVAL;
+  const int has_k0 = ph->beta_k_init != 0.0 || ph->beta_k_init_elem != NULL;
+  if (has_k0 && xo_assemble_k0(m, ph->beta_k_init, ph->beta_k_init_elem) < 0) return XG_EINVAL;
+  const double dt = ph->dt, gam = ph->gamma, bet = ph->beta;
+  const double c1 = 1.0, c2 = gam / (bet * dt), c3 = 1.0 / (bet * dt * dt);
+  const double a1 = 1.0 - gam / bet, a2 = dt * (1.0 - 0.5 * gam / bet);
+  const double a3 = -1.0 / (bet * dt), a4 = 1.0 - 0.5 / bet;
+  const double bk0 = has_k0 ? 1.0 : 0.0;   /* K0vals carry betaK0 */
+  double *Vt = (double *)calloc(nu, sizeof(double)), *At = (double *)calloc(nu, sizeof(double));
+  double *K0v = (double *)calloc(n > 0 ? n : 1, sizeof(double));
+  double *Veq = (double *)calloc(n > 0 ? n : 1, sizeof(double));
+  int rc = 0;
+  for (int s = 0; s < ph->num_steps; s++) {
+    double t0 = now_s(), solve_t = 0.0;
+    /* newStep */
+    memcpy(Vt, m->V, sizeof(double) * nu);
+    memcpy(At, m->A, sizeof(double) * nu);
+    for (int i = 0; i < nu; i++) {
+      if (m->eqn[i] < 0) continue;
+      m->V[i] = m->V[i] * a1 + At[i] * a2;
+      m->A[i] = m->A[i] * a4 + Vt[i] * a3;
+    }
+    m->time += dt;
+    xo_elem_update(m);
+    int it = 0, ok = 0;
+    while (1) {
+      /* formUnbalance */
+      xo_form_fext(m, m->time);
+      for (int i = 0; i < n; i++) m->B[i] = m->fext[i];
+      for (int a = 0; a < nu; a++) {
+        const int e = m->eqn[a];
+        if (e < 0) continue;
+        const double mass = d->node_mass ? d->node_mass[a] : 0.0;
+        if (mass == 0.0) continue;
+        if (ph->gm_npts > 0 && a % ndf == ph->gm_dof) {
+          const int rec = ph->gm_node_record ? ph->gm_node_record[a / ndf] : 0;
+          const double ag = xo_path(ph->gm_accel + (size_t)rec * ph->gm_npts, ph->gm_npts,
+                                    ph->gm_dt, m->time);
+          m->B[e] -= mass * ag;
+        }
+        const double am = ph->alpha_m_node ? ph->alpha_m_node[a / ndf] : ph->alpha_m;
+        m->B[e] -= mass * m->A[a];
+        if (am != 0.0) m->B[e] -= am * mass * m->V[a];
+      }
+      for (int i = 0; i < n; i++) m->B[i] -= m->resid[i];
+      if (bk0 != 0.0) {
+        for (int a = 0; a < nu; a++) if (m->eqn[a] >= 0) Veq[m->eqn[a]] = m->V[a];
+        for (int r = 0; r < n; r++) {
+          double t = 0.0;
+          for (int k = m->rowptr[r]; k < m->rowptr[r + 1]; k++) t += m->K0vals[k] * Veq[m->colidx[k]];
+          K0v[r] = t;
+        }
+        for (int i = 0; i < n; i++) m->B[i] -= bk0 * K0v[i];
+      }
+      if (it > 0) {
+        double norm = 0.0;
+        if (ph->test == XG_TEST_NORM_DISP_INCR)
+          for (int i = 0; i < n; i++) norm += m->dU[i] * m->dU[i];
+        else
+          for (int i = 0; i < n; i++) norm += m->B[i] * m->B[i];
+        if (sqrt(norm) <= ph->tol) { ok = 1; break; }
+        if (it >= ph->max_iter) break;
+      }
+      /* formTangent: c1 Kt + c2 betaK0 K0 + nodal (c2 alphaM + c3) M */
+      for (int k = 0; k < m->nnz; k++) {
+        m->vals[k] *= c1;
+        if (bk0 != 0.0) m->vals[k] += c2 * bk0 * m->K0vals[k];
+      }
+      for (int a = 0; a < nu; a++) {
+        const int e = m->eqn[a];
+        const double mass = d->node_mass ? d->node_mass[a] : 0.0;
+        if (e < 0 || mass == 0.0) continue;
+        const double am = ph->alpha_m_node ? ph->alpha_m_node[a / ndf] : ph->alpha_m;
+        m->vals[csr_find(m, e, e)] += c2 * am * mass + c3 * mass;
+      }
+      if (xo_solve_timed(m, m->B, m->dU, 1, &solve_t) < 0) { rc = XG_ESOLVE; break; }
+      /* update */
+      xo_incr_disp(m, m->dU, 1.0);
+      for (int a = 0; a < nu; a++) {
+        const int e = m->eqn[a];
+        if (e < 0) continue;
+        m->V[a] += m->dU[e] * c2;
+        m->A[a] += m->dU[e] * c3;
+      }
+      xo_elem_update(m);
+      it++;
+    }
+    if (rc) break;
+    if (!ok) { rc = XG_ENOCONV; break; }
+    xo_commit(m);
+    double tt = now_s() - t0;
+    m->solve_s += solve_t;
+    m->elem_s += tt - solve_t;
+    if (step_u) memcpy(step_u + (size_t)s * nu, m->Uc, sizeof(double) * nu);
+    if (step_lambda) step_lambda[s] = m->time;
+    if (step_iters) step_iters[s] = it;
+  }
+  free(Vt); free(At); free(K0v); free(Veq);
+  return rc;
+}
+
 int xo_run_phase(xo_model *m, const xg_phase_desc *ph, double *step_u, double *step_lambda,
                  int *step_iters) {
   const xg_model_desc *d = &m->d;
   int n = m->neq;
+  if (ph->integrator == XG_INT_NEWMARK) {
+    if (ph->pattern >= 0 && ph->pattern < 8) m->added[ph->pattern] = 1;
+    return xo_run_newmark(m, ph, step_u, step_lambda, step_iters);
+  }
   if (ph->integrator != XG_INT_LOAD_CONTROL && ph->integrator != XG_INT_DISP_CONTROL)
     return XG_EINVAL;
   if (ph->pattern >= 0 && ph->pattern < 8) m->added[ph->pattern] = 1;

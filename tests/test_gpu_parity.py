@@ -166,7 +166,7 @@ def test_round_trip_history_checkpoint(gpu_mod):
     assert np.array_equal(v1, v2) and np.array_equal(r1, r2)
 
 
-FRAMES = ["frame2d_2x3", "frame3d_1x1x2", "frame3d_2x1x3"]
+FRAMES = ["frame2d_2x3", "frame3d_1x1x2", "frame3d_2x1x3", "frame2d_eq_2x3"]
 
 
 @pytest.mark.parametrize("name", FRAMES)
@@ -229,3 +229,27 @@ def test_revert_to_last_commit(gpu_mod, name):
                                              fx["P" + key])
             assert relerr(resid, r_ref) < RTOL_STATE, key
             assert relerr(vals, v_ref) < RTOL_STATE, key
+
+
+@pytest.mark.parametrize("system", ["profile", "pcg"])
+def test_frame_batch_parts_match_separate_runs(gpu_mod, system):
+    """Six frames under their own records in one device model (Newmark,
+    per-frame Rayleigh factors, per-node ground-motion records, per-part
+    convergence) against every frame run alone through the oracle: each
+    frame's displacement history within 1e-8."""
+    from oracle import port
+    from xara_gb300 import configs
+    desc, phases, parts = configs.frame_batch(6, steps=60, seed=3, return_parts=True)
+    with gpu_mod.DeviceModel(desc) as m:
+        m.set_system(gpu_mod.XG_SYSTEM_PROFILE_SPD if system == "profile"
+                     else gpu_mod.XG_SYSTEM_BJPCG)
+        U, _, stats = m.run(phases)
+    off = 0
+    for d, p in parts:
+        o = port.OracleModel(d)
+        Uf, _, its = o.run(p)
+        o.close()
+        nu = d.num_nodes * d.ndf
+        assert relerr(U[:, off:off + nu], Uf) < RTOL_HISTORY, off
+        off += nu
+    assert off == U.shape[1]

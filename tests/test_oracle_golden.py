@@ -64,7 +64,7 @@ def test_replay_element_state(name):
         o.close()
 
 
-FRAMES = ["frame2d_2x3", "frame3d_1x1x2", "frame3d_2x1x3"]
+FRAMES = ["frame2d_2x3", "frame3d_1x1x2", "frame3d_2x1x3", "frame2d_eq_2x3"]
 
 
 def test_uniaxial_paths():

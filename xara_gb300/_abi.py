@@ -48,8 +48,10 @@ class xg_phase_desc(C.Structure):
         ("dc_incr", C.c_double), ("dt", C.c_double), ("gamma", C.c_double),
         ("beta", C.c_double), ("alpha_m", C.c_double), ("beta_k", C.c_double),
         ("beta_k_init", C.c_double), ("beta_k_comm", C.c_double),
+        ("alpha_m_node", _pd), ("beta_k_init_elem", _pd),
         ("gm_dof", C.c_int), ("gm_npts", C.c_int), ("gm_dt", C.c_double),
-        ("gm_accel", _pd), ("test", C.c_int), ("tol", C.c_double),
+        ("gm_accel", _pd), ("gm_count", C.c_int), ("gm_node_record", _pi),
+        ("test", C.c_int), ("tol", C.c_double),
         ("max_iter", C.c_int), ("load_const", C.c_int),
     ]
 
@@ -162,7 +164,8 @@ class PhaseDesc:
     def __init__(self, integrator=XG_INT_LOAD_CONTROL, pattern=0, num_steps=1,
                  d_lambda=0.0, dc_node=0, dc_dof=0, dc_incr=0.0, dt=0.0,
                  gamma=0.5, beta=0.25, alpha_m=0.0, beta_k=0.0, beta_k_init=0.0,
-                 beta_k_comm=0.0, gm_dof=0, gm_accel=None, gm_dt=0.0,
+                 beta_k_comm=0.0, gm_dof=0, gm_accel=None, gm_dt=0.0, gm_node_record=None,
+                 alpha_m_node=None, beta_k_init_elem=None,
                  test=XG_TEST_NORM_DISP_INCR, tol=1e-10, max_iter=25, load_const=0):
         self.kw = dict(integrator=integrator, pattern=pattern, num_steps=num_steps,
                        d_lambda=d_lambda, dc_node=dc_node, dc_dof=dc_dof, dc_incr=dc_incr,
@@ -170,7 +173,14 @@ class PhaseDesc:
                        beta_k_init=beta_k_init, beta_k_comm=beta_k_comm, gm_dof=gm_dof,
                        gm_dt=gm_dt, test=test, tol=tol, max_iter=max_iter,
                        load_const=load_const)
+        # gm_accel: one record [npts] or one per record index [count, npts]
         self.gm_accel = None if gm_accel is None else np.ascontiguousarray(gm_accel, np.float64)
+        self.gm_node_record = None if gm_node_record is None else \
+            np.ascontiguousarray(gm_node_record, np.int32)
+        self.alpha_m_node = None if alpha_m_node is None else \
+            np.ascontiguousarray(alpha_m_node, np.float64)
+        self.beta_k_init_elem = None if beta_k_init_elem is None else \
+            np.ascontiguousarray(beta_k_init_elem, np.float64)
 
     def __getattr__(self, name):
         kw = self.__dict__.get("kw")
@@ -180,7 +190,14 @@ class PhaseDesc:
 
     def struct(self):
         s = xg_phase_desc(**self.kw)
-        s.gm_npts = 0 if self.gm_accel is None else len(self.gm_accel)
+        if self.gm_accel is None:
+            s.gm_npts, s.gm_count = 0, 0
+        else:
+            a = self.gm_accel if self.gm_accel.ndim == 2 else self.gm_accel[None, :]
+            s.gm_count, s.gm_npts = a.shape
         s.gm_accel = _ptr(self.gm_accel, "d")
+        s.gm_node_record = _ptr(self.gm_node_record, "i")
+        s.alpha_m_node = _ptr(self.alpha_m_node, "d")
+        s.beta_k_init_elem = _ptr(self.beta_k_init_elem, "d")
         self._struct = s
         return s

@@ -24,7 +24,8 @@ Workloads (all FP64):
 import numpy as np
 
 from ._abi import (ModelDesc, PhaseDesc, XG_ELE_BRICK, XG_ELE_QUAD,
-                   XG_HANDLER_PLAIN, XG_INT_DISP_CONTROL, XG_TEST_NORM_DISP_INCR)
+                   XG_HANDLER_PLAIN, XG_INT_DISP_CONTROL, XG_INT_NEWMARK,
+                   XG_TEST_NORM_DISP_INCR)
 
 # nDMaterial J2Plasticity K G sigma0 sigma_inf delta H eta rho
 J2_STEEL = (166.7e9, 76.9e9, 250e6, 250e6, 0.0, 1e9, 0.0, 0.0)
@@ -386,3 +387,175 @@ def rc_frame_3d(bays_x=10, bays_y=10, stories=20, bay=6.0, story=3.5, col_fibers
                   max_iter=max_iter),
     ]
     return desc, phases
+
+
+# ---------------------------------------------------------------------------
+# transient: synthetic ground motions and frames under them
+# ---------------------------------------------------------------------------
+G = 9.81
+
+
+def kanai_tajimi(npts, dt, pga, seed, wg=15.6, zg=0.6, t_rise=2.0, t_decay=None):
+    """Seeded Kanai-Tajimi filtered white noise (ground filter frequency wg,
+    damping zg) under a trapezoidal envelope, scaled to peak ground
+    acceleration ``pga`` (m/s^2).  The filter is integrated exactly for a
+    piecewise-constant input over each sample interval."""
+    rng = np.random.default_rng(seed)
+    w = rng.normal(size=npts)
+    A = np.array([[0.0, 1.0], [-wg * wg, -2.0 * zg * wg]])
+    lam, V = np.linalg.eig(A)
+    Ad = np.real(V @ np.diag(np.exp(lam * dt)) @ np.linalg.inv(V))
+    Bd = np.real(np.linalg.solve(A, (Ad - np.eye(2)) @ np.array([0.0, -1.0])))
+    x = np.zeros(2)
+    ag = np.zeros(npts)
+    for k in range(npts):
+        x = Ad @ x + Bd * w[k]
+        ag[k] = -(2.0 * zg * wg * x[1] + wg * wg * x[0])
+    t = np.arange(npts) * dt
+    T = npts * dt
+    t_decay = 0.3 * T if t_decay is None else t_decay
+    env = np.minimum(1.0, t / t_rise) * np.minimum(1.0, np.maximum(0.0, (T - t) / t_decay))
+    ag *= env
+    peak = np.abs(ag).max()
+    return ag * (pga / peak) if peak > 0 else ag
+
+
+def rayleigh_2pct(stories, zeta=0.02):
+    """Rayleigh factors (alphaM, betaK0) giving ``zeta`` at the first and third
+    modes, with the periods estimated as T1 = 0.1 s per story and T3 = T1/5
+    (a uniform shear building's third mode), so no eigen-solution is needed
+    for thousands of frames; betaK multiplies the initial stiffness."""
+    w1 = 2.0 * np.pi / (0.1 * stories)
+    w3 = 5.0 * w1
+    return 2.0 * zeta * w1 * w3 / (w1 + w3), 2.0 * zeta / (w1 + w3)
+
+
+def steel_frame_2d_eq(bays=2, stories=3, steps=200, dt=0.01, pga=0.4 * G, seed=1,
+                      grav_steps=10, floor_mass=None, with_gravity=True, record=None,
+                      **frame_kw):
+    """The 2D steel frame of ``steel_frame_2d`` with lumped floor masses (the
+    gravity load over g at every floor node, horizontal and vertical),
+    gravity by LoadControl then `loadConst`, and a transient phase:
+    `integrator Newmark 0.5 0.25`, 2 % Rayleigh on the initial stiffness,
+    `pattern UniformExcitation` in x with a Kanai-Tajimi record."""
+    kw = dict(frame_kw)
+    kw.setdefault("seed", seed)
+    desc, phases = steel_frame_2d(bays, stories, steps=1, grav_steps=grav_steps, **kw)
+    gravity = kw.get("gravity", -150e3)
+    m = abs(gravity) / G if floor_mass is None else floor_mass
+    nn = desc.num_nodes
+    mass = np.zeros((nn, 3))
+    tags = np.asarray(desc.node_tag)
+    crd = desc.node_crd.reshape(-1, 2)
+    mass[crd[:, 1] > 0, 0] = m
+    mass[crd[:, 1] > 0, 1] = m
+    desc.arrays["node_mass"] = mass.ravel()
+    am, bk0 = rayleigh_2pct(stories)
+    rec = kanai_tajimi(steps + 2, dt, pga, seed + 1000) if record is None else record
+    quake = PhaseDesc(integrator=XG_INT_NEWMARK, pattern=2, num_steps=steps, dt=dt,
+                      gamma=0.5, beta=0.25, alpha_m=am, beta_k_init=bk0, gm_dof=0,
+                      gm_accel=rec, gm_dt=dt, tol=1e-10, max_iter=50)
+    phases = [phases[0], quake] if with_gravity else [quake]
+    desc.meta = dict(desc.meta, record_pga=pga, alpha_m=am, beta_k0=bk0)
+    del tags
+    return desc, phases
+
+
+def kanai_tajimi_batch(n, npts, dt, pgas, seed, wg=15.6, zg=0.6, t_rise=2.0):
+    """``n`` Kanai-Tajimi records at once (the filter of ``kanai_tajimi``
+    stepped over all records together), record r scaled to ``pgas[r]``."""
+    rng = np.random.default_rng(seed)
+    w = rng.normal(size=(n, npts))
+    A = np.array([[0.0, 1.0], [-wg * wg, -2.0 * zg * wg]])
+    lam, V = np.linalg.eig(A)
+    Ad = np.real(V @ np.diag(np.exp(lam * dt)) @ np.linalg.inv(V))
+    Bd = np.real(np.linalg.solve(A, (Ad - np.eye(2)) @ np.array([0.0, -1.0])))
+    x = np.zeros((2, n))
+    ag = np.zeros((n, npts))
+    for k in range(npts):
+        x = Ad @ x + Bd[:, None] * w[:, k][None, :]
+        ag[:, k] = -(2.0 * zg * wg * x[1] + wg * wg * x[0])
+    t = np.arange(npts) * dt
+    T = npts * dt
+    env = np.minimum(1.0, t / t_rise) * np.minimum(1.0, np.maximum(0.0, (T - t) / (0.3 * T)))
+    ag *= env[None, :]
+    peak = np.abs(ag).max(axis=1)
+    return ag * (np.asarray(pgas) / np.where(peak > 0, peak, 1.0))[:, None]
+
+
+def frame_batch(n_frames=4096, steps=2000, dt=0.01, seed=0, nfib=40, return_parts=False):
+    """``n_frames`` independent 2D steel moment frames in one model: bays
+    uniform in 1..12 and stories in 2..20, 40-fiber Steel02 wide-flange
+    sections with fy lognormal (median 350 MPa, CoV 0.1) and b uniform in
+    [0.005, 0.02] per frame, lumped floor masses, each under its own seeded
+    Kanai-Tajimi record (PGA uniform in [0.1, 0.8] g, dt 0.01 s), Newmark
+    (0.5, 0.25), 2 % Rayleigh on the initial stiffness with every frame's
+    own factors.  The frames share no node, so the model's parts converge
+    one by one; ``return_parts`` also returns every frame's own (desc,
+    phases) for comparisons."""
+    rng = np.random.default_rng(seed)
+    bays = rng.integers(1, 13, size=n_frames)
+    stories = rng.integers(2, 21, size=n_frames)
+    pgas = rng.uniform(0.1, 0.8, size=n_frames) * G
+    recs = kanai_tajimi_batch(n_frames, steps + 2, dt, pgas, seed + 7)
+    keys = ("node_tag", "node_crd", "node_mass", "elem_tag", "elem_conn", "elem_mat",
+            "uni_param", "fib_y", "fib_area", "fib_mat", "sp_node", "sp_dof", "sp_pattern",
+            "sp_value")
+    acc = {k: [] for k in keys}
+    uni_type, sec_start, node_rec, am_node, bk0_elem = [], [0], [], [], []
+    parts = []
+    node_off = elem_off = sec_off = uni_off = fib_off = 0
+    for f in range(n_frames):
+        d, ph = steel_frame_2d_eq(int(bays[f]), int(stories[f]), steps=steps, dt=dt,
+                                  seed=seed * 100003 + f + 1, with_gravity=False,
+                                  record=recs[f], nfib=nfib)
+        a = d.arrays
+        if return_parts:
+            parts.append((d, ph))
+        nn, ne = len(a["node_tag"]), len(a["elem_tag"])
+        acc["node_tag"].append(np.asarray(a["node_tag"]) + node_off)
+        acc["node_crd"].append(np.asarray(a["node_crd"]).reshape(-1, 2))
+        acc["node_mass"].append(np.asarray(a["node_mass"]))
+        acc["elem_tag"].append(np.asarray(a["elem_tag"]) + elem_off)
+        acc["elem_conn"].append(np.asarray(a["elem_conn"]).reshape(-1, 2) + node_off)
+        acc["elem_mat"].append(np.asarray(a["elem_mat"]) + sec_off)
+        acc["uni_param"].append(np.asarray(a["uni_param"]).reshape(-1, XG_UNI_NPARAM))
+        acc["fib_y"].append(np.asarray(a["fib_y"]))
+        acc["fib_area"].append(np.asarray(a["fib_area"]))
+        acc["fib_mat"].append(np.asarray(a["fib_mat"]) + uni_off)
+        acc["sp_node"].append(np.asarray(a["sp_node"]) + node_off)
+        acc["sp_dof"].append(np.asarray(a["sp_dof"]))
+        acc["sp_pattern"].append(np.asarray(a["sp_pattern"]))
+        acc["sp_value"].append(np.asarray(a["sp_value"]))
+        uni_type.extend(list(np.asarray(a["uni_type"])))
+        ss = np.asarray(a["sec_fiber_start"])
+        sec_start.extend(list(ss[1:] + fib_off))
+        node_rec.extend([f] * nn)
+        am_node.extend([ph[0].alpha_m] * nn)
+        bk0_elem.extend([ph[0].beta_k_init] * ne)
+        node_off = int(acc["node_tag"][-1].max())
+        elem_off = int(acc["elem_tag"][-1].max())
+        sec_off += len(ss) - 1
+        uni_off += len(a["uni_type"])
+        fib_off += int(ss[-1])
+    cat = {k: np.concatenate(v) for k, v in acc.items()}
+    desc = ModelDesc(
+        ndm=2, ndf=3, elem_type=XG_ELE_FBC2D, geom_transf=0, fbc_num_ip=5,
+        node_tag=cat["node_tag"], node_crd=cat["node_crd"], node_mass=cat["node_mass"],
+        elem_tag=cat["elem_tag"], elem_conn=cat["elem_conn"], elem_mat=cat["elem_mat"],
+        uni_type=uni_type, uni_param=cat["uni_param"], sec_fiber_start=sec_start,
+        fib_y=cat["fib_y"], fib_area=cat["fib_area"], fib_mat=cat["fib_mat"],
+        sp_node=cat["sp_node"], sp_dof=cat["sp_dof"], sp_pattern=cat["sp_pattern"],
+        sp_value=cat["sp_value"])
+    nfp = int(np.diff(np.asarray(sec_start))[cat["elem_mat"]].sum() * 5)
+    desc.meta = dict(workload=f"{n_frames} 2D steel frames", frames=n_frames,
+                     fiber_points=nfp, elements=len(cat["elem_tag"]),
+                     nodes=len(cat["node_tag"]))
+    quake = PhaseDesc(integrator=XG_INT_NEWMARK, pattern=2, num_steps=steps, dt=dt,
+                      gamma=0.5, beta=0.25, gm_dof=0, gm_accel=recs, gm_dt=dt,
+                      gm_node_record=np.asarray(node_rec, np.int32),
+                      alpha_m_node=np.asarray(am_node), beta_k_init_elem=np.asarray(bk0_elem),
+                      tol=1e-10, max_iter=50)
+    if return_parts:
+        return desc, [quake], parts
+    return desc, [quake]

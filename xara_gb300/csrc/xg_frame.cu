@@ -778,6 +778,48 @@ int launch_fbc_assemble(const FrameView &v, cudaStream_t s) {
   return cudaGetLastError() == cudaSuccess ? 0 : XG_ECUDA;
 }
 
+namespace {
+// ForceBeamColumn2d/3d::getInitialStiff (ForceBeamColumn2d.cpp:379-397,
+// getInitialFlexibility :1777-1830): f0 = sum of b' fs0 b wL, kv0 = f0^-1.
+template <int NB, int ORD>
+__global__ void k_fbc_kv0(FrameView v, double *st) {
+  const int e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= v.ne) return;
+  const int sec = v.sec[e];
+  const double *fs0 = v.fs0 + 16 * (long)sec;
+  const double L = v.L[e];
+  double f[NB * NB];
+#pragma unroll
+  for (int i = 0; i < NB * NB; i++) f[i] = 0.0;
+  constexpr int kRow[6] = {0, 1, 1, 2, 2, 3};
+  for (int ip = 0; ip < v.nip; ip++) {
+    const double xL = v.xi[ip], xL1 = xL - 1.0, wtL = v.wt[ip] * L;
+    const double ca[6] = {1.0, xL1, xL, xL1, xL, 1.0};
+#pragma unroll
+    for (int a = 0; a < NB; a++) {
+      const double wa = ca[a] * wtL;
+#pragma unroll
+      for (int c = 0; c < NB; c++) f[a * NB + c] += wa * (fs0[kRow[a] * ORD + kRow[c]] * ca[c]);
+    }
+  }
+  double kv[NB * NB];
+  elem_inverse<NB>(f, kv);
+  double *rec = st + (long)e * st_stride(v.nip);
+#pragma unroll
+  for (int i = 0; i < 6; i++) rec[i] = 0.0;
+#pragma unroll
+  for (int i = 0; i < NB * NB; i++) rec[6 + i] = kv[i];
+}
+}  // namespace
+
+int launch_fbc_kv0(const FrameView &v, double *st_scratch, cudaStream_t s) {
+  if (v.ne == 0) return 0;
+  const int grid = (v.ne + 127) / 128;
+  if (v.nb == 3) k_fbc_kv0<3, 2><<<grid, 128, 0, s>>>(v, st_scratch);
+  else k_fbc_kv0<6, 4><<<grid, 128, 0, s>>>(v, st_scratch);
+  return cudaGetLastError() == cudaSuccess ? 0 : XG_ECUDA;
+}
+
 int launch_fbc_commit(const FrameView &v, double *st_c, double *fh_c, long nrec, cudaStream_t s) {
   const long nst = (long)v.ne * frame_state_stride(v.nip);
   const long n = nst > nrec ? nst : nrec;

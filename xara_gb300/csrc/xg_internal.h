@@ -151,4 +151,43 @@ int launch_fbc_update(const FrameView &v, cudaStream_t s);
 int launch_fbc_assemble(const FrameView &v, cudaStream_t s);
 int launch_fbc_commit(const FrameView &v, double *st_c, double *fh_c, long nrec, cudaStream_t s);
 int launch_fbc_revert(const FrameView &v, const double *st_c, long nrec, cudaStream_t s);
+// Fill st_scratch (frame_state_stride records) with Se = 0 and kv = the
+// initial element stiffness (ForceBeamColumn*::getInitialStiff), so that
+// launch_fbc_assemble on a view whose st is st_scratch gives K0 per element.
+int launch_fbc_kv0(const FrameView &v, double *st_scratch, cudaStream_t s);
+
+// Transient step (xg_dynamic.cu)
+struct DynView {
+  int nu, neq, ndf;
+  long nnz;
+  const int *eqn;             // [nu] equation of each (node, dof)
+  double *U, *V, *A;          // [nu] trial displacement, velocity, acceleration
+  const double *Vc, *Ac;      // [nu] committed velocity, acceleration
+  const double *mass;         // [nu] lumped mass
+  const int *eq_ptr, *eq_dofs;  // (node, dof) list of each equation
+  const double *meq;          // [neq] mass summed on each equation
+  const double *meq_am;       // [neq] alphaM-weighted mass on each equation
+  const double *am_node;      // [nn] alphaM per node or null
+  const int *diag_pos;        // [neq] CSR position of each diagonal
+  int gm_npts, gm_dof;        // UniformExcitation records
+  double gm_dt;
+  const double *gm;           // [records*gm_npts]
+  const int *gm_rec;          // [nn] record of each node or null
+};
+int launch_newmark_predict(const DynView &d, double a1, double a2, double a3, double a4,
+                           cudaStream_t s);
+int launch_newmark_correct(const DynView &d, const double *dU, double c2, double c3,
+                           cudaStream_t s);
+int launch_dyn_unbalance(const DynView &d, const double *fext, const double *pint,
+                         const double *k0vals, const int *rowptr, const int *colidx,
+                         double bk0, double am, double t, double *veq, double *k0v, double *B,
+                         cudaStream_t s);
+int launch_dyn_tangent(const DynView &d, double *vals, const double *k0vals, double c1,
+                       double c2bk0, double c2, double c3, cudaStream_t s);
+// x[b*len + i] *= scale ? scale[b] : s0
+int launch_scale_blocks(int nblk, int len, const double *scale, double s0, double *x,
+                        cudaStream_t s);
+int launch_comp_norm2(int ncomp, const int *cstart, const double *x, double *out,
+                      cudaStream_t s);
+int launch_comp_mask(int neq, const int *comp_of, const int *active, double *B, cudaStream_t s);
 }  // namespace xg

@@ -172,6 +172,26 @@ struct xg_model {
   // Newton vectors
   DBuf<double> d_fext, d_B, d_dU, d_phat, d_dUhat, d_x, d_b, d_norm, d_Fref;
   std::vector<int> ref_patterns;               // pattern id of each d_Fref row
+  // transient (Newmark, Rayleigh, UniformExcitation)
+  std::vector<double> node_mass;               // [nn*ndf]
+  DBuf<double> d_V, d_A, d_Vc, d_Ac, d_mass, d_meq, d_meq_am, d_am_node, d_bk0_elem;
+  DBuf<double> d_K0vals, d_veq, d_k0v, d_gm, d_cnorm;
+  DBuf<int> d_eq_ptr, d_eq_dofs, d_diag_pos, d_gm_rec, d_cstart, d_comp_of, d_active;
+  std::vector<int> comp_start;                 // equation ranges of disconnected parts
+  bool k0_ready = false;
+  DynView dview() {
+    DynView v{};
+    v.nu = nn * ndf; v.neq = neq; v.ndf = ndf; v.nnz = nnz;
+    v.eqn = d_eqn.p; v.U = d_U.p; v.V = d_V.p; v.A = d_A.p; v.Vc = d_Vc.p; v.Ac = d_Ac.p;
+    v.mass = d_mass.p; v.eq_ptr = d_eq_ptr.p; v.eq_dofs = d_eq_dofs.p; v.meq = d_meq.p;
+    v.meq_am = d_meq_am.p; v.am_node = phase.alpha_m_node ? d_am_node.p : nullptr;
+    v.diag_pos = d_diag_pos.p;
+    v.gm_npts = phase.gm_npts; v.gm_dof = phase.gm_dof; v.gm_dt = phase.gm_dt;
+    v.gm = d_gm.p; v.gm_rec = phase.gm_node_record ? d_gm_rec.p : nullptr;
+    return v;
+  }
+  int upload_dynamics();
+  int step_newmark(xg_step_stats *st);
   // analysis state
   xg_phase_desc phase{};
   bool have_phase = false;
@@ -613,6 +633,7 @@ int xg_model::upload(const HostGather &gk_h, const HostGather &gr_h) {
       }
     }
   if (!F.empty()) RET(d_Fref.upload(F.data(), F.size(), s));
+  RET(upload_dynamics());
   if (frames()) {
     RET(upload_frames());
   } else {
@@ -813,6 +834,162 @@ int xg_model::upload_frames() {
 
 // Domain::update (when compute) and the element K / P assembled into the
 // CSR values and the resisting force.
+// Per-equation (node, dof) lists, masses and diagonal positions, zero
+// velocity and acceleration, and the disconnected parts of the model (each
+// a contiguous equation range after RCM) for per-part convergence.
+int xg_model::upload_dynamics() {
+  cudaStream_t s = stream;
+  const int nu = nn * ndf;
+  std::vector<int> cnt(neq + 1, 0), ptr(neq + 1, 0), dofs(std::max(nu, 1), 0);
+  for (int a = 0; a < nu; a++)
+    if (eqn[a] >= 0) cnt[eqn[a]]++;
+  for (int e = 0; e < neq; e++) ptr[e + 1] = ptr[e] + cnt[e];
+  std::vector<int> fillp(ptr.begin(), ptr.end() - 1);
+  std::vector<double> meq(std::max(neq, 1), 0.0);
+  for (int a = 0; a < nu; a++) {
+    const int e = eqn[a];
+    if (e < 0) continue;
+    dofs[fillp[e]++] = a;
+    meq[e] += node_mass[a];
+  }
+  std::vector<int> dpos(std::max(neq, 1), 0);
+  for (int e = 0; e < neq; e++) {
+    const int *b = colidx.data() + rowptr[e], *en = colidx.data() + rowptr[e + 1];
+    dpos[e] = (int)(std::lower_bound(b, en, e) - colidx.data());
+  }
+  RET(d_eq_ptr.upload(ptr.data(), ptr.size(), s));
+  RET(d_eq_dofs.upload(dofs.data(), dofs.size(), s));
+  RET(d_meq.upload(meq.data(), meq.size(), s));
+  RET(d_diag_pos.upload(dpos.data(), dpos.size(), s));
+  RET(d_mass.upload(node_mass.data(), std::max<size_t>(node_mass.size(), 1), s));
+  for (auto *b : {&d_V, &d_A, &d_Vc, &d_Ac}) {
+    RET(b->alloc(std::max(nu, 1)));
+    CK(cudaMemsetAsync(b->p, 0, std::max(nu, 1) * sizeof(double), s));
+  }
+  RET(d_veq.alloc(std::max(neq, 1)));
+  RET(d_k0v.alloc(std::max(neq, 1)));
+  // disconnected parts: union of the nodes of every element and equalDOF pair
+  std::vector<int> parent(nn);
+  for (int i = 0; i < nn; i++) parent[i] = i;
+  auto find = [&](int x) {
+    while (parent[x] != x) x = parent[x] = parent[parent[x]];
+    return x;
+  };
+  for (int e = 0; e < ne; e++)
+    for (int a = 1; a < nen; a++) {
+      const int x = find(conn[(size_t)e * nen]), y = find(conn[(size_t)e * nen + a]);
+      if (x != y) parent[std::max(x, y)] = std::min(x, y);
+    }
+  for (size_t q = 0; q < mp_c.size(); q++) {
+    const int x = find(mp_c[q]), y = find(mp_r[q]);
+    if (x != y) parent[std::max(x, y)] = std::min(x, y);
+  }
+  std::vector<int> lo(nn, INT32_MAX), hi(nn, -1), count(nn, 0);
+  for (int a = 0; a < nu; a++) {
+    const int e = eqn[a];
+    if (e < 0) continue;
+    const int r = find(a / ndf);
+    lo[r] = std::min(lo[r], e);
+    hi[r] = std::max(hi[r], e);
+  }
+  for (int e = 0; e < neq; e++) count[find(dofs[ptr[e]] / ndf)]++;
+  std::vector<std::pair<int, int>> ranges;
+  bool contiguous = true;
+  for (int r = 0; r < nn; r++) {
+    if (hi[r] < 0) continue;
+    if (hi[r] - lo[r] + 1 != count[r]) contiguous = false;
+    ranges.push_back({lo[r], hi[r] + 1});
+  }
+  std::sort(ranges.begin(), ranges.end());
+  comp_start.assign(1, 0);
+  if (contiguous) {
+    for (auto &rg : ranges) comp_start.push_back(rg.second);
+  } else {
+    comp_start.push_back(neq);
+  }
+  const int ncomp = (int)comp_start.size() - 1;
+  std::vector<int> comp_of(std::max(neq, 1), 0);
+  for (int c = 0; c < ncomp; c++)
+    for (int e = comp_start[c]; e < comp_start[c + 1]; e++) comp_of[e] = c;
+  RET(d_cstart.upload(comp_start.data(), comp_start.size(), s));
+  RET(d_comp_of.upload(comp_of.data(), comp_of.size(), s));
+  RET(d_active.alloc(std::max(ncomp, 1)));
+  RET(d_cnorm.alloc(std::max(ncomp, 1)));
+  return 0;
+}
+
+// One transient step: Newmark::newStep, NewtonRaphson::solveCurrentStep with
+// the effective tangent and the dynamic unbalance, then commit.  Each
+// disconnected part of the model carries its own convergence test: a part
+// whose displacement increment (or unbalance) norm has passed stops
+// iterating -- its right-hand side is zeroed, so its state does not move --
+// while the others go on, exactly as if every part ran alone.
+int xg_model::step_newmark(xg_step_stats *st) {
+  cudaStream_t s = stream;
+  last_solver_iters = 0;
+  const double t_commit = time;
+  const double dt = phase.dt, gam = phase.gamma, bet = phase.beta;
+  const double c1 = 1.0, c2 = gam / (bet * dt), c3 = 1.0 / (bet * dt * dt);
+  const double a1 = 1.0 - gam / bet, a2 = dt * (1.0 - 0.5 * gam / bet);
+  const double a3 = -1.0 / (bet * dt), a4 = 1.0 - 0.5 / bet;
+  const double am = phase.alpha_m;
+  DynView dv = dview();
+  const int ncomp = (int)comp_start.size() - 1;
+  std::vector<int> active(std::max(ncomp, 1), 1), iters(std::max(ncomp, 1), 0);
+  std::vector<double> cn(std::max(ncomp, 1));
+  CK(cudaMemcpyAsync(d_active.p, active.data(), ncomp * sizeof(int), cudaMemcpyHostToDevice, s));
+  RET(launch_newmark_predict(dv, a1, a2, a3, a4, s));
+  time += dt;
+  RET(element_state(true));          // Domain::update in updateDomain
+  int it = 0, nactive = ncomp;
+  bool ok = false;
+  while (true) {
+    RET(form_fext(time));
+    RET(launch_dyn_unbalance(dv, d_fext.p, d_resid.p, d_K0vals.p, d_rowptr.p, d_colidx.p,
+                             k0_ready ? 1.0 : 0.0, am, time, d_veq.p, d_k0v.p, d_B.p, s));
+    if (it > 0) {
+      RET(launch_comp_norm2(ncomp, d_cstart.p,
+                            phase.test == XG_TEST_NORM_DISP_INCR ? d_dU.p : d_B.p, d_cnorm.p, s));
+      CK(cudaMemcpyAsync(cn.data(), d_cnorm.p, ncomp * sizeof(double), cudaMemcpyDeviceToHost, s));
+      CK(cudaStreamSynchronize(s));
+      for (int c = 0; c < ncomp; c++)
+        if (active[c] && std::sqrt(cn[c]) <= phase.tol) {
+          active[c] = 0;
+          iters[c] = it;
+          nactive--;
+        }
+      if (nactive == 0) { ok = true; break; }
+      if (it >= phase.max_iter) break;
+      CK(cudaMemcpyAsync(d_active.p, active.data(), ncomp * sizeof(int), cudaMemcpyHostToDevice,
+                         s));
+      if (ncomp > 1) RET(launch_comp_mask(neq, d_comp_of.p, d_active.p, d_B.p, s));
+    }
+    RET(launch_dyn_tangent(dv, d_vals.p, d_K0vals.p, c1, k0_ready ? c2 : 0.0, c2, c3, s));
+    blocks_factored = false;
+    prof_factored = false;
+    RET(solve(d_B.p, d_dU.p, nullptr));
+    RET(launch_newmark_correct(dv, d_dU.p, c2, c3, s));
+    RET(element_state(true));
+    it++;
+  }
+  if (st) {
+    st->newton_iters = it;
+    st->solver_iters = last_solver_iters;
+    st->elem_iters = 0;
+    st->status = ok ? 0 : XG_ENOCONV;
+  }
+  if (!ok) {
+    time = t_commit;
+    return fail(XG_ENOCONV, "Newton did not converge in %d iterations (%d of %d parts)", it,
+                nactive, ncomp);
+  }
+  RET(commit_state());
+  CK(cudaMemcpyAsync(d_Vc.p, d_V.p, (size_t)nn * ndf * sizeof(double), cudaMemcpyDeviceToDevice, s));
+  CK(cudaMemcpyAsync(d_Ac.p, d_A.p, (size_t)nn * ndf * sizeof(double), cudaMemcpyDeviceToDevice, s));
+  time_c = time;
+  return 0;
+}
+
 int xg_model::element_state(bool compute) {
   ContinuumView v = view();
   cudaStream_t s = stream;
@@ -967,8 +1144,58 @@ int xg_model::init_phase() {
     RET(form_fext(time + 1.0));
     RET(element_state(false));
     RET(launch_sub(neq, d_fext.p, d_resid.p, d_phat.p, stream));
+  } else if (phase.integrator == XG_INT_NEWMARK) {
+    if (phase.dt <= 0.0 || phase.beta == 0.0)
+      return fail(XG_EINVAL, "Newmark needs dt > 0 and beta != 0");
+    if (phase.beta_k != 0.0 || phase.beta_k_comm != 0.0)
+      return fail(XG_EINVAL, "Rayleigh betaK and betaKc are not supported (use betaK0)");
+    const bool any_bk0 = phase.beta_k_init != 0.0 || phase.beta_k_init_elem != nullptr;
+    if (any_bk0 && !frames())
+      return fail(XG_EINVAL, "Rayleigh betaK0 needs force-based frame elements");
+    {
+      // alphaM-weighted mass on each equation
+      std::vector<double> meq_am(std::max(neq, 1), 0.0), amn;
+      if (phase.alpha_m_node) amn.assign(phase.alpha_m_node, phase.alpha_m_node + nn);
+      for (int a = 0; a < nn * ndf; a++) {
+        const int e = eqn[a];
+        if (e < 0) continue;
+        meq_am[e] += (phase.alpha_m_node ? amn[a / ndf] : phase.alpha_m) * node_mass[a];
+      }
+      RET(d_meq_am.upload(meq_am.data(), meq_am.size(), stream));
+      if (phase.alpha_m_node) RET(d_am_node.upload(amn.data(), amn.size(), stream));
+    }
+    if (phase.gm_npts > 0) {
+      const int nrec = std::max(phase.gm_count, 1);
+      if (!phase.gm_accel || phase.gm_dt <= 0.0 || phase.gm_dof < 0 || phase.gm_dof >= ndf)
+        return fail(XG_EINVAL, "bad ground motion");
+      RET(d_gm.upload(phase.gm_accel, (size_t)nrec * phase.gm_npts, stream));
+      if (phase.gm_node_record) {
+        for (int i = 0; i < nn; i++)
+          if (phase.gm_node_record[i] < 0 || phase.gm_node_record[i] >= nrec)
+            return fail(XG_EINVAL, "ground-motion record of node %d out of range", i);
+        RET(d_gm_rec.upload(phase.gm_node_record, nn, stream));
+      }
+    }
+    k0_ready = false;
+    if (any_bk0) {
+      // betaK0 K0: K0 per element (records with Se = 0, kv = kv0), scaled
+      // by the element's betaK0, gathered into CSR values
+      DBuf<double> st0;
+      RET(st0.alloc((size_t)ne * frame_state_stride(fb_nip)));
+      RET(launch_fbc_kv0(fview(), st0.p, stream));
+      FrameView fv = fview();
+      fv.st = st0.p;
+      RET(launch_fbc_assemble(fv, stream));
+      if (phase.beta_k_init_elem) RET(d_bk0_elem.upload(phase.beta_k_init_elem, ne, stream));
+      RET(launch_scale_blocks(ne, ke_size(), phase.beta_k_init_elem ? d_bk0_elem.p : nullptr,
+                              phase.beta_k_init, d_Ke.p, stream));
+      RET(d_K0vals.alloc(nnz > 0 ? nnz : 1));
+      RET(launch_gather(gk, d_Ke.p, d_partial.p, d_K0vals.p, stream));
+      CK(cudaStreamSynchronize(stream));
+      k0_ready = true;
+    }
   } else if (phase.integrator != XG_INT_LOAD_CONTROL) {
-    return fail(XG_EINVAL, "integrator %d not supported by the continuum set", phase.integrator);
+    return fail(XG_EINVAL, "integrator %d not supported", phase.integrator);
   }
   return 0;
 }
@@ -982,6 +1209,7 @@ static int read_scalar(const double *d, double *h, cudaStream_t s) {
 // One step: integrator newStep, NewtonRaphson::solveCurrentStep, commit
 // (runtime/runtime/BasicAnalysisBuilder.cpp:337-420).
 int xg_model::step(xg_step_stats *st) {
+  if (phase.integrator == XG_INT_NEWMARK) return step_newmark(st);
   cudaStream_t s = stream;
   last_solver_iters = 0;
   const int nu = nn * ndf;
@@ -1076,6 +1304,9 @@ int xg_model::revert_state() {
     CK(cudaMemcpyAsync(d_tan.p, d_tan_c.p, np * ntan() * sizeof(double), cudaMemcpyDeviceToDevice, s));
   }
   CK(cudaMemcpyAsync(d_U.p, d_Uc.p, (size_t)nn * ndf * sizeof(double), cudaMemcpyDeviceToDevice, s));
+  // Newmark::revertToLastStep
+  CK(cudaMemcpyAsync(d_V.p, d_Vc.p, (size_t)nn * ndf * sizeof(double), cudaMemcpyDeviceToDevice, s));
+  CK(cudaMemcpyAsync(d_A.p, d_Ac.p, (size_t)nn * ndf * sizeof(double), cudaMemcpyDeviceToDevice, s));
   // Domain::revertToLastCommit ends with Domain::update at the committed
   // displacements (domain/domain/Domain.cpp:1925-1949)
   return element_state(true);
@@ -1168,6 +1399,8 @@ static int plan_model(const xg_model_desc *d, xg_model **out) {
   m->ned = m->nen * m->ndf;
   m->thickness = d->thickness;
   m->node_tag.assign(d->node_tag, d->node_tag + m->nn);
+  if (d->node_mass) m->node_mass.assign(d->node_mass, d->node_mass + (size_t)m->nn * d->ndf);
+  else m->node_mass.assign((size_t)m->nn * d->ndf, 0.0);
   for (int i = 1; i < m->nn; i++)
     if (m->node_tag[i] <= m->node_tag[i - 1]) {
       delete m;
@@ -1537,6 +1770,8 @@ int xg_reset(xg_model *m) {
   const size_t nu = (size_t)m->nn * m->ndf;
   CK(cudaMemsetAsync(m->d_U.p, 0, nu * sizeof(double), s));
   CK(cudaMemsetAsync(m->d_Uc.p, 0, nu * sizeof(double), s));
+  for (auto *b : {&m->d_V, &m->d_A, &m->d_Vc, &m->d_Ac})
+    CK(cudaMemsetAsync(b->p, 0, std::max<size_t>(nu, 1) * sizeof(double), s));
   if (m->frames()) {
     RET(m->upload_frames());
   } else {
