@@ -21,7 +21,13 @@ iterations/s is reported beside it.
 Workload `brick`: the element phase of the stdBrick J2 block 128 x 128 x 64
 (1,048,576 bricks, 8,388,608 integration points), one pass per step.
 
-  python bench.py [--workload frame3d|brick] [--gpus N] [--steps K] [--warmup W]
+Workload `batch`: 4,096 independent 2D steel frames (1-12 bays, 2-20
+stories, 40-fiber Steel02 sections), each under its own Kanai-Tajimi record,
+in one device model; a step is one Newmark time step of every frame (its
+Newton iterations, each frame converging on its own).  Metric: frame time
+steps/s, beside the same kernels run one frame per model.
+
+  python bench.py [--workload frame3d|brick|batch] [--gpus N] [--steps K] [--warmup W]
                   [--impl xara|reference]
 
 --impl reference times the reference algorithm's CPU path (the C oracle, a
@@ -478,6 +484,209 @@ def run_reference_frame(args):
 
 
 # ---------------------------------------------------------------------------
+# batch: thousands of independent 2D frames under their own ground motions
+# ---------------------------------------------------------------------------
+BATCH_FRAMES = 4096
+BATCH_SAMPLE = 32          # frames of the per-model GPU loop
+BATCH_CPU_FRAMES = 8       # frames of the one-core CPU sample
+
+
+def batch_model(nframes, steps):
+    from xara_gb300 import configs
+    return configs.frame_batch(nframes, steps=steps, seed=0, return_parts=True)
+
+
+def run_batch(args):
+    world, rank, local, torch, dist = dist_setup()
+    from xara_gb300 import gpu
+    lead, nsteps = args.batch_lead, args.batch_lead + args.warmup + args.steps
+    desc, phases, parts = batch_model(args.frames, nsteps)
+    t_setup = time.perf_counter()
+    m = gpu.DeviceModel(desc)
+    m.set_system(gpu.XG_SYSTEM_BJPCG)
+    m.set_phase(phases[0])
+    t_setup = time.perf_counter() - t_setup
+    stream = torch.cuda.ExternalStream(gpu.model_stream(m))
+
+    def barrier():
+        if world > 1:
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    m.analyze(lead + args.warmup)                 # into the strong motion, untimed
+    gpu.profile_enable(m, True)
+    sampler = ClockSampler(local if world == 1 else 0)
+    sampler.start()
+    ev0 = torch.cuda.Event(enable_timing=True)
+    ev1 = torch.cuda.Event(enable_timing=True)
+    barrier()
+    ev0.record(stream)
+    stats = m.analyze(args.steps)
+    ev1.record(stream)
+    barrier()
+    clocks = sampler.stop()
+    dt = max_over_ranks(ev0.elapsed_time(ev1) * 1e-3, world, torch, dist)
+    points, sections, elems = gpu.profile_counters(m)
+    prof = gpu.profile_read(m)
+    gpu.profile_enable(m, False)
+    frame_steps = args.frames * args.steps * world
+    value = frame_steps / dt
+    newton = sum(s_[0] for s_ in stats)
+
+    # end to end through the C ABI: every step xg_analyze, then the committed
+    # displacements of all frames copied to pinned host memory (a recorder)
+    uh = torch.empty(m.nu, dtype=torch.float64).pin_memory()
+    L = gpu.lib()
+    lam = C.c_double()
+    st_buf = (gpu.xg_step_stats * 1)()
+    barrier()
+    t0 = time.perf_counter()
+    for _ in range(args.e2e_steps):
+        gpu._check(L.xg_analyze(m.h, 1, st_buf))
+        gpu._check(L.xg_get_disp(m.h, C.c_void_p(uh.data_ptr()), C.byref(lam)))
+    barrier()
+    dt_e2e = max_over_ranks(time.perf_counter() - t0, world, torch, dist)
+    e2e_value = args.frames * args.e2e_steps * world / dt_e2e
+    m.close()
+
+    # the per-model GPU loop: the same kernels, one frame per model, on a
+    # sample of the batch's frames over the same window of their records
+    t_loop, n_loop = 0.0, 0
+    for d, p in parts[:BATCH_SAMPLE]:
+        mm = gpu.DeviceModel(d)
+        mm.set_system(gpu.XG_SYSTEM_BJPCG)
+        mm.set_phase(p[0])
+        mm.analyze(lead + args.warmup)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        mm.analyze(args.steps)
+        torch.cuda.synchronize()
+        t_loop += time.perf_counter() - t0
+        n_loop += args.steps
+        mm.close()
+    loop_value = n_loop / t_loop
+    if rank != 0:
+        dist.destroy_process_group()
+        return 0
+    kernels = {k: v for k, v in prof.items() if v[1] > 0 and k != "return_map_cap_hits"}
+    dominant = max(kernels, key=lambda k: kernels[k][0])
+    dom_ms, dom_launches = kernels[dominant]
+    peak, peak_kind = measured_peaks()
+    alg = frame_alg_bytes(desc, 0, 0)["fbc_update"]
+    achieved = alg / (dom_ms * 1e-3 / max(dom_launches, 1)) / 1e9 if dominant == "fbc_update" \
+        else None
+    line = {
+        "metric": "frame-steps/s (batched)", "value": value, "unit": "frame time steps/s",
+        "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": 1e3 * dt / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic (seeded frames and Kanai-Tajimi records)",
+        "config": {"workload": f"{args.frames} independent 2D steel frames (BASELINE config 3): "
+                               "Newmark time steps, each frame under its own record",
+                   "frames": args.frames, "elements": desc.meta["elements"],
+                   "fiber_points": desc.meta["fiber_points"], "equations": m.neq,
+                   "timed_window": f"steps {lead + args.warmup}..{lead + args.warmup + args.steps}"
+                                   f" of the records (dt 0.01 s)",
+                   "system": "block-Jacobi PCG (rtol 1e-12)", "parallelism": f"replicas x{world}"},
+        "ip_updates_per_s": points / dt,
+        "newton_iters_per_step": newton / args.steps,
+        "per_model_gpu_loop": {"value": loop_value, "unit": "frame time steps/s",
+                               "frames": min(BATCH_SAMPLE, len(parts)),
+                               "note": "the same kernels, one frame per model, same steps"},
+        "batched_over_per_model": value / loop_value,
+        "e2e": {"value": e2e_value, "unit": "frame time steps/s", "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": int(uh.numel() * 8),
+                "path": "xg_analyze + xg_get_disp into pinned host memory every step; the "
+                        "records are resident"},
+        "gpu_launches": int(sum(v[1] for v in kernels.values())),
+        "roofline": {"bound": "hbm", "kernel": dominant,
+                     "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": achieved / peak if achieved and peak else None,
+                     "peak_source": peak_kind, "traffic": ncu_traffic("batch", dominant),
+                     "algorithmic_bytes_per_launch": alg},
+        "kernels_ms_per_step": {k: v[0] / args.steps for k, v in kernels.items()},
+        "clocks": clocks,
+        "setup_s": t_setup,
+    }
+    if not args.no_cpu_baseline:
+        rate, sample = batch_cpu_sample(parts[:BATCH_CPU_FRAMES], lead + args.warmup,
+                                        args.steps)
+        line["cpu_baseline"] = {"value": rate, "unit": "frame time steps/s", "cores": 1,
+                                "kind": "port", "sample": sample}
+    print(json.dumps(line))
+    if world > 1:
+        dist.destroy_process_group()
+    return 0
+
+
+def _batch_cpu(parts, lead, steps):
+    from oracle import port
+    from xara_gb300._abi import PhaseDesc
+    t, n = 0.0, 0
+    for d, p in parts:
+        o = port.OracleModel(d)
+        kw = dict(p[0].kw)
+        a = PhaseDesc(**{**kw, "num_steps": lead}, gm_accel=p[0].gm_accel)
+        o.run([a])
+        b = PhaseDesc(**{**kw, "num_steps": steps}, gm_accel=p[0].gm_accel)
+        t0 = time.perf_counter()
+        o.run([b])
+        t += time.perf_counter() - t0
+        n += steps
+        o.close()
+    return n, t
+
+
+def batch_cpu_sample(parts, lead, steps):
+    n, t = _batch_cpu(parts, lead, steps)
+    return n / t, (f"{len(parts)} frames of the batch, steps {lead}..{lead + steps} each "
+                   f"(Newmark, Newton, ProfileSPD), 1 thread")
+
+
+def _batch_worker(args):
+    idx, lead, steps, nframes = args
+    _, _, parts = batch_model(nframes, lead + steps + 2)
+    return _batch_cpu([parts[i] for i in idx], lead, steps)
+
+
+def run_reference_batch(args):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return 0
+    import multiprocessing as mp
+    cores = os.cpu_count() or 1
+    lead = args.batch_lead + args.warmup
+    per = 2
+    jobs = [(list(range(c * per, (c + 1) * per)), lead, args.steps, args.frames)
+            for c in range(cores)]
+    ctx = mp.get_context("spawn")
+    t0 = time.perf_counter()
+    with ctx.Pool(cores) as pool:
+        res = pool.map(_batch_worker, jobs, chunksize=1)
+    wall = time.perf_counter() - t0
+    n = sum(r[0] for r in res)
+    tmax = max(r[1] for r in res)
+    value = n / tmax
+    line = {
+        "impl": "reference", "metric": "frame-steps/s (batched)", "value": value,
+        "unit": "frame time steps/s", "n_gpus": args.gpus, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": 1e3 * tmax / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic (seeded frames and Kanai-Tajimi records)",
+        "config": {"workload": f"{args.frames} independent 2D steel frames (BASELINE config 3)"},
+        "cpu_baseline": {"value": value, "unit": "frame time steps/s", "cores": cores,
+                         "kind": "port",
+                         "sample": f"{cores} processes x {per} frames, steps {lead}.."
+                                   f"{lead + args.steps}"},
+        "e2e": {"value": value, "unit": "frame time steps/s", "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+        "wall_s": wall,
+    }
+    print(json.dumps(line))
+    return 0
+
+
+# ---------------------------------------------------------------------------
 # brick: the element phase of the stdBrick J2 block
 # ---------------------------------------------------------------------------
 def brick_trial_field(desc, nx, ny, nz, eps=2.5e-3):
@@ -674,7 +883,7 @@ def run_brick(args):
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--workload", default="frame3d", choices=["frame3d", "brick"])
+    ap.add_argument("--workload", default="frame3d", choices=["frame3d", "brick", "batch"])
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
@@ -683,12 +892,15 @@ def main():
     ap.add_argument("--no-analysis", action="store_true")
     ap.add_argument("--analysis-steps", type=int, default=5)
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
+    ap.add_argument("--frames", type=int, default=BATCH_FRAMES)
+    ap.add_argument("--batch-lead", type=int, default=150)
+    ap.add_argument("--e2e-steps", type=int, default=3)
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     if args.impl == "reference":
-        return run_reference_frame(args) if args.workload == "frame3d" else \
-            run_reference_brick(args)
-    return run_frame(args) if args.workload == "frame3d" else run_brick(args)
+        return {"frame3d": run_reference_frame, "brick": run_reference_brick,
+                "batch": run_reference_batch}[args.workload](args)
+    return {"frame3d": run_frame, "brick": run_brick, "batch": run_batch}[args.workload](args)
 
 
 if __name__ == "__main__":
