@@ -14,6 +14,7 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <cstdlib>
 #include <vector>
 #include <array>
 
@@ -408,10 +409,11 @@ int xref_run_phase(void *hp, const xg_phase_desc *ph, int cap_begin, int cap_end
   add_pattern(h, ph->pattern);
 
   ConvergenceTest *test = nullptr;
+  const int print_flag = getenv("XREF_TEST_PRINT") ? 1 : 0;   // the test's own trace
   if (ph->test == XG_TEST_NORM_DISP_INCR)
-    test = new CTestNormDispIncr(ph->tol, ph->max_iter, 0);
+    test = new CTestNormDispIncr(ph->tol, ph->max_iter, print_flag);
   else
-    test = new CTestNormUnbalance(ph->tol, ph->max_iter, 0);
+    test = new CTestNormUnbalance(ph->tol, ph->max_iter, print_flag);
   NewtonRaphson *algo = new NewtonRaphson(*test);
   IncrementalIntegrator *integ = nullptr;
   TransientIntegrator *transient = nullptr;

@@ -135,6 +135,8 @@ def main():
     model_fixture("frame3d_2x1x3", configs.rc_frame_3d, (2, 1, 3),
                   {"col_fibers": 60, "beam_fibers": 40, "steps": 30, "pdelta": 1})
     model_fixture("frame2d_eq_2x3", configs.steel_frame_2d_eq, (2, 3), {"steps": 150})
+    model_fixture("frame2d_pd_2x3", configs.steel_frame_2d, (2, 3), {"steps": 12, "pdelta": 1},
+                  capture_steps=(0,))
     revert_fixture("revert_frame2d_2x3", configs.steel_frame_2d, (2, 3), {"steps": 10})
     revert_fixture("revert_frame3d_1x1x2", configs.rc_frame_3d, (1, 1, 2),
                    {"col_fibers": 40, "beam_fibers": 24, "steps": 10, "pdelta": 1})

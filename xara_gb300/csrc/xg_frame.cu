@@ -705,6 +705,22 @@ __global__ void k_fbc_assemble(FrameView v) {
     for (int k = 0; k < NB; k++) p += T[k][i] * Se[k];
     Re[i] = p;
   }
+  if (NB == 3 && v.pdelta2d) {
+    // PDeltaCrdTransf2d (coordTransformation/PDeltaCrdTransf2d.cpp:508-700):
+    // K += (N/L) g g', P += (N/L)(g . u) g with g = [-s c 0 s -c 0]
+    const double cs = R[0], sn = R[1];
+    const int a = v.conn[2 * e], b = v.conn[2 * e + 1];
+    const double *uI = v.U + (long)a * v.ndf, *uJ = v.U + (long)b * v.ndf;
+    const double ul14 = (-sn * uI[0] + cs * uI[1]) - (-sn * uJ[0] + cs * uJ[1]);
+    const double NoverL = Se[0] / L;
+    const double g[6] = {-sn, cs, 0.0, sn, -cs, 0.0};
+#pragma unroll
+    for (int i = 0; i < 6; i++) {
+      Re[i] += NoverL * ul14 * g[i];
+#pragma unroll
+      for (int j = 0; j < 6; j++) Ke[i * 6 + j] += NoverL * g[i] * g[j];
+    }
+  }
 }
 
 // ForceBeamColumn*::commitState (ForceBeamColumn2d.cpp:277-306): committed

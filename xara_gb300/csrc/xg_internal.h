@@ -145,6 +145,7 @@ struct FrameView {
   int *nfail;                 // elements whose compatibility iteration failed
   double *Ke, *Re;            // element tangent / force scratch
   unsigned long long *work;   // [2] fiber and section state determinations
+  int pdelta2d;               // PDeltaCrdTransf2d geometric terms
 };
 int frame_state_stride(int nip);
 int launch_fbc_update(const FrameView &v, cudaStream_t s);

@@ -269,7 +269,7 @@ struct xg_model {
     return etype == XG_ELE_QUAD ? 64 : 324;
   }
   // force-based frames: section and material tables, element state
-  int fb_nb = 0, fb_nip = 0, fb_max_iters = 10;
+  int fb_nb = 0, fb_nip = 0, fb_max_iters = 10, geom_transf = 0;
   double fb_tol = 1e-12;
   std::vector<int> sec_fstart, fmat, utype;
   std::vector<double> fy, fz, fA, GJ, uparam;
@@ -293,6 +293,7 @@ struct xg_model {
     v.fh_t = d_fh_t.p; v.st = d_st.p; v.max_iters = fb_max_iters; v.tol = fb_tol;
     for (int i = 0; i < 10; i++) { v.xi[i] = lob_xi[i]; v.wt[i] = lob_wt[i]; }
     v.nfail = d_nfail.p; v.Ke = d_Ke.p; v.Re = d_Re.p; v.work = d_work.p;
+    v.pdelta2d = (fb_nb == 3 && geom_transf == 1) ? 1 : 0;
     return v;
   }
   int upload_frames();
@@ -1371,8 +1372,8 @@ static int plan_model(const xg_model_desc *d, xg_model **out) {
     return fail(XG_EINVAL, "forceBeamColumn 3D needs ndm 3, ndf 6");
   if (fr && (d->fbc_num_ip < 3 || d->fbc_num_ip > 5))
     return fail(XG_EINVAL, "forceBeamColumn needs 3..5 Lobatto points");
-  if (fr && d->elem_type == XG_ELE_FBC2D && d->geom_transf != 0)
-    return fail(XG_EINVAL, "2D P-Delta transformation not supported");
+  if (fr && d->geom_transf != 0 && d->geom_transf != 1)
+    return fail(XG_EINVAL, "geomTransf %d not supported (0 Linear, 1 PDelta)", d->geom_transf);
   if (fr && (d->num_sec <= 0 || !d->sec_fiber_start || !d->fib_y || !d->fib_area ||
              !d->fib_mat || d->num_uni <= 0 || !d->uni_type || !d->uni_param))
     return fail(XG_EINVAL, "forceBeamColumn needs fiber sections and uniaxial materials");
@@ -1434,6 +1435,7 @@ static int plan_model(const xg_model_desc *d, xg_model **out) {
   } else {
     const int nsec = d->num_sec, nuni = d->num_uni;
     m->fb_nb = d->elem_type == XG_ELE_FBC2D ? 3 : 6;
+    m->geom_transf = d->geom_transf;
     m->fb_nip = d->fbc_num_ip;
     m->fb_max_iters = d->fbc_max_iters > 0 ? d->fbc_max_iters : 10;
     m->fb_tol = d->fbc_tol > 0 ? d->fbc_tol : 1e-12;
