@@ -505,6 +505,7 @@ def run_batch(args):
     m = gpu.DeviceModel(desc)
     m.set_system(gpu.XG_SYSTEM_BJPCG)
     m.set_phase(phases[0])
+    gpu.autotune(m, element=True, pcg=True)
     t_setup = time.perf_counter() - t_setup
     stream = torch.cuda.ExternalStream(gpu.model_stream(m))
 
@@ -514,6 +515,7 @@ def run_batch(args):
         torch.cuda.synchronize()
 
     m.analyze(lead + args.warmup)                 # into the strong motion, untimed
+    tuned = gpu.autotune_result(m)
     gpu.profile_enable(m, True)
     sampler = ClockSampler(local if world == 1 else 0)
     sampler.start()
@@ -594,6 +596,8 @@ def run_batch(args):
                                "frames": min(BATCH_SAMPLE, len(parts)),
                                "note": "the same kernels, one frame per model, same steps"},
         "batched_over_per_model": value / loop_value,
+        "autotuned": {"elements_per_block": tuned[0], "pcg_rows_per_block": tuned[1],
+                      "still_sampling": tuned[2]},
         "e2e": {"value": e2e_value, "unit": "frame time steps/s", "h2d_bytes_per_step": 0,
                 "d2h_bytes_per_step": int(uh.numel() * 8),
                 "path": "xg_analyze + xg_get_disp into pinned host memory every step; the "

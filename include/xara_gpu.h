@@ -300,6 +300,20 @@ int xg_profile_enable(xg_model *m, int enable);
    the end. */
 int xg_profile_get(const xg_model *m, int k, char *name, int cap, double *ms, long *launches);
 
+/* Autotuner (no counterpart in the reference).  what = XG_TUNE_ELEMENT:
+   elements per block of the force-based element kernel (1, 2, 4, 8);
+   XG_TUNE_PCG: rows per block of the PCG launch (32..256).  The next
+   launches of the analysis try the candidates in turn (three timed samples
+   each, CUDA events, normalised by fiber state determinations or PCG
+   iterations) and keep the cheapest.  Element shapes give bit-identical
+   results; PCG grids change the reduction tree (rounding only). */
+#define XG_TUNE_ELEMENT 1
+#define XG_TUNE_PCG     2
+int xg_analysis_autotune(xg_model *m, int what);
+/* The current choices and the number of tunings still sampling. */
+int xg_autotune_result(const xg_model *m, int *elem_warps, int *pcg_rows_per_block,
+                       int *pending);
+
 /* The CUDA stream (a cudaStream_t) every kernel of the model runs on, for
    callers that time or order their own work against it. */
 int xg_model_stream(const xg_model *m, void **stream);

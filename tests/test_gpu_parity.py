@@ -253,3 +253,22 @@ def test_frame_batch_parts_match_separate_runs(gpu_mod, system):
         assert relerr(U[:, off:off + nu], Uf) < RTOL_HISTORY, off
         off += nu
     assert off == U.shape[1]
+
+
+def test_autotuned_element_shape_gives_identical_results(gpu_mod):
+    """The element kernel's block shape (chosen by the autotuner) does not
+    change a single bit of the analysis."""
+    from xara_gb300 import configs
+    desc, phases = configs.frame_batch(3, steps=30, seed=5)
+    runs = []
+    for tune in (False, True):
+        with gpu_mod.DeviceModel(desc) as m:
+            m.set_system(gpu_mod.XG_SYSTEM_PROFILE_SPD)
+            if tune:
+                gpu_mod.autotune(m, element=True, pcg=False)
+            U, _, _ = m.run(phases)
+            runs.append(U)
+            if tune:
+                warps, _, pending = gpu_mod.autotune_result(m)
+                assert warps in (1, 2, 4, 8) and pending == 0
+    assert np.array_equal(runs[0], runs[1])

@@ -430,11 +430,11 @@ struct FbcSmem {
 
 // ForceBeamColumn2d::update (element/Frame/Other/Force/ForceBeamColumn2d.cpp:
 // 559-935) and ForceBeamColumn3d::update (ForceBeamColumn3d.cpp:588-1066).
-template <int NB, int ORD>
-__global__ void __launch_bounds__(32 * kFbcWarps) k_fbc_update(FrameView v) {
-  __shared__ FbcSmem<NB, ORD> sm_all[kFbcWarps];
+template <int NB, int ORD, int WARPS>
+__global__ void __launch_bounds__(32 * WARPS) k_fbc_update(FrameView v) {
+  __shared__ FbcSmem<NB, ORD> sm_all[WARPS];
   const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int e = blockIdx.x * kFbcWarps + w;
+  const int e = blockIdx.x * WARPS + w;
   if (e >= v.ne) return;
   FbcSmem<NB, ORD> &S = sm_all[w];
   const int nip = v.nip;
@@ -777,12 +777,24 @@ __global__ void __launch_bounds__(32 * kFbcWarps) k_fbc_revert_sections(FrameVie
 
 int frame_state_stride(int nip) { return 6 + 36 + nip * 24 + 6 + 1; }
 
-int launch_fbc_update(const FrameView &v, cudaStream_t s) {
+template <int WARPS>
+static void fbc_update_as(const FrameView &v, cudaStream_t s) {
+  const int grid = (v.ne + WARPS - 1) / WARPS;
+  if (v.nb == 3) k_fbc_update<3, 2, WARPS><<<grid, 32 * WARPS, 0, s>>>(v);
+  else k_fbc_update<6, 4, WARPS><<<grid, 32 * WARPS, 0, s>>>(v);
+}
+
+// warps: elements (warps) per block, one of 1, 2, 4, 8 (the autotuner's
+// choice; 4 otherwise)
+int launch_fbc_update(const FrameView &v, cudaStream_t s, int warps) {
   if (v.ne == 0) return 0;
   if (v.nip > kMaxIp) return XG_EINVAL;
-  const int grid = (v.ne + kFbcWarps - 1) / kFbcWarps;
-  if (v.nb == 3) k_fbc_update<3, 2><<<grid, 32 * kFbcWarps, 0, s>>>(v);
-  else k_fbc_update<6, 4><<<grid, 32 * kFbcWarps, 0, s>>>(v);
+  switch (warps) {
+    case 1: fbc_update_as<1>(v, s); break;
+    case 2: fbc_update_as<2>(v, s); break;
+    case 8: fbc_update_as<8>(v, s); break;
+    default: fbc_update_as<4>(v, s); break;
+  }
   return cudaGetLastError() == cudaSuccess ? 0 : XG_ECUDA;
 }
 

@@ -74,8 +74,10 @@ struct PcgSystem {
 int pcg_factor_blocks(const PcgSystem &S, cudaStream_t s);
 // Solve A x = b (device vectors).  x holds the initial guess (usually 0).
 // Returns 0 when converged, XG_ESOLVE on breakdown, maxit or a barrier timeout.
+// rows_per_block: the grid gets one block per that many rows (capped by
+// co-residency); 0 takes the default of 64
 int pcg_solve(const PcgSystem &S, const double *b, double *x, double rtol, int maxit,
-              int *iters, double *relres, cudaStream_t s);
+              int *iters, double *relres, cudaStream_t s, int rows_per_block = 0);
 int pcg_max_blocks();
 
 // Skyline LDL' without pivoting on 32 x 32 tiles (xg_profile.cu)
@@ -148,7 +150,7 @@ struct FrameView {
   int pdelta2d;               // PDeltaCrdTransf2d geometric terms
 };
 int frame_state_stride(int nip);
-int launch_fbc_update(const FrameView &v, cudaStream_t s);
+int launch_fbc_update(const FrameView &v, cudaStream_t s, int warps = 4);
 int launch_fbc_assemble(const FrameView &v, cudaStream_t s);
 int launch_fbc_commit(const FrameView &v, double *st_c, double *fh_c, long nrec, cudaStream_t s);
 int launch_fbc_revert(const FrameView &v, const double *st_c, long nrec, cudaStream_t s);

@@ -204,6 +204,39 @@ struct xg_model {
   int phase_steps_done = 0;
   bool phase_closed = false;
   int last_nfail = 0;
+  // online autotuner: candidates tried in turn on the first launches of an
+  // analysis, each timed with CUDA events and normalised by its work (fiber
+  // state determinations, PCG iterations); the cheapest is kept
+  struct Tuner {
+    bool on = false, done = true;
+    std::vector<int> cand;
+    std::vector<double> cost;
+    std::vector<int> samples;
+    int chosen = 0, reps = 3;
+    void start(std::vector<int> c, int dflt) {
+      cand = c; cost.assign(c.size(), 0.0); samples.assign(c.size(), 0);
+      on = true; done = false; chosen = dflt;
+    }
+    int next() const {            // candidate index to try, or -1 when done
+      for (size_t k = 0; k < cand.size(); k++)
+        if (samples[k] < reps) return (int)k;
+      return -1;
+    }
+    void record(int k, double c) {
+      cost[k] += c;
+      samples[k]++;
+      if (next() < 0) {
+        size_t best = 0;
+        for (size_t j = 1; j < cand.size(); j++)
+          if (cost[j] < cost[best]) best = j;
+        chosen = cand[best];
+        done = true;
+      }
+    }
+  };
+  Tuner tune_elem, tune_pcg;
+  int fbc_warps = 4, pcg_rows = 64;
+  cudaEvent_t tune_a = nullptr, tune_b = nullptr;
   // per-kernel CUDA-event timing on the model's stream (xg_profile_*)
   struct ProfSlot {
     const char *name;
@@ -305,6 +338,8 @@ struct xg_model {
       cudaEventDestroy(p.a);
       cudaEventDestroy(p.b);
     }
+    if (tune_a) cudaEventDestroy(tune_a);
+    if (tune_b) cudaEventDestroy(tune_b);
     if (stream) cudaStreamDestroy(stream);
   }
 
@@ -1000,7 +1035,22 @@ int xg_model::element_state(bool compute) {
       CK(cudaMemsetAsync(d_nfail.p, 0, sizeof(int), s));
       prof_begin(P_UPDATE);
       elem_updates += ne;
-      RET(launch_fbc_update(fv, s));
+      const int k = (tune_elem.on && !tune_elem.done) ? tune_elem.next() : -1;
+      if (k >= 0) {
+        unsigned long long w0 = 0, w1 = 0;
+        CK(cudaMemcpyAsync(&w0, d_work.p, sizeof w0, cudaMemcpyDeviceToHost, s));
+        CK(cudaEventRecord(tune_a, s));
+        RET(launch_fbc_update(fv, s, tune_elem.cand[k]));
+        CK(cudaEventRecord(tune_b, s));
+        CK(cudaMemcpyAsync(&w1, d_work.p, sizeof w1, cudaMemcpyDeviceToHost, s));
+        CK(cudaStreamSynchronize(s));
+        float ms = 0.0f;
+        CK(cudaEventElapsedTime(&ms, tune_a, tune_b));
+        if (w1 > w0) tune_elem.record(k, ms / ((double)(w1 - w0) * 1e-6));
+        if (tune_elem.done) fbc_warps = tune_elem.chosen;
+      } else {
+        RET(launch_fbc_update(fv, s, fbc_warps));
+      }
       prof_end(P_UPDATE, 1);
     }
     prof_begin(P_ASSEMBLE);
@@ -1111,7 +1161,18 @@ int xg_model::solve(const double *b, double *x, int *iters) {
   double relres = 0.0;
   int it = 0;
   prof_begin(P_PCG);
-  int r = pcg_solve(pcg, b, x, rtol, maxit, &it, &relres, stream);
+  const int k = (tune_pcg.on && !tune_pcg.done) ? tune_pcg.next() : -1;
+  if (k >= 0) CK(cudaEventRecord(tune_a, stream));
+  int r = pcg_solve(pcg, b, x, rtol, maxit, &it, &relres, stream,
+                    k >= 0 ? tune_pcg.cand[k] : pcg_rows);
+  if (k >= 0) {
+    CK(cudaEventRecord(tune_b, stream));
+    CK(cudaEventSynchronize(tune_b));
+    float ms = 0.0f;
+    CK(cudaEventElapsedTime(&ms, tune_a, tune_b));
+    if (it > 0) tune_pcg.record(k, ms / it);
+    if (tune_pcg.done) pcg_rows = tune_pcg.chosen;
+  }
   prof_end(P_PCG, 1);
   prof_flush();
   last_solver_iters += it;
@@ -1564,6 +1625,26 @@ int xg_profile_enable(xg_model *m, int enable) {
   for (auto &p : m->prof) { p.ms = 0.0; p.launches = 0; }
   m->point_updates = m->elem_updates = 0;
   if (m->d_work.p) CK(cudaMemsetAsync(m->d_work.p, 0, 2 * sizeof(unsigned long long), m->stream));
+  return 0;
+}
+
+int xg_analysis_autotune(xg_model *m, int what) {
+  if (!m) return fail(XG_EINVAL, "null model");
+  if (!m->tune_a) {
+    CK(cudaEventCreate(&m->tune_a));
+    CK(cudaEventCreate(&m->tune_b));
+  }
+  if ((what & XG_TUNE_ELEMENT) && m->frames()) m->tune_elem.start({1, 2, 4, 8}, m->fbc_warps);
+  if (what & XG_TUNE_PCG) m->tune_pcg.start({32, 64, 128, 256}, m->pcg_rows);
+  return 0;
+}
+
+int xg_autotune_result(const xg_model *m, int *elem_warps, int *pcg_rows_per_block,
+                       int *pending) {
+  if (!m) return fail(XG_EINVAL, "null model");
+  if (elem_warps) *elem_warps = m->fbc_warps;
+  if (pcg_rows_per_block) *pcg_rows_per_block = m->pcg_rows;
+  if (pending) *pending = (m->tune_elem.on && !m->tune_elem.done) + (m->tune_pcg.on && !m->tune_pcg.done);
   return 0;
 }
 

@@ -288,7 +288,7 @@ int pcg_factor_blocks(const PcgSystem &S, cudaStream_t s) {
 }
 
 int pcg_solve(const PcgSystem &S, const double *b, double *x, double rtol, int maxit,
-              int *iters, double *relres, cudaStream_t s) {
+              int *iters, double *relres, cudaStream_t s, int rows_per_block) {
   if (S.n == 0) {
     if (iters) *iters = 0;
     if (relres) *relres = 0.0;
@@ -297,7 +297,8 @@ int pcg_solve(const PcgSystem &S, const double *b, double *x, double rtol, int m
   // about four rows per warp: SpMV rows are latency-bound chains (row
   // pointer, column index, vector entry), so mid-size systems want many
   // warps; the grid barrier's cost grows slowly with the block count
-  long want = ((long)S.n + 63) / 64;
+  const long rpb = rows_per_block > 0 ? rows_per_block : 64;
+  long want = ((long)S.n + rpb - 1) / rpb;
   int nb = (int)(want < 1 ? 1 : want);
   const int maxb = pcg_max_blocks();
   if (nb > maxb) nb = maxb;

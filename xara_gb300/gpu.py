@@ -235,6 +235,22 @@ def profile_enable(model, on=True):
     _check(lib().xg_profile_enable(model.h, 1 if on else 0))
 
 
+def autotune(model, element=True, pcg=True):
+    """Start the online autotuner (element kernel block shape, PCG grid)."""
+    L = lib()
+    L.xg_analysis_autotune.argtypes = [C.c_void_p, C.c_int]
+    _check(L.xg_analysis_autotune(model.h, (1 if element else 0) | (2 if pcg else 0)))
+
+
+def autotune_result(model):
+    """(elements per block, PCG rows per block, tunings still sampling)."""
+    L = lib()
+    L.xg_autotune_result.argtypes = [C.c_void_p] + [C.POINTER(C.c_int)] * 3
+    a, b, c = C.c_int(), C.c_int(), C.c_int()
+    _check(L.xg_autotune_result(model.h, C.byref(a), C.byref(b), C.byref(c)))
+    return a.value, b.value, c.value
+
+
 def model_stream(model):
     """The model's CUDA stream as an integer handle (cudaStream_t)."""
     L = lib()
