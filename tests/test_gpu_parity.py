@@ -272,3 +272,28 @@ def test_autotuned_element_shape_gives_identical_results(gpu_mod):
                 warps, _, pending = gpu_mod.autotune_result(m)
                 assert warps in (1, 2, 4, 8) and pending == 0
     assert np.array_equal(runs[0], runs[1])
+
+
+def test_profile_pipelined_sweeps_residual(gpu_mod):
+    """A system with enough tile rows (8,514 equations, 267 tile rows) for
+    the substitutions to run pipelined over many blocks: the LDL' solution's
+    relative residual, and agreement with a tightly converged PCG."""
+    sp = pytest.importorskip("scipy.sparse")
+    from xara_gb300 import configs
+    desc, _ = configs.quad_block(128, 32)
+    with gpu_mod.DeviceModel(desc) as m:
+        u = np.zeros(m.nu)
+        crd = desc.node_crd.reshape(-1, 2)
+        u[1::2] = -2e-3 * crd[:, 1] * (1 + 0.3 * np.sin(crd[:, 0] / 9.0))
+        m.set_trial_disp(u)
+        vals, _, _ = m.update()
+        rp, ci = m.pattern()
+        assert m.neq >= 128 * 32
+        A = sp.csr_matrix((vals, ci, rp), shape=(m.neq, m.neq))
+        b = np.random.default_rng(9).normal(size=m.neq)
+        m.set_system(gpu_mod.XG_SYSTEM_PROFILE_SPD)
+        x, _, _ = m.solve(b)
+        assert np.linalg.norm(A @ x - b) / np.linalg.norm(b) < 1e-12
+        m.set_system(gpu_mod.XG_SYSTEM_BJPCG)
+        xp, _, rr = m.solve(b, rtol=1e-14)
+        assert relerr(x, xp) < 1e-9

@@ -92,6 +92,7 @@ struct ProfileSystem {
   int ntasks;
   int *next_task;          // [1] task counter
   int *upd, *done;         // [nt*(W+1)] per tile: updates applied, factored
+  int *sweep_flags;        // [2*nt] rows solved in the forward / backward sweep
   int *flags;              // [4]
   double min_diag_tol;
 };

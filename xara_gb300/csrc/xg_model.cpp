@@ -164,7 +164,7 @@ struct xg_model {
   ProfileSystem psys{};
   bool prof_ready = false, prof_factored = false;
   std::vector<int> ftile;
-  DBuf<int> d_ftile, d_pflags, d_ptasks, d_pnext, d_pupd, d_pdone;
+  DBuf<int> d_ftile, d_pflags, d_ptasks, d_pnext, d_pupd, d_pdone, d_psweep;
   DBuf<double> d_L, d_invD, d_piv, d_px;
   int prof_ldx = 0;
   int ensure_profile();
@@ -1106,6 +1106,8 @@ int xg_model::ensure_profile() {
   RET(d_pupd.alloc((size_t)nt * (W + 1)));
   RET(d_pdone.alloc((size_t)nt * (W + 1)));
   RET(d_pflags.alloc(4));
+  RET(d_psweep.alloc(2 * (size_t)std::max(nt, 1)));
+  psys.sweep_flags = d_psweep.p;
   psys.n = neq; psys.nt = nt; psys.W = W;
   psys.rowptr = d_rowptr.p; psys.colidx = d_colidx.p; psys.vals = d_vals.p;
   psys.ftile = d_ftile.p; psys.L = d_L.p; psys.invD = d_invD.p; psys.piv = d_piv.p;

@@ -100,31 +100,34 @@ __global__ void k_prof_fill(ProfileSystem S) {
 __device__ bool factor_diag(const ProfileSystem &S, int J, double (*sA)[kT + 1], double *col,
                             volatile int *flags) {
   double *g = tile_at(S, J, 0);
-  __shared__ double lcol[kT], sinv[kT + 1];
+  __shared__ double colbuf[2][kT], sinv[kT + 1];
+  (void)col;
   for (int k = threadIdx.x; k < kTT; k += blockDim.x) sA[k >> 5][k & 31] = __ldcg(g + k);
   __syncthreads();
+  if (threadIdx.x < kT) colbuf[0][threadIdx.x] = sA[threadIdx.x][0];
   if (threadIdx.x == 0) sinv[0] = __drcp_rn(sA[0][0]);
   __syncthreads();
   const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5, nty = blockDim.x >> 5;
-  for (int c = 0; c < kT; c++) {
+  // one barrier per column: the threads of column c+1 hand its entries and
+  // its pivot's reciprocal to the next column through a second buffer
+  for (int c = 0; c < kT - 1; c++) {
+    const double *cl = colbuf[c & 1];
+    double *cn = colbuf[(c + 1) & 1];
     const double inv = sinv[c];
-    if (threadIdx.x < kT) {
-      const double v = sA[threadIdx.x][c];
-      col[threadIdx.x] = v;
-      lcol[threadIdx.x] = v * inv;
-    }
-    __syncthreads();
-    // a_rs -= l_r a_sc for c < s <= r
     const int s = c + 1 + tx;
     if (s < kT) {
-      const double as = col[s];
+      const double as = cl[s];
       for (int r = s + ((ty - tx) % nty + nty) % nty; r < kT; r += nty) {
-        const double v = fma(-lcol[r], as, sA[r][s]);
+        const double l = cl[r] * inv;
+        const double v = fma(-l, as, sA[r][s]);
         sA[r][s] = v;
-        if (r == s && r == c + 1) sinv[c + 1] = __drcp_rn(v);
+        if (s == c + 1) {
+          cn[r] = v;
+          sA[r][c] = l;
+          if (r == s) sinv[c + 1] = __drcp_rn(v);
+        }
       }
     }
-    if (threadIdx.x > c && threadIdx.x < kT) sA[threadIdx.x][c] = lcol[threadIdx.x];
     __syncthreads();
   }
   if (threadIdx.x < kT) {
@@ -381,6 +384,126 @@ __global__ void __launch_bounds__(kSolveBlock) k_prof_solve(ProfileSystem S, int
   }
 }
 
+// Pipelined substitutions on kPipeBlocks co-resident blocks (cooperative
+// launch): block b owns the tile rows J = b, b + P, ... .  Forward, in
+// increasing J: the contributions of the solved tiles J-o (oldest first)
+// are accumulated as each tile's flag appears, then the diagonal tile is
+// solved and its flag set; the tile of the newest dependency and the
+// diagonal tile are loaded before the wait, so a row costs about one flag
+// round trip plus the 32-step shuffle solve.  Backward, in decreasing J:
+// z_J = D^-1 y_J, minus the transposed contributions of the rows below,
+// then the unit upper solve.  Waits are bounded by the global timer.
+constexpr int kPipeBlocks = 64;
+constexpr int kPipeThreads = 256;
+
+__device__ __forceinline__ bool wait_flag(const int *p, volatile int *flags) {
+  return wait_geq(p, 1, flags);
+}
+
+__global__ void __launch_bounds__(kPipeThreads) k_prof_solve_pipe(ProfileSystem S, int nrhs,
+                                                                  double *x, int ldx,
+                                                                  int *fdone, int *bdone) {
+  __shared__ double sL[kT][kT + 1];
+  __shared__ double part[4][kT];
+  __shared__ int ok;
+  volatile int *flags = S.flags;
+  const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
+  const int r = tid >> 3, g = tid & 7;          // tile row, column group (4 columns)
+  const int nt = S.nt, W = S.W, P = gridDim.x;
+  // ---------------- forward
+  for (int J = blockIdx.x; J < nt; J += P) {
+    const double *Ld = tile_at(S, J, 0);
+    for (int k = tid; k < kTT; k += kPipeThreads) sL[k >> 5][k & 31] = __ldcg(Ld + k);
+    double acc[4] = {0.0, 0.0, 0.0, 0.0};
+    const int ohi = min(W, J - S.ftile[J]);
+    for (int o = ohi; o >= 1; o--) {
+      const double *Lt = tile_at(S, J, o) + r * kT + g;
+      const double l0 = __ldcg(Lt), l1 = __ldcg(Lt + 8), l2 = __ldcg(Lt + 16), l3 = __ldcg(Lt + 24);
+      if (tid == 0) ok = wait_flag(fdone + (J - o), flags) ? 1 : 0;
+      __syncthreads();
+      if (!ok) return;
+      const int c0 = (J - o) * kT + g;
+      for (int q = 0; q < nrhs; q++) {
+        const double *y = x + (size_t)q * ldx + c0;
+        acc[q] += l0 * __ldcg(y) + l1 * __ldcg(y + 8) + l2 * __ldcg(y + 16) + l3 * __ldcg(y + 24);
+      }
+    }
+    for (int q = 0; q < nrhs; q++) {
+      double v = acc[q];
+      v += __shfl_xor_sync(0xffffffffu, v, 4);
+      v += __shfl_xor_sync(0xffffffffu, v, 2);
+      v += __shfl_xor_sync(0xffffffffu, v, 1);
+      if (g == 0) part[q][r] = v;
+    }
+    __syncthreads();
+    if (w < nrhs) {
+      const int q = w;
+      double v = __ldcg(x + (size_t)q * ldx + J * kT + lane) - part[q][lane];
+      for (int c = 0; c < kT - 1; c++) {
+        const double yc = __shfl_sync(0xffffffffu, v, c);
+        if (lane > c) v -= sL[lane][c] * yc;
+      }
+      x[(size_t)q * ldx + J * kT + lane] = v;
+      __threadfence();
+    }
+    __syncthreads();
+    if (tid == 0) {
+      __threadfence();
+      atomicExch(fdone + J, 1);
+    }
+  }
+  // ---------------- backward
+  const int jlast = blockIdx.x + ((nt - 1 - (int)blockIdx.x) / P) * P;
+  for (int J = jlast; J >= 0; J -= P) {
+    if (J >= nt) continue;
+    const double *Ld = tile_at(S, J, 0);
+    for (int k = tid; k < kTT; k += kPipeThreads) sL[k >> 5][k & 31] = __ldcg(Ld + k);
+    double acc[4] = {0.0, 0.0, 0.0, 0.0};
+    const int ohi = min(W, nt - 1 - J);
+    // column c = r of the result; rows g, g+8, g+16, g+24 of tile (J+o, J)
+    for (int o = ohi; o >= 1; o--) {
+      if (S.ftile[J + o] > J) continue;
+      const double *Lt = tile_at(S, J + o, o) + r;
+      const double l0 = __ldcg(Lt + g * kT), l1 = __ldcg(Lt + (g + 8) * kT);
+      const double l2 = __ldcg(Lt + (g + 16) * kT), l3 = __ldcg(Lt + (g + 24) * kT);
+      if (tid == 0) ok = wait_flag(bdone + (J + o), flags) ? 1 : 0;
+      __syncthreads();
+      if (!ok) return;
+      const int r0 = (J + o) * kT + g;
+      for (int q = 0; q < nrhs; q++) {
+        const double *xr = x + (size_t)q * ldx + r0;
+        acc[q] += l0 * __ldcg(xr) + l1 * __ldcg(xr + 8) + l2 * __ldcg(xr + 16) +
+                  l3 * __ldcg(xr + 24);
+      }
+    }
+    for (int q = 0; q < nrhs; q++) {
+      double v = acc[q];
+      v += __shfl_xor_sync(0xffffffffu, v, 4);
+      v += __shfl_xor_sync(0xffffffffu, v, 2);
+      v += __shfl_xor_sync(0xffffffffu, v, 1);
+      if (g == 0) part[q][r] = v;
+    }
+    __syncthreads();
+    if (w < nrhs) {
+      const int q = w;
+      // z_J = D^-1 y_J (ProfileSPD divides by the pivots before the back sweep)
+      const double z = __ldcg(x + (size_t)q * ldx + J * kT + lane) * S.invD[J * kT + lane];
+      double v = z - part[q][lane];
+      for (int cc = kT - 1; cc > 0; cc--) {
+        const double xc = __shfl_sync(0xffffffffu, v, cc);
+        if (lane < cc) v -= sL[cc][lane] * xc;
+      }
+      x[(size_t)q * ldx + J * kT + lane] = v;
+      __threadfence();
+    }
+    __syncthreads();
+    if (tid == 0) {
+      __threadfence();
+      atomicExch(bdone + J, 1);
+    }
+  }
+}
+
 int g_factor_blocks = -1;
 
 }  // namespace
@@ -485,6 +608,25 @@ int profile_factor(const ProfileSystem &S, cudaStream_t s, int *bad_eq) {
 int profile_solve(const ProfileSystem &S, int nrhs, double *x, int ldx, cudaStream_t s) {
   if (S.n == 0) return 0;
   if (nrhs < 1 || nrhs > 4 || ldx < S.nt * kT) return XG_EINVAL;
+  if (S.sweep_flags && S.nt >= 2 * kPipeBlocks) {
+    // pipelined over co-resident blocks (the flags of both sweeps are zeroed
+    // first); small systems keep the one-block sweep
+    if (cudaMemsetAsync(S.sweep_flags, 0, 2 * (size_t)S.nt * sizeof(int), s) != cudaSuccess)
+      return XG_ECUDA;
+    if (cudaMemsetAsync(S.flags, 0, 4 * sizeof(int), s) != cudaSuccess) return XG_ECUDA;
+    ProfileSystem Sv = S;
+    int *fd = S.sweep_flags, *bd = S.sweep_flags + S.nt;
+    void *args[] = {(void *)&Sv, (void *)&nrhs, (void *)&x, (void *)&ldx, (void *)&fd,
+                    (void *)&bd};
+    if (cudaLaunchCooperativeKernel((void *)k_prof_solve_pipe, dim3(kPipeBlocks),
+                                    dim3(kPipeThreads), args, 0, s) != cudaSuccess)
+      return XG_ECUDA;
+    int hflag = 0;
+    if (cudaMemcpyAsync(&hflag, S.flags, sizeof hflag, cudaMemcpyDeviceToHost, s) != cudaSuccess)
+      return XG_ECUDA;
+    if (cudaStreamSynchronize(s) != cudaSuccess) return XG_ECUDA;
+    return hflag != 0 ? XG_ESOLVE : 0;   // a sweep wait timed out
+  }
   const size_t win = (size_t)nrhs * (S.W + 1) * kT * sizeof(double);
   const size_t stat = (4 * kT * (kT + 1) + kT * (kT + 1)) * sizeof(double);
   if (win + stat > 227 * 1024)
