@@ -97,39 +97,59 @@ __global__ void k_prof_fill(ProfileSystem S) {
 // next pivot takes its reciprocal at once (__drcp_rn: the correctly rounded
 // 1/d, the value of the reference's 1.0/aii), so the chain of dependent
 // FP64 operations per column stays short.
+// 1/d for the elimination: an FP32 seed refined by two Newton steps in FP64
+// (four dependent FMAs, against about six for a correctly rounded FP64
+// reciprocal, whose FP64 latency sets the pace of the pivot chain); the
+// stored reciprocal pivots are the correctly rounded ones.
+__device__ __forceinline__ double elim_rcp(double d) {
+  const double ad = fabs(d);
+  if (!(ad > 1e-30 && ad < 1e30)) return __drcp_rn(d);
+  double x = (double)__frcp_rn((float)d);
+  double e = fma(-d, x, 1.0);
+  x = fma(x, e, x);
+  e = fma(-d, x, 1.0);
+  return fma(x, e, x);
+}
+
 __device__ bool factor_diag(const ProfileSystem &S, int J, double (*sA)[kT + 1], double *col,
                             volatile int *flags) {
   double *g = tile_at(S, J, 0);
-  __shared__ double colbuf[2][kT], sinv[kT + 1];
+  __shared__ double colbuf[2][kT], lcol[kT], sinv[kT + 1];
   (void)col;
   for (int k = threadIdx.x; k < kTT; k += blockDim.x) sA[k >> 5][k & 31] = __ldcg(g + k);
   __syncthreads();
   if (threadIdx.x < kT) colbuf[0][threadIdx.x] = sA[threadIdx.x][0];
-  if (threadIdx.x == 0) sinv[0] = __drcp_rn(sA[0][0]);
+  if (threadIdx.x == 0) sinv[0] = elim_rcp(sA[0][0]);
   __syncthreads();
-  const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5, nty = blockDim.x >> 5;
-  // one barrier per column: the threads of column c+1 hand its entries and
-  // its pivot's reciprocal to the next column through a second buffer
+  // Column c: warp 0 scales the column below the pivot (l = a / d), then the
+  // trailing triangle (rows and columns c+1..31, packed densely over the
+  // threads through the lower-triangle table) takes one FMA per entry; the
+  // threads that finish column c+1 hand it, and its pivot's reciprocal, to
+  // the next column through a second buffer.
   for (int c = 0; c < kT - 1; c++) {
     const double *cl = colbuf[c & 1];
     double *cn = colbuf[(c + 1) & 1];
-    const double inv = sinv[c];
-    const int s = c + 1 + tx;
-    if (s < kT) {
-      const double as = cl[s];
-      for (int r = s + ((ty - tx) % nty + nty) % nty; r < kT; r += nty) {
-        const double l = cl[r] * inv;
-        const double v = fma(-l, as, sA[r][s]);
-        sA[r][s] = v;
-        if (s == c + 1) {
-          cn[r] = v;
-          sA[r][c] = l;
-          if (r == s) sinv[c + 1] = __drcp_rn(v);
-        }
+    if (threadIdx.x < kT && threadIdx.x > c) {
+      const double l = cl[threadIdx.x] * sinv[c];
+      lcol[threadIdx.x] = l;
+      sA[threadIdx.x][c] = l;
+    }
+    __syncthreads();
+    const int m = kT - 1 - c, tri = m * (m + 1) / 2;
+    for (int k = threadIdx.x; k < tri; k += blockDim.x) {
+      const int rs = kLowerRS[k];
+      const int r = c + 1 + (rs >> 5), s = c + 1 + (rs & 31);
+      const double v = fma(-lcol[r], cl[s], sA[r][s]);
+      sA[r][s] = v;
+      if (s == c + 1) {
+        cn[r] = v;
+        if (r == s) sinv[c + 1] = elim_rcp(v);
       }
     }
     __syncthreads();
   }
+  if (threadIdx.x < kT) sinv[threadIdx.x] = __drcp_rn(sA[threadIdx.x][threadIdx.x]);
+  __syncwarp();
   if (threadIdx.x < kT) {
     const int eq = J * kT + threadIdx.x;
     const double d = sA[threadIdx.x][threadIdx.x];
