@@ -503,9 +503,9 @@ def run_batch(args):
     desc, phases, parts = batch_model(args.frames, nsteps)
     t_setup = time.perf_counter()
     m = gpu.DeviceModel(desc)
-    m.set_system(gpu.XG_SYSTEM_BJPCG)
+    m.set_system(gpu.XG_SYSTEM_PROFILE_SPD)      # one band per frame, one launch
     m.set_phase(phases[0])
-    gpu.autotune(m, element=True, pcg=True)
+    gpu.autotune(m, element=True, pcg=False)
     t_setup = time.perf_counter() - t_setup
     stream = torch.cuda.ExternalStream(gpu.model_stream(m))
 
@@ -556,7 +556,7 @@ def run_batch(args):
     t_loop, n_loop = 0.0, 0
     for d, p in parts[:BATCH_SAMPLE]:
         mm = gpu.DeviceModel(d)
-        mm.set_system(gpu.XG_SYSTEM_BJPCG)
+        mm.set_system(gpu.XG_SYSTEM_PROFILE_SPD)
         mm.set_phase(p[0])
         mm.analyze(lead + args.warmup)
         torch.cuda.synchronize()
@@ -589,7 +589,8 @@ def run_batch(args):
                    "fiber_points": desc.meta["fiber_points"], "equations": m.neq,
                    "timed_window": f"steps {lead + args.warmup}..{lead + args.warmup + args.steps}"
                                    f" of the records (dt 0.01 s)",
-                   "system": "block-Jacobi PCG (rtol 1e-12)", "parallelism": f"replicas x{world}"},
+                   "system": "ProfileSPD: every frame's LDL' in its own band, one launch",
+                   "parallelism": f"replicas x{world}"},
         "ip_updates_per_s": points / dt,
         "newton_iters_per_step": newton / args.steps,
         "per_model_gpu_loop": {"value": loop_value, "unit": "frame time steps/s",

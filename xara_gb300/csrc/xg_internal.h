@@ -108,6 +108,28 @@ int profile_factor(const ProfileSystem &S, cudaStream_t s, int *bad_eq);
 // nt*32, entries past n zero), the solution on return; nrhs <= 4.
 int profile_solve(const ProfileSystem &S, int nrhs, double *x, int ldx, cudaStream_t s);
 
+// ProfileSPD for many small disconnected parts, one band per part
+// (xg_band.cu)
+struct BandSystem {
+  int ncomp;
+  const int *cstart;       // [ncomp+1] equation range of each part
+  const int *bw;           // [ncomp] envelope width of each part
+  const long *boff;        // [ncomp+1] band offset of each part
+  double *band;            // [boff[ncomp]]
+  const int *rowptr, *colidx;
+  const double *vals;
+  double *invD;            // [neq]
+  int *flags;              // [4]
+  double min_diag_tol;
+};
+// Widths and offsets of the parts' bands; XG_EINVAL when a part couples to
+// another or is wider than the kernel's staging.
+int band_plan(int neq, const int *rowptr, const int *colidx, const std::vector<int> &cstart,
+              std::vector<int> &bw, std::vector<long> &boff);
+int band_factor(const BandSystem &S, cudaStream_t s, int *bad_eq);
+// x[r*ldx + i] right-hand side r in, solution out (equation numbering)
+int band_solve(const BandSystem &S, int nrhs, double *x, int ldx, cudaStream_t s);
+
 // small device helpers (xg_kernels.cu)
 int launch_axpy(int n, double a, const double *x, double *y, cudaStream_t s);
 int launch_scatter_incr(int nu, const int *eqn, const double *dU, double f, double *U,

@@ -167,6 +167,11 @@ struct xg_model {
   DBuf<int> d_ftile, d_pflags, d_ptasks, d_pnext, d_pupd, d_pdone, d_psweep;
   DBuf<double> d_L, d_invD, d_piv, d_px;
   int prof_ldx = 0;
+  bool prof_band = false;                      // many small parts: one band each
+  BandSystem bsys{};
+  DBuf<int> d_bw;
+  DBuf<long> d_boff;
+  DBuf<double> d_band;
   int ensure_profile();
   int solve_profile(int nrhs, const double *const *b, double *const *x);
   // Newton vectors
@@ -1084,6 +1089,32 @@ int xg_model::element_state(bool compute) {
 // Envelope plan and tile storage of the device LDL' (once per model).
 int xg_model::ensure_profile() {
   if (prof_ready) return 0;
+  const int ncomp = (int)comp_start.size() - 1;
+  if (ncomp > 1) {
+    // disconnected parts: each part's LDL' in its own band, all in one launch
+    std::vector<int> bw;
+    std::vector<long> boff;
+    if (band_plan(neq, rowptr.data(), colidx.data(), comp_start, bw, boff) == 0) {
+      size_t free_b = 0, total_b = 0;
+      CK(cudaMemGetInfo(&free_b, &total_b));
+      if ((size_t)boff[ncomp] * sizeof(double) < free_b / 2) {
+        RET(d_bw.upload(bw.data(), bw.size(), stream));
+        RET(d_boff.upload(boff.data(), boff.size(), stream));
+        RET(d_band.alloc(std::max<long>(boff[ncomp], 1)));
+        RET(d_invD.alloc(std::max(neq, 1)));
+        RET(d_pflags.alloc(4));
+        prof_ldx = std::max(neq, 1);
+        RET(d_px.alloc((size_t)prof_ldx * 4));
+        bsys.ncomp = ncomp; bsys.cstart = d_cstart.p; bsys.bw = d_bw.p; bsys.boff = d_boff.p;
+        bsys.band = d_band.p; bsys.rowptr = d_rowptr.p; bsys.colidx = d_colidx.p;
+        bsys.vals = d_vals.p; bsys.invD = d_invD.p; bsys.flags = d_pflags.p;
+        bsys.min_diag_tol = 1.0e-12;   // ProfileSPDLinDirectSolver.h:49 default
+        prof_band = true;
+        prof_ready = true;
+        return 0;
+      }
+    }
+  }
   int nt = 0, W = 0;
   RET(profile_plan(neq, rowptr.data(), colidx.data(), ftile, nt, W));
   const size_t tiles = profile_tile_doubles(nt, W);
@@ -1126,7 +1157,7 @@ int xg_model::solve_profile(int nrhs, const double *const *b, double *const *x) 
   if (!prof_factored) {
     prof_begin(P_LDL_FACTOR);
     int bad = -1;
-    const int r = profile_factor(psys, stream, &bad);
+    const int r = prof_band ? band_factor(bsys, stream, &bad) : profile_factor(psys, stream, &bad);
     prof_end(P_LDL_FACTOR, 2);
     if (r) {
       if (bad >= 0) return fail(XG_ESOLVE, "ProfileSPD: pivot %d fails the check (aii == 0, "
@@ -1139,7 +1170,8 @@ int xg_model::solve_profile(int nrhs, const double *const *b, double *const *x) 
     CK(cudaMemcpyAsync(d_px.p + (size_t)r * prof_ldx, b[r], (size_t)neq * sizeof(double),
                        cudaMemcpyDeviceToDevice, stream));
   prof_begin(P_LDL_SOLVE);
-  RET(profile_solve(psys, nrhs, d_px.p, prof_ldx, stream));
+  RET(prof_band ? band_solve(bsys, nrhs, d_px.p, prof_ldx, stream)
+                : profile_solve(psys, nrhs, d_px.p, prof_ldx, stream));
   prof_end(P_LDL_SOLVE, 1);
   for (int r = 0; r < nrhs; r++)
     CK(cudaMemcpyAsync(x[r], d_px.p + (size_t)r * prof_ldx, (size_t)neq * sizeof(double),
