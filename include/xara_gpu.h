@@ -329,6 +329,42 @@ int xg_profile_counters(xg_model *m, long long *point_updates, long long *sectio
    kernel with no memory traffic), the ceiling of the FP64 element kernels. */
 int xg_measure_fp64_peak(double *tflops);
 
+/* ---- Adjoint of a transient run (no counterpart in the reference; its
+        DDM sensitivity, `computeGradients` (runtime/commands/analysis/
+        sensitivity.cpp:22-41, Newmark.cpp:904-959), has no Steel02 stress
+        sensitivity).  Gradients of J = sum over the steps n = 1..N and the
+        terms k of weight_k * u(node_k, dof_k, t_n)^2 with respect to the
+        first three parameters of every uniaxial material (Steel02: Fy, E0,
+        b; elastic: E).  Covers force-based frames with linear
+        transformations whose elements each use one material (Steel02
+        without initial stress, or elastic), Newmark with alphaM / betaK0
+        Rayleigh damping and UniformExcitation, from the model's initial
+        state. ---- */
+typedef struct xg_objective_desc {
+  int num_terms;
+  const int *node;            /* node tags */
+  const int *dof;             /* 0-based dof */
+  const double *weight;
+} xg_objective_desc;
+/* Replace the uniaxial parameters (num_uni x XG_UNI_NPARAM, the model
+   description's layout) and reset the model to its initial state. */
+int xg_model_set_uniaxial_params(xg_model *m, const double *uni_param, int num_uni);
+/* Run num_steps steps of the Newmark phase ph from the initial state, keep
+   the committed state every ckpt_every steps, and return J. */
+int xg_adjoint_forward(xg_model *m, const xg_phase_desc *ph, int num_steps, int ckpt_every,
+                       const xg_objective_desc *obj, double *J);
+/* Reverse sweep of the last xg_adjoint_forward: each segment between
+   checkpoints is run again and swept backwards.  grad[u*3 + k] = scale *
+   dJ/d uni_param[u][k], k = 0, 1, 2, for the num_uni materials.  The model
+   is left at the state after the run's last step. */
+int xg_adjoint_backward(xg_model *m, double scale, double *grad, int num_uni);
+/* Vector-Jacobian product of one material point's trial record (host only;
+   Steel02 or elastic): given the adjoint yb[12] of the trial record (fields
+   0-6 history, 9 stress, 10 strain), the adjoints of the committed record
+   hb[12], of the strain *sb and of parameters 0-2 qb[3]. */
+int xg_uniaxial_vjp(int type, const double *q, const double *hc, double strain,
+                    const double *yb, double *hb, double *sb, double *qb);
+
 /* ---- Allocation-free solve.  No counterpart in the reference: it exists
         for callers that cannot allocate device memory when they solve -- a
         host application or framework whose device memory is owned by its own

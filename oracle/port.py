@@ -60,6 +60,8 @@ def lib():
         L.xo_set_history.argtypes = [vp, vp, vp]
         L.xo_j2_path.argtypes = [C.c_int, vp, C.c_int, vp, vp, vp, vp]
         L.xo_uniaxial_path.argtypes = [C.c_int, vp, C.c_int, vp, vp, vp, vp]
+        L.xo_uniaxial_init.argtypes = [C.c_int, vp, vp]
+        L.xo_uniaxial_trial.argtypes = [C.c_int, vp, vp, C.c_double, vp]
         _lib = L
     return _lib
 
@@ -187,3 +189,19 @@ def uniaxial_path(kind, param, strain, commit):
     t = np.zeros(len(strain))
     L.xo_uniaxial_path(kind, _p(param), len(strain), _p(strain), _p(commit), _p(s), _p(t))
     return s, t
+
+
+def uniaxial_init(kind, param):
+    """Committed record (12 doubles) of a fresh material."""
+    h = np.zeros(12)
+    lib().xo_uniaxial_init(kind, _p(np.ascontiguousarray(param, np.float64)), _p(h))
+    return h
+
+
+def uniaxial_trial(kind, param, hc, eps):
+    """Trial record from a committed record and a trial strain."""
+    ht = np.zeros(12)
+    hc = np.ascontiguousarray(hc, np.float64)
+    lib().xo_uniaxial_trial(kind, _p(np.ascontiguousarray(param, np.float64)), _p(hc),
+                            float(eps), _p(ht))
+    return ht

@@ -1,0 +1,209 @@
+"""Adjoint of a Newmark run of force-based frames.
+
+CPU: the material point's vector-Jacobian product (the library's host entry)
+against central finite differences of the oracle's Steel02 on every branch
+(first loading, same branch, reversals with and without a new extreme
+strain, zero increments, isotropic shift).  GPU: gradients of the roof-drift
+objective with respect to per-member Steel02 parameters against central
+finite differences of the device forward run, and the checkpoint interval
+changing nothing.
+"""
+import numpy as np
+import pytest
+
+from oracle import port
+from xara_gb300 import configs
+from xara_gb300._abi import XG_UNI_ELASTIC, XG_UNI_STEEL02
+
+FIELDS = (0, 1, 2, 3, 4, 5, 6, 9, 10)            # continuous record fields
+
+
+def _gpu():
+    from xara_gb300 import gpu
+    return gpu
+
+
+def _path_states(q, strains):
+    """(committed record, trial strain) at every point of a committed path."""
+    hc = port.uniaxial_init(XG_UNI_STEEL02, q)
+    out = []
+    for e in strains:
+        out.append((hc.copy(), float(e)))
+        hc = port.uniaxial_trial(XG_UNI_STEEL02, q, hc, e)
+    return out
+
+
+def _scales(q):
+    ey = q[0] / q[1]
+    s = np.full(12, ey)
+    s[4] = s[6] = s[9] = q[0]
+    return s
+
+
+def _fd_check(q, hc, eps, rng, rel=1e-7):
+    gpu = _gpu()
+    sc = _scales(q)
+    yb = np.zeros(12)
+    yb[list(FIELDS)] = rng.normal(size=len(FIELDS)) / sc[list(FIELDS)]
+    hb, sb, qb = gpu.uniaxial_vjp(XG_UNI_STEEL02, q, hc, eps, yb)
+
+    def J(hc_, eps_, q_):
+        return float(yb @ port.uniaxial_trial(XG_UNI_STEEL02, q_, hc_, eps_))
+
+    checks = []
+    h = rel * sc[10]
+    checks.append(("strain", sb, (J(hc, eps + h, q) - J(hc, eps - h, q)) / (2 * h), sc[10]))
+    # on the first loading branch epspl == epss0 and the law's R has a kink
+    # in epspl - epss0: there the two move together (both are +-Fy/E0), so
+    # only their sum is checked
+    kink = int(hc[7]) in (1, 2) and hc[2] == hc[3]
+    groups = [(f,) for f in FIELDS if not (kink and f in (2, 3))]
+    if kink:
+        groups.append((2, 3))
+    for g in groups:
+        h = rel * sc[g[0]]
+        hp, hm = hc.copy(), hc.copy()
+        hp[list(g)] += h
+        hm[list(g)] -= h
+        checks.append((f"record{g}", sum(hb[f] for f in g),
+                       (J(hp, eps, q) - J(hm, eps, q)) / (2 * h), sc[g[0]]))
+    for k, s in enumerate((q[0], q[1], q[2])):
+        h = rel * s
+        qp, qm = q.copy(), q.copy()
+        qp[k] += h
+        qm[k] -= h
+        checks.append((f"param[{k}]", qb[k], (J(hc, eps, qp) - J(hc, eps, qm)) / (2 * h), s))
+    total = sum(abs(a) * s for _, a, _, s in checks) + 1e-12
+    for name, a, b, s in checks:
+        assert abs(a - b) * s <= 2e-6 * total, (name, a, b)
+
+
+@pytest.mark.parametrize("shift", [False, True])
+def test_steel02_vjp_against_finite_differences(shift):
+    q = configs.steel02_row(fy=350e6, E=200e9, b=0.015, R0=18.0)
+    if shift:                                    # Filippou isotropic shift a1..a4
+        q[6:10] = [0.04, 1.0, 0.04, 1.0]
+    ey = q[0] / q[1]
+    t = np.linspace(0.0, 6.0 * np.pi, 240)
+    strains = ey * (0.5 + 0.05 * t) * np.sin(t) * 3.0
+    rng = np.random.default_rng(3)
+    states = _path_states(q, strains)
+    kinds = set()
+    for hc, eps in states[1:]:
+        deps = eps - hc[10]
+        if abs(deps) < 1e-4 * ey:
+            continue                             # too close to a branch switch for FD
+        kon = int(hc[7])
+        kinds.add((kon, deps > 0))
+        _fd_check(q, hc, eps, rng)
+    # every branch of the law was visited: first loading from kon 0, same
+    # branch and reversal from kon 1 and 2
+    assert {(1, True), (1, False), (2, True), (2, False)} <= kinds
+    # first loading from the fresh record, both directions
+    for e in (0.3 * ey, -0.7 * ey, 2.5 * ey):
+        _fd_check(q, port.uniaxial_init(XG_UNI_STEEL02, q), e, rng)
+
+
+def test_steel02_vjp_zero_increment_and_elastic():
+    gpu = _gpu()
+    q = configs.steel02_row()
+    hc = port.uniaxial_init(XG_UNI_STEEL02, q)
+    yb = np.arange(12, dtype=float)
+    hb, sb, qb = gpu.uniaxial_vjp(XG_UNI_STEEL02, q, hc, 0.0, yb)
+    assert np.array_equal(hb[:7], yb[:7]) and sb == yb[10] and not qb.any()
+    qe = np.zeros(12)
+    qe[0] = 2.0e11
+    hb, sb, qb = gpu.uniaxial_vjp(XG_UNI_ELASTIC, qe, np.zeros(12), 1e-3, yb)
+    assert sb == pytest.approx(2.0e11 * yb[9] + yb[10]) and qb[0] == pytest.approx(1e-3 * yb[9])
+    with pytest.raises(gpu.XaraGpuError):
+        q2 = q.copy()
+        q2[10] = 1e6                             # initial stress: not covered
+        gpu.uniaxial_vjp(XG_UNI_STEEL02, q2, hc, 1e-3, yb)
+
+
+# ---------------------------------------------------------------------------
+# GPU: gradients of a transient run
+# ---------------------------------------------------------------------------
+def _adjoint_model(n_frames=2, steps=40, seed=5):
+    """Small frames of the batched-frames workload, one Steel02 per member."""
+    desc, phases = configs.adjoint_frames(n_frames=n_frames, steps=steps, seed=seed)
+    return desc, phases[0]
+
+
+def _objective(desc):
+    return desc.meta["obj_node"], desc.meta["obj_dof"], desc.meta["obj_weight"]
+
+
+@pytest.mark.gpu
+def test_adjoint_gradient_matches_finite_differences(need_gpu):
+    gpu = _gpu()
+    desc, ph = _adjoint_model()
+    node, dof, w = _objective(desc)
+    steps = ph.num_steps
+    q0 = desc.uni_param.reshape(-1, 12).copy()
+    with gpu.DeviceModel(desc) as m:
+        J0 = gpu.adjoint_forward(m, ph, steps, 10, node, dof, w)
+        g = gpu.adjoint_backward(m)
+        assert J0 > 0 and np.isfinite(g).all()
+
+        def J(q):
+            gpu.set_uniaxial_params(m, q)
+            return gpu.adjoint_forward(m, ph, steps, 10, node, dof, w)
+
+        rng = np.random.default_rng(11)
+        scale = np.abs(q0[:, :3])
+        # directional derivative along a random direction over all parameters
+        d = rng.normal(size=q0[:, :3].shape) * scale
+        h = 1e-6
+        qp, qm = q0.copy(), q0.copy()
+        qp[:, :3] += h * d
+        qm[:, :3] -= h * d
+        fd = (J(qp) - J(qm)) / (2 * h)
+        ad = float((g * d).sum())
+        assert ad == pytest.approx(fd, rel=1e-4), (ad, fd)
+        # a few single parameters: the members with the largest sensitivities
+        gs = np.abs(g) * scale
+        for idx in np.argsort(gs.ravel())[-4:]:
+            u, k = divmod(int(idx), 3)
+            qp, qm = q0.copy(), q0.copy()
+            qp[u, k] *= 1 + h
+            qm[u, k] *= 1 - h
+            fd = (J(qp) - J(qm)) / (2 * h * q0[u, k])
+            assert g[u, k] == pytest.approx(fd, rel=1e-3, abs=1e-4 * gs.max() / q0[u, k]), (u, k)
+
+
+@pytest.mark.gpu
+def test_adjoint_checkpoint_interval_and_end_state(need_gpu):
+    gpu = _gpu()
+    desc, ph = _adjoint_model(n_frames=3, steps=30, seed=9)
+    node, dof, w = _objective(desc)
+    with gpu.DeviceModel(desc) as m:
+        Ja = gpu.adjoint_forward(m, ph, 30, 7, node, dof, w)
+        ua, _ = m.disp()
+        ga = gpu.adjoint_backward(m)
+        ub, _ = m.disp()
+        np.testing.assert_array_equal(ua, ub)   # left at the run's last state
+        m.reset()
+        Jb = gpu.adjoint_forward(m, ph, 30, 30, node, dof, w)
+        gb = gpu.adjoint_backward(m)
+    assert Ja == Jb
+    np.testing.assert_allclose(ga, gb, rtol=1e-12, atol=1e-12 * np.abs(ga).max())
+
+
+@pytest.mark.gpu
+def test_adjoint_through_torch_autograd(need_gpu):
+    import torch
+    gpu = _gpu()
+    from xara_gb300.adjoint import frame_response
+    desc, ph = _adjoint_model(n_frames=2, steps=20, seed=2)
+    obj = _objective(desc)
+    q0 = desc.uni_param.reshape(-1, 12)
+    with gpu.DeviceModel(desc) as m:
+        theta = torch.tensor(q0[:, :3], dtype=torch.float64, requires_grad=True)
+        J = frame_response(theta, m, ph, 20, 5, obj)
+        (2.0 * J).backward()
+        m.reset()
+        J2 = gpu.adjoint_forward(m, ph, 20, 5, *obj)
+        g = gpu.adjoint_backward(m)
+    assert float(J) == J2
+    np.testing.assert_allclose(theta.grad.numpy(), 2.0 * g, rtol=1e-13, atol=0)

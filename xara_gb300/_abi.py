@@ -56,6 +56,10 @@ class xg_phase_desc(C.Structure):
     ]
 
 
+class xg_objective_desc(C.Structure):
+    _fields_ = [("num_terms", C.c_int), ("node", _pi), ("dof", _pi), ("weight", _pd)]
+
+
 class xg_step_stats(C.Structure):
     _fields_ = [("newton_iters", C.c_int), ("solver_iters", C.c_int),
                 ("elem_iters", C.c_int), ("status", C.c_int)]

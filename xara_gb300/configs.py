@@ -559,3 +559,50 @@ def frame_batch(n_frames=4096, steps=2000, dt=0.01, seed=0, nfib=40, return_part
     if return_parts:
         return desc, [quake], parts
     return desc, [quake]
+
+
+def adjoint_frames(n_frames=64, steps=2000, dt=0.01, seed=0, nfib=40, member_cov=0.05,
+                   pga_scale=1.0):
+    """Frames of the batched-frames workload with one Steel02 material per
+    member (fy and b varied per member by a lognormal factor of CoV
+    ``member_cov``), for gradients with respect to per-member parameters.
+    The objective terms in ``desc.meta`` are every frame's roof drift: the
+    roof-left node's horizontal displacement over the frame height, squared
+    and summed over the steps (node tags, dof 0, weight 1/H^2)."""
+    desc, phases = frame_batch(n_frames=n_frames, steps=steps, dt=dt, seed=seed, nfib=nfib)
+    a = desc.arrays
+    ss, em, fmat = a["sec_fiber_start"], a["elem_mat"], a["fib_mat"]
+    uni = a["uni_param"].reshape(-1, XG_UNI_NPARAM)
+    rng = np.random.default_rng(seed + 11)
+    ne = len(em)
+    lo, hi = ss[em], ss[em + 1]
+    counts = hi - lo
+    idx = np.concatenate([np.arange(l, h) for l, h in zip(lo, hi)])
+    rows = uni[fmat[lo]].copy()
+    rows[:, 0] *= np.exp(rng.normal(0.0, member_cov, ne))
+    rows[:, 2] *= np.exp(rng.normal(0.0, member_cov, ne))
+    kw = {k: v for k, v in a.items() if v is not None}
+    kw.update(elem_mat=np.arange(ne), sec_fiber_start=np.concatenate([[0], np.cumsum(counts)]),
+              fib_y=a["fib_y"][idx], fib_area=a["fib_area"][idx],
+              fib_mat=np.repeat(np.arange(ne), counts), uni_type=np.full(ne, XG_UNI_STEEL02),
+              uni_param=rows)
+    out = ModelDesc(ndm=desc.ndm, ndf=desc.ndf, elem_type=desc.elem_type,
+                    geom_transf=desc.geom_transf, fbc_num_ip=desc.fbc_num_ip, **kw)
+    ph = phases[0]
+    rec = np.asarray(ph.gm_node_record)
+    crd = a["node_crd"].reshape(-1, 2)
+    tags = a["node_tag"]
+    obj_node, obj_w = [], []
+    for f in range(n_frames):
+        nodes = np.nonzero(rec == f)[0]
+        top = crd[nodes, 1].max()
+        roof = nodes[crd[nodes, 1] == top]
+        obj_node.append(int(tags[roof[np.argmin(crd[roof, 0])]]))
+        obj_w.append(1.0 / (top * top))
+    if pga_scale != 1.0:
+        ph.gm_accel = np.ascontiguousarray(ph.gm_accel * pga_scale)
+    out.meta = dict(desc.meta, workload=f"{n_frames} 2D steel frames, one Steel02 per member",
+                    obj_node=np.asarray(obj_node, np.int32),
+                    obj_dof=np.zeros(n_frames, np.int32), obj_weight=np.asarray(obj_w),
+                    members=ne)
+    return out, [ph]

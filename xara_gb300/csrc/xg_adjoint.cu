@@ -1,0 +1,495 @@
+// xg_adjoint.cu -- reverse sweep of a Newmark run of force-based frames:
+// the discrete adjoint of the converged step sequence with respect to the
+// uniaxial materials' first three parameters (Steel02: Fy, E0, b).
+//
+// A converged step n satisfies R(U_n; U', V', A', h', theta) = 0 (the
+// dynamic unbalance of Newmark.cpp:262-302 with the resisting force of
+// ForceBeamColumn2d/3d::update at the committed fiber records h'), and
+// commits the fiber records h_n = H(eps(U_n), h', theta).  Its adjoint, with
+// the effective tangent K (symmetric, the one the forward step factors):
+//   K mu = Ubar_n + c2 Vbar_n + c3 Abar_n + (dh_n/dU_n)' hbar_n
+//   hbar' = (dh_n/dh')' hbar_n - (dP/dh')' mu,   thetabar += the same in theta
+// plus the Newmark predictor's terms for (U', V', A').  Inside an element the
+// converged compatibility state (basic forces Se, section deformations e_s)
+// is an implicit function of the basic deformations v, h' and theta:
+//   dSe  = kv (dv + sum_s w_s b_s' fs_s q_s),   de_s = fs_s (b_s dSe - q_s),
+//   q_s  = sum_f A_f a_f dsigma_f (strain fixed),  a_f = (1, -y [, z])
+// so one reverse pass over an element needs the section flexibilities fs_s,
+// kv and e_s of the converged state and two vector-Jacobian products of the
+// fiber law: one with the records' adjoint (giving the strain adjoint that
+// flows into e_s) and one with the stress adjoint the section equations
+// pass down.
+#include <cuda_runtime.h>
+
+#include "xg_internal.h"
+#include "xg_uniaxial_adj.h"
+
+namespace xg {
+
+namespace {
+
+constexpr int kAdjWarps = 4;
+
+__device__ __forceinline__ double warp_sum_adj(double v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
+__device__ __forceinline__ int stride_of(int nip) { return 6 + 36 + nip * 24 + 6 + 1; }
+
+// kv0 = f0^-1: Gauss-Jordan with partial pivoting; in 3D the torsion row and
+// column are uncoupled, so the 5x5 block is inverted and kv0(5,5) = 1/f0(5,5)
+template <int NB>
+__device__ void small_inverse(const double *f, double *kv) {
+  constexpr int N = NB == 3 ? 3 : 5;
+  double M[N][2 * N];
+  for (int i = 0; i < N; i++)
+    for (int j = 0; j < 2 * N; j++) M[i][j] = j < N ? f[i * NB + j] : (j - N == i ? 1.0 : 0.0);
+  for (int c = 0; c < N; c++) {
+    int piv = c;
+    for (int i = c + 1; i < N; i++)
+      if (fabs(M[i][c]) > fabs(M[piv][c])) piv = i;
+    if (piv != c)
+      for (int j = 0; j < 2 * N; j++) { const double t = M[c][j]; M[c][j] = M[piv][j]; M[piv][j] = t; }
+    const double inv = 1.0 / M[c][c];
+    for (int j = 0; j < 2 * N; j++) M[c][j] *= inv;
+    for (int i = 0; i < N; i++) {
+      if (i == c) continue;
+      const double m = M[i][c];
+      for (int j = 0; j < 2 * N; j++) M[i][j] -= m * M[c][j];
+    }
+  }
+  for (int i = 0; i < NB * NB; i++) kv[i] = 0.0;
+  for (int i = 0; i < N; i++)
+    for (int j = 0; j < N; j++) kv[i * NB + j] = M[i][N + j];
+  if (NB == 6) kv[35] = 1.0 / f[35];
+}
+
+// basic <- global transformation of a linear frame transformation
+// (LinearCrdTransf2d.cpp:248-299, BasicFrameTransf.cpp:90-104)
+template <int NB>
+__device__ void basic_T(const FrameView &v, int e, double (*T)[NB == 3 ? 6 : 12]) {
+  constexpr int NU = NB == 3 ? 6 : 12;
+  const double L = v.L[e];
+  const double *R = v.R + 9 * (long)e;
+#pragma unroll
+  for (int i = 0; i < NB; i++)
+#pragma unroll
+    for (int j = 0; j < NU; j++) T[i][j] = 0.0;
+  if (NB == 3) {
+    const double cs = R[0], sn = R[1], sl = sn / L, cl = cs / L;
+    T[0][0] = -cs; T[0][1] = -sn; T[0][3] = cs; T[0][4] = sn;
+    T[1][0] = -sl; T[1][1] = cl; T[1][2] = 1.0; T[1][3] = sl; T[1][4] = -cl;
+    T[2][0] = -sl; T[2][1] = cl; T[2][3] = sl; T[2][4] = -cl; T[2][5] = 1.0;
+  } else {
+#pragma unroll
+    for (int j = 0; j < 3; j++) {
+      const double e1 = R[3 * j + 0], e2 = R[3 * j + 1], e3 = R[3 * j + 2];
+      T[0][0 + j] = -e1; T[0][6 + j] = e1;
+      T[1][3 + j] = e3; T[1][0 + j] = e2 / L; T[1][6 + j] = -e2 / L;
+      T[2][9 + j] = e3; T[2][0 + j] = e2 / L; T[2][6 + j] = -e2 / L;
+      T[3][3 + j] = e2; T[3][0 + j] = -e3 / L; T[3][6 + j] = e3 / L;
+      T[4][9 + j] = e2; T[4][0 + j] = -e3 / L; T[4][6 + j] = e3 / L;
+      T[5][3 + j] = -e1; T[5][9 + j] = e1;
+    }
+  }
+}
+
+__device__ __forceinline__ void fiber_vjp(int type, const double *q, const double *hc,
+                                          double strain, const double *yb, double *hb,
+                                          double *sb, double *qb) {
+  if (type == XG_UNI_STEEL02) steel02_vjp(q, hc, strain, yb, hb, sb, qb);
+  else elastic_vjp(q, strain, yb, hb, sb, qb);
+}
+
+// Pass A (warp per element): every fiber's record adjoint through the law
+// gives the adjoint of the committed record (in place), of the parameters,
+// and of the fiber strain; the strain adjoints reduce to ebar_s per section,
+// which the element equations turn into the adjoint of the basic
+// deformations z = kv sum_s b_s' fs_s ebar_s and, through T', of the
+// element's global displacements (written to the element force scratch).
+template <int NB, int ORD>
+__global__ void __launch_bounds__(32 * kAdjWarps) k_adj_elem_a(FrameView v, AdjView a) {
+  constexpr int NU = NB == 3 ? 6 : 12;
+  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int e = blockIdx.x * kAdjWarps + w;
+  if (e >= v.ne) return;
+  const int nip = v.nip;
+  const double *st = a.st + (long)e * stride_of(nip);
+  const int sec = v.sec[e];
+  const int f0 = v.sec_fstart[sec], nf = v.sec_fstart[sec + 1] - f0;
+  const double ybar = v.ybar[sec], zbar = ORD == 4 ? v.zbar[sec] : 0.0;
+  const long fbase = v.foff[e];
+  double *scr = a.scr + (long)e * (6 + nip * 4);
+  double tq0 = 0.0, tq1 = 0.0, tq2 = 0.0;
+  double Sb[NB];
+#pragma unroll
+  for (int i = 0; i < NB; i++) Sb[i] = 0.0;
+  constexpr int kRow[6] = {0, 1, 1, 2, 2, 3};
+  for (int ip = 0; ip < nip; ip++) {
+    const double xL = v.xi[ip], xL1 = xL - 1.0;
+    const double ca[6] = {1.0, xL1, xL, xL1, xL, 1.0};
+    double vsec[ORD];
+#pragma unroll
+    for (int r = 0; r < ORD; r++) vsec[r] = st[42 + ip * 4 + r];
+    double eb0 = 0.0, eb1 = 0.0, eb2 = 0.0;
+    const long rec0 = (fbase + (long)ip * nf) * 12;
+    for (int fi = lane; fi < nf; fi += 32) {
+      const int kf = f0 + fi;
+      const double y = v.fy[kf] - ybar;
+      double strain = vsec[0] - y * vsec[1];
+      double z = 0.0;
+      if (ORD == 4) {
+        z = v.fz[kf] - zbar;
+        strain += z * vsec[2];
+      }
+      const int u = v.fmat[kf];
+      const double *q = v.uparam + (long)u * XG_UNI_NPARAM;
+      const double *hcp = a.fh_prev + rec0 + 12L * fi;
+      double *hbr = a.hbar + rec0 + 12L * fi;
+      double hc[12], yb[12], hb[12], sb, qb[3];
+#pragma unroll
+      for (int k = 0; k < 12; k++) { hc[k] = hcp[k]; yb[k] = hbr[k]; }
+      fiber_vjp(v.utype[u], q, hc, strain, yb, hb, &sb, qb);
+#pragma unroll
+      for (int k = 0; k < 12; k++) hbr[k] = hb[k];
+      tq0 += qb[0]; tq1 += qb[1]; tq2 += qb[2];
+      eb0 += sb;
+      eb1 += -y * sb;
+      if (ORD == 4) eb2 += z * sb;
+    }
+    double eb[ORD];
+    eb[0] = warp_sum_adj(eb0);
+    eb[1] = warp_sum_adj(eb1);
+    if (ORD == 4) { eb[2] = warp_sum_adj(eb2); eb[3] = 0.0; }
+    if (lane == 0) {
+#pragma unroll
+      for (int r = 0; r < ORD; r++) scr[6 + ip * 4 + r] = eb[r];
+    }
+    const double *fs = st + 42 + nip * 4 + ip * 16;
+    double t[ORD];
+#pragma unroll
+    for (int r = 0; r < ORD; r++) {
+      double s = 0.0;
+#pragma unroll
+      for (int k = 0; k < ORD; k++) s += fs[r * ORD + k] * eb[k];
+      t[r] = s;
+    }
+#pragma unroll
+    for (int c = 0; c < NB; c++) Sb[c] += ca[c] * t[kRow[c]];
+  }
+  const double *kv = st + 6;
+  double zA[NB];
+#pragma unroll
+  for (int i = 0; i < NB; i++) {
+    double s = 0.0;
+#pragma unroll
+    for (int k = 0; k < NB; k++) s += kv[i * NB + k] * Sb[k];
+    zA[i] = s;
+  }
+  tq0 = warp_sum_adj(tq0);
+  tq1 = warp_sum_adj(tq1);
+  tq2 = warp_sum_adj(tq2);
+  if (lane == 0) {
+    double T[NB][NU];
+    basic_T<NB>(v, e, T);
+    double *ue = v.Re + (long)e * NU;
+#pragma unroll
+    for (int j = 0; j < NU; j++) {
+      double s = 0.0;
+#pragma unroll
+      for (int k = 0; k < NB; k++) s += T[k][j] * zA[k];
+      ue[j] = s;
+    }
+#pragma unroll
+    for (int i = 0; i < NB; i++) scr[i] = zA[i];
+    a.theta[3L * e + 0] += tq0;
+    a.theta[3L * e + 1] += tq1;
+    a.theta[3L * e + 2] += tq2;
+  }
+}
+
+// Pass B (warp per element), after the adjoint solve: the basic-force
+// adjoint -T mu_e and pass A's terms give the section adjoints
+// qbar_s = w_s fs_s b_s z - fs_s ebar_s; each fiber's stress adjoint
+// A_f a_f . qbar_s goes through the law into the committed record's and the
+// parameters' adjoints.  The betaK0 K0 damping adds -betaK0/E (T mu)' kv0
+// (T V_n) to the element material's modulus (K0 is linear in it).
+template <int NB, int ORD>
+__global__ void __launch_bounds__(32 * kAdjWarps) k_adj_elem_b(FrameView v, AdjView a) {
+  constexpr int NU = NB == 3 ? 6 : 12;
+  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int e = blockIdx.x * kAdjWarps + w;
+  if (e >= v.ne) return;
+  const int nip = v.nip, ndf = v.ndf;
+  const double *st = a.st + (long)e * stride_of(nip);
+  const int sec = v.sec[e];
+  const int f0 = v.sec_fstart[sec], nf = v.sec_fstart[sec + 1] - f0;
+  const double ybar = v.ybar[sec], zbar = ORD == 4 ? v.zbar[sec] : 0.0;
+  const double L = v.L[e];
+  const long fbase = v.foff[e];
+  const double *scr = a.scr + (long)e * (6 + nip * 4);
+  double T[NB][NU];
+  basic_T<NB>(v, e, T);
+  double mue[NU], ve[NU];
+  const int nd = NU / 2;
+#pragma unroll
+  for (int j = 0; j < NU; j++) {
+    const int node = v.conn[2 * e + j / nd];
+    const long dof = (long)node * ndf + (j % nd);
+    const int eq = a.eqn[dof];
+    mue[j] = eq >= 0 ? a.mu[eq] : 0.0;
+    ve[j] = a.Vn ? a.Vn[dof] : 0.0;
+  }
+  const double *kv = st + 6;
+  double pb[NB], z[NB];
+#pragma unroll
+  for (int i = 0; i < NB; i++) {
+    double s = 0.0;
+#pragma unroll
+    for (int j = 0; j < NU; j++) s += T[i][j] * mue[j];
+    pb[i] = s;                         // T mu_e; the basic-force adjoint is -pb
+  }
+#pragma unroll
+  for (int i = 0; i < NB; i++) {
+    double s = 0.0;
+#pragma unroll
+    for (int k = 0; k < NB; k++) s -= kv[i * NB + k] * pb[k];
+    z[i] = scr[i] + s;
+  }
+  double tq0 = 0.0, tq1 = 0.0, tq2 = 0.0;
+  constexpr int kRow[6] = {0, 1, 1, 2, 2, 3};
+  for (int ip = 0; ip < nip; ip++) {
+    const double xL = v.xi[ip], xL1 = xL - 1.0, wtL = v.wt[ip] * L;
+    const double ca[6] = {1.0, xL1, xL, xL1, xL, 1.0};
+    double bz[ORD];
+#pragma unroll
+    for (int r = 0; r < ORD; r++) bz[r] = 0.0;
+#pragma unroll
+    for (int c = 0; c < NB; c++) bz[kRow[c]] += ca[c] * z[c];
+    double g[ORD];
+#pragma unroll
+    for (int r = 0; r < ORD; r++) g[r] = wtL * bz[r] - scr[6 + ip * 4 + r];
+    const double *fs = st + 42 + nip * 4 + ip * 16;
+    double qs[ORD];
+#pragma unroll
+    for (int r = 0; r < ORD; r++) {
+      double s = 0.0;
+#pragma unroll
+      for (int k = 0; k < ORD; k++) s += fs[r * ORD + k] * g[k];
+      qs[r] = s;
+    }
+    double vsec[ORD];
+#pragma unroll
+    for (int r = 0; r < ORD; r++) vsec[r] = st[42 + ip * 4 + r];
+    const long rec0 = (fbase + (long)ip * nf) * 12;
+    for (int fi = lane; fi < nf; fi += 32) {
+      const int kf = f0 + fi;
+      const double y = v.fy[kf] - ybar, A = v.fA[kf];
+      double strain = vsec[0] - y * vsec[1];
+      double rf = qs[0] - y * qs[1];
+      if (ORD == 4) {
+        const double zz = v.fz[kf] - zbar;
+        strain += zz * vsec[2];
+        rf += zz * qs[2];
+      }
+      rf *= A;
+      const int u = v.fmat[kf];
+      const double *q = v.uparam + (long)u * XG_UNI_NPARAM;
+      const double *hcp = a.fh_prev + rec0 + 12L * fi;
+      double *hbr = a.hbar + rec0 + 12L * fi;
+      double hc[12], yb[12], hb[12], sb, qb[3];
+#pragma unroll
+      for (int k = 0; k < 12; k++) { hc[k] = hcp[k]; yb[k] = 0.0; }
+      yb[9] = rf;
+      fiber_vjp(v.utype[u], q, hc, strain, yb, hb, &sb, qb);
+#pragma unroll
+      for (int k = 0; k < 12; k++) hbr[k] += hb[k];
+      tq0 += qb[0]; tq1 += qb[1]; tq2 += qb[2];
+    }
+  }
+  tq0 = warp_sum_adj(tq0);
+  tq1 = warp_sum_adj(tq1);
+  tq2 = warp_sum_adj(tq2);
+  if (lane == 0) {
+    if (a.use_k0) {
+      // kv0 = (sum_s w_s b_s' fs0 b_s)^-1 (ForceBeamColumn2d/3d::getInitialStiff)
+      const double *fs0 = v.fs0 + 16 * (long)sec;
+      double f[NB * NB];
+#pragma unroll
+      for (int i = 0; i < NB * NB; i++) f[i] = 0.0;
+      for (int ip = 0; ip < nip; ip++) {
+        const double xL = v.xi[ip], xL1 = xL - 1.0, wtL = v.wt[ip] * L;
+        const double ca[6] = {1.0, xL1, xL, xL1, xL, 1.0};
+#pragma unroll
+        for (int c = 0; c < NB; c++) {
+          const double wa = ca[c] * wtL;
+#pragma unroll
+          for (int d = 0; d < NB; d++) f[c * NB + d] += wa * (fs0[kRow[c] * ORD + kRow[d]] * ca[d]);
+        }
+      }
+      double kv0[NB * NB];
+      small_inverse<NB>(f, kv0);
+      double rv[NB];
+#pragma unroll
+      for (int i = 0; i < NB; i++) {
+        double s = 0.0;
+#pragma unroll
+        for (int j = 0; j < NU; j++) s += T[i][j] * ve[j];
+        rv[i] = s;
+      }
+      double val = 0.0;
+#pragma unroll
+      for (int i = 0; i < NB; i++)
+#pragma unroll
+        for (int k = 0; k < NB; k++) val += pb[i] * kv0[i * NB + k] * rv[k];
+      const int u = a.elem_uni[e];
+      const int ie = v.utype[u] == XG_UNI_STEEL02 ? 1 : 0;
+      const double E = v.uparam[(long)u * XG_UNI_NPARAM + ie];
+      const double bk = a.bk0 ? a.bk0[e] : a.bk0_all;
+      const double d = -bk / E * val;
+      if (ie == 1) tq1 += d; else tq0 += d;
+    }
+    a.theta[3L * e + 0] += tq0;
+    a.theta[3L * e + 1] += tq1;
+    a.theta[3L * e + 2] += tq2;
+  }
+}
+
+// The fresh records' dependence on the parameters (Steel02 revertToStart,
+// Steel02.cpp:70-95: epsmax = Fy/E0, epsmin = -Fy/E0).
+__global__ void k_adj_init_records(FrameView v, AdjView a) {
+  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int e = blockIdx.x * kAdjWarps + w;
+  if (e >= v.ne) return;
+  const int sec = v.sec[e];
+  const int f0 = v.sec_fstart[sec], nf = v.sec_fstart[sec + 1] - f0;
+  double t0 = 0.0, t1 = 0.0;
+  for (int k = lane; k < v.nip * nf; k += 32) {
+    const int kf = f0 + k % nf;
+    const int u = v.fmat[kf];
+    if (v.utype[u] != XG_UNI_STEEL02) continue;
+    const double *q = v.uparam + (long)u * XG_UNI_NPARAM;
+    const double *hb = a.hbar + (v.foff[e] + k) * 12;
+    const double d = hb[1] - hb[0];
+    t0 += d / q[1];
+    t1 -= d * q[0] / (q[1] * q[1]);
+  }
+  t0 = warp_sum_adj(t0);
+  t1 = warp_sum_adj(t1);
+  if (lane == 0) {
+    a.theta[3L * e + 0] += t0;
+    a.theta[3L * e + 1] += t1;
+  }
+}
+
+// J += sum_k w_k U[dof_k]^2 (one thread, term order)
+__global__ void k_adj_objective(int nterm, const int *dof, const double *w, const double *U,
+                                double *J) {
+  if (blockIdx.x != 0 || threadIdx.x != 0) return;
+  double s = 0.0;
+  for (int k = 0; k < nterm; k++) s += w[k] * U[dof[k]] * U[dof[k]];
+  *J += s;
+}
+
+// Ubar[eqn[dof_k]] += 2 w_k U[dof_k] (one thread, term order)
+__global__ void k_adj_objective_grad(int nterm, const int *dof, const double *w, const int *eqn,
+                                     const double *U, double *Ubar) {
+  if (blockIdx.x != 0 || threadIdx.x != 0) return;
+  for (int k = 0; k < nterm; k++) {
+    const int eq = eqn[dof[k]];
+    if (eq >= 0) Ubar[eq] += 2.0 * w[k] * U[dof[k]];
+  }
+}
+
+__global__ void k_adj_rhs(int neq, const double *Ub, const double *Vb, const double *Ab,
+                          const double *uA, double c2, double c3, double *rhs) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < neq) rhs[i] = Ub[i] + c2 * Vb[i] + c3 * Ab[i] + uA[i];
+}
+
+__global__ void k_adj_prev(int neq, const double *mu, const double *kmu, const double *meq,
+                           const double *meq_am, NewmarkCoef c, double *Ub, double *Vb,
+                           double *Ab) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= neq) return;
+  const double m = meq[i] * mu[i], ma = meq_am[i] * mu[i], km = kmu ? kmu[i] : 0.0;
+  const double vb = Vb[i], ab = Ab[i];
+  Ub[i] = c.c3 * m + c.c2 * (ma + km) - c.c2 * vb - c.c3 * ab;
+  Vb[i] = -(c.a3 * m + c.a1 * (ma + km)) + c.a1 * vb + c.a3 * ab;
+  Ab[i] = -(c.a4 * m + c.a2 * (ma + km)) + c.a2 * vb + c.a4 * ab;
+}
+
+inline int grid_of(long n, int b) { return (int)((n + b - 1) / b); }
+
+}  // namespace
+
+int launch_adj_elem_a(const FrameView &v, const AdjView &a, cudaStream_t s) {
+  if (v.ne == 0) return 0;
+  const int grid = grid_of(v.ne, kAdjWarps);
+  if (v.nb == 3) k_adj_elem_a<3, 2><<<grid, 32 * kAdjWarps, 0, s>>>(v, a);
+  else k_adj_elem_a<6, 4><<<grid, 32 * kAdjWarps, 0, s>>>(v, a);
+  return cudaGetLastError() == cudaSuccess ? 0 : XG_ECUDA;
+}
+
+int launch_adj_elem_b(const FrameView &v, const AdjView &a, cudaStream_t s) {
+  if (v.ne == 0) return 0;
+  const int grid = grid_of(v.ne, kAdjWarps);
+  if (v.nb == 3) k_adj_elem_b<3, 2><<<grid, 32 * kAdjWarps, 0, s>>>(v, a);
+  else k_adj_elem_b<6, 4><<<grid, 32 * kAdjWarps, 0, s>>>(v, a);
+  return cudaGetLastError() == cudaSuccess ? 0 : XG_ECUDA;
+}
+
+int launch_adj_init_records(const FrameView &v, const AdjView &a, cudaStream_t s) {
+  if (v.ne == 0) return 0;
+  k_adj_init_records<<<grid_of(v.ne, kAdjWarps), 32 * kAdjWarps, 0, s>>>(v, a);
+  return cudaGetLastError() == cudaSuccess ? 0 : XG_ECUDA;
+}
+
+int launch_adj_objective(int nterm, const int *dof, const double *w, const double *U, double *J,
+                         cudaStream_t s) {
+  if (nterm == 0) return 0;
+  k_adj_objective<<<1, 32, 0, s>>>(nterm, dof, w, U, J);
+  return cudaGetLastError() == cudaSuccess ? 0 : XG_ECUDA;
+}
+
+int launch_adj_objective_grad(int nterm, const int *dof, const double *w, const int *eqn,
+                              const double *U, double *Ubar, cudaStream_t s) {
+  if (nterm == 0) return 0;
+  k_adj_objective_grad<<<1, 32, 0, s>>>(nterm, dof, w, eqn, U, Ubar);
+  return cudaGetLastError() == cudaSuccess ? 0 : XG_ECUDA;
+}
+
+int launch_adj_rhs(int neq, const double *Ub, const double *Vb, const double *Ab,
+                   const double *uA, double c2, double c3, double *rhs, cudaStream_t s) {
+  if (neq == 0) return 0;
+  k_adj_rhs<<<grid_of(neq, 256), 256, 0, s>>>(neq, Ub, Vb, Ab, uA, c2, c3, rhs);
+  return cudaGetLastError() == cudaSuccess ? 0 : XG_ECUDA;
+}
+
+int launch_adj_prev(int neq, const double *mu, const double *kmu, const double *meq,
+                    const double *meq_am, const NewmarkCoef &c, double *Ub, double *Vb,
+                    double *Ab, cudaStream_t s) {
+  if (neq == 0) return 0;
+  k_adj_prev<<<grid_of(neq, 256), 256, 0, s>>>(neq, mu, kmu, meq, meq_am, c, Ub, Vb, Ab);
+  return cudaGetLastError() == cudaSuccess ? 0 : XG_ECUDA;
+}
+
+}  // namespace xg
+
+// Host entry for the derivative tests: the vector-Jacobian product of one
+// material point (no device work).
+extern "C" int xg_uniaxial_vjp(int type, const double *q, const double *hc, double strain,
+                               const double *yb, double *hb, double *sb, double *qb) {
+  if (!q || !hc || !yb || !hb || !sb || !qb) return XG_EINVAL;
+  if (type == XG_UNI_STEEL02) {
+    if (q[10] != 0.0) return XG_EINVAL;
+    xg::steel02_vjp(q, hc, strain, yb, hb, sb, qb);
+  } else if (type == XG_UNI_ELASTIC) {
+    xg::elastic_vjp(q, strain, yb, hb, sb, qb);
+  } else {
+    return XG_EINVAL;
+  }
+  return 0;
+}

@@ -176,6 +176,13 @@ int launch_dyn_unbalance(const DynView &d, const double *fext, const double *pin
   return cudaGetLastError() == cudaSuccess ? 0 : XG_ECUDA;
 }
 
+int launch_spmv(int n, const int *rowptr, const int *colidx, const double *vals, const double *x,
+                double *y, cudaStream_t s) {
+  if (n == 0) return 0;
+  k_spmv<<<grid((long)n * 32, 256), 256, 0, s>>>(n, rowptr, colidx, vals, x, y);
+  return cudaGetLastError() == cudaSuccess ? 0 : XG_ECUDA;
+}
+
 int launch_dyn_tangent(const DynView &d, double *vals, const double *k0vals, double c1,
                        double c2bk0, double c2, double c3, cudaStream_t s) {
   if (d.nnz > 0) k_dyn_tangent<<<grid(d.nnz, 256), 256, 0, s>>>(d, vals, k0vals, c1, c2bk0, c2, c3);

@@ -216,4 +216,39 @@ int launch_scale_blocks(int nblk, int len, const double *scale, double s0, doubl
 int launch_comp_norm2(int ncomp, const int *cstart, const double *x, double *out,
                       cudaStream_t s);
 int launch_comp_mask(int neq, const int *comp_of, const int *active, double *B, cudaStream_t s);
+// y = A x over the CSR pattern
+int launch_spmv(int n, const int *rowptr, const int *colidx, const double *vals, const double *x,
+                double *y, cudaStream_t s);
+
+// Adjoint of a Newmark run of force-based frames (xg_adjoint.cu)
+struct NewmarkCoef {
+  double c2, c3;              // velocity / acceleration per displacement increment
+  double a1, a2, a3, a4;      // predictor: V = a1 Vc + a2 Ac, A = a4 Ac + a3 Vc
+};
+struct AdjView {
+  const double *st;           // converged element state of the step [ne*stride]
+  const double *fh_prev;      // committed fiber records before the step [nrec*12]
+  double *hbar;               // [nrec*12] record adjoint: after the step in, before it out
+  double *theta;              // [ne*3] parameter adjoint of each element's material
+  double *scr;                // [ne*(6+nip*4)] pass A's z and section ebar
+  const int *eqn;             // [nn*ndf]
+  const double *mu;           // [neq] adjoint solution of the step
+  const double *Vn;           // [nn*ndf] velocity after the step (betaK0 term)
+  const double *bk0;          // [ne] betaK0 per element, or null
+  double bk0_all;             // betaK0 when bk0 is null
+  int use_k0;                 // betaK0 K0 damping present
+  const int *elem_uni;        // [ne] the single material of each element's fibers
+};
+int launch_adj_elem_a(const FrameView &v, const AdjView &a, cudaStream_t s);
+int launch_adj_elem_b(const FrameView &v, const AdjView &a, cudaStream_t s);
+int launch_adj_init_records(const FrameView &v, const AdjView &a, cudaStream_t s);
+int launch_adj_objective(int nterm, const int *dof, const double *w, const double *U, double *J,
+                         cudaStream_t s);
+int launch_adj_objective_grad(int nterm, const int *dof, const double *w, const int *eqn,
+                              const double *U, double *Ubar, cudaStream_t s);
+int launch_adj_rhs(int neq, const double *Ub, const double *Vb, const double *Ab,
+                   const double *uA, double c2, double c3, double *rhs, cudaStream_t s);
+int launch_adj_prev(int neq, const double *mu, const double *kmu, const double *meq,
+                    const double *meq_am, const NewmarkCoef &c, double *Ub, double *Vb,
+                    double *Ab, cudaStream_t s);
 }  // namespace xg

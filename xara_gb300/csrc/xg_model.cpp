@@ -197,6 +197,26 @@ struct xg_model {
   }
   int upload_dynamics();
   int step_newmark(xg_step_stats *st);
+  // adjoint of a Newmark run (xg_adjoint_forward / xg_adjoint_backward): the
+  // committed state every K steps (U V A, fiber records, element state), the
+  // K+1 states of the segment being swept, and the adjoint vectors
+  struct AdjRun {
+    bool have = false;
+    int N = 0, K = 0, nterm = 0, nck = 0;
+    size_t len = 0;                        // doubles in one saved state
+    std::vector<double> ck_time;
+    std::vector<int> elem_uni;
+    DBuf<int> dof, d_elem_uni;
+    DBuf<double> w, J, ck, seg, Ub, Vb, Ab, hbar, theta, scr, mu, rhs, tmp, kmu;
+  } adj;
+  long steps_since_reset = 0;
+  size_t adj_off_fh() const { return 3 * (size_t)nn * ndf; }
+  size_t adj_off_st() const { return adj_off_fh() + (size_t)fb_nrec * 12; }
+  int adj_save(double *dst);
+  int adj_load(const double *src, double t);
+  int adjoint_forward(const xg_phase_desc *ph, int N, int K, const xg_objective_desc *obj,
+                      double *J);
+  int adjoint_backward(double scale, double *grad, int num_uni);
   // analysis state
   xg_phase_desc phase{};
   bool have_phase = false;
@@ -1305,6 +1325,7 @@ static int read_scalar(const double *d, double *h, cudaStream_t s) {
 // One step: integrator newStep, NewtonRaphson::solveCurrentStep, commit
 // (runtime/runtime/BasicAnalysisBuilder.cpp:337-420).
 int xg_model::step(xg_step_stats *st) {
+  steps_since_reset++;
   if (phase.integrator == XG_INT_NEWMARK) return step_newmark(st);
   cudaStream_t s = stream;
   last_solver_iters = 0;
@@ -1405,6 +1426,223 @@ int xg_model::revert_state() {
   CK(cudaMemcpyAsync(d_A.p, d_Ac.p, (size_t)nn * ndf * sizeof(double), cudaMemcpyDeviceToDevice, s));
   // Domain::revertToLastCommit ends with Domain::update at the committed
   // displacements (domain/domain/Domain.cpp:1925-1949)
+  return element_state(true);
+}
+
+// ---------------------------------------------------------------------------
+// adjoint of a Newmark run
+// ---------------------------------------------------------------------------
+// committed state -> dst: U V A [nn*ndf each], fiber records, element state
+int xg_model::adj_save(double *dst) {
+  cudaStream_t s = stream;
+  const size_t nu = (size_t)nn * ndf, nst = (size_t)ne * frame_state_stride(fb_nip);
+  CK(cudaMemcpyAsync(dst, d_Uc.p, nu * sizeof(double), cudaMemcpyDeviceToDevice, s));
+  CK(cudaMemcpyAsync(dst + nu, d_Vc.p, nu * sizeof(double), cudaMemcpyDeviceToDevice, s));
+  CK(cudaMemcpyAsync(dst + 2 * nu, d_Ac.p, nu * sizeof(double), cudaMemcpyDeviceToDevice, s));
+  CK(cudaMemcpyAsync(dst + adj_off_fh(), d_fh_c.p, (size_t)fb_nrec * 12 * sizeof(double),
+                     cudaMemcpyDeviceToDevice, s));
+  CK(cudaMemcpyAsync(dst + adj_off_st(), d_st_c.p, nst * sizeof(double), cudaMemcpyDeviceToDevice, s));
+  return 0;
+}
+
+// a saved state becomes the committed and the trial state (as right after
+// the commit that produced it)
+int xg_model::adj_load(const double *src, double t) {
+  cudaStream_t s = stream;
+  const size_t nu = (size_t)nn * ndf, nst = (size_t)ne * frame_state_stride(fb_nip);
+  const size_t nrec = (size_t)fb_nrec * 12;
+  for (double *d : {d_U.p, d_Uc.p})
+    CK(cudaMemcpyAsync(d, src, nu * sizeof(double), cudaMemcpyDeviceToDevice, s));
+  for (double *d : {d_V.p, d_Vc.p})
+    CK(cudaMemcpyAsync(d, src + nu, nu * sizeof(double), cudaMemcpyDeviceToDevice, s));
+  for (double *d : {d_A.p, d_Ac.p})
+    CK(cudaMemcpyAsync(d, src + 2 * nu, nu * sizeof(double), cudaMemcpyDeviceToDevice, s));
+  for (double *d : {d_fh_c.p, d_fh_t.p})
+    CK(cudaMemcpyAsync(d, src + adj_off_fh(), nrec * sizeof(double), cudaMemcpyDeviceToDevice, s));
+  for (double *d : {d_st.p, d_st_c.p})
+    CK(cudaMemcpyAsync(d, src + adj_off_st(), nst * sizeof(double), cudaMemcpyDeviceToDevice, s));
+  time = time_c = t;
+  blocks_factored = false;
+  prof_factored = false;
+  return 0;
+}
+
+// Newmark run of num_steps from the initial state with the objective
+// J = sum over steps n and terms k of w_k U_n[dof_k]^2, keeping the
+// committed state every K steps for the reverse sweep.
+int xg_model::adjoint_forward(const xg_phase_desc *ph, int N, int K, const xg_objective_desc *obj,
+                              double *J) {
+  adj.have = false;
+  if (!frames()) return fail(XG_EINVAL, "the adjoint covers force-based frame models");
+  if (!ph || ph->integrator != XG_INT_NEWMARK)
+    return fail(XG_EINVAL, "the adjoint covers Newmark runs");
+  if (N < 1 || K < 1 || !obj || obj->num_terms < 0 || (obj->num_terms > 0 &&
+      (!obj->node || !obj->dof || !obj->weight)))
+    return fail(XG_EINVAL, "bad adjoint run settings");
+  if (fb_nb == 3 && geom_transf == 1)
+    return fail(XG_EINVAL, "the adjoint covers linear frame transformations");
+  if (steps_since_reset != 0 || have_phase)
+    return fail(XG_ESTATE, "the adjoint runs from the model's initial state (xg_reset first)");
+  // every element's fibers share one material: Steel02 without initial
+  // stress, or elastic
+  adj.elem_uni.assign(ne, 0);
+  for (int e = 0; e < ne; e++) {
+    const int sc = mat[e];
+    const int u0 = fmat[sec_fstart[sc]];
+    for (int f = sec_fstart[sc]; f < sec_fstart[sc + 1]; f++)
+      if (fmat[f] != u0)
+        return fail(XG_EINVAL, "the adjoint needs one material per element (element %d)", e);
+    if (utype[u0] == XG_UNI_STEEL02) {
+      if (uparam[(size_t)u0 * XG_UNI_NPARAM + 10] != 0.0)
+        return fail(XG_EINVAL, "the adjoint does not cover Steel02 with an initial stress");
+    } else if (utype[u0] != XG_UNI_ELASTIC) {
+      return fail(XG_EINVAL, "the adjoint covers Steel02 and elastic fibers");
+    }
+    adj.elem_uni[e] = u0;
+  }
+  std::vector<int> dofs(obj->num_terms);
+  for (int k = 0; k < obj->num_terms; k++) {
+    auto it = std::lower_bound(node_tag.begin(), node_tag.end(), obj->node[k]);
+    if (it == node_tag.end() || *it != obj->node[k] || obj->dof[k] < 0 || obj->dof[k] >= ndf)
+      return fail(XG_EINVAL, "objective term %d: bad node or dof", k);
+    dofs[k] = (int)(it - node_tag.begin()) * ndf + obj->dof[k];
+  }
+  RET(xg_analysis_set_phase(this, ph));
+  cudaStream_t s = stream;
+  adj.N = N;
+  adj.K = K;
+  adj.nterm = obj->num_terms;
+  adj.nck = (N + K - 1) / K;
+  adj.len = adj_off_st() + (size_t)ne * frame_state_stride(fb_nip);
+  const size_t segslots = (size_t)std::min(K, N) + 1;
+  size_t free_b = 0, total_b = 0;
+  CK(cudaMemGetInfo(&free_b, &total_b));
+  const size_t need = ((size_t)adj.nck + 1 + segslots) * adj.len * sizeof(double);
+  if (need > free_b / 10 * 8)
+    return fail(XG_ENOMEM, "adjoint checkpoints need %.1f GB (fewer steps per checkpoint "
+                "lower it)", need * 1e-9);
+  RET(adj.ck.alloc(((size_t)adj.nck + 1) * adj.len));
+  RET(adj.seg.alloc(segslots * adj.len));
+  RET(adj.dof.upload(dofs.data(), std::max<size_t>(dofs.size(), 1), s));
+  std::vector<double> wv(obj->weight, obj->weight + obj->num_terms);
+  wv.resize(std::max<size_t>(wv.size(), 1));
+  RET(adj.w.upload(wv.data(), wv.size(), s));
+  RET(adj.d_elem_uni.upload(adj.elem_uni.data(), std::max<size_t>(adj.elem_uni.size(), 1), s));
+  RET(adj.J.alloc(1));
+  CK(cudaMemsetAsync(adj.J.p, 0, sizeof(double), s));
+  adj.ck_time.assign(adj.nck + 1, 0.0);
+  RET(adj_save(adj.ck.p));
+  adj.ck_time[0] = time_c;
+  for (int n = 1; n <= N; n++) {
+    RET(step(nullptr));
+    phase_steps_done++;
+    RET(launch_adj_objective(adj.nterm, adj.dof.p, adj.w.p, d_Uc.p, adj.J.p, s));
+    if (n % K == 0 && n < N) {
+      RET(adj_save(adj.ck.p + (size_t)(n / K) * adj.len));
+      adj.ck_time[n / K] = time_c;
+    }
+  }
+  RET(adj_save(adj.ck.p + (size_t)adj.nck * adj.len));
+  adj.ck_time[adj.nck] = time_c;
+  double Jh = 0.0;
+  CK(cudaMemcpyAsync(&Jh, adj.J.p, sizeof(double), cudaMemcpyDeviceToHost, s));
+  CK(cudaStreamSynchronize(s));
+  if (J) *J = Jh;
+  adj.have = true;
+  return 0;
+}
+
+// Reverse sweep: segment by segment from the last, the segment's steps are
+// run again from its checkpoint (the kernels are deterministic, so the
+// states repeat bit for bit) and swept backwards.  grad[u*3+k] = scale *
+// dJ/d uni_param[u][k], k = 0..2.  The model ends at the run's last state.
+int xg_model::adjoint_backward(double scale, double *grad, int num_uni) {
+  if (!adj.have) return fail(XG_ESTATE, "no adjoint run (xg_adjoint_forward first)");
+  if (!grad || num_uni != (int)utype.size()) return fail(XG_EINVAL, "bad gradient buffer");
+  cudaStream_t s = stream;
+  const size_t nu = (size_t)nn * ndf, nrec = (size_t)fb_nrec * 12;
+  const size_t ne1 = std::max(neq, 1);
+  for (auto *b : {&adj.Ub, &adj.Vb, &adj.Ab, &adj.mu, &adj.rhs, &adj.tmp, &adj.kmu}) {
+    RET(b->alloc(ne1));
+    CK(cudaMemsetAsync(b->p, 0, ne1 * sizeof(double), s));
+  }
+  RET(adj.hbar.alloc(std::max<size_t>(nrec, 1)));
+  CK(cudaMemsetAsync(adj.hbar.p, 0, std::max<size_t>(nrec, 1) * sizeof(double), s));
+  RET(adj.theta.alloc(std::max<size_t>((size_t)ne * 3, 1)));
+  CK(cudaMemsetAsync(adj.theta.p, 0, std::max<size_t>((size_t)ne * 3, 1) * sizeof(double), s));
+  RET(adj.scr.alloc(std::max<size_t>((size_t)ne * (6 + fb_nip * 4), 1)));
+  const double dt = phase.dt, gam = phase.gamma, bet = phase.beta;
+  NewmarkCoef c{};
+  c.c2 = gam / (bet * dt);
+  c.c3 = 1.0 / (bet * dt * dt);
+  c.a1 = 1.0 - gam / bet;
+  c.a2 = dt * (1.0 - 0.5 * gam / bet);
+  c.a3 = -1.0 / (bet * dt);
+  c.a4 = 1.0 - 0.5 / bet;
+  AdjView av{};
+  av.hbar = adj.hbar.p;
+  av.theta = adj.theta.p;
+  av.scr = adj.scr.p;
+  av.eqn = d_eqn.p;
+  av.mu = adj.mu.p;
+  av.bk0 = phase.beta_k_init_elem ? d_bk0_elem.p : nullptr;
+  av.bk0_all = phase.beta_k_init;
+  av.use_k0 = k0_ready ? 1 : 0;
+  av.elem_uni = adj.d_elem_uni.p;
+  const int N = adj.N, K = adj.K;
+  // the objective's last term
+  RET(launch_adj_objective_grad(adj.nterm, adj.dof.p, adj.w.p, d_eqn.p,
+                                adj.ck.p + (size_t)adj.nck * adj.len, adj.Ub.p, s));
+  const size_t nst = (size_t)ne * frame_state_stride(fb_nip);
+  for (int sg = adj.nck - 1; sg >= 0; sg--) {
+    const int n0 = sg * K, n1 = std::min(N, n0 + K);
+    const double *ckp = adj.ck.p + (size_t)sg * adj.len;
+    RET(adj_load(ckp, adj.ck_time[sg]));
+    CK(cudaMemcpyAsync(adj.seg.p, ckp, adj.len * sizeof(double), cudaMemcpyDeviceToDevice, s));
+    for (int n = n0 + 1; n <= n1; n++) {
+      RET(step_newmark(nullptr));
+      RET(adj_save(adj.seg.p + (size_t)(n - n0) * adj.len));
+    }
+    for (int n = n1; n > n0; n--) {
+      const double *Sj = adj.seg.p + (size_t)(n - n0) * adj.len;
+      const double *Sp = Sj - adj.len;
+      // effective tangent at the step's converged state (the committed
+      // element state after it), as the forward step forms it
+      CK(cudaMemcpyAsync(d_st.p, Sj + adj_off_st(), nst * sizeof(double),
+                         cudaMemcpyDeviceToDevice, s));
+      CK(cudaMemcpyAsync(d_U.p, Sj, nu * sizeof(double), cudaMemcpyDeviceToDevice, s));
+      FrameView fv = fview();
+      RET(launch_fbc_assemble(fv, s));
+      RET(launch_gather(gk, d_Ke.p, d_partial.p, d_vals.p, s));
+      RET(launch_dyn_tangent(dview(), d_vals.p, d_K0vals.p, 1.0, k0_ready ? c.c2 : 0.0, c.c2,
+                             c.c3, s));
+      blocks_factored = false;
+      prof_factored = false;
+      av.st = Sj + adj_off_st();
+      av.fh_prev = Sp + adj_off_fh();
+      av.Vn = Sj + nu;
+      RET(launch_adj_elem_a(fv, av, s));
+      RET(launch_gather(gr, d_Re.p, d_partial.p, adj.tmp.p, s));
+      RET(launch_adj_rhs(neq, adj.Ub.p, adj.Vb.p, adj.Ab.p, adj.tmp.p, c.c2, c.c3, adj.rhs.p, s));
+      RET(solve(adj.rhs.p, adj.mu.p, nullptr));
+      RET(launch_adj_elem_b(fv, av, s));
+      if (k0_ready) RET(launch_spmv(neq, d_rowptr.p, d_colidx.p, d_K0vals.p, adj.mu.p, adj.kmu.p, s));
+      RET(launch_adj_prev(neq, adj.mu.p, k0_ready ? adj.kmu.p : nullptr, d_meq.p, d_meq_am.p, c,
+                          adj.Ub.p, adj.Vb.p, adj.Ab.p, s));
+      if (n - 1 >= 1)
+        RET(launch_adj_objective_grad(adj.nterm, adj.dof.p, adj.w.p, d_eqn.p, Sp, adj.Ub.p, s));
+    }
+  }
+  // the fresh records' parameters
+  RET(launch_adj_init_records(fview(), av, s));
+  std::vector<double> th((size_t)ne * 3);
+  if (ne) CK(cudaMemcpyAsync(th.data(), adj.theta.p, th.size() * sizeof(double),
+                             cudaMemcpyDeviceToHost, s));
+  CK(cudaStreamSynchronize(s));
+  for (int k = 0; k < num_uni * 3; k++) grad[k] = 0.0;
+  for (int e = 0; e < ne; e++)
+    for (int k = 0; k < 3; k++) grad[(size_t)adj.elem_uni[e] * 3 + k] += scale * th[(size_t)e * 3 + k];
+  RET(adj_load(adj.ck.p + (size_t)adj.nck * adj.len, adj.ck_time[adj.nck]));
   return element_state(true);
 }
 
@@ -1905,7 +2143,33 @@ int xg_reset(xg_model *m) {
     m->lambda_const[p] = 0.0;
   }
   m->have_phase = false;
+  m->steps_since_reset = 0;
+  m->adj.have = false;
   return 0;
+}
+
+int xg_model_set_uniaxial_params(xg_model *m, const double *uni_param, int num_uni) {
+  if (!m || !uni_param) return fail(XG_EINVAL, "null argument");
+  if (!m->frames()) return fail(XG_EINVAL, "the model has no uniaxial materials");
+  if (num_uni != (int)m->utype.size())
+    return fail(XG_EINVAL, "%d materials given, the model has %zu", num_uni, m->utype.size());
+  m->uparam.assign(uni_param, uni_param + (size_t)num_uni * XG_UNI_NPARAM);
+  return xg_reset(m);
+}
+
+int xg_adjoint_forward(xg_model *m, const xg_phase_desc *ph, int num_steps, int ckpt_every,
+                       const xg_objective_desc *obj, double *J) {
+  if (!m) return fail(XG_EINVAL, "null model");
+  g_err.clear();
+  const int r = m->adjoint_forward(ph, num_steps, ckpt_every, obj, J);
+  if (r) m->adj.have = false;
+  return r;
+}
+
+int xg_adjoint_backward(xg_model *m, double scale, double *grad, int num_uni) {
+  if (!m) return fail(XG_EINVAL, "null model");
+  g_err.clear();
+  return m->adjoint_backward(scale, grad, num_uni);
 }
 
 }  // extern "C"

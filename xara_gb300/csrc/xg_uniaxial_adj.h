@@ -1,0 +1,202 @@
+// xg_uniaxial_adj.h -- reverse-mode derivatives of the uniaxial laws the
+// adjoint supports, for host and device.
+//
+// A law maps (trial strain, committed record, parameters) to the trial
+// record.  The vector-Jacobian product takes the adjoint of the trial
+// record's continuous fields and returns the adjoints of the strain, of the
+// committed record's fields and of the first three parameters.
+//
+// Record layout (12 doubles): 0 epsmin 1 epsmax 2 epspl 3 epss0 4 sigs0
+// 5 epsr 6 sigr 7 kon 8 e 9 sig 10 eps.  Field 7 (the loading branch) is
+// discrete and field 8 (the tangent) is read by no later step, so their
+// adjoints are not formed.
+#pragma once
+
+#include <float.h>
+#include <math.h>
+
+#ifdef __CUDACC__
+#define XG_HD __host__ __device__
+#else
+#define XG_HD
+#endif
+
+namespace xg {
+
+// Steel02::setTrialStrain (material/uniaxial/steel/Steel02.cpp:113-227),
+// primal recomputed with the same operations as the forward kernel (the
+// Menegotto-Pinto powers through log/exp, the isotropic shift through pow),
+// then swept backwards branch by branch.  Parameters q: Fy E0 b R0 cR1 cR2
+// a1 a2 a3 a4 sigini; qb receives d/d(Fy, E0, b).  sigini must be 0 (the
+// adjoint refuses models with an initial stress).
+XG_HD inline void steel02_vjp(const double *q, const double *hc, double strain, const double *yb,
+                              double *hb, double *sb, double *qb) {
+  const double Fy = q[0], E0 = q[1], b = q[2], R0 = q[3], cR1 = q[4], cR2 = q[5];
+  const double a1 = q[6], a2 = q[7], a3 = q[8], a4 = q[9];
+  const double Esh = b * E0, epsy = Fy / E0;
+  const double eps = strain;
+  const double epsP = hc[10], sigP = hc[9];
+  const double deps = eps - epsP;
+  double epsmax = hc[1], epsmin = hc[0], epspl = hc[2], epss0 = hc[3], sigs0 = hc[4];
+  double epsr = hc[5], sigr = hc[6];
+  int kon = (int)hc[7];
+  for (int k = 0; k < 12; k++) hb[k] = 0.0;
+  qb[0] = qb[1] = qb[2] = 0.0;
+  if ((kon == 0 || kon == 3) && fabs(deps) < 10.0 * DBL_EPSILON) {
+    // zero increment: the record passes through, the stress is sigini
+    for (int k = 0; k < 7; k++) hb[k] = yb[k];
+    *sb = yb[10];
+    return;
+  }
+  // ---- primal ----
+  int br = 0;            // 0 same branch, 1 first loading, 2 reversal 2->1, 3 reversal 1->2
+  bool first_neg = false, moved = false;
+  double d1 = 0.0, shft = 1.0;
+  if (kon == 0 || kon == 3) {
+    br = 1;
+    epsmax = epsy;
+    epsmin = -epsy;
+    if (deps < 0.0) { kon = 2; epss0 = epsmin; sigs0 = -Fy; epspl = epsmin; first_neg = true; }
+    else { kon = 1; epss0 = epsmax; sigs0 = Fy; epspl = epsmax; }
+  }
+  if (kon == 2 && deps > 0.0) {
+    br = 2;
+    kon = 1;
+    epsr = epsP;
+    sigr = sigP;
+    if (epsP < epsmin) { epsmin = epsP; moved = true; }
+    d1 = (epsmax - epsmin) / (2.0 * (a4 * epsy));
+    shft = 1.0 + a3 * pow(d1, 0.8);
+    epss0 = (Fy * shft - Esh * epsy * shft - sigr + E0 * epsr) / (E0 - Esh);
+    sigs0 = Fy * shft + Esh * (epss0 - epsy * shft);
+    epspl = epsmax;
+  } else if (kon == 1 && deps < 0.0) {
+    br = 3;
+    kon = 2;
+    epsr = epsP;
+    sigr = sigP;
+    if (epsP > epsmax) { epsmax = epsP; moved = true; }
+    d1 = (epsmax - epsmin) / (2.0 * (a2 * epsy));
+    shft = 1.0 + a1 * pow(d1, 0.8);
+    epss0 = (-Fy * shft + Esh * epsy * shft - sigr + E0 * epsr) / (E0 - Esh);
+    sigs0 = -Fy * shft + Esh * (epss0 + epsy * shft);
+    epspl = epsmin;
+  }
+  const double w = (epspl - epss0) / epsy;
+  const double xi = fabs(w);
+  const double R = R0 * (1.0 - (cR1 * xi) / (cR2 + xi));
+  const double den = epss0 - epsr;
+  const double rho = (eps - epsr) / den;
+  const double ae = fabs(rho);
+  const double lae = ae > 0.0 ? log(ae) : 0.0;
+  const double pr = ae > 0.0 ? exp(R * lae) : 0.0;
+  const double dum1 = 1.0 + pr;
+  const double ld1 = log(dum1);
+  const double dum2 = exp(ld1 / R);
+  const double sst = b * rho + (1.0 - b) * rho / dum2;
+  // ---- reverse ----
+  double b_epsmin = yb[0], b_epsmax = yb[1], b_epspl = yb[2], b_epss0 = yb[3];
+  double b_sigs0 = yb[4], b_epsr = yb[5], b_sigr = yb[6];
+  const double b_sig = yb[9];
+  double b_eps = yb[10];
+  double b_Fy = 0.0, b_E0 = 0.0, b_b = 0.0, b_epsy = 0.0, b_Esh = 0.0;
+  double b_epsP = 0.0, b_sigP = 0.0;
+  // sig = sst (sigs0 - sigr) + sigr
+  const double b_sst = b_sig * (sigs0 - sigr);
+  b_sigs0 += b_sig * sst;
+  b_sigr += b_sig * (1.0 - sst);
+  // sst = b rho + (1 - b) rho / dum2
+  double b_rho = b_sst * (b + (1.0 - b) / dum2);
+  b_b += b_sst * (rho - rho / dum2);
+  const double b_dum2 = -b_sst * (1.0 - b) * rho / (dum2 * dum2);
+  // dum2 = dum1^(1/R), dum1 = 1 + |rho|^R
+  const double b_dum1 = b_dum2 * dum2 / (R * dum1);
+  double b_R = -b_dum2 * dum2 * ld1 / (R * R);
+  if (ae > 0.0) {
+    b_rho += b_dum1 * R * pr / rho;
+    b_R += b_dum1 * pr * lae;
+  }
+  // rho = (eps - epsr) / (epss0 - epsr)
+  b_eps += b_rho / den;
+  b_epsr += b_rho * (rho - 1.0) / den;
+  b_epss0 -= b_rho * rho / den;
+  // R = R0 (1 - cR1 xi / (cR2 + xi)), xi = |epspl - epss0| / epsy
+  const double b_xi = -b_R * R0 * cR1 * cR2 / ((cR2 + xi) * (cR2 + xi));
+  const double b_w = w >= 0.0 ? b_xi : -b_xi;
+  b_epspl += b_w / epsy;
+  b_epss0 -= b_w / epsy;
+  b_epsy -= b_w * w / epsy;
+  if (br == 2 || br == 3) {
+    const double sg = br == 2 ? 1.0 : -1.0;       // +Fy branch (2->1) or -Fy (1->2)
+    const double aa = br == 2 ? a3 : a1, ad = br == 2 ? a4 : a2;
+    const double D = E0 - Esh;
+    // epspl = epsmax (2->1) or epsmin (1->2)
+    if (br == 2) b_epsmax += b_epspl; else b_epsmin += b_epspl;
+    // sigs0 = sg Fy shft + Esh (epss0 - sg epsy shft)
+    b_Fy += sg * b_sigs0 * shft;
+    double b_shft = b_sigs0 * (sg * Fy - sg * Esh * epsy);
+    b_Esh += b_sigs0 * (epss0 - sg * epsy * shft);
+    b_epss0 += b_sigs0 * Esh;
+    b_epsy -= sg * b_sigs0 * Esh * shft;
+    // epss0 = (sg Fy shft - sg Esh epsy shft - sigr + E0 epsr) / (E0 - Esh)
+    const double b_num = b_epss0 / D, b_D = -b_epss0 * epss0 / D;
+    b_Fy += sg * b_num * shft;
+    b_shft += b_num * (sg * Fy - sg * Esh * epsy);
+    b_Esh -= sg * b_num * epsy * shft;
+    b_epsy -= sg * b_num * Esh * shft;
+    b_sigr -= b_num;
+    b_E0 += b_num * epsr;
+    b_epsr += b_num * E0;
+    b_E0 += b_D;
+    b_Esh -= b_D;
+    // shft = 1 + aa d1^0.8, d1 = (epsmax - epsmin) / (2 ad epsy)
+    if (aa != 0.0 && d1 > 0.0) {
+      const double b_d1 = b_shft * aa * 0.8 * pow(d1, -0.2);
+      b_epsmax += b_d1 / (2.0 * ad * epsy);
+      b_epsmin -= b_d1 / (2.0 * ad * epsy);
+      b_epsy -= b_d1 * d1 / epsy;
+    }
+    // the extreme strain reached before the reversal
+    if (moved) {
+      if (br == 2) { b_epsP += b_epsmin; b_epsmin = 0.0; }
+      else { b_epsP += b_epsmax; b_epsmax = 0.0; }
+    }
+    // the reversal point is the last committed state
+    b_epsP += b_epsr;
+    b_sigP += b_sigr;
+    hb[0] = b_epsmin;
+    hb[1] = b_epsmax;
+  } else if (br == 1) {
+    // epsmax = epsy, epsmin = -epsy, epss0 = epspl = +-epsy, sigs0 = +-Fy
+    const double sg = first_neg ? -1.0 : 1.0;
+    b_epsy += b_epsmax - b_epsmin + sg * (b_epss0 + b_epspl);
+    b_Fy += sg * b_sigs0;
+    hb[5] = b_epsr;
+    hb[6] = b_sigr;
+  } else {
+    hb[0] = b_epsmin; hb[1] = b_epsmax; hb[2] = b_epspl; hb[3] = b_epss0;
+    hb[4] = b_sigs0; hb[5] = b_epsr; hb[6] = b_sigr;
+  }
+  hb[9] = b_sigP;
+  hb[10] = b_epsP;
+  *sb = b_eps;
+  // epsy = Fy / E0, Esh = b E0
+  b_Fy += b_epsy / E0;
+  b_E0 -= b_epsy * epsy / E0;
+  b_b += b_Esh * E0;
+  b_E0 += b_Esh * b;
+  qb[0] = b_Fy;
+  qb[1] = b_E0;
+  qb[2] = b_b;
+}
+
+// Elastic fiber: sig = E eps (parameter 0).
+XG_HD inline void elastic_vjp(const double *q, double strain, const double *yb, double *hb,
+                              double *sb, double *qb) {
+  for (int k = 0; k < 12; k++) hb[k] = 0.0;
+  *sb = q[0] * yb[9] + yb[10];
+  qb[0] = strain * yb[9];
+  qb[1] = qb[2] = 0.0;
+}
+
+}  // namespace xg

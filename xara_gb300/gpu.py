@@ -284,3 +284,57 @@ def profile_read(model):
         out[buf.value.decode()] = (ms.value, n.value)
         k += 1
     return out
+
+
+def set_uniaxial_params(model, uni_param):
+    """Replace the uniaxial parameters ([num_uni, XG_UNI_NPARAM]) and reset
+    the model to its initial state."""
+    q = np.ascontiguousarray(uni_param, np.float64).reshape(-1, _abi.XG_UNI_NPARAM)
+    L = lib()
+    L.xg_model_set_uniaxial_params.argtypes = [C.c_void_p, C.c_void_p, C.c_int]
+    _check(L.xg_model_set_uniaxial_params(model.h, _p(q), q.shape[0]))
+
+
+def adjoint_forward(model, phase, num_steps, ckpt_every, node, dof, weight):
+    """Newmark run of num_steps from the initial state with checkpoints every
+    ckpt_every steps; returns J = sum over steps and terms of
+    weight * u(node, dof)^2."""
+    L = lib()
+    L.xg_adjoint_forward.argtypes = [C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_void_p,
+                                     C.POINTER(C.c_double)]
+    node = np.ascontiguousarray(node, np.int32)
+    dof = np.ascontiguousarray(dof, np.int32)
+    weight = np.ascontiguousarray(weight, np.float64)
+    obj = _abi.xg_objective_desc(len(node), node.ctypes.data_as(C.POINTER(C.c_int)),
+                                 dof.ctypes.data_as(C.POINTER(C.c_int)),
+                                 weight.ctypes.data_as(C.POINTER(C.c_double)))
+    model._ps = phase.struct()
+    J = C.c_double()
+    _check(L.xg_adjoint_forward(model.h, C.byref(model._ps), int(num_steps), int(ckpt_every),
+                                C.byref(obj), C.byref(J)))
+    return J.value
+
+
+def adjoint_backward(model, scale=1.0):
+    """dJ/d(parameters 0..2) of every uniaxial material, [num_uni, 3]."""
+    L = lib()
+    L.xg_adjoint_backward.argtypes = [C.c_void_p, C.c_double, C.c_void_p, C.c_int]
+    nu = len(model.desc.uni_type)
+    g = np.zeros((nu, 3))
+    _check(L.xg_adjoint_backward(model.h, float(scale), _p(g), nu))
+    return g
+
+
+def uniaxial_vjp(kind, param, hc, strain, yb):
+    """Host vector-Jacobian product of one material point's trial record:
+    (adjoint of the committed record [12], of the strain, of parameters 0-2)."""
+    L = lib()
+    L.xg_uniaxial_vjp.argtypes = [C.c_int, C.c_void_p, C.c_void_p, C.c_double, C.c_void_p,
+                                  C.c_void_p, C.POINTER(C.c_double), C.c_void_p]
+    q = np.ascontiguousarray(param, np.float64)
+    hc = np.ascontiguousarray(hc, np.float64)
+    yb = np.ascontiguousarray(yb, np.float64)
+    hb, qb, sb = np.zeros(12), np.zeros(3), C.c_double()
+    _check(L.xg_uniaxial_vjp(int(kind), _p(q), _p(hc), float(strain), _p(yb), _p(hb),
+                             C.byref(sb), _p(qb)))
+    return hb, sb.value, qb
