@@ -27,8 +27,14 @@ in one device model; a step is one Newmark time step of every frame (its
 Newton iterations, each frame converging on its own).  Metric: frame time
 steps/s, beside the same kernels run one frame per model.
 
-  python bench.py [--workload frame3d|brick|batch] [--gpus N] [--steps K] [--warmup W]
-                  [--impl xara|reference]
+Workload `adjoint`: gradients of the summed squared roof drift of 64 such
+frames (one Steel02 material per member) over 2,000 Newmark steps with
+respect to every member's Fy, E0 and b, checkpoints every 100 steps.
+Metric: reverse-sweep time / forward-run time (lower is better), with a
+central finite-difference check of one directional derivative.
+
+  python bench.py [--workload frame3d|brick|batch|adjoint] [--gpus N] [--steps K]
+                  [--warmup W] [--impl xara|reference]
 
 --impl reference times the reference algorithm's CPU path (the C oracle, a
 restatement of the reference's classes compiled on this host) on every host
@@ -692,6 +698,143 @@ def run_reference_batch(args):
 
 
 # ---------------------------------------------------------------------------
+# adjoint: gradients of a transient response (64 frames, 2,000 steps)
+# ---------------------------------------------------------------------------
+def run_adjoint(args):
+    world, rank, local, torch, dist = dist_setup()
+    from xara_gb300 import configs, gpu
+    from xara_gb300.adjoint import frame_response
+    N, K = args.adj_steps, args.ckpt_every
+    desc, phases = configs.adjoint_frames(n_frames=args.adj_frames, steps=N, seed=0)
+    ph = phases[0]
+    obj = (desc.meta["obj_node"], desc.meta["obj_dof"], desc.meta["obj_weight"])
+    q0 = desc.uni_param.reshape(-1, 12).copy()
+    m = gpu.DeviceModel(desc)
+    m.set_system(gpu.XG_SYSTEM_PROFILE_SPD)
+    stream = torch.cuda.ExternalStream(gpu.model_stream(m))
+
+    def barrier():
+        if world > 1:
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    def timed(fn):
+        ev0 = torch.cuda.Event(enable_timing=True)
+        ev1 = torch.cuda.Event(enable_timing=True)
+        barrier()
+        ev0.record(stream)
+        out = fn()
+        ev1.record(stream)
+        barrier()
+        return out, max_over_ranks(ev0.elapsed_time(ev1) * 1e-3, world, torch, dist)
+
+    # warm-up: a short run forward and backward
+    w = min(N, 10 * args.warmup)
+    gpu.adjoint_forward(m, ph, w, max(1, w // 3), *obj)
+    gpu.adjoint_backward(m)
+    # the plain forward run (xg_analyze)
+    m.reset()
+    m.set_phase(ph)
+    sampler = ClockSampler(local if world == 1 else 0)
+    sampler.start()
+    gpu.profile_enable(m, True)
+    stats, t_fwd = timed(lambda: m.analyze(N))
+    prof = gpu.profile_read(m)
+    gpu.profile_enable(m, False)
+    # the same run with checkpoints, then the reverse sweep
+    m.reset()
+    J, t_fwd_ck = timed(lambda: gpu.adjoint_forward(m, ph, N, K, *obj))
+    g, t_bwd = timed(lambda: gpu.adjoint_backward(m))
+    clocks = sampler.stop()
+    # end to end through the autograd function: parameters from and the
+    # gradient to host memory
+    theta = torch.tensor(q0[:, :3], dtype=torch.float64, requires_grad=True)
+    barrier()
+    t0 = time.perf_counter()
+    Jt = frame_response(theta, m, ph, N, K, obj)
+    Jt.backward()
+    barrier()
+    t_e2e = max_over_ranks(time.perf_counter() - t0, world, torch, dist)
+    # central finite differences (h = 1e-6 relative) of one directional
+    # derivative, frame by frame: every frame's objective term against the
+    # adjoint restricted to its members.  The hysteretic response is only
+    # piecewise smooth (a fiber's load reversal can move by a step under a
+    # perturbation), so a few frames' difference quotients do not converge
+    # in h; the check reports how many frames agree.
+    nf = args.adj_frames
+    efr = desc.meta["member_frame"]
+    rng = np.random.default_rng(1)
+    d = rng.normal(size=q0[:, :3].shape) * np.abs(q0[:, :3])
+    h = 1e-6
+    Jt = {}
+    for sgn in (1, -1):
+        q = q0.copy()
+        q[:, :3] += sgn * h * d
+        gpu.set_uniaxial_params(m, q)
+        gpu.adjoint_forward(m, ph, N, K, *obj)
+        Jt[sgn] = gpu.adjoint_objective_terms(m, nf)
+    fd_f = (Jt[1] - Jt[-1]) / (2 * h)
+    ad_f = np.array([(g[efr == f] * d[efr == f]).sum() for f in range(nf)])
+    rel = np.abs(ad_f - fd_f) / np.maximum(np.abs(fd_f), 1e-300)
+    ad, fd = float(ad_f.sum()), float(fd_f.sum())
+    m.close()
+    if rank != 0:
+        dist.destroy_process_group()
+        return 0
+    kernels = {k: v for k, v in prof.items() if v[1] > 0 and k != "return_map_cap_hits"}
+    newton = sum(s_[0] for s_ in stats)
+    line = {
+        "metric": "adjoint/forward time", "value": t_bwd / t_fwd, "unit": "ratio",
+        "n_gpus": world, "steps": N, "warmup": w, "ms_per_step": 1e3 * t_bwd / N,
+        "higher_is_better": False, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic (seeded frames and Kanai-Tajimi records)",
+        "config": {"workload": f"gradient of the summed squared roof drift of {args.adj_frames} "
+                               f"2D steel frames over {N} Newmark steps (BASELINE config 4) "
+                               f"w.r.t. every member's Steel02 Fy, E0, b",
+                   "frames": args.adj_frames, "members": int(desc.num_elems),
+                   "parameters": int(3 * desc.num_elems), "checkpoint_every": K,
+                   "system": "ProfileSPD (a band per frame)",
+                   "parallelism": f"replicas x{world}"},
+        "forward_s": t_fwd, "forward_with_checkpoints_s": t_fwd_ck, "reverse_sweep_s": t_bwd,
+        "gradient_over_forward": (t_fwd_ck + t_bwd) / t_fwd,
+        "newton_iters_per_step": newton / N,
+        "J": J,
+        "fd_check": {"h": h, "frames": nf,
+                     "median_relative_difference": float(np.median(rel)),
+                     "frames_within_1e-6": int((rel < 1e-6).sum()),
+                     "frames_within_1e-3": int((rel < 1e-3).sum()),
+                     "directional_adjoint_all_frames": ad, "central_fd_all_frames": fd},
+        "e2e": {"value": t_e2e / t_fwd, "unit": "ratio (autograd forward+backward / forward)",
+                "seconds": t_e2e, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0,
+                "path": "xara_gb300.adjoint.frame_response(theta on the host) then backward()"},
+        "gpu_launches": int(sum(v[1] for v in kernels.values())),
+        "kernels_ms_forward": {k: v[0] for k, v in kernels.items()},
+        "clocks": clocks,
+    }
+    if not args.no_cpu_baseline:
+        _, _, parts = configs.frame_batch(2, steps=60, seed=0, return_parts=True)
+        rate, sample = batch_cpu_sample(parts, 0, 50)
+        line["cpu_baseline"] = {
+            "value": rate, "unit": "frame time steps/s (forward)", "cores": 1, "kind": "port",
+            "sample": sample + "; the reference has no Steel02 sensitivity, so a CPU gradient "
+                      f"by central differences costs {2 * 3 * int(desc.num_elems)} forward runs"}
+    print(json.dumps(line))
+    if world > 1:
+        dist.destroy_process_group()
+    return 0
+
+
+def run_reference_adjoint(args):
+    if int(os.environ.get("RANK", "0")) != 0:
+        return 0
+    print(json.dumps({"impl": "reference", "unavailable":
+                      "the reference has no Steel02 stress sensitivity (its DDM, "
+                      "computeGradients, covers Steel01/Concrete01), so it has no gradient "
+                      "path for this workload; its CPU forward is timed by --workload batch"}))
+    return 0
+
+
+# ---------------------------------------------------------------------------
 # brick: the element phase of the stdBrick J2 block
 # ---------------------------------------------------------------------------
 def brick_trial_field(desc, nx, ny, nz, eps=2.5e-3):
@@ -888,7 +1031,8 @@ def run_brick(args):
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--workload", default="frame3d", choices=["frame3d", "brick", "batch"])
+    ap.add_argument("--workload", default="frame3d",
+                    choices=["frame3d", "brick", "batch", "adjoint"])
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
@@ -900,12 +1044,17 @@ def main():
     ap.add_argument("--frames", type=int, default=BATCH_FRAMES)
     ap.add_argument("--batch-lead", type=int, default=150)
     ap.add_argument("--e2e-steps", type=int, default=3)
+    ap.add_argument("--adj-frames", type=int, default=64)
+    ap.add_argument("--adj-steps", type=int, default=2000)
+    ap.add_argument("--ckpt-every", type=int, default=100)
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     if args.impl == "reference":
         return {"frame3d": run_reference_frame, "brick": run_reference_brick,
-                "batch": run_reference_batch}[args.workload](args)
-    return {"frame3d": run_frame, "brick": run_brick, "batch": run_batch}[args.workload](args)
+                "batch": run_reference_batch,
+                "adjoint": run_reference_adjoint}[args.workload](args)
+    return {"frame3d": run_frame, "brick": run_brick, "batch": run_batch,
+            "adjoint": run_adjoint}[args.workload](args)
 
 
 if __name__ == "__main__":

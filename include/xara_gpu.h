@@ -245,7 +245,10 @@ int xg_elemset_revert(xg_model *m);             /* revertToLastCommit      */
 int xg_elemset_revert_to_start(xg_model *m);    /* revertToStart           */
 
 /* Committed material history, SoA, for checkpoints and tests.
-   which = 0: J2 plastic strain (ncomp x nip) + xi; 1: fiber uniaxial state.
+   which = 0: J2 plastic strain (ncomp x nip) + xi.  Force-based frames:
+   1 = fiber records, 12 doubles per fiber and section in element order
+   (Steel02: epsmin epsmax epspl epss0 sigs0 epsr sigr kon e sig eps),
+   2 = element states (Se, kv, section deformations, flexibilities, forces).
    Writes at most cap doubles, returns the count written (or < 0). */
 int xg_elemset_get_history(const xg_model *m, int which, double *out, long cap);
 int xg_elemset_set_history(xg_model *m, int which, const double *in, long n);
@@ -353,6 +356,9 @@ int xg_model_set_uniaxial_params(xg_model *m, const double *uni_param, int num_u
    the committed state every ckpt_every steps, and return J. */
 int xg_adjoint_forward(xg_model *m, const xg_phase_desc *ph, int num_steps, int ckpt_every,
                        const xg_objective_desc *obj, double *J);
+/* The last run's objective term by term (J_k summed over the steps; J is
+   their sum in term order). */
+int xg_adjoint_objective_terms(const xg_model *m, double *Jk, int num_terms);
 /* Reverse sweep of the last xg_adjoint_forward: each segment between
    checkpoints is run again and swept backwards.  grad[u*3 + k] = scale *
    dJ/d uni_param[u][k], k = 0, 1, 2, for the num_uni materials.  The model

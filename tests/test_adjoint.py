@@ -124,9 +124,10 @@ def test_steel02_vjp_zero_increment_and_elastic():
 # ---------------------------------------------------------------------------
 # GPU: gradients of a transient run
 # ---------------------------------------------------------------------------
-def _adjoint_model(n_frames=2, steps=40, seed=5):
+def _adjoint_model(n_frames=2, steps=40, seed=5, pga_scale=1.0):
     """Small frames of the batched-frames workload, one Steel02 per member."""
-    desc, phases = configs.adjoint_frames(n_frames=n_frames, steps=steps, seed=seed)
+    desc, phases = configs.adjoint_frames(n_frames=n_frames, steps=steps, seed=seed,
+                                          pga_scale=pga_scale)
     return desc, phases[0]
 
 
@@ -135,16 +136,22 @@ def _objective(desc):
 
 
 @pytest.mark.gpu
-def test_adjoint_gradient_matches_finite_differences(need_gpu):
+@pytest.mark.parametrize("pga_scale,steps", [(1.0, 40), (6.0, 120)])
+def test_adjoint_gradient_matches_finite_differences(need_gpu, pga_scale, steps):
     gpu = _gpu()
-    desc, ph = _adjoint_model()
+    desc, ph = _adjoint_model(steps=steps, pga_scale=pga_scale)
     node, dof, w = _objective(desc)
-    steps = ph.num_steps
     q0 = desc.uni_param.reshape(-1, 12).copy()
     with gpu.DeviceModel(desc) as m:
         J0 = gpu.adjoint_forward(m, ph, steps, 10, node, dof, w)
+        rec = m.fiber_records()
         g = gpu.adjoint_backward(m)
         assert J0 > 0 and np.isfinite(g).all()
+        if pga_scale > 1.0:
+            # the strong case runs through yielding and load reversals
+            ey = q0[0, 0] / q0[0, 1]
+            assert (np.abs(rec[:, 10]) > ey).mean() > 0.01
+            assert (rec[:, 5] != 0.0).mean() > 0.05
 
         def J(q):
             gpu.set_uniaxial_params(m, q)

@@ -601,7 +601,10 @@ def adjoint_frames(n_frames=64, steps=2000, dt=0.01, seed=0, nfib=40, member_cov
         obj_w.append(1.0 / (top * top))
     if pga_scale != 1.0:
         ph.gm_accel = np.ascontiguousarray(ph.gm_accel * pga_scale)
+    node_idx = {int(t): i for i, t in enumerate(tags)}
+    member_frame = rec[[node_idx[int(n_)] for n_ in a["elem_conn"].reshape(-1, 2)[:, 0]]]
     out.meta = dict(desc.meta, workload=f"{n_frames} 2D steel frames, one Steel02 per member",
+                    member_frame=np.asarray(member_frame),
                     obj_node=np.asarray(obj_node, np.int32),
                     obj_dof=np.zeros(n_frames, np.int32), obj_weight=np.asarray(obj_w),
                     members=ne)

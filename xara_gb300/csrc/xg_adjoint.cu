@@ -384,13 +384,11 @@ __global__ void k_adj_init_records(FrameView v, AdjView a) {
   }
 }
 
-// J += sum_k w_k U[dof_k]^2 (one thread, term order)
+// J_k += w_k U[dof_k]^2, one accumulator per term
 __global__ void k_adj_objective(int nterm, const int *dof, const double *w, const double *U,
                                 double *J) {
-  if (blockIdx.x != 0 || threadIdx.x != 0) return;
-  double s = 0.0;
-  for (int k = 0; k < nterm; k++) s += w[k] * U[dof[k]] * U[dof[k]];
-  *J += s;
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k < nterm) J[k] += w[k] * U[dof[k]] * U[dof[k]];
 }
 
 // Ubar[eqn[dof_k]] += 2 w_k U[dof_k] (one thread, term order)
@@ -450,7 +448,7 @@ int launch_adj_init_records(const FrameView &v, const AdjView &a, cudaStream_t s
 int launch_adj_objective(int nterm, const int *dof, const double *w, const double *U, double *J,
                          cudaStream_t s) {
   if (nterm == 0) return 0;
-  k_adj_objective<<<1, 32, 0, s>>>(nterm, dof, w, U, J);
+  k_adj_objective<<<grid_of(nterm, 128), 128, 0, s>>>(nterm, dof, w, U, J);
   return cudaGetLastError() == cudaSuccess ? 0 : XG_ECUDA;
 }
 

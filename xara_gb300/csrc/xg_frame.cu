@@ -423,6 +423,99 @@ __device__ __forceinline__ void fbc_section(const FrameView &v, int f0, int nf, 
   }
 }
 
+// Sum over the G lanes of a section's lane group (a fixed tree: the lane of
+// rank r adds the rank r+o of its group, o = P2/2 .. 1, P2 the power of two
+// at or above G), the result broadcast from the group's first lane.
+__device__ __forceinline__ double group_sum(double v, int rank, int G, int P2) {
+  for (int o = P2 >> 1; o > 0; o >>= 1) {
+    const double t = __shfl_down_sync(0xffffffffu, v, o);
+    if (rank + o < G) v += t;
+  }
+  return __shfl_sync(0xffffffffu, v, (int)(threadIdx.x & 31) - rank);
+}
+
+// fbc_section for one section per lane group: the lane of rank r takes the
+// section's fibers r, r+G, ...; lanes outside every group (on = false) take
+// none and write nothing.
+template <int ORD>
+__device__ __forceinline__ void fbc_section_group(const FrameView &v, int f0, int nf, double ybar,
+                                                  double zbar, double GJ, long rec0, int rank,
+                                                  int G, int P2, bool on, const double *vsec,
+                                                  double *ks, double *Ssr) {
+  double k0 = 0, k1 = 0, k2 = 0, k5 = 0, k6 = 0, k10 = 0, s0 = 0, s1 = 0, s2 = 0;
+  for (int fi = rank; on && fi < nf; fi += G) {
+    const int kf = f0 + fi;
+    const double y = v.fy[kf] - ybar, A = v.fA[kf];
+    const int u = v.fmat[kf];
+    double strain = vsec[0] - y * vsec[1];
+    double z = 0.0;
+    if (ORD == 4) {
+      z = v.fz[kf] - zbar;
+      strain += z * vsec[2];
+    }
+    const double *hc = v.fh_c + rec0 + 12L * fi;
+    double *ht = v.fh_t + rec0 + 12L * fi;
+    const double *q = v.uparam + (long)u * XG_UNI_NPARAM;
+    const int type = v.utype[u];
+    double stress, tangent;
+    if (type == XG_UNI_STEEL02) {
+      double hcl[11], htl[11];
+#pragma unroll
+      for (int c = 0; c < 11; c++) hcl[c] = c == 8 ? 0.0 : hc[c];
+      steel02_trial(q, hcl, strain, htl);
+#pragma unroll
+      for (int c = 0; c < 11; c++) ht[c] = htl[c];
+      stress = htl[9];
+      tangent = htl[8];
+    } else if (type == XG_UNI_CONCRETE02) {
+      double hcl[11], htl[11];
+      hcl[0] = hc[0]; hcl[1] = hc[1]; hcl[9] = hc[9]; hcl[10] = hc[10];
+      if (fabs(strain - hcl[10]) < kDblEps) {
+        // Concrete02.cpp:182-183: the previous trial stress and tangent stay
+        ht[0] = hcl[0]; ht[1] = hcl[1]; ht[10] = strain;
+        stress = ht[9];
+        tangent = ht[8];
+      } else {
+        concrete02_trial(q, hcl, strain, htl);
+        ht[0] = htl[0]; ht[1] = htl[1]; ht[8] = htl[8]; ht[9] = htl[9]; ht[10] = htl[10];
+        stress = htl[9];
+        tangent = htl[8];
+      }
+    } else {
+      stress = q[0] * strain;
+      tangent = q[0];
+      ht[8] = tangent; ht[9] = stress; ht[10] = strain;
+    }
+    if (ORD == 2) {
+      const double ks0 = tangent * A, ks1 = ks0 * -y;
+      k0 += ks0; k1 += ks1; k5 += ks1 * -y;
+      const double fs0v = stress * A;
+      s0 += fs0v; s1 += fs0v * -y;
+    } else {
+      const double EA = tangent * A;
+      k0 += EA; k1 += -y * EA; k2 += z * EA;
+      k5 += y * y * EA; k10 += z * z * EA; k6 += -y * z * EA;
+      const double fsv = stress * A;
+      s0 += fsv; s1 += -y * fsv; s2 += z * fsv;
+    }
+  }
+  k0 = group_sum(k0, rank, G, P2); k1 = group_sum(k1, rank, G, P2);
+  k5 = group_sum(k5, rank, G, P2);
+  s0 = group_sum(s0, rank, G, P2); s1 = group_sum(s1, rank, G, P2);
+  if (ORD == 2) {
+    ks[0] = k0; ks[1] = k1; ks[2] = k1; ks[3] = k5;
+    Ssr[0] = s0; Ssr[1] = s1;
+  } else {
+    k2 = group_sum(k2, rank, G, P2); k6 = group_sum(k6, rank, G, P2);
+    k10 = group_sum(k10, rank, G, P2); s2 = group_sum(s2, rank, G, P2);
+    ks[0] = k0; ks[1] = k1; ks[2] = k2; ks[3] = 0.0;
+    ks[4] = k1; ks[5] = k5; ks[6] = k6; ks[7] = 0.0;
+    ks[8] = k2; ks[9] = k6; ks[10] = k10; ks[11] = 0.0;
+    ks[12] = 0.0; ks[13] = 0.0; ks[14] = 0.0; ks[15] = GJ;
+    Ssr[0] = s0; Ssr[1] = s1; Ssr[2] = s2; Ssr[3] = GJ * vsec[3];
+  }
+}
+
 constexpr int kFbcWarps = 4;
 constexpr int kMaxIp = 10;
 constexpr int kFbcMaxRounds = 4096;
@@ -477,6 +570,12 @@ __global__ void __launch_bounds__(32 * WARPS) k_fbc_update(FrameView v) {
   }
   __syncwarp();
 
+  // lane groups: sec_G lanes per section, section sec_ip, rank sec_rank
+  const int sec_G = 32 / nip;
+  int sec_P2 = 1;
+  while (sec_P2 < sec_G) sec_P2 <<= 1;
+  const int sec_ip = lane / sec_G, sec_rank = lane % sec_G;
+  const bool sec_on = sec_ip < nip;
   const int maxSub = NB == 3 ? 4 : 10;
   int numSub = 1;
   bool converged = false;
@@ -514,7 +613,10 @@ __global__ void __launch_bounds__(32 * WARPS) k_fbc_update(FrameView v) {
         for (int i = 0; i < NB * NB; i++) f[i] = 0.0;
 #pragma unroll
         for (int i = 0; i < NB; i++) vr[i] = 0.0;
-        for (int ip = 0; ip < nip; ip++) {
+        {
+          // every section at once, one lane group each (lanes past the
+          // last group mirror the last section and write nothing)
+          const int ip = sec_on ? sec_ip : nip - 1;
           const double xL = v.xi[ip], xL1 = xL - 1.0, wtL = v.wt[ip] * L;
           // Ss = b SeT (codes P MZ [MY T])
           double Ss[ORD], dSs[ORD], dvs[ORD];
@@ -538,18 +640,22 @@ __global__ void __launch_bounds__(32 * WARPS) k_fbc_update(FrameView v) {
 #pragma unroll
           for (int r = 0; r < ORD; r++) vsec[r] = S.vsS[ip][r] + (init != 0 ? dvs[r] : 0.0);
           double ks[ORD * ORD], Ssr[ORD];
-          fbc_section<ORD>(v, f0, nf, ybar, zbar, GJ, (fbase + (long)ip * nf) * 12, lane, vsec,
-                           ks, Ssr);
+          fbc_section_group<ORD>(v, f0, nf, ybar, zbar, GJ, (fbase + (long)ip * nf) * 12,
+                                 sec_rank, sec_G, sec_P2, sec_on, vsec, ks, Ssr);
           double fsec[ORD * ORD];
           sec_inverse<ORD>(ks, fsec);
+          __syncwarp();
+          if (sec_on && sec_rank == 0) {
 #pragma unroll
-          for (int r = 0; r < ORD; r++) {
-            S.vsS[ip][r] = vsec[r];
-            S.SsrS[ip][r] = Ssr[r];
-            dSs[r] = Ss[r] - Ssr[r];
+            for (int r = 0; r < ORD; r++) {
+              S.vsS[ip][r] = vsec[r];
+              S.SsrS[ip][r] = Ssr[r];
+            }
+#pragma unroll
+            for (int r = 0; r < ORD * ORD; r++) S.fsS[ip][r] = fsec[r];
           }
 #pragma unroll
-          for (int r = 0; r < ORD * ORD; r++) S.fsS[ip][r] = fsec[r];
+          for (int r = 0; r < ORD; r++) dSs[r] = Ss[r] - Ssr[r];
 #pragma unroll
           for (int r = 0; r < ORD; r++) {
             double t = 0.0;
@@ -560,15 +666,24 @@ __global__ void __launch_bounds__(32 * WARPS) k_fbc_update(FrameView v) {
           // f += b' fs b wL ; vr += b' (vs + dvs) wL.  Each column a of the
           // force interpolation b has one entry: row kRow[a], value ca[a]
           // (ForceBeamColumn3d::getForceInterpolatMatrix, :1068-1110).
+          // the sections' terms summed in section order from their groups'
+          // first lanes
           constexpr int kRow[6] = {0, 1, 1, 2, 2, 3};
           const double ca[6] = {1.0, xL1, xL, xL1, xL, 1.0};
+          double fc[NB * NB], vc[NB];
 #pragma unroll
           for (int a = 0; a < NB; a++) {
             const double wa = ca[a] * wtL;
 #pragma unroll
-            for (int c = 0; c < NB; c++)
-              f[a * NB + c] += wa * (fsec[kRow[a] * ORD + kRow[c]] * ca[c]);
-            vr[a] += wa * dvs[kRow[a]];
+            for (int c = 0; c < NB; c++) fc[a * NB + c] = wa * (fsec[kRow[a] * ORD + kRow[c]] * ca[c]);
+            vc[a] = wa * dvs[kRow[a]];
+          }
+          for (int g = 0; g < nip; g++) {
+            const int src = g * sec_G;
+#pragma unroll
+            for (int i = 0; i < NB * NB; i++) f[i] += __shfl_sync(0xffffffffu, fc[i], src);
+#pragma unroll
+            for (int i = 0; i < NB; i++) vr[i] += __shfl_sync(0xffffffffu, vc[i], src);
           }
         }
         double kvT[NB * NB];

@@ -121,14 +121,20 @@ struct BandSystem {
   double *invD;            // [neq]
   int *flags;              // [4]
   double min_diag_tol;
+  int bmax, nmax;          // widest band and largest part (launch shapes)
 };
 // Widths and offsets of the parts' bands; XG_EINVAL when a part couples to
 // another or is wider than the kernel's staging.
 int band_plan(int neq, const int *rowptr, const int *colidx, const std::vector<int> &cstart,
               std::vector<int> &bw, std::vector<long> &boff);
-int band_factor(const BandSystem &S, cudaStream_t s, int *bad_eq);
+// Factor every part; with nrhs > 0 (at most 4) the right-hand sides x[r*ldx
+// + eq] are carried through the forward substitution and the diagonal
+// scaling on the way (band_solve(forward = false) completes them).
+int band_factor(const BandSystem &S, cudaStream_t s, int *bad_eq, int nrhs = 0,
+                double *x = nullptr, int ldx = 0);
 // x[r*ldx + i] right-hand side r in, solution out (equation numbering)
-int band_solve(const BandSystem &S, int nrhs, double *x, int ldx, cudaStream_t s);
+int band_solve(const BandSystem &S, int nrhs, double *x, int ldx, cudaStream_t s,
+               bool forward = true);
 
 // small device helpers (xg_kernels.cu)
 int launch_axpy(int n, double a, const double *x, double *y, cudaStream_t s);

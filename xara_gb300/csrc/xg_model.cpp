@@ -204,7 +204,7 @@ struct xg_model {
     bool have = false;
     int N = 0, K = 0, nterm = 0, nck = 0;
     size_t len = 0;                        // doubles in one saved state
-    std::vector<double> ck_time;
+    std::vector<double> ck_time, Jk;        // checkpoint times; the objective's terms
     std::vector<int> elem_uni;
     DBuf<int> dof, d_elem_uni;
     DBuf<double> w, J, ck, seg, Ub, Vb, Ab, hbar, theta, scr, mu, rhs, tmp, kmu;
@@ -1129,6 +1129,10 @@ int xg_model::ensure_profile() {
         bsys.band = d_band.p; bsys.rowptr = d_rowptr.p; bsys.colidx = d_colidx.p;
         bsys.vals = d_vals.p; bsys.invD = d_invD.p; bsys.flags = d_pflags.p;
         bsys.min_diag_tol = 1.0e-12;   // ProfileSPDLinDirectSolver.h:49 default
+        bsys.bmax = *std::max_element(bw.begin(), bw.end());
+        bsys.nmax = 0;
+        for (int c = 0; c < ncomp; c++)
+          bsys.nmax = std::max(bsys.nmax, comp_start[c + 1] - comp_start[c]);
         prof_band = true;
         prof_ready = true;
         return 0;
@@ -1174,10 +1178,38 @@ int xg_model::ensure_profile() {
 // Factor once per tangent, then solve nrhs systems sharing the factors.
 int xg_model::solve_profile(int nrhs, const double *const *b, double *const *x) {
   RET(ensure_profile());
+  if (prof_band) {
+    // the band factorisation carries the right-hand sides through the
+    // forward substitution
+    for (int r = 0; r < nrhs; r++)
+      CK(cudaMemcpyAsync(d_px.p + (size_t)r * prof_ldx, b[r], (size_t)neq * sizeof(double),
+                         cudaMemcpyDeviceToDevice, stream));
+    const bool fused = !prof_factored;
+    if (fused) {
+      prof_begin(P_LDL_FACTOR);
+      int bad = -1;
+      const int r = band_factor(bsys, stream, &bad, nrhs, d_px.p, prof_ldx);
+      prof_end(P_LDL_FACTOR, 1);
+      if (r) {
+        if (bad >= 0) return fail(XG_ESOLVE, "ProfileSPD: pivot %d fails the check (aii == 0, "
+                                  "|aii| <= 1e-12, or a first pivot <= 0)", bad);
+        return fail(r, "ProfileSPD: band factorisation failed");
+      }
+      prof_factored = true;
+    }
+    prof_begin(P_LDL_SOLVE);
+    RET(band_solve(bsys, nrhs, d_px.p, prof_ldx, stream, !fused));
+    prof_end(P_LDL_SOLVE, fused ? 1 : 2);
+    for (int r = 0; r < nrhs; r++)
+      CK(cudaMemcpyAsync(x[r], d_px.p + (size_t)r * prof_ldx, (size_t)neq * sizeof(double),
+                         cudaMemcpyDeviceToDevice, stream));
+    prof_flush();
+    return 0;
+  }
   if (!prof_factored) {
     prof_begin(P_LDL_FACTOR);
     int bad = -1;
-    const int r = prof_band ? band_factor(bsys, stream, &bad) : profile_factor(psys, stream, &bad);
+    const int r = profile_factor(psys, stream, &bad);
     prof_end(P_LDL_FACTOR, 2);
     if (r) {
       if (bad >= 0) return fail(XG_ESOLVE, "ProfileSPD: pivot %d fails the check (aii == 0, "
@@ -1190,8 +1222,7 @@ int xg_model::solve_profile(int nrhs, const double *const *b, double *const *x) 
     CK(cudaMemcpyAsync(d_px.p + (size_t)r * prof_ldx, b[r], (size_t)neq * sizeof(double),
                        cudaMemcpyDeviceToDevice, stream));
   prof_begin(P_LDL_SOLVE);
-  RET(prof_band ? band_solve(bsys, nrhs, d_px.p, prof_ldx, stream)
-                : profile_solve(psys, nrhs, d_px.p, prof_ldx, stream));
+  RET(profile_solve(psys, nrhs, d_px.p, prof_ldx, stream));
   prof_end(P_LDL_SOLVE, 1);
   for (int r = 0; r < nrhs; r++)
     CK(cudaMemcpyAsync(x[r], d_px.p + (size_t)r * prof_ldx, (size_t)neq * sizeof(double),
@@ -1528,8 +1559,8 @@ int xg_model::adjoint_forward(const xg_phase_desc *ph, int N, int K, const xg_ob
   wv.resize(std::max<size_t>(wv.size(), 1));
   RET(adj.w.upload(wv.data(), wv.size(), s));
   RET(adj.d_elem_uni.upload(adj.elem_uni.data(), std::max<size_t>(adj.elem_uni.size(), 1), s));
-  RET(adj.J.alloc(1));
-  CK(cudaMemsetAsync(adj.J.p, 0, sizeof(double), s));
+  RET(adj.J.alloc(std::max(adj.nterm, 1)));
+  CK(cudaMemsetAsync(adj.J.p, 0, std::max(adj.nterm, 1) * sizeof(double), s));
   adj.ck_time.assign(adj.nck + 1, 0.0);
   RET(adj_save(adj.ck.p));
   adj.ck_time[0] = time_c;
@@ -1544,9 +1575,12 @@ int xg_model::adjoint_forward(const xg_phase_desc *ph, int N, int K, const xg_ob
   }
   RET(adj_save(adj.ck.p + (size_t)adj.nck * adj.len));
   adj.ck_time[adj.nck] = time_c;
-  double Jh = 0.0;
-  CK(cudaMemcpyAsync(&Jh, adj.J.p, sizeof(double), cudaMemcpyDeviceToHost, s));
+  adj.Jk.assign(std::max(adj.nterm, 1), 0.0);
+  CK(cudaMemcpyAsync(adj.Jk.data(), adj.J.p, adj.Jk.size() * sizeof(double),
+                     cudaMemcpyDeviceToHost, s));
   CK(cudaStreamSynchronize(s));
+  double Jh = 0.0;
+  for (int k = 0; k < adj.nterm; k++) Jh += adj.Jk[k];
   if (J) *J = Jh;
   adj.have = true;
   return 0;
@@ -1979,7 +2013,17 @@ int xg_elemset_revert_to_start(xg_model *m) { return xg_reset(m); }
 
 int xg_elemset_get_history(const xg_model *m, int which, double *out, long cap) {
   if (!m || !out) return fail(XG_EINVAL, "null argument");
-  if (which != 0) return fail(XG_EINVAL, "history kind %d not held by this model", which);
+  if (m->frames() && (which == 1 || which == 2)) {
+    // committed fiber records [nrec*12] or committed element states
+    const long need = which == 1 ? m->fb_nrec * 12 : (long)m->ne * frame_state_stride(m->fb_nip);
+    if (cap < need) return fail(XG_EINVAL, "history needs %ld doubles", need);
+    CK(cudaMemcpyAsync(out, which == 1 ? m->d_fh_c.p : m->d_st_c.p, need * sizeof(double),
+                       cudaMemcpyDeviceToHost, m->stream));
+    CK(cudaStreamSynchronize(m->stream));
+    return (int)std::min<long>(need, 0x7fffffff);
+  }
+  if (which != 0 || m->frames())
+    return fail(XG_EINVAL, "history kind %d not held by this model", which);
   const long np = m->npts(), nh = m->nhist();
   const long need = np * (nh + 1);
   if (cap < need) return fail(XG_EINVAL, "history needs %ld doubles", need);
@@ -2164,6 +2208,14 @@ int xg_adjoint_forward(xg_model *m, const xg_phase_desc *ph, int num_steps, int 
   const int r = m->adjoint_forward(ph, num_steps, ckpt_every, obj, J);
   if (r) m->adj.have = false;
   return r;
+}
+
+int xg_adjoint_objective_terms(const xg_model *m, double *Jk, int num_terms) {
+  if (!m || !Jk) return fail(XG_EINVAL, "null argument");
+  if (!m->adj.have) return fail(XG_ESTATE, "no adjoint run (xg_adjoint_forward first)");
+  if (num_terms != m->adj.nterm) return fail(XG_EINVAL, "the run has %d terms", m->adj.nterm);
+  for (int k = 0; k < num_terms; k++) Jk[k] = m->adj.Jk[k];
+  return 0;
 }
 
 int xg_adjoint_backward(xg_model *m, double scale, double *grad, int num_uni) {

@@ -175,6 +175,14 @@ class DeviceModel:
         del r
         return buf
 
+    def fiber_records(self):
+        """Committed fiber records of a frame model, [fibers x sections, 12]."""
+        nf = np.diff(np.asarray(self.desc.sec_fiber_start))[np.asarray(self.desc.elem_mat)]
+        n = int(nf.sum()) * self.desc.fbc_num_ip * 12
+        buf = np.zeros(max(n, 1))
+        _check(lib().xg_elemset_get_history(self.h, 1, _p(buf), n))
+        return buf[:n].reshape(-1, 12)
+
     def set_history(self, buf):
         buf = np.ascontiguousarray(buf, np.float64)
         _check(lib().xg_elemset_set_history(self.h, 0, _p(buf), buf.size))
@@ -313,6 +321,15 @@ def adjoint_forward(model, phase, num_steps, ckpt_every, node, dof, weight):
     _check(L.xg_adjoint_forward(model.h, C.byref(model._ps), int(num_steps), int(ckpt_every),
                                 C.byref(obj), C.byref(J)))
     return J.value
+
+
+def adjoint_objective_terms(model, num_terms):
+    """The last adjoint run's objective, term by term."""
+    L = lib()
+    L.xg_adjoint_objective_terms.argtypes = [C.c_void_p, C.c_void_p, C.c_int]
+    Jk = np.zeros(num_terms)
+    _check(L.xg_adjoint_objective_terms(model.h, _p(Jk), int(num_terms)))
+    return Jk
 
 
 def adjoint_backward(model, scale=1.0):
