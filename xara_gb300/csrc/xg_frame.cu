@@ -24,33 +24,41 @@ constexpr double kDblEps = 2.220446049250313e-16;
 // ---------------------------------------------------------------------------
 // uniaxial laws on a 12-double record:
 //   Steel02: 0 epsmin 1 epsmax 2 epspl 3 epss0 4 sigs0 5 epsr 6 sigr 7 kon
+//            11 R of the current branch
 //   Concrete02: 0 ecmin 1 dept;  all: 8 e 9 sig 10 eps
 // ---------------------------------------------------------------------------
 
-// Steel02::setTrialStrain (material/uniaxial/steel/Steel02.cpp:113-227)
+// Steel02::setTrialStrain (material/uniaxial/steel/Steel02.cpp:113-227).
+// Record slot 11 keeps R, which changes only where the branch does (the
+// reference recomputes the same value every call); q[11] holds Fy/E0 (the
+// model's device parameter table).  The Menegotto-Pinto powers go through
+// log/exp and 1/(epss0 - epsr), 1/dum2 are formed once: the stress and
+// tangent differ from the reference's expression order by a few ulps.
 __device__ void steel02_trial(const double *q, const double *hc, double trialStrain,
                               double *ht) {
   const double Fy = q[0], E0 = q[1], b = q[2], R0 = q[3], cR1 = q[4], cR2 = q[5];
   const double a1 = q[6], a2 = q[7], a3 = q[8], a4 = q[9], sigini = q[10];
-  const double Esh = b * E0, epsy = Fy / E0;
+  const double Esh = b * E0, epsy = q[11];
   double eps = trialStrain;
   if (sigini != 0.0) eps = trialStrain + sigini / E0;
   const double epsP = hc[10], sigP = hc[9];
   const double deps = eps - epsP;
   double epsmax = hc[1], epsmin = hc[0], epspl = hc[2], epss0 = hc[3], sigs0 = hc[4];
-  double epsr = hc[5], sigr = hc[6];
+  double epsr = hc[5], sigr = hc[6], R = hc[11];
   int kon = (int)hc[7];
+  bool newR = false;
   ht[10] = eps;
   if (kon == 0 || kon == 3) {
     if (fabs(deps) < 10.0 * kDblEps) {
       ht[0] = epsmin; ht[1] = epsmax; ht[2] = epspl; ht[3] = epss0; ht[4] = sigs0;
-      ht[5] = epsr; ht[6] = sigr; ht[7] = 3.0; ht[8] = E0; ht[9] = sigini;
+      ht[5] = epsr; ht[6] = sigr; ht[7] = 3.0; ht[8] = E0; ht[9] = sigini; ht[11] = R;
       return;
     }
     epsmax = epsy;
     epsmin = -epsy;
     if (deps < 0.0) { kon = 2; epss0 = epsmin; sigs0 = -Fy; epspl = epsmin; }
     else { kon = 1; epss0 = epsmax; sigs0 = Fy; epspl = epsmax; }
+    newR = true;
   }
   if (kon == 2 && deps > 0.0) {
     kon = 1;
@@ -62,6 +70,7 @@ __device__ void steel02_trial(const double *q, const double *hc, double trialStr
     epss0 = (Fy * shft - Esh * epsy * shft - sigr + E0 * epsr) / (E0 - Esh);
     sigs0 = Fy * shft + Esh * (epss0 - epsy * shft);
     epspl = epsmax;
+    newR = true;
   } else if (kon == 1 && deps < 0.0) {
     kon = 2;
     epsr = epsP;
@@ -72,24 +81,26 @@ __device__ void steel02_trial(const double *q, const double *hc, double trialStr
     epss0 = (-Fy * shft + Esh * epsy * shft - sigr + E0 * epsr) / (E0 - Esh);
     sigs0 = -Fy * shft + Esh * (epss0 + epsy * shft);
     epspl = epsmin;
+    newR = true;
   }
-  const double xi = fabs((epspl - epss0) / epsy);
-  const double R = R0 * (1.0 - (cR1 * xi) / (cR2 + xi));
-  const double epsrat = (eps - epsr) / (epss0 - epsr);
-  // |e*|^R and (1 + |e*|^R)^(1/R) through one log and two exps (pow costs
-  // about twice as much in FP64, and every Steel02 fiber takes this path in
-  // every compatibility iteration); the results differ from pow by a few
-  // ulps times |R log|e*||
+  if (newR) {
+    const double xi = fabs((epspl - epss0) / epsy);
+    R = R0 * (1.0 - (cR1 * xi) / (cR2 + xi));
+  }
+  const double rden = 1.0 / (epss0 - epsr);
+  const double epsrat = (eps - epsr) * rden;
+  // |e*|^R and 1 / (1 + |e*|^R)^(1/R) through logs and exps
   const double ae = fabs(epsrat);
   const double pr = ae > 0.0 ? exp(R * log(ae)) : 0.0;
   const double dum1 = 1.0 + pr;
-  const double dum2 = exp(log(dum1) / R);
-  double sig = b * epsrat + (1.0 - b) * epsrat / dum2;
-  sig = sig * (sigs0 - sigr) + sigr;
-  double e = b + (1.0 - b) / (dum1 * dum2);
-  e = e * (sigs0 - sigr) / (epss0 - epsr);
+  const double rdum2 = exp(-log(dum1) / R);
+  const double dsig = sigs0 - sigr;
+  double sig = b * epsrat + (1.0 - b) * epsrat * rdum2;
+  sig = sig * dsig + sigr;
+  double e = b + (1.0 - b) * rdum2 / dum1;
+  e = e * dsig * rden;
   ht[0] = epsmin; ht[1] = epsmax; ht[2] = epspl; ht[3] = epss0; ht[4] = sigs0;
-  ht[5] = epsr; ht[6] = sigr; ht[7] = (double)kon; ht[8] = e; ht[9] = sig;
+  ht[5] = epsr; ht[6] = sigr; ht[7] = (double)kon; ht[8] = e; ht[9] = sig; ht[11] = R;
 }
 
 struct C02 {
@@ -368,12 +379,12 @@ __device__ __forceinline__ void fbc_section(const FrameView &v, int f0, int nf, 
     const int type = v.utype[u];
     double stress, tangent;
     if (type == XG_UNI_STEEL02) {
-      double hcl[11], htl[11];
+      double hcl[12], htl[12];
 #pragma unroll
-      for (int c = 0; c < 11; c++) hcl[c] = c == 8 ? 0.0 : hc[c];
+      for (int c = 0; c < 12; c++) hcl[c] = c == 8 ? 0.0 : hc[c];
       steel02_trial(q, hcl, strain, htl);
 #pragma unroll
-      for (int c = 0; c < 11; c++) ht[c] = htl[c];
+      for (int c = 0; c < 12; c++) ht[c] = htl[c];
       stress = htl[9];
       tangent = htl[8];
     } else if (type == XG_UNI_CONCRETE02) {
@@ -459,12 +470,12 @@ __device__ __forceinline__ void fbc_section_group(const FrameView &v, int f0, in
     const int type = v.utype[u];
     double stress, tangent;
     if (type == XG_UNI_STEEL02) {
-      double hcl[11], htl[11];
+      double hcl[12], htl[12];
 #pragma unroll
-      for (int c = 0; c < 11; c++) hcl[c] = c == 8 ? 0.0 : hc[c];
+      for (int c = 0; c < 12; c++) hcl[c] = c == 8 ? 0.0 : hc[c];
       steel02_trial(q, hcl, strain, htl);
 #pragma unroll
-      for (int c = 0; c < 11; c++) ht[c] = htl[c];
+      for (int c = 0; c < 12; c++) ht[c] = htl[c];
       stress = htl[9];
       tangent = htl[8];
     } else if (type == XG_UNI_CONCRETE02) {
