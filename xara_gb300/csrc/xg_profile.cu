@@ -14,15 +14,20 @@
 //   B  every tile below it becomes W_IJ = A_IJ L_JJ^-T (kept in a scratch
 //      slot) and L_IJ = W_IJ D^-1 (stored in place);
 //   C  every trailing tile pair loses W_IJ L_KJ' (one 32^3 product each).
-// The tasks (A: diagonal, B: panel tile, C: tile pair of one column) run as
-// a dataflow: one persistent launch whose blocks take tasks from a list in a
-// fixed order -- for column J: A(J), B(., J), the C tasks of column J-1 that
-// reach columns J+1 and beyond, then the C tasks of column J that reach
-// column J+1 -- and wait (bounded by the global timer) on per-tile counters
-// for the tasks each one depends on.  Every dependency sits earlier in the
-// list, so the look-ahead is built in: column J+1's diagonal and panels run
-// while the rest of column J's trailing update is still going.  C recovers
-// W_IJ as L_IJ D_J.  Pivot checks follow the reference: the first pivot must
+// The tasks (A: diagonal, B: panel tile in four row parts, C: tile pair of
+// one column, and the chain task of column J: C for the pair (J+1, J+1)
+// and A(J+1) in one block's shared memory -- the critical path of the
+// factorisation) run as a dataflow: one persistent launch whose blocks take
+// tasks from a list in a fixed order -- for column J: A(J) when no column
+// updates it, the C tasks of column J-1 that reach column J+1, the panel
+// (J+1, J), the chain task, the other panels B(., J), the C tasks of column
+// J that reach column J+1, then the rest of column J-1's trailing update --
+// and
+// wait (bounded by the global timer) on per-tile counters for the tasks
+// each one depends on.  Every dependency sits earlier in the list, so the
+// look-ahead is built in: column J+1's diagonal and panels run while the
+// rest of column J's trailing update is still going.  C recovers W_IJ as
+// L_IJ D_J.  Pivot checks follow the reference: the first pivot must
 // be positive, later ones only non-zero and above minDiagTol in magnitude.
 //
 // The substitutions stream the tiles through one block: every step reads
@@ -97,78 +102,109 @@ __global__ void k_prof_fill(ProfileSystem S) {
 // next pivot takes its reciprocal at once (__drcp_rn: the correctly rounded
 // 1/d, the value of the reference's 1.0/aii), so the chain of dependent
 // FP64 operations per column stays short.
-// 1/d for the elimination: an FP32 seed refined by two Newton steps in FP64
-// (four dependent FMAs, against about six for a correctly rounded FP64
-// reciprocal, whose FP64 latency sets the pace of the pivot chain); the
-// stored reciprocal pivots are the correctly rounded ones.
+// 1/d for the elimination (three dependent FMAs after the estimate, against
+// about six for a correctly rounded FP64 reciprocal, whose FP64 latency
+// sets the pace of the pivot chain); the stored reciprocal pivots are the
+// correctly rounded ones.
 __device__ __forceinline__ double elim_rcp(double d) {
   const double ad = fabs(d);
   if (!(ad > 1e-30 && ad < 1e30)) return __drcp_rn(d);
-  double x = (double)__frcp_rn((float)d);
-  double e = fma(-d, x, 1.0);
-  x = fma(x, e, x);
-  e = fma(-d, x, 1.0);
-  return fma(x, e, x);
+  // hardware FP64 reciprocal estimate, then one cubic Newton step
+  // x (1 + e + e^2), e = 1 - d x, which triples its correct bits
+  double x;
+  asm("rcp.approx.ftz.f64 %0, %1;" : "=d"(x) : "d"(d));
+  const double e = fma(-d, x, 1.0);
+  return fma(x, fma(e, e, e), x);
 }
 
-__device__ bool factor_diag(const ProfileSystem &S, int J, double (*sA)[kT + 1], double *col,
+__device__ bool factor_tile(const ProfileSystem &S, int J, double (*sA)[kT + 1],
                             volatile int *flags) {
   double *g = tile_at(S, J, 0);
-  __shared__ double colbuf[2][kT], lcol[kT], sinv[kT + 1];
-  (void)col;
-  for (int k = threadIdx.x; k < kTT; k += blockDim.x) sA[k >> 5][k & 31] = __ldcg(g + k);
+  __shared__ double colbuf[2][kT], lcol[kT], sinv[kT + 1], pivv;
+  const int tid = threadIdx.x;
+  // this thread's entries of the trailing triangles (row-major, relative to
+  // the pivot's successor; at most 31 x 32 / 2 = 496 of them), fixed for
+  // every column; entry 0 -- the next pivot -- is thread kT's.  Warps 1 and
+  // 5 share the sub-partition of the pivot chain (thread kT's scaling, FMA
+  // and reciprocal), so they take no trailing entries: every warp-wide FP64
+  // instruction occupies its sub-partition's pipe for the same time, and
+  // the chain's sub-partition sets the pace of the column.
+  const int warp = tid >> 5;
+  const bool trailing = warp != 1 && warp != 5;
+  const int tw = trailing ? (warp - (warp > 1) - (warp > 5)) * 32 + (tid & 31) : -1;
+  const int ntw = ((int)blockDim.x / 32 - 2) * 32;         // 192 trailing threads
+  int ent[3];
+#pragma unroll
+  for (int u = 0; u < 3; u++) {
+    const int k = tw + u * ntw;
+    ent[u] = (trailing && k < 496) ? kLowerRS[k] : -1;
+  }
+  if (tid < kT) colbuf[0][tid] = sA[tid][0];
+  if (tid == 0) sinv[0] = elim_rcp(sA[0][0]);
   __syncthreads();
-  if (threadIdx.x < kT) colbuf[0][threadIdx.x] = sA[threadIdx.x][0];
-  if (threadIdx.x == 0) sinv[0] = elim_rcp(sA[0][0]);
-  __syncthreads();
-  // Column c: warp 0 scales the column below the pivot (l = a / d), then the
-  // trailing triangle (rows and columns c+1..31, packed densely over the
-  // threads through the lower-triangle table) takes one FMA per entry; the
-  // threads that finish column c+1 hand it, and its pivot's reciprocal, to
-  // the next column through a second buffer.
+  // Column c: the threads below the pivot scale the column (l = a / d)
+  // while thread kT applies it to the next pivot and takes that pivot's
+  // reciprocal, which runs alongside the rest of the trailing triangle (one
+  // FMA per entry); the threads that finish column c+1's entries hand them
+  // to the next column through a second buffer.
   for (int c = 0; c < kT - 1; c++) {
     const double *cl = colbuf[c & 1];
     double *cn = colbuf[(c + 1) & 1];
-    if (threadIdx.x < kT && threadIdx.x > c) {
-      const double l = cl[threadIdx.x] * sinv[c];
-      lcol[threadIdx.x] = l;
-      sA[threadIdx.x][c] = l;
+    const double inv = sinv[c];
+    if (tid < kT && tid > c) {
+      const double l = cl[tid] * inv;
+      lcol[tid] = l;
+      sA[tid][c] = l;
+    } else if (tid == kT) {
+      const double l1 = cl[c + 1] * inv;
+      pivv = fma(-l1, cl[c + 1], sA[c + 1][c + 1]);
+      sA[c + 1][c + 1] = pivv;
     }
     __syncthreads();
-    const int m = kT - 1 - c, tri = m * (m + 1) / 2;
-    for (int k = threadIdx.x; k < tri; k += blockDim.x) {
-      const int rs = kLowerRS[k];
-      const int r = c + 1 + (rs >> 5), s = c + 1 + (rs & 31);
-      const double v = fma(-lcol[r], cl[s], sA[r][s]);
-      sA[r][s] = v;
-      if (s == c + 1) {
-        cn[r] = v;
-        if (r == s) sinv[c + 1] = elim_rcp(v);
+    const int m = kT - 1 - c;
+#pragma unroll
+    for (int u = 0; u < 3; u++) {
+      const int e = ent[u];
+      const int ti = e >> 5, tk = e & 31;
+      if (e > 0 && ti < m) {
+        const int r = c + 1 + ti, sc = c + 1 + tk;
+        const double v = fma(-lcol[r], cl[sc], sA[r][sc]);
+        sA[r][sc] = v;
+        if (tk == 0) cn[r] = v;
       }
     }
+    if (tid == kT) sinv[c + 1] = elim_rcp(pivv);
     __syncthreads();
   }
-  if (threadIdx.x < kT) sinv[threadIdx.x] = __drcp_rn(sA[threadIdx.x][threadIdx.x]);
+  if (tid < kT) sinv[tid] = __drcp_rn(sA[tid][tid]);
   __syncwarp();
-  if (threadIdx.x < kT) {
-    const int eq = J * kT + threadIdx.x;
-    const double d = sA[threadIdx.x][threadIdx.x];
-    S.invD[eq] = sinv[threadIdx.x];
+  if (tid < kT) {
+    const int eq = J * kT + tid;
+    const double d = sA[tid][tid];
+    S.invD[eq] = sinv[tid];
     S.piv[eq] = d;
     // ProfileSPDLinDirectSolver.cpp:134-138 (first pivot), :189-199; the
     // first failing pivot of the tile is reported
     const bool fail = eq < S.n && ((eq == 0) ? !(d > 0.0)
                                              : (d == 0.0 || fabs(d) <= S.min_diag_tol));
     const unsigned bad = __ballot_sync(0xffffffffu, fail);
-    if (bad && threadIdx.x == 0) {
+    if (bad && tid == 0) {
       flags[1] = J * kT + __ffs(bad) - 1;
       __threadfence();
       flags[0] = 3;
     }
   }
-  for (int k = threadIdx.x; k < kTT; k += blockDim.x) g[k] = sA[k >> 5][k & 31];
+  for (int k = tid; k < kTT; k += blockDim.x) g[k] = sA[k >> 5][k & 31];
   __syncthreads();
   return flags[0] != 3;
+}
+
+__device__ bool factor_diag(const ProfileSystem &S, int J, double (*sA)[kT + 1],
+                            volatile int *flags) {
+  const double *g = tile_at(S, J, 0);
+  for (int k = threadIdx.x; k < kTT; k += blockDim.x) sA[k >> 5][k & 31] = __ldcg(g + k);
+  __syncthreads();
+  return factor_tile(S, J, sA, flags);
 }
 
 // Phase B on rows 8q..8q+7 of tile (I = J+o, J): W = A L_JJ^-T, L = W
@@ -232,6 +268,44 @@ __device__ void pair_update(const ProfileSystem &S, int J, int a, int b, double 
   __syncthreads();
 }
 
+__device__ __forceinline__ int slot_of(const ProfileSystem &S, int I, int o) {
+  return I * (S.W + 1) + o;
+}
+
+// Column J's critical chain in one block, in shared memory: once the four
+// row parts of panel (J+1, J) are done (phase B on four other SMs), the
+// last update of diagonal tile J+1 (phase C for the pair (J+1, J+1)) and
+// that tile's LDL'.
+__device__ bool chain_task(const ProfileSystem &S, int J, double (*sA)[kT + 1],
+                           double (*sB)[kT + 1], double (*sC)[kT + 1], volatile int *flags) {
+  const int I = J + 1, tid = threadIdx.x;
+  const double *gp = tile_at(S, I, 1);
+  const double *gd = tile_at(S, I, 0);
+  const double *piv = S.piv + (size_t)J * kT;
+  for (int k = tid; k < kTT; k += blockDim.x) {
+    const double l = __ldcg(gp + k);
+    sB[k >> 5][k & 31] = l;
+    sA[k >> 5][k & 31] = l * __ldcg(piv + (k & 31));
+    sC[k >> 5][k & 31] = __ldcg(gd + k);
+  }
+  __syncthreads();
+  // diagonal tile J+1 loses (L D) L' (its lower triangle)
+  for (int k = tid; k < kT * (kT + 1) / 2; k += blockDim.x) {
+    const int rs = kLowerRS[k], r = rs >> 5, sc = rs & 31;
+    double a0 = 0.0, a1 = 0.0, a2 = 0.0, a3 = 0.0;
+#pragma unroll
+    for (int c = 0; c < kT; c += 4) {
+      a0 = fma(sA[r][c], sB[sc][c], a0);
+      a1 = fma(sA[r][c + 1], sB[sc][c + 1], a1);
+      a2 = fma(sA[r][c + 2], sB[sc][c + 2], a2);
+      a3 = fma(sA[r][c + 3], sB[sc][c + 3], a3);
+    }
+    sC[r][sc] -= (a0 + a1) + (a2 + a3);
+  }
+  __syncthreads();
+  return factor_tile(S, I, sC, flags);
+}
+
 // Wait until *p >= target (thread 0 of a block); false on a raised error
 // flag or after kBarrierTimeoutNs (flags[0] = 2).
 __device__ bool wait_geq(const int *p, int target, volatile int *flags) {
@@ -249,10 +323,6 @@ __device__ bool wait_geq(const int *p, int target, volatile int *flags) {
   return true;
 }
 
-__device__ __forceinline__ int slot_of(const ProfileSystem &S, int I, int o) {
-  return I * (S.W + 1) + o;
-}
-
 // Dependencies of a task: every update of its tile from earlier columns
 // (the count of columns J' < J both tile rows reach), and the diagonal /
 // panel tiles it reads.
@@ -260,6 +330,9 @@ __device__ bool wait_task(const ProfileSystem &S, int4 t, volatile int *flags) {
   const int type = t.x, I = t.y, K = t.z, J = t.w;
   if (type == 0)
     return wait_geq(S.upd + slot_of(S, J, 0), J - S.ftile[J], flags);
+  if (type == 4)
+    return wait_geq(S.done + slot_of(S, I, 1), kPanelParts, flags) &&
+           wait_geq(S.upd + slot_of(S, I, 0), J - S.ftile[I], flags);
   if (type == 1)
     return wait_geq(S.done + slot_of(S, J, 0), 1, flags) &&
            wait_geq(S.upd + slot_of(S, I, I - J), J - max(S.ftile[I], S.ftile[J]), flags);
@@ -269,8 +342,7 @@ __device__ bool wait_task(const ProfileSystem &S, int4 t, volatile int *flags) {
 }
 
 __global__ void __launch_bounds__(kFactorThreads) k_prof_factor(ProfileSystem S) {
-  __shared__ double sA[kT][kT + 1], sB[kT][kT + 1];
-  __shared__ double col[kT];
+  __shared__ double sA[kT][kT + 1], sB[kT][kT + 1], sC[kT][kT + 1];
   __shared__ int task, ok;
   volatile int *flags = S.flags;
   while (true) {
@@ -285,21 +357,20 @@ __global__ void __launch_bounds__(kFactorThreads) k_prof_factor(ProfileSystem S)
     const int4 t = S.tasks[task];
     bool fine = true;
     if (t.x == 0) {
-      fine = factor_diag(S, t.w, sA, col, flags);
+      fine = factor_diag(S, t.w, sA, flags);
     } else if (t.x == 1) {
       panel_solve(S, t.w, t.y - t.w, t.z, sA, sB);
-    } else {
+    } else if (t.x == 2) {
       pair_update(S, t.w, t.y - t.w, t.z - t.w, sA, sB);
-      // type 3: the last update of diagonal tile J+1, factored at once
-      if (t.x == 3) fine = factor_diag(S, t.y, sA, col, flags);
+    } else {
+      fine = chain_task(S, t.w, sA, sB, sC, flags);
     }
     if (!fine) break;
     __syncthreads();
     if (threadIdx.x == 0) {
       __threadfence();
       if (t.x >= 2) atomicAdd(S.upd + slot_of(S, t.y, t.y - t.z), 1);
-      if (t.x == 3) atomicExch(S.done + slot_of(S, t.y, 0), 1);
-      if (t.x == 0) atomicExch(S.done + slot_of(S, t.y, 0), 1);
+      if (t.x == 0 || t.x == 4) atomicExch(S.done + slot_of(S, t.y, 0), 1);
       if (t.x == 1) atomicAdd(S.done + slot_of(S, t.y, t.y - t.w), 1);
     }
     __syncthreads();
@@ -557,25 +628,30 @@ void profile_tasks(int nt, int W, const std::vector<int> &ftile, std::vector<int
   };
   // the updates of column J (0 <= J < nt) whose target column is J+b for b
   // in [blo, bhi]
+  // (the pair (J+1, J+1) of column J belongs to column J's chain task)
   auto updates = [&](int J, int blo, int bhi) {
     if (J < 0) return;
     const int omax = std::min(W, nt - 1 - J);
     for (int b = blo; b <= std::min(bhi, omax); b++) {
       if (ftile[J + b] > J) continue;
       for (int a = b; a <= omax; a++)
-        if (ftile[J + a] <= J) emit(a == 1 && b == 1 ? 3 : 2, J + a, J + b, J);
+        if (ftile[J + a] <= J && !(a == 1 && b == 1)) emit(2, J + a, J + b, J);
     }
   };
-  // Column J: its panels, then what column J+1 still lacks (the updates of
-  // columns J-1 and J that reach it, the diagonal's fused one included),
-  // then the rest of column J-1's trailing update.
+  // Column J: the updates of column J-1 that reach column J+1 (the
+  // diagonal's included), the chain task (panel (J+1, J), the last update
+  // and the LDL' of diagonal tile J+1), the other panels, column J's
+  // updates of column J+1, then the rest of column J-1's trailing update.
   for (int J = 0; J < nt; J++) {
     if (ftile[J] == J) emit(0, J, J, J);   // no column updates this tile
+    updates(J - 1, 2, 2);
     const int omax = std::min(W, nt - 1 - J);
-    for (int o = 1; o <= omax; o++)
+    if (omax >= 1 && ftile[J + 1] <= J)
+      for (int q = 0; q < kPanelParts; q++) emit(1, J + 1, q, J);
+    if (J + 1 < nt && ftile[J + 1] <= J) emit(4, J + 1, J + 1, J);
+    for (int o = 2; o <= omax; o++)
       if (ftile[J + o] <= J)
         for (int q = 0; q < kPanelParts; q++) emit(1, J + o, q, J);
-    updates(J - 1, 2, 2);
     updates(J, 1, 1);
     updates(J - 1, 3, W);
   }
