@@ -317,6 +317,18 @@ int xg_analysis_autotune(xg_model *m, int what);
 int xg_autotune_result(const xg_model *m, int *elem_warps, int *pcg_rows_per_block,
                        int *pending);
 
+/* Newmark steps as CUDA graphs (no counterpart in the reference): with
+   enable = 1, a transient step of a model made of several parts (a batch of
+   frames, per-part band LDL') whose external loads are constant runs as one
+   graph launch -- the predictor, then a conditional loop whose body is one
+   Newton iteration ending in a device-side per-part convergence check --
+   and the host reads the outcome once per step.  Other steps, and steps
+   while per-kernel timing or the autotuner is active, keep the host-driven
+   loop; results are the same bit for bit.  xg_analysis_graph_steps counts
+   the steps that ran as graphs. */
+int xg_analysis_set_graph(xg_model *m, int enable);
+int xg_analysis_graph_steps(const xg_model *m, long *steps);
+
 /* The CUDA stream (a cudaStream_t) every kernel of the model runs on, for
    callers that time or order their own work against it. */
 int xg_model_stream(const xg_model *m, void **stream);

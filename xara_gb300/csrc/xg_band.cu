@@ -389,7 +389,7 @@ int band_plan(int neq, const int *rowptr, const int *colidx, const std::vector<i
   return 0;
 }
 
-int band_factor(const BandSystem &S, cudaStream_t s, int *bad_eq, int nrhs, double *x, int ldx) {
+int band_factor_async(const BandSystem &S, cudaStream_t s, int nrhs, double *x, int ldx) {
   if (S.ncomp == 0) return 0;
   if (nrhs < 0 || nrhs > kBandMaxRhs) return XG_EINVAL;
   if (cudaMemsetAsync(S.flags, 0, 4 * sizeof(int), s) != cudaSuccess) return XG_ECUDA;
@@ -408,6 +408,13 @@ int band_factor(const BandSystem &S, cudaStream_t s, int *bad_eq, int nrhs, doub
     default: return XG_EINVAL;
   }
   if (err || cudaGetLastError() != cudaSuccess) return XG_ECUDA;
+  return 0;
+}
+
+int band_factor(const BandSystem &S, cudaStream_t s, int *bad_eq, int nrhs, double *x, int ldx) {
+  if (S.ncomp == 0) return 0;
+  const int r = band_factor_async(S, s, nrhs, x, ldx);
+  if (r) return r;
   int hflags[4];
   if (cudaMemcpyAsync(hflags, S.flags, sizeof hflags, cudaMemcpyDeviceToHost, s) != cudaSuccess)
     return XG_ECUDA;

@@ -8,6 +8,8 @@
 // frames in one system) converge one by one.
 #include <cuda_runtime.h>
 
+#include <algorithm>
+
 #include "xg_internal.h"
 
 namespace xg {
@@ -71,10 +73,11 @@ __global__ void k_spmv(int n, const int *rowptr, const int *colidx, const double
 // -m (a + alphaM v) - m ag(t) on the excited direction.  The equation's
 // (node, dof) list is in node order, so the sum is deterministic.
 __global__ void k_dyn_unbalance(DynView d, const double *fext, const double *pint,
-                                const double *k0v, double bk0, double am, double t,
-                                double *B) {
+                                const double *k0v, double bk0, double am, double t_arg,
+                                const double *t_dev, double *B) {
   const int e = blockIdx.x * blockDim.x + threadIdx.x;
   if (e >= d.neq) return;
+  const double t = t_dev ? *t_dev : t_arg;
   double nodal = 0.0;
   for (int k = d.eq_ptr[e]; k < d.eq_ptr[e + 1]; k++) {
     const int a = d.eq_dofs[k];
@@ -145,9 +148,59 @@ __global__ void k_comp_mask(int neq, const int *comp_of, const int *active, doub
   if (e < neq && !active[comp_of[e]]) B[e] = 0.0;
 }
 
+// Start of a captured Newmark step: t += dt on the device, every part
+// active, the iteration count cleared.
+__global__ void k_step_begin(double *t, double dt, int *stat, int *active, int ncomp) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i == 0) {
+    *t += dt;
+    stat[0] = 0;
+    stat[1] = 0;
+    stat[2] = ncomp;
+  }
+  if (i < ncomp) active[i] = 1;
+}
+
+// End of a captured Newton iteration (CTestNormDispIncr / CTestNormUnbalance
+// per part): parts whose norm passed stop; the loop goes on while any part
+// is active and fewer than max_iter iterations have run.  stat: [0]
+// iterations, [1] 1 converged / 2 not converged, [2] parts still active.
+__global__ void k_newton_check(int ncomp, const double *cnorm, double tol, int max_iter,
+                               int *active, int *stat, cudaGraphConditionalHandle h) {
+  __shared__ int nact;
+  if (threadIdx.x == 0) nact = 0;
+  __syncthreads();
+  int mine = 0;
+  for (int c = threadIdx.x; c < ncomp; c += blockDim.x) {
+    if (active[c] && sqrt(cnorm[c]) <= tol) active[c] = 0;
+    mine += active[c];
+  }
+  atomicAdd(&nact, mine);
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    const int it = ++stat[0];
+    stat[2] = nact;
+    unsigned go = 1;
+    if (nact == 0) { stat[1] = 1; go = 0; }
+    else if (it >= max_iter) { stat[1] = 2; go = 0; }
+    cudaGraphSetConditional(h, go);
+  }
+}
+
 inline int grid(long n, int b) { return (int)((n + b - 1) / b); }
 
 }  // namespace
+
+int launch_step_begin(double *t, double dt, int *stat, int *active, int ncomp, cudaStream_t s) {
+  k_step_begin<<<grid(std::max(ncomp, 1), 256), 256, 0, s>>>(t, dt, stat, active, ncomp);
+  return cudaGetLastError() == cudaSuccess ? 0 : XG_ECUDA;
+}
+
+int launch_newton_check(int ncomp, const double *cnorm, double tol, int max_iter, int *active,
+                        int *stat, cudaGraphConditionalHandle h, cudaStream_t s) {
+  k_newton_check<<<1, 256, 0, s>>>(ncomp, cnorm, tol, max_iter, active, stat, h);
+  return cudaGetLastError() == cudaSuccess ? 0 : XG_ECUDA;
+}
 
 int launch_newmark_predict(const DynView &d, double a1, double a2, double a3, double a4,
                            cudaStream_t s) {
@@ -166,13 +219,13 @@ int launch_newmark_correct(const DynView &d, const double *dU, double c2, double
 int launch_dyn_unbalance(const DynView &d, const double *fext, const double *pint,
                          const double *k0vals, const int *rowptr, const int *colidx,
                          double bk0, double am, double t, double *veq, double *k0v, double *B,
-                         cudaStream_t s) {
+                         cudaStream_t s, const double *t_dev) {
   if (d.neq == 0) return 0;
   if (bk0 != 0.0) {
     k_vel_eq<<<grid(d.neq, 256), 256, 0, s>>>(d, veq);
     k_spmv<<<grid((long)d.neq * 32, 256), 256, 0, s>>>(d.neq, rowptr, colidx, k0vals, veq, k0v);
   }
-  k_dyn_unbalance<<<grid(d.neq, 256), 256, 0, s>>>(d, fext, pint, k0v, bk0, am, t, B);
+  k_dyn_unbalance<<<grid(d.neq, 256), 256, 0, s>>>(d, fext, pint, k0v, bk0, am, t, t_dev, B);
   return cudaGetLastError() == cudaSuccess ? 0 : XG_ECUDA;
 }
 

@@ -132,6 +132,9 @@ int band_plan(int neq, const int *rowptr, const int *colidx, const std::vector<i
 // scaling on the way (band_solve(forward = false) completes them).
 int band_factor(const BandSystem &S, cudaStream_t s, int *bad_eq, int nrhs = 0,
                 double *x = nullptr, int ldx = 0);
+// the same without the host read of the pivot flags (stream capture); the
+// flags stay in S.flags
+int band_factor_async(const BandSystem &S, cudaStream_t s, int nrhs, double *x, int ldx);
 // x[r*ldx + i] right-hand side r in, solution out (equation numbering)
 int band_solve(const BandSystem &S, int nrhs, double *x, int ldx, cudaStream_t s,
                bool forward = true);
@@ -210,10 +213,15 @@ int launch_newmark_predict(const DynView &d, double a1, double a2, double a3, do
                            cudaStream_t s);
 int launch_newmark_correct(const DynView &d, const double *dU, double c2, double c3,
                            cudaStream_t s);
+// t_dev: the time read from device memory instead of t (captured steps)
 int launch_dyn_unbalance(const DynView &d, const double *fext, const double *pint,
                          const double *k0vals, const int *rowptr, const int *colidx,
                          double bk0, double am, double t, double *veq, double *k0v, double *B,
-                         cudaStream_t s);
+                         cudaStream_t s, const double *t_dev = nullptr);
+// captured Newmark step (a graph with a conditional loop over Newton iterations)
+int launch_step_begin(double *t, double dt, int *stat, int *active, int ncomp, cudaStream_t s);
+int launch_newton_check(int ncomp, const double *cnorm, double tol, int max_iter, int *active,
+                        int *stat, cudaGraphConditionalHandle h, cudaStream_t s);
 int launch_dyn_tangent(const DynView &d, double *vals, const double *k0vals, double c1,
                        double c2bk0, double c2, double c3, cudaStream_t s);
 // x[b*len + i] *= scale ? scale[b] : s0

@@ -260,6 +260,27 @@ struct xg_model {
     }
   };
   Tuner tune_elem, tune_pcg;
+  // a Newmark step of a many-part model as one CUDA graph: the predictor,
+  // then a conditional loop whose body is one Newton iteration ending in a
+  // device-side convergence check (xg_analysis_set_graph)
+  struct StepGraph {
+    bool want = false, built = false;
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    DBuf<double> t;
+    DBuf<int> stat;
+    long launches = 0;
+  } sg;
+  void free_step_graph() {
+    if (sg.exec) cudaGraphExecDestroy(sg.exec);
+    if (sg.graph) cudaGraphDestroy(sg.graph);
+    sg.exec = nullptr;
+    sg.graph = nullptr;
+    sg.built = false;
+  }
+  bool step_graph_usable() const;
+  int build_step_graph();
+  int step_newmark_graph(xg_step_stats *st);
   int fbc_warps = 4, pcg_rows = 64;
   cudaEvent_t tune_a = nullptr, tune_b = nullptr;
   // per-kernel CUDA-event timing on the model's stream (xg_profile_*)
@@ -359,6 +380,7 @@ struct xg_model {
   int revert_state();
 
   ~xg_model() {
+    free_step_graph();
     for (auto &p : prof) {
       cudaEventDestroy(p.a);
       cudaEventDestroy(p.b);
@@ -990,7 +1012,133 @@ int xg_model::upload_dynamics() {
 // whose displacement increment (or unbalance) norm has passed stops
 // iterating -- its right-hand side is zeroed, so its state does not move --
 // while the others go on, exactly as if every part ran alone.
+// The captured step applies to Newmark runs of models in several parts with
+// the per-part band LDL', constant external loads, and no per-kernel timing
+// or autotuning in progress (those read the device between launches).
+bool xg_model::step_graph_usable() const {
+  if (!sg.want || phase.integrator != XG_INT_NEWMARK || system != XG_SYSTEM_PROFILE_SPD) return false;
+  if (!prof_ready || !prof_band || prof_on) return false;
+  if ((tune_elem.on && !tune_elem.done) || (tune_pcg.on && !tune_pcg.done)) return false;
+  for (int p : ref_patterns)
+    if (p >= 0 && p < 8 && added[p] && !pattern_const[p]) return false;
+  return true;
+}
+
+int xg_model::build_step_graph() {
+  free_step_graph();
+  cudaStream_t s = stream;
+  const int ncomp = (int)comp_start.size() - 1;
+  const double dt = phase.dt, gam = phase.gamma, bet = phase.beta;
+  const double c1 = 1.0, c2 = gam / (bet * dt), c3 = 1.0 / (bet * dt * dt);
+  const double a1 = 1.0 - gam / bet, a2 = dt * (1.0 - 0.5 * gam / bet);
+  const double a3 = -1.0 / (bet * dt), a4 = 1.0 - 0.5 / bet;
+  DynView dv = dview();
+  RET(sg.t.alloc(1));
+  RET(sg.stat.alloc(4));
+  RET(form_fext(time));                  // constant over the phase
+  CK(cudaStreamSynchronize(s));
+  cudaGraph_t parent = nullptr, pre = nullptr;
+  CK(cudaGraphCreate(&parent, 0));
+  CK(cudaGraphCreate(&pre, 0));
+  auto give_up = [&](int code, const char *what) {
+    cudaGraph_t dummy = nullptr;
+    cudaStreamEndCapture(s, &dummy);
+    cudaGraphDestroy(pre);
+    cudaGraphDestroy(parent);
+    return fail(code, "step graph: %s", what);
+  };
+  // Newmark::newStep and the first unbalance
+  CK(cudaStreamBeginCaptureToGraph(s, pre, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal));
+  int r = launch_step_begin(sg.t.p, dt, sg.stat.p, d_active.p, ncomp, s);
+  if (!r) r = launch_newmark_predict(dv, a1, a2, a3, a4, s);
+  if (!r) r = element_state(true);
+  if (!r) r = launch_dyn_unbalance(dv, d_fext.p, d_resid.p, d_K0vals.p, d_rowptr.p, d_colidx.p,
+                                   k0_ready ? 1.0 : 0.0, phase.alpha_m, 0.0, d_veq.p, d_k0v.p,
+                                   d_B.p, s, sg.t.p);
+  if (r) return give_up(r, "capture of the predictor failed");
+  cudaGraph_t got = nullptr;
+  CK(cudaStreamEndCapture(s, &got));
+  // the Newton loop: a conditional while node, one iteration per pass
+  cudaGraphConditionalHandle h;
+  CK(cudaGraphConditionalHandleCreate(&h, parent, 1, cudaGraphCondAssignDefault));
+  cudaGraphNode_t npre, ncond;
+  CK(cudaGraphAddChildGraphNode(&npre, parent, nullptr, 0, pre));
+  cudaGraphDestroy(pre);
+  pre = nullptr;
+  cudaGraphNodeParams cp{};
+  cp.type = cudaGraphNodeTypeConditional;
+  cp.conditional.handle = h;
+  cp.conditional.type = cudaGraphCondTypeWhile;
+  cp.conditional.size = 1;
+  CK(cudaGraphAddNode(&ncond, parent, &npre, nullptr, 1, &cp));
+  cudaGraph_t body = cp.conditional.phGraph_out[0];
+  CK(cudaStreamBeginCaptureToGraph(s, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal));
+  r = launch_dyn_tangent(dv, d_vals.p, d_K0vals.p, c1, k0_ready ? c2 : 0.0, c2, c3, s);
+  if (!r && cudaMemcpyAsync(d_px.p, d_B.p, (size_t)neq * sizeof(double), cudaMemcpyDeviceToDevice,
+                            s) != cudaSuccess)
+    r = XG_ECUDA;
+  if (!r) r = band_factor_async(bsys, s, 1, d_px.p, prof_ldx);
+  if (!r) r = band_solve(bsys, 1, d_px.p, prof_ldx, s, false);
+  if (!r && cudaMemcpyAsync(d_dU.p, d_px.p, (size_t)neq * sizeof(double), cudaMemcpyDeviceToDevice,
+                            s) != cudaSuccess)
+    r = XG_ECUDA;
+  if (!r) r = launch_newmark_correct(dv, d_dU.p, c2, c3, s);
+  if (!r) r = element_state(true);
+  if (!r) r = launch_dyn_unbalance(dv, d_fext.p, d_resid.p, d_K0vals.p, d_rowptr.p, d_colidx.p,
+                                   k0_ready ? 1.0 : 0.0, phase.alpha_m, 0.0, d_veq.p, d_k0v.p,
+                                   d_B.p, s, sg.t.p);
+  if (!r) r = launch_comp_norm2(ncomp, d_cstart.p,
+                                phase.test == XG_TEST_NORM_DISP_INCR ? d_dU.p : d_B.p, d_cnorm.p, s);
+  if (!r) r = launch_newton_check(ncomp, d_cnorm.p, phase.tol, phase.max_iter, d_active.p,
+                                  sg.stat.p, h, s);
+  if (!r && ncomp > 1) r = launch_comp_mask(neq, d_comp_of.p, d_active.p, d_B.p, s);
+  if (r) return give_up(r, "capture of the Newton iteration failed");
+  CK(cudaStreamEndCapture(s, &got));
+  CK(cudaGraphInstantiate(&sg.exec, parent, 0));
+  sg.graph = parent;
+  sg.built = true;
+  // the graph's kernels per step: 5 before the loop (plus the element
+  // state's), 12 per Newton iteration
+  return 0;
+}
+
+// One Newmark step as a graph launch; the host reads the iteration count,
+// the status and the pivot flags once, then commits (or reverts).
+int xg_model::step_newmark_graph(xg_step_stats *st) {
+  cudaStream_t s = stream;
+  if (!sg.built) RET(build_step_graph());
+  CK(cudaMemcpyAsync(sg.t.p, &time, sizeof(double), cudaMemcpyHostToDevice, s));
+  CK(cudaGraphLaunch(sg.exec, s));
+  sg.launches++;
+  int hstat[4] = {0, 0, 0, 0}, hflags[4] = {0, 0, 0, 0};
+  CK(cudaMemcpyAsync(hstat, sg.stat.p, sizeof hstat, cudaMemcpyDeviceToHost, s));
+  CK(cudaMemcpyAsync(hflags, bsys.flags, sizeof hflags, cudaMemcpyDeviceToHost, s));
+  CK(cudaStreamSynchronize(s));
+  blocks_factored = false;
+  prof_factored = false;
+  const int ncomp = (int)comp_start.size() - 1;
+  if (st) {
+    st->newton_iters = hstat[0];
+    st->solver_iters = 0;
+    st->elem_iters = 0;
+    st->status = hstat[1] == 1 ? 0 : XG_ENOCONV;
+  }
+  if (hflags[0] == 3)
+    return fail(XG_ESOLVE, "ProfileSPD: pivot %d fails the check (aii == 0, |aii| <= 1e-12, or "
+                "a first pivot <= 0)", hflags[1]);
+  if (hstat[1] != 1)
+    return fail(XG_ENOCONV, "Newton did not converge in %d iterations (%d of %d parts)",
+                hstat[0], hstat[2], ncomp);
+  time += phase.dt;
+  RET(commit_state());
+  CK(cudaMemcpyAsync(d_Vc.p, d_V.p, (size_t)nn * ndf * sizeof(double), cudaMemcpyDeviceToDevice, s));
+  CK(cudaMemcpyAsync(d_Ac.p, d_A.p, (size_t)nn * ndf * sizeof(double), cudaMemcpyDeviceToDevice, s));
+  time_c = time;
+  return 0;
+}
+
 int xg_model::step_newmark(xg_step_stats *st) {
+  if (step_graph_usable()) return step_newmark_graph(st);
   cudaStream_t s = stream;
   last_solver_iters = 0;
   const double t_commit = time;
@@ -2120,6 +2268,7 @@ int xg_analysis_set_phase(xg_model *m, const xg_phase_desc *ph) {
   m->have_phase = true;
   m->phase_steps_done = 0;
   m->phase_closed = false;
+  m->free_step_graph();
   return m->init_phase();
 }
 
@@ -2128,6 +2277,7 @@ int xg_analysis_set_system(xg_model *m, int system) {
   if (system != XG_SYSTEM_BJPCG && system != XG_SYSTEM_PROFILE_SPD)
     return fail(XG_EINVAL, "unknown system %d", system);
   m->system = system;
+  m->free_step_graph();
   if (system == XG_SYSTEM_PROFILE_SPD) RET(m->ensure_profile());
   return 0;
 }
@@ -2194,6 +2344,20 @@ int xg_reset(xg_model *m) {
   m->have_phase = false;
   m->steps_since_reset = 0;
   m->adj.have = false;
+  m->free_step_graph();
+  return 0;
+}
+
+int xg_analysis_set_graph(xg_model *m, int enable) {
+  if (!m) return fail(XG_EINVAL, "null model");
+  m->sg.want = enable != 0;
+  m->free_step_graph();
+  return 0;
+}
+
+int xg_analysis_graph_steps(const xg_model *m, long *steps) {
+  if (!m || !steps) return fail(XG_EINVAL, "null argument");
+  *steps = m->sg.launches;
   return 0;
 }
 

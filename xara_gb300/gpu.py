@@ -355,3 +355,19 @@ def uniaxial_vjp(kind, param, hc, strain, yb):
     _check(L.xg_uniaxial_vjp(int(kind), _p(q), _p(hc), float(strain), _p(yb), _p(hb),
                              C.byref(sb), _p(qb)))
     return hb, sb.value, qb
+
+
+def set_graph(model, enable=True):
+    """Run Newmark steps of many-part models as CUDA graphs (see xg_analysis_set_graph)."""
+    L = lib()
+    L.xg_analysis_set_graph.argtypes = [C.c_void_p, C.c_int]
+    _check(L.xg_analysis_set_graph(model.h, 1 if enable else 0))
+
+
+def graph_steps(model):
+    """Steps that ran as CUDA graphs."""
+    L = lib()
+    L.xg_analysis_graph_steps.argtypes = [C.c_void_p, C.POINTER(C.c_long)]
+    n = C.c_long()
+    _check(L.xg_analysis_graph_steps(model.h, C.byref(n)))
+    return n.value
