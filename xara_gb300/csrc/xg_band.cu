@@ -26,6 +26,7 @@
 #include <algorithm>
 
 #include "xg_internal.h"
+#include "xg_rcp.h"
 
 namespace xg {
 
@@ -38,17 +39,9 @@ constexpr int kBandAhead = 8;           // rows fetched ahead of use
 constexpr int kBandMaxRhs = 4;
 constexpr int kBackWarps = 4;
 
-// reciprocal from a single-precision seed and two Newton steps (the pivot
-// chain's latency); the stored reciprocals are the correctly rounded ones
-__device__ __forceinline__ double chain_rcp(double d) {
-  const double ad = fabs(d);
-  if (!(ad > 1e-30 && ad < 1e30)) return __drcp_rn(d);
-  double x = (double)__frcp_rn((float)d);
-  double e = fma(-d, x, 1.0);
-  x = fma(x, e, x);
-  e = fma(-d, x, 1.0);
-  return fma(x, e, x);
-}
+// reciprocal on the pivot chain (xg_rcp.h); the stored reciprocals are the
+// correctly rounded ones
+__device__ __forceinline__ double chain_rcp(double d) { return chain_reciprocal(d); }
 
 __device__ __forceinline__ void cp_async8(double *dst, const double *src) {
   const unsigned sa = (unsigned)__cvta_generic_to_shared(dst);

@@ -42,6 +42,7 @@
 #include <cstdint>
 
 #include "xg_internal.h"
+#include "xg_rcp.h"
 
 namespace xg {
 
@@ -102,80 +103,84 @@ __global__ void k_prof_fill(ProfileSystem S) {
 // next pivot takes its reciprocal at once (__drcp_rn: the correctly rounded
 // 1/d, the value of the reference's 1.0/aii), so the chain of dependent
 // FP64 operations per column stays short.
-// 1/d for the elimination (three dependent FMAs after the estimate, against
-// about six for a correctly rounded FP64 reciprocal, whose FP64 latency
-// sets the pace of the pivot chain); the stored reciprocal pivots are the
+// 1/d for the elimination (xg_rcp.h); the stored reciprocal pivots are the
 // correctly rounded ones.
-__device__ __forceinline__ double elim_rcp(double d) {
-  const double ad = fabs(d);
-  if (!(ad > 1e-30 && ad < 1e30)) return __drcp_rn(d);
-  // hardware FP64 reciprocal estimate, then one cubic Newton step
-  // x (1 + e + e^2), e = 1 - d x, which triples its correct bits
-  double x;
-  asm("rcp.approx.ftz.f64 %0, %1;" : "=d"(x) : "d"(d));
-  const double e = fma(-d, x, 1.0);
-  return fma(x, fma(e, e, e), x);
+__device__ __forceinline__ double elim_rcp(double d) { return chain_reciprocal(d); }
+
+__device__ __forceinline__ void named_sync(int id, int count) {
+  asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(count) : "memory");
 }
+__device__ __forceinline__ void named_arrive(int id, int count) {
+  asm volatile("bar.arrive %0, %1;" ::"r"(id), "r"(count) : "memory");
+}
+
+// LDL' of the diagonal tile in sA (shared memory), as a two-stage pipeline.
+// Warp 1 carries the pivot chain: step c applies column c-1 to column c
+// (one FMA per row, the factors kept in its registers), takes the pivot's
+// reciprocal (FP64 estimate and one cubic Newton step, every lane), scales
+// the column (L below the diagonal, the unscaled column in the upper
+// triangle for the trailing update).  Warps 0, 2, 3, 4, 6 and 7 apply
+// column c to the rest of the trailing triangle (columns c+2 and beyond,
+// one FMA per entry, each thread owning up to three fixed entries) while
+// the chain goes on with column c+1; warp 5 sits out, so the chain has its
+// sub-partition's FP64 pipe to itself.  Hand-offs: named barriers 1-2
+// (chain -> trailing, by column parity) and 3-4 (trailing -> chain); the
+// chain's step c waits for the trailing update of column c-2 only.  The FMAs
+// and their operands are those of the plain right-looking order.
+constexpr int kPipeCount = 224;        // the chain warp and six trailing warps
 
 __device__ bool factor_tile(const ProfileSystem &S, int J, double (*sA)[kT + 1],
                             volatile int *flags) {
   double *g = tile_at(S, J, 0);
-  __shared__ double colbuf[2][kT], lcol[kT], sinv[kT + 1], pivv;
-  const int tid = threadIdx.x;
-  // this thread's entries of the trailing triangles (row-major, relative to
-  // the pivot's successor; at most 31 x 32 / 2 = 496 of them), fixed for
-  // every column; entry 0 -- the next pivot -- is thread kT's.  Warps 1 and
-  // 5 share the sub-partition of the pivot chain (thread kT's scaling, FMA
-  // and reciprocal), so they take no trailing entries: every warp-wide FP64
-  // instruction occupies its sub-partition's pipe for the same time, and
-  // the chain's sub-partition sets the pace of the column.
-  const int warp = tid >> 5;
-  const bool trailing = warp != 1 && warp != 5;
-  const int tw = trailing ? (warp - (warp > 1) - (warp > 5)) * 32 + (tid & 31) : -1;
-  const int ntw = ((int)blockDim.x / 32 - 2) * 32;         // 192 trailing threads
-  int ent[3];
-#pragma unroll
-  for (int u = 0; u < 3; u++) {
-    const int k = tw + u * ntw;
-    ent[u] = (trailing && k < 496) ? kLowerRS[k] : -1;
-  }
-  if (tid < kT) colbuf[0][tid] = sA[tid][0];
-  if (tid == 0) sinv[0] = elim_rcp(sA[0][0]);
-  __syncthreads();
-  // Column c: the threads below the pivot scale the column (l = a / d)
-  // while thread kT applies it to the next pivot and takes that pivot's
-  // reciprocal, which runs alongside the rest of the trailing triangle (one
-  // FMA per entry); the threads that finish column c+1's entries hand them
-  // to the next column through a second buffer.
-  for (int c = 0; c < kT - 1; c++) {
-    const double *cl = colbuf[c & 1];
-    double *cn = colbuf[(c + 1) & 1];
-    const double inv = sinv[c];
-    if (tid < kT && tid > c) {
-      const double l = cl[tid] * inv;
-      lcol[tid] = l;
-      sA[tid][c] = l;
-    } else if (tid == kT) {
-      const double l1 = cl[c + 1] * inv;
-      pivv = fma(-l1, cl[c + 1], sA[c + 1][c + 1]);
-      sA[c + 1][c + 1] = pivv;
+  __shared__ double sinv[kT];
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  if (warp == 1) {
+    double lprev = 0.0, uprev = 0.0;
+    for (int c = 0; c < kT; c++) {
+      if (c >= 2) named_sync(3 + (c & 1), kPipeCount);
+      double x = sA[lane][c];
+      if (c >= 1) {
+        const double ucc = __shfl_sync(0xffffffffu, uprev, c);
+        x = fma(-lprev, ucc, x);
+      }
+      const double d = __shfl_sync(0xffffffffu, x, c);
+      const double inv = elim_rcp(d);
+      const double l = x * inv;
+      if (lane > c) {
+        sA[lane][c] = l;
+        sA[c][lane] = x;
+      } else if (lane == c) {
+        sA[c][c] = x;
+      }
+      lprev = l;
+      uprev = x;
+      if (c <= kT - 3) named_arrive(1 + (c & 1), kPipeCount);
     }
-    __syncthreads();
-    const int m = kT - 1 - c;
+  } else if (warp != 5) {
+    // this thread's entries (r, s), 2 <= s <= r < 32, column-major order
+    const int tw = (warp == 0 ? 0 : warp - 1 - (warp > 5)) * 32 + lane;
+    int ent[3];
 #pragma unroll
     for (int u = 0; u < 3; u++) {
-      const int e = ent[u];
-      const int ti = e >> 5, tk = e & 31;
-      if (e > 0 && ti < m) {
-        const int r = c + 1 + ti, sc = c + 1 + tk;
-        const double v = fma(-lcol[r], cl[sc], sA[r][sc]);
-        sA[r][sc] = v;
-        if (tk == 0) cn[r] = v;
+      int e = tw + u * 192;
+      ent[u] = -1;
+      for (int sc = 2; sc < kT && e >= 0; sc++) {
+        if (e < kT - sc) { ent[u] = ((sc + e) << 5) | sc; break; }
+        e -= kT - sc;
       }
     }
-    if (tid == kT) sinv[c + 1] = elim_rcp(pivv);
-    __syncthreads();
+    for (int c = 0; c < kT - 2; c++) {
+      named_sync(1 + (c & 1), kPipeCount);
+#pragma unroll
+      for (int u = 0; u < 3; u++) {
+        const int e = ent[u];
+        const int r = e >> 5, sc = e & 31;
+        if (e >= 0 && sc >= c + 2) sA[r][sc] = fma(-sA[r][c], sA[c][sc], sA[r][sc]);
+      }
+      named_arrive(3 + (c & 1), kPipeCount);
+    }
   }
+  __syncthreads();
   if (tid < kT) sinv[tid] = __drcp_rn(sA[tid][tid]);
   __syncwarp();
   if (tid < kT) {
@@ -194,7 +199,11 @@ __device__ bool factor_tile(const ProfileSystem &S, int J, double (*sA)[kT + 1],
       flags[0] = 3;
     }
   }
-  for (int k = tid; k < kTT; k += blockDim.x) g[k] = sA[k >> 5][k & 31];
+  // the lower triangle (the upper one held the unscaled columns)
+  for (int k = tid; k < kTT; k += blockDim.x) {
+    const int r = k >> 5, c = k & 31;
+    g[k] = c > r ? 0.0 : sA[r][c];
+  }
   __syncthreads();
   return flags[0] != 3;
 }
