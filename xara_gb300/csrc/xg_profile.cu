@@ -15,9 +15,9 @@
 //      slot) and L_IJ = W_IJ D^-1 (stored in place);
 //   C  every trailing tile pair loses W_IJ L_KJ' (one 32^3 product each).
 // The tasks (A: diagonal, B: panel tile in four row parts, C: tile pair of
-// one column, and the chain task of column J: C for the pair (J+1, J+1)
-// and A(J+1) in one block's shared memory -- the critical path of the
-// factorisation) run as a dataflow: one persistent launch whose blocks take
+// one column; for tile (J+1, J) the four panel parts also apply a quarter
+// each of the pair (J+1, J+1)'s update, and the chain task of column J
+// factors diagonal tile J+1 -- the critical path of the factorisation) run as a dataflow: one persistent launch whose blocks take
 // tasks from a list in a fixed order -- for column J: A(J) when no column
 // updates it, the C tasks of column J-1 that reach column J+1, the panel
 // (J+1, J), the chain task, the other panels B(., J), the C tasks of column
@@ -217,31 +217,83 @@ __device__ bool factor_diag(const ProfileSystem &S, int J, double (*sA)[kT + 1],
 }
 
 // Phase B on rows 8q..8q+7 of tile (I = J+o, J): W = A L_JJ^-T, L = W
-// D^-1 (rows are independent, so a tile is four tasks).  Column sweep: once
-// column c of W is final, every later column s loses W(:, c) l_sc; thread t
-// updates row 8q + t%8 of columns c+1+t/8, c+33+t/8, ...
+// D^-1 (rows are independent, so a tile is four tasks).  A warp per row: once
+// column c of W is final (broadcast by shuffle), every later column s loses
+// W(r, c) l_sc -- no block barriers inside the sweep.
 constexpr int kPanelRows = 8;
 constexpr int kPanelParts = kT / kPanelRows;
 
 __device__ void panel_solve(const ProfileSystem &S, int J, int o, int q, double (*sA)[kT + 1],
                             double (*sB)[kT + 1]) {
+  (void)sA;
   const double *Ljj = tile_at(S, J, 0);
   double *g = tile_at(S, J + o, o) + q * kPanelRows * kT;
+  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
   for (int k = threadIdx.x; k < kTT; k += blockDim.x) sB[k >> 5][k & 31] = __ldcg(Ljj + k);
-  for (int k = threadIdx.x; k < kPanelRows * kT; k += blockDim.x)
-    sA[k >> 5][k & 31] = __ldcg(g + k);
+  // warp w solves row 8q+w: lane s holds W(r, s); column c is final once
+  // the columns before it have been applied, then the later columns take it
+  double x = w < kPanelRows ? __ldcg(g + w * kT + lane) : 0.0;
+  const double inv = __ldcg(S.invD + (size_t)J * kT + lane);
   __syncthreads();
-  const int r = threadIdx.x % kPanelRows, sy = threadIdx.x / kPanelRows;
-  const int nsy = blockDim.x / kPanelRows;
-  for (int c = 0; c < kT - 1; c++) {
-    const double wc = sA[r][c];
-    for (int s = c + 1 + sy; s < kT; s += nsy) sA[r][s] = fma(-wc, sB[s][c], sA[r][s]);
-    __syncthreads();
+  if (w < kPanelRows) {
+    for (int c = 0; c < kT - 1; c++) {
+      const double wc = __shfl_sync(0xffffffffu, x, c);
+      if (lane > c) x = fma(-wc, sB[lane][c], x);
+    }
+    g[w * kT + lane] = x * inv;
   }
-  const double *invD = S.invD + (size_t)J * kT;
-  for (int k = threadIdx.x; k < kPanelRows * kT; k += blockDim.x)
-    g[k] = sA[k >> 5][k & 31] * __ldcg(invD + (k & 31));
   __syncthreads();
+}
+
+// The panel of tile (J+1, J) in four row parts whose tasks, once all four
+// are written, apply a quarter each of that panel's update of diagonal tile
+// J+1 (phase C for the pair (J+1, J+1), 132 of its 528 lower entries), so
+// the chain task only factors.  The wait for the sibling parts is bounded;
+// they sit right after this task in the list, so the blocks that take them
+// never wait on this one.
+__device__ bool wait_geq_dev(const int *p, int target, volatile int *flags);
+__device__ bool panel_update_task(const ProfileSystem &S, int J, int q, double (*sA)[kT + 1],
+                                  double (*sB)[kT + 1], volatile int *flags) {
+  const int I = J + 1, tid = threadIdx.x;
+  panel_solve(S, J, 1, q, sA, sB);
+  __shared__ int ok;
+  if (tid == 0) {
+    __threadfence();
+    atomicAdd(S.done + (size_t)I * (S.W + 1) + 1, 1);
+    ok = wait_geq_dev(S.done + (size_t)I * (S.W + 1) + 1, kPanelParts, flags) &&
+         wait_geq_dev(S.upd + (size_t)I * (S.W + 1), J - S.ftile[I], flags);
+    __threadfence();
+  }
+  __syncthreads();
+  if (!ok) return false;
+  const double *gp = tile_at(S, I, 1);
+  double *gd = tile_at(S, I, 0);
+  const double *piv = S.piv + (size_t)J * kT;
+  for (int k = tid; k < kTT; k += blockDim.x) {
+    const double l = __ldcg(gp + k);
+    sB[k >> 5][k & 31] = l;
+    sA[k >> 5][k & 31] = l * __ldcg(piv + (k & 31));
+  }
+  __syncthreads();
+  constexpr int kQuarter = kT * (kT + 1) / 2 / kPanelParts;   // 132
+  for (int k = q * kQuarter + tid; k < (q + 1) * kQuarter; k += blockDim.x) {
+    const int rs = kLowerRS[k], r = rs >> 5, sc = rs & 31;
+    double a0 = 0.0, a1 = 0.0, a2 = 0.0, a3 = 0.0;
+#pragma unroll
+    for (int c = 0; c < kT; c += 4) {
+      a0 = fma(sA[r][c], sB[sc][c], a0);
+      a1 = fma(sA[r][c + 1], sB[sc][c + 1], a1);
+      a2 = fma(sA[r][c + 2], sB[sc][c + 2], a2);
+      a3 = fma(sA[r][c + 3], sB[sc][c + 3], a3);
+    }
+    gd[r * kT + sc] = __ldcg(gd + r * kT + sc) - ((a0 + a1) + (a2 + a3));
+  }
+  __syncthreads();
+  if (tid == 0) {
+    __threadfence();
+    atomicAdd(S.upd + (size_t)I * (S.W + 1), 1);
+  }
+  return true;
 }
 
 // Phase C on pair (I = J+a, K = J+b), b <= a: A_IK -= (L_IJ D_J) L_KJ'.
@@ -277,42 +329,21 @@ __device__ void pair_update(const ProfileSystem &S, int J, int a, int b, double 
   __syncthreads();
 }
 
+__device__ bool wait_geq(const int *p, int target, volatile int *flags);
+__device__ bool wait_geq_dev(const int *p, int target, volatile int *flags) {
+  return wait_geq(p, target, flags);
+}
+
 __device__ __forceinline__ int slot_of(const ProfileSystem &S, int I, int o) {
   return I * (S.W + 1) + o;
 }
 
-// Column J's critical chain in one block, in shared memory: once the four
-// row parts of panel (J+1, J) are done (phase B on four other SMs), the
-// last update of diagonal tile J+1 (phase C for the pair (J+1, J+1)) and
-// that tile's LDL'.
-__device__ bool chain_task(const ProfileSystem &S, int J, double (*sA)[kT + 1],
-                           double (*sB)[kT + 1], double (*sC)[kT + 1], volatile int *flags) {
-  const int I = J + 1, tid = threadIdx.x;
-  const double *gp = tile_at(S, I, 1);
-  const double *gd = tile_at(S, I, 0);
-  const double *piv = S.piv + (size_t)J * kT;
-  for (int k = tid; k < kTT; k += blockDim.x) {
-    const double l = __ldcg(gp + k);
-    sB[k >> 5][k & 31] = l;
-    sA[k >> 5][k & 31] = l * __ldcg(piv + (k & 31));
-    sC[k >> 5][k & 31] = __ldcg(gd + k);
-  }
-  __syncthreads();
-  // diagonal tile J+1 loses (L D) L' (its lower triangle)
-  for (int k = tid; k < kT * (kT + 1) / 2; k += blockDim.x) {
-    const int rs = kLowerRS[k], r = rs >> 5, sc = rs & 31;
-    double a0 = 0.0, a1 = 0.0, a2 = 0.0, a3 = 0.0;
-#pragma unroll
-    for (int c = 0; c < kT; c += 4) {
-      a0 = fma(sA[r][c], sB[sc][c], a0);
-      a1 = fma(sA[r][c + 1], sB[sc][c + 1], a1);
-      a2 = fma(sA[r][c + 2], sB[sc][c + 2], a2);
-      a3 = fma(sA[r][c + 3], sB[sc][c + 3], a3);
-    }
-    sC[r][sc] -= (a0 + a1) + (a2 + a3);
-  }
-  __syncthreads();
-  return factor_tile(S, I, sC, flags);
+// Column J's critical chain: once the four panel-part tasks of tile
+// (J+1, J) have applied their quarters of its update of diagonal tile J+1,
+// that tile's LDL' in shared memory.
+__device__ bool chain_task(const ProfileSystem &S, int J, double (*sC)[kT + 1],
+                           volatile int *flags) {
+  return factor_diag(S, J + 1, sC, flags);
 }
 
 // Wait until *p >= target (thread 0 of a block); false on a raised error
@@ -340,8 +371,10 @@ __device__ bool wait_task(const ProfileSystem &S, int4 t, volatile int *flags) {
   if (type == 0)
     return wait_geq(S.upd + slot_of(S, J, 0), J - S.ftile[J], flags);
   if (type == 4)
-    return wait_geq(S.done + slot_of(S, I, 1), kPanelParts, flags) &&
-           wait_geq(S.upd + slot_of(S, I, 0), J - S.ftile[I], flags);
+    return wait_geq(S.upd + slot_of(S, I, 0), J - S.ftile[I] + kPanelParts, flags);
+  if (type == 5)
+    return wait_geq(S.done + slot_of(S, J, 0), 1, flags) &&
+           wait_geq(S.upd + slot_of(S, I, 1), J - max(S.ftile[I], S.ftile[J]), flags);
   if (type == 1)
     return wait_geq(S.done + slot_of(S, J, 0), 1, flags) &&
            wait_geq(S.upd + slot_of(S, I, I - J), J - max(S.ftile[I], S.ftile[J]), flags);
@@ -371,14 +404,16 @@ __global__ void __launch_bounds__(kFactorThreads) k_prof_factor(ProfileSystem S)
       panel_solve(S, t.w, t.y - t.w, t.z, sA, sB);
     } else if (t.x == 2) {
       pair_update(S, t.w, t.y - t.w, t.z - t.w, sA, sB);
+    } else if (t.x == 4) {
+      fine = chain_task(S, t.w, sC, flags);
     } else {
-      fine = chain_task(S, t.w, sA, sB, sC, flags);
+      fine = panel_update_task(S, t.w, t.z, sA, sB, flags);
     }
     if (!fine) break;
     __syncthreads();
     if (threadIdx.x == 0) {
       __threadfence();
-      if (t.x >= 2) atomicAdd(S.upd + slot_of(S, t.y, t.y - t.z), 1);
+      if (t.x == 2) atomicAdd(S.upd + slot_of(S, t.y, t.y - t.z), 1);
       if (t.x == 0 || t.x == 4) atomicExch(S.done + slot_of(S, t.y, 0), 1);
       if (t.x == 1) atomicAdd(S.done + slot_of(S, t.y, t.y - t.w), 1);
     }
@@ -656,7 +691,7 @@ void profile_tasks(int nt, int W, const std::vector<int> &ftile, std::vector<int
     updates(J - 1, 2, 2);
     const int omax = std::min(W, nt - 1 - J);
     if (omax >= 1 && ftile[J + 1] <= J)
-      for (int q = 0; q < kPanelParts; q++) emit(1, J + 1, q, J);
+      for (int q = 0; q < kPanelParts; q++) emit(5, J + 1, q, J);
     if (J + 1 < nt && ftile[J + 1] <= J) emit(4, J + 1, J + 1, J);
     for (int o = 2; o <= omax; o++)
       if (ftile[J + o] <= J)
