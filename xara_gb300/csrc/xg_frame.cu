@@ -536,6 +536,7 @@ struct FbcSmem {
   double Se[6], kv[36], SeT[6], kvT[36], f[36], vr[6];
   double vs[kMaxIp][4], fs[kMaxIp][16], Ssr[kMaxIp][4];
   double vsS[kMaxIp][4], fsS[kMaxIp][16], SsrS[kMaxIp][4];
+  double dvsS[kMaxIp][4];
 };
 
 // ForceBeamColumn2d::update (element/Frame/Other/Force/ForceBeamColumn2d.cpp:
@@ -677,26 +678,41 @@ __global__ void __launch_bounds__(32 * WARPS) k_fbc_update(FrameView v) {
           // f += b' fs b wL ; vr += b' (vs + dvs) wL.  Each column a of the
           // force interpolation b has one entry: row kRow[a], value ca[a]
           // (ForceBeamColumn3d::getForceInterpolatMatrix, :1068-1110).
-          // the sections' terms summed in section order from their groups'
-          // first lanes
-          constexpr int kRow[6] = {0, 1, 1, 2, 2, 3};
-          const double ca[6] = {1.0, xL1, xL, xL1, xL, 1.0};
-          double fc[NB * NB], vc[NB];
+          if (sec_on && sec_rank == 0) {
 #pragma unroll
-          for (int a = 0; a < NB; a++) {
-            const double wa = ca[a] * wtL;
-#pragma unroll
-            for (int c = 0; c < NB; c++) fc[a * NB + c] = wa * (fsec[kRow[a] * ORD + kRow[c]] * ca[c]);
-            vc[a] = wa * dvs[kRow[a]];
+            for (int r = 0; r < ORD; r++) S.dvsS[ip][r] = dvs[r];
           }
-          for (int g = 0; g < nip; g++) {
-            const int src = g * sec_G;
-#pragma unroll
-            for (int i = 0; i < NB * NB; i++) f[i] += __shfl_sync(0xffffffffu, fc[i], src);
-#pragma unroll
-            for (int i = 0; i < NB; i++) vr[i] += __shfl_sync(0xffffffffu, vc[i], src);
+          (void)wtL;
+        }
+        // f += b' fs b wL and vr += b' (vs + dvs) wL over the sections, in
+        // section order: one entry per lane from the sections' flexibilities
+        // and deformations in shared memory.  Each column a of the force
+        // interpolation b has one entry: row kRow[a], value ca[a]
+        // (ForceBeamColumn3d::getForceInterpolatMatrix, :1068-1110).
+        __syncwarp();
+        {
+          // kRow = {0, 1, 1, 2, 2, 3} = (a + 1) / 2; ca = {1, xL-1, xL, xL-1, xL, 1}
+          for (int i = lane; i < NB * NB + NB; i += 32) {
+            const bool isf = i < NB * NB;
+            const int a = isf ? i / NB : i - NB * NB, c = isf ? i % NB : 0;
+            const int ra = (a + 1) >> 1, rc = (c + 1) >> 1;
+            double acc = 0.0;
+            for (int ip = 0; ip < nip; ip++) {
+              const double xL = v.xi[ip], xL1 = xL - 1.0, wtL = v.wt[ip] * L;
+              const double caa = (a == 0 || a == 5) ? 1.0 : ((a & 1) ? xL1 : xL);
+              const double cac = (c == 0 || c == 5) ? 1.0 : ((c & 1) ? xL1 : xL);
+              const double wa = caa * wtL;
+              acc += isf ? wa * (S.fsS[ip][ra * ORD + rc] * cac) : wa * S.dvsS[ip][ra];
+            }
+            if (isf) S.f[i] = acc;
+            else S.vr[a] = acc;
           }
         }
+        __syncwarp();
+#pragma unroll
+        for (int i = 0; i < NB * NB; i++) f[i] = S.f[i];
+#pragma unroll
+        for (int i = 0; i < NB; i++) vr[i] = S.vr[i];
         double kvT[NB * NB];
         elem_inverse<NB>(f, kvT);
         double dvv[NB], dW = 0.0;
