@@ -985,9 +985,45 @@ def run_brick(args):
     dt = max_over_ranks(dt, world, torch, dist)
     value = npts * args.steps * world / dt
 
+    # a whole Newton iteration: the element phase, then the block-Jacobi PCG
+    # solve of the assembled tangent to rtol 1e-10 (the configuration's
+    # `system CudaBJPCG`), the right-hand side the assembled residual
+    L = gpu.lib()
+    L.xg_soe_solve_device.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_double, C.c_int,
+                                      C.POINTER(C.c_int), C.POINTER(C.c_double)]
+    bdev = torch.empty(m.neq, dtype=torch.float64, device="cuda")
+    xdev = torch.empty(m.neq, dtype=torch.float64, device="cuda")
+    newton = None
+    if not args.no_analysis:
+        gen = torch.Generator(device="cpu").manual_seed(3)
+        bdev.copy_(torch.randn(m.neq, generator=gen, dtype=torch.float64))
+        it_c, rr_c = C.c_int(), C.c_double()
+        gpu.profile_enable(m, True)
+        t_it = []
+        for k in range(2):
+            barrier()
+            ev0.record(stream)
+            m.update(False, False)
+            gpu._check(L.xg_soe_solve_device(m.h, C.c_void_p(bdev.data_ptr()),
+                                             C.c_void_p(xdev.data_ptr()), 1e-10, 20000,
+                                             C.byref(it_c), C.byref(rr_c)))
+            ev1.record(stream)
+            barrier()
+            t_it.append(ev0.elapsed_time(ev1) * 1e-3)
+        gpu.profile_enable(m, False)
+        pcg_it = it_c.value
+        pcg_bytes = 12 * m.nnz + 100 * m.neq       # per PCG iteration
+        pcg_s = t_it[-1] - dt / args.steps         # the iteration less its element phase
+        newton = {"newton_iters_per_s": 1.0 / t_it[-1], "ms_per_newton_iteration": 1e3 * t_it[-1],
+                  "pcg_iterations": pcg_it, "pcg_relative_residual": rr_c.value,
+                  "pcg_ms": 1e3 * pcg_s, "pcg_ms_per_iteration": 1e3 * pcg_s / max(pcg_it, 1),
+                  "pcg_GBps": pcg_bytes * pcg_it / pcg_s / 1e9 if pcg_s > 0 else None,
+                  "pcg_bytes_per_iteration": pcg_bytes,
+                  "rhs": "seeded random right-hand side, x0 = 0, rtol 1e-10",
+                  "ip_updates_per_s": npts / t_it[-1]}
+
     Uh = torch.from_numpy(U).pin_memory()
     resid = torch.empty(m.neq, dtype=torch.float64).pin_memory()
-    L = gpu.lib()
     ph = C.c_void_p(Uh.data_ptr())
     pr = C.c_void_p(resid.data_ptr())
     for _ in range(2):
@@ -1038,7 +1074,10 @@ def run_brick(args):
         "kernels_ms_per_step": {k: v[0] / args.steps for k, v in kernels.items()},
         "clocks": clocks,
         "setup_s": t_setup,
+        "newton_iteration": newton,
     }
+    if newton and newton.get("pcg_GBps") and peak:
+        newton["pcg_roofline_frac"] = newton["pcg_GBps"] / peak
     if not args.no_cpu_baseline:
         rate, sample = brick_cpu_sample()
         line["cpu_baseline"] = {"value": rate, "unit": UNIT, "cores": 1, "kind": "port",
