@@ -95,6 +95,9 @@ struct ProfileSystem {
   int *sweep_flags;        // [2*nt] rows solved in the forward / backward sweep
   int *flags;              // [4]
   double min_diag_tol;
+  // per tile row J, for the substitutions: W_J = L_JJ^-T, F_J = L_JJ^-1
+  // L_J,J-1 and G_J = L_JJ^-T L_J+1,J' (row-major 32 x 32 each, [nt*1024])
+  double *Winv, *F, *G;
 };
 int profile_plan(int n, const int *rowptr, const int *colidx, std::vector<int> &ftile, int &nt,
                  int &W);

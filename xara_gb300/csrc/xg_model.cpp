@@ -165,7 +165,7 @@ struct xg_model {
   bool prof_ready = false, prof_factored = false;
   std::vector<int> ftile;
   DBuf<int> d_ftile, d_pflags, d_ptasks, d_pnext, d_pupd, d_pdone, d_psweep;
-  DBuf<double> d_L, d_invD, d_piv, d_px;
+  DBuf<double> d_L, d_invD, d_piv, d_px, d_Winv, d_Fc, d_Gc;
   int prof_ldx = 0;
   bool prof_band = false;                      // many small parts: one band each
   BandSystem bsys{};
@@ -1305,6 +1305,9 @@ int xg_model::ensure_profile() {
   RET(d_ftile.upload(ftile.data(), ftile.size(), stream));
   RET(d_ptasks.upload(tasks.data(), tasks.size(), stream));
   RET(d_L.alloc(tiles));
+  RET(d_Winv.alloc((size_t)nt * 1024));
+  RET(d_Fc.alloc((size_t)nt * 1024));
+  RET(d_Gc.alloc((size_t)nt * 1024));
   RET(d_invD.alloc((size_t)nt * 32));
   RET(d_piv.alloc((size_t)nt * 32));
   prof_ldx = nt * 32;
@@ -1319,6 +1322,7 @@ int xg_model::ensure_profile() {
   psys.n = neq; psys.nt = nt; psys.W = W;
   psys.rowptr = d_rowptr.p; psys.colidx = d_colidx.p; psys.vals = d_vals.p;
   psys.ftile = d_ftile.p; psys.L = d_L.p; psys.invD = d_invD.p; psys.piv = d_piv.p;
+  psys.Winv = d_Winv.p; psys.F = d_Fc.p; psys.G = d_Gc.p;
   psys.tasks = reinterpret_cast<const int4 *>(d_ptasks.p);
   psys.ntasks = (int)(tasks.size() / 4);
   psys.next_task = d_pnext.p; psys.upd = d_pupd.p; psys.done = d_pdone.p;

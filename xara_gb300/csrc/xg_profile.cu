@@ -296,6 +296,61 @@ __device__ bool panel_update_task(const ProfileSystem &S, int J, int q, double (
   return true;
 }
 
+// For the substitutions, off the factorisation's critical path: W_J =
+// L_JJ^-T (rows r of W solve w L_JJ' = e_r, a warp per row as in phase B),
+// F_J = L_JJ^-1 L_J,J-1 = W' L_J,J-1 and G_J = L_JJ^-T L_J+1,J' = W
+// L_J+1,J' (zero where the tile is outside the envelope).  The sweeps then
+// need one 32 x 32 product with the neighbouring row's result on their
+// dependency chain.
+__device__ void coupling_task(const ProfileSystem &S, int J, double (*sA)[kT + 1],
+                              double (*sB)[kT + 1], double (*sC)[kT + 1]) {
+  const int tid = threadIdx.x, w = tid >> 5, lane = tid & 31;
+  const double *Ljj = tile_at(S, J, 0);
+  for (int k = tid; k < kTT; k += blockDim.x) sB[k >> 5][k & 31] = __ldcg(Ljj + k);
+  __syncthreads();
+  // W = I L^-T: warp w takes rows w, w+8, w+16, w+24
+  for (int r = w; r < kT; r += blockDim.x / 32) {
+    double x = lane == r ? 1.0 : 0.0;
+    for (int c = 0; c < kT - 1; c++) {
+      const double wc = __shfl_sync(0xffffffffu, x, c);
+      if (lane > c) x = fma(-wc, sB[lane][c], x);
+    }
+    sA[r][lane] = x;
+    S.Winv[(size_t)J * kTT + r * kT + lane] = x;
+  }
+  __syncthreads();
+  for (int pass = 0; pass < 2; pass++) {
+    // pass 0: F = W' P, P = L_J,J-1;  pass 1: G = W Q', Q = L_J+1,J
+    const bool has = pass == 0 ? (J >= 1 && S.ftile[J] <= J - 1)
+                               : (J + 1 < S.nt && S.ftile[J + 1] <= J);
+    double *out = (pass == 0 ? S.F : S.G) + (size_t)J * kTT;
+    if (!has) {
+      for (int k = tid; k < kTT; k += blockDim.x) out[k] = 0.0;
+      continue;
+    }
+    const double *T = pass == 0 ? tile_at(S, J, 1) : tile_at(S, J + 1, 1);
+    for (int k = tid; k < kTT; k += blockDim.x) sC[k >> 5][k & 31] = __ldcg(T + k);
+    __syncthreads();
+    for (int k = tid; k < kTT; k += blockDim.x) {
+      const int i = k >> 5, c = k & 31;
+      double a0 = 0.0, a1 = 0.0;
+      if (pass == 0) {
+        for (int q = 0; q < kT; q += 2) {
+          a0 = fma(sA[q][i], sC[q][c], a0);
+          a1 = fma(sA[q + 1][i], sC[q + 1][c], a1);
+        }
+      } else {
+        for (int q = 0; q < kT; q += 2) {
+          a0 = fma(sA[i][q], sC[c][q], a0);
+          a1 = fma(sA[i][q + 1], sC[c][q + 1], a1);
+        }
+      }
+      out[k] = a0 + a1;
+    }
+    __syncthreads();
+  }
+}
+
 // Phase C on pair (I = J+a, K = J+b), b <= a: A_IK -= (L_IJ D_J) L_KJ'.
 __device__ void pair_update(const ProfileSystem &S, int J, int a, int b, double (*sA)[kT + 1],
                             double (*sB)[kT + 1]) {
@@ -375,6 +430,11 @@ __device__ bool wait_task(const ProfileSystem &S, int4 t, volatile int *flags) {
   if (type == 5)
     return wait_geq(S.done + slot_of(S, J, 0), 1, flags) &&
            wait_geq(S.upd + slot_of(S, I, 1), J - max(S.ftile[I], S.ftile[J]), flags);
+  if (type == 6)
+    return wait_geq(S.done + slot_of(S, J, 0), 1, flags) &&
+           (J < 1 || S.ftile[J] > J - 1 || wait_geq(S.done + slot_of(S, J, 1), kPanelParts, flags)) &&
+           (J + 1 >= S.nt || S.ftile[J + 1] > J ||
+            wait_geq(S.done + slot_of(S, J + 1, 1), kPanelParts, flags));
   if (type == 1)
     return wait_geq(S.done + slot_of(S, J, 0), 1, flags) &&
            wait_geq(S.upd + slot_of(S, I, I - J), J - max(S.ftile[I], S.ftile[J]), flags);
@@ -406,8 +466,10 @@ __global__ void __launch_bounds__(kFactorThreads) k_prof_factor(ProfileSystem S)
       pair_update(S, t.w, t.y - t.w, t.z - t.w, sA, sB);
     } else if (t.x == 4) {
       fine = chain_task(S, t.w, sC, flags);
-    } else {
+    } else if (t.x == 5) {
       fine = panel_update_task(S, t.w, t.z, sA, sB, flags);
+    } else {
+      coupling_task(S, t.w, sA, sB, sC);
     }
     if (!fine) break;
     __syncthreads();
@@ -521,13 +583,14 @@ __global__ void __launch_bounds__(kSolveBlock) k_prof_solve(ProfileSystem S, int
 
 // Pipelined substitutions on kPipeBlocks co-resident blocks (cooperative
 // launch): block b owns the tile rows J = b, b + P, ... .  Forward, in
-// increasing J: the contributions of the solved tiles J-o (oldest first)
-// are accumulated as each tile's flag appears, then the diagonal tile is
-// solved and its flag set; the tile of the newest dependency and the
-// diagonal tile are loaded before the wait, so a row costs about one flag
-// round trip plus the 32-step shuffle solve.  Backward, in decreasing J:
-// z_J = D^-1 y_J, minus the transposed contributions of the rows below,
-// then the unit upper solve.  Waits are bounded by the global timer.
+// increasing J: r_J = b_J minus the contributions of the solved rows J-o,
+// o >= 2 (accumulated as each row's flag appears), c_J = L_JJ^-1 r_J, and
+// y_J = c_J - F_J y_J-1 with the factorisation's coupling matrices; only the
+// last 32 x 32 product waits for the previous row, so a row of the chain
+// costs one flag round trip plus a short reduction instead of a 32-step
+// triangular solve.  Backward, in decreasing J: x_J = L_JJ^-T (D_J^-1 y_J
+// minus the transposed contributions of rows J+o, o >= 2) - G_J x_J+1.
+// Waits are bounded by the global timer.
 constexpr int kPipeBlocks = 64;
 constexpr int kPipeThreads = 256;
 
@@ -538,20 +601,24 @@ __device__ __forceinline__ bool wait_flag(const int *p, volatile int *flags) {
 __global__ void __launch_bounds__(kPipeThreads) k_prof_solve_pipe(ProfileSystem S, int nrhs,
                                                                   double *x, int ldx,
                                                                   int *fdone, int *bdone) {
-  __shared__ double sL[kT][kT + 1];
-  __shared__ double part[4][kT];
+  __shared__ double rv[4][kT], cv[4][kT];
   __shared__ int ok;
   volatile int *flags = S.flags;
-  const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
+  const int tid = threadIdx.x;
   const int r = tid >> 3, g = tid & 7;          // tile row, column group (4 columns)
   const int nt = S.nt, W = S.W, P = gridDim.x;
-  // ---------------- forward
+  // reduce over the eight column groups of a row (lanes r*8 .. r*8+7)
+  auto group_sum = [](double v) {
+    v += __shfl_xor_sync(0xffffffffu, v, 4);
+    v += __shfl_xor_sync(0xffffffffu, v, 2);
+    v += __shfl_xor_sync(0xffffffffu, v, 1);
+    return v;
+  };
+  // ---------------- forward: y_J = W_J' (b_J - sum_{o>=2} L_J,J-o y_J-o) - F_J y_J-1
   for (int J = blockIdx.x; J < nt; J += P) {
-    const double *Ld = tile_at(S, J, 0);
-    for (int k = tid; k < kTT; k += kPipeThreads) sL[k >> 5][k & 31] = __ldcg(Ld + k);
     double acc[4] = {0.0, 0.0, 0.0, 0.0};
     const int ohi = min(W, J - S.ftile[J]);
-    for (int o = ohi; o >= 1; o--) {
+    for (int o = ohi; o >= 2; o--) {
       const double *Lt = tile_at(S, J, o) + r * kT + g;
       const double l0 = __ldcg(Lt), l1 = __ldcg(Lt + 8), l2 = __ldcg(Lt + 16), l3 = __ldcg(Lt + 24);
       if (tid == 0) ok = wait_flag(fdone + (J - o), flags) ? 1 : 0;
@@ -564,39 +631,58 @@ __global__ void __launch_bounds__(kPipeThreads) k_prof_solve_pipe(ProfileSystem 
       }
     }
     for (int q = 0; q < nrhs; q++) {
-      double v = acc[q];
-      v += __shfl_xor_sync(0xffffffffu, v, 4);
-      v += __shfl_xor_sync(0xffffffffu, v, 2);
-      v += __shfl_xor_sync(0xffffffffu, v, 1);
-      if (g == 0) part[q][r] = v;
+      const double v = group_sum(acc[q]);
+      if (g == 0) rv[q][r] = __ldcg(x + (size_t)q * ldx + J * kT + r) - v;
     }
     __syncthreads();
-    if (w < nrhs) {
-      const int q = w;
-      double v = __ldcg(x + (size_t)q * ldx + J * kT + lane) - part[q][lane];
-      for (int c = 0; c < kT - 1; c++) {
-        const double yc = __shfl_sync(0xffffffffu, v, c);
-        if (lane > c) v -= sL[lane][c] * yc;
-      }
-      x[(size_t)q * ldx + J * kT + lane] = v;
-      __threadfence();
+    // c = W' rhs, and F's entries ahead of the wait for row J-1
+    const double *Wt = S.Winv + (size_t)J * kTT, *Ft = S.F + (size_t)J * kTT;
+    double wv[4], fv[4];
+#pragma unroll
+    for (int m = 0; m < 4; m++) {
+      wv[m] = __ldcg(Wt + (g + 8 * m) * kT + r);
+      fv[m] = __ldcg(Ft + r * kT + g + 8 * m);
     }
+    for (int q = 0; q < nrhs; q++) {
+      double t = 0.0;
+#pragma unroll
+      for (int m = 0; m < 4; m++) t = fma(wv[m], rv[q][g + 8 * m], t);
+      t = group_sum(t);
+      if (g == 0) cv[q][r] = t;
+    }
+    const bool hasF = J >= 1 && S.ftile[J] <= J - 1;
+    if (hasF) {
+      if (tid == 0) ok = wait_flag(fdone + (J - 1), flags) ? 1 : 0;
+      __syncthreads();
+      if (!ok) return;
+    } else {
+      __syncthreads();
+    }
+    for (int q = 0; q < nrhs; q++) {
+      double t = 0.0;
+      if (hasF) {
+        const double *yp = x + (size_t)q * ldx + (J - 1) * kT + g;
+#pragma unroll
+        for (int m = 0; m < 4; m++) t = fma(fv[m], __ldcg(yp + 8 * m), t);
+      }
+      t = group_sum(t);
+      if (g == 0) x[(size_t)q * ldx + J * kT + r] = cv[q][r] - t;
+    }
+    __threadfence();
     __syncthreads();
     if (tid == 0) {
       __threadfence();
       atomicExch(fdone + J, 1);
     }
   }
-  // ---------------- backward
+  // ---------------- backward: x_J = W_J (D_J^-1 y_J - sum_{o>=2} L_J+o,J' x_J+o) - G_J x_J+1
   const int jlast = blockIdx.x + ((nt - 1 - (int)blockIdx.x) / P) * P;
   for (int J = jlast; J >= 0; J -= P) {
     if (J >= nt) continue;
-    const double *Ld = tile_at(S, J, 0);
-    for (int k = tid; k < kTT; k += kPipeThreads) sL[k >> 5][k & 31] = __ldcg(Ld + k);
     double acc[4] = {0.0, 0.0, 0.0, 0.0};
     const int ohi = min(W, nt - 1 - J);
     // column c = r of the result; rows g, g+8, g+16, g+24 of tile (J+o, J)
-    for (int o = ohi; o >= 1; o--) {
+    for (int o = ohi; o >= 2; o--) {
       if (S.ftile[J + o] > J) continue;
       const double *Lt = tile_at(S, J + o, o) + r;
       const double l0 = __ldcg(Lt + g * kT), l1 = __ldcg(Lt + (g + 8) * kT);
@@ -612,25 +698,45 @@ __global__ void __launch_bounds__(kPipeThreads) k_prof_solve_pipe(ProfileSystem 
       }
     }
     for (int q = 0; q < nrhs; q++) {
-      double v = acc[q];
-      v += __shfl_xor_sync(0xffffffffu, v, 4);
-      v += __shfl_xor_sync(0xffffffffu, v, 2);
-      v += __shfl_xor_sync(0xffffffffu, v, 1);
-      if (g == 0) part[q][r] = v;
+      const double v = group_sum(acc[q]);
+      // z_J = D^-1 y_J (ProfileSPD divides by the pivots before the back sweep)
+      if (g == 0)
+        rv[q][r] = __ldcg(x + (size_t)q * ldx + J * kT + r) * S.invD[J * kT + r] - v;
     }
     __syncthreads();
-    if (w < nrhs) {
-      const int q = w;
-      // z_J = D^-1 y_J (ProfileSPD divides by the pivots before the back sweep)
-      const double z = __ldcg(x + (size_t)q * ldx + J * kT + lane) * S.invD[J * kT + lane];
-      double v = z - part[q][lane];
-      for (int cc = kT - 1; cc > 0; cc--) {
-        const double xc = __shfl_sync(0xffffffffu, v, cc);
-        if (lane < cc) v -= sL[cc][lane] * xc;
-      }
-      x[(size_t)q * ldx + J * kT + lane] = v;
-      __threadfence();
+    const double *Wt = S.Winv + (size_t)J * kTT, *Gt = S.G + (size_t)J * kTT;
+    double wv[4], gv[4];
+#pragma unroll
+    for (int m = 0; m < 4; m++) {
+      wv[m] = __ldcg(Wt + r * kT + g + 8 * m);
+      gv[m] = __ldcg(Gt + r * kT + g + 8 * m);
     }
+    for (int q = 0; q < nrhs; q++) {
+      double t = 0.0;
+#pragma unroll
+      for (int m = 0; m < 4; m++) t = fma(wv[m], rv[q][g + 8 * m], t);
+      t = group_sum(t);
+      if (g == 0) cv[q][r] = t;
+    }
+    const bool hasG = J + 1 < nt && S.ftile[J + 1] <= J;
+    if (hasG) {
+      if (tid == 0) ok = wait_flag(bdone + (J + 1), flags) ? 1 : 0;
+      __syncthreads();
+      if (!ok) return;
+    } else {
+      __syncthreads();
+    }
+    for (int q = 0; q < nrhs; q++) {
+      double t = 0.0;
+      if (hasG) {
+        const double *xn = x + (size_t)q * ldx + (J + 1) * kT + g;
+#pragma unroll
+        for (int m = 0; m < 4; m++) t = fma(gv[m], __ldcg(xn + 8 * m), t);
+      }
+      t = group_sum(t);
+      if (g == 0) x[(size_t)q * ldx + J * kT + r] = cv[q][r] - t;
+    }
+    __threadfence();
     __syncthreads();
     if (tid == 0) {
       __threadfence();
@@ -698,8 +804,10 @@ void profile_tasks(int nt, int W, const std::vector<int> &ftile, std::vector<int
         for (int q = 0; q < kPanelParts; q++) emit(1, J + o, q, J);
     updates(J, 1, 1);
     updates(J - 1, 3, W);
+    if (J >= 2) emit(6, J - 2, J - 2, J - 2);
   }
   updates(nt - 1, 2, W);
+  for (int J = std::max(nt - 2, 0); J < nt; J++) emit(6, J, J, J);
 }
 
 size_t profile_tile_doubles(int nt, int W) { return (size_t)nt * (W + 1) * kTT; }
