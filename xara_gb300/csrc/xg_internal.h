@@ -92,7 +92,7 @@ struct ProfileSystem {
   int ntasks;
   int *next_task;          // [1] task counter
   int *upd, *done;         // [nt*(W+1)] per tile: updates applied, factored
-  int *sweep_flags;        // [2*nt] rows solved in the forward / backward sweep
+  double *sweep;           // [2*4*nt*32] values published by the forward / backward sweep
   int *flags;              // [4]
   double min_diag_tol;
   // per tile row J, for the substitutions: W_J = L_JJ^-T, F_J = L_JJ^-1

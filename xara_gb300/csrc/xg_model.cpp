@@ -164,8 +164,8 @@ struct xg_model {
   ProfileSystem psys{};
   bool prof_ready = false, prof_factored = false;
   std::vector<int> ftile;
-  DBuf<int> d_ftile, d_pflags, d_ptasks, d_pnext, d_pupd, d_pdone, d_psweep;
-  DBuf<double> d_L, d_invD, d_piv, d_px, d_Winv, d_Fc, d_Gc;
+  DBuf<int> d_ftile, d_pflags, d_ptasks, d_pnext, d_pupd, d_pdone;
+  DBuf<double> d_L, d_invD, d_piv, d_px, d_Winv, d_Fc, d_Gc, d_psweep;
   int prof_ldx = 0;
   bool prof_band = false;                      // many small parts: one band each
   BandSystem bsys{};
@@ -1317,8 +1317,8 @@ int xg_model::ensure_profile() {
   RET(d_pupd.alloc((size_t)nt * (W + 1)));
   RET(d_pdone.alloc((size_t)nt * (W + 1)));
   RET(d_pflags.alloc(4));
-  RET(d_psweep.alloc(2 * (size_t)std::max(nt, 1)));
-  psys.sweep_flags = d_psweep.p;
+  RET(d_psweep.alloc(2 * 4 * (size_t)std::max(nt, 1) * 32));
+  psys.sweep = d_psweep.p;
   psys.n = neq; psys.nt = nt; psys.W = W;
   psys.rowptr = d_rowptr.p; psys.colidx = d_colidx.p; psys.vals = d_vals.p;
   psys.ftile = d_ftile.p; psys.L = d_L.p; psys.invD = d_invD.p; psys.piv = d_piv.p;

@@ -584,29 +584,67 @@ __global__ void __launch_bounds__(kSolveBlock) k_prof_solve(ProfileSystem S, int
 // Pipelined substitutions on kPipeBlocks co-resident blocks (cooperative
 // launch): block b owns the tile rows J = b, b + P, ... .  Forward, in
 // increasing J: r_J = b_J minus the contributions of the solved rows J-o,
-// o >= 2 (accumulated as each row's flag appears), c_J = L_JJ^-1 r_J, and
-// y_J = c_J - F_J y_J-1 with the factorisation's coupling matrices; only the
-// last 32 x 32 product waits for the previous row, so a row of the chain
-// costs one flag round trip plus a short reduction instead of a 32-step
-// triangular solve.  Backward, in decreasing J: x_J = L_JJ^-T (D_J^-1 y_J
-// minus the transposed contributions of rows J+o, o >= 2) - G_J x_J+1.
-// Waits are bounded by the global timer.
+// o >= 2, c_J = L_JJ^-1 r_J, and y_J = c_J - F_J y_J-1 with the
+// factorisation's coupling matrices, so only the last 32 x 32 product waits
+// for the previous row.  Backward, in decreasing J: x_J = L_JJ^-T (D_J^-1
+// y_J minus the transposed contributions of rows J+o, o >= 2) - G_J x_J+1.
+// There are no row flags: every solved value is published to a scratch
+// vector filled with kUnset beforehand (a NaN pattern that no arithmetic
+// result is stored as), and a consumer thread polls exactly the values it
+// reads, so the chain costs one store-to-load hop per row.  Waits are
+// bounded by the global timer.
 constexpr int kPipeBlocks = 64;
 constexpr int kPipeThreads = 256;
+constexpr unsigned long long kUnset = 0xFFFFFFFFFFFFFFFFull;   // byte fill 0xFF
 
-__device__ __forceinline__ bool wait_flag(const int *p, volatile int *flags) {
-  return wait_geq(p, 1, flags);
+__device__ __forceinline__ double ld_relaxed(const double *p) {
+  double v;
+  asm volatile("ld.relaxed.gpu.global.f64 %0, [%1];" : "=d"(v) : "l"(p));
+  return v;
+}
+
+// *p once its producer has published it; 0 after a failed wait (flags[0]
+// is then nonzero and the host reports the solve as failed)
+__device__ __forceinline__ double await_value(const double *p, volatile int *flags) {
+  double v = ld_relaxed(p);
+  if ((unsigned long long)__double_as_longlong(v) != kUnset) return v;
+  const unsigned long long t0 = global_ns();
+  for (;;) {
+    v = ld_relaxed(p);
+    if ((unsigned long long)__double_as_longlong(v) != kUnset) return v;
+    if (flags[0] != 0) return 0.0;
+    if (global_ns() - t0 > kBarrierTimeoutNs) {
+      flags[0] = 2;
+      return 0.0;
+    }
+  }
+}
+
+// p[0], p[8], p[16], p[24] (the four loads in flight together)
+__device__ __forceinline__ void await4(const double *p, double v[4], volatile int *flags) {
+  bool ready = true;
+#pragma unroll
+  for (int m = 0; m < 4; m++) v[m] = ld_relaxed(p + 8 * m);
+#pragma unroll
+  for (int m = 0; m < 4; m++) ready &= (unsigned long long)__double_as_longlong(v[m]) != kUnset;
+  if (!ready)
+    for (int m = 0; m < 4; m++) v[m] = await_value(p + 8 * m, flags);
+}
+
+__device__ __forceinline__ void publish(double *p, double v) {
+  if ((unsigned long long)__double_as_longlong(v) == kUnset)
+    v = __longlong_as_double(0x7FF8000000000000ll);   // keep a NaN a NaN
+  asm volatile("st.relaxed.gpu.global.f64 [%0], %1;" ::"l"(p), "d"(v) : "memory");
 }
 
 __global__ void __launch_bounds__(kPipeThreads) k_prof_solve_pipe(ProfileSystem S, int nrhs,
                                                                   double *x, int ldx,
-                                                                  int *fdone, int *bdone) {
-  __shared__ double rv[4][kT], cv[4][kT];
-  __shared__ int ok;
+                                                                  double *ys, double *xs) {
+  __shared__ double rv[2][4][kT];
   volatile int *flags = S.flags;
   const int tid = threadIdx.x;
   const int r = tid >> 3, g = tid & 7;          // tile row, column group (4 columns)
-  const int nt = S.nt, W = S.W, P = gridDim.x;
+  const int nt = S.nt, W = S.W, P = gridDim.x, ls = nt * kT;
   // reduce over the eight column groups of a row (lanes r*8 .. r*8+7)
   auto group_sum = [](double v) {
     v += __shfl_xor_sync(0xffffffffu, v, 4);
@@ -614,28 +652,25 @@ __global__ void __launch_bounds__(kPipeThreads) k_prof_solve_pipe(ProfileSystem 
     v += __shfl_xor_sync(0xffffffffu, v, 1);
     return v;
   };
+  int it = 0;                                   // rv is double-buffered by iteration
   // ---------------- forward: y_J = W_J' (b_J - sum_{o>=2} L_J,J-o y_J-o) - F_J y_J-1
-  for (int J = blockIdx.x; J < nt; J += P) {
+  for (int J = blockIdx.x; J < nt; J += P, it++) {
     double acc[4] = {0.0, 0.0, 0.0, 0.0};
     const int ohi = min(W, J - S.ftile[J]);
     for (int o = ohi; o >= 2; o--) {
       const double *Lt = tile_at(S, J, o) + r * kT + g;
       const double l0 = __ldcg(Lt), l1 = __ldcg(Lt + 8), l2 = __ldcg(Lt + 16), l3 = __ldcg(Lt + 24);
-      if (tid == 0) ok = wait_flag(fdone + (J - o), flags) ? 1 : 0;
-      __syncthreads();
-      if (!ok) return;
-      const int c0 = (J - o) * kT + g;
       for (int q = 0; q < nrhs; q++) {
-        const double *y = x + (size_t)q * ldx + c0;
-        acc[q] += l0 * __ldcg(y) + l1 * __ldcg(y + 8) + l2 * __ldcg(y + 16) + l3 * __ldcg(y + 24);
+        double y[4];
+        await4(ys + (size_t)q * ls + (J - o) * kT + g, y, flags);
+        acc[q] += l0 * y[0] + l1 * y[1] + l2 * y[2] + l3 * y[3];
       }
     }
+    double(*rb)[kT] = rv[it & 1];
     for (int q = 0; q < nrhs; q++) {
       const double v = group_sum(acc[q]);
-      if (g == 0) rv[q][r] = __ldcg(x + (size_t)q * ldx + J * kT + r) - v;
+      if (g == 0) rb[q][r] = __ldcg(x + (size_t)q * ldx + J * kT + r) - v;
     }
-    __syncthreads();
-    // c = W' rhs, and F's entries ahead of the wait for row J-1
     const double *Wt = S.Winv + (size_t)J * kTT, *Ft = S.F + (size_t)J * kTT;
     double wv[4], fv[4];
 #pragma unroll
@@ -643,41 +678,27 @@ __global__ void __launch_bounds__(kPipeThreads) k_prof_solve_pipe(ProfileSystem 
       wv[m] = __ldcg(Wt + (g + 8 * m) * kT + r);
       fv[m] = __ldcg(Ft + r * kT + g + 8 * m);
     }
-    for (int q = 0; q < nrhs; q++) {
-      double t = 0.0;
-#pragma unroll
-      for (int m = 0; m < 4; m++) t = fma(wv[m], rv[q][g + 8 * m], t);
-      t = group_sum(t);
-      if (g == 0) cv[q][r] = t;
-    }
+    __syncthreads();
     const bool hasF = J >= 1 && S.ftile[J] <= J - 1;
-    if (hasF) {
-      if (tid == 0) ok = wait_flag(fdone + (J - 1), flags) ? 1 : 0;
-      __syncthreads();
-      if (!ok) return;
-    } else {
-      __syncthreads();
-    }
     for (int q = 0; q < nrhs; q++) {
+      double c = 0.0;
+#pragma unroll
+      for (int m = 0; m < 4; m++) c = fma(wv[m], rb[q][g + 8 * m], c);
+      c = group_sum(c);
       double t = 0.0;
       if (hasF) {
-        const double *yp = x + (size_t)q * ldx + (J - 1) * kT + g;
+        double y[4];
+        await4(ys + (size_t)q * ls + (J - 1) * kT + g, y, flags);
 #pragma unroll
-        for (int m = 0; m < 4; m++) t = fma(fv[m], __ldcg(yp + 8 * m), t);
+        for (int m = 0; m < 4; m++) t = fma(fv[m], y[m], t);
       }
       t = group_sum(t);
-      if (g == 0) x[(size_t)q * ldx + J * kT + r] = cv[q][r] - t;
-    }
-    __threadfence();
-    __syncthreads();
-    if (tid == 0) {
-      __threadfence();
-      atomicExch(fdone + J, 1);
+      if (g == 0) publish(ys + (size_t)q * ls + J * kT + r, c - t);
     }
   }
   // ---------------- backward: x_J = W_J (D_J^-1 y_J - sum_{o>=2} L_J+o,J' x_J+o) - G_J x_J+1
   const int jlast = blockIdx.x + ((nt - 1 - (int)blockIdx.x) / P) * P;
-  for (int J = jlast; J >= 0; J -= P) {
+  for (int J = jlast; J >= 0; J -= P, it++) {
     if (J >= nt) continue;
     double acc[4] = {0.0, 0.0, 0.0, 0.0};
     const int ohi = min(W, nt - 1 - J);
@@ -687,23 +708,20 @@ __global__ void __launch_bounds__(kPipeThreads) k_prof_solve_pipe(ProfileSystem 
       const double *Lt = tile_at(S, J + o, o) + r;
       const double l0 = __ldcg(Lt + g * kT), l1 = __ldcg(Lt + (g + 8) * kT);
       const double l2 = __ldcg(Lt + (g + 16) * kT), l3 = __ldcg(Lt + (g + 24) * kT);
-      if (tid == 0) ok = wait_flag(bdone + (J + o), flags) ? 1 : 0;
-      __syncthreads();
-      if (!ok) return;
-      const int r0 = (J + o) * kT + g;
       for (int q = 0; q < nrhs; q++) {
-        const double *xr = x + (size_t)q * ldx + r0;
-        acc[q] += l0 * __ldcg(xr) + l1 * __ldcg(xr + 8) + l2 * __ldcg(xr + 16) +
-                  l3 * __ldcg(xr + 24);
+        double xv[4];
+        await4(xs + (size_t)q * ls + (J + o) * kT + g, xv, flags);
+        acc[q] += l0 * xv[0] + l1 * xv[1] + l2 * xv[2] + l3 * xv[3];
       }
     }
+    double(*rb)[kT] = rv[it & 1];
     for (int q = 0; q < nrhs; q++) {
       const double v = group_sum(acc[q]);
-      // z_J = D^-1 y_J (ProfileSPD divides by the pivots before the back sweep)
+      // z_J = D^-1 y_J (ProfileSPD divides by the pivots before the back
+      // sweep); y_J[r] was published by this same thread in the forward sweep
       if (g == 0)
-        rv[q][r] = __ldcg(x + (size_t)q * ldx + J * kT + r) * S.invD[J * kT + r] - v;
+        rb[q][r] = ld_relaxed(ys + (size_t)q * ls + J * kT + r) * S.invD[J * kT + r] - v;
     }
-    __syncthreads();
     const double *Wt = S.Winv + (size_t)J * kTT, *Gt = S.G + (size_t)J * kTT;
     double wv[4], gv[4];
 #pragma unroll
@@ -711,36 +729,25 @@ __global__ void __launch_bounds__(kPipeThreads) k_prof_solve_pipe(ProfileSystem 
       wv[m] = __ldcg(Wt + r * kT + g + 8 * m);
       gv[m] = __ldcg(Gt + r * kT + g + 8 * m);
     }
-    for (int q = 0; q < nrhs; q++) {
-      double t = 0.0;
-#pragma unroll
-      for (int m = 0; m < 4; m++) t = fma(wv[m], rv[q][g + 8 * m], t);
-      t = group_sum(t);
-      if (g == 0) cv[q][r] = t;
-    }
+    __syncthreads();
     const bool hasG = J + 1 < nt && S.ftile[J + 1] <= J;
-    if (hasG) {
-      if (tid == 0) ok = wait_flag(bdone + (J + 1), flags) ? 1 : 0;
-      __syncthreads();
-      if (!ok) return;
-    } else {
-      __syncthreads();
-    }
     for (int q = 0; q < nrhs; q++) {
+      double c = 0.0;
+#pragma unroll
+      for (int m = 0; m < 4; m++) c = fma(wv[m], rb[q][g + 8 * m], c);
+      c = group_sum(c);
       double t = 0.0;
       if (hasG) {
-        const double *xn = x + (size_t)q * ldx + (J + 1) * kT + g;
+        double xv[4];
+        await4(xs + (size_t)q * ls + (J + 1) * kT + g, xv, flags);
 #pragma unroll
-        for (int m = 0; m < 4; m++) t = fma(gv[m], __ldcg(xn + 8 * m), t);
+        for (int m = 0; m < 4; m++) t = fma(gv[m], xv[m], t);
       }
       t = group_sum(t);
-      if (g == 0) x[(size_t)q * ldx + J * kT + r] = cv[q][r] - t;
-    }
-    __threadfence();
-    __syncthreads();
-    if (tid == 0) {
-      __threadfence();
-      atomicExch(bdone + J, 1);
+      if (g == 0) {
+        publish(xs + (size_t)q * ls + J * kT + r, c - t);
+        x[(size_t)q * ldx + J * kT + r] = c - t;
+      }
     }
   }
 }
@@ -856,16 +863,17 @@ int profile_factor(const ProfileSystem &S, cudaStream_t s, int *bad_eq) {
 int profile_solve(const ProfileSystem &S, int nrhs, double *x, int ldx, cudaStream_t s) {
   if (S.n == 0) return 0;
   if (nrhs < 1 || nrhs > 4 || ldx < S.nt * kT) return XG_EINVAL;
-  if (S.sweep_flags && S.nt >= 2 * kPipeBlocks) {
-    // pipelined over co-resident blocks (the flags of both sweeps are zeroed
-    // first); small systems keep the one-block sweep
-    if (cudaMemsetAsync(S.sweep_flags, 0, 2 * (size_t)S.nt * sizeof(int), s) != cudaSuccess)
+  if (S.sweep && S.nt >= 2 * kPipeBlocks) {
+    // pipelined over co-resident blocks (both sweeps' published values are
+    // reset to kUnset first); small systems keep the one-block sweep
+    const size_t ls = (size_t)S.nt * kT;
+    if (cudaMemsetAsync(S.sweep, 0xFF, 2 * (size_t)nrhs * ls * sizeof(double), s) != cudaSuccess)
       return XG_ECUDA;
     if (cudaMemsetAsync(S.flags, 0, 4 * sizeof(int), s) != cudaSuccess) return XG_ECUDA;
     ProfileSystem Sv = S;
-    int *fd = S.sweep_flags, *bd = S.sweep_flags + S.nt;
-    void *args[] = {(void *)&Sv, (void *)&nrhs, (void *)&x, (void *)&ldx, (void *)&fd,
-                    (void *)&bd};
+    double *ys = S.sweep, *xs = S.sweep + (size_t)nrhs * ls;
+    void *args[] = {(void *)&Sv, (void *)&nrhs, (void *)&x, (void *)&ldx, (void *)&ys,
+                    (void *)&xs};
     if (cudaLaunchCooperativeKernel((void *)k_prof_solve_pipe, dim3(kPipeBlocks),
                                     dim3(kPipeThreads), args, 0, s) != cudaSuccess)
       return XG_ECUDA;
