@@ -89,11 +89,18 @@ __device__ void steel02_trial(const double *q, const double *hc, double trialStr
   }
   const double rden = 1.0 / (epss0 - epsr);
   const double epsrat = (eps - epsr) * rden;
-  // |e*|^R and 1 / (1 + |e*|^R)^(1/R) through logs and exps
+  // |e*|^R and 1 / (1 + |e*|^R)^(1/R) through logs and exps.  Where a
+  // single-precision estimate puts |e*|^R below 2^-60 (R log2|e*| < -60 with
+  // a margin of several units over the estimate's error), 1 + |e*|^R rounds
+  // to 1 and both values are exactly 1: the logs and exps, half of a fiber
+  // update's FP64 work, are skipped with bit-identical results.
   const double ae = fabs(epsrat);
-  const double pr = ae > 0.0 ? exp(R * log(ae)) : 0.0;
-  const double dum1 = 1.0 + pr;
-  const double rdum2 = exp(-log(dum1) / R);
+  double dum1 = 1.0, rdum2 = 1.0;
+  if (!((float)R * __log2f(fmaxf((float)ae, 1.17549435e-38f)) < -60.0f)) {
+    const double pr = ae > 0.0 ? exp(R * log(ae)) : 0.0;
+    dum1 = 1.0 + pr;
+    rdum2 = exp(-log(dum1) / R);
+  }
   const double dsig = sigs0 - sigr;
   double sig = b * epsrat + (1.0 - b) * epsrat * rdum2;
   sig = sig * dsig + sigr;
