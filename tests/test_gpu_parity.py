@@ -137,6 +137,32 @@ def test_pcg_against_dense_solve(gpu_mod):
     assert relerr(x, xd) < 1e-9
 
 
+def test_pcg_long_constraint_row(gpu_mod):
+    """Block-Jacobi PCG on a brick block whose top face is tied in z to one
+    node: that node's row (1,446 entries) is summed in chunks of 512 entries
+    by separate warps, the other rows one thread each from the sliced copy of
+    the matrix.  The solution against the device LDL' and the residual."""
+    sp = pytest.importorskip("scipy.sparse")
+    from xara_gb300 import configs
+    desc, _ = configs.brick_block(nx=16, ny=16, nz=4, steps=1)
+    with gpu_mod.DeviceModel(desc) as m:
+        u = np.zeros(m.nu)
+        u[2::3] = -1e-4 * desc.node_crd.reshape(-1, 3)[:, 2]    # uniform compression
+        m.set_trial_disp(u)
+        vals, _, _ = m.update()
+        rp, ci = m.pattern()
+        assert np.diff(rp).max() > 1024
+        A = sp.csr_matrix((vals, ci, rp), shape=(m.neq, m.neq))
+        b = np.random.default_rng(5).normal(size=m.neq)
+        m.set_system(gpu_mod.XG_SYSTEM_BJPCG)
+        x, it, rr = m.solve(b, rtol=1e-13)
+        assert rr <= 1e-13 and it > 0
+        assert np.linalg.norm(A @ x - b) / np.linalg.norm(b) < 1e-11
+        m.set_system(gpu_mod.XG_SYSTEM_PROFILE_SPD)
+        xl, _, _ = m.solve(b)
+    assert relerr(x, xl) < 1e-9
+
+
 def test_oracle_full_size_quad_against_device(gpu_mod):
     """C0 at full size through the oracle restatement and the device."""
     from oracle import port

@@ -93,18 +93,21 @@ __device__ void steel02_trial(const double *q, const double *hc, double trialStr
   // single-precision estimate puts |e*|^R below 2^-60 (R log2|e*| < -60 with
   // a margin of several units over the estimate's error), 1 + |e*|^R rounds
   // to 1 and both values are exactly 1: the logs and exps, half of a fiber
-  // update's FP64 work, are skipped with bit-identical results.
+  // update's FP64 work, are skipped, and so is the tangent's division in
+  // sig = b e* + (1-b) e* rdum2, e = b + (1-b) rdum2 / dum1.
   const double ae = fabs(epsrat);
-  double dum1 = 1.0, rdum2 = 1.0;
+  double se = (1.0 - b) * epsrat, te = 1.0 - b;
   if (!((float)R * __log2f(fmaxf((float)ae, 1.17549435e-38f)) < -60.0f)) {
     const double pr = ae > 0.0 ? exp(R * log(ae)) : 0.0;
-    dum1 = 1.0 + pr;
-    rdum2 = exp(-log(dum1) / R);
+    const double dum1 = 1.0 + pr;
+    const double rdum2 = exp(-log(dum1) / R);
+    se *= rdum2;
+    te = te * rdum2 / dum1;
   }
   const double dsig = sigs0 - sigr;
-  double sig = b * epsrat + (1.0 - b) * epsrat * rdum2;
+  double sig = b * epsrat + se;
   sig = sig * dsig + sigr;
-  double e = b + (1.0 - b) * rdum2 / dum1;
+  double e = b + te;
   e = e * dsig * rden;
   ht[0] = epsmin; ht[1] = epsmax; ht[2] = epspl; ht[3] = epss0; ht[4] = sigs0;
   ht[5] = epsr; ht[6] = sigr; ht[7] = (double)kon; ht[8] = e; ht[9] = sig; ht[11] = R;

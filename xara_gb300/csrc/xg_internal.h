@@ -70,8 +70,30 @@ struct PcgSystem {
   unsigned int *barrier;  // [2] grid barrier state
   int *flags;             // [4] status words
   double *scalars;        // [8]
+  // optional sliced ELL copy of the matrix (thread-per-row SpMV) for rows of
+  // at most sell_cap entries, longer rows in chunks of CSR entries, a warp
+  // each; sell_vals null: every row is read from the CSR arrays warp per row
+  const long *sell_off;   // [ceil(n/32)+1] slice offsets
+  const int *sell_cols;   // [sell_off[last]]
+  double *sell_vals;      // [sell_off[last]], packed from vals by pcg_factor_blocks
+  int sell_cap;
+  int nlong, nchunks;     // long rows, their chunks
+  const int *chunk_row;   // [nchunks] row of each chunk
+  const int *chunk_beg;   // [nchunks] first CSR entry of each chunk
+  const int *long_chunk0; // [nlong+1] chunk range of each long row
+  double *chunk_part;     // [nchunks] partial sums
 };
+// Factor the diagonal blocks (and pack the sliced ELL values when present)
+// after the matrix values changed.
 int pcg_factor_blocks(const PcgSystem &S, cudaStream_t s);
+// Sliced ELL layout of a CSR pattern for rows of at most cap entries (slice
+// offsets, then the column array) and the chunks of the longer rows.
+void sell_layout(int n, const int *rowptr, int cap, std::vector<long> &off,
+                 std::vector<int> &chunk_row, std::vector<int> &chunk_beg,
+                 std::vector<int> &long_chunk0);
+void sell_columns(int n, const int *rowptr, const int *colidx, int cap,
+                  const std::vector<long> &off, std::vector<int> &cols);
+int pcg_sell_max_blocks();
 // Solve A x = b (device vectors).  x holds the initial guess (usually 0).
 // Returns 0 when converged, XG_ESOLVE on breakdown, maxit or a barrier timeout.
 // rows_per_block: the grid gets one block per that many rows (capped by

@@ -157,6 +157,16 @@ struct xg_model {
   DBuf<int> d_flags;
   PcgSystem pcg{};
   bool blocks_factored = false;
+  // sliced ELL copy of the matrix for the PCG's SpMV, built at the first
+  // PCG solve (skipped, keeping the CSR SpMV, when it would take more than
+  // half of the free device memory)
+  DBuf<long> d_sell_off;
+  DBuf<int> d_sell_cols;
+  DBuf<double> d_sell_vals, d_chunk_part;
+  DBuf<int> d_chunk_row, d_chunk_beg, d_long_chunk0;
+  bool sell_tried = false;
+  int ensure_pcg_sell();
+  int pcg_prepare();
   double rtol = 1e-12;
   int maxit = 20000;
   // `system ProfileSPD` on the device (xg_profile.cu)
@@ -690,7 +700,7 @@ int xg_model::upload(const HostGather &gk_h, const HostGather &gr_h) {
   RET(d_binv.alloc((size_t)std::max(nblk, 1) * 36));
   const size_t nv = neq > 0 ? neq : 1;
   RET(d_r.alloc(nv)); RET(d_z.alloc(nv)); RET(d_p.alloc(nv)); RET(d_q.alloc(nv));
-  RET(d_pcg_part.alloc(3 * (size_t)pcg_max_blocks() + 8));
+  RET(d_pcg_part.alloc(3 * (size_t)std::max(pcg_max_blocks(), pcg_sell_max_blocks()) + 8));
   RET(d_scalars.alloc(8));
   RET(d_barrier.alloc(2));
   RET(d_flags.alloc(4));
@@ -1388,6 +1398,50 @@ int xg_model::solve_profile(int nrhs, const double *const *b, double *const *x) 
   return 0;
 }
 
+int xg_model::ensure_pcg_sell() {
+  if (sell_tried || neq == 0) return 0;
+  sell_tried = true;
+  constexpr int kCap = 256;   // longer rows go in chunks
+  std::vector<long> off;
+  std::vector<int> chunk_row, chunk_beg, long_chunk0;
+  sell_layout(neq, rowptr.data(), kCap, off, chunk_row, chunk_beg, long_chunk0);
+  if (off.back() == 0) return 0;
+  size_t freeb = 0, totalb = 0;
+  CK(cudaMemGetInfo(&freeb, &totalb));
+  const size_t need = (size_t)off.back() * (sizeof(double) + sizeof(int)) + off.size() * sizeof(long);
+  if (need > freeb / 2) return 0;
+  std::vector<int> cols;
+  sell_columns(neq, rowptr.data(), colidx.data(), kCap, off, cols);
+  RET(d_sell_off.upload(off.data(), off.size(), stream));
+  RET(d_sell_cols.upload(cols.data(), cols.size(), stream));
+  RET(d_sell_vals.alloc(cols.size()));
+  const int nch = (int)chunk_row.size();
+  RET(d_chunk_row.upload(chunk_row.data(), chunk_row.size(), stream));
+  RET(d_chunk_beg.upload(chunk_beg.data(), chunk_beg.size(), stream));
+  RET(d_long_chunk0.upload(long_chunk0.data(), long_chunk0.size(), stream));
+  RET(d_chunk_part.alloc(std::max(nch, 1)));
+  pcg.sell_off = d_sell_off.p;
+  pcg.sell_cols = d_sell_cols.p;
+  pcg.sell_vals = d_sell_vals.p;
+  pcg.sell_cap = kCap;
+  pcg.nlong = (int)long_chunk0.size() - 1;
+  pcg.nchunks = nch;
+  pcg.chunk_row = d_chunk_row.p;
+  pcg.chunk_beg = d_chunk_beg.p;
+  pcg.long_chunk0 = d_long_chunk0.p;
+  pcg.chunk_part = d_chunk_part.p;
+  return 0;
+}
+
+// Before a PCG solve on new matrix values: the diagonal blocks' inverses and
+// the sliced ELL values.
+int xg_model::pcg_prepare() {
+  RET(ensure_pcg_sell());
+  RET(pcg_factor_blocks(pcg, stream));
+  blocks_factored = true;
+  return 0;
+}
+
 int xg_model::solve(const double *b, double *x, int *iters) {
   if (system == XG_SYSTEM_PROFILE_SPD) {
     if (iters) *iters = 0;
@@ -1395,9 +1449,8 @@ int xg_model::solve(const double *b, double *x, int *iters) {
   }
   if (!blocks_factored) {
     prof_begin(P_PCG_FACTOR);
-    RET(pcg_factor_blocks(pcg, stream));
+    RET(pcg_prepare());
     prof_end(P_PCG_FACTOR, 1);
-    blocks_factored = true;
   }
   CK(cudaMemsetAsync(x, 0, (neq > 0 ? neq : 1) * sizeof(double), stream));
   double relres = 0.0;
@@ -2215,10 +2268,7 @@ int xg_soe_solve(xg_model *m, const double *b, double *x, double rtol, int maxit
     if (relres) *relres = 0.0;
     return 0;
   }
-  if (!m->blocks_factored) {
-    RET(pcg_factor_blocks(m->pcg, m->stream));
-    m->blocks_factored = true;
-  }
+  if (!m->blocks_factored) RET(m->pcg_prepare());
   CK(cudaMemsetAsync(m->d_x.p, 0, (size_t)std::max(m->neq, 1) * sizeof(double), m->stream));
   int it = 0;
   double rr = 0.0;
@@ -2241,10 +2291,7 @@ int xg_soe_solve_device(xg_model *m, const double *b_dev, double *x_dev, double 
     if (relres) *relres = 0.0;
     return 0;
   }
-  if (!m->blocks_factored) {
-    RET(pcg_factor_blocks(m->pcg, m->stream));
-    m->blocks_factored = true;
-  }
+  if (!m->blocks_factored) RET(m->pcg_prepare());
   CK(cudaMemsetAsync(x_dev, 0, (size_t)std::max(m->neq, 1) * sizeof(double), m->stream));
   int it = 0;
   double rr = 0.0;

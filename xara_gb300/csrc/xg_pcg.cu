@@ -11,7 +11,9 @@
 #include <cooperative_groups.h>
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cstdint>
+#include <vector>
 
 #include "xg_internal.h"
 
@@ -93,6 +95,85 @@ __device__ __forceinline__ double spmv_row(const PcgSystem &S, int row, const do
   return s;  // lane 0
 }
 
+// Sliced ELL copy of the CSR matrix (thread per row): slice s holds rows
+// 32s .. 32s+31 column-major over the slice's longest row, entry k of row r
+// at sell_off[r/32] + 32k + r%32, so a warp's 32 rows load each entry
+// position with one coalesced access.  Each row is summed in its CSR order
+// into four interleaved partial sums, a fixed order.
+__device__ __forceinline__ double spmv_sell(const PcgSystem &S, int row, const double *x) {
+  const int b = S.rowptr[row], len = S.rowptr[row + 1] - b;
+  const long base = S.sell_off[row >> 5] + (row & 31);
+  const int *cp = S.sell_cols + base;
+  const double *vp = S.sell_vals + base;
+  double a0 = 0.0, a1 = 0.0, a2 = 0.0, a3 = 0.0;
+  int k = 0;
+  for (; k + 4 <= len; k += 4) {
+    const int c0 = __ldcs(cp + 32 * k), c1 = __ldcs(cp + 32 * (k + 1));
+    const int c2 = __ldcs(cp + 32 * (k + 2)), c3 = __ldcs(cp + 32 * (k + 3));
+    const double v0 = __ldcs(vp + 32 * k), v1 = __ldcs(vp + 32 * (k + 1));
+    const double v2 = __ldcs(vp + 32 * (k + 2)), v3 = __ldcs(vp + 32 * (k + 3));
+    a0 = fma(v0, x[c0], a0);
+    a1 = fma(v1, x[c1], a1);
+    a2 = fma(v2, x[c2], a2);
+    a3 = fma(v3, x[c3], a3);
+  }
+  for (; k < len; k++) a0 = fma(__ldcs(vp + 32 * k), x[__ldcs(cp + 32 * k)], a0);
+  return (a0 + a1) + (a2 + a3);
+}
+
+// f(row, (A x)[row]) for this thread's rows: thread per row over the sliced
+// ELL copy (kSell; rows longer than S.sell_cap are left to
+// long_row_chunks), else warp per CSR row (lane 0 calls f).
+template <bool kSell, typename F>
+__device__ __forceinline__ void for_rows_Ax(const PcgSystem &S, const double *x, F f) {
+  const int gtid = blockIdx.x * blockDim.x + threadIdx.x;
+  const int gthreads = gridDim.x * blockDim.x;
+  if (kSell) {
+    for (int row = gtid; row < S.n; row += gthreads)
+      if (S.rowptr[row + 1] - S.rowptr[row] <= S.sell_cap) f(row, spmv_sell(S, row, x));
+  } else {
+    const int lane = threadIdx.x & 31;
+    for (int row = gtid >> 5; row < S.n; row += gthreads >> 5) {
+      const double ax = spmv_row(S, row, x, lane);
+      if (lane == 0) f(row, ax);
+    }
+  }
+}
+
+// Rows longer than S.sell_cap (a node tied to a whole face by a
+// multi-point constraint couples to every node of that face) in chunks of
+// at most kLongChunk CSR entries, a warp per chunk: g(chunk, row, partial)
+// on lane 0.  A warp per row would leave one warp thousands of entries.
+constexpr int kLongChunk = 512;
+template <typename G>
+__device__ __forceinline__ void long_row_chunks(const PcgSystem &S, const double *x, G g) {
+  const int gtid = blockIdx.x * blockDim.x + threadIdx.x;
+  const int lane = threadIdx.x & 31, nwarps = (gridDim.x * blockDim.x) >> 5;
+  for (int c = gtid >> 5; c < S.nchunks; c += nwarps) {
+    const int row = S.chunk_row[c];
+    const int b = S.chunk_beg[c], e = min(b + kLongChunk, S.rowptr[row + 1]);
+    double t = 0.0;
+    for (int k = b + lane; k < e; k += 32) t += S.vals[k] * x[S.colidx[k]];
+    for (int o = 16; o > 0; o >>= 1) t += __shfl_down_sync(0xffffffffu, t, o);
+    if (lane == 0) g(c, row, t);
+  }
+}
+
+// (A x)[row] of every long row from its chunk partials, in chunk order
+// (lane-strided, then a fixed butterfly): h(row, sum) on lane 0 of a warp
+// per long row.
+template <typename H>
+__device__ __forceinline__ void long_row_sums(const PcgSystem &S, H h) {
+  const int gtid = blockIdx.x * blockDim.x + threadIdx.x;
+  const int lane = threadIdx.x & 31, nwarps = (gridDim.x * blockDim.x) >> 5;
+  for (int i = gtid >> 5; i < S.nlong; i += nwarps) {
+    double t = 0.0;
+    for (int c = S.long_chunk0[i] + lane; c < S.long_chunk0[i + 1]; c += 32) t += S.chunk_part[c];
+    for (int o = 16; o > 0; o >>= 1) t += __shfl_down_sync(0xffffffffu, t, o);
+    if (lane == 0) h(S.chunk_row[S.long_chunk0[i]], t);
+  }
+}
+
 // Vector work is done per diagonal block (<= 6 equations of one node), so
 // every equation is read and written by exactly one thread in a phase.
 struct BlockRange { int b, m; };
@@ -116,23 +197,24 @@ __device__ __forceinline__ void precondition_block(const PcgSystem &S, int k, Bl
 }
 
 // scalars: [0] rz  [1] bb  [2] rr  [3] iterations  [4] relres
+template <bool kSell>
 __global__ void __launch_bounds__(kPcgThreads) k_pcg(PcgSystem S, const double *b, double *x,
                                                      double rtol, int maxit) {
   __shared__ double smem[40];
   volatile int *flags = S.flags;
   const int gtid = blockIdx.x * blockDim.x + threadIdx.x;
   const int gthreads = gridDim.x * blockDim.x;
-  const int lane = threadIdx.x & 31;
-  const int gwarp = gtid >> 5, nwarps = gthreads >> 5;
   const int nb = gridDim.x;
   double *part = S.partials;          // [3*nb]
 
   // r = b - A x ; (x is the initial guess)
-  for (int row = gwarp; row < S.n; row += nwarps) {
-    const double ax = spmv_row(S, row, x, lane);
-    if (lane == 0) S.r[row] = b[row] - ax;
-  }
+  for_rows_Ax<kSell>(S, x, [&](int row, double ax) { S.r[row] = b[row] - ax; });
+  if (kSell) long_row_chunks(S, x, [&](int c, int, double t) { S.chunk_part[c] = t; });
   if (!grid_barrier(S.barrier, flags)) return;
+  if (kSell && S.nlong > 0) {
+    long_row_sums(S, [&](int row, double ax) { S.r[row] = b[row] - ax; });
+    if (!grid_barrier(S.barrier, flags)) return;
+  }
   double lrz = 0.0, lbb = 0.0, lrr = 0.0;
   for (int k = gtid; k < S.nblk; k += gthreads) {
     const BlockRange br = block_range(S, k);
@@ -165,20 +247,23 @@ __global__ void __launch_bounds__(kPcgThreads) k_pcg(PcgSystem S, const double *
     // q = A p ; pq = p.q
     if (!grid_barrier(S.barrier, flags)) return;   // partial sums consumed
     double lpq = 0.0;
-    for (int row = gwarp; row < S.n; row += nwarps) {
-      const double ap = spmv_row(S, row, S.p, lane);
-      if (lane == 0) {
-        S.q[row] = ap;
-        lpq += ap * S.p[row];
-      }
-    }
+    for_rows_Ax<kSell>(S, S.p, [&](int row, double ap) {
+      S.q[row] = ap;
+      lpq += ap * S.p[row];
+    });
+    if (kSell)
+      long_row_chunks(S, S.p, [&](int c, int row, double t) {
+        S.chunk_part[c] = t;
+        lpq += t * S.p[row];
+      });
     lpq = block_reduce(lpq, smem);
     if (threadIdx.x == 0) part[blockIdx.x] = lpq;
     if (!grid_barrier(S.barrier, flags)) return;
     const double pq = sum_partials(part, nb, smem);
     if (!(pq > 0.0)) { status = -1; break; }
     const double alpha = rz / pq;
-    if (!grid_barrier(S.barrier, flags)) return;   // partial sums consumed
+    if (kSell) long_row_sums(S, [&](int row, double ap) { S.q[row] = ap; });
+    if (!grid_barrier(S.barrier, flags)) return;   // partial sums consumed, q complete
     lrz = 0.0; lrr = 0.0;
     for (int k = gtid; k < S.nblk; k += gthreads) {
       const BlockRange br = block_range(S, k);
@@ -265,26 +350,84 @@ __global__ void k_factor_blocks(PcgSystem S) {
     for (int j = 0; j < m; j++) B[6 * i + j] = A[i][m + j];
 }
 
-int g_max_blocks = -1;
+// CSR values into the sliced ELL copy, thread per row
+__global__ void k_pack_sell(PcgSystem S) {
+  const int row = blockIdx.x * blockDim.x + threadIdx.x;
+  if (row >= S.n) return;
+  const int b = S.rowptr[row], len = S.rowptr[row + 1] - b;
+  if (len > S.sell_cap) return;
+  double *vp = S.sell_vals + S.sell_off[row >> 5] + (row & 31);
+  for (int k = 0; k < len; k++) vp[32 * k] = S.vals[b + k];
+}
+
+int g_max_blocks = -1, g_sell_max_blocks = -1;
+
+int max_coresident(const void *kernel) {
+  int dev = 0, sms = 0, per = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kernel, kPcgThreads, 0);
+  if (per < 1) per = 1;
+  return sms * per;
+}
 
 }  // namespace
 
 int pcg_max_blocks() {
-  if (g_max_blocks < 0) {
-    int dev = 0, sms = 0, per = 0;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_pcg, kPcgThreads, 0);
-    if (per < 1) per = 1;
-    g_max_blocks = sms * per;
-  }
+  if (g_max_blocks < 0) g_max_blocks = max_coresident((const void *)k_pcg<false>);
   return g_max_blocks;
+}
+
+int pcg_sell_max_blocks() {
+  if (g_sell_max_blocks < 0) g_sell_max_blocks = max_coresident((const void *)k_pcg<true>);
+  return g_sell_max_blocks;
+}
+
+void sell_layout(int n, const int *rowptr, int cap, std::vector<long> &off,
+                 std::vector<int> &chunk_row, std::vector<int> &chunk_beg,
+                 std::vector<int> &long_chunk0) {
+  const int ns = (n + 31) / 32;
+  off.assign((size_t)ns + 1, 0);
+  chunk_row.clear();
+  chunk_beg.clear();
+  long_chunk0.assign(1, 0);
+  for (int s = 0; s < ns; s++) {
+    int w = 0;
+    for (int r = 32 * s; r < std::min(n, 32 * s + 32); r++) {
+      const int len = rowptr[r + 1] - rowptr[r];
+      if (len <= cap) {
+        w = std::max(w, len);
+        continue;
+      }
+      for (int k = rowptr[r]; k < rowptr[r + 1]; k += kLongChunk) {
+        chunk_row.push_back(r);
+        chunk_beg.push_back(k);
+      }
+      long_chunk0.push_back((int)chunk_row.size());
+    }
+    off[s + 1] = off[s] + 32L * w;
+  }
+}
+
+void sell_columns(int n, const int *rowptr, const int *colidx, int cap,
+                  const std::vector<long> &off, std::vector<int> &cols) {
+  cols.assign((size_t)off.back(), 0);
+  for (int r = 0; r < n; r++) {
+    if (rowptr[r + 1] - rowptr[r] > cap) continue;
+    for (int k = rowptr[r]; k < rowptr[r + 1]; k++)
+      cols[(size_t)off[r / 32] + 32L * (k - rowptr[r]) + r % 32] = colidx[k];
+  }
 }
 
 int pcg_factor_blocks(const PcgSystem &S, cudaStream_t s) {
   if (S.nblk == 0) return 0;
   k_factor_blocks<<<(S.nblk + 127) / 128, 128, 0, s>>>(S);
-  return cudaGetLastError() == cudaSuccess ? 0 : XG_ECUDA;
+  if (cudaGetLastError() != cudaSuccess) return XG_ECUDA;
+  if (S.sell_vals && S.n > 0) {
+    k_pack_sell<<<(S.n + 255) / 256, 256, 0, s>>>(S);
+    if (cudaGetLastError() != cudaSuccess) return XG_ECUDA;
+  }
+  return 0;
 }
 
 int pcg_solve(const PcgSystem &S, const double *b, double *x, double rtol, int maxit,
@@ -300,14 +443,15 @@ int pcg_solve(const PcgSystem &S, const double *b, double *x, double rtol, int m
   const long rpb = rows_per_block > 0 ? rows_per_block : 64;
   long want = ((long)S.n + rpb - 1) / rpb;
   int nb = (int)(want < 1 ? 1 : want);
-  const int maxb = pcg_max_blocks();
+  const bool sell = S.sell_vals != nullptr;
+  const int maxb = sell ? pcg_sell_max_blocks() : pcg_max_blocks();
   if (nb > maxb) nb = maxb;
   if (cudaMemsetAsync(S.barrier, 0, 2 * sizeof(unsigned int), s) != cudaSuccess) return XG_ECUDA;
   if (cudaMemsetAsync(S.flags, 0, 4 * sizeof(int), s) != cudaSuccess) return XG_ECUDA;
   PcgSystem Sv = S;
   void *args[] = {(void *)&Sv, (void *)&b, (void *)&x, (void *)&rtol, (void *)&maxit};
-  cudaError_t err = cudaLaunchCooperativeKernel((void *)k_pcg, dim3(nb), dim3(kPcgThreads), args,
-                                                0, s);
+  const void *kernel = sell ? (const void *)k_pcg<true> : (const void *)k_pcg<false>;
+  cudaError_t err = cudaLaunchCooperativeKernel(kernel, dim3(nb), dim3(kPcgThreads), args, 0, s);
   if (err != cudaSuccess) return XG_ECUDA;
   int hflags[4];
   double hs[8];
