@@ -394,58 +394,67 @@ __device__ __constant__ unsigned char kPairB[36] = {
     0, 1, 2, 3, 4, 5, 6, 7, 1, 2, 3, 4, 5, 6, 7, 2, 3, 4,
     5, 6, 7, 3, 4, 5, 6, 7, 4, 5, 6, 7, 5, 6, 7, 6, 7, 7};
 
-constexpr int kBrickWarps = 4;
+constexpr int kBrickWarps = 2;
+constexpr int kBrickEPW = 4;   // elements per warp
 
-// One warp per element: Brick::formResidAndTangent (Brick.cpp:844-1021) from
-// the stored point state, K in upper node-pair blocks:
+// Four elements per warp: Brick::formResidAndTangent (Brick.cpp:844-1021)
+// from the stored point state, K in upper node-pair blocks:
 // Ke[e*324 + p*9 + 3*i + k] = K(3a+i, 3b+k) for the pair p = (a <= b).
-// Re[e*24 + 3a + i].
+// Re[e*24 + 3a + i].  The lanes take (element, point) for the shape
+// gradients, then the elements' 96 residual entries and 144 node pairs
+// three and five at a time: on an FP64 pipe that issues a warp instruction
+// whatever its active lanes, one element per warp left 3/4 of the lanes
+// idle in the first phase and 7/16 of the pair slots empty.
 __global__ void __launch_bounds__(32 * kBrickWarps) k_brick_assemble(ContinuumView v) {
-  __shared__ double sg[kBrickWarps][8][8][3];   // dN/dx per point, node
-  __shared__ double sh[kBrickWarps][8][8][3];   // N . dN/dx
-  __shared__ double sc[kBrickWarps][8][3];      // dvol*a, dvol*b/2, dvol*c
-  __shared__ double ss[kBrickWarps][8][6];      // dvol*stress
+  __shared__ double sg[kBrickWarps][kBrickEPW][8][8][3];   // dN/dx per point, node
+  __shared__ double sh[kBrickWarps][kBrickEPW][8][8][3];   // N . dN/dx
+  __shared__ double sc[kBrickWarps][kBrickEPW][8][3];      // dvol*a, dvol*b/2, dvol*c
+  __shared__ double ss[kBrickWarps][kBrickEPW][8][6];      // dvol*stress
   const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int e = blockIdx.x * kBrickWarps + w;
-  if (e >= v.ne) return;
+  const int e0 = (blockIdx.x * kBrickWarps + w) * kBrickEPW;
+  if (e0 >= v.ne) return;
   const long npts = (long)v.ne * 8;
-  if (lane < 8) {
-    const int ip = lane;
-    const long pt = (long)e * 8 + ip;
-    double xl[3][8], g[3][8];
+  {
+    const int el = lane >> 3, ip = lane & 7, e = e0 + el;
+    if (e < v.ne) {
+      const long pt = (long)e * 8 + ip;
+      double xl[3][8], g[3][8];
 #pragma unroll
-    for (int a = 0; a < 8; a++) {
-      const int nd = v.conn[a * v.ne + e];
-      xl[0][a] = v.crd[nd];
-      xl[1][a] = v.crd[v.nn + nd];
-      xl[2][a] = v.crd[2 * (long)v.nn + nd];
-    }
-    double xn[3];
-    brick_gauss(ip, xn);
-    const double dvol = 1.0 * shp3d_grad(xn, xl, g);
-    const double ca = v.tan[pt], cb = v.tan[npts + pt], cc = v.tan[2 * npts + pt];
-    double n[6];
+      for (int a = 0; a < 8; a++) {
+        const int nd = v.conn[a * v.ne + e];
+        xl[0][a] = v.crd[nd];
+        xl[1][a] = v.crd[v.nn + nd];
+        xl[2][a] = v.crd[2 * (long)v.nn + nd];
+      }
+      double xn[3];
+      brick_gauss(ip, xn);
+      const double dvol = 1.0 * shp3d_grad(xn, xl, g);
+      const double ca = v.tan[pt], cb = v.tan[npts + pt], cc = v.tan[2 * npts + pt];
+      double n[6];
 #pragma unroll
-    for (int c = 0; c < 6; c++) n[c] = v.tan[(3 + c) * npts + pt];
-    sc[w][ip][0] = dvol * ca;
-    sc[w][ip][1] = dvol * (0.5 * cb);
-    sc[w][ip][2] = dvol * cc;
+      for (int c = 0; c < 6; c++) n[c] = v.tan[(3 + c) * npts + pt];
+      sc[w][el][ip][0] = dvol * ca;
+      sc[w][el][ip][1] = dvol * (0.5 * cb);
+      sc[w][el][ip][2] = dvol * cc;
 #pragma unroll
-    for (int c = 0; c < 6; c++) ss[w][ip][c] = dvol * v.sig[c * npts + pt];
+      for (int c = 0; c < 6; c++) ss[w][el][ip][c] = dvol * v.sig[c * npts + pt];
 #pragma unroll
-    for (int a = 0; a < 8; a++) {
-      const double g0 = g[0][a], g1 = g[1][a], g2 = g[2][a];
-      sg[w][ip][a][0] = g0;
-      sg[w][ip][a][1] = g1;
-      sg[w][ip][a][2] = g2;
-      sh[w][ip][a][0] = n[0] * g0 + n[3] * g1 + n[5] * g2;
-      sh[w][ip][a][1] = n[3] * g0 + n[1] * g1 + n[4] * g2;
-      sh[w][ip][a][2] = n[5] * g0 + n[4] * g1 + n[2] * g2;
+      for (int a = 0; a < 8; a++) {
+        const double g0 = g[0][a], g1 = g[1][a], g2 = g[2][a];
+        sg[w][el][ip][a][0] = g0;
+        sg[w][el][ip][a][1] = g1;
+        sg[w][el][ip][a][2] = g2;
+        sh[w][el][ip][a][0] = n[0] * g0 + n[3] * g1 + n[5] * g2;
+        sh[w][el][ip][a][1] = n[3] * g0 + n[1] * g1 + n[4] * g2;
+        sh[w][el][ip][a][2] = n[5] * g0 + n[4] * g1 + n[2] * g2;
+      }
     }
   }
   __syncwarp();
-  if (lane < 24) {
-    const int a = lane / 3, i = lane % 3;
+  for (int t = lane; t < kBrickEPW * 24; t += 32) {
+    const int el = t / 24, q = t % 24, e = e0 + el;
+    if (e >= v.ne) continue;
+    const int a = q / 3, i = q % 3;
     // stress tensor row i in [xx yy zz xy yz zx] storage
     const int r0 = (i == 0) ? 0 : (i == 1) ? 3 : 5;
     const int r1 = (i == 0) ? 3 : (i == 1) ? 1 : 4;
@@ -453,11 +462,13 @@ __global__ void __launch_bounds__(32 * kBrickWarps) k_brick_assemble(ContinuumVi
     double r = 0.0;
 #pragma unroll
     for (int ip = 0; ip < 8; ip++)
-      r += sg[w][ip][a][0] * ss[w][ip][r0] + sg[w][ip][a][1] * ss[w][ip][r1] +
-           sg[w][ip][a][2] * ss[w][ip][r2];
-    v.Re[(long)e * 24 + lane] = r;
+      r += sg[w][el][ip][a][0] * ss[w][el][ip][r0] + sg[w][el][ip][a][1] * ss[w][el][ip][r1] +
+           sg[w][el][ip][a][2] * ss[w][el][ip][r2];
+    v.Re[(long)e * 24 + q] = r;
   }
-  for (int pp = lane; pp < 36; pp += 32) {
+  for (int t = lane; t < kBrickEPW * 36; t += 32) {
+    const int el = t / 36, pp = t % 36, e = e0 + el;
+    if (e >= v.ne) continue;
     const int a = kPairA[pp], b = kPairB[pp];
     double acc[3][3];
 #pragma unroll
@@ -466,11 +477,12 @@ __global__ void __launch_bounds__(32 * kBrickWarps) k_brick_assemble(ContinuumVi
       for (int k = 0; k < 3; k++) acc[i][k] = 0.0;
 #pragma unroll 2
     for (int ip = 0; ip < 8; ip++) {
-      const double ga0 = sg[w][ip][a][0], ga1 = sg[w][ip][a][1], ga2 = sg[w][ip][a][2];
-      const double gb0 = sg[w][ip][b][0], gb1 = sg[w][ip][b][1], gb2 = sg[w][ip][b][2];
-      const double ha[3] = {sh[w][ip][a][0], sh[w][ip][a][1], sh[w][ip][a][2]};
-      const double hb[3] = {sh[w][ip][b][0], sh[w][ip][b][1], sh[w][ip][b][2]};
-      const double da = sc[w][ip][0], dbh = sc[w][ip][1], dc = sc[w][ip][2];
+      const double *Ga = sg[w][el][ip][a], *Gb = sg[w][el][ip][b];
+      const double ga0 = Ga[0], ga1 = Ga[1], ga2 = Ga[2];
+      const double gb0 = Gb[0], gb1 = Gb[1], gb2 = Gb[2];
+      const double ha[3] = {sh[w][el][ip][a][0], sh[w][el][ip][a][1], sh[w][el][ip][a][2]};
+      const double hb[3] = {sh[w][el][ip][b][0], sh[w][el][ip][b][1], sh[w][el][ip][b][2]};
+      const double da = sc[w][el][ip][0], dbh = sc[w][el][ip][1], dc = sc[w][el][ip][2];
       const double ga[3] = {ga0, ga1, ga2}, gb[3] = {gb0, gb1, gb2};
       const double dot = dbh * (ga0 * gb0 + ga1 * gb1 + ga2 * gb2);
       double ua[3], va[3], wa[3];
@@ -622,7 +634,8 @@ int launch_brick_update(const ContinuumView &v, cudaStream_t s) {
 }
 int launch_brick_assemble(const ContinuumView &v, cudaStream_t s) {
   if (v.ne == 0) return 0;
-  k_brick_assemble<<<(v.ne + kBrickWarps - 1) / kBrickWarps, 32 * kBrickWarps, 0, s>>>(v);
+  constexpr int per_block = kBrickWarps * kBrickEPW;
+  k_brick_assemble<<<(v.ne + per_block - 1) / per_block, 32 * kBrickWarps, 0, s>>>(v);
   return check_launch();
 }
 int launch_j2_zero_state(const ContinuumView &v, cudaStream_t s) {
