@@ -33,6 +33,10 @@ struct ContinuumView {
   // element outputs (element-major scratch)
   double *Ke;             // quad: [ne][64]; brick: [ne][324] upper node-pair blocks
   double *Re;             // [ne][ned]
+  // bricks: shape-function gradients dN_a/dx_i at [(8i+a)*npts + pt] and the
+  // Jacobian determinant at [24*npts + pt], formed once (the geometry does
+  // not change); null: formed in every kernel that needs them
+  const double *geo;
 };
 
 // CSR system and deterministic gather assembly.
@@ -52,6 +56,7 @@ int launch_quad_update(const ContinuumView &v, cudaStream_t s);
 int launch_quad_assemble(const ContinuumView &v, cudaStream_t s);
 int launch_brick_update(const ContinuumView &v, cudaStream_t s);
 int launch_brick_assemble(const ContinuumView &v, cudaStream_t s);
+int launch_brick_geometry(const ContinuumView &v, double *geo, cudaStream_t s);
 int launch_gather(const GatherMap &g, const double *scratch, double *partial, double *out,
                   cudaStream_t s);
 int launch_j2_zero_state(const ContinuumView &v, cudaStream_t s);

@@ -338,23 +338,56 @@ __device__ __forceinline__ void brick_gauss(int ip, double xn[3]) {
 // D_ijkl = a d_ij d_kl + b I^sym_ijkl + c n_ij n_kl, which equals the
 // reference's K IbunI + 2G IIdev + c2 NbunN + c3 (IIdev - NbunN) for
 // a = K - b/3, b = 2G + c3, c = c2 - c3.
+// dN/dx and the Jacobian determinant of brick point pt = 8e + ip, from the
+// stored geometry when there is one
+__device__ __forceinline__ double brick_point_grad(const ContinuumView &v, long npts, long pt,
+                                                   double g[3][8]) {
+  if (v.geo) {
+#pragma unroll
+    for (int i = 0; i < 3; i++)
+#pragma unroll
+      for (int a = 0; a < 8; a++) g[i][a] = v.geo[(8 * i + a) * npts + pt];
+    return v.geo[24 * npts + pt];
+  }
+  const int e = (int)(pt >> 3), ip = (int)(pt & 7);
+  double xl[3][8];
+#pragma unroll
+  for (int a = 0; a < 8; a++) {
+    const int nd = v.conn[a * v.ne + e];
+    xl[0][a] = v.crd[nd];
+    xl[1][a] = v.crd[v.nn + nd];
+    xl[2][a] = v.crd[2 * (long)v.nn + nd];
+  }
+  double xn[3];
+  brick_gauss(ip, xn);
+  return shp3d_grad(xn, xl, g);
+}
+
+__global__ void k_brick_geometry(ContinuumView v, double *geo) {
+  const long npts = (long)v.ne * 8;
+  const long pt = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (pt >= npts) return;
+  ContinuumView u = v;
+  u.geo = nullptr;
+  double g[3][8];
+  const double dvol = brick_point_grad(u, npts, pt, g);
+#pragma unroll
+  for (int i = 0; i < 3; i++)
+#pragma unroll
+    for (int a = 0; a < 8; a++) geo[(8 * i + a) * npts + pt] = g[i][a];
+  geo[24 * npts + pt] = dvol;
+}
+
 __global__ void k_brick_update(ContinuumView v) {
   const long npts = (long)v.ne * 8;
   const long pt = (long)blockIdx.x * blockDim.x + threadIdx.x;
   if (pt >= npts) return;
-  const int e = (int)(pt >> 3), ip = (int)(pt & 7);
-  double xl[3][8], g[3][8], eps[6] = {0, 0, 0, 0, 0, 0};
+  const int e = (int)(pt >> 3);
+  double g[3][8], eps[6] = {0, 0, 0, 0, 0, 0};
   int nd[8];
 #pragma unroll
-  for (int a = 0; a < 8; a++) {
-    nd[a] = v.conn[a * v.ne + e];
-    xl[0][a] = v.crd[nd[a]];
-    xl[1][a] = v.crd[v.nn + nd[a]];
-    xl[2][a] = v.crd[2 * (long)v.nn + nd[a]];
-  }
-  double xn[3];
-  brick_gauss(ip, xn);
-  shp3d_grad(xn, xl, g);
+  for (int a = 0; a < 8; a++) nd[a] = v.conn[a * v.ne + e];
+  brick_point_grad(v, npts, pt, g);
 #pragma unroll
   for (int a = 0; a < 8; a++) {
     const double u0 = v.U[3 * (long)nd[a]], u1 = v.U[3 * (long)nd[a] + 1];
@@ -418,17 +451,8 @@ __global__ void __launch_bounds__(32 * kBrickWarps) k_brick_assemble(ContinuumVi
     const int el = lane >> 3, ip = lane & 7, e = e0 + el;
     if (e < v.ne) {
       const long pt = (long)e * 8 + ip;
-      double xl[3][8], g[3][8];
-#pragma unroll
-      for (int a = 0; a < 8; a++) {
-        const int nd = v.conn[a * v.ne + e];
-        xl[0][a] = v.crd[nd];
-        xl[1][a] = v.crd[v.nn + nd];
-        xl[2][a] = v.crd[2 * (long)v.nn + nd];
-      }
-      double xn[3];
-      brick_gauss(ip, xn);
-      const double dvol = 1.0 * shp3d_grad(xn, xl, g);
+      double g[3][8];
+      const double dvol = brick_point_grad(v, npts, pt, g);
       const double ca = v.tan[pt], cb = v.tan[npts + pt], cc = v.tan[2 * npts + pt];
       double n[6];
 #pragma unroll
@@ -630,6 +654,11 @@ int launch_quad_assemble(const ContinuumView &v, cudaStream_t s) {
 int launch_brick_update(const ContinuumView &v, cudaStream_t s) {
   if (v.ne == 0) return 0;
   k_brick_update<<<nblocks((long)v.ne * 8), kThreads, 0, s>>>(v);
+  return check_launch();
+}
+int launch_brick_geometry(const ContinuumView &v, double *geo, cudaStream_t s) {
+  if (v.ne == 0) return 0;
+  k_brick_geometry<<<nblocks((long)v.ne * 8), kThreads, 0, s>>>(v, geo);
   return check_launch();
 }
 int launch_brick_assemble(const ContinuumView &v, cudaStream_t s) {

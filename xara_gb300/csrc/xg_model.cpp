@@ -163,6 +163,7 @@ struct xg_model {
   DBuf<long> d_sell_off;
   DBuf<int> d_sell_cols;
   DBuf<double> d_sell_vals, d_chunk_part;
+  DBuf<double> d_geo;   // bricks: per-point shape-function gradients and Jacobian determinant
   DBuf<int> d_chunk_row, d_chunk_beg, d_long_chunk0;
   bool sell_tried = false;
   int ensure_pcg_sell();
@@ -346,6 +347,7 @@ struct xg_model {
     v.ep_c = d_epc.p; v.xi_c = d_xic.p; v.ep_t = d_ept.p; v.xi_t = d_xit.p;
     v.sig = d_sig.p; v.tan = d_tan.p; v.nfail = d_nfail.p;
     v.Ke = d_Ke.p; v.Re = d_Re.p;
+    v.geo = d_geo.p;
     return v;
   }
   bool frames() const { return etype == XG_ELE_FBC2D || etype == XG_ELE_FBC3D; }
@@ -730,6 +732,10 @@ int xg_model::upload(const HostGather &gk_h, const HostGather &gr_h) {
   if (frames()) {
     RET(upload_frames());
   } else {
+    if (etype == XG_ELE_BRICK) {
+      RET(d_geo.alloc((size_t)25 * np));
+      RET(launch_brick_geometry(view(), d_geo.p, s));
+    }
     // zero-strain material state
     RET(launch_j2_zero_state(view(), s));
     CK(cudaMemcpyAsync(d_sig_c.p, d_sig.p, np * nsig() * sizeof(double), cudaMemcpyDeviceToDevice, s));
