@@ -427,24 +427,34 @@ __device__ __constant__ unsigned char kPairB[36] = {
     0, 1, 2, 3, 4, 5, 6, 7, 1, 2, 3, 4, 5, 6, 7, 2, 3, 4,
     5, 6, 7, 3, 4, 5, 6, 7, 4, 5, 6, 7, 5, 6, 7, 6, 7, 7};
 
-constexpr int kBrickWarps = 2;
+constexpr int kBrickWarps = 1;
 constexpr int kBrickEPW = 4;   // elements per warp
 
 // Four elements per warp: Brick::formResidAndTangent (Brick.cpp:844-1021)
 // from the stored point state, K in upper node-pair blocks:
 // Ke[e*324 + p*9 + 3*i + k] = K(3a+i, 3b+k) for the pair p = (a <= b).
-// Re[e*24 + 3a + i].  The lanes take (element, point) for the shape
-// gradients, then the elements' 96 residual entries and 144 node pairs
-// three and five at a time: on an FP64 pipe that issues a warp instruction
-// whatever its active lanes, one element per warp left 3/4 of the lanes
-// idle in the first phase and 7/16 of the pair slots empty.
+// Re[e*24 + 3a + i].  The lanes take (element, point) to stage the point
+// terms of every node -- dN/dx, its product with the tangent's deviatoric
+// direction and the three scalings of the node-pair sum -- then the
+// elements' 96 residual entries and 144 node pairs three and five at a
+// time: on an FP64 pipe that issues a warp instruction whatever its active
+// lanes, one element per warp left 3/4 of the lanes idle in the first phase
+// and 7/16 of the pair slots empty.
+struct BrickSmem {
+  double g[kBrickEPW][8][8][3];    // dN/dx per point, node
+  double h[kBrickEPW][8][8][3];    // n . dN/dx
+  double u[kBrickEPW][8][8][3];    // dvol*a dN/dx
+  double vv[kBrickEPW][8][8][3];   // dvol*b/2 dN/dx
+  double w[kBrickEPW][8][8][3];    // dvol*c n . dN/dx
+  double sb[kBrickEPW][8];         // dvol*b/2
+  double ss[kBrickEPW][8][6];      // dvol*stress
+};
+
 __global__ void __launch_bounds__(32 * kBrickWarps) k_brick_assemble(ContinuumView v) {
-  __shared__ double sg[kBrickWarps][kBrickEPW][8][8][3];   // dN/dx per point, node
-  __shared__ double sh[kBrickWarps][kBrickEPW][8][8][3];   // N . dN/dx
-  __shared__ double sc[kBrickWarps][kBrickEPW][8][3];      // dvol*a, dvol*b/2, dvol*c
-  __shared__ double ss[kBrickWarps][kBrickEPW][8][6];      // dvol*stress
-  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int e0 = (blockIdx.x * kBrickWarps + w) * kBrickEPW;
+  __shared__ BrickSmem sm_all[kBrickWarps];
+  const int wi = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  BrickSmem &S = sm_all[wi];
+  const int e0 = (blockIdx.x * kBrickWarps + wi) * kBrickEPW;
   if (e0 >= v.ne) return;
   const long npts = (long)v.ne * 8;
   {
@@ -457,20 +467,24 @@ __global__ void __launch_bounds__(32 * kBrickWarps) k_brick_assemble(ContinuumVi
       double n[6];
 #pragma unroll
       for (int c = 0; c < 6; c++) n[c] = v.tan[(3 + c) * npts + pt];
-      sc[w][el][ip][0] = dvol * ca;
-      sc[w][el][ip][1] = dvol * (0.5 * cb);
-      sc[w][el][ip][2] = dvol * cc;
+      const double da = dvol * ca, dbh = dvol * (0.5 * cb), dc = dvol * cc;
+      S.sb[el][ip] = dbh;
 #pragma unroll
-      for (int c = 0; c < 6; c++) ss[w][el][ip][c] = dvol * v.sig[c * npts + pt];
+      for (int c = 0; c < 6; c++) S.ss[el][ip][c] = dvol * v.sig[c * npts + pt];
 #pragma unroll
       for (int a = 0; a < 8; a++) {
-        const double g0 = g[0][a], g1 = g[1][a], g2 = g[2][a];
-        sg[w][el][ip][a][0] = g0;
-        sg[w][el][ip][a][1] = g1;
-        sg[w][el][ip][a][2] = g2;
-        sh[w][el][ip][a][0] = n[0] * g0 + n[3] * g1 + n[5] * g2;
-        sh[w][el][ip][a][1] = n[3] * g0 + n[1] * g1 + n[4] * g2;
-        sh[w][el][ip][a][2] = n[5] * g0 + n[4] * g1 + n[2] * g2;
+        const double gi[3] = {g[0][a], g[1][a], g[2][a]};
+        const double hi[3] = {n[0] * gi[0] + n[3] * gi[1] + n[5] * gi[2],
+                              n[3] * gi[0] + n[1] * gi[1] + n[4] * gi[2],
+                              n[5] * gi[0] + n[4] * gi[1] + n[2] * gi[2]};
+#pragma unroll
+        for (int i = 0; i < 3; i++) {
+          S.g[el][ip][a][i] = gi[i];
+          S.h[el][ip][a][i] = hi[i];
+          S.u[el][ip][a][i] = da * gi[i];
+          S.vv[el][ip][a][i] = dbh * gi[i];
+          S.w[el][ip][a][i] = dc * hi[i];
+        }
       }
     }
   }
@@ -486,8 +500,8 @@ __global__ void __launch_bounds__(32 * kBrickWarps) k_brick_assemble(ContinuumVi
     double r = 0.0;
 #pragma unroll
     for (int ip = 0; ip < 8; ip++)
-      r += sg[w][el][ip][a][0] * ss[w][el][ip][r0] + sg[w][el][ip][a][1] * ss[w][el][ip][r1] +
-           sg[w][el][ip][a][2] * ss[w][el][ip][r2];
+      r += S.g[el][ip][a][0] * S.ss[el][ip][r0] + S.g[el][ip][a][1] * S.ss[el][ip][r1] +
+           S.g[el][ip][a][2] * S.ss[el][ip][r2];
     v.Re[(long)e * 24 + q] = r;
   }
   for (int t = lane; t < kBrickEPW * 36; t += 32) {
@@ -501,17 +515,12 @@ __global__ void __launch_bounds__(32 * kBrickWarps) k_brick_assemble(ContinuumVi
       for (int k = 0; k < 3; k++) acc[i][k] = 0.0;
 #pragma unroll 2
     for (int ip = 0; ip < 8; ip++) {
-      const double *Ga = sg[w][el][ip][a], *Gb = sg[w][el][ip][b];
-      const double ga0 = Ga[0], ga1 = Ga[1], ga2 = Ga[2];
-      const double gb0 = Gb[0], gb1 = Gb[1], gb2 = Gb[2];
-      const double ha[3] = {sh[w][el][ip][a][0], sh[w][el][ip][a][1], sh[w][el][ip][a][2]};
-      const double hb[3] = {sh[w][el][ip][b][0], sh[w][el][ip][b][1], sh[w][el][ip][b][2]};
-      const double da = sc[w][el][ip][0], dbh = sc[w][el][ip][1], dc = sc[w][el][ip][2];
-      const double ga[3] = {ga0, ga1, ga2}, gb[3] = {gb0, gb1, gb2};
-      const double dot = dbh * (ga0 * gb0 + ga1 * gb1 + ga2 * gb2);
-      double ua[3], va[3], wa[3];
-#pragma unroll
-      for (int i = 0; i < 3; i++) { ua[i] = da * ga[i]; va[i] = dbh * ga[i]; wa[i] = dc * ha[i]; }
+      const double *Ga = S.g[el][ip][a], *Gb = S.g[el][ip][b], *Hb = S.h[el][ip][b];
+      const double *Ua = S.u[el][ip][a], *Va = S.vv[el][ip][a], *Wa = S.w[el][ip][a];
+      const double gb[3] = {Gb[0], Gb[1], Gb[2]}, hb[3] = {Hb[0], Hb[1], Hb[2]};
+      const double ua[3] = {Ua[0], Ua[1], Ua[2]}, va[3] = {Va[0], Va[1], Va[2]};
+      const double wa[3] = {Wa[0], Wa[1], Wa[2]};
+      const double dot = S.sb[el][ip] * (Ga[0] * gb[0] + Ga[1] * gb[1] + Ga[2] * gb[2]);
 #pragma unroll
       for (int i = 0; i < 3; i++) {
 #pragma unroll
