@@ -927,7 +927,7 @@ def run_reference_brick(args):
             rates.append(sum(pool.map(_brick_worker, [(per_step,)] * cores)))
         wall = time.perf_counter() - t0
     value = float(np.mean(rates))
-    npts = BRICK["nx"] * BRICK["ny"] * BRICK["nz"] * 8
+    npts = int(np.prod(args.brick_dims)) * 8
     s = BRICK_SAMPLE
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT,
@@ -949,13 +949,14 @@ def run_reference_brick(args):
 def run_brick(args):
     world, rank, local, torch, dist = dist_setup()
     from xara_gb300 import configs, gpu
-    desc, _ = configs.brick_block(**BRICK, steps=1)
+    dims = dict(zip(("nx", "ny", "nz"), args.brick_dims))
+    desc, _ = configs.brick_block(**dims, steps=1)
     npts = desc.num_elems * 8
     t_setup = time.perf_counter()
     m = gpu.DeviceModel(desc)
     m.set_system(gpu.XG_SYSTEM_BJPCG)
     t_setup = time.perf_counter() - t_setup
-    U = brick_trial_field(desc, **BRICK)
+    U = brick_trial_field(desc, **dims)
     m.set_trial_disp(U)
     fp64_peak = fp64_peak_probe()
     stream = torch.cuda.ExternalStream(gpu.model_stream(m))
@@ -1056,7 +1057,7 @@ def run_brick(args):
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * phase_s,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f64", "data": "synthetic (seeded trial displacement field)",
-        "config": {"workload": f"stdBrick J2 {BRICK['nx']}x{BRICK['ny']}x{BRICK['nz']} "
+        "config": {"workload": f"stdBrick J2 {dims['nx']}x{dims['ny']}x{dims['nz']} "
                                "element phase (one Newton iteration)",
                    "elements": desc.num_elems, "points": npts, "equations": m.neq,
                    "nnz": m.nnz, "parallelism": f"replicas x{world}",
@@ -1106,6 +1107,8 @@ def main():
     ap.add_argument("--adj-frames", type=int, default=64)
     ap.add_argument("--adj-steps", type=int, default=2000)
     ap.add_argument("--ckpt-every", type=int, default=100)
+    ap.add_argument("--brick-dims", type=int, nargs=3, default=[BRICK["nx"], BRICK["ny"], BRICK["nz"]],
+                    metavar=("NX", "NY", "NZ"), help="brick workload mesh (a smaller case for profiling)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     if args.impl == "reference":
