@@ -13,7 +13,7 @@ import pytest
 
 from oracle import port
 from xara_gb300 import configs
-from xara_gb300._abi import XG_UNI_ELASTIC, XG_UNI_STEEL02
+from xara_gb300._abi import XG_UNI_CONCRETE02, XG_UNI_ELASTIC, XG_UNI_STEEL02
 
 FIELDS = (0, 1, 2, 3, 4, 5, 6, 9, 10)            # continuous record fields
 
@@ -119,6 +119,112 @@ def test_steel02_vjp_zero_increment_and_elastic():
         q2 = q.copy()
         q2[10] = 1e6                             # initial stress: not covered
         gpu.uniaxial_vjp(XG_UNI_STEEL02, q2, hc, 1e-3, yb)
+
+
+C02_FIELDS = (0, 1, 9, 10)                       # ecmin, dept, sig, eps
+
+
+def _c02_branch(q, hc, eps):
+    """Which piece of Concrete02's law a trial strain lands on (a label;
+    finite differences are taken only where every perturbation stays on
+    it)."""
+    fc, e0, fcu, ecu = (-abs(v) for v in q[:4])
+    rat, ft, Ets = q[4], q[5], q[6]
+
+    def compr(x):
+        if x >= e0:
+            return "c0", fc * (x / e0) * (2 - x / e0)
+        if x > ecu:
+            return "c1", (fcu - fc) * (x - e0) / (ecu - e0) + fc
+        return "c2", fcu
+
+    def tens(x):
+        Ec0 = 2 * fc / e0
+        if x <= ft / Ec0:
+            return "t0"
+        return "t1" if x <= ft * (1 / Ets + 1 / Ec0) else "t2"
+
+    if abs(eps - hc[10]) < np.finfo(float).eps:
+        return "zero"
+    if eps < hc[0]:
+        return "env-" + compr(eps)[0]
+    ec0 = 2 * fc / e0
+    epsr = (fcu - rat * ec0 * ecu) / (ec0 * (1 - rat))
+    _, sigmm = compr(hc[0])
+    er = (sigmm - ec0 * epsr) / (hc[0] - epsr)
+    ept = hc[0] - sigmm / er
+    if eps <= ept:
+        sig = hc[9] + ec0 * (eps - hc[10])
+        which = "elastic"
+        if sig <= sigmm + er * (eps - hc[0]):
+            sig, which = sigmm + er * (eps - hc[0]), "lower"
+        if sig >= er * 0.5 * (eps - ept):
+            which = "upper"
+        return "unload-" + which
+    if eps <= ept + hc[1]:
+        return "reload-" + tens(hc[1])
+    return "tension-" + tens(eps - ept)
+
+
+def _c02_fd_check(q, hc, eps, rng, rel=1e-7):
+    gpu = _gpu()
+    sc = np.full(12, abs(q[1]))
+    sc[9] = abs(q[0])
+    yb = np.zeros(12)
+    yb[list(C02_FIELDS)] = rng.normal(size=len(C02_FIELDS)) / sc[list(C02_FIELDS)]
+    hb, sb, qb = gpu.uniaxial_vjp(XG_UNI_CONCRETE02, q, hc, eps, yb)
+    label = _c02_branch(q, hc, eps)
+
+    def J(hc_, eps_, q_):
+        return float(yb @ port.uniaxial_trial(XG_UNI_CONCRETE02, q_, hc_, eps_))
+
+    checks = []
+    h = rel * sc[10]
+    if _c02_branch(q, hc, eps + h) == label == _c02_branch(q, hc, eps - h):
+        checks.append(("strain", sb, (J(hc, eps + h, q) - J(hc, eps - h, q)) / (2 * h), sc[10]))
+    for f in C02_FIELDS:
+        h = rel * sc[f]
+        hp, hm = hc.copy(), hc.copy()
+        hp[f] += h
+        hm[f] -= h
+        if _c02_branch(q, hp, eps) == label == _c02_branch(q, hm, eps):
+            checks.append((f"record{f}", hb[f], (J(hp, eps, q) - J(hm, eps, q)) / (2 * h), sc[f]))
+    for k in range(3):
+        h = rel * abs(q[k])
+        qp, qm = q.copy(), q.copy()
+        qp[k] += h
+        qm[k] -= h
+        if _c02_branch(qp, hc, eps) == label == _c02_branch(qm, hc, eps):
+            checks.append((f"param[{k}]", qb[k], (J(hc, eps, qp) - J(hc, eps, qm)) / (2 * h),
+                           abs(q[k])))
+    total = sum(abs(a) * s for _, a, _, s in checks) + 1e-30
+    for name, a, b, s in checks:
+        assert abs(a - b) * s <= 2e-6 * total, (label, name, a, b)
+    return label
+
+
+def test_concrete02_vjp_against_finite_differences():
+    """Concrete02's vector-Jacobian product against central differences of
+    the oracle's law along a path through every piece of it: the compression
+    envelope's three regions, unloading (elastic step, lower and upper
+    bound), reloading towards the tension point and along the tension
+    envelope and its softening branch."""
+    q = configs.concrete02_row(fc=30e6)
+    segs = [np.linspace(0, -0.003, 25), np.linspace(-0.003, -0.0012, 12),
+            np.linspace(-0.0012, -0.0045, 20), np.linspace(-0.0045, 0.0004, 40),
+            np.linspace(0.0004, -0.0005, 12), np.linspace(-0.0005, 0.0012, 25),
+            np.linspace(0.0012, -0.0075, 50), np.linspace(-0.0075, -0.004, 10)]
+    strains = np.concatenate(segs)
+    hc = port.uniaxial_init(XG_UNI_CONCRETE02, q)
+    rng = np.random.default_rng(7)
+    labels = set()
+    for e in strains[1:]:
+        if abs(e - hc[10]) > 1e-9:
+            labels.add(_c02_fd_check(q, hc, float(e), rng))
+        hc = port.uniaxial_trial(XG_UNI_CONCRETE02, q, hc, float(e))
+    need = {"env-c0", "env-c1", "env-c2", "unload-elastic", "unload-lower", "unload-upper",
+            "tension-t0", "tension-t1"}
+    assert need <= labels, labels
 
 
 # ---------------------------------------------------------------------------

@@ -100,6 +100,7 @@ __device__ __forceinline__ void fiber_vjp(int type, const double *q, const doubl
                                           double strain, const double *yb, double *hb,
                                           double *sb, double *qb) {
   if (type == XG_UNI_STEEL02) steel02_vjp(q, hc, strain, yb, hb, sb, qb);
+  else if (type == XG_UNI_CONCRETE02) concrete02_vjp(q, hc, strain, yb, hb, sb, qb);
   else elastic_vjp(q, strain, yb, hb, sb, qb);
 }
 
@@ -484,6 +485,8 @@ extern "C" int xg_uniaxial_vjp(int type, const double *q, const double *hc, doub
   if (type == XG_UNI_STEEL02) {
     if (q[10] != 0.0) return XG_EINVAL;
     xg::steel02_vjp(q, hc, strain, yb, hb, sb, qb);
+  } else if (type == XG_UNI_CONCRETE02) {
+    xg::concrete02_vjp(q, hc, strain, yb, hb, sb, qb);
   } else if (type == XG_UNI_ELASTIC) {
     xg::elastic_vjp(q, strain, yb, hb, sb, qb);
   } else {

@@ -6,10 +6,10 @@
 // record's continuous fields and returns the adjoints of the strain, of the
 // committed record's fields and of the first three parameters.
 //
-// Record layout (12 doubles): 0 epsmin 1 epsmax 2 epspl 3 epss0 4 sigs0
-// 5 epsr 6 sigr 7 kon 8 e 9 sig 10 eps.  Field 7 (the loading branch) is
-// discrete and field 8 (the tangent) is read by no later step, so their
-// adjoints are not formed.
+// Record layout (12 doubles): Steel02 0 epsmin 1 epsmax 2 epspl 3 epss0
+// 4 sigs0 5 epsr 6 sigr 7 kon; Concrete02 0 ecmin 1 dept; all 8 e 9 sig
+// 10 eps.  Field 7 (the loading branch) is discrete and field 8 (the
+// tangent) is read by no later step, so their adjoints are not formed.
 #pragma once
 
 #include <float.h>
@@ -188,6 +188,189 @@ XG_HD inline void steel02_vjp(const double *q, const double *hc, double strain, 
   qb[0] = b_Fy;
   qb[1] = b_E0;
   qb[2] = b_b;
+}
+
+// Concrete02 compression envelope (Concrete02.cpp:448-497) and its partial
+// derivatives in the strain and in fc, epsc0, fcu (signs already negative).
+XG_HD inline double c02_compr_d(double fc, double epsc0, double fcu, double epscu, double x,
+                                double *d_x, double *d_fc, double *d_e0, double *d_fcu) {
+  if (x >= epsc0) {
+    const double r = x / epsc0;
+    *d_x = fc * (2.0 - 2.0 * r) / epsc0;
+    *d_fc = r * (2.0 - r);
+    *d_e0 = -fc * (2.0 - 2.0 * r) * r / epsc0;
+    *d_fcu = 0.0;
+    return fc * r * (2.0 - r);
+  }
+  if (x > epscu) {
+    const double D = epscu - epsc0, t = (x - epsc0) / D;
+    *d_x = (fcu - fc) / D;
+    *d_fc = 1.0 - t;
+    *d_e0 = (fcu - fc) * (x - epscu) / (D * D);
+    *d_fcu = t;
+    return (fcu - fc) * t + fc;
+  }
+  *d_x = *d_fc = *d_e0 = 0.0;
+  *d_fcu = 1.0;
+  return fcu;
+}
+
+// Concrete02 tension envelope (Concrete02.cpp:421-446) and its partial
+// derivatives in the strain and in the initial modulus Ec0 = 2 fc / epsc0
+// (ft and Ets are held fixed).
+XG_HD inline double c02_tens_d(double Ec0, double ft, double Ets, double x, double *d_x,
+                               double *d_Ec0) {
+  const double eps0 = ft / Ec0;
+  const double epsu = ft * (1.0 / Ets + 1.0 / Ec0);
+  if (x <= eps0) {
+    *d_x = Ec0;
+    *d_Ec0 = x;
+    return x * Ec0;
+  }
+  if (x <= epsu) {
+    *d_x = -Ets;
+    *d_Ec0 = -Ets * ft / (Ec0 * Ec0);
+    return ft - Ets * (x - eps0);
+  }
+  *d_x = *d_Ec0 = 0.0;
+  return 0.0;
+}
+
+// Concrete02::setTrialStrain (Concrete02.cpp:167-271), swept backwards
+// branch by branch: the compression envelope (three regions), unloading
+// from it (the elastic step, the lower and the upper bound of the
+// unloading fan), and reloading in tension towards and along the tension
+// envelope.  Record fields: 0 ecmin, 1 dept, 9 sig, 10 eps.  Parameters q:
+// fc epsc0 fcu epscu rat ft Ets (the constructor's sign normalisation,
+// Concrete02.cpp:97-111, applies); qb receives d/d(fc, epsc0, fcu) of the
+// unnormalised parameters.  A strain within DBL_EPSILON of the committed one
+// keeps the previous trial stress, which after a commit is the committed
+// stress.
+XG_HD inline void concrete02_vjp(const double *q, const double *hc, double strain,
+                                 const double *yb, double *hb, double *sb, double *qb) {
+  const double s_fc = q[0] > 0 ? -1.0 : 1.0, s_e0 = q[1] > 0 ? -1.0 : 1.0;
+  const double s_fcu = q[2] > 0 ? -1.0 : 1.0;
+  const double fc = s_fc * q[0], epsc0 = s_e0 * q[1], fcu = s_fcu * q[2];
+  const double epscu = q[3] > 0 ? -q[3] : q[3], rat = q[4], ft = q[5], Ets = q[6];
+  const double eps = strain;
+  const double ecmin_c = hc[0], dept_c = hc[1], sigP = hc[9], epsP = hc[10];
+  const double deps = eps - epsP;
+  for (int k = 0; k < 12; k++) hb[k] = 0.0;
+  qb[0] = qb[1] = qb[2] = 0.0;
+  if (fabs(deps) < DBL_EPSILON) {
+    hb[0] = yb[0];
+    hb[1] = yb[1];
+    hb[9] = yb[9];
+    *sb = yb[10];
+    return;
+  }
+  const double ec0 = fc * 2. / epsc0;
+  const double b_sig = yb[9];
+  double b_eps = yb[10], b_fc = 0.0, b_e0 = 0.0, b_fcu = 0.0, b_ec0 = 0.0;
+  double hb0 = 0.0, hb1 = 0.0, b_sigP = 0.0, b_epsP = 0.0;
+  if (eps < ecmin_c) {
+    // on the compression envelope; ecmin = eps
+    double dx, dfc, de0, dfcu;
+    c02_compr_d(fc, epsc0, fcu, epscu, eps, &dx, &dfc, &de0, &dfcu);
+    b_eps += yb[0] + b_sig * dx;
+    b_fc += b_sig * dfc;
+    b_e0 += b_sig * de0;
+    b_fcu += b_sig * dfcu;
+    hb1 = yb[1];
+  } else {
+    hb0 = yb[0];
+    const double Dn = ec0 * (1.0 - rat);
+    const double epsr = (fcu - rat * ec0 * epscu) / Dn;
+    const double sigmr = ec0 * epsr;
+    double mdx, mdfc, mde0, mdfcu;
+    const double sigmm = c02_compr_d(fc, epsc0, fcu, epscu, ecmin_c, &mdx, &mdfc, &mde0, &mdfcu);
+    const double den = ecmin_c - epsr;
+    const double er = (sigmm - sigmr) / den;
+    const double ept = ecmin_c - sigmm / er;
+    double b_er = 0.0, b_ept = 0.0, b_sigmm = 0.0;
+    if (eps <= ept) {
+      hb1 = yb[1];
+      const double sigmin = sigmm + er * (eps - ecmin_c);
+      const double sigmax = er * .5 * (eps - ept);
+      double sig = sigP + ec0 * deps;
+      int which = 0;
+      if (sig <= sigmin) { sig = sigmin; which = 1; }
+      if (sig >= sigmax) { sig = sigmax; which = 2; }
+      if (which == 0) {
+        b_sigP += b_sig;
+        b_ec0 += b_sig * deps;
+        b_eps += b_sig * ec0;
+        b_epsP -= b_sig * ec0;
+      } else if (which == 1) {
+        b_sigmm += b_sig;
+        b_er += b_sig * (eps - ecmin_c);
+        b_eps += b_sig * er;
+        hb0 -= b_sig * er;
+      } else {
+        b_er += b_sig * .5 * (eps - ept);
+        b_eps += b_sig * .5 * er;
+        b_ept -= b_sig * .5 * er;
+      }
+    } else if (eps <= ept + dept_c) {
+      // towards the tension envelope's last point: sig = e (eps - ept),
+      // e = sicn / dept (ec0 when dept is zero)
+      hb1 = yb[1];
+      double e, de_dept = 0.0, de_dEc0 = 0.0;
+      if (dept_c != 0.0) {
+        double tdx, tdE;
+        const double sicn = c02_tens_d(ec0, ft, Ets, dept_c, &tdx, &tdE);
+        e = sicn / dept_c;
+        de_dept = (tdx * dept_c - sicn) / (dept_c * dept_c);
+        de_dEc0 = tdE / dept_c;
+      } else {
+        e = ec0;
+        de_dEc0 = 1.0;
+      }
+      const double b_e = b_sig * (eps - ept);
+      b_eps += b_sig * e;
+      b_ept -= b_sig * e;
+      hb1 += b_e * de_dept;
+      b_ec0 += b_e * de_dEc0;
+    } else {
+      // on the tension envelope; dept = eps - ept
+      double tdx, tdE;
+      c02_tens_d(ec0, ft, Ets, eps - ept, &tdx, &tdE);
+      b_eps += yb[1] + b_sig * tdx;
+      b_ept -= yb[1] + b_sig * tdx;
+      b_ec0 += b_sig * tdE;
+    }
+    // ept = ecmin - sigmm / er
+    hb0 += b_ept;
+    b_sigmm -= b_ept / er;
+    b_er += b_ept * sigmm / (er * er);
+    // er = (sigmm - sigmr) / (ecmin - epsr)
+    b_sigmm += b_er / den;
+    const double b_sigmr = -b_er / den;
+    const double b_den = -b_er * er / den;
+    hb0 += b_den;
+    double b_epsr = -b_den;
+    // sigmm = Compr_Envlp(ecmin)
+    hb0 += b_sigmm * mdx;
+    b_fc += b_sigmm * mdfc;
+    b_e0 += b_sigmm * mde0;
+    b_fcu += b_sigmm * mdfcu;
+    // sigmr = ec0 epsr, epsr = (fcu - rat ec0 epscu) / (ec0 (1 - rat))
+    b_ec0 += b_sigmr * epsr;
+    b_epsr += b_sigmr * ec0;
+    b_fcu += b_epsr / Dn;
+    b_ec0 += b_epsr * (-rat * epscu - epsr * (1.0 - rat)) / Dn;
+  }
+  // ec0 = 2 fc / epsc0
+  b_fc += b_ec0 * 2.0 / epsc0;
+  b_e0 -= b_ec0 * ec0 / epsc0;
+  hb[0] = hb0;
+  hb[1] = hb1;
+  hb[9] = b_sigP;
+  hb[10] = b_epsP;
+  *sb = b_eps;
+  qb[0] = s_fc * b_fc;
+  qb[1] = s_e0 * b_e0;
+  qb[2] = s_fcu * b_fcu;
 }
 
 // Elastic fiber: sig = E eps (parameter 0).
