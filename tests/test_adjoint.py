@@ -286,6 +286,70 @@ def test_adjoint_gradient_matches_finite_differences(need_gpu, pga_scale, steps)
 
 
 @pytest.mark.gpu
+@pytest.mark.parametrize("pga_scale,steps", [(1.0, 40), (3.0, 80)])
+def test_adjoint_rc_frames_match_finite_differences(need_gpu, pga_scale, steps):
+    """Reinforced-concrete members (Concrete02 layers and Steel02 bars, two
+    materials per member): gradients with respect to every member's fc,
+    epsc0, fcu and Fy, E0, b against central differences of the device
+    forward run, through cracking, crushing and yielding at the stronger
+    record; betaK0 damping on such members is refused."""
+    gpu = _gpu()
+    desc, phases = configs.adjoint_rc_frames(n_frames=2, steps=steps, seed=5,
+                                             pga_scale=pga_scale)
+    ph = phases[0]
+    node, dof, w = _objective(desc)
+    q0 = desc.uni_param.reshape(-1, 12).copy()
+    conc = np.asarray(desc.uni_type) == XG_UNI_CONCRETE02
+    with gpu.DeviceModel(desc) as m:
+        J0 = gpu.adjoint_forward(m, ph, steps, 10, node, dof, w)
+        rec = m.fiber_records()
+        g = gpu.adjoint_backward(m)
+        assert J0 > 0 and np.isfinite(g).all()
+        assert np.abs(g[conc]).max() > 0 and np.abs(g[~conc]).max() > 0
+        if pga_scale > 1.0:
+            # cracked concrete (a tension excursion recorded) and yielded bars
+            ss, fm = desc.arrays["sec_fiber_start"], desc.arrays["fib_mat"]
+            kinds = np.concatenate([np.tile(np.asarray(desc.uni_type)[fm[ss[s_]:ss[s_ + 1]]],
+                                            desc.fbc_num_ip)
+                                    for s_ in desc.arrays["elem_mat"]])
+            c_rec, s_rec = rec[kinds == XG_UNI_CONCRETE02], rec[kinds == XG_UNI_STEEL02]
+            assert (c_rec[:, 1] > 0).mean() > 0.05
+            assert (np.abs(s_rec[:, 10]) > 420e6 / 200e9).mean() > 0.001
+
+        def J(q):
+            gpu.set_uniaxial_params(m, q)
+            return gpu.adjoint_forward(m, ph, steps, 10, node, dof, w)
+
+        rng = np.random.default_rng(13)
+        scale = np.abs(q0[:, :3])
+        d = rng.normal(size=scale.shape) * scale
+        h = 1e-6
+        qp, qm = q0.copy(), q0.copy()
+        qp[:, :3] += h * d
+        qm[:, :3] -= h * d
+        fd = (J(qp) - J(qm)) / (2 * h)
+        ad = float((g * d).sum())
+        assert ad == pytest.approx(fd, rel=1e-4), (ad, fd)
+        gs = np.abs(g) * scale
+        for sel in (conc, ~conc):
+            idx = np.nonzero(sel)[0]
+            top = idx[np.argsort(gs[idx].max(axis=1))[-2:]]
+            for u in top:
+                k = int(np.argmax(gs[u]))
+                qp, qm = q0.copy(), q0.copy()
+                qp[u, k] *= 1 + h
+                qm[u, k] *= 1 - h
+                fd = (J(qp) - J(qm)) / (2 * h * q0[u, k])
+                assert g[u, k] == pytest.approx(fd, rel=1e-3, abs=1e-4 * gs.max() / abs(q0[u, k])), \
+                    (u, k)
+        # betaK0 Rayleigh damping is covered for single-material members only
+        gpu.set_uniaxial_params(m, q0)
+        phk = configs.adjoint_frames(n_frames=2, steps=steps, seed=5)[1][0]
+        with pytest.raises(gpu.XaraGpuError, match="betaK0"):
+            gpu.adjoint_forward(m, phk, steps, 10, node, dof, w)
+
+
+@pytest.mark.gpu
 def test_adjoint_checkpoint_interval_and_end_state(need_gpu):
     gpu = _gpu()
     desc, ph = _adjoint_model(n_frames=3, steps=30, seed=9)

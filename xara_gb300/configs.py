@@ -609,3 +609,47 @@ def adjoint_frames(n_frames=64, steps=2000, dt=0.01, seed=0, nfib=40, member_cov
                     obj_dof=np.zeros(n_frames, np.int32), obj_weight=np.asarray(obj_w),
                     members=ne)
     return out, [ph]
+
+
+
+def adjoint_rc_frames(n_frames=2, steps=2000, dt=0.01, seed=0, member_cov=0.05, pga_scale=1.0,
+                      ncl=12):
+    """The frames of :func:`adjoint_frames` with reinforced-concrete members:
+    every member a 0.4 x 0.5 m section of ``ncl`` Concrete02 layers (fc
+    30 MPa, epsc0 0.002, fcu 0.2 fc, epscu 0.006, ft 0.1 fc) and two layers of
+    Steel02 bars (4 x 491 mm^2 each, 50 mm cover; fy 420 MPa, E 200 GPa,
+    b 0.01), one concrete and one steel material per member with fc and fy
+    varied by a lognormal factor of CoV ``member_cov``; mass-proportional
+    Rayleigh damping only.  Same objective terms as :func:`adjoint_frames`."""
+    desc, phases = adjoint_frames(n_frames=n_frames, steps=steps, dt=dt, seed=seed,
+                                  member_cov=member_cov, pga_scale=pga_scale)
+    a = desc.arrays
+    ne = len(a["elem_tag"])
+    rng = np.random.default_rng(seed + 23)
+    b, h, cover, bar = 0.4, 0.5, 0.05, 4 * 491e-6
+    yc = (np.arange(ncl) + 0.5) * h / ncl - h / 2
+    ys = np.array([h / 2 - cover, -(h / 2 - cover)])
+    fy_sec = np.concatenate([yc, ys])
+    fa_sec = np.concatenate([np.full(ncl, b * h / ncl), np.full(2, bar)])
+    nf = ncl + 2
+    rows, types = [], []
+    fc = 30e6 * np.exp(rng.normal(0.0, member_cov, ne))
+    fy = 420e6 * np.exp(rng.normal(0.0, member_cov, ne))
+    for e in range(ne):
+        rows.append(concrete02_row(fc=fc[e]))
+        rows.append(steel02_row(fy=fy[e], E=200e9, b=0.01, R0=18.0))
+        types += [XG_UNI_CONCRETE02, XG_UNI_STEEL02]
+    fib_mat = np.concatenate([np.r_[np.full(ncl, 2 * e), np.full(2, 2 * e + 1)]
+                              for e in range(ne)])
+    kw = {k: v for k, v in a.items() if v is not None}
+    kw.update(elem_mat=np.arange(ne), sec_fiber_start=np.arange(ne + 1) * nf,
+              fib_y=np.tile(fy_sec, ne), fib_area=np.tile(fa_sec, ne), fib_mat=fib_mat,
+              uni_type=np.asarray(types), uni_param=np.asarray(rows))
+    out = ModelDesc(ndm=desc.ndm, ndf=desc.ndf, elem_type=desc.elem_type,
+                    geom_transf=desc.geom_transf, fbc_num_ip=desc.fbc_num_ip, **kw)
+    ph = phases[0]
+    ph.beta_k_init_elem = np.zeros(ne)
+    ph.kw["beta_k_init"] = 0.0
+    out.meta = dict(desc.meta, workload=f"{n_frames} 2D RC frames, Concrete02 and Steel02 per "
+                    "member")
+    return out, [ph]

@@ -96,6 +96,29 @@ __device__ void basic_T(const FrameView &v, int e, double (*T)[NB == 3 ? 6 : 12]
   }
 }
 
+// tq[slot] += qb, slot known only at run time (no dynamic register indexing)
+__device__ __forceinline__ void add_slot(double (&tq)[kAdjSlots][3], int slot, const double *qb) {
+#pragma unroll
+  for (int m = 0; m < kAdjSlots; m++)
+    if (slot == m) {
+      tq[m][0] += qb[0];
+      tq[m][1] += qb[1];
+      tq[m][2] += qb[2];
+    }
+}
+
+// warp sums of tq, added to the element's slots by lane 0
+__device__ __forceinline__ void theta_add(const AdjView &a, int e, int lane,
+                                          double (&tq)[kAdjSlots][3]) {
+#pragma unroll
+  for (int m = 0; m < kAdjSlots; m++)
+#pragma unroll
+    for (int k = 0; k < 3; k++) {
+      const double t = warp_sum_adj(tq[m][k]);
+      if (lane == 0) a.theta[(3L * kAdjSlots) * e + 3 * m + k] += t;
+    }
+}
+
 __device__ __forceinline__ void fiber_vjp(int type, const double *q, const double *hc,
                                           double strain, const double *yb, double *hb,
                                           double *sb, double *qb) {
@@ -123,7 +146,7 @@ __global__ void __launch_bounds__(32 * kAdjWarps) k_adj_elem_a(FrameView v, AdjV
   const double ybar = v.ybar[sec], zbar = ORD == 4 ? v.zbar[sec] : 0.0;
   const long fbase = v.foff[e];
   double *scr = a.scr + (long)e * (6 + nip * 4);
-  double tq0 = 0.0, tq1 = 0.0, tq2 = 0.0;
+  double tq[kAdjSlots][3] = {};
   double Sb[NB];
 #pragma unroll
   for (int i = 0; i < NB; i++) Sb[i] = 0.0;
@@ -155,7 +178,7 @@ __global__ void __launch_bounds__(32 * kAdjWarps) k_adj_elem_a(FrameView v, AdjV
       fiber_vjp(v.utype[u], q, hc, strain, yb, hb, &sb, qb);
 #pragma unroll
       for (int k = 0; k < 12; k++) hbr[k] = hb[k];
-      tq0 += qb[0]; tq1 += qb[1]; tq2 += qb[2];
+      add_slot(tq, a.fslot[kf], qb);
       eb0 += sb;
       eb1 += -y * sb;
       if (ORD == 4) eb2 += z * sb;
@@ -189,9 +212,7 @@ __global__ void __launch_bounds__(32 * kAdjWarps) k_adj_elem_a(FrameView v, AdjV
     for (int k = 0; k < NB; k++) s += kv[i * NB + k] * Sb[k];
     zA[i] = s;
   }
-  tq0 = warp_sum_adj(tq0);
-  tq1 = warp_sum_adj(tq1);
-  tq2 = warp_sum_adj(tq2);
+  theta_add(a, e, lane, tq);
   if (lane == 0) {
     double T[NB][NU];
     basic_T<NB>(v, e, T);
@@ -205,9 +226,6 @@ __global__ void __launch_bounds__(32 * kAdjWarps) k_adj_elem_a(FrameView v, AdjV
     }
 #pragma unroll
     for (int i = 0; i < NB; i++) scr[i] = zA[i];
-    a.theta[3L * e + 0] += tq0;
-    a.theta[3L * e + 1] += tq1;
-    a.theta[3L * e + 2] += tq2;
   }
 }
 
@@ -259,7 +277,7 @@ __global__ void __launch_bounds__(32 * kAdjWarps) k_adj_elem_b(FrameView v, AdjV
     for (int k = 0; k < NB; k++) s -= kv[i * NB + k] * pb[k];
     z[i] = scr[i] + s;
   }
-  double tq0 = 0.0, tq1 = 0.0, tq2 = 0.0;
+  double tq[kAdjSlots][3] = {};
   constexpr int kRow[6] = {0, 1, 1, 2, 2, 3};
   for (int ip = 0; ip < nip; ip++) {
     const double xL = v.xi[ip], xL1 = xL - 1.0, wtL = v.wt[ip] * L;
@@ -307,14 +325,14 @@ __global__ void __launch_bounds__(32 * kAdjWarps) k_adj_elem_b(FrameView v, AdjV
       fiber_vjp(v.utype[u], q, hc, strain, yb, hb, &sb, qb);
 #pragma unroll
       for (int k = 0; k < 12; k++) hbr[k] += hb[k];
-      tq0 += qb[0]; tq1 += qb[1]; tq2 += qb[2];
+      add_slot(tq, a.fslot[kf], qb);
     }
   }
-  tq0 = warp_sum_adj(tq0);
-  tq1 = warp_sum_adj(tq1);
-  tq2 = warp_sum_adj(tq2);
+  theta_add(a, e, lane, tq);
   if (lane == 0) {
     if (a.use_k0) {
+      // elements under betaK0 damping have one Steel02 or elastic material
+      // (slot 0), in which K0 is linear
       // kv0 = (sum_s w_s b_s' fs0 b_s)^-1 (ForceBeamColumn2d/3d::getInitialStiff)
       const double *fs0 = v.fs0 + 16 * (long)sec;
       double f[NB * NB];
@@ -350,11 +368,8 @@ __global__ void __launch_bounds__(32 * kAdjWarps) k_adj_elem_b(FrameView v, AdjV
       const double E = v.uparam[(long)u * XG_UNI_NPARAM + ie];
       const double bk = a.bk0 ? a.bk0[e] : a.bk0_all;
       const double d = -bk / E * val;
-      if (ie == 1) tq1 += d; else tq0 += d;
+      a.theta[(3L * kAdjSlots) * e + ie] += d;
     }
-    a.theta[3L * e + 0] += tq0;
-    a.theta[3L * e + 1] += tq1;
-    a.theta[3L * e + 2] += tq2;
   }
 }
 
@@ -366,7 +381,7 @@ __global__ void k_adj_init_records(FrameView v, AdjView a) {
   if (e >= v.ne) return;
   const int sec = v.sec[e];
   const int f0 = v.sec_fstart[sec], nf = v.sec_fstart[sec + 1] - f0;
-  double t0 = 0.0, t1 = 0.0;
+  double tq[kAdjSlots][3] = {};
   for (int k = lane; k < v.nip * nf; k += 32) {
     const int kf = f0 + k % nf;
     const int u = v.fmat[kf];
@@ -374,15 +389,10 @@ __global__ void k_adj_init_records(FrameView v, AdjView a) {
     const double *q = v.uparam + (long)u * XG_UNI_NPARAM;
     const double *hb = a.hbar + (v.foff[e] + k) * 12;
     const double d = hb[1] - hb[0];
-    t0 += d / q[1];
-    t1 -= d * q[0] / (q[1] * q[1]);
+    const double qb[3] = {d / q[1], -d * q[0] / (q[1] * q[1]), 0.0};
+    add_slot(tq, a.fslot[kf], qb);
   }
-  t0 = warp_sum_adj(t0);
-  t1 = warp_sum_adj(t1);
-  if (lane == 0) {
-    a.theta[3L * e + 0] += t0;
-    a.theta[3L * e + 1] += t1;
-  }
+  theta_add(a, e, lane, tq);
 }
 
 // J_k += w_k U[dof_k]^2, one accumulator per term

@@ -269,11 +269,15 @@ struct NewmarkCoef {
   double c2, c3;              // velocity / acceleration per displacement increment
   double a1, a2, a3, a4;      // predictor: V = a1 Vc + a2 Ac, A = a4 Ac + a3 Vc
 };
+// materials per element section the adjoint keeps apart (parameter adjoints
+// are accumulated per element and material slot)
+constexpr int kAdjSlots = 4;
+
 struct AdjView {
   const double *st;           // converged element state of the step [ne*stride]
   const double *fh_prev;      // committed fiber records before the step [nrec*12]
   double *hbar;               // [nrec*12] record adjoint: after the step in, before it out
-  double *theta;              // [ne*3] parameter adjoint of each element's material
+  double *theta;              // [ne*kAdjSlots*3] parameter adjoint per element and material slot
   double *scr;                // [ne*(6+nip*4)] pass A's z and section ebar
   const int *eqn;             // [nn*ndf]
   const double *mu;           // [neq] adjoint solution of the step
@@ -281,7 +285,8 @@ struct AdjView {
   const double *bk0;          // [ne] betaK0 per element, or null
   double bk0_all;             // betaK0 when bk0 is null
   int use_k0;                 // betaK0 K0 damping present
-  const int *elem_uni;        // [ne] the single material of each element's fibers
+  const int *elem_uni;        // [ne] the material of slot 0 (the betaK0 term's single material)
+  const int *fslot;           // [section fibers] slot of each fiber's material in its section
 };
 int launch_adj_elem_a(const FrameView &v, const AdjView &a, cudaStream_t s);
 int launch_adj_elem_b(const FrameView &v, const AdjView &a, cudaStream_t s);

@@ -216,8 +216,8 @@ struct xg_model {
     int N = 0, K = 0, nterm = 0, nck = 0;
     size_t len = 0;                        // doubles in one saved state
     std::vector<double> ck_time, Jk;        // checkpoint times; the objective's terms
-    std::vector<int> elem_uni;
-    DBuf<int> dof, d_elem_uni;
+    std::vector<int> elem_uni, fslot, sec_slots;   // sec_slots: [nsec*kAdjSlots] materials
+    DBuf<int> dof, d_elem_uni, d_fslot;
     DBuf<double> w, J, ck, seg, Ub, Vb, Ab, hbar, theta, scr, mu, rhs, tmp, kmu;
   } adj;
   long steps_since_reset = 0;
@@ -1730,29 +1730,48 @@ int xg_model::adjoint_forward(const xg_phase_desc *ph, int N, int K, const xg_ob
     return fail(XG_EINVAL, "the adjoint covers linear frame transformations");
   if (steps_since_reset != 0 || have_phase)
     return fail(XG_ESTATE, "the adjoint runs from the model's initial state (xg_reset first)");
-  // every element's fibers share one material: Steel02 without initial
-  // stress, or elastic
-  adj.elem_uni.assign(ne, 0);
-  for (int e = 0; e < ne; e++) {
-    const int sc = mat[e];
-    const int u0 = fmat[sec_fstart[sc]];
-    for (int f = sec_fstart[sc]; f < sec_fstart[sc + 1]; f++)
-      if (fmat[f] != u0)
-        return fail(XG_EINVAL, "the adjoint needs one material per element (element %d)", e);
-    if (utype[u0] == XG_UNI_STEEL02) {
-      if (uparam[(size_t)u0 * XG_UNI_NPARAM + 10] != 0.0)
-        return fail(XG_EINVAL, "the adjoint does not cover Steel02 with an initial stress");
-    } else if (utype[u0] != XG_UNI_ELASTIC) {
-      return fail(XG_EINVAL, "the adjoint covers Steel02 and elastic fibers");
+  // fiber materials: Steel02 without initial stress, Concrete02 or elastic,
+  // at most kAdjSlots of them per section (slots in order of first fiber)
+  const int nsec = (int)sec_fstart.size() - 1;
+  adj.fslot.assign(std::max(sec_fstart.back(), 1), 0);
+  adj.sec_slots.assign((size_t)std::max(nsec, 1) * kAdjSlots, -1);
+  std::vector<char> sec_single(std::max(nsec, 1), 1);   // one Steel02 / elastic material
+  for (int sc = 0; sc < nsec; sc++) {
+    int *sl = adj.sec_slots.data() + (size_t)sc * kAdjSlots;
+    for (int f = sec_fstart[sc]; f < sec_fstart[sc + 1]; f++) {
+      const int u = fmat[f];
+      int m = 0;
+      while (m < kAdjSlots && sl[m] >= 0 && sl[m] != u) m++;
+      if (m == kAdjSlots)
+        return fail(XG_EINVAL, "the adjoint keeps at most %d materials per section (section %d)",
+                    kAdjSlots, sc);
+      sl[m] = u;
+      adj.fslot[f] = m;
+      if (utype[u] == XG_UNI_STEEL02) {
+        if (uparam[(size_t)u * XG_UNI_NPARAM + 10] != 0.0)
+          return fail(XG_EINVAL, "the adjoint does not cover Steel02 with an initial stress");
+      } else if (utype[u] == XG_UNI_CONCRETE02) {
+        sec_single[sc] = 0;
+      } else if (utype[u] != XG_UNI_ELASTIC) {
+        return fail(XG_EINVAL, "the adjoint covers Steel02, Concrete02 and elastic fibers");
+      }
+      if (m > 0) sec_single[sc] = 0;
     }
-    adj.elem_uni[e] = u0;
   }
+  adj.elem_uni.assign(ne, 0);
+  for (int e = 0; e < ne; e++) adj.elem_uni[e] = std::max(adj.sec_slots[(size_t)mat[e] * kAdjSlots], 0);
   std::vector<int> dofs(obj->num_terms);
   for (int k = 0; k < obj->num_terms; k++) {
     auto it = std::lower_bound(node_tag.begin(), node_tag.end(), obj->node[k]);
     if (it == node_tag.end() || *it != obj->node[k] || obj->dof[k] < 0 || obj->dof[k] >= ndf)
       return fail(XG_EINVAL, "objective term %d: bad node or dof", k);
     dofs[k] = (int)(it - node_tag.begin()) * ndf + obj->dof[k];
+  }
+  for (int e = 0; e < ne; e++) {
+    const double bk = ph->beta_k_init_elem ? ph->beta_k_init_elem[e] : ph->beta_k_init;
+    if (bk != 0.0 && !sec_single[mat[e]])
+      return fail(XG_EINVAL, "betaK0 damping in the adjoint needs one Steel02 or elastic "
+                  "material per element (element %d)", e);
   }
   RET(xg_analysis_set_phase(this, ph));
   cudaStream_t s = stream;
@@ -1775,6 +1794,7 @@ int xg_model::adjoint_forward(const xg_phase_desc *ph, int N, int K, const xg_ob
   wv.resize(std::max<size_t>(wv.size(), 1));
   RET(adj.w.upload(wv.data(), wv.size(), s));
   RET(adj.d_elem_uni.upload(adj.elem_uni.data(), std::max<size_t>(adj.elem_uni.size(), 1), s));
+  RET(adj.d_fslot.upload(adj.fslot.data(), adj.fslot.size(), s));
   RET(adj.J.alloc(std::max(adj.nterm, 1)));
   CK(cudaMemsetAsync(adj.J.p, 0, std::max(adj.nterm, 1) * sizeof(double), s));
   adj.ck_time.assign(adj.nck + 1, 0.0);
@@ -1818,8 +1838,9 @@ int xg_model::adjoint_backward(double scale, double *grad, int num_uni) {
   }
   RET(adj.hbar.alloc(std::max<size_t>(nrec, 1)));
   CK(cudaMemsetAsync(adj.hbar.p, 0, std::max<size_t>(nrec, 1) * sizeof(double), s));
-  RET(adj.theta.alloc(std::max<size_t>((size_t)ne * 3, 1)));
-  CK(cudaMemsetAsync(adj.theta.p, 0, std::max<size_t>((size_t)ne * 3, 1) * sizeof(double), s));
+  const size_t nth = std::max<size_t>((size_t)ne * kAdjSlots * 3, 1);
+  RET(adj.theta.alloc(nth));
+  CK(cudaMemsetAsync(adj.theta.p, 0, nth * sizeof(double), s));
   RET(adj.scr.alloc(std::max<size_t>((size_t)ne * (6 + fb_nip * 4), 1)));
   const double dt = phase.dt, gam = phase.gamma, bet = phase.beta;
   NewmarkCoef c{};
@@ -1839,6 +1860,7 @@ int xg_model::adjoint_backward(double scale, double *grad, int num_uni) {
   av.bk0_all = phase.beta_k_init;
   av.use_k0 = k0_ready ? 1 : 0;
   av.elem_uni = adj.d_elem_uni.p;
+  av.fslot = adj.d_fslot.p;
   const int N = adj.N, K = adj.K;
   // the objective's last term
   RET(launch_adj_objective_grad(adj.nterm, adj.dof.p, adj.w.p, d_eqn.p,
@@ -1885,13 +1907,18 @@ int xg_model::adjoint_backward(double scale, double *grad, int num_uni) {
   }
   // the fresh records' parameters
   RET(launch_adj_init_records(fview(), av, s));
-  std::vector<double> th((size_t)ne * 3);
+  std::vector<double> th((size_t)ne * kAdjSlots * 3);
   if (ne) CK(cudaMemcpyAsync(th.data(), adj.theta.p, th.size() * sizeof(double),
                              cudaMemcpyDeviceToHost, s));
   CK(cudaStreamSynchronize(s));
   for (int k = 0; k < num_uni * 3; k++) grad[k] = 0.0;
   for (int e = 0; e < ne; e++)
-    for (int k = 0; k < 3; k++) grad[(size_t)adj.elem_uni[e] * 3 + k] += scale * th[(size_t)e * 3 + k];
+    for (int m = 0; m < kAdjSlots; m++) {
+      const int u = adj.sec_slots[(size_t)mat[e] * kAdjSlots + m];
+      if (u < 0) continue;
+      for (int k = 0; k < 3; k++)
+        grad[(size_t)u * 3 + k] += scale * th[((size_t)e * kAdjSlots + m) * 3 + k];
+    }
   RET(adj_load(adj.ck.p + (size_t)adj.nck * adj.len, adj.ck_time[adj.nck]));
   return element_state(true);
 }
