@@ -350,11 +350,12 @@ int xg_measure_fp64_peak(double *tflops);
         sensitivity).  Gradients of J = sum over the steps n = 1..N and the
         terms k of weight_k * u(node_k, dof_k, t_n)^2 with respect to the
         first three parameters of every uniaxial material (Steel02: Fy, E0,
-        b; elastic: E).  Covers force-based frames with linear
-        transformations whose elements each use one material (Steel02
-        without initial stress, or elastic), Newmark with alphaM / betaK0
-        Rayleigh damping and UniformExcitation, from the model's initial
-        state. ---- */
+        b; Concrete02: fc, epsc0, fcu; elastic: E).  Covers force-based
+        frames with linear transformations whose sections use at most four
+        materials (Steel02 without initial stress, Concrete02, elastic),
+        Newmark with alphaM Rayleigh damping (betaK0 as well where an
+        element has a single Steel02 or elastic material) and
+        UniformExcitation, from the model's initial state. ---- */
 typedef struct xg_objective_desc {
   int num_terms;
   const int *node;            /* node tags */
@@ -377,9 +378,10 @@ int xg_adjoint_objective_terms(const xg_model *m, double *Jk, int num_terms);
    is left at the state after the run's last step. */
 int xg_adjoint_backward(xg_model *m, double scale, double *grad, int num_uni);
 /* Vector-Jacobian product of one material point's trial record (host only;
-   Steel02 or elastic): given the adjoint yb[12] of the trial record (fields
-   0-6 history, 9 stress, 10 strain), the adjoints of the committed record
-   hb[12], of the strain *sb and of parameters 0-2 qb[3]. */
+   Steel02, Concrete02 or elastic): given the adjoint yb[12] of the trial
+   record (history fields: Steel02 0-6, Concrete02 0-1; 9 stress, 10
+   strain), the adjoints of the committed record hb[12], of the strain *sb
+   and of parameters 0-2 qb[3]. */
 int xg_uniaxial_vjp(int type, const double *q, const double *hc, double strain,
                     const double *yb, double *hb, double *sb, double *qb);
 
