@@ -119,12 +119,16 @@ struct ProfileSystem {
   int ntasks;
   int *next_task;          // [1] task counter
   int *upd, *done;         // [nt*(W+1)] per tile: updates applied, factored
-  double *sweep;           // [2*4*nt*32] values published by the forward / backward sweep
+  double *sweep;           // [4*4*nt*32] values published by the sweeps (y, c, x, c')
   int *flags;              // [4]
   double min_diag_tol;
-  // per tile row J, for the substitutions: W_J = L_JJ^-T, F_J = L_JJ^-1
-  // L_J,J-1 and G_J = L_JJ^-T L_J+1,J' (row-major 32 x 32 each, [nt*1024])
-  double *Winv, *F, *G;
+  // per tile row J, for the substitutions (row-major 32 x 32 each,
+  // [nt*1024]): W_J = L_JJ^-T, F_J = L_JJ^-1 L_J,J-1, G_J = L_JJ^-T
+  // L_J+1,J', E_J = L_JJ^-1 L_J,J-2, H_J = L_JJ^-T L_J+2,J',
+  // Q_J = E_J - F_J F_J-1 and R_J = H_J - G_J G_J+1 (zero where a tile is
+  // outside the envelope)
+  double *Winv, *F, *G, *E, *H, *Q, *R;
+  int *cpl;                // [nt] row J's coupling matrices written
 };
 int profile_plan(int n, const int *rowptr, const int *colidx, std::vector<int> &ftile, int &nt,
                  int &W);

@@ -176,7 +176,8 @@ struct xg_model {
   bool prof_ready = false, prof_factored = false;
   std::vector<int> ftile;
   DBuf<int> d_ftile, d_pflags, d_ptasks, d_pnext, d_pupd, d_pdone;
-  DBuf<double> d_L, d_invD, d_piv, d_px, d_Winv, d_Fc, d_Gc, d_psweep;
+  DBuf<double> d_L, d_invD, d_piv, d_px, d_Winv, d_Fc, d_Gc, d_Ec, d_Hc, d_Qc, d_Rc, d_psweep;
+  DBuf<int> d_pcpl;
   int prof_ldx = 0;
   bool prof_band = false;                      // many small parts: one band each
   BandSystem bsys{};
@@ -1333,12 +1334,15 @@ int xg_model::ensure_profile() {
   RET(d_pupd.alloc((size_t)nt * (W + 1)));
   RET(d_pdone.alloc((size_t)nt * (W + 1)));
   RET(d_pflags.alloc(4));
-  RET(d_psweep.alloc(2 * 4 * (size_t)std::max(nt, 1) * 32));
+  for (auto *b : {&d_Ec, &d_Hc, &d_Qc, &d_Rc}) RET(b->alloc((size_t)nt * 1024));
+  RET(d_pcpl.alloc((size_t)std::max(nt, 1)));
+  RET(d_psweep.alloc(4 * 4 * (size_t)std::max(nt, 1) * 32));
   psys.sweep = d_psweep.p;
   psys.n = neq; psys.nt = nt; psys.W = W;
   psys.rowptr = d_rowptr.p; psys.colidx = d_colidx.p; psys.vals = d_vals.p;
   psys.ftile = d_ftile.p; psys.L = d_L.p; psys.invD = d_invD.p; psys.piv = d_piv.p;
   psys.Winv = d_Winv.p; psys.F = d_Fc.p; psys.G = d_Gc.p;
+  psys.E = d_Ec.p; psys.H = d_Hc.p; psys.Q = d_Qc.p; psys.R = d_Rc.p; psys.cpl = d_pcpl.p;
   psys.tasks = reinterpret_cast<const int4 *>(d_ptasks.p);
   psys.ntasks = (int)(tasks.size() / 4);
   psys.next_task = d_pnext.p; psys.upd = d_pupd.p; psys.done = d_pdone.p;

@@ -298,13 +298,16 @@ __device__ bool panel_update_task(const ProfileSystem &S, int J, int q, double (
 
 // For the substitutions, off the factorisation's critical path: W_J =
 // L_JJ^-T (rows r of W solve w L_JJ' = e_r, a warp per row as in phase B),
-// F_J = L_JJ^-1 L_J,J-1 = W' L_J,J-1 and G_J = L_JJ^-T L_J+1,J' = W
-// L_J+1,J' (zero where the tile is outside the envelope).  The sweeps then
-// need one 32 x 32 product with the neighbouring row's result on their
-// dependency chain.
+// F_J = W' L_J,J-1, E_J = W' L_J,J-2, G_J = W L_J+1,J', H_J = W L_J+2,J'
+// (zero where the tile is outside the envelope), then, once row J-1's task
+// has finished, Q_J = E_J - F_J F_J-1 and R_J-1 = H_J-1 - G_J-1 G_J.  With
+// them a sweep row depends on the row two back: y_J = c3_J - F_J c_J-1 -
+// Q_J y_J-2, c_J = c3_J - E_J y_J-2 (c3_J: W' times the right-hand side
+// less rows J-3 and older), and the same backwards with G, H, R.
 __device__ void coupling_task(const ProfileSystem &S, int J, double (*sA)[kT + 1],
-                              double (*sB)[kT + 1], double (*sC)[kT + 1]) {
+                              double (*sB)[kT + 1], double (*sC)[kT + 1], volatile int *flags) {
   const int tid = threadIdx.x, w = tid >> 5, lane = tid & 31;
+  const size_t off = (size_t)J * kTT;
   const double *Ljj = tile_at(S, J, 0);
   for (int k = tid; k < kTT; k += blockDim.x) sB[k >> 5][k & 31] = __ldcg(Ljj + k);
   __syncthreads();
@@ -316,25 +319,27 @@ __device__ void coupling_task(const ProfileSystem &S, int J, double (*sA)[kT + 1
       if (lane > c) x = fma(-wc, sB[lane][c], x);
     }
     sA[r][lane] = x;
-    S.Winv[(size_t)J * kTT + r * kT + lane] = x;
+    S.Winv[off + r * kT + lane] = x;
   }
   __syncthreads();
-  for (int pass = 0; pass < 2; pass++) {
-    // pass 0: F = W' P, P = L_J,J-1;  pass 1: G = W Q', Q = L_J+1,J
-    const bool has = pass == 0 ? (J >= 1 && S.ftile[J] <= J - 1)
-                               : (J + 1 < S.nt && S.ftile[J + 1] <= J);
-    double *out = (pass == 0 ? S.F : S.G) + (size_t)J * kTT;
+  for (int pass = 0; pass < 4; pass++) {
+    // F = W' L_J,J-1, G = W L_J+1,J', E = W' L_J,J-2, H = W L_J+2,J'
+    const int o = pass < 2 ? 1 : 2;
+    const bool lower = (pass & 1) == 0;      // W' times a tile of row J
+    const bool has = lower ? (J >= o && S.ftile[J] <= J - o)
+                           : (J + o < S.nt && S.ftile[J + o] <= J);
+    double *out = (pass == 0 ? S.F : pass == 1 ? S.G : pass == 2 ? S.E : S.H) + off;
     if (!has) {
       for (int k = tid; k < kTT; k += blockDim.x) out[k] = 0.0;
       continue;
     }
-    const double *T = pass == 0 ? tile_at(S, J, 1) : tile_at(S, J + 1, 1);
+    const double *T = lower ? tile_at(S, J, o) : tile_at(S, J + o, o);
     for (int k = tid; k < kTT; k += blockDim.x) sC[k >> 5][k & 31] = __ldcg(T + k);
     __syncthreads();
     for (int k = tid; k < kTT; k += blockDim.x) {
       const int i = k >> 5, c = k & 31;
       double a0 = 0.0, a1 = 0.0;
-      if (pass == 0) {
+      if (lower) {
         for (int q = 0; q < kT; q += 2) {
           a0 = fma(sA[q][i], sC[q][c], a0);
           a1 = fma(sA[q + 1][i], sC[q + 1][c], a1);
@@ -348,6 +353,47 @@ __device__ void coupling_task(const ProfileSystem &S, int J, double (*sA)[kT + 1
       out[k] = a0 + a1;
     }
     __syncthreads();
+  }
+  // Q_J and R_J-1 need row J-1's matrices (the task before this one)
+  __shared__ int ok;
+  if (tid == 0) ok = J == 0 || wait_geq_dev(S.cpl + (J - 1), 1, flags);
+  __syncthreads();
+  if (!ok) return;
+  for (int pass = 0; pass < 2; pass++) {
+    // pass 0: Q_J = E_J - F_J F_J-1;  pass 1: R_J-1 = H_J-1 - G_J-1 G_J
+    if (pass == 1 && J == 0) break;
+    const size_t oa = pass == 0 ? off : off - kTT, ob = pass == 0 ? off - kTT : off;
+    const double *A = pass == 0 ? S.F + oa : S.G + oa;
+    const double *B = pass == 0 ? S.F + ob : S.G + ob;
+    const double *C0 = pass == 0 ? S.E + off : S.H + (off - kTT);
+    double *out = pass == 0 ? S.Q + off : S.R + (off - kTT);
+    if (J == 0) {
+      for (int k = tid; k < kTT; k += blockDim.x) out[k] = __ldcg(C0 + k);
+      continue;
+    }
+    for (int k = tid; k < kTT; k += blockDim.x) {
+      sA[k >> 5][k & 31] = __ldcg(A + k);
+      sC[k >> 5][k & 31] = __ldcg(B + k);
+    }
+    __syncthreads();
+    for (int k = tid; k < kTT; k += blockDim.x) {
+      const int i = k >> 5, c = k & 31;
+      double a0 = 0.0, a1 = 0.0;
+      for (int q = 0; q < kT; q += 2) {
+        a0 = fma(sA[i][q], sC[q][c], a0);
+        a1 = fma(sA[i][q + 1], sC[q + 1][c], a1);
+      }
+      out[k] = __ldcg(C0 + k) - (a0 + a1);
+    }
+    __syncthreads();
+  }
+  // the last row's R: G_nt-1 is zero, R = H (zero as well)
+  if (J == S.nt - 1)
+    for (int k = tid; k < kTT; k += blockDim.x) S.R[off + k] = __ldcg(S.H + off + k);
+  __syncthreads();
+  if (tid == 0) {
+    __threadfence();
+    atomicExch(S.cpl + J, 1);
   }
 }
 
@@ -430,11 +476,18 @@ __device__ bool wait_task(const ProfileSystem &S, int4 t, volatile int *flags) {
   if (type == 5)
     return wait_geq(S.done + slot_of(S, J, 0), 1, flags) &&
            wait_geq(S.upd + slot_of(S, I, 1), J - max(S.ftile[I], S.ftile[J]), flags);
-  if (type == 6)
-    return wait_geq(S.done + slot_of(S, J, 0), 1, flags) &&
-           (J < 1 || S.ftile[J] > J - 1 || wait_geq(S.done + slot_of(S, J, 1), kPanelParts, flags)) &&
-           (J + 1 >= S.nt || S.ftile[J + 1] > J ||
-            wait_geq(S.done + slot_of(S, J + 1, 1), kPanelParts, flags));
+  if (type == 6) {
+    if (!wait_geq(S.done + slot_of(S, J, 0), 1, flags)) return false;
+    for (int o = 1; o <= 2; o++) {
+      if (J >= o && S.ftile[J] <= J - o &&
+          !wait_geq(S.done + slot_of(S, J, o), kPanelParts, flags))
+        return false;
+      if (J + o < S.nt && S.ftile[J + o] <= J &&
+          !wait_geq(S.done + slot_of(S, J + o, o), kPanelParts, flags))
+        return false;
+    }
+    return true;
+  }
   if (type == 1)
     return wait_geq(S.done + slot_of(S, J, 0), 1, flags) &&
            wait_geq(S.upd + slot_of(S, I, I - J), J - max(S.ftile[I], S.ftile[J]), flags);
@@ -469,7 +522,7 @@ __global__ void __launch_bounds__(kFactorThreads) k_prof_factor(ProfileSystem S)
     } else if (t.x == 5) {
       fine = panel_update_task(S, t.w, t.z, sA, sB, flags);
     } else {
-      coupling_task(S, t.w, sA, sB, sC);
+      coupling_task(S, t.w, sA, sB, sC, flags);
     }
     if (!fine) break;
     __syncthreads();
@@ -583,16 +636,18 @@ __global__ void __launch_bounds__(kSolveBlock) k_prof_solve(ProfileSystem S, int
 
 // Pipelined substitutions on kPipeBlocks co-resident blocks (cooperative
 // launch): block b owns the tile rows J = b, b + P, ... .  Forward, in
-// increasing J: r_J = b_J minus the contributions of the solved rows J-o,
-// o >= 2, c_J = L_JJ^-1 r_J, and y_J = c_J - F_J y_J-1 with the
-// factorisation's coupling matrices, so only the last 32 x 32 product waits
-// for the previous row.  Backward, in decreasing J: x_J = L_JJ^-T (D_J^-1
-// y_J minus the transposed contributions of rows J+o, o >= 2) - G_J x_J+1.
-// There are no row flags: every solved value is published to a scratch
-// vector filled with kUnset beforehand (a NaN pattern that no arithmetic
-// result is stored as), and a consumer thread polls exactly the values it
-// reads, so the chain costs one store-to-load hop per row.  Waits are
-// bounded by the global timer.
+// increasing J: c3_J = L_JJ^-1 (b_J minus the contributions of rows J-3 and
+// older), then with the factorisation's coupling matrices
+//   y_J = c3_J - F_J c_J-1 - Q_J y_J-2,   c_J = c3_J - E_J y_J-2,
+// so a row waits for the row two back (and for c_J-1, which its owner
+// publishes as soon as y_J-3 is known): the two interleaved chains halve
+// the serial length.  Backward, in decreasing J, the same with
+// c3'_J = L_JJ^-T (D_J^-1 y_J minus the transposed contributions of rows J+3
+// and beyond):  x_J = c3'_J - G_J c'_J+1 - R_J x_J+2,  c'_J = c3'_J -
+// H_J x_J+2.  There are no row flags: every solved value is published to a
+// scratch vector filled with kUnset beforehand (a NaN pattern that no
+// arithmetic result is stored as), and a consumer thread polls exactly the
+// values it reads.  Waits are bounded by the global timer.
 constexpr int kPipeBlocks = 64;
 constexpr int kPipeThreads = 256;
 constexpr unsigned long long kUnset = 0xFFFFFFFFFFFFFFFFull;   // byte fill 0xFF
@@ -639,7 +694,8 @@ __device__ __forceinline__ void publish(double *p, double v) {
 
 __global__ void __launch_bounds__(kPipeThreads) k_prof_solve_pipe(ProfileSystem S, int nrhs,
                                                                   double *x, int ldx,
-                                                                  double *ys, double *xs) {
+                                                                  double *ys, double *cs,
+                                                                  double *xs, double *ds) {
   __shared__ double rv[2][4][kT];
   volatile int *flags = S.flags;
   const int tid = threadIdx.x;
@@ -652,12 +708,26 @@ __global__ void __launch_bounds__(kPipeThreads) k_prof_solve_pipe(ProfileSystem 
     v += __shfl_xor_sync(0xffffffffu, v, 1);
     return v;
   };
+  // this thread's four entries of row r of a 32 x 32 matrix (loaded ahead
+  // of the waits), and their product with the vector published at p
+  auto row_of = [&](const double *M, double (&mv)[4]) {
+#pragma unroll
+    for (int m = 0; m < 4; m++) mv[m] = __ldcg(M + r * kT + g + 8 * m);
+  };
+  auto row_times = [&](const double (&mv)[4], const double *p) {
+    double v[4];
+    await4(p + g, v, flags);
+    double t = 0.0;
+#pragma unroll
+    for (int m = 0; m < 4; m++) t = fma(mv[m], v[m], t);
+    return group_sum(t);
+  };
   int it = 0;                                   // rv is double-buffered by iteration
-  // ---------------- forward: y_J = W_J' (b_J - sum_{o>=2} L_J,J-o y_J-o) - F_J y_J-1
+  // ---------------- forward
   for (int J = blockIdx.x; J < nt; J += P, it++) {
     double acc[4] = {0.0, 0.0, 0.0, 0.0};
     const int ohi = min(W, J - S.ftile[J]);
-    for (int o = ohi; o >= 2; o--) {
+    for (int o = ohi; o >= 3; o--) {
       const double *Lt = tile_at(S, J, o) + r * kT + g;
       const double l0 = __ldcg(Lt), l1 = __ldcg(Lt + 8), l2 = __ldcg(Lt + 16), l3 = __ldcg(Lt + 24);
       for (int q = 0; q < nrhs; q++) {
@@ -671,39 +741,40 @@ __global__ void __launch_bounds__(kPipeThreads) k_prof_solve_pipe(ProfileSystem 
       const double v = group_sum(acc[q]);
       if (g == 0) rb[q][r] = __ldcg(x + (size_t)q * ldx + J * kT + r) - v;
     }
-    const double *Wt = S.Winv + (size_t)J * kTT, *Ft = S.F + (size_t)J * kTT;
-    double wv[4], fv[4];
+    const double *Wt = S.Winv + (size_t)J * kTT;
+    double wv[4];
 #pragma unroll
-    for (int m = 0; m < 4; m++) {
-      wv[m] = __ldcg(Wt + (g + 8 * m) * kT + r);
-      fv[m] = __ldcg(Ft + r * kT + g + 8 * m);
-    }
+    for (int m = 0; m < 4; m++) wv[m] = __ldcg(Wt + (g + 8 * m) * kT + r);
+    const size_t off = (size_t)J * kTT;
+    double fv[4], qv[4], ev[4];
+    row_of(S.F + off, fv);
+    row_of(S.Q + off, qv);
+    row_of(S.E + off, ev);
     __syncthreads();
     const bool hasF = J >= 1 && S.ftile[J] <= J - 1;
     for (int q = 0; q < nrhs; q++) {
-      double c = 0.0;
+      double c3 = 0.0;
 #pragma unroll
-      for (int m = 0; m < 4; m++) c = fma(wv[m], rb[q][g + 8 * m], c);
-      c = group_sum(c);
-      double t = 0.0;
-      if (hasF) {
-        double y[4];
-        await4(ys + (size_t)q * ls + (J - 1) * kT + g, y, flags);
-#pragma unroll
-        for (int m = 0; m < 4; m++) t = fma(fv[m], y[m], t);
-      }
-      t = group_sum(t);
-      if (g == 0) publish(ys + (size_t)q * ls + J * kT + r, c - t);
+      for (int m = 0; m < 4; m++) c3 = fma(wv[m], rb[q][g + 8 * m], c3);
+      c3 = group_sum(c3);
+      const size_t vq = (size_t)q * ls;
+      // c_J first: it needs only y_J-2, and row J+1 waits for it
+      double t2 = 0.0, t3 = 0.0;
+      if (J >= 2) t3 = row_times(ev, ys + vq + (J - 2) * kT);
+      if (g == 0) publish(cs + vq + J * kT + r, c3 - t3);
+      if (J >= 2) t2 = row_times(qv, ys + vq + (J - 2) * kT);
+      const double t1 = hasF ? row_times(fv, cs + vq + (J - 1) * kT) : 0.0;
+      if (g == 0) publish(ys + vq + J * kT + r, (c3 - t1) - t2);
     }
   }
-  // ---------------- backward: x_J = W_J (D_J^-1 y_J - sum_{o>=2} L_J+o,J' x_J+o) - G_J x_J+1
+  // ---------------- backward
   const int jlast = blockIdx.x + ((nt - 1 - (int)blockIdx.x) / P) * P;
   for (int J = jlast; J >= 0; J -= P, it++) {
     if (J >= nt) continue;
     double acc[4] = {0.0, 0.0, 0.0, 0.0};
     const int ohi = min(W, nt - 1 - J);
     // column c = r of the result; rows g, g+8, g+16, g+24 of tile (J+o, J)
-    for (int o = ohi; o >= 2; o--) {
+    for (int o = ohi; o >= 3; o--) {
       if (S.ftile[J + o] > J) continue;
       const double *Lt = tile_at(S, J + o, o) + r;
       const double l0 = __ldcg(Lt + g * kT), l1 = __ldcg(Lt + (g + 8) * kT);
@@ -722,31 +793,33 @@ __global__ void __launch_bounds__(kPipeThreads) k_prof_solve_pipe(ProfileSystem 
       if (g == 0)
         rb[q][r] = ld_relaxed(ys + (size_t)q * ls + J * kT + r) * S.invD[J * kT + r] - v;
     }
-    const double *Wt = S.Winv + (size_t)J * kTT, *Gt = S.G + (size_t)J * kTT;
-    double wv[4], gv[4];
+    const double *Wt = S.Winv + (size_t)J * kTT;
+    double wv[4];
 #pragma unroll
-    for (int m = 0; m < 4; m++) {
-      wv[m] = __ldcg(Wt + r * kT + g + 8 * m);
-      gv[m] = __ldcg(Gt + r * kT + g + 8 * m);
-    }
+    for (int m = 0; m < 4; m++) wv[m] = __ldcg(Wt + r * kT + g + 8 * m);
+    const size_t off = (size_t)J * kTT;
+    double gv[4], rv4[4], hv[4];
+    row_of(S.G + off, gv);
+    row_of(S.R + off, rv4);
+    row_of(S.H + off, hv);
     __syncthreads();
     const bool hasG = J + 1 < nt && S.ftile[J + 1] <= J;
     for (int q = 0; q < nrhs; q++) {
-      double c = 0.0;
+      double c3 = 0.0;
 #pragma unroll
-      for (int m = 0; m < 4; m++) c = fma(wv[m], rb[q][g + 8 * m], c);
-      c = group_sum(c);
-      double t = 0.0;
-      if (hasG) {
-        double xv[4];
-        await4(xs + (size_t)q * ls + (J + 1) * kT + g, xv, flags);
-#pragma unroll
-        for (int m = 0; m < 4; m++) t = fma(gv[m], xv[m], t);
-      }
-      t = group_sum(t);
+      for (int m = 0; m < 4; m++) c3 = fma(wv[m], rb[q][g + 8 * m], c3);
+      c3 = group_sum(c3);
+      const size_t vq = (size_t)q * ls;
+      // c'_J first: it needs only x_J+2, and row J-1 waits for it
+      double t2 = 0.0, t3 = 0.0;
+      if (J + 2 < nt) t3 = row_times(hv, xs + vq + (J + 2) * kT);
+      if (g == 0) publish(ds + vq + J * kT + r, c3 - t3);
+      if (J + 2 < nt) t2 = row_times(rv4, xs + vq + (J + 2) * kT);
+      const double t1 = hasG ? row_times(gv, ds + vq + (J + 1) * kT) : 0.0;
       if (g == 0) {
-        publish(xs + (size_t)q * ls + J * kT + r, c - t);
-        x[(size_t)q * ldx + J * kT + r] = c - t;
+        const double xj = (c3 - t1) - t2;
+        publish(xs + vq + J * kT + r, xj);
+        x[(size_t)q * ldx + J * kT + r] = xj;
       }
     }
   }
@@ -845,6 +918,7 @@ int profile_factor(const ProfileSystem &S, cudaStream_t s, int *bad_eq) {
   const size_t nslots = (size_t)S.nt * (S.W + 1);
   if (cudaMemsetAsync(S.upd, 0, nslots * sizeof(int), s) != cudaSuccess) return XG_ECUDA;
   if (cudaMemsetAsync(S.done, 0, nslots * sizeof(int), s) != cudaSuccess) return XG_ECUDA;
+  if (cudaMemsetAsync(S.cpl, 0, (size_t)S.nt * sizeof(int), s) != cudaSuccess) return XG_ECUDA;
   if (cudaMemsetAsync(S.next_task, 0, sizeof(int), s) != cudaSuccess) return XG_ECUDA;
   if (cudaMemsetAsync(S.flags, 0, 4 * sizeof(int), s) != cudaSuccess) return XG_ECUDA;
   const int nb = (int)std::min<long>(g_factor_blocks, std::max(S.ntasks, 1));
@@ -867,13 +941,14 @@ int profile_solve(const ProfileSystem &S, int nrhs, double *x, int ldx, cudaStre
     // pipelined over co-resident blocks (both sweeps' published values are
     // reset to kUnset first); small systems keep the one-block sweep
     const size_t ls = (size_t)S.nt * kT;
-    if (cudaMemsetAsync(S.sweep, 0xFF, 2 * (size_t)nrhs * ls * sizeof(double), s) != cudaSuccess)
+    if (cudaMemsetAsync(S.sweep, 0xFF, 4 * (size_t)nrhs * ls * sizeof(double), s) != cudaSuccess)
       return XG_ECUDA;
     if (cudaMemsetAsync(S.flags, 0, 4 * sizeof(int), s) != cudaSuccess) return XG_ECUDA;
     ProfileSystem Sv = S;
-    double *ys = S.sweep, *xs = S.sweep + (size_t)nrhs * ls;
-    void *args[] = {(void *)&Sv, (void *)&nrhs, (void *)&x, (void *)&ldx, (void *)&ys,
-                    (void *)&xs};
+    double *ys = S.sweep, *cs = ys + (size_t)nrhs * ls, *xs = cs + (size_t)nrhs * ls;
+    double *ds = xs + (size_t)nrhs * ls;
+    void *args[] = {(void *)&Sv, (void *)&nrhs, (void *)&x,  (void *)&ldx,
+                    (void *)&ys, (void *)&cs,   (void *)&xs, (void *)&ds};
     if (cudaLaunchCooperativeKernel((void *)k_prof_solve_pipe, dim3(kPipeBlocks),
                                     dim3(kPipeThreads), args, 0, s) != cudaSuccess)
       return XG_ECUDA;

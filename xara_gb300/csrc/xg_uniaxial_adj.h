@@ -23,6 +23,17 @@
 
 namespace xg {
 
+// True where a single-precision estimate puts |rho|^R below 2^-60 (R
+// log2|rho| < -60, several units inside the estimate's error): there
+// 1 + |rho|^R rounds to 1.
+XG_HD inline bool mp_power_negligible(double R, double ae) {
+#ifdef __CUDA_ARCH__
+  return (float)R * __log2f(fmaxf((float)ae, 1.17549435e-38f)) < -60.0f;
+#else
+  return (float)R * log2f(fmaxf((float)ae, 1.17549435e-38f)) < -60.0f;
+#endif
+}
+
 // Steel02::setTrialStrain (material/uniaxial/steel/Steel02.cpp:113-227),
 // primal recomputed with the same operations as the forward kernel (the
 // Menegotto-Pinto powers through log/exp, the isotropic shift through pow),
@@ -88,11 +99,16 @@ XG_HD inline void steel02_vjp(const double *q, const double *hc, double strain, 
   const double den = epss0 - epsr;
   const double rho = (eps - epsr) / den;
   const double ae = fabs(rho);
-  const double lae = ae > 0.0 ? log(ae) : 0.0;
-  const double pr = ae > 0.0 ? exp(R * lae) : 0.0;
-  const double dum1 = 1.0 + pr;
-  const double ld1 = log(dum1);
-  const double dum2 = exp(ld1 / R);
+  // as in the forward kernel: where |rho|^R < 2^-60 the powers are exactly
+  // 1 and every term through |rho|^R is below 2^-60 of the others
+  double lae = 0.0, pr = 0.0, dum1 = 1.0, ld1 = 0.0, dum2 = 1.0;
+  if (!mp_power_negligible(R, ae)) {
+    lae = ae > 0.0 ? log(ae) : 0.0;
+    pr = ae > 0.0 ? exp(R * lae) : 0.0;
+    dum1 = 1.0 + pr;
+    ld1 = log(dum1);
+    dum2 = exp(ld1 / R);
+  }
   const double sst = b * rho + (1.0 - b) * rho / dum2;
   // ---- reverse ----
   double b_epsmin = yb[0], b_epsmax = yb[1], b_epspl = yb[2], b_epss0 = yb[3];
