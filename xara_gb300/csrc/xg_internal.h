@@ -47,6 +47,7 @@ struct GatherMap {
   const int64_t *chunk_begin;  // [nchunks+1] into src
   const int *slot_chunk;  // [nslots+1] chunk range per slot
   const int64_t *src;     // contribution source indices into the scratch
+  const int *src32;       // the same as 32-bit indices when the scratch is small enough, or null
 };
 
 // ---------------------------------------------------------------------------

@@ -575,22 +575,32 @@ __global__ void k_j2_zero(ContinuumView v) {
 // ---------------------------------------------------------------------------
 // deterministic gather assembly
 // ---------------------------------------------------------------------------
-__global__ void k_gather_chunks(GatherMap g, const double *__restrict__ scratch,
-                                double *__restrict__ partial) {
+// Chunk sums in list order; a slot made of one chunk (every slot of a mesh
+// whose nodes have few elements) is written to its output directly, the
+// others leave partial sums for k_gather_slots.  The same additions in the
+// same order either way.
+template <typename Idx>
+__global__ void k_gather_chunks(GatherMap g, const Idx *__restrict__ src,
+                                const double *__restrict__ scratch, double *__restrict__ partial,
+                                double *__restrict__ out) {
   const int c = blockIdx.x * blockDim.x + threadIdx.x;
   if (c >= g.nchunks) return;
   double s = 0.0;
   const int64_t b = g.chunk_begin[c], end = g.chunk_begin[c + 1];
-  for (int64_t k = b; k < end; k++) s += scratch[g.src[k]];
-  partial[c] = s;
+  for (int64_t k = b; k < end; k++) s += scratch[src[k]];
+  const int slot = g.chunk_slot[c];
+  if (g.slot_chunk[slot + 1] - g.slot_chunk[slot] == 1) out[slot] = s;
+  else partial[c] = s;
 }
 
 __global__ void k_gather_slots(GatherMap g, const double *__restrict__ partial,
                                double *__restrict__ out) {
   const int s = blockIdx.x * blockDim.x + threadIdx.x;
   if (s >= g.nslots) return;
+  const int c0 = g.slot_chunk[s], c1 = g.slot_chunk[s + 1];
+  if (c1 - c0 == 1) return;               // written by its chunk
   double v = 0.0;
-  for (int c = g.slot_chunk[s]; c < g.slot_chunk[s + 1]; c++) v += partial[c];
+  for (int c = c0; c < c1; c++) v += partial[c];
   out[s] = v;
 }
 
@@ -684,7 +694,11 @@ int launch_j2_zero_state(const ContinuumView &v, cudaStream_t s) {
 int launch_gather(const GatherMap &g, const double *scratch, double *partial, double *out,
                   cudaStream_t s) {
   if (g.nslots == 0) return 0;
-  k_gather_chunks<<<nblocks(g.nchunks), kThreads, 0, s>>>(g, scratch, partial);
+  if (g.src32)
+    k_gather_chunks<int><<<nblocks(g.nchunks), kThreads, 0, s>>>(g, g.src32, scratch, partial, out);
+  else
+    k_gather_chunks<int64_t><<<nblocks(g.nchunks), kThreads, 0, s>>>(g, g.src, scratch, partial,
+                                                                      out);
   k_gather_slots<<<nblocks(g.nslots), kThreads, 0, s>>>(g, partial, out);
   return check_launch();
 }

@@ -150,6 +150,7 @@ struct xg_model {
   DBuf<double> d_vals, d_resid;
   DBuf<int> d_gk_slot_chunk, d_gk_chunk_slot, d_gr_slot_chunk, d_gr_chunk_slot;
   DBuf<int64_t> d_gk_chunk_begin, d_gk_src, d_gr_chunk_begin, d_gr_src;
+  DBuf<int> d_gk_src32, d_gr_src32;
   GatherMap gk{}, gr{};
   // solver
   DBuf<double> d_binv, d_r, d_z, d_p, d_q, d_pcg_part, d_scalars;
@@ -686,17 +687,27 @@ int xg_model::upload(const HostGather &gk_h, const HostGather &gr_h) {
   RET(d_gk_slot_chunk.upload(gk_h.slot_chunk.data(), gk_h.slot_chunk.size(), s));
   RET(d_gk_chunk_slot.upload(gk_h.chunk_slot.data(), gk_h.chunk_slot.size(), s));
   RET(d_gk_chunk_begin.upload(gk_h.chunk_begin.data(), gk_h.chunk_begin.size(), s));
-  RET(d_gk_src.upload(gk_h.src.data(), gk_h.src.size(), s));
+  // 32-bit source indices when every index fits (the usual case)
+  auto upload_src = [&](const std::vector<int64_t> &src, DBuf<int64_t> &d64, DBuf<int> &d32) {
+    int64_t mx = 0;
+    for (int64_t v : src) mx = std::max(mx, v);
+    if (mx < INT32_MAX) {
+      std::vector<int> s32(src.begin(), src.end());
+      return d32.upload(s32.data(), s32.size(), s);
+    }
+    return d64.upload(src.data(), src.size(), s);
+  };
+  RET(upload_src(gk_h.src, d_gk_src, d_gk_src32));
   RET(d_gr_slot_chunk.upload(gr_h.slot_chunk.data(), gr_h.slot_chunk.size(), s));
   RET(d_gr_chunk_slot.upload(gr_h.chunk_slot.data(), gr_h.chunk_slot.size(), s));
   RET(d_gr_chunk_begin.upload(gr_h.chunk_begin.data(), gr_h.chunk_begin.size(), s));
-  RET(d_gr_src.upload(gr_h.src.data(), gr_h.src.size(), s));
+  RET(upload_src(gr_h.src, d_gr_src, d_gr_src32));
   gk.nslots = nnz; gk.nchunks = (int)gk_h.chunk_slot.size();
   gk.chunk_slot = d_gk_chunk_slot.p; gk.chunk_begin = d_gk_chunk_begin.p;
-  gk.slot_chunk = d_gk_slot_chunk.p; gk.src = d_gk_src.p;
+  gk.slot_chunk = d_gk_slot_chunk.p; gk.src = d_gk_src.p; gk.src32 = d_gk_src32.p;
   gr.nslots = neq; gr.nchunks = (int)gr_h.chunk_slot.size();
   gr.chunk_slot = d_gr_chunk_slot.p; gr.chunk_begin = d_gr_chunk_begin.p;
-  gr.slot_chunk = d_gr_slot_chunk.p; gr.src = d_gr_src.p;
+  gr.slot_chunk = d_gr_slot_chunk.p; gr.src = d_gr_src.p; gr.src32 = d_gr_src32.p;
   RET(d_partial.alloc(std::max(gk.nchunks, gr.nchunks) + 1));
   // solver
   const int nblk = (int)blk_start.size() - 1;
