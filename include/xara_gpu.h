@@ -340,6 +340,28 @@ int xg_model_stream(const xg_model *m, void **stream);
 int xg_profile_counters(xg_model *m, long long *point_updates, long long *section_updates,
                         long long *element_updates);
 
+/* ---- Recorders (recorder/NodeRecorder.cpp, EnvelopeNodeRecorder.cpp; the
+        `recorder Node|EnvelopeNode -file f <-time> <-dT dt> -node ... -dof
+        ... disp|vel|accel` commands).  Values are gathered on the device
+        after every committed step of xg_analyze (no host traffic per step);
+        dofs are 0-based here (the command's are 1-based), a dof a node does
+        not have records 0. ---- */
+#define XG_REC_NODE     0   /* one row per recorded step: [time] values */
+#define XG_REC_ENVELOPE 1   /* three rows: min, max, max |.| ([time value] pairs with echo_time) */
+#define XG_REC_DISP     0
+#define XG_REC_VEL      1
+#define XG_REC_ACCEL    2
+int xg_recorder_add(xg_model *m, int kind, int response, const int *node_tags, int num_nodes,
+                    const int *dofs, int num_dofs, int echo_time, double dT, int *id);
+/* Rows recorded so far (3 for an envelope once it has a record) and columns. */
+int xg_recorder_size(const xg_model *m, int id, int *rows, int *cols);
+/* Copy up to max_rows rows (row-major); returns the number of rows copied. */
+int xg_recorder_read(const xg_model *m, int id, double *out, int max_rows);
+/* Write the rows as the reference's DataFileStream does (values separated by
+   blanks, %g with the given number of significant digits, 6 by default in
+   the reference). */
+int xg_recorder_write(const xg_model *m, int id, const char *path, int precision);
+
 /* FP64 FMA throughput of the current device in TFLOP/s (a short probe
    kernel with no memory traffic), the ceiling of the FP64 element kernels. */
 int xg_measure_fp64_peak(double *tflops);

@@ -382,5 +382,5 @@ def test_adjoint_through_torch_autograd(need_gpu):
         m.reset()
         J2 = gpu.adjoint_forward(m, ph, 20, 5, *obj)
         g = gpu.adjoint_backward(m)
-    assert float(J) == J2
+    assert float(J.detach()) == J2
     np.testing.assert_allclose(theta.grad.numpy(), 2.0 * g, rtol=1e-13, atol=0)

@@ -137,6 +137,24 @@ def test_pcg_against_dense_solve(gpu_mod):
     assert relerr(x, xd) < 1e-9
 
 
+def test_pipelined_sweeps_two_rhs_displacement_control(gpu_mod):
+    """DisplacementControl solves two right-hand sides per factorisation; on
+    8,128 equations (254 tile rows) they run through the pipelined
+    substitutions at distance two: four steps against the oracle."""
+    from oracle import port
+    from xara_gb300 import configs
+    desc, phases = configs.quad_block(128, 32, steps=4)
+    o = port.OracleModel(desc)
+    Uo, lo, _ = o.run(phases)
+    o.close()
+    with gpu_mod.DeviceModel(desc) as m:
+        m.set_system(gpu_mod.XG_SYSTEM_PROFILE_SPD)
+        assert m.neq >= 128 * 32
+        U, lam, _ = m.run(phases)
+    assert relerr(U, Uo) < RTOL_HISTORY
+    assert relerr(lam, lo) < RTOL_HISTORY
+
+
 def test_pcg_long_constraint_row(gpu_mod):
     """Block-Jacobi PCG on a brick block whose top face is tied in z to one
     node: that node's row (1,446 entries) is summed in chunks of 512 entries

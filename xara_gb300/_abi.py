@@ -13,6 +13,8 @@ XG_HANDLER_PLAIN, XG_HANDLER_TRANSFORMATION = 0, 1
 XG_INT_LOAD_CONTROL, XG_INT_DISP_CONTROL, XG_INT_NEWMARK = 0, 1, 2
 XG_TEST_NORM_DISP_INCR, XG_TEST_NORM_UNBALANCE = 0, 1
 XG_SYSTEM_BJPCG, XG_SYSTEM_PROFILE_SPD = 0, 1
+XG_REC_NODE, XG_REC_ENVELOPE = 0, 1
+XG_REC_DISP, XG_REC_VEL, XG_REC_ACCEL = 0, 1, 2
 XG_J2_NPARAM = 8
 XG_UNI_NPARAM = 12
 

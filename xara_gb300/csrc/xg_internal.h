@@ -58,6 +58,9 @@ int launch_quad_assemble(const ContinuumView &v, cudaStream_t s);
 int launch_brick_update(const ContinuumView &v, cudaStream_t s);
 int launch_brick_assemble(const ContinuumView &v, cudaStream_t s);
 int launch_brick_geometry(const ContinuumView &v, double *geo, cudaStream_t s);
+// recorders: kind 0 writes one row ([t] values), kind 1 updates an envelope
+int launch_record(int kind, int n, const int *idx, const double *src, double t, int echo,
+                  int first, double *out, cudaStream_t s);
 int launch_gather(const GatherMap &g, const double *scratch, double *partial, double *out,
                   cudaStream_t s);
 int launch_j2_zero_state(const ContinuumView &v, cudaStream_t s);

@@ -8,6 +8,8 @@
 // fixed (element tag order) and the result is bit-identical run to run.
 #include <cuda_runtime.h>
 
+#include <algorithm>
+
 #include <cstdint>
 
 #include "xg_internal.h"
@@ -605,6 +607,53 @@ __global__ void k_gather_slots(GatherMap g, const double *__restrict__ partial,
 }
 
 // ---------------------------------------------------------------------------
+// recorders (recorder/NodeRecorder.cpp:180-476, EnvelopeNodeRecorder.cpp:
+// 191-470): one committed step's selected nodal values, gathered on the
+// device
+// ---------------------------------------------------------------------------
+// row = [time] v_0 .. v_n-1, v_i = src[idx[i]] (0 where the dof does not exist)
+__global__ void k_record_row(int n, const int *idx, const double *src, double t, int echo,
+                             double *row) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (echo && i == 0) row[0] = t;
+  if (i < n) row[echo + i] = idx[i] >= 0 ? src[idx[i]] : 0.0;
+}
+
+// Envelope [3][ncol]: rows min, max, max |.|; with echo every value has its
+// time in the column before it.  The first record sets all three, later
+// records update the minimum, else the maximum, and then the absolute value
+// (EnvelopeNodeRecorder.cpp:401-468).
+__global__ void k_record_envelope(int n, const int *idx, const double *src, double t, int echo,
+                                  int first, double *env) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const double v = idx[i] >= 0 ? src[idx[i]] : 0.0;
+  const int w = echo ? 2 : 1, ncol = n * w, c = i * w + (echo ? 1 : 0);
+  double *mn = env, *mx = env + ncol, *ab = env + 2 * ncol;
+  if (first) {
+    mn[c] = v;
+    mx[c] = v;
+    ab[c] = fabs(v);
+    if (echo) mn[c - 1] = mx[c - 1] = ab[c - 1] = t;
+    return;
+  }
+  bool moved = false;
+  if (mn[c] > v) {
+    mn[c] = v;
+    if (echo) mn[c - 1] = t;
+    moved = true;
+  } else if (mx[c] < v) {
+    mx[c] = v;
+    if (echo) mx[c - 1] = t;
+    moved = true;
+  }
+  if (moved && ab[c] < fabs(v)) {
+    ab[c] = fabs(v);
+    if (echo) ab[c - 1] = t;
+  }
+}
+
+// ---------------------------------------------------------------------------
 // vector helpers
 // ---------------------------------------------------------------------------
 __global__ void k_axpy(int n, double a, const double *x, double *y) {
@@ -700,6 +749,14 @@ int launch_gather(const GatherMap &g, const double *scratch, double *partial, do
     k_gather_chunks<int64_t><<<nblocks(g.nchunks), kThreads, 0, s>>>(g, g.src, scratch, partial,
                                                                       out);
   k_gather_slots<<<nblocks(g.nslots), kThreads, 0, s>>>(g, partial, out);
+  return check_launch();
+}
+int launch_record(int kind, int n, const int *idx, const double *src, double t, int echo,
+                  int first, double *out, cudaStream_t s) {
+  if (n == 0 && !echo) return 0;
+  const int nb = (std::max(n, 1) + kThreads - 1) / kThreads;
+  if (kind == 0) k_record_row<<<nb, kThreads, 0, s>>>(n, idx, src, t, echo, out);
+  else k_record_envelope<<<nb, kThreads, 0, s>>>(n, idx, src, t, echo, first, out);
   return check_launch();
 }
 int launch_axpy(int n, double a, const double *x, double *y, cudaStream_t s) {

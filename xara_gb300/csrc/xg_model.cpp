@@ -18,6 +18,7 @@
 #include <cstring>
 #include <numeric>
 #include <string>
+#include <memory>
 #include <vector>
 
 #include "xg_internal.h"
@@ -156,6 +157,17 @@ struct xg_model {
   DBuf<double> d_binv, d_r, d_z, d_p, d_q, d_pcg_part, d_scalars;
   DBuf<unsigned int> d_barrier;
   DBuf<int> d_flags;
+  // recorders (NodeRecorder / EnvelopeNodeRecorder): values gathered on the
+  // device after every committed step of xg_analyze
+  struct Recorder {
+    int kind = 0, response = 0, echo = 0, ncol = 0, rows = 0, cap = 0, nvals = 0;
+    double dT = 0.0, next = 0.0;
+    bool first = true;
+    DBuf<int> idx;
+    DBuf<double> data;     // node: [cap][ncol]; envelope: [3][ncol]
+  };
+  std::vector<std::unique_ptr<Recorder>> recorders;
+  int record_step();
   PcgSystem pcg{};
   bool blocks_factored = false;
   // sliced ELL copy of the matrix for the PCG's SpMV, built at the first
@@ -1419,6 +1431,40 @@ int xg_model::solve_profile(int nrhs, const double *const *b, double *const *x) 
   return 0;
 }
 
+// Recorder::record (NodeRecorder.cpp:180-210): at the committed time, when
+// dT is zero or the time has reached the next stamp less dT * 1e-6.
+int xg_model::record_step() {
+  for (auto &rp : recorders) {
+    Recorder &r = *rp;
+    if (!(r.dT == 0.0 || time_c - r.next >= -r.dT * 1e-6)) continue;
+    if (r.dT != 0.0) r.next = time_c + r.dT;
+    const double *src = r.response == 0 ? d_Uc.p : r.response == 1 ? d_Vc.p : d_Ac.p;
+    if (r.kind == 0) {
+      if (r.rows == r.cap) {
+        // grow by doubling (a device copy; no host round trip per step)
+        const int cap = std::max(2 * r.cap, 64);
+        DBuf<double> nd;
+        RET(nd.alloc((size_t)cap * r.ncol));
+        if (r.rows) CK(cudaMemcpyAsync(nd.p, r.data.p, (size_t)r.rows * r.ncol * sizeof(double),
+                                       cudaMemcpyDeviceToDevice, stream));
+        CK(cudaStreamSynchronize(stream));
+        std::swap(r.data.p, nd.p);
+        std::swap(r.data.n, nd.n);
+        r.cap = cap;
+      }
+      RET(launch_record(0, r.nvals, r.idx.p, src, time_c, r.echo, 0,
+                        r.data.p + (size_t)r.rows * r.ncol, stream));
+      r.rows++;
+    } else {
+      RET(launch_record(1, r.nvals, r.idx.p, src, time_c, r.echo, r.first ? 1 : 0, r.data.p,
+                        stream));
+      r.first = false;
+      r.rows = 3;
+    }
+  }
+  return 0;
+}
+
 int xg_model::ensure_pcg_sell() {
   if (sell_tried || neq == 0) return 0;
   sell_tried = true;
@@ -2402,6 +2448,7 @@ int xg_analyze(xg_model *m, int num_steps, xg_step_stats *stats) {
       return r;
     }
     m->phase_steps_done++;
+    RET(m->record_step());
   }
   return 0;
 }
@@ -2414,6 +2461,86 @@ int xg_get_disp(const xg_model *m, double *u, double *lambda) {
     CK(cudaStreamSynchronize(m->stream));
   }
   if (lambda) *lambda = m->time_c;
+  return 0;
+}
+
+int xg_recorder_add(xg_model *m, int kind, int response, const int *node_tags, int num_nodes,
+                    const int *dofs, int num_dofs, int echo_time, double dT, int *id) {
+  if (!m || !id || num_nodes < 0 || num_dofs < 0 || (num_nodes && !node_tags) ||
+      (num_dofs && !dofs) || (kind != XG_REC_NODE && kind != XG_REC_ENVELOPE) ||
+      response < XG_REC_DISP || response > XG_REC_ACCEL || dT < 0.0)
+    return fail(XG_EINVAL, "bad recorder settings");
+  std::vector<int> idx;
+  for (int i = 0; i < num_nodes; i++) {
+    auto it = std::lower_bound(m->node_tag.begin(), m->node_tag.end(), node_tags[i]);
+    if (it == m->node_tag.end() || *it != node_tags[i])
+      return fail(XG_EINVAL, "recorder: no node %d", node_tags[i]);
+    const int n = (int)(it - m->node_tag.begin());
+    for (int j = 0; j < num_dofs; j++) {
+      if (dofs[j] < 0) return fail(XG_EINVAL, "recorder: bad dof %d", dofs[j]);
+      // a dof the node does not have records 0 (NodeRecorder.cpp:258-262)
+      idx.push_back(dofs[j] < m->ndf ? n * m->ndf + dofs[j] : -1);
+    }
+  }
+  auto r = std::make_unique<xg_model::Recorder>();
+  r->kind = kind;
+  r->response = response;
+  r->echo = echo_time ? 1 : 0;
+  r->dT = dT;
+  r->nvals = (int)idx.size();
+  RET(r->idx.upload(idx.data(), idx.size(), m->stream));
+  if (kind == XG_REC_NODE) {
+    r->ncol = r->echo + r->nvals;
+  } else {
+    r->ncol = (r->echo ? 2 : 1) * r->nvals;
+    RET(r->data.alloc(std::max<size_t>((size_t)3 * r->ncol, 1)));
+    CK(cudaMemsetAsync(r->data.p, 0, std::max<size_t>((size_t)3 * r->ncol, 1) * sizeof(double),
+                       m->stream));
+  }
+  CK(cudaStreamSynchronize(m->stream));
+  m->recorders.push_back(std::move(r));
+  *id = (int)m->recorders.size() - 1;
+  return 0;
+}
+
+int xg_recorder_size(const xg_model *m, int id, int *rows, int *cols) {
+  if (!m || id < 0 || id >= (int)m->recorders.size()) return fail(XG_EINVAL, "no recorder %d", id);
+  const auto &r = *m->recorders[id];
+  if (rows) *rows = r.rows;
+  if (cols) *cols = r.ncol;
+  return 0;
+}
+
+int xg_recorder_read(const xg_model *m, int id, double *out, int max_rows) {
+  if (!m || id < 0 || id >= (int)m->recorders.size() || (!out && max_rows > 0))
+    return fail(XG_EINVAL, "bad recorder read");
+  const auto &r = *m->recorders[id];
+  const int n = std::min(max_rows, r.rows);
+  if (n > 0 && r.ncol > 0) {
+    CK(cudaMemcpyAsync(out, r.data.p, (size_t)n * r.ncol * sizeof(double),
+                       cudaMemcpyDeviceToHost, m->stream));
+    CK(cudaStreamSynchronize(m->stream));
+  }
+  return n;
+}
+
+// DataFileStream::write (handler/DataFileStream.cpp:463-483): the values of
+// a row separated by blanks, a newline after the last, printed as a C++
+// stream with setprecision(precision) prints them (%g).
+int xg_recorder_write(const xg_model *m, int id, const char *path, int precision) {
+  if (!m || !path || precision < 1 || precision > 17 || id < 0 ||
+      id >= (int)m->recorders.size())
+    return fail(XG_EINVAL, "bad recorder write");
+  const auto &r = *m->recorders[id];
+  std::vector<double> h((size_t)r.rows * r.ncol);
+  if (!h.empty()) RET(xg_recorder_read(m, id, h.data(), r.rows) < 0 ? XG_ECUDA : 0);
+  FILE *f = fopen(path, "w");
+  if (!f) return fail(XG_EINVAL, "recorder: cannot open %s", path);
+  for (int i = 0; i < r.rows; i++) {
+    for (int j = 0; j < r.ncol; j++)
+      fprintf(f, j + 1 < r.ncol ? "%.*g " : "%.*g\n", precision, h[(size_t)i * r.ncol + j]);
+  }
+  fclose(f);
   return 0;
 }
 

@@ -12,6 +12,8 @@ import numpy as np
 
 from . import _abi
 from ._abi import XG_SYSTEM_BJPCG, XG_SYSTEM_PROFILE_SPD, xg_step_stats  # noqa: F401
+from ._abi import (XG_REC_ACCEL, XG_REC_DISP, XG_REC_ENVELOPE, XG_REC_NODE,  # noqa: F401
+                   XG_REC_VEL)
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB = os.path.join(HERE, "libxara_gpu.so")
@@ -174,6 +176,42 @@ class DeviceModel:
         _check(lib().xg_elemset_get_history(self.h, 0, _p(buf), n))
         del r
         return buf
+
+    # -- recorders ------------------------------------------------------------
+    def add_recorder(self, nodes, dofs, response=XG_REC_DISP, kind=XG_REC_NODE, time=False,
+                     dT=0.0):
+        """`recorder Node|EnvelopeNode <-time> <-dT dT> -node nodes -dof dofs
+        disp|vel|accel` (dofs 0-based); recorded on the device after every
+        committed step of :meth:`analyze`.  Returns the recorder id."""
+        L = lib()
+        L.xg_recorder_add.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_void_p, C.c_int,
+                                      C.c_void_p, C.c_int, C.c_int, C.c_double,
+                                      C.POINTER(C.c_int)]
+        nodes = np.ascontiguousarray(nodes, np.int32)
+        dofs = np.ascontiguousarray(dofs, np.int32)
+        rid = C.c_int()
+        _check(L.xg_recorder_add(self.h, int(kind), int(response), _p(nodes), len(nodes),
+                                 _p(dofs), len(dofs), 1 if time else 0, float(dT),
+                                 C.byref(rid)))
+        return rid.value
+
+    def recorder(self, rid):
+        """The recorder's rows so far ([rows, cols])."""
+        L = lib()
+        L.xg_recorder_size.argtypes = [C.c_void_p, C.c_int, C.POINTER(C.c_int),
+                                       C.POINTER(C.c_int)]
+        L.xg_recorder_read.argtypes = [C.c_void_p, C.c_int, C.c_void_p, C.c_int]
+        rows, cols = C.c_int(), C.c_int()
+        _check(L.xg_recorder_size(self.h, int(rid), C.byref(rows), C.byref(cols)))
+        out = np.zeros((rows.value, cols.value))
+        _check(L.xg_recorder_read(self.h, int(rid), _p(out), rows.value))
+        return out
+
+    def write_recorder(self, rid, path, precision=6):
+        """Write the rows as the reference's DataFileStream does."""
+        L = lib()
+        L.xg_recorder_write.argtypes = [C.c_void_p, C.c_int, C.c_char_p, C.c_int]
+        _check(L.xg_recorder_write(self.h, int(rid), str(path).encode(), int(precision)))
 
     def fiber_records(self):
         """Committed fiber records of a frame model, [fibers x sections, 12]."""
