@@ -340,6 +340,33 @@ int xg_model_stream(const xg_model *m, void **stream);
 int xg_profile_counters(xg_model *m, long long *point_updates, long long *section_updates,
                         long long *element_updates);
 
+/* ---- A standalone linear system on the device: LinearSOE
+        (system_of_eqn/linearSOE/LinearSOE.h: setSize, zeroA, zeroB, addA,
+        addB, setB, solve, getX, getB) for callers that keep the
+        reference's own element loop (FE_Element::addAtoSOE feeding addA).
+        The pattern is CSR with sorted columns (SparseGenColLinSOE::setSize
+        order); addA / addB / setB follow SparseGenColLinSOE.cpp:214-350 (an
+        equation number < 0 is skipped; an entry outside the pattern is an
+        error) and accumulate on the host; solve runs block-Jacobi PCG on
+        the device (blocks of 1-6 equations, or point Jacobi when nblk is
+        0) and copies X back.  Not reentrant per handle. ---- */
+typedef struct xg_linsoe xg_linsoe;
+int xg_linsoe_create(int num_eqn, const int *rowptr, const int *colidx, const int *blk_start,
+                     int nblk, xg_linsoe **out);
+void xg_linsoe_destroy(xg_linsoe *s);
+int xg_linsoe_zero_a(xg_linsoe *s);                               /* zeroA */
+int xg_linsoe_zero_b(xg_linsoe *s);                               /* zeroB */
+/* A(id[i], id[j]) += fact * m[i*ndof + j] (addA, m row-major ndof x ndof) */
+int xg_linsoe_add_a(xg_linsoe *s, const double *m, const int *id, int ndof, double fact);
+int xg_linsoe_add_b(xg_linsoe *s, const double *v, const int *id, int ndof, double fact);
+int xg_linsoe_set_b(xg_linsoe *s, const double *v, double fact);  /* B = fact * v */
+int xg_linsoe_get_a(const xg_linsoe *s, double *vals);            /* CSR values */
+int xg_linsoe_get_b(const xg_linsoe *s, double *b);
+/* PCG to ||r|| <= rtol ||b||; XG_ESOLVE on breakdown or maxit (X holds the
+   last iterate); the device copy of the pattern is made at the first call. */
+int xg_linsoe_solve(xg_linsoe *s, double rtol, int maxit, int *iters, double *relres);
+int xg_linsoe_get_x(const xg_linsoe *s, double *x);
+
 /* ---- Recorders (recorder/NodeRecorder.cpp, EnvelopeNodeRecorder.cpp; the
         `recorder Node|EnvelopeNode -file f <-time> <-dT dt> -node ... -dof
         ... disp|vel|accel` commands).  Values are gathered on the device

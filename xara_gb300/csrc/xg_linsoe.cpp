@@ -1,0 +1,266 @@
+// xg_linsoe.cpp -- a standalone linear system of equations solved on the
+// device: the reference's LinearSOE interface (system_of_eqn/linearSOE/
+// LinearSOE.h) for callers that keep their own element loop.  The pattern
+// comes in as CSR with sorted columns per row; assembly follows
+// SparseGenColLinSOE (sparseGEN/SparseGenColLinSOE.cpp:214-350: addA adds
+// fact * m(i,j) where both equation numbers are >= 0, locating the column by
+// a search of the row; addB / setB likewise) and accumulates in host memory,
+// the way the reference's FE_Element loop feeds it; solve() runs the
+// block-Jacobi PCG of the model path (sliced ELL SpMV, long rows in chunks)
+// on the device and returns X to the host.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstdio>
+#include <vector>
+
+#include "xg_internal.h"
+
+namespace {
+
+int lfail(int code, const char *msg) {
+  xg::record_error(msg);
+  return code;
+}
+
+template <typename T>
+struct DevArray {
+  T *p = nullptr;
+  int alloc(size_t n) {
+    if (p) cudaFree(p);
+    p = nullptr;
+    if (n == 0) return 0;
+    return cudaMalloc(&p, n * sizeof(T)) == cudaSuccess ? 0 : XG_ENOMEM;
+  }
+  int upload(const T *h, size_t n, cudaStream_t s) {
+    if (alloc(n)) return XG_ENOMEM;
+    if (n && cudaMemcpyAsync(p, h, n * sizeof(T), cudaMemcpyHostToDevice, s) != cudaSuccess)
+      return XG_ECUDA;
+    return 0;
+  }
+  ~DevArray() {
+    if (p) cudaFree(p);
+  }
+};
+
+}  // namespace
+
+struct xg_linsoe {
+  int n = 0;
+  std::vector<int> rowptr, colidx, blk;
+  std::vector<double> A, B, X;
+  // device copies, set up at the first solve
+  bool ready = false;
+  cudaStream_t stream = nullptr;
+  DevArray<int> rp, ci, bs, chunk_row, chunk_beg, long_chunk0, sell_cols, flags;
+  DevArray<long> sell_off;
+  DevArray<unsigned int> barrier;
+  DevArray<double> vals, b, x, binv, r, z, p, q, partials, scalars, sell_vals, chunk_part;
+  xg::PcgSystem S{};
+
+  ~xg_linsoe() {
+    if (stream) cudaStreamDestroy(stream);
+  }
+
+  // Column slot of (row, col) in the pattern, or -1.
+  long slot(int row, int col) const {
+    const int *b = colidx.data() + rowptr[row], *e = colidx.data() + rowptr[row + 1];
+    const int *it = std::lower_bound(b, e, col);
+    return (it != e && *it == col) ? (long)(it - colidx.data()) : -1;
+  }
+
+  int setup() {
+    if (ready) return 0;
+    if (cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking) != cudaSuccess)
+      return lfail(XG_ECUDA, "xg_linsoe: stream creation failed");
+    const int nblk = (int)blk.size() - 1;
+    const size_t nnz = colidx.size(), nv = std::max(n, 1);
+    constexpr int kCap = 256;
+    std::vector<long> off;
+    std::vector<int> crow, cbeg, lc0, cols;
+    xg::sell_layout(n, rowptr.data(), kCap, off, crow, cbeg, lc0);
+    xg::sell_columns(n, rowptr.data(), colidx.data(), kCap, off, cols);
+    int e = 0;
+    e |= rp.upload(rowptr.data(), rowptr.size(), stream);
+    e |= ci.upload(colidx.data(), nnz, stream);
+    e |= bs.upload(blk.data(), blk.size(), stream);
+    e |= vals.alloc(std::max<size_t>(nnz, 1)) | b.alloc(nv) | x.alloc(nv);
+    e |= binv.alloc((size_t)std::max(nblk, 1) * 36);
+    e |= r.alloc(nv) | z.alloc(nv) | p.alloc(nv) | q.alloc(nv);
+    e |= partials.alloc(3 * (size_t)std::max(xg::pcg_max_blocks(), xg::pcg_sell_max_blocks()) + 8);
+    e |= scalars.alloc(8) | barrier.alloc(2) | flags.alloc(4);
+    e |= sell_off.upload(off.data(), off.size(), stream);
+    e |= sell_cols.upload(cols.data(), cols.size(), stream);
+    e |= sell_vals.alloc(std::max<size_t>(cols.size(), 1));
+    e |= chunk_row.upload(crow.data(), crow.size(), stream);
+    e |= chunk_beg.upload(cbeg.data(), cbeg.size(), stream);
+    e |= long_chunk0.upload(lc0.data(), lc0.size(), stream);
+    e |= chunk_part.alloc(std::max<size_t>(crow.size(), 1));
+    if (e) return lfail(XG_ENOMEM, "xg_linsoe: device allocation failed");
+    S.n = n;
+    S.rowptr = rp.p;
+    S.colidx = ci.p;
+    S.vals = vals.p;
+    S.nblk = nblk;
+    S.blk_start = bs.p;
+    S.binv = binv.p;
+    S.r = r.p;
+    S.z = z.p;
+    S.p = p.p;
+    S.q = q.p;
+    S.partials = partials.p;
+    S.barrier = barrier.p;
+    S.flags = flags.p;
+    S.scalars = scalars.p;
+    S.sell_off = sell_off.p;
+    S.sell_cols = sell_cols.p;
+    S.sell_vals = sell_vals.p;
+    S.sell_cap = kCap;
+    S.nlong = (int)lc0.size() - 1;
+    S.nchunks = (int)crow.size();
+    S.chunk_row = chunk_row.p;
+    S.chunk_beg = chunk_beg.p;
+    S.long_chunk0 = long_chunk0.p;
+    S.chunk_part = chunk_part.p;
+    if (cudaStreamSynchronize(stream) != cudaSuccess)
+      return lfail(XG_ECUDA, "xg_linsoe: set-up copies failed");
+    ready = true;
+    return 0;
+  }
+};
+
+extern "C" {
+
+int xg_linsoe_create(int n, const int *rowptr, const int *colidx, const int *blk_start, int nblk,
+                     xg_linsoe **out) {
+  if (!out || n < 0 || !rowptr || (n > 0 && !colidx) || nblk < 0 || (nblk > 0 && !blk_start))
+    return lfail(XG_EINVAL, "xg_linsoe_create: bad argument");
+  *out = nullptr;
+  if (rowptr[0] != 0) return lfail(XG_EINVAL, "xg_linsoe_create: rowptr[0] must be 0");
+  for (int i = 0; i < n; i++) {
+    if (rowptr[i + 1] < rowptr[i]) return lfail(XG_EINVAL, "xg_linsoe_create: rowptr decreases");
+    for (int k = rowptr[i]; k < rowptr[i + 1]; k++)
+      if (colidx[k] < 0 || colidx[k] >= n || (k > rowptr[i] && colidx[k] <= colidx[k - 1]))
+        return lfail(XG_EINVAL, "xg_linsoe_create: columns must be sorted, distinct, in range");
+  }
+  std::vector<int> blk;
+  if (nblk > 0) {
+    if (blk_start[0] != 0 || blk_start[nblk] != n)
+      return lfail(XG_EINVAL, "xg_linsoe_create: blocks must run from 0 to n");
+    for (int k = 0; k < nblk; k++)
+      if (blk_start[k + 1] - blk_start[k] < 1 || blk_start[k + 1] - blk_start[k] > 6)
+        return lfail(XG_EINVAL, "xg_linsoe_create: blocks of 1 to 6 equations");
+    blk.assign(blk_start, blk_start + nblk + 1);
+  } else {
+    blk.resize(n + 1);
+    for (int i = 0; i <= n; i++) blk[i] = i;   // point Jacobi
+  }
+  auto *s = new xg_linsoe;
+  s->n = n;
+  s->rowptr.assign(rowptr, rowptr + n + 1);
+  s->colidx.assign(colidx, colidx + rowptr[n]);
+  s->blk = std::move(blk);
+  s->A.assign(rowptr[n], 0.0);
+  s->B.assign(n, 0.0);
+  s->X.assign(n, 0.0);
+  *out = s;
+  return 0;
+}
+
+void xg_linsoe_destroy(xg_linsoe *s) { delete s; }
+
+int xg_linsoe_zero_a(xg_linsoe *s) {
+  if (!s) return lfail(XG_EINVAL, "null system");
+  std::fill(s->A.begin(), s->A.end(), 0.0);
+  return 0;
+}
+
+int xg_linsoe_zero_b(xg_linsoe *s) {
+  if (!s) return lfail(XG_EINVAL, "null system");
+  std::fill(s->B.begin(), s->B.end(), 0.0);
+  return 0;
+}
+
+int xg_linsoe_add_a(xg_linsoe *s, const double *m, const int *id, int ndof, double fact) {
+  if (!s || ndof < 0 || (ndof && (!m || !id))) return lfail(XG_EINVAL, "bad addA argument");
+  if (fact == 0.0) return 0;
+  for (int i = 0; i < ndof; i++) {
+    const int row = id[i];
+    if (row < 0) continue;
+    if (row >= s->n) return lfail(XG_EINVAL, "addA: equation number out of range");
+    for (int j = 0; j < ndof; j++) {
+      const int col = id[j];
+      if (col < 0) continue;
+      const long k = s->slot(row, col);
+      if (k < 0) return lfail(XG_EINVAL, "addA: entry outside the pattern");
+      s->A[k] += fact * m[(size_t)i * ndof + j];
+    }
+  }
+  return 0;
+}
+
+int xg_linsoe_add_b(xg_linsoe *s, const double *v, const int *id, int ndof, double fact) {
+  if (!s || ndof < 0 || (ndof && (!v || !id))) return lfail(XG_EINVAL, "bad addB argument");
+  for (int i = 0; i < ndof; i++) {
+    if (id[i] < 0) continue;
+    if (id[i] >= s->n) return lfail(XG_EINVAL, "addB: equation number out of range");
+    s->B[id[i]] += fact * v[i];
+  }
+  return 0;
+}
+
+int xg_linsoe_set_b(xg_linsoe *s, const double *v, double fact) {
+  if (!s || (s->n && !v)) return lfail(XG_EINVAL, "bad setB argument");
+  for (int i = 0; i < s->n; i++) s->B[i] = fact * v[i];
+  return 0;
+}
+
+int xg_linsoe_get_a(const xg_linsoe *s, double *vals) {
+  if (!s || (!vals && !s->A.empty())) return lfail(XG_EINVAL, "bad argument");
+  std::copy(s->A.begin(), s->A.end(), vals);
+  return 0;
+}
+
+int xg_linsoe_solve(xg_linsoe *s, double rtol, int maxit, int *iters, double *relres) {
+  if (!s || !(rtol > 0.0) || maxit < 1) return lfail(XG_EINVAL, "bad solve settings");
+  if (s->n == 0) return 0;
+  if (int e = s->setup()) return e;
+  cudaStream_t st = s->stream;
+  if (cudaMemcpyAsync(s->vals.p, s->A.data(), s->A.size() * sizeof(double),
+                      cudaMemcpyHostToDevice, st) != cudaSuccess ||
+      cudaMemcpyAsync(s->b.p, s->B.data(), s->B.size() * sizeof(double), cudaMemcpyHostToDevice,
+                      st) != cudaSuccess ||
+      cudaMemsetAsync(s->x.p, 0, s->n * sizeof(double), st) != cudaSuccess)
+    return lfail(XG_ECUDA, "xg_linsoe_solve: copies failed");
+  if (xg::pcg_factor_blocks(s->S, st) != 0) return lfail(XG_ECUDA, "xg_linsoe_solve: blocks");
+  int it = 0;
+  double rr = 0.0;
+  const int r = xg::pcg_solve(s->S, s->b.p, s->x.p, rtol, maxit, &it, &rr, st);
+  if (cudaMemcpyAsync(s->X.data(), s->x.p, s->n * sizeof(double), cudaMemcpyDeviceToHost, st) !=
+          cudaSuccess ||
+      cudaStreamSynchronize(st) != cudaSuccess)
+    return lfail(XG_ECUDA, "xg_linsoe_solve: copy of X failed");
+  if (iters) *iters = it;
+  if (relres) *relres = rr;
+  if (r) {
+    char msg[128];
+    snprintf(msg, sizeof msg, "xg_linsoe_solve: PCG did not converge (%d iterations, %.3e)", it,
+             rr);
+    return lfail(XG_ESOLVE, msg);
+  }
+  return 0;
+}
+
+int xg_linsoe_get_x(const xg_linsoe *s, double *x) {
+  if (!s || (!x && s->n)) return lfail(XG_EINVAL, "bad argument");
+  std::copy(s->X.begin(), s->X.end(), x);
+  return 0;
+}
+
+int xg_linsoe_get_b(const xg_linsoe *s, double *b) {
+  if (!s || (!b && s->n)) return lfail(XG_EINVAL, "bad argument");
+  std::copy(s->B.begin(), s->B.end(), b);
+  return 0;
+}
+
+}  // extern "C"

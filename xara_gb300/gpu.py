@@ -395,6 +395,90 @@ def uniaxial_vjp(kind, param, hc, strain, yb):
     return hb, sb.value, qb
 
 
+class LinearSystem:
+    """A standalone device linear system with the reference's LinearSOE
+    calls (``xg_linsoe_*``): CSR pattern with sorted columns, host-side
+    addA / addB / setB, block-Jacobi PCG solve on the device."""
+
+    def __init__(self, rowptr, colidx, blk_start=None):
+        L = lib()
+        L.xg_linsoe_create.argtypes = [C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int,
+                                       C.POINTER(C.c_void_p)]
+        L.xg_linsoe_destroy.argtypes = [C.c_void_p]
+        for name in ("xg_linsoe_zero_a", "xg_linsoe_zero_b"):
+            getattr(L, name).argtypes = [C.c_void_p]
+        L.xg_linsoe_add_a.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_double]
+        L.xg_linsoe_add_b.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_double]
+        L.xg_linsoe_set_b.argtypes = [C.c_void_p, C.c_void_p, C.c_double]
+        for name in ("xg_linsoe_get_a", "xg_linsoe_get_b", "xg_linsoe_get_x"):
+            getattr(L, name).argtypes = [C.c_void_p, C.c_void_p]
+        L.xg_linsoe_solve.argtypes = [C.c_void_p, C.c_double, C.c_int, C.POINTER(C.c_int),
+                                      C.POINTER(C.c_double)]
+        self._rp = np.ascontiguousarray(rowptr, np.int32)
+        self._ci = np.ascontiguousarray(colidx, np.int32)
+        self.n = len(self._rp) - 1
+        blk = None if blk_start is None else np.ascontiguousarray(blk_start, np.int32)
+        h = C.c_void_p()
+        _check(L.xg_linsoe_create(self.n, _p(self._rp), _p(self._ci),
+                                  _p(blk) if blk is not None else None,
+                                  0 if blk is None else len(blk) - 1, C.byref(h)))
+        self.h = h
+
+    def close(self):
+        if self.h:
+            lib().xg_linsoe_destroy(self.h)
+            self.h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def zero_a(self):
+        _check(lib().xg_linsoe_zero_a(self.h))
+
+    def zero_b(self):
+        _check(lib().xg_linsoe_zero_b(self.h))
+
+    def add_a(self, m, ids, fact=1.0):
+        m = np.ascontiguousarray(m, np.float64)
+        ids = np.ascontiguousarray(ids, np.int32)
+        _check(lib().xg_linsoe_add_a(self.h, _p(m), _p(ids), len(ids), float(fact)))
+
+    def add_b(self, v, ids, fact=1.0):
+        v = np.ascontiguousarray(v, np.float64)
+        ids = np.ascontiguousarray(ids, np.int32)
+        _check(lib().xg_linsoe_add_b(self.h, _p(v), _p(ids), len(ids), float(fact)))
+
+    def set_b(self, v, fact=1.0):
+        v = np.ascontiguousarray(v, np.float64)
+        _check(lib().xg_linsoe_set_b(self.h, _p(v), float(fact)))
+
+    def values(self):
+        out = np.zeros(len(self._ci))
+        _check(lib().xg_linsoe_get_a(self.h, _p(out)))
+        return out
+
+    def rhs(self):
+        out = np.zeros(self.n)
+        _check(lib().xg_linsoe_get_b(self.h, _p(out)))
+        return out
+
+    def solve(self, rtol=1e-12, maxit=20000):
+        it, rr = C.c_int(), C.c_double()
+        _check(lib().xg_linsoe_solve(self.h, float(rtol), int(maxit), C.byref(it), C.byref(rr)))
+        x = np.zeros(self.n)
+        _check(lib().xg_linsoe_get_x(self.h, _p(x)))
+        return x, it.value, rr.value
+
+
 def set_graph(model, enable=True):
     """Run Newmark steps of many-part models as CUDA graphs (see xg_analysis_set_graph)."""
     L = lib()
