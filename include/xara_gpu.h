@@ -258,6 +258,11 @@ int xg_elemset_set_history(xg_model *m, int which, const double *in, long n);
         runtime/runtime/BasicAnalysisBuilder.cpp:820) or block-Jacobi PCG,
         both on the device ---- */
 
+/* `loadConst -time t`: every load pattern applied so far keeps its current
+   factor from now on and the domain time becomes t (the same happens at the
+   next xg_analysis_set_phase when a finished phase has load_const set). */
+int xg_analysis_load_const(xg_model *m, double time);
+
 /* Choose the system (XG_SYSTEM_*); the default is XG_SYSTEM_PROFILE_SPD.
    Choosing the profile allocates its envelope tiles and fails with
    XG_ENOMEM when they would take more than half the free device memory. */

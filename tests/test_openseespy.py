@@ -1,0 +1,162 @@
+"""The OpenSeesPy-style front-end (xara_gb300.openseespy): command sequences
+as a user of the reference's Python interface writes them give the same
+model description as the library's builders (CPU), and the same analysis on
+the GPU -- including a load pattern defined after loadConst, which rebuilds
+the device model and replays the analysis so far."""
+import numpy as np
+import pytest
+
+from xara_gb300 import configs
+from xara_gb300 import openseespy as ops
+
+
+def _quad_script(nx=8, ny=4, steps=4):
+    ops.wipe()
+    ops.model("basic", "-ndm", 2, "-ndf", 2)
+    for j in range(ny + 1):
+        for i in range(nx + 1):
+            ops.node(j * (nx + 1) + i + 1, float(i), float(j))
+    ops.nDMaterial("J2Plasticity", 1, *configs.J2_STEEL[:6])
+    t = 1
+    for j in range(ny):
+        for i in range(nx):
+            n1 = j * (nx + 1) + i + 1
+            ops.element("quad", t, n1, n1 + 1, n1 + nx + 2, n1 + nx + 1, 1.0, "PlaneStrain", 1)
+            t += 1
+    for i in range(nx + 1):
+        ops.fix(i + 1, 1, 1)
+    master = ny * (nx + 1) + 1
+    for i in range(1, nx + 1):
+        ops.equalDOF(master, master + i, 2)
+    ops.timeSeries("Linear", 1)
+    ops.pattern("Plain", 1, 1)
+    ops.load(master, 0.0, -1.0)
+    ops.constraints("Plain")
+    ops.numberer("RCM")
+    ops.system("ProfileSPD")
+    ops.test("NormDispIncr", 1e-10, 25)
+    ops.algorithm("Newton")
+    ops.integrator("DisplacementControl", master, 2, -0.005 * ny / steps)
+    ops.analysis("Static")
+    return master
+
+
+def _frame_script(bays=2, stories=3, nfib=40, steps=5, grav_steps=4, gravity=-150e3):
+    ops.wipe()
+    ops.model("basic", "-ndm", 2, "-ndf", 3)
+    nx = bays + 1
+    for j in range(stories + 1):
+        for i in range(nx):
+            ops.node(j * nx + i + 1, i * 6.0, j * 3.5)
+    for i in range(nx):
+        ops.fix(i + 1, 1, 1, 1)
+    ops.uniaxialMaterial("Steel02", 1, 350e6, 200e9, 0.01, 18.0, 0.925, 0.15)
+    for tag, dims in ((1, (0.45, 0.3, 0.022, 0.014)), (2, (0.5, 0.2, 0.016, 0.010))):
+        ops.section("Fiber", tag)
+        for y, A in zip(*configs.wide_flange_fibers(*dims, nfib)):
+            ops.fiber(y, 0.0, A, 1)
+    ops.geomTransf("Linear", 1)
+    ops.beamIntegration("Lobatto", 1, 1, 5)
+    ops.beamIntegration("Lobatto", 2, 2, 5)
+    t = 1
+    for j in range(stories):
+        for i in range(nx):
+            ops.element("forceBeamColumn", t, j * nx + i + 1, (j + 1) * nx + i + 1, 1, 1)
+            t += 1
+    for j in range(1, stories + 1):
+        for i in range(bays):
+            ops.element("forceBeamColumn", t, j * nx + i + 1, j * nx + i + 2, 1, 2)
+            t += 1
+    ops.timeSeries("Linear", 1)
+    ops.pattern("Plain", 1, 1)
+    for n in range(nx + 1, (stories + 1) * nx + 1):
+        ops.load(n, 0.0, gravity, 0.0)
+    ops.constraints("Plain")
+    ops.numberer("RCM")
+    ops.system("ProfileSPD")
+    ops.test("NormDispIncr", 1e-10, 50)
+    ops.algorithm("Newton")
+    ops.integrator("LoadControl", 1.0 / grav_steps)
+    ops.analysis("Static")
+    roof = stories * nx + 1
+    return roof, nx
+
+
+def _lateral(roof, nx, stories=3, steps=5):
+    ops.loadConst("-time", 0.0)
+    ops.timeSeries("Linear", 2)
+    ops.pattern("Plain", 2, 2)
+    for j in range(1, stories + 1):
+        ops.load(j * nx + 1, float(j) / stories, 0.0, 0.0)
+    ops.integrator("DisplacementControl", roof, 1, 0.02 * stories * 3.5 / steps)
+
+
+def _same_desc(a, b, skip=()):
+    assert (a.ndm, a.ndf, a.elem_type) == (b.ndm, b.ndf, b.elem_type)
+    for k, v in b.arrays.items():
+        if k in skip or v is None:
+            continue
+        assert a.arrays[k] is not None, k
+        np.testing.assert_array_equal(a.arrays[k], v, err_msg=k)
+
+
+def test_quad_commands_give_the_builders_model():
+    _quad_script()
+    d, _ = configs.quad_block(8, 4, steps=4)
+    _same_desc(ops.build_desc(), d)
+    ops.wipe()
+
+
+def test_frame_commands_give_the_builders_model():
+    roof, nx = _frame_script()
+    _lateral(roof, nx)
+    d, _ = configs.steel_frame_2d(2, 3, steps=5, grav_steps=4)
+    _same_desc(ops.build_desc(), d)
+    ops.wipe()
+
+
+def test_unsupported_commands_are_named():
+    ops.wipe()
+    ops.model("basic", "-ndm", 2, "-ndf", 3)
+    with pytest.raises(NotImplementedError, match="uniaxialMaterial Steel01"):
+        ops.uniaxialMaterial("Steel01", 1, 1.0, 1.0, 0.01)
+    with pytest.raises(NotImplementedError, match="algorithm KrylovNewton"):
+        ops.algorithm("KrylovNewton")
+    ops.wipe()
+
+
+@pytest.mark.gpu
+def test_frame_commands_run_like_the_builders(need_gpu, tmp_path):
+    from xara_gb300 import gpu
+    roof, nx = _frame_script()
+    ops.recorder("Node", "-file", str(tmp_path / "roof.out"), "-time", "-node", roof,
+                 "-dof", 1, "disp")
+    assert ops.analyze(4) == 0
+    _lateral(roof, nx)
+    assert ops.analyze(5) == 0               # rebuilds with pattern 2 and replays gravity
+    u_ops = ops.nodeDisp(roof, 1)
+    lines = (tmp_path / "roof.out").read_text().splitlines()
+    ops.wipe()
+    desc, phases = configs.steel_frame_2d(2, 3, steps=5, grav_steps=4)
+    with gpu.DeviceModel(desc) as m:
+        m.set_system(gpu.XG_SYSTEM_PROFILE_SPD)
+        U, lam, _ = m.run(phases)
+    i = list(desc.node_tag).index(roof)
+    assert u_ops == U[-1, i * 3]
+    # the recorder: 4 gravity steps and 5 pushover steps, time then roof drift
+    assert len(lines) == 9
+    assert float(lines[-1].split()[1]) == pytest.approx(U[-1, i * 3], rel=1e-5)
+
+
+@pytest.mark.gpu
+def test_quad_commands_run_like_the_builders(need_gpu):
+    from xara_gb300 import gpu
+    master = _quad_script()
+    assert ops.analyze(4) == 0
+    u = ops.nodeDisp(master)
+    ops.wipe()
+    desc, phases = configs.quad_block(8, 4, steps=4)
+    with gpu.DeviceModel(desc) as m:
+        U, _, _ = m.run(phases)
+    i = list(desc.node_tag).index(master)
+    np.testing.assert_array_equal(u, U[-1, 2 * i:2 * i + 2])

@@ -2417,6 +2417,20 @@ int xg_analysis_set_phase(xg_model *m, const xg_phase_desc *ph) {
   return m->init_phase();
 }
 
+// loadConst -time t (domain/domain/Domain.cpp setLoadConstant + setCurrentTime):
+// every pattern applied so far keeps its current factor, the time becomes t
+int xg_analysis_load_const(xg_model *m, double time) {
+  if (!m) return fail(XG_EINVAL, "null model");
+  for (int p = 0; p < 8; p++)
+    if (m->added[p] && !m->pattern_const[p]) {
+      m->pattern_const[p] = 1;
+      m->lambda_const[p] = m->time;
+    }
+  m->time = m->time_c = time;
+  m->phase_closed = true;
+  return 0;
+}
+
 int xg_analysis_set_system(xg_model *m, int system) {
   if (!m) return fail(XG_EINVAL, "null model");
   if (system != XG_SYSTEM_BJPCG && system != XG_SYSTEM_PROFILE_SPD)
