@@ -383,6 +383,10 @@ int xg_linsoe_get_x(const xg_linsoe *s, double *x);
 #define XG_REC_DISP     0
 #define XG_REC_VEL      1
 #define XG_REC_ACCEL    2
+/* The committed displacements, velocities or accelerations (XG_REC_DISP /
+   VEL / ACCEL) of every node, [num_nodes * ndf] in node-tag order
+   (Node::getDisp / getVel / getAccel). */
+int xg_get_response(const xg_model *m, int response, double *out);
 int xg_recorder_add(xg_model *m, int kind, int response, const int *node_tags, int num_nodes,
                     const int *dofs, int num_dofs, int echo_time, double dT, int *id);
 /* Rows recorded so far (3 for an envelope once it has a record) and columns. */

@@ -61,6 +61,8 @@ def test_node_and_envelope_recorders(need_gpu, tmp_path):
         vel, vel3, acc = m.recorder(r_vel), m.recorder(r_vel3), m.recorder(r_acc)
         m.write_recorder(r_disp, tmp_path / "disp.out")
         m.write_recorder(r_env, tmp_path / "env.out", precision=10)
+        v_end, a_end = m.response(gpu.XG_REC_VEL), m.response(gpu.XG_REC_ACCEL)
+        np.testing.assert_array_equal(m.response(gpu.XG_REC_DISP), m.disp()[0])
     ndf = desc.ndf
     idx = [np.searchsorted(tags, n) for n in nodes]
     expect = np.zeros((len(U), len(nodes) * len(dofs)))
@@ -83,6 +85,9 @@ def test_node_and_envelope_recorders(need_gpu, tmp_path):
             nxt = t + 3 * dt
     np.testing.assert_array_equal(vel3, vel[keep])
     assert vel.shape == (len(U), len(nodes)) and np.abs(vel).max() > 0
+    # the last rows are the committed velocities and accelerations
+    np.testing.assert_array_equal(vel[-1], v_end[[i * ndf for i in idx]])
+    np.testing.assert_array_equal(acc[-1], a_end[[i * ndf + 1 for i in idx]])
     assert acc.shape == (len(U), len(nodes)) and np.abs(acc).max() > 0
     # DataFileStream: blank-separated values, %g with the precision
     text = (tmp_path / "disp.out").read_text().splitlines()

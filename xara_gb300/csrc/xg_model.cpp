@@ -2478,6 +2478,17 @@ int xg_get_disp(const xg_model *m, double *u, double *lambda) {
   return 0;
 }
 
+int xg_get_response(const xg_model *m, int response, double *out) {
+  if (!m || !out || response < XG_REC_DISP || response > XG_REC_ACCEL)
+    return fail(XG_EINVAL, "bad argument");
+  const double *src = response == XG_REC_DISP ? m->d_Uc.p
+                      : response == XG_REC_VEL ? m->d_Vc.p : m->d_Ac.p;
+  CK(cudaMemcpyAsync(out, src, (size_t)m->nn * m->ndf * sizeof(double), cudaMemcpyDeviceToHost,
+                     m->stream));
+  CK(cudaStreamSynchronize(m->stream));
+  return 0;
+}
+
 int xg_recorder_add(xg_model *m, int kind, int response, const int *node_tags, int num_nodes,
                     const int *dofs, int num_dofs, int echo_time, double dT, int *id) {
   if (!m || !id || num_nodes < 0 || num_dofs < 0 || (num_nodes && !node_tags) ||

@@ -259,6 +259,12 @@ class DeviceModel:
         _check(lib().xg_get_disp(self.h, _p(u), C.byref(lam)))
         return u, lam.value
 
+    def response(self, which=XG_REC_DISP):
+        """Committed displacements, velocities or accelerations [nu]."""
+        out = np.zeros(self.nu)
+        _check(lib().xg_get_response(self.h, int(which), _p(out)))
+        return out
+
     def reset(self):
         _check(lib().xg_reset(self.h))
 

@@ -22,7 +22,8 @@ transformations; one element type per model), ``fix``, ``equalDOF``,
 ``constraints Plain|Transformation``, ``numberer RCM``, ``system
 ProfileSPD|CudaBJPCG``, ``test NormDispIncr|NormUnbalance``, ``algorithm
 Newton``, ``integrator LoadControl|DisplacementControl|Newmark``,
-``loadConst``, ``recorder Node|EnvelopeNode``.  Anything else raises
+``loadConst``, ``nodeDisp|nodeVel|nodeAccel``, ``getTime``, ``recorder
+Node|EnvelopeNode``.  Anything else raises
 ``NotImplementedError`` naming the command.
 
 The device model is built at the first ``analyze``.  A command that changes
@@ -564,6 +565,20 @@ def nodeDisp(tag, dof=-1):
     u, _ = _committed()
     i = sorted(_S.nodes).index(int(tag))
     return list(u[i]) if int(dof) < 1 else float(u[i, int(dof) - 1])
+
+
+def _node_response(which, tag, dof):
+    u = _S.model.response(which).reshape(-1, _S.ndf)
+    i = sorted(_S.nodes).index(int(tag))
+    return list(u[i]) if int(dof) < 1 else float(u[i, int(dof) - 1])
+
+
+def nodeVel(tag, dof=-1):
+    return _node_response(XG_REC_VEL, tag, dof)
+
+
+def nodeAccel(tag, dof=-1):
+    return _node_response(XG_REC_ACCEL, tag, dof)
 
 
 def getTime():
