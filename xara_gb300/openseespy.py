@@ -510,15 +510,24 @@ def _run(ph_kw, n):
     return 0
 
 
+def _apply_system():
+    """The `system` chosen last (it may change between analyses)."""
+    want = (_S.system, _S.solver)
+    if getattr(_S, "applied", None) != want:
+        _S.model.set_system(_S.system)
+        if _S.system == XG_SYSTEM_BJPCG:
+            _S.model.set_solver(*_S.solver)
+        _S.applied = want
+
+
 def _ensure_model():
     if _S.model is not None and _S.built_version == _S.version:
         return
     if _S.model is not None:
         _S.model.close()
     _S.model = gpu.DeviceModel(build_desc())
-    _S.model.set_system(_S.system)
-    if _S.system == XG_SYSTEM_BJPCG:
-        _S.model.set_solver(*_S.solver)
+    _S.applied = None
+    _apply_system()
     _S.built_version = _S.version
     _attach_recorders()
     for h in _S.history:                     # replay the analysis so far
@@ -534,6 +543,7 @@ def analyze(numIncr=1, dt=0.0, *args):
     """``analyze numIncr <dt>``: 0 on success, < 0 when a step fails (the
     model is then back at its last committed state)."""
     _ensure_model()
+    _apply_system()
     ph = _phase(int(numIncr), dt)
     r = _run(ph, int(numIncr))
     if r == 0:
