@@ -362,7 +362,7 @@ def run_frame(args):
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * step_s,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f64", "data": "synthetic (seeded model and lateral trial fields)",
-        "config": {"workload": "3D RC frame 10x10x20 (BASELINE config 1 model): one Newton "
+        "config": {"workload": "3D RC frame 10x10x20 (6,820 force-based elements): one Newton "
                                "iteration per step -- forceBeamColumn state determination, "
                                "assembly, ProfileSPD LDL' solve",
                    "elements": desc.num_elems, "equations": m.neq, "nnz": m.nnz,
@@ -476,7 +476,7 @@ def run_reference_frame(args):
         "ms_per_step": 1e3 * wall / args.steps, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded model and lateral "
                                                      "trial fields)",
-        "config": {"workload": "3D RC frame 10x10x20 (BASELINE config 1 model): one Newton "
+        "config": {"workload": "3D RC frame 10x10x20 (6,820 force-based elements): one Newton "
                                "iteration per step -- forceBeamColumn state determination, "
                                "assembly, ProfileSPD LDL' solve"},
         "newton_iters_per_s": args.steps * cores / wall,
@@ -601,7 +601,7 @@ def run_batch(args):
         "ms_per_step": 1e3 * dt / args.steps, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64",
         "data": "synthetic (seeded frames and Kanai-Tajimi records)",
-        "config": {"workload": f"{args.frames} independent 2D steel frames (BASELINE config 3): "
+        "config": {"workload": f"{args.frames} independent 2D steel frames under their own ground motions: "
                                "Newmark time steps, each frame under its own record",
                    "frames": args.frames, "elements": desc.meta["elements"],
                    "fiber_points": desc.meta["fiber_points"], "equations": m.neq,
@@ -704,7 +704,7 @@ def run_reference_batch(args):
         "warmup": args.warmup, "ms_per_step": 1e3 * tmax / args.steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
         "data": "synthetic (seeded frames and Kanai-Tajimi records)",
-        "config": {"workload": f"{args.frames} independent 2D steel frames (BASELINE config 3)"},
+        "config": {"workload": f"{args.frames} independent 2D steel frames under their own ground motions"},
         "cpu_baseline": {"value": value, "unit": "frame time steps/s", "cores": cores,
                          "kind": "port",
                          "sample": f"{cores} processes x {per} frames, steps {lead}.."
@@ -809,7 +809,7 @@ def run_adjoint(args):
         "higher_is_better": False, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
         "data": "synthetic (seeded frames and Kanai-Tajimi records)",
         "config": {"workload": f"gradient of the summed squared roof drift of {args.adj_frames} "
-                               f"2D steel frames over {N} Newmark steps (BASELINE config 4) "
+                               f"2D steel frames over {N} Newmark steps "
                                f"w.r.t. every member's Steel02 Fy, E0, b",
                    "frames": args.adj_frames, "members": int(desc.num_elems),
                    "parameters": int(3 * desc.num_elems), "checkpoint_every": K,
