@@ -96,6 +96,19 @@ __device__ void basic_T(const FrameView &v, int e, double (*T)[NB == 3 ? 6 : 12]
   }
 }
 
+// Sum over the G lanes of a section's lane group (lanes ip*G .. ip*G+G-1; a
+// fixed tree: rank r adds rank r+o, o = P2/2 .. 1), broadcast from the
+// group's first lane.
+__device__ __forceinline__ double group_sum_adj(double v, int rank, int G, int P2) {
+  for (int o = P2 >> 1; o > 0; o >>= 1) {
+    const double t = __shfl_down_sync(0xffffffffu, v, o);
+    if (rank + o < G) v += t;
+  }
+  return __shfl_sync(0xffffffffu, v, (int)(threadIdx.x & 31) - rank);
+}
+
+constexpr int kAdjMaxIp = 10;
+
 // tq[slot] += qb, slot known only at run time (no dynamic register indexing)
 __device__ __forceinline__ void add_slot(double (&tq)[kAdjSlots][3], int slot, const double *qb) {
 #pragma unroll
@@ -147,19 +160,24 @@ __global__ void __launch_bounds__(32 * kAdjWarps) k_adj_elem_a(FrameView v, AdjV
   const long fbase = v.foff[e];
   double *scr = a.scr + (long)e * (6 + nip * 4);
   double tq[kAdjSlots][3] = {};
-  double Sb[NB];
-#pragma unroll
-  for (int i = 0; i < NB; i++) Sb[i] = 0.0;
+  __shared__ double tsec_all[kAdjWarps][kAdjMaxIp][4];
+  double(*tsec)[4] = tsec_all[w];
   constexpr int kRow[6] = {0, 1, 1, 2, 2, 3};
-  for (int ip = 0; ip < nip; ip++) {
-    const double xL = v.xi[ip], xL1 = xL - 1.0;
-    const double ca[6] = {1.0, xL1, xL, xL1, xL, 1.0};
+  // every section at once, a group of G lanes each (the forward kernel's
+  // layout); lanes past the last group take no fiber
+  const int G = 32 / nip;
+  int P2 = 1;
+  while (P2 < G) P2 <<= 1;
+  const int gip = lane / G, rank = lane % G;
+  const bool on = gip < nip;
+  {
+    const int ip = on ? gip : nip - 1;
     double vsec[ORD];
 #pragma unroll
     for (int r = 0; r < ORD; r++) vsec[r] = st[42 + ip * 4 + r];
     double eb0 = 0.0, eb1 = 0.0, eb2 = 0.0;
     const long rec0 = (fbase + (long)ip * nf) * 12;
-    for (int fi = lane; fi < nf; fi += 32) {
+    for (int fi = rank; on && fi < nf; fi += G) {
       const int kf = f0 + fi;
       const double y = v.fy[kf] - ybar;
       double strain = vsec[0] - y * vsec[1];
@@ -184,24 +202,32 @@ __global__ void __launch_bounds__(32 * kAdjWarps) k_adj_elem_a(FrameView v, AdjV
       if (ORD == 4) eb2 += z * sb;
     }
     double eb[ORD];
-    eb[0] = warp_sum_adj(eb0);
-    eb[1] = warp_sum_adj(eb1);
-    if (ORD == 4) { eb[2] = warp_sum_adj(eb2); eb[3] = 0.0; }
-    if (lane == 0) {
+    eb[0] = group_sum_adj(eb0, rank, G, P2);
+    eb[1] = group_sum_adj(eb1, rank, G, P2);
+    if (ORD == 4) { eb[2] = group_sum_adj(eb2, rank, G, P2); eb[3] = 0.0; }
+    if (on && rank == 0) {
 #pragma unroll
       for (int r = 0; r < ORD; r++) scr[6 + ip * 4 + r] = eb[r];
+      const double *fs = st + 42 + nip * 4 + ip * 16;
+#pragma unroll
+      for (int r = 0; r < ORD; r++) {
+        double t = 0.0;
+#pragma unroll
+        for (int k = 0; k < ORD; k++) t += fs[r * ORD + k] * eb[k];
+        tsec[ip][r] = t;
+      }
     }
-    const double *fs = st + 42 + nip * 4 + ip * 16;
-    double t[ORD];
+  }
+  __syncwarp();
+  // Sb = sum over the sections, in section order, of b_s' t_s
+  double Sb[NB];
 #pragma unroll
-    for (int r = 0; r < ORD; r++) {
-      double s = 0.0;
+  for (int i = 0; i < NB; i++) Sb[i] = 0.0;
+  for (int ip = 0; ip < nip; ip++) {
+    const double xL = v.xi[ip], xL1 = xL - 1.0;
+    const double ca[6] = {1.0, xL1, xL, xL1, xL, 1.0};
 #pragma unroll
-      for (int k = 0; k < ORD; k++) s += fs[r * ORD + k] * eb[k];
-      t[r] = s;
-    }
-#pragma unroll
-    for (int c = 0; c < NB; c++) Sb[c] += ca[c] * t[kRow[c]];
+    for (int c = 0; c < NB; c++) Sb[c] += ca[c] * tsec[ip][kRow[c]];
   }
   const double *kv = st + 6;
   double zA[NB];
@@ -279,7 +305,12 @@ __global__ void __launch_bounds__(32 * kAdjWarps) k_adj_elem_b(FrameView v, AdjV
   }
   double tq[kAdjSlots][3] = {};
   constexpr int kRow[6] = {0, 1, 1, 2, 2, 3};
-  for (int ip = 0; ip < nip; ip++) {
+  // every section at once, a group of G lanes each
+  const int G = 32 / nip;
+  const int gip = lane / G, rank = lane % G;
+  const bool on = gip < nip;
+  if (on) {
+    const int ip = gip;
     const double xL = v.xi[ip], xL1 = xL - 1.0, wtL = v.wt[ip] * L;
     const double ca[6] = {1.0, xL1, xL, xL1, xL, 1.0};
     double bz[ORD];
@@ -294,16 +325,16 @@ __global__ void __launch_bounds__(32 * kAdjWarps) k_adj_elem_b(FrameView v, AdjV
     double qs[ORD];
 #pragma unroll
     for (int r = 0; r < ORD; r++) {
-      double s = 0.0;
+      double t = 0.0;
 #pragma unroll
-      for (int k = 0; k < ORD; k++) s += fs[r * ORD + k] * g[k];
-      qs[r] = s;
+      for (int k = 0; k < ORD; k++) t += fs[r * ORD + k] * g[k];
+      qs[r] = t;
     }
     double vsec[ORD];
 #pragma unroll
     for (int r = 0; r < ORD; r++) vsec[r] = st[42 + ip * 4 + r];
     const long rec0 = (fbase + (long)ip * nf) * 12;
-    for (int fi = lane; fi < nf; fi += 32) {
+    for (int fi = rank; fi < nf; fi += G) {
       const int kf = f0 + fi;
       const double y = v.fy[kf] - ybar, A = v.fA[kf];
       double strain = vsec[0] - y * vsec[1];
