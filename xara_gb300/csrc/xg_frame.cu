@@ -113,12 +113,19 @@ __device__ void steel02_trial(const double *q, const double *hc, double trialStr
   ht[5] = epsr; ht[6] = sigr; ht[7] = (double)kon; ht[8] = e; ht[9] = sig; ht[11] = R;
 }
 
+// Concrete02 parameters after the constructor's sign normalisation
+// (Concrete02.cpp:97-111) and the constants setTrialStrain and the
+// envelopes form on every call: Ec0 = 2 fc / epsc0, the unloading reference
+// point epsr = (fcu - rat Ec0 epscu) / (Ec0 (1 - rat)), sigmr = Ec0 epsr,
+// and the tension envelope's eps0 = ft / Ec0 and epsu = ft (1/Ets + 1/Ec0).
+// The device parameter table keeps the constants in slots 7-11 of every
+// Concrete02 row (k_c02_constants, the same expressions).
 struct C02 {
   double fc, epsc0, fcu, epscu, rat, ft, Ets;
+  double ec0, epsr, sigmr, eps0, epsu;
 };
 
-// Concrete02 constructor sign normalisation (Concrete02.cpp:97-111)
-__device__ __forceinline__ C02 c02_params(const double *q) {
+__device__ __forceinline__ C02 c02_base(const double *q) {
   C02 c;
   c.fc = q[0] > 0 ? -q[0] : q[0];
   c.epsc0 = q[1] > 0 ? -q[1] : q[1];
@@ -130,17 +137,27 @@ __device__ __forceinline__ C02 c02_params(const double *q) {
   return c;
 }
 
+__device__ __forceinline__ C02 c02_params(const double *q) {
+  C02 c = c02_base(q);
+  c.ec0 = q[7];
+  c.epsr = q[8];
+  c.sigmr = q[9];
+  c.eps0 = q[10];
+  c.epsu = q[11];
+  return c;
+}
+
 // Concrete02::Tens_Envlp / Compr_Envlp (Concrete02.cpp:421-497)
 __device__ __forceinline__ void c02_tens(const C02 &c, double epsc, double &sigc, double &Ect) {
-  const double Ec0 = 2.0 * c.fc / c.epsc0;
-  const double eps0 = c.ft / Ec0;
-  const double epsu = c.ft * (1.0 / c.Ets + 1.0 / Ec0);
+  const double Ec0 = c.ec0;
+  const double eps0 = c.eps0;
+  const double epsu = c.epsu;
   if (epsc <= eps0) { sigc = epsc * Ec0; Ect = Ec0; }
   else if (epsc <= epsu) { Ect = -c.Ets; sigc = c.ft - c.Ets * (epsc - eps0); }
   else { Ect = 1.0e-10; sigc = 0.0; }
 }
 __device__ __forceinline__ void c02_compr(const C02 &c, double epsc, double &sigc, double &Ect) {
-  const double Ec0 = 2.0 * c.fc / c.epsc0;
+  const double Ec0 = c.ec0;
   const double ratLocal = epsc / c.epsc0;
   if (epsc >= c.epsc0) {
     sigc = c.fc * ratLocal * (2.0 - ratLocal);
@@ -158,7 +175,7 @@ __device__ __forceinline__ void c02_compr(const C02 &c, double epsc, double &sig
 // keeps the record's previous trial stress and tangent.
 __device__ void concrete02_trial(const double *q, const double *hc, double eps, double *ht) {
   const C02 c = c02_params(q);
-  const double ec0 = c.fc * 2. / c.epsc0;
+  const double ec0 = c.ec0;
   double ecmin = hc[0], dept = hc[1];
   ht[0] = ecmin;
   ht[1] = dept;
@@ -171,8 +188,8 @@ __device__ void concrete02_trial(const double *q, const double *hc, double eps, 
     c02_compr(c, eps, sig, e);
     ecmin = eps;
   } else {
-    const double epsr = (c.fcu - c.rat * ec0 * c.epscu) / (ec0 * (1.0 - c.rat));
-    const double sigmr = ec0 * epsr;
+    const double epsr = c.epsr;
+    const double sigmr = c.sigmr;
     double sigmm, dumy;
     c02_compr(c, ecmin, sigmm, dumy);
     const double er = (sigmm - sigmr) / (ecmin - epsr);
@@ -931,7 +948,31 @@ __global__ void __launch_bounds__(32 * kFbcWarps) k_fbc_revert_sections(FrameVie
   if (lane == 0) st[6 + 36 + nip * 24 + 6] = 0.0;
 }
 
+// The per-material Concrete02 constants into slots 7-11 of the device
+// parameter table, with the expressions setTrialStrain and the envelopes
+// use (Concrete02.cpp:190-191, 421-446).
+__global__ void k_c02_constants(double *up, const int *ut, int n) {
+  const int u = blockIdx.x * blockDim.x + threadIdx.x;
+  if (u >= n || ut[u] != XG_UNI_CONCRETE02) return;
+  double *q = up + (long)u * XG_UNI_NPARAM;
+  const C02 c = c02_base(q);
+  const double ec0 = c.fc * 2. / c.epsc0;
+  const double epsr = (c.fcu - c.rat * ec0 * c.epscu) / (ec0 * (1.0 - c.rat));
+  const double Ec0 = 2.0 * c.fc / c.epsc0;
+  q[7] = ec0;
+  q[8] = epsr;
+  q[9] = ec0 * epsr;
+  q[10] = c.ft / Ec0;
+  q[11] = c.ft * (1.0 / c.Ets + 1.0 / Ec0);
+}
+
 }  // namespace
+
+int launch_c02_constants(double *uparam, const int *utype, int n, cudaStream_t s) {
+  if (n <= 0) return 0;
+  k_c02_constants<<<(n + 127) / 128, 128, 0, s>>>(uparam, utype, n);
+  return cudaGetLastError() == cudaSuccess ? 0 : XG_ECUDA;
+}
 
 int frame_state_stride(int nip) { return 6 + 36 + nip * 24 + 6 + 1; }
 

@@ -220,6 +220,9 @@ struct FrameView {
   int pdelta2d;               // PDeltaCrdTransf2d geometric terms
 };
 int frame_state_stride(int nip);
+// Concrete02 rows of the device parameter table: the per-material constants
+// into slots 7-11
+int launch_c02_constants(double *uparam, const int *utype, int n, cudaStream_t s);
 int launch_fbc_update(const FrameView &v, cudaStream_t s, int warps = 4);
 int launch_fbc_assemble(const FrameView &v, cudaStream_t s);
 int launch_fbc_commit(const FrameView &v, double *st_c, double *fh_c, long nrec, cudaStream_t s);

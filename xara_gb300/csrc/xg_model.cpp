@@ -935,12 +935,14 @@ int xg_model::upload_frames() {
   RET(d_GJ.upload(GJ.data(), GJ.size(), s));
   RET(d_fs0.upload(fs0.data(), fs0.size(), s));
   RET(d_utype.upload(utype.data(), utype.size(), s));
-  // device parameter table: Steel02 rows carry Fy/E0 in slot 11
+  // device parameter table: Steel02 rows carry Fy/E0 in slot 11, Concrete02
+  // rows their per-material constants in slots 7-11
   std::vector<double> up_dev(uparam);
   for (size_t u = 0; u < utype.size(); u++)
     if (utype[u] == XG_UNI_STEEL02)
       up_dev[u * XG_UNI_NPARAM + 11] = up_dev[u * XG_UNI_NPARAM] / up_dev[u * XG_UNI_NPARAM + 1];
   RET(d_uparam.upload(up_dev.data(), up_dev.size(), s));
+  RET(launch_c02_constants(d_uparam.p, d_utype.p, (int)utype.size(), s));
   RET(d_foff.upload(foff.data(), foff.size(), s));
   RET(d_work.alloc(2));
   CK(cudaMemsetAsync(d_work.p, 0, 2 * sizeof(unsigned long long), s));
