@@ -115,6 +115,36 @@ def test_frame_commands_give_the_builders_model():
     ops.wipe()
 
 
+def test_transient_commands_give_the_builders_phase():
+    """Masses, a Path series under UniformExcitation, rayleigh and Newmark:
+    the description and the transient phase equal the builder's."""
+    desc, phases = configs.steel_frame_2d_eq(2, 3, steps=40, dt=0.01, grav_steps=4,
+                                             with_gravity=True)
+    quake = phases[1]
+    roof, nx = _frame_script(grav_steps=4)
+    q = desc.uni_param.reshape(-1, 12)[0]                  # the builder's seeded fy and b
+    ops.uniaxialMaterial("Steel02", 1, *q[:6])
+    tags = list(desc.node_tag)
+    mass = desc.node_mass.reshape(-1, 3)
+    for t, m in zip(tags, mass):
+        if m.any():
+            ops.mass(t, *m)
+    ops.analysis("Transient")
+    ops.loadConst("-time", 0.0)
+    ops.timeSeries("Path", 7, "-dt", quake.gm_dt, "-values", *quake.gm_accel)
+    ops.pattern("UniformExcitation", 8, 1, "-accel", 7)
+    ops.rayleigh(desc.meta["alpha_m"], 0.0, desc.meta["beta_k0"], 0.0)
+    ops.integrator("Newmark", 0.5, 0.25)
+    ops.test("NormDispIncr", 1e-10, 50)
+    _same_desc(ops.build_desc(), desc, skip=("load_node", "load_pattern", "load_value"))
+    ph = ops._phase(40, 0.01)
+    for k in ("integrator", "num_steps", "dt", "gamma", "beta", "alpha_m", "beta_k_init",
+              "gm_dof", "gm_dt", "tol", "max_iter"):
+        assert ph[k] == getattr(quake, k), k
+    np.testing.assert_array_equal(ph["gm_accel"], quake.gm_accel)
+    ops.wipe()
+
+
 def test_unsupported_commands_are_named():
     ops.wipe()
     ops.model("basic", "-ndm", 2, "-ndf", 3)
