@@ -144,6 +144,19 @@ def test_tcl_language_pieces():
         it.eval("no_such_command 1 2")
 
 
+def test_one_line_bodies():
+    tcl.eval_script("""wipe
+model basic -ndm 2 -ndf 3
+uniaxialMaterial Elastic 1 2.0e11
+section Fiber 1 { fiber 0.1 0.0 0.01 1; fiber -0.1 0.0 0.01 1 }
+timeSeries Linear 1
+pattern Plain 1 1 { load 2 1.0 0.0 0.0 }
+""", fresh=True)
+    assert len(ops._S.sections[1]["fibers"]) == 2
+    assert ops._S.patterns[0]["loads"] == [(2, [1.0, 0.0, 0.0])]
+    ops.wipe()
+
+
 @pytest.mark.gpu
 def test_quad_script_runs_like_the_builders(need_gpu):
     from xara_gb300 import gpu

@@ -135,6 +135,12 @@ def _ternary(e):
     raise TclError(f"expr {e!r}: '?' without ':'")
 
 
+def _is_body(word):
+    """A script argument (several words, a newline, or empty), not a number
+    or a flag."""
+    return isinstance(word, str) and (not word.strip() or any(c.isspace() for c in word.strip()))
+
+
 _INT_LITERAL = re.compile(r"(?<![\w.])(\d+)(?![\w.])")
 
 _MATH = {n: getattr(math, n) for n in ("sqrt", "sin", "cos", "tan", "asin", "acos", "atan",
@@ -297,7 +303,7 @@ class Interp:
     # pattern Plain tag series {...}) or a list (timeSeries Path -values {...})
     def _cmd_section(self, kind, tag, *rest):
         rest = list(rest)
-        body = rest.pop() if rest and isinstance(rest[-1], str) and "\n" in rest[-1] else None
+        body = rest.pop() if rest and _is_body(rest[-1]) else None
         ops.section(_fmt(kind), _number(tag), *[_number(a) for a in rest])
         if body is not None:
             self.eval(body)
@@ -305,10 +311,7 @@ class Interp:
 
     def _cmd_pattern(self, kind, tag, *rest):
         rest = list(rest)
-        body = None
-        if rest and isinstance(rest[-1], str) and ("\n" in rest[-1] or " " in rest[-1].strip()
-                                                   or rest[-1].strip() == ""):
-            body = rest.pop()
+        body = rest.pop() if rest and _is_body(rest[-1]) else None
         if _fmt(kind) == "Plain" and rest and isinstance(_number(rest[0]), str):
             # an inline series: pattern Plain tag Linear {...}
             ts = -int(_number(tag))
