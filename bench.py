@@ -157,16 +157,35 @@ def dist_setup():
     import torch.distributed as dist
     if world > 1:
         dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
-        torch.cuda.set_device(0)
+        if torch.cuda.is_available():
+            torch.cuda.set_device(0)
     return world, rank, local, torch, dist
 
 
-def max_over_ranks(x, world, torch, dist):
+def _over_ranks(x, world, torch, dist, op):
     if world == 1:
         return x
-    t = torch.tensor([x], device="cuda")
-    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    # NCCL reduces device tensors only; gloo (the host-side runs) host ones
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([float(x)], dtype=torch.float64, device=dev)
+    dist.all_reduce(t, op=op)
     return float(t.item())
+
+
+def max_over_ranks(x, world, torch, dist):
+    """The slowest rank's time: the whole job ends when it does."""
+    return _over_ranks(x, world, torch, dist, dist.ReduceOp.MAX if world > 1 else None)
+
+
+def sum_over_ranks(x, world, torch, dist):
+    """Units processed by all ranks together."""
+    return _over_ranks(x, world, torch, dist, dist.ReduceOp.SUM if world > 1 else None)
+
+
+def job_rate(units, dt, world, torch, dist):
+    """Whole-job throughput: the units of every replica over the slowest
+    replica's time (each rank passes its own units and its own time)."""
+    return sum_over_ranks(units, world, torch, dist) / max_over_ranks(dt, world, torch, dist)
 
 
 # ---------------------------------------------------------------------------
@@ -286,8 +305,8 @@ def run_frame(args):
     points, sections, elems = gpu.profile_counters(m)
     prof = gpu.profile_read(m)
     gpu.profile_enable(m, False)
+    value = job_rate(points, dt, world, torch, dist)
     dt = max_over_ranks(dt, world, torch, dist)
-    value = points * world / dt
 
     # end to end through the C ABI with host buffers (the reference-facing
     # element-set + LinearSOE calls): trial displacements in, the resisting
@@ -316,8 +335,7 @@ def run_frame(args):
     dt_e2e = time.perf_counter() - t0
     points_e2e, _, _ = gpu.profile_counters(m)
     gpu.profile_enable(m, False)
-    dt_e2e = max_over_ranks(dt_e2e, world, torch, dist)
-    e2e_value = points_e2e * world / dt_e2e
+    e2e_value = job_rate(points_e2e, dt_e2e, world, torch, dist)
 
     # the full analysis through the device Newton driver: gravity, then
     # pushover steps (DisplacementControl), for Newton iterations/s
@@ -983,8 +1001,8 @@ def run_brick(args):
     dt = ev0.elapsed_time(ev1) * 1e-3
     prof = gpu.profile_read(m)
     gpu.profile_enable(m, False)
+    value = job_rate(npts * args.steps, dt, world, torch, dist)
     dt = max_over_ranks(dt, world, torch, dist)
-    value = npts * args.steps * world / dt
 
     # a whole Newton iteration: the element phase, then the block-Jacobi PCG
     # solve of the assembled tangent to rtol 1e-10 (the configuration's
@@ -1036,8 +1054,7 @@ def run_brick(args):
         gpu._check(L.xg_elemset_set_trial_disp(m.h, ph))
         gpu._check(L.xg_elemset_update(m.h, None, pr))
     barrier()
-    dt_e2e = max_over_ranks(time.perf_counter() - t0, world, torch, dist)
-    e2e_value = npts * args.steps * world / dt_e2e
+    e2e_value = job_rate(npts * args.steps, time.perf_counter() - t0, world, torch, dist)
     if rank != 0:
         dist.destroy_process_group()
         return 0
