@@ -27,6 +27,7 @@ import sys
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 OUT = os.path.join(HERE, "_ref")
+DEFAULT_SRC = "/root/reference/SRC"
 
 # Reference translation units (paths relative to SRC).
 SOURCES = """
@@ -193,7 +194,7 @@ def write_stubs(kinds, path):
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--src", default="/root/reference/SRC")
+    ap.add_argument("--src", default=DEFAULT_SRC)
     ap.add_argument("-j", type=int, default=os.cpu_count() or 4)
     ap.add_argument("--opt", default="-O2")
     a = ap.parse_args()

@@ -47,13 +47,17 @@ def _p(a):
 class RefRun:
     """Run a model through the reference's analysis loop and keep the record."""
 
-    def __init__(self, desc, phases, capture=(0, 0), cap_solves=0):
+    def __init__(self, desc, phases, capture=(0, 0), cap_solves=0, attach=None):
+        """attach(handle), when given, runs after the Domain is built and
+        before the first phase (e.g. to hand the harness a second LinearSOE)."""
         L = lib()
         self.desc = desc
         self._s = desc.struct()
         self.h = L.xref_create(C.byref(self._s))
         if not self.h:
             raise RuntimeError("xref_create failed")
+        if attach is not None:
+            attach(self.h)
         nu = desc.num_nodes * desc.ndf
         self.step_u, self.step_lambda, self.step_iters = [], [], []
         for ph in phases:

@@ -136,28 +136,41 @@ class CaptureSOE : public LinearSOE {
     LinearSOE::setLinks(m);
     gen_.setLinks(m);
     prof_.setLinks(m);
+    if (obs) obs->setLinks(m);
     return 0;
   }
   int setSize(Graph &g) override {
     int r = gen_.setSize(g);
     if (r < 0) return r;
+    if (obs && obs->setSize(g) < 0) return -1;
     return prof_.setSize(g);
   }
   int getNumEqn() const override { return prof_.getNumEqn(); }
   int addA(const Matrix &m, const ID &id, double f) override {
     gen_.addA(m, id, f);
+    if (obs && obs->addA(m, id, f) < 0) obs_errors++;
     return prof_.addA(m, id, f);
   }
   int addB(const Vector &v, const ID &id, double f) override {
     gen_.addB(v, id, f);
+    if (obs && obs->addB(v, id, f) < 0) obs_errors++;
     return prof_.addB(v, id, f);
   }
   int setB(const Vector &v, double f) override {
     gen_.setB(v, f);
+    if (obs && obs->setB(v, f) < 0) obs_errors++;
     return prof_.setB(v, f);
   }
-  void zeroA() override { gen_.zeroA(); prof_.zeroA(); }
-  void zeroB() override { gen_.zeroB(); prof_.zeroB(); }
+  void zeroA() override {
+    gen_.zeroA();
+    prof_.zeroA();
+    if (obs) obs->zeroA();
+  }
+  void zeroB() override {
+    gen_.zeroB();
+    prof_.zeroB();
+    if (obs) obs->zeroB();
+  }
   const Vector &getX() override { return prof_.getX(); }
   const Vector &getB() override { return prof_.getB(); }
   double normRHS() override { return prof_.normRHS(); }
@@ -169,6 +182,12 @@ class CaptureSOE : public LinearSOE {
 
   GenAccess &gen() { return gen_; }
   double solveSeconds = 0.0;
+  // A second LinearSOE fed the same calls (a system under test), and a
+  // callback run before every solve, while both hold the same A and B.
+  LinearSOE *obs = nullptr;
+  void (*on_solve)(void *) = nullptr;
+  void *on_solve_ctx = nullptr;
+  int obs_errors = 0;
 
  private:
   Harness *h_;
@@ -190,6 +209,9 @@ struct Harness {
   int totalSteps = 0;
   double elemSeconds = 0.0, stepSeconds = 0.0;
   std::vector<LoadPattern *> patterns;
+  LinearSOE *observer = nullptr;
+  void (*on_solve)(void *) = nullptr;
+  void *on_solve_ctx = nullptr;
 
   void snapshotU(double *out) {
     int ndf = d.ndf;
@@ -215,6 +237,7 @@ int CaptureSOE::solve() {
     c.U.resize(off + nu);
     h_->snapshotU(&c.U[off]);
   }
+  if (on_solve) on_solve(on_solve_ctx);
   auto t0 = clk::now();
   int r = prof_.solve();
   solveSeconds += std::chrono::duration<double>(clk::now() - t0).count();
@@ -454,6 +477,9 @@ int xref_run_phase(void *hp, const xg_phase_desc *ph, int cap_begin, int cap_end
       h->handler = new PlainHandler();
     h->numberer = new DOF_Numberer(*(new RCM(false)));
     h->soe = new CaptureSOE(h);
+    h->soe->obs = h->observer;
+    h->soe->on_solve = h->on_solve;
+    h->soe->on_solve_ctx = h->on_solve_ctx;
   }
   // wiring as BasicAnalysisBuilder::setLinks(STATIC_ANALYSIS)
   h->soe->setLinks(*h->model);
@@ -540,6 +566,23 @@ int xref_pattern(void *hp, int *colstart, int *rowidx) {
   memcpy(colstart, g.colStart(), sizeof(int) * (g.n() + 1));
   memcpy(rowidx, g.rows(), sizeof(int) * g.nz());
   return 0;
+}
+
+// Feed every LinearSOE call of the analysis also to `soe` (a LinearSOE*)
+// and run on_solve(ctx) before each solve.  Before the first phase only.
+int xref_set_observer(void *hp, void *soe, void (*on_solve)(void *), void *ctx) {
+  Harness *h = (Harness *)hp;
+  if (h->soe) return -1;
+  h->observer = (LinearSOE *)soe;
+  h->on_solve = on_solve;
+  h->on_solve_ctx = ctx;
+  return 0;
+}
+
+// Calls the observer answered with a negative status.
+int xref_observer_errors(void *hp) {
+  Harness *h = (Harness *)hp;
+  return h->soe ? h->soe->obs_errors : 0;
 }
 
 int xref_num_captured(void *hp) { return ((Harness *)hp)->cap.count; }

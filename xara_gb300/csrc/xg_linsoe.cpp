@@ -184,13 +184,18 @@ int xg_linsoe_zero_b(xg_linsoe *s) {
 int xg_linsoe_add_a(xg_linsoe *s, const double *m, const int *id, int ndof, double fact) {
   if (!s || ndof < 0 || (ndof && (!m || !id))) return lfail(XG_EINVAL, "bad addA argument");
   if (fact == 0.0) return 0;
-  for (int i = 0; i < ndof; i++) {
-    const int row = id[i];
-    if (row < 0) continue;
-    if (row >= s->n) return lfail(XG_EINVAL, "addA: equation number out of range");
-    for (int j = 0; j < ndof; j++) {
-      const int col = id[j];
-      if (col < 0) continue;
+  for (int i = 0; i < ndof; i++)
+    if (id[i] >= s->n) return lfail(XG_EINVAL, "addA: equation number out of range");
+  // Column-outer, row-inner, as SparseGenColLinSOE::addA
+  // (sparseGEN/SparseGenColLinSOE.cpp:262-310): an ID that names one
+  // equation twice (nodes tied by a constraint) then sums the entry's terms
+  // in the reference's order.
+  for (int j = 0; j < ndof; j++) {
+    const int col = id[j];
+    if (col < 0) continue;
+    for (int i = 0; i < ndof; i++) {
+      const int row = id[i];
+      if (row < 0) continue;
       const long k = s->slot(row, col);
       if (k < 0) return lfail(XG_EINVAL, "addA: entry outside the pattern");
       s->A[k] += fact * m[(size_t)i * ndof + j];
@@ -201,6 +206,7 @@ int xg_linsoe_add_a(xg_linsoe *s, const double *m, const int *id, int ndof, doub
 
 int xg_linsoe_add_b(xg_linsoe *s, const double *v, const int *id, int ndof, double fact) {
   if (!s || ndof < 0 || (ndof && (!v || !id))) return lfail(XG_EINVAL, "bad addB argument");
+  if (fact == 0.0) return 0;   // the quick return of SparseGenColLinSOE::addB
   for (int i = 0; i < ndof; i++) {
     if (id[i] < 0) continue;
     if (id[i] >= s->n) return lfail(XG_EINVAL, "addB: equation number out of range");
