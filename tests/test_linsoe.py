@@ -65,6 +65,37 @@ def test_assembly_matches_dense():
         assert not s.rhs().any()
 
 
+def test_repeated_equation_sums_in_reference_order():
+    """An ID that names one equation twice (two nodes tied by equalDOF under
+    the Transformation handler) gives that entry several terms in one addA.
+    SparseGenColLinSOE::addA (SparseGenColLinSOE.cpp:262-310) walks columns
+    outside, rows inside; the sum is bit-identical only in that order."""
+    rp = np.array([0, 2, 4], np.int32)
+    ci = np.array([0, 1, 0, 1], np.int32)
+    ids = np.array([0, 1, 0], np.int32)                # equation 0 twice
+    e = 2.0 ** -53
+    m = np.array([[1.0, 3.0, -1.0],
+                  [5.0, 7.0, 11.0],
+                  [e, 13.0, 0.0]])                     # (1 + e) - 1 = 0, (1 - 1) + e = e
+    expect = {}
+    for i in range(3):                                 # the reference's loop: column i
+        for j in range(3):                             # row j
+            key = (int(ids[j]), int(ids[i]))
+            expect[key] = expect.get(key, 0.0) + m[j, i]
+    with gpu.LinearSystem(rp, ci) as s:
+        s.add_a(m, ids)
+        got = s.values()
+    want = np.array([expect[(0, 0)], expect[(0, 1)], expect[(1, 0)], expect[(1, 1)]])
+    np.testing.assert_array_equal(got, want)
+    # the row-outer order would give another (0,0) entry: the case matters
+    row_outer = 0.0
+    for i in range(3):
+        for j in range(3):
+            if ids[i] == 0 and ids[j] == 0:
+                row_outer += m[i, j]
+    assert row_outer != want[0]
+
+
 def test_argument_checks():
     n, elems, K, rp, ci, blk = _problem()
     with pytest.raises(gpu.XaraGpuError, match="sorted"):
