@@ -364,7 +364,8 @@ int xg_linsoe_zero_b(xg_linsoe *s);                               /* zeroB */
 /* A(id[i], id[j]) += fact * m[i*ndof + j] (addA, m row-major ndof x ndof) */
 int xg_linsoe_add_a(xg_linsoe *s, const double *m, const int *id, int ndof, double fact);
 int xg_linsoe_add_b(xg_linsoe *s, const double *v, const int *id, int ndof, double fact);
-int xg_linsoe_set_b(xg_linsoe *s, const double *v, double fact);  /* B = fact * v */
+/* B = fact * v; fact == 0 leaves B unchanged (SparseGenColLinSOE::setB) */
+int xg_linsoe_set_b(xg_linsoe *s, const double *v, double fact);
 int xg_linsoe_get_a(const xg_linsoe *s, double *vals);            /* CSR values */
 int xg_linsoe_get_b(const xg_linsoe *s, double *b);
 /* PCG to ||r|| <= rtol ||b||; XG_ESOLVE on breakdown or maxit (X holds the

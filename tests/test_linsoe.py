@@ -61,6 +61,10 @@ def test_assembly_matches_dense():
         expect = 2.0 * b
         expect[[0, 5]] += 0.5
         np.testing.assert_array_equal(s.rhs(), expect)
+        s.set_b(np.ones(n), 0.0)             # the quick return: B unchanged
+        np.testing.assert_array_equal(s.rhs(), expect)
+        s.add_b(np.ones(3), [0, 1, 2], fact=0.0)
+        np.testing.assert_array_equal(s.rhs(), expect)
         s.zero_b()
         assert not s.rhs().any()
 

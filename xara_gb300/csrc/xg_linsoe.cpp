@@ -217,6 +217,7 @@ int xg_linsoe_add_b(xg_linsoe *s, const double *v, const int *id, int ndof, doub
 
 int xg_linsoe_set_b(xg_linsoe *s, const double *v, double fact) {
   if (!s || (s->n && !v)) return lfail(XG_EINVAL, "bad setB argument");
+  if (fact == 0.0) return 0;   // SparseGenColLinSOE::setB leaves B as it is
   for (int i = 0; i < s->n; i++) s->B[i] = fact * v[i];
   return 0;
 }
