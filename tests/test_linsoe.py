@@ -70,8 +70,9 @@ def test_assembly_matches_dense():
 
 
 def test_repeated_equation_sums_in_reference_order():
-    """An ID that names one equation twice (two nodes tied by equalDOF under
-    the Transformation handler) gives that entry several terms in one addA.
+    """An ID that names one equation twice (two nodes of an element tied to
+    one master by equalDOF: the PlainHandler's numbering copies the master's
+    equation numbers to them) gives that entry several terms in one addA.
     SparseGenColLinSOE::addA (SparseGenColLinSOE.cpp:262-310) walks columns
     outside, rows inside; the sum is bit-identical only in that order."""
     rp = np.array([0, 2, 4], np.int32)
