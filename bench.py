@@ -71,8 +71,8 @@ class ClockSampler:
          "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
          "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
 
-    def __init__(self, index=0):
-        self.index = index
+    def __init__(self):
+        self.id = gpu_smi_id()
         self.rows = []
         self.proc = None
         self.thread = None
@@ -80,7 +80,7 @@ class ClockSampler:
     def start(self):
         try:
             self.proc = subprocess.Popen(
-                ["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.Q}",
+                ["nvidia-smi", f"--id={self.id}", f"--query-gpu={self.Q}",
                  "--format=csv,noheader,nounits", "-lms", "100"],
                 stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
         except OSError:
@@ -117,6 +117,18 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(self.rows)}
 
 
+def gpu_smi_id():
+    """nvidia-smi's name for the GPU this process computes on: its UUID.
+    nvidia-smi numbers GPUs physically and ignores CUDA_VISIBLE_DEVICES, so
+    an index could name another process's GPU."""
+    try:
+        import torch
+        uuid = str(torch.cuda.get_device_properties(torch.cuda.current_device()).uuid)
+        return uuid if uuid.startswith("GPU-") else "GPU-" + uuid
+    except Exception:
+        return "0"
+
+
 def measured_peaks():
     p = os.path.join(ROOT, "MEASURED_PEAKS.json")
     if os.path.exists(p):
@@ -151,8 +163,18 @@ def dist_setup():
     rank = int(os.environ.get("RANK", "0"))
     local = int(os.environ.get("LOCAL_RANK", "0"))
     if world > 1:
-        # one replica per GPU: one model's Newton iteration does not shard
-        os.environ["CUDA_VISIBLE_DEVICES"] = str(local)
+        # one replica per GPU: one model's Newton iteration does not shard.
+        # The rank takes the local-rank-th GPU of the list it was given and
+        # never widens that list.
+        visible = os.environ.get("CUDA_VISIBLE_DEVICES")
+        if visible:
+            devices = [d for d in visible.split(",") if d.strip()]
+            if local >= len(devices):
+                raise RuntimeError(f"local rank {local} has no GPU in "
+                                   f"CUDA_VISIBLE_DEVICES={visible}")
+            os.environ["CUDA_VISIBLE_DEVICES"] = devices[local]
+        else:
+            os.environ["CUDA_VISIBLE_DEVICES"] = str(local)
     import torch
     import torch.distributed as dist
     if world > 1:
@@ -290,7 +312,7 @@ def run_frame(args):
     for k in range(args.warmup):
         iteration(k)
     gpu.profile_enable(m, True)
-    sampler = ClockSampler(local if world == 1 else 0)
+    sampler = ClockSampler()
     sampler.start()
     ev0 = torch.cuda.Event(enable_timing=True)
     ev1 = torch.cuda.Event(enable_timing=True)
@@ -557,7 +579,7 @@ def run_batch(args):
     # Newton loop with the device-side convergence check)
     gpu.set_graph(m, True)
     m.analyze(1)                                   # builds the graph, untimed
-    sampler = ClockSampler(local if world == 1 else 0)
+    sampler = ClockSampler()
     sampler.start()
     barrier()
     ev0.record(stream)
@@ -773,7 +795,7 @@ def run_adjoint(args):
     # the plain forward run (xg_analyze)
     m.reset()
     m.set_phase(ph)
-    sampler = ClockSampler(local if world == 1 else 0)
+    sampler = ClockSampler()
     sampler.start()
     gpu.profile_enable(m, True)
     stats, t_fwd = timed(lambda: m.analyze(N))
@@ -987,7 +1009,7 @@ def run_brick(args):
     for _ in range(args.warmup):
         m.update(False, False)
     gpu.profile_enable(m, True)
-    sampler = ClockSampler(local if world == 1 else 0)
+    sampler = ClockSampler()
     sampler.start()
     ev0 = torch.cuda.Event(enable_timing=True)
     ev1 = torch.cuda.Event(enable_timing=True)

@@ -147,13 +147,16 @@ class CudaBJPCGLinSOE : public LinearSOE {
 
  private:
   // Preconditioner blocks: the equations of one DOF group when they are
-  // contiguous and number 1 to 6 (DOF_Numberer gives a node's free dofs
-  // consecutive numbers); point Jacobi when any group breaks that rule.
+  // contiguous, number 1 to 6 and belong to no other group (DOF_Numberer
+  // gives a node's free dofs consecutive numbers).  The equations of a group
+  // that breaks the rule -- a node tied to another by equalDOF shares the
+  // retained node's equation -- and equations of no group are blocks of
+  // their own.
   void node_blocks() {
     blk_.clear();
     if (theModel == nullptr || n_ == 0) return;
-    std::vector<int> start(n_, -1);     // start[e] = first equation of e's block
-    std::vector<int> len(n_, 0);
+    std::vector<int> claims(n_, 0);
+    std::vector<std::pair<int, int>> runs;     // [lo, hi] of the contiguous groups
     DOF_GrpIter &groups = theModel->getDOFs();
     DOF_Group *g;
     while ((g = groups()) != nullptr) {
@@ -161,24 +164,23 @@ class CudaBJPCGLinSOE : public LinearSOE {
       int lo = -1, hi = -1, cnt = 0;
       for (int k = 0; k < eq.Size(); k++) {
         const int e = eq(k);
-        if (e < 0) continue;
-        if (e >= n_) return;
+        if (e < 0 || e >= n_) continue;
+        claims[e]++;
         lo = (lo < 0 || e < lo) ? e : lo;
         hi = e > hi ? e : hi;
         cnt++;
       }
-      if (cnt == 0) continue;
-      if (hi - lo + 1 != cnt || cnt > 6) return;
-      for (int e = lo; e <= hi; e++) {
-        if (start[e] >= 0) return;      // an equation in two groups
-        start[e] = lo;
-      }
-      len[lo] = cnt;
+      if (cnt > 0 && cnt <= 6 && hi - lo + 1 == cnt) runs.emplace_back(lo, hi);
+    }
+    std::vector<int> len(n_, 0);   // len[lo] > 0: a node block starts at lo
+    for (const auto &r : runs) {
+      bool own = true;
+      for (int e = r.first; e <= r.second; e++) own = own && claims[e] == 1;
+      if (own) len[r.first] = r.second - r.first + 1;
     }
     std::vector<int> blk{0};
     for (int e = 0; e < n_;) {
-      if (start[e] != e) return;        // an equation outside every group
-      e += len[e];
+      e += len[e] > 0 ? len[e] : 1;
       blk.push_back(e);
     }
     blk_.swap(blk);

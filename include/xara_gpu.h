@@ -351,8 +351,8 @@ int xg_profile_counters(xg_model *m, long long *point_updates, long long *sectio
         reference's own element loop (FE_Element::addAtoSOE feeding addA).
         The pattern is CSR with sorted columns (SparseGenColLinSOE::setSize
         order); addA / addB / setB follow SparseGenColLinSOE.cpp:214-350 (an
-        equation number < 0 is skipped; an entry outside the pattern is an
-        error) and accumulate on the host; solve runs block-Jacobi PCG on
+        equation number outside 0..n-1 and an entry outside the pattern are
+        skipped, as the reference skips them) and accumulate on the host; solve runs block-Jacobi PCG on
         the device (blocks of 1-6 equations, or point Jacobi when nblk is
         0) and copies X back.  Not reentrant per handle. ---- */
 typedef struct xg_linsoe xg_linsoe;
@@ -402,6 +402,13 @@ int xg_recorder_write(const xg_model *m, int id, const char *path, int precision
 /* FP64 FMA throughput of the current device in TFLOP/s (a short probe
    kernel with no memory traffic), the ceiling of the FP64 element kernels. */
 int xg_measure_fp64_peak(double *tflops);
+
+/* The reciprocal the LDL' kernels use on their pivot chains (a single-
+   precision seed refined by one cubically convergent step) and the
+   correctly rounded __drcp_rn, both evaluated on the device for the n host
+   values d: y[i] and y_rn[i].  For testing its error bound; no counterpart
+   in the reference (ProfileSPDLinDirectSolver divides). */
+int xg_chain_reciprocal_check(int n, const double *d, double *y, double *y_rn);
 
 /* ---- Adjoint of a transient run (no counterpart in the reference; its
         DDM sensitivity, `computeGradients` (runtime/commands/analysis/
@@ -459,7 +466,10 @@ int xg_uniaxial_vjp(int type, const double *q, const double *hc, double strain,
    than 36*nblk + 4*n + 3*(cooperative blocks) + 24 doubles of it (about
    260,000 equations with 3x3 node blocks, 100,000 with 1x1 blocks) is
    rejected with XG_EINVAL.  The first call on a device looks up the array's
-   device address; make that first call before any stream capture.  All
+   device address and keeps it for the life of the process; make that first
+   call before any stream capture.  cudaDeviceReset ends the context that
+   address belongs to: do not call this entry point on a device after
+   resetting it.  The call waits on its stream before it returns.  All
    calls share the one array: calls that overlap on the GPU race and must be
    serialised by the caller.  Allocates no device memory. ---- */
 #define XG_NOALLOC_MAX_DOUBLES 4194304

@@ -16,7 +16,8 @@ Our own harness (``ref_harness.cpp``) builds models through the reference's C++
 API (the pattern of ``tests/Other/UnitTests/Example1/main.cpp``) and exports a
 small ``extern "C"`` surface for ctypes.
 
-Usage: python oracle/build_ref.py [--src /root/reference/SRC] [-j N]
+Usage: python oracle/build_ref.py [--src SRC] [-j N]   (SRC defaults to
+$XARA_REFERENCE_SRC, else /root/reference/SRC)
 """
 import argparse
 import concurrent.futures as cf
@@ -28,6 +29,12 @@ import sys
 HERE = os.path.dirname(os.path.abspath(__file__))
 OUT = os.path.join(HERE, "_ref")
 DEFAULT_SRC = "/root/reference/SRC"
+
+
+def source_dir():
+    """The reference's SRC folder: $XARA_REFERENCE_SRC when set, else the
+    default location of the read-only reference checkout."""
+    return os.environ.get("XARA_REFERENCE_SRC") or DEFAULT_SRC
 
 # Reference translation units (paths relative to SRC).
 SOURCES = """
@@ -194,7 +201,7 @@ def write_stubs(kinds, path):
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--src", default=DEFAULT_SRC)
+    ap.add_argument("--src", default=source_dir())
     ap.add_argument("-j", type=int, default=os.cpu_count() or 4)
     ap.add_argument("--opt", default="-O2")
     a = ap.parse_args()

@@ -7,7 +7,9 @@ PlainHandler, RCM, DOF_Numberer, SparseGenColLinSOE, ProfileSPD,
 NewtonRaphson, DisplacementControl, ...) compiled from source.  The GPU machine
 has no reference; tests there read these fixtures.
 
-Usage: python tests/golden/make_golden.py
+Usage: python tests/golden/make_golden.py        (the small fixtures)
+       python tests/golden/make_golden.py c1     (frame3d_c1: the full-size 3D RC
+                                                  frame pushover, about half an hour)
 """
 import os
 import sys
@@ -117,9 +119,50 @@ def revert_fixture(name, builder, args, kw, seed=5, scale=2e-4):
          K1=K1, P1=P1, K2=K2, P2=P2)
 
 
+def c1_pushover(name="frame3d_c1", sample=50_000, seed=11, every=10):
+    """The 3D RC frame 10x10x20 at full size (6,820 forceBeamColumn elements,
+    120 / 64 fibers, P-Delta): gravity by LoadControl, loadConst, then the
+    DisplacementControl pushover of the roof corner to 2 % drift in 200
+    steps, through the reference's own classes.  Kept: the numbering and
+    pattern; the roof node's six displacements and the load factor after
+    every step; every free displacement after every ``every``-th step; and
+    every solve of the first pushover step (trial displacements, right-hand
+    sides, the row maxima of the tangent and the tangent values at
+    ``sample`` seeded CSC slots)."""
+    desc, phases = configs.rc_frame_3d()
+    grav = phases[0].num_steps
+    r = ref.RefRun(desc, phases, capture=(grav, grav + 1), cap_solves=64)
+    ndf = desc.ndf
+    roof = int(np.searchsorted(desc.node_tag, desc.meta["roof"]))
+    free = np.nonzero(r.eqn >= 0)[0].astype(np.int32)
+    snap = np.arange(every - 1, len(r.step_u), every, dtype=np.int32)
+    rng = np.random.default_rng(seed)
+    slots = np.sort(rng.choice(r.nnz, size=sample, replace=False)).astype(np.int32)
+    cs, ri = r.colstart, r.rowidx
+    cols = np.repeat(np.arange(r.neq), np.diff(cs))
+    rowmax = np.zeros((len(r.cap_A), r.neq))
+    for k, a in enumerate(r.cap_A):
+        # the pattern is symmetric: the largest |entry| of row i is that of column i
+        rowmax[k] = np.maximum.reduceat(np.abs(a), cs[:-1])
+    save(name, builder=np.array("rc_frame_3d"), args=np.asarray([], np.int64),
+         kw_keys=np.array([], dtype="<U1"), kw_vals=np.asarray([], np.float64),
+         eqn=r.eqn, colstart=cs, rowidx=ri,
+         step_lambda=r.step_lambda, step_iters=r.step_iters,
+         roof_u=r.step_u[:, roof * ndf:(roof + 1) * ndf],
+         free=free, snap_steps=snap, snap_u=r.step_u[snap][:, free],
+         cap_step=r.cap_step, cap_iter=r.cap_iter, cap_B=r.cap_B,
+         cap_U=r.cap_U[:, free], cap_lambda=r.cap_lambda,
+         slot=slots, slot_col=cols[slots].astype(np.int32), cap_A_slot=r.cap_A[:, slots],
+         cap_A_rowmax=rowmax,
+         ref_seconds=np.array([r.elem_seconds, r.solve_seconds, r.step_seconds]))
+
+
 def main():
     if not ref.available():
         sys.exit("oracle/_ref/libxara_ref.so missing: run python oracle/build_ref.py")
+    if sys.argv[1:] == ["c1"]:
+        c1_pushover()
+        return
     j2_paths()
     model_fixture("quad_8x4", configs.quad_block, (8, 4), {}, capture_steps=(0, 6))
     model_fixture("quad_64x16", configs.quad_block, (64, 16), {})

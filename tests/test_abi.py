@@ -80,3 +80,26 @@ def test_plan_disconnected_and_empty_rows():
     assert np.array_equal(o.numbering(), eqn)
     orp, oci = o.pattern()
     assert np.array_equal(orp, rp) and np.array_equal(oci, ci)
+
+
+@pytest.mark.gpu
+def test_chain_reciprocal_error_bound(need_gpu):
+    """The LDL' pivot chains' reciprocal (single-precision seed, one cubic
+    refinement step) against the correctly rounded __drcp_rn over a
+    log-uniform sweep of both signs: within one unit in the last place, and
+    equal to it outside 2^-100 .. 2^100 where it falls back to it."""
+    L = gpu.lib()
+    rng = np.random.default_rng(17)
+    mag = np.exp2(rng.uniform(-110.0, 110.0, size=200_000))
+    d = mag * np.where(rng.random(mag.size) < 0.5, -1.0, 1.0)
+    d = np.concatenate([d, [1.0, -1.0, 3.0, 0.1, 2.0 ** -100, 2.0 ** 100, np.nextafter(2.0, 0)]])
+    y, yrn = np.zeros_like(d), np.zeros_like(d)
+    vp = C.c_void_p
+    L.xg_chain_reciprocal_check.argtypes = [C.c_int, vp, vp, vp]
+    assert L.xg_chain_reciprocal_check(d.size, d.ctypes.data_as(vp), y.ctypes.data_as(vp),
+                                       yrn.ctypes.data_as(vp)) == 0
+    assert np.array_equal(yrn, 1.0 / d)                 # __drcp_rn is the IEEE quotient
+    ulps = np.abs(y - yrn) / np.spacing(np.abs(yrn))
+    assert ulps.max() <= 1.0, ulps.max()
+    outside = (np.abs(d) < 2.0 ** -100) | (np.abs(d) >= 2.0 ** 100)
+    assert outside.sum() > 1000 and np.array_equal(y[outside], yrn[outside])

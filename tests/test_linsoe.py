@@ -109,10 +109,26 @@ def test_argument_checks():
         gpu.LinearSystem(rp, bad)
     with pytest.raises(gpu.XaraGpuError, match="blocks"):
         gpu.LinearSystem(rp, ci, np.array([0, 7, n], np.int32))
+
+
+def test_terms_outside_the_system_are_skipped():
+    """SparseGenColLinSOE::addA / addB (SparseGenColLinSOE.cpp:263-350) skip
+    an equation number outside 0..n-1 and an entry missing from the pattern
+    and add every other term."""
+    n, elems, K, rp, ci, blk = _problem()
+    j = int(np.setdiff1d(np.arange(n), ci[rp[0]:rp[1]])[0])      # not coupled to 0
+    m = np.array([[1.0, 2.0, 3.0], [4.0, 5.0, 6.0], [7.0, 8.0, 9.0]])
     with gpu.LinearSystem(rp, ci) as s:
-        with pytest.raises(gpu.XaraGpuError, match="outside the pattern"):
-            j = int(np.setdiff1d(np.arange(n), ci[rp[0]:rp[1]])[0])   # not coupled to 0
-            s.add_a(np.ones((2, 2)), [0, j])
+        s.add_a(m, [0, j, n + 3])
+        s.add_b(np.array([1.0, 2.0, 3.0]), [0, j, n])
+        vals, b = s.values(), s.rhs()
+    want = np.zeros(len(ci))
+    want[rp[0] + np.searchsorted(ci[rp[0]:rp[1]], 0)] = 1.0
+    want[rp[j] + np.searchsorted(ci[rp[j]:rp[j + 1]], j)] = 5.0
+    assert np.array_equal(vals, want)
+    wb = np.zeros(n)
+    wb[0], wb[j] = 1.0, 2.0
+    assert np.array_equal(b, wb)
 
 
 @pytest.mark.gpu

@@ -24,7 +24,8 @@ def _free_port():
 
 def _rank_main(rank, world, port, out_dir):
     os.environ.update(MASTER_ADDR="127.0.0.1", MASTER_PORT=str(port), RANK=str(rank),
-                      LOCAL_RANK=str(rank), WORLD_SIZE=str(world))
+                      LOCAL_RANK=str(rank), WORLD_SIZE=str(world),
+                      CUDA_VISIBLE_DEVICES="4,6")    # the GPUs this job was given
     sys.path.insert(0, ROOT)
     import bench
     w, r, local, torch, dist = bench.dist_setup()
@@ -35,6 +36,7 @@ def _rank_main(rank, world, port, out_dir):
         "max": bench.max_over_ranks(rank + 1.5, w, torch, dist),
         "sum": bench.sum_over_ranks(rank + 1.5, w, torch, dist),
         "rate": bench.job_rate(units, dt, w, torch, dist),
+        "visible": os.environ["CUDA_VISIBLE_DEVICES"],
     }
     dist.barrier()
     dist.destroy_process_group()
@@ -54,6 +56,7 @@ def test_two_gloo_ranks(tmp_path):
         assert res["max"] == 2.5                  # every rank sees the slowest time
         assert res["sum"] == 4.0
         assert res["rate"] == 400.0 / 2.0         # all units over the slowest rank's time
+        assert res["visible"] == ["4", "6"][rank]  # its own GPU of the job's list
 
 
 def test_single_rank_needs_no_process_group(monkeypatch):

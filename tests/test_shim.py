@@ -84,9 +84,10 @@ def run_with_shim(D, desc, phases):
     return run, rp, ci, blk[:nblk.value + 1] if nblk.value else blk[:0], A, B, errors
 
 
-# (builder, node blocks expected): the continuum blocks tie their loaded
-# edge / face to a master node with equalDOF, so the tied equations belong to
-# several DOF groups and the shim falls back to point Jacobi there
+# (builder, every block a whole node's): the continuum blocks tie their
+# loaded edge / face to a master node with equalDOF, so the tied equations
+# belong to several DOF groups; those groups' equations get blocks of one
+# equation and every other node keeps its node block
 MODELS = {
     "quad J2, DisplacementControl": (lambda: configs.quad_block(8, 4, steps=4), False),
     "brick J2, DisplacementControl": (lambda: configs.brick_block(4, 3, 2, steps=3), False),
@@ -97,9 +98,22 @@ MODELS = {
 }
 
 
+def expected_blocks(eqn, n):
+    """Block starts the shim should give: a node's free equations form one
+    block when they are contiguous, at most six, and no other node shares
+    them; all other equations are blocks of one."""
+    claims = np.bincount(eqn[eqn >= 0], minlength=n)
+    starts = set(range(n))
+    for e in eqn:
+        f = np.sort(e[e >= 0])
+        if f.size and f.size <= 6 and f[-1] - f[0] + 1 == f.size and (claims[f] == 1).all():
+            starts -= set(int(x) for x in f[1:])
+    return np.array(sorted(starts) + [n], np.int32)
+
+
 @pytest.mark.parametrize("name", list(MODELS))
 def test_shim_assembles_what_the_reference_assembles(driver, name):
-    build, node_blocks = MODELS[name]
+    build, whole_nodes = MODELS[name]
     desc, phases = build()
     run, rp, ci, blk, A, B, errors = run_with_shim(driver, desc, phases)
     assert errors == 0
@@ -115,13 +129,16 @@ def test_shim_assembles_what_the_reference_assembles(driver, name):
         assert np.array_equal(ref_csr.indptr, rp) and np.array_equal(ref_csr.indices, ci)
         assert np.array_equal(A[k], ref_csr.data), (name, k)
         assert np.array_equal(B[k], run.cap_B[k]), (name, k)
-    # preconditioner blocks: one per node with free dofs, covering 0..n
-    if not node_blocks:
-        assert blk.size == 0
-        return
-    assert blk.size >= 2 and blk[0] == 0 and blk[-1] == n
+    # preconditioner blocks: node blocks, single equations where nodes share one
+    eqn = run.eqn.reshape(desc.num_nodes, desc.ndf)
+    assert np.array_equal(blk, expected_blocks(eqn, n))
     sizes = np.diff(blk)
     assert sizes.min() >= 1 and sizes.max() <= desc.ndf
-    eqn = run.eqn.reshape(desc.num_nodes, desc.ndf)
     free = [np.sort(e[e >= 0]) for e in eqn if (e >= 0).any()]
-    assert sorted(int(f[0]) for f in free) == list(blk[:-1])
+    if whole_nodes:
+        assert sorted(int(f[0]) for f in free) == list(blk[:-1])
+    else:
+        # only the tied edge / face and its master fall back to single equations
+        singles = int((sizes == 1).sum())
+        tied = int(np.sum(np.bincount(run.eqn[run.eqn >= 0]) > 1))
+        assert tied >= 1 and (sizes == desc.ndf).sum() >= len(free) // 2, (singles, tied)

@@ -6,10 +6,13 @@ ABI, ``include/xara_gpu.h``).  This package is the Python layer above it:
 * :mod:`xara_gb300._abi`   -- ctypes mirror of the C structs;
 * :mod:`xara_gb300.gpu`    -- the device model handle (element set, system,
   Newton driver);
-* :mod:`xara_gb300.model`  -- the reference's modelling commands
-  (``node``, ``fix``, ``equalDOF``, ``element``, ``nDMaterial``, ``pattern``,
-  ``integrator``, ``test``, ``algorithm``, ``system``, ``analysis``,
-  ``analyze``) building a model for the device;
+* :mod:`xara_gb300.openseespy` -- the reference's OpenSeesPy modelling and
+  analysis commands for the path's scope (``node``, ``fix``, ``equalDOF``,
+  ``element``, ``nDMaterial``, ``uniaxialMaterial``, ``section``,
+  ``pattern``, ``integrator``, ``test``, ``algorithm``, ``system``,
+  ``analyze``, ``nodeDisp``) building and running a device model;
+* :mod:`xara_gb300.adjoint` -- gradients of a frame response with respect
+  to material parameters as a ``torch.autograd.Function``;
 * :mod:`xara_gb300.configs` -- seeded synthetic workloads.
 
 There is no CPU fallback: loading the package on a machine without the

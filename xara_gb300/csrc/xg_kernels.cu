@@ -13,6 +13,7 @@
 #include <cstdint>
 
 #include "xg_internal.h"
+#include "xg_rcp.h"
 
 namespace xg {
 
@@ -834,4 +835,38 @@ extern "C" int xg_measure_fp64_peak(double *tflops) {
   const double flops = 2.0 * 64.0 * (double)iters * blocks * threads;
   *tflops = flops / (ms * 1e-3) / 1e12;
   return 0;
+}
+
+// ---------------------------------------------------------------------------
+// The LDL' kernels' pivot-chain reciprocal next to the correctly rounded one,
+// for its error bound test.
+// ---------------------------------------------------------------------------
+namespace xg {
+namespace {
+__global__ void k_reciprocal_pair(int n, const double *d, double *y, double *y_rn) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  y[i] = chain_reciprocal(d[i]);
+  y_rn[i] = __drcp_rn(d[i]);
+}
+}  // namespace
+}  // namespace xg
+
+extern "C" int xg_chain_reciprocal_check(int n, const double *d, double *y, double *y_rn) {
+  if (n < 0 || (n > 0 && (!d || !y || !y_rn))) return XG_EINVAL;
+  if (n == 0) return 0;
+  double *buf = nullptr;
+  const size_t bytes = sizeof(double) * (size_t)n;
+  if (cudaMalloc(&buf, 3 * bytes) != cudaSuccess) return XG_ENOMEM;
+  int rc = 0;
+  if (cudaMemcpy(buf, d, bytes, cudaMemcpyHostToDevice) != cudaSuccess) rc = XG_ECUDA;
+  if (!rc) {
+    xg::k_reciprocal_pair<<<(n + 255) / 256, 256>>>(n, buf, buf + n, buf + 2 * (size_t)n);
+    if (cudaGetLastError() != cudaSuccess ||
+        cudaMemcpy(y, buf + n, bytes, cudaMemcpyDeviceToHost) != cudaSuccess ||
+        cudaMemcpy(y_rn, buf + 2 * (size_t)n, bytes, cudaMemcpyDeviceToHost) != cudaSuccess)
+      rc = XG_ECUDA;
+  }
+  cudaFree(buf);
+  return rc;
 }

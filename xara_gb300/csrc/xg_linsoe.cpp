@@ -184,20 +184,19 @@ int xg_linsoe_zero_b(xg_linsoe *s) {
 int xg_linsoe_add_a(xg_linsoe *s, const double *m, const int *id, int ndof, double fact) {
   if (!s || ndof < 0 || (ndof && (!m || !id))) return lfail(XG_EINVAL, "bad addA argument");
   if (fact == 0.0) return 0;
-  for (int i = 0; i < ndof; i++)
-    if (id[i] >= s->n) return lfail(XG_EINVAL, "addA: equation number out of range");
   // Column-outer, row-inner, as SparseGenColLinSOE::addA
-  // (sparseGEN/SparseGenColLinSOE.cpp:262-310): an ID that names one
+  // (sparseGEN/SparseGenColLinSOE.cpp:263-313): an ID that names one
   // equation twice (nodes tied by a constraint) then sums the entry's terms
-  // in the reference's order.
+  // in the reference's order.  Equation numbers outside 0..n-1 and entries
+  // outside the pattern are skipped, as the reference skips them.
   for (int j = 0; j < ndof; j++) {
     const int col = id[j];
-    if (col < 0) continue;
+    if (col < 0 || col >= s->n) continue;
     for (int i = 0; i < ndof; i++) {
       const int row = id[i];
-      if (row < 0) continue;
+      if (row < 0 || row >= s->n) continue;
       const long k = s->slot(row, col);
-      if (k < 0) return lfail(XG_EINVAL, "addA: entry outside the pattern");
+      if (k < 0) continue;
       s->A[k] += fact * m[(size_t)i * ndof + j];
     }
   }
@@ -208,8 +207,8 @@ int xg_linsoe_add_b(xg_linsoe *s, const double *v, const int *id, int ndof, doub
   if (!s || ndof < 0 || (ndof && (!v || !id))) return lfail(XG_EINVAL, "bad addB argument");
   if (fact == 0.0) return 0;   // the quick return of SparseGenColLinSOE::addB
   for (int i = 0; i < ndof; i++) {
-    if (id[i] < 0) continue;
-    if (id[i] >= s->n) return lfail(XG_EINVAL, "addB: equation number out of range");
+    // SparseGenColLinSOE::addB (:317-350) skips numbers outside 0..n-1
+    if (id[i] < 0 || id[i] >= s->n) continue;
     s->B[id[i]] += fact * v[i];
   }
   return 0;

@@ -15,7 +15,9 @@
 // stand-in, never a device address, so its device address is looked up with
 // cudaGetSymbolAddress once per device, with that device current, on the
 // first call made on the device; make that first call before any stream
-// capture.  All calls share the array and find the previous call's contents
+// capture.  The address is kept for the life of the process, so the entry
+// point must not be called on a device after cudaDeviceReset (the reset ends
+// the context the address belongs to).  All calls share the array and find the previous call's contents
 // in it: the solver clears what must start at zero (the grid-barrier counter
 // and the status words) and overwrites the rest before reading it.  Calls
 // that overlap on the GPU (two streams, two host threads, two devices'
