@@ -3,16 +3,20 @@
 
 Workload `frame3d` (default): the 3D RC frame of 10 x 10 bays x 20 stories
 (6,820 forceBeamColumn elements, 5 Lobatto sections each, 120-fiber columns
-and 64-fiber beams with Concrete02 / Steel02, 14,520 equations), FP64.  A
-step is one Newton iteration of the hot path at a seeded lateral trial
-displacement field: state determination of every element (the force-based
+and 64-fiber beams with Concrete02 / Steel02, 14,520 equations), FP64, under
+its BASELINE analysis: gravity by LoadControl, loadConst, then the
+DisplacementControl pushover of a roof corner to 2 % drift in 200 steps.  A
+step is one pushover load step through the device Newton driver: per Newton
+iteration the state determination of every element (the force-based
 compatibility iteration over every fiber of every section), assembly of the
-tangent and the resisting force, and the `system ProfileSPD` solve (LDL'
-factorisation and substitution) of the tangent.  The trial fields grow
-monotonically from step to step, so the fibers load along a pushover path.
-Inputs (model, trial fields, load vector) are resident in HBM when the timed
-region starts; the factor tiles (89 MB) and the fiber records (275 MB) are
-rewritten every step.
+tangent and the resisting force, the `system ProfileSPD` LDL' factorisation
+and two right-hand sides (DisplacementControl), and the NormDispIncr test.
+Gravity and the first W pushover steps are untimed; the next K are timed.
+The rest of the pushover then runs to 2 % drift and its roof history is
+compared with the reference's own record (tests/golden/frame3d_c1.npz).
+`e2e` runs the same K steps with the reference's Newton loop on the host
+calling the reference-facing C ABI with host buffers.  The line also carries
+the brick, batch and adjoint workloads below as sub-blocks (`workloads`).
 
 Metric: IP updates/s -- fiber state determinations per second, every fiber
 counted once per inner compatibility iteration of its element; Newton
@@ -219,30 +223,26 @@ def frame_model():
     return desc, phases
 
 
-def lateral_field(desc, frac, drift=0.02):
-    """Seeded lateral displacement field: roof drift frac*drift in x with a
-    first-mode shape, a smaller y component and twist, the matching floor
-    rotations; base nodes stay fixed."""
-    rng = np.random.default_rng(3)
-    crd = desc.node_crd.reshape(-1, 3)
-    H = crd[:, 2].max()
-    z = crd[:, 2] / H
-    shape = np.sin(0.5 * np.pi * z)
-    dshape = 0.5 * np.pi * np.cos(0.5 * np.pi * z) / H
-    u = np.zeros((len(crd), 6))
-    a = frac * drift * H
-    u[:, 0] = a * shape
-    u[:, 1] = 0.25 * a * shape
-    u[:, 4] = a * dshape                      # rotation about y follows dux/dz
-    u[:, 3] = -0.25 * a * dshape              # rotation about x follows -duy/dz
-    u[:, 5] = 1e-4 * frac * z
-    u[:, :3] += rng.normal(0.0, 1e-6, size=(len(crd), 3)) * (z[:, None] > 0)
-    u[z == 0] = 0.0
-    return u.ravel()
+C1_FIXTURE = os.path.join(ROOT, "tests", "golden", "frame3d_c1.npz")
+C1_PARITY_TESTS = ["tests/test_full_size.py::test_c1_first_pushover_step_entrywise",
+                   "tests/test_full_size.py::test_c1_pushover_history"]
 
 
-def frame_fields(desc, n):
-    return [lateral_field(desc, (k + 1) / n) for k in range(n)]
+def c1_reference():
+    """The reference's own C1 pushover record (roof history every step,
+    snapshots of every free displacement every 10 steps), made by
+    tests/golden/make_golden.py from the reference's classes."""
+    if not os.path.exists(C1_FIXTURE):
+        return None
+    z = np.load(C1_FIXTURE)
+    return {k: z[k] for k in ("roof_u", "step_lambda", "step_iters", "snap_steps", "snap_u",
+                              "free")}
+
+
+def relerr(a, b):
+    a, b = np.ravel(a), np.ravel(b)
+    d = np.linalg.norm(b)
+    return float(np.linalg.norm(a - b) / (d if d > 0 else 1.0))
 
 
 def profile_stats(rowptr, colidx):
@@ -274,43 +274,131 @@ def frame_alg_bytes(desc, nnz, neq):
             "gather_tangent": nnz * 8.0, "gather_resid": neq * 8.0}
 
 
+def pattern_loads(desc, eqn, neq, pattern):
+    """Reference load vector of one load pattern, per equation."""
+    f = np.zeros(neq)
+    tags = np.asarray(desc.node_tag)
+    vals = np.asarray(desc.load_value).reshape(-1, desc.ndf)
+    for i, n in enumerate(desc.load_node):
+        if desc.load_pattern[i] != pattern:
+            continue
+        idx = int(np.searchsorted(tags, n))
+        for j in range(desc.ndf):
+            r = eqn[idx * desc.ndf + j]
+            if r >= 0:
+                f[r] += vals[i, j]
+    return f
+
+
+class HostDisplacementControl:
+    """The reference's own analysis loop driving the library through its
+    reference-facing C ABI, as the element-set and LinearSOE shims do:
+    NewtonRaphson::solveCurrentStep (NewtonRaphson.cpp:125-222) with
+    DisplacementControl::newStep / update (DisplacementControl.cpp:121-281)
+    and CTestNormDispIncr on the host, every element update
+    (xg_elemset_set_trial_disp + xg_elemset_update) and every solve
+    (xg_soe_solve, the device LDL') through host buffers in pinned memory."""
+
+    def __init__(self, m, desc, phase, const_factor, torch):
+        from xara_gb300 import gpu
+        self.gpu, self.L, self.m = gpu, gpu.lib(), m
+        eqn = m.numbering()
+        self.map = np.nonzero(eqn >= 0)[0]
+        self.eq = eqn[self.map]
+        nd = int(np.searchsorted(np.asarray(desc.node_tag), phase.dc_node))
+        self.ceq = int(eqn[nd * desc.ndf + phase.dc_dof])
+        self.incr, self.tol, self.maxit = phase.dc_incr, phase.tol, phase.max_iter
+        # gravity, held at its last factor by loadConst
+        self.fconst = const_factor * pattern_loads(desc, eqn, m.neq, 0)
+        self.phat = pattern_loads(desc, eqn, m.neq, phase.pattern)
+        pin = lambda n: torch.zeros(n, dtype=torch.float64).pin_memory()  # noqa: E731
+        self.Uh, self.Rh = pin(m.nu), pin(m.neq)
+        self.bh, self.xh = pin(m.neq), pin(m.neq)
+        self.U, self.R = self.Uh.numpy(), self.Rh.numpy()
+        self.b, self.x = self.bh.numpy(), self.xh.numpy()
+        u, lam = m.disp()
+        self.U[:] = u
+        self.lam = lam
+        self.h2d = self.d2h = 0
+        self.ptr = lambda t: C.c_void_p(t.data_ptr())  # noqa: E731
+
+    def _update(self):
+        g, L, m = self.gpu, self.L, self.m
+        g._check(L.xg_elemset_set_trial_disp(m.h, self.ptr(self.Uh)))
+        r = L.xg_elemset_update(m.h, None, self.ptr(self.Rh))
+        if r < 0:
+            raise RuntimeError(f"element state determination failed ({r})")
+        self.h2d += self.U.nbytes
+        self.d2h += self.R.nbytes
+
+    def _solve(self, rhs):
+        g, L, m = self.gpu, self.L, self.m
+        self.b[:] = rhs
+        it_, rr_ = C.c_int(), C.c_double()
+        g._check(L.xg_soe_solve(m.h, self.ptr(self.bh), self.ptr(self.xh), 1e-12, 20000,
+                                C.byref(it_), C.byref(rr_)))
+        self.h2d += self.b.nbytes
+        self.d2h += self.x.nbytes
+        return self.x.copy()
+
+    def _incr(self, dU):
+        np.add.at(self.U, self.map, dU[self.eq])
+
+    def step(self):
+        """One load step; returns the Newton iterations."""
+        dUhat = self._solve(self.phat)                   # newStep: tangent of the last update
+        dlam = self.incr / dUhat[self.ceq]
+        self.lam += dlam
+        self._incr(dlam * dUhat)
+        self._update()
+        it = 0
+        while True:
+            dUbar = self._solve(self.fconst + self.lam * self.phat - self.R)
+            dUhat = self._solve(self.phat)
+            dl = -dUbar[self.ceq] / dUhat[self.ceq]
+            dU = dUbar + dl * dUhat
+            self.lam += dl
+            self._incr(dU)
+            self._update()
+            it += 1
+            if np.linalg.norm(dU) <= self.tol:
+                break
+            if it >= self.maxit:
+                raise RuntimeError("host DisplacementControl step did not converge")
+        self.gpu._check(self.L.xg_elemset_commit(self.m.h))
+        return it
+
+
 def run_frame(args):
     world, rank, local, torch, dist = dist_setup()
     from xara_gb300 import gpu
-    L = gpu.lib()
-    L.xg_elemset_set_trial_disp_device.argtypes = [C.c_void_p, C.c_void_p]
-    L.xg_soe_solve_device.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_double, C.c_int,
-                                      C.c_void_p, C.c_void_p]
     desc, phases = frame_model()
+    grav, push = phases
+    W, K = args.warmup, args.steps
     t_setup = time.perf_counter()
     m = gpu.DeviceModel(desc)
     m.set_system(gpu.XG_SYSTEM_PROFILE_SPD)
     t_setup = time.perf_counter() - t_setup
     rowptr, colidx = m.pattern()
     envelope, ldl_fma = profile_stats(rowptr, colidx)
-    nsteps = args.warmup + args.steps
-    fields = frame_fields(desc, nsteps)
-    dev = torch.device("cuda")
-    U = torch.from_numpy(np.stack(fields)).to(dev)
-    b = torch.from_numpy(np.random.default_rng(5).normal(size=m.neq)).to(dev)
-    x = torch.empty(m.neq, dtype=torch.float64, device=dev)
     stream = torch.cuda.ExternalStream(gpu.model_stream(m))
-    torch.cuda.synchronize()
     fp64_peak = fp64_peak_probe()
-
-    def iteration(k):
-        gpu._check(L.xg_elemset_set_trial_disp_device(m.h, C.c_void_p(U[k].data_ptr())))
-        gpu._check(L.xg_elemset_update(m.h, None, None))
-        gpu._check(L.xg_soe_solve_device(m.h, C.c_void_p(b.data_ptr()),
-                                         C.c_void_p(x.data_ptr()), 1e-12, 20000, None, None))
+    rid = m.add_recorder([desc.meta["roof"]], dofs=list(range(6)))
 
     def barrier():
         if world > 1:
             dist.barrier()
         torch.cuda.synchronize()
 
-    for k in range(args.warmup):
-        iteration(k)
+    # gravity (LoadControl, loadConst), then W pushover steps: untimed
+    m.set_phase(grav)
+    it_lead = sum(s[0] for s in m.analyze(grav.num_steps))
+    grav_factor = m.disp()[1]          # the gravity pattern's factor from now on
+    m.set_phase(push)
+    it_lead += sum(s[0] for s in m.analyze(W))
+    # the timed steps: K DisplacementControl steps of the pushover through the
+    # device Newton driver (element state, assembly, LDL' factor, two
+    # right-hand sides per iteration, the norm test), inputs resident
     gpu.profile_enable(m, True)
     sampler = ClockSampler()
     sampler.start()
@@ -318,8 +406,7 @@ def run_frame(args):
     ev1 = torch.cuda.Event(enable_timing=True)
     barrier()
     ev0.record(stream)
-    for k in range(args.warmup, nsteps):
-        iteration(k)
+    stats = m.analyze(K)
     ev1.record(stream)
     barrier()
     clocks = sampler.stop()
@@ -327,151 +414,182 @@ def run_frame(args):
     points, sections, elems = gpu.profile_counters(m)
     prof = gpu.profile_read(m)
     gpu.profile_enable(m, False)
+    newton = sum(s[0] for s in stats)
     value = job_rate(points, dt, world, torch, dist)
+    newton_rate = job_rate(newton, dt, world, torch, dist)
     dt = max_over_ranks(dt, world, torch, dist)
+    u_dev, lam_dev = m.disp()
 
-    # end to end through the C ABI with host buffers (the reference-facing
-    # element-set + LinearSOE calls): trial displacements in, the resisting
-    # force out, the load vector in and the solution out, every step
-    m.revert()
-    Uh = [torch.from_numpy(f).pin_memory() for f in fields]
-    bh = torch.from_numpy(b.cpu().numpy()).pin_memory()
-    rh = torch.empty(m.neq, dtype=torch.float64).pin_memory()
-    xh = torch.empty(m.neq, dtype=torch.float64).pin_memory()
-    ptr = lambda t: C.c_void_p(t.data_ptr())  # noqa: E731
-    it_, rr_ = C.c_int(), C.c_double()
-    for k in range(args.warmup):
-        gpu._check(L.xg_elemset_set_trial_disp(m.h, ptr(Uh[k])))
-        gpu._check(L.xg_elemset_update(m.h, None, ptr(rh)))
-        gpu._check(L.xg_soe_solve(m.h, ptr(bh), ptr(xh), 1e-12, 20000, C.byref(it_),
-                                  C.byref(rr_)))
+    # the rest of the pushover to 2 % roof drift, in chunks of ten steps
+    # (the snapshots' spacing), against the reference's record
+    ref = c1_reference()
+    full = None
+    if not args.no_analysis:
+        done = grav.num_steps + W + K
+        total = grav.num_steps + push.num_steps
+        snaps = {}
+        t0 = time.perf_counter()
+        it_rest = 0
+        while done < total:
+            n = min(10 - done % 10 if done % 10 else 10, total - done)
+            it_rest += sum(s[0] for s in m.analyze(n))
+            done += n
+            if done % 10 == 0:
+                snaps[done - 1] = m.disp()[0]
+        t_rest = time.perf_counter() - t0
+        hist = m.recorder(rid)
+        full = {"steps": push.num_steps, "drift": 0.02,
+                "rest_seconds": t_rest, "rest_newton_iterations": it_rest,
+                "note": f"pushover steps {W + K + 1}..{push.num_steps} after the timed ones, "
+                        "host clock, displacements read every 10 steps"}
+        if ref is not None:
+            nrec = hist.shape[0]
+            full.update({
+                "roof_relerr": relerr(hist[:, -6:], ref["roof_u"][:nrec]),
+                "lambda_relerr": relerr(np.asarray([lam_dev]),
+                                        ref["step_lambda"][grav.num_steps + W + K - 1]),
+                "snapshot_relerr": max(relerr(snaps[s][ref["free"]],
+                                              ref["snap_u"][i])
+                                       for i, s in enumerate(ref["snap_steps"]) if s in snaps),
+                "snapshots": len(snaps), "recorded_steps": int(nrec),
+                "reference_newton_iterations": int(ref["step_iters"].sum()),
+                "device_newton_iterations": int(it_lead + newton + it_rest),
+            })
+
+    # end to end: the same timed window again through the reference-facing C
+    # ABI (the reference's own Newton loop on the host, host buffers)
+    m.reset()
+    m.set_phase(grav)
+    m.analyze(grav.num_steps)
+    m.set_phase(push)
+    m.analyze(W)
+    host = HostDisplacementControl(m, desc, push, grav_factor, torch)
     gpu.profile_enable(m, True)
     barrier()
     t0 = time.perf_counter()
-    for k in range(args.warmup, nsteps):
-        gpu._check(L.xg_elemset_set_trial_disp(m.h, ptr(Uh[k])))
-        gpu._check(L.xg_elemset_update(m.h, None, ptr(rh)))
-        gpu._check(L.xg_soe_solve(m.h, ptr(bh), ptr(xh), 1e-12, 20000, C.byref(it_),
-                                  C.byref(rr_)))
+    it_e2e = sum(host.step() for _ in range(K))
     barrier()
     dt_e2e = time.perf_counter() - t0
     points_e2e, _, _ = gpu.profile_counters(m)
     gpu.profile_enable(m, False)
     e2e_value = job_rate(points_e2e, dt_e2e, world, torch, dist)
-
-    # the full analysis through the device Newton driver: gravity, then
-    # pushover steps (DisplacementControl), for Newton iterations/s
-    analysis = None
-    if not args.no_analysis:
-        m.reset()
-        m.set_phase(phases[0])
-        m.analyze(phases[0].num_steps)
-        m.set_phase(phases[1])
-        m.analyze(2)
-        torch.cuda.synchronize()
-        t0 = time.perf_counter()
-        st = m.analyze(args.analysis_steps)
-        dta = time.perf_counter() - t0
-        newton = sum(s[0] for s in st)
-        analysis = {"pushover_steps": args.analysis_steps, "newton_iterations": newton,
-                    "pushover_steps_per_s": args.analysis_steps / dta,
-                    "newton_iters_per_s": newton / dta,
-                    "note": "DisplacementControl pushover steps after gravity and loadConst, "
-                            "device Newton driver, host clock"}
+    e2e_vs_device = relerr(host.U, u_dev)
 
     if rank != 0:
         dist.destroy_process_group()
-        return 0
+        return None
 
     kernels = {k: v for k, v in prof.items() if v[1] > 0 and k != "return_map_cap_hits"}
     gpu_launches = sum(v[1] for v in kernels.values())
     dominant = max(kernels, key=lambda k: kernels[k][0])
-    groups = {"ldl_factor": 1, "gather_tangent": 1, "gather_resid": 1}
-    dom_ms, dom_launches = kernels[dominant]
-    per_group_s = dom_ms * 1e-3 / max(dom_launches // (2 if dominant in groups else 1), 1)
+    peak, peak_kind = measured_peaks()
     alg = frame_alg_bytes(desc, m.nnz, m.neq)
     alg["ldl_factor"] = envelope * 16.0        # envelope read, factor written
     alg["ldl_solve"] = envelope * 16.0         # forward and backward sweeps
-    peak, peak_kind = measured_peaks()
-    achieved = alg[dominant] / per_group_s / 1e9
-    step_s = dt / args.steps
-    ldl_ms = kernels.get("ldl_factor", (0, 1))
-    ldl_s = ldl_ms[0] * 1e-3 / max(ldl_ms[1] // 2, 1)
+    ldl_ms, ldl_n = kernels.get("ldl_factor", (0.0, 0))
+    factorisations = max(ldl_n // 2, 1)        # two timed kernel groups per factorisation
+    ldl_s = ldl_ms * 1e-3 / factorisations
+    ldl_flops = 2.0 * ldl_fma
+    if dominant == "ldl_factor":
+        tf = ldl_flops / ldl_s / 1e12
+        gbs = alg["ldl_factor"] / ldl_s / 1e9
+        roof_line = {"bound": "fp64", "kernel": dominant, "achieved": tf,
+                     "peak": fp64_peak, "unit": "TFLOP/s",
+                     "frac": tf / fp64_peak if fp64_peak else None,
+                     "peak_source": "of the FP64 probe (xg_measure_fp64_peak, this run): "
+                                    "MEASURED_PEAKS.json holds no FP64 figure",
+                     "flops_per_launch": ldl_flops,
+                     "traffic": ncu_traffic("frame3d", dominant),
+                     "hbm": {"achieved": gbs, "peak": peak, "unit": "GB/s",
+                             "frac": gbs / peak if peak else None, "peak_source": peak_kind,
+                             "algorithmic_bytes_per_launch": alg["ldl_factor"]}}
+    else:
+        dom_ms, dom_n = kernels[dominant]
+        per = dom_ms * 1e-3 / max(dom_n, 1)
+        gbs = alg.get(dominant, 0.0) / per / 1e9
+        roof_line = {"bound": "hbm", "kernel": dominant, "achieved": gbs, "peak": peak,
+                     "unit": "GB/s", "frac": gbs / peak if peak else None,
+                     "peak_source": peak_kind, "traffic": ncu_traffic("frame3d", dominant),
+                     "algorithmic_bytes_per_launch": alg.get(dominant)}
+    window = f"pushover steps {W + 1}..{W + K} of 200 (after gravity and loadConst)"
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
-        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * step_s,
+        "steps": K, "warmup": W, "ms_per_step": 1e3 * dt / K,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-        "dtype": "f64", "data": "synthetic (seeded model and lateral trial fields)",
-        "config": {"workload": "3D RC frame 10x10x20 (6,820 force-based elements): one Newton "
-                               "iteration per step -- forceBeamColumn state determination, "
-                               "assembly, ProfileSPD LDL' solve",
-                   "elements": desc.num_elems, "equations": m.neq, "nnz": m.nnz,
-                   "fiber_points": desc.meta["fiber_points"], "envelope": envelope,
-                   "system": "ProfileSPD (device LDL')", "parallelism": f"replicas x{world}",
+        "dtype": "f64", "data": "synthetic (seeded RC frame model; the BASELINE pushover)",
+        "config": {"workload": "3D RC frame 10x10x20 (6,820 force-based elements), "
+                               "DisplacementControl pushover: one load step per step -- "
+                               "forceBeamColumn state determination, assembly, ProfileSPD "
+                               "LDL' factor, two right-hand sides per Newton iteration, "
+                               "NormDispIncr 1e-10",
+                   "timed_window": window, "elements": desc.num_elems, "equations": m.neq,
+                   "nnz": m.nnz, "fiber_points": desc.meta["fiber_points"],
+                   "envelope": envelope, "system": "ProfileSPD (device LDL')",
+                   "parallelism": f"replicas x{world}",
                    "l2": "per-step working set (factor tiles 89 MB rewritten, fiber records "
                          "275 MB) exceeds L2; no flush"},
-        "newton_iters_per_s": args.steps * world / dt,
-        "point_updates_per_step": points / args.steps,
-        "section_updates_per_step": sections / args.steps,
+        "newton_iters_per_s": newton_rate,
+        "newton_iters_per_step": newton / K,
+        "point_updates_per_step": points / K,
+        "section_updates_per_step": sections / K,
         "e2e": {"value": e2e_value, "unit": UNIT,
-                "h2d_bytes_per_step": int(Uh[0].numel() * 8 + bh.numel() * 8),
-                "d2h_bytes_per_step": int(rh.numel() * 8 + xh.numel() * 8),
-                "path": "xg_elemset_set_trial_disp + xg_elemset_update + xg_soe_solve, "
-                        "pinned host buffers"},
+                "h2d_bytes_per_step": int(host.h2d / K), "d2h_bytes_per_step": int(host.d2h / K),
+                "newton_iterations": it_e2e, "relerr_vs_device_driver": e2e_vs_device,
+                "path": "the reference's NewtonRaphson + DisplacementControl on the host over "
+                        "xg_elemset_set_trial_disp + xg_elemset_update + xg_soe_solve (two "
+                        "right-hand sides per iteration) + xg_elemset_commit, pinned host "
+                        "buffers"},
         "gpu_launches": int(gpu_launches),
-        "roofline": {"bound": "hbm", "kernel": dominant, "achieved": achieved, "peak": peak,
-                     "unit": "GB/s", "frac": achieved / peak if peak else None,
-                     "peak_source": peak_kind, "traffic": ncu_traffic("frame3d", dominant),
-                     "algorithmic_bytes_per_launch": alg[dominant]},
-        "fp64": {"ldl_factor_flops": 2.0 * ldl_fma, "ldl_factor_ms": 1e3 * ldl_s,
-                 "achieved_tflops": 2.0 * ldl_fma / ldl_s / 1e12 if ldl_s > 0 else None,
-                 "peak_tflops_probe": fp64_peak,
-                 "frac": (2.0 * ldl_fma / ldl_s / 1e12) / fp64_peak if fp64_peak and ldl_s else None,
-                 "note": "the LDL' is FP64-bound: its roofline is the FP64 rate, not HBM"},
-        "kernels_ms_per_step": {k: v[0] / args.steps for k, v in kernels.items()},
-        "analysis": analysis,
+        "roofline": roof_line,
+        "ldl": {"factorisations_per_step": factorisations / K, "ms_per_factorisation": 1e3 * ldl_s,
+                "flops_per_factorisation": ldl_flops},
+        "kernels_ms_per_step": {k: v[0] / K for k, v in kernels.items()},
+        "parity": {"tests": C1_PARITY_TESTS, "fixture": "tests/golden/frame3d_c1.npz",
+                   "full_pushover": full},
         "clocks": clocks,
         "setup_s": t_setup,
     }
     if not args.no_cpu_baseline:
-        rate, its, sample = frame_cpu_sample(seconds=args.cpu_seconds)
+        rate, its, sample = frame_cpu_sample(W, seconds=args.cpu_seconds)
         line["cpu_baseline"] = {"value": rate, "unit": UNIT, "cores": 1, "kind": "port",
                                 "sample": sample, "newton_iters_per_s": its}
-    print(json.dumps(line))
-    if world > 1:
-        dist.destroy_process_group()
-    return 0
+    m.close()
+    return line
 
 
 class FrameCpu:
-    """The oracle's path (element state, assembly, ProfileSPD) on one model."""
+    """The oracle's path (element state, assembly, ProfileSPD) on one model,
+    brought through gravity and the first pushover steps."""
 
-    def __init__(self, nsteps):
+    def __init__(self, lead):
         from oracle import port
-        self.desc, _ = frame_model()
+        from xara_gb300._abi import PhaseDesc
+        self.desc, (grav, push) = frame_model()
         self.o = port.OracleModel(self.desc)
-        self.fields = frame_fields(self.desc, nsteps)
-        self.b = np.random.default_rng(5).normal(size=self.o.neq)
+        self.o.run([grav, PhaseDesc(**{**push.kw, "num_steps": lead})])
+        self.push = push
+        self.PhaseDesc = PhaseDesc
 
-    def iteration(self, k):
+    def steps(self, n):
+        """n pushover steps; returns (point updates, Newton iterations)."""
         p0, _ = self.o.work()
-        self.o.elem_state(self.fields[k])
-        self.o.soe_solve(self.b)
-        return self.o.work()[0] - p0
+        _, _, its = self.o.run([self.PhaseDesc(**{**self.push.kw, "num_steps": n})])
+        return self.o.work()[0] - p0, int(its.sum())
 
 
-def frame_cpu_sample(seconds=12.0, nsteps=23):
+def frame_cpu_sample(lead, seconds=12.0):
     t0 = time.perf_counter()
-    cpu = FrameCpu(nsteps)
-    pts, n, t1 = 0, 0, time.perf_counter()
-    while n < nsteps and (n < 2 or time.perf_counter() - t1 < seconds):
-        pts += cpu.iteration(n)
-        n += 1
+    cpu = FrameCpu(lead)
+    pts, its, n, t1 = 0, 0, 0, time.perf_counter()
+    while n < 1 or time.perf_counter() - t1 < seconds:
+        p, i = cpu.steps(1)
+        pts, its, n = pts + p, its + i, n + 1
     dt = time.perf_counter() - t1
-    sample = (f"3D RC frame 10x10x20 at full size, {n} Newton iterations (element state, "
-              f"assembly, ProfileSPD factor + solve) along the seeded lateral fields, "
-              f"1 thread; model set-up {t1 - t0:.1f} s untimed")
-    return pts / dt, n / dt, sample
+    sample = (f"3D RC frame 10x10x20 at full size, pushover steps {lead + 1}..{lead + n} "
+              f"({its} Newton iterations: element state, assembly, ProfileSPD factor and "
+              f"two right-hand sides each), 1 thread; model set-up, gravity and the first "
+              f"{lead} pushover steps ({t1 - t0:.0f} s) untimed")
+    return pts / dt, its / dt, sample
 
 
 _CPU = None
@@ -479,54 +597,58 @@ _CPU = None
 
 def _frame_worker(args):
     global _CPU
-    kind, k, nsteps = args
+    kind, n = args
     if kind == "init":
-        _CPU = FrameCpu(nsteps)
+        _CPU = FrameCpu(n)
         return 0
     t0 = time.perf_counter()
-    pts = _CPU.iteration(k)
-    return pts, time.perf_counter() - t0
+    pts, its = _CPU.steps(n)
+    return pts, its, time.perf_counter() - t0
 
 
 def run_reference_frame(args):
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
-        return 0
+        return None
     import multiprocessing as mp
     cores = os.cpu_count() or 1
-    nsteps = args.warmup + args.steps
+    W, K = args.warmup, args.steps
     ctx = mp.get_context("spawn")
     with ctx.Pool(cores) as pool:
-        pool.map(_frame_worker, [("init", 0, nsteps)] * cores, chunksize=1)
-        for k in range(args.warmup):
-            pool.map(_frame_worker, [("step", k, nsteps)] * cores, chunksize=1)
+        pool.map(_frame_worker, [("init", W)] * cores, chunksize=1)
         t0 = time.perf_counter()
-        pts = 0
-        for k in range(args.warmup, nsteps):
-            res = pool.map(_frame_worker, [("step", k, nsteps)] * cores, chunksize=1)
-            pts += sum(r[0] for r in res)
+        res = pool.map(_frame_worker, [("steps", K)] * cores, chunksize=1)
         wall = time.perf_counter() - t0
+    pts = sum(r[0] for r in res)
+    its = sum(r[1] for r in res)
     value = pts / wall
     sample = (f"3D RC frame 10x10x20 at full size, one model per process on {cores} "
-              f"processes, one Newton iteration (element state, assembly, ProfileSPD factor "
-              f"+ solve) per process per step")
-    line = {
+              f"processes: gravity and pushover steps 1..{W} untimed, then steps "
+              f"{W + 1}..{W + K} timed (element state, assembly, ProfileSPD factor and two "
+              f"right-hand sides per Newton iteration)")
+    desc, _ = frame_model()
+    return {
         "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT,
-        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
-        "ms_per_step": 1e3 * wall / args.steps, "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded model and lateral "
-                                                     "trial fields)",
-        "config": {"workload": "3D RC frame 10x10x20 (6,820 force-based elements): one Newton "
-                               "iteration per step -- forceBeamColumn state determination, "
-                               "assembly, ProfileSPD LDL' solve"},
-        "newton_iters_per_s": args.steps * cores / wall,
+        "n_gpus": args.gpus, "steps": K, "warmup": W,
+        "ms_per_step": 1e3 * wall / K, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic (seeded RC frame model; the BASELINE pushover)",
+        "config": {"workload": "3D RC frame 10x10x20 (6,820 force-based elements), "
+                               "DisplacementControl pushover: one load step per step -- "
+                               "forceBeamColumn state determination, assembly, ProfileSPD "
+                               "LDL' factor, two right-hand sides per Newton iteration, "
+                               "NormDispIncr 1e-10",
+                   "timed_window": f"pushover steps {W + 1}..{W + K} of 200 (after gravity "
+                                   f"and loadConst)",
+                   "elements": desc.num_elems, "fiber_points": desc.meta["fiber_points"],
+                   "system": "ProfileSPD (the oracle's skyline LDL')",
+                   "parallelism": f"{cores} processes, one model each"},
+        "newton_iters_per_s": its / wall,
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
                          "sample": sample},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
         "wall_s": wall,
     }
-    print(json.dumps(line))
-    return 0
 
 
 # ---------------------------------------------------------------------------
@@ -627,7 +749,7 @@ def run_batch(args):
     loop_value = n_loop / t_loop
     if rank != 0:
         dist.destroy_process_group()
-        return 0
+        return None
     kernels = {k: v for k, v in prof.items() if v[1] > 0 and k != "return_map_cap_hits"}
     dominant = max(kernels, key=lambda k: kernels[k][0])
     dom_ms, dom_launches = kernels[dominant]
@@ -684,10 +806,9 @@ def run_batch(args):
                                         args.steps)
         line["cpu_baseline"] = {"value": rate, "unit": "frame time steps/s", "cores": 1,
                                 "kind": "port", "sample": sample}
-    print(json.dumps(line))
     if world > 1:
         dist.destroy_process_group()
-    return 0
+    return line
 
 
 def _batch_cpu(parts, lead, steps):
@@ -723,7 +844,7 @@ def _batch_worker(args):
 def run_reference_batch(args):
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
-        return 0
+        return None
     import multiprocessing as mp
     cores = os.cpu_count() or 1
     lead = args.batch_lead + args.warmup
@@ -753,8 +874,7 @@ def run_reference_batch(args):
                 "d2h_bytes_per_step": 0},
         "wall_s": wall,
     }
-    print(json.dumps(line))
-    return 0
+    return line
 
 
 # ---------------------------------------------------------------------------
@@ -840,7 +960,7 @@ def run_adjoint(args):
     m.close()
     if rank != 0:
         dist.destroy_process_group()
-        return 0
+        return None
     kernels = {k: v for k, v in prof.items() if v[1] > 0 and k != "return_map_cap_hits"}
     newton = sum(s_[0] for s_ in stats)
     line = {
@@ -878,20 +998,18 @@ def run_adjoint(args):
             "value": rate, "unit": "frame time steps/s (forward)", "cores": 1, "kind": "port",
             "sample": sample + "; the reference has no Steel02 sensitivity, so a CPU gradient "
                       f"by central differences costs {2 * 3 * int(desc.num_elems)} forward runs"}
-    print(json.dumps(line))
     if world > 1:
         dist.destroy_process_group()
-    return 0
+    return line
 
 
 def run_reference_adjoint(args):
     if int(os.environ.get("RANK", "0")) != 0:
-        return 0
-    print(json.dumps({"impl": "reference", "unavailable":
-                      "the reference has no Steel02 stress sensitivity (its DDM, "
-                      "computeGradients, covers Steel01/Concrete01), so it has no gradient "
-                      "path for this workload; its CPU forward is timed by --workload batch"}))
-    return 0
+        return None
+    return {"impl": "reference", "unavailable":
+            "the reference has no Steel02 stress sensitivity (its DDM, computeGradients, "
+            "covers Steel01/Concrete01), so it has no gradient path for this workload; its "
+            "CPU forward is timed by --workload batch"}
 
 
 # ---------------------------------------------------------------------------
@@ -953,7 +1071,7 @@ def _brick_worker(args):
 def run_reference_brick(args):
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
-        return 0
+        return None
     import multiprocessing as mp
     cores = os.cpu_count() or 1
     per_step = 4.0
@@ -982,8 +1100,7 @@ def run_reference_brick(args):
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
         "wall_s": wall,
     }
-    print(json.dumps(line))
-    return 0
+    return line
 
 
 def run_brick(args):
@@ -1079,7 +1196,7 @@ def run_brick(args):
     e2e_value = job_rate(npts * args.steps, time.perf_counter() - t0, world, torch, dist)
     if rank != 0:
         dist.destroy_process_group()
-        return 0
+        return None
     alg = brick_alg_bytes(npts, desc.num_elems, desc.num_nodes, m.nnz, m.neq)
     kernels = {k: v for k, v in prof.items() if v[1] > 0 and k != "return_map_cap_hits"}
     dominant = max(kernels, key=lambda k: kernels[k][0])
@@ -1122,10 +1239,33 @@ def run_brick(args):
         rate, sample = brick_cpu_sample()
         line["cpu_baseline"] = {"value": rate, "unit": UNIT, "cores": 1, "kind": "port",
                                 "sample": sample}
-    print(json.dumps(line))
     if world > 1:
         dist.destroy_process_group()
-    return 0
+    return line
+
+
+SUB_WORKLOADS = (("brick", "run_brick", dict(steps=10, warmup=3)),
+                 ("batch", "run_batch", dict(steps=20, warmup=3)),
+                 ("adjoint", "run_adjoint", dict(warmup=3)))
+
+
+def sub_workloads(args):
+    """The other BASELINE configurations, each measured as its own workload
+    would measure it (own clocks, own CPU sample): the stdBrick J2 block
+    128x128x64 (config 2), 4,096 batched frames (config 3) and the adjoint
+    of 64 frames over 2,000 steps (config 4)."""
+    import torch
+    out = {}
+    for name, fn, over in SUB_WORKLOADS:
+        a = argparse.Namespace(**{**vars(args), **over, "workload": name})
+        t0 = time.perf_counter()
+        try:
+            out[name] = globals()[fn](a)
+        except Exception as e:            # one failing block must not lose the others
+            out[name] = {"error": f"{type(e).__name__}: {e}"}
+        out[name]["wall_s"] = time.perf_counter() - t0
+        torch.cuda.empty_cache()
+    return out
 
 
 def main():
@@ -1137,8 +1277,10 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="xara", choices=["xara", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--no-analysis", action="store_true")
-    ap.add_argument("--analysis-steps", type=int, default=5)
+    ap.add_argument("--no-analysis", action="store_true",
+                    help="frame3d: skip the rest of the pushover after the timed steps")
+    ap.add_argument("--no-sub", action="store_true",
+                    help="frame3d: skip the brick, batch and adjoint blocks")
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--frames", type=int, default=BATCH_FRAMES)
     ap.add_argument("--batch-lead", type=int, default=150)
@@ -1151,11 +1293,18 @@ def main():
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     if args.impl == "reference":
-        return {"frame3d": run_reference_frame, "brick": run_reference_brick,
+        line = {"frame3d": run_reference_frame, "brick": run_reference_brick,
                 "batch": run_reference_batch,
                 "adjoint": run_reference_adjoint}[args.workload](args)
-    return {"frame3d": run_frame, "brick": run_brick, "batch": run_batch,
-            "adjoint": run_adjoint}[args.workload](args)
+    else:
+        line = {"frame3d": run_frame, "brick": run_brick, "batch": run_batch,
+                "adjoint": run_adjoint}[args.workload](args)
+        if (line is not None and args.workload == "frame3d" and not args.no_sub
+                and line["n_gpus"] == 1):
+            line["workloads"] = sub_workloads(args)
+    if line is not None:
+        print(json.dumps(line))
+    return 0
 
 
 if __name__ == "__main__":

@@ -368,8 +368,19 @@ int xg_linsoe_add_b(xg_linsoe *s, const double *v, const int *id, int ndof, doub
 int xg_linsoe_set_b(xg_linsoe *s, const double *v, double fact);
 int xg_linsoe_get_a(const xg_linsoe *s, double *vals);            /* CSR values */
 int xg_linsoe_get_b(const xg_linsoe *s, double *b);
-/* PCG to ||r|| <= rtol ||b||; XG_ESOLVE on breakdown or maxit (X holds the
-   last iterate); the device copy of the pattern is made at the first call. */
+/* The solver behind solve(): XG_SYSTEM_BJPCG (the default, `system
+   CudaBJPCG`) or XG_SYSTEM_PROFILE_SPD (`system ProfileSPD`,
+   profileSPD/ProfileSPDLinSOE.cpp and ProfileSPDLinDirectSolver.cpp: addA
+   keeps only the terms with row <= col, as ProfileSPDLinSOE::addA, stored
+   in the lower triangle's slot (col, row); get_a returns that lower
+   triangle, the upper is zero).  Switching the system zeroes A. */
+int xg_linsoe_set_system(xg_linsoe *s, int system);
+/* BJPCG: PCG to ||r|| <= rtol ||b||; XG_ESOLVE on breakdown or maxit (X
+   holds the last iterate).  PROFILE_SPD: the device LDL' (factored once per
+   matrix: again only after zeroA or addA) and its substitutions; rtol and
+   maxit unused, iters = relres = 0; XG_ESOLVE when a pivot fails the
+   reference's checks (a first pivot <= 0, a pivot == 0 or |pivot| <=
+   1e-12).  The device copy of the pattern is made at the first call. */
 int xg_linsoe_solve(xg_linsoe *s, double rtol, int maxit, int *iters, double *relres);
 int xg_linsoe_get_x(const xg_linsoe *s, double *x);
 

@@ -238,7 +238,10 @@ def main():
     stub_o = os.path.join(objdir, "stubs.o")
     sh(["gcc", "-O0", "-fPIC", "-w", "-c", stub_c, "-o", stub_o])
     lib = os.path.join(OUT, "libxara_ref.so")
-    sh(["g++", "-shared", "-o", lib] + objs + [stub_o, "-Wl,--no-undefined", "-lm"])
+    # link beside it, then rename: a process that has the old library loaded
+    # keeps its mapping
+    sh(["g++", "-shared", "-o", lib + ".tmp"] + objs + [stub_o, "-Wl,--no-undefined", "-lm"])
+    os.replace(lib + ".tmp", lib)
     print(f"built {lib}: {len(objs)} objects, {len(kinds)} stubbed symbols")
     return 0
 

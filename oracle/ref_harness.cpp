@@ -112,7 +112,20 @@ class GenAccess : public SparseGenColLinSOE {
   const int *colStart() const { return colStartA; }
 };
 
+// The reference's own profile storage (ProfileSPDLinSOE.h: A, iDiagLoc), for
+// comparing a device system's assembly with it.
+class ProfAccess : public ProfileSPDLinSOE {
+ public:
+  explicit ProfAccess(ProfileSPDLinSolver &s) : ProfileSPDLinSOE(s) {}
+  const double *a() const { return A; }
+  const int *diagLoc() const { return iDiagLoc; }
+  int psize() const { return profileSize; }
+  bool factored() const { return isAfactored; }
+};
+
 struct Capture {
+  int profile = 0;    // also keep ProfileSPDLinSOE's A at every captured solve
+  std::vector<double> P, lastP;
   int enabled = 0;
   int cap = 0;
   int count = 0;
@@ -181,6 +194,7 @@ class CaptureSOE : public LinearSOE {
   int recvSelf(int, Channel &, FEM_ObjectBroker &) override { return 0; }
 
   GenAccess &gen() { return gen_; }
+  const ProfAccess &profile() const { return prof_; }
   double solveSeconds = 0.0;
   // A second LinearSOE fed the same calls (a system under test), and a
   // callback run before every solve, while both hold the same A and B.
@@ -193,7 +207,7 @@ class CaptureSOE : public LinearSOE {
   Harness *h_;
   NoSolve nosolve_;
   GenAccess gen_;
-  ProfileSPDLinSOE prof_;
+  ProfAccess prof_;
 };
 
 struct Harness {
@@ -233,6 +247,13 @@ int CaptureSOE::solve() {
     const Vector &b = prof_.getB();
     for (int i = 0; i < n; i++) c.B.push_back(b(i));
     c.A.insert(c.A.end(), gen_.a(), gen_.a() + nz);
+    if (c.profile) {
+      // ProfileSPDLinDirectSolver factors A in place: a second solve with
+      // the same matrix finds the factor there, so keep the assembled A
+      // from the last solve that had not factored it yet
+      if (!prof_.factored()) c.lastP.assign(prof_.a(), prof_.a() + prof_.psize());
+      c.P.insert(c.P.end(), c.lastP.begin(), c.lastP.end());
+    }
     size_t off = c.U.size();
     c.U.resize(off + nu);
     h_->snapshotU(&c.U[off]);
@@ -586,6 +607,31 @@ int xref_observer_errors(void *hp) {
 }
 
 int xref_num_captured(void *hp) { return ((Harness *)hp)->cap.count; }
+
+// Keep ProfileSPDLinSOE's own profile A at every captured solve as well
+// (before the first phase).
+extern "C" int xref_capture_profile(void *hp, int on) {
+  ((Harness *)hp)->cap.profile = on;
+  return 0;
+}
+
+// The profile layout (iDiagLoc[n], 1-based as the reference keeps it) and
+// size, then the captured profiles [count][size].
+extern "C" int xref_profile_layout(void *hp, int *diag_loc, int *size) {
+  Harness *h = (Harness *)hp;
+  if (!h->soe) return -1;
+  const int n = h->soe->getNumEqn();
+  const ProfAccess &p = h->soe->profile();
+  if (diag_loc) memcpy(diag_loc, p.diagLoc(), sizeof(int) * n);
+  if (size) *size = p.psize();
+  return 0;
+}
+
+extern "C" int xref_captured_profile(void *hp, double *out) {
+  Capture &c = ((Harness *)hp)->cap;
+  if (out) memcpy(out, c.P.data(), sizeof(double) * c.P.size());
+  return (int)c.P.size();
+}
 
 int xref_captured(void *hp, int *step, int *iter, double *B, double *A, double *X, double *U) {
   Capture &c = ((Harness *)hp)->cap;

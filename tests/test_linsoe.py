@@ -149,3 +149,56 @@ def test_pcg_solve_matches_dense(need_gpu, blocks):
             s.add_a(k, ids, fact=2.0)
         x2, _, _ = s.solve(rtol=1e-13)
         np.testing.assert_allclose(x2, 0.5 * np.linalg.solve(K, b), rtol=1e-9, atol=1e-12)
+
+
+@pytest.mark.gpu
+def test_profile_ldl_solve_matches_dense(need_gpu):
+    """`system ProfileSPD` on the device: ProfileSPDLinSOE's assembly (the
+    row <= col terms) and the device LDL' against a dense solve; a second
+    right-hand side reuses the factors, new values refactor."""
+    n, elems, K, rp, ci, blk = _problem(seed=5)
+    rng = np.random.default_rng(6)
+    b1, b2 = rng.normal(size=n), rng.normal(size=n)
+    with gpu.LinearSystem(rp, ci, system=gpu.XG_SYSTEM_PROFILE_SPD) as s:
+        for k, ids in elems:
+            s.add_a(k, ids)
+        vals = s.values()
+        rows = np.repeat(np.arange(n), np.diff(rp))
+        assert not vals[ci > rows].any()                   # only the lower triangle
+        s.set_b(b1)
+        x1, it, rr = s.solve()
+        assert it == 0 and rr == 0.0
+        np.testing.assert_allclose(x1, np.linalg.solve(K, b1), rtol=1e-10, atol=1e-13)
+        s.set_b(b2)
+        x2, _, _ = s.solve()
+        np.testing.assert_allclose(x2, np.linalg.solve(K, b2), rtol=1e-10, atol=1e-13)
+        s.zero_a()
+        for k, ids in elems:
+            s.add_a(k, ids, fact=4.0)
+        x3, _, _ = s.solve()
+        np.testing.assert_allclose(x3, 0.25 * np.linalg.solve(K, b2), rtol=1e-10, atol=1e-13)
+
+
+@pytest.mark.gpu
+def test_profile_ldl_pivot_checks(need_gpu):
+    """ProfileSPDLinDirectSolver's checks: a first pivot <= 0 fails the
+    solve (XG_ESOLVE naming the equation); a later negative pivot does not."""
+    n, elems, K, rp, ci, blk = _problem(seed=7)
+    with gpu.LinearSystem(rp, ci, system=gpu.XG_SYSTEM_PROFILE_SPD) as s:
+        for k, ids in elems:
+            s.add_a(k, ids)
+        s.add_a(np.array([[-2.0 * K[0, 0]]]), [0])           # a negative first pivot
+        s.set_b(np.ones(n))
+        with pytest.raises(gpu.XaraGpuError, match="pivot 0"):
+            s.solve()
+    with gpu.LinearSystem(rp, ci, system=gpu.XG_SYSTEM_PROFILE_SPD) as s:
+        Kn = K.copy()
+        for k, ids in elems:
+            s.add_a(k, ids)
+        last = n - 1
+        s.add_a(np.array([[-3.0 * K[last, last]]]), [last])   # indefinite, last pivot < 0
+        Kn[last, last] -= 3.0 * K[last, last]
+        b = np.random.default_rng(8).normal(size=n)
+        s.set_b(b)
+        x, _, _ = s.solve()
+        np.testing.assert_allclose(x, np.linalg.solve(Kn, b), rtol=1e-9, atol=1e-12)

@@ -79,5 +79,5 @@ def test_reference_arm_other_ranks_exit_without_work(monkeypatch, capsys, arm):
     sys.path.insert(0, ROOT)
     import bench
     monkeypatch.setenv("RANK", "1")
-    assert getattr(bench, arm)(None) == 0
+    assert getattr(bench, arm)(None) is None
     assert capsys.readouterr().out == ""

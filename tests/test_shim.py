@@ -1,12 +1,15 @@
-"""The `system CudaBJPCG` shim (include/CudaBJPCGLinSOE.h) inside the
+"""The `system` shims (include/CudaBJPCGLinSOE.h: SparseGenColLinSOE's
+assembly; include/CudaProfileSPDLinSOE.h: ProfileSPDLinSOE's) inside the
 reference's own analysis loop.
 
 The shim is compiled against the reference's headers and handed to the
 reference harness (oracle/_ref) as a second LinearSOE: the reference's
 AnalysisModel graph sizes it, and its integrators and FE_Elements feed it the
 same zeroA / zeroB / addA / addB / setB calls they feed the reference's
-SparseGenColLinSOE.  Before every solve the shim's pattern, assembled values
-and right-hand side must equal the reference's bit for bit.  Host work only
+SparseGenColLinSOE and ProfileSPDLinSOE.  Before every solve the shim's
+pattern, assembled values and right-hand side must equal the reference's bit
+for bit (the ProfileSPD shim's against ProfileSPDLinSOE's own profile
+storage).  Host work only
 (the device solve is covered by tests/test_linsoe.py); skipped where the
 reference sources or the compiled harness are absent.
 """
@@ -49,7 +52,7 @@ def driver(tmp_path_factory):
     ref.lib()                                  # the harness instance the driver links
     D = C.CDLL(out)
     D.shim_attach.restype = C.c_void_p
-    D.shim_attach.argtypes = [C.c_void_p, C.c_int]
+    D.shim_attach.argtypes = [C.c_void_p, C.c_int, C.c_int]
     D.shim_free.argtypes = [C.c_void_p]
     D.shim_sizes.argtypes = [C.c_void_p] + [C.c_void_p] * 4
     D.shim_pattern.argtypes = [C.c_void_p] + [C.c_void_p] * 3
@@ -61,12 +64,14 @@ def _p(a):
     return a.ctypes.data_as(C.c_void_p)
 
 
-def run_with_shim(D, desc, phases):
+def run_with_shim(D, desc, phases, system=gpu.XG_SYSTEM_BJPCG):
     rec = {}
 
     def attach(h):
-        rec["r"] = D.shim_attach(h, CAP)
+        rec["r"] = D.shim_attach(h, CAP, system)
         assert rec["r"]
+        if system == gpu.XG_SYSTEM_PROFILE_SPD:
+            ref.lib().xref_capture_profile(C.c_void_p(h), 1)
 
     run = ref.RefRun(desc, phases, capture=(0, 1 << 20), cap_solves=CAP, attach=attach)
     r = rec["r"]
@@ -142,3 +147,38 @@ def test_shim_assembles_what_the_reference_assembles(driver, name):
         singles = int((sizes == 1).sum())
         tied = int(np.sum(np.bincount(run.eqn[run.eqn >= 0]) > 1))
         assert tied >= 1 and (sizes == desc.ndf).sum() >= len(free) // 2, (singles, tied)
+
+
+@pytest.mark.parametrize("name", list(MODELS))
+def test_profile_shim_assembles_what_profilespd_assembles(driver, name):
+    """`system ProfileSPD` on the device (include/CudaProfileSPDLinSOE.h): at
+    every solve the values its LDL' reads (the lower triangle, holding the
+    terms ProfileSPDLinSOE::addA keeps, row <= col) equal ProfileSPDLinSOE's
+    own profile storage bit for bit, profile entries outside the pattern
+    included (zero in both), and the right-hand side equals the reference's."""
+    L = ref.lib()
+    L.xref_profile_layout.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p]
+    L.xref_captured_profile.argtypes = [C.c_void_p, C.c_void_p]
+    L.xref_capture_profile.argtypes = [C.c_void_p, C.c_int]
+    desc, phases = MODELS[name][0]()
+    run, rp, ci, blk, A, B, errors = run_with_shim(driver, desc, phases,
+                                                   gpu.XG_SYSTEM_PROFILE_SPD)
+    assert errors == 0
+    n = run.neq
+    diag = np.zeros(n, np.int32)
+    psize = C.c_int()
+    assert L.xref_profile_layout(C.c_void_p(run.h), _p(diag), C.byref(psize)) == 0
+    ns = A.shape[0]
+    P = np.zeros(ns * psize.value)
+    assert L.xref_captured_profile(C.c_void_p(run.h), _p(P)) == ns * psize.value
+    P = P.reshape(ns, psize.value)
+    rows = np.repeat(np.arange(n), np.diff(rp))
+    lower = ci <= rows
+    # CSR (c, r), r <= c, sits at profile position iDiagLoc[c] - 1 - (c - r)
+    pos = diag[rows[lower]] - 1 - (rows[lower] - ci[lower])
+    for k in range(ns):
+        mine = np.zeros(psize.value)
+        mine[pos] = A[k][lower]
+        assert np.array_equal(mine, P[k]), (name, k)
+        assert np.array_equal(A[k][~lower], np.zeros((~lower).sum())), (name, k)
+        assert np.array_equal(B[k], run.cap_B[k]), (name, k)

@@ -146,6 +146,47 @@ int profile_factor(const ProfileSystem &S, cudaStream_t s, int *bad_eq);
 // nt*32, entries past n zero), the solution on return; nrhs <= 4.
 int profile_solve(const ProfileSystem &S, int nrhs, double *x, int ldx, cudaStream_t s);
 
+// The tiled envelope LDL' with its device buffers: planned once per pattern,
+// factored once per tangent, then up to four right-hand sides per solve.
+// Used by the device model (`system ProfileSPD`) and by the standalone linear
+// system (xg_linsoe_*).
+class ProfileSolver {
+ public:
+  ProfileSolver() = default;
+  ProfileSolver(const ProfileSolver &) = delete;
+  ProfileSolver &operator=(const ProfileSolver &) = delete;
+  ~ProfileSolver();
+  // Plan the envelope of the n-equation CSR pattern (host arrays, sorted
+  // columns) and allocate its tiles; d_rowptr, d_colidx and d_vals are the
+  // device copies the factorisation reads (the lower triangle).  XG_ENOMEM
+  // (with the error text set) when the tiles would take more than half of
+  // the free device memory.
+  int setup(int n, const int *rowptr, const int *colidx, const int *d_rowptr,
+            const int *d_colidx, const double *d_vals, cudaStream_t s);
+  bool ready() const { return ready_; }
+  // Factor the values now in d_vals.  XG_ESOLVE on a failed pivot check
+  // (*bad_eq = the equation) or a dependency wait that timed out (*bad_eq =
+  // -1).
+  int factor(cudaStream_t s, int *bad_eq);
+  // x[r] = A^-1 b[r] for r < nrhs (1..4; device vectors of n entries) with
+  // the last factorisation.
+  int solve(int nrhs, const double *const *b, double *const *x, cudaStream_t s);
+  const ProfileSystem &system() const { return S_; }
+
+ private:
+  template <class T>
+  struct Buf {
+    T *p = nullptr;
+    int alloc(size_t count);
+    ~Buf();
+  };
+  ProfileSystem S_{};
+  bool ready_ = false;
+  int ldx_ = 0;
+  Buf<int> ftile_, flags_, tasks_, next_, upd_, done_, cpl_;
+  Buf<double> L_, invD_, piv_, px_, Winv_, F_, G_, E_, H_, Q_, R_, sweep_;
+};
+
 // ProfileSPD for many small disconnected parts, one band per part
 // (xg_band.cu)
 struct BandSystem {

@@ -7,7 +7,12 @@
 // a search of the row; addB / setB likewise) and accumulates in host memory,
 // the way the reference's FE_Element loop feeds it; solve() runs the
 // block-Jacobi PCG of the model path (sliced ELL SpMV, long rows in chunks)
-// on the device and returns X to the host.
+// on the device and returns X to the host.  With `system ProfileSPD`
+// (xg_linsoe_set_system) addA follows ProfileSPDLinSOE instead
+// (profileSPD/ProfileSPDLinSOE.cpp:214-269: only the terms with row <= col,
+// kept here in the lower triangle's slot (col, row)) and solve() factors
+// with the device LDL' once per matrix (the reference's isAfactored), with
+// ProfileSPDLinDirectSolver's pivot checks.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -57,6 +62,11 @@ struct xg_linsoe {
   DevArray<unsigned int> barrier;
   DevArray<double> vals, b, x, binv, r, z, p, q, partials, scalars, sell_vals, chunk_part;
   xg::PcgSystem S{};
+  // `system ProfileSPD`: the device LDL', factored once per matrix
+  int system = XG_SYSTEM_BJPCG;
+  xg::ProfileSolver prof;
+  bool prof_factored = false;
+  bool prof_vals_stale = true;
 
   ~xg_linsoe() {
     if (stream) cudaStreamDestroy(stream);
@@ -69,9 +79,22 @@ struct xg_linsoe {
     return (it != e && *it == col) ? (long)(it - colidx.data()) : -1;
   }
 
+  // Device copies of the pattern for the LDL' (and the envelope tiles).
+  int setup_profile() {
+    if (prof.ready()) return 0;
+    if (!stream && cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking) != cudaSuccess)
+      return lfail(XG_ECUDA, "xg_linsoe: stream creation failed");
+    const size_t nnz = colidx.size(), nv = std::max(n, 1);
+    int e = rp.upload(rowptr.data(), rowptr.size(), stream);
+    e |= ci.upload(colidx.data(), nnz, stream);
+    e |= vals.alloc(std::max<size_t>(nnz, 1)) | b.alloc(nv) | x.alloc(nv);
+    if (e) return lfail(XG_ENOMEM, "xg_linsoe: device allocation failed");
+    return prof.setup(n, rowptr.data(), colidx.data(), rp.p, ci.p, vals.p, stream);
+  }
+
   int setup() {
     if (ready) return 0;
-    if (cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking) != cudaSuccess)
+    if (!stream && cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking) != cudaSuccess)
       return lfail(XG_ECUDA, "xg_linsoe: stream creation failed");
     const int nblk = (int)blk.size() - 1;
     const size_t nnz = colidx.size(), nv = std::max(n, 1);
@@ -172,6 +195,21 @@ void xg_linsoe_destroy(xg_linsoe *s) { delete s; }
 int xg_linsoe_zero_a(xg_linsoe *s) {
   if (!s) return lfail(XG_EINVAL, "null system");
   std::fill(s->A.begin(), s->A.end(), 0.0);
+  s->prof_factored = false;
+  s->prof_vals_stale = true;
+  return 0;
+}
+
+int xg_linsoe_set_system(xg_linsoe *s, int system) {
+  if (!s || (system != XG_SYSTEM_BJPCG && system != XG_SYSTEM_PROFILE_SPD))
+    return lfail(XG_EINVAL, "xg_linsoe_set_system: XG_SYSTEM_BJPCG or XG_SYSTEM_PROFILE_SPD");
+  if (system != s->system) {
+    // the two systems keep A in different forms: start from zero
+    s->system = system;
+    std::fill(s->A.begin(), s->A.end(), 0.0);
+  }
+  s->prof_factored = false;
+  s->prof_vals_stale = true;
   return 0;
 }
 
@@ -184,6 +222,26 @@ int xg_linsoe_zero_b(xg_linsoe *s) {
 int xg_linsoe_add_a(xg_linsoe *s, const double *m, const int *id, int ndof, double fact) {
   if (!s || ndof < 0 || (ndof && (!m || !id))) return lfail(XG_EINVAL, "bad addA argument");
   if (fact == 0.0) return 0;
+  s->prof_factored = false;
+  s->prof_vals_stale = true;
+  if (s->system == XG_SYSTEM_PROFILE_SPD) {
+    // ProfileSPDLinSOE::addA (profileSPD/ProfileSPDLinSOE.cpp:214-269):
+    // column-outer, row-inner, A(row, col) += m(row, col) for row <= col
+    // only; the entry sits in the lower triangle's slot (col, row), which
+    // the LDL' reads.
+    for (int j = 0; j < ndof; j++) {
+      const int col = id[j];
+      if (col < 0 || col >= s->n) continue;
+      for (int i = 0; i < ndof; i++) {
+        const int row = id[i];
+        if (row < 0 || row > col) continue;
+        const long k = s->slot(col, row);
+        if (k < 0) continue;
+        s->A[k] += fact * m[(size_t)i * ndof + j];
+      }
+    }
+    return 0;
+  }
   // Column-outer, row-inner, as SparseGenColLinSOE::addA
   // (sparseGEN/SparseGenColLinSOE.cpp:263-313): an ID that names one
   // equation twice (nodes tied by a constraint) then sums the entry's terms
@@ -227,8 +285,52 @@ int xg_linsoe_get_a(const xg_linsoe *s, double *vals) {
   return 0;
 }
 
+// ProfileSPDLinDirectSolver::solve (profileSPD/ProfileSPDLinDirectSolver.cpp:
+// 100-256): factor when A changed since the last factorisation, then the
+// substitutions; a pivot that fails the reference's checks is XG_ESOLVE.
+static int linsoe_solve_profile(xg_linsoe *s, int *iters, double *relres) {
+  if (int e = s->setup_profile()) return e;
+  cudaStream_t st = s->stream;
+  if (s->prof_vals_stale &&
+      cudaMemcpyAsync(s->vals.p, s->A.data(), s->A.size() * sizeof(double),
+                      cudaMemcpyHostToDevice, st) != cudaSuccess)
+    return lfail(XG_ECUDA, "xg_linsoe_solve: copy of A failed");
+  s->prof_vals_stale = false;
+  if (!s->prof_factored) {
+    int bad = -1;
+    if (s->prof.factor(st, &bad) != 0) {
+      char msg[160];
+      if (bad >= 0)
+        snprintf(msg, sizeof msg, "xg_linsoe_solve: ProfileSPD pivot %d fails the check (aii == "
+                 "0, |aii| <= 1e-12, or a first pivot <= 0)", bad);
+      else
+        snprintf(msg, sizeof msg, "xg_linsoe_solve: ProfileSPD factorisation wait timed out");
+      return lfail(XG_ESOLVE, msg);
+    }
+    s->prof_factored = true;
+  }
+  const double *bp = s->b.p;
+  double *xp = s->x.p;
+  if (cudaMemcpyAsync(s->b.p, s->B.data(), s->B.size() * sizeof(double), cudaMemcpyHostToDevice,
+                      st) != cudaSuccess)
+    return lfail(XG_ECUDA, "xg_linsoe_solve: copy of B failed");
+  if (int e = s->prof.solve(1, &bp, &xp, st)) return lfail(e, "xg_linsoe_solve: substitutions failed");
+  if (cudaMemcpyAsync(s->X.data(), s->x.p, s->n * sizeof(double), cudaMemcpyDeviceToHost, st) !=
+          cudaSuccess ||
+      cudaStreamSynchronize(st) != cudaSuccess)
+    return lfail(XG_ECUDA, "xg_linsoe_solve: copy of X failed");
+  if (iters) *iters = 0;
+  if (relres) *relres = 0.0;
+  return 0;
+}
+
 int xg_linsoe_solve(xg_linsoe *s, double rtol, int maxit, int *iters, double *relres) {
-  if (!s || !(rtol > 0.0) || maxit < 1) return lfail(XG_EINVAL, "bad solve settings");
+  if (!s) return lfail(XG_EINVAL, "null system");
+  if (s->system == XG_SYSTEM_PROFILE_SPD) {
+    if (s->n == 0) return 0;
+    return linsoe_solve_profile(s, iters, relres);
+  }
+  if (!(rtol > 0.0) || maxit < 1) return lfail(XG_EINVAL, "bad solve settings");
   if (s->n == 0) return 0;
   if (int e = s->setup()) return e;
   cudaStream_t st = s->stream;

@@ -185,12 +185,10 @@ struct xg_model {
   int maxit = 20000;
   // `system ProfileSPD` on the device (xg_profile.cu)
   int system = XG_SYSTEM_PROFILE_SPD;
-  ProfileSystem psys{};
+  ProfileSolver envelope;                      // one envelope (connected model)
   bool prof_ready = false, prof_factored = false;
-  std::vector<int> ftile;
-  DBuf<int> d_ftile, d_pflags, d_ptasks, d_pnext, d_pupd, d_pdone;
-  DBuf<double> d_L, d_invD, d_piv, d_px, d_Winv, d_Fc, d_Gc, d_Ec, d_Hc, d_Qc, d_Rc, d_psweep;
-  DBuf<int> d_pcpl;
+  DBuf<int> d_pflags;
+  DBuf<double> d_invD, d_px;
   int prof_ldx = 0;
   bool prof_band = false;                      // many small parts: one band each
   BandSystem bsys{};
@@ -1334,45 +1332,11 @@ int xg_model::ensure_profile() {
       }
     }
   }
-  int nt = 0, W = 0;
-  RET(profile_plan(neq, rowptr.data(), colidx.data(), ftile, nt, W));
-  const size_t tiles = profile_tile_doubles(nt, W);
-  size_t free_b = 0, total_b = 0;
-  CK(cudaMemGetInfo(&free_b, &total_b));
-  if ((tiles + (size_t)nt * 32 * 6) * sizeof(double) > free_b / 2)
-    return fail(XG_ENOMEM, "ProfileSPD envelope needs %.1f GB (%d tile rows x %d): use the "
-                "block-Jacobi PCG system", tiles * 8e-9, nt, W + 1);
-  std::vector<int> tasks;
-  profile_tasks(nt, W, ftile, tasks);
-  RET(d_ftile.upload(ftile.data(), ftile.size(), stream));
-  RET(d_ptasks.upload(tasks.data(), tasks.size(), stream));
-  RET(d_L.alloc(tiles));
-  RET(d_Winv.alloc((size_t)nt * 1024));
-  RET(d_Fc.alloc((size_t)nt * 1024));
-  RET(d_Gc.alloc((size_t)nt * 1024));
-  RET(d_invD.alloc((size_t)nt * 32));
-  RET(d_piv.alloc((size_t)nt * 32));
-  prof_ldx = nt * 32;
-  RET(d_px.alloc((size_t)prof_ldx * 4));
-  CK(cudaMemsetAsync(d_px.p, 0, (size_t)prof_ldx * 4 * sizeof(double), stream));
-  RET(d_pnext.alloc(1));
-  RET(d_pupd.alloc((size_t)nt * (W + 1)));
-  RET(d_pdone.alloc((size_t)nt * (W + 1)));
-  RET(d_pflags.alloc(4));
-  for (auto *b : {&d_Ec, &d_Hc, &d_Qc, &d_Rc}) RET(b->alloc((size_t)nt * 1024));
-  RET(d_pcpl.alloc((size_t)std::max(nt, 1)));
-  RET(d_psweep.alloc(4 * 4 * (size_t)std::max(nt, 1) * 32));
-  psys.sweep = d_psweep.p;
-  psys.n = neq; psys.nt = nt; psys.W = W;
-  psys.rowptr = d_rowptr.p; psys.colidx = d_colidx.p; psys.vals = d_vals.p;
-  psys.ftile = d_ftile.p; psys.L = d_L.p; psys.invD = d_invD.p; psys.piv = d_piv.p;
-  psys.Winv = d_Winv.p; psys.F = d_Fc.p; psys.G = d_Gc.p;
-  psys.E = d_Ec.p; psys.H = d_Hc.p; psys.Q = d_Qc.p; psys.R = d_Rc.p; psys.cpl = d_pcpl.p;
-  psys.tasks = reinterpret_cast<const int4 *>(d_ptasks.p);
-  psys.ntasks = (int)(tasks.size() / 4);
-  psys.next_task = d_pnext.p; psys.upd = d_pupd.p; psys.done = d_pdone.p;
-  psys.flags = d_pflags.p;
-  psys.min_diag_tol = 1.0e-12;   // ProfileSPDLinDirectSolver.h:49 default
+  {
+    const int r = envelope.setup(neq, rowptr.data(), colidx.data(), d_rowptr.p, d_colidx.p,
+                                 d_vals.p, stream);
+    if (r) return r;   // envelope.setup set the error text
+  }
   prof_ready = true;
   return 0;
 }
@@ -1411,7 +1375,7 @@ int xg_model::solve_profile(int nrhs, const double *const *b, double *const *x) 
   if (!prof_factored) {
     prof_begin(P_LDL_FACTOR);
     int bad = -1;
-    const int r = profile_factor(psys, stream, &bad);
+    const int r = envelope.factor(stream, &bad);
     prof_end(P_LDL_FACTOR, 2);
     if (r) {
       if (bad >= 0) return fail(XG_ESOLVE, "ProfileSPD: pivot %d fails the check (aii == 0, "
@@ -1420,15 +1384,9 @@ int xg_model::solve_profile(int nrhs, const double *const *b, double *const *x) 
     }
     prof_factored = true;
   }
-  for (int r = 0; r < nrhs; r++)
-    CK(cudaMemcpyAsync(d_px.p + (size_t)r * prof_ldx, b[r], (size_t)neq * sizeof(double),
-                       cudaMemcpyDeviceToDevice, stream));
   prof_begin(P_LDL_SOLVE);
-  RET(profile_solve(psys, nrhs, d_px.p, prof_ldx, stream));
+  RET(envelope.solve(nrhs, b, x, stream));
   prof_end(P_LDL_SOLVE, 1);
-  for (int r = 0; r < nrhs; r++)
-    CK(cudaMemcpyAsync(x[r], d_px.p + (size_t)r * prof_ldx, (size_t)neq * sizeof(double),
-                       cudaMemcpyDeviceToDevice, stream));
   prof_flush();
   return 0;
 }

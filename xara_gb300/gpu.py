@@ -404,9 +404,11 @@ def uniaxial_vjp(kind, param, hc, strain, yb):
 class LinearSystem:
     """A standalone device linear system with the reference's LinearSOE
     calls (``xg_linsoe_*``): CSR pattern with sorted columns, host-side
-    addA / addB / setB, block-Jacobi PCG solve on the device."""
+    addA / addB / setB, and on the device either block-Jacobi PCG
+    (``system=XG_SYSTEM_BJPCG``, SparseGenColLinSOE's assembly) or the LDL'
+    (``system=XG_SYSTEM_PROFILE_SPD``, ProfileSPDLinSOE's assembly)."""
 
-    def __init__(self, rowptr, colidx, blk_start=None):
+    def __init__(self, rowptr, colidx, blk_start=None, system=None):
         L = lib()
         L.xg_linsoe_create.argtypes = [C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int,
                                        C.POINTER(C.c_void_p)]
@@ -429,6 +431,9 @@ class LinearSystem:
                                   _p(blk) if blk is not None else None,
                                   0 if blk is None else len(blk) - 1, C.byref(h)))
         self.h = h
+        if system is not None:
+            L.xg_linsoe_set_system.argtypes = [C.c_void_p, C.c_int]
+            _check(L.xg_linsoe_set_system(self.h, int(system)))
 
     def close(self):
         if self.h:
