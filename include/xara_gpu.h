@@ -240,6 +240,14 @@ int xg_elemset_set_trial_disp(xg_model *m, const double *u);
    elements whose state determination failed as a negative code. */
 int xg_elemset_update(xg_model *m, double *csr_vals, double *resid);
 
+/* Per-element results of the last xg_elemset_update, in element order, for
+   callers that assemble through their own loop (FE_Element::addKtToTang /
+   addRtoResidual, analysis/fe_ele/FE_Element.cpp:266-430): K[num_elems *
+   ned * ned] the element tangent (Element::getTangentStiff), P[num_elems *
+   ned] the resisting force (Element::getResistingForce), row-major in the
+   element's dof order (node by node, then dof).  Either may be NULL. */
+int xg_elemset_element_matrices(const xg_model *m, double *K, double *P);
+
 int xg_elemset_commit(xg_model *m);             /* Domain::commit          */
 int xg_elemset_revert(xg_model *m);             /* revertToLastCommit      */
 int xg_elemset_revert_to_start(xg_model *m);    /* revertToStart           */

@@ -62,6 +62,7 @@ domain/domain/single/SingleDomAllSP_Iter.cpp domain/domain/single/SingleDomPC_It
 domain/domain/single/SingleDomParamIter.cpp
 domain/load/ElementalLoadIter.cpp
 element/Element.cpp element/Information.cpp
+recorder/response/Response.cpp recorder/response/ElementResponse.cpp
 element/Plane/FourNodeQuad.cpp element/Brick/Brick.cpp interpolate/shp3d.cpp
 element/Frame/Other/Force/ForceBeamColumn2d.cpp
 element/Frame/Other/Force/ForceBeamColumn3d.cpp

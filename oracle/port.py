@@ -62,6 +62,7 @@ def lib():
         L.xo_uniaxial_path.argtypes = [C.c_int, vp, C.c_int, vp, vp, vp, vp]
         L.xo_uniaxial_init.argtypes = [C.c_int, vp, vp]
         L.xo_uniaxial_trial.argtypes = [C.c_int, vp, vp, C.c_double, vp]
+        L.xo_keep_element_matrices.argtypes = [vp, vp, vp]
         _lib = L
     return _lib
 
@@ -113,6 +114,20 @@ class OracleModel:
         resid = np.zeros(self.neq)
         lib().xo_elem_state(self.h, _p(U), _p(vals), _p(resid))
         return vals, resid
+
+    def element_matrices(self, U):
+        """Every element's tangent [ne, ned, ned] and resisting force [ne,
+        ned] at the trial displacements U (the element state of elem_state)."""
+        d = self.desc
+        ned = (2 if d.elem_type in (3, 4) else 4 if d.elem_type == 1 else 8) * d.ndf
+        K = np.zeros((d.num_elems, ned, ned))
+        P = np.zeros((d.num_elems, ned))
+        lib().xo_keep_element_matrices(self.h, _p(K), _p(P))
+        try:
+            self.elem_state(U)
+        finally:
+            lib().xo_keep_element_matrices(self.h, None, None)
+        return K, P
 
     def commit(self):
         lib().xo_commit(self.h)

@@ -608,6 +608,10 @@ int xref_observer_errors(void *hp) {
 
 int xref_num_captured(void *hp) { return ((Harness *)hp)->cap.count; }
 
+// The reference Domain the harness built (for shims that work on it, before
+// the first phase).
+extern "C" void *xref_domain(void *hp) { return ((Harness *)hp)->domain; }
+
 // Keep ProfileSPDLinSOE's own profile A at every captured solve as well
 // (before the first phase).
 extern "C" int xref_capture_profile(void *hp, int on) {

@@ -428,7 +428,16 @@ typedef struct xo_model {
   long long work_pts, work_fib, work_sec;   /* work counters (benchmarks) */
   double *V, *A, *Vc, *Ac;           /* Newmark trial / committed vel, accel [nu] */
   double *K0vals;                    /* assembled initial stiffness (CSR)    */
+  double *keepK, *keepP;             /* caller buffers for every element's K, P, or NULL */
 } xo_model;
+
+/* Every element's K [ned*ned] and P [ned] also go to these buffers (element
+   order, dof order node by node) at each element phase, as
+   Element::getTangentStiff / getResistingForce return them; NULL stops it. */
+static void xo_keep(xo_model *m, int e, int ned, const double *K, const double *P) {
+  if (m->keepK) memcpy(m->keepK + (size_t)e * ned * ned, K, sizeof(double) * ned * ned);
+  if (m->keepP) memcpy(m->keepP + (size_t)e * ned, P, sizeof(double) * ned);
+}
 
 static int csr_find(const struct xo_model *m, int row, int col);
 #include "xara_oracle_frame.inc"
@@ -718,6 +727,7 @@ int xo_elem_update_flag(xo_model *m, int compute) {
                             (double(*)[6])(m->sig_t + 6 * h0), (double(*)[36])(m->D_t + 36 * h0),
                             K, P) < 0;
     }
+    xo_keep(m, e, ned, K, P);
     for (int i = 0; i < ned; i++) {
       int r = ids[i];
       if (r < 0) continue;
@@ -730,6 +740,11 @@ int xo_elem_update_flag(xo_model *m, int compute) {
     }
   }
   return -bad;
+}
+
+void xo_keep_element_matrices(xo_model *m, double *K, double *P) {
+  m->keepK = K;
+  m->keepP = P;
 }
 
 int xo_elem_update(xo_model *m) {

@@ -341,3 +341,27 @@ def test_profile_pipelined_sweeps_residual(gpu_mod):
         m.set_system(gpu_mod.XG_SYSTEM_BJPCG)
         xp, _, rr = m.solve(b, rtol=1e-14)
         assert relerr(x, xp) < 1e-9
+
+
+@pytest.mark.parametrize("name", ["quad_8x4", "brick_4x3x2", "frame2d_2x3", "frame3d_1x1x2"])
+def test_element_matrices_match_the_oracle(gpu_mod, name):
+    """xg_elemset_element_matrices (what the element-set shim hands the
+    reference's FE_Elements): every element's tangent and resisting force
+    after an update at a trial displacement of the reference's record,
+    against the oracle's element by element, entry-wise against the
+    element's largest entry within 1e-12."""
+    from oracle import port
+    fx = load(name)
+    desc, _ = model_of(fx)
+    U = fx["step_u"][min(3, len(fx["step_u"]) - 1)]
+    o = port.OracleModel(desc)
+    Ko, Po = o.element_matrices(U)
+    o.close()
+    with gpu_mod.DeviceModel(desc) as m:
+        m.set_trial_disp(U)
+        m.update()
+        K, P = m.element_matrices()
+    kscale = np.abs(Ko).reshape(len(Ko), -1).max(axis=1)[:, None, None]
+    pscale = np.maximum(np.abs(Po).max(axis=1)[:, None], 1e-300)
+    assert np.max(np.abs(K - Ko) / kscale) < RTOL_STATE
+    assert np.max(np.abs(P - Po) / pscale) < RTOL_STATE

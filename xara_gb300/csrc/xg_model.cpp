@@ -2189,6 +2189,43 @@ int xg_elemset_update(xg_model *m, double *csr_vals, double *resid) {
   return 0;
 }
 
+int xg_elemset_element_matrices(const xg_model *m, double *K, double *P) {
+  if (!m) return fail(XG_EINVAL, "null model");
+  const int ned = m->ned;
+  const size_t nk = (size_t)m->ne * m->ke_size();
+  if (K) {
+    std::vector<double> ke(nk);
+    CK(cudaMemcpyAsync(ke.data(), m->d_Ke.p, nk * sizeof(double), cudaMemcpyDeviceToHost,
+                       m->stream));
+    CK(cudaStreamSynchronize(m->stream));
+    for (int e = 0; e < m->ne; e++) {
+      double *out = K + (size_t)e * ned * ned;
+      const double *in = ke.data() + (size_t)e * m->ke_size();
+      if (m->etype != XG_ELE_BRICK) {
+        std::copy(in, in + (size_t)ned * ned, out);
+        continue;
+      }
+      // bricks keep the node-pair blocks a <= b (9 entries each, row-major);
+      // the element tangent is symmetric
+      int p = 0;
+      for (int a = 0; a < 8; a++)
+        for (int b = a; b < 8; b++, p++)
+          for (int i = 0; i < 3; i++)
+            for (int k = 0; k < 3; k++) {
+              const double v = in[p * 9 + 3 * i + k];
+              out[(3 * a + i) * ned + 3 * b + k] = v;
+              out[(3 * b + k) * ned + 3 * a + i] = v;
+            }
+    }
+  }
+  if (P) {
+    CK(cudaMemcpyAsync(P, m->d_Re.p, (size_t)m->ne * ned * sizeof(double),
+                       cudaMemcpyDeviceToHost, m->stream));
+    CK(cudaStreamSynchronize(m->stream));
+  }
+  return 0;
+}
+
 int xg_profile_enable(xg_model *m, int enable) {
   if (!m) return fail(XG_EINVAL, "null model");
   m->prof_on = enable != 0;

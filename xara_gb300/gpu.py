@@ -158,6 +158,19 @@ class DeviceModel:
             _check(r)
         return vals, resid, r
 
+    def element_matrices(self):
+        """Every element's tangent [ne, ned, ned] and resisting force [ne,
+        ned] from the last update (xg_elemset_element_matrices)."""
+        L = lib()
+        L.xg_elemset_element_matrices.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p]
+        d = self.desc
+        ned = (2 if d.elem_type in (_abi.XG_ELE_FBC2D, _abi.XG_ELE_FBC3D) else
+               4 if d.elem_type == _abi.XG_ELE_QUAD else 8) * d.ndf
+        K = np.zeros((d.num_elems, ned, ned))
+        P = np.zeros((d.num_elems, ned))
+        _check(L.xg_elemset_element_matrices(self.h, _p(K), _p(P)))
+        return K, P
+
     def commit(self):
         _check(lib().xg_elemset_commit(self.h))
 
