@@ -1003,6 +1003,130 @@ def run_adjoint(args):
     return line
 
 
+def run_adjoint_fd(args):
+    """Where central differences and the adjoint of the 2,000-step gradient
+    disagree, and why.  For the frames of the adjoint workload (64 frames,
+    one Steel02 per member, the same random direction of every member's Fy,
+    E0, b as the adjoint workload's check):
+
+    * the per-frame relative difference of the adjoint directional
+      derivative and h = 1e-6 central differences over the whole record;
+    * for every frame, the first step at which the +h and -h runs put a
+      Steel02 fiber of the frame on different branches (the Menegotto-Pinto
+      state kon of any fiber differs between the two runs' committed
+      records): past it the response is not differentiable along the
+      perturbation, and the difference quotient measures a branch switch;
+    * for the frames that disagree, adjoint and central differences again,
+      over the record up to the step before that switch;
+    * the adjoint and central differences at h = 1e-4 ... 1e-8 over 300,
+      1,000 and 2,000 steps."""
+    world, rank, local, torch, dist = dist_setup()
+    if rank != 0:
+        return None
+    from xara_gb300 import configs, gpu
+    N, K = args.adj_steps, args.ckpt_every
+    desc, phases = configs.adjoint_frames(n_frames=args.adj_frames, steps=N, seed=0)
+    ph = phases[0]
+    obj = (desc.meta["obj_node"], desc.meta["obj_dof"], desc.meta["obj_weight"])
+    q0 = desc.uni_param.reshape(-1, 12).copy()
+    nf = args.adj_frames
+    efr = np.asarray(desc.meta["member_frame"])
+    d = np.random.default_rng(1).normal(size=q0[:, :3].shape) * np.abs(q0[:, :3])
+    m = gpu.DeviceModel(desc)
+    m.set_system(gpu.XG_SYSTEM_PROFILE_SPD)
+    t0 = time.perf_counter()
+
+    def adjoint(H):
+        gpu.set_uniaxial_params(m, q0)
+        gpu.adjoint_forward(m, ph, H, K, *obj)
+        g = gpu.adjoint_backward(m)
+        return np.array([(g[efr == f] * d[efr == f]).sum() for f in range(nf)])
+
+    def central(H, h):
+        J = {}
+        for sgn in (1, -1):
+            q = q0.copy()
+            q[:, :3] += sgn * h * d
+            gpu.set_uniaxial_params(m, q)
+            gpu.adjoint_forward(m, ph, H, K, *obj)
+            J[sgn] = gpu.adjoint_objective_terms(m, nf)
+        gpu.set_uniaxial_params(m, q0)
+        return (J[1] - J[-1]) / (2 * h)
+
+    def rel(a, b):
+        return np.abs(a - b) / np.maximum(np.abs(b), 1e-300)
+
+    h0 = 1e-6
+    ad_full = adjoint(N)
+    fd_full = central(N, h0)
+    rel_full = rel(ad_full, fd_full)
+    bad = [int(f) for f in np.nonzero(rel_full > 1e-3)[0]]
+
+    # the first step at which the +h and -h runs take different branches
+    runs = []
+    for sgn in (1, -1):
+        mm = gpu.DeviceModel(desc)
+        mm.set_system(gpu.XG_SYSTEM_PROFILE_SPD)
+        q = q0.copy()
+        q[:, :3] += sgn * h0 * d
+        gpu.set_uniaxial_params(mm, q)
+        mm.set_phase(ph)
+        runs.append(mm)
+    first = np.full(nf, -1)
+    ne = desc.num_elems
+    for n in range(N):
+        kons = []
+        for mm in runs:
+            mm.analyze(1)
+            kons.append(mm.fiber_records()[:, 7].reshape(ne, -1))
+        switched = np.unique(efr[(kons[0] != kons[1]).any(axis=1)])
+        new = switched[first[switched] < 0]
+        first[new] = n + 1
+        if (first >= 0).all():
+            break
+    for mm in runs:
+        mm.close()
+
+    # the disagreeing frames before their first branch switch
+    before = {}
+    for H in sorted({int(first[f]) - 1 for f in bad if first[f] > 1}):
+        ad_h, fd_h = adjoint(H), central(H, h0)
+        for f in bad:
+            if int(first[f]) - 1 == H:
+                before[f] = {"steps": H, "adjoint": float(ad_h[f]), "central": float(fd_h[f]),
+                             "relative_difference": float(rel(ad_h[f], fd_h[f]))}
+    # h sweeps over three horizons
+    sweep = {}
+    for H in (300, 1000, N):
+        ad_h = adjoint(H)
+        rows = {}
+        for h in (1e-4, 1e-5, 1e-6, 1e-7, 1e-8):
+            fd_h = central(H, h)
+            r = rel(ad_h, fd_h)
+            rows[f"{h:g}"] = {"median": float(np.median(r)), "within_1e-6": int((r < 1e-6).sum()),
+                              "within_1e-3": int((r < 1e-3).sum()),
+                              "disagreeing_frames_central": [float(fd_h[f]) for f in bad]}
+        sweep[str(H)] = {"adjoint_of_disagreeing_frames": [float(ad_h[f]) for f in bad],
+                         "h": rows}
+    m.close()
+    return {
+        "metric": "adjoint vs central differences, frame by frame", "unit": "relative difference",
+        "config": {"workload": f"gradient of the summed squared roof drift of {nf} 2D steel "
+                               f"frames over {N} Newmark steps w.r.t. every member's Steel02 Fy, "
+                               f"E0, b; one random direction",
+                   "frames": nf, "members": int(ne), "checkpoint_every": K},
+        "whole_record": {"h": h0, "median": float(np.median(rel_full)),
+                         "within_1e-6": int((rel_full < 1e-6).sum()),
+                         "within_1e-3": int((rel_full < 1e-3).sum()),
+                         "disagreeing_frames": bad,
+                         "relative_difference": [float(rel_full[f]) for f in bad]},
+        "first_branch_switch_step": {str(f): int(first[f]) for f in range(nf)},
+        "disagreeing_frames_before_their_switch": {str(f): v for f, v in before.items()},
+        "h_sweep": sweep,
+        "wall_s": time.perf_counter() - t0,
+    }
+
+
 def run_reference_adjoint(args):
     if int(os.environ.get("RANK", "0")) != 0:
         return None
@@ -1271,7 +1395,7 @@ def sub_workloads(args):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--workload", default="frame3d",
-                    choices=["frame3d", "brick", "batch", "adjoint"])
+                    choices=["frame3d", "brick", "batch", "adjoint", "adjoint-fd"])
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
@@ -1294,11 +1418,11 @@ def main():
     args.warmup = max(args.warmup, 3)
     if args.impl == "reference":
         line = {"frame3d": run_reference_frame, "brick": run_reference_brick,
-                "batch": run_reference_batch,
-                "adjoint": run_reference_adjoint}[args.workload](args)
+                "batch": run_reference_batch, "adjoint": run_reference_adjoint,
+                "adjoint-fd": run_reference_adjoint}[args.workload](args)
     else:
         line = {"frame3d": run_frame, "brick": run_brick, "batch": run_batch,
-                "adjoint": run_adjoint}[args.workload](args)
+                "adjoint": run_adjoint, "adjoint-fd": run_adjoint_fd}[args.workload](args)
         if (line is not None and args.workload == "frame3d" and not args.no_sub
                 and line["n_gpus"] == 1):
             line["workloads"] = sub_workloads(args)

@@ -81,10 +81,15 @@ struct PcgSystem {
   double *scalars;        // [8]
   // optional sliced ELL copy of the matrix (thread-per-row SpMV) for rows of
   // at most sell_cap entries, longer rows in chunks of CSR entries, a warp
-  // each; sell_vals null: every row is read from the CSR arrays warp per row
+  // each; sell_vals null: every row is read from the CSR arrays warp per row.
+  // The sliced SpMV computes in float-float (each value and each entry of p
+  // split into two single-precision numbers) on the single-precision pipes;
+  // rows with a value outside 2^-100 .. 2^100 in magnitude stay in FP64.
   const long *sell_off;   // [ceil(n/32)+1] slice offsets
   const int *sell_cols;   // [sell_off[last]]
-  double *sell_vals;      // [sell_off[last]], packed from vals by pcg_factor_blocks
+  float2 *sell_vals;      // [sell_off[last]] (hi, lo), packed from vals by pcg_factor_blocks
+  unsigned char *row_ff;  // [n] 1: the row's values lie in the split's range
+  float2 *p2;             // [n] p split into (hi, lo)
   int sell_cap;
   int nlong, nchunks;     // long rows, their chunks
   const int *chunk_row;   // [nchunks] row of each chunk

@@ -60,7 +60,9 @@ struct xg_linsoe {
   DevArray<int> rp, ci, bs, chunk_row, chunk_beg, long_chunk0, sell_cols, flags;
   DevArray<long> sell_off;
   DevArray<unsigned int> barrier;
-  DevArray<double> vals, b, x, binv, r, z, p, q, partials, scalars, sell_vals, chunk_part;
+  DevArray<double> vals, b, x, binv, r, z, p, q, partials, scalars, chunk_part;
+  DevArray<float2> sell_vals, p2;
+  DevArray<unsigned char> row_ff;
   xg::PcgSystem S{};
   // `system ProfileSPD`: the device LDL', factored once per matrix
   int system = XG_SYSTEM_BJPCG;
@@ -114,7 +116,7 @@ struct xg_linsoe {
     e |= scalars.alloc(8) | barrier.alloc(2) | flags.alloc(4);
     e |= sell_off.upload(off.data(), off.size(), stream);
     e |= sell_cols.upload(cols.data(), cols.size(), stream);
-    e |= sell_vals.alloc(std::max<size_t>(cols.size(), 1));
+    e |= sell_vals.alloc(std::max<size_t>(cols.size(), 1)) | p2.alloc(nv) | row_ff.alloc(nv);
     e |= chunk_row.upload(crow.data(), crow.size(), stream);
     e |= chunk_beg.upload(cbeg.data(), cbeg.size(), stream);
     e |= long_chunk0.upload(lc0.data(), lc0.size(), stream);
@@ -138,6 +140,8 @@ struct xg_linsoe {
     S.sell_off = sell_off.p;
     S.sell_cols = sell_cols.p;
     S.sell_vals = sell_vals.p;
+    S.p2 = p2.p;
+    S.row_ff = row_ff.p;
     S.sell_cap = kCap;
     S.nlong = (int)lc0.size() - 1;
     S.nchunks = (int)crow.size();

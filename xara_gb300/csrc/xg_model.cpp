@@ -175,7 +175,8 @@ struct xg_model {
   // half of the free device memory)
   DBuf<long> d_sell_off;
   DBuf<int> d_sell_cols;
-  DBuf<double> d_sell_vals, d_chunk_part;
+  DBuf<double> d_sell_vals, d_chunk_part, d_p2;   // (hi, lo) float pairs, 8 bytes each
+  DBuf<unsigned char> d_row_ff;
   DBuf<double> d_geo;   // bricks: per-point shape-function gradients and Jacobian determinant
   DBuf<int> d_chunk_row, d_chunk_beg, d_long_chunk0;
   bool sell_tried = false;
@@ -1442,6 +1443,8 @@ int xg_model::ensure_pcg_sell() {
   RET(d_sell_off.upload(off.data(), off.size(), stream));
   RET(d_sell_cols.upload(cols.data(), cols.size(), stream));
   RET(d_sell_vals.alloc(cols.size()));
+  RET(d_p2.alloc(neq));
+  RET(d_row_ff.alloc(neq));
   const int nch = (int)chunk_row.size();
   RET(d_chunk_row.upload(chunk_row.data(), chunk_row.size(), stream));
   RET(d_chunk_beg.upload(chunk_beg.data(), chunk_beg.size(), stream));
@@ -1449,7 +1452,9 @@ int xg_model::ensure_pcg_sell() {
   RET(d_chunk_part.alloc(std::max(nch, 1)));
   pcg.sell_off = d_sell_off.p;
   pcg.sell_cols = d_sell_cols.p;
-  pcg.sell_vals = d_sell_vals.p;
+  pcg.sell_vals = reinterpret_cast<float2 *>(d_sell_vals.p);
+  pcg.p2 = reinterpret_cast<float2 *>(d_p2.p);
+  pcg.row_ff = d_row_ff.p;
   pcg.sell_cap = kCap;
   pcg.nlong = (int)long_chunk0.size() - 1;
   pcg.nchunks = nch;

@@ -95,42 +95,95 @@ __device__ __forceinline__ double spmv_row(const PcgSystem &S, int row, const do
   return s;  // lane 0
 }
 
+// Float-float arithmetic on the single-precision pipes (GB300's FP64 pipe
+// is the bottleneck of an FP64 SpMV: one FMA per non-zero).  A double v is
+// kept as hi + lo, hi = v rounded to single precision and lo = (v - hi)
+// rounded: 48 of its 53 bits.  A product of two such pairs is
+// hi_a hi_x exactly (the rounding error of the single-precision product
+// recovered by an FMA: Dekker's TwoProduct, 1971, with a fused
+// multiply-add) plus the cross terms hi_a lo_x + lo_a hi_x in single
+// precision (lo_a lo_x, below 2^-48 of the product, is dropped); sums add
+// the high parts exactly (Knuth's TwoSum, TAOCP vol. 2, 4.2.2) and collect
+// every error in the low part.  Each product is good to about 2^-46 of its
+// magnitude.  __fmul_rn keeps the compiler from fusing the product into the
+// following addition, which would break the error-free transformations.
+__device__ __forceinline__ float2 split2(double v) {
+  const float hi = __double2float_rn(v);
+  return make_float2(hi, __double2float_rn(v - (double)hi));
+}
+
+__device__ __forceinline__ void ff_madd(float2 a, float2 x, float &sh, float &sl) {
+  const float p = __fmul_rn(a.x, x.x);
+  float e = __fmaf_rn(a.x, x.x, -p);
+  e = __fmaf_rn(a.x, x.y, e);
+  e = __fmaf_rn(a.y, x.x, e);
+  const float t = __fadd_rn(sh, p);
+  const float bp = __fsub_rn(t, sh);
+  const float err = __fadd_rn(__fsub_rn(sh, __fsub_rn(t, bp)), __fsub_rn(p, bp));
+  sh = t;
+  sl = __fadd_rn(sl, __fadd_rn(err, e));
+}
+
+// Whether a value can be split without leaving single precision's range
+// (products of two split values stay finite and normal).
+__device__ __forceinline__ bool ff_range(double v) {
+  const double a = fabs(v);
+  return a == 0.0 || (a >= 0x1p-100 && a < 0x1p100);
+}
+
+// Row of (A x) from the CSR arrays in FP64, one thread.
+__device__ __forceinline__ double csr_row64(const PcgSystem &S, int row, const double *x) {
+  double s = 0.0;
+  for (int k = S.rowptr[row]; k < S.rowptr[row + 1]; k++) s = fma(S.vals[k], x[S.colidx[k]], s);
+  return s;
+}
+
 // Sliced ELL copy of the CSR matrix (thread per row): slice s holds rows
 // 32s .. 32s+31 column-major over the slice's longest row, entry k of row r
 // at sell_off[r/32] + 32k + r%32, so a warp's 32 rows load each entry
 // position with one coalesced access.  Each row is summed in its CSR order
-// into four interleaved partial sums, a fixed order.
-__device__ __forceinline__ double spmv_sell(const PcgSystem &S, int row, const double *x) {
-  const int b = S.rowptr[row], len = S.rowptr[row + 1] - b;
+// into four interleaved float-float partial sums, a fixed order, against
+// p split into (hi, lo) (x2); rows whose values the split cannot hold, or
+// every row when fp64 is set, in FP64 against x.
+__device__ __forceinline__ double spmv_sell(const PcgSystem &S, int row, const double *x,
+                                            const float2 *x2, bool fp64) {
+  if (fp64 || !S.row_ff[row]) return csr_row64(S, row, x);
+  const int len = S.rowptr[row + 1] - S.rowptr[row];
   const long base = S.sell_off[row >> 5] + (row & 31);
   const int *cp = S.sell_cols + base;
-  const double *vp = S.sell_vals + base;
-  double a0 = 0.0, a1 = 0.0, a2 = 0.0, a3 = 0.0;
+  const float2 *vp = S.sell_vals + base;
+  float h0 = 0.f, l0 = 0.f, h1 = 0.f, l1 = 0.f, h2 = 0.f, l2 = 0.f, h3 = 0.f, l3 = 0.f;
   int k = 0;
   for (; k + 4 <= len; k += 4) {
     const int c0 = __ldcs(cp + 32 * k), c1 = __ldcs(cp + 32 * (k + 1));
     const int c2 = __ldcs(cp + 32 * (k + 2)), c3 = __ldcs(cp + 32 * (k + 3));
-    const double v0 = __ldcs(vp + 32 * k), v1 = __ldcs(vp + 32 * (k + 1));
-    const double v2 = __ldcs(vp + 32 * (k + 2)), v3 = __ldcs(vp + 32 * (k + 3));
-    a0 = fma(v0, x[c0], a0);
-    a1 = fma(v1, x[c1], a1);
-    a2 = fma(v2, x[c2], a2);
-    a3 = fma(v3, x[c3], a3);
+    const float2 v0 = __ldcs(vp + 32 * k), v1 = __ldcs(vp + 32 * (k + 1));
+    const float2 v2 = __ldcs(vp + 32 * (k + 2)), v3 = __ldcs(vp + 32 * (k + 3));
+    ff_madd(v0, x2[c0], h0, l0);
+    ff_madd(v1, x2[c1], h1, l1);
+    ff_madd(v2, x2[c2], h2, l2);
+    ff_madd(v3, x2[c3], h3, l3);
   }
-  for (; k < len; k++) a0 = fma(__ldcs(vp + 32 * k), x[__ldcs(cp + 32 * k)], a0);
-  return (a0 + a1) + (a2 + a3);
+  for (; k < len; k++) ff_madd(__ldcs(vp + 32 * k), x2[__ldcs(cp + 32 * k)], h0, l0);
+  return (((double)h0 + (double)l0) + ((double)h1 + (double)l1)) +
+         (((double)h2 + (double)l2) + ((double)h3 + (double)l3));
 }
 
 // f(row, (A x)[row]) for this thread's rows: thread per row over the sliced
 // ELL copy (kSell; rows longer than S.sell_cap are left to
 // long_row_chunks), else warp per CSR row (lane 0 calls f).
+// With kSell: x2 is x split into (hi, lo) for the float-float SpMV, or null
+// for FP64 throughout (the initial residual, or a p outside the split's
+// range).
 template <bool kSell, typename F>
-__device__ __forceinline__ void for_rows_Ax(const PcgSystem &S, const double *x, F f) {
+__device__ __forceinline__ void for_rows_Ax(const PcgSystem &S, const double *x,
+                                            const float2 *x2, F f) {
   const int gtid = blockIdx.x * blockDim.x + threadIdx.x;
   const int gthreads = gridDim.x * blockDim.x;
   if (kSell) {
     for (int row = gtid; row < S.n; row += gthreads)
-      if (S.rowptr[row + 1] - S.rowptr[row] <= S.sell_cap) f(row, spmv_sell(S, row, x));
+      if (S.rowptr[row + 1] - S.rowptr[row] <= S.sell_cap)
+        f(row, spmv_sell(S, row, x, x2, x2 == nullptr));
   } else {
     const int lane = threadIdx.x & 31;
     for (int row = gtid >> 5; row < S.n; row += gthreads >> 5) {
@@ -208,7 +261,7 @@ __global__ void __launch_bounds__(kPcgThreads) k_pcg(PcgSystem S, const double *
   double *part = S.partials;          // [3*nb]
 
   // r = b - A x ; (x is the initial guess)
-  for_rows_Ax<kSell>(S, x, [&](int row, double ax) { S.r[row] = b[row] - ax; });
+  for_rows_Ax<kSell>(S, x, nullptr, [&](int row, double ax) { S.r[row] = b[row] - ax; });
   if (kSell) long_row_chunks(S, x, [&](int c, int, double t) { S.chunk_part[c] = t; });
   if (!grid_barrier(S.barrier, flags)) return;
   if (kSell && S.nlong > 0) {
@@ -216,17 +269,23 @@ __global__ void __launch_bounds__(kPcgThreads) k_pcg(PcgSystem S, const double *
     if (!grid_barrier(S.barrier, flags)) return;
   }
   double lrz = 0.0, lbb = 0.0, lrr = 0.0;
+  bool p_out = false;                 // an entry of p outside the split's range
   for (int k = gtid; k < S.nblk; k += gthreads) {
     const BlockRange br = block_range(S, k);
     precondition_block(S, k, br);
     for (int i = br.b; i < br.b + br.m; i++) {
       S.p[i] = S.z[i];
+      if (kSell) {
+        S.p2[i] = split2(S.z[i]);
+        p_out |= !ff_range(S.z[i]);
+      }
       lrz += S.r[i] * S.z[i];
       lbb += b[i] * b[i];
       lrr += S.r[i] * S.r[i];
     }
   }
   // p = z is read across blocks in the next SpMV: barrier before it
+  if (kSell && p_out) flags[2] = 1;   // FP64 SpMV from now on (read after a barrier)
   lrz = block_reduce(lrz, smem);
   if (threadIdx.x == 0) part[blockIdx.x] = lrz;
   lbb = block_reduce(lbb, smem);
@@ -247,7 +306,7 @@ __global__ void __launch_bounds__(kPcgThreads) k_pcg(PcgSystem S, const double *
     // q = A p ; pq = p.q
     if (!grid_barrier(S.barrier, flags)) return;   // partial sums consumed
     double lpq = 0.0;
-    for_rows_Ax<kSell>(S, S.p, [&](int row, double ap) {
+    for_rows_Ax<kSell>(S, S.p, flags[2] ? nullptr : S.p2, [&](int row, double ap) {
       S.q[row] = ap;
       lpq += ap * S.p[row];
     });
@@ -288,10 +347,19 @@ __global__ void __launch_bounds__(kPcgThreads) k_pcg(PcgSystem S, const double *
     if (sqrt(rr) <= rtol * bnorm) { status = 1; break; }
     const double beta = rz_new / rz;
     rz = rz_new;
+    p_out = false;
     for (int k = gtid; k < S.nblk; k += gthreads) {
       const BlockRange br = block_range(S, k);
-      for (int i = br.b; i < br.b + br.m; i++) S.p[i] = S.z[i] + beta * S.p[i];
+      for (int i = br.b; i < br.b + br.m; i++) {
+        const double pi = S.z[i] + beta * S.p[i];
+        S.p[i] = pi;
+        if (kSell) {
+          S.p2[i] = split2(pi);
+          p_out |= !ff_range(pi);
+        }
+      }
     }
+    if (kSell && p_out) flags[2] = 1;
   }
   if (blockIdx.x == 0 && threadIdx.x == 0) {
     S.scalars[3] = it;
@@ -350,14 +418,21 @@ __global__ void k_factor_blocks(PcgSystem S) {
     for (int j = 0; j < m; j++) B[6 * i + j] = A[i][m + j];
 }
 
-// CSR values into the sliced ELL copy, thread per row
+// CSR values into the sliced ELL copy, split into (hi, lo), thread per row;
+// row_ff records whether every value of the row lies in the split's range.
 __global__ void k_pack_sell(PcgSystem S) {
   const int row = blockIdx.x * blockDim.x + threadIdx.x;
   if (row >= S.n) return;
   const int b = S.rowptr[row], len = S.rowptr[row + 1] - b;
   if (len > S.sell_cap) return;
-  double *vp = S.sell_vals + S.sell_off[row >> 5] + (row & 31);
-  for (int k = 0; k < len; k++) vp[32 * k] = S.vals[b + k];
+  float2 *vp = S.sell_vals + S.sell_off[row >> 5] + (row & 31);
+  bool ok = true;
+  for (int k = 0; k < len; k++) {
+    const double v = S.vals[b + k];
+    ok = ok && ff_range(v);
+    vp[32 * k] = split2(v);
+  }
+  S.row_ff[row] = ok ? 1 : 0;
 }
 
 int g_max_blocks = -1, g_sell_max_blocks = -1;
