@@ -1123,6 +1123,9 @@ int xo_run_phase(xo_model *m, const xg_phase_desc *ph, double *step_u, double *s
       double dlambda = ph->dc_incr / dUahat;
       m->time += dlambda;
       xo_incr_disp(m, dUhat, dlambda);
+      /* applyLoadDomain(currentLambda): the Transformation handler enforces
+         the sp values (DisplacementControl.cpp:213) */
+      if (d->handler == XG_HANDLER_TRANSFORMATION) xo_enforce_sps(m);
       xo_elem_update(m);
     }
     xo_form_fext(m, m->time);
@@ -1139,6 +1142,8 @@ int xo_run_phase(xo_model *m, const xg_phase_desc *ph, double *step_u, double *s
         m->time += dLambda;
       }
       xo_incr_disp(m, m->dU, 1.0);
+      if (ph->integrator == XG_INT_DISP_CONTROL && d->handler == XG_HANDLER_TRANSFORMATION)
+        xo_enforce_sps(m);   /* DisplacementControl::update's applyLoadDomain (:269) */
       xo_elem_update(m);
       xo_form_fext(m, m->time);
       for (int i = 0; i < n; i++) m->B[i] = m->fext[i] - m->resid[i];

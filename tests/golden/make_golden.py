@@ -10,6 +10,7 @@ has no reference; tests there read these fixtures.
 Usage: python tests/golden/make_golden.py        (the small fixtures)
        python tests/golden/make_golden.py c1     (frame3d_c1: the full-size 3D RC
                                                   frame pushover, about half an hour)
+       python tests/golden/make_golden.py settle (frame2d_settle_2x3 alone)
 """
 import os
 import sys
@@ -157,11 +158,22 @@ def c1_pushover(name="frame3d_c1", sample=50_000, seed=11, every=10):
          ref_seconds=np.array([r.elem_seconds, r.solve_seconds, r.step_seconds]))
 
 
+def settlement_fixture():
+    """The 2D steel frame with a support settlement imposed through the
+    Transformation handler (gravity and settlement by LoadControl, then the
+    pushover), every solve of the first gravity step captured."""
+    model_fixture("frame2d_settle_2x3", configs.settlement_frame_2d, (2, 3), {},
+                  capture_steps=(0,))
+
+
 def main():
     if not ref.available():
         sys.exit("oracle/_ref/libxara_ref.so missing: run python oracle/build_ref.py")
     if sys.argv[1:] == ["c1"]:
         c1_pushover()
+        return
+    if sys.argv[1:] == ["settle"]:
+        settlement_fixture()
         return
     j2_paths()
     model_fixture("quad_8x4", configs.quad_block, (8, 4), {}, capture_steps=(0, 6))
@@ -184,6 +196,7 @@ def main():
     revert_fixture("revert_frame3d_1x1x2", configs.rc_frame_3d, (1, 1, 2),
                    {"col_fibers": 40, "beam_fibers": 24, "steps": 10, "pdelta": 1})
     revert_fixture("revert_quad_8x4", configs.quad_block, (8, 4), {}, scale=1e-4)
+    settlement_fixture()
 
 
 if __name__ == "__main__":

@@ -10,7 +10,7 @@ from golden_util import load, model_of
 from xara_gb300 import configs, gpu
 
 MODELS = ["quad_8x4", "quad_64x16", "brick_4x3x2", "brick_8x8x4", "frame2d_2x3",
-          "frame3d_1x1x2", "frame3d_2x1x3"]
+          "frame3d_1x1x2", "frame3d_2x1x3", "frame2d_settle_2x3"]
 
 
 def test_exports_every_declared_symbol():

@@ -64,7 +64,8 @@ def test_replay_element_state(name):
         o.close()
 
 
-FRAMES = ["frame2d_2x3", "frame3d_1x1x2", "frame3d_2x1x3", "frame2d_eq_2x3", "frame2d_pd_2x3"]
+FRAMES = ["frame2d_2x3", "frame3d_1x1x2", "frame3d_2x1x3", "frame2d_eq_2x3", "frame2d_pd_2x3",
+          "frame2d_settle_2x3"]
 
 
 def test_uniaxial_paths():
@@ -90,7 +91,8 @@ def test_frame_numbering_and_history(name):
     assert np.array_equal(its, fx["step_iters"])
 
 
-@pytest.mark.parametrize("name", ["frame2d_2x3", "frame3d_1x1x2", "frame2d_pd_2x3"])
+@pytest.mark.parametrize("name", ["frame2d_2x3", "frame3d_1x1x2", "frame2d_pd_2x3",
+                                  "frame2d_settle_2x3"])
 def test_frame_replay_first_step(name):
     """Every Newton iteration of the first gravity step, replayed in order
     (the force-based element state is incremental, so the trial displacements

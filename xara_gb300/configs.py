@@ -24,7 +24,8 @@ Workloads (all FP64):
 import numpy as np
 
 from ._abi import (ModelDesc, PhaseDesc, XG_ELE_BRICK, XG_ELE_QUAD,
-                   XG_HANDLER_PLAIN, XG_INT_DISP_CONTROL, XG_INT_NEWMARK,
+                   XG_HANDLER_PLAIN, XG_HANDLER_TRANSFORMATION, XG_INT_DISP_CONTROL,
+                   XG_INT_NEWMARK,
                    XG_TEST_NORM_DISP_INCR)
 
 # nDMaterial J2Plasticity K G sigma0 sigma_inf delta H eta rho
@@ -242,6 +243,33 @@ def steel_frame_2d(bays=2, stories=3, bay=6.0, story=3.5, nfib=40, fy=350e6, E=2
                   max_iter=max_iter),
     ]
     return desc, phases
+
+
+def settlement_frame_2d(bays=2, stories=3, settlement=-0.03, steps=12, grav_steps=10,
+                        **kw):
+    """The 2D steel frame of ``steel_frame_2d`` under `constraints
+    Transformation`: its middle (or second) base node settles vertically by
+    ``settlement`` metres, imposed as an `sp` in the gravity pattern and so
+    applied with the gravity load by LoadControl; after `loadConst` the
+    settled support holds while the pushover runs."""
+    desc, phases = steel_frame_2d(bays, stories, steps=steps, grav_steps=grav_steps, **kw)
+    a = desc.arrays
+    settle_node = bays // 2 + 1
+    sp_node = np.asarray(a["sp_node"]).copy()
+    sp_dof = np.asarray(a["sp_dof"]).copy()
+    sp_pat = np.asarray(a["sp_pattern"]).copy()
+    sp_val = np.asarray(a["sp_value"]).copy()
+    k = int(np.nonzero((sp_node == settle_node) & (sp_dof == 1))[0][0])
+    sp_pat[k] = 0
+    sp_val[k] = settlement
+    kw_ = {key: v for key, v in a.items() if v is not None}
+    kw_.update(sp_pattern=sp_pat, sp_value=sp_val)
+    out = ModelDesc(ndm=desc.ndm, ndf=desc.ndf, elem_type=desc.elem_type,
+                    geom_transf=desc.geom_transf, fbc_num_ip=desc.fbc_num_ip,
+                    handler=XG_HANDLER_TRANSFORMATION, **kw_)
+    out.meta = dict(desc.meta, workload=f"2D steel frame {bays}x{stories}, support settlement "
+                                        f"{settlement} m (Transformation handler)")
+    return out, phases
 
 
 def rc_section_fibers(b, h, cover, n_core_y, n_core_z, n_cover, n_bars, bar_area):

@@ -228,6 +228,11 @@ int launch_axpy(int n, double a, const double *x, double *y, cudaStream_t s);
 int launch_scatter_incr(int nu, const int *eqn, const double *dU, double f, double *U,
                         cudaStream_t s);
 int launch_sub(int n, const double *a, const double *b, double *out, cudaStream_t s);
+// the load factor of each of the eight load patterns
+struct SpFactors { double f[8]; };
+// U[idx[k]] = lam.f[pat[k]] * val[k] for the n imposed single-point constraints
+int launch_enforce_sps(int n, const int *idx, const int *pat, const double *val,
+                       const SpFactors &lam, double *U, cudaStream_t s);
 // deterministic 2-norm squared of x (n) into *out (device), partials scratch
 int launch_norm2(int n, const double *x, double *partials, double *out, cudaStream_t s);
 

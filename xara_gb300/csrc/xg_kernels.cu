@@ -669,6 +669,13 @@ __global__ void k_scatter_incr(int nu, const int *eqn, const double *dU, double 
   if (e >= 0) U[i] += f * dU[e];
 }
 
+// TransformationDOF_Group::enforceSPs: U[idx[k]] = lam[pat[k]] * val[k]
+__global__ void k_enforce_sps(int n, const int *idx, const int *pat, const double *val,
+                              SpFactors lam, double *U) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k < n) U[idx[k]] = lam.f[pat[k]] * val[k];
+}
+
 __global__ void k_sub(int n, const double *a, const double *b, double *out) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i < n) out[i] = a[i] - b[i];
@@ -769,6 +776,12 @@ int launch_scatter_incr(int nu, const int *eqn, const double *dU, double f, doub
                         cudaStream_t s) {
   if (nu == 0) return 0;
   k_scatter_incr<<<nblocks(nu), kThreads, 0, s>>>(nu, eqn, dU, f, U);
+  return check_launch();
+}
+int launch_enforce_sps(int n, const int *idx, const int *pat, const double *val,
+                       const SpFactors &lam, double *U, cudaStream_t s) {
+  if (n == 0) return 0;
+  k_enforce_sps<<<nblocks(n), kThreads, 0, s>>>(n, idx, pat, val, lam, U);
   return check_launch();
 }
 int launch_sub(int n, const double *a, const double *b, double *out, cudaStream_t s) {

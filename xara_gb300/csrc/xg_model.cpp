@@ -133,6 +133,12 @@ struct xg_model {
   std::vector<double> j2;
   int num_sp = 0, num_mp = 0, num_loads = 0, handler = 0;
   std::vector<int> sp_node, sp_dof, sp_pat, mp_r, mp_c, mp_dof, load_node, load_pat;
+  // Transformation handler: the imposed single-point constraints (sp in a
+  // load pattern) as (U index, pattern, value) on the device
+  int num_isp = 0;
+  DBuf<int> d_isp_idx, d_isp_pat;
+  DBuf<double> d_isp_val;
+  int enforce_sps(double t);
   std::vector<double> sp_val, load_val;
 
   // numbering
@@ -751,6 +757,24 @@ int xg_model::upload(const HostGather &gk_h, const HostGather &gr_h) {
       }
     }
   if (!F.empty()) RET(d_Fref.upload(F.data(), F.size(), s));
+  if (handler == XG_HANDLER_TRANSFORMATION) {
+    // the imposed values: U index (sp_node holds node indices by now),
+    // pattern and reference value of every sp inside a load pattern
+    std::vector<int> idx, pat;
+    std::vector<double> val;
+    for (int k = 0; k < num_sp; k++)
+      if (sp_pat[k] >= 0) {
+        idx.push_back(sp_node[k] * ndf + sp_dof[k]);
+        pat.push_back(sp_pat[k]);
+        val.push_back(sp_val[k]);
+      }
+    num_isp = (int)idx.size();
+    if (num_isp) {
+      RET(d_isp_idx.upload(idx.data(), idx.size(), s));
+      RET(d_isp_pat.upload(pat.data(), pat.size(), s));
+      RET(d_isp_val.upload(val.data(), val.size(), s));
+    }
+  }
   RET(upload_dynamics());
   if (frames()) {
     RET(upload_frames());
@@ -1604,11 +1628,15 @@ int xg_model::step(xg_step_stats *st) {
   last_solver_iters = 0;
   const int nu = nn * ndf;
   const double t_commit = time;
+  const bool transformation = handler == XG_HANDLER_TRANSFORMATION;
   if (phase.integrator == XG_INT_LOAD_CONTROL) {
-    // LoadControl::newStep (Static/LoadControl.cpp:70-100); PlainHandler
-    // updates no element before formUnbalance
+    // LoadControl::newStep (Static/LoadControl.cpp:70-100):
+    // applyLoadDomain; PlainHandler updates no element before
+    // formUnbalance, the Transformation handler enforces the sp values and
+    // updates every element
     time += phase.d_lambda;
-    RET(element_state(false));
+    if (transformation) RET(enforce_sps(time));
+    RET(element_state(transformation));
   } else {
     // DisplacementControl::newStep (Static/DisplacementControl.cpp:121-200)
     RET(element_state(false));
@@ -1619,6 +1647,7 @@ int xg_model::step(xg_step_stats *st) {
     const double dlambda = phase.dc_incr / dUahat;
     time += dlambda;
     RET(launch_scatter_incr(nu, d_eqn.p, d_dUhat.p, dlambda, d_U.p, s));
+    if (transformation) RET(enforce_sps(time));   // applyLoadDomain(currentLambda)
     RET(element_state(true));
   }
   RET(form_fext(time));
@@ -1639,6 +1668,7 @@ int xg_model::step(xg_step_stats *st) {
       time += dLambda;
     }
     RET(launch_scatter_incr(nu, d_eqn.p, d_dU.p, 1.0, d_U.p, s));
+    if (transformation && phase.integrator == XG_INT_DISP_CONTROL) RET(enforce_sps(time));
     RET(element_state(true));
     RET(form_fext(time));
     RET(launch_sub(neq, d_fext.p, d_resid.p, d_B.p, s));
@@ -1664,6 +1694,18 @@ int xg_model::step(xg_step_stats *st) {
   RET(commit_state());
   time_c = time;
   return 0;
+}
+
+// TransformationConstraintHandler::applyLoad -> enforceSPs
+// (analysis/handler/TransformationConstraintHandler.cpp:456-480): every
+// imposed sp sets its dof's trial displacement to its pattern's load
+// factor at time t times its value; the caller then updates every element
+// (FE_Element::updateElement there).
+int xg_model::enforce_sps(double t) {
+  if (num_isp == 0) return 0;
+  SpFactors lam{};
+  for (int p = 0; p < 8; p++) lam.f[p] = lambda_of(p, t);
+  return launch_enforce_sps(num_isp, d_isp_idx.p, d_isp_pat.p, d_isp_val.p, lam, d_U.p, stream);
 }
 
 int xg_model::commit_state() {
@@ -2023,11 +2065,17 @@ static int plan_model(const xg_model_desc *d, xg_model **out) {
     return fail(XG_EINVAL, "empty model");
   if (d->num_elems > 0 && (!d->elem_tag || !d->elem_conn || !d->elem_mat || (!fr && !d->j2_param)))
     return fail(XG_EINVAL, "missing element arrays");
-  if (d->handler != XG_HANDLER_PLAIN)
-    return fail(XG_EINVAL, "only the Plain constraint handler is supported");
-  for (int i = 0; i < d->num_sp; i++)
-    if (d->sp_pattern && d->sp_pattern[i] >= 0)
+  if (d->handler != XG_HANDLER_PLAIN && d->handler != XG_HANDLER_TRANSFORMATION)
+    return fail(XG_EINVAL, "constraint handler %d not supported", d->handler);
+  if (d->handler == XG_HANDLER_TRANSFORMATION && d->num_mp > 0)
+    return fail(XG_EINVAL, "the Transformation handler is supported with single-point "
+                "constraints only (no equalDOF)");
+  for (int i = 0; i < d->num_sp; i++) {
+    if (!d->sp_pattern || d->sp_pattern[i] < 0) continue;
+    if (d->handler != XG_HANDLER_TRANSFORMATION)
       return fail(XG_EINVAL, "imposed sp values need the Transformation handler");
+    if (d->sp_pattern[i] >= 8) return fail(XG_EINVAL, "sp pattern must be in [0, 8)");
+  }
   auto *m = new xg_model();
   m->ndm = d->ndm; m->ndf = d->ndf; m->nn = d->num_nodes; m->ne = d->num_elems;
   m->etype = d->elem_type;
@@ -2114,6 +2162,10 @@ static int plan_model(const xg_model_desc *d, xg_model **out) {
   if (m->num_sp) {
     m->sp_node.assign(d->sp_node, d->sp_node + m->num_sp);
     m->sp_dof.assign(d->sp_dof, d->sp_dof + m->num_sp);
+    if (d->sp_pattern) m->sp_pat.assign(d->sp_pattern, d->sp_pattern + m->num_sp);
+    else m->sp_pat.assign(m->num_sp, -1);
+    if (d->sp_value) m->sp_val.assign(d->sp_value, d->sp_value + m->num_sp);
+    else m->sp_val.assign(m->num_sp, 0.0);
   }
   if (m->num_mp) {
     m->mp_r.assign(d->mp_retained, d->mp_retained + m->num_mp);

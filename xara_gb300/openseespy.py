@@ -19,7 +19,8 @@ Concrete02 and Elastic fibers, Lobatto integration, Linear and PDelta
 transformations; one element type per model), ``fix``, ``equalDOF``,
 ``mass``, Plain patterns with a Linear series (nodal loads, ``sp``),
 ``pattern UniformExcitation`` with a Path series, ``rayleigh``,
-``constraints Plain``, ``numberer RCM``, ``system
+``constraints Plain|Transformation`` (Transformation with single-point
+constraints only: imposed `sp` values, no ``equalDOF``), ``numberer RCM``, ``system
 ProfileSPD|CudaBJPCG``, ``test NormDispIncr|NormUnbalance``, ``algorithm
 Newton``, ``integrator LoadControl|DisplacementControl|Newmark``,
 ``loadConst``, ``nodeDisp|nodeVel|nodeAccel``, ``getTime``, ``recorder
@@ -36,7 +37,7 @@ import numpy as np
 
 from . import gpu
 from ._abi import (ModelDesc, PhaseDesc, XG_ELE_BRICK, XG_ELE_FBC2D, XG_ELE_FBC3D, XG_ELE_QUAD,
-                   XG_HANDLER_PLAIN, XG_INT_DISP_CONTROL,
+                   XG_HANDLER_PLAIN, XG_HANDLER_TRANSFORMATION, XG_INT_DISP_CONTROL,
                    XG_INT_LOAD_CONTROL, XG_INT_NEWMARK, XG_REC_ACCEL, XG_REC_DISP,
                    XG_REC_ENVELOPE, XG_REC_NODE, XG_REC_VEL, XG_SYSTEM_BJPCG,
                    XG_SYSTEM_PROFILE_SPD, XG_TEST_NORM_DISP_INCR, XG_TEST_NORM_UNBALANCE,
@@ -328,10 +329,7 @@ def rayleigh(alphaM, betaK, betaKinit, betaKcomm):
 # analysis settings
 # ---------------------------------------------------------------------------
 def constraints(kind, *args):
-    if kind == "Transformation":
-        _unsupported("constraints Transformation (the device path numbers with the Plain "
-                     "handler: equalDOF ties share equations, fixed dofs are removed)")
-    h = {"Plain": XG_HANDLER_PLAIN}.get(kind)
+    h = {"Plain": XG_HANDLER_PLAIN, "Transformation": XG_HANDLER_TRANSFORMATION}.get(kind)
     if h is None:
         _unsupported(f"constraints {kind}")
     if h != _S.handler:
