@@ -41,15 +41,19 @@ def _quad_script(nx=8, ny=4, steps=4):
     return master
 
 
-def _frame_script(bays=2, stories=3, nfib=40, steps=5, grav_steps=4, gravity=-150e3):
+def _frame_script(bays=2, stories=3, nfib=40, steps=5, grav_steps=4, gravity=-150e3,
+                  settle=None):
+    """settle: a vertical settlement (metres) of the middle base node, an
+    `sp` of the gravity pattern under `constraints Transformation`."""
     ops.wipe()
     ops.model("basic", "-ndm", 2, "-ndf", 3)
     nx = bays + 1
     for j in range(stories + 1):
         for i in range(nx):
             ops.node(j * nx + i + 1, i * 6.0, j * 3.5)
+    mid = bays // 2 + 1
     for i in range(nx):
-        ops.fix(i + 1, 1, 1, 1)
+        ops.fix(i + 1, 1, 0 if (settle is not None and i + 1 == mid) else 1, 1)
     ops.uniaxialMaterial("Steel02", 1, 350e6, 200e9, 0.01, 18.0, 0.925, 0.15)
     for tag, dims in ((1, (0.45, 0.3, 0.022, 0.014)), (2, (0.5, 0.2, 0.016, 0.010))):
         ops.section("Fiber", tag)
@@ -71,7 +75,9 @@ def _frame_script(bays=2, stories=3, nfib=40, steps=5, grav_steps=4, gravity=-15
     ops.pattern("Plain", 1, 1)
     for n in range(nx + 1, (stories + 1) * nx + 1):
         ops.load(n, 0.0, gravity, 0.0)
-    ops.constraints("Plain")
+    if settle is not None:
+        ops.sp(mid, 2, settle)
+    ops.constraints("Plain" if settle is None else "Transformation")
     ops.numberer("RCM")
     ops.system("ProfileSPD")
     ops.test("NormDispIncr", 1e-10, 50)
@@ -190,3 +196,26 @@ def test_quad_commands_run_like_the_builders(need_gpu):
         U, _, _ = m.run(phases)
     i = list(desc.node_tag).index(master)
     np.testing.assert_array_equal(u, U[-1, 2 * i:2 * i + 2])
+
+
+@pytest.mark.gpu
+def test_transformation_commands_run_like_the_builders(need_gpu):
+    """`constraints Transformation` with a support settlement imposed by an
+    `sp` inside the gravity pattern: the same displacements, bit for bit, as
+    the builder's model of it (configs.settlement_frame_2d)."""
+    from xara_gb300 import gpu
+    roof, nx = _frame_script(settle=-0.03)
+    assert ops.analyze(4) == 0
+    _lateral(roof, nx)
+    assert ops.analyze(5) == 0
+    u_roof = ops.nodeDisp(roof)
+    u_mid = ops.nodeDisp(2)
+    ops.wipe()
+    desc, phases = configs.settlement_frame_2d(2, 3, settlement=-0.03, steps=5, grav_steps=4)
+    with gpu.DeviceModel(desc) as m:
+        U, _, _ = m.run(phases)
+    tags = list(desc.node_tag)
+    i, k = tags.index(roof), tags.index(2)
+    np.testing.assert_array_equal(u_roof, U[-1, 3 * i:3 * i + 3])
+    np.testing.assert_array_equal(u_mid, U[-1, 3 * k:3 * k + 3])
+    assert u_mid[1] == pytest.approx(-0.03, rel=1e-12)
