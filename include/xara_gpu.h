@@ -45,6 +45,7 @@ extern "C" {
 #define XG_UNI_STEEL02     1   /* material/uniaxial/steel/Steel02.cpp      */
 #define XG_UNI_CONCRETE02  2   /* material/uniaxial/concrete/Concrete02.cpp */
 #define XG_UNI_ELASTIC     3   /* linear elastic fiber (known-answer tests) */
+#define XG_UNI_STEEL01     4   /* material/uniaxial/steel/Steel01.cpp      */
 
 /* constraint handlers (analysis/handler) */
 #define XG_HANDLER_PLAIN           0  /* PlainHandler.cpp                   */
@@ -68,7 +69,8 @@ extern "C" {
 #define XG_J2_NPARAM 8         /* K G sigma0 sigma_inf delta H eta rho */
 /* uniaxial parameter row, Steel02: fy E0 b R0 cR1 cR2 a1 a2 a3 a4 sigInit
    (material/uniaxial/steel/Steel02.h:47-50); Concrete02: fc epsc0 fcu epscu
-   rat ft Ets (material/uniaxial/concrete/Concrete02.h:48-49); Elastic: E */
+   rat ft Ets (material/uniaxial/concrete/Concrete02.h:48-49); Steel01: fy
+   E0 b a1 a2 a3 a4 (material/uniaxial/steel/Steel01.h:48-49); Elastic: E */
 #define XG_UNI_NPARAM 12
 
 /*

@@ -34,6 +34,7 @@
 #include <Brick.h>
 #include <J2PlaneStrain.h>
 #include <J2ThreeDimensional.h>
+#include <Steel01.h>
 #include <Steel02.h>
 #include <Concrete02.h>
 #include <ElasticMaterial.h>
@@ -277,6 +278,8 @@ UniaxialMaterial *make_uniaxial(int type, const double *q, int tag) {
       return new Steel02(tag, q[0], q[1], q[2], q[3], q[4], q[5], q[6], q[7], q[8], q[9], q[10]);
     case XG_UNI_CONCRETE02:
       return new Concrete02(tag, q[0], q[1], q[2], q[3], q[4], q[5], q[6]);
+    case XG_UNI_STEEL01:
+      return new Steel01(tag, q[0], q[1], q[2], q[3], q[4], q[5], q[6]);
     case XG_UNI_ELASTIC:
       return new ElasticMaterial(tag, q[0]);
   }

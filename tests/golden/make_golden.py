@@ -11,6 +11,7 @@ Usage: python tests/golden/make_golden.py        (the small fixtures)
        python tests/golden/make_golden.py c1     (frame3d_c1: the full-size 3D RC
                                                   frame pushover, about half an hour)
        python tests/golden/make_golden.py settle (frame2d_settle_2x3 alone)
+       python tests/golden/make_golden.py steel01 (uniaxial paths, Steel01 frames)
 """
 import os
 import sys
@@ -25,6 +26,15 @@ from xara_gb300 import configs  # noqa: E402
 from xara_gb300._abi import PhaseDesc  # noqa: E402
 
 OUT = os.path.dirname(os.path.abspath(__file__))
+
+
+def kw_array(kw):
+    """Builder keyword values: numbers as float64, or as text when one is a
+    string (golden_util.model_of reads both)."""
+    vals = list(kw.values())
+    if any(isinstance(v, str) for v in vals):
+        return np.array([str(v) for v in vals])
+    return np.asarray(vals, np.float64)
 
 
 def save(name, **arrays):
@@ -57,7 +67,9 @@ def uniaxial_paths(seed=2):
     rng = np.random.default_rng(seed)
     out = {}
     for kind, param, scale in ((1, configs.steel02_row(350e6, 200e9, 0.01), 4e-3),
-                               (2, configs.concrete02_row(30e6), 2e-3)):
+                               (2, configs.concrete02_row(30e6), 2e-3),
+                               (4, configs.steel01_row(350e6, 200e9, 0.01, 0.02, 2.0, 0.03, 3.0),
+                                4e-3)):
         n = 400
         strain = np.cumsum(rng.normal(0.0, scale / 3, size=n))
         commit = (rng.random(n) < 0.5).astype(np.int32)
@@ -75,7 +87,7 @@ def model_fixture(name, builder, args, kw, capture_steps=(), cap_solves=400):
     keep = np.isin(r.cap_step, np.asarray(capture_steps, np.int32))
     arrays = dict(
         builder=np.array(builder.__name__), args=np.asarray(args),
-        kw_keys=np.array(list(kw.keys())), kw_vals=np.asarray(list(kw.values()), np.float64),
+        kw_keys=np.array(list(kw.keys())), kw_vals=kw_array(kw),
         eqn=r.eqn, colstart=r.colstart, rowidx=r.rowidx,
         step_u=r.step_u, step_lambda=r.step_lambda, step_iters=r.step_iters,
     )
@@ -115,7 +127,7 @@ def revert_fixture(name, builder, args, kw, seed=5, scale=2e-4):
     K1, P1 = r.elem_response(u + du)
     K2, P2 = r.elem_response(u + 0.5 * du, revert_first=True)
     save(name, builder=np.array(builder.__name__), args=np.asarray(args),
-         kw_keys=np.array(list(kw.keys())), kw_vals=np.asarray(list(kw.values()), np.float64),
+         kw_keys=np.array(list(kw.keys())), kw_vals=kw_array(kw),
          eqn=r.eqn, colstart=r.colstart, rowidx=r.rowidx, u=u, du=du,
          K1=K1, P1=P1, K2=K2, P2=P2)
 
@@ -158,6 +170,16 @@ def c1_pushover(name="frame3d_c1", sample=50_000, seed=11, every=10):
          ref_seconds=np.array([r.elem_seconds, r.solve_seconds, r.step_seconds]))
 
 
+def steel01_fixtures():
+    """2D steel frames with Steel01 fibers: gravity and pushover (every solve
+    of the first gravity step captured) and gravity then a ground motion
+    (Newmark, Rayleigh on the initial stiffness)."""
+    model_fixture("frame2d_s01_2x3", configs.steel_frame_2d, (2, 3),
+                  {"steps": 12, "law": "Steel01"}, capture_steps=(0,))
+    model_fixture("frame2d_s01_eq_2x3", configs.steel_frame_2d_eq, (2, 3),
+                  {"steps": 150, "law": "Steel01"})
+
+
 def settlement_fixture():
     """The 2D steel frame with a support settlement imposed through the
     Transformation handler (gravity and settlement by LoadControl, then the
@@ -174,6 +196,10 @@ def main():
         return
     if sys.argv[1:] == ["settle"]:
         settlement_fixture()
+        return
+    if sys.argv[1:] == ["steel01"]:
+        uniaxial_paths()
+        steel01_fixtures()
         return
     j2_paths()
     model_fixture("quad_8x4", configs.quad_block, (8, 4), {}, capture_steps=(0, 6))
@@ -197,6 +223,7 @@ def main():
                    {"col_fibers": 40, "beam_fibers": 24, "steps": 10, "pdelta": 1})
     revert_fixture("revert_quad_8x4", configs.quad_block, (8, 4), {}, scale=1e-4)
     settlement_fixture()
+    steel01_fixtures()
 
 
 if __name__ == "__main__":

@@ -20,8 +20,13 @@ def load(name):
 def model_of(fx):
     builder = getattr(configs, str(fx["builder"]))
     args = tuple(int(a) for a in fx["args"])
-    kw = {str(k): (int(v) if float(v).is_integer() else float(v))
-          for k, v in zip(fx["kw_keys"], fx["kw_vals"])}
+    def value(v):
+        try:
+            f = float(v)
+        except ValueError:
+            return str(v)
+        return int(f) if f.is_integer() else f
+    kw = {str(k): value(v) for k, v in zip(fx["kw_keys"], fx["kw_vals"])}
     return builder(*args, **kw)
 
 

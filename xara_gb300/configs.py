@@ -142,7 +142,8 @@ def brick_block(nx=128, ny=128, nz=64, strain=0.01, steps=50, j2=J2_STEEL,
 # frames: `element forceBeamColumn` with Lobatto points and fiber sections
 # ---------------------------------------------------------------------------
 from ._abi import (XG_ELE_FBC2D, XG_ELE_FBC3D, XG_INT_LOAD_CONTROL,  # noqa: E402
-                   XG_UNI_CONCRETE02, XG_UNI_ELASTIC, XG_UNI_STEEL02, XG_UNI_NPARAM)
+                   XG_UNI_CONCRETE02, XG_UNI_ELASTIC, XG_UNI_STEEL01, XG_UNI_STEEL02,
+                   XG_UNI_NPARAM)
 
 
 def steel02_row(fy=350e6, E=200e9, b=0.01, R0=18.0, cR1=0.925, cR2=0.15):
@@ -150,6 +151,26 @@ def steel02_row(fy=350e6, E=200e9, b=0.01, R0=18.0, cR1=0.925, cR2=0.15):
     r = np.zeros(XG_UNI_NPARAM)
     r[:11] = [fy, E, b, R0, cR1, cR2, 0.0, 1.0, 0.0, 1.0, 0.0]
     return r
+
+
+def steel01_row(fy=350e6, E=200e9, b=0.01, a1=0.0, a2=1.0, a3=0.0, a4=1.0):
+    """`uniaxialMaterial Steel01 tag fy E b a1 a2 a3 a4` (no isotropic
+    hardening by default)."""
+    r = np.zeros(XG_UNI_NPARAM)
+    r[:7] = [fy, E, b, a1, a2, a3, a4]
+    return r
+
+
+def steel_row(law, fy, E, b):
+    """The steel row of a frame section: Steel02 (R0 18, cR1 0.925, cR2
+    0.15) or Steel01."""
+    if law == "Steel01":
+        return steel01_row(fy, E, b)
+    return steel02_row(fy, E, b)
+
+
+def steel_type(law):
+    return XG_UNI_STEEL01 if law == "Steel01" else XG_UNI_STEEL02
 
 
 def concrete02_row(fc, epsc0=0.002, fcu_ratio=0.2, epscu=0.006, rat=0.1, ft_ratio=0.1):
@@ -181,9 +202,10 @@ def wide_flange_fibers(d=0.4, bf=0.2, tf=0.015, tw=0.01, nf=40):
 
 def steel_frame_2d(bays=2, stories=3, bay=6.0, story=3.5, nfib=40, fy=350e6, E=200e9,
                    b=0.01, pdelta=0, gravity=-150e3, drift=0.02, steps=20, grav_steps=10,
-                   max_iter=50, tol=1e-10, seed=None):
+                   max_iter=50, tol=1e-10, seed=None, law="Steel02"):
     """2D steel moment frame: `forceBeamColumn` columns and beams with 5
-    Lobatto points and Steel02 wide-flange fiber sections, base fixed,
+    Lobatto points and Steel02 (or, with law="Steel01", Steel01)
+    wide-flange fiber sections, base fixed,
     gravity at every floor node (LoadControl, then `loadConst -time 0`), and a
     lateral pushover of the roof-left node by DisplacementControl against a
     triangular reference load pattern."""
@@ -210,7 +232,7 @@ def steel_frame_2d(bays=2, stories=3, bay=6.0, story=3.5, nfib=40, fy=350e6, E=2
         b = float(rng.uniform(0.005, 0.02))
     yc, Ac = wide_flange_fibers(0.45, 0.3, 0.022, 0.014, nfib)
     yb, Ab = wide_flange_fibers(0.5, 0.2, 0.016, 0.010, nfib)
-    uni = np.stack([steel02_row(fy, E, b)])
+    uni = np.stack([steel_row(law, fy, E, b)])
     fib_y = np.concatenate([yc, yb])
     fib_A = np.concatenate([Ac, Ab])
     fib_m = np.zeros(len(fib_y), np.int32)
@@ -226,7 +248,7 @@ def steel_frame_2d(bays=2, stories=3, bay=6.0, story=3.5, nfib=40, fy=350e6, E=2
         ndm=2, ndf=3, elem_type=XG_ELE_FBC2D, geom_transf=pdelta, fbc_num_ip=5,
         node_tag=tags, node_crd=crd,
         elem_tag=np.arange(1, ne + 1), elem_conn=conn, elem_mat=sec,
-        uni_type=[XG_UNI_STEEL02], uni_param=uni,
+        uni_type=[steel_type(law)], uni_param=uni,
         sec_fiber_start=[0, nfib, 2 * nfib], fib_y=fib_y, fib_area=fib_A, fib_mat=fib_m,
         sp_node=sp_node, sp_dof=sp_dof, sp_pattern=np.full(len(sp_node), -1),
         sp_value=np.zeros(len(sp_node)),

@@ -25,8 +25,55 @@ constexpr double kDblEps = 2.220446049250313e-16;
 // uniaxial laws on a 12-double record:
 //   Steel02: 0 epsmin 1 epsmax 2 epspl 3 epss0 4 sigs0 5 epsr 6 sigr 7 kon
 //            11 R of the current branch
-//   Concrete02: 0 ecmin 1 dept;  all: 8 e 9 sig 10 eps
+//   Concrete02: 0 ecmin 1 dept
+//   Steel01: 0 minStrain 1 maxStrain 2 shiftP 3 shiftN 4 loading
+//   all: 8 e 9 sig 10 eps
 // ---------------------------------------------------------------------------
+
+// Steel01::setTrialStrain / determineTrialState
+// (material/uniaxial/steel/Steel01.cpp:68-92, 124-198): bilinear kinematic
+// hardening with the isotropic shifts a1..a4 applied at load reversals;
+// q = fy E0 b a1 a2 a3 a4.  A strain within DBL_EPSILON of the committed one
+// leaves the committed state (strain included) as the trial state.
+__device__ __forceinline__ void steel01_trial(const double *q, const double *hc,
+                                              double trialStrain, double *ht) {
+  const double fy = q[0], E0 = q[1], b = q[2], a1 = q[3], a2 = q[4], a3 = q[5], a4 = q[6];
+  const double Cstrain = hc[10], Cstress = hc[9];
+  double TminStrain = hc[0], TmaxStrain = hc[1], TshiftP = hc[2], TshiftN = hc[3];
+  int Tloading = (int)hc[4];
+  const double dStrain = trialStrain - Cstrain;
+  if (!(fabs(dStrain) > kDblEps)) {
+    for (int c = 0; c < 12; c++) ht[c] = hc[c];
+    return;
+  }
+  const double fyOneMinusB = fy * (1.0 - b);
+  const double Esh = b * E0;
+  const double epsy = fy / E0;
+  const double c1 = Esh * trialStrain;
+  const double c2 = TshiftN * fyOneMinusB;
+  const double c3 = TshiftP * fyOneMinusB;
+  const double c = Cstress + E0 * dStrain;
+  const double c1c3 = c1 + c3;
+  double Tstress = c1c3 < c ? c1c3 : c;
+  const double c1c2 = c1 - c2;
+  if (c1c2 > Tstress) Tstress = c1c2;
+  const double Ttangent = fabs(Tstress - c) < kDblEps ? E0 : Esh;
+  if (Tloading == 0 && dStrain != 0.0) Tloading = dStrain > 0.0 ? 1 : -1;
+  if (Tloading == 1 && dStrain < 0.0) {
+    Tloading = -1;
+    if (Cstrain > TmaxStrain) TmaxStrain = Cstrain;
+    TshiftN = 1 + a1 * pow((TmaxStrain - TminStrain) / (2.0 * a2 * epsy), 0.8);
+  }
+  if (Tloading == -1 && dStrain > 0.0) {
+    Tloading = 1;
+    if (Cstrain < TminStrain) TminStrain = Cstrain;
+    TshiftP = 1 + a3 * pow((TmaxStrain - TminStrain) / (2.0 * a4 * epsy), 0.8);
+  }
+  ht[0] = TminStrain; ht[1] = TmaxStrain; ht[2] = TshiftP; ht[3] = TshiftN;
+  ht[4] = (double)Tloading;
+  ht[5] = hc[5]; ht[6] = hc[6]; ht[7] = hc[7]; ht[11] = hc[11];
+  ht[8] = Ttangent; ht[9] = Tstress; ht[10] = trialStrain;
+}
 
 // Steel02::setTrialStrain (material/uniaxial/steel/Steel02.cpp:113-227).
 // Record slot 11 keeps R, which changes only where the branch does (the
@@ -414,6 +461,15 @@ __device__ __forceinline__ void fbc_section(const FrameView &v, int f0, int nf, 
       for (int c = 0; c < 12; c++) ht[c] = htl[c];
       stress = htl[9];
       tangent = htl[8];
+    } else if (type == XG_UNI_STEEL01) {
+      double hcl[12], htl[12];
+#pragma unroll
+      for (int c = 0; c < 12; c++) hcl[c] = hc[c];
+      steel01_trial(q, hcl, strain, htl);
+#pragma unroll
+      for (int c = 0; c < 12; c++) ht[c] = htl[c];
+      stress = htl[9];
+      tangent = htl[8];
     } else if (type == XG_UNI_CONCRETE02) {
       double hcl[11], htl[11];
       hcl[0] = hc[0]; hcl[1] = hc[1]; hcl[9] = hc[9]; hcl[10] = hc[10];
@@ -501,6 +557,15 @@ __device__ __forceinline__ void fbc_section_group(const FrameView &v, int f0, in
 #pragma unroll
       for (int c = 0; c < 12; c++) hcl[c] = c == 8 ? 0.0 : hc[c];
       steel02_trial(q, hcl, strain, htl);
+#pragma unroll
+      for (int c = 0; c < 12; c++) ht[c] = htl[c];
+      stress = htl[9];
+      tangent = htl[8];
+    } else if (type == XG_UNI_STEEL01) {
+      double hcl[12], htl[12];
+#pragma unroll
+      for (int c = 0; c < 12; c++) hcl[c] = hc[c];
+      steel01_trial(q, hcl, strain, htl);
 #pragma unroll
       for (int c = 0; c < 12; c++) ht[c] = htl[c];
       stress = htl[9];

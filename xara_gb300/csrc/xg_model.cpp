@@ -815,7 +815,7 @@ void lobatto_points(int n, double *xi, double *wt) {
 // Initial tangent of a uniaxial row (Steel02 E0; Concrete02 2 fc / epsc0
 // after the constructor's sign normalisation, Concrete02.cpp:97-111).
 double uniaxial_initial_tangent(int type, const double *q) {
-  if (type == XG_UNI_STEEL02) return q[1];
+  if (type == XG_UNI_STEEL02 || type == XG_UNI_STEEL01) return q[1];
   if (type == XG_UNI_CONCRETE02) {
     const double fc = q[0] > 0 ? -q[0] : q[0], e0 = q[1] > 0 ? -q[1] : q[1];
     return 2.0 * fc / e0;
@@ -832,6 +832,11 @@ void uniaxial_initial_record(int type, const double *q, double *h) {
     h[0] = -h[1];
     h[8] = q[1];
     if (q[10] != 0.0) { h[10] = q[10] / q[1]; h[9] = q[10]; }
+  } else if (type == XG_UNI_STEEL01) {
+    // Steel01::revertToStart (Steel01.cpp:285-310): shifts 1, tangent E0
+    h[2] = 1.0;
+    h[3] = 1.0;
+    h[8] = q[1];
   } else {
     h[8] = uniaxial_initial_tangent(type, q);
   }
@@ -2146,7 +2151,7 @@ static int plan_model(const xg_model_desc *d, xg_model **out) {
       }
     for (int u = 0; u < nuni; u++)
       if (m->utype[u] != XG_UNI_STEEL02 && m->utype[u] != XG_UNI_CONCRETE02 &&
-          m->utype[u] != XG_UNI_ELASTIC) {
+          m->utype[u] != XG_UNI_ELASTIC && m->utype[u] != XG_UNI_STEEL01) {
         delete m;
         return fail(XG_EINVAL, "uniaxial row %d: unknown type %d", u, m->utype[u]);
       }
