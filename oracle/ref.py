@@ -142,3 +142,31 @@ def uniaxial_path(kind, param, strain, commit):
     t = np.zeros(len(strain))
     L.xref_uniaxial_path(kind, _p(param), len(strain), _p(strain), _p(commit), _p(s), _p(t))
     return s, t
+
+
+def ddm_gradient(desc, phases, params, obj):
+    """The reference's DDM sensitivity (computeGradients at every step) of J
+    = sum over steps and terms of w u(node, dof)^2: params is a list of
+    (element tag, name) with name 0 fy, 1 E, 2 b; obj = (node tags, dofs,
+    weights).  Returns (dJ/dparam, J)."""
+    L = lib()
+    L.xref_ddm_setup.argtypes = [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_int,
+                                 C.c_void_p, C.c_void_p, C.c_void_p]
+    L.xref_ddm_result.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p]
+    tags = np.ascontiguousarray([p[0] for p in params], np.int32)
+    names = np.ascontiguousarray([p[1] for p in params], np.int32)
+    nodes = np.ascontiguousarray(obj[0], np.int32)
+    dofs = np.ascontiguousarray(obj[1], np.int32)
+    w = np.ascontiguousarray(obj[2], np.float64)
+
+    def attach(h):
+        r = L.xref_ddm_setup(C.c_void_p(h), len(tags), _p(tags), _p(names), len(nodes),
+                             _p(nodes), _p(dofs), _p(w))
+        if r != 0:
+            raise RuntimeError(f"xref_ddm_setup failed: {r}")
+
+    run = RefRun(desc, phases, attach=attach)
+    grad = np.zeros(len(tags))
+    J = C.c_double()
+    L.xref_ddm_result(C.c_void_p(run.h), _p(grad), C.byref(J))
+    return grad, J.value, run

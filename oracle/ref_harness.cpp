@@ -59,6 +59,7 @@
 #include <LoadControl.h>
 #include <DisplacementControl.h>
 #include <Newmark.h>
+#include <Parameter.h>
 #include <TransientIntegrator.h>
 #include <UniformExcitation.h>
 #include <GroundMotion.h>
@@ -227,6 +228,15 @@ struct Harness {
   LinearSOE *observer = nullptr;
   void (*on_solve)(void *) = nullptr;
   void *on_solve_ctx = nullptr;
+  // DDM sensitivity (the reference's computeGradients): parameters added to
+  // the Domain, and the objective J = sum over steps and terms of
+  // w_k u(node_k, dof_k)^2 with its gradient accumulated after every step
+  struct Ddm {
+    int active = 0;
+    std::vector<int> node_index, dof;
+    std::vector<double> w, grad;
+    double J = 0.0;
+  } ddm;
 
   void snapshotU(double *out) {
     int ndf = d.ndf;
@@ -474,6 +484,12 @@ int xref_run_phase(void *hp, const xg_phase_desc *ph, int cap_begin, int cap_end
     // `pattern UniformExcitation` over a `timeSeries Path -dt` record
     transient = new Newmark(ph->gamma, ph->beta);
     integ = transient;
+    if (h->ddm.active) {
+      // `sensitivityAlgorithm -computeAtEachStep`
+      // (runtime/commands/analysis/sensitivity.cpp:124-139)
+      transient->setComputeType(1);
+      transient->activateSensitivityKey();
+    }
     h->domain->setRayleighDampingFactors(ph->alpha_m, ph->beta_k, ph->beta_k_init,
                                          ph->beta_k_comm);
     if (ph->gm_npts > 0) {
@@ -543,6 +559,20 @@ int xref_run_phase(void *hp, const xg_phase_desc *ph, int cap_begin, int cap_end
       fprintf(stderr, "xref_run_phase: step %d failed (%d)\n", gstep, r);
       return -1000 - s;
     }
+    if (transient && h->ddm.active) {
+      // BasicAnalysisBuilder::analyzeTransient (runtime/runtime/
+      // BasicAnalysisBuilder.cpp:502-511): the sensitivities of the
+      // converged step before its commit; then dJ/dtheta += 2 w u du/dtheta
+      if (transient->computeSensitivities() < 0) return -30;
+      Harness::Ddm &dd = h->ddm;
+      for (size_t k = 0; k < dd.w.size(); k++) {
+        Node *nd = h->nodes[dd.node_index[k]];
+        const double u = nd->getTrialDisp()(dd.dof[k]);
+        dd.J += dd.w[k] * u * u;
+        for (size_t g = 0; g < dd.grad.size(); g++)
+          dd.grad[g] += 2.0 * dd.w[k] * u * nd->getDispSensitivity(dd.dof[k] + 1, (int)g);
+      }
+    }
     if (integ->commit() < 0) return -20;
     double dt = std::chrono::duration<double>(clk::now() - t0).count();
     h->stepSeconds += dt;
@@ -563,6 +593,48 @@ int xref_run_phase(void *hp, const xg_phase_desc *ph, int cap_begin, int cap_end
     h->domain->setCommittedTime(0.0);
   }
   return 0;
+}
+
+// DDM set-up before the first phase: one Parameter per (element tag,
+// name), name 0 "fy", 1 "E", 2 "b", reaching every fiber material of the
+// element (ForceBeamColumn2d::setParameter -> FiberSection2d::setParameter
+// -> the materials' setParameter, ForceBeamColumn2d.cpp:2763-2846,
+// FiberSection2d.cpp:877-960), added to the Domain in order (gradient index
+// = position); the objective's terms by node tag and 0-based dof.
+extern "C" int xref_ddm_setup(void *hp, int nparam, const int *elem_tag, const int *name,
+                              int nterm, const int *node_tag, const int *dof,
+                              const double *w) {
+  Harness *h = (Harness *)hp;
+  if (h->soe) return -1;
+  static const char *names[3] = {"fy", "E", "b"};
+  for (int k = 0; k < nparam; k++) {
+    Element *el = h->domain->getElement(elem_tag[k]);
+    if (!el || name[k] < 0 || name[k] > 2) return -2;
+    const char *argv[1] = {names[name[k]]};
+    Parameter *p = new Parameter(k + 1, el, argv, 1);
+    if (!h->domain->addParameter(p)) return -3;
+  }
+  Harness::Ddm &dd = h->ddm;
+  dd.active = 1;
+  dd.grad.assign(nparam, 0.0);
+  dd.J = 0.0;
+  for (int k = 0; k < nterm; k++) {
+    int idx = -1;
+    for (size_t i = 0; i < h->nodes.size(); i++)
+      if (h->nodes[i]->getTag() == node_tag[k]) idx = (int)i;
+    if (idx < 0) return -4;
+    dd.node_index.push_back(idx);
+    dd.dof.push_back(dof[k]);
+    dd.w.push_back(w[k]);
+  }
+  return 0;
+}
+
+extern "C" int xref_ddm_result(void *hp, double *grad, double *J) {
+  Harness *h = (Harness *)hp;
+  for (size_t g = 0; g < h->ddm.grad.size(); g++) grad[g] = h->ddm.grad[g];
+  *J = h->ddm.J;
+  return (int)h->ddm.grad.size();
 }
 
 // Equation numbers per (node, dof) after the first phase was set up.

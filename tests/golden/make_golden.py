@@ -180,6 +180,20 @@ def steel01_fixtures():
                   {"steps": 150, "law": "Steel01"})
 
 
+def ddm_fixture(name="ddm_steel01_frame"):
+    """The reference's DDM gradient (computeGradients at every step) of the
+    summed squared roof drift of configs.ddm_steel01_frame with respect to
+    every member's Steel01 fy, E0 and b, and the objective itself."""
+    desc, phases = configs.ddm_steel01_frame()
+    params = [(int(t), k) for t in desc.elem_tag for k in range(3)]
+    obj = (desc.meta["obj_node"], desc.meta["obj_dof"], desc.meta["obj_weight"])
+    grad, J, run = ref.ddm_gradient(desc, phases, params, obj)
+    save(name, builder=np.array("ddm_steel01_frame"), args=np.asarray([], np.int64),
+         kw_keys=np.array([], dtype="<U1"), kw_vals=np.asarray([], np.float64),
+         grad=grad.reshape(-1, 3), J=np.array([J]), step_u=run.step_u,
+         step_iters=run.step_iters)
+
+
 def settlement_fixture():
     """The 2D steel frame with a support settlement imposed through the
     Transformation handler (gravity and settlement by LoadControl, then the
@@ -200,6 +214,7 @@ def main():
     if sys.argv[1:] == ["steel01"]:
         uniaxial_paths()
         steel01_fixtures()
+        ddm_fixture()
         return
     j2_paths()
     model_fixture("quad_8x4", configs.quad_block, (8, 4), {}, capture_steps=(0, 6))
@@ -224,6 +239,7 @@ def main():
     revert_fixture("revert_quad_8x4", configs.quad_block, (8, 4), {}, scale=1e-4)
     settlement_fixture()
     steel01_fixtures()
+    ddm_fixture()
 
 
 if __name__ == "__main__":

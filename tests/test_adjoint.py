@@ -13,7 +13,7 @@ import pytest
 
 from oracle import port
 from xara_gb300 import configs
-from xara_gb300._abi import XG_UNI_CONCRETE02, XG_UNI_ELASTIC, XG_UNI_STEEL02
+from xara_gb300._abi import XG_UNI_CONCRETE02, XG_UNI_ELASTIC, XG_UNI_STEEL01, XG_UNI_STEEL02
 
 FIELDS = (0, 1, 2, 3, 4, 5, 6, 9, 10)            # continuous record fields
 
@@ -119,6 +119,73 @@ def test_steel02_vjp_zero_increment_and_elastic():
         q2 = q.copy()
         q2[10] = 1e6                             # initial stress: not covered
         gpu.uniaxial_vjp(XG_UNI_STEEL02, q2, hc, 1e-3, yb)
+
+
+S01_FIELDS = (0, 1, 2, 3, 9, 10)     # minStrain, maxStrain, shiftP, shiftN, sig, eps
+
+
+@pytest.mark.parametrize("shift", [False, True])
+def test_steel01_vjp_against_finite_differences(shift):
+    """Steel01's vector-Jacobian product (the library's host entry) against
+    central differences of the oracle's law, along a cyclic path of growing
+    amplitude: the elastic predictor, both hardening bounds, reversals with
+    and without a new extreme strain, with and without the isotropic shifts."""
+    gpu = _gpu()
+    q = configs.steel01_row(350e6, 200e9, 0.015, *((0.04, 1.0, 0.03, 1.5) if shift
+                                                    else (0.0, 1.0, 0.0, 1.0)))
+    ey = q[0] / q[1]
+    t = np.linspace(0.0, 6.0 * np.pi, 240)
+    strains = ey * (0.5 + 0.05 * t) * np.sin(t) * 3.0
+    rng = np.random.default_rng(5)
+    sc = np.full(12, ey)
+    sc[2] = sc[3] = 1.0
+    sc[9] = q[0]
+    hc = port.uniaxial_init(XG_UNI_STEEL01, q)
+    branches = set()
+    checked = 0
+    for e in strains:
+        deps = e - hc[10]
+        ht = port.uniaxial_trial(XG_UNI_STEEL01, q, hc, float(e))
+        if abs(deps) > 1e-4 * ey and abs(abs(ht[9]) - abs(hc[9] + q[1] * deps)) > 1e-6 * q[0]:
+            branches.add("bound")
+        elif abs(deps) > 1e-4 * ey:
+            branches.add("elastic")
+        if abs(deps) > 1e-4 * ey and int(hc[4]) * deps < 0:
+            branches.add("reversal")
+        yb = np.zeros(12)
+        yb[list(S01_FIELDS)] = rng.normal(size=len(S01_FIELDS)) / sc[list(S01_FIELDS)]
+        hb, sb, qb = gpu.uniaxial_vjp(XG_UNI_STEEL01, q, hc, float(e), yb)
+
+        def J(hc_, eps_, q_):
+            return float(yb @ port.uniaxial_trial(XG_UNI_STEEL01, q_, hc_, eps_))
+
+        rel = 1e-7
+        checks = [("strain", sb, (J(hc, e + rel * ey, q) - J(hc, e - rel * ey, q)) /
+                   (2 * rel * ey), ey)]
+        for f in S01_FIELDS:
+            hp, hm = hc.copy(), hc.copy()
+            hp[f] += rel * sc[f]
+            hm[f] -= rel * sc[f]
+            checks.append((f"record[{f}]", hb[f], (J(hp, e, q) - J(hm, e, q)) /
+                           (2 * rel * sc[f]), sc[f]))
+        for k in range(3):
+            qp, qm = q.copy(), q.copy()
+            qp[k] += rel * q[k]
+            qm[k] -= rel * q[k]
+            checks.append((f"param[{k}]", qb[k], (J(hc, e, qp) - J(hc, e, qm)) / (2 * rel * q[k]),
+                           q[k]))
+        total = sum(abs(a) * s_ for _, a, _, s_ in checks) + 1e-12
+        # the kinks of the law: the elastic predictor at a hardening bound
+        c = hc[9] + q[1] * deps
+        c1, fyomb = q[2] * q[1] * e, q[0] * (1 - q[2])
+        kink = min(abs(c - (c1 + hc[2] * fyomb)), abs(c - (c1 - hc[3] * fyomb))) < 1e-3 * q[0]
+        if abs(deps) > 1e-4 * ey and not kink:
+            for name, a, b, s_ in checks:
+                assert abs(a - b) * s_ <= 2e-6 * total, (name, a, b)
+            checked += 1
+        hc = ht
+    assert {"bound", "elastic", "reversal"} <= branches
+    assert checked > 200
 
 
 C02_FIELDS = (0, 1, 9, 10)                       # ecmin, dept, sig, eps
@@ -384,3 +451,47 @@ def test_adjoint_through_torch_autograd(need_gpu):
         g = gpu.adjoint_backward(m)
     assert float(J.detach()) == J2
     np.testing.assert_allclose(theta.grad.numpy(), 2.0 * g, rtol=1e-13, atol=0)
+
+
+def _ddm_case():
+    from golden_util import load, model_of
+    fx = load("ddm_steel01_frame")
+    desc, phases = model_of(fx)
+    obj = (desc.meta["obj_node"], desc.meta["obj_dof"], desc.meta["obj_weight"])
+    return fx, desc, phases, obj
+
+
+def test_ddm_surrogate_forward_matches_the_reference():
+    """The massless Steel01 ramp the reference's DDM runs on: the oracle's
+    history and objective equal the reference's (the fixture)."""
+    fx, desc, phases, obj = _ddm_case()
+    o = port.OracleModel(desc)
+    U, _, its = o.run(phases)
+    o.close()
+    assert np.array_equal(its, fx["step_iters"])
+    assert np.linalg.norm(U - fx["step_u"]) <= 1e-12 * np.linalg.norm(fx["step_u"])
+    roof = list(desc.node_tag).index(int(obj[0][0]))
+    J = obj[2][0] * np.sum(U[:, 3 * roof] ** 2)
+    assert abs(J - fx["J"][0]) <= 1e-12 * fx["J"][0]
+
+
+@pytest.mark.gpu
+def test_adjoint_matches_the_reference_ddm(need_gpu):
+    """The device adjoint against the reference's own DDM sensitivity
+    (Newmark::computeSensitivities after every step, the gradient of the
+    summed squared roof drift accumulated from Node::getDispSensitivity):
+    every member's d/d(fy, E0, b) of Steel01, each parameter kind within
+    1e-6 relative of its largest entry, and the objective within 1e-12."""
+    gpu = _gpu()
+    fx, desc, phases, obj = _ddm_case()
+    ph = phases[0]
+    with gpu.DeviceModel(desc) as m:
+        m.set_system(gpu.XG_SYSTEM_PROFILE_SPD)
+        J = gpu.adjoint_forward(m, ph, ph.num_steps, 25, *obj)
+        g = gpu.adjoint_backward(m)
+    ref = fx["grad"]
+    assert abs(J - fx["J"][0]) <= 1e-12 * fx["J"][0]
+    assert g.shape == ref.shape
+    for k in range(3):
+        scale = np.abs(ref[:, k]).max()
+        assert np.max(np.abs(g[:, k] - ref[:, k])) <= 1e-6 * scale, (k, g[:, k], ref[:, k])

@@ -662,6 +662,57 @@ def adjoint_frames(n_frames=64, steps=2000, dt=0.01, seed=0, nfib=40, member_cov
 
 
 
+def ddm_steel01_frame(bays=2, stories=3, steps=100, dt=0.01, base_shear=720e3, seed=3,
+                      member_cov=0.05, nfib=40):
+    """One 2D steel frame for comparing gradients with the reference's DDM
+    sensitivity (its Steel01 has stress sensitivities, its Steel02 has
+    none).  The reference's transient DDM cannot run with nodal mass
+    (Node::getMassSensitivity, domain/node/Node.cpp:1445-1469, returns a
+    local Matrix through the move constructor, which throws,
+    matrix/Matrix.cpp:130-141), so the frame carries no mass and no
+    damping: `integrator Newmark 0.5 0.25` with a triangular lateral load
+    pattern on a Linear series, ramped to ``base_shear`` at the last step (1.5 %
+    roof drift for the default frame) -- a path-dependent, quasi-static
+    response through yielding.  One Steel01 material per member (fy and b
+    varied by a lognormal factor of CoV ``member_cov``, E 200 GPa).  The
+    objective is the summed squared roof drift, as in
+    :func:`adjoint_frames`."""
+    desc, _ = steel_frame_2d(bays, stories, steps=1, grav_steps=1, law="Steel01", gravity=0.0,
+                             nfib=nfib)
+    a = desc.arrays
+    ss, em = a["sec_fiber_start"], a["elem_mat"]
+    uni = a["uni_param"].reshape(-1, XG_UNI_NPARAM)
+    rng = np.random.default_rng(seed + 13)
+    ne = len(em)
+    lo, hi = ss[em], ss[em + 1]
+    counts = hi - lo
+    idx = np.concatenate([np.arange(l_, h_) for l_, h_ in zip(lo, hi)])
+    rows = np.repeat(uni[:1], ne, axis=0)
+    rows[:, 0] *= np.exp(rng.normal(0.0, member_cov, ne))
+    rows[:, 2] *= np.exp(rng.normal(0.0, member_cov, ne))
+    # the lateral pattern only (pattern 0), scaled so that lambda = t reaches
+    # the base shear at t = steps * dt
+    lat = np.asarray(a["load_pattern"]) == 1
+    load_val = np.asarray(a["load_value"]).reshape(-1, 3)[lat] * base_shear / (steps * dt)
+    kw = {k: v for k, v in a.items() if v is not None}
+    kw.update(elem_mat=np.arange(ne), sec_fiber_start=np.concatenate([[0], np.cumsum(counts)]),
+              fib_y=a["fib_y"][idx], fib_area=a["fib_area"][idx],
+              fib_mat=np.repeat(np.arange(ne), counts), uni_type=np.full(ne, XG_UNI_STEEL01),
+              uni_param=rows, load_node=np.asarray(a["load_node"])[lat],
+              load_pattern=np.zeros(int(lat.sum()), np.int32), load_value=load_val)
+    out = ModelDesc(ndm=desc.ndm, ndf=desc.ndf, elem_type=desc.elem_type,
+                    geom_transf=desc.geom_transf, fbc_num_ip=desc.fbc_num_ip, **kw)
+    ramp = PhaseDesc(integrator=XG_INT_NEWMARK, pattern=0, num_steps=steps, dt=dt,
+                     gamma=0.5, beta=0.25, tol=1e-10, max_iter=50)
+    H = stories * 3.5
+    roof = stories * (bays + 1) + 1
+    out.meta = dict(desc.meta, workload=f"2D steel frame {bays}x{stories}, one Steel01 per "
+                                        f"member, massless Newmark ramp",
+                    obj_node=np.array([roof], np.int32), obj_dof=np.zeros(1, np.int32),
+                    obj_weight=np.array([1.0 / (H * H)]), members=ne)
+    return out, [ramp]
+
+
 def adjoint_rc_frames(n_frames=2, steps=2000, dt=0.01, seed=0, member_cov=0.05, pga_scale=1.0,
                       ncl=12):
     """The frames of :func:`adjoint_frames` with reinforced-concrete members:

@@ -137,6 +137,7 @@ __device__ __forceinline__ void fiber_vjp(int type, const double *q, const doubl
                                           double *sb, double *qb) {
   if (type == XG_UNI_STEEL02) steel02_vjp(q, hc, strain, yb, hb, sb, qb);
   else if (type == XG_UNI_CONCRETE02) concrete02_vjp(q, hc, strain, yb, hb, sb, qb);
+  else if (type == XG_UNI_STEEL01) steel01_vjp(q, hc, strain, yb, hb, sb, qb);
   else elastic_vjp(q, strain, yb, hb, sb, qb);
 }
 
@@ -395,7 +396,7 @@ __global__ void __launch_bounds__(32 * kAdjWarps) k_adj_elem_b(FrameView v, AdjV
 #pragma unroll
         for (int k = 0; k < NB; k++) val += pb[i] * kv0[i * NB + k] * rv[k];
       const int u = a.elem_uni[e];
-      const int ie = v.utype[u] == XG_UNI_STEEL02 ? 1 : 0;
+      const int ie = (v.utype[u] == XG_UNI_STEEL02 || v.utype[u] == XG_UNI_STEEL01) ? 1 : 0;
       const double E = v.uparam[(long)u * XG_UNI_NPARAM + ie];
       const double bk = a.bk0 ? a.bk0[e] : a.bk0_all;
       const double d = -bk / E * val;
@@ -528,6 +529,8 @@ extern "C" int xg_uniaxial_vjp(int type, const double *q, const double *hc, doub
     xg::steel02_vjp(q, hc, strain, yb, hb, sb, qb);
   } else if (type == XG_UNI_CONCRETE02) {
     xg::concrete02_vjp(q, hc, strain, yb, hb, sb, qb);
+  } else if (type == XG_UNI_STEEL01) {
+    xg::steel01_vjp(q, hc, strain, yb, hb, sb, qb);
   } else if (type == XG_UNI_ELASTIC) {
     xg::elastic_vjp(q, strain, yb, hb, sb, qb);
   } else {

@@ -1825,8 +1825,9 @@ int xg_model::adjoint_forward(const xg_phase_desc *ph, int N, int K, const xg_ob
           return fail(XG_EINVAL, "the adjoint does not cover Steel02 with an initial stress");
       } else if (utype[u] == XG_UNI_CONCRETE02) {
         sec_single[sc] = 0;
-      } else if (utype[u] != XG_UNI_ELASTIC) {
-        return fail(XG_EINVAL, "the adjoint covers Steel02, Concrete02 and elastic fibers");
+      } else if (utype[u] != XG_UNI_ELASTIC && utype[u] != XG_UNI_STEEL01) {
+        return fail(XG_EINVAL, "the adjoint covers Steel02, Steel01, Concrete02 and elastic "
+                    "fibers");
       }
       if (m > 0) sec_single[sc] = 0;
     }
@@ -1843,8 +1844,8 @@ int xg_model::adjoint_forward(const xg_phase_desc *ph, int N, int K, const xg_ob
   for (int e = 0; e < ne; e++) {
     const double bk = ph->beta_k_init_elem ? ph->beta_k_init_elem[e] : ph->beta_k_init;
     if (bk != 0.0 && !sec_single[mat[e]])
-      return fail(XG_EINVAL, "betaK0 damping in the adjoint needs one Steel02 or elastic "
-                  "material per element (element %d)", e);
+      return fail(XG_EINVAL, "betaK0 damping in the adjoint needs one Steel02, Steel01 or "
+                  "elastic material per element (element %d)", e);
   }
   RET(xg_analysis_set_phase(this, ph));
   cudaStream_t s = stream;

@@ -7,9 +7,11 @@
 // committed record's fields and of the first three parameters.
 //
 // Record layout (12 doubles): Steel02 0 epsmin 1 epsmax 2 epspl 3 epss0
-// 4 sigs0 5 epsr 6 sigr 7 kon; Concrete02 0 ecmin 1 dept; all 8 e 9 sig
-// 10 eps.  Field 7 (the loading branch) is discrete and field 8 (the
-// tangent) is read by no later step, so their adjoints are not formed.
+// 4 sigs0 5 epsr 6 sigr 7 kon; Concrete02 0 ecmin 1 dept; Steel01
+// 0 minStrain 1 maxStrain 2 shiftP 3 shiftN 4 loading; all 8 e 9 sig
+// 10 eps.  The loading fields (Steel02 7, Steel01 4) are discrete and field
+// 8 (the tangent) is read by no later step, so their adjoints are not
+// formed.
 #pragma once
 
 #include <float.h>
@@ -390,6 +392,90 @@ XG_HD inline void concrete02_vjp(const double *q, const double *hc, double strai
 }
 
 // Elastic fiber: sig = E eps (parameter 0).
+// Steel01::setTrialStrain / determineTrialState (material/uniaxial/steel/
+// Steel01.cpp:68-92, 124-198), swept backwards: the stress is one of the
+// elastic predictor Cstress + E0 dStrain, the upper bound b E0 eps +
+// shiftP fy (1 - b) or the lower bound b E0 eps - shiftN fy (1 - b) (the
+// primal is recomputed to find which); at a load reversal the new shift is
+// 1 + a (dmax / (2 a' epsy))^0.8 with epsy = fy / E0 and the extreme strain
+// taken from the committed strain when it goes further.  Parameters q: fy
+// E0 b a1 a2 a3 a4; qb receives d/d(fy, E0, b).
+XG_HD inline void steel01_vjp(const double *q, const double *hc, double strain, const double *yb,
+                              double *hb, double *sb, double *qb) {
+  const double fy = q[0], E0 = q[1], b = q[2], a1 = q[3], a2 = q[4], a3 = q[5], a4 = q[6];
+  for (int k = 0; k < 12; k++) hb[k] = 0.0;
+  qb[0] = qb[1] = qb[2] = 0.0;
+  *sb = 0.0;
+  const double Cstrain = hc[10], Cstress = hc[9];
+  const double dStrain = strain - Cstrain;
+  if (!(fabs(dStrain) > DBL_EPSILON)) {
+    // the committed state passes through unchanged
+    hb[0] = yb[0]; hb[1] = yb[1]; hb[2] = yb[2]; hb[3] = yb[3];
+    hb[9] = yb[9]; hb[10] = yb[10];
+    return;
+  }
+  const double fyomb = fy * (1.0 - b), epsy = fy / E0;
+  const double c1 = b * E0 * strain, c2 = hc[3] * fyomb, c3 = hc[2] * fyomb;
+  const double c = Cstress + E0 * dStrain;
+  int branch = 0;                       // 0 predictor, 1 upper bound, 2 lower bound
+  double t = c;
+  if (c1 + c3 < c) { t = c1 + c3; branch = 1; }
+  if (c1 - c2 > t) branch = 2;
+  int loading = (int)hc[4];
+  if (loading == 0) loading = dStrain > 0.0 ? 1 : -1;
+  const bool revN = loading == 1 && dStrain < 0.0;
+  const bool revP = !revN && loading == -1 && dStrain > 0.0;
+  double gTmin = yb[0], gTmax = yb[1], gEps = yb[10], gEpsy = 0.0;
+  double gFy = 0.0, gE0 = 0.0, gB = 0.0, gCstrain = 0.0, gCstress = 0.0;
+  double gShiftP = 0.0, gShiftN = 0.0;
+  if (revN || revP) {
+    const double Tmin = revP && Cstrain < hc[0] ? Cstrain : hc[0];
+    const double Tmax = revN && Cstrain > hc[1] ? Cstrain : hc[1];
+    const double a = revN ? a1 : a3, den = 2.0 * (revN ? a2 : a4) * epsy;
+    const double X = (Tmax - Tmin) / den;
+    const double gShift = revN ? yb[3] : yb[2];
+    const double gX = (a != 0.0 && X > 0.0) ? gShift * a * 0.8 * pow(X, -0.2) : 0.0;
+    gTmax += gX / den;
+    gTmin -= gX / den;
+    gEpsy -= gX * X / epsy;
+    if (revN) {
+      gShiftP += yb[2];                 // the other shift passes through
+      if (Cstrain > hc[1]) { gCstrain += gTmax; gTmax = 0.0; }
+    } else {
+      gShiftN += yb[3];
+      if (Cstrain < hc[0]) { gCstrain += gTmin; gTmin = 0.0; }
+    }
+  } else {
+    gShiftP += yb[2];
+    gShiftN += yb[3];
+  }
+  const double gs = yb[9];
+  if (branch == 0) {
+    gCstress += gs;
+    gE0 += gs * dStrain;
+    gEps += gs * E0;
+    gCstrain -= gs * E0;
+  } else if (branch == 1) {
+    gB += gs * (E0 * strain - hc[2] * fy);
+    gE0 += gs * b * strain;
+    gEps += gs * b * E0;
+    gShiftP += gs * fyomb;
+    gFy += gs * hc[2] * (1.0 - b);
+  } else {
+    gB += gs * (E0 * strain + hc[3] * fy);
+    gE0 += gs * b * strain;
+    gEps += gs * b * E0;
+    gShiftN -= gs * fyomb;
+    gFy -= gs * hc[3] * (1.0 - b);
+  }
+  gFy += gEpsy / E0;
+  gE0 -= gEpsy * fy / (E0 * E0);
+  hb[0] = gTmin; hb[1] = gTmax; hb[2] = gShiftP; hb[3] = gShiftN;
+  hb[9] = gCstress; hb[10] = gCstrain;
+  *sb = gEps;
+  qb[0] = gFy; qb[1] = gE0; qb[2] = gB;
+}
+
 XG_HD inline void elastic_vjp(const double *q, double strain, const double *yb, double *hb,
                               double *sb, double *qb) {
   for (int k = 0; k < 12; k++) hb[k] = 0.0;
