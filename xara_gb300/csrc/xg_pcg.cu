@@ -15,6 +15,7 @@
 #include <cstdint>
 #include <vector>
 
+#include "xg_ff.h"
 #include "xg_internal.h"
 
 namespace xg {
@@ -93,42 +94,6 @@ __device__ __forceinline__ double spmv_row(const PcgSystem &S, int row, const do
   for (int k = b + lane; k < e; k += 32) s += S.vals[k] * x[S.colidx[k]];
   for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
   return s;  // lane 0
-}
-
-// Float-float arithmetic on the single-precision pipes (GB300's FP64 pipe
-// is the bottleneck of an FP64 SpMV: one FMA per non-zero).  A double v is
-// kept as hi + lo, hi = v rounded to single precision and lo = (v - hi)
-// rounded: 48 of its 53 bits.  A product of two such pairs is
-// hi_a hi_x exactly (the rounding error of the single-precision product
-// recovered by an FMA: Dekker's TwoProduct, 1971, with a fused
-// multiply-add) plus the cross terms hi_a lo_x + lo_a hi_x in single
-// precision (lo_a lo_x, below 2^-48 of the product, is dropped); sums add
-// the high parts exactly (Knuth's TwoSum, TAOCP vol. 2, 4.2.2) and collect
-// every error in the low part.  Each product is good to about 2^-46 of its
-// magnitude.  __fmul_rn keeps the compiler from fusing the product into the
-// following addition, which would break the error-free transformations.
-__device__ __forceinline__ float2 split2(double v) {
-  const float hi = __double2float_rn(v);
-  return make_float2(hi, __double2float_rn(v - (double)hi));
-}
-
-__device__ __forceinline__ void ff_madd(float2 a, float2 x, float &sh, float &sl) {
-  const float p = __fmul_rn(a.x, x.x);
-  float e = __fmaf_rn(a.x, x.x, -p);
-  e = __fmaf_rn(a.x, x.y, e);
-  e = __fmaf_rn(a.y, x.x, e);
-  const float t = __fadd_rn(sh, p);
-  const float bp = __fsub_rn(t, sh);
-  const float err = __fadd_rn(__fsub_rn(sh, __fsub_rn(t, bp)), __fsub_rn(p, bp));
-  sh = t;
-  sl = __fadd_rn(sl, __fadd_rn(err, e));
-}
-
-// Whether a value can be split without leaving single precision's range
-// (products of two split values stay finite and normal).
-__device__ __forceinline__ bool ff_range(double v) {
-  const double a = fabs(v);
-  return a == 0.0 || (a >= 0x1p-100 && a < 0x1p100);
 }
 
 // Row of (A x) from the CSR arrays in FP64, one thread.
