@@ -202,16 +202,18 @@ def test_quad_commands_run_like_the_builders(need_gpu):
 def test_transformation_commands_run_like_the_builders(need_gpu):
     """`constraints Transformation` with a support settlement imposed by an
     `sp` inside the gravity pattern: the same displacements, bit for bit, as
-    the builder's model of it (configs.settlement_frame_2d)."""
+    the builder's model of it (configs.settlement_frame_2d).  Ten gravity
+    steps, as in the golden fixture: the 3 cm settlement in four steps makes
+    the first Newton step diverge, in the reference as in the oracle."""
     from xara_gb300 import gpu
-    roof, nx = _frame_script(settle=-0.03)
-    assert ops.analyze(4) == 0
+    roof, nx = _frame_script(settle=-0.03, grav_steps=10)
+    assert ops.analyze(10) == 0
     _lateral(roof, nx)
     assert ops.analyze(5) == 0
     u_roof = ops.nodeDisp(roof)
     u_mid = ops.nodeDisp(2)
     ops.wipe()
-    desc, phases = configs.settlement_frame_2d(2, 3, settlement=-0.03, steps=5, grav_steps=4)
+    desc, phases = configs.settlement_frame_2d(2, 3, settlement=-0.03, steps=5, grav_steps=10)
     with gpu.DeviceModel(desc) as m:
         U, _, _ = m.run(phases)
     tags = list(desc.node_tag)

@@ -39,11 +39,13 @@ __device__ __forceinline__ void ff_madd(float2 a, float2 x, float &sh, float &sl
   sl = __fadd_rn(sl, __fadd_rn(err, e));
 }
 
-// Whether a value can be split without leaving single precision's range
-// (products of two split values stay finite and normal).
+// Whether a value can enter a float-float product: zero, or 2^-50 <= |v|
+// < 2^50.  A product of two such values lies in [2^-100, 2^100], its
+// rounding error and cross terms (2^-24 and 2^-48 of it) stay normal
+// single-precision numbers, and a sum of up to 2^20 of them stays finite.
 __device__ __forceinline__ bool ff_range(double v) {
   const double a = fabs(v);
-  return a == 0.0 || (a >= 0x1p-100 && a < 0x1p100);
+  return a == 0.0 || (a >= 0x1p-50 && a < 0x1p50);
 }
 
 // The pair as a double.

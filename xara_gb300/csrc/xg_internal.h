@@ -37,6 +37,9 @@ struct ContinuumView {
   // Jacobian determinant at [24*npts + pt], formed once (the geometry does
   // not change); null: formed in every kernel that needs them
   const double *geo;
+  // bricks: the same dN/dx split into float pairs (hi, lo), for the
+  // float-float tangent; null: the tangent is formed in FP64
+  const float2 *geo2;
 };
 
 // CSR system and deterministic gather assembly.
@@ -57,7 +60,8 @@ int launch_quad_update(const ContinuumView &v, cudaStream_t s);
 int launch_quad_assemble(const ContinuumView &v, cudaStream_t s);
 int launch_brick_update(const ContinuumView &v, cudaStream_t s);
 int launch_brick_assemble(const ContinuumView &v, cudaStream_t s);
-int launch_brick_geometry(const ContinuumView &v, double *geo, cudaStream_t s);
+int launch_brick_geometry(const ContinuumView &v, double *geo, float2 *geo2, int *bad,
+                          cudaStream_t s);
 // recorders: kind 0 writes one row ([t] values), kind 1 updates an envelope
 int launch_record(int kind, int n, const int *idx, const double *src, double t, int echo,
                   int first, double *out, cudaStream_t s);

@@ -12,6 +12,7 @@
 
 #include <cstdint>
 
+#include "xg_ff.h"
 #include "xg_internal.h"
 #include "xg_rcp.h"
 
@@ -366,7 +367,17 @@ __device__ __forceinline__ double brick_point_grad(const ContinuumView &v, long 
   return shp3d_grad(xn, xl, g);
 }
 
-__global__ void k_brick_geometry(ContinuumView v, double *geo) {
+// Whether a geometric value splits into a float pair without leaving the
+// normal single-precision range: zero, or 2^-100 <= |v| < 2^100.
+__device__ __forceinline__ bool geo_splits(double v) {
+  const double a = fabs(v);
+  return a == 0.0 || (a >= 0x1p-100 && a < 0x1p100);
+}
+
+// Stored geometry of every point; geo2 (when given) receives dN/dx split
+// into float pairs for the float-float tangent, *bad counts the points with
+// a value outside the split's range.
+__global__ void k_brick_geometry(ContinuumView v, double *geo, float2 *geo2, int *bad) {
   const long npts = (long)v.ne * 8;
   const long pt = (long)blockIdx.x * blockDim.x + threadIdx.x;
   if (pt >= npts) return;
@@ -374,11 +385,19 @@ __global__ void k_brick_geometry(ContinuumView v, double *geo) {
   u.geo = nullptr;
   double g[3][8];
   const double dvol = brick_point_grad(u, npts, pt, g);
+  bool ok = true;
 #pragma unroll
   for (int i = 0; i < 3; i++)
 #pragma unroll
-    for (int a = 0; a < 8; a++) geo[(8 * i + a) * npts + pt] = g[i][a];
+    for (int a = 0; a < 8; a++) {
+      geo[(8 * i + a) * npts + pt] = g[i][a];
+      if (geo2) {
+        geo2[(8 * i + a) * npts + pt] = split2(g[i][a]);
+        ok = ok && geo_splits(g[i][a]);
+      }
+    }
   geo[24 * npts + pt] = dvol;
+  if (!ok) atomicAdd(bad, 1);
 }
 
 __global__ void k_brick_update(ContinuumView v) {
@@ -537,6 +556,198 @@ __global__ void __launch_bounds__(32 * kBrickWarps) k_brick_assemble(ContinuumVi
     for (int i = 0; i < 3; i++)
 #pragma unroll
       for (int k = 0; k < 3; k++) Ke[3 * i + k] = acc[i][k];
+  }
+}
+
+// The float-float form of k_brick_assemble: the same staging and lane
+// layout, the 36 node-pair blocks summed on the single-precision pipes.  An
+// FP64 FMA holds GB300's FP64 pipe for many cycles; a float-float product
+// (xg_ff.h) costs about twelve single-precision instructions and keeps 46
+// bits of each product, so the tangent carries the reference's values to a
+// few units of 2^-46 of the row's largest entry.  The resisting force stays
+// in FP64 (it sets the converged state).  Each element's staged values are
+// scaled by powers of two -- the dN/dx by 2^-eg, the tangent scalings
+// dvol*{a, b/2, c} by 2^-ed, the largest magnitudes of the element -- so
+// every product lies near 1 whatever the model's units; the scale comes back
+// exactly in the exponent when the pair is written as a double.
+struct BrickSmemFF {
+  float2 g[kBrickEPW][8][8][3];    // dN/dx * 2^-eg per point, node
+  float2 h[kBrickEPW][8][8][3];    // n . dN/dx * 2^-eg
+  float2 u[kBrickEPW][8][8][3];    // dvol*a * 2^-ed * dN/dx * 2^-eg
+  float2 vv[kBrickEPW][8][8][3];   // dvol*b/2 * 2^-ed * dN/dx * 2^-eg
+  float2 w[kBrickEPW][8][8][3];    // dvol*c * 2^-ed * n . dN/dx * 2^-eg
+  double gd[kBrickEPW][8][8][3];   // dN/dx (FP64, for the resisting force)
+  double ss[kBrickEPW][8][6];      // dvol*stress
+  int scale[kBrickEPW];            // 2 eg + ed
+};
+
+// Unbiased exponent of a nonzero float / double from its bits (-127 / -1023
+// for zero).
+__device__ __forceinline__ int f32_exponent(float f) {
+  return (int)((__float_as_uint(f) >> 23) & 0xff) - 127;
+}
+__device__ __forceinline__ int f64_exponent(double d) {
+  return (int)(((unsigned)__double2hiint(d) >> 20) & 0x7ff) - 1023;
+}
+
+// (h, l) = a * b rounded to a float pair
+__device__ __forceinline__ float2 ff_mul(float2 a, float2 b) {
+  const float p = __fmul_rn(a.x, b.x);
+  float e = __fmaf_rn(a.x, b.x, -p);
+  e = __fmaf_rn(a.x, b.y, e);
+  e = __fmaf_rn(a.y, b.x, e);
+  const float hi = __fadd_rn(p, e);
+  return make_float2(hi, __fsub_rn(e, __fsub_rn(hi, p)));
+}
+
+// (sh, sl) += (dh, dl)
+__device__ __forceinline__ void ff_add(float dh, float dl, float &sh, float &sl) {
+  const float t = __fadd_rn(sh, dh);
+  const float bp = __fsub_rn(t, sh);
+  const float err = __fadd_rn(__fsub_rn(sh, __fsub_rn(t, bp)), __fsub_rn(dh, bp));
+  sh = t;
+  sl = __fadd_rn(sl, __fadd_rn(err, dl));
+}
+
+// f * 2^s as a double, from the bits (no FP64 instruction); a subnormal f
+// (below 2^-126 of the element's unit scale) is taken as zero.
+__device__ __forceinline__ double f32_to_f64_scaled(float f, int s) {
+  const unsigned u = __float_as_uint(f);
+  const unsigned sign = u & 0x80000000u, m = u & 0x7fffffu;
+  const int e8 = (int)((u >> 23) & 0xff);
+  if (e8 == 0) return 0.0;
+  if (e8 == 255) return __hiloint2double((int)(sign | 0x7ff00000u | (m >> 3)), (int)(m << 29));
+  const int de = e8 + (1023 - 127) + s;
+  if (de <= 0) return 0.0;
+  if (de >= 2047) return __hiloint2double((int)(sign | 0x7ff00000u), 0);
+  return __hiloint2double((int)(sign | ((unsigned)de << 20) | (m >> 3)), (int)(m << 29));
+}
+
+__global__ void __launch_bounds__(32 * kBrickWarps) k_brick_assemble_ff(ContinuumView v) {
+  __shared__ BrickSmemFF sm_all[kBrickWarps];
+  const int wi = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  BrickSmemFF &S = sm_all[wi];
+  const int e0 = (blockIdx.x * kBrickWarps + wi) * kBrickEPW;
+  if (e0 >= v.ne) return;
+  const long npts = (long)v.ne * 8;
+  {
+    const int el = lane >> 3, ip = lane & 7, e = e0 + el;
+    const bool live = e < v.ne;
+    const long pt = (long)(live ? e : e0) * 8 + ip;
+    // FP64 dN/dx for the resisting force, and the element's largest exponent
+    int eg = -1000, ed = -1000;
+#pragma unroll
+    for (int i = 0; i < 3; i++)
+#pragma unroll
+      for (int a = 0; a < 8; a++) {
+        const double gv = v.geo[(8 * i + a) * npts + pt];
+        S.gd[el][ip][a][i] = gv;
+        eg = max(eg, f64_exponent(gv));
+      }
+    const double dvol = v.geo[24 * npts + pt];
+    const double ca = v.tan[pt], cb = v.tan[npts + pt], cc = v.tan[2 * npts + pt];
+    const double da = dvol * ca, dbh = dvol * (0.5 * cb), dc = dvol * cc;
+    ed = max(max(f64_exponent(da), f64_exponent(dbh)), f64_exponent(dc));
+#pragma unroll
+    for (int o = 1; o < 8; o <<= 1) {
+      eg = max(eg, __shfl_xor_sync(0xffffffffu, eg, o));
+      ed = max(ed, __shfl_xor_sync(0xffffffffu, ed, o));
+    }
+    if (eg < -126) eg = 0;      // all of dN/dx zero: a degenerate element
+    if (ed < -1000) ed = 0;
+    ed = min(ed, 1022);         // a non-finite scaling stays non-finite below
+    if (ip == 0) S.scale[el] = 2 * eg + ed;
+#pragma unroll
+    for (int c = 0; c < 6; c++) S.ss[el][ip][c] = dvol * v.sig[c * npts + pt];
+    // 2^-ed as a double and 2^-eg as a float (|eg| < 100 for split geometry)
+    const double pd = __hiloint2double((int)((unsigned)(1023 - ed) << 20), 0);
+    const float fg = __uint_as_float((unsigned)(127 - eg) << 23);
+    const float2 sa = split2(da * pd), sb = split2(dbh * pd), sc = split2(dc * pd);
+    float2 n[6];
+#pragma unroll
+    for (int c = 0; c < 6; c++) n[c] = split2(v.tan[(3 + c) * npts + pt]);
+#pragma unroll 2
+    for (int a = 0; a < 8; a++) {
+      float2 gi[3];
+#pragma unroll
+      for (int i = 0; i < 3; i++) {
+        const float2 q = v.geo2[(8 * i + a) * npts + pt];
+        gi[i] = make_float2(__fmul_rn(q.x, fg), __fmul_rn(q.y, fg));
+      }
+      // h = n . g with n = [xx yy zz xy yz zx]
+      const int row[3][3] = {{0, 3, 5}, {3, 1, 4}, {5, 4, 2}};
+#pragma unroll
+      for (int i = 0; i < 3; i++) {
+        float hh = 0.f, hl = 0.f;
+#pragma unroll
+        for (int j = 0; j < 3; j++) ff_madd(n[row[i][j]], gi[j], hh, hl);
+        const float hs = __fadd_rn(hh, hl);
+        const float2 hi = make_float2(hs, __fsub_rn(hl, __fsub_rn(hs, hh)));
+        S.g[el][ip][a][i] = gi[i];
+        S.h[el][ip][a][i] = hi;
+        S.u[el][ip][a][i] = ff_mul(sa, gi[i]);
+        S.vv[el][ip][a][i] = ff_mul(sb, gi[i]);
+        S.w[el][ip][a][i] = ff_mul(sc, hi);
+      }
+    }
+  }
+  __syncwarp();
+  for (int t = lane; t < kBrickEPW * 24; t += 32) {
+    const int el = t / 24, q = t % 24, e = e0 + el;
+    if (e >= v.ne) continue;
+    const int a = q / 3, i = q % 3;
+    const int r0 = (i == 0) ? 0 : (i == 1) ? 3 : 5;
+    const int r1 = (i == 0) ? 3 : (i == 1) ? 1 : 4;
+    const int r2 = (i == 0) ? 5 : (i == 1) ? 4 : 2;
+    double r = 0.0;
+#pragma unroll
+    for (int ip = 0; ip < 8; ip++)
+      r += S.gd[el][ip][a][0] * S.ss[el][ip][r0] + S.gd[el][ip][a][1] * S.ss[el][ip][r1] +
+           S.gd[el][ip][a][2] * S.ss[el][ip][r2];
+    v.Re[(long)e * 24 + q] = r;
+  }
+  for (int t = lane; t < kBrickEPW * 36; t += 32) {
+    const int el = t / 36, pp = t % 36, e = e0 + el;
+    if (e >= v.ne) continue;
+    const int a = kPairA[pp], b = kPairB[pp];
+    float ah[3][3], al[3][3];
+#pragma unroll
+    for (int i = 0; i < 3; i++)
+#pragma unroll
+      for (int k = 0; k < 3; k++) ah[i][k] = al[i][k] = 0.f;
+#pragma unroll 2
+    for (int ip = 0; ip < 8; ip++) {
+      float2 gb[3], hb[3], ua[3], va[3], wa[3];
+#pragma unroll
+      for (int j = 0; j < 3; j++) {
+        gb[j] = S.g[el][ip][b][j];
+        hb[j] = S.h[el][ip][b][j];
+        ua[j] = S.u[el][ip][a][j];
+        va[j] = S.vv[el][ip][a][j];
+        wa[j] = S.w[el][ip][a][j];
+      }
+      // (b/2) dvol dNa . dNb on the diagonal
+      float dh = 0.f, dl = 0.f;
+#pragma unroll
+      for (int j = 0; j < 3; j++) ff_madd(va[j], gb[j], dh, dl);
+#pragma unroll
+      for (int i = 0; i < 3; i++) {
+#pragma unroll
+        for (int k = 0; k < 3; k++) {
+          ff_madd(ua[i], gb[k], ah[i][k], al[i][k]);
+          ff_madd(va[k], gb[i], ah[i][k], al[i][k]);
+          ff_madd(wa[i], hb[k], ah[i][k], al[i][k]);
+        }
+        ff_add(dh, dl, ah[i][i], al[i][i]);
+      }
+    }
+    const int sc = S.scale[el];
+    double *Ke = v.Ke + (long)e * 324 + pp * 9;
+#pragma unroll
+    for (int i = 0; i < 3; i++)
+#pragma unroll
+      for (int k = 0; k < 3; k++)
+        Ke[3 * i + k] = f32_to_f64_scaled(ah[i][k], sc) + f32_to_f64_scaled(al[i][k], sc);
   }
 }
 
@@ -732,15 +943,19 @@ int launch_brick_update(const ContinuumView &v, cudaStream_t s) {
   k_brick_update<<<nblocks((long)v.ne * 8), kThreads, 0, s>>>(v);
   return check_launch();
 }
-int launch_brick_geometry(const ContinuumView &v, double *geo, cudaStream_t s) {
+int launch_brick_geometry(const ContinuumView &v, double *geo, float2 *geo2, int *bad,
+                          cudaStream_t s) {
   if (v.ne == 0) return 0;
-  k_brick_geometry<<<nblocks((long)v.ne * 8), kThreads, 0, s>>>(v, geo);
+  k_brick_geometry<<<nblocks((long)v.ne * 8), kThreads, 0, s>>>(v, geo, geo2, bad);
   return check_launch();
 }
 int launch_brick_assemble(const ContinuumView &v, cudaStream_t s) {
   if (v.ne == 0) return 0;
   constexpr int per_block = kBrickWarps * kBrickEPW;
-  k_brick_assemble<<<(v.ne + per_block - 1) / per_block, 32 * kBrickWarps, 0, s>>>(v);
+  if (v.geo && v.geo2)
+    k_brick_assemble_ff<<<(v.ne + per_block - 1) / per_block, 32 * kBrickWarps, 0, s>>>(v);
+  else
+    k_brick_assemble<<<(v.ne + per_block - 1) / per_block, 32 * kBrickWarps, 0, s>>>(v);
   return check_launch();
 }
 int launch_j2_zero_state(const ContinuumView &v, cudaStream_t s) {

@@ -184,6 +184,7 @@ struct xg_model {
   DBuf<double> d_sell_vals, d_chunk_part, d_p2;   // (hi, lo) float pairs, 8 bytes each
   DBuf<unsigned char> d_row_ff;
   DBuf<double> d_geo;   // bricks: per-point shape-function gradients and Jacobian determinant
+  DBuf<float2> d_geo2;  // bricks: the gradients split into float pairs (float-float tangent)
   DBuf<int> d_chunk_row, d_chunk_beg, d_long_chunk0;
   bool sell_tried = false;
   int ensure_pcg_sell();
@@ -367,6 +368,7 @@ struct xg_model {
     v.sig = d_sig.p; v.tan = d_tan.p; v.nfail = d_nfail.p;
     v.Ke = d_Ke.p; v.Re = d_Re.p;
     v.geo = d_geo.p;
+    v.geo2 = d_geo2.p;
     return v;
   }
   bool frames() const { return etype == XG_ELE_FBC2D || etype == XG_ELE_FBC3D; }
@@ -781,7 +783,15 @@ int xg_model::upload(const HostGather &gk_h, const HostGather &gr_h) {
   } else {
     if (etype == XG_ELE_BRICK) {
       RET(d_geo.alloc((size_t)25 * np));
-      RET(launch_brick_geometry(view(), d_geo.p, s));
+      RET(d_geo2.alloc((size_t)24 * np));
+      CK(cudaMemsetAsync(d_nfail.p, 0, sizeof(int), s));
+      RET(launch_brick_geometry(view(), d_geo.p, d_geo2.p, d_nfail.p, s));
+      int bad = 0;
+      CK(cudaMemcpyAsync(&bad, d_nfail.p, sizeof(int), cudaMemcpyDeviceToHost, s));
+      CK(cudaStreamSynchronize(s));
+      CK(cudaMemsetAsync(d_nfail.p, 0, sizeof(int), s));
+      // a gradient outside the float pairs' range: the tangent in FP64
+      if (bad) d_geo2.free();
     }
     // zero-strain material state
     RET(launch_j2_zero_state(view(), s));
