@@ -1168,6 +1168,19 @@ def brick_alg_bytes(npts, ne, nn, nnz, neq):
     }
 
 
+def pcg_iteration_bytes(kb, blocks, nnz, neq):
+    """Bytes one PCG iteration must move.  With the node-block copy (block
+    order kb > 0): per block its kb*kb values as float pairs (8 B each, the
+    zero padding of nodes with fewer free dofs included) and a 4 B column
+    index; without it: per CSR entry an 8 B value and a 4 B column.  Per
+    equation 131 B of vectors: q written and p read by the SpMV (16), x and r
+    read and written, p and q read, z written (56), the inverted diagonal
+    block (24 for 3 x 3 blocks), z and p read, p written and its split copy
+    (35)."""
+    matrix = blocks * (8 * kb * kb + 4) if kb > 0 else 12 * nnz
+    return matrix + 131 * neq
+
+
 def brick_cpu_sample(seconds=12.0):
     from oracle import port
     from xara_gb300 import configs
@@ -1294,13 +1307,17 @@ def run_brick(args):
             t_it.append(ev0.elapsed_time(ev1) * 1e-3)
         gpu.profile_enable(m, False)
         pcg_it = it_c.value
-        pcg_bytes = 12 * m.nnz + 100 * m.neq       # per PCG iteration
+        kb, nblocks, nchunked = C.c_int(), C.c_longlong(), C.c_longlong()
+        gpu._check(L.xg_model_pcg_layout(m.h, C.byref(kb), C.byref(nblocks), C.byref(nchunked)))
+        pcg_bytes = pcg_iteration_bytes(kb.value, nblocks.value, m.nnz, m.neq)
         pcg_s = t_it[-1] - dt / args.steps         # the iteration less its element phase
         newton = {"newton_iters_per_s": 1.0 / t_it[-1], "ms_per_newton_iteration": 1e3 * t_it[-1],
                   "pcg_iterations": pcg_it, "pcg_relative_residual": rr_c.value,
                   "pcg_ms": 1e3 * pcg_s, "pcg_ms_per_iteration": 1e3 * pcg_s / max(pcg_it, 1),
                   "pcg_GBps": pcg_bytes * pcg_it / pcg_s / 1e9 if pcg_s > 0 else None,
                   "pcg_bytes_per_iteration": pcg_bytes,
+                  "pcg_block_order": kb.value, "pcg_blocks": nblocks.value,
+                  "pcg_chunked_rows": nchunked.value,
                   "rhs": "seeded random right-hand side, x0 = 0, rtol 1e-10",
                   "ip_updates_per_s": npts / t_it[-1]}
 

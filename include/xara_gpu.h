@@ -348,6 +348,14 @@ int xg_analysis_graph_steps(const xg_model *m, long *steps);
    callers that time or order their own work against it. */
 int xg_model_stream(const xg_model *m, void **stream);
 
+/* Layout of the PCG's node-block copy of the tangent (built at the first
+   PCG solve): its block order (2, 3 or 6: the largest number of free dofs
+   of a node; 0 while no copy exists, the solve then reading the CSR arrays),
+   the number of node-pair blocks held and the rows left to the CSR chunks
+   (those of nodes coupled to more than 96 nodes). */
+int xg_model_pcg_layout(const xg_model *m, int *block_order, long long *blocks,
+                        long long *chunked_rows);
+
 /* Work counters since xg_profile_enable: material-point state
    determinations (J2 points; for frames every fiber of every section in
    every compatibility iteration), section state determinations (frames)

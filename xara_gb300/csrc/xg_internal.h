@@ -76,42 +76,57 @@ struct PcgSystem {
   const double *vals;
   int nblk;
   const int *blk_start;   // [nblk+1] equation ranges of the diagonal blocks (<= 6)
-  double *binv;           // [nblk*36] inverted diagonal blocks (row major, padded to 6x6)
+  double *binv;           // inverted diagonal blocks, row major: [nblk*kb*kb], or [nblk*36]
+                          // (padded to 6 x 6) when kb is 0
   // work vectors [n]
   double *r, *z, *p, *q;
-  double *partials;       // [2*max_blocks + 8]
+  double *partials;       // [3*pcg_max_blocks() + 8]
   unsigned int *barrier;  // [2] grid barrier state
   int *flags;             // [4] status words
   double *scalars;        // [8]
-  // optional sliced ELL copy of the matrix (thread-per-row SpMV) for rows of
-  // at most sell_cap entries, longer rows in chunks of CSR entries, a warp
-  // each; sell_vals null: every row is read from the CSR arrays warp per row.
-  // The sliced SpMV computes in float-float (each value and each entry of p
-  // split into two single-precision numbers) on the single-precision pipes;
-  // rows with a value outside 2^-100 .. 2^100 in magnitude stay in FP64.
-  const long *sell_off;   // [ceil(n/32)+1] slice offsets
-  const int *sell_cols;   // [sell_off[last]]
-  float2 *sell_vals;      // [sell_off[last]] (hi, lo), packed from vals by pcg_factor_blocks
-  unsigned char *row_ff;  // [n] 1: the row's values lie in the split's range
-  float2 *p2;             // [n] p split into (hi, lo)
-  int sell_cap;
+  // optional node-block sliced ELL copy of the matrix (thread per node row:
+  // the equations of one diagonal block against KB x KB blocks of the nodes
+  // it couples to, one column index per block) for node rows of at most
+  // nb_cap blocks; the rows of longer node rows in chunks of CSR entries, a
+  // warp each; nb_vals null: every row is read from the CSR arrays warp per
+  // row.  The block SpMV computes in float-float (each value and each entry
+  // of p split into two single-precision numbers, xg_ff.h) on the
+  // single-precision pipes; node rows with a value outside the split's range
+  // stay in FP64.
+  int kb;                 // block order: 2, 3 or 6 (the largest diagonal block), 0: no copy
+  const long *nb_off;     // [ceil(nblk/32)+1] slice offsets, in blocks
+  const int *nb_cols;     // [nb_off[last]] column node of each block
+  const int *nb_len;      // [nblk] blocks of each node row
+  const int *nb_pos;      // [nnz] slot of each CSR entry in nb_vals (-1: a long node row's)
+  float2 *nb_vals;        // [nb_off[last]*kb*kb] (hi, lo), packed by pcg_factor_blocks
+  unsigned char *blk_ff;  // [nblk] 1: the node row's values lie in the split's range
+  float2 *p2;             // [nblk*(kb == 3 ? 4 : kb)] p split, node-major, padding zero
+  int nb_cap;
   int nlong, nchunks;     // long rows, their chunks
   const int *chunk_row;   // [nchunks] row of each chunk
   const int *chunk_beg;   // [nchunks] first CSR entry of each chunk
   const int *long_chunk0; // [nlong+1] chunk range of each long row
   double *chunk_part;     // [nchunks] partial sums
 };
-// Factor the diagonal blocks (and pack the sliced ELL values when present)
+// Factor the diagonal blocks (and pack the node-block values when present)
 // after the matrix values changed.
 int pcg_factor_blocks(const PcgSystem &S, cudaStream_t s);
-// Sliced ELL layout of a CSR pattern for rows of at most cap entries (slice
-// offsets, then the column array) and the chunks of the longer rows.
-void sell_layout(int n, const int *rowptr, int cap, std::vector<long> &off,
-                 std::vector<int> &chunk_row, std::vector<int> &chunk_beg,
-                 std::vector<int> &long_chunk0);
-void sell_columns(int n, const int *rowptr, const int *colidx, int cap,
-                  const std::vector<long> &off, std::vector<int> &cols);
-int pcg_sell_max_blocks();
+// Host layout of the node-block copy of a CSR pattern whose diagonal blocks
+// are blk_start's equation ranges (1..6 equations each): block order,
+// slices, column nodes, each CSR entry's slot, and the chunks of the rows of
+// node rows with more than cap blocks.  kb stays 0 (no copy) when a block
+// is larger than 6 or the slots overflow 32-bit positions.
+struct BlockEll {
+  int kb = 0;
+  std::vector<long> off;
+  std::vector<int> cols, len, pos;
+  std::vector<int> chunk_row, chunk_beg, long_chunk0;
+};
+int block_ell_layout(int n, const int *rowptr, const int *colidx, int nblk, const int *blk_start,
+                     int cap, BlockEll &h);
+// Device bytes of the copy (columns, values, positions, offsets, per-node
+// arrays and p2).
+size_t block_ell_bytes(const BlockEll &h, int nblk);
 // Solve A x = b (device vectors).  x holds the initial guess (usually 0).
 // Returns 0 when converged, XG_ESOLVE on breakdown, maxit or a barrier timeout.
 // rows_per_block: the grid gets one block per that many rows (capped by

@@ -57,12 +57,12 @@ struct xg_linsoe {
   // device copies, set up at the first solve
   bool ready = false;
   cudaStream_t stream = nullptr;
-  DevArray<int> rp, ci, bs, chunk_row, chunk_beg, long_chunk0, sell_cols, flags;
-  DevArray<long> sell_off;
+  DevArray<int> rp, ci, bs, chunk_row, chunk_beg, long_chunk0, nb_cols, nb_len, nb_pos, flags;
+  DevArray<long> nb_off;
   DevArray<unsigned int> barrier;
   DevArray<double> vals, b, x, binv, r, z, p, q, partials, scalars, chunk_part;
-  DevArray<float2> sell_vals, p2;
-  DevArray<unsigned char> row_ff;
+  DevArray<float2> nb_vals, p2;
+  DevArray<unsigned char> blk_ff;
   xg::PcgSystem S{};
   // `system ProfileSPD`: the device LDL', factored once per matrix
   int system = XG_SYSTEM_BJPCG;
@@ -100,11 +100,13 @@ struct xg_linsoe {
       return lfail(XG_ECUDA, "xg_linsoe: stream creation failed");
     const int nblk = (int)blk.size() - 1;
     const size_t nnz = colidx.size(), nv = std::max(n, 1);
-    constexpr int kCap = 256;
-    std::vector<long> off;
-    std::vector<int> crow, cbeg, lc0, cols;
-    xg::sell_layout(n, rowptr.data(), kCap, off, crow, cbeg, lc0);
-    xg::sell_columns(n, rowptr.data(), colidx.data(), kCap, off, cols);
+    constexpr int kCap = 96;
+    xg::BlockEll h;
+    xg::block_ell_layout(n, rowptr.data(), colidx.data(), nblk, blk.data(), kCap, h);
+    size_t freeb = 0, totalb = 0;
+    if (h.kb && (cudaMemGetInfo(&freeb, &totalb) != cudaSuccess ||
+                 xg::block_ell_bytes(h, nblk) > freeb / 2))
+      h = xg::BlockEll{};
     int e = 0;
     e |= rp.upload(rowptr.data(), rowptr.size(), stream);
     e |= ci.upload(colidx.data(), nnz, stream);
@@ -112,16 +114,26 @@ struct xg_linsoe {
     e |= vals.alloc(std::max<size_t>(nnz, 1)) | b.alloc(nv) | x.alloc(nv);
     e |= binv.alloc((size_t)std::max(nblk, 1) * 36);
     e |= r.alloc(nv) | z.alloc(nv) | p.alloc(nv) | q.alloc(nv);
-    e |= partials.alloc(3 * (size_t)std::max(xg::pcg_max_blocks(), xg::pcg_sell_max_blocks()) + 8);
+    e |= partials.alloc(3 * (size_t)xg::pcg_max_blocks() + 8);
     e |= scalars.alloc(8) | barrier.alloc(2) | flags.alloc(4);
-    e |= sell_off.upload(off.data(), off.size(), stream);
-    e |= sell_cols.upload(cols.data(), cols.size(), stream);
-    e |= sell_vals.alloc(std::max<size_t>(cols.size(), 1)) | p2.alloc(nv) | row_ff.alloc(nv);
-    e |= chunk_row.upload(crow.data(), crow.size(), stream);
-    e |= chunk_beg.upload(cbeg.data(), cbeg.size(), stream);
-    e |= long_chunk0.upload(lc0.data(), lc0.size(), stream);
-    e |= chunk_part.alloc(std::max<size_t>(crow.size(), 1));
+    size_t nvals = 0, np2 = 0;
+    if (h.kb) {
+      nvals = std::max<size_t>((size_t)h.off.back() * h.kb * h.kb, 1);
+      np2 = (size_t)nblk * (h.kb == 3 ? 4 : h.kb);
+      e |= nb_off.upload(h.off.data(), h.off.size(), stream);
+      e |= nb_cols.upload(h.cols.data(), h.cols.size(), stream);
+      e |= nb_len.upload(h.len.data(), h.len.size(), stream);
+      e |= nb_pos.upload(h.pos.data(), h.pos.size(), stream);
+      e |= nb_vals.alloc(nvals) | p2.alloc(np2) | blk_ff.alloc(std::max(nblk, 1));
+      e |= chunk_row.upload(h.chunk_row.data(), h.chunk_row.size(), stream);
+      e |= chunk_beg.upload(h.chunk_beg.data(), h.chunk_beg.size(), stream);
+      e |= long_chunk0.upload(h.long_chunk0.data(), h.long_chunk0.size(), stream);
+      e |= chunk_part.alloc(std::max<size_t>(h.chunk_row.size(), 1));
+    }
     if (e) return lfail(XG_ENOMEM, "xg_linsoe: device allocation failed");
+    if (h.kb && (cudaMemsetAsync(nb_vals.p, 0, nvals * sizeof(float2), stream) != cudaSuccess ||
+                 cudaMemsetAsync(p2.p, 0, np2 * sizeof(float2), stream) != cudaSuccess))
+      return lfail(XG_ECUDA, "xg_linsoe: set-up copies failed");
     S.n = n;
     S.rowptr = rp.p;
     S.colidx = ci.p;
@@ -137,18 +149,23 @@ struct xg_linsoe {
     S.barrier = barrier.p;
     S.flags = flags.p;
     S.scalars = scalars.p;
-    S.sell_off = sell_off.p;
-    S.sell_cols = sell_cols.p;
-    S.sell_vals = sell_vals.p;
-    S.p2 = p2.p;
-    S.row_ff = row_ff.p;
-    S.sell_cap = kCap;
-    S.nlong = (int)lc0.size() - 1;
-    S.nchunks = (int)crow.size();
-    S.chunk_row = chunk_row.p;
-    S.chunk_beg = chunk_beg.p;
-    S.long_chunk0 = long_chunk0.p;
-    S.chunk_part = chunk_part.p;
+    S.kb = h.kb;
+    if (h.kb) {
+      S.nb_off = nb_off.p;
+      S.nb_cols = nb_cols.p;
+      S.nb_len = nb_len.p;
+      S.nb_pos = nb_pos.p;
+      S.nb_vals = nb_vals.p;
+      S.blk_ff = blk_ff.p;
+      S.p2 = p2.p;
+      S.nb_cap = kCap;
+      S.nlong = (int)h.long_chunk0.size() - 1;
+      S.nchunks = (int)h.chunk_row.size();
+      S.chunk_row = chunk_row.p;
+      S.chunk_beg = chunk_beg.p;
+      S.long_chunk0 = long_chunk0.p;
+      S.chunk_part = chunk_part.p;
+    }
     if (cudaStreamSynchronize(stream) != cudaSuccess)
       return lfail(XG_ECUDA, "xg_linsoe: set-up copies failed");
     ready = true;

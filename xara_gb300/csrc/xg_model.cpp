@@ -179,15 +179,17 @@ struct xg_model {
   // sliced ELL copy of the matrix for the PCG's SpMV, built at the first
   // PCG solve (skipped, keeping the CSR SpMV, when it would take more than
   // half of the free device memory)
-  DBuf<long> d_sell_off;
-  DBuf<int> d_sell_cols;
-  DBuf<double> d_sell_vals, d_chunk_part, d_p2;   // (hi, lo) float pairs, 8 bytes each
-  DBuf<unsigned char> d_row_ff;
+  DBuf<long> d_nb_off;
+  DBuf<int> d_nb_cols, d_nb_len, d_nb_pos;
+  DBuf<float2> d_nb_vals, d_p2;
+  DBuf<double> d_chunk_part;
+  DBuf<unsigned char> d_blk_ff;
   DBuf<double> d_geo;   // bricks: per-point shape-function gradients and Jacobian determinant
   DBuf<float2> d_geo2;  // bricks: the gradients split into float pairs (float-float tangent)
   DBuf<int> d_chunk_row, d_chunk_beg, d_long_chunk0;
-  bool sell_tried = false;
-  int ensure_pcg_sell();
+  bool blocks_tried = false;
+  long long pcg_blocks = 0;   // node-pair blocks of the PCG's copy
+  int ensure_pcg_blocks();
   int pcg_prepare();
   double rtol = 1e-12;
   int maxit = 20000;
@@ -733,7 +735,7 @@ int xg_model::upload(const HostGather &gk_h, const HostGather &gr_h) {
   RET(d_binv.alloc((size_t)std::max(nblk, 1) * 36));
   const size_t nv = neq > 0 ? neq : 1;
   RET(d_r.alloc(nv)); RET(d_z.alloc(nv)); RET(d_p.alloc(nv)); RET(d_q.alloc(nv));
-  RET(d_pcg_part.alloc(3 * (size_t)std::max(pcg_max_blocks(), pcg_sell_max_blocks()) + 8));
+  RET(d_pcg_part.alloc(3 * (size_t)pcg_max_blocks() + 8));
   RET(d_scalars.alloc(8));
   RET(d_barrier.alloc(2));
   RET(d_flags.alloc(4));
@@ -1465,37 +1467,45 @@ int xg_model::record_step() {
   return 0;
 }
 
-int xg_model::ensure_pcg_sell() {
-  if (sell_tried || neq == 0) return 0;
-  sell_tried = true;
-  constexpr int kCap = 256;   // longer rows go in chunks
-  std::vector<long> off;
-  std::vector<int> chunk_row, chunk_beg, long_chunk0;
-  sell_layout(neq, rowptr.data(), kCap, off, chunk_row, chunk_beg, long_chunk0);
-  if (off.back() == 0) return 0;
+int xg_model::ensure_pcg_blocks() {
+  if (blocks_tried || neq == 0) return 0;
+  blocks_tried = true;
+  constexpr int kCap = 96;   // node rows with more blocks go in chunks of CSR entries
+  BlockEll h;
+  const int nblk = (int)blk_start.size() - 1;
+  if (!block_ell_layout(neq, rowptr.data(), colidx.data(), nblk, blk_start.data(), kCap, h))
+    return 0;
   size_t freeb = 0, totalb = 0;
   CK(cudaMemGetInfo(&freeb, &totalb));
-  const size_t need = (size_t)off.back() * (sizeof(double) + sizeof(int)) + off.size() * sizeof(long);
-  if (need > freeb / 2) return 0;
-  std::vector<int> cols;
-  sell_columns(neq, rowptr.data(), colidx.data(), kCap, off, cols);
-  RET(d_sell_off.upload(off.data(), off.size(), stream));
-  RET(d_sell_cols.upload(cols.data(), cols.size(), stream));
-  RET(d_sell_vals.alloc(cols.size()));
-  RET(d_p2.alloc(neq));
-  RET(d_row_ff.alloc(neq));
-  const int nch = (int)chunk_row.size();
-  RET(d_chunk_row.upload(chunk_row.data(), chunk_row.size(), stream));
-  RET(d_chunk_beg.upload(chunk_beg.data(), chunk_beg.size(), stream));
-  RET(d_long_chunk0.upload(long_chunk0.data(), long_chunk0.size(), stream));
+  if (block_ell_bytes(h, nblk) > freeb / 2) return 0;
+  const int ks = h.kb == 3 ? 4 : h.kb;
+  RET(d_nb_off.upload(h.off.data(), h.off.size(), stream));
+  RET(d_nb_cols.upload(h.cols.data(), h.cols.size(), stream));
+  RET(d_nb_len.upload(h.len.data(), h.len.size(), stream));
+  RET(d_nb_pos.upload(h.pos.data(), h.pos.size(), stream));
+  RET(d_nb_vals.alloc(std::max<size_t>((size_t)h.off.back() * h.kb * h.kb, 1)));
+  CK(cudaMemsetAsync(d_nb_vals.p, 0, d_nb_vals.n * sizeof(float2), stream));
+  RET(d_p2.alloc((size_t)nblk * ks));
+  CK(cudaMemsetAsync(d_p2.p, 0, d_p2.n * sizeof(float2), stream));
+  RET(d_blk_ff.alloc(nblk));
+  const int nch = (int)h.chunk_row.size();
+  RET(d_chunk_row.upload(h.chunk_row.data(), h.chunk_row.size(), stream));
+  RET(d_chunk_beg.upload(h.chunk_beg.data(), h.chunk_beg.size(), stream));
+  RET(d_long_chunk0.upload(h.long_chunk0.data(), h.long_chunk0.size(), stream));
   RET(d_chunk_part.alloc(std::max(nch, 1)));
-  pcg.sell_off = d_sell_off.p;
-  pcg.sell_cols = d_sell_cols.p;
-  pcg.sell_vals = reinterpret_cast<float2 *>(d_sell_vals.p);
-  pcg.p2 = reinterpret_cast<float2 *>(d_p2.p);
-  pcg.row_ff = d_row_ff.p;
-  pcg.sell_cap = kCap;
-  pcg.nlong = (int)long_chunk0.size() - 1;
+  pcg.kb = h.kb;
+  pcg_blocks = 0;
+  for (int i = 0; i < nblk; i++)
+    if (h.len[i] <= kCap) pcg_blocks += h.len[i];
+  pcg.nb_off = d_nb_off.p;
+  pcg.nb_cols = d_nb_cols.p;
+  pcg.nb_len = d_nb_len.p;
+  pcg.nb_pos = d_nb_pos.p;
+  pcg.nb_vals = d_nb_vals.p;
+  pcg.blk_ff = d_blk_ff.p;
+  pcg.p2 = d_p2.p;
+  pcg.nb_cap = kCap;
+  pcg.nlong = (int)h.long_chunk0.size() - 1;
   pcg.nchunks = nch;
   pcg.chunk_row = d_chunk_row.p;
   pcg.chunk_beg = d_chunk_beg.p;
@@ -1505,9 +1515,9 @@ int xg_model::ensure_pcg_sell() {
 }
 
 // Before a PCG solve on new matrix values: the diagonal blocks' inverses and
-// the sliced ELL values.
+// the node-block values.
 int xg_model::pcg_prepare() {
-  RET(ensure_pcg_sell());
+  RET(ensure_pcg_blocks());
   RET(pcg_factor_blocks(pcg, stream));
   blocks_factored = true;
   return 0;
@@ -2331,6 +2341,15 @@ int xg_autotune_result(const xg_model *m, int *elem_warps, int *pcg_rows_per_blo
 int xg_model_stream(const xg_model *m, void **stream) {
   if (!m || !stream) return fail(XG_EINVAL, "null argument");
   *stream = (void *)m->stream;
+  return 0;
+}
+
+int xg_model_pcg_layout(const xg_model *m, int *block_order, long long *blocks,
+                        long long *chunked_rows) {
+  if (!m || !block_order || !blocks || !chunked_rows) return fail(XG_EINVAL, "null argument");
+  *block_order = m->pcg.nb_vals ? m->pcg.kb : 0;
+  *blocks = m->pcg_blocks;
+  *chunked_rows = m->pcg.nb_vals ? m->pcg.nlong : 0;
   return 0;
 }
 

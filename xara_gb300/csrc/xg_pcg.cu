@@ -13,6 +13,7 @@
 
 #include <algorithm>
 #include <cstdint>
+#include <iterator>
 #include <vector>
 
 #include "xg_ff.h"
@@ -103,52 +104,112 @@ __device__ __forceinline__ double csr_row64(const PcgSystem &S, int row, const d
   return s;
 }
 
-// Sliced ELL copy of the CSR matrix (thread per row): slice s holds rows
-// 32s .. 32s+31 column-major over the slice's longest row, entry k of row r
-// at sell_off[r/32] + 32k + r%32, so a warp's 32 rows load each entry
-// position with one coalesced access.  Each row is summed in its CSR order
-// into four interleaved float-float partial sums, a fixed order, against
-// p split into (hi, lo) (x2); rows whose values the split cannot hold, or
-// every row when fp64 is set, in FP64 against x.
-__device__ __forceinline__ double spmv_sell(const PcgSystem &S, int row, const double *x,
-                                            const float2 *x2, bool fp64) {
-  if (fp64 || !S.row_ff[row]) return csr_row64(S, row, x);
-  const int len = S.rowptr[row + 1] - S.rowptr[row];
-  const long base = S.sell_off[row >> 5] + (row & 31);
-  const int *cp = S.sell_cols + base;
-  const float2 *vp = S.sell_vals + base;
-  float h0 = 0.f, l0 = 0.f, h1 = 0.f, l1 = 0.f, h2 = 0.f, l2 = 0.f, h3 = 0.f, l3 = 0.f;
-  int k = 0;
-  for (; k + 4 <= len; k += 4) {
-    const int c0 = __ldcs(cp + 32 * k), c1 = __ldcs(cp + 32 * (k + 1));
-    const int c2 = __ldcs(cp + 32 * (k + 2)), c3 = __ldcs(cp + 32 * (k + 3));
-    const float2 v0 = __ldcs(vp + 32 * k), v1 = __ldcs(vp + 32 * (k + 1));
-    const float2 v2 = __ldcs(vp + 32 * (k + 2)), v3 = __ldcs(vp + 32 * (k + 3));
-    ff_madd(v0, x2[c0], h0, l0);
-    ff_madd(v1, x2[c1], h1, l1);
-    ff_madd(v2, x2[c2], h2, l2);
-    ff_madd(v3, x2[c3], h3, l3);
+// Order of the stored inverse diagonal blocks: the node-block order, or 6
+// (each block padded to 6 x 6) for a system without a node-block copy.
+__device__ __forceinline__ int binv_order(const PcgSystem &S) { return S.kb > 0 ? S.kb : 6; }
+
+// Stride of a node's slots in p2: the block order, 3 rounded up to 4 so that
+// a node's entries are one aligned 32-byte sector.
+template <int KB>
+struct NodeSlots {
+  static constexpr int kStride = KB == 3 ? 4 : KB;
+};
+
+template <int KB>
+__device__ __forceinline__ void load_p2_node(const float2 *p2, int j, float2 *xb) {
+  constexpr int KS = NodeSlots<KB>::kStride;
+  if constexpr (KS == 1) {
+    xb[0] = p2[j];
+  } else {
+    const float4 *src = reinterpret_cast<const float4 *>(p2 + (long)j * KS);
+#pragma unroll
+    for (int t = 0; t < KS / 2; t++) {
+      const float4 v = src[t];
+      xb[2 * t] = make_float2(v.x, v.y);
+      xb[2 * t + 1] = make_float2(v.z, v.w);
+    }
   }
-  for (; k < len; k++) ff_madd(__ldcs(vp + 32 * k), x2[__ldcs(cp + 32 * k)], h0, l0);
-  return (((double)h0 + (double)l0) + ((double)h1 + (double)l1)) +
-         (((double)h2 + (double)l2) + ((double)h3 + (double)l3));
 }
 
-// f(row, (A x)[row]) for this thread's rows: thread per row over the sliced
-// ELL copy (kSell; rows longer than S.sell_cap are left to
-// long_row_chunks), else warp per CSR row (lane 0 calls f).
-// With kSell: x2 is x split into (hi, lo) for the float-float SpMV, or null
-// for FP64 throughout (the initial residual, or a p outside the split's
-// range).
-template <bool kSell, typename F>
-__device__ __forceinline__ void for_rows_Ax(const PcgSystem &S, const double *x,
-                                            const float2 *x2, F f) {
+// Node-block sliced ELL copy of the matrix, thread per node row: the
+// equations of node i (its diagonal block, m <= KB of them) against the
+// nodes j it couples to, each coupling a KB x KB block (zero-padded where a
+// node has fewer free dofs).  Slice s holds node rows 32s .. 32s+31; block k
+// of node row i has its column node at nb_cols[nb_off[s] + 32k + i%32] and
+// entry (a, b) at nb_vals[nb_off[s]*KB*KB + (k*KB*KB + a*KB + b)*32 + i%32],
+// so a warp's 32 node rows read each entry position with one coalesced
+// access and one column index serves KB*KB values.  p is held split into
+// (hi, lo) float pairs, node-major with NodeSlots<KB>::kStride slots per
+// node (p2), so a block's KB entries of p are one aligned load.  Each row is
+// summed in float-float (xg_ff.h) over the node's blocks in order, even and
+// odd blocks into separate partial sums, a fixed order.
+template <int KB>
+__device__ __forceinline__ void node_row_ff(const PcgSystem &S, int i, double *y) {
+  constexpr int KS = NodeSlots<KB>::kStride;
+  constexpr int KK = KB * KB;
+  const int len = S.nb_len[i];
+  const long base = S.nb_off[i >> 5];
+  const int *cp = S.nb_cols + base + (i & 31);
+  const float2 *vp = S.nb_vals + base * KK + (i & 31);
+  float h0[KB], l0[KB], h1[KB], l1[KB];
+#pragma unroll
+  for (int a = 0; a < KB; a++) h0[a] = l0[a] = h1[a] = l1[a] = 0.f;
+  int k = 0;
+  for (; k + 2 <= len; k += 2) {
+    const int j0 = __ldcs(cp + 32 * k), j1 = __ldcs(cp + 32 * (k + 1));
+    float2 x0[KS], x1[KS];
+    load_p2_node<KB>(S.p2, j0, x0);
+    load_p2_node<KB>(S.p2, j1, x1);
+    const float2 *v0 = vp + 32L * KK * k;
+    const float2 *v1 = v0 + 32 * KK;
+#pragma unroll
+    for (int a = 0; a < KB; a++)
+#pragma unroll
+      for (int b = 0; b < KB; b++) ff_madd(__ldcs(v0 + 32 * (a * KB + b)), x0[b], h0[a], l0[a]);
+#pragma unroll
+    for (int a = 0; a < KB; a++)
+#pragma unroll
+      for (int b = 0; b < KB; b++) ff_madd(__ldcs(v1 + 32 * (a * KB + b)), x1[b], h1[a], l1[a]);
+  }
+  if (k < len) {
+    const int j0 = __ldcs(cp + 32 * k);
+    float2 x0[KS];
+    load_p2_node<KB>(S.p2, j0, x0);
+    const float2 *v0 = vp + 32L * KK * k;
+#pragma unroll
+    for (int a = 0; a < KB; a++)
+#pragma unroll
+      for (int b = 0; b < KB; b++) ff_madd(__ldcs(v0 + 32 * (a * KB + b)), x0[b], h0[a], l0[a]);
+  }
+#pragma unroll
+  for (int a = 0; a < KB; a++)
+    y[a] = ((double)h0[a] + (double)l0[a]) + ((double)h1[a] + (double)l1[a]);
+}
+
+// f(row, (A x)[row]) for this thread's rows.  KB > 0: thread per node row
+// over the node-block copy (node rows with more than S.nb_cap blocks are
+// left to long_row_chunks), in float-float when ff is set and the node's
+// values lie in the split's range, else each of its rows in FP64 from the
+// CSR arrays against x (the initial residual, or a p outside the split's
+// range).  KB == 0: warp per CSR row (lane 0 calls f).
+template <int KB, typename F>
+__device__ __forceinline__ void for_rows_Ax(const PcgSystem &S, const double *x, bool ff, F f) {
   const int gtid = blockIdx.x * blockDim.x + threadIdx.x;
   const int gthreads = gridDim.x * blockDim.x;
-  if (kSell) {
-    for (int row = gtid; row < S.n; row += gthreads)
-      if (S.rowptr[row + 1] - S.rowptr[row] <= S.sell_cap)
-        f(row, spmv_sell(S, row, x, x2, x2 == nullptr));
+  if constexpr (KB > 0) {
+    for (int i = gtid; i < S.nblk; i += gthreads) {
+      if (S.nb_len[i] > S.nb_cap) continue;
+      const int b = S.blk_start[i], m = S.blk_start[i + 1] - b;
+      if (ff && S.blk_ff[i]) {
+        double y[KB];
+        node_row_ff<KB>(S, i, y);
+#pragma unroll
+        for (int a = 0; a < KB; a++)
+          if (a < m) f(b + a, y[a]);
+      } else {
+        for (int a = 0; a < m; a++) f(b + a, csr_row64(S, b + a, x));
+      }
+    }
   } else {
     const int lane = threadIdx.x & 31;
     for (int row = gtid >> 5; row < S.n; row += gthreads >> 5) {
@@ -158,10 +219,11 @@ __device__ __forceinline__ void for_rows_Ax(const PcgSystem &S, const double *x,
   }
 }
 
-// Rows longer than S.sell_cap (a node tied to a whole face by a
-// multi-point constraint couples to every node of that face) in chunks of
-// at most kLongChunk CSR entries, a warp per chunk: g(chunk, row, partial)
-// on lane 0.  A warp per row would leave one warp thousands of entries.
+// The rows of node rows with more than S.nb_cap blocks (a node tied to a
+// whole face by a multi-point constraint couples to every node of that
+// face) in chunks of at most kLongChunk CSR entries, a warp per chunk:
+// g(chunk, row, partial) on lane 0.  A warp per row would leave one warp
+// thousands of entries.
 constexpr int kLongChunk = 512;
 template <typename G>
 __device__ __forceinline__ void long_row_chunks(const PcgSystem &S, const double *x, G g) {
@@ -202,20 +264,28 @@ __device__ __forceinline__ BlockRange block_range(const PcgSystem &S, int k) {
   return r;
 }
 
-// z = Binv r on block k
+// z = Binv r on block k (MB: the largest block order, so that the block's
+// entries of r stay in registers)
+template <int MB>
 __device__ __forceinline__ void precondition_block(const PcgSystem &S, int k, BlockRange br) {
-  const double *B = S.binv + (long)k * 36;
-  double rr[6];
-  for (int i = 0; i < br.m; i++) rr[i] = S.r[br.b + i];
-  for (int i = 0; i < br.m; i++) {
+  const int bo = binv_order(S);
+  const double *B = S.binv + (long)k * bo * bo;
+  double rr[MB];
+#pragma unroll
+  for (int i = 0; i < MB; i++) rr[i] = i < br.m ? S.r[br.b + i] : 0.0;
+#pragma unroll
+  for (int i = 0; i < MB; i++) {
+    if (i >= br.m) break;
     double t = 0.0;
-    for (int j = 0; j < br.m; j++) t += B[6 * i + j] * rr[j];
+#pragma unroll
+    for (int j = 0; j < MB; j++)
+      if (j < br.m) t += B[bo * i + j] * rr[j];
     S.z[br.b + i] = t;
   }
 }
 
 // scalars: [0] rz  [1] bb  [2] rr  [3] iterations  [4] relres
-template <bool kSell>
+template <int KB>
 __global__ void __launch_bounds__(kPcgThreads) k_pcg(PcgSystem S, const double *b, double *x,
                                                      double rtol, int maxit) {
   __shared__ double smem[40];
@@ -226,10 +296,10 @@ __global__ void __launch_bounds__(kPcgThreads) k_pcg(PcgSystem S, const double *
   double *part = S.partials;          // [3*nb]
 
   // r = b - A x ; (x is the initial guess)
-  for_rows_Ax<kSell>(S, x, nullptr, [&](int row, double ax) { S.r[row] = b[row] - ax; });
-  if (kSell) long_row_chunks(S, x, [&](int c, int, double t) { S.chunk_part[c] = t; });
+  for_rows_Ax<KB>(S, x, false, [&](int row, double ax) { S.r[row] = b[row] - ax; });
+  if ((KB > 0)) long_row_chunks(S, x, [&](int c, int, double t) { S.chunk_part[c] = t; });
   if (!grid_barrier(S.barrier, flags)) return;
-  if (kSell && S.nlong > 0) {
+  if ((KB > 0) && S.nlong > 0) {
     long_row_sums(S, [&](int row, double ax) { S.r[row] = b[row] - ax; });
     if (!grid_barrier(S.barrier, flags)) return;
   }
@@ -237,11 +307,11 @@ __global__ void __launch_bounds__(kPcgThreads) k_pcg(PcgSystem S, const double *
   bool p_out = false;                 // an entry of p outside the split's range
   for (int k = gtid; k < S.nblk; k += gthreads) {
     const BlockRange br = block_range(S, k);
-    precondition_block(S, k, br);
+    precondition_block<(KB > 0 ? KB : 6)>(S, k, br);
     for (int i = br.b; i < br.b + br.m; i++) {
       S.p[i] = S.z[i];
-      if (kSell) {
-        S.p2[i] = split2(S.z[i]);
+      if (KB > 0) {
+        S.p2[(long)k * NodeSlots<KB>::kStride + (i - br.b)] = split2(S.z[i]);
         p_out |= !ff_range(S.z[i]);
       }
       lrz += S.r[i] * S.z[i];
@@ -250,7 +320,7 @@ __global__ void __launch_bounds__(kPcgThreads) k_pcg(PcgSystem S, const double *
     }
   }
   // p = z is read across blocks in the next SpMV: barrier before it
-  if (kSell && p_out) flags[2] = 1;   // FP64 SpMV from now on (read after a barrier)
+  if ((KB > 0) && p_out) flags[2] = 1;   // FP64 SpMV from now on (read after a barrier)
   lrz = block_reduce(lrz, smem);
   if (threadIdx.x == 0) part[blockIdx.x] = lrz;
   lbb = block_reduce(lbb, smem);
@@ -271,11 +341,11 @@ __global__ void __launch_bounds__(kPcgThreads) k_pcg(PcgSystem S, const double *
     // q = A p ; pq = p.q
     if (!grid_barrier(S.barrier, flags)) return;   // partial sums consumed
     double lpq = 0.0;
-    for_rows_Ax<kSell>(S, S.p, flags[2] ? nullptr : S.p2, [&](int row, double ap) {
+    for_rows_Ax<KB>(S, S.p, flags[2] == 0, [&](int row, double ap) {
       S.q[row] = ap;
       lpq += ap * S.p[row];
     });
-    if (kSell)
+    if ((KB > 0))
       long_row_chunks(S, S.p, [&](int c, int row, double t) {
         S.chunk_part[c] = t;
         lpq += t * S.p[row];
@@ -286,7 +356,7 @@ __global__ void __launch_bounds__(kPcgThreads) k_pcg(PcgSystem S, const double *
     const double pq = sum_partials(part, nb, smem);
     if (!(pq > 0.0)) { status = -1; break; }
     const double alpha = rz / pq;
-    if (kSell) long_row_sums(S, [&](int row, double ap) { S.q[row] = ap; });
+    if ((KB > 0)) long_row_sums(S, [&](int row, double ap) { S.q[row] = ap; });
     if (!grid_barrier(S.barrier, flags)) return;   // partial sums consumed, q complete
     lrz = 0.0; lrr = 0.0;
     for (int k = gtid; k < S.nblk; k += gthreads) {
@@ -295,7 +365,7 @@ __global__ void __launch_bounds__(kPcgThreads) k_pcg(PcgSystem S, const double *
         x[i] += alpha * S.p[i];
         S.r[i] -= alpha * S.q[i];
       }
-      precondition_block(S, k, br);
+      precondition_block<(KB > 0 ? KB : 6)>(S, k, br);
       for (int i = br.b; i < br.b + br.m; i++) {
         lrz += S.r[i] * S.z[i];
         lrr += S.r[i] * S.r[i];
@@ -318,13 +388,13 @@ __global__ void __launch_bounds__(kPcgThreads) k_pcg(PcgSystem S, const double *
       for (int i = br.b; i < br.b + br.m; i++) {
         const double pi = S.z[i] + beta * S.p[i];
         S.p[i] = pi;
-        if (kSell) {
-          S.p2[i] = split2(pi);
+        if (KB > 0) {
+          S.p2[(long)k * NodeSlots<KB>::kStride + (i - br.b)] = split2(pi);
           p_out |= !ff_range(pi);
         }
       }
     }
-    if (kSell && p_out) flags[2] = 1;
+    if ((KB > 0) && p_out) flags[2] = 1;
   }
   if (blockIdx.x == 0 && threadIdx.x == 0) {
     S.scalars[3] = it;
@@ -366,8 +436,9 @@ __global__ void k_factor_blocks(PcgSystem S) {
         for (int j = 0; j < 2 * m; j++) A[i][j] -= f * A[c][j];
     }
   }
-  double *B = S.binv + (long)k * 36;
-  for (int i = 0; i < 36; i++) B[i] = 0.0;
+  const int bo = binv_order(S);
+  double *B = S.binv + (long)k * bo * bo;
+  for (int i = 0; i < bo * bo; i++) B[i] = 0.0;
   if (singular) {
     // fall back to the point-Jacobi inverse of whatever diagonal exists
     for (int i = 0; i < m; i++) {
@@ -375,32 +446,45 @@ __global__ void k_factor_blocks(PcgSystem S) {
       const int row = b + i;
       for (int q = S.rowptr[row]; q < S.rowptr[row + 1]; q++)
         if (S.colidx[q] == row) d = S.vals[q];
-      B[6 * i + i] = d != 0.0 ? 1.0 / d : 1.0;
+      B[bo * i + i] = d != 0.0 ? 1.0 / d : 1.0;
     }
     return;
   }
   for (int i = 0; i < m; i++)
-    for (int j = 0; j < m; j++) B[6 * i + j] = A[i][m + j];
+    for (int j = 0; j < m; j++) B[bo * i + j] = A[i][m + j];
 }
 
-// CSR values into the sliced ELL copy, split into (hi, lo), thread per row;
-// row_ff records whether every value of the row lies in the split's range.
-__global__ void k_pack_sell(PcgSystem S) {
-  const int row = blockIdx.x * blockDim.x + threadIdx.x;
-  if (row >= S.n) return;
-  const int b = S.rowptr[row], len = S.rowptr[row + 1] - b;
-  if (len > S.sell_cap) return;
-  float2 *vp = S.sell_vals + S.sell_off[row >> 5] + (row & 31);
+// CSR values into the node-block copy, split into (hi, lo), thread per node
+// row (once per matrix); blk_ff records whether every value of the node's
+// rows lies in the split's range.  Slots no CSR entry maps to stay zero.
+__global__ void k_pack_blocks(PcgSystem S) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= S.nblk) return;
   bool ok = true;
-  for (int k = 0; k < len; k++) {
-    const double v = S.vals[b + k];
-    ok = ok && ff_range(v);
-    vp[32 * k] = split2(v);
+  if (S.nb_len[i] <= S.nb_cap) {
+    for (int r = S.blk_start[i]; r < S.blk_start[i + 1]; r++)
+      for (int q = S.rowptr[r]; q < S.rowptr[r + 1]; q++) {
+        const double v = S.vals[q];
+        ok = ok && ff_range(v);
+        S.nb_vals[S.nb_pos[q]] = split2(v);
+      }
   }
-  S.row_ff[row] = ok ? 1 : 0;
+  S.blk_ff[i] = ok ? 1 : 0;
 }
 
-int g_max_blocks = -1, g_sell_max_blocks = -1;
+int g_max_blocks[5] = {-1, -1, -1, -1, -1};
+
+int kb_index(int kb) { return kb == 1 ? 1 : kb == 2 ? 2 : kb == 3 ? 3 : kb == 6 ? 4 : 0; }
+
+const void *pcg_kernel(int kb) {
+  switch (kb) {
+    case 1: return (const void *)k_pcg<1>;
+    case 2: return (const void *)k_pcg<2>;
+    case 3: return (const void *)k_pcg<3>;
+    case 6: return (const void *)k_pcg<6>;
+    default: return (const void *)k_pcg<0>;
+  }
+}
 
 int max_coresident(const void *kernel) {
   int dev = 0, sms = 0, per = 0;
@@ -411,60 +495,119 @@ int max_coresident(const void *kernel) {
   return sms * per;
 }
 
+int coresident(int kb) {
+  int &c = g_max_blocks[kb_index(kb)];
+  if (c < 0) c = max_coresident(pcg_kernel(kb));
+  return c;
+}
+
 }  // namespace
 
 int pcg_max_blocks() {
-  if (g_max_blocks < 0) g_max_blocks = max_coresident((const void *)k_pcg<false>);
-  return g_max_blocks;
+  int m = 1;
+  for (int kb : {0, 1, 2, 3, 6}) m = std::max(m, coresident(kb));
+  return m;
 }
 
-int pcg_sell_max_blocks() {
-  if (g_sell_max_blocks < 0) g_sell_max_blocks = max_coresident((const void *)k_pcg<true>);
-  return g_sell_max_blocks;
-}
-
-void sell_layout(int n, const int *rowptr, int cap, std::vector<long> &off,
-                 std::vector<int> &chunk_row, std::vector<int> &chunk_beg,
-                 std::vector<int> &long_chunk0) {
-  const int ns = (n + 31) / 32;
-  off.assign((size_t)ns + 1, 0);
-  chunk_row.clear();
-  chunk_beg.clear();
-  long_chunk0.assign(1, 0);
+int block_ell_layout(int n, const int *rowptr, const int *colidx, int nblk, const int *blk_start,
+                     int cap, BlockEll &h) {
+  h = BlockEll{};
+  int maxm = 0;
+  for (int i = 0; i < nblk; i++) maxm = std::max(maxm, blk_start[i + 1] - blk_start[i]);
+  if (nblk == 0 || maxm < 1 || maxm > 6) return 0;
+  const int kb = maxm == 1 ? 1 : maxm == 2 ? 2 : maxm == 3 ? 3 : 6;
+  std::vector<int> node_of(n);
+  for (int i = 0; i < nblk; i++)
+    for (int r = blk_start[i]; r < blk_start[i + 1]; r++) node_of[r] = i;
+  // block columns of every node row: the union over its rows (sorted)
+  std::vector<long> lptr(nblk + 1, 0);
+  std::vector<int> lst, row_l, merged;
+  std::vector<int> all;
+  all.reserve((size_t)rowptr[n] / (kb * kb) + nblk);
+  for (int i = 0; i < nblk; i++) {
+    lst.clear();
+    for (int r = blk_start[i]; r < blk_start[i + 1]; r++) {
+      row_l.clear();
+      for (int q = rowptr[r]; q < rowptr[r + 1]; q++) {
+        const int j = node_of[colidx[q]];
+        if (row_l.empty() || row_l.back() != j) row_l.push_back(j);
+      }
+      if (r == blk_start[i]) {
+        lst.swap(row_l);
+      } else if (row_l != lst) {
+        merged.clear();
+        std::set_union(lst.begin(), lst.end(), row_l.begin(), row_l.end(),
+                       std::back_inserter(merged));
+        lst.swap(merged);
+      }
+    }
+    all.insert(all.end(), lst.begin(), lst.end());
+    lptr[i + 1] = (long)all.size();
+  }
+  const int ns = (nblk + 31) / 32;
+  h.off.assign((size_t)ns + 1, 0);
+  h.len.assign(nblk, 0);
+  h.chunk_row.clear();
+  h.chunk_beg.clear();
+  h.long_chunk0.assign(1, 0);
   for (int s = 0; s < ns; s++) {
     int w = 0;
-    for (int r = 32 * s; r < std::min(n, 32 * s + 32); r++) {
-      const int len = rowptr[r + 1] - rowptr[r];
+    for (int i = 32 * s; i < std::min(nblk, 32 * s + 32); i++) {
+      const int len = (int)(lptr[i + 1] - lptr[i]);
+      h.len[i] = len;
       if (len <= cap) {
         w = std::max(w, len);
         continue;
       }
-      for (int k = rowptr[r]; k < rowptr[r + 1]; k += kLongChunk) {
-        chunk_row.push_back(r);
-        chunk_beg.push_back(k);
+      for (int r = blk_start[i]; r < blk_start[i + 1]; r++) {
+        for (int q = rowptr[r]; q < rowptr[r + 1]; q += kLongChunk) {
+          h.chunk_row.push_back(r);
+          h.chunk_beg.push_back(q);
+        }
+        h.long_chunk0.push_back((int)h.chunk_row.size());
       }
-      long_chunk0.push_back((int)chunk_row.size());
     }
-    off[s + 1] = off[s] + 32L * w;
+    h.off[s + 1] = h.off[s] + 32L * w;
   }
+  if (h.off.back() * kb * kb >= (long)INT32_MAX) return 0;   // positions as 32-bit ints
+  h.cols.assign((size_t)h.off.back(), 0);
+  h.pos.assign((size_t)rowptr[n], -1);
+  for (int i = 0; i < nblk; i++) {
+    const int len = h.len[i];
+    if (len > cap) continue;
+    const long base = h.off[i / 32];
+    const int lane = i % 32;
+    const int *L = all.data() + lptr[i];
+    for (int k = 0; k < len; k++) h.cols[(size_t)base + 32L * k + lane] = L[k];
+    for (int r = blk_start[i]; r < blk_start[i + 1]; r++) {
+      const int a = r - blk_start[i];
+      int k = 0;
+      for (int q = rowptr[r]; q < rowptr[r + 1]; q++) {
+        const int j = node_of[colidx[q]];
+        while (L[k] != j) k++;
+        const int b = colidx[q] - blk_start[j];
+        h.pos[q] = (int)(base * kb * kb + ((long)(k * kb + a) * kb + b) * 32 + lane);
+      }
+    }
+  }
+  h.kb = kb;
+  return kb;
 }
 
-void sell_columns(int n, const int *rowptr, const int *colidx, int cap,
-                  const std::vector<long> &off, std::vector<int> &cols) {
-  cols.assign((size_t)off.back(), 0);
-  for (int r = 0; r < n; r++) {
-    if (rowptr[r + 1] - rowptr[r] > cap) continue;
-    for (int k = rowptr[r]; k < rowptr[r + 1]; k++)
-      cols[(size_t)off[r / 32] + 32L * (k - rowptr[r]) + r % 32] = colidx[k];
-  }
+size_t block_ell_bytes(const BlockEll &h, int nblk) {
+  if (h.kb == 0) return 0;
+  const int ks = h.kb == 3 ? 4 : h.kb;
+  return (size_t)h.off.back() * (sizeof(int) + sizeof(float2) * h.kb * h.kb) +
+         h.pos.size() * sizeof(int) + h.off.size() * sizeof(long) +
+         (size_t)nblk * (sizeof(int) + 1 + ks * sizeof(float2));
 }
 
 int pcg_factor_blocks(const PcgSystem &S, cudaStream_t s) {
   if (S.nblk == 0) return 0;
   k_factor_blocks<<<(S.nblk + 127) / 128, 128, 0, s>>>(S);
   if (cudaGetLastError() != cudaSuccess) return XG_ECUDA;
-  if (S.sell_vals && S.n > 0) {
-    k_pack_sell<<<(S.n + 255) / 256, 256, 0, s>>>(S);
+  if (S.nb_vals && S.kb > 0) {
+    k_pack_blocks<<<(S.nblk + 255) / 256, 256, 0, s>>>(S);
     if (cudaGetLastError() != cudaSuccess) return XG_ECUDA;
   }
   return 0;
@@ -483,15 +626,16 @@ int pcg_solve(const PcgSystem &S, const double *b, double *x, double rtol, int m
   const long rpb = rows_per_block > 0 ? rows_per_block : 64;
   long want = ((long)S.n + rpb - 1) / rpb;
   int nb = (int)(want < 1 ? 1 : want);
-  const bool sell = S.sell_vals != nullptr;
-  const int maxb = sell ? pcg_sell_max_blocks() : pcg_max_blocks();
+  const int kb = (S.nb_vals && S.kb > 0) ? S.kb : 0;
+  const int maxb = coresident(kb);
   if (nb > maxb) nb = maxb;
   if (cudaMemsetAsync(S.barrier, 0, 2 * sizeof(unsigned int), s) != cudaSuccess) return XG_ECUDA;
   if (cudaMemsetAsync(S.flags, 0, 4 * sizeof(int), s) != cudaSuccess) return XG_ECUDA;
   PcgSystem Sv = S;
+  if (kb == 0) Sv.nb_vals = nullptr;
   void *args[] = {(void *)&Sv, (void *)&b, (void *)&x, (void *)&rtol, (void *)&maxit};
-  const void *kernel = sell ? (const void *)k_pcg<true> : (const void *)k_pcg<false>;
-  cudaError_t err = cudaLaunchCooperativeKernel(kernel, dim3(nb), dim3(kPcgThreads), args, 0, s);
+  cudaError_t err =
+      cudaLaunchCooperativeKernel(pcg_kernel(kb), dim3(nb), dim3(kPcgThreads), args, 0, s);
   if (err != cudaSuccess) return XG_ECUDA;
   int hflags[4];
   double hs[8];
