@@ -80,7 +80,7 @@ struct PcgSystem {
                           // (padded to 6 x 6) when kb is 0
   // work vectors [n]
   double *r, *z, *p, *q;
-  double *partials;       // [3*pcg_max_blocks() + 8]
+  double *partials;       // [4*pcg_max_blocks() + 8] (3*... + 8 without the node-block copy)
   unsigned int *barrier;  // [2] grid barrier state
   int *flags;             // [4] status words
   double *scalars;        // [8]

@@ -114,7 +114,7 @@ struct xg_linsoe {
     e |= vals.alloc(std::max<size_t>(nnz, 1)) | b.alloc(nv) | x.alloc(nv);
     e |= binv.alloc((size_t)std::max(nblk, 1) * 36);
     e |= r.alloc(nv) | z.alloc(nv) | p.alloc(nv) | q.alloc(nv);
-    e |= partials.alloc(3 * (size_t)xg::pcg_max_blocks() + 8);
+    e |= partials.alloc(4 * (size_t)xg::pcg_max_blocks() + 8);
     e |= scalars.alloc(8) | barrier.alloc(2) | flags.alloc(4);
     size_t nvals = 0, np2 = 0;
     if (h.kb) {

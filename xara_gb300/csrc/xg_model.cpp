@@ -735,7 +735,7 @@ int xg_model::upload(const HostGather &gk_h, const HostGather &gr_h) {
   RET(d_binv.alloc((size_t)std::max(nblk, 1) * 36));
   const size_t nv = neq > 0 ? neq : 1;
   RET(d_r.alloc(nv)); RET(d_z.alloc(nv)); RET(d_p.alloc(nv)); RET(d_q.alloc(nv));
-  RET(d_pcg_part.alloc(3 * (size_t)pcg_max_blocks() + 8));
+  RET(d_pcg_part.alloc(4 * (size_t)pcg_max_blocks() + 8));
   RET(d_scalars.alloc(8));
   RET(d_barrier.alloc(2));
   RET(d_flags.alloc(4));

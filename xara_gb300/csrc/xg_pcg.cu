@@ -76,6 +76,47 @@ __device__ double block_reduce(double v, double *smem) {
   return t;  // valid in thread 0
 }
 
+__device__ double block_reduce_max(double v, double *smem) {
+  for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_down_sync(0xffffffffu, v, o));
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  if (lane == 0) smem[w] = v;
+  __syncthreads();
+  double t = 0.0;
+  if (w == 0) {
+    t = (lane < (int)(blockDim.x >> 5)) ? smem[lane] : 0.0;
+    for (int o = 16; o > 0; o >>= 1) t = fmax(t, __shfl_down_sync(0xffffffffu, t, o));
+  }
+  __syncthreads();
+  return t;  // valid in thread 0
+}
+
+// Largest of partials[0..nb) (all >= 0), broadcast to the whole block.
+__device__ double max_partials(const double *partials, int nb, double *smem) {
+  double s = 0.0;
+  for (int i = threadIdx.x; i < nb; i += blockDim.x) s = fmax(s, partials[i]);
+  s = block_reduce_max(s, smem);
+  if (threadIdx.x == 0) smem[32] = s;
+  __syncthreads();
+  const double r = smem[32];
+  __syncthreads();
+  return r;
+}
+
+// Power-of-two scale of p's split: p2 = p * 2^-s with s the exponent of a
+// bound on max |p|, so that every entry of the split lies below 2 whatever
+// the size of the residual (p shrinks with it over a solve; a fixed range
+// would send the late iterations to FP64).  Entries more than 2^126 below
+// the bound fall into the single-precision subnormals or to zero: a change
+// of at most 2^-126 of max |p| per entry, below the split's own rounding.
+__device__ __forceinline__ int split_exponent(double bound) {
+  if (!(bound > 0.0) || !isfinite(bound)) return 0;
+  const int e = (int)(((unsigned)__double2hiint(bound) >> 20) & 0x7ff) - 1023;
+  return e < -1000 ? -1000 : (e > 1000 ? 1000 : e);
+}
+__device__ __forceinline__ double pow2(int e) {
+  return __hiloint2double((int)((unsigned)(1023 + e) << 20), 0);
+}
+
 // Sum of partials[0..nb) in a fixed order, broadcast to the whole block.
 __device__ double sum_partials(const double *partials, int nb, double *smem) {
   double s = 0.0;
@@ -188,12 +229,13 @@ __device__ __forceinline__ void node_row_ff(const PcgSystem &S, int i, double *y
 
 // f(row, (A x)[row]) for this thread's rows.  KB > 0: thread per node row
 // over the node-block copy (node rows with more than S.nb_cap blocks are
-// left to long_row_chunks), in float-float when ff is set and the node's
-// values lie in the split's range, else each of its rows in FP64 from the
-// CSR arrays against x (the initial residual, or a p outside the split's
-// range).  KB == 0: warp per CSR row (lane 0 calls f).
+// left to long_row_chunks), in float-float against p2 = x * 2^-s when ff is
+// set and the node's values lie in the split's range (the sums times
+// scale = 2^s), else each of its rows in FP64 from the CSR arrays against x
+// (the initial residual).  KB == 0: warp per CSR row (lane 0 calls f).
 template <int KB, typename F>
-__device__ __forceinline__ void for_rows_Ax(const PcgSystem &S, const double *x, bool ff, F f) {
+__device__ __forceinline__ void for_rows_Ax(const PcgSystem &S, const double *x, bool ff,
+                                            double scale, F f) {
   const int gtid = blockIdx.x * blockDim.x + threadIdx.x;
   const int gthreads = gridDim.x * blockDim.x;
   if constexpr (KB > 0) {
@@ -205,7 +247,7 @@ __device__ __forceinline__ void for_rows_Ax(const PcgSystem &S, const double *x,
         node_row_ff<KB>(S, i, y);
 #pragma unroll
         for (int a = 0; a < KB; a++)
-          if (a < m) f(b + a, y[a]);
+          if (a < m) f(b + a, y[a] * scale);
       } else {
         for (int a = 0; a < m; a++) f(b + a, csr_row64(S, b + a, x));
       }
@@ -285,6 +327,8 @@ __device__ __forceinline__ void precondition_block(const PcgSystem &S, int k, Bl
 }
 
 // scalars: [0] rz  [1] bb  [2] rr  [3] iterations  [4] relres
+// partials: [0, 3 nb) the inner products' block sums; with KB > 0 also
+// [3 nb, 4 nb) the blocks' largest |z| or |p| for the split's scale.
 template <int KB>
 __global__ void __launch_bounds__(kPcgThreads) k_pcg(PcgSystem S, const double *b, double *x,
                                                      double rtol, int maxit) {
@@ -293,44 +337,57 @@ __global__ void __launch_bounds__(kPcgThreads) k_pcg(PcgSystem S, const double *
   const int gtid = blockIdx.x * blockDim.x + threadIdx.x;
   const int gthreads = gridDim.x * blockDim.x;
   const int nb = gridDim.x;
-  double *part = S.partials;          // [3*nb]
+  double *part = S.partials;
+  constexpr int KS = NodeSlots<(KB > 0 ? KB : 1)>::kStride;
 
   // r = b - A x ; (x is the initial guess)
-  for_rows_Ax<KB>(S, x, false, [&](int row, double ax) { S.r[row] = b[row] - ax; });
-  if ((KB > 0)) long_row_chunks(S, x, [&](int c, int, double t) { S.chunk_part[c] = t; });
+  for_rows_Ax<KB>(S, x, false, 1.0, [&](int row, double ax) { S.r[row] = b[row] - ax; });
+  if (KB > 0) long_row_chunks(S, x, [&](int c, int, double t) { S.chunk_part[c] = t; });
   if (!grid_barrier(S.barrier, flags)) return;
-  if ((KB > 0) && S.nlong > 0) {
+  if (KB > 0 && S.nlong > 0) {
     long_row_sums(S, [&](int row, double ax) { S.r[row] = b[row] - ax; });
     if (!grid_barrier(S.barrier, flags)) return;
   }
-  double lrz = 0.0, lbb = 0.0, lrr = 0.0;
-  bool p_out = false;                 // an entry of p outside the split's range
+  double lrz = 0.0, lbb = 0.0, lrr = 0.0, lmax = 0.0;
   for (int k = gtid; k < S.nblk; k += gthreads) {
     const BlockRange br = block_range(S, k);
     precondition_block<(KB > 0 ? KB : 6)>(S, k, br);
     for (int i = br.b; i < br.b + br.m; i++) {
       S.p[i] = S.z[i];
-      if (KB > 0) {
-        S.p2[(long)k * NodeSlots<KB>::kStride + (i - br.b)] = split2(S.z[i]);
-        p_out |= !ff_range(S.z[i]);
-      }
+      lmax = fmax(lmax, fabs(S.z[i]));
       lrz += S.r[i] * S.z[i];
       lbb += b[i] * b[i];
       lrr += S.r[i] * S.r[i];
     }
   }
-  // p = z is read across blocks in the next SpMV: barrier before it
-  if ((KB > 0) && p_out) flags[2] = 1;   // FP64 SpMV from now on (read after a barrier)
   lrz = block_reduce(lrz, smem);
   if (threadIdx.x == 0) part[blockIdx.x] = lrz;
   lbb = block_reduce(lbb, smem);
   if (threadIdx.x == 0) part[nb + blockIdx.x] = lbb;
   lrr = block_reduce(lrr, smem);
   if (threadIdx.x == 0) part[2 * nb + blockIdx.x] = lrr;
+  if (KB > 0) {
+    lmax = block_reduce_max(lmax, smem);
+    if (threadIdx.x == 0) part[3 * nb + blockIdx.x] = lmax;
+  }
   if (!grid_barrier(S.barrier, flags)) return;
   double rz = sum_partials(part, nb, smem);
   const double bb = sum_partials(part + nb, nb, smem);
   double rr = sum_partials(part + 2 * nb, nb, smem);
+  int sp = 0;                         // p2 = p * 2^-sp
+  if (KB > 0) {
+    const double bound = max_partials(part + 3 * nb, nb, smem);
+    if (!isfinite(bound)) flags[2] = 1;   // FP64 SpMV throughout
+    sp = split_exponent(bound);
+    const double down = pow2(-sp);
+    for (int k = gtid; k < S.nblk; k += gthreads) {
+      const BlockRange br = block_range(S, k);
+      for (int i = br.b; i < br.b + br.m; i++)
+        S.p2[(long)k * KS + (i - br.b)] = split2(S.p[i] * down);
+    }
+  }
+  // p and its split are read across blocks in the next SpMV: the barrier at
+  // the top of the loop comes first
   const double bnorm = sqrt(bb);
   int it = 0;
   int status = 0;
@@ -339,26 +396,35 @@ __global__ void __launch_bounds__(kPcgThreads) k_pcg(PcgSystem S, const double *
   }
   while (status == 0 && it < maxit) {
     // q = A p ; pq = p.q
-    if (!grid_barrier(S.barrier, flags)) return;   // partial sums consumed
-    double lpq = 0.0;
-    for_rows_Ax<KB>(S, S.p, flags[2] == 0, [&](int row, double ap) {
+    if (!grid_barrier(S.barrier, flags)) return;   // partial sums consumed, p complete
+    double lpq = 0.0, lpmax = 0.0;
+    for_rows_Ax<KB>(S, S.p, flags[2] == 0, pow2(sp), [&](int row, double ap) {
       S.q[row] = ap;
-      lpq += ap * S.p[row];
+      const double pr = S.p[row];
+      lpq += ap * pr;
+      lpmax = fmax(lpmax, fabs(pr));
     });
-    if ((KB > 0))
+    if (KB > 0)
       long_row_chunks(S, S.p, [&](int c, int row, double t) {
         S.chunk_part[c] = t;
         lpq += t * S.p[row];
+        lpmax = fmax(lpmax, fabs(S.p[row]));
       });
     lpq = block_reduce(lpq, smem);
     if (threadIdx.x == 0) part[blockIdx.x] = lpq;
+    if (KB > 0) {
+      lpmax = block_reduce_max(lpmax, smem);
+      if (threadIdx.x == 0) part[3 * nb + blockIdx.x] = lpmax;
+    }
     if (!grid_barrier(S.barrier, flags)) return;
     const double pq = sum_partials(part, nb, smem);
+    const double pmax = KB > 0 ? max_partials(part + 3 * nb, nb, smem) : 0.0;
     if (!(pq > 0.0)) { status = -1; break; }
     const double alpha = rz / pq;
-    if ((KB > 0)) long_row_sums(S, [&](int row, double ap) { S.q[row] = ap; });
+    if (KB > 0) long_row_sums(S, [&](int row, double ap) { S.q[row] = ap; });
     if (!grid_barrier(S.barrier, flags)) return;   // partial sums consumed, q complete
     lrz = 0.0; lrr = 0.0;
+    double lzmax = 0.0;
     for (int k = gtid; k < S.nblk; k += gthreads) {
       const BlockRange br = block_range(S, k);
       for (int i = br.b; i < br.b + br.m; i++) {
@@ -369,32 +435,41 @@ __global__ void __launch_bounds__(kPcgThreads) k_pcg(PcgSystem S, const double *
       for (int i = br.b; i < br.b + br.m; i++) {
         lrz += S.r[i] * S.z[i];
         lrr += S.r[i] * S.r[i];
+        lzmax = fmax(lzmax, fabs(S.z[i]));
       }
     }
     lrz = block_reduce(lrz, smem);
     if (threadIdx.x == 0) part[blockIdx.x] = lrz;
     lrr = block_reduce(lrr, smem);
     if (threadIdx.x == 0) part[nb + blockIdx.x] = lrr;
+    if (KB > 0) {
+      lzmax = block_reduce_max(lzmax, smem);
+      if (threadIdx.x == 0) part[3 * nb + blockIdx.x] = lzmax;
+    }
     if (!grid_barrier(S.barrier, flags)) return;
     const double rz_new = sum_partials(part, nb, smem);
     rr = sum_partials(part + nb, nb, smem);
+    const double zmax = KB > 0 ? max_partials(part + 3 * nb, nb, smem) : 0.0;
     it++;
     if (sqrt(rr) <= rtol * bnorm) { status = 1; break; }
     const double beta = rz_new / rz;
     rz = rz_new;
-    p_out = false;
+    double down = 1.0;
+    if (KB > 0) {
+      // |z + beta p| <= max|z| + beta max|p| (beta > 0)
+      const double bound = zmax + fabs(beta) * pmax;
+      if (!isfinite(bound) && threadIdx.x == 0) flags[2] = 1;
+      sp = split_exponent(bound);
+      down = pow2(-sp);
+    }
     for (int k = gtid; k < S.nblk; k += gthreads) {
       const BlockRange br = block_range(S, k);
       for (int i = br.b; i < br.b + br.m; i++) {
         const double pi = S.z[i] + beta * S.p[i];
         S.p[i] = pi;
-        if (KB > 0) {
-          S.p2[(long)k * NodeSlots<KB>::kStride + (i - br.b)] = split2(pi);
-          p_out |= !ff_range(pi);
-        }
+        if (KB > 0) S.p2[(long)k * KS + (i - br.b)] = split2(pi * down);
       }
     }
-    if ((KB > 0) && p_out) flags[2] = 1;
   }
   if (blockIdx.x == 0 && threadIdx.x == 0) {
     S.scalars[3] = it;
