@@ -37,8 +37,9 @@ struct ContinuumView {
   // Jacobian determinant at [24*npts + pt], formed once (the geometry does
   // not change); null: formed in every kernel that needs them
   const double *geo;
-  // bricks: the same dN/dx split into float pairs (hi, lo), for the
-  // float-float tangent; null: the tangent is formed in FP64
+  // bricks: the same dN/dx split into float pairs (hi, lo) at
+  // [(pt*3 + i)*8 + a], for the float-float tangent; null: the tangent is
+  // formed in FP64
   const float2 *geo2;
 };
 

@@ -375,8 +375,9 @@ __device__ __forceinline__ bool geo_splits(double v) {
 }
 
 // Stored geometry of every point; geo2 (when given) receives dN/dx split
-// into float pairs for the float-float tangent, *bad counts the points with
-// a value outside the split's range.
+// into float pairs for the float-float tangent, element-major
+// ([point][i][node], so the lanes of one point's nodes read it contiguously),
+// *bad counts the points with a value outside the split's range.
 __global__ void k_brick_geometry(ContinuumView v, double *geo, float2 *geo2, int *bad) {
   const long npts = (long)v.ne * 8;
   const long pt = (long)blockIdx.x * blockDim.x + threadIdx.x;
@@ -392,7 +393,7 @@ __global__ void k_brick_geometry(ContinuumView v, double *geo, float2 *geo2, int
     for (int a = 0; a < 8; a++) {
       geo[(8 * i + a) * npts + pt] = g[i][a];
       if (geo2) {
-        geo2[(8 * i + a) * npts + pt] = split2(g[i][a]);
+        geo2[(pt * 3 + i) * 8 + a] = split2(g[i][a]);
         ok = ok && geo_splits(g[i][a]);
       }
     }
@@ -559,33 +560,7 @@ __global__ void __launch_bounds__(32 * kBrickWarps) k_brick_assemble(ContinuumVi
   }
 }
 
-// The float-float form of k_brick_assemble: the same staging and lane
-// layout, the 36 node-pair blocks summed on the single-precision pipes.  An
-// FP64 FMA holds GB300's FP64 pipe for many cycles; a float-float product
-// (xg_ff.h) costs about twelve single-precision instructions and keeps 46
-// bits of each product, so the tangent carries the reference's values to a
-// few units of 2^-46 of the row's largest entry.  The resisting force stays
-// in FP64 (it sets the converged state).  Each element's staged values are
-// scaled by powers of two -- the dN/dx by 2^-eg, the tangent scalings
-// dvol*{a, b/2, c} by 2^-ed, the largest magnitudes of the element -- so
-// every product lies near 1 whatever the model's units; the scale comes back
-// exactly in the exponent when the pair is written as a double.
-struct BrickSmemFF {
-  float2 g[kBrickEPW][8][8][3];    // dN/dx * 2^-eg per point, node
-  float2 h[kBrickEPW][8][8][3];    // n . dN/dx * 2^-eg
-  float2 u[kBrickEPW][8][8][3];    // dvol*a * 2^-ed * dN/dx * 2^-eg
-  float2 vv[kBrickEPW][8][8][3];   // dvol*b/2 * 2^-ed * dN/dx * 2^-eg
-  float2 w[kBrickEPW][8][8][3];    // dvol*c * 2^-ed * n . dN/dx * 2^-eg
-  double gd[kBrickEPW][8][8][3];   // dN/dx (FP64, for the resisting force)
-  double ss[kBrickEPW][8][6];      // dvol*stress
-  int scale[kBrickEPW];            // 2 eg + ed
-};
-
-// Unbiased exponent of a nonzero float / double from its bits (-127 / -1023
-// for zero).
-__device__ __forceinline__ int f32_exponent(float f) {
-  return (int)((__float_as_uint(f) >> 23) & 0xff) - 127;
-}
+// Unbiased exponent of a nonzero double from its bits (-1023 for zero).
 __device__ __forceinline__ int f64_exponent(double d) {
   return (int)(((unsigned)__double2hiint(d) >> 20) & 0x7ff) - 1023;
 }
@@ -623,6 +598,34 @@ __device__ __forceinline__ double f32_to_f64_scaled(float f, int s) {
   return __hiloint2double((int)(sign | ((unsigned)de << 20) | (m >> 3)), (int)(m << 29));
 }
 
+// The float-float form of k_brick_assemble, four elements per warp.  An
+// FP64 FMA holds GB300's FP64 pipe for many cycles; a float-float product
+// (xg_ff.h) costs about twelve single-precision instructions and keeps 46
+// bits of each product, so the tangent carries the reference's values to a
+// few units of 2^-46 of the row's largest entry.  The resisting force stays
+// in FP64 (it sets the converged state).  Each element's staged values are
+// scaled by powers of two -- the dN/dx by 2^-eg, the tangent scalings
+// dvol*{a, b/2, c} by 2^-ed, the element's largest magnitudes -- so every
+// product lies near 1 whatever the model's units; the scale comes back
+// exactly in the exponent when a pair is written as a double.
+//
+// Two phases.  Per point (lane = element, point; coalesced loads of the
+// point-major geometry and state): the scale exponents, the split tangent
+// scalings and deviatoric direction, and the point's FP64 residual terms.
+// Then over the eight points (lane = element, node): the node's split
+// gradient at that point (element-major geo2, coalesced), its projection
+// h = n . dN/dx and its three scalings, staged in a double-buffered 3.8 KB
+// slice, after which every lane adds the point's terms to the node-pair
+// blocks it owns (144 per warp, 4.5 per lane) in registers.  The element
+// arrays never sit in shared memory whole (17 KB per warp instead of 38),
+// so three times as many warps fit on an SM.
+struct BrickSmemFF {
+  float2 pt[kBrickEPW][8][9];         // per point: dvol*{a, b/2, c}*2^-ed, n[6] (split)
+  double rt[kBrickEPW][8][8][3];      // per point, node: the point's residual terms
+  float2 nd[2][5][kBrickEPW][8][3];   // per point being summed: g h u v w per node
+  int eg[kBrickEPW], scale[kBrickEPW];
+};
+
 __global__ void __launch_bounds__(32 * kBrickWarps) k_brick_assemble_ff(ContinuumView v) {
   __shared__ BrickSmemFF sm_all[kBrickWarps];
   const int wi = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -632,22 +635,30 @@ __global__ void __launch_bounds__(32 * kBrickWarps) k_brick_assemble_ff(Continuu
   const long npts = (long)v.ne * 8;
   {
     const int el = lane >> 3, ip = lane & 7, e = e0 + el;
-    const bool live = e < v.ne;
-    const long pt = (long)(live ? e : e0) * 8 + ip;
-    // FP64 dN/dx for the resisting force, and the element's largest exponent
-    int eg = -1000, ed = -1000;
+    const long pt = (long)(e < v.ne ? e : e0) * 8 + ip;
+    int eg = -1000;
+    double g[3][8];
 #pragma unroll
     for (int i = 0; i < 3; i++)
 #pragma unroll
       for (int a = 0; a < 8; a++) {
-        const double gv = v.geo[(8 * i + a) * npts + pt];
-        S.gd[el][ip][a][i] = gv;
-        eg = max(eg, f64_exponent(gv));
+        g[i][a] = v.geo[(8 * i + a) * npts + pt];
+        eg = max(eg, f64_exponent(g[i][a]));
       }
     const double dvol = v.geo[24 * npts + pt];
+    double ss[6];
+#pragma unroll
+    for (int c = 0; c < 6; c++) ss[c] = dvol * v.sig[c * npts + pt];
+    // the point's residual terms, node a, row i of the stress tensor
+#pragma unroll
+    for (int a = 0; a < 8; a++) {
+      S.rt[el][ip][a][0] = g[0][a] * ss[0] + g[1][a] * ss[3] + g[2][a] * ss[5];
+      S.rt[el][ip][a][1] = g[0][a] * ss[3] + g[1][a] * ss[1] + g[2][a] * ss[4];
+      S.rt[el][ip][a][2] = g[0][a] * ss[5] + g[1][a] * ss[4] + g[2][a] * ss[2];
+    }
     const double ca = v.tan[pt], cb = v.tan[npts + pt], cc = v.tan[2 * npts + pt];
     const double da = dvol * ca, dbh = dvol * (0.5 * cb), dc = dvol * cc;
-    ed = max(max(f64_exponent(da), f64_exponent(dbh)), f64_exponent(dc));
+    int ed = max(max(f64_exponent(da), f64_exponent(dbh)), f64_exponent(dc));
 #pragma unroll
     for (int o = 1; o < 8; o <<= 1) {
       eg = max(eg, __shfl_xor_sync(0xffffffffu, eg, o));
@@ -656,98 +667,111 @@ __global__ void __launch_bounds__(32 * kBrickWarps) k_brick_assemble_ff(Continuu
     if (eg < -126) eg = 0;      // all of dN/dx zero: a degenerate element
     if (ed < -1000) ed = 0;
     ed = min(ed, 1022);         // a non-finite scaling stays non-finite below
-    if (ip == 0) S.scale[el] = 2 * eg + ed;
-#pragma unroll
-    for (int c = 0; c < 6; c++) S.ss[el][ip][c] = dvol * v.sig[c * npts + pt];
-    // 2^-ed as a double and 2^-eg as a float (|eg| < 100 for split geometry)
+    if (ip == 0) {
+      S.eg[el] = eg;
+      S.scale[el] = 2 * eg + ed;
+    }
     const double pd = __hiloint2double((int)((unsigned)(1023 - ed) << 20), 0);
-    const float fg = __uint_as_float((unsigned)(127 - eg) << 23);
-    const float2 sa = split2(da * pd), sb = split2(dbh * pd), sc = split2(dc * pd);
-    float2 n[6];
+    S.pt[el][ip][0] = split2(da * pd);
+    S.pt[el][ip][1] = split2(dbh * pd);
+    S.pt[el][ip][2] = split2(dc * pd);
 #pragma unroll
-    for (int c = 0; c < 6; c++) n[c] = split2(v.tan[(3 + c) * npts + pt]);
-#pragma unroll 2
-    for (int a = 0; a < 8; a++) {
+    for (int c = 0; c < 6; c++) S.pt[el][ip][3 + c] = split2(v.tan[(3 + c) * npts + pt]);
+  }
+  __syncwarp();
+  const int el = lane >> 3, a = lane & 7, e = e0 + el;
+  const bool live = e < v.ne;
+  const long ebase = (long)(live ? e : e0) * 8;
+  // resisting force of node a: the points' terms in point order
+  if (live) {
+#pragma unroll
+    for (int i = 0; i < 3; i++) {
+      double r = 0.0;
+#pragma unroll
+      for (int ip = 0; ip < 8; ip++) r += S.rt[el][ip][a][i];
+      v.Re[(long)e * 24 + 3 * a + i] = r;
+    }
+  }
+  const float fg = __uint_as_float((unsigned)(127 - S.eg[el]) << 23);
+  constexpr int kTasks = kBrickEPW * 36;
+  constexpr int kPer = (kTasks + 31) / 32;
+  float ah[kPer][9], al[kPer][9];
+#pragma unroll
+  for (int j = 0; j < kPer; j++)
+#pragma unroll
+    for (int q = 0; q < 9; q++) ah[j][q] = al[j][q] = 0.f;
+#pragma unroll 1
+  for (int ip = 0; ip < 8; ip++) {
+    const int buf = ip & 1;
+    {
+      // node a of element el at point ip
+      const float2 *gp = v.geo2 + (ebase + ip) * 24 + a;
       float2 gi[3];
 #pragma unroll
       for (int i = 0; i < 3; i++) {
-        const float2 q = v.geo2[(8 * i + a) * npts + pt];
+        const float2 q = gp[8 * i];
         gi[i] = make_float2(__fmul_rn(q.x, fg), __fmul_rn(q.y, fg));
       }
-      // h = n . g with n = [xx yy zz xy yz zx]
+      const float2 *P = S.pt[el][ip];
       const int row[3][3] = {{0, 3, 5}, {3, 1, 4}, {5, 4, 2}};
 #pragma unroll
       for (int i = 0; i < 3; i++) {
         float hh = 0.f, hl = 0.f;
 #pragma unroll
-        for (int j = 0; j < 3; j++) ff_madd(n[row[i][j]], gi[j], hh, hl);
+        for (int j = 0; j < 3; j++) ff_madd(P[3 + row[i][j]], gi[j], hh, hl);
         const float hs = __fadd_rn(hh, hl);
         const float2 hi = make_float2(hs, __fsub_rn(hl, __fsub_rn(hs, hh)));
-        S.g[el][ip][a][i] = gi[i];
-        S.h[el][ip][a][i] = hi;
-        S.u[el][ip][a][i] = ff_mul(sa, gi[i]);
-        S.vv[el][ip][a][i] = ff_mul(sb, gi[i]);
-        S.w[el][ip][a][i] = ff_mul(sc, hi);
+        S.nd[buf][0][el][a][i] = gi[i];
+        S.nd[buf][1][el][a][i] = hi;
+        S.nd[buf][2][el][a][i] = ff_mul(P[0], gi[i]);
+        S.nd[buf][3][el][a][i] = ff_mul(P[1], gi[i]);
+        S.nd[buf][4][el][a][i] = ff_mul(P[2], hi);
       }
     }
-  }
-  __syncwarp();
-  for (int t = lane; t < kBrickEPW * 24; t += 32) {
-    const int el = t / 24, q = t % 24, e = e0 + el;
-    if (e >= v.ne) continue;
-    const int a = q / 3, i = q % 3;
-    const int r0 = (i == 0) ? 0 : (i == 1) ? 3 : 5;
-    const int r1 = (i == 0) ? 3 : (i == 1) ? 1 : 4;
-    const int r2 = (i == 0) ? 5 : (i == 1) ? 4 : 2;
-    double r = 0.0;
+    __syncwarp();
 #pragma unroll
-    for (int ip = 0; ip < 8; ip++)
-      r += S.gd[el][ip][a][0] * S.ss[el][ip][r0] + S.gd[el][ip][a][1] * S.ss[el][ip][r1] +
-           S.gd[el][ip][a][2] * S.ss[el][ip][r2];
-    v.Re[(long)e * 24 + q] = r;
-  }
-  for (int t = lane; t < kBrickEPW * 36; t += 32) {
-    const int el = t / 36, pp = t % 36, e = e0 + el;
-    if (e >= v.ne) continue;
-    const int a = kPairA[pp], b = kPairB[pp];
-    float ah[3][3], al[3][3];
+    for (int j = 0; j < kPer; j++) {
+      const int t = lane + 32 * j;
+      if (t < kTasks && e0 + t / 36 < v.ne) {
+        const int te = t / 36, pp = t % 36;
+        const int ta = kPairA[pp], tb = kPairB[pp];
+        float2 gb[3], hb[3], ua[3], va[3], wa[3];
 #pragma unroll
-    for (int i = 0; i < 3; i++)
-#pragma unroll
-      for (int k = 0; k < 3; k++) ah[i][k] = al[i][k] = 0.f;
-#pragma unroll 2
-    for (int ip = 0; ip < 8; ip++) {
-      float2 gb[3], hb[3], ua[3], va[3], wa[3];
-#pragma unroll
-      for (int j = 0; j < 3; j++) {
-        gb[j] = S.g[el][ip][b][j];
-        hb[j] = S.h[el][ip][b][j];
-        ua[j] = S.u[el][ip][a][j];
-        va[j] = S.vv[el][ip][a][j];
-        wa[j] = S.w[el][ip][a][j];
-      }
-      // (b/2) dvol dNa . dNb on the diagonal
-      float dh = 0.f, dl = 0.f;
-#pragma unroll
-      for (int j = 0; j < 3; j++) ff_madd(va[j], gb[j], dh, dl);
-#pragma unroll
-      for (int i = 0; i < 3; i++) {
-#pragma unroll
-        for (int k = 0; k < 3; k++) {
-          ff_madd(ua[i], gb[k], ah[i][k], al[i][k]);
-          ff_madd(va[k], gb[i], ah[i][k], al[i][k]);
-          ff_madd(wa[i], hb[k], ah[i][k], al[i][k]);
+        for (int q = 0; q < 3; q++) {
+          gb[q] = S.nd[buf][0][te][tb][q];
+          hb[q] = S.nd[buf][1][te][tb][q];
+          ua[q] = S.nd[buf][2][te][ta][q];
+          va[q] = S.nd[buf][3][te][ta][q];
+          wa[q] = S.nd[buf][4][te][ta][q];
         }
-        ff_add(dh, dl, ah[i][i], al[i][i]);
+        // (b/2) dvol dNa . dNb on the diagonal
+        float dh = 0.f, dl = 0.f;
+#pragma unroll
+        for (int q = 0; q < 3; q++) ff_madd(va[q], gb[q], dh, dl);
+#pragma unroll
+        for (int i = 0; i < 3; i++) {
+#pragma unroll
+          for (int k = 0; k < 3; k++) {
+            ff_madd(ua[i], gb[k], ah[j][3 * i + k], al[j][3 * i + k]);
+            ff_madd(va[k], gb[i], ah[j][3 * i + k], al[j][3 * i + k]);
+            ff_madd(wa[i], hb[k], ah[j][3 * i + k], al[j][3 * i + k]);
+          }
+          ff_add(dh, dl, ah[j][4 * i], al[j][4 * i]);
+        }
       }
     }
-    const int sc = S.scale[el];
-    double *Ke = v.Ke + (long)e * 324 + pp * 9;
+  }
 #pragma unroll
-    for (int i = 0; i < 3; i++)
+  for (int j = 0; j < kPer; j++) {
+    const int t = lane + 32 * j;
+    if (t < kTasks && e0 + t / 36 < v.ne) {
+      const int te = t / 36, pp = t % 36;
+      const int sc = S.scale[te];
+      double *Ke = v.Ke + (long)(e0 + te) * 324 + pp * 9;
 #pragma unroll
-      for (int k = 0; k < 3; k++)
-        Ke[3 * i + k] = f32_to_f64_scaled(ah[i][k], sc) + f32_to_f64_scaled(al[i][k], sc);
+      for (int q = 0; q < 9; q++)
+        Ke[q] = f32_to_f64_scaled(ah[j][q], sc) + f32_to_f64_scaled(al[j][q], sc);
+    }
   }
 }
 
