@@ -696,10 +696,18 @@ __global__ void __launch_bounds__(32 * kBrickWarps) k_brick_assemble_ff(Continuu
   constexpr int kTasks = kBrickEPW * 36;
   constexpr int kPer = (kTasks + 31) / 32;
   float ah[kPer][9], al[kPer][9];
+  // this lane's node-pair tasks, decoded once: element | a << 8 | b << 16,
+  // or -1 (the pair table lives in constant memory, which serialises lanes
+  // that read different entries)
+  int task[kPer];
 #pragma unroll
-  for (int j = 0; j < kPer; j++)
+  for (int j = 0; j < kPer; j++) {
+    const int t = lane + 32 * j, te = t / 36, pp = t % 36;
+    task[j] = (t < kTasks && e0 + te < v.ne) ? (te | (int)kPairA[pp] << 8 | (int)kPairB[pp] << 16)
+                                             : -1;
 #pragma unroll
     for (int q = 0; q < 9; q++) ah[j][q] = al[j][q] = 0.f;
+  }
 #pragma unroll 1
   for (int ip = 0; ip < 8; ip++) {
     const int buf = ip & 1;
@@ -731,10 +739,8 @@ __global__ void __launch_bounds__(32 * kBrickWarps) k_brick_assemble_ff(Continuu
     __syncwarp();
 #pragma unroll
     for (int j = 0; j < kPer; j++) {
-      const int t = lane + 32 * j;
-      if (t < kTasks && e0 + t / 36 < v.ne) {
-        const int te = t / 36, pp = t % 36;
-        const int ta = kPairA[pp], tb = kPairB[pp];
+      if (task[j] >= 0) {
+        const int te = task[j] & 0xff, ta = (task[j] >> 8) & 0xff, tb = task[j] >> 16;
         float2 gb[3], hb[3], ua[3], va[3], wa[3];
 #pragma unroll
         for (int q = 0; q < 3; q++) {
@@ -763,9 +769,8 @@ __global__ void __launch_bounds__(32 * kBrickWarps) k_brick_assemble_ff(Continuu
   }
 #pragma unroll
   for (int j = 0; j < kPer; j++) {
-    const int t = lane + 32 * j;
-    if (t < kTasks && e0 + t / 36 < v.ne) {
-      const int te = t / 36, pp = t % 36;
+    if (task[j] >= 0) {
+      const int t = lane + 32 * j, te = t / 36, pp = t % 36;
       const int sc = S.scale[te];
       double *Ke = v.Ke + (long)(e0 + te) * 324 + pp * 9;
 #pragma unroll

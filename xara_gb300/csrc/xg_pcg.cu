@@ -329,9 +329,11 @@ __device__ __forceinline__ void precondition_block(const PcgSystem &S, int k, Bl
 // scalars: [0] rz  [1] bb  [2] rr  [3] iterations  [4] relres
 // partials: [0, 3 nb) the inner products' block sums; with KB > 0 also
 // [3 nb, 4 nb) the blocks' largest |z| or |p| for the split's scale.
+// KB > 0: one 512-thread block per SM with up to 128 registers a thread, so
+// that a thread keeps two whole blocks' loads of the SpMV in flight.
 template <int KB>
-__global__ void __launch_bounds__(kPcgThreads) k_pcg(PcgSystem S, const double *b, double *x,
-                                                     double rtol, int maxit) {
+__global__ void __launch_bounds__(kPcgThreads, KB > 0 ? 1 : 2)
+    k_pcg(PcgSystem S, const double *b, double *x, double rtol, int maxit) {
   __shared__ double smem[40];
   volatile int *flags = S.flags;
   const int gtid = blockIdx.x * blockDim.x + threadIdx.x;
