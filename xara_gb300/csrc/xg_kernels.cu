@@ -609,20 +609,22 @@ __device__ __forceinline__ double f32_to_f64_scaled(float f, int s) {
 // product lies near 1 whatever the model's units; the scale comes back
 // exactly in the exponent when a pair is written as a double.
 //
-// Two phases.  Per point (lane = element, point; coalesced loads of the
-// point-major geometry and state): the scale exponents, the split tangent
-// scalings and deviatoric direction, and the point's FP64 residual terms.
-// Then over the eight points (lane = element, node): the node's split
-// gradient at that point (element-major geo2, coalesced), its projection
-// h = n . dN/dx and its three scalings, staged in a double-buffered 3.8 KB
-// slice, after which every lane adds the point's terms to the node-pair
-// blocks it owns (144 per warp, 4.5 per lane) in registers.  The element
-// arrays never sit in shared memory whole (17 KB per warp instead of 38),
-// so three times as many warps fit on an SM.
+// Per point first (lane = element, point): the scale exponents, the split
+// tangent scalings and deviatoric direction, dvol * stress.  Then over the
+// eight points (lane = element, node): the node's resisting-force terms in
+// FP64, its split gradient at that point (element-major geo2), the
+// projection h = n . dN/dx and the three scalings, staged in a 3.8 KB
+// slice; then every lane adds the point's terms to the node-pair blocks it
+// owns (144 per warp, 4.5 per lane), whose float-float sums sit in shared
+// memory, transposed so that neighbouring lanes use neighbouring banks.  The
+// task loop is a real loop: with the accumulators in registers its five
+// unrolled copies made a 32 KB loop body that the warps' instruction
+// fetches thrashed.
 struct BrickSmemFF {
   float2 pt[kBrickEPW][8][9];         // per point: dvol*{a, b/2, c}*2^-ed, n[6] (split)
-  double rt[kBrickEPW][8][8][3];      // per point, node: the point's residual terms
-  float2 nd[2][5][kBrickEPW][8][3];   // per point being summed: g h u v w per node
+  double ss[kBrickEPW][8][6];         // per point: dvol * stress
+  float2 nd[5][kBrickEPW][8][3];      // the point being summed: g h u v w per node
+  float2 acc[9][kBrickEPW * 36];      // node-pair block sums (hi, lo), [entry][task]
   int eg[kBrickEPW], scale[kBrickEPW];
 };
 
@@ -633,29 +635,16 @@ __global__ void __launch_bounds__(32 * kBrickWarps) k_brick_assemble_ff(Continuu
   const int e0 = (blockIdx.x * kBrickWarps + wi) * kBrickEPW;
   if (e0 >= v.ne) return;
   const long npts = (long)v.ne * 8;
+  constexpr int kTasks = kBrickEPW * 36;
   {
     const int el = lane >> 3, ip = lane & 7, e = e0 + el;
     const long pt = (long)(e < v.ne ? e : e0) * 8 + ip;
     int eg = -1000;
-    double g[3][8];
 #pragma unroll
-    for (int i = 0; i < 3; i++)
-#pragma unroll
-      for (int a = 0; a < 8; a++) {
-        g[i][a] = v.geo[(8 * i + a) * npts + pt];
-        eg = max(eg, f64_exponent(g[i][a]));
-      }
+    for (int q = 0; q < 24; q++) eg = max(eg, f64_exponent(v.geo[q * npts + pt]));
     const double dvol = v.geo[24 * npts + pt];
-    double ss[6];
 #pragma unroll
-    for (int c = 0; c < 6; c++) ss[c] = dvol * v.sig[c * npts + pt];
-    // the point's residual terms, node a, row i of the stress tensor
-#pragma unroll
-    for (int a = 0; a < 8; a++) {
-      S.rt[el][ip][a][0] = g[0][a] * ss[0] + g[1][a] * ss[3] + g[2][a] * ss[5];
-      S.rt[el][ip][a][1] = g[0][a] * ss[3] + g[1][a] * ss[1] + g[2][a] * ss[4];
-      S.rt[el][ip][a][2] = g[0][a] * ss[5] + g[1][a] * ss[4] + g[2][a] * ss[2];
-    }
+    for (int c = 0; c < 6; c++) S.ss[el][ip][c] = dvol * v.sig[c * npts + pt];
     const double ca = v.tan[pt], cb = v.tan[npts + pt], cc = v.tan[2 * npts + pt];
     const double da = dvol * ca, dbh = dvol * (0.5 * cb), dc = dvol * cc;
     int ed = max(max(f64_exponent(da), f64_exponent(dbh)), f64_exponent(dc));
@@ -677,42 +666,26 @@ __global__ void __launch_bounds__(32 * kBrickWarps) k_brick_assemble_ff(Continuu
     S.pt[el][ip][2] = split2(dc * pd);
 #pragma unroll
     for (int c = 0; c < 6; c++) S.pt[el][ip][3 + c] = split2(v.tan[(3 + c) * npts + pt]);
+    for (int t = lane; t < 9 * kTasks; t += 32) (&S.acc[0][0])[t] = make_float2(0.f, 0.f);
   }
   __syncwarp();
   const int el = lane >> 3, a = lane & 7, e = e0 + el;
   const bool live = e < v.ne;
   const long ebase = (long)(live ? e : e0) * 8;
-  // resisting force of node a: the points' terms in point order
-  if (live) {
-#pragma unroll
-    for (int i = 0; i < 3; i++) {
-      double r = 0.0;
-#pragma unroll
-      for (int ip = 0; ip < 8; ip++) r += S.rt[el][ip][a][i];
-      v.Re[(long)e * 24 + 3 * a + i] = r;
-    }
-  }
   const float fg = __uint_as_float((unsigned)(127 - S.eg[el]) << 23);
-  constexpr int kTasks = kBrickEPW * 36;
-  constexpr int kPer = (kTasks + 31) / 32;
-  float ah[kPer][9], al[kPer][9];
-  // this lane's node-pair tasks, decoded once: element | a << 8 | b << 16,
-  // or -1 (the pair table lives in constant memory, which serialises lanes
-  // that read different entries)
-  int task[kPer];
-#pragma unroll
-  for (int j = 0; j < kPer; j++) {
-    const int t = lane + 32 * j, te = t / 36, pp = t % 36;
-    task[j] = (t < kTasks && e0 + te < v.ne) ? (te | (int)kPairA[pp] << 8 | (int)kPairB[pp] << 16)
-                                             : -1;
-#pragma unroll
-    for (int q = 0; q < 9; q++) ah[j][q] = al[j][q] = 0.f;
-  }
+  double r0 = 0.0, r1 = 0.0, r2 = 0.0;     // resisting force of node a
 #pragma unroll 1
   for (int ip = 0; ip < 8; ip++) {
-    const int buf = ip & 1;
     {
-      // node a of element el at point ip
+      // node a of element el at point ip: resisting-force terms (FP64, the
+      // points in order) and the staged float-float terms
+      const double *Sg = S.ss[el][ip];
+      const double g0 = v.geo[a * npts + ebase + ip];
+      const double g1 = v.geo[(8 + a) * npts + ebase + ip];
+      const double g2 = v.geo[(16 + a) * npts + ebase + ip];
+      r0 += g0 * Sg[0] + g1 * Sg[3] + g2 * Sg[5];
+      r1 += g0 * Sg[3] + g1 * Sg[1] + g2 * Sg[4];
+      r2 += g0 * Sg[5] + g1 * Sg[4] + g2 * Sg[2];
       const float2 *gp = v.geo2 + (ebase + ip) * 24 + a;
       float2 gi[3];
 #pragma unroll
@@ -729,53 +702,68 @@ __global__ void __launch_bounds__(32 * kBrickWarps) k_brick_assemble_ff(Continuu
         for (int j = 0; j < 3; j++) ff_madd(P[3 + row[i][j]], gi[j], hh, hl);
         const float hs = __fadd_rn(hh, hl);
         const float2 hi = make_float2(hs, __fsub_rn(hl, __fsub_rn(hs, hh)));
-        S.nd[buf][0][el][a][i] = gi[i];
-        S.nd[buf][1][el][a][i] = hi;
-        S.nd[buf][2][el][a][i] = ff_mul(P[0], gi[i]);
-        S.nd[buf][3][el][a][i] = ff_mul(P[1], gi[i]);
-        S.nd[buf][4][el][a][i] = ff_mul(P[2], hi);
+        S.nd[0][el][a][i] = gi[i];
+        S.nd[1][el][a][i] = hi;
+        S.nd[2][el][a][i] = ff_mul(P[0], gi[i]);
+        S.nd[3][el][a][i] = ff_mul(P[1], gi[i]);
+        S.nd[4][el][a][i] = ff_mul(P[2], hi);
       }
     }
     __syncwarp();
+#pragma unroll 1
+    for (int t = lane; t < kTasks; t += 32) {
+      const int te = t / 36, pp = t % 36;
+      if (e0 + te >= v.ne) continue;
+      const int ta = kPairA[pp], tb = kPairB[pp];
+      float2 gb[3], hb[3], ua[3], va[3], wa[3];
 #pragma unroll
-    for (int j = 0; j < kPer; j++) {
-      if (task[j] >= 0) {
-        const int te = task[j] & 0xff, ta = (task[j] >> 8) & 0xff, tb = task[j] >> 16;
-        float2 gb[3], hb[3], ua[3], va[3], wa[3];
-#pragma unroll
-        for (int q = 0; q < 3; q++) {
-          gb[q] = S.nd[buf][0][te][tb][q];
-          hb[q] = S.nd[buf][1][te][tb][q];
-          ua[q] = S.nd[buf][2][te][ta][q];
-          va[q] = S.nd[buf][3][te][ta][q];
-          wa[q] = S.nd[buf][4][te][ta][q];
-        }
-        // (b/2) dvol dNa . dNb on the diagonal
-        float dh = 0.f, dl = 0.f;
-#pragma unroll
-        for (int q = 0; q < 3; q++) ff_madd(va[q], gb[q], dh, dl);
-#pragma unroll
-        for (int i = 0; i < 3; i++) {
-#pragma unroll
-          for (int k = 0; k < 3; k++) {
-            ff_madd(ua[i], gb[k], ah[j][3 * i + k], al[j][3 * i + k]);
-            ff_madd(va[k], gb[i], ah[j][3 * i + k], al[j][3 * i + k]);
-            ff_madd(wa[i], hb[k], ah[j][3 * i + k], al[j][3 * i + k]);
-          }
-          ff_add(dh, dl, ah[j][4 * i], al[j][4 * i]);
-        }
+      for (int q = 0; q < 3; q++) {
+        gb[q] = S.nd[0][te][tb][q];
+        hb[q] = S.nd[1][te][tb][q];
+        ua[q] = S.nd[2][te][ta][q];
+        va[q] = S.nd[3][te][ta][q];
+        wa[q] = S.nd[4][te][ta][q];
       }
+      float ah[9], al[9];
+#pragma unroll
+      for (int q = 0; q < 9; q++) {
+        const float2 c = S.acc[q][t];
+        ah[q] = c.x;
+        al[q] = c.y;
+      }
+      // (b/2) dvol dNa . dNb on the diagonal
+      float dh = 0.f, dl = 0.f;
+#pragma unroll
+      for (int q = 0; q < 3; q++) ff_madd(va[q], gb[q], dh, dl);
+#pragma unroll
+      for (int i = 0; i < 3; i++) {
+#pragma unroll
+        for (int k = 0; k < 3; k++) {
+          ff_madd(ua[i], gb[k], ah[3 * i + k], al[3 * i + k]);
+          ff_madd(va[k], gb[i], ah[3 * i + k], al[3 * i + k]);
+          ff_madd(wa[i], hb[k], ah[3 * i + k], al[3 * i + k]);
+        }
+        ff_add(dh, dl, ah[4 * i], al[4 * i]);
+      }
+#pragma unroll
+      for (int q = 0; q < 9; q++) S.acc[q][t] = make_float2(ah[q], al[q]);
     }
+    __syncwarp();   // the slice is restaged for the next point
   }
+  if (live) {
+    v.Re[(long)e * 24 + 3 * a] = r0;
+    v.Re[(long)e * 24 + 3 * a + 1] = r1;
+    v.Re[(long)e * 24 + 3 * a + 2] = r2;
+  }
+  for (int t = lane; t < kTasks; t += 32) {
+    const int te = t / 36, pp = t % 36;
+    if (e0 + te >= v.ne) continue;
+    const int sc = S.scale[te];
+    double *Ke = v.Ke + (long)(e0 + te) * 324 + pp * 9;
 #pragma unroll
-  for (int j = 0; j < kPer; j++) {
-    if (task[j] >= 0) {
-      const int t = lane + 32 * j, te = t / 36, pp = t % 36;
-      const int sc = S.scale[te];
-      double *Ke = v.Ke + (long)(e0 + te) * 324 + pp * 9;
-#pragma unroll
-      for (int q = 0; q < 9; q++)
-        Ke[q] = f32_to_f64_scaled(ah[j][q], sc) + f32_to_f64_scaled(al[j][q], sc);
+    for (int q = 0; q < 9; q++) {
+      const float2 c = S.acc[q][t];
+      Ke[q] = f32_to_f64_scaled(c.x, sc) + f32_to_f64_scaled(c.y, sc);
     }
   }
 }
