@@ -1162,7 +1162,7 @@ def brick_alg_bytes(npts, ne, nn, nnz, neq):
     return {
         "phase": npts * 112 + nn * 48 + nnz * 8 + neq * 8,
         "brick_update": npts * (112 + 48 + 72) + nn * 48,
-        "brick_assemble": npts * (48 + 72) + ne * (324 + 24) * 8 + nn * 24,
+        "brick_assemble": npts * (48 + 72) + ne * (576 + 24) * 8 + nn * 24,
         "gather_tangent": nnz * 8,
         "gather_resid": neq * 8,
     }

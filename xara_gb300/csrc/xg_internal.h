@@ -31,7 +31,7 @@ struct ContinuumView {
   double *tan;            // trial tangent: quad 6 unique D entries; brick a b c n(6)
   int *nfail;             // [1] points whose return map hit the iteration cap
   // element outputs (element-major scratch)
-  double *Ke;             // quad: [ne][64]; brick: [ne][324] upper node-pair blocks
+  double *Ke;             // [ne][ned*ned] row-major (quad 64, brick 576)
   double *Re;             // [ne][ned]
   // bricks: shape-function gradients dN_a/dx_i at [(8i+a)*npts + pt] and the
   // Jacobian determinant at [24*npts + pt], formed once (the geometry does
@@ -52,7 +52,21 @@ struct GatherMap {
   const int *slot_chunk;  // [nslots+1] chunk range per slot
   const int64_t *src;     // contribution source indices into the scratch
   const int *src32;       // the same as 32-bit indices when the scratch is small enough, or null
+  // runs (built when every source fits 32 bits): consecutive slots whose
+  // contribution lists match term by term with sources one apart (the
+  // columns of one node's dofs in a row), summed by one thread that reads a
+  // single source index per contribution; slots with more than kRunMaxTerms
+  // contributions stay with the chunks above (long_chunks, long_slots)
+  int nruns;
+  const int *run_slot;    // [nruns] first slot
+  const int *run_meta;    // [nruns] length (bits 0-3) | contributions << 4
+  const int *run_begin;   // [nruns] first source of the run's first slot in run_src
+  const int *run_src;     // sources of each run's first slot
+  int nlong_chunks, nlong_slots;
+  const int *long_chunks; // chunks of the long slots
+  const int *long_slots;  // the long slots
 };
+constexpr int kRunMaxLen = 6, kRunMaxTerms = 32;
 
 // ---------------------------------------------------------------------------
 // kernel launchers (xg_kernels.cu)
@@ -68,6 +82,7 @@ int launch_record(int kind, int n, const int *idx, const double *src, double t, 
                   int first, double *out, cudaStream_t s);
 int launch_gather(const GatherMap &g, const double *scratch, double *partial, double *out,
                   cudaStream_t s);
+int gather_launch_count(const GatherMap &g);   // kernels launch_gather issues
 int launch_j2_zero_state(const ContinuumView &v, cudaStream_t s);
 
 // Block-Jacobi preconditioned CG (xg_pcg.cu)

@@ -454,9 +454,10 @@ constexpr int kBrickWarps = 1;
 constexpr int kBrickEPW = 4;   // elements per warp
 
 // Four elements per warp: Brick::formResidAndTangent (Brick.cpp:844-1021)
-// from the stored point state, K in upper node-pair blocks:
-// Ke[e*324 + p*9 + 3*i + k] = K(3a+i, 3b+k) for the pair p = (a <= b).
-// Re[e*24 + 3a + i].  The lanes take (element, point) to stage the point
+// from the stored point state, formed per node-pair block a <= b and written
+// with its transpose: Ke[e*576 + (3a+i)*24 + 3b+k] = K(3a+i, 3b+k), row-major
+// like every element's scratch, so each assembled slot's contributions lie
+// consecutive for consecutive columns.  Re[e*24 + 3a + i].  The lanes take (element, point) to stage the point
 // terms of every node -- dN/dx, its product with the tangent's deviatoric
 // direction and the three scalings of the node-pair sum -- then the
 // elements' 96 residual entries and 144 node pairs three and five at a
@@ -552,11 +553,14 @@ __global__ void __launch_bounds__(32 * kBrickWarps) k_brick_assemble(ContinuumVi
         acc[i][i] += dot;
       }
     }
-    double *Ke = v.Ke + (long)e * 324 + pp * 9;
+    double *Ke = v.Ke + (long)e * 576;
 #pragma unroll
     for (int i = 0; i < 3; i++)
 #pragma unroll
-      for (int k = 0; k < 3; k++) Ke[3 * i + k] = acc[i][k];
+      for (int k = 0; k < 3; k++) {
+        Ke[(3 * a + i) * 24 + 3 * b + k] = acc[i][k];
+        if (a != b) Ke[(3 * b + k) * 24 + 3 * a + i] = acc[i][k];
+      }
   }
 }
 
@@ -759,12 +763,17 @@ __global__ void __launch_bounds__(32 * kBrickWarps) k_brick_assemble_ff(Continuu
     const int te = t / 36, pp = t % 36;
     if (e0 + te >= v.ne) continue;
     const int sc = S.scale[te];
-    double *Ke = v.Ke + (long)(e0 + te) * 324 + pp * 9;
+    const int ta = kPairA[pp], tb = kPairB[pp];
+    double *Ke = v.Ke + (long)(e0 + te) * 576;
 #pragma unroll
-    for (int q = 0; q < 9; q++) {
-      const float2 c = S.acc[q][t];
-      Ke[q] = f32_to_f64_scaled(c.x, sc) + f32_to_f64_scaled(c.y, sc);
-    }
+    for (int i = 0; i < 3; i++)
+#pragma unroll
+      for (int k = 0; k < 3; k++) {
+        const float2 c = S.acc[3 * i + k][t];
+        const double kv = f32_to_f64_scaled(c.x, sc) + f32_to_f64_scaled(c.y, sc);
+        Ke[(3 * ta + i) * 24 + 3 * tb + k] = kv;
+        if (ta != tb) Ke[(3 * tb + k) * 24 + 3 * ta + i] = kv;
+      }
   }
 }
 
@@ -822,6 +831,59 @@ __global__ void k_gather_chunks(GatherMap g, const Idx *__restrict__ src,
   const int slot = g.chunk_slot[c];
   if (g.slot_chunk[slot + 1] - g.slot_chunk[slot] == 1) out[slot] = s;
   else partial[c] = s;
+}
+
+// Thread per run: the run's slots summed in contribution order (the element
+// order, as the chunks sum), each contribution's values read as one
+// contiguous piece.
+__global__ void k_gather_runs(GatherMap g, const double *__restrict__ scratch,
+                              double *__restrict__ out) {
+  const int r = blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= g.nruns) return;
+  const int s0 = g.run_slot[r], meta = g.run_meta[r];
+  const int len = meta & 15, n = meta >> 4;
+  const int *src = g.run_src + g.run_begin[r];
+  double acc[kRunMaxLen];
+#pragma unroll
+  for (int t = 0; t < kRunMaxLen; t++) acc[t] = 0.0;
+  for (int q = 0; q < n; q++) {
+    const double *p = scratch + (unsigned)src[q];
+#pragma unroll
+    for (int t = 0; t < kRunMaxLen; t++)
+      if (t < len) acc[t] += p[t];
+  }
+#pragma unroll
+  for (int t = 0; t < kRunMaxLen; t++)
+    if (t < len) out[s0 + t] = acc[t];
+}
+
+// The chunk and slot kernels over a list of chunks / slots (the long slots
+// of a map with runs), or over all of them when the list is null.
+template <typename Idx>
+__global__ void k_gather_chunk_list(GatherMap g, const Idx *__restrict__ src,
+                                    const double *__restrict__ scratch,
+                                    double *__restrict__ partial, double *__restrict__ out) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= g.nlong_chunks) return;
+  const int c = g.long_chunks[i];
+  double s = 0.0;
+  const int64_t b = g.chunk_begin[c], end = g.chunk_begin[c + 1];
+  for (int64_t k = b; k < end; k++) s += scratch[src[k]];
+  const int slot = g.chunk_slot[c];
+  if (g.slot_chunk[slot + 1] - g.slot_chunk[slot] == 1) out[slot] = s;
+  else partial[c] = s;
+}
+
+__global__ void k_gather_slot_list(GatherMap g, const double *__restrict__ partial,
+                                   double *__restrict__ out) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= g.nlong_slots) return;
+  const int s = g.long_slots[i];
+  const int c0 = g.slot_chunk[s], c1 = g.slot_chunk[s + 1];
+  if (c1 - c0 == 1) return;               // written by its chunk
+  double v = 0.0;
+  for (int c = c0; c < c1; c++) v += partial[c];
+  out[s] = v;
 }
 
 __global__ void k_gather_slots(GatherMap g, const double *__restrict__ partial,
@@ -980,9 +1042,23 @@ int launch_j2_zero_state(const ContinuumView &v, cudaStream_t s) {
   k_j2_zero<<<nblocks((long)v.ne * v.nip), kThreads, 0, s>>>(v);
   return check_launch();
 }
+int gather_launch_count(const GatherMap &g) {
+  if (g.nslots == 0) return 0;
+  if (g.run_slot && g.src32) return (g.nruns > 0) + (g.nlong_chunks > 0) + (g.nlong_slots > 0);
+  return 2;
+}
 int launch_gather(const GatherMap &g, const double *scratch, double *partial, double *out,
                   cudaStream_t s) {
   if (g.nslots == 0) return 0;
+  if (g.run_slot && g.src32) {
+    if (g.nruns) k_gather_runs<<<nblocks(g.nruns), kThreads, 0, s>>>(g, scratch, out);
+    if (g.nlong_chunks)
+      k_gather_chunk_list<int><<<nblocks(g.nlong_chunks), kThreads, 0, s>>>(g, g.src32, scratch,
+                                                                             partial, out);
+    if (g.nlong_slots)
+      k_gather_slot_list<<<nblocks(g.nlong_slots), kThreads, 0, s>>>(g, partial, out);
+    return check_launch();
+  }
   if (g.src32)
     k_gather_chunks<int><<<nblocks(g.nchunks), kThreads, 0, s>>>(g, g.src32, scratch, partial, out);
   else

@@ -87,6 +87,8 @@ struct HostGather {
   std::vector<int> slot_chunk, chunk_slot;
   std::vector<int64_t> chunk_begin;
   std::vector<int64_t> src;
+  // runs (GatherMap): empty when a source does not fit 32 bits
+  std::vector<int> run_slot, run_meta, run_begin, run_src, long_chunks, long_slots;
 };
 
 // Build chunked gather lists from (slot, src) pairs given in assembly order.
@@ -119,6 +121,37 @@ void build_gather(int nslots, const std::vector<int> &slot_of, const std::vector
   // chunk c sums src[chunk_begin[c], chunk_begin[c+1]): the chunks of a slot
   // and of consecutive slots tile [0, total) (an empty slot has one empty
   // chunk starting where the next slot starts).
+
+  // runs: slot s opens a run that slots s+1 .. s+len-1 continue while they
+  // have the same number of contributions (at most kRunMaxTerms) and each
+  // contribution's source is the run's first slot's plus the offset
+  g.run_slot.clear(); g.run_meta.clear(); g.run_begin.clear(); g.run_src.clear();
+  g.long_chunks.clear(); g.long_slots.clear();
+  int64_t mx = 0;
+  for (int64_t v : g.src) mx = std::max(mx, v);
+  if (mx + kRunMaxLen >= INT32_MAX || (int64_t)g.src.size() >= INT32_MAX) return;
+  for (int s0 = 0; s0 < nslots;) {
+    const int64_t b = ptr[s0], n = ptr[s0 + 1] - b;
+    if (n > kRunMaxTerms) {
+      g.long_slots.push_back(s0);
+      for (int c = g.slot_chunk[s0]; c < g.slot_chunk[s0 + 1]; c++) g.long_chunks.push_back(c);
+      s0++;
+      continue;
+    }
+    int len = 1;
+    while (len < kRunMaxLen && s0 + len < nslots && ptr[s0 + len + 1] - ptr[s0 + len] == n) {
+      const int64_t bl = ptr[s0 + len];
+      bool same = true;
+      for (int64_t q = 0; q < n && same; q++) same = g.src[bl + q] == g.src[b + q] + len;
+      if (!same) break;
+      len++;
+    }
+    g.run_slot.push_back(s0);
+    g.run_meta.push_back(len | (int)n << 4);
+    g.run_begin.push_back((int)g.run_src.size());
+    for (int64_t q = 0; q < n; q++) g.run_src.push_back((int)g.src[b + q]);
+    s0 += len;
+  }
 }
 
 }  // namespace
@@ -158,6 +191,7 @@ struct xg_model {
   DBuf<int> d_gk_slot_chunk, d_gk_chunk_slot, d_gr_slot_chunk, d_gr_chunk_slot;
   DBuf<int64_t> d_gk_chunk_begin, d_gk_src, d_gr_chunk_begin, d_gr_src;
   DBuf<int> d_gk_src32, d_gr_src32;
+  DBuf<int> d_gk_run[6], d_gr_run[6];   // run_slot run_meta run_begin run_src long_chunks long_slots
   GatherMap gk{}, gr{};
   // solver
   DBuf<double> d_binv, d_r, d_z, d_p, d_q, d_pcg_part, d_scalars;
@@ -380,7 +414,7 @@ struct xg_model {
   long npts() const { return (long)ne * nip; }
   int ke_size() const {
     if (frames()) return ned * ned;
-    return etype == XG_ELE_QUAD ? 64 : 324;
+    return ned * ned;
   }
   // force-based frames: section and material tables, element state
   int fb_nb = 0, fb_nip = 0, fb_max_iters = 10, geom_transf = 0;
@@ -630,10 +664,6 @@ int xg_model::build_maps(HostGather &gk_h, HostGather &gr_h) {
   slot_of.reserve((size_t)ne * ned * ned);
   src_of.reserve((size_t)ne * ned * ned);
   std::vector<int> ids(ned);
-  // pair index for the brick's upper node-pair blocks
-  int pair_of[8][8];
-  for (int a = 0, p = 0; a < 8; a++)
-    for (int b = a; b < 8; b++, p++) { pair_of[a][b] = p; pair_of[b][a] = p; }
   for (int e = 0; e < ne; e++) {
     for (int a = 0; a < nen; a++)
       for (int j = 0; j < ndf; j++) ids[a * ndf + j] = eqn[(size_t)conn[(size_t)e * nen + a] * ndf + j];
@@ -647,15 +677,7 @@ int xg_model::build_maps(HostGather &gk_h, HostGather &gr_h) {
         const int *pos = std::lower_bound(rb, re, c);
         if (pos == re || *pos != c) return fail(XG_EINVAL, "pattern lookup failed");
         slot_of.push_back((int)(pos - colidx.data()));
-        int64_t src;
-        if (etype != XG_ELE_BRICK) {
-          src = (int64_t)e * ks + i * ned + j;
-        } else {
-          const int a = i / 3, ii = i % 3, b = j / 3, kk = j % 3;
-          const int p = pair_of[a][b];
-          src = (int64_t)e * ks + p * 9 + (a <= b ? ii * 3 + kk : kk * 3 + ii);
-        }
-        src_of.push_back(src);
+        src_of.push_back((int64_t)e * ks + i * ned + j);
       }
     }
   }
@@ -708,6 +730,19 @@ int xg_model::upload(const HostGather &gk_h, const HostGather &gr_h) {
   RET(d_gk_slot_chunk.upload(gk_h.slot_chunk.data(), gk_h.slot_chunk.size(), s));
   RET(d_gk_chunk_slot.upload(gk_h.chunk_slot.data(), gk_h.chunk_slot.size(), s));
   RET(d_gk_chunk_begin.upload(gk_h.chunk_begin.data(), gk_h.chunk_begin.size(), s));
+  // the runs of a map, when it has them
+  auto upload_runs = [&](const HostGather &h, DBuf<int> *d, GatherMap &g) -> int {
+    if (h.run_slot.empty() && h.long_slots.empty()) return 0;
+    const std::vector<int> *v[6] = {&h.run_slot, &h.run_meta, &h.run_begin, &h.run_src,
+                                    &h.long_chunks, &h.long_slots};
+    for (int k = 0; k < 6; k++) RET(d[k].upload(v[k]->data(), v[k]->size(), s));
+    g.nruns = (int)h.run_slot.size();
+    g.run_slot = d[0].p ? d[0].p : d[5].p;   // non-null marks a map with runs
+    g.run_meta = d[1].p; g.run_begin = d[2].p; g.run_src = d[3].p;
+    g.nlong_chunks = (int)h.long_chunks.size(); g.long_chunks = d[4].p;
+    g.nlong_slots = (int)h.long_slots.size(); g.long_slots = d[5].p;
+    return 0;
+  };
   // 32-bit source indices when every index fits (the usual case)
   auto upload_src = [&](const std::vector<int64_t> &src, DBuf<int64_t> &d64, DBuf<int> &d32) {
     int64_t mx = 0;
@@ -726,6 +761,8 @@ int xg_model::upload(const HostGather &gk_h, const HostGather &gr_h) {
   gk.nslots = nnz; gk.nchunks = (int)gk_h.chunk_slot.size();
   gk.chunk_slot = d_gk_chunk_slot.p; gk.chunk_begin = d_gk_chunk_begin.p;
   gk.slot_chunk = d_gk_slot_chunk.p; gk.src = d_gk_src.p; gk.src32 = d_gk_src32.p;
+  RET(upload_runs(gk_h, d_gk_run, gk));
+  RET(upload_runs(gr_h, d_gr_run, gr));
   gr.nslots = neq; gr.nchunks = (int)gr_h.chunk_slot.size();
   gr.chunk_slot = d_gr_chunk_slot.p; gr.chunk_begin = d_gr_chunk_begin.p;
   gr.slot_chunk = d_gr_slot_chunk.p; gr.src = d_gr_src.p; gr.src32 = d_gr_src32.p;
@@ -1331,10 +1368,10 @@ int xg_model::element_state(bool compute) {
   }
   prof_begin(P_GATHER_K);
   RET(launch_gather(gk, d_Ke.p, d_partial.p, d_vals.p, s));
-  prof_end(P_GATHER_K, 2);
+  prof_end(P_GATHER_K, gather_launch_count(gk));
   prof_begin(P_GATHER_R);
   RET(launch_gather(gr, d_Re.p, d_partial.p, d_resid.p, s));
-  prof_end(P_GATHER_R, 2);
+  prof_end(P_GATHER_R, gather_launch_count(gr));
   prof_flush();
   blocks_factored = false;
   prof_factored = false;
@@ -2284,21 +2321,7 @@ int xg_elemset_element_matrices(const xg_model *m, double *K, double *P) {
     for (int e = 0; e < m->ne; e++) {
       double *out = K + (size_t)e * ned * ned;
       const double *in = ke.data() + (size_t)e * m->ke_size();
-      if (m->etype != XG_ELE_BRICK) {
-        std::copy(in, in + (size_t)ned * ned, out);
-        continue;
-      }
-      // bricks keep the node-pair blocks a <= b (9 entries each, row-major);
-      // the element tangent is symmetric
-      int p = 0;
-      for (int a = 0; a < 8; a++)
-        for (int b = a; b < 8; b++, p++)
-          for (int i = 0; i < 3; i++)
-            for (int k = 0; k < 3; k++) {
-              const double v = in[p * 9 + 3 * i + k];
-              out[(3 * a + i) * ned + 3 * b + k] = v;
-              out[(3 * b + k) * ned + 3 * a + i] = v;
-            }
+      std::copy(in, in + (size_t)ned * ned, out);
     }
   }
   if (P) {
