@@ -14,6 +14,7 @@
 #include <cstdint>
 
 #include "xg_internal.h"
+#include "xg_rcp.h"
 
 namespace xg {
 
@@ -79,8 +80,10 @@ __device__ __forceinline__ void steel01_trial(const double *q, const double *hc,
 // Record slot 11 keeps R, which changes only where the branch does (the
 // reference recomputes the same value every call); q[11] holds Fy/E0 (the
 // model's device parameter table).  The Menegotto-Pinto powers go through
-// log/exp and 1/(epss0 - epsr), 1/dum2 are formed once: the stress and
-// tangent differ from the reference's expression order by a few ulps.
+// log/exp and 1/(epss0 - epsr), 1/dum2 are formed once, by the three-FMA
+// reciprocal of xg_rcp.h (within an ulp of the correctly rounded one): the
+// stress and tangent differ from the reference's expression order by a few
+// ulps.
 __device__ void steel02_trial(const double *q, const double *hc, double trialStrain,
                               double *ht) {
   const double Fy = q[0], E0 = q[1], b = q[2], R0 = q[3], cR1 = q[4], cR2 = q[5];
@@ -134,7 +137,7 @@ __device__ void steel02_trial(const double *q, const double *hc, double trialStr
     const double xi = fabs((epspl - epss0) / epsy);
     R = R0 * (1.0 - (cR1 * xi) / (cR2 + xi));
   }
-  const double rden = 1.0 / (epss0 - epsr);
+  const double rden = chain_reciprocal(epss0 - epsr);
   const double epsrat = (eps - epsr) * rden;
   // |e*|^R and 1 / (1 + |e*|^R)^(1/R) through logs and exps.  Where a
   // single-precision estimate puts |e*|^R below 2^-60 (R log2|e*| < -60 with
@@ -147,9 +150,9 @@ __device__ void steel02_trial(const double *q, const double *hc, double trialStr
   if (!((float)R * __log2f(fmaxf((float)ae, 1.17549435e-38f)) < -60.0f)) {
     const double pr = ae > 0.0 ? exp(R * log(ae)) : 0.0;
     const double dum1 = 1.0 + pr;
-    const double rdum2 = exp(-log(dum1) / R);
+    const double rdum2 = exp(-log(dum1) * chain_reciprocal(R));
     se *= rdum2;
-    te = te * rdum2 / dum1;
+    te = te * rdum2 * chain_reciprocal(dum1);
   }
   const double dsig = sigs0 - sigr;
   double sig = b * epsrat + se;

@@ -833,9 +833,28 @@ __global__ void k_gather_chunks(GatherMap g, const Idx *__restrict__ src,
   else partial[c] = s;
 }
 
-// Thread per run: the run's slots summed in contribution order (the element
+// One run of L slots: its slots summed in contribution order (the element
 // order, as the chunks sum), each contribution's values read as one
 // contiguous piece.
+template <int L>
+__device__ __forceinline__ void gather_run(const int *src, int n, const double *scratch,
+                                           double *out) {
+  double acc[L];
+#pragma unroll
+  for (int t = 0; t < L; t++) acc[t] = 0.0;
+  for (int q = 0; q < n; q++) {
+    const double *p = scratch + (unsigned)src[q];
+#pragma unroll
+    for (int t = 0; t < L; t++) acc[t] += p[t];
+  }
+#pragma unroll
+  for (int t = 0; t < L; t++) out[t] = acc[t];
+}
+
+// Thread per run.  The runs are ordered by length and contribution count, so
+// a warp's threads take the same branch and loop as often: the FP64 adds,
+// which hold the FP64 pipe per warp instruction whatever its active lanes,
+// are then issued once per useful add.
 __global__ void k_gather_runs(GatherMap g, const double *__restrict__ scratch,
                               double *__restrict__ out) {
   const int r = blockIdx.x * blockDim.x + threadIdx.x;
@@ -843,18 +862,14 @@ __global__ void k_gather_runs(GatherMap g, const double *__restrict__ scratch,
   const int s0 = g.run_slot[r], meta = g.run_meta[r];
   const int len = meta & 15, n = meta >> 4;
   const int *src = g.run_src + g.run_begin[r];
-  double acc[kRunMaxLen];
-#pragma unroll
-  for (int t = 0; t < kRunMaxLen; t++) acc[t] = 0.0;
-  for (int q = 0; q < n; q++) {
-    const double *p = scratch + (unsigned)src[q];
-#pragma unroll
-    for (int t = 0; t < kRunMaxLen; t++)
-      if (t < len) acc[t] += p[t];
+  switch (len) {
+    case 1: gather_run<1>(src, n, scratch, out + s0); break;
+    case 2: gather_run<2>(src, n, scratch, out + s0); break;
+    case 3: gather_run<3>(src, n, scratch, out + s0); break;
+    case 4: gather_run<4>(src, n, scratch, out + s0); break;
+    case 5: gather_run<5>(src, n, scratch, out + s0); break;
+    default: gather_run<6>(src, n, scratch, out + s0); break;
   }
-#pragma unroll
-  for (int t = 0; t < kRunMaxLen; t++)
-    if (t < len) out[s0 + t] = acc[t];
 }
 
 // The chunk and slot kernels over a list of chunks / slots (the long slots
@@ -874,16 +889,20 @@ __global__ void k_gather_chunk_list(GatherMap g, const Idx *__restrict__ src,
   else partial[c] = s;
 }
 
+// Warp per long slot: its chunk partials lane-strided in chunk order, then a
+// fixed butterfly (the multi-point constraint's retained slots have
+// thousands of chunks).
 __global__ void k_gather_slot_list(GatherMap g, const double *__restrict__ partial,
                                    double *__restrict__ out) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= g.nlong_slots) return;
-  const int s = g.long_slots[i];
+  const int w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+  if (w >= g.nlong_slots) return;
+  const int s = g.long_slots[w];
   const int c0 = g.slot_chunk[s], c1 = g.slot_chunk[s + 1];
   if (c1 - c0 == 1) return;               // written by its chunk
   double v = 0.0;
-  for (int c = c0; c < c1; c++) v += partial[c];
-  out[s] = v;
+  for (int c = c0 + lane; c < c1; c += 32) v += partial[c];
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  if (lane == 0) out[s] = v;
 }
 
 __global__ void k_gather_slots(GatherMap g, const double *__restrict__ partial,
@@ -1056,7 +1075,7 @@ int launch_gather(const GatherMap &g, const double *scratch, double *partial, do
       k_gather_chunk_list<int><<<nblocks(g.nlong_chunks), kThreads, 0, s>>>(g, g.src32, scratch,
                                                                              partial, out);
     if (g.nlong_slots)
-      k_gather_slot_list<<<nblocks(g.nlong_slots), kThreads, 0, s>>>(g, partial, out);
+      k_gather_slot_list<<<nblocks(32L * g.nlong_slots), kThreads, 0, s>>>(g, partial, out);
     return check_launch();
   }
   if (g.src32)

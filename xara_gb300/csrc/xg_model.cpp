@@ -152,6 +152,23 @@ void build_gather(int nslots, const std::vector<int> &slot_of, const std::vector
     for (int64_t q = 0; q < n; q++) g.run_src.push_back((int)g.src[b + q]);
     s0 += len;
   }
+  // runs ordered by (length, contributions, first slot): a warp's threads
+  // then run the same loop
+  std::vector<int> ord(g.run_slot.size());
+  for (size_t i = 0; i < ord.size(); i++) ord[i] = (int)i;
+  std::stable_sort(ord.begin(), ord.end(), [&](int x, int y) {
+    const int mx = g.run_meta[x], my = g.run_meta[y];
+    return (mx & 15) != (my & 15) ? (mx & 15) < (my & 15) : (mx >> 4) < (my >> 4);
+  });
+  std::vector<int> rs(ord.size()), rm(ord.size()), rb(ord.size());
+  for (size_t i = 0; i < ord.size(); i++) {
+    rs[i] = g.run_slot[ord[i]];
+    rm[i] = g.run_meta[ord[i]];
+    rb[i] = g.run_begin[ord[i]];
+  }
+  g.run_slot.swap(rs);
+  g.run_meta.swap(rm);
+  g.run_begin.swap(rb);
 }
 
 }  // namespace
