@@ -842,7 +842,25 @@ __device__ __forceinline__ void gather_run(const int *src, int n, const double *
   double acc[L];
 #pragma unroll
   for (int t = 0; t < L; t++) acc[t] = 0.0;
-  for (int q = 0; q < n; q++) {
+  int q = 0;
+  // four contributions' loads in flight, added in their order
+  for (; q + 4 <= n; q += 4) {
+    const unsigned a0 = (unsigned)src[q], a1 = (unsigned)src[q + 1];
+    const unsigned a2 = (unsigned)src[q + 2], a3 = (unsigned)src[q + 3];
+    double v[4][L];
+#pragma unroll
+    for (int t = 0; t < L; t++) {
+      v[0][t] = scratch[a0 + t];
+      v[1][t] = scratch[a1 + t];
+      v[2][t] = scratch[a2 + t];
+      v[3][t] = scratch[a3 + t];
+    }
+#pragma unroll
+    for (int u = 0; u < 4; u++)
+#pragma unroll
+      for (int t = 0; t < L; t++) acc[t] += v[u][t];
+  }
+  for (; q < n; q++) {
     const double *p = scratch + (unsigned)src[q];
 #pragma unroll
     for (int t = 0; t < L; t++) acc[t] += p[t];
