@@ -84,6 +84,44 @@ def test_displacement_history(gpu_mod, name, system):
     assert np.mean(iters == fx["step_iters"]) >= 0.8, (iters, fx["step_iters"])
 
 
+@pytest.mark.parametrize("name,kb", [("brick_8x8x4", 3), ("quad_64x16", 2),
+                                     ("frame3d_2x1x3", 6)])
+def test_pcg_node_block_layout(gpu_mod, name, kb):
+    """After a PCG solve the tangent's node-block copy has the block order of
+    the model's nodes and one block per coupled node pair of the pattern
+    (node rows coupled to more than 96 nodes left to the CSR chunks)."""
+    fx = load(name)
+    desc, phases = model_of(fx)
+    with gpu_mod.DeviceModel(desc) as m:
+        assert gpu_mod.pcg_layout(m)[0] == 0
+        m.set_system(gpu_mod.XG_SYSTEM_BJPCG)
+        m.set_phase(phases[0])
+        m.analyze(1)
+        order, blocks, chunked = gpu_mod.pcg_layout(m)
+        rp, ci = m.pattern()
+        eqn = np.asarray(m.numbering()).reshape(-1, desc.ndf)
+    assert order == kb
+    # the node owning each equation: its free dofs, not the equalDOF-tied
+    # ones (those carry the retained node's equation)
+    tags = list(np.asarray(desc.node_tag))
+    tied = set()
+    if desc.arrays.get("mp_constrained") is not None:
+        for t, d in zip(desc.arrays["mp_constrained"], desc.arrays["mp_dof"]):
+            tied.add((tags.index(int(t)), int(d)))
+    node_of = np.full(len(rp) - 1, -1)
+    for n, row in enumerate(eqn):
+        for d, r in enumerate(row):
+            if r >= 0 and (n, d) not in tied:
+                node_of[r] = n
+    assert (node_of >= 0).all()
+    pairs = {}
+    for r in range(len(rp) - 1):
+        pairs.setdefault(node_of[r], set()).update(node_of[ci[rp[r]:rp[r + 1]]].tolist())
+    want = sum(len(v) for v in pairs.values() if len(v) <= 96)
+    long_rows = sum(int(np.sum(node_of == n)) for n, v in pairs.items() if len(v) > 96)
+    assert blocks == want and chunked == long_rows
+
+
 def test_assembly_is_deterministic(gpu_mod):
     fx = load("brick_4x3x2")
     desc, _ = model_of(fx)

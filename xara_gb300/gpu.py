@@ -316,6 +316,18 @@ def autotune_result(model):
     return a.value, b.value, c.value
 
 
+def pcg_layout(model):
+    """(block order, node-pair blocks, rows left to CSR chunks) of the PCG's
+    node-block copy of the tangent; block order 0 before the first PCG solve
+    or when no copy was built."""
+    L = lib()
+    L.xg_model_pcg_layout.argtypes = [C.c_void_p, C.POINTER(C.c_int),
+                                      C.POINTER(C.c_longlong), C.POINTER(C.c_longlong)]
+    kb, nb, nc = C.c_int(), C.c_longlong(), C.c_longlong()
+    _check(L.xg_model_pcg_layout(model.h, C.byref(kb), C.byref(nb), C.byref(nc)))
+    return kb.value, nb.value, nc.value
+
+
 def model_stream(model):
     """The model's CUDA stream as an integer handle (cudaStream_t)."""
     L = lib()
