@@ -440,14 +440,10 @@ __device__ __forceinline__ void fbc_section(const FrameView &v, int f0, int nf, 
   double k0 = 0, k1 = 0, k2 = 0, k5 = 0, k6 = 0, k10 = 0, s0 = 0, s1 = 0, s2 = 0;
   for (int fi = lane; fi < nf; fi += 32) {
     const int kf = f0 + fi;
-    const double y = v.fy[kf] - ybar, A = v.fA[kf];
+    const double y = v.fyc[kf];
     const int u = v.fmat[kf];
     double strain = vsec[0] - y * vsec[1];
-    double z = 0.0;
-    if (ORD == 4) {
-      z = v.fz[kf] - zbar;
-      strain += z * vsec[2];
-    }
+    if (ORD == 4) strain += v.fzc[kf] * vsec[2];
     // material state from the committed record and the trial strain; only
     // the fields a law reads are loaded and only those it sets are stored
     const double *hc = v.fh_c + rec0 + 12L * fi;
@@ -492,17 +488,22 @@ __device__ __forceinline__ void fbc_section(const FrameView &v, int f0, int nf, 
       tangent = q[0];
       ht[8] = tangent; ht[9] = stress; ht[10] = strain;
     }
-    if (ORD == 2) {
-      const double ks0 = tangent * A, ks1 = ks0 * -y;
-      k0 += ks0; k1 += ks1; k5 += ks1 * -y;
-      const double fs0v = stress * A;
-      s0 += fs0v; s1 += fs0v * -y;
-    } else {
-      const double EA = tangent * A;
-      k0 += EA; k1 += -y * EA; k2 += z * EA;
-      k5 += y * y * EA; k10 += z * z * EA; k6 += -y * z * EA;
-      const double fsv = stress * A;
-      s0 += fsv; s1 += -y * fsv; s2 += z * fsv;
+    // sums of E A (1, -y, z, y^2, z^2, -y z) and of s A (1, -y, z) with
+    // the products per fiber formed once (FrameView::fk): one FMA a term
+    const long nfk = v.nfib;
+    const double fA = v.fk[kf], fmy = v.fk[nfk + kf], fy2 = v.fk[3 * nfk + kf];
+    k0 = fma(tangent, fA, k0);
+    k1 = fma(tangent, fmy, k1);
+    k5 = fma(tangent, fy2, k5);
+    s0 = fma(stress, fA, s0);
+    s1 = fma(stress, fmy, s1);
+    if (ORD == 4) {
+      const double fz1 = v.fk[2 * nfk + kf], fz2 = v.fk[4 * nfk + kf];
+      const double fyz = v.fk[5 * nfk + kf];
+      k2 = fma(tangent, fz1, k2);
+      k10 = fma(tangent, fz2, k10);
+      k6 = fma(tangent, fyz, k6);
+      s2 = fma(stress, fz1, s2);
     }
   }
   k0 = warp_sum(k0); k1 = warp_sum(k1); k5 = warp_sum(k5);
@@ -542,14 +543,10 @@ __device__ __forceinline__ void fbc_section_group(const FrameView &v, int f0, in
   double k0 = 0, k1 = 0, k2 = 0, k5 = 0, k6 = 0, k10 = 0, s0 = 0, s1 = 0, s2 = 0;
   for (int fi = rank; on && fi < nf; fi += G) {
     const int kf = f0 + fi;
-    const double y = v.fy[kf] - ybar, A = v.fA[kf];
+    const double y = v.fyc[kf];
     const int u = v.fmat[kf];
     double strain = vsec[0] - y * vsec[1];
-    double z = 0.0;
-    if (ORD == 4) {
-      z = v.fz[kf] - zbar;
-      strain += z * vsec[2];
-    }
+    if (ORD == 4) strain += v.fzc[kf] * vsec[2];
     const double *hc = v.fh_c + rec0 + 12L * fi;
     double *ht = v.fh_t + rec0 + 12L * fi;
     const double *q = v.uparam + (long)u * XG_UNI_NPARAM;
@@ -592,17 +589,22 @@ __device__ __forceinline__ void fbc_section_group(const FrameView &v, int f0, in
       tangent = q[0];
       ht[8] = tangent; ht[9] = stress; ht[10] = strain;
     }
-    if (ORD == 2) {
-      const double ks0 = tangent * A, ks1 = ks0 * -y;
-      k0 += ks0; k1 += ks1; k5 += ks1 * -y;
-      const double fs0v = stress * A;
-      s0 += fs0v; s1 += fs0v * -y;
-    } else {
-      const double EA = tangent * A;
-      k0 += EA; k1 += -y * EA; k2 += z * EA;
-      k5 += y * y * EA; k10 += z * z * EA; k6 += -y * z * EA;
-      const double fsv = stress * A;
-      s0 += fsv; s1 += -y * fsv; s2 += z * fsv;
+    // sums of E A (1, -y, z, y^2, z^2, -y z) and of s A (1, -y, z) with
+    // the products per fiber formed once (FrameView::fk): one FMA a term
+    const long nfk = v.nfib;
+    const double fA = v.fk[kf], fmy = v.fk[nfk + kf], fy2 = v.fk[3 * nfk + kf];
+    k0 = fma(tangent, fA, k0);
+    k1 = fma(tangent, fmy, k1);
+    k5 = fma(tangent, fy2, k5);
+    s0 = fma(stress, fA, s0);
+    s1 = fma(stress, fmy, s1);
+    if (ORD == 4) {
+      const double fz1 = v.fk[2 * nfk + kf], fz2 = v.fk[4 * nfk + kf];
+      const double fyz = v.fk[5 * nfk + kf];
+      k2 = fma(tangent, fz1, k2);
+      k10 = fma(tangent, fz2, k10);
+      k6 = fma(tangent, fyz, k6);
+      s2 = fma(stress, fz1, s2);
     }
   }
   k0 = group_sum(k0, rank, G, P2); k1 = group_sum(k1, rank, G, P2);

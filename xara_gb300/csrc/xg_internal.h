@@ -288,6 +288,10 @@ struct FrameView {
   const int *sec;             // [ne] section row
   const int *sec_fstart;      // [nsec+1]
   const double *fy, *fz, *fA; // fiber geometry per section
+  // per fiber: coordinates about the section centroid and the products of
+  // the section sums, [6][nfib]: A, -y A, z A, y^2 A, z^2 A, -y z A
+  const double *fyc, *fzc, *fk;
+  int nfib;
   const int *fmat;            // fiber uniaxial row
   const double *ybar, *zbar, *GJ;   // [nsec]
   const double *fs0;          // [nsec*16] initial section flexibility

@@ -442,6 +442,7 @@ struct xg_model {
   DBuf<int> d_fconn, d_fsec, d_sec_fstart, d_fmat, d_utype;
   DBuf<long> d_foff;
   DBuf<double> d_fL, d_fR, d_fy, d_fz, d_fA, d_ybar, d_zbar, d_GJ, d_fs0, d_uparam;
+  DBuf<double> d_fyc, d_fzc, d_fk;   // centred fiber coordinates, section-sum products
   DBuf<double> d_fh_c, d_fh_t, d_st, d_st_c;
   DBuf<unsigned long long> d_work;        // frame work counters
   long long point_updates = 0, elem_updates = 0;   // continuum work counters
@@ -453,6 +454,7 @@ struct xg_model {
     v.ne = ne; v.nb = fb_nb; v.nip = fb_nip; v.ndf = ndf;
     v.U = d_U.p; v.conn = d_fconn.p; v.L = d_fL.p; v.R = d_fR.p; v.sec = d_fsec.p;
     v.sec_fstart = d_sec_fstart.p; v.fy = d_fy.p; v.fz = d_fz.p; v.fA = d_fA.p;
+    v.fyc = d_fyc.p; v.fzc = d_fzc.p; v.fk = d_fk.p; v.nfib = (int)fy.size();
     v.fmat = d_fmat.p; v.ybar = d_ybar.p; v.zbar = d_zbar.p; v.GJ = d_GJ.p; v.fs0 = d_fs0.p;
     v.utype = d_utype.p; v.uparam = d_uparam.p; v.foff = d_foff.p; v.fh_c = d_fh_c.p;
     v.fh_t = d_fh_t.p; v.st = d_st.p; v.max_iters = fb_max_iters; v.tol = fb_tol;
@@ -1026,6 +1028,27 @@ int xg_model::upload_frames() {
   RET(d_fmat.upload(fmat.data(), fmat.size(), s));
   RET(d_ybar.upload(ybar.data(), ybar.size(), s));
   RET(d_zbar.upload(zbar.data(), zbar.size(), s));
+  {
+    // the fibers' centred coordinates and the products the section sums
+    // take (the tangent and the stress times each of them)
+    const size_t nf = fy.size();
+    std::vector<double> yc(nf), zc(nf), fk(6 * nf);
+    for (int sc = 0; sc < nsec; sc++)
+      for (int f = sec_fstart[sc]; f < sec_fstart[sc + 1]; f++) {
+        const double y = fy[f] - ybar[sc], z = fz[f] - zbar[sc], A = fA[f];
+        yc[f] = y;
+        zc[f] = z;
+        fk[f] = A;
+        fk[nf + f] = -y * A;
+        fk[2 * nf + f] = z * A;
+        fk[3 * nf + f] = y * y * A;
+        fk[4 * nf + f] = z * z * A;
+        fk[5 * nf + f] = -y * z * A;
+      }
+    RET(d_fyc.upload(yc.data(), nf, s));
+    RET(d_fzc.upload(zc.data(), nf, s));
+    RET(d_fk.upload(fk.data(), fk.size(), s));
+  }
   RET(d_GJ.upload(GJ.data(), GJ.size(), s));
   RET(d_fs0.upload(fs0.data(), fs0.size(), s));
   RET(d_utype.upload(utype.data(), utype.size(), s));

@@ -14,8 +14,8 @@
 //   B  every tile below it becomes W_IJ = A_IJ L_JJ^-T (kept in a scratch
 //      slot) and L_IJ = W_IJ D^-1 (stored in place);
 //   C  every trailing tile pair loses W_IJ L_KJ' (one 32^3 product each).
-// The tasks (A: diagonal, B: panel tile in eight row parts, C: tile pair of
-// one column; for tile (J+1, J) the eight panel parts also apply an eighth
+// The tasks (A: diagonal, B: panel tile in four row parts, C: tile pair of
+// one column; for tile (J+1, J) the four panel parts also apply a quarter
 // each of the pair (J+1, J+1)'s update, and the chain task of column J
 // factors diagonal tile J+1 -- the critical path of the factorisation) run as a dataflow: one persistent launch whose blocks take
 // tasks from a list in a fixed order -- for column J: A(J) when no column
@@ -216,14 +216,11 @@ __device__ bool factor_diag(const ProfileSystem &S, int J, double (*sA)[kT + 1],
   return factor_tile(S, J, sA, flags);
 }
 
-// Phase B on rows 4q..4q+3 of tile (I = J+o, J): W = A L_JJ^-T, L = W
-// D^-1 (rows are independent, so a tile is eight tasks).  A warp per row: once
+// Phase B on rows 8q..8q+7 of tile (I = J+o, J): W = A L_JJ^-T, L = W
+// D^-1 (rows are independent, so a tile is four tasks).  A warp per row: once
 // column c of W is final (broadcast by shuffle), every later column s loses
-// W(r, c) l_sc -- no block barriers inside the sweep.  Four rows a task put
-// one row's warp on each sub-partition: a warp-wide FP64 FMA holds its
-// sub-partition's pipe for many cycles, and two row sweeps sharing a pipe
-// took half as long again.
-constexpr int kPanelRows = 4;
+// W(r, c) l_sc -- no block barriers inside the sweep.
+constexpr int kPanelRows = 8;
 constexpr int kPanelParts = kT / kPanelRows;
 
 __device__ void panel_solve(const ProfileSystem &S, int J, int o, int q, double (*sA)[kT + 1],
@@ -248,9 +245,9 @@ __device__ void panel_solve(const ProfileSystem &S, int J, int o, int q, double 
   __syncthreads();
 }
 
-// The panel of tile (J+1, J) in eight row parts whose tasks, once all eight
-// are written, apply an eighth each of that panel's update of diagonal tile
-// J+1 (phase C for the pair (J+1, J+1), 66 of its 528 lower entries), so
+// The panel of tile (J+1, J) in four row parts whose tasks, once all four
+// are written, apply a quarter each of that panel's update of diagonal tile
+// J+1 (phase C for the pair (J+1, J+1), 132 of its 528 lower entries), so
 // the chain task only factors.  The wait for the sibling parts is bounded;
 // they sit right after this task in the list, so the blocks that take them
 // never wait on this one.
@@ -278,7 +275,7 @@ __device__ bool panel_update_task(const ProfileSystem &S, int J, int q, double (
     sA[k >> 5][k & 31] = l * __ldcg(piv + (k & 31));
   }
   __syncthreads();
-  constexpr int kQuarter = kT * (kT + 1) / 2 / kPanelParts;   // 66
+  constexpr int kQuarter = kT * (kT + 1) / 2 / kPanelParts;   // 132
   for (int k = q * kQuarter + tid; k < (q + 1) * kQuarter; k += blockDim.x) {
     const int rs = kLowerRS[k], r = rs >> 5, sc = rs & 31;
     double a0 = 0.0, a1 = 0.0, a2 = 0.0, a3 = 0.0;
@@ -442,8 +439,8 @@ __device__ __forceinline__ int slot_of(const ProfileSystem &S, int I, int o) {
   return I * (S.W + 1) + o;
 }
 
-// Column J's critical chain: once the eight panel-part tasks of tile
-// (J+1, J) have applied their eighths of its update of diagonal tile J+1,
+// Column J's critical chain: once the four panel-part tasks of tile
+// (J+1, J) have applied their quarters of its update of diagonal tile J+1,
 // that tile's LDL' in shared memory.
 __device__ bool chain_task(const ProfileSystem &S, int J, double (*sC)[kT + 1],
                            volatile int *flags) {
