@@ -494,11 +494,8 @@ int xg_uniaxial_vjp(int type, const double *q, const double *hc, double strain,
    using the library holds until the process exits; a system needing more
    than 36*nblk + 4*n + 3*(cooperative blocks) + 24 doubles of it (about
    260,000 equations with 3x3 node blocks, 100,000 with 1x1 blocks) is
-   rejected with XG_EINVAL.  The first call on a device looks up the array's
-   device address and keeps it for the life of the process; make that first
-   call before any stream capture.  cudaDeviceReset ends the context that
-   address belongs to: do not call this entry point on a device after
-   resetting it.  The call waits on its stream before it returns.  All
+   rejected with XG_EINVAL.  Every call looks up the array's device address
+   in the current context.  The call waits on its stream before it returns.  All
    calls share the one array: calls that overlap on the GPU race and must be
    serialised by the caller.  Allocates no device memory. ---- */
 #define XG_NOALLOC_MAX_DOUBLES 4194304

@@ -13,11 +13,8 @@
 // doubles (32 MiB): every GPU that loads this library holds it until the
 // process exits.  In host code the array's name is only a host-side
 // stand-in, never a device address, so its device address is looked up with
-// cudaGetSymbolAddress once per device, with that device current, on the
-// first call made on the device; make that first call before any stream
-// capture.  The address is kept for the life of the process, so the entry
-// point must not be called on a device after cudaDeviceReset (the reset ends
-// the context the address belongs to).  All calls share the array and find the previous call's contents
+// cudaGetSymbolAddress, in the current device's context, on every call.  All
+// calls share the array and find the previous call's contents
 // in it: the solver clears what must start at zero (the grid-barrier counter
 // and the status words) and overwrites the rest before reading it.  Calls
 // that overlap on the GPU (two streams, two host threads, two devices'
@@ -26,7 +23,6 @@
 #include <cuda_runtime.h>
 
 #include <cstdio>
-#include <mutex>
 
 #include "xg_internal.h"
 
@@ -34,34 +30,22 @@ namespace {
 
 __device__ __align__(256) double g_noalloc_scratch[XG_NOALLOC_MAX_DOUBLES];
 
-constexpr int kMaxDevices = 64;
-double *g_scratch_ptr[kMaxDevices] = {nullptr};
-std::mutex g_scratch_mu;
-
 int noalloc_fail(int code, const char *msg) {
   xg::record_error(msg);   // readable through xg_last_error()
   return code;
 }
 
-// Device address of the scratch array for the current device (looked up on
-// the first call on each device).
+// Device address of the scratch array in the current device's context,
+// looked up on every call (a cheap driver query), so that a context
+// created again -- after cudaDeviceReset, say -- gets its own address.
 double *scratch_for_current_device(int *err) {
-  int dev = -1;
-  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices) {
+  void *p = nullptr;
+  if (cudaGetSymbolAddress(&p, g_noalloc_scratch) != cudaSuccess || p == nullptr) {
     *err = XG_ECUDA;
     return nullptr;
   }
-  std::lock_guard<std::mutex> lock(g_scratch_mu);
-  if (g_scratch_ptr[dev] == nullptr) {
-    void *p = nullptr;
-    if (cudaGetSymbolAddress(&p, g_noalloc_scratch) != cudaSuccess || p == nullptr) {
-      *err = XG_ECUDA;
-      return nullptr;
-    }
-    g_scratch_ptr[dev] = static_cast<double *>(p);
-  }
   *err = 0;
-  return g_scratch_ptr[dev];
+  return static_cast<double *>(p);
 }
 
 // Checks a caller-given block partition: starts at 0, ends at n, every block
