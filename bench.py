@@ -1319,6 +1319,9 @@ def run_brick(args):
                   "pcg_block_order": kb.value, "pcg_blocks": nblocks.value,
                   "pcg_chunked_rows": nchunked.value,
                   "rhs": "seeded random right-hand side, x0 = 0, rtol 1e-10",
+                  "arithmetic": "vectors, inner products and preconditioner in FP64; the SpMV's "
+                                "products in float-float (2^-46 of each product); the "
+                                "relative residual above is the recurrence's",
                   "ip_updates_per_s": npts / t_it[-1]}
 
     Uh = torch.from_numpy(U).pin_memory()
@@ -1358,7 +1361,11 @@ def run_brick(args):
                                "element phase (one Newton iteration)",
                    "elements": desc.num_elems, "points": npts, "equations": m.neq,
                    "nnz": m.nnz, "parallelism": f"replicas x{world}",
-                   "l2": "inputs larger than L2 (no flush needed)"},
+                   "l2": "inputs larger than L2 (no flush needed)",
+                   "arithmetic": "J2 state, resisting force and assembled values in FP64; the "
+                                 "tangent's node-pair sums in float-float (pairs of floats, "
+                                 "2^-46 of each product), within 1e-12 of each row's largest "
+                                 "entry of the FP64 oracle"},
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(U.nbytes),
                 "d2h_bytes_per_step": int(resid.numel() * 8)},
         "gpu_launches": int(sum(v[1] for v in kernels.values())),
