@@ -173,6 +173,10 @@ struct ProfileSystem {
   // outside the envelope)
   double *Winv, *F, *G, *E, *H, *Q, *R;
   int *cpl;                // [nt] row J's coupling matrices written
+  // right-hand sides whose forward sweep runs inside the factorisation
+  // (fwd_nrhs 0: none), column r at fwd_x[r*fwd_ldx]
+  int fwd_nrhs, fwd_ldx;
+  const double *fwd_x;
 };
 int profile_plan(int n, const int *rowptr, const int *colidx, std::vector<int> &ftile, int &nt,
                  int &W);
@@ -184,7 +188,13 @@ int profile_tile_edge();
 int profile_factor(const ProfileSystem &S, cudaStream_t s, int *bad_eq);
 // Solve in place: x[r*ldx + i] holds right-hand side r on entry (ldx >=
 // nt*32, entries past n zero), the solution on return; nrhs <= 4.
-int profile_solve(const ProfileSystem &S, int nrhs, double *x, int ldx, cudaStream_t s);
+// backward_only: the factorisation ran the forward sweep of these
+// right-hand sides (ProfileSystem::fwd_nrhs, the pipelined path only).
+int profile_solve(const ProfileSystem &S, int nrhs, double *x, int ldx, cudaStream_t s,
+                  bool backward_only = false);
+// Whether the substitutions of this system run pipelined over co-resident
+// blocks (the path whose forward sweep the factorisation can carry).
+bool profile_pipelined(const ProfileSystem &S);
 
 // The tiled envelope LDL' with its device buffers: planned once per pattern,
 // factored once per tangent, then up to four right-hand sides per solve.
@@ -211,6 +221,13 @@ class ProfileSolver {
   // x[r] = A^-1 b[r] for r < nrhs (1..4; device vectors of n entries) with
   // the last factorisation.
   int solve(int nrhs, const double *const *b, double *const *x, cudaStream_t s);
+  // Factor with the forward sweep of b[0..nrhs) running as tasks of the
+  // factorisation (right behind its front); solve_backward then finishes
+  // x[r] = A^-1 b[r].  Only for systems whose substitutions are pipelined
+  // (can_fuse()).
+  bool can_fuse() const { return ready_ && profile_pipelined(S_); }
+  int factor_forward(int nrhs, const double *const *b, cudaStream_t s, int *bad_eq);
+  int solve_backward(int nrhs, double *const *x, cudaStream_t s);
   const ProfileSystem &system() const { return S_; }
 
  private:
@@ -221,6 +238,7 @@ class ProfileSolver {
     ~Buf();
   };
   ProfileSystem S_{};
+  int fwd_nrhs_ = 0;         // right-hand sides factor_forward swept
   bool ready_ = false;
   int ldx_ = 0;
   Buf<int> ftile_, flags_, tasks_, next_, upd_, done_, cpl_;

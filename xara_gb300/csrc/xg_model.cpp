@@ -1497,6 +1497,25 @@ int xg_model::solve_profile(int nrhs, const double *const *b, double *const *x) 
     prof_flush();
     return 0;
   }
+  if (!prof_factored && envelope.can_fuse()) {
+    // the tangent is new and its right-hand sides are known: the forward
+    // sweep runs inside the factorisation, then the backward sweep
+    prof_begin(P_LDL_FACTOR);
+    int bad = -1;
+    const int r = envelope.factor_forward(nrhs, b, stream, &bad);
+    prof_end(P_LDL_FACTOR, 2);
+    if (r) {
+      if (bad >= 0) return fail(XG_ESOLVE, "ProfileSPD: pivot %d fails the check (aii == 0, "
+                                "|aii| <= 1e-12, or a first pivot <= 0)", bad);
+      return fail(XG_ESOLVE, "ProfileSPD: factorisation barrier timed out");
+    }
+    prof_factored = true;
+    prof_begin(P_LDL_SOLVE);
+    RET(envelope.solve_backward(nrhs, x, stream));
+    prof_end(P_LDL_SOLVE, 1);
+    prof_flush();
+    return 0;
+  }
   if (!prof_factored) {
     prof_begin(P_LDL_FACTOR);
     int bad = -1;

@@ -488,12 +488,157 @@ __device__ bool wait_task(const ProfileSystem &S, int4 t, volatile int *flags) {
     }
     return true;
   }
+  if (type == 7) {
+    // row J's forward step: its coupling matrices and the panel tiles of
+    // the row further left (the y values of the rows before it are polled
+    // inside the step)
+    if (S.fwd_nrhs == 0) return true;
+    if (!wait_geq(S.cpl + J, 1, flags)) return false;
+    const int ohi = min(S.W, J - S.ftile[J]);
+    for (int o = 3; o <= ohi; o++)
+      if (!wait_geq(S.done + slot_of(S, J, o), kPanelParts, flags)) return false;
+    return true;
+  }
   if (type == 1)
     return wait_geq(S.done + slot_of(S, J, 0), 1, flags) &&
            wait_geq(S.upd + slot_of(S, I, I - J), J - max(S.ftile[I], S.ftile[J]), flags);
   return wait_geq(S.done + slot_of(S, I, I - J), kPanelParts, flags) &&
          wait_geq(S.done + slot_of(S, K, K - J), kPanelParts, flags) &&
          wait_geq(S.upd + slot_of(S, I, I - K), J - max(S.ftile[I], S.ftile[K]), flags);
+}
+
+// Pipelined substitutions on kPipeBlocks co-resident blocks (cooperative
+// launch): block b owns the tile rows J = b, b + P, ... .  Forward, in
+// increasing J: c3_J = L_JJ^-1 (b_J minus the contributions of rows J-3 and
+// older), then with the factorisation's coupling matrices
+//   y_J = c3_J - F_J c_J-1 - Q_J y_J-2,   c_J = c3_J - E_J y_J-2,
+// so a row waits for the row two back (and for c_J-1, which its owner
+// publishes as soon as y_J-3 is known): the two interleaved chains halve
+// the serial length.  Backward, in decreasing J, the same with
+// c3'_J = L_JJ^-T (D_J^-1 y_J minus the transposed contributions of rows J+3
+// and beyond):  x_J = c3'_J - G_J c'_J+1 - R_J x_J+2,  c'_J = c3'_J -
+// H_J x_J+2.  There are no row flags: every solved value is published to a
+// scratch vector filled with kUnset beforehand (a NaN pattern that no
+// arithmetic result is stored as), and a consumer thread polls exactly the
+// values it reads.  Waits are bounded by the global timer.
+constexpr int kPipeBlocks = 64;
+constexpr int kPipeThreads = 256;
+constexpr unsigned long long kUnset = 0xFFFFFFFFFFFFFFFFull;   // byte fill 0xFF
+
+__device__ __forceinline__ double ld_relaxed(const double *p) {
+  double v;
+  asm volatile("ld.relaxed.gpu.global.f64 %0, [%1];" : "=d"(v) : "l"(p));
+  return v;
+}
+
+// *p once its producer has published it; 0 after a failed wait (flags[0]
+// is then nonzero and the host reports the solve as failed)
+__device__ __forceinline__ double await_value(const double *p, volatile int *flags) {
+  double v = ld_relaxed(p);
+  if ((unsigned long long)__double_as_longlong(v) != kUnset) return v;
+  const unsigned long long t0 = global_ns();
+  for (;;) {
+    v = ld_relaxed(p);
+    if ((unsigned long long)__double_as_longlong(v) != kUnset) return v;
+    if (flags[0] != 0) return 0.0;
+    if (global_ns() - t0 > kBarrierTimeoutNs) {
+      flags[0] = 2;
+      return 0.0;
+    }
+  }
+}
+
+// p[0], p[8], p[16], p[24] (the four loads in flight together)
+__device__ __forceinline__ void await4(const double *p, double v[4], volatile int *flags) {
+  bool ready = true;
+#pragma unroll
+  for (int m = 0; m < 4; m++) v[m] = ld_relaxed(p + 8 * m);
+#pragma unroll
+  for (int m = 0; m < 4; m++) ready &= (unsigned long long)__double_as_longlong(v[m]) != kUnset;
+  if (!ready)
+    for (int m = 0; m < 4; m++) v[m] = await_value(p + 8 * m, flags);
+}
+
+__device__ __forceinline__ void publish(double *p, double v) {
+  if ((unsigned long long)__double_as_longlong(v) == kUnset)
+    v = __longlong_as_double(0x7FF8000000000000ll);   // keep a NaN a NaN
+  asm volatile("st.relaxed.gpu.global.f64 [%0], %1;" ::"l"(p), "d"(v) : "memory");
+}
+
+// Forward substitution of tile row J for the right-hand sides given to the
+// factorisation (S.fwd_nrhs > 0), as a task of the factorisation itself:
+// the right-hand sides are known before the tangent is factored (the
+// unbalance and the reference load of a Newton iteration), so row J's step
+// runs as soon as its coupling matrices are written, a few columns behind
+// the factorisation's front, instead of after it.  The step is the pipelined
+// sweep's (k_prof_solve_pipe) for one row: c3_J = L_JJ^-1 (b_J minus rows
+// J-3 and older), y_J = c3_J - F_J c_J-1 - Q_J y_J-2, c_J = c3_J - E_J
+// y_J-2, published to the sweep's scratch (y, c) for the rows after it and
+// for the backward sweep.
+__device__ bool forward_row(const ProfileSystem &S, int J, double (*rb)[kT],
+                            volatile int *flags) {
+  const int tid = threadIdx.x;
+  const int r = tid >> 3, g = tid & 7;
+  const int nrhs = S.fwd_nrhs, ls = S.nt * kT;
+  double *ys = S.sweep, *cs = ys + (size_t)nrhs * ls;
+  auto group_sum = [](double v) {
+    v += __shfl_xor_sync(0xffffffffu, v, 4);
+    v += __shfl_xor_sync(0xffffffffu, v, 2);
+    v += __shfl_xor_sync(0xffffffffu, v, 1);
+    return v;
+  };
+  auto row_of = [&](const double *M, double (&mv)[4]) {
+#pragma unroll
+    for (int m = 0; m < 4; m++) mv[m] = __ldcg(M + r * kT + g + 8 * m);
+  };
+  auto row_times = [&](const double (&mv)[4], const double *p) {
+    double v[4];
+    await4(p + g, v, flags);
+    double t = 0.0;
+#pragma unroll
+    for (int m = 0; m < 4; m++) t = fma(mv[m], v[m], t);
+    return group_sum(t);
+  };
+  double acc[4] = {0.0, 0.0, 0.0, 0.0};
+  const int ohi = min(S.W, J - S.ftile[J]);
+  for (int o = ohi; o >= 3; o--) {
+    const double *Lt = tile_at(S, J, o) + r * kT + g;
+    const double l0 = __ldcg(Lt), l1 = __ldcg(Lt + 8), l2 = __ldcg(Lt + 16), l3 = __ldcg(Lt + 24);
+    for (int q = 0; q < nrhs; q++) {
+      double y[4];
+      await4(ys + (size_t)q * ls + (J - o) * kT + g, y, flags);
+      acc[q] += l0 * y[0] + l1 * y[1] + l2 * y[2] + l3 * y[3];
+    }
+  }
+  for (int q = 0; q < nrhs; q++) {
+    const double v = group_sum(acc[q]);
+    if (g == 0) rb[q][r] = __ldcg(S.fwd_x + (size_t)q * S.fwd_ldx + J * kT + r) - v;
+  }
+  const double *Wt = S.Winv + (size_t)J * kTT;
+  double wv[4];
+#pragma unroll
+  for (int m = 0; m < 4; m++) wv[m] = __ldcg(Wt + (g + 8 * m) * kT + r);
+  const size_t off = (size_t)J * kTT;
+  double fv[4], qv[4], ev[4];
+  row_of(S.F + off, fv);
+  row_of(S.Q + off, qv);
+  row_of(S.E + off, ev);
+  __syncthreads();
+  const bool hasF = J >= 1 && S.ftile[J] <= J - 1;
+  for (int q = 0; q < nrhs; q++) {
+    double c3 = 0.0;
+#pragma unroll
+    for (int m = 0; m < 4; m++) c3 = fma(wv[m], rb[q][g + 8 * m], c3);
+    c3 = group_sum(c3);
+    const size_t vq = (size_t)q * ls;
+    double t2 = 0.0, t3 = 0.0;
+    if (J >= 2) t3 = row_times(ev, ys + vq + (J - 2) * kT);
+    if (g == 0) publish(cs + vq + J * kT + r, c3 - t3);
+    if (J >= 2) t2 = row_times(qv, ys + vq + (J - 2) * kT);
+    const double t1 = hasF ? row_times(fv, cs + vq + (J - 1) * kT) : 0.0;
+    if (g == 0) publish(ys + vq + J * kT + r, (c3 - t1) - t2);
+  }
+  return flags[0] == 0;
 }
 
 __global__ void __launch_bounds__(kFactorThreads) k_prof_factor(ProfileSystem S) {
@@ -521,6 +666,9 @@ __global__ void __launch_bounds__(kFactorThreads) k_prof_factor(ProfileSystem S)
       fine = chain_task(S, t.w, sC, flags);
     } else if (t.x == 5) {
       fine = panel_update_task(S, t.w, t.z, sA, sB, flags);
+    } else if (t.x == 7) {
+      if (S.fwd_nrhs > 0) fine = forward_row(S, t.w, reinterpret_cast<double (*)[kT]>(&sA[0][0]),
+                                             flags);
     } else {
       coupling_task(S, t.w, sA, sB, sC, flags);
     }
@@ -634,68 +782,11 @@ __global__ void __launch_bounds__(kSolveBlock) k_prof_solve(ProfileSystem S, int
   }
 }
 
-// Pipelined substitutions on kPipeBlocks co-resident blocks (cooperative
-// launch): block b owns the tile rows J = b, b + P, ... .  Forward, in
-// increasing J: c3_J = L_JJ^-1 (b_J minus the contributions of rows J-3 and
-// older), then with the factorisation's coupling matrices
-//   y_J = c3_J - F_J c_J-1 - Q_J y_J-2,   c_J = c3_J - E_J y_J-2,
-// so a row waits for the row two back (and for c_J-1, which its owner
-// publishes as soon as y_J-3 is known): the two interleaved chains halve
-// the serial length.  Backward, in decreasing J, the same with
-// c3'_J = L_JJ^-T (D_J^-1 y_J minus the transposed contributions of rows J+3
-// and beyond):  x_J = c3'_J - G_J c'_J+1 - R_J x_J+2,  c'_J = c3'_J -
-// H_J x_J+2.  There are no row flags: every solved value is published to a
-// scratch vector filled with kUnset beforehand (a NaN pattern that no
-// arithmetic result is stored as), and a consumer thread polls exactly the
-// values it reads.  Waits are bounded by the global timer.
-constexpr int kPipeBlocks = 64;
-constexpr int kPipeThreads = 256;
-constexpr unsigned long long kUnset = 0xFFFFFFFFFFFFFFFFull;   // byte fill 0xFF
-
-__device__ __forceinline__ double ld_relaxed(const double *p) {
-  double v;
-  asm volatile("ld.relaxed.gpu.global.f64 %0, [%1];" : "=d"(v) : "l"(p));
-  return v;
-}
-
-// *p once its producer has published it; 0 after a failed wait (flags[0]
-// is then nonzero and the host reports the solve as failed)
-__device__ __forceinline__ double await_value(const double *p, volatile int *flags) {
-  double v = ld_relaxed(p);
-  if ((unsigned long long)__double_as_longlong(v) != kUnset) return v;
-  const unsigned long long t0 = global_ns();
-  for (;;) {
-    v = ld_relaxed(p);
-    if ((unsigned long long)__double_as_longlong(v) != kUnset) return v;
-    if (flags[0] != 0) return 0.0;
-    if (global_ns() - t0 > kBarrierTimeoutNs) {
-      flags[0] = 2;
-      return 0.0;
-    }
-  }
-}
-
-// p[0], p[8], p[16], p[24] (the four loads in flight together)
-__device__ __forceinline__ void await4(const double *p, double v[4], volatile int *flags) {
-  bool ready = true;
-#pragma unroll
-  for (int m = 0; m < 4; m++) v[m] = ld_relaxed(p + 8 * m);
-#pragma unroll
-  for (int m = 0; m < 4; m++) ready &= (unsigned long long)__double_as_longlong(v[m]) != kUnset;
-  if (!ready)
-    for (int m = 0; m < 4; m++) v[m] = await_value(p + 8 * m, flags);
-}
-
-__device__ __forceinline__ void publish(double *p, double v) {
-  if ((unsigned long long)__double_as_longlong(v) == kUnset)
-    v = __longlong_as_double(0x7FF8000000000000ll);   // keep a NaN a NaN
-  asm volatile("st.relaxed.gpu.global.f64 [%0], %1;" ::"l"(p), "d"(v) : "memory");
-}
-
 __global__ void __launch_bounds__(kPipeThreads) k_prof_solve_pipe(ProfileSystem S, int nrhs,
                                                                   double *x, int ldx,
                                                                   double *ys, double *cs,
-                                                                  double *xs, double *ds) {
+                                                                  double *xs, double *ds,
+                                                                  int backward_only) {
   __shared__ double rv[2][4][kT];
   volatile int *flags = S.flags;
   const int tid = threadIdx.x;
@@ -723,8 +814,8 @@ __global__ void __launch_bounds__(kPipeThreads) k_prof_solve_pipe(ProfileSystem 
     return group_sum(t);
   };
   int it = 0;                                   // rv is double-buffered by iteration
-  // ---------------- forward
-  for (int J = blockIdx.x; J < nt; J += P, it++) {
+  // ---------------- forward (done by the factorisation when backward_only)
+  for (int J = blockIdx.x; J < nt && !backward_only; J += P, it++) {
     double acc[4] = {0.0, 0.0, 0.0, 0.0};
     const int ohi = min(W, J - S.ftile[J]);
     for (int o = ohi; o >= 3; o--) {
@@ -884,10 +975,16 @@ void profile_tasks(int nt, int W, const std::vector<int> &ftile, std::vector<int
         for (int q = 0; q < kPanelParts; q++) emit(1, J + o, q, J);
     updates(J, 1, 1);
     updates(J - 1, 3, W);
-    if (J >= 2) emit(6, J - 2, J - 2, J - 2);
+    if (J >= 2) {
+      emit(6, J - 2, J - 2, J - 2);
+      emit(7, J - 2, J - 2, J - 2);
+    }
   }
   updates(nt - 1, 2, W);
-  for (int J = std::max(nt - 2, 0); J < nt; J++) emit(6, J, J, J);
+  for (int J = std::max(nt - 2, 0); J < nt; J++) {
+    emit(6, J, J, J);
+    emit(7, J, J, J);
+  }
 }
 
 size_t profile_tile_doubles(int nt, int W) { return (size_t)nt * (W + 1) * kTT; }
@@ -916,6 +1013,14 @@ int profile_factor(const ProfileSystem &S, cudaStream_t s, int *bad_eq) {
                          kFactorSoloSmem);
   }
   const size_t nslots = (size_t)S.nt * (S.W + 1);
+  if (S.fwd_nrhs > 0) {
+    // the forward sweep runs inside: its published values start unset
+    if (!profile_pipelined(S) || S.fwd_nrhs > 4 || !S.fwd_x) return XG_EINVAL;
+    const size_t ls = (size_t)S.nt * kT;
+    if (cudaMemsetAsync(S.sweep, 0xFF, 2 * (size_t)S.fwd_nrhs * ls * sizeof(double), s) !=
+        cudaSuccess)
+      return XG_ECUDA;
+  }
   if (cudaMemsetAsync(S.upd, 0, nslots * sizeof(int), s) != cudaSuccess) return XG_ECUDA;
   if (cudaMemsetAsync(S.done, 0, nslots * sizeof(int), s) != cudaSuccess) return XG_ECUDA;
   if (cudaMemsetAsync(S.cpl, 0, (size_t)S.nt * sizeof(int), s) != cudaSuccess) return XG_ECUDA;
@@ -934,21 +1039,30 @@ int profile_factor(const ProfileSystem &S, cudaStream_t s, int *bad_eq) {
   return 0;
 }
 
-int profile_solve(const ProfileSystem &S, int nrhs, double *x, int ldx, cudaStream_t s) {
+bool profile_pipelined(const ProfileSystem &S) { return S.sweep && S.nt >= 2 * kPipeBlocks; }
+
+int profile_solve(const ProfileSystem &S, int nrhs, double *x, int ldx, cudaStream_t s,
+                  bool backward_only) {
   if (S.n == 0) return 0;
   if (nrhs < 1 || nrhs > 4 || ldx < S.nt * kT) return XG_EINVAL;
-  if (S.sweep && S.nt >= 2 * kPipeBlocks) {
-    // pipelined over co-resident blocks (both sweeps' published values are
-    // reset to kUnset first); small systems keep the one-block sweep
+  if (backward_only && !profile_pipelined(S)) return XG_EINVAL;
+  if (profile_pipelined(S)) {
+    // pipelined over co-resident blocks (the sweeps' published values are
+    // reset to kUnset first; after a factorisation that ran the forward
+    // sweep, only the backward sweep's); small systems keep the one-block
+    // sweep
     const size_t ls = (size_t)S.nt * kT;
-    if (cudaMemsetAsync(S.sweep, 0xFF, 4 * (size_t)nrhs * ls * sizeof(double), s) != cudaSuccess)
+    double *ys = S.sweep, *cs = ys + (size_t)nrhs * ls, *xs = cs + (size_t)nrhs * ls;
+    double *ds = xs + (size_t)nrhs * ls;
+    double *reset = backward_only ? xs : ys;
+    const size_t nreset = (backward_only ? 2 : 4) * (size_t)nrhs * ls;
+    if (cudaMemsetAsync(reset, 0xFF, nreset * sizeof(double), s) != cudaSuccess)
       return XG_ECUDA;
     if (cudaMemsetAsync(S.flags, 0, 4 * sizeof(int), s) != cudaSuccess) return XG_ECUDA;
     ProfileSystem Sv = S;
-    double *ys = S.sweep, *cs = ys + (size_t)nrhs * ls, *xs = cs + (size_t)nrhs * ls;
-    double *ds = xs + (size_t)nrhs * ls;
-    void *args[] = {(void *)&Sv, (void *)&nrhs, (void *)&x,  (void *)&ldx,
-                    (void *)&ys, (void *)&cs,   (void *)&xs, (void *)&ds};
+    int bonly = backward_only ? 1 : 0;
+    void *args[] = {(void *)&Sv, (void *)&nrhs, (void *)&x,  (void *)&ldx, (void *)&ys,
+                    (void *)&cs, (void *)&xs,   (void *)&ds, (void *)&bonly};
     if (cudaLaunchCooperativeKernel((void *)k_prof_solve_pipe, dim3(kPipeBlocks),
                                     dim3(kPipeThreads), args, 0, s) != cudaSuccess)
       return XG_ECUDA;

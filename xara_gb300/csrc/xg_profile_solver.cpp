@@ -89,6 +89,7 @@ int ProfileSolver::setup(int n, const int *rowptr, const int *colidx, const int 
 
 int ProfileSolver::factor(cudaStream_t s, int *bad_eq) {
   if (!ready_) return XG_ESTATE;
+  fwd_nrhs_ = 0;
   return profile_factor(S_, s, bad_eq);
 }
 
@@ -101,6 +102,38 @@ int ProfileSolver::solve(int nrhs, const double *const *b, double *const *x, cud
         cudaSuccess)
       return XG_ECUDA;
   if (int e = profile_solve(S_, nrhs, px_.p, ldx_, s)) return e;
+  for (int r = 0; r < nrhs; r++)
+    if (cudaMemcpyAsync(x[r], px_.p + (size_t)r * ldx_, bytes, cudaMemcpyDeviceToDevice, s) !=
+        cudaSuccess)
+      return XG_ECUDA;
+  return 0;
+}
+
+int ProfileSolver::factor_forward(int nrhs, const double *const *b, cudaStream_t s,
+                                  int *bad_eq) {
+  if (!ready_) return XG_ESTATE;
+  if (nrhs < 1 || nrhs > 4 || !can_fuse()) return XG_EINVAL;
+  fwd_nrhs_ = 0;
+  const size_t bytes = (size_t)S_.n * sizeof(double);
+  for (int r = 0; r < nrhs; r++)
+    if (cudaMemcpyAsync(px_.p + (size_t)r * ldx_, b[r], bytes, cudaMemcpyDeviceToDevice, s) !=
+        cudaSuccess)
+      return XG_ECUDA;
+  ProfileSystem Sf = S_;
+  Sf.fwd_nrhs = nrhs;
+  Sf.fwd_ldx = ldx_;
+  Sf.fwd_x = px_.p;
+  if (int e = profile_factor(Sf, s, bad_eq)) return e;
+  fwd_nrhs_ = nrhs;
+  return 0;
+}
+
+int ProfileSolver::solve_backward(int nrhs, double *const *x, cudaStream_t s) {
+  if (!ready_) return XG_ESTATE;
+  if (nrhs != fwd_nrhs_ || nrhs < 1) return XG_ESTATE;   // no matching forward sweep
+  fwd_nrhs_ = 0;
+  if (int e = profile_solve(S_, nrhs, px_.p, ldx_, s, true)) return e;
+  const size_t bytes = (size_t)S_.n * sizeof(double);
   for (int r = 0; r < nrhs; r++)
     if (cudaMemcpyAsync(x[r], px_.p + (size_t)r * ldx_, bytes, cudaMemcpyDeviceToDevice, s) !=
         cudaSuccess)
