@@ -31,7 +31,8 @@ struct ContinuumView {
   double *tan;            // trial tangent: quad 6 unique D entries; brick a b c n(6)
   int *nfail;             // [1] points whose return map hit the iteration cap
   // element outputs (element-major scratch)
-  double *Ke;             // [ne][ned*ned] row-major (quad 64, brick 576)
+  double *Ke;             // [ne][ned*ned] row-major (quad 64, brick 576); bricks with geo2
+                          // write float pairs (hi, lo) there
   double *Re;             // [ne][ned]
   // bricks: shape-function gradients dN_a/dx_i at [(8i+a)*npts + pt] and the
   // Jacobian determinant at [24*npts + pt], formed once (the geometry does
@@ -80,9 +81,11 @@ int launch_brick_geometry(const ContinuumView &v, double *geo, float2 *geo2, int
 // recorders: kind 0 writes one row ([t] values), kind 1 updates an envelope
 int launch_record(int kind, int n, const int *idx, const double *src, double t, int echo,
                   int first, double *out, cudaStream_t s);
+// pairs: the scratch holds float pairs (hi, lo), 8 bytes an entry (the
+// float-float brick tangent); needs the run map (GatherMap::run_slot).
 int launch_gather(const GatherMap &g, const double *scratch, double *partial, double *out,
-                  cudaStream_t s);
-int gather_launch_count(const GatherMap &g);   // kernels launch_gather issues
+                  cudaStream_t s, bool pairs = false);
+int gather_launch_count(const GatherMap &g, bool pairs = false);   // kernels launch_gather issues
 int launch_j2_zero_state(const ContinuumView &v, cudaStream_t s);
 
 // Block-Jacobi preconditioned CG (xg_pcg.cu)

@@ -632,6 +632,20 @@ struct BrickSmemFF {
   int eg[kBrickEPW], scale[kBrickEPW];
 };
 
+// f * 2^s in single precision from the bits: exact where the result is a
+// normal number; below that range zero (under 2^-126 of the model's units,
+// negligible against any stiffness term), above it infinity.
+__device__ __forceinline__ float f32_ldexp(float f, int s) {
+  const unsigned u = __float_as_uint(f);
+  const int e8 = (int)((u >> 23) & 0xff);
+  if (e8 == 0) return 0.0f;
+  if (e8 == 255) return f;
+  const int ne = e8 + s;
+  if (ne <= 0) return 0.0f;
+  if (ne >= 255) return __uint_as_float((u & 0x80000000u) | 0x7f800000u);
+  return __uint_as_float((u & 0x807fffffu) | ((unsigned)ne << 23));
+}
+
 __global__ void __launch_bounds__(32 * kBrickWarps) k_brick_assemble_ff(ContinuumView v) {
   __shared__ BrickSmemFF sm_all[kBrickWarps];
   const int wi = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -764,13 +778,15 @@ __global__ void __launch_bounds__(32 * kBrickWarps) k_brick_assemble_ff(Continuu
     if (e0 + te >= v.ne) continue;
     const int sc = S.scale[te];
     const int ta = kPairA[pp], tb = kPairB[pp];
-    double *Ke = v.Ke + (long)(e0 + te) * 576;
+    // the element matrix as float pairs in the model's units (the scale put
+    // back into the exponents); the gather sums them in float-float
+    float2 *Ke = reinterpret_cast<float2 *>(v.Ke) + (long)(e0 + te) * 576;
 #pragma unroll
     for (int i = 0; i < 3; i++)
 #pragma unroll
       for (int k = 0; k < 3; k++) {
         const float2 c = S.acc[3 * i + k][t];
-        const double kv = f32_to_f64_scaled(c.x, sc) + f32_to_f64_scaled(c.y, sc);
+        const float2 kv = make_float2(f32_ldexp(c.x, sc), f32_ldexp(c.y, sc));
         Ke[(3 * ta + i) * 24 + 3 * tb + k] = kv;
         if (ta != tb) Ke[(3 * tb + k) * 24 + 3 * ta + i] = kv;
       }
@@ -836,6 +852,40 @@ __global__ void k_gather_chunks(GatherMap g, const Idx *__restrict__ src,
 // One run of L slots: its slots summed in contribution order (the element
 // order, as the chunks sum), each contribution's values read as one
 // contiguous piece.
+// The same over float pairs (the float-float brick tangent), summed in
+// float-float; one double per slot.
+template <int L>
+__device__ __forceinline__ void gather_run_pairs(const int *src, int n, const float2 *scratch,
+                                                 double *out) {
+  float ah[L], al[L];
+#pragma unroll
+  for (int t = 0; t < L; t++) ah[t] = al[t] = 0.f;
+  int q = 0;
+  for (; q + 4 <= n; q += 4) {
+    const unsigned a0 = (unsigned)src[q], a1 = (unsigned)src[q + 1];
+    const unsigned a2 = (unsigned)src[q + 2], a3 = (unsigned)src[q + 3];
+    float2 v[4][L];
+#pragma unroll
+    for (int t = 0; t < L; t++) {
+      v[0][t] = scratch[a0 + t];
+      v[1][t] = scratch[a1 + t];
+      v[2][t] = scratch[a2 + t];
+      v[3][t] = scratch[a3 + t];
+    }
+#pragma unroll
+    for (int u = 0; u < 4; u++)
+#pragma unroll
+      for (int t = 0; t < L; t++) ff_add(v[u][t].x, v[u][t].y, ah[t], al[t]);
+  }
+  for (; q < n; q++) {
+    const float2 *p = scratch + (unsigned)src[q];
+#pragma unroll
+    for (int t = 0; t < L; t++) ff_add(p[t].x, p[t].y, ah[t], al[t]);
+  }
+#pragma unroll
+  for (int t = 0; t < L; t++) out[t] = f32_to_f64_scaled(ah[t], 0) + f32_to_f64_scaled(al[t], 0);
+}
+
 template <int L>
 __device__ __forceinline__ void gather_run(const int *src, int n, const double *scratch,
                                            double *out) {
@@ -873,6 +923,7 @@ __device__ __forceinline__ void gather_run(const int *src, int n, const double *
 // a warp's threads take the same branch and loop as often: the FP64 adds,
 // which hold the FP64 pipe per warp instruction whatever its active lanes,
 // are then issued once per useful add.
+template <bool kPairs>
 __global__ void k_gather_runs(GatherMap g, const double *__restrict__ scratch,
                               double *__restrict__ out) {
   const int r = blockIdx.x * blockDim.x + threadIdx.x;
@@ -880,6 +931,18 @@ __global__ void k_gather_runs(GatherMap g, const double *__restrict__ scratch,
   const int s0 = g.run_slot[r], meta = g.run_meta[r];
   const int len = meta & 15, n = meta >> 4;
   const int *src = g.run_src + g.run_begin[r];
+  if (kPairs) {
+    const float2 *sp = reinterpret_cast<const float2 *>(scratch);
+    switch (len) {
+      case 1: gather_run_pairs<1>(src, n, sp, out + s0); break;
+      case 2: gather_run_pairs<2>(src, n, sp, out + s0); break;
+      case 3: gather_run_pairs<3>(src, n, sp, out + s0); break;
+      case 4: gather_run_pairs<4>(src, n, sp, out + s0); break;
+      case 5: gather_run_pairs<5>(src, n, sp, out + s0); break;
+      default: gather_run_pairs<6>(src, n, sp, out + s0); break;
+    }
+    return;
+  }
   switch (len) {
     case 1: gather_run<1>(src, n, scratch, out + s0); break;
     case 2: gather_run<2>(src, n, scratch, out + s0); break;
@@ -892,7 +955,7 @@ __global__ void k_gather_runs(GatherMap g, const double *__restrict__ scratch,
 
 // The chunk and slot kernels over a list of chunks / slots (the long slots
 // of a map with runs), or over all of them when the list is null.
-template <typename Idx>
+template <typename Idx, bool kPairs>
 __global__ void k_gather_chunk_list(GatherMap g, const Idx *__restrict__ src,
                                     const double *__restrict__ scratch,
                                     double *__restrict__ partial, double *__restrict__ out) {
@@ -901,7 +964,15 @@ __global__ void k_gather_chunk_list(GatherMap g, const Idx *__restrict__ src,
   const int c = g.long_chunks[i];
   double s = 0.0;
   const int64_t b = g.chunk_begin[c], end = g.chunk_begin[c + 1];
-  for (int64_t k = b; k < end; k++) s += scratch[src[k]];
+  if (kPairs) {
+    const float2 *sp = reinterpret_cast<const float2 *>(scratch);
+    for (int64_t k = b; k < end; k++) {
+      const float2 v = sp[src[k]];
+      s += (double)v.x + (double)v.y;
+    }
+  } else {
+    for (int64_t k = b; k < end; k++) s += scratch[src[k]];
+  }
   const int slot = g.chunk_slot[c];
   if (g.slot_chunk[slot + 1] - g.slot_chunk[slot] == 1) out[slot] = s;
   else partial[c] = s;
@@ -1079,19 +1150,29 @@ int launch_j2_zero_state(const ContinuumView &v, cudaStream_t s) {
   k_j2_zero<<<nblocks((long)v.ne * v.nip), kThreads, 0, s>>>(v);
   return check_launch();
 }
-int gather_launch_count(const GatherMap &g) {
+int gather_launch_count(const GatherMap &g, bool pairs) {
+  if (pairs && !(g.run_slot && g.src32)) return 0;
   if (g.nslots == 0) return 0;
   if (g.run_slot && g.src32) return (g.nruns > 0) + (g.nlong_chunks > 0) + (g.nlong_slots > 0);
   return 2;
 }
 int launch_gather(const GatherMap &g, const double *scratch, double *partial, double *out,
-                  cudaStream_t s) {
+                  cudaStream_t s, bool pairs) {
   if (g.nslots == 0) return 0;
+  if (pairs && !(g.run_slot && g.src32)) return XG_EINVAL;   // pairs need the run map
   if (g.run_slot && g.src32) {
-    if (g.nruns) k_gather_runs<<<nblocks(g.nruns), kThreads, 0, s>>>(g, scratch, out);
-    if (g.nlong_chunks)
-      k_gather_chunk_list<int><<<nblocks(g.nlong_chunks), kThreads, 0, s>>>(g, g.src32, scratch,
-                                                                             partial, out);
+    if (g.nruns) {
+      if (pairs) k_gather_runs<true><<<nblocks(g.nruns), kThreads, 0, s>>>(g, scratch, out);
+      else k_gather_runs<false><<<nblocks(g.nruns), kThreads, 0, s>>>(g, scratch, out);
+    }
+    if (g.nlong_chunks) {
+      if (pairs)
+        k_gather_chunk_list<int, true><<<nblocks(g.nlong_chunks), kThreads, 0, s>>>(
+            g, g.src32, scratch, partial, out);
+      else
+        k_gather_chunk_list<int, false><<<nblocks(g.nlong_chunks), kThreads, 0, s>>>(
+            g, g.src32, scratch, partial, out);
+    }
     if (g.nlong_slots)
       k_gather_slot_list<<<nblocks(32L * g.nlong_slots), kThreads, 0, s>>>(g, partial, out);
     return check_launch();

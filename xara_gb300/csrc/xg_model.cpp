@@ -435,6 +435,8 @@ struct xg_model {
   int nsig() const { return etype == XG_ELE_QUAD ? 3 : 6; }
   int ntan() const { return etype == XG_ELE_QUAD ? 6 : 9; }
   long npts() const { return (long)ne * nip; }
+  // the element scratch holds float pairs (the float-float brick tangent)
+  bool ke_pairs() const { return etype == XG_ELE_BRICK && d_geo2.p != nullptr; }
   int ke_size() const {
     if (frames()) return ned * ned;
     return ned * ned;
@@ -847,7 +849,9 @@ int xg_model::upload(const HostGather &gk_h, const HostGather &gr_h) {
   } else {
     if (etype == XG_ELE_BRICK) {
       RET(d_geo.alloc((size_t)25 * np));
-      RET(d_geo2.alloc((size_t)24 * np));
+      // the float-float tangent writes float pairs that only the run gather
+      // reads: without a run map (a scratch past 32-bit indices) the FP64 one
+      if (gk.run_slot && gk.src32) RET(d_geo2.alloc((size_t)24 * np));
       CK(cudaMemsetAsync(d_nfail.p, 0, sizeof(int), s));
       RET(launch_brick_geometry(view(), d_geo.p, d_geo2.p, d_nfail.p, s));
       int bad = 0;
@@ -1413,8 +1417,8 @@ int xg_model::element_state(bool compute) {
     prof_end(P_ASSEMBLE, 1);
   }
   prof_begin(P_GATHER_K);
-  RET(launch_gather(gk, d_Ke.p, d_partial.p, d_vals.p, s));
-  prof_end(P_GATHER_K, gather_launch_count(gk));
+  RET(launch_gather(gk, d_Ke.p, d_partial.p, d_vals.p, s, ke_pairs()));
+  prof_end(P_GATHER_K, gather_launch_count(gk, ke_pairs()));
   prof_begin(P_GATHER_R);
   RET(launch_gather(gr, d_Re.p, d_partial.p, d_resid.p, s));
   prof_end(P_GATHER_R, gather_launch_count(gr));
@@ -2386,7 +2390,13 @@ int xg_elemset_element_matrices(const xg_model *m, double *K, double *P) {
     for (int e = 0; e < m->ne; e++) {
       double *out = K + (size_t)e * ned * ned;
       const double *in = ke.data() + (size_t)e * m->ke_size();
-      std::copy(in, in + (size_t)ned * ned, out);
+      if (!m->ke_pairs()) {
+        std::copy(in, in + (size_t)ned * ned, out);
+        continue;
+      }
+      // float pairs (hi, lo), 8 bytes an entry
+      const float *pr = reinterpret_cast<const float *>(in);
+      for (int k = 0; k < ned * ned; k++) out[k] = (double)pr[2 * k] + (double)pr[2 * k + 1];
     }
   }
   if (P) {
