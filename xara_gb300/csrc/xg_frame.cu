@@ -84,18 +84,50 @@ __device__ __forceinline__ void steel01_trial(const double *q, const double *hc,
 // reciprocal of xg_rcp.h (within an ulp of the correctly rounded one): the
 // stress and tangent differ from the reference's expression order by a few
 // ulps.
+// Tests and conversions on the bits of a double (integer instructions): the
+// FP64 pipe, this law's bottleneck, then takes only arithmetic.  Exact for
+// every non-NaN value.
+__device__ __forceinline__ bool d_nonzero(double x) {
+  return ((unsigned long long)__double_as_longlong(x) << 1) != 0ull;
+}
+__device__ __forceinline__ bool d_pos(double x) {    // x > 0
+  const long long b = __double_as_longlong(x);
+  return b > 0;
+}
+__device__ __forceinline__ bool d_neg(double x) {    // x < 0
+  const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+  return (b >> 63) != 0ull && (b << 1) != 0ull;
+}
+// kon (0..3) as the record keeps it (a double) and back
+__device__ __forceinline__ int kon_of(double k) {
+  const unsigned hi = (unsigned)__double2hiint(k);
+  return hi == 0x3FF00000u ? 1 : hi == 0x40000000u ? 2 : hi == 0x40080000u ? 3 : 0;
+}
+__device__ __forceinline__ double kon_value(int k) {
+  return k == 1 ? 1.0 : k == 2 ? 2.0 : k == 3 ? 3.0 : 0.0;
+}
+// |x| in single precision, truncated, clamped to the normal range (for
+// estimates with a margin)
+__device__ __forceinline__ float f32_abs_trunc(double x) {
+  const unsigned long long b = (unsigned long long)__double_as_longlong(x) & 0x7fffffffffffffffull;
+  const int e = (int)(b >> 52) - 1023;
+  if (e < -126) return 1.17549435e-38f;
+  if (e > 127) return 3.40282347e+38f;
+  return __uint_as_float((unsigned)((e + 127) << 23) | (unsigned)((b >> 29) & 0x7fffffu));
+}
+
 __device__ void steel02_trial(const double *q, const double *hc, double trialStrain,
                               double *ht) {
   const double Fy = q[0], E0 = q[1], b = q[2], R0 = q[3], cR1 = q[4], cR2 = q[5];
   const double a1 = q[6], a2 = q[7], a3 = q[8], a4 = q[9], sigini = q[10];
   const double Esh = b * E0, epsy = q[11];
   double eps = trialStrain;
-  if (sigini != 0.0) eps = trialStrain + sigini / E0;
+  if (d_nonzero(sigini)) eps = trialStrain + sigini / E0;
   const double epsP = hc[10], sigP = hc[9];
   const double deps = eps - epsP;
   double epsmax = hc[1], epsmin = hc[0], epspl = hc[2], epss0 = hc[3], sigs0 = hc[4];
   double epsr = hc[5], sigr = hc[6], R = hc[11];
-  int kon = (int)hc[7];
+  int kon = kon_of(hc[7]);
   bool newR = false;
   ht[10] = eps;
   if (kon == 0 || kon == 3) {
@@ -106,11 +138,11 @@ __device__ void steel02_trial(const double *q, const double *hc, double trialStr
     }
     epsmax = epsy;
     epsmin = -epsy;
-    if (deps < 0.0) { kon = 2; epss0 = epsmin; sigs0 = -Fy; epspl = epsmin; }
+    if (d_neg(deps)) { kon = 2; epss0 = epsmin; sigs0 = -Fy; epspl = epsmin; }
     else { kon = 1; epss0 = epsmax; sigs0 = Fy; epspl = epsmax; }
     newR = true;
   }
-  if (kon == 2 && deps > 0.0) {
+  if (kon == 2 && d_pos(deps)) {
     kon = 1;
     epsr = epsP;
     sigr = sigP;
@@ -121,7 +153,7 @@ __device__ void steel02_trial(const double *q, const double *hc, double trialStr
     sigs0 = Fy * shft + Esh * (epss0 - epsy * shft);
     epspl = epsmax;
     newR = true;
-  } else if (kon == 1 && deps < 0.0) {
+  } else if (kon == 1 && d_neg(deps)) {
     kon = 2;
     epsr = epsP;
     sigr = sigP;
@@ -147,7 +179,8 @@ __device__ void steel02_trial(const double *q, const double *hc, double trialStr
   // sig = b e* + (1-b) e* rdum2, e = b + (1-b) rdum2 / dum1.
   const double ae = fabs(epsrat);
   double se = (1.0 - b) * epsrat, te = 1.0 - b;
-  if (!((float)R * __log2f(fmaxf((float)ae, 1.17549435e-38f)) < -60.0f)) {
+  const float Rf = d_neg(R) ? -f32_abs_trunc(R) : f32_abs_trunc(R);
+  if (!(Rf * __log2f(f32_abs_trunc(ae)) < -60.0f)) {
     const double pr = ae > 0.0 ? exp(R * log(ae)) : 0.0;
     const double dum1 = 1.0 + pr;
     const double rdum2 = exp(-log(dum1) * chain_reciprocal(R));
@@ -160,7 +193,7 @@ __device__ void steel02_trial(const double *q, const double *hc, double trialStr
   double e = b + te;
   e = e * dsig * rden;
   ht[0] = epsmin; ht[1] = epsmax; ht[2] = epspl; ht[3] = epss0; ht[4] = sigs0;
-  ht[5] = epsr; ht[6] = sigr; ht[7] = (double)kon; ht[8] = e; ht[9] = sig; ht[11] = R;
+  ht[5] = epsr; ht[6] = sigr; ht[7] = kon_value(kon); ht[8] = e; ht[9] = sig; ht[11] = R;
 }
 
 // Concrete02 parameters after the constructor's sign normalisation
