@@ -383,6 +383,36 @@ def test_profile_pipelined_sweeps_residual(gpu_mod):
         assert relerr(x, xp) < 1e-9
 
 
+def test_brick_tangent_outside_the_split_range(gpu_mod):
+    """A brick block whose coordinates (and displacements) are scaled by
+    1e-35: the strains are unchanged but dN/dx reaches 1e35, past the range
+    a float pair holds, so the model forms the tangent with its FP64 kernel
+    (and gathers doubles).  Element matrices and resisting forces against
+    the oracle's within 1e-12, as at ordinary scales."""
+    from oracle import port
+    from xara_gb300._abi import ModelDesc
+    fx = load("brick_4x3x2")
+    desc, _ = model_of(fx)
+    s = 1e-35
+    kw = {k: v for k, v in desc.arrays.items() if v is not None}
+    kw["node_crd"] = np.asarray(desc.arrays["node_crd"]) * s
+    small = ModelDesc(ndm=desc.ndm, ndf=desc.ndf, elem_type=desc.elem_type,
+                      handler=desc.handler, **kw)
+    U = fx["step_u"][3] * s
+    o = port.OracleModel(small)
+    Ko, Po = o.element_matrices(U)
+    o.close()
+    with gpu_mod.DeviceModel(small) as m:
+        m.set_trial_disp(U)
+        m.update()
+        K, P = m.element_matrices()
+    kscale = np.abs(Ko).reshape(len(Ko), -1).max(axis=1)[:, None, None]
+    pscale = np.abs(Po).max(axis=1)[:, None]
+    assert np.abs(Ko).max() < 1e-20                      # the model's own units
+    assert np.max(np.abs(K - Ko) / kscale) < RTOL_STATE
+    assert np.max(np.abs(P - Po) / pscale) < RTOL_STATE
+
+
 @pytest.mark.parametrize("name", ["quad_8x4", "brick_4x3x2", "frame2d_2x3", "frame3d_1x1x2"])
 def test_element_matrices_match_the_oracle(gpu_mod, name):
     """xg_elemset_element_matrices (what the element-set shim hands the
