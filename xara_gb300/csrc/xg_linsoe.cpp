@@ -6,7 +6,8 @@
 // fact * m(i,j) where both equation numbers are >= 0, locating the column by
 // a search of the row; addB / setB likewise) and accumulates in host memory,
 // the way the reference's FE_Element loop feeds it; solve() runs the
-// block-Jacobi PCG of the model path (sliced ELL SpMV, long rows in chunks)
+// block-Jacobi PCG of the model path (node-block sliced ELL SpMV, long node
+// rows in chunks)
 // on the device and returns X to the host.  With `system ProfileSPD`
 // (xg_linsoe_set_system) addA follows ProfileSPDLinSOE instead
 // (profileSPD/ProfileSPDLinSOE.cpp:214-269: only the terms with row <= col,

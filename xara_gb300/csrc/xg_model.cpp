@@ -233,9 +233,9 @@ struct xg_model {
   int record_step();
   PcgSystem pcg{};
   bool blocks_factored = false;
-  // sliced ELL copy of the matrix for the PCG's SpMV, built at the first
-  // PCG solve (skipped, keeping the CSR SpMV, when it would take more than
-  // half of the free device memory)
+  // node-block sliced ELL copy of the matrix for the PCG's SpMV, built at
+  // the first PCG solve (skipped, keeping the CSR SpMV, when it would take
+  // more than half of the free device memory)
   DBuf<long> d_nb_off;
   DBuf<int> d_nb_cols, d_nb_len, d_nb_pos;
   DBuf<float2> d_nb_vals, d_p2;

@@ -1,8 +1,11 @@
-// xg_pcg.cu -- block-Jacobi preconditioned conjugate gradients, FP64.
+// xg_pcg.cu -- block-Jacobi preconditioned conjugate gradients: vectors,
+// inner products and the preconditioner in FP64, the SpMV's products in
+// float-float over a node-block copy of the matrix (FP64 warp per CSR row
+// without one).
 //
 // The whole solve is one cooperative, persistent launch: every block owns a
-// grid-stride share of the rows, SpMV runs warp-per-row over the CSR arrays,
-// and the three inner products of an iteration are reduced deterministically
+// grid-stride share of the node rows (of the rows without the copy), and the
+// three inner products of an iteration are reduced deterministically
 // (fixed-order block partials, then every block sums the partials in the same
 // order), so the iterates are bit-identical run to run.  Blocks meet at a
 // grid barrier whose wait is bounded by the global timer: a block that waits
