@@ -796,7 +796,10 @@ def run_batch(args):
                      "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak if achieved and peak else None,
                      "peak_source": peak_kind, "traffic": ncu_traffic("batch", dominant),
-                     "algorithmic_bytes_per_launch": alg},
+                     "algorithmic_bytes_per_launch": alg,
+                     "limit": "the FP64 pipe, not HBM: 78.6 % active under ncu "
+                              "(profiles/k_fbc_update_batch_c3.md); the fraction above is the "
+                              "kernel's HBM view"},
         "kernels_ms_per_step": {k: v[0] / args.steps for k, v in kernels.items()},
         "clocks": clocks,
         "setup_s": t_setup,
@@ -1372,7 +1375,10 @@ def run_brick(args):
         "roofline": {"bound": "hbm", "kernel": dominant, "achieved": achieved, "peak": peak,
                      "unit": "GB/s", "frac": achieved / peak if peak else None,
                      "peak_source": peak_kind, "traffic": ncu_traffic("brick", dominant),
-                     "algorithmic_bytes_per_launch": alg.get(dominant, alg["phase"])},
+                     "algorithmic_bytes_per_launch": alg.get(dominant, alg["phase"]),
+                     "limit": "instruction issue on the single-precision pipes, not HBM: the "
+                              "tangent's float-float sums (IPC 2.3 of 4, FMA pipe 42 % under "
+                              "ncu: profiles/k_brick_assemble_brick_c2_small.md)"},
         "fp64": {"est_flops_per_step": flops, "achieved_tflops": flops / phase_s / 1e12,
                  "peak_tflops_probe": fp64_peak,
                  "frac": (flops / phase_s / 1e12) / fp64_peak if fp64_peak else None},
