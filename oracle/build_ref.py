@@ -46,6 +46,8 @@ tagged/storage/MapOfTaggedObjectsIter.cpp tagged/storage/ArrayOfTaggedObjects.cp
 tagged/storage/ArrayOfTaggedObjectsIter.cpp
 actor/actor/MovableObject.cpp
 handler/OPS_Stream.cpp handler/StandardStream.cpp handler/DummyStream.cpp
+handler/DataFileStream.cpp recorder/Recorder.cpp recorder/NodeRecorder.cpp
+recorder/EnvelopeNodeRecorder.cpp
 domain/domain/Domain.cpp domain/node/Node.cpp domain/node/NodalLoad.cpp
 domain/component/DomainComponent.cpp domain/component/Parameter.cpp
 domain/constraints/SP_Constraint.cpp domain/constraints/MP_Constraint.cpp

@@ -74,6 +74,10 @@
 #include <SparseGenColLinSolver.h>
 #include <Graph.h>
 #include <DOF_Group.h>
+#include <DataFileStream.h>
+#include <NodeRecorder.h>
+#include <EnvelopeNodeRecorder.h>
+#include <NodeData.h>
 #include <Vector.h>
 #include <Matrix.h>
 #include <ID.h>
@@ -428,6 +432,40 @@ void xref_destroy(void *hp) {
   // code the harness does not link; the process exits soon after, so the
   // objects are left to it.
   delete h;
+}
+
+// `recorder Node|EnvelopeNode -file path [-time] [-dT dT] [-precision p]
+// -node tags... -dof dofs... disp|vel|accel` on the reference's domain
+// (runtime/commands/domain/recorder.cpp: a DataFileStream, NodeData
+// DisplTrial / VelocTrial / AccelTrial, relDeltaTTol 1e-5); dofs 0-based.
+// The Domain's commit records; xref_close_recorders deletes them (the
+// envelope writes its three rows then) and closes the files.
+extern "C" int xref_add_node_recorder(void *hp, const char *path, int envelope, int nnodes,
+                                      const int *nodes, int ndofs, const int *dofs,
+                                      int response, int echo_time, double dT, int precision) {
+  Harness *h = (Harness *)hp;
+  if (!h || !path || nnodes < 1 || ndofs < 1 || response < 0 || response > 2) return -1;
+  ID nid(nnodes), did(ndofs);
+  for (int i = 0; i < nnodes; i++) nid(i) = nodes[i];
+  for (int i = 0; i < ndofs; i++) did(i) = dofs[i];
+  const NodeData flag = response == 0 ? NodeData::DisplTrial
+                        : response == 1 ? NodeData::VelocTrial : NodeData::AccelTrial;
+  OPS_Stream *out = new DataFileStream(path, openMode::OVERWRITE, 2, 0, false, precision, false);
+  Recorder *rec;
+  if (envelope)
+    rec = new EnvelopeNodeRecorder(did, &nid, flag, -1, *h->domain, *out, dT, 1e-5,
+                                   echo_time != 0, nullptr);
+  else
+    rec = new NodeRecorder(did, &nid, -1, flag, -1, *h->domain, *out, dT, 1e-5,
+                           echo_time != 0, nullptr);
+  return h->domain->addRecorder(*rec) == 0 ? 0 : -1;
+}
+
+extern "C" int xref_close_recorders(void *hp) {
+  Harness *h = (Harness *)hp;
+  if (!h) return -1;
+  h->domain->removeRecorders();
+  return 0;
 }
 
 // Add load pattern p (its nodal loads and imposed SP values) to the domain.

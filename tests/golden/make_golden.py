@@ -202,11 +202,63 @@ def settlement_fixture():
                   capture_steps=(0,))
 
 
+# The recorders of the transient 2D frame fixture: file, envelope, dofs
+# (0-based; 5 does not exist in 2D), response (0 disp, 1 vel, 2 accel),
+# -time, -dT (in record steps), -precision.
+RECORDER_SPECS = [
+    ("disp", 0, [0, 1, 2, 5], 0, 1, 0, 6),
+    ("env", 1, [0, 2], 0, 1, 0, 10),
+    ("env0", 1, [0], 0, 0, 0, 6),
+    ("vel", 0, [0], 1, 0, 0, 6),
+    ("vel3", 0, [0], 1, 0, 3, 6),
+    ("acc", 0, [1], 2, 0, 0, 6),
+]
+
+
+def recorder_fixture(name="recorders_frame2d_eq"):
+    """`recorder Node` / `recorder EnvelopeNode` of the reference
+    (NodeRecorder, EnvelopeNodeRecorder, DataFileStream) on the transient
+    2D steel frame: gravity by LoadControl, loadConst -time 0, 40 Newmark
+    steps; the files' lines as the reference wrote them."""
+    import ctypes as C
+    import tempfile
+    desc, phases = configs.steel_frame_2d_eq(2, 3, steps=40)
+    tags = np.asarray(desc.arrays["node_tag"])
+    nodes = np.array([tags[1], tags[len(tags) // 2], tags[-1]], np.int32)
+    dt = phases[-1].dt
+    L = ref.lib()
+    L.xref_add_node_recorder.argtypes = [C.c_void_p, C.c_char_p, C.c_int, C.c_int, C.c_void_p,
+                                         C.c_int, C.c_void_p, C.c_int, C.c_int, C.c_double,
+                                         C.c_int]
+    L.xref_close_recorders.argtypes = [C.c_void_p]
+    tmp = tempfile.mkdtemp()
+
+    def attach(h):
+        for f, env, dofs, resp, echo, dsteps, prec in RECORDER_SPECS:
+            da = np.array(dofs, np.int32)
+            r = L.xref_add_node_recorder(C.c_void_p(h), os.path.join(tmp, f + ".out").encode(),
+                                         env, len(nodes), nodes.ctypes.data_as(C.c_void_p),
+                                         len(dofs), da.ctypes.data_as(C.c_void_p), resp, echo,
+                                         dsteps * dt, prec)
+            assert r == 0, f
+
+    run = ref.RefRun(desc, phases, attach=attach)
+    L.xref_close_recorders(C.c_void_p(run.h))
+    arrays = {"nodes": nodes}
+    for f, *_ in RECORDER_SPECS:
+        with open(os.path.join(tmp, f + ".out")) as fh:
+            arrays[f] = np.array(fh.read().splitlines())
+    save(name, **arrays)
+
+
 def main():
     if not ref.available():
         sys.exit("oracle/_ref/libxara_ref.so missing: run python oracle/build_ref.py")
     if sys.argv[1:] == ["c1"]:
         c1_pushover()
+        return
+    if sys.argv[1:] == ["recorders"]:
+        recorder_fixture()
         return
     if sys.argv[1:] == ["settle"]:
         settlement_fixture()

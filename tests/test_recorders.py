@@ -2,7 +2,8 @@
 EnvelopeNodeRecorder.cpp): values gathered on the device after every
 committed step, against the displacement history the analysis returns, a
 host restatement of the envelope's update rule, the -dT thinning, and the
-reference's file format (DataFileStream: blank-separated %g rows)."""
+reference's file format (DataFileStream: blank-separated %g rows), and
+against the files of the reference's own recorders on the same analysis."""
 import numpy as np
 import pytest
 
@@ -94,6 +95,53 @@ def test_node_and_envelope_recorders(need_gpu, tmp_path):
     assert text == [" ".join(f"{v:.6g}" for v in r) for r in rows]
     text = (tmp_path / "env.out").read_text().splitlines()
     assert text == [" ".join(f"{v:.10g}" for v in r) for r in env]
+
+
+def test_recorder_files_match_the_reference(need_gpu, tmp_path):
+    """The same six recorders as the reference's `recorder Node` /
+    `recorder EnvelopeNode` (NodeRecorder, EnvelopeNodeRecorder and
+    DataFileStream compiled from its sources; tests/golden/make_golden.py
+    recorders) on the transient 2D frame: gravity by LoadControl, loadConst
+    -time 0, 40 Newmark steps.  Every file has the reference's lines and
+    columns; times and the envelope's time stamps equal; values within the
+    printed precision of each column's largest magnitude (roundoff-level
+    entries such as 1e-21 vertical drifts print differently)."""
+    import os
+    from golden_util import GOLDEN
+    from xara_gb300 import configs, gpu
+    path = os.path.join(GOLDEN, "recorders_frame2d_eq.npz")
+    if not os.path.exists(path):
+        pytest.skip("recorders_frame2d_eq.npz not generated")
+    z = np.load(path)
+    specs = [("disp", 0, [0, 1, 2, 5], 0, 1, 0, 6), ("env", 1, [0, 2], 0, 1, 0, 10),
+             ("env0", 1, [0], 0, 0, 0, 6), ("vel", 0, [0], 1, 0, 0, 6),
+             ("vel3", 0, [0], 1, 0, 3, 6), ("acc", 0, [1], 2, 0, 0, 6)]
+    responses = [gpu.XG_REC_DISP, gpu.XG_REC_VEL, gpu.XG_REC_ACCEL]
+    desc, phases = configs.steel_frame_2d_eq(2, 3, steps=40)
+    nodes = [int(n) for n in z["nodes"]]
+    dt = phases[-1].dt
+    with gpu.DeviceModel(desc) as m:
+        m.set_system(gpu.XG_SYSTEM_PROFILE_SPD)
+        ids = {}
+        for f, env, dofs, resp, echo, dsteps, prec in specs:
+            ids[f] = m.add_recorder(nodes, dofs, response=responses[resp],
+                                    kind=gpu.XG_REC_ENVELOPE if env else gpu.XG_REC_NODE,
+                                    time=bool(echo), dT=dsteps * dt)
+        m.run(phases)
+        for f, *rest in specs:
+            m.write_recorder(ids[f], tmp_path / (f + ".out"), precision=rest[-1])
+    for f, env, dofs, resp, echo, dsteps, prec in specs:
+        got = (tmp_path / (f + ".out")).read_text().splitlines()
+        want = [str(x) for x in z[f]]
+        assert len(got) == len(want), (f, len(got), len(want))
+        g = np.array([[float(x) for x in line.split()] for line in got])
+        w = np.array([[float(x) for x in line.split()] for line in want])
+        assert g.shape == w.shape, f
+        tcols = [c for c in range(w.shape[1]) if echo and (env and c % 2 == 0 or not env and c == 0)]
+        np.testing.assert_array_equal(g[:, tcols], w[:, tcols])     # times
+        vcols = [c for c in range(w.shape[1]) if c not in tcols]
+        scale = np.maximum(np.abs(w[:, vcols]).max(axis=0), 1e-300)
+        assert np.all(np.abs(g[:, vcols] - w[:, vcols]) <= 2 * 10.0 ** (1 - prec) * scale), f
 
 
 def test_recorder_rejects_unknown_nodes(need_gpu):
