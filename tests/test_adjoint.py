@@ -5,8 +5,9 @@ against central finite differences of the oracle's Steel02 on every branch
 (first loading, same branch, reversals with and without a new extreme
 strain, zero increments, isotropic shift).  GPU: gradients of the roof-drift
 objective with respect to per-member Steel02 parameters against central
-finite differences of the device forward run, and the checkpoint interval
-changing nothing.
+finite differences of the device forward run (2D steel and RC frames, 2D
+frames under P-Delta, a 3D RC frame), and the checkpoint interval changing
+nothing.
 """
 import numpy as np
 import pytest
@@ -414,6 +415,92 @@ def test_adjoint_rc_frames_match_finite_differences(need_gpu, pga_scale, steps):
         phk = configs.adjoint_frames(n_frames=2, steps=steps, seed=5)[1][0]
         with pytest.raises(gpu.XaraGpuError, match="betaK0"):
             gpu.adjoint_forward(m, phk, steps, 10, node, dof, w)
+
+
+def _fd_gradient_checks(m, desc, ph, steps, g, seed, nsingle=4):
+    """The adjoint gradient ``g`` against central differences of the device
+    forward run: along a seeded direction over every parameter (relative
+    1e-4) and for the ``nsingle`` parameters with the largest scaled
+    sensitivities (relative 1e-3)."""
+    gpu = _gpu()
+    node, dof, w = _objective(desc)
+    q0 = desc.uni_param.reshape(-1, 12).copy()
+
+    def J(q):
+        gpu.set_uniaxial_params(m, q)
+        return gpu.adjoint_forward(m, ph, steps, 10, node, dof, w)
+
+    rng = np.random.default_rng(seed)
+    scale = np.abs(q0[:, :3])
+    d = rng.normal(size=scale.shape) * scale
+    h = 1e-6
+    qp, qm = q0.copy(), q0.copy()
+    qp[:, :3] += h * d
+    qm[:, :3] -= h * d
+    fd = (J(qp) - J(qm)) / (2 * h)
+    ad = float((g * d).sum())
+    assert ad == pytest.approx(fd, rel=1e-4), (ad, fd)
+    gs = np.abs(g) * scale
+    for idx in np.argsort(gs.ravel())[len(gs.ravel()) - nsingle:]:
+        u, k = divmod(int(idx), 3)
+        qp, qm = q0.copy(), q0.copy()
+        qp[u, k] *= 1 + h
+        qm[u, k] *= 1 - h
+        fd = (J(qp) - J(qm)) / (2 * h * q0[u, k])
+        assert g[u, k] == pytest.approx(fd, rel=1e-3, abs=1e-4 * gs.max() / abs(q0[u, k])), (u, k)
+    gpu.set_uniaxial_params(m, q0)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("pga_scale,steps", [(1.0, 40), (3.0, 80)])
+def test_adjoint_pdelta_frames_match_finite_differences(need_gpu, pga_scale, steps):
+    """2D frames under `geomTransf PDelta` with growing floor weights: the
+    adjoint carries the transformation's force term (N / L) ul14 g into the
+    basic-force adjoint and its tangent's non-symmetric part by a fixed
+    point on the factored tangent.  Gradients against central differences
+    of the device forward run; the P-Delta terms move the gradients well
+    past the tolerance (the same frames with linear transformations)."""
+    gpu = _gpu()
+    desc, phases = configs.adjoint_pdelta_frames(steps=steps, pga_scale=pga_scale, seed=5)
+    lin, lphases = configs.adjoint_pdelta_frames(steps=steps, pga_scale=pga_scale, seed=5,
+                                                 pdelta=0)
+    assert desc.geom_transf == 1 and lin.geom_transf == 0
+    node, dof, w = _objective(desc)
+    with gpu.DeviceModel(lin) as m:
+        gpu.adjoint_forward(m, lphases[0], steps, 10, node, dof, w)
+        g_lin = gpu.adjoint_backward(m)
+    with gpu.DeviceModel(desc) as m:
+        J0 = gpu.adjoint_forward(m, phases[0], steps, 10, node, dof, w)
+        g = gpu.adjoint_backward(m)
+        assert J0 > 0 and np.isfinite(g).all()
+        assert np.abs(g - g_lin).max() > 1e-3 * np.abs(g).max()
+        _fd_gradient_checks(m, desc, phases[0], steps, g, seed=17)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("pga_scale,steps", [(1.0, 40), (3.0, 80)])
+def test_adjoint_rc_frame_3d_matches_finite_differences(need_gpu, pga_scale, steps):
+    """A 3D RC frame (Concrete02 cover and core, Steel02 bars, elastic
+    torsion, `geomTransf PDelta`, whose 3D terms cancel in the reference's
+    transformation) under a ground motion in x: gradients with respect to
+    every material's first three parameters against central differences of
+    the device forward run, through cracking at both records."""
+    gpu = _gpu()
+    desc, phases = configs.adjoint_rc_frame_3d(steps=steps, pga_scale=pga_scale)
+    node, dof, w = _objective(desc)
+    conc = np.asarray(desc.uni_type) == XG_UNI_CONCRETE02
+    with gpu.DeviceModel(desc) as m:
+        J0 = gpu.adjoint_forward(m, phases[0], steps, 10, node, dof, w)
+        rec = m.fiber_records()
+        g = gpu.adjoint_backward(m)
+        assert J0 > 0 and np.isfinite(g).all()
+        assert np.abs(g[conc]).max() > 0 and np.abs(g[~conc]).max() > 0
+        ss, fm = desc.arrays["sec_fiber_start"], desc.arrays["fib_mat"]
+        kinds = np.concatenate([np.tile(np.asarray(desc.uni_type)[fm[ss[s_]:ss[s_ + 1]]],
+                                        desc.fbc_num_ip)
+                                for s_ in desc.arrays["elem_mat"]])
+        assert (rec[kinds == XG_UNI_CONCRETE02, 1] > 0).mean() > 0.05    # cracked
+        _fd_gradient_checks(m, desc, phases[0], steps, g, seed=19)
 
 
 @pytest.mark.gpu

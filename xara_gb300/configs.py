@@ -754,3 +754,72 @@ def adjoint_rc_frames(n_frames=2, steps=2000, dt=0.01, seed=0, member_cov=0.05, 
     out.meta = dict(desc.meta, workload=f"{n_frames} 2D RC frames, Concrete02 and Steel02 per "
                     "member")
     return out, [ph]
+
+def _with_geometry(desc, geom_transf=None, **arrays):
+    """A copy of ``desc`` with some arrays (and the transformation) replaced."""
+    kw = {k: v for k, v in desc.arrays.items() if v is not None}
+    kw.update(arrays)
+    out = ModelDesc(ndm=desc.ndm, ndf=desc.ndf, elem_type=desc.elem_type,
+                    geom_transf=desc.geom_transf if geom_transf is None else geom_transf,
+                    fbc_num_ip=desc.fbc_num_ip, **kw)
+    out.meta = dict(desc.meta)
+    return out
+
+
+def adjoint_pdelta_frames(n_frames=2, steps=40, dt=0.01, seed=0, pga_scale=1.0,
+                          weight_factor=1.0, pdelta=1):
+    """The frames of :func:`adjoint_frames` under `geomTransf PDelta` with the
+    floor weights as vertical nodal loads in the transient phase's pattern
+    (a Linear series, so the loads grow with time to ``weight_factor`` times
+    every floor node's weight at the last step): columns carry axial loads
+    while the record sways them.  ``pdelta=0`` gives the same model with
+    linear transformations."""
+    desc, phases = adjoint_frames(n_frames=n_frames, steps=steps, dt=dt, seed=seed,
+                                  pga_scale=pga_scale)
+    a = desc.arrays
+    mass = a["node_mass"].reshape(-1, 3)
+    floor = np.nonzero(mass[:, 0] > 0)[0]
+    val = np.zeros((len(floor), 3))
+    val[:, 1] = -weight_factor * mass[floor, 0] * G / (steps * dt)
+    ph = phases[0]
+    out = _with_geometry(desc, geom_transf=pdelta, load_node=a["node_tag"][floor],
+                         load_pattern=np.full(len(floor), ph.pattern), load_value=val)
+    out.meta["workload"] = (f"{n_frames} 2D steel frames under P-Delta, one Steel02 per member, "
+                            "growing floor weights")
+    return out, [ph]
+
+
+def adjoint_rc_frame_3d(bays_x=1, bays_y=1, stories=2, steps=40, dt=0.01, seed=0,
+                        pga=0.4 * G, pga_scale=1.0, col_fibers=40, beam_fibers=24, pdelta=1,
+                        gravity=-250e3):
+    """A small 3D RC frame of :func:`rc_frame_3d` (Concrete02 cover and core,
+    Steel02 bars, elastic torsion) for gradients of the transient run: floor
+    masses (the gravity load over g at every floor node in x, y and z), the
+    gravity loads in the transient phase's pattern growing with time to their
+    full value at the last step, `integrator Newmark 0.5 0.25`, mass-
+    proportional 2 % Rayleigh damping, `pattern UniformExcitation` in x with a
+    Kanai-Tajimi record.  The objective terms are the roof corner's x
+    displacement over the height, squared and summed over the steps."""
+    desc, _ = rc_frame_3d(bays_x, bays_y, stories, col_fibers=col_fibers,
+                          beam_fibers=beam_fibers, pdelta=pdelta, steps=1, grav_steps=1,
+                          seed=seed, gravity=gravity)
+    a = desc.arrays
+    crd = a["node_crd"].reshape(-1, 3)
+    floor = np.nonzero(crd[:, 2] > 0)[0]
+    m = abs(gravity) / G
+    mass = np.zeros((len(crd), 6))
+    mass[floor, :3] = m
+    val = np.zeros((len(floor), 6))
+    val[:, 2] = gravity / (steps * dt)
+    am, _ = rayleigh_2pct(stories)
+    rec = kanai_tajimi(steps + 2, dt, pga * pga_scale, seed + 1000)
+    out = _with_geometry(desc, node_mass=mass, load_node=a["node_tag"][floor],
+                         load_pattern=np.full(len(floor), 2), load_value=val)
+    quake = PhaseDesc(integrator=XG_INT_NEWMARK, pattern=2, num_steps=steps, dt=dt,
+                      gamma=0.5, beta=0.25, alpha_m=am, gm_dof=0, gm_accel=rec, gm_dt=dt,
+                      tol=1e-10, max_iter=50)
+    H = stories * 3.5
+    out.meta = dict(desc.meta, workload=f"3D RC frame {bays_x}x{bays_y}x{stories} under a "
+                    "ground motion", obj_node=np.array([desc.meta["roof"]], np.int32),
+                    obj_dof=np.zeros(1, np.int32), obj_weight=np.array([1.0 / (H * H)]))
+    return out, [quake]

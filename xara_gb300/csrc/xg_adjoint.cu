@@ -6,8 +6,12 @@
 // dynamic unbalance of Newmark.cpp:262-302 with the resisting force of
 // ForceBeamColumn2d/3d::update at the committed fiber records h'), and
 // commits the fiber records h_n = H(eps(U_n), h', theta).  Its adjoint, with
-// the effective tangent K (symmetric, the one the forward step factors):
-//   K mu = Ubar_n + c2 Vbar_n + c3 Abar_n + (dh_n/dU_n)' hbar_n
+// J the exact effective tangent -dR/dU_n:
+//   J' mu = Ubar_n + c2 Vbar_n + c3 Abar_n + (dh_n/dU_n)' hbar_n
+// Under linear transformations J is the symmetric tangent the forward step
+// factors; the 2D P-Delta transformation's tangent leaves out one
+// non-symmetric term per element (k_adj_pdelta), which the host carries by a
+// fixed-point iteration on the factored tangent.
 //   hbar' = (dh_n/dh')' hbar_n - (dP/dh')' mu,   thetabar += the same in theta
 // plus the Newmark predictor's terms for (U', V', A').  Inside an element the
 // converged compatibility state (basic forces Se, section deformations e_s)
@@ -94,6 +98,19 @@ __device__ void basic_T(const FrameView &v, int e, double (*T)[NB == 3 ? 6 : 12]
       T[5][3 + j] = -e1; T[5][9 + j] = e1;
     }
   }
+}
+
+// PDeltaCrdTransf2d (coordTransformation/PDeltaCrdTransf2d.cpp:508-560) adds
+// (Se_0 / L) ul14 g to the global force, g = [-s c 0 s -c 0] and ul14 = g . u
+// the chord's transverse offset at the trial displacements
+__device__ __forceinline__ double pdelta_ul14(const FrameView &v, int e) {
+  const double cs = v.R[9 * (long)e], sn = v.R[9 * (long)e + 1];
+  const double *uI = v.U + (long)v.conn[2 * e] * v.ndf, *uJ = v.U + (long)v.conn[2 * e + 1] * v.ndf;
+  return (-sn * uI[0] + cs * uI[1]) - (-sn * uJ[0] + cs * uJ[1]);
+}
+__device__ __forceinline__ double pdelta_g_dot(const FrameView &v, int e, const double *x) {
+  const double cs = v.R[9 * (long)e], sn = v.R[9 * (long)e + 1];
+  return -sn * x[0] + cs * x[1] + sn * x[3] - cs * x[4];
 }
 
 // Sum over the G lanes of a section's lane group (lanes ip*G .. ip*G+G-1; a
@@ -257,7 +274,9 @@ __global__ void __launch_bounds__(32 * kAdjWarps) k_adj_elem_a(FrameView v, AdjV
 }
 
 // Pass B (warp per element), after the adjoint solve: the basic-force
-// adjoint -T mu_e and pass A's terms give the section adjoints
+// adjoint -(dP/dSe)' mu_e (-T mu_e, and under the 2D P-Delta
+// transformation -(ul14 / L)(g . mu_e) more in the axial force) and pass A's
+// terms give the section adjoints
 // qbar_s = w_s fs_s b_s z - fs_s ebar_s; each fiber's stress adjoint
 // A_f a_f . qbar_s goes through the law into the committed record's and the
 // parameters' adjoints.  The betaK0 K0 damping adds -betaK0/E (T mu)' kv0
@@ -289,19 +308,21 @@ __global__ void __launch_bounds__(32 * kAdjWarps) k_adj_elem_b(FrameView v, AdjV
     ve[j] = a.Vn ? a.Vn[dof] : 0.0;
   }
   const double *kv = st + 6;
-  double pb[NB], z[NB];
+  double pb[NB], pq[NB], z[NB];
 #pragma unroll
   for (int i = 0; i < NB; i++) {
     double s = 0.0;
 #pragma unroll
     for (int j = 0; j < NU; j++) s += T[i][j] * mue[j];
-    pb[i] = s;                         // T mu_e; the basic-force adjoint is -pb
+    pb[i] = s;                         // T mu_e
+    pq[i] = s;                         // (dP/dSe)' mu_e; the basic-force adjoint is -pq
   }
+  if (NB == 3 && v.pdelta2d) pq[0] += pdelta_ul14(v, e) / L * pdelta_g_dot(v, e, mue);
 #pragma unroll
   for (int i = 0; i < NB; i++) {
     double s = 0.0;
 #pragma unroll
-    for (int k = 0; k < NB; k++) s -= kv[i * NB + k] * pb[k];
+    for (int k = 0; k < NB; k++) s -= kv[i * NB + k] * pq[k];
     z[i] = scr[i] + s;
   }
   double tq[kAdjSlots][3] = {};
@@ -405,6 +426,31 @@ __global__ void __launch_bounds__(32 * kAdjWarps) k_adj_elem_b(FrameView v, AdjV
   }
 }
 
+// The part of the transposed tangent that the 2D P-Delta transformation's
+// symmetric tangent leaves out.  With P = T' Se + (Se_0 / L) ul14 g,
+//   dP/du = T' kv T + (Se_0 / L) g g' + (ul14 / L) g (T' kv e_0)'
+// and getGlobalStiffMatrix (PDeltaCrdTransf2d.cpp:567-700) keeps the first
+// two terms; the third's transpose applied to mu_e is
+// (ul14 / L)(g . mu_e) T' kv e_0 (kv symmetric), written to the element
+// force scratch for the residual's gather.  Thread per element.
+__global__ void k_adj_pdelta(FrameView v, AdjView a) {
+  const int e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= v.ne) return;
+  const double *kv = a.st + (long)e * stride_of(v.nip) + 6;
+  double T[3][6];
+  basic_T<3>(v, e, T);
+  double mue[6];
+#pragma unroll
+  for (int j = 0; j < 6; j++) {
+    const int eq = a.eqn[(long)v.conn[2 * e + j / 3] * v.ndf + j % 3];
+    mue[j] = eq >= 0 ? a.mu[eq] : 0.0;
+  }
+  const double f = pdelta_ul14(v, e) / v.L[e] * pdelta_g_dot(v, e, mue);
+  double *re = v.Re + 6L * e;
+#pragma unroll
+  for (int j = 0; j < 6; j++) re[j] = f * (T[0][j] * kv[0] + T[1][j] * kv[3] + T[2][j] * kv[6]);
+}
+
 // The fresh records' dependence on the parameters (Steel02 revertToStart,
 // Steel02.cpp:70-95: epsmax = Fy/E0, epsmin = -Fy/E0).
 __global__ void k_adj_init_records(FrameView v, AdjView a) {
@@ -479,6 +525,13 @@ int launch_adj_elem_b(const FrameView &v, const AdjView &a, cudaStream_t s) {
   const int grid = grid_of(v.ne, kAdjWarps);
   if (v.nb == 3) k_adj_elem_b<3, 2><<<grid, 32 * kAdjWarps, 0, s>>>(v, a);
   else k_adj_elem_b<6, 4><<<grid, 32 * kAdjWarps, 0, s>>>(v, a);
+  return cudaGetLastError() == cudaSuccess ? 0 : XG_ECUDA;
+}
+
+int launch_adj_pdelta(const FrameView &v, const AdjView &a, cudaStream_t s) {
+  if (v.ne == 0) return 0;
+  if (v.nb != 3) return XG_EINVAL;
+  k_adj_pdelta<<<grid_of(v.ne, 128), 128, 0, s>>>(v, a);
   return cudaGetLastError() == cudaSuccess ? 0 : XG_ECUDA;
 }
 

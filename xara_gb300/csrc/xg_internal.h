@@ -412,6 +412,7 @@ struct AdjView {
 };
 int launch_adj_elem_a(const FrameView &v, const AdjView &a, cudaStream_t s);
 int launch_adj_elem_b(const FrameView &v, const AdjView &a, cudaStream_t s);
+int launch_adj_pdelta(const FrameView &v, const AdjView &a, cudaStream_t s);
 int launch_adj_init_records(const FrameView &v, const AdjView &a, cudaStream_t s);
 int launch_adj_objective(int nterm, const int *dof, const double *w, const double *U, double *J,
                          cudaStream_t s);

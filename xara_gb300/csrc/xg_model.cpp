@@ -297,7 +297,8 @@ struct xg_model {
     std::vector<double> ck_time, Jk;        // checkpoint times; the objective's terms
     std::vector<int> elem_uni, fslot, sec_slots;   // sec_slots: [nsec*kAdjSlots] materials
     DBuf<int> dof, d_elem_uni, d_fslot;
-    DBuf<double> w, J, ck, seg, Ub, Vb, Ab, hbar, theta, scr, mu, rhs, tmp, kmu;
+    DBuf<double> w, J, ck, seg, Ub, Vb, Ab, hbar, theta, scr, mu, rhs, tmp, kmu, mu2, rhs2;
+    int pd_solves = 0;                     // solves of the P-Delta fixed point, last sweep
   } adj;
   long steps_since_reset = 0;
   size_t adj_off_fh() const { return 3 * (size_t)nn * ndf; }
@@ -307,6 +308,7 @@ struct xg_model {
   int adjoint_forward(const xg_phase_desc *ph, int N, int K, const xg_objective_desc *obj,
                       double *J);
   int adjoint_backward(double scale, double *grad, int num_uni);
+  int adj_pdelta_refine(const xg::FrameView &fv, const xg::AdjView &av);
   // analysis state
   xg_phase_desc phase{};
   bool have_phase = false;
@@ -1925,8 +1927,6 @@ int xg_model::adjoint_forward(const xg_phase_desc *ph, int N, int K, const xg_ob
   if (N < 1 || K < 1 || !obj || obj->num_terms < 0 || (obj->num_terms > 0 &&
       (!obj->node || !obj->dof || !obj->weight)))
     return fail(XG_EINVAL, "bad adjoint run settings");
-  if (fb_nb == 3 && geom_transf == 1)
-    return fail(XG_EINVAL, "the adjoint covers linear frame transformations");
   if (steps_since_reset != 0 || have_phase)
     return fail(XG_ESTATE, "the adjoint runs from the model's initial state (xg_reset first)");
   // fiber materials: Steel02 without initial stress, Concrete02 or elastic,
@@ -2022,17 +2022,48 @@ int xg_model::adjoint_forward(const xg_phase_desc *ph, int N, int K, const xg_ob
   return 0;
 }
 
+// The 2D P-Delta step's adjoint equation J' mu = rhs, J' = K + C' with K the
+// factored symmetric tangent and C' the per-element terms of k_adj_pdelta:
+// mu <- K^-1 (rhs - C' mu) from the first solve's mu until a solve changes
+// mu by no more than the solver's accuracy.  The iteration contracts as the
+// forward step's Newton iteration on the same tangent does.
+int xg_model::adj_pdelta_refine(const xg::FrameView &fv, const xg::AdjView &av) {
+  cudaStream_t s = stream;
+  constexpr int kMaxSolves = 100;
+  const double tol = system == XG_SYSTEM_PROFILE_SPD ? 1e-14 : std::max(1e-14, 10.0 * rtol);
+  for (int k = 0; k < kMaxSolves; k++) {
+    RET(launch_adj_pdelta(fv, av, s));
+    RET(launch_gather(gr, d_Re.p, d_partial.p, adj.tmp.p, s));
+    RET(launch_sub(neq, adj.rhs.p, adj.tmp.p, adj.rhs2.p, s));
+    RET(solve(adj.rhs2.p, adj.mu2.p, nullptr));
+    adj.pd_solves++;
+    RET(launch_sub(neq, adj.mu2.p, adj.mu.p, adj.tmp.p, s));
+    double dn = 0.0, mn = 0.0;
+    RET(launch_norm2(neq, adj.tmp.p, d_partial.p, d_norm.p, s));
+    RET(read_scalar(d_norm.p, &dn, s));
+    RET(launch_norm2(neq, adj.mu2.p, d_partial.p, d_norm.p, s));
+    RET(read_scalar(d_norm.p, &mn, s));
+    CK(cudaMemcpyAsync(adj.mu.p, adj.mu2.p, (size_t)neq * sizeof(double),
+                       cudaMemcpyDeviceToDevice, s));
+    if (std::sqrt(dn) <= tol * std::sqrt(mn)) return 0;
+  }
+  return fail(XG_ENOCONV, "adjoint: the P-Delta terms' fixed-point iteration did not converge "
+              "in %d solves", kMaxSolves);
+}
+
 // Reverse sweep: segment by segment from the last, the segment's steps are
 // run again from its checkpoint (the kernels are deterministic, so the
 // states repeat bit for bit) and swept backwards.  grad[u*3+k] = scale *
 // dJ/d uni_param[u][k], k = 0..2.  The model ends at the run's last state.
 int xg_model::adjoint_backward(double scale, double *grad, int num_uni) {
   if (!adj.have) return fail(XG_ESTATE, "no adjoint run (xg_adjoint_forward first)");
+  adj.pd_solves = 0;
   if (!grad || num_uni != (int)utype.size()) return fail(XG_EINVAL, "bad gradient buffer");
   cudaStream_t s = stream;
   const size_t nu = (size_t)nn * ndf, nrec = (size_t)fb_nrec * 12;
   const size_t ne1 = std::max(neq, 1);
-  for (auto *b : {&adj.Ub, &adj.Vb, &adj.Ab, &adj.mu, &adj.rhs, &adj.tmp, &adj.kmu}) {
+  for (auto *b : {&adj.Ub, &adj.Vb, &adj.Ab, &adj.mu, &adj.rhs, &adj.tmp, &adj.kmu, &adj.mu2,
+                  &adj.rhs2}) {
     RET(b->alloc(ne1));
     CK(cudaMemsetAsync(b->p, 0, ne1 * sizeof(double), s));
   }
@@ -2097,6 +2128,7 @@ int xg_model::adjoint_backward(double scale, double *grad, int num_uni) {
       RET(launch_gather(gr, d_Re.p, d_partial.p, adj.tmp.p, s));
       RET(launch_adj_rhs(neq, adj.Ub.p, adj.Vb.p, adj.Ab.p, adj.tmp.p, c.c2, c.c3, adj.rhs.p, s));
       RET(solve(adj.rhs.p, adj.mu.p, nullptr));
+      if (fv.pdelta2d) RET(adj_pdelta_refine(fv, av));
       RET(launch_adj_elem_b(fv, av, s));
       if (k0_ready) RET(launch_spmv(neq, d_rowptr.p, d_colidx.p, d_K0vals.p, adj.mu.p, adj.kmu.p, s));
       RET(launch_adj_prev(neq, adj.mu.p, k0_ready ? adj.kmu.p : nullptr, d_meq.p, d_meq_am.p, c,
