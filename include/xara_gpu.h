@@ -445,12 +445,13 @@ int xg_chain_reciprocal_check(int n, const double *d, double *y, double *y_rn);
         sensitivity).  Gradients of J = sum over the steps n = 1..N and the
         terms k of weight_k * u(node_k, dof_k, t_n)^2 with respect to the
         first three parameters of every uniaxial material (Steel02: Fy, E0,
-        b; Concrete02: fc, epsc0, fcu; elastic: E).  Covers force-based
-        frames with linear transformations whose sections use at most four
-        materials (Steel02 without initial stress, Concrete02, elastic),
-        Newmark with alphaM Rayleigh damping (betaK0 as well where an
-        element has a single Steel02 or elastic material) and
-        UniformExcitation, from the model's initial state. ---- */
+        b; Steel01: fy, E0, b; Concrete02: fc, epsc0, fcu; elastic: E).
+        Covers 2D and 3D force-based frames (Linear or PDelta
+        transformations) whose sections use at most four materials (Steel02
+        without initial stress, Steel01, Concrete02, elastic), Newmark with
+        alphaM Rayleigh damping (betaK0 as well where an element has a
+        single Steel02, Steel01 or elastic material), UniformExcitation and
+        nodal load patterns, from the model's initial state. ---- */
 typedef struct xg_objective_desc {
   int num_terms;
   const int *node;            /* node tags */
