@@ -189,6 +189,68 @@ def test_steel01_vjp_against_finite_differences(shift):
     assert checked > 200
 
 
+@pytest.mark.parametrize("shift", [False, True])
+def test_steel01_jvp_against_finite_differences_and_the_vjp(shift):
+    """Steel01's Jacobian-vector product (the DDM's law in forward mode)
+    along the cyclic path of the VJP test: against central differences of the
+    oracle's law in a random direction of (strain, record, parameters), and
+    equal to the vector-Jacobian product through y . (J t) = (J' y) . t."""
+    gpu = _gpu()
+    q = configs.steel01_row(350e6, 200e9, 0.015, *((0.04, 1.0, 0.03, 1.5) if shift
+                                                    else (0.0, 1.0, 0.0, 1.0)))
+    ey = q[0] / q[1]
+    t = np.linspace(0.0, 6.0 * np.pi, 240)
+    strains = ey * (0.5 + 0.05 * t) * np.sin(t) * 3.0
+    rng = np.random.default_rng(7)
+    sc = np.full(12, ey)
+    sc[2] = sc[3] = 1.0
+    sc[9] = q[0]
+    hc = port.uniaxial_init(XG_UNI_STEEL01, q)
+    checked = 0
+    for e in strains:
+        deps = e - hc[10]
+        ht = port.uniaxial_trial(XG_UNI_STEEL01, q, hc, float(e))
+        de = rng.normal() * ey
+        dhc = np.zeros(12)
+        dhc[list(S01_FIELDS)] = rng.normal(size=len(S01_FIELDS)) * sc[list(S01_FIELDS)]
+        dq = rng.normal(size=3) * q[:3]
+        dht = gpu.uniaxial_jvp(XG_UNI_STEEL01, q, hc, float(e), de, dhc, dq)
+        # forward against reverse mode: exact up to rounding
+        yb = np.zeros(12)
+        yb[list(S01_FIELDS)] = rng.normal(size=len(S01_FIELDS)) / sc[list(S01_FIELDS)]
+        hb, sb, qb = gpu.uniaxial_vjp(XG_UNI_STEEL01, q, hc, float(e), yb)
+        lhs = float(yb @ dht)
+        terms = [sb * de, *(hb[f] * dhc[f] for f in S01_FIELDS), *(qb * dq)]
+        rhs = float(sum(terms))
+        assert abs(lhs - rhs) <= 1e-12 * sum(abs(x) for x in terms) + 1e-300, (e, lhs, rhs)
+        # against central differences, away from the law's kinks
+        rel = 1e-7
+        hp, hm = hc + rel * dhc, hc - rel * dhc
+        hp[4] = hm[4] = hc[4]
+        qp, qm = q.copy(), q.copy()
+        qp[:3] += rel * dq
+        qm[:3] -= rel * dq
+        fd = (port.uniaxial_trial(XG_UNI_STEEL01, qp, hp, float(e + rel * de)) -
+              port.uniaxial_trial(XG_UNI_STEEL01, qm, hm, float(e - rel * de))) / (2 * rel)
+        c = hc[9] + q[1] * deps
+        c1, fyomb = q[2] * q[1] * e, q[0] * (1 - q[2])
+        kink = min(abs(c - (c1 + hc[2] * fyomb)), abs(c - (c1 - hc[3] * fyomb))) < 1e-3 * q[0]
+        if abs(deps) > 1e-4 * ey and not kink:
+            for f in S01_FIELDS:
+                assert abs(dht[f] - fd[f]) <= 1e-7 * sc[f], (f, dht[f], fd[f])
+            checked += 1
+        hc = ht
+    assert checked > 200
+    # the elastic law and a refused type
+    de, dq = 1e-4, np.array([2e9, 0.0, 0.0])
+    dht = gpu.uniaxial_jvp(XG_UNI_ELASTIC, np.r_[200e9, np.zeros(11)], np.zeros(12), 1e-3, de,
+                           np.zeros(12), dq)
+    assert dht[9] == pytest.approx(2e9 * 1e-3 + 200e9 * 1e-4) and dht[10] == de
+    with pytest.raises(_gpu().XaraGpuError):
+        gpu.uniaxial_jvp(XG_UNI_STEEL02, configs.steel02_row(), np.zeros(12), 1e-3, de,
+                         np.zeros(12), dq)
+
+
 C02_FIELDS = (0, 1, 9, 10)                       # ecmin, dept, sig, eps
 
 
@@ -582,3 +644,122 @@ def test_adjoint_matches_the_reference_ddm(need_gpu):
     for k in range(3):
         scale = np.abs(ref[:, k]).max()
         assert np.max(np.abs(g[:, k] - ref[:, k])) <= 1e-6 * scale, (k, g[:, k], ref[:, k])
+
+
+# ---------------------------------------------------------------------------
+# GPU: direct differentiation (DDM), forward mode
+# ---------------------------------------------------------------------------
+def _unit_directions(nu):
+    """One direction per (material, parameter 0..2)."""
+    return np.eye(nu * 3).reshape(nu * 3, nu, 3)
+
+
+@pytest.mark.gpu
+def test_ddm_matches_the_reference_ddm_and_the_adjoint(need_gpu):
+    """The device DDM on the massless Steel01 ramp, one direction per member
+    and parameter: against the reference's own DDM (each parameter kind
+    within 1e-6 of its largest entry; the reference solves with the last
+    Newton iteration's factors, the device at the converged state) and
+    against the device adjoint (1e-10: both are exact derivatives of the
+    same discrete path, by independent code)."""
+    gpu = _gpu()
+    fx, desc, phases, obj = _ddm_case()
+    ph = phases[0]
+    nu = len(desc.uni_type)
+    with gpu.DeviceModel(desc) as m:
+        m.set_system(gpu.XG_SYSTEM_PROFILE_SPD)
+        J, dJ = gpu.ddm_forward(m, ph, ph.num_steps, _unit_directions(nu), *obj)
+        m.reset()
+        Ja = gpu.adjoint_forward(m, ph, ph.num_steps, 25, *obj)
+        ga = gpu.adjoint_backward(m)
+    g = dJ.reshape(nu, 3)
+    ref = fx["grad"]
+    assert J == Ja
+    assert abs(J - fx["J"][0]) <= 1e-12 * fx["J"][0]
+    for k in range(3):
+        scale = np.abs(ref[:, k]).max()
+        assert np.max(np.abs(g[:, k] - ref[:, k])) <= 1e-6 * scale, (k, g[:, k], ref[:, k])
+        assert np.max(np.abs(g[:, k] - ga[:, k])) <= 1e-10 * scale, (k, g[:, k], ga[:, k])
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("pga_scale,steps", [(1.0, 40), (6.0, 120)])
+def test_ddm_under_ground_motion_matches_the_adjoint(need_gpu, pga_scale, steps):
+    """Two Steel01 frames with floor masses under their records (the second
+    at six times the record, through yielding and reversals): the DDM along
+    seeded directions equals the adjoint's gradient projected on them (1e-9)
+    and central differences of the forward run (1e-4); at the unscaled
+    record the displacement tangent after the last step against central
+    differences of the final displacements (at six times the record a
+    single displacement sees a fiber change branch within h)."""
+    gpu = _gpu()
+    desc, phases = configs.ddm_steel01_frames_eq(steps=steps, pga_scale=pga_scale, seed=5)
+    ph = phases[0]
+    node, dof, w = _objective(desc)
+    q0 = desc.uni_param.reshape(-1, 12).copy()
+    nu = len(q0)
+    rng = np.random.default_rng(23)
+    dirs = rng.normal(size=(3, nu, 3)) * np.abs(q0[:, :3])
+    with gpu.DeviceModel(desc) as m:
+        J, dJ = gpu.ddm_forward(m, ph, steps, dirs, node, dof, w)
+        du = gpu.ddm_disp_sensitivity(m, 0)
+        rec = m.fiber_records()
+        m.reset()
+        Ja = gpu.adjoint_forward(m, ph, steps, 10, node, dof, w)
+        ga = gpu.adjoint_backward(m)
+        assert J == Ja and np.abs(dJ).min() > 0
+        if pga_scale > 1.0:
+            ey = q0[0, 0] / q0[0, 1]
+            assert (np.abs(rec[:, 10]) > ey).mean() > 0.01
+        for k in range(3):
+            assert dJ[k] == pytest.approx(float((ga * dirs[k]).sum()), rel=1e-9), k
+        h = 1e-6
+        m.reset()
+        gpu.set_uniaxial_params(m, np.c_[q0[:, :3] + h * dirs[0], q0[:, 3:]])
+        Jp = gpu.adjoint_forward(m, ph, steps, steps, node, dof, w)
+        up, _ = m.disp()
+        m.reset()
+        gpu.set_uniaxial_params(m, np.c_[q0[:, :3] - h * dirs[0], q0[:, 3:]])
+        Jm = gpu.adjoint_forward(m, ph, steps, steps, node, dof, w)
+        um, _ = m.disp()
+    assert dJ[0] == pytest.approx((Jp - Jm) / (2 * h), rel=1e-4)
+    fdu = (np.asarray(up) - np.asarray(um)).reshape(du.shape) / (2 * h)
+    if pga_scale == 1.0:
+        assert np.abs(du - fdu).max() <= 1e-4 * np.abs(fdu).max()
+
+
+@pytest.mark.gpu
+def test_ddm_3d_frame_and_refusals(need_gpu):
+    """A 3D frame (the RC frame's sections with Steel01 fibers) under a
+    ground motion: DDM against the adjoint along seeded directions (1e-9);
+    Steel02 fibers and betaK0 damping are refused."""
+    gpu = _gpu()
+    base, phases = configs.adjoint_rc_frame_3d(steps=40, pga_scale=3.0)
+    nu = len(base.uni_type)
+    rows = np.stack([configs.steel01_row(fy=30e6, E=30e9, b=0.01)] * nu)
+    rows[-1] = configs.steel01_row(fy=420e6, E=200e9, b=0.01)
+    desc = configs._with_geometry(base, uni_type=np.full(nu, XG_UNI_STEEL01), uni_param=rows)
+    ph = phases[0]
+    node, dof, w = _objective(base)
+    rng = np.random.default_rng(29)
+    dirs = rng.normal(size=(2, nu, 3)) * np.abs(rows[:, :3])
+    with gpu.DeviceModel(desc) as m:
+        J, dJ = gpu.ddm_forward(m, ph, 40, dirs, node, dof, w)
+        rec = m.fiber_records()
+        m.reset()
+        Ja = gpu.adjoint_forward(m, ph, 40, 10, node, dof, w)
+        ga = gpu.adjoint_backward(m)
+    assert J == Ja
+    assert (np.abs(rec[:, 10]) > 1e-3).mean() > 0.01          # some fibers yield
+    for k in range(2):
+        assert dJ[k] == pytest.approx(float((ga * dirs[k]).sum()), rel=1e-9), k
+    d2, p2 = configs.adjoint_frames(n_frames=1, steps=5, seed=3)
+    with gpu.DeviceModel(d2) as m:
+        with pytest.raises(gpu.XaraGpuError, match="Steel01"):
+            gpu.ddm_forward(m, p2[0], 5, np.zeros((1, len(d2.uni_type), 3)),
+                            *_objective(d2))
+    d3, p3 = configs.ddm_steel01_frames_eq(n_frames=1, steps=5, seed=3)
+    p3[0].beta_k_init_elem = np.full(len(d3.arrays["elem_tag"]), 1e-3)
+    with gpu.DeviceModel(d3) as m:
+        with pytest.raises(gpu.XaraGpuError, match="betaK0"):
+            gpu.ddm_forward(m, p3[0], 5, np.zeros((1, len(d3.uni_type), 3)), *_objective(d3))

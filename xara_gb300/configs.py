@@ -823,3 +823,21 @@ def adjoint_rc_frame_3d(bays_x=1, bays_y=1, stories=2, steps=40, dt=0.01, seed=0
                     "ground motion", obj_node=np.array([desc.meta["roof"]], np.int32),
                     obj_dof=np.zeros(1, np.int32), obj_weight=np.array([1.0 / (H * H)]))
     return out, [quake]
+
+
+def ddm_steel01_frames_eq(n_frames=2, steps=40, dt=0.01, seed=0, pga_scale=1.0):
+    """The frames of :func:`adjoint_frames` with their members' Steel02
+    replaced by Steel01 of the same fy, E and b (the law whose stress
+    sensitivity the reference's DDM has) and mass-proportional Rayleigh
+    damping only: a transient, path-dependent case for the direct
+    differentiation.  Same objective terms."""
+    desc, phases = adjoint_frames(n_frames=n_frames, steps=steps, dt=dt, seed=seed,
+                                  pga_scale=pga_scale)
+    uni = desc.uni_param.reshape(-1, XG_UNI_NPARAM)
+    rows = np.stack([steel01_row(fy=r[0], E=r[1], b=r[2]) for r in uni])
+    out = _with_geometry(desc, uni_type=np.full(len(rows), XG_UNI_STEEL01), uni_param=rows)
+    ph = phases[0]
+    ph.beta_k_init_elem = np.zeros(len(desc.arrays["elem_tag"]))
+    ph.kw["beta_k_init"] = 0.0
+    out.meta["workload"] = f"{n_frames} 2D steel frames, one Steel01 per member"
+    return out, [ph]

@@ -508,6 +508,239 @@ __global__ void k_adj_prev(int neq, const double *mu, const double *kmu, const d
   Ab[i] = -(c.a4 * m + c.a2 * (ma + km)) + c.a2 * vb + c.a4 * ab;
 }
 
+// ---------------------------------------------------------------------------
+// Direct differentiation (DDM), forward mode along one parameter direction:
+// the reference's Newmark::computeSensitivities (Newmark.cpp:904-959), with
+// ForceBeamColumn2d's basic-force sensitivity at fixed deformation and its
+// commitSensitivity (ForceBeamColumn2d.cpp:2890-3007) restated on the
+// element equations of the adjoint above:
+//   dSe = kv (dv + z),   z = sum_s w_s L b_s' fs_s q_s,
+//   de_s = fs_s (b_s dSe - q_s),   q_s = sum_f A_f a_f dsigma_f (strain fixed)
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ void fiber_jvp(int type, const double *q, const double *hc,
+                                          double strain, double dstrain, const double *dhc,
+                                          const double *dq, double *dht) {
+  if (type == XG_UNI_STEEL01) steel01_jvp(q, hc, strain, dstrain, dhc, dq, dht);
+  else elastic_jvp(q, strain, dstrain, dq, dht);
+}
+
+// Pass 1 (warp per element, a lane group per section): every fiber's stress
+// tangent at fixed strain gives q_s; z and the conditional force tangent
+// T' kv z (written to the element force scratch for the residual's gather).
+template <int NB, int ORD>
+__global__ void __launch_bounds__(32 * kAdjWarps) k_ddm_cond(FrameView v, DdmView d) {
+  constexpr int NU = NB == 3 ? 6 : 12;
+  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int e = blockIdx.x * kAdjWarps + w;
+  if (e >= v.ne) return;
+  const int nip = v.nip;
+  const double *st = v.st + (long)e * stride_of(nip);
+  const int sec = v.sec[e];
+  const int f0 = v.sec_fstart[sec], nf = v.sec_fstart[sec + 1] - f0;
+  const double ybar = v.ybar[sec], zbar = ORD == 4 ? v.zbar[sec] : 0.0;
+  const double L = v.L[e];
+  const long fbase = v.foff[e];
+  __shared__ double tsec_all[kAdjWarps][kAdjMaxIp][4];
+  double(*tsec)[4] = tsec_all[w];
+  constexpr int kRow[6] = {0, 1, 1, 2, 2, 3};
+  const int G = 32 / nip;
+  int P2 = 1;
+  while (P2 < G) P2 <<= 1;
+  const int gip = lane / G, rank = lane % G;
+  const bool on = gip < nip;
+  {
+    const int ip = on ? gip : nip - 1;
+    double vsec[ORD];
+#pragma unroll
+    for (int r = 0; r < ORD; r++) vsec[r] = st[42 + ip * 4 + r];
+    double q0 = 0.0, q1 = 0.0, q2 = 0.0;
+    const long rec0 = (fbase + (long)ip * nf) * 12;
+    for (int fi = rank; on && fi < nf; fi += G) {
+      const int kf = f0 + fi;
+      const double y = v.fy[kf] - ybar, A = v.fA[kf];
+      double strain = vsec[0] - y * vsec[1];
+      double zz = 0.0;
+      if (ORD == 4) {
+        zz = v.fz[kf] - zbar;
+        strain += zz * vsec[2];
+      }
+      const int u = v.fmat[kf];
+      double dht[12];
+      fiber_jvp(v.utype[u], v.uparam + (long)u * XG_UNI_NPARAM, d.fh_prev + rec0 + 12L * fi,
+                strain, 0.0, d.dh + rec0 + 12L * fi, d.dth + 3L * u, dht);
+      const double ds = A * dht[9];
+      q0 += ds;
+      q1 -= y * ds;
+      if (ORD == 4) q2 += zz * ds;
+    }
+    double qs[ORD];
+    qs[0] = group_sum_adj(q0, rank, G, P2);
+    qs[1] = group_sum_adj(q1, rank, G, P2);
+    if (ORD == 4) { qs[2] = group_sum_adj(q2, rank, G, P2); qs[3] = 0.0; }
+    if (on && rank == 0) {
+      const double *fs = st + 42 + nip * 4 + ip * 16;
+#pragma unroll
+      for (int r = 0; r < ORD; r++) {
+        d.q[((long)e * nip + ip) * 4 + r] = qs[r];
+        double t = 0.0;
+#pragma unroll
+        for (int k = 0; k < ORD; k++) t += fs[r * ORD + k] * qs[k];
+        tsec[ip][r] = t;
+      }
+    }
+  }
+  __syncwarp();
+  if (lane != 0) return;
+  double z[NB];
+#pragma unroll
+  for (int c = 0; c < NB; c++) z[c] = 0.0;
+  for (int ip = 0; ip < nip; ip++) {
+    const double xL = v.xi[ip], xL1 = xL - 1.0, wtL = v.wt[ip] * L;
+    const double ca[6] = {1.0, xL1, xL, xL1, xL, 1.0};
+#pragma unroll
+    for (int c = 0; c < NB; c++) z[c] += wtL * ca[c] * tsec[ip][kRow[c]];
+  }
+  const double *kv = st + 6;
+  double dS[NB];
+#pragma unroll
+  for (int i = 0; i < NB; i++) {
+    double t = 0.0;
+#pragma unroll
+    for (int k = 0; k < NB; k++) t += kv[i * NB + k] * z[k];
+    dS[i] = t;
+    d.z[6L * e + i] = z[i];
+  }
+  double T[NB][NU];
+  basic_T<NB>(v, e, T);
+  double *re = v.Re + (long)e * NU;
+#pragma unroll
+  for (int j = 0; j < NU; j++) {
+    double t = 0.0;
+#pragma unroll
+    for (int k = 0; k < NB; k++) t += T[k][j] * dS[k];
+    re[j] = t;
+  }
+}
+
+// Pass 2 (warp per element), after the step's tangent solve: dv = T dU_e
+// gives dSe, each section's de_s and each fiber's strain tangent, and the
+// law in forward mode the record tangents after the step (in place).
+template <int NB, int ORD>
+__global__ void __launch_bounds__(32 * kAdjWarps) k_ddm_commit(FrameView v, DdmView d) {
+  constexpr int NU = NB == 3 ? 6 : 12;
+  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int e = blockIdx.x * kAdjWarps + w;
+  if (e >= v.ne) return;
+  const int nip = v.nip, ndf = v.ndf;
+  const double *st = v.st + (long)e * stride_of(nip);
+  const int sec = v.sec[e];
+  const int f0 = v.sec_fstart[sec], nf = v.sec_fstart[sec + 1] - f0;
+  const double ybar = v.ybar[sec], zbar = ORD == 4 ? v.zbar[sec] : 0.0;
+  const long fbase = v.foff[e];
+  double T[NB][NU];
+  basic_T<NB>(v, e, T);
+  double due[NU];
+  const int nd = NU / 2;
+#pragma unroll
+  for (int j = 0; j < NU; j++) {
+    const int eq = d.eqn[(long)v.conn[2 * e + j / nd] * ndf + (j % nd)];
+    due[j] = eq >= 0 ? d.dU[eq] : 0.0;
+  }
+  const double *kv = st + 6;
+  double dvz[NB], dS[NB];
+#pragma unroll
+  for (int i = 0; i < NB; i++) {
+    double t = d.z[6L * e + i];
+#pragma unroll
+    for (int j = 0; j < NU; j++) t += T[i][j] * due[j];
+    dvz[i] = t;
+  }
+#pragma unroll
+  for (int i = 0; i < NB; i++) {
+    double t = 0.0;
+#pragma unroll
+    for (int k = 0; k < NB; k++) t += kv[i * NB + k] * dvz[k];
+    dS[i] = t;
+  }
+  constexpr int kRow[6] = {0, 1, 1, 2, 2, 3};
+  const int G = 32 / nip;
+  const int gip = lane / G, rank = lane % G;
+  if (gip >= nip) return;
+  const int ip = gip;
+  const double xL = v.xi[ip], xL1 = xL - 1.0;
+  const double ca[6] = {1.0, xL1, xL, xL1, xL, 1.0};
+  double g[ORD];
+#pragma unroll
+  for (int r = 0; r < ORD; r++) g[r] = -d.q[((long)e * nip + ip) * 4 + r];
+#pragma unroll
+  for (int c = 0; c < NB; c++) g[kRow[c]] += ca[c] * dS[c];
+  const double *fs = st + 42 + nip * 4 + ip * 16;
+  double de[ORD], vsec[ORD];
+#pragma unroll
+  for (int r = 0; r < ORD; r++) {
+    double t = 0.0;
+#pragma unroll
+    for (int k = 0; k < ORD; k++) t += fs[r * ORD + k] * g[k];
+    de[r] = t;
+    vsec[r] = st[42 + ip * 4 + r];
+  }
+  const long rec0 = (fbase + (long)ip * nf) * 12;
+  for (int fi = rank; fi < nf; fi += G) {
+    const int kf = f0 + fi;
+    const double y = v.fy[kf] - ybar;
+    double strain = vsec[0] - y * vsec[1], dstrain = de[0] - y * de[1];
+    if (ORD == 4) {
+      const double zz = v.fz[kf] - zbar;
+      strain += zz * vsec[2];
+      dstrain += zz * de[2];
+    }
+    const int u = v.fmat[kf];
+    double *dhr = d.dh + rec0 + 12L * fi;
+    double dhc[12], dht[12];
+#pragma unroll
+    for (int k = 0; k < 12; k++) dhc[k] = dhr[k];
+    fiber_jvp(v.utype[u], v.uparam + (long)u * XG_UNI_NPARAM, d.fh_prev + rec0 + 12L * fi,
+              strain, dstrain, dhc, d.dth + 3L * u, dht);
+#pragma unroll
+    for (int k = 0; k < 12; k++) dhr[k] = dht[k];
+  }
+}
+
+// rhs = -dP_cond + M (c3 dU' - a3 dV' - a4 dA') + alphaM M (c2 dU' - a1 dV' - a2 dA'):
+// the derivative of the step's unbalance at fixed displacement, with the
+// Newmark relations A = c3 (U - U') + a3 V' + a4 A', V = c2 (U - U') + a1 V' + a2 A'
+__global__ void k_ddm_rhs(int neq, const double *dPc, const double *dU, const double *dV,
+                          const double *dA, const double *meq, const double *meq_am,
+                          NewmarkCoef c, double *rhs) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= neq) return;
+  rhs[i] = -dPc[i] + meq[i] * (c.c3 * dU[i] - c.a3 * dV[i] - c.a4 * dA[i]) +
+           meq_am[i] * (c.c2 * dU[i] - c.a1 * dV[i] - c.a2 * dA[i]);
+}
+
+// the step's displacement tangent x and the Newmark relations give dA, dV
+__global__ void k_ddm_update(int neq, const double *x, NewmarkCoef c, double *dU, double *dV,
+                             double *dA) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= neq) return;
+  const double du = x[i] - dU[i], v = dV[i], a = dA[i];
+  dA[i] = c.c3 * du + c.a3 * v + c.a4 * a;
+  dV[i] = c.c2 * du + c.a1 * v + c.a2 * a;
+  dU[i] = x[i];
+}
+
+// dJ += sum over the terms (in order) of 2 w_k U[dof_k] dU[eqn[dof_k]]
+__global__ void k_ddm_objective(int nterm, const int *dof, const double *w, const int *eqn,
+                                const double *U, const double *dU, double *dJ) {
+  if (blockIdx.x != 0 || threadIdx.x != 0) return;
+  double s = 0.0;
+  for (int k = 0; k < nterm; k++) {
+    const int eq = eqn[dof[k]];
+    if (eq >= 0) s += 2.0 * w[k] * U[dof[k]] * dU[eq];
+  }
+  *dJ += s;
+}
+
 inline int grid_of(long n, int b) { return (int)((n + b - 1) / b); }
 
 }  // namespace
@@ -532,6 +765,44 @@ int launch_adj_pdelta(const FrameView &v, const AdjView &a, cudaStream_t s) {
   if (v.ne == 0) return 0;
   if (v.nb != 3) return XG_EINVAL;
   k_adj_pdelta<<<grid_of(v.ne, 128), 128, 0, s>>>(v, a);
+  return cudaGetLastError() == cudaSuccess ? 0 : XG_ECUDA;
+}
+
+int launch_ddm_cond(const FrameView &v, const DdmView &d, cudaStream_t s) {
+  if (v.ne == 0) return 0;
+  const int grid = grid_of(v.ne, kAdjWarps);
+  if (v.nb == 3) k_ddm_cond<3, 2><<<grid, 32 * kAdjWarps, 0, s>>>(v, d);
+  else k_ddm_cond<6, 4><<<grid, 32 * kAdjWarps, 0, s>>>(v, d);
+  return cudaGetLastError() == cudaSuccess ? 0 : XG_ECUDA;
+}
+
+int launch_ddm_commit(const FrameView &v, const DdmView &d, cudaStream_t s) {
+  if (v.ne == 0) return 0;
+  const int grid = grid_of(v.ne, kAdjWarps);
+  if (v.nb == 3) k_ddm_commit<3, 2><<<grid, 32 * kAdjWarps, 0, s>>>(v, d);
+  else k_ddm_commit<6, 4><<<grid, 32 * kAdjWarps, 0, s>>>(v, d);
+  return cudaGetLastError() == cudaSuccess ? 0 : XG_ECUDA;
+}
+
+int launch_ddm_rhs(int neq, const double *dPc, const double *dU, const double *dV,
+                   const double *dA, const double *meq, const double *meq_am,
+                   const NewmarkCoef &c, double *rhs, cudaStream_t s) {
+  if (neq == 0) return 0;
+  k_ddm_rhs<<<grid_of(neq, 256), 256, 0, s>>>(neq, dPc, dU, dV, dA, meq, meq_am, c, rhs);
+  return cudaGetLastError() == cudaSuccess ? 0 : XG_ECUDA;
+}
+
+int launch_ddm_update(int neq, const double *x, const NewmarkCoef &c, double *dU, double *dV,
+                      double *dA, cudaStream_t s) {
+  if (neq == 0) return 0;
+  k_ddm_update<<<grid_of(neq, 256), 256, 0, s>>>(neq, x, c, dU, dV, dA);
+  return cudaGetLastError() == cudaSuccess ? 0 : XG_ECUDA;
+}
+
+int launch_ddm_objective(int nterm, const int *dof, const double *w, const int *eqn,
+                         const double *U, const double *dU, double *dJ, cudaStream_t s) {
+  if (nterm == 0) return 0;
+  k_ddm_objective<<<1, 32, 0, s>>>(nterm, dof, w, eqn, U, dU, dJ);
   return cudaGetLastError() == cudaSuccess ? 0 : XG_ECUDA;
 }
 
@@ -571,6 +842,18 @@ int launch_adj_prev(int neq, const double *mu, const double *kmu, const double *
 }
 
 }  // namespace xg
+
+// Host entry for the derivative tests: the Jacobian-vector product of one
+// material point (no device work).
+extern "C" int xg_uniaxial_jvp(int type, const double *q, const double *hc, double strain,
+                               double dstrain, const double *dhc, const double *dq,
+                               double *dht) {
+  if (!q || !hc || !dhc || !dq || !dht) return XG_EINVAL;
+  if (type == XG_UNI_STEEL01) xg::steel01_jvp(q, hc, strain, dstrain, dhc, dq, dht);
+  else if (type == XG_UNI_ELASTIC) xg::elastic_jvp(q, strain, dstrain, dq, dht);
+  else return XG_EINVAL;
+  return 0;
+}
 
 // Host entry for the derivative tests: the vector-Jacobian product of one
 // material point (no device work).

@@ -413,6 +413,28 @@ struct AdjView {
 int launch_adj_elem_a(const FrameView &v, const AdjView &a, cudaStream_t s);
 int launch_adj_elem_b(const FrameView &v, const AdjView &a, cudaStream_t s);
 int launch_adj_pdelta(const FrameView &v, const AdjView &a, cudaStream_t s);
+
+// Direct differentiation (DDM) of a Newmark run along one direction in the
+// materials' parameters, after each converged step (the element state in the
+// FrameView is the step's converged one)
+struct DdmView {
+  const double *fh_prev;      // committed fiber records before the step [nrec*12]
+  double *dh;                 // [nrec*12] record tangents: before the step in, after it out
+  const double *dth;          // [num_uni*3] the direction's tangent of parameters 0-2
+  double *q;                  // [ne*nip*4] section force tangents at fixed deformation
+  double *z;                  // [ne*6] sum over sections of w L b' fs q
+  const int *eqn;             // [nn*ndf]
+  const double *dU;           // [neq] the step's displacement tangent (pass 2)
+};
+int launch_ddm_cond(const FrameView &v, const DdmView &d, cudaStream_t s);
+int launch_ddm_commit(const FrameView &v, const DdmView &d, cudaStream_t s);
+int launch_ddm_rhs(int neq, const double *dPc, const double *dU, const double *dV,
+                   const double *dA, const double *meq, const double *meq_am,
+                   const NewmarkCoef &c, double *rhs, cudaStream_t s);
+int launch_ddm_update(int neq, const double *x, const NewmarkCoef &c, double *dU, double *dV,
+                      double *dA, cudaStream_t s);
+int launch_ddm_objective(int nterm, const int *dof, const double *w, const int *eqn,
+                         const double *U, const double *dU, double *dJ, cudaStream_t s);
 int launch_adj_init_records(const FrameView &v, const AdjView &a, cudaStream_t s);
 int launch_adj_objective(int nterm, const int *dof, const double *w, const double *U, double *J,
                          cudaStream_t s);

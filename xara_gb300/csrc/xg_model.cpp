@@ -309,6 +309,18 @@ struct xg_model {
                       double *J);
   int adjoint_backward(double scale, double *grad, int num_uni);
   int adj_pdelta_refine(const xg::FrameView &fv, const xg::AdjView &av);
+  // direct differentiation (xg_ddm_forward): per direction the displacement,
+  // velocity and acceleration tangents [nd*neq] and the record tangents
+  // [nd*nrec*12]; the committed records before the running step
+  struct DdmRun {
+    bool have = false;
+    int nd = 0, nterm = 0;
+    std::vector<double> dJ;
+    DBuf<int> dof;
+    DBuf<double> w, J, dJd, dth, dU, dV, dA, dh, fh_prev, q, z, rhs, x;
+  } ddm;
+  int ddm_forward(const xg_phase_desc *ph, int N, int nd, const double *dtheta,
+                  const xg_objective_desc *obj, double *J, double *dJ);
   // analysis state
   xg_phase_desc phase{};
   bool have_phase = false;
@@ -2155,6 +2167,120 @@ int xg_model::adjoint_backward(double scale, double *grad, int num_uni) {
   return element_state(true);
 }
 
+// Newmark run of num_steps from the initial state with the direct
+// differentiation after every converged step (Newmark::computeSensitivities,
+// Newmark.cpp:904-959, one direction per parameter combination):
+//   K_eff dU = -dP|_U + M (c3 dU' - a3 dV' - a4 dA') + alphaM M (c2 dU' - a1 dV' - a2 dA')
+// with K_eff formed again at the converged state (the reference solves with
+// the last Newton iteration's factors), then the record tangents committed.
+// J as xg_adjoint_forward; dJ[k] = dJ/dtheta along direction k.
+int xg_model::ddm_forward(const xg_phase_desc *ph, int N, int nd, const double *dtheta,
+                          const xg_objective_desc *obj, double *J, double *dJ) {
+  ddm.have = false;
+  if (!frames()) return fail(XG_EINVAL, "the DDM covers force-based frame models");
+  if (!ph || ph->integrator != XG_INT_NEWMARK) return fail(XG_EINVAL, "the DDM covers Newmark runs");
+  if (N < 1 || nd < 1 || !dtheta || !obj || obj->num_terms < 0 ||
+      (obj->num_terms > 0 && (!obj->node || !obj->dof || !obj->weight)))
+    return fail(XG_EINVAL, "bad DDM run settings");
+  if (fb_nb == 3 && geom_transf == 1)
+    return fail(XG_EINVAL, "the DDM covers linear frame transformations in 2D");
+  if (steps_since_reset != 0 || have_phase)
+    return fail(XG_ESTATE, "the DDM runs from the model's initial state (xg_reset first)");
+  for (size_t u = 0; u < utype.size(); u++)
+    if (utype[u] != XG_UNI_STEEL01 && utype[u] != XG_UNI_ELASTIC)
+      return fail(XG_EINVAL, "the DDM covers Steel01 and elastic fibers (material %d)", (int)u);
+  bool bk0 = ph->beta_k_init != 0.0;
+  if (ph->beta_k_init_elem)
+    for (int e = 0; e < ne; e++) bk0 = bk0 || ph->beta_k_init_elem[e] != 0.0;
+  if (bk0) return fail(XG_EINVAL, "the DDM covers alphaM Rayleigh damping only (no betaK0)");
+  std::vector<int> dofs(obj->num_terms);
+  for (int k = 0; k < obj->num_terms; k++) {
+    auto it = std::lower_bound(node_tag.begin(), node_tag.end(), obj->node[k]);
+    if (it == node_tag.end() || *it != obj->node[k] || obj->dof[k] < 0 || obj->dof[k] >= ndf)
+      return fail(XG_EINVAL, "objective term %d: bad node or dof", k);
+    dofs[k] = (int)(it - node_tag.begin()) * ndf + obj->dof[k];
+  }
+  RET(xg_analysis_set_phase(this, ph));
+  cudaStream_t s = stream;
+  const size_t ne1 = std::max(neq, 1), nrec = std::max<size_t>((size_t)fb_nrec * 12, 1);
+  const size_t nuni3 = utype.size() * 3;
+  ddm.nd = nd;
+  ddm.nterm = obj->num_terms;
+  for (auto *b : {&ddm.dU, &ddm.dV, &ddm.dA}) {
+    RET(b->alloc((size_t)nd * ne1));
+    CK(cudaMemsetAsync(b->p, 0, (size_t)nd * ne1 * sizeof(double), s));
+  }
+  RET(ddm.dh.alloc((size_t)nd * nrec));
+  CK(cudaMemsetAsync(ddm.dh.p, 0, (size_t)nd * nrec * sizeof(double), s));   // fresh records
+  RET(ddm.dth.upload(dtheta, (size_t)nd * nuni3, s));
+  RET(ddm.fh_prev.alloc(nrec));
+  RET(ddm.q.alloc(std::max<size_t>((size_t)ne * fb_nip * 4, 1)));
+  RET(ddm.z.alloc(std::max<size_t>((size_t)ne * 6, 1)));
+  RET(ddm.rhs.alloc(ne1));
+  RET(ddm.x.alloc(ne1));
+  RET(ddm.dof.upload(dofs.data(), std::max<size_t>(dofs.size(), 1), s));
+  std::vector<double> wv(obj->weight, obj->weight + obj->num_terms);
+  wv.resize(std::max<size_t>(wv.size(), 1));
+  RET(ddm.w.upload(wv.data(), wv.size(), s));
+  RET(ddm.J.alloc(std::max(ddm.nterm, 1)));
+  CK(cudaMemsetAsync(ddm.J.p, 0, std::max(ddm.nterm, 1) * sizeof(double), s));
+  RET(ddm.dJd.alloc(nd));
+  CK(cudaMemsetAsync(ddm.dJd.p, 0, nd * sizeof(double), s));
+  const double dt = phase.dt, gam = phase.gamma, bet = phase.beta;
+  NewmarkCoef c{};
+  c.c2 = gam / (bet * dt);
+  c.c3 = 1.0 / (bet * dt * dt);
+  c.a1 = 1.0 - gam / bet;
+  c.a2 = dt * (1.0 - 0.5 * gam / bet);
+  c.a3 = -1.0 / (bet * dt);
+  c.a4 = 1.0 - 0.5 / bet;
+  for (int n = 1; n <= N; n++) {
+    CK(cudaMemcpyAsync(ddm.fh_prev.p, d_fh_c.p, (size_t)fb_nrec * 12 * sizeof(double),
+                       cudaMemcpyDeviceToDevice, s));
+    RET(step(nullptr));
+    phase_steps_done++;
+    RET(launch_adj_objective(ddm.nterm, ddm.dof.p, ddm.w.p, d_Uc.p, ddm.J.p, s));
+    // the effective tangent at the converged state
+    FrameView fv = fview();
+    RET(launch_fbc_assemble(fv, s));
+    RET(launch_gather(gk, d_Ke.p, d_partial.p, d_vals.p, s));
+    RET(launch_dyn_tangent(dview(), d_vals.p, d_K0vals.p, 1.0, 0.0, c.c2, c.c3, s));
+    blocks_factored = false;
+    prof_factored = false;
+    for (int k = 0; k < nd; k++) {
+      DdmView dv{};
+      dv.fh_prev = ddm.fh_prev.p;
+      dv.dh = ddm.dh.p + (size_t)k * nrec;
+      dv.dth = ddm.dth.p + (size_t)k * nuni3;
+      dv.q = ddm.q.p;
+      dv.z = ddm.z.p;
+      dv.eqn = d_eqn.p;
+      double *dUk = ddm.dU.p + (size_t)k * ne1, *dVk = ddm.dV.p + (size_t)k * ne1,
+             *dAk = ddm.dA.p + (size_t)k * ne1;
+      RET(launch_ddm_cond(fv, dv, s));
+      RET(launch_gather(gr, d_Re.p, d_partial.p, ddm.x.p, s));
+      RET(launch_ddm_rhs(neq, ddm.x.p, dUk, dVk, dAk, d_meq.p, d_meq_am.p, c, ddm.rhs.p, s));
+      RET(solve(ddm.rhs.p, ddm.x.p, nullptr));
+      RET(launch_ddm_update(neq, ddm.x.p, c, dUk, dVk, dAk, s));
+      dv.dU = dUk;
+      RET(launch_ddm_commit(fv, dv, s));
+      RET(launch_ddm_objective(ddm.nterm, ddm.dof.p, ddm.w.p, d_eqn.p, d_Uc.p, dUk,
+                               ddm.dJd.p + k, s));
+    }
+  }
+  std::vector<double> Jk(std::max(ddm.nterm, 1));
+  ddm.dJ.assign(nd, 0.0);
+  CK(cudaMemcpyAsync(Jk.data(), ddm.J.p, Jk.size() * sizeof(double), cudaMemcpyDeviceToHost, s));
+  CK(cudaMemcpyAsync(ddm.dJ.data(), ddm.dJd.p, nd * sizeof(double), cudaMemcpyDeviceToHost, s));
+  CK(cudaStreamSynchronize(s));
+  double Jh = 0.0;
+  for (int k = 0; k < ddm.nterm; k++) Jh += Jk[k];
+  if (J) *J = Jh;
+  if (dJ) std::copy(ddm.dJ.begin(), ddm.dJ.end(), dJ);
+  ddm.have = true;
+  return 0;
+}
+
 // ---------------------------------------------------------------------------
 // C ABI
 // ---------------------------------------------------------------------------
@@ -2861,6 +2987,27 @@ int xg_adjoint_backward(xg_model *m, double scale, double *grad, int num_uni) {
   if (!m) return fail(XG_EINVAL, "null model");
   g_err.clear();
   return m->adjoint_backward(scale, grad, num_uni);
+}
+
+int xg_ddm_forward(xg_model *m, const xg_phase_desc *ph, int num_steps, int num_dir,
+                   const double *dtheta, const xg_objective_desc *obj, double *J, double *dJ) {
+  g_err.clear();
+  if (!m) return fail(XG_EINVAL, "null model");
+  return m->ddm_forward(ph, num_steps, num_dir, dtheta, obj, J, dJ);
+}
+
+int xg_ddm_disp_sensitivity(const xg_model *m, int dir, double *out) {
+  g_err.clear();
+  if (!m || !out) return fail(XG_EINVAL, "null argument");
+  if (!m->ddm.have) return fail(XG_ESTATE, "no DDM run (xg_ddm_forward first)");
+  if (dir < 0 || dir >= m->ddm.nd) return fail(XG_EINVAL, "bad direction %d", dir);
+  std::vector<double> x(std::max(m->neq, 1));
+  const size_t ne1 = std::max(m->neq, 1);
+  if (cudaMemcpy(x.data(), m->ddm.dU.p + (size_t)dir * ne1, ne1 * sizeof(double),
+                 cudaMemcpyDeviceToHost) != cudaSuccess)
+    return fail(XG_ECUDA, "copy failed");
+  for (size_t a = 0; a < m->eqn.size(); a++) out[a] = m->eqn[a] >= 0 ? x[m->eqn[a]] : 0.0;
+  return 0;
 }
 
 }  // extern "C"

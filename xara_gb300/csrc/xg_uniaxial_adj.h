@@ -1,10 +1,14 @@
-// xg_uniaxial_adj.h -- reverse-mode derivatives of the uniaxial laws the
-// adjoint supports, for host and device.
+// xg_uniaxial_adj.h -- derivatives of the uniaxial laws, for host and
+// device: reverse mode for the adjoint, forward mode for the direct
+// differentiation (DDM).
 //
 // A law maps (trial strain, committed record, parameters) to the trial
 // record.  The vector-Jacobian product takes the adjoint of the trial
 // record's continuous fields and returns the adjoints of the strain, of the
-// committed record's fields and of the first three parameters.
+// committed record's fields and of the first three parameters.  The
+// Jacobian-vector product takes the tangents of the strain, of the committed
+// record's continuous fields and of the first three parameters and returns
+// the tangent of the trial record's continuous fields.
 //
 // Record layout (12 doubles): Steel02 0 epsmin 1 epsmax 2 epspl 3 epss0
 // 4 sigs0 5 epsr 6 sigr 7 kon; Concrete02 0 ecmin 1 dept; Steel01
@@ -474,6 +478,67 @@ XG_HD inline void steel01_vjp(const double *q, const double *hc, double strain, 
   hb[9] = gCstress; hb[10] = gCstrain;
   *sb = gEps;
   qb[0] = gFy; qb[1] = gE0; qb[2] = gB;
+}
+
+// Steel01::setTrialStrain / determineTrialState (Steel01.cpp:68-92,
+// 124-198) in forward mode, written from the law itself (the reference's own
+// DDM, Steel01::getStressSensitivity / commitSensitivity, Steel01.cpp:
+// 552-660, is the quantity it is checked against).  The branch (elastic
+// predictor, upper or lower bound, a load reversal) is the primal's; the
+// bounds use the committed shifts; a reversal sets the new shift from the
+// extreme strains.  dq = d(fy, E0, b); dht receives fields 0-3, 9, 10.
+XG_HD inline void steel01_jvp(const double *q, const double *hc, double strain, double dstrain,
+                              const double *dhc, const double *dq, double *dht) {
+  const double fy = q[0], E0 = q[1], b = q[2], a1 = q[3], a2 = q[4], a3 = q[5], a4 = q[6];
+  const double dfy = dq[0], dE0 = dq[1], db = dq[2];
+  for (int k = 0; k < 12; k++) dht[k] = 0.0;
+  const double Cstrain = hc[10], Cstress = hc[9];
+  const double dStrain = strain - Cstrain;
+  if (!(fabs(dStrain) > DBL_EPSILON)) {
+    // the committed state is the trial state, strain included
+    dht[0] = dhc[0]; dht[1] = dhc[1]; dht[2] = dhc[2]; dht[3] = dhc[3];
+    dht[9] = dhc[9]; dht[10] = dhc[10];
+    return;
+  }
+  const double fyomb = fy * (1.0 - b), dfyomb = dfy * (1.0 - b) - fy * db;
+  const double epsy = fy / E0, depsy = dfy / E0 - fy * dE0 / (E0 * E0);
+  const double c1 = b * E0 * strain, c2 = hc[3] * fyomb, c3 = hc[2] * fyomb;
+  const double c = Cstress + E0 * dStrain;
+  int branch = 0;                       // 0 predictor, 1 upper bound, 2 lower bound
+  double t = c;
+  if (c1 + c3 < c) { t = c1 + c3; branch = 1; }
+  if (c1 - c2 > t) branch = 2;
+  int loading = (int)hc[4];
+  if (loading == 0) loading = dStrain > 0.0 ? 1 : -1;
+  const bool revN = loading == 1 && dStrain < 0.0;
+  const bool revP = !revN && loading == -1 && dStrain > 0.0;
+  double dTmin = dhc[0], dTmax = dhc[1], dShiftP = dhc[2], dShiftN = dhc[3];
+  if (revN || revP) {
+    double Tmin = hc[0], Tmax = hc[1];
+    if (revP && Cstrain < hc[0]) { Tmin = Cstrain; dTmin = dhc[10]; }
+    if (revN && Cstrain > hc[1]) { Tmax = Cstrain; dTmax = dhc[10]; }
+    const double a = revN ? a1 : a3, den = 2.0 * (revN ? a2 : a4) * epsy;
+    const double X = (Tmax - Tmin) / den;
+    const double dX = (dTmax - dTmin) / den - X * depsy / epsy;
+    const double dShift = (a != 0.0 && X > 0.0) ? a * 0.8 * pow(X, -0.2) * dX : 0.0;
+    if (revN) dShiftN = dShift;
+    else dShiftP = dShift;
+  }
+  const double dEsh = db * E0 + b * dE0;
+  double ds;
+  if (branch == 0) ds = dhc[9] + dE0 * dStrain + E0 * (dstrain - dhc[10]);
+  else if (branch == 1) ds = dEsh * strain + b * E0 * dstrain + dhc[2] * fyomb + hc[2] * dfyomb;
+  else ds = dEsh * strain + b * E0 * dstrain - dhc[3] * fyomb - hc[3] * dfyomb;
+  dht[0] = dTmin; dht[1] = dTmax; dht[2] = dShiftP; dht[3] = dShiftN;
+  dht[9] = ds; dht[10] = dstrain;
+}
+
+// the elastic law sigma = E eps in forward mode (dq[0] = dE)
+XG_HD inline void elastic_jvp(const double *q, double strain, double dstrain, const double *dq,
+                              double *dht) {
+  for (int k = 0; k < 12; k++) dht[k] = 0.0;
+  dht[9] = dq[0] * strain + q[0] * dstrain;
+  dht[10] = dstrain;
 }
 
 XG_HD inline void elastic_vjp(const double *q, double strain, const double *yb, double *hb,

@@ -411,6 +411,55 @@ def adjoint_backward(model, scale=1.0):
     return g
 
 
+def ddm_forward(model, phase, num_steps, dtheta, node, dof, weight):
+    """Newmark run of num_steps from the initial state with the direct
+    differentiation along the directions ``dtheta`` [num_dir, num_uni, 3];
+    returns (J, dJ[num_dir])."""
+    L = lib()
+    L.xg_ddm_forward.argtypes = [C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_void_p,
+                                 C.c_void_p, C.POINTER(C.c_double), C.c_void_p]
+    nu = len(model.desc.uni_type)
+    dth = np.ascontiguousarray(np.asarray(dtheta, np.float64).reshape(-1, nu, 3))
+    node = np.ascontiguousarray(node, np.int32)
+    dof = np.ascontiguousarray(dof, np.int32)
+    weight = np.ascontiguousarray(weight, np.float64)
+    obj = _abi.xg_objective_desc(len(node), node.ctypes.data_as(C.POINTER(C.c_int)),
+                                 dof.ctypes.data_as(C.POINTER(C.c_int)),
+                                 weight.ctypes.data_as(C.POINTER(C.c_double)))
+    model._ps = phase.struct()
+    J = C.c_double()
+    dJ = np.zeros(dth.shape[0])
+    _check(L.xg_ddm_forward(model.h, C.byref(model._ps), int(num_steps), dth.shape[0], _p(dth),
+                            C.byref(obj), C.byref(J), _p(dJ)))
+    return J.value, dJ
+
+
+def ddm_disp_sensitivity(model, direction):
+    """The last DDM run's displacement tangent along ``direction`` after its
+    last step, [num_nodes, ndf]."""
+    L = lib()
+    L.xg_ddm_disp_sensitivity.argtypes = [C.c_void_p, C.c_int, C.c_void_p]
+    out = np.zeros((model.desc.num_nodes, model.desc.ndf))
+    _check(L.xg_ddm_disp_sensitivity(model.h, int(direction), _p(out)))
+    return out
+
+
+def uniaxial_jvp(kind, param, hc, strain, dstrain, dhc, dq):
+    """Host Jacobian-vector product of one material point's trial record: the
+    tangent of the trial record [12]."""
+    L = lib()
+    L.xg_uniaxial_jvp.argtypes = [C.c_int, C.c_void_p, C.c_void_p, C.c_double, C.c_double,
+                                  C.c_void_p, C.c_void_p, C.c_void_p]
+    q = np.ascontiguousarray(param, np.float64)
+    hc = np.ascontiguousarray(hc, np.float64)
+    dhc = np.ascontiguousarray(dhc, np.float64)
+    dq = np.ascontiguousarray(dq, np.float64)
+    dht = np.zeros(12)
+    _check(L.xg_uniaxial_jvp(int(kind), _p(q), _p(hc), float(strain), float(dstrain), _p(dhc),
+                             _p(dq), _p(dht)))
+    return dht
+
+
 def uniaxial_vjp(kind, param, hc, strain, yb):
     """Host vector-Jacobian product of one material point's trial record:
     (adjoint of the committed record [12], of the strain, of parameters 0-2)."""
