@@ -46,6 +46,7 @@ extern "C" {
 #define XG_UNI_CONCRETE02  2   /* material/uniaxial/concrete/Concrete02.cpp */
 #define XG_UNI_ELASTIC     3   /* linear elastic fiber (known-answer tests) */
 #define XG_UNI_STEEL01     4   /* material/uniaxial/steel/Steel01.cpp      */
+#define XG_UNI_CONCRETE01  5   /* material/uniaxial/concrete/Concrete01.cpp */
 
 /* constraint handlers (analysis/handler) */
 #define XG_HANDLER_PLAIN           0  /* PlainHandler.cpp                   */
@@ -445,13 +446,14 @@ int xg_chain_reciprocal_check(int n, const double *d, double *y, double *y_rn);
         sensitivity).  Gradients of J = sum over the steps n = 1..N and the
         terms k of weight_k * u(node_k, dof_k, t_n)^2 with respect to the
         first three parameters of every uniaxial material (Steel02: Fy, E0,
-        b; Steel01: fy, E0, b; Concrete02: fc, epsc0, fcu; elastic: E).
-        Covers 2D and 3D force-based frames (Linear or PDelta
-        transformations) whose sections use at most four materials (Steel02
-        without initial stress, Steel01, Concrete02, elastic), Newmark with
-        alphaM Rayleigh damping (betaK0 as well where an element has a
-        single Steel02, Steel01 or elastic material), UniformExcitation and
-        nodal load patterns, from the model's initial state. ---- */
+        b; Steel01: fy, E0, b; Concrete02: fc, epsc0, fcu; Concrete01: fpc,
+        epsc0, fpcu; elastic: E).  Covers 2D and 3D force-based frames
+        (Linear or PDelta transformations) whose sections use at most four
+        materials (Steel02 without initial stress, Steel01, Concrete02,
+        Concrete01, elastic), Newmark with alphaM Rayleigh damping (betaK0
+        as well where an element has a single Steel02, Steel01 or elastic
+        material), UniformExcitation and nodal load patterns, from the
+        model's initial state. ---- */
 typedef struct xg_objective_desc {
   int num_terms;
   const int *node;            /* node tags */
@@ -479,17 +481,19 @@ int xg_adjoint_backward(xg_model *m, double scale, double *grad, int num_uni);
         Newmark::computeSensitivities, Newmark.cpp:904-959;
         ForceBeamColumn2d's basic-force sensitivity and commitSensitivity,
         ForceBeamColumn2d.cpp:2890-3007; Steel01::getStressSensitivity and
-        commitSensitivity, Steel01.cpp:552-660), a forward-mode path
+        commitSensitivity, Steel01.cpp:552-660; Concrete01's, Concrete01.cpp:
+        655-775), a forward-mode path
         independent of the adjoint above.  Covers 2D and 3D force-based frames
-        (Linear transformations in 2D; Linear or PDelta in 3D) with Steel01
-        and elastic fibers, Newmark with alphaM Rayleigh damping (no
+        (Linear transformations in 2D; Linear or PDelta in 3D) with Steel01,
+        Concrete01 and elastic fibers, Newmark with alphaM Rayleigh damping (no
         betaK0), UniformExcitation and nodal load patterns, from the model's
         initial state.  After each converged step the effective tangent is
         formed again at the converged state (the reference solves with the
         last Newton iteration's factors). ---- */
 /* Newmark run of num_steps from the initial state carrying num_dir
    directions: dtheta[(k*num_uni + u)*3 + j] is direction k's tangent of
-   parameter j (0..2) of material u (Steel01: fy, E0, b; elastic: E).
+   parameter j (0..2) of material u (Steel01: fy, E0, b; Concrete01: fpc,
+   epsc0, fpcu; elastic: E).
    J as xg_adjoint_forward; dJ[k] = the derivative of J along direction k. */
 int xg_ddm_forward(xg_model *m, const xg_phase_desc *ph, int num_steps, int num_dir,
                    const double *dtheta, const xg_objective_desc *obj, double *J, double *dJ);
@@ -497,16 +501,17 @@ int xg_ddm_forward(xg_model *m, const xg_phase_desc *ph, int num_steps, int num_
    step, out[num_nodes*ndf] (zero on constrained dofs; `sensNodeDisp`). */
 int xg_ddm_disp_sensitivity(const xg_model *m, int dir, double *out);
 /* Jacobian-vector product of one material point's trial record (host only;
-   Steel01 or elastic): given the tangents of the strain, of the committed
-   record dhc[12] and of parameters 0-2 dq[3], the tangent of the trial
-   record dht[12] (Steel01 fields 0-3, 9 stress, 10 strain). */
+   Steel01, Concrete01 or elastic): given the tangents of the strain, of
+   the committed record dhc[12] and of parameters 0-2 dq[3], the tangent of
+   the trial record dht[12] (Steel01 fields 0-3, Concrete01 0-2, 9 stress,
+   10 strain). */
 int xg_uniaxial_jvp(int type, const double *q, const double *hc, double strain,
                     double dstrain, const double *dhc, const double *dq, double *dht);
 /* Vector-Jacobian product of one material point's trial record (host only;
-   Steel02, Concrete02 or elastic): given the adjoint yb[12] of the trial
-   record (history fields: Steel02 0-6, Concrete02 0-1; 9 stress, 10
-   strain), the adjoints of the committed record hb[12], of the strain *sb
-   and of parameters 0-2 qb[3]. */
+   Steel02, Concrete02, Steel01, Concrete01 or elastic): given the adjoint
+   yb[12] of the trial record (history fields: Steel02 0-6, Concrete02 0-1,
+   Steel01 0-3, Concrete01 0-2; 9 stress, 10 strain), the adjoints of the
+   committed record hb[12], of the strain *sb and of parameters 0-2 qb[3]. */
 int xg_uniaxial_vjp(int type, const double *q, const double *hc, double strain,
                     const double *yb, double *hb, double *sb, double *qb);
 

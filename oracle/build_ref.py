@@ -73,7 +73,7 @@ material/uniaxial/UniaxialMaterial.cpp
 material/plastic/J2Plasticity.cpp material/Plane/J2PlaneStrain.cpp
 material/plastic/J2ThreeDimensional.cpp
 material/uniaxial/steel/Steel02.cpp material/uniaxial/concrete/Concrete02.cpp
-material/uniaxial/steel/Steel01.cpp
+material/uniaxial/steel/Steel01.cpp material/uniaxial/concrete/Concrete01.cpp
 material/uniaxial/ElasticMaterial.cpp
 material/section/SectionForceDeformation.cpp
 material/section/FiberSection2d.cpp material/section/FiberSection3d.cpp

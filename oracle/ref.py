@@ -147,8 +147,9 @@ def uniaxial_path(kind, param, strain, commit):
 def ddm_gradient(desc, phases, params, obj):
     """The reference's DDM sensitivity (computeGradients at every step) of J
     = sum over steps and terms of w u(node, dof)^2: params is a list of
-    (element tag, name) with name 0 fy, 1 E, 2 b; obj = (node tags, dofs,
-    weights).  Returns (dJ/dparam, J)."""
+    (element tag, name) with name 0 fy, 1 E, 2 b (Steel01), 3 fc, 4 epsco,
+    5 fcu (Concrete01); obj = (node tags, dofs, weights).  Returns
+    (dJ/dparam, J)."""
     L = lib()
     L.xref_ddm_setup.argtypes = [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_int,
                                  C.c_void_p, C.c_void_p, C.c_void_p]

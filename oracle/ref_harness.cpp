@@ -36,6 +36,7 @@
 #include <J2ThreeDimensional.h>
 #include <Steel01.h>
 #include <Steel02.h>
+#include <Concrete01.h>
 #include <Concrete02.h>
 #include <ElasticMaterial.h>
 #include <FiberSection2d.h>
@@ -294,6 +295,8 @@ UniaxialMaterial *make_uniaxial(int type, const double *q, int tag) {
       return new Concrete02(tag, q[0], q[1], q[2], q[3], q[4], q[5], q[6]);
     case XG_UNI_STEEL01:
       return new Steel01(tag, q[0], q[1], q[2], q[3], q[4], q[5], q[6]);
+    case XG_UNI_CONCRETE01:
+      return new Concrete01(tag, q[0], q[1], q[2], q[3]);
     case XG_UNI_ELASTIC:
       return new ElasticMaterial(tag, q[0]);
   }
@@ -634,8 +637,9 @@ int xref_run_phase(void *hp, const xg_phase_desc *ph, int cap_begin, int cap_end
 }
 
 // DDM set-up before the first phase: one Parameter per (element tag,
-// name), name 0 "fy", 1 "E", 2 "b", reaching every fiber material of the
-// element (ForceBeamColumn2d::setParameter -> FiberSection2d::setParameter
+// name), name 0 "fy", 1 "E", 2 "b" (Steel01), 3 "fc", 4 "epsco", 5 "fcu"
+// (Concrete01), reaching every fiber material of the element that has it
+// (ForceBeamColumn2d::setParameter -> FiberSection2d::setParameter
 // -> the materials' setParameter, ForceBeamColumn2d.cpp:2763-2846,
 // FiberSection2d.cpp:877-960), added to the Domain in order (gradient index
 // = position); the objective's terms by node tag and 0-based dof.
@@ -644,10 +648,10 @@ extern "C" int xref_ddm_setup(void *hp, int nparam, const int *elem_tag, const i
                               const double *w) {
   Harness *h = (Harness *)hp;
   if (h->soe) return -1;
-  static const char *names[3] = {"fy", "E", "b"};
+  static const char *names[6] = {"fy", "E", "b", "fc", "epsco", "fcu"};
   for (int k = 0; k < nparam; k++) {
     Element *el = h->domain->getElement(elem_tag[k]);
-    if (!el || name[k] < 0 || name[k] > 2) return -2;
+    if (!el || name[k] < 0 || name[k] > 5) return -2;
     const char *argv[1] = {names[name[k]]};
     Parameter *p = new Parameter(k + 1, el, argv, 1);
     if (!h->domain->addParameter(p)) return -3;

@@ -12,6 +12,8 @@ Usage: python tests/golden/make_golden.py        (the small fixtures)
                                                   frame pushover, about half an hour)
        python tests/golden/make_golden.py settle (frame2d_settle_2x3 alone)
        python tests/golden/make_golden.py steel01 (uniaxial paths, Steel01 frames)
+       python tests/golden/make_golden.py concrete01 (uniaxial paths, the Steel01 /
+           Concrete01 surrogate frame and its DDM gradient)
 """
 import os
 import sys
@@ -63,13 +65,14 @@ def j2_paths(seed=1):
 
 
 def uniaxial_paths(seed=2):
-    """Random strain paths through Steel02 and Concrete02."""
+    """Random strain paths through Steel02, Concrete02, Steel01 and Concrete01."""
     rng = np.random.default_rng(seed)
     out = {}
     for kind, param, scale in ((1, configs.steel02_row(350e6, 200e9, 0.01), 4e-3),
                                (2, configs.concrete02_row(30e6), 2e-3),
                                (4, configs.steel01_row(350e6, 200e9, 0.01, 0.02, 2.0, 0.03, 3.0),
-                                4e-3)):
+                                4e-3),
+                               (5, configs.concrete01_row(30e6), 2e-3)):
         n = 400
         strain = np.cumsum(rng.normal(0.0, scale / 3, size=n))
         commit = (rng.random(n) < 0.5).astype(np.int32)
@@ -194,6 +197,48 @@ def ddm_fixture(name="ddm_steel01_frame"):
          step_iters=run.step_iters)
 
 
+def concrete01_fixtures():
+    """The Steel01 / Concrete01 surrogate: the 2D RC frame's gravity and
+    pushover (every solve of the first gravity step captured), and the
+    reference's DDM gradient of the summed squared roof drift of the
+    massless ramp with respect to every member's Concrete01 fc, epsco, fcu
+    and Steel01 fy, E, b (checked against central differences of the oracle
+    before it is written)."""
+    model_fixture("frame2d_rc01_2x3", configs.rc_frame_2d, (2, 3), {"steps": 20},
+                  capture_steps=(0,))
+    desc, phases = configs.ddm_rc01_frame()
+    params = [(int(t), k) for t in desc.elem_tag for k in (3, 4, 5, 0, 1, 2)]
+    obj = (desc.meta["obj_node"], desc.meta["obj_dof"], desc.meta["obj_weight"])
+    grad, J, run = ref.ddm_gradient(desc, phases, params, obj)
+    grad = grad.reshape(-1, 3)
+    q0 = desc.uni_param.reshape(-1, 12)
+    roof = list(desc.node_tag).index(int(obj[0][0]))
+
+    def J_of(q):
+        d = configs._with_geometry(desc, uni_param=q)
+        o = port.OracleModel(d)
+        U, _, _ = o.run(phases)
+        o.close()
+        return obj[2][0] * np.sum(U[:, 3 * roof] ** 2)
+
+    worst = 0.0
+    for k in range(3):
+        scale = np.abs(grad[:, k] * q0[:, k]).max()
+        for u in np.argsort(np.abs(grad[:, k] * q0[:, k]))[-3:]:
+            h = 1e-6 * abs(q0[u, k])
+            qp, qm = q0.copy(), q0.copy()
+            qp[u, k] += h
+            qm[u, k] -= h
+            fd = (J_of(qp) - J_of(qm)) / (2 * h)
+            worst = max(worst, abs(fd - grad[u, k]) * abs(q0[u, k]) / scale)
+    print(f"ddm_rc01_frame: reference DDM against central differences of the oracle: "
+          f"{worst:.2e} of each kind's largest scaled entry")
+    save("ddm_rc01_frame", builder=np.array("ddm_rc01_frame"), args=np.asarray([], np.int64),
+         kw_keys=np.array([], dtype="<U1"), kw_vals=np.asarray([], np.float64),
+         grad=grad, J=np.array([J]), step_u=run.step_u, step_iters=run.step_iters,
+         fd_check=np.array([worst]))
+
+
 def settlement_fixture():
     """The 2D steel frame with a support settlement imposed through the
     Transformation handler (gravity and settlement by LoadControl, then the
@@ -263,6 +308,10 @@ def main():
     if sys.argv[1:] == ["settle"]:
         settlement_fixture()
         return
+    if sys.argv[1:] == ["concrete01"]:
+        uniaxial_paths()
+        concrete01_fixtures()
+        return
     if sys.argv[1:] == ["steel01"]:
         uniaxial_paths()
         steel01_fixtures()
@@ -292,6 +341,7 @@ def main():
     settlement_fixture()
     steel01_fixtures()
     ddm_fixture()
+    concrete01_fixtures()
 
 
 if __name__ == "__main__":

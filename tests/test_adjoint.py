@@ -14,7 +14,8 @@ import pytest
 
 from oracle import port
 from xara_gb300 import configs
-from xara_gb300._abi import XG_UNI_CONCRETE02, XG_UNI_ELASTIC, XG_UNI_STEEL01, XG_UNI_STEEL02
+from xara_gb300._abi import (XG_UNI_CONCRETE01, XG_UNI_CONCRETE02, XG_UNI_ELASTIC,
+                             XG_UNI_STEEL01, XG_UNI_STEEL02)
 
 FIELDS = (0, 1, 2, 3, 4, 5, 6, 9, 10)            # continuous record fields
 
@@ -249,6 +250,72 @@ def test_steel01_jvp_against_finite_differences_and_the_vjp(shift):
     with pytest.raises(_gpu().XaraGpuError):
         gpu.uniaxial_jvp(XG_UNI_STEEL02, configs.steel02_row(), np.zeros(12), 1e-3, de,
                          np.zeros(12), dq)
+
+
+C01_FIELDS = (0, 1, 2, 9, 10)          # minStrain, endStrain, unloadSlope, sig, eps
+
+
+def test_concrete01_derivatives_against_finite_differences():
+    """Concrete01 in forward mode (the DDM's law) against central differences
+    of the oracle's law in random directions of (strain, record, fpc, epsc0,
+    fpcu), along a compression path of growing amplitude with excursions
+    into tension: the parabola, the linear descent and the crushed plateau
+    of the envelope, unloading, reloading, the return line and tension; the
+    reverse mode (the adjoint's) equal to it through y.(Jt) = (J'y).t.
+    Finite differences skip the points where the return line and the
+    reloading line coincide (the committed point lies on the unloading line
+    and the law takes the larger of two equal stresses) and strains at the
+    committed one (the law keeps the committed state there)."""
+    gpu = _gpu()
+    q = configs.concrete01_row(30e6)
+    e0 = 0.002
+    t = np.linspace(0.0, 8.0 * np.pi, 400)
+    strains = -e0 * (0.2 + 0.5 * t / np.pi) * np.abs(np.sin(t)) * 1.2 + 0.0004 * np.sin(3 * t)
+    rng = np.random.default_rng(3)
+    sc = np.zeros(12)
+    sc[[0, 1, 10]] = e0
+    sc[2] = 15e9
+    sc[9] = 30e6
+    hc = port.uniaxial_init(XG_UNI_CONCRETE01, q)
+    labels, checked = set(), 0
+    for e in strains:
+        e = float(e)
+        ht = port.uniaxial_trial(XG_UNI_CONCRETE01, q, hc, e)
+        de = rng.normal() * e0
+        dhc = np.zeros(12)
+        dhc[list(C01_FIELDS)] = rng.normal(size=len(C01_FIELDS)) * sc[list(C01_FIELDS)]
+        dq = rng.normal(size=3) * np.abs(q[:3])
+        dht = gpu.uniaxial_jvp(XG_UNI_CONCRETE01, q, hc, e, de, dhc, dq)
+        yb = np.zeros(12)
+        yb[list(C01_FIELDS)] = rng.normal(size=len(C01_FIELDS)) / sc[list(C01_FIELDS)]
+        hb, sb, qb = gpu.uniaxial_vjp(XG_UNI_CONCRETE01, q, hc, e, yb)
+        terms = [sb * de, *(hb[f] * dhc[f] for f in C01_FIELDS), *(qb * dq)]
+        assert abs(float(yb @ dht) - sum(terms)) <= 1e-12 * sum(abs(x) for x in terms) + 1e-300
+        # branch labels and the coincident-lines kink
+        temp = hc[9] + hc[2] * (e - hc[10])
+        kink = False
+        if e > 0:
+            labels.add("tension")
+        elif e <= hc[10] and e <= hc[0]:
+            labels.add("parabola" if e > -e0 else "descent" if e > -0.006 else "crushed")
+        elif e <= hc[10] and e <= hc[1]:
+            labels.add("reload")
+            kink = abs(temp - hc[2] * (e - hc[1])) < 1e-6 * 30e6
+        elif e > hc[10] and temp <= 0:
+            labels.add("return")
+        rel = 1e-7
+        qp, qm = q.copy(), q.copy()
+        qp[:3] += rel * dq
+        qm[:3] -= rel * dq
+        fd = (port.uniaxial_trial(XG_UNI_CONCRETE01, qp, hc + rel * dhc, e + rel * de) -
+              port.uniaxial_trial(XG_UNI_CONCRETE01, qm, hc - rel * dhc, e - rel * de)) / (2 * rel)
+        if not kink and abs(e - hc[10]) > 1e-4 * e0:
+            for f in C01_FIELDS:
+                assert abs(dht[f] - fd[f]) <= 1e-7 * sc[f], (e, f, dht[f], fd[f])
+            checked += 1
+        hc = ht
+    assert {"tension", "parabola", "descent", "crushed", "reload", "return"} <= labels, labels
+    assert checked > 300
 
 
 C02_FIELDS = (0, 1, 9, 10)                       # ecmin, dept, sig, eps
@@ -602,18 +669,33 @@ def test_adjoint_through_torch_autograd(need_gpu):
     np.testing.assert_allclose(theta.grad.numpy(), 2.0 * g, rtol=1e-13, atol=0)
 
 
-def _ddm_case():
+DDM_CASES = ["ddm_steel01_frame", "ddm_rc01_frame"]
+
+
+def _kinds(desc):
+    """(material rows of one law, parameter index): the parameter kinds the
+    gradient checks scale separately."""
+    ut = np.asarray(desc.uni_type)
+    return [(np.nonzero(ut == t)[0], k) for t in np.unique(ut) for k in range(3)]
+
+
+def _ddm_case(name="ddm_steel01_frame"):
     from golden_util import load, model_of
-    fx = load("ddm_steel01_frame")
+    fx = load(name)
     desc, phases = model_of(fx)
     obj = (desc.meta["obj_node"], desc.meta["obj_dof"], desc.meta["obj_weight"])
     return fx, desc, phases, obj
 
 
-def test_ddm_surrogate_forward_matches_the_reference():
-    """The massless Steel01 ramp the reference's DDM runs on: the oracle's
-    history and objective equal the reference's (the fixture)."""
-    fx, desc, phases, obj = _ddm_case()
+@pytest.mark.parametrize("name", DDM_CASES)
+def test_ddm_surrogate_forward_matches_the_reference(name):
+    """The massless ramps the reference's DDM runs on (Steel01 members; RC
+    members of Concrete01 and Steel01): the oracle's history and objective
+    equal the reference's (the fixture), and the fixture's gradient passed
+    central differences of the oracle when it was made."""
+    fx, desc, phases, obj = _ddm_case(name)
+    if "fd_check" in fx:
+        assert fx["fd_check"][0] < 1e-7
     o = port.OracleModel(desc)
     U, _, its = o.run(phases)
     o.close()
@@ -625,14 +707,16 @@ def test_ddm_surrogate_forward_matches_the_reference():
 
 
 @pytest.mark.gpu
-def test_adjoint_matches_the_reference_ddm(need_gpu):
+@pytest.mark.parametrize("name", DDM_CASES)
+def test_adjoint_matches_the_reference_ddm(need_gpu, name):
     """The device adjoint against the reference's own DDM sensitivity
     (Newmark::computeSensitivities after every step, the gradient of the
-    summed squared roof drift accumulated from Node::getDispSensitivity):
-    every member's d/d(fy, E0, b) of Steel01, each parameter kind within
-    1e-6 relative of its largest entry, and the objective within 1e-12."""
+    summed squared roof drift accumulated from Node::getDispSensitivity) on
+    the massless ramps: every member's d/d(fy, E0, b) of Steel01 and
+    d/d(fpc, epsc0, fpcu) of Concrete01, each parameter kind within 1e-6
+    relative of its largest entry, and the objective within 1e-12."""
     gpu = _gpu()
-    fx, desc, phases, obj = _ddm_case()
+    fx, desc, phases, obj = _ddm_case(name)
     ph = phases[0]
     with gpu.DeviceModel(desc) as m:
         m.set_system(gpu.XG_SYSTEM_PROFILE_SPD)
@@ -641,9 +725,10 @@ def test_adjoint_matches_the_reference_ddm(need_gpu):
     ref = fx["grad"]
     assert abs(J - fx["J"][0]) <= 1e-12 * fx["J"][0]
     assert g.shape == ref.shape
-    for k in range(3):
-        scale = np.abs(ref[:, k]).max()
-        assert np.max(np.abs(g[:, k] - ref[:, k])) <= 1e-6 * scale, (k, g[:, k], ref[:, k])
+    for rows, k in _kinds(desc):
+        scale = np.abs(ref[rows, k]).max()
+        assert np.max(np.abs(g[rows, k] - ref[rows, k])) <= 1e-6 * scale, (k, g[rows, k],
+                                                                           ref[rows, k])
 
 
 # ---------------------------------------------------------------------------
@@ -655,15 +740,17 @@ def _unit_directions(nu):
 
 
 @pytest.mark.gpu
-def test_ddm_matches_the_reference_ddm_and_the_adjoint(need_gpu):
-    """The device DDM on the massless Steel01 ramp, one direction per member
-    and parameter: against the reference's own DDM (each parameter kind
+@pytest.mark.parametrize("name", DDM_CASES)
+def test_ddm_matches_the_reference_ddm_and_the_adjoint(need_gpu, name):
+    """The device DDM on the massless ramps (Steel01 members; Concrete01 and
+    Steel01 members), one direction per material and parameter: against the
+    reference's own DDM (each parameter kind
     within 1e-6 of its largest entry; the reference solves with the last
     Newton iteration's factors, the device at the converged state) and
     against the device adjoint (1e-10: both are exact derivatives of the
     same discrete path, by independent code)."""
     gpu = _gpu()
-    fx, desc, phases, obj = _ddm_case()
+    fx, desc, phases, obj = _ddm_case(name)
     ph = phases[0]
     nu = len(desc.uni_type)
     with gpu.DeviceModel(desc) as m:
@@ -676,10 +763,12 @@ def test_ddm_matches_the_reference_ddm_and_the_adjoint(need_gpu):
     ref = fx["grad"]
     assert J == Ja
     assert abs(J - fx["J"][0]) <= 1e-12 * fx["J"][0]
-    for k in range(3):
-        scale = np.abs(ref[:, k]).max()
-        assert np.max(np.abs(g[:, k] - ref[:, k])) <= 1e-6 * scale, (k, g[:, k], ref[:, k])
-        assert np.max(np.abs(g[:, k] - ga[:, k])) <= 1e-10 * scale, (k, g[:, k], ga[:, k])
+    for rows, k in _kinds(desc):
+        scale = np.abs(ref[rows, k]).max()
+        assert np.max(np.abs(g[rows, k] - ref[rows, k])) <= 1e-6 * scale, (k, g[rows, k],
+                                                                           ref[rows, k])
+        assert np.max(np.abs(g[rows, k] - ga[rows, k])) <= 1e-10 * scale, (k, g[rows, k],
+                                                                            ga[rows, k])
 
 
 @pytest.mark.gpu
@@ -726,6 +815,48 @@ def test_ddm_under_ground_motion_matches_the_adjoint(need_gpu, pga_scale, steps)
     fdu = (np.asarray(up) - np.asarray(um)).reshape(du.shape) / (2 * h)
     if pga_scale == 1.0:
         assert np.abs(du - fdu).max() <= 1e-4 * np.abs(fdu).max()
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("pga_scale,steps", [(1.0, 40), (3.0, 80)])
+def test_ddm_rc01_frames_under_ground_motion(need_gpu, pga_scale, steps):
+    """Two RC frames with Concrete01 layers and Steel01 bars, floor masses,
+    under their records (the second at three times the record, through
+    cracking and crushing): the DDM along seeded directions against the
+    adjoint (1e-9) and central differences of the forward run (1e-4)."""
+    gpu = _gpu()
+    desc, phases = configs.adjoint_rc_frames(n_frames=2, steps=steps, seed=5,
+                                             pga_scale=pga_scale, laws="01")
+    ph = phases[0]
+    node, dof, w = _objective(desc)
+    q0 = desc.uni_param.reshape(-1, 12).copy()
+    nu = len(q0)
+    rng = np.random.default_rng(31)
+    dirs = rng.normal(size=(3, nu, 3)) * np.abs(q0[:, :3])
+    with gpu.DeviceModel(desc) as m:
+        J, dJ = gpu.ddm_forward(m, ph, steps, dirs, node, dof, w)
+        rec = m.fiber_records()
+        m.reset()
+        Ja = gpu.adjoint_forward(m, ph, steps, 10, node, dof, w)
+        ga = gpu.adjoint_backward(m)
+        assert J == Ja and np.abs(dJ).min() > 0
+        ss, fm = desc.arrays["sec_fiber_start"], desc.arrays["fib_mat"]
+        kinds = np.concatenate([np.tile(np.asarray(desc.uni_type)[fm[ss[s_]:ss[s_ + 1]]],
+                                        desc.fbc_num_ip)
+                                for s_ in desc.arrays["elem_mat"]])
+        c_rec = rec[kinds == XG_UNI_CONCRETE01]
+        assert (c_rec[:, 0] < -1e-4).mean() > 0.01               # compressed beyond 1e-4
+        for k in range(3):
+            assert dJ[k] == pytest.approx(float((ga * dirs[k]).sum()), rel=1e-9), k
+        h = 1e-6
+        qp, qm = q0.copy(), q0.copy()
+        qp[:, :3] += h * dirs[0]
+        qm[:, :3] -= h * dirs[0]
+        gpu.set_uniaxial_params(m, qp)
+        Jp = gpu.adjoint_forward(m, ph, steps, steps, node, dof, w)
+        gpu.set_uniaxial_params(m, qm)
+        Jm = gpu.adjoint_forward(m, ph, steps, steps, node, dof, w)
+    assert dJ[0] == pytest.approx((Jp - Jm) / (2 * h), rel=1e-4)
 
 
 @pytest.mark.gpu

@@ -249,7 +249,8 @@ def test_round_trip_history_checkpoint(gpu_mod):
 
 
 FRAMES = ["frame2d_2x3", "frame3d_1x1x2", "frame3d_2x1x3", "frame2d_eq_2x3", "frame2d_pd_2x3",
-          "frame2d_settle_2x3", "frame2d_s01_2x3", "frame2d_s01_eq_2x3"]
+          "frame2d_settle_2x3", "frame2d_s01_2x3", "frame2d_s01_eq_2x3",
+          "frame2d_rc01_2x3"]
 
 
 @pytest.mark.parametrize("name", FRAMES)
@@ -271,7 +272,8 @@ def test_frame_numbering_pattern_and_history(gpu_mod, name):
 
 
 @pytest.mark.parametrize("name", ["frame2d_2x3", "frame3d_1x1x2", "frame2d_pd_2x3",
-                                  "frame2d_settle_2x3", "frame2d_s01_2x3"])
+                                  "frame2d_settle_2x3", "frame2d_s01_2x3",
+                                  "frame2d_rc01_2x3"])
 def test_frame_replay_first_step(gpu_mod, name):
     """Every Newton iteration of the first gravity step, replayed in the
     reference's order (the element state is incremental): resisting force

@@ -121,6 +121,57 @@ def test_frame_commands_give_the_builders_model():
     ops.wipe()
 
 
+def test_rc01_frame_commands_give_the_builders_model():
+    """Steel01 bars and Concrete01 layers (`uniaxialMaterial Concrete01 tag
+    fpc epsc0 fpcu epscu`, `Steel01 tag fy E0 b a1 a2 a3 a4`) in layered
+    fiber sections give the RC frame builder's model."""
+    ops.wipe()
+    ops.model("basic", "-ndm", 2, "-ndf", 3)
+    bays, stories, nx = 2, 3, 3
+    for j in range(stories + 1):
+        for i in range(nx):
+            ops.node(j * nx + i + 1, i * 6.0, j * 3.5)
+    for i in range(nx):
+        ops.fix(i + 1, 1, 1, 1)
+    ops.uniaxialMaterial("Concrete01", 1, -30e6, -0.002, -6e6, -0.006)
+    ops.uniaxialMaterial("Steel01", 2, 420e6, 200e9, 0.01, 0.0, 1.0, 0.0, 1.0)
+    for tag, (bw, h, nbar) in ((1, (0.5, 0.5, 3)), (2, (0.4, 0.6, 4))):
+        ops.section("Fiber", tag)
+        for y in (np.arange(10) + 0.5) * h / 10 - h / 2:
+            ops.fiber(y, 0.0, bw * h / 10, 1)
+        for y in (h / 2 - 0.05, -(h / 2 - 0.05)):
+            ops.fiber(y, 0.0, nbar * 491e-6, 2)
+    ops.geomTransf("Linear", 1)
+    ops.beamIntegration("Lobatto", 1, 1, 5)
+    ops.beamIntegration("Lobatto", 2, 2, 5)
+    t = 1
+    for j in range(stories):
+        for i in range(nx):
+            ops.element("forceBeamColumn", t, j * nx + i + 1, (j + 1) * nx + i + 1, 1, 1)
+            t += 1
+    for j in range(1, stories + 1):
+        for i in range(bays):
+            ops.element("forceBeamColumn", t, j * nx + i + 1, j * nx + i + 2, 1, 2)
+            t += 1
+    ops.timeSeries("Linear", 1)
+    ops.pattern("Plain", 1, 1)
+    for n in range(nx + 1, (stories + 1) * nx + 1):
+        ops.load(n, 0.0, -100e3, 0.0)
+    ops.constraints("Plain")
+    ops.numberer("RCM")
+    ops.system("ProfileSPD")
+    ops.test("NormDispIncr", 1e-10, 50)
+    ops.algorithm("Newton")
+    ops.integrator("LoadControl", 0.25)
+    ops.analysis("Static")
+    _lateral(stories * nx + 1, nx)
+    d, _ = configs.rc_frame_2d(2, 3, steps=5, grav_steps=4)
+    _same_desc(ops.build_desc(), d)
+    ops.wipe()
+    with pytest.raises(NotImplementedError, match="Concrete04"):
+        ops.uniaxialMaterial("Concrete04", 3, -30e6, -0.002, -0.004, 30e9)
+
+
 def test_transient_commands_give_the_builders_phase():
     """Masses, a Path series under UniformExcitation, rayleigh and Newmark:
     the description and the transient phase equal the builder's."""
@@ -154,8 +205,8 @@ def test_transient_commands_give_the_builders_phase():
 def test_unsupported_commands_are_named():
     ops.wipe()
     ops.model("basic", "-ndm", 2, "-ndf", 3)
-    with pytest.raises(NotImplementedError, match="uniaxialMaterial Steel01"):
-        ops.uniaxialMaterial("Steel01", 1, 1.0, 1.0, 0.01)
+    with pytest.raises(NotImplementedError, match="uniaxialMaterial Hysteretic"):
+        ops.uniaxialMaterial("Hysteretic", 1, 1.0, 1.0, 0.01)
     with pytest.raises(NotImplementedError, match="algorithm KrylovNewton"):
         ops.algorithm("KrylovNewton")
     ops.wipe()

@@ -65,12 +65,13 @@ def test_replay_element_state(name):
 
 
 FRAMES = ["frame2d_2x3", "frame3d_1x1x2", "frame3d_2x1x3", "frame2d_eq_2x3", "frame2d_pd_2x3",
-          "frame2d_settle_2x3", "frame2d_s01_2x3", "frame2d_s01_eq_2x3"]
+          "frame2d_settle_2x3", "frame2d_s01_2x3", "frame2d_s01_eq_2x3",
+          "frame2d_rc01_2x3"]
 
 
 def test_uniaxial_paths():
     fx = load("uniaxial_paths")
-    for kind in (1, 2, 4):         # Steel02, Concrete02, Steel01
+    for kind in (1, 2, 4, 5):      # Steel02, Concrete02, Steel01, Concrete01
         s, t = port.uniaxial_path(kind, fx[f"k{kind}_param"], fx[f"k{kind}_strain"],
                                   fx[f"k{kind}_commit"])
         assert relerr(s, fx[f"k{kind}_stress"]) < RTOL_STATE
@@ -92,7 +93,8 @@ def test_frame_numbering_and_history(name):
 
 
 @pytest.mark.parametrize("name", ["frame2d_2x3", "frame3d_1x1x2", "frame2d_pd_2x3",
-                                  "frame2d_settle_2x3", "frame2d_s01_2x3"])
+                                  "frame2d_settle_2x3", "frame2d_s01_2x3",
+                                  "frame2d_rc01_2x3"])
 def test_frame_replay_first_step(name):
     """Every Newton iteration of the first gravity step, replayed in order
     (the force-based element state is incremental, so the trial displacements

@@ -8,7 +8,7 @@ import ctypes as C
 import numpy as np
 
 XG_ELE_QUAD, XG_ELE_BRICK, XG_ELE_FBC2D, XG_ELE_FBC3D = 1, 2, 3, 4
-XG_UNI_STEEL02, XG_UNI_CONCRETE02, XG_UNI_ELASTIC, XG_UNI_STEEL01 = 1, 2, 3, 4
+XG_UNI_STEEL02, XG_UNI_CONCRETE02, XG_UNI_ELASTIC, XG_UNI_STEEL01, XG_UNI_CONCRETE01 = 1, 2, 3, 4, 5
 XG_HANDLER_PLAIN, XG_HANDLER_TRANSFORMATION = 0, 1
 XG_INT_LOAD_CONTROL, XG_INT_DISP_CONTROL, XG_INT_NEWMARK = 0, 1, 2
 XG_TEST_NORM_DISP_INCR, XG_TEST_NORM_UNBALANCE = 0, 1

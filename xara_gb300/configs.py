@@ -142,8 +142,8 @@ def brick_block(nx=128, ny=128, nz=64, strain=0.01, steps=50, j2=J2_STEEL,
 # frames: `element forceBeamColumn` with Lobatto points and fiber sections
 # ---------------------------------------------------------------------------
 from ._abi import (XG_ELE_FBC2D, XG_ELE_FBC3D, XG_INT_LOAD_CONTROL,  # noqa: E402
-                   XG_UNI_CONCRETE02, XG_UNI_ELASTIC, XG_UNI_STEEL01, XG_UNI_STEEL02,
-                   XG_UNI_NPARAM)
+                   XG_UNI_CONCRETE01, XG_UNI_CONCRETE02, XG_UNI_ELASTIC, XG_UNI_STEEL01,
+                   XG_UNI_STEEL02, XG_UNI_NPARAM)
 
 
 def steel02_row(fy=350e6, E=200e9, b=0.01, R0=18.0, cR1=0.925, cR2=0.15):
@@ -171,6 +171,15 @@ def steel_row(law, fy, E, b):
 
 def steel_type(law):
     return XG_UNI_STEEL01 if law == "Steel01" else XG_UNI_STEEL02
+
+
+def concrete01_row(fc, epsc0=0.002, fcu_ratio=0.2, epscu=0.006):
+    """`uniaxialMaterial Concrete01 tag fpc epsc0 fpcu epscu` with the
+    compressive values negative, as the command takes them: fpc = -fc,
+    fpcu = -fcu_ratio fc."""
+    r = np.zeros(XG_UNI_NPARAM)
+    r[:4] = (-abs(fc), -abs(epsc0), -abs(fcu_ratio * fc), -abs(epscu))
+    return r
 
 
 def concrete02_row(fc, epsc0=0.002, fcu_ratio=0.2, epscu=0.006, rat=0.1, ft_ratio=0.1):
@@ -714,14 +723,16 @@ def ddm_steel01_frame(bays=2, stories=3, steps=100, dt=0.01, base_shear=720e3, s
 
 
 def adjoint_rc_frames(n_frames=2, steps=2000, dt=0.01, seed=0, member_cov=0.05, pga_scale=1.0,
-                      ncl=12):
+                      ncl=12, laws="02"):
     """The frames of :func:`adjoint_frames` with reinforced-concrete members:
     every member a 0.4 x 0.5 m section of ``ncl`` Concrete02 layers (fc
     30 MPa, epsc0 0.002, fcu 0.2 fc, epscu 0.006, ft 0.1 fc) and two layers of
     Steel02 bars (4 x 491 mm^2 each, 50 mm cover; fy 420 MPa, E 200 GPa,
     b 0.01), one concrete and one steel material per member with fc and fy
     varied by a lognormal factor of CoV ``member_cov``; mass-proportional
-    Rayleigh damping only.  Same objective terms as :func:`adjoint_frames`."""
+    Rayleigh damping only.  Same objective terms as :func:`adjoint_frames`.
+    ``laws="01"`` gives the Concrete01 / Steel01 surrogate of the same
+    members (fc and fy as above, b 0.01)."""
     desc, phases = adjoint_frames(n_frames=n_frames, steps=steps, dt=dt, seed=seed,
                                   member_cov=member_cov, pga_scale=pga_scale)
     a = desc.arrays
@@ -737,9 +748,14 @@ def adjoint_rc_frames(n_frames=2, steps=2000, dt=0.01, seed=0, member_cov=0.05, 
     fc = 30e6 * np.exp(rng.normal(0.0, member_cov, ne))
     fy = 420e6 * np.exp(rng.normal(0.0, member_cov, ne))
     for e in range(ne):
-        rows.append(concrete02_row(fc=fc[e]))
-        rows.append(steel02_row(fy=fy[e], E=200e9, b=0.01, R0=18.0))
-        types += [XG_UNI_CONCRETE02, XG_UNI_STEEL02]
+        if laws == "01":
+            rows.append(concrete01_row(fc=fc[e]))
+            rows.append(steel01_row(fy=fy[e], E=200e9, b=0.01))
+            types += [XG_UNI_CONCRETE01, XG_UNI_STEEL01]
+        else:
+            rows.append(concrete02_row(fc=fc[e]))
+            rows.append(steel02_row(fy=fy[e], E=200e9, b=0.01, R0=18.0))
+            types += [XG_UNI_CONCRETE02, XG_UNI_STEEL02]
     fib_mat = np.concatenate([np.r_[np.full(ncl, 2 * e), np.full(2, 2 * e + 1)]
                               for e in range(ne)])
     kw = {k: v for k, v in a.items() if v is not None}
@@ -841,3 +857,113 @@ def ddm_steel01_frames_eq(n_frames=2, steps=40, dt=0.01, seed=0, pga_scale=1.0):
     ph.kw["beta_k_init"] = 0.0
     out.meta["workload"] = f"{n_frames} 2D steel frames, one Steel01 per member"
     return out, [ph]
+
+
+def rc_frame_2d(bays=2, stories=3, bay=6.0, story=3.5, ncl=10, fc=30e6, fy=420e6, E=200e9,
+                b=0.01, gravity=-100e3, drift=0.015, steps=20, grav_steps=10, max_iter=50,
+                tol=1e-10):
+    """2D reinforced-concrete frame of `forceBeamColumn` members (5 Lobatto
+    points) with layered fiber sections: ``ncl`` Concrete01 layers (fc,
+    epsc0 0.002, fcu 0.2 fc, epscu 0.006) and two layers of Steel01 bars
+    (fy, E, b; 50 mm cover); columns 0.5 x 0.5 m with 3 x 491 mm^2 per layer,
+    beams 0.4 x 0.6 m with 4 x 491 mm^2 per layer.  Gravity at every floor
+    node (LoadControl, then `loadConst -time 0`) and a pushover of the
+    roof-left node by DisplacementControl against a triangular pattern --
+    the Steel01 / Concrete01 surrogate of the reinforced-concrete frames."""
+    nx = bays + 1
+    tags, crd = [], []
+    for j in range(stories + 1):
+        for i in range(nx):
+            tags.append(j * nx + i + 1)
+            crd.append([i * bay, j * story])
+    conn, sec = [], []
+    for j in range(stories):
+        for i in range(nx):
+            conn.append([j * nx + i + 1, (j + 1) * nx + i + 1])
+            sec.append(0)
+    for j in range(1, stories + 1):
+        for i in range(bays):
+            conn.append([j * nx + i + 1, j * nx + i + 2])
+            sec.append(1)
+    fib_y, fib_A, fib_m, sec_start = [], [], [], [0]
+    for (bw, h, nbar) in ((0.5, 0.5, 3), (0.4, 0.6, 4)):
+        yc = (np.arange(ncl) + 0.5) * h / ncl - h / 2
+        ys = np.array([h / 2 - 0.05, -(h / 2 - 0.05)])
+        fib_y += [yc, ys]
+        fib_A += [np.full(ncl, bw * h / ncl), np.full(2, nbar * 491e-6)]
+        fib_m += [np.zeros(ncl, np.int32), np.ones(2, np.int32)]
+        sec_start.append(sec_start[-1] + ncl + 2)
+    uni = np.stack([concrete01_row(fc), steel01_row(fy, E, b)])
+    sp_node = np.repeat(np.arange(1, nx + 1), 3)
+    sp_dof = np.tile([0, 1, 2], nx)
+    floors = np.arange(nx + 1, (stories + 1) * nx + 1)
+    load_node = list(floors) + [j * nx + 1 for j in range(1, stories + 1)]
+    load_pat = [0] * len(floors) + [1] * stories
+    load_val = [[0.0, gravity, 0.0]] * len(floors) + \
+               [[float(j) / stories, 0.0, 0.0] for j in range(1, stories + 1)]
+    desc = ModelDesc(
+        ndm=2, ndf=3, elem_type=XG_ELE_FBC2D, geom_transf=0, fbc_num_ip=5,
+        node_tag=tags, node_crd=np.asarray(crd), elem_tag=np.arange(1, len(conn) + 1),
+        elem_conn=conn, elem_mat=sec, uni_type=[XG_UNI_CONCRETE01, XG_UNI_STEEL01],
+        uni_param=uni, sec_fiber_start=sec_start, fib_y=np.concatenate(fib_y),
+        fib_area=np.concatenate(fib_A), fib_mat=np.concatenate(fib_m),
+        sp_node=sp_node, sp_dof=sp_dof, sp_pattern=np.full(len(sp_node), -1),
+        sp_value=np.zeros(len(sp_node)), load_node=load_node, load_pattern=load_pat,
+        load_value=load_val)
+    roof = stories * nx + 1
+    H = stories * story
+    desc.meta = dict(workload=f"2D RC frame {bays}x{stories} (Steel01, Concrete01)",
+                     roof=roof, elements=len(conn))
+    phases = [
+        PhaseDesc(integrator=XG_INT_LOAD_CONTROL, pattern=0, num_steps=grav_steps,
+                  d_lambda=1.0 / grav_steps, tol=tol, max_iter=max_iter, load_const=1),
+        PhaseDesc(integrator=XG_INT_DISP_CONTROL, pattern=1, num_steps=steps,
+                  dc_node=roof, dc_dof=0, dc_incr=drift * H / steps, tol=tol,
+                  max_iter=max_iter),
+    ]
+    return desc, phases
+
+
+def ddm_rc01_frame(bays=2, stories=3, steps=100, dt=0.01, base_shear=230e3, seed=4,
+                   member_cov=0.05, ncl=10):
+    """The frame of :func:`rc_frame_2d` as the reference's DDM can run it
+    (massless, undamped `integrator Newmark 0.5 0.25` under a triangular
+    lateral pattern on a Linear series ramped to ``base_shear`` at the last
+    step, no gravity) with one Concrete01 and one Steel01 material per
+    member (fc and fy varied by a lognormal factor of CoV ``member_cov``):
+    the Steel01 / Concrete01 surrogate frame for comparing gradients with the
+    reference's DDM.  Objective: the summed squared roof drift."""
+    desc, _ = rc_frame_2d(bays, stories, ncl=ncl, gravity=0.0)
+    a = desc.arrays
+    ss, em = a["sec_fiber_start"], a["elem_mat"]
+    rng = np.random.default_rng(seed)
+    ne = len(em)
+    lo, hi = ss[em], ss[em + 1]
+    counts = hi - lo
+    idx = np.concatenate([np.arange(l_, h_) for l_, h_ in zip(lo, hi)])
+    fm = a["fib_mat"][idx] + 2 * np.repeat(np.arange(ne), counts)
+    fcs = 30e6 * np.exp(rng.normal(0.0, member_cov, ne))
+    fys = 420e6 * np.exp(rng.normal(0.0, member_cov, ne))
+    rows, types = [], []
+    for e in range(ne):
+        rows += [concrete01_row(fcs[e]), steel01_row(fys[e], 200e9, 0.01)]
+        types += [XG_UNI_CONCRETE01, XG_UNI_STEEL01]
+    lat = np.asarray(a["load_pattern"]) == 1
+    load_val = np.asarray(a["load_value"]).reshape(-1, 3)[lat] * base_shear / (steps * dt)
+    kw = {k: v for k, v in a.items() if v is not None}
+    kw.update(elem_mat=np.arange(ne), sec_fiber_start=np.concatenate([[0], np.cumsum(counts)]),
+              fib_y=a["fib_y"][idx], fib_area=a["fib_area"][idx], fib_mat=fm,
+              uni_type=np.asarray(types), uni_param=np.stack(rows),
+              load_node=np.asarray(a["load_node"])[lat],
+              load_pattern=np.zeros(int(lat.sum()), np.int32), load_value=load_val)
+    out = ModelDesc(ndm=2, ndf=3, elem_type=desc.elem_type, geom_transf=0,
+                    fbc_num_ip=desc.fbc_num_ip, **kw)
+    ramp = PhaseDesc(integrator=XG_INT_NEWMARK, pattern=0, num_steps=steps, dt=dt,
+                     gamma=0.5, beta=0.25, tol=1e-10, max_iter=50)
+    H = stories * 3.5
+    out.meta = dict(workload=f"2D RC frame {bays}x{stories}, one Concrete01 and one Steel01 "
+                             "per member, massless Newmark ramp",
+                    obj_node=np.array([desc.meta["roof"]], np.int32),
+                    obj_dof=np.zeros(1, np.int32), obj_weight=np.array([1.0 / (H * H)]),
+                    members=ne)
+    return out, [ramp]

@@ -155,6 +155,7 @@ __device__ __forceinline__ void fiber_vjp(int type, const double *q, const doubl
   if (type == XG_UNI_STEEL02) steel02_vjp(q, hc, strain, yb, hb, sb, qb);
   else if (type == XG_UNI_CONCRETE02) concrete02_vjp(q, hc, strain, yb, hb, sb, qb);
   else if (type == XG_UNI_STEEL01) steel01_vjp(q, hc, strain, yb, hb, sb, qb);
+  else if (type == XG_UNI_CONCRETE01) concrete01_vjp(q, hc, strain, yb, hb, sb, qb);
   else elastic_vjp(q, strain, yb, hb, sb, qb);
 }
 
@@ -452,7 +453,8 @@ __global__ void k_adj_pdelta(FrameView v, AdjView a) {
 }
 
 // The fresh records' dependence on the parameters (Steel02 revertToStart,
-// Steel02.cpp:70-95: epsmax = Fy/E0, epsmin = -Fy/E0).
+// Steel02.cpp:70-95: epsmax = Fy/E0, epsmin = -Fy/E0; Concrete01
+// revertToStart, Concrete01.cpp:435-457: unloading slope 2 fpc / epsc0).
 __global__ void k_adj_init_records(FrameView v, AdjView a) {
   const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int e = blockIdx.x * kAdjWarps + w;
@@ -463,12 +465,20 @@ __global__ void k_adj_init_records(FrameView v, AdjView a) {
   for (int k = lane; k < v.nip * nf; k += 32) {
     const int kf = f0 + k % nf;
     const int u = v.fmat[kf];
-    if (v.utype[u] != XG_UNI_STEEL02) continue;
     const double *q = v.uparam + (long)u * XG_UNI_NPARAM;
     const double *hb = a.hbar + (v.foff[e] + k) * 12;
-    const double d = hb[1] - hb[0];
-    const double qb[3] = {d / q[1], -d * q[0] / (q[1] * q[1]), 0.0};
-    add_slot(tq, a.fslot[kf], qb);
+    if (v.utype[u] == XG_UNI_STEEL02) {
+      const double d = hb[1] - hb[0];
+      const double qb[3] = {d / q[1], -d * q[0] / (q[1] * q[1]), 0.0};
+      add_slot(tq, a.fslot[kf], qb);
+    } else if (v.utype[u] == XG_UNI_CONCRETE01) {
+      // Concrete01::revertToStart: unloading slope Ec0 = 2 fpc / epsc0
+      const C01d c = c01d_params(q);
+      const double g = hb[2];
+      const double qb[3] = {c.sg0 * 2.0 * g / c.epsc0,
+                            -c.sg1 * 2.0 * g * c.fpc / (c.epsc0 * c.epsc0), 0.0};
+      add_slot(tq, a.fslot[kf], qb);
+    }
   }
   theta_add(a, e, lane, tq);
 }
@@ -521,6 +531,7 @@ __device__ __forceinline__ void fiber_jvp(int type, const double *q, const doubl
                                           double strain, double dstrain, const double *dhc,
                                           const double *dq, double *dht) {
   if (type == XG_UNI_STEEL01) steel01_jvp(q, hc, strain, dstrain, dhc, dq, dht);
+  else if (type == XG_UNI_CONCRETE01) concrete01_jvp(q, hc, strain, dstrain, dhc, dq, dht);
   else elastic_jvp(q, strain, dstrain, dq, dht);
 }
 
@@ -706,6 +717,26 @@ __global__ void __launch_bounds__(32 * kAdjWarps) k_ddm_commit(FrameView v, DdmV
   }
 }
 
+// Record tangents of the fresh materials: Concrete01's unloading slope
+// Ec0 = 2 fpc / epsc0 (Concrete01::revertToStart); Steel01 and elastic
+// records do not depend on the parameters.  Thread per fiber record.
+__global__ void k_ddm_init_records(FrameView v, DdmView d) {
+  const int e = blockIdx.y;
+  if (e >= v.ne) return;
+  const int sec = v.sec[e];
+  const int f0 = v.sec_fstart[sec], nf = v.sec_fstart[sec + 1] - f0;
+  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < v.nip * nf; k += gridDim.x * blockDim.x) {
+    const int kf = f0 + k % nf;
+    const int u = v.fmat[kf];
+    double *dh = d.dh + (v.foff[e] + k) * 12;
+    for (int j = 0; j < 12; j++) dh[j] = 0.0;
+    if (v.utype[u] != XG_UNI_CONCRETE01) continue;
+    const C01d c = c01d_params(v.uparam + (long)u * XG_UNI_NPARAM);
+    const double *dq = d.dth + 3L * u;
+    dh[2] = 2.0 * c.sg0 * dq[0] / c.epsc0 - 2.0 * c.fpc * c.sg1 * dq[1] / (c.epsc0 * c.epsc0);
+  }
+}
+
 // rhs = -dP_cond + M (c3 dU' - a3 dV' - a4 dA') + alphaM M (c2 dU' - a1 dV' - a2 dA'):
 // the derivative of the step's unbalance at fixed displacement, with the
 // Newmark relations A = c3 (U - U') + a3 V' + a4 A', V = c2 (U - U') + a1 V' + a2 A'
@@ -784,6 +815,12 @@ int launch_ddm_commit(const FrameView &v, const DdmView &d, cudaStream_t s) {
   return cudaGetLastError() == cudaSuccess ? 0 : XG_ECUDA;
 }
 
+int launch_ddm_init_records(const FrameView &v, const DdmView &d, cudaStream_t s) {
+  if (v.ne == 0) return 0;
+  k_ddm_init_records<<<dim3(1, v.ne), 128, 0, s>>>(v, d);
+  return cudaGetLastError() == cudaSuccess ? 0 : XG_ECUDA;
+}
+
 int launch_ddm_rhs(int neq, const double *dPc, const double *dU, const double *dV,
                    const double *dA, const double *meq, const double *meq_am,
                    const NewmarkCoef &c, double *rhs, cudaStream_t s) {
@@ -850,6 +887,7 @@ extern "C" int xg_uniaxial_jvp(int type, const double *q, const double *hc, doub
                                double *dht) {
   if (!q || !hc || !dhc || !dq || !dht) return XG_EINVAL;
   if (type == XG_UNI_STEEL01) xg::steel01_jvp(q, hc, strain, dstrain, dhc, dq, dht);
+  else if (type == XG_UNI_CONCRETE01) xg::concrete01_jvp(q, hc, strain, dstrain, dhc, dq, dht);
   else if (type == XG_UNI_ELASTIC) xg::elastic_jvp(q, strain, dstrain, dq, dht);
   else return XG_EINVAL;
   return 0;
@@ -867,6 +905,8 @@ extern "C" int xg_uniaxial_vjp(int type, const double *q, const double *hc, doub
     xg::concrete02_vjp(q, hc, strain, yb, hb, sb, qb);
   } else if (type == XG_UNI_STEEL01) {
     xg::steel01_vjp(q, hc, strain, yb, hb, sb, qb);
+  } else if (type == XG_UNI_CONCRETE01) {
+    xg::concrete01_vjp(q, hc, strain, yb, hb, sb, qb);
   } else if (type == XG_UNI_ELASTIC) {
     xg::elastic_vjp(q, strain, yb, hb, sb, qb);
   } else {

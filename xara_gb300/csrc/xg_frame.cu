@@ -76,6 +76,79 @@ __device__ __forceinline__ void steel01_trial(const double *q, const double *hc,
   ht[8] = Ttangent; ht[9] = Tstress; ht[10] = trialStrain;
 }
 
+// Concrete01::setTrial (material/uniaxial/concrete/Concrete01.cpp:209-278)
+// with reload, envelope and unload (:313-385): Kent-Scott-Park envelope
+// (parabola to epsc0, linear to the crushing strain, flat beyond), no
+// tension, unloading toward the end strain of the Karsan-Jirsa ratio.
+// q = fpc epsc0 fpcu epscu, made negative as the constructor does
+// (:89-112).  Record: 0 minStrain 1 endStrain 2 unloadSlope.  A strain
+// within DBL_EPSILON of the committed one leaves the committed state.
+__device__ __forceinline__ void concrete01_trial(const double *q, const double *hc, double strain,
+                                                 double *ht) {
+  const double fpc = -fabs(q[0]), epsc0 = -fabs(q[1]), fpcu = -fabs(q[2]), epscu = -fabs(q[3]);
+  for (int c = 0; c < 12; c++) ht[c] = hc[c];
+  const double Cstrain = hc[10], Cstress = hc[9];
+  if (fabs(strain - Cstrain) < kDblEps) return;
+  double minS = hc[0], endS = hc[1], slope = hc[2];
+  double stress = Cstress, tangent = hc[8];
+  ht[10] = strain;
+  if (strain > 0.0) {
+    ht[8] = 0.0;
+    ht[9] = 0.0;
+    return;
+  }
+  const double tempStress = Cstress + slope * strain - slope * Cstrain;
+  if (strain <= Cstrain) {
+    if (strain <= minS) {
+      minS = strain;
+      const double Ec0 = 2.0 * fpc / epsc0;
+      if (strain > epsc0) {
+        const double eta = strain / epsc0;
+        stress = fpc * (2 * eta - eta * eta);
+        tangent = Ec0 * (1.0 - eta);
+      } else if (strain > epscu) {
+        tangent = (fpc - fpcu) / (epsc0 - epscu);
+        stress = fpc + tangent * (strain - epsc0);
+      } else {
+        stress = fpcu;
+        tangent = 0.0;
+      }
+      const double ts = minS < epscu ? epscu : minS;
+      const double eta = ts / epsc0;
+      const double ratio = eta < 2.0 ? 0.145 * eta * eta + 0.13 * eta : 0.707 * (eta - 2.0) + 0.834;
+      endS = ratio * epsc0;
+      const double temp1 = minS - endS, temp2 = stress / Ec0;
+      if (temp1 > -kDblEps) {
+        slope = Ec0;
+      } else if (temp1 <= temp2) {
+        endS = minS - temp1;
+        slope = stress / temp1;
+      } else {
+        endS = minS - temp2;
+        slope = Ec0;
+      }
+    } else if (strain <= endS) {
+      tangent = slope;
+      stress = tangent * (strain - endS);
+    } else {
+      stress = 0.0;
+      tangent = 0.0;
+    }
+    if (tempStress > stress) {
+      stress = tempStress;
+      tangent = slope;
+    }
+  } else if (tempStress <= 0.0) {
+    stress = tempStress;
+    tangent = slope;
+  } else {
+    stress = 0.0;
+    tangent = 0.0;
+  }
+  ht[0] = minS; ht[1] = endS; ht[2] = slope;
+  ht[8] = tangent; ht[9] = stress;
+}
+
 // Steel02::setTrialStrain (material/uniaxial/steel/Steel02.cpp:113-227).
 // Record slot 11 keeps R, which changes only where the branch does (the
 // reference recomputes the same value every call); q[11] holds Fy/E0 (the
@@ -502,6 +575,15 @@ __device__ __forceinline__ void fbc_section(const FrameView &v, int f0, int nf, 
       for (int c = 0; c < 12; c++) ht[c] = htl[c];
       stress = htl[9];
       tangent = htl[8];
+    } else if (type == XG_UNI_CONCRETE01) {
+      double hcl[12], htl[12];
+#pragma unroll
+      for (int c = 0; c < 12; c++) hcl[c] = hc[c];
+      concrete01_trial(q, hcl, strain, htl);
+#pragma unroll
+      for (int c = 0; c < 12; c++) ht[c] = htl[c];
+      stress = htl[9];
+      tangent = htl[8];
     } else if (type == XG_UNI_CONCRETE02) {
       double hcl[11], htl[11];
       hcl[0] = hc[0]; hcl[1] = hc[1]; hcl[9] = hc[9]; hcl[10] = hc[10];
@@ -599,6 +681,15 @@ __device__ __forceinline__ void fbc_section_group(const FrameView &v, int f0, in
 #pragma unroll
       for (int c = 0; c < 12; c++) hcl[c] = hc[c];
       steel01_trial(q, hcl, strain, htl);
+#pragma unroll
+      for (int c = 0; c < 12; c++) ht[c] = htl[c];
+      stress = htl[9];
+      tangent = htl[8];
+    } else if (type == XG_UNI_CONCRETE01) {
+      double hcl[12], htl[12];
+#pragma unroll
+      for (int c = 0; c < 12; c++) hcl[c] = hc[c];
+      concrete01_trial(q, hcl, strain, htl);
 #pragma unroll
       for (int c = 0; c < 12; c++) ht[c] = htl[c];
       stress = htl[9];

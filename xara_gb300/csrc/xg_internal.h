@@ -426,6 +426,7 @@ struct DdmView {
   const int *eqn;             // [nn*ndf]
   const double *dU;           // [neq] the step's displacement tangent (pass 2)
 };
+int launch_ddm_init_records(const FrameView &v, const DdmView &d, cudaStream_t s);
 int launch_ddm_cond(const FrameView &v, const DdmView &d, cudaStream_t s);
 int launch_ddm_commit(const FrameView &v, const DdmView &d, cudaStream_t s);
 int launch_ddm_rhs(int neq, const double *dPc, const double *dU, const double *dV,

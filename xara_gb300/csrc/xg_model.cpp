@@ -904,11 +904,12 @@ void lobatto_points(int n, double *xi, double *wt) {
   }
 }
 
-// Initial tangent of a uniaxial row (Steel02 E0; Concrete02 2 fc / epsc0
-// after the constructor's sign normalisation, Concrete02.cpp:97-111).
+// Initial tangent of a uniaxial row (Steel02 E0; Concrete02 and Concrete01
+// 2 fc / epsc0 after the constructors' sign normalisation, Concrete02.cpp:
+// 97-111, Concrete01.cpp:89-112).
 double uniaxial_initial_tangent(int type, const double *q) {
   if (type == XG_UNI_STEEL02 || type == XG_UNI_STEEL01) return q[1];
-  if (type == XG_UNI_CONCRETE02) {
+  if (type == XG_UNI_CONCRETE02 || type == XG_UNI_CONCRETE01) {
     const double fc = q[0] > 0 ? -q[0] : q[0], e0 = q[1] > 0 ? -q[1] : q[1];
     return 2.0 * fc / e0;
   }
@@ -929,6 +930,11 @@ void uniaxial_initial_record(int type, const double *q, double *h) {
     h[2] = 1.0;
     h[3] = 1.0;
     h[8] = q[1];
+  } else if (type == XG_UNI_CONCRETE01) {
+    // Concrete01::revertToStart (Concrete01.cpp:435-457): unloading slope
+    // and tangent Ec0
+    h[2] = uniaxial_initial_tangent(type, q);
+    h[8] = h[2];
   } else {
     h[8] = uniaxial_initial_tangent(type, q);
   }
@@ -1961,11 +1967,11 @@ int xg_model::adjoint_forward(const xg_phase_desc *ph, int N, int K, const xg_ob
       if (utype[u] == XG_UNI_STEEL02) {
         if (uparam[(size_t)u * XG_UNI_NPARAM + 10] != 0.0)
           return fail(XG_EINVAL, "the adjoint does not cover Steel02 with an initial stress");
-      } else if (utype[u] == XG_UNI_CONCRETE02) {
+      } else if (utype[u] == XG_UNI_CONCRETE02 || utype[u] == XG_UNI_CONCRETE01) {
         sec_single[sc] = 0;
       } else if (utype[u] != XG_UNI_ELASTIC && utype[u] != XG_UNI_STEEL01) {
-        return fail(XG_EINVAL, "the adjoint covers Steel02, Steel01, Concrete02 and elastic "
-                    "fibers");
+        return fail(XG_EINVAL, "the adjoint covers Steel02, Steel01, Concrete02, Concrete01 and "
+                    "elastic fibers");
       }
       if (m > 0) sec_single[sc] = 0;
     }
@@ -2187,8 +2193,9 @@ int xg_model::ddm_forward(const xg_phase_desc *ph, int N, int nd, const double *
   if (steps_since_reset != 0 || have_phase)
     return fail(XG_ESTATE, "the DDM runs from the model's initial state (xg_reset first)");
   for (size_t u = 0; u < utype.size(); u++)
-    if (utype[u] != XG_UNI_STEEL01 && utype[u] != XG_UNI_ELASTIC)
-      return fail(XG_EINVAL, "the DDM covers Steel01 and elastic fibers (material %d)", (int)u);
+    if (utype[u] != XG_UNI_STEEL01 && utype[u] != XG_UNI_CONCRETE01 && utype[u] != XG_UNI_ELASTIC)
+      return fail(XG_EINVAL, "the DDM covers Steel01, Concrete01 and elastic fibers (material %d)",
+                  (int)u);
   bool bk0 = ph->beta_k_init != 0.0;
   if (ph->beta_k_init_elem)
     for (int e = 0; e < ne; e++) bk0 = bk0 || ph->beta_k_init_elem[e] != 0.0;
@@ -2211,8 +2218,13 @@ int xg_model::ddm_forward(const xg_phase_desc *ph, int N, int nd, const double *
     CK(cudaMemsetAsync(b->p, 0, (size_t)nd * ne1 * sizeof(double), s));
   }
   RET(ddm.dh.alloc((size_t)nd * nrec));
-  CK(cudaMemsetAsync(ddm.dh.p, 0, (size_t)nd * nrec * sizeof(double), s));   // fresh records
   RET(ddm.dth.upload(dtheta, (size_t)nd * nuni3, s));
+  for (int k = 0; k < nd; k++) {             // the fresh records' tangents
+    DdmView dv{};
+    dv.dh = ddm.dh.p + (size_t)k * nrec;
+    dv.dth = ddm.dth.p + (size_t)k * nuni3;
+    RET(launch_ddm_init_records(fview(), dv, s));
+  }
   RET(ddm.fh_prev.alloc(nrec));
   RET(ddm.q.alloc(std::max<size_t>((size_t)ne * fb_nip * 4, 1)));
   RET(ddm.z.alloc(std::max<size_t>((size_t)ne * 6, 1)));
@@ -2436,7 +2448,8 @@ static int plan_model(const xg_model_desc *d, xg_model **out) {
       }
     for (int u = 0; u < nuni; u++)
       if (m->utype[u] != XG_UNI_STEEL02 && m->utype[u] != XG_UNI_CONCRETE02 &&
-          m->utype[u] != XG_UNI_ELASTIC && m->utype[u] != XG_UNI_STEEL01) {
+          m->utype[u] != XG_UNI_ELASTIC && m->utype[u] != XG_UNI_STEEL01 &&
+          m->utype[u] != XG_UNI_CONCRETE01) {
         delete m;
         return fail(XG_EINVAL, "uniaxial row %d: unknown type %d", u, m->utype[u]);
       }

@@ -533,6 +533,235 @@ XG_HD inline void steel01_jvp(const double *q, const double *hc, double strain, 
   dht[9] = ds; dht[10] = dstrain;
 }
 
+// Concrete01 (material/uniaxial/concrete/Concrete01.cpp:209-385) in both
+// modes.  Parameters q = fpc epsc0 fpcu epscu, made negative as the
+// constructor does (:89-112); the derivatives are taken with respect to
+// q[0..2] as given (sg = d internal / d q = -1 for a positive entry).
+// Record: 0 minStrain 1 endStrain 2 unloadSlope, 9 stress, 10 strain.  The
+// branches are the primal's: the committed state kept (a strain within
+// DBL_EPSILON), tension (no stress), a new extreme compression strain (the
+// Kent-Scott-Park envelope, then the unloading slope and end strain from the
+// Karsan-Jirsa ratio), reloading on the committed unloading line, or the
+// elastic return line Cstress + slope (eps - Cstrain) where it governs.
+struct C01d {
+  double fpc, epsc0, fpcu, epscu, sg0, sg1, sg2;
+};
+XG_HD inline C01d c01d_params(const double *q) {
+  C01d c;
+  c.fpc = q[0] > 0.0 ? -q[0] : q[0];
+  c.sg0 = q[0] > 0.0 ? -1.0 : 1.0;
+  c.epsc0 = q[1] > 0.0 ? -q[1] : q[1];
+  c.sg1 = q[1] > 0.0 ? -1.0 : 1.0;
+  c.fpcu = q[2] > 0.0 ? -q[2] : q[2];
+  c.sg2 = q[2] > 0.0 ? -1.0 : 1.0;
+  c.epscu = q[3] > 0.0 ? -q[3] : q[3];
+  return c;
+}
+
+// the new extreme strain's primal quantities (envelope and unloading)
+struct C01Env {
+  int env;                  // 0 parabola, 1 linear descent, 2 crushed
+  int unl;                  // 0 slope Ec0 (no room), 1 secant to the end strain, 2 Ec0 line
+  bool clamp;               // the unloading ratio reads epscu
+  double Ec0, eta, t, den, sig, ts, etau, ratio, rprime, endS0, temp1, temp2;
+};
+XG_HD inline C01Env c01_envelope(const C01d &c, double strain) {
+  C01Env v;
+  v.Ec0 = 2.0 * c.fpc / c.epsc0;
+  v.eta = v.t = v.den = 0.0;
+  if (strain > c.epsc0) {
+    v.env = 0;
+    v.eta = strain / c.epsc0;
+    v.sig = c.fpc * (2 * v.eta - v.eta * v.eta);
+  } else if (strain > c.epscu) {
+    v.env = 1;
+    v.den = c.epsc0 - c.epscu;
+    v.t = (c.fpc - c.fpcu) / v.den;
+    v.sig = c.fpc + v.t * (strain - c.epsc0);
+  } else {
+    v.env = 2;
+    v.sig = c.fpcu;
+  }
+  v.clamp = strain < c.epscu;
+  v.ts = v.clamp ? c.epscu : strain;
+  v.etau = v.ts / c.epsc0;
+  if (v.etau < 2.0) {
+    v.ratio = 0.145 * v.etau * v.etau + 0.13 * v.etau;
+    v.rprime = 0.29 * v.etau + 0.13;
+  } else {
+    v.ratio = 0.707 * (v.etau - 2.0) + 0.834;
+    v.rprime = 0.707;
+  }
+  v.endS0 = v.ratio * c.epsc0;
+  v.temp1 = strain - v.endS0;
+  v.temp2 = v.sig / v.Ec0;
+  v.unl = v.temp1 > -DBL_EPSILON ? 0 : (v.temp1 <= v.temp2 ? 1 : 2);
+  return v;
+}
+
+XG_HD inline void concrete01_jvp(const double *q, const double *hc, double strain, double dstrain,
+                                 const double *dhc, const double *dq, double *dht) {
+  const C01d c = c01d_params(q);
+  const double dfpc = c.sg0 * dq[0], de0 = c.sg1 * dq[1], dfpcu = c.sg2 * dq[2];
+  for (int k = 0; k < 12; k++) dht[k] = 0.0;
+  const double Cstrain = hc[10], Cstress = hc[9];
+  if (fabs(strain - Cstrain) < DBL_EPSILON) {
+    dht[0] = dhc[0]; dht[1] = dhc[1]; dht[2] = dhc[2]; dht[9] = dhc[9]; dht[10] = dhc[10];
+    return;
+  }
+  double dmin = dhc[0], dend = dhc[1], dslope = dhc[2], ds = 0.0;
+  dht[10] = dstrain;
+  if (!(strain > 0.0)) {
+    const double slope = hc[2];
+    const double temp = Cstress + slope * strain - slope * Cstrain;
+    const double dtemp = dhc[9] + dhc[2] * (strain - Cstrain) + slope * (dstrain - dhc[10]);
+    if (strain <= Cstrain) {
+      double stress;
+      if (strain <= hc[0]) {
+        const C01Env v = c01_envelope(c, strain);
+        const double e02 = c.epsc0 * c.epsc0;
+        const double dEc0 = 2.0 * dfpc / c.epsc0 - 2.0 * c.fpc * de0 / e02;
+        double dsig;
+        if (v.env == 0) {
+          const double deta = dstrain / c.epsc0 - strain * de0 / e02;
+          dsig = dfpc * (2 * v.eta - v.eta * v.eta) + c.fpc * (2.0 - 2.0 * v.eta) * deta;
+        } else if (v.env == 1) {
+          const double dt = (dfpc - dfpcu) / v.den - v.t * de0 / v.den;
+          dsig = dfpc + dt * (strain - c.epsc0) + v.t * (dstrain - de0);
+        } else {
+          dsig = dfpcu;
+        }
+        dmin = dstrain;
+        const double dts = v.clamp ? 0.0 : dmin;
+        const double detau = dts / c.epsc0 - v.ts * de0 / e02;
+        const double dend0 = v.rprime * detau * c.epsc0 + v.ratio * de0;
+        const double dtemp1 = dmin - dend0;
+        const double dtemp2 = dsig / v.Ec0 - v.sig * dEc0 / (v.Ec0 * v.Ec0);
+        if (v.unl == 0) {
+          dslope = dEc0;
+          dend = dend0;
+        } else if (v.unl == 1) {
+          dend = dmin - dtemp1;
+          dslope = dsig / v.temp1 - v.sig * dtemp1 / (v.temp1 * v.temp1);
+        } else {
+          dend = dmin - dtemp2;
+          dslope = dEc0;
+        }
+        stress = v.sig;
+        ds = dsig;
+      } else if (strain <= hc[1]) {
+        stress = slope * (strain - hc[1]);
+        ds = dhc[2] * (strain - hc[1]) + slope * (dstrain - dhc[1]);
+      } else {
+        stress = 0.0;
+      }
+      if (temp > stress) ds = dtemp;
+    } else if (temp <= 0.0) {
+      ds = dtemp;
+    }
+  }
+  dht[0] = dmin; dht[1] = dend; dht[2] = dslope; dht[9] = ds;
+}
+
+XG_HD inline void concrete01_vjp(const double *q, const double *hc, double strain, const double *yb,
+                                 double *hb, double *sb, double *qb) {
+  const C01d c = c01d_params(q);
+  for (int k = 0; k < 12; k++) hb[k] = 0.0;
+  qb[0] = qb[1] = qb[2] = 0.0;
+  *sb = 0.0;
+  const double Cstrain = hc[10], Cstress = hc[9];
+  if (fabs(strain - Cstrain) < DBL_EPSILON) {
+    hb[0] = yb[0]; hb[1] = yb[1]; hb[2] = yb[2]; hb[9] = yb[9]; hb[10] = yb[10];
+    return;
+  }
+  double g_eps = yb[10];
+  if (strain > 0.0) {
+    hb[0] = yb[0]; hb[1] = yb[1]; hb[2] = yb[2];
+    *sb = g_eps;
+    return;
+  }
+  const double gs = yb[9];
+  const double slope = hc[2];
+  const double temp = Cstress + slope * strain - slope * Cstrain;
+  double g_temp = 0.0, g_fpc = 0.0, g_e0 = 0.0, g_fpcu = 0.0;
+  if (strain <= Cstrain) {
+    if (strain <= hc[0]) {
+      const C01Env v = c01_envelope(c, strain);
+      const bool use_temp = temp > v.sig;
+      const double e02 = c.epsc0 * c.epsc0;
+      double g_sig = use_temp ? 0.0 : gs;
+      if (use_temp) g_temp = gs;
+      double g_min = yb[0], g_Ec0 = 0.0, g_end0 = 0.0, g_temp1 = 0.0, g_temp2 = 0.0;
+      const double gend = yb[1], gslope = yb[2];
+      if (v.unl == 0) {
+        g_Ec0 += gslope;
+        g_end0 += gend;
+      } else if (v.unl == 1) {
+        g_min += gend;
+        g_temp1 -= gend;
+        g_sig += gslope / v.temp1;
+        g_temp1 -= gslope * v.sig / (v.temp1 * v.temp1);
+      } else {
+        g_min += gend;
+        g_temp2 -= gend;
+        g_Ec0 += gslope;
+      }
+      g_sig += g_temp2 / v.Ec0;
+      g_Ec0 -= g_temp2 * v.sig / (v.Ec0 * v.Ec0);
+      g_min += g_temp1;
+      g_end0 -= g_temp1;
+      const double g_etau = g_end0 * c.epsc0 * v.rprime;
+      g_e0 += g_end0 * v.ratio;
+      if (!v.clamp) g_min += g_etau / c.epsc0;
+      g_e0 -= g_etau * v.ts / e02;
+      if (v.env == 0) {
+        g_fpc += g_sig * (2 * v.eta - v.eta * v.eta);
+        const double g_eta = g_sig * c.fpc * (2.0 - 2.0 * v.eta);
+        g_eps += g_eta / c.epsc0;
+        g_e0 -= g_eta * strain / e02;
+      } else if (v.env == 1) {
+        g_fpc += g_sig;
+        const double g_t = g_sig * (strain - c.epsc0);
+        g_eps += g_sig * v.t;
+        g_e0 -= g_sig * v.t;
+        g_fpc += g_t / v.den;
+        g_fpcu -= g_t / v.den;
+        g_e0 -= g_t * v.t / v.den;
+      } else {
+        g_fpcu += g_sig;
+      }
+      g_fpc += 2.0 * g_Ec0 / c.epsc0;
+      g_e0 -= 2.0 * g_Ec0 * c.fpc / e02;
+      g_eps += g_min;
+    } else {
+      hb[0] = yb[0]; hb[1] = yb[1]; hb[2] = yb[2];
+      if (strain <= hc[1]) {
+        const double stress = slope * (strain - hc[1]);
+        if (temp > stress) {
+          g_temp = gs;
+        } else {
+          hb[2] += gs * (strain - hc[1]);
+          g_eps += gs * slope;
+          hb[1] -= gs * slope;
+        }
+      } else if (temp > 0.0) {
+        g_temp = gs;
+      }
+    }
+  } else {
+    hb[0] = yb[0]; hb[1] = yb[1]; hb[2] = yb[2];
+    if (temp <= 0.0) g_temp = gs;
+  }
+  hb[9] += g_temp;
+  hb[2] += g_temp * (strain - Cstrain);
+  g_eps += g_temp * slope;
+  hb[10] -= g_temp * slope;
+  *sb = g_eps;
+  qb[0] = c.sg0 * g_fpc;
+  qb[1] = c.sg1 * g_e0;
+  qb[2] = c.sg2 * g_fpcu;
+}
+
 // the elastic law sigma = E eps in forward mode (dq[0] = dE)
 XG_HD inline void elastic_jvp(const double *q, double strain, double dstrain, const double *dq,
                               double *dht) {

@@ -15,7 +15,8 @@ GPU through :class:`xara_gb300.gpu.DeviceModel`::
 
 Covered: ``element quad`` (plane strain J2Plasticity), ``element stdBrick``
 (J2Plasticity), ``element forceBeamColumn`` (fiber sections of Steel02,
-Concrete02 and Elastic fibers, Lobatto integration, Linear and PDelta
+Concrete02, Steel01, Concrete01 and Elastic fibers, Lobatto integration,
+Linear and PDelta
 transformations; one element type per model), ``fix``, ``equalDOF``,
 ``mass``, Plain patterns with a Linear series (nodal loads, ``sp``),
 ``pattern UniformExcitation`` with a Path series, ``rayleigh``,
@@ -41,7 +42,8 @@ from ._abi import (ModelDesc, PhaseDesc, XG_ELE_BRICK, XG_ELE_FBC2D, XG_ELE_FBC3
                    XG_INT_LOAD_CONTROL, XG_INT_NEWMARK, XG_REC_ACCEL, XG_REC_DISP,
                    XG_REC_ENVELOPE, XG_REC_NODE, XG_REC_VEL, XG_SYSTEM_BJPCG,
                    XG_SYSTEM_PROFILE_SPD, XG_TEST_NORM_DISP_INCR, XG_TEST_NORM_UNBALANCE,
-                   XG_UNI_CONCRETE02, XG_UNI_ELASTIC, XG_UNI_NPARAM, XG_UNI_STEEL02)
+                   XG_UNI_CONCRETE01, XG_UNI_CONCRETE02, XG_UNI_ELASTIC, XG_UNI_NPARAM,
+                   XG_UNI_STEEL01, XG_UNI_STEEL02)
 
 
 class _State:
@@ -159,6 +161,17 @@ def uniaxialMaterial(kind, tag, *args):
     elif kind == "Concrete02":
         row[:7] = v[:7]
         _S.uni[int(tag)] = (XG_UNI_CONCRETE02, row)
+    elif kind == "Steel01":
+        # fy E0 b <a1 a2 a3 a4> (Steel01.h defaults 0 55 0 55)
+        d = [None, None, None, 0.0, 55.0, 0.0, 55.0]
+        for i, x in enumerate(v[:7]):
+            d[i] = x
+        row[:7] = d
+        _S.uni[int(tag)] = (XG_UNI_STEEL01, row)
+    elif kind == "Concrete01":
+        # fpc epsc0 fpcu epscu
+        row[:4] = v[:4]
+        _S.uni[int(tag)] = (XG_UNI_CONCRETE01, row)
     elif kind == "Elastic":
         row[0] = v[0]
         _S.uni[int(tag)] = (XG_UNI_ELASTIC, row)
