@@ -719,13 +719,14 @@ __global__ void __launch_bounds__(32 * kAdjWarps) k_ddm_commit(FrameView v, DdmV
 
 // Record tangents of the fresh materials: Concrete01's unloading slope
 // Ec0 = 2 fpc / epsc0 (Concrete01::revertToStart); Steel01 and elastic
-// records do not depend on the parameters.  Thread per fiber record.
+// records do not depend on the parameters.  Block per element, a thread
+// per fiber record.
 __global__ void k_ddm_init_records(FrameView v, DdmView d) {
-  const int e = blockIdx.y;
+  const int e = blockIdx.x;
   if (e >= v.ne) return;
   const int sec = v.sec[e];
   const int f0 = v.sec_fstart[sec], nf = v.sec_fstart[sec + 1] - f0;
-  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < v.nip * nf; k += gridDim.x * blockDim.x) {
+  for (int k = threadIdx.x; k < v.nip * nf; k += blockDim.x) {
     const int kf = f0 + k % nf;
     const int u = v.fmat[kf];
     double *dh = d.dh + (v.foff[e] + k) * 12;
@@ -817,7 +818,7 @@ int launch_ddm_commit(const FrameView &v, const DdmView &d, cudaStream_t s) {
 
 int launch_ddm_init_records(const FrameView &v, const DdmView &d, cudaStream_t s) {
   if (v.ne == 0) return 0;
-  k_ddm_init_records<<<dim3(1, v.ne), 128, 0, s>>>(v, d);
+  k_ddm_init_records<<<v.ne, 128, 0, s>>>(v, d);
   return cudaGetLastError() == cudaSuccess ? 0 : XG_ECUDA;
 }
 
