@@ -3016,8 +3016,9 @@ int xg_ddm_disp_sensitivity(const xg_model *m, int dir, double *out) {
   if (dir < 0 || dir >= m->ddm.nd) return fail(XG_EINVAL, "bad direction %d", dir);
   std::vector<double> x(std::max(m->neq, 1));
   const size_t ne1 = std::max(m->neq, 1);
-  if (cudaMemcpy(x.data(), m->ddm.dU.p + (size_t)dir * ne1, ne1 * sizeof(double),
-                 cudaMemcpyDeviceToHost) != cudaSuccess)
+  if (cudaMemcpyAsync(x.data(), m->ddm.dU.p + (size_t)dir * ne1, ne1 * sizeof(double),
+                      cudaMemcpyDeviceToHost, m->stream) != cudaSuccess ||
+      cudaStreamSynchronize(m->stream) != cudaSuccess)
     return fail(XG_ECUDA, "copy failed");
   for (size_t a = 0; a < m->eqn.size(); a++) out[a] = m->eqn[a] >= 0 ? x[m->eqn[a]] : 0.0;
   return 0;
