@@ -1022,7 +1022,12 @@ def run_adjoint_fd(args):
     * for the frames that disagree, adjoint and central differences again,
       over the record up to the step before that switch;
     * the adjoint and central differences at h = 1e-4 ... 1e-8 over 300,
-      1,000 and 2,000 steps."""
+      1,000 and 2,000 steps;
+    * the direct differentiation (DDM, forward mode, independent code) along
+      the same direction, frame by frame through each frame's objective
+      term, against the adjoint over the whole record.
+
+    ``--fd-parts ddm`` stops after the whole-record comparison of the three."""
     world, rank, local, torch, dist = dist_setup()
     if rank != 0:
         return None
@@ -1060,10 +1065,41 @@ def run_adjoint_fd(args):
         return np.abs(a - b) / np.maximum(np.abs(b), 1e-300)
 
     h0 = 1e-6
+    ta = time.perf_counter()
     ad_full = adjoint(N)
+    t_adjoint = time.perf_counter() - ta
     fd_full = central(N, h0)
     rel_full = rel(ad_full, fd_full)
     bad = [int(f) for f in np.nonzero(rel_full > 1e-3)[0]]
+    # the DDM along d: every frame's directional derivative from its term
+    m.reset()
+    gpu.set_uniaxial_params(m, q0)
+    td = time.perf_counter()
+    gpu.ddm_forward(m, ph, N, d[None], *obj)
+    t_ddm = time.perf_counter() - td
+    ddm_full = gpu.ddm_objective_terms(m, 0, nf)
+    m.reset()
+    rel_ddm = rel(ad_full, ddm_full)
+    ddm = {"median_relative_difference_to_adjoint": float(np.median(rel_ddm)),
+           "max_relative_difference_to_adjoint": float(rel_ddm.max()),
+           "frames_within_1e-9": int((rel_ddm < 1e-9).sum()),
+           "disagreeing_frames": {str(f): {"adjoint": float(ad_full[f]), "ddm": float(ddm_full[f]),
+                                           "central": float(fd_full[f])} for f in bad},
+           "adjoint_s": t_adjoint, "ddm_s": t_ddm}
+    if getattr(args, "fd_parts", "all") == "ddm":
+        m.close()
+        return {
+            "metric": "adjoint vs DDM vs central differences, frame by frame",
+            "unit": "relative difference",
+            "config": {"workload": f"gradient of the summed squared roof drift of {nf} 2D steel "
+                                   f"frames over {N} Newmark steps w.r.t. every member's Steel02 "
+                                   f"Fy, E0, b; one random direction", "frames": nf,
+                       "members": int(desc.num_elems), "checkpoint_every": K},
+            "whole_record": {"h": h0, "median": float(np.median(rel_full)),
+                             "within_1e-6": int((rel_full < 1e-6).sum()),
+                             "within_1e-3": int((rel_full < 1e-3).sum()),
+                             "disagreeing_frames": bad},
+            "ddm": ddm, "wall_s": time.perf_counter() - t0}
 
     # the first step at which the +h and -h runs take different branches
     runs = []
@@ -1126,6 +1162,7 @@ def run_adjoint_fd(args):
         "first_branch_switch_step": {str(f): int(first[f]) for f in range(nf)},
         "disagreeing_frames_before_their_switch": {str(f): v for f, v in before.items()},
         "h_sweep": sweep,
+        "ddm": ddm,
         "wall_s": time.perf_counter() - t0,
     }
 
@@ -1442,6 +1479,9 @@ def main():
     ap.add_argument("--adj-frames", type=int, default=64)
     ap.add_argument("--adj-steps", type=int, default=2000)
     ap.add_argument("--ckpt-every", type=int, default=100)
+    ap.add_argument("--fd-parts", default="all", choices=["all", "ddm"],
+                    help="adjoint-fd: the whole study, or only the adjoint / DDM / central "
+                         "difference comparison over the whole record")
     ap.add_argument("--brick-dims", type=int, nargs=3, default=[BRICK["nx"], BRICK["ny"], BRICK["nz"]],
                     metavar=("NX", "NY", "NZ"), help="brick workload mesh (a smaller case for profiling)")
     args = ap.parse_args()

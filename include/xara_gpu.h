@@ -482,29 +482,34 @@ int xg_adjoint_backward(xg_model *m, double scale, double *grad, int num_uni);
         ForceBeamColumn2d's basic-force sensitivity and commitSensitivity,
         ForceBeamColumn2d.cpp:2890-3007; Steel01::getStressSensitivity and
         commitSensitivity, Steel01.cpp:552-660; Concrete01's, Concrete01.cpp:
-        655-775), a forward-mode path
-        independent of the adjoint above.  Covers 2D and 3D force-based frames
-        (Linear transformations in 2D; Linear or PDelta in 3D) with Steel01,
-        Concrete01 and elastic fibers, Newmark with alphaM Rayleigh damping (no
-        betaK0), UniformExcitation and nodal load patterns, from the model's
-        initial state.  After each converged step the effective tangent is
-        formed again at the converged state (the reference solves with the
-        last Newton iteration's factors). ---- */
+        655-775), a forward-mode path independent of the adjoint above.
+        Covers 2D and 3D force-based frames (Linear transformations in 2D;
+        Linear or PDelta in 3D) with Steel02 (no initial stress; the
+        reference has no Steel02 sensitivity), Steel01, Concrete01 and
+        elastic fibers, Newmark with alphaM Rayleigh damping (no betaK0),
+        UniformExcitation and nodal load patterns, from the model's initial
+        state.  After each converged step the effective tangent is formed
+        again at the converged state (the reference solves with the last
+        Newton iteration's factors). ---- */
 /* Newmark run of num_steps from the initial state carrying num_dir
    directions: dtheta[(k*num_uni + u)*3 + j] is direction k's tangent of
-   parameter j (0..2) of material u (Steel01: fy, E0, b; Concrete01: fpc,
-   epsc0, fpcu; elastic: E).
+   parameter j (0..2) of material u (Steel02 and Steel01: fy, E0, b;
+   Concrete01: fpc, epsc0, fpcu; elastic: E).
    J as xg_adjoint_forward; dJ[k] = the derivative of J along direction k. */
 int xg_ddm_forward(xg_model *m, const xg_phase_desc *ph, int num_steps, int num_dir,
                    const double *dtheta, const xg_objective_desc *obj, double *J, double *dJ);
+/* The last DDM run's dJ along direction dir term by term (dJ[dir] is their
+   sum in term order); for separate models batched into one, each term
+   gives its own model's directional derivative. */
+int xg_ddm_objective_terms(const xg_model *m, int dir, double *dJk, int num_terms);
 /* The last DDM run's displacement tangent of direction dir after its last
    step, out[num_nodes*ndf] (zero on constrained dofs; `sensNodeDisp`). */
 int xg_ddm_disp_sensitivity(const xg_model *m, int dir, double *out);
 /* Jacobian-vector product of one material point's trial record (host only;
-   Steel01, Concrete01 or elastic): given the tangents of the strain, of
-   the committed record dhc[12] and of parameters 0-2 dq[3], the tangent of
-   the trial record dht[12] (Steel01 fields 0-3, Concrete01 0-2, 9 stress,
-   10 strain). */
+   Steel02, Steel01, Concrete01 or elastic): given the tangents of the
+   strain, of the committed record dhc[12] and of parameters 0-2 dq[3], the
+   tangent of the trial record dht[12] (Steel02 fields 0-6, Steel01 0-3,
+   Concrete01 0-2, 9 stress, 10 strain). */
 int xg_uniaxial_jvp(int type, const double *q, const double *hc, double strain,
                     double dstrain, const double *dhc, const double *dq, double *dht);
 /* Vector-Jacobian product of one material point's trial record (host only;

@@ -106,6 +106,56 @@ def test_steel02_vjp_against_finite_differences(shift):
         _fd_check(q, port.uniaxial_init(XG_UNI_STEEL02, q), e, rng)
 
 
+@pytest.mark.parametrize("shift", [False, True])
+def test_steel02_jvp_against_the_vjp_and_finite_differences(shift):
+    """Steel02 in forward mode (the DDM's law, written step by step from the
+    primal) along the VJP test's path: equal to the reverse mode through
+    y.(Jt) = (J'y).t at every point, and to central differences of the
+    oracle's law in random directions of (strain, record, parameters) --
+    where the record sits on a first-loading branch (epspl = epss0, the kink
+    of R in their difference) the two move together."""
+    gpu = _gpu()
+    q = configs.steel02_row(fy=350e6, E=200e9, b=0.015, R0=18.0)
+    if shift:
+        q[6:10] = [0.04, 1.0, 0.04, 1.0]
+    ey = q[0] / q[1]
+    t = np.linspace(0.0, 6.0 * np.pi, 240)
+    strains = ey * (0.5 + 0.05 * t) * np.sin(t) * 3.0
+    rng = np.random.default_rng(17)
+    sc = _scales(q)
+    fields = list(FIELDS)
+    checked = 0
+    for hc, eps in _path_states(q, strains)[1:]:
+        de = rng.normal() * ey
+        dhc = np.zeros(12)
+        dhc[fields] = rng.normal(size=len(fields)) * sc[fields]
+        if int(hc[7]) in (1, 2) and hc[2] == hc[3]:
+            dhc[3] = dhc[2]
+        dq = rng.normal(size=3) * q[:3]
+        dht = gpu.uniaxial_jvp(XG_UNI_STEEL02, q, hc, eps, de, dhc, dq)
+        yb = np.zeros(12)
+        yb[fields] = rng.normal(size=len(fields)) / sc[fields]
+        hb, sb, qb = gpu.uniaxial_vjp(XG_UNI_STEEL02, q, hc, eps, yb)
+        terms = [sb * de, *(hb[f] * dhc[f] for f in fields), *(qb * dq)]
+        assert abs(float(yb @ dht) - sum(terms)) <= 1e-11 * sum(abs(x) for x in terms), eps
+        if abs(eps - hc[10]) < 1e-4 * ey:
+            continue
+        rel = 1e-7
+        hp, hm = hc + rel * dhc, hc - rel * dhc
+        hp[7] = hm[7] = hc[7]
+        qp, qm = q.copy(), q.copy()
+        qp[:3] += rel * dq
+        qm[:3] -= rel * dq
+        qp[11] = qp[0] / qp[1]
+        qm[11] = qm[0] / qm[1]
+        fd = (port.uniaxial_trial(XG_UNI_STEEL02, qp, hp, eps + rel * de) -
+              port.uniaxial_trial(XG_UNI_STEEL02, qm, hm, eps - rel * de)) / (2 * rel)
+        for f in (0, 1, 2, 3, 4, 5, 6, 9, 10):
+            assert abs(dht[f] - fd[f]) <= 1e-7 * sc[f], (eps, f, dht[f], fd[f])
+        checked += 1
+    assert checked > 200
+
+
 def test_steel02_vjp_zero_increment_and_elastic():
     gpu = _gpu()
     q = configs.steel02_row()
@@ -248,8 +298,8 @@ def test_steel01_jvp_against_finite_differences_and_the_vjp(shift):
                            np.zeros(12), dq)
     assert dht[9] == pytest.approx(2e9 * 1e-3 + 200e9 * 1e-4) and dht[10] == de
     with pytest.raises(_gpu().XaraGpuError):
-        gpu.uniaxial_jvp(XG_UNI_STEEL02, configs.steel02_row(), np.zeros(12), 1e-3, de,
-                         np.zeros(12), dq)
+        gpu.uniaxial_jvp(XG_UNI_CONCRETE02, configs.concrete02_row(30e6), np.zeros(12), 1e-3,
+                         de, np.zeros(12), dq)
 
 
 C01_FIELDS = (0, 1, 2, 9, 10)          # minStrain, endStrain, unloadSlope, sig, eps
@@ -884,13 +934,41 @@ def test_ddm_3d_frame_and_refusals(need_gpu):
     assert (np.abs(rec[:, 10]) > 1e-3).mean() > 0.01          # some fibers yield
     for k in range(2):
         assert dJ[k] == pytest.approx(float((ga * dirs[k]).sum()), rel=1e-9), k
-    d2, p2 = configs.adjoint_frames(n_frames=1, steps=5, seed=3)
+    d2, p2 = configs.adjoint_rc_frames(n_frames=1, steps=5, seed=3)
     with gpu.DeviceModel(d2) as m:
-        with pytest.raises(gpu.XaraGpuError, match="Steel01"):
+        with pytest.raises(gpu.XaraGpuError, match="Concrete01"):
             gpu.ddm_forward(m, p2[0], 5, np.zeros((1, len(d2.uni_type), 3)),
                             *_objective(d2))
-    d3, p3 = configs.ddm_steel01_frames_eq(n_frames=1, steps=5, seed=3)
+    d3, p3 = configs.adjoint_rc_frames(n_frames=1, steps=5, seed=3, laws="01")
     p3[0].beta_k_init_elem = np.full(len(d3.arrays["elem_tag"]), 1e-3)
     with gpu.DeviceModel(d3) as m:
         with pytest.raises(gpu.XaraGpuError, match="betaK0"):
             gpu.ddm_forward(m, p3[0], 5, np.zeros((1, len(d3.uni_type), 3)), *_objective(d3))
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("pga_scale,steps", [(1.0, 40), (6.0, 120)])
+def test_ddm_of_the_adjoint_frames_frame_by_frame(need_gpu, pga_scale, steps):
+    """The adjoint's own frames (Steel02 members, 2 % Rayleigh with betaK0 per
+    frame; the second case through yielding and reversals): one DDM
+    direction over every member gives each frame's directional derivative
+    through that frame's objective term, equal to the adjoint's gradient
+    projected on the frame's members (1e-9 of the frame's value)."""
+    gpu = _gpu()
+    desc, ph = _adjoint_model(n_frames=3, steps=steps, pga_scale=pga_scale, seed=7)
+    node, dof, w = _objective(desc)
+    q0 = desc.uni_param.reshape(-1, 12)
+    frame = np.asarray(desc.meta["member_frame"])
+    rng = np.random.default_rng(37)
+    d = rng.normal(size=(1, len(q0), 3)) * np.abs(q0[:, :3])
+    with gpu.DeviceModel(desc) as m:
+        J, dJ = gpu.ddm_forward(m, ph, steps, d, node, dof, w)
+        per_frame = gpu.ddm_objective_terms(m, 0, len(node))
+        m.reset()
+        Ja = gpu.adjoint_forward(m, ph, steps, 10, node, dof, w)
+        ga = gpu.adjoint_backward(m)
+    assert J == Ja
+    assert dJ[0] == pytest.approx(per_frame.sum(), rel=1e-12)
+    for f in range(len(node)):
+        proj = float((ga[frame == f] * d[0][frame == f]).sum())
+        assert per_frame[f] == pytest.approx(proj, rel=1e-9), f

@@ -530,7 +530,8 @@ __global__ void k_adj_prev(int neq, const double *mu, const double *kmu, const d
 __device__ __forceinline__ void fiber_jvp(int type, const double *q, const double *hc,
                                           double strain, double dstrain, const double *dhc,
                                           const double *dq, double *dht) {
-  if (type == XG_UNI_STEEL01) steel01_jvp(q, hc, strain, dstrain, dhc, dq, dht);
+  if (type == XG_UNI_STEEL02) steel02_jvp(q, hc, strain, dstrain, dhc, dq, dht);
+  else if (type == XG_UNI_STEEL01) steel01_jvp(q, hc, strain, dstrain, dhc, dq, dht);
   else if (type == XG_UNI_CONCRETE01) concrete01_jvp(q, hc, strain, dstrain, dhc, dq, dht);
   else elastic_jvp(q, strain, dstrain, dq, dht);
 }
@@ -717,7 +718,8 @@ __global__ void __launch_bounds__(32 * kAdjWarps) k_ddm_commit(FrameView v, DdmV
   }
 }
 
-// Record tangents of the fresh materials: Concrete01's unloading slope
+// Record tangents of the fresh materials: Steel02's epsmax = Fy/E0 and
+// epsmin = -Fy/E0 (Steel02::revertToStart), Concrete01's unloading slope
 // Ec0 = 2 fpc / epsc0 (Concrete01::revertToStart); Steel01 and elastic
 // records do not depend on the parameters.  Block per element, a thread
 // per fiber record.
@@ -731,11 +733,85 @@ __global__ void k_ddm_init_records(FrameView v, DdmView d) {
     const int u = v.fmat[kf];
     double *dh = d.dh + (v.foff[e] + k) * 12;
     for (int j = 0; j < 12; j++) dh[j] = 0.0;
-    if (v.utype[u] != XG_UNI_CONCRETE01) continue;
-    const C01d c = c01d_params(v.uparam + (long)u * XG_UNI_NPARAM);
+    const double *q = v.uparam + (long)u * XG_UNI_NPARAM;
     const double *dq = d.dth + 3L * u;
-    dh[2] = 2.0 * c.sg0 * dq[0] / c.epsc0 - 2.0 * c.fpc * c.sg1 * dq[1] / (c.epsc0 * c.epsc0);
+    if (v.utype[u] == XG_UNI_STEEL02) {
+      dh[1] = dq[0] / q[1] - q[0] * dq[1] / (q[1] * q[1]);
+      dh[0] = -dh[1];
+    } else if (v.utype[u] == XG_UNI_CONCRETE01) {
+      const C01d c = c01d_params(q);
+      dh[2] = 2.0 * c.sg0 * dq[0] / c.epsc0 - 2.0 * c.fpc * c.sg1 * dq[1] / (c.epsc0 * c.epsc0);
+    }
   }
+}
+
+// The betaK0 damping force's tangent at fixed velocity, added to the
+// conditional force tangent: an element under betaK0 has one Steel02,
+// Steel01 or elastic material, in which its initial stiffness K0 = T' kv0 T
+// (ForceBeamColumn2d/3d::getInitialStiff) is linear in E, so d(betaK0 K0 V)
+// = betaK0 (dE / E) K0 V.  Thread per element.
+template <int NB, int ORD>
+__global__ void k_ddm_k0(FrameView v, DdmView d) {
+  constexpr int NU = NB == 3 ? 6 : 12;
+  const int e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= v.ne) return;
+  const double bk = d.bk0 ? d.bk0[e] : d.bk0_all;
+  if (bk == 0.0) return;
+  const int u = d.elem_uni[e];
+  const int ie = (v.utype[u] == XG_UNI_STEEL02 || v.utype[u] == XG_UNI_STEEL01) ? 1 : 0;
+  const double E = v.uparam[(long)u * XG_UNI_NPARAM + ie], dE = d.dth[3L * u + ie];
+  if (dE == 0.0) return;
+  constexpr int kRow[6] = {0, 1, 1, 2, 2, 3};
+  const double L = v.L[e];
+  const double *fs0 = v.fs0 + 16 * (long)v.sec[e];
+  double f[NB * NB];
+#pragma unroll
+  for (int i = 0; i < NB * NB; i++) f[i] = 0.0;
+  for (int ip = 0; ip < v.nip; ip++) {
+    const double xL = v.xi[ip], xL1 = xL - 1.0, wtL = v.wt[ip] * L;
+    const double ca[6] = {1.0, xL1, xL, xL1, xL, 1.0};
+#pragma unroll
+    for (int c = 0; c < NB; c++)
+#pragma unroll
+      for (int k = 0; k < NB; k++) f[c * NB + k] += ca[c] * wtL * (fs0[kRow[c] * ORD + kRow[k]] * ca[k]);
+  }
+  double kv0[NB * NB];
+  small_inverse<NB>(f, kv0);
+  double T[NB][NU];
+  basic_T<NB>(v, e, T);
+  const int nd = NU / 2;
+  double rv[NB];
+#pragma unroll
+  for (int i = 0; i < NB; i++) {
+    double t = 0.0;
+#pragma unroll
+    for (int j = 0; j < NU; j++) t += T[i][j] * d.Vn[(long)v.conn[2 * e + j / nd] * v.ndf + j % nd];
+    rv[i] = t;
+  }
+  double kr[NB];
+#pragma unroll
+  for (int i = 0; i < NB; i++) {
+    double t = 0.0;
+#pragma unroll
+    for (int k = 0; k < NB; k++) t += kv0[i * NB + k] * rv[k];
+    kr[i] = bk * dE / E * t;
+  }
+  double *re = v.Re + (long)e * NU;
+#pragma unroll
+  for (int j = 0; j < NU; j++) {
+    double t = 0.0;
+#pragma unroll
+    for (int k = 0; k < NB; k++) t += T[k][j] * kr[k];
+    re[j] += t;
+  }
+}
+
+// c2 dU' - a1 dV' - a2 dA': the previous step's tangents as the damping
+// term K0 (c2 (U - U') - a1 V' - a2 A') sees them
+__global__ void k_ddm_k0_vec(int neq, const double *dU, const double *dV, const double *dA,
+                             NewmarkCoef c, double *out) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < neq) out[i] = c.c2 * dU[i] - c.a1 * dV[i] - c.a2 * dA[i];
 }
 
 // rhs = -dP_cond + M (c3 dU' - a3 dV' - a4 dA') + alphaM M (c2 dU' - a1 dV' - a2 dA'):
@@ -761,16 +837,13 @@ __global__ void k_ddm_update(int neq, const double *x, NewmarkCoef c, double *dU
   dU[i] = x[i];
 }
 
-// dJ += sum over the terms (in order) of 2 w_k U[dof_k] dU[eqn[dof_k]]
+// dJ[k] += 2 w_k U[dof_k] dU[eqn[dof_k]], one accumulator per term
 __global__ void k_ddm_objective(int nterm, const int *dof, const double *w, const int *eqn,
                                 const double *U, const double *dU, double *dJ) {
-  if (blockIdx.x != 0 || threadIdx.x != 0) return;
-  double s = 0.0;
-  for (int k = 0; k < nterm; k++) {
-    const int eq = eqn[dof[k]];
-    if (eq >= 0) s += 2.0 * w[k] * U[dof[k]] * dU[eq];
-  }
-  *dJ += s;
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= nterm) return;
+  const int eq = eqn[dof[k]];
+  if (eq >= 0) dJ[k] += 2.0 * w[k] * U[dof[k]] * dU[eq];
 }
 
 inline int grid_of(long n, int b) { return (int)((n + b - 1) / b); }
@@ -822,6 +895,20 @@ int launch_ddm_init_records(const FrameView &v, const DdmView &d, cudaStream_t s
   return cudaGetLastError() == cudaSuccess ? 0 : XG_ECUDA;
 }
 
+int launch_ddm_k0(const FrameView &v, const DdmView &d, cudaStream_t s) {
+  if (v.ne == 0) return 0;
+  if (v.nb == 3) k_ddm_k0<3, 2><<<grid_of(v.ne, 128), 128, 0, s>>>(v, d);
+  else k_ddm_k0<6, 4><<<grid_of(v.ne, 128), 128, 0, s>>>(v, d);
+  return cudaGetLastError() == cudaSuccess ? 0 : XG_ECUDA;
+}
+
+int launch_ddm_k0_vec(int neq, const double *dU, const double *dV, const double *dA,
+                      const NewmarkCoef &c, double *out, cudaStream_t s) {
+  if (neq == 0) return 0;
+  k_ddm_k0_vec<<<grid_of(neq, 256), 256, 0, s>>>(neq, dU, dV, dA, c, out);
+  return cudaGetLastError() == cudaSuccess ? 0 : XG_ECUDA;
+}
+
 int launch_ddm_rhs(int neq, const double *dPc, const double *dU, const double *dV,
                    const double *dA, const double *meq, const double *meq_am,
                    const NewmarkCoef &c, double *rhs, cudaStream_t s) {
@@ -840,7 +927,7 @@ int launch_ddm_update(int neq, const double *x, const NewmarkCoef &c, double *dU
 int launch_ddm_objective(int nterm, const int *dof, const double *w, const int *eqn,
                          const double *U, const double *dU, double *dJ, cudaStream_t s) {
   if (nterm == 0) return 0;
-  k_ddm_objective<<<1, 32, 0, s>>>(nterm, dof, w, eqn, U, dU, dJ);
+  k_ddm_objective<<<grid_of(nterm, 128), 128, 0, s>>>(nterm, dof, w, eqn, U, dU, dJ);
   return cudaGetLastError() == cudaSuccess ? 0 : XG_ECUDA;
 }
 
@@ -887,7 +974,10 @@ extern "C" int xg_uniaxial_jvp(int type, const double *q, const double *hc, doub
                                double dstrain, const double *dhc, const double *dq,
                                double *dht) {
   if (!q || !hc || !dhc || !dq || !dht) return XG_EINVAL;
-  if (type == XG_UNI_STEEL01) xg::steel01_jvp(q, hc, strain, dstrain, dhc, dq, dht);
+  if (type == XG_UNI_STEEL02) {
+    if (q[10] != 0.0) return XG_EINVAL;
+    xg::steel02_jvp(q, hc, strain, dstrain, dhc, dq, dht);
+  } else if (type == XG_UNI_STEEL01) xg::steel01_jvp(q, hc, strain, dstrain, dhc, dq, dht);
   else if (type == XG_UNI_CONCRETE01) xg::concrete01_jvp(q, hc, strain, dstrain, dhc, dq, dht);
   else if (type == XG_UNI_ELASTIC) xg::elastic_jvp(q, strain, dstrain, dq, dht);
   else return XG_EINVAL;

@@ -425,8 +425,15 @@ struct DdmView {
   double *z;                  // [ne*6] sum over sections of w L b' fs q
   const int *eqn;             // [nn*ndf]
   const double *dU;           // [neq] the step's displacement tangent (pass 2)
+  const double *Vn;           // [nn*ndf] velocity after the step (betaK0 term)
+  const double *bk0;          // [ne] betaK0 per element, or null
+  double bk0_all;             // betaK0 when bk0 is null
+  const int *elem_uni;        // [ne] the single material of a betaK0 element
 };
 int launch_ddm_init_records(const FrameView &v, const DdmView &d, cudaStream_t s);
+int launch_ddm_k0(const FrameView &v, const DdmView &d, cudaStream_t s);
+int launch_ddm_k0_vec(int neq, const double *dU, const double *dV, const double *dA,
+                      const NewmarkCoef &c, double *out, cudaStream_t s);
 int launch_ddm_cond(const FrameView &v, const DdmView &d, cudaStream_t s);
 int launch_ddm_commit(const FrameView &v, const DdmView &d, cudaStream_t s);
 int launch_ddm_rhs(int neq, const double *dPc, const double *dU, const double *dV,

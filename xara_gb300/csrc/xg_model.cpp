@@ -315,9 +315,9 @@ struct xg_model {
   struct DdmRun {
     bool have = false;
     int nd = 0, nterm = 0;
-    std::vector<double> dJ;
-    DBuf<int> dof;
-    DBuf<double> w, J, dJd, dth, dU, dV, dA, dh, fh_prev, q, z, rhs, x;
+    std::vector<double> dJt;               // [nd][nterm] the objective's tangent term by term
+    DBuf<int> dof, elem_uni;
+    DBuf<double> w, J, dJd, dth, dU, dV, dA, dh, fh_prev, q, z, rhs, x, t0, t1;
   } ddm;
   int ddm_forward(const xg_phase_desc *ph, int N, int nd, const double *dtheta,
                   const xg_objective_desc *obj, double *J, double *dJ);
@@ -2192,14 +2192,30 @@ int xg_model::ddm_forward(const xg_phase_desc *ph, int N, int nd, const double *
     return fail(XG_EINVAL, "the DDM covers linear frame transformations in 2D");
   if (steps_since_reset != 0 || have_phase)
     return fail(XG_ESTATE, "the DDM runs from the model's initial state (xg_reset first)");
-  for (size_t u = 0; u < utype.size(); u++)
-    if (utype[u] != XG_UNI_STEEL01 && utype[u] != XG_UNI_CONCRETE01 && utype[u] != XG_UNI_ELASTIC)
-      return fail(XG_EINVAL, "the DDM covers Steel01, Concrete01 and elastic fibers (material %d)",
-                  (int)u);
-  bool bk0 = ph->beta_k_init != 0.0;
-  if (ph->beta_k_init_elem)
-    for (int e = 0; e < ne; e++) bk0 = bk0 || ph->beta_k_init_elem[e] != 0.0;
-  if (bk0) return fail(XG_EINVAL, "the DDM covers alphaM Rayleigh damping only (no betaK0)");
+  for (size_t u = 0; u < utype.size(); u++) {
+    if (utype[u] != XG_UNI_STEEL02 && utype[u] != XG_UNI_STEEL01 &&
+        utype[u] != XG_UNI_CONCRETE01 && utype[u] != XG_UNI_ELASTIC)
+      return fail(XG_EINVAL, "the DDM covers Steel02, Steel01, Concrete01 and elastic fibers "
+                  "(material %d)", (int)u);
+    if (utype[u] == XG_UNI_STEEL02 && uparam[u * XG_UNI_NPARAM + 10] != 0.0)
+      return fail(XG_EINVAL, "the DDM does not cover Steel02 with an initial stress");
+  }
+  // betaK0 damping on elements with a single Steel02, Steel01 or elastic
+  // material, in which K0 is linear in E
+  std::vector<int> elem_uni(std::max(ne, 1), 0);
+  for (int e = 0; e < ne; e++) {
+    const int sc = mat[e];
+    const int u0 = fmat[sec_fstart[sc]];
+    elem_uni[e] = u0;
+    const double bk = ph->beta_k_init_elem ? ph->beta_k_init_elem[e] : ph->beta_k_init;
+    if (bk == 0.0) continue;
+    bool single = utype[u0] == XG_UNI_STEEL02 || utype[u0] == XG_UNI_STEEL01 ||
+                  utype[u0] == XG_UNI_ELASTIC;
+    for (int f = sec_fstart[sc]; f < sec_fstart[sc + 1]; f++) single = single && fmat[f] == u0;
+    if (!single)
+      return fail(XG_EINVAL, "betaK0 damping in the DDM needs one Steel02, Steel01 or elastic "
+                  "material per element (element %d)", e);
+  }
   std::vector<int> dofs(obj->num_terms);
   for (int k = 0; k < obj->num_terms; k++) {
     auto it = std::lower_bound(node_tag.begin(), node_tag.end(), obj->node[k]);
@@ -2230,14 +2246,18 @@ int xg_model::ddm_forward(const xg_phase_desc *ph, int N, int nd, const double *
   RET(ddm.z.alloc(std::max<size_t>((size_t)ne * 6, 1)));
   RET(ddm.rhs.alloc(ne1));
   RET(ddm.x.alloc(ne1));
+  RET(ddm.t0.alloc(ne1));
+  RET(ddm.t1.alloc(ne1));
+  RET(ddm.elem_uni.upload(elem_uni.data(), elem_uni.size(), s));
   RET(ddm.dof.upload(dofs.data(), std::max<size_t>(dofs.size(), 1), s));
   std::vector<double> wv(obj->weight, obj->weight + obj->num_terms);
   wv.resize(std::max<size_t>(wv.size(), 1));
   RET(ddm.w.upload(wv.data(), wv.size(), s));
   RET(ddm.J.alloc(std::max(ddm.nterm, 1)));
   CK(cudaMemsetAsync(ddm.J.p, 0, std::max(ddm.nterm, 1) * sizeof(double), s));
-  RET(ddm.dJd.alloc(nd));
-  CK(cudaMemsetAsync(ddm.dJd.p, 0, nd * sizeof(double), s));
+  const size_t nt1 = std::max(ddm.nterm, 1);
+  RET(ddm.dJd.alloc((size_t)nd * nt1));
+  CK(cudaMemsetAsync(ddm.dJd.p, 0, (size_t)nd * nt1 * sizeof(double), s));
   const double dt = phase.dt, gam = phase.gamma, bet = phase.beta;
   NewmarkCoef c{};
   c.c2 = gam / (bet * dt);
@@ -2256,7 +2276,8 @@ int xg_model::ddm_forward(const xg_phase_desc *ph, int N, int nd, const double *
     FrameView fv = fview();
     RET(launch_fbc_assemble(fv, s));
     RET(launch_gather(gk, d_Ke.p, d_partial.p, d_vals.p, s));
-    RET(launch_dyn_tangent(dview(), d_vals.p, d_K0vals.p, 1.0, 0.0, c.c2, c.c3, s));
+    RET(launch_dyn_tangent(dview(), d_vals.p, d_K0vals.p, 1.0, k0_ready ? c.c2 : 0.0, c.c2,
+                           c.c3, s));
     blocks_factored = false;
     prof_factored = false;
     for (int k = 0; k < nd; k++) {
@@ -2267,28 +2288,45 @@ int xg_model::ddm_forward(const xg_phase_desc *ph, int N, int nd, const double *
       dv.q = ddm.q.p;
       dv.z = ddm.z.p;
       dv.eqn = d_eqn.p;
+      dv.Vn = d_Vc.p;
+      dv.bk0 = phase.beta_k_init_elem ? d_bk0_elem.p : nullptr;
+      dv.bk0_all = phase.beta_k_init;
+      dv.elem_uni = ddm.elem_uni.p;
       double *dUk = ddm.dU.p + (size_t)k * ne1, *dVk = ddm.dV.p + (size_t)k * ne1,
              *dAk = ddm.dA.p + (size_t)k * ne1;
       RET(launch_ddm_cond(fv, dv, s));
+      if (k0_ready) RET(launch_ddm_k0(fv, dv, s));
       RET(launch_gather(gr, d_Re.p, d_partial.p, ddm.x.p, s));
       RET(launch_ddm_rhs(neq, ddm.x.p, dUk, dVk, dAk, d_meq.p, d_meq_am.p, c, ddm.rhs.p, s));
+      if (k0_ready) {
+        // + betaK0 K0 (c2 dU' - a1 dV' - a2 dA')
+        RET(launch_ddm_k0_vec(neq, dUk, dVk, dAk, c, ddm.t0.p, s));
+        RET(launch_spmv(neq, d_rowptr.p, d_colidx.p, d_K0vals.p, ddm.t0.p, ddm.t1.p, s));
+        RET(launch_axpy(neq, 1.0, ddm.t1.p, ddm.rhs.p, s));
+      }
       RET(solve(ddm.rhs.p, ddm.x.p, nullptr));
       RET(launch_ddm_update(neq, ddm.x.p, c, dUk, dVk, dAk, s));
       dv.dU = dUk;
       RET(launch_ddm_commit(fv, dv, s));
       RET(launch_ddm_objective(ddm.nterm, ddm.dof.p, ddm.w.p, d_eqn.p, d_Uc.p, dUk,
-                               ddm.dJd.p + k, s));
+                               ddm.dJd.p + (size_t)k * nt1, s));
     }
   }
-  std::vector<double> Jk(std::max(ddm.nterm, 1));
-  ddm.dJ.assign(nd, 0.0);
+  std::vector<double> Jk(nt1);
+  ddm.dJt.assign((size_t)nd * nt1, 0.0);
   CK(cudaMemcpyAsync(Jk.data(), ddm.J.p, Jk.size() * sizeof(double), cudaMemcpyDeviceToHost, s));
-  CK(cudaMemcpyAsync(ddm.dJ.data(), ddm.dJd.p, nd * sizeof(double), cudaMemcpyDeviceToHost, s));
+  CK(cudaMemcpyAsync(ddm.dJt.data(), ddm.dJd.p, ddm.dJt.size() * sizeof(double),
+                     cudaMemcpyDeviceToHost, s));
   CK(cudaStreamSynchronize(s));
   double Jh = 0.0;
   for (int k = 0; k < ddm.nterm; k++) Jh += Jk[k];
   if (J) *J = Jh;
-  if (dJ) std::copy(ddm.dJ.begin(), ddm.dJ.end(), dJ);
+  if (dJ)
+    for (int k = 0; k < nd; k++) {
+      double t = 0.0;
+      for (int j = 0; j < ddm.nterm; j++) t += ddm.dJt[(size_t)k * nt1 + j];
+      dJ[k] = t;
+    }
   ddm.have = true;
   return 0;
 }
@@ -3007,6 +3045,17 @@ int xg_ddm_forward(xg_model *m, const xg_phase_desc *ph, int num_steps, int num_
   g_err.clear();
   if (!m) return fail(XG_EINVAL, "null model");
   return m->ddm_forward(ph, num_steps, num_dir, dtheta, obj, J, dJ);
+}
+
+int xg_ddm_objective_terms(const xg_model *m, int dir, double *dJk, int num_terms) {
+  g_err.clear();
+  if (!m || !dJk) return fail(XG_EINVAL, "null argument");
+  if (!m->ddm.have) return fail(XG_ESTATE, "no DDM run (xg_ddm_forward first)");
+  if (dir < 0 || dir >= m->ddm.nd) return fail(XG_EINVAL, "bad direction %d", dir);
+  if (num_terms != m->ddm.nterm) return fail(XG_EINVAL, "the run has %d terms", m->ddm.nterm);
+  const size_t nt1 = std::max(m->ddm.nterm, 1);
+  for (int j = 0; j < num_terms; j++) dJk[j] = m->ddm.dJt[(size_t)dir * nt1 + j];
+  return 0;
 }
 
 int xg_ddm_disp_sensitivity(const xg_model *m, int dir, double *out) {

@@ -212,6 +212,102 @@ XG_HD inline void steel02_vjp(const double *q, const double *hc, double strain, 
   qb[2] = b_b;
 }
 
+// Steel02::setTrialStrain in forward mode: the same primal steps as the
+// vector-Jacobian product above (first loading, a reversal with the
+// Filippou shift and the new asymptote's origin, the Menegotto-Pinto curve
+// with R from the plastic excursion), differentiated step by step.  dq =
+// d(Fy, E0, b); dht receives fields 0-6, 9 and 10.  sigini must be 0.
+XG_HD inline void steel02_jvp(const double *q, const double *hc, double strain, double dstrain,
+                              const double *dhc, const double *dq, double *dht) {
+  const double Fy = q[0], E0 = q[1], b = q[2], R0 = q[3], cR1 = q[4], cR2 = q[5];
+  const double a1 = q[6], a2 = q[7], a3 = q[8], a4 = q[9];
+  const double dFy = dq[0], dE0 = dq[1], db = dq[2];
+  const double Esh = b * E0, epsy = Fy / E0;
+  const double dEsh = db * E0 + b * dE0, depsy = dFy / E0 - Fy * dE0 / (E0 * E0);
+  const double eps = strain;
+  const double epsP = hc[10], sigP = hc[9];
+  const double deps = eps - epsP;
+  double epsmax = hc[1], epsmin = hc[0], epspl = hc[2], epss0 = hc[3], sigs0 = hc[4];
+  double epsr = hc[5], sigr = hc[6];
+  double t_epsmin = dhc[0], t_epsmax = dhc[1], t_epspl = dhc[2], t_epss0 = dhc[3];
+  double t_sigs0 = dhc[4], t_epsr = dhc[5], t_sigr = dhc[6];
+  const double t_epsP = dhc[10], t_sigP = dhc[9];
+  int kon = (int)hc[7];
+  for (int k = 0; k < 12; k++) dht[k] = 0.0;
+  if ((kon == 0 || kon == 3) && fabs(deps) < 10.0 * DBL_EPSILON) {
+    for (int k = 0; k < 7; k++) dht[k] = dhc[k];
+    dht[10] = dstrain;
+    return;
+  }
+  if (kon == 0 || kon == 3) {
+    epsmax = epsy;
+    epsmin = -epsy;
+    t_epsmax = depsy;
+    t_epsmin = -depsy;
+    if (deps < 0.0) {
+      kon = 2;
+      epss0 = epsmin; sigs0 = -Fy; epspl = epsmin;
+      t_epss0 = -depsy; t_sigs0 = -dFy; t_epspl = -depsy;
+    } else {
+      kon = 1;
+      epss0 = epsmax; sigs0 = Fy; epspl = epsmax;
+      t_epss0 = depsy; t_sigs0 = dFy; t_epspl = depsy;
+    }
+  }
+  const bool rev21 = kon == 2 && deps > 0.0, rev12 = !rev21 && kon == 1 && deps < 0.0;
+  if (rev21 || rev12) {
+    const double sg = rev21 ? 1.0 : -1.0;
+    const double aa = rev21 ? a3 : a1, ad = rev21 ? a4 : a2;
+    epsr = epsP; sigr = sigP;
+    t_epsr = t_epsP; t_sigr = t_sigP;
+    if (rev21 && epsP < epsmin) { epsmin = epsP; t_epsmin = t_epsP; }
+    if (rev12 && epsP > epsmax) { epsmax = epsP; t_epsmax = t_epsP; }
+    const double d1 = (epsmax - epsmin) / (2.0 * (ad * epsy));
+    const double t_d1 = (t_epsmax - t_epsmin) / (2.0 * (ad * epsy)) - d1 * depsy / epsy;
+    const double shft = 1.0 + aa * pow(d1, 0.8);
+    const double t_shft = (aa != 0.0 && d1 > 0.0) ? aa * 0.8 * pow(d1, -0.2) * t_d1 : 0.0;
+    const double D = E0 - Esh, t_D = dE0 - dEsh;
+    const double num = sg * Fy * shft - sg * Esh * epsy * shft - sigr + E0 * epsr;
+    const double t_num = sg * (dFy * shft + Fy * t_shft) -
+                         sg * (dEsh * epsy * shft + Esh * depsy * shft + Esh * epsy * t_shft) -
+                         t_sigr + dE0 * epsr + E0 * t_epsr;
+    epss0 = num / D;
+    t_epss0 = t_num / D - epss0 * t_D / D;
+    sigs0 = sg * Fy * shft + Esh * (epss0 - sg * epsy * shft);
+    t_sigs0 = sg * (dFy * shft + Fy * t_shft) + dEsh * (epss0 - sg * epsy * shft) +
+              Esh * (t_epss0 - sg * (depsy * shft + epsy * t_shft));
+    epspl = rev21 ? epsmax : epsmin;
+    t_epspl = rev21 ? t_epsmax : t_epsmin;
+  }
+  const double w = (epspl - epss0) / epsy;
+  const double t_w = (t_epspl - t_epss0) / epsy - w * depsy / epsy;
+  const double xi = fabs(w), t_xi = w >= 0.0 ? t_w : -t_w;
+  const double R = R0 * (1.0 - (cR1 * xi) / (cR2 + xi));
+  const double t_R = -R0 * cR1 * cR2 / ((cR2 + xi) * (cR2 + xi)) * t_xi;
+  const double den = epss0 - epsr;
+  const double rho = (eps - epsr) / den;
+  const double t_rho = (dstrain - t_epsr) / den - rho * (t_epss0 - t_epsr) / den;
+  const double ae = fabs(rho);
+  double lae = 0.0, pr = 0.0, dum1 = 1.0, ld1 = 0.0, dum2 = 1.0;
+  if (!mp_power_negligible(R, ae)) {
+    lae = ae > 0.0 ? log(ae) : 0.0;
+    pr = ae > 0.0 ? exp(R * lae) : 0.0;
+    dum1 = 1.0 + pr;
+    ld1 = log(dum1);
+    dum2 = exp(ld1 / R);
+  }
+  const double t_pr = ae > 0.0 ? pr * (t_R * lae + R * t_rho / rho) : 0.0;
+  const double t_dum2 = dum2 * (t_pr / (R * dum1) - ld1 * t_R / (R * R));
+  const double sst = b * rho + (1.0 - b) * rho / dum2;
+  const double t_sst = db * rho + b * t_rho - db * rho / dum2 +
+                       (1.0 - b) * (t_rho / dum2 - rho * t_dum2 / (dum2 * dum2));
+  const double t_sig = t_sst * (sigs0 - sigr) + sst * (t_sigs0 - t_sigr) + t_sigr;
+  dht[0] = t_epsmin; dht[1] = t_epsmax; dht[2] = t_epspl; dht[3] = t_epss0;
+  dht[4] = t_sigs0; dht[5] = t_epsr; dht[6] = t_sigr;
+  dht[9] = t_sig;
+  dht[10] = dstrain;
+}
+
 // Concrete02 compression envelope (Concrete02.cpp:448-497) and its partial
 // derivatives in the strain and in fc, epsc0, fcu (signs already negative).
 XG_HD inline double c02_compr_d(double fc, double epsc0, double fcu, double epscu, double x,

@@ -434,6 +434,15 @@ def ddm_forward(model, phase, num_steps, dtheta, node, dof, weight):
     return J.value, dJ
 
 
+def ddm_objective_terms(model, direction, num_terms):
+    """The last DDM run's objective tangent along ``direction``, term by term."""
+    L = lib()
+    L.xg_ddm_objective_terms.argtypes = [C.c_void_p, C.c_int, C.c_void_p, C.c_int]
+    out = np.zeros(num_terms)
+    _check(L.xg_ddm_objective_terms(model.h, int(direction), _p(out), int(num_terms)))
+    return out
+
+
 def ddm_disp_sensitivity(model, direction):
     """The last DDM run's displacement tangent along ``direction`` after its
     last step, [num_nodes, ndf]."""
