@@ -292,14 +292,15 @@ def test_steel01_jvp_against_finite_differences_and_the_vjp(shift):
             checked += 1
         hc = ht
     assert checked > 200
-    # the elastic law and a refused type
+    # the elastic law and a refused case
     de, dq = 1e-4, np.array([2e9, 0.0, 0.0])
     dht = gpu.uniaxial_jvp(XG_UNI_ELASTIC, np.r_[200e9, np.zeros(11)], np.zeros(12), 1e-3, de,
                            np.zeros(12), dq)
     assert dht[9] == pytest.approx(2e9 * 1e-3 + 200e9 * 1e-4) and dht[10] == de
+    q2 = configs.steel02_row()
+    q2[10] = 1e6                                 # Steel02 initial stress: not covered
     with pytest.raises(_gpu().XaraGpuError):
-        gpu.uniaxial_jvp(XG_UNI_CONCRETE02, configs.concrete02_row(30e6), np.zeros(12), 1e-3,
-                         de, np.zeros(12), dq)
+        gpu.uniaxial_jvp(XG_UNI_STEEL02, q2, np.zeros(12), 1e-3, de, np.zeros(12), dq)
 
 
 C01_FIELDS = (0, 1, 2, 9, 10)          # minStrain, endStrain, unloadSlope, sig, eps
@@ -469,6 +470,56 @@ def test_concrete02_vjp_against_finite_differences():
         if abs(e - hc[10]) > 1e-9:
             labels.add(_c02_fd_check(q, hc, float(e), rng))
         hc = port.uniaxial_trial(XG_UNI_CONCRETE02, q, hc, float(e))
+    need = {"env-c0", "env-c1", "env-c2", "unload-elastic", "unload-lower", "unload-upper",
+            "tension-t0", "tension-t1"}
+    assert need <= labels, labels
+
+
+def test_concrete02_jvp_against_the_vjp_and_finite_differences():
+    """Concrete02 in forward mode (the DDM's law) along the VJP test's path:
+    equal to the reverse mode through y.(Jt) = (J'y).t at every point, and to
+    central differences of the oracle's law in random directions of
+    (strain, ecmin, dept, stress, strain, fc, epsc0, fcu) wherever the
+    perturbed inputs stay on the same piece of the law."""
+    gpu = _gpu()
+    q = configs.concrete02_row(fc=30e6)
+    segs = [np.linspace(0, -0.003, 25), np.linspace(-0.003, -0.0012, 12),
+            np.linspace(-0.0012, -0.0045, 20), np.linspace(-0.0045, 0.0004, 40),
+            np.linspace(0.0004, -0.0005, 12), np.linspace(-0.0005, 0.0012, 25),
+            np.linspace(0.0012, -0.0075, 50), np.linspace(-0.0075, -0.004, 10)]
+    strains = np.concatenate(segs)
+    hc = port.uniaxial_init(XG_UNI_CONCRETE02, q)
+    rng = np.random.default_rng(41)
+    sc = np.full(12, abs(q[1]))
+    sc[9] = abs(q[0])
+    fields = list(C02_FIELDS)
+    labels = set()
+    for e in strains[1:]:
+        e = float(e)
+        de = rng.normal() * abs(q[1])
+        dhc = np.zeros(12)
+        dhc[fields] = rng.normal(size=len(fields)) * sc[fields]
+        dq = rng.normal(size=3) * np.abs(q[:3])
+        dht = gpu.uniaxial_jvp(XG_UNI_CONCRETE02, q, hc, e, de, dhc, dq)
+        yb = np.zeros(12)
+        yb[fields] = rng.normal(size=len(fields)) / sc[fields]
+        hb, sb, qb = gpu.uniaxial_vjp(XG_UNI_CONCRETE02, q, hc, e, yb)
+        terms = [sb * de, *(hb[f] * dhc[f] for f in fields), *(qb * dq)]
+        assert abs(float(yb @ dht) - sum(terms)) <= 1e-11 * sum(abs(x) for x in terms), e
+        rel = 1e-7
+        qp, qm = q.copy(), q.copy()
+        qp[:3] += rel * dq
+        qm[:3] -= rel * dq
+        hp, hm = hc + rel * dhc, hc - rel * dhc
+        label = _c02_branch(q, hc, e)
+        if abs(e - hc[10]) > 1e-9 and \
+                _c02_branch(qp, hp, e + rel * de) == label == _c02_branch(qm, hm, e - rel * de):
+            fd = (port.uniaxial_trial(XG_UNI_CONCRETE02, qp, hp, e + rel * de) -
+                  port.uniaxial_trial(XG_UNI_CONCRETE02, qm, hm, e - rel * de)) / (2 * rel)
+            for f in fields:
+                assert abs(dht[f] - fd[f]) <= 1e-6 * sc[f], (label, f, dht[f], fd[f])
+            labels.add(label)
+        hc = port.uniaxial_trial(XG_UNI_CONCRETE02, q, hc, e)
     need = {"env-c0", "env-c1", "env-c2", "unload-elastic", "unload-lower", "unload-upper",
             "tension-t0", "tension-t1"}
     assert need <= labels, labels
@@ -913,7 +964,8 @@ def test_ddm_rc01_frames_under_ground_motion(need_gpu, pga_scale, steps):
 def test_ddm_3d_frame_and_refusals(need_gpu):
     """A 3D frame (the RC frame's sections with Steel01 fibers) under a
     ground motion: DDM against the adjoint along seeded directions (1e-9);
-    Steel02 fibers and betaK0 damping are refused."""
+    Steel02 with an initial stress and betaK0 damping on mixed members are
+    refused."""
     gpu = _gpu()
     base, phases = configs.adjoint_rc_frame_3d(steps=40, pga_scale=3.0)
     nu = len(base.uni_type)
@@ -934,9 +986,12 @@ def test_ddm_3d_frame_and_refusals(need_gpu):
     assert (np.abs(rec[:, 10]) > 1e-3).mean() > 0.01          # some fibers yield
     for k in range(2):
         assert dJ[k] == pytest.approx(float((ga * dirs[k]).sum()), rel=1e-9), k
-    d2, p2 = configs.adjoint_rc_frames(n_frames=1, steps=5, seed=3)
+    d2, p2 = configs.adjoint_frames(n_frames=1, steps=5, seed=3)
+    q2 = d2.uni_param.reshape(-1, 12).copy()
+    q2[:, 10] = 1e6                                     # Steel02 initial stress
+    d2 = configs._with_geometry(d2, uni_param=q2)
     with gpu.DeviceModel(d2) as m:
-        with pytest.raises(gpu.XaraGpuError, match="Concrete01"):
+        with pytest.raises(gpu.XaraGpuError, match="initial stress"):
             gpu.ddm_forward(m, p2[0], 5, np.zeros((1, len(d2.uni_type), 3)),
                             *_objective(d2))
     d3, p3 = configs.adjoint_rc_frames(n_frames=1, steps=5, seed=3, laws="01")
@@ -944,6 +999,30 @@ def test_ddm_3d_frame_and_refusals(need_gpu):
     with gpu.DeviceModel(d3) as m:
         with pytest.raises(gpu.XaraGpuError, match="betaK0"):
             gpu.ddm_forward(m, p3[0], 5, np.zeros((1, len(d3.uni_type), 3)), *_objective(d3))
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("pga_scale,steps", [(1.0, 40), (3.0, 80)])
+def test_ddm_of_rc_frames_matches_the_adjoint(need_gpu, pga_scale, steps):
+    """The adjoint's RC frames (Concrete02 layers and Steel02 bars, the second
+    record through cracking, crushing and yielding): the DDM along seeded
+    directions equals the adjoint's gradient projected on them (1e-9)."""
+    gpu = _gpu()
+    desc, phases = configs.adjoint_rc_frames(n_frames=2, steps=steps, seed=5,
+                                             pga_scale=pga_scale)
+    ph = phases[0]
+    node, dof, w = _objective(desc)
+    q0 = desc.uni_param.reshape(-1, 12)
+    rng = np.random.default_rng(43)
+    dirs = rng.normal(size=(3, len(q0), 3)) * np.abs(q0[:, :3])
+    with gpu.DeviceModel(desc) as m:
+        J, dJ = gpu.ddm_forward(m, ph, steps, dirs, node, dof, w)
+        m.reset()
+        Ja = gpu.adjoint_forward(m, ph, steps, 10, node, dof, w)
+        ga = gpu.adjoint_backward(m)
+    assert J == Ja and np.abs(dJ).min() > 0
+    for k in range(3):
+        assert dJ[k] == pytest.approx(float((ga * dirs[k]).sum()), rel=1e-9), k
 
 
 @pytest.mark.gpu

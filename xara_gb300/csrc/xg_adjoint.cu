@@ -531,6 +531,7 @@ __device__ __forceinline__ void fiber_jvp(int type, const double *q, const doubl
                                           double strain, double dstrain, const double *dhc,
                                           const double *dq, double *dht) {
   if (type == XG_UNI_STEEL02) steel02_jvp(q, hc, strain, dstrain, dhc, dq, dht);
+  else if (type == XG_UNI_CONCRETE02) concrete02_jvp(q, hc, strain, dstrain, dhc, dq, dht);
   else if (type == XG_UNI_STEEL01) steel01_jvp(q, hc, strain, dstrain, dhc, dq, dht);
   else if (type == XG_UNI_CONCRETE01) concrete01_jvp(q, hc, strain, dstrain, dhc, dq, dht);
   else elastic_jvp(q, strain, dstrain, dq, dht);
@@ -977,7 +978,8 @@ extern "C" int xg_uniaxial_jvp(int type, const double *q, const double *hc, doub
   if (type == XG_UNI_STEEL02) {
     if (q[10] != 0.0) return XG_EINVAL;
     xg::steel02_jvp(q, hc, strain, dstrain, dhc, dq, dht);
-  } else if (type == XG_UNI_STEEL01) xg::steel01_jvp(q, hc, strain, dstrain, dhc, dq, dht);
+  } else if (type == XG_UNI_CONCRETE02) xg::concrete02_jvp(q, hc, strain, dstrain, dhc, dq, dht);
+  else if (type == XG_UNI_STEEL01) xg::steel01_jvp(q, hc, strain, dstrain, dhc, dq, dht);
   else if (type == XG_UNI_CONCRETE01) xg::concrete01_jvp(q, hc, strain, dstrain, dhc, dq, dht);
   else if (type == XG_UNI_ELASTIC) xg::elastic_jvp(q, strain, dstrain, dq, dht);
   else return XG_EINVAL;

@@ -2194,9 +2194,10 @@ int xg_model::ddm_forward(const xg_phase_desc *ph, int N, int nd, const double *
     return fail(XG_ESTATE, "the DDM runs from the model's initial state (xg_reset first)");
   for (size_t u = 0; u < utype.size(); u++) {
     if (utype[u] != XG_UNI_STEEL02 && utype[u] != XG_UNI_STEEL01 &&
-        utype[u] != XG_UNI_CONCRETE01 && utype[u] != XG_UNI_ELASTIC)
-      return fail(XG_EINVAL, "the DDM covers Steel02, Steel01, Concrete01 and elastic fibers "
-                  "(material %d)", (int)u);
+        utype[u] != XG_UNI_CONCRETE02 && utype[u] != XG_UNI_CONCRETE01 &&
+        utype[u] != XG_UNI_ELASTIC)
+      return fail(XG_EINVAL, "the DDM covers Steel02, Steel01, Concrete02, Concrete01 and "
+                  "elastic fibers (material %d)", (int)u);
     if (utype[u] == XG_UNI_STEEL02 && uparam[u * XG_UNI_NPARAM + 10] != 0.0)
       return fail(XG_EINVAL, "the DDM does not cover Steel02 with an initial stress");
   }

@@ -491,6 +491,83 @@ XG_HD inline void concrete02_vjp(const double *q, const double *hc, double strai
   qb[2] = s_fcu * b_fcu;
 }
 
+// Concrete02::setTrialStrain in forward mode: the branches of the
+// vector-Jacobian product above (the compression envelope, unloading from
+// it between the lower and upper bounds of the unloading fan, reloading
+// toward the tension envelope's last point and along the tension envelope)
+// differentiated forward.  dq = d(fc, epsc0, fcu) of the unnormalised
+// parameters; dht receives fields 0, 1, 9 and 10.
+XG_HD inline void concrete02_jvp(const double *q, const double *hc, double strain, double dstrain,
+                                 const double *dhc, const double *dq, double *dht) {
+  const double s_fc = q[0] > 0 ? -1.0 : 1.0, s_e0 = q[1] > 0 ? -1.0 : 1.0;
+  const double s_fcu = q[2] > 0 ? -1.0 : 1.0;
+  const double fc = s_fc * q[0], epsc0 = s_e0 * q[1], fcu = s_fcu * q[2];
+  const double dfc = s_fc * dq[0], de0 = s_e0 * dq[1], dfcu = s_fcu * dq[2];
+  const double epscu = q[3] > 0 ? -q[3] : q[3], rat = q[4], ft = q[5], Ets = q[6];
+  const double eps = strain;
+  const double ecmin_c = hc[0], dept_c = hc[1], sigP = hc[9], epsP = hc[10];
+  const double deps = eps - epsP;
+  for (int k = 0; k < 12; k++) dht[k] = 0.0;
+  if (fabs(deps) < DBL_EPSILON) {
+    dht[0] = dhc[0]; dht[1] = dhc[1]; dht[9] = dhc[9]; dht[10] = dstrain;
+    return;
+  }
+  const double ec0 = fc * 2. / epsc0;
+  const double dec0 = 2.0 * dfc / epsc0 - ec0 * de0 / epsc0;
+  double dsig = 0.0, t_ecmin = dhc[0], t_dept = dhc[1];
+  if (eps < ecmin_c) {
+    double dx, dfc_, de0_, dfcu_;
+    c02_compr_d(fc, epsc0, fcu, epscu, eps, &dx, &dfc_, &de0_, &dfcu_);
+    dsig = dx * dstrain + dfc_ * dfc + de0_ * de0 + dfcu_ * dfcu;
+    t_ecmin = dstrain;
+  } else {
+    const double Dn = ec0 * (1.0 - rat);
+    const double epsr = (fcu - rat * ec0 * epscu) / Dn;
+    const double t_epsr = dfcu / Dn + dec0 * (-rat * epscu - epsr * (1.0 - rat)) / Dn;
+    const double sigmr = ec0 * epsr, t_sigmr = dec0 * epsr + ec0 * t_epsr;
+    double mdx, mdfc, mde0, mdfcu;
+    const double sigmm = c02_compr_d(fc, epsc0, fcu, epscu, ecmin_c, &mdx, &mdfc, &mde0, &mdfcu);
+    const double t_sigmm = mdx * dhc[0] + mdfc * dfc + mde0 * de0 + mdfcu * dfcu;
+    const double den = ecmin_c - epsr, t_den = dhc[0] - t_epsr;
+    const double er = (sigmm - sigmr) / den;
+    const double t_er = (t_sigmm - t_sigmr) / den - er * t_den / den;
+    const double ept = ecmin_c - sigmm / er;
+    const double t_ept = dhc[0] - t_sigmm / er + sigmm * t_er / (er * er);
+    if (eps <= ept) {
+      const double sigmin = sigmm + er * (eps - ecmin_c);
+      const double sigmax = er * .5 * (eps - ept);
+      double sig = sigP + ec0 * deps;
+      int which = 0;
+      if (sig <= sigmin) { sig = sigmin; which = 1; }
+      if (sig >= sigmax) { sig = sigmax; which = 2; }
+      if (which == 0) dsig = dhc[9] + dec0 * deps + ec0 * (dstrain - dhc[10]);
+      else if (which == 1) dsig = t_sigmm + t_er * (eps - ecmin_c) + er * (dstrain - dhc[0]);
+      else dsig = .5 * t_er * (eps - ept) + .5 * er * (dstrain - t_ept);
+    } else if (eps <= ept + dept_c) {
+      double e, t_e;
+      if (dept_c != 0.0) {
+        double tdx, tdE;
+        const double sicn = c02_tens_d(ec0, ft, Ets, dept_c, &tdx, &tdE);
+        e = sicn / dept_c;
+        t_e = (tdx * dept_c - sicn) / (dept_c * dept_c) * dhc[1] + tdE / dept_c * dec0;
+      } else {
+        e = ec0;
+        t_e = dec0;
+      }
+      dsig = t_e * (eps - ept) + e * (dstrain - t_ept);
+    } else {
+      double tdx, tdE;
+      c02_tens_d(ec0, ft, Ets, eps - ept, &tdx, &tdE);
+      t_dept = dstrain - t_ept;
+      dsig = tdx * t_dept + tdE * dec0;
+    }
+  }
+  dht[0] = t_ecmin;
+  dht[1] = t_dept;
+  dht[9] = dsig;
+  dht[10] = dstrain;
+}
+
 // Elastic fiber: sig = E eps (parameter 0).
 // Steel01::setTrialStrain / determineTrialState (material/uniaxial/steel/
 // Steel01.cpp:68-92, 124-198), swept backwards: the stress is one of the
