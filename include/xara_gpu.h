@@ -484,9 +484,11 @@ int xg_adjoint_backward(xg_model *m, double scale, double *grad, int num_uni);
         commitSensitivity, Steel01.cpp:552-660; Concrete01's, Concrete01.cpp:
         655-775), a forward-mode path independent of the adjoint above.
         Covers 2D and 3D force-based frames (Linear transformations in 2D;
-        Linear or PDelta in 3D) with Steel02 (no initial stress; the
-        reference has no Steel02 sensitivity), Steel01, Concrete01 and
-        elastic fibers, Newmark with alphaM Rayleigh damping (no betaK0),
+        Linear or PDelta in 3D) with Steel02 (no initial stress) and
+        Concrete02 (the reference has no sensitivity for either), Steel01,
+        Concrete01 and elastic fibers, Newmark with alphaM Rayleigh damping
+        (betaK0 as well on elements of one Steel02, Steel01 or elastic
+        material),
         UniformExcitation and nodal load patterns, from the model's initial
         state.  After each converged step the effective tangent is formed
         again at the converged state (the reference solves with the last
@@ -494,7 +496,7 @@ int xg_adjoint_backward(xg_model *m, double scale, double *grad, int num_uni);
 /* Newmark run of num_steps from the initial state carrying num_dir
    directions: dtheta[(k*num_uni + u)*3 + j] is direction k's tangent of
    parameter j (0..2) of material u (Steel02 and Steel01: fy, E0, b;
-   Concrete01: fpc, epsc0, fpcu; elastic: E).
+   Concrete02: fc, epsc0, fcu; Concrete01: fpc, epsc0, fpcu; elastic: E).
    J as xg_adjoint_forward; dJ[k] = the derivative of J along direction k. */
 int xg_ddm_forward(xg_model *m, const xg_phase_desc *ph, int num_steps, int num_dir,
                    const double *dtheta, const xg_objective_desc *obj, double *J, double *dJ);
@@ -506,10 +508,10 @@ int xg_ddm_objective_terms(const xg_model *m, int dir, double *dJk, int num_term
    step, out[num_nodes*ndf] (zero on constrained dofs; `sensNodeDisp`). */
 int xg_ddm_disp_sensitivity(const xg_model *m, int dir, double *out);
 /* Jacobian-vector product of one material point's trial record (host only;
-   Steel02, Steel01, Concrete01 or elastic): given the tangents of the
-   strain, of the committed record dhc[12] and of parameters 0-2 dq[3], the
-   tangent of the trial record dht[12] (Steel02 fields 0-6, Steel01 0-3,
-   Concrete01 0-2, 9 stress, 10 strain). */
+   Steel02, Concrete02, Steel01, Concrete01 or elastic): given the tangents
+   of the strain, of the committed record dhc[12] and of parameters 0-2
+   dq[3], the tangent of the trial record dht[12] (Steel02 fields 0-6,
+   Concrete02 0-1, Steel01 0-3, Concrete01 0-2, 9 stress, 10 strain). */
 int xg_uniaxial_jvp(int type, const double *q, const double *hc, double strain,
                     double dstrain, const double *dhc, const double *dq, double *dht);
 /* Vector-Jacobian product of one material point's trial record (host only;
