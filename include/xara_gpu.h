@@ -483,8 +483,8 @@ int xg_adjoint_backward(xg_model *m, double scale, double *grad, int num_uni);
         ForceBeamColumn2d.cpp:2890-3007; Steel01::getStressSensitivity and
         commitSensitivity, Steel01.cpp:552-660; Concrete01's, Concrete01.cpp:
         655-775), a forward-mode path independent of the adjoint above.
-        Covers 2D and 3D force-based frames (Linear transformations in 2D;
-        Linear or PDelta in 3D) with Steel02 (no initial stress) and
+        Covers 2D and 3D force-based frames (Linear or PDelta
+        transformations) with Steel02 (no initial stress) and
         Concrete02 (the reference has no sensitivity for either), Steel01,
         Concrete01 and elastic fibers, Newmark with alphaM Rayleigh damping
         (betaK0 as well on elements of one Steel02, Steel01 or elastic

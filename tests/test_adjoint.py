@@ -1026,6 +1026,31 @@ def test_ddm_of_rc_frames_matches_the_adjoint(need_gpu, pga_scale, steps):
 
 
 @pytest.mark.gpu
+@pytest.mark.parametrize("pga_scale,steps", [(1.0, 40), (3.0, 80)])
+def test_ddm_of_pdelta_frames_matches_the_adjoint(need_gpu, pga_scale, steps):
+    """2D frames under `geomTransf PDelta` with growing floor weights and
+    betaK0 damping: the DDM (the P-Delta force's axial term at fixed
+    displacements, the tangent's non-symmetric term by a fixed point on the
+    factored tangent) along seeded directions equals the adjoint's gradient
+    projected on them (1e-9)."""
+    gpu = _gpu()
+    desc, phases = configs.adjoint_pdelta_frames(steps=steps, pga_scale=pga_scale, seed=5)
+    ph = phases[0]
+    node, dof, w = _objective(desc)
+    q0 = desc.uni_param.reshape(-1, 12)
+    rng = np.random.default_rng(47)
+    dirs = rng.normal(size=(2, len(q0), 3)) * np.abs(q0[:, :3])
+    with gpu.DeviceModel(desc) as m:
+        J, dJ = gpu.ddm_forward(m, ph, steps, dirs, node, dof, w)
+        m.reset()
+        Ja = gpu.adjoint_forward(m, ph, steps, 10, node, dof, w)
+        ga = gpu.adjoint_backward(m)
+    assert J == Ja and np.abs(dJ).min() > 0
+    for k in range(2):
+        assert dJ[k] == pytest.approx(float((ga * dirs[k]).sum()), rel=1e-9), k
+
+
+@pytest.mark.gpu
 @pytest.mark.parametrize("pga_scale,steps", [(1.0, 40), (6.0, 120)])
 def test_ddm_of_the_adjoint_frames_frame_by_frame(need_gpu, pga_scale, steps):
     """The adjoint's own frames (Steel02 members, 2 % Rayleigh with betaK0 per

@@ -633,6 +633,42 @@ __global__ void __launch_bounds__(32 * kAdjWarps) k_ddm_cond(FrameView v, DdmVie
     for (int k = 0; k < NB; k++) t += T[k][j] * dS[k];
     re[j] = t;
   }
+  if (NB == 3 && v.pdelta2d) {
+    // the 2D P-Delta force (Se_0 / L) ul14 g at fixed displacements
+    const double cs = v.R[9 * (long)e], sn = v.R[9 * (long)e + 1];
+    const double f = dS[0] / L * pdelta_ul14(v, e);
+    re[0] -= f * sn; re[1] += f * cs; re[3] += f * sn; re[4] -= f * cs;
+  }
+}
+
+// The 2D P-Delta tangent's term that the factored symmetric tangent leaves
+// out, applied to a displacement tangent x: per element (ul14 / L)
+// (kv T x_e)_0 g (the forward counterpart of k_adj_pdelta).  Thread per
+// element, into the element force scratch.
+__global__ void k_ddm_pdelta(FrameView v, const int *eqn, const double *x) {
+  const int e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= v.ne) return;
+  const double *kv = v.st + (long)e * stride_of(v.nip) + 6;
+  double T[3][6];
+  basic_T<3>(v, e, T);
+  double xe[6];
+#pragma unroll
+  for (int j = 0; j < 6; j++) {
+    const int eq = eqn[(long)v.conn[2 * e + j / 3] * v.ndf + j % 3];
+    xe[j] = eq >= 0 ? x[eq] : 0.0;
+  }
+  double t = 0.0;
+#pragma unroll
+  for (int k = 0; k < 3; k++) {
+    double tv = 0.0;
+#pragma unroll
+    for (int j = 0; j < 6; j++) tv += T[k][j] * xe[j];
+    t += kv[k] * tv;
+  }
+  const double cs = v.R[9 * (long)e], sn = v.R[9 * (long)e + 1];
+  const double f = pdelta_ul14(v, e) / v.L[e] * t;
+  double *re = v.Re + 6L * e;
+  re[0] = -f * sn; re[1] = f * cs; re[2] = 0.0; re[3] = f * sn; re[4] = -f * cs; re[5] = 0.0;
 }
 
 // Pass 2 (warp per element), after the step's tangent solve: dv = T dU_e
@@ -887,6 +923,13 @@ int launch_ddm_commit(const FrameView &v, const DdmView &d, cudaStream_t s) {
   const int grid = grid_of(v.ne, kAdjWarps);
   if (v.nb == 3) k_ddm_commit<3, 2><<<grid, 32 * kAdjWarps, 0, s>>>(v, d);
   else k_ddm_commit<6, 4><<<grid, 32 * kAdjWarps, 0, s>>>(v, d);
+  return cudaGetLastError() == cudaSuccess ? 0 : XG_ECUDA;
+}
+
+int launch_ddm_pdelta(const FrameView &v, const int *eqn, const double *x, cudaStream_t s) {
+  if (v.ne == 0) return 0;
+  if (v.nb != 3) return XG_EINVAL;
+  k_ddm_pdelta<<<grid_of(v.ne, 128), 128, 0, s>>>(v, eqn, x);
   return cudaGetLastError() == cudaSuccess ? 0 : XG_ECUDA;
 }
 

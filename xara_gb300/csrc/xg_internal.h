@@ -431,6 +431,7 @@ struct DdmView {
   const int *elem_uni;        // [ne] the single material of a betaK0 element
 };
 int launch_ddm_init_records(const FrameView &v, const DdmView &d, cudaStream_t s);
+int launch_ddm_pdelta(const FrameView &v, const int *eqn, const double *x, cudaStream_t s);
 int launch_ddm_k0(const FrameView &v, const DdmView &d, cudaStream_t s);
 int launch_ddm_k0_vec(int neq, const double *dU, const double *dV, const double *dA,
                       const NewmarkCoef &c, double *out, cudaStream_t s);

@@ -321,6 +321,7 @@ struct xg_model {
   } ddm;
   int ddm_forward(const xg_phase_desc *ph, int N, int nd, const double *dtheta,
                   const xg_objective_desc *obj, double *J, double *dJ);
+  int ddm_pdelta_refine(const xg::FrameView &fv);
   // analysis state
   xg_phase_desc phase{};
   bool have_phase = false;
@@ -2173,6 +2174,34 @@ int xg_model::adjoint_backward(double scale, double *grad, int num_uni) {
   return element_state(true);
 }
 
+// The 2D P-Delta step's tangent equation (K + C) x = rhs, K the factored
+// symmetric tangent and C the per-element terms of k_ddm_pdelta:
+// x <- K^-1 (rhs - C x) from the first solve's x until a solve changes x by
+// no more than the solver's accuracy (as adj_pdelta_refine does for the
+// transposed equation).
+int xg_model::ddm_pdelta_refine(const xg::FrameView &fv) {
+  cudaStream_t s = stream;
+  constexpr int kMaxSolves = 100;
+  const double tol = system == XG_SYSTEM_PROFILE_SPD ? 1e-14 : std::max(1e-14, 10.0 * rtol);
+  for (int k = 0; k < kMaxSolves; k++) {
+    RET(launch_ddm_pdelta(fv, d_eqn.p, ddm.x.p, s));
+    RET(launch_gather(gr, d_Re.p, d_partial.p, ddm.t0.p, s));
+    RET(launch_sub(neq, ddm.rhs.p, ddm.t0.p, ddm.t1.p, s));
+    RET(solve(ddm.t1.p, ddm.t0.p, nullptr));
+    RET(launch_sub(neq, ddm.t0.p, ddm.x.p, ddm.t1.p, s));
+    double dn = 0.0, xn = 0.0;
+    RET(launch_norm2(neq, ddm.t1.p, d_partial.p, d_norm.p, s));
+    RET(read_scalar(d_norm.p, &dn, s));
+    RET(launch_norm2(neq, ddm.t0.p, d_partial.p, d_norm.p, s));
+    RET(read_scalar(d_norm.p, &xn, s));
+    CK(cudaMemcpyAsync(ddm.x.p, ddm.t0.p, (size_t)neq * sizeof(double), cudaMemcpyDeviceToDevice,
+                       s));
+    if (std::sqrt(dn) <= tol * std::sqrt(xn)) return 0;
+  }
+  return fail(XG_ENOCONV, "DDM: the P-Delta terms' fixed-point iteration did not converge in %d "
+              "solves", kMaxSolves);
+}
+
 // Newmark run of num_steps from the initial state with the direct
 // differentiation after every converged step (Newmark::computeSensitivities,
 // Newmark.cpp:904-959, one direction per parameter combination):
@@ -2188,8 +2217,6 @@ int xg_model::ddm_forward(const xg_phase_desc *ph, int N, int nd, const double *
   if (N < 1 || nd < 1 || !dtheta || !obj || obj->num_terms < 0 ||
       (obj->num_terms > 0 && (!obj->node || !obj->dof || !obj->weight)))
     return fail(XG_EINVAL, "bad DDM run settings");
-  if (fb_nb == 3 && geom_transf == 1)
-    return fail(XG_EINVAL, "the DDM covers linear frame transformations in 2D");
   if (steps_since_reset != 0 || have_phase)
     return fail(XG_ESTATE, "the DDM runs from the model's initial state (xg_reset first)");
   for (size_t u = 0; u < utype.size(); u++) {
@@ -2306,6 +2333,7 @@ int xg_model::ddm_forward(const xg_phase_desc *ph, int N, int nd, const double *
         RET(launch_axpy(neq, 1.0, ddm.t1.p, ddm.rhs.p, s));
       }
       RET(solve(ddm.rhs.p, ddm.x.p, nullptr));
+      if (fv.pdelta2d) RET(ddm_pdelta_refine(fv));
       RET(launch_ddm_update(neq, ddm.x.p, c, dUk, dVk, dAk, s));
       dv.dU = dUk;
       RET(launch_ddm_commit(fv, dv, s));
