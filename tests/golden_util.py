@@ -7,7 +7,8 @@ from xara_gb300 import configs
 
 GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
 
-# tolerance for floating-point parity (relative, norm-wise per vector)
+# tolerance for floating-point parity (relative, norm-wise per vector; the
+# tangent's values also row by row, row_relerr)
 RTOL_STATE = 1e-12      # resisting force / tangent values per iteration
 RTOL_HISTORY = 1e-8     # converged displacement histories
 
@@ -35,6 +36,23 @@ def relerr(a, b):
     b = np.asarray(b, np.float64).ravel()
     den = np.linalg.norm(b)
     return np.linalg.norm(a - b) / (den if den > 0 else 1.0)
+
+
+def row_relerr(fx, a, b):
+    """Largest difference of CSR values a and b in each row over that row's
+    largest |b| (the rows of the fixture's pattern; it is symmetric, so the
+    column starts are the row pointers): every coefficient is held to the
+    scale of its own row, not to the norm of the whole matrix."""
+    rp = np.asarray(fx["colstart"])
+    a = np.asarray(a, np.float64).ravel()
+    b = np.asarray(b, np.float64).ravel()
+    n = len(rp) - 1
+    rows = np.repeat(np.arange(n), np.diff(rp))
+    dmax = np.zeros(n)
+    smax = np.zeros(n)
+    np.maximum.at(dmax, rows, np.abs(a - b))
+    np.maximum.at(smax, rows, np.abs(b))
+    return float((dmax / np.where(smax > 0, smax, 1.0)).max())
 
 
 def unbalance_solves(fx, desc, phase):

@@ -10,7 +10,8 @@ import numpy as np
 import pytest
 
 from golden_util import (RTOL_HISTORY, RTOL_STATE, assemble_elements, csc_to_csr_values,
-                         external_load, load, model_of, relerr, unbalance_solves)
+                         external_load, load, model_of, relerr, row_relerr,
+                         unbalance_solves)
 
 pytestmark = pytest.mark.gpu
 
@@ -59,7 +60,9 @@ def test_replay_element_state(gpu_mod, name):
                 vals, resid, st = m.update()
                 fext = external_load(fx, desc, k, eqn)
                 assert relerr(resid, fext - fx["cap_B"][k]) < RTOL_STATE
-                assert relerr(vals, csc_to_csr_values(fx, fx["cap_A"][k])) < RTOL_STATE
+                ref = csc_to_csr_values(fx, fx["cap_A"][k])
+                assert relerr(vals, ref) < RTOL_STATE
+                assert row_relerr(fx, vals, ref) < RTOL_STATE
                 checked += 1
         assert checked >= 4
 
@@ -287,7 +290,9 @@ def test_frame_replay_first_step(gpu_mod, name):
             vals, resid, st = m.update()
             fext = external_load(fx, desc, k, eqn)
             assert relerr(resid, fext - fx["cap_B"][k]) < RTOL_STATE
-            assert relerr(vals, csc_to_csr_values(fx, fx["cap_A"][k])) < RTOL_STATE
+            ref = csc_to_csr_values(fx, fx["cap_A"][k])
+            assert relerr(vals, ref) < RTOL_STATE
+            assert row_relerr(fx, vals, ref) < RTOL_STATE
 
 
 @pytest.mark.parametrize("name", ["revert_frame2d_2x3", "revert_frame3d_1x1x2",
@@ -315,6 +320,7 @@ def test_revert_to_last_commit(gpu_mod, name):
                                              fx["P" + key])
             assert relerr(resid, r_ref) < RTOL_STATE, key
             assert relerr(vals, v_ref) < RTOL_STATE, key
+            assert row_relerr(fx, vals, v_ref) < RTOL_STATE, key
 
 
 @pytest.mark.parametrize("system", ["profile", "pcg"])

@@ -5,7 +5,7 @@ import pytest
 
 from oracle import port
 from golden_util import (RTOL_HISTORY, RTOL_STATE, assemble_elements, csc_to_csr_values,
-                         external_load, load, model_of, relerr, unbalance_solves)
+                         external_load, load, model_of, relerr, row_relerr, unbalance_solves)
 
 MODELS = ["quad_8x4", "quad_64x16", "brick_4x3x2", "brick_8x8x4"]
 
@@ -60,7 +60,9 @@ def test_replay_element_state(name):
             vals, resid = o.elem_state(fx["cap_U"][k])
             fext = external_load(fx, desc, k, eqn)
             assert relerr(resid, fext - fx["cap_B"][k]) < RTOL_STATE
-            assert relerr(vals, csc_to_csr_values(fx, fx["cap_A"][k])) < RTOL_STATE
+            ref = csc_to_csr_values(fx, fx["cap_A"][k])
+            assert relerr(vals, ref) < RTOL_STATE
+            assert row_relerr(fx, vals, ref) < RTOL_STATE
         o.close()
 
 
@@ -107,7 +109,9 @@ def test_frame_replay_first_step(name):
         vals, resid = o.elem_state(fx["cap_U"][k])
         fext = external_load(fx, desc, k, eqn)
         assert relerr(resid, fext - fx["cap_B"][k]) < RTOL_STATE
-        assert relerr(vals, csc_to_csr_values(fx, fx["cap_A"][k])) < RTOL_STATE
+        ref = csc_to_csr_values(fx, fx["cap_A"][k])
+        assert relerr(vals, ref) < RTOL_STATE
+        assert row_relerr(fx, vals, ref) < RTOL_STATE
 
 
 REVERTS = ["revert_frame2d_2x3", "revert_frame3d_1x1x2", "revert_quad_8x4"]
@@ -131,4 +135,5 @@ def test_revert_to_last_commit(name):
         v_ref, r_ref = assemble_elements(desc, fx["eqn"], rp, ci, fx["K" + key], fx["P" + key])
         assert relerr(resid, r_ref) < RTOL_STATE, key
         assert relerr(vals, v_ref) < RTOL_STATE, key
+        assert row_relerr(fx, vals, v_ref) < RTOL_STATE, key
     o.close()
