@@ -1076,3 +1076,29 @@ def test_ddm_of_the_adjoint_frames_frame_by_frame(need_gpu, pga_scale, steps):
     for f in range(len(node)):
         proj = float((ga[frame == f] * d[0][frame == f]).sum())
         assert per_frame[f] == pytest.approx(proj, rel=1e-9), f
+
+
+@pytest.mark.gpu
+def test_ddm_argument_checks(need_gpu):
+    """The DDM entry points refuse what they cannot serve: reads before a
+    run, a direction out of range, a term count that is not the run's, no
+    directions, a run that does not start from the initial state."""
+    gpu = _gpu()
+    desc, ph = _adjoint_model(n_frames=1, steps=5, seed=3)
+    node, dof, w = _objective(desc)
+    nu = len(desc.uni_type)
+    with gpu.DeviceModel(desc) as m:
+        with pytest.raises(gpu.XaraGpuError, match="no DDM run"):
+            gpu.ddm_objective_terms(m, 0, len(node))
+        with pytest.raises(gpu.XaraGpuError):
+            gpu.ddm_forward(m, ph, 5, np.zeros((0, nu, 3)), node, dof, w)
+        J, dJ = gpu.ddm_forward(m, ph, 5, np.ones((1, nu, 3)), node, dof, w)
+        assert np.isfinite(J) and np.isfinite(dJ).all()
+        with pytest.raises(gpu.XaraGpuError, match="bad direction"):
+            gpu.ddm_objective_terms(m, 1, len(node))
+        with pytest.raises(gpu.XaraGpuError, match="terms"):
+            gpu.ddm_objective_terms(m, 0, len(node) + 1)
+        with pytest.raises(gpu.XaraGpuError, match="bad direction"):
+            gpu.ddm_disp_sensitivity(m, 2)
+        with pytest.raises(gpu.XaraGpuError, match="initial state"):
+            gpu.ddm_forward(m, ph, 5, np.ones((1, nu, 3)), node, dof, w)
