@@ -780,6 +780,31 @@ def _kinds(desc):
     return [(np.nonzero(ut == t)[0], k) for t in np.unique(ut) for k in range(3)]
 
 
+@pytest.mark.gpu
+def test_forward_mode_through_torch(need_gpu):
+    """torch's forward-mode AD (a dual tensor through frame_response) runs
+    the DDM: its tangent equals the reverse-mode gradient projected on the
+    tangent direction (1e-9), and the primal equals the plain run's J."""
+    import torch
+    import torch.autograd.forward_ad as fwAD
+    gpu = _gpu()
+    from xara_gb300.adjoint import frame_response
+    desc, ph = _adjoint_model(n_frames=2, steps=30, seed=2)
+    obj = _objective(desc)
+    q0 = desc.uni_param.reshape(-1, 12)
+    d = np.random.default_rng(53).normal(size=q0[:, :3].shape) * np.abs(q0[:, :3])
+    with gpu.DeviceModel(desc) as m:
+        theta = torch.tensor(q0[:, :3], dtype=torch.float64)
+        with fwAD.dual_level():
+            J = frame_response(fwAD.make_dual(theta, torch.tensor(d)), m, ph, 30, 10, obj)
+            Jp, dJ = fwAD.unpack_dual(J)
+        m.reset()
+        J2 = gpu.adjoint_forward(m, ph, 30, 10, *obj)
+        g = gpu.adjoint_backward(m)
+    assert float(Jp) == J2
+    assert float(dJ) == pytest.approx(float((g * d).sum()), rel=1e-9)
+
+
 def _ddm_case(name="ddm_steel01_frame"):
     from golden_util import load, model_of
     fx = load(name)

@@ -10,10 +10,13 @@ committed state every ``ckpt_every`` steps) and returns
 the backward pass is the library's reverse sweep (``xg_adjoint_backward``),
 which recomputes each segment from its checkpoint and sweeps it backwards
 through the Newmark step, the force-based elements' compatibility state and
-the Steel02 fibers.  ``theta`` holds the first three parameters of every
-uniaxial material ([num_uni, 3]; Steel02: Fy, E0, b), float64 on any
-device.  PyTorch only carries the parameters and the gradient; all work runs
-in ``libxara_gpu.so``.
+the fibers' laws.  Forward-mode AD (``torch.func.jvp``, dual tensors of
+``torch.autograd.forward_ad``) runs the library's direct differentiation
+(``xg_ddm_forward``) along the tangent of ``theta`` from the initial state
+instead.  ``theta`` holds the first three parameters of every uniaxial
+material ([num_uni, 3]; Steel02: Fy, E0, b), float64 on any device.  PyTorch
+only carries the parameters, the tangents and the gradient; all work runs in
+``libxara_gpu.so``.
 """
 import numpy as np
 import torch
@@ -36,8 +39,18 @@ class FrameResponse(torch.autograd.Function):
         node, dof, weight = objective
         J = gpu.adjoint_forward(model, phase, num_steps, ckpt_every, node, dof, weight)
         ctx.model = model
+        ctx.phase, ctx.num_steps, ctx.objective = phase, num_steps, objective
         ctx.theta_device, ctx.theta_dtype = theta.device, theta.dtype
         return torch.tensor(J, dtype=torch.float64, device=theta.device)
+
+    @staticmethod
+    def jvp(ctx, dtheta, *_):
+        """dJ along dtheta: the DDM of the same run from the initial state."""
+        t = dtheta.detach().to("cpu", torch.float64).numpy().reshape(1, -1, 3)
+        ctx.model.reset()
+        node, dof, weight = ctx.objective
+        _, dJ = gpu.ddm_forward(ctx.model, ctx.phase, ctx.num_steps, t, node, dof, weight)
+        return torch.tensor(dJ[0], dtype=torch.float64, device=ctx.theta_device)
 
     @staticmethod
     def backward(ctx, grad_J):
