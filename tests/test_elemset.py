@@ -31,7 +31,7 @@ import build_ref  # noqa: E402
 import ref  # noqa: E402
 
 MODELS = ["quad_8x4", "brick_4x3x2", "frame2d_2x3", "frame3d_1x1x2", "frame2d_pd_2x3",
-          "frame2d_eq_2x3"]
+          "frame2d_eq_2x3", "frame2d_rc01_2x3"]
 
 
 @pytest.fixture(scope="module")

@@ -100,6 +100,8 @@ MODELS = {
     "3D RC frame, gravity and pushover": (lambda: configs.rc_frame_3d(1, 1, 2), True),
     "2D steel frame, Newmark with Rayleigh damping":
         (lambda: configs.steel_frame_2d_eq(1, 2, steps=6), True),
+    "2D RC frame of Concrete01 and Steel01, gravity and pushover":
+        (lambda: configs.rc_frame_2d(2, 3, steps=6), True),
 }
 
 
