@@ -2257,6 +2257,15 @@ int xg_model::ddm_forward(const xg_phase_desc *ph, int N, int nd, const double *
   const size_t nuni3 = utype.size() * 3;
   ddm.nd = nd;
   ddm.nterm = obj->num_terms;
+  {
+    // per direction: U, V, A tangents and the record tangents
+    size_t free_b = 0, total_b = 0;
+    CK(cudaMemGetInfo(&free_b, &total_b));
+    const size_t need = (size_t)nd * (3 * ne1 + nrec + nuni3) * sizeof(double);
+    if (need > free_b / 10 * 8)
+      return fail(XG_ENOMEM, "the DDM's %d directions need %.1f GB (fewer directions per run "
+                  "lower it)", nd, need * 1e-9);
+  }
   for (auto *b : {&ddm.dU, &ddm.dV, &ddm.dA}) {
     RET(b->alloc((size_t)nd * ne1));
     CK(cudaMemsetAsync(b->p, 0, (size_t)nd * ne1 * sizeof(double), s));
