@@ -488,12 +488,12 @@ int xg_adjoint_backward(xg_model *m, double scale, double *grad, int num_uni);
         Concrete02 (the reference has no sensitivity for either), Steel01,
         Concrete01 and elastic fibers, Newmark with alphaM Rayleigh damping
         (betaK0 as well on elements of one Steel02, Steel01 or elastic
-        material),
+        material) or LoadControl (LoadControl::computeSensitivities),
         UniformExcitation and nodal load patterns, from the model's initial
         state.  After each converged step the effective tangent is formed
         again at the converged state (the reference solves with the last
         Newton iteration's factors). ---- */
-/* Newmark run of num_steps from the initial state carrying num_dir
+/* Newmark or LoadControl run of num_steps from the initial state carrying num_dir
    directions: dtheta[(k*num_uni + u)*3 + j] is direction k's tangent of
    parameter j (0..2) of material u (Steel02 and Steel01: fy, E0, b;
    Concrete02: fc, epsc0, fcu; Concrete01: fpc, epsc0, fpcu; elastic: E).

@@ -1104,6 +1104,43 @@ def test_ddm_of_the_adjoint_frames_frame_by_frame(need_gpu, pga_scale, steps):
 
 
 @pytest.mark.gpu
+def test_ddm_of_a_static_pushover(need_gpu):
+    """LoadControl (the reference's LoadControl::computeSensitivities: no
+    inertia, K dU = -dP at fixed U): a 2D steel frame pushed laterally into
+    Steel02's nonlinear transition, the DDM of the summed squared roof drift
+    along seeded directions against central differences of the device run
+    (1e-5)."""
+    from xara_gb300._abi import PhaseDesc, XG_INT_LOAD_CONTROL
+    gpu = _gpu()
+    desc, _ = configs.steel_frame_2d(2, 3, gravity=0.0)
+    ph = PhaseDesc(integrator=XG_INT_LOAD_CONTROL, pattern=1, num_steps=20, d_lambda=25e3,
+                   tol=1e-10, max_iter=50)
+    roof = int(desc.meta["roof"])
+    obj = (np.array([roof], np.int32), np.zeros(1, np.int32), np.array([1.0 / 10.5 ** 2]))
+    q0 = desc.uni_param.reshape(-1, 12).copy()
+    rng = np.random.default_rng(59)
+    dirs = rng.normal(size=(2, len(q0), 3)) * np.abs(q0[:, :3])
+    none = np.zeros((1, len(q0), 3))
+
+    def J(m, q):
+        gpu.set_uniaxial_params(m, q)
+        m.reset()
+        return gpu.ddm_forward(m, ph, 20, none, *obj)[0]
+
+    with gpu.DeviceModel(desc) as m:
+        J0, dJ = gpu.ddm_forward(m, ph, 20, dirs, *obj)
+        rec = m.fiber_records()
+        # the extreme fibers well into Steel02's curved transition
+        assert np.abs(rec[:, 10]).max() > 0.7 * q0[0, 0] / q0[0, 1]
+        assert J(m, q0) == J0
+        h = 1e-6
+        for k in range(2):
+            fd = (J(m, q0 + np.c_[h * dirs[k], np.zeros((len(q0), 9))]) -
+                  J(m, q0 - np.c_[h * dirs[k], np.zeros((len(q0), 9))])) / (2 * h)
+            assert dJ[k] == pytest.approx(fd, rel=1e-5), k
+
+
+@pytest.mark.gpu
 def test_ddm_argument_checks(need_gpu):
     """The DDM entry points refuse what they cannot serve: reads before a
     run, a direction out of range, a term count that is not the run's, no

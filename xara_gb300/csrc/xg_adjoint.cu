@@ -859,8 +859,10 @@ __global__ void k_ddm_rhs(int neq, const double *dPc, const double *dU, const do
                           NewmarkCoef c, double *rhs) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= neq) return;
-  rhs[i] = -dPc[i] + meq[i] * (c.c3 * dU[i] - c.a3 * dV[i] - c.a4 * dA[i]) +
-           meq_am[i] * (c.c2 * dU[i] - c.a1 * dV[i] - c.a2 * dA[i]);
+  double r = -dPc[i];
+  if (meq) r += meq[i] * (c.c3 * dU[i] - c.a3 * dV[i] - c.a4 * dA[i]);   // null: no inertia
+  if (meq_am) r += meq_am[i] * (c.c2 * dU[i] - c.a1 * dV[i] - c.a2 * dA[i]);
+  rhs[i] = r;
 }
 
 // the step's displacement tangent x and the Newmark relations give dA, dV

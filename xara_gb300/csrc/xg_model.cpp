@@ -2213,7 +2213,9 @@ int xg_model::ddm_forward(const xg_phase_desc *ph, int N, int nd, const double *
                           const xg_objective_desc *obj, double *J, double *dJ) {
   ddm.have = false;
   if (!frames()) return fail(XG_EINVAL, "the DDM covers force-based frame models");
-  if (!ph || ph->integrator != XG_INT_NEWMARK) return fail(XG_EINVAL, "the DDM covers Newmark runs");
+  if (!ph || (ph->integrator != XG_INT_NEWMARK && ph->integrator != XG_INT_LOAD_CONTROL))
+    return fail(XG_EINVAL, "the DDM covers Newmark and LoadControl runs");
+  const bool dyn = ph->integrator == XG_INT_NEWMARK;
   if (N < 1 || nd < 1 || !dtheta || !obj || obj->num_terms < 0 ||
       (obj->num_terms > 0 && (!obj->node || !obj->dof || !obj->weight)))
     return fail(XG_EINVAL, "bad DDM run settings");
@@ -2295,14 +2297,18 @@ int xg_model::ddm_forward(const xg_phase_desc *ph, int N, int nd, const double *
   const size_t nt1 = std::max(ddm.nterm, 1);
   RET(ddm.dJd.alloc((size_t)nd * nt1));
   CK(cudaMemsetAsync(ddm.dJd.p, 0, (size_t)nd * nt1 * sizeof(double), s));
-  const double dt = phase.dt, gam = phase.gamma, bet = phase.beta;
+  // Newmark's relations; a LoadControl step has no inertia and no velocity
+  // (LoadControl::computeSensitivities: K dU = -dP at fixed U), all zero
   NewmarkCoef c{};
-  c.c2 = gam / (bet * dt);
-  c.c3 = 1.0 / (bet * dt * dt);
-  c.a1 = 1.0 - gam / bet;
-  c.a2 = dt * (1.0 - 0.5 * gam / bet);
-  c.a3 = -1.0 / (bet * dt);
-  c.a4 = 1.0 - 0.5 / bet;
+  if (dyn) {
+    const double dt = phase.dt, gam = phase.gamma, bet = phase.beta;
+    c.c2 = gam / (bet * dt);
+    c.c3 = 1.0 / (bet * dt * dt);
+    c.a1 = 1.0 - gam / bet;
+    c.a2 = dt * (1.0 - 0.5 * gam / bet);
+    c.a3 = -1.0 / (bet * dt);
+    c.a4 = 1.0 - 0.5 / bet;
+  }
   for (int n = 1; n <= N; n++) {
     CK(cudaMemcpyAsync(ddm.fh_prev.p, d_fh_c.p, (size_t)fb_nrec * 12 * sizeof(double),
                        cudaMemcpyDeviceToDevice, s));
@@ -2313,8 +2319,9 @@ int xg_model::ddm_forward(const xg_phase_desc *ph, int N, int nd, const double *
     FrameView fv = fview();
     RET(launch_fbc_assemble(fv, s));
     RET(launch_gather(gk, d_Ke.p, d_partial.p, d_vals.p, s));
-    RET(launch_dyn_tangent(dview(), d_vals.p, d_K0vals.p, 1.0, k0_ready ? c.c2 : 0.0, c.c2,
-                           c.c3, s));
+    if (dyn)
+      RET(launch_dyn_tangent(dview(), d_vals.p, d_K0vals.p, 1.0, k0_ready ? c.c2 : 0.0, c.c2,
+                             c.c3, s));
     blocks_factored = false;
     prof_factored = false;
     for (int k = 0; k < nd; k++) {
@@ -2332,10 +2339,11 @@ int xg_model::ddm_forward(const xg_phase_desc *ph, int N, int nd, const double *
       double *dUk = ddm.dU.p + (size_t)k * ne1, *dVk = ddm.dV.p + (size_t)k * ne1,
              *dAk = ddm.dA.p + (size_t)k * ne1;
       RET(launch_ddm_cond(fv, dv, s));
-      if (k0_ready) RET(launch_ddm_k0(fv, dv, s));
+      if (dyn && k0_ready) RET(launch_ddm_k0(fv, dv, s));
       RET(launch_gather(gr, d_Re.p, d_partial.p, ddm.x.p, s));
-      RET(launch_ddm_rhs(neq, ddm.x.p, dUk, dVk, dAk, d_meq.p, d_meq_am.p, c, ddm.rhs.p, s));
-      if (k0_ready) {
+      RET(launch_ddm_rhs(neq, ddm.x.p, dUk, dVk, dAk, dyn ? d_meq.p : nullptr,
+                         dyn ? d_meq_am.p : nullptr, c, ddm.rhs.p, s));
+      if (dyn && k0_ready) {
         // + betaK0 K0 (c2 dU' - a1 dV' - a2 dA')
         RET(launch_ddm_k0_vec(neq, dUk, dVk, dAk, c, ddm.t0.p, s));
         RET(launch_spmv(neq, d_rowptr.p, d_colidx.p, d_K0vals.p, ddm.t0.p, ddm.t1.p, s));
