@@ -2202,9 +2202,10 @@ int xg_model::ddm_pdelta_refine(const xg::FrameView &fv) {
               "solves", kMaxSolves);
 }
 
-// Newmark run of num_steps from the initial state with the direct
-// differentiation after every converged step (Newmark::computeSensitivities,
-// Newmark.cpp:904-959, one direction per parameter combination):
+// Newmark (or LoadControl) run of num_steps from the initial state with the
+// direct differentiation after every converged step
+// (Newmark::computeSensitivities, Newmark.cpp:904-959, one direction per
+// parameter combination):
 //   K_eff dU = -dP|_U + M (c3 dU' - a3 dV' - a4 dA') + alphaM M (c2 dU' - a1 dV' - a2 dA')
 // with K_eff formed again at the converged state (the reference solves with
 // the last Newton iteration's factors), then the record tangents committed.

@@ -412,9 +412,9 @@ def adjoint_backward(model, scale=1.0):
 
 
 def ddm_forward(model, phase, num_steps, dtheta, node, dof, weight):
-    """Newmark run of num_steps from the initial state with the direct
-    differentiation along the directions ``dtheta`` [num_dir, num_uni, 3];
-    returns (J, dJ[num_dir])."""
+    """Newmark or LoadControl run of num_steps from the initial state with the
+    direct differentiation along the directions ``dtheta`` [num_dir, num_uni,
+    3]; returns (J, dJ[num_dir])."""
     L = lib()
     L.xg_ddm_forward.argtypes = [C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_void_p,
                                  C.c_void_p, C.POINTER(C.c_double), C.c_void_p]
