@@ -1164,3 +1164,33 @@ def test_ddm_argument_checks(need_gpu):
             gpu.ddm_disp_sensitivity(m, 2)
         with pytest.raises(gpu.XaraGpuError, match="initial state"):
             gpu.ddm_forward(m, ph, 5, np.ones((1, nu, 3)), node, dof, w)
+
+
+@pytest.mark.parametrize("kind", [XG_UNI_STEEL02, XG_UNI_CONCRETE02, XG_UNI_STEEL01,
+                                  XG_UNI_CONCRETE01])
+def test_jvp_at_the_committed_strain(kind):
+    """A trial strain equal to the committed one keeps the committed state
+    in every law; its forward mode passes the record's tangents through
+    (the strain's own tangent for the strain field) and agrees with the
+    reverse mode there too."""
+    gpu = _gpu()
+    q = {XG_UNI_STEEL02: configs.steel02_row(), XG_UNI_CONCRETE02: configs.concrete02_row(30e6),
+         XG_UNI_STEEL01: configs.steel01_row(), XG_UNI_CONCRETE01: configs.concrete01_row(30e6)}[kind]
+    hc = port.uniaxial_trial(kind, q, port.uniaxial_init(kind, q), -1e-3)   # a committed state
+    rng = np.random.default_rng(61)
+    dhc = rng.normal(size=12)
+    dhc[[7, 8, 11]] = 0.0
+    dq = rng.normal(size=3)
+    de = rng.normal()
+    eps = float(hc[10])
+    dht = gpu.uniaxial_jvp(kind, q, hc, eps, de, dhc, dq)
+    fields = {XG_UNI_STEEL02: list(range(7)), XG_UNI_CONCRETE02: [0, 1],
+              XG_UNI_STEEL01: [0, 1, 2, 3], XG_UNI_CONCRETE01: [0, 1, 2]}[kind]
+    np.testing.assert_array_equal(dht[fields], dhc[fields])
+    yb = rng.normal(size=12)
+    yb[[7, 8, 11]] = 0.0
+    hb, sb, qb = gpu.uniaxial_vjp(kind, q, hc, eps, yb)
+    keep = fields + [9, 10]
+    lhs = float(yb[keep] @ dht[keep])
+    rhs = sb * de + float(hb[keep] @ dhc[keep]) + float(qb @ dq)
+    assert lhs == pytest.approx(rhs, rel=1e-12, abs=1e-300)
